@@ -1,0 +1,56 @@
+"""ctypes binding of libbsq_gb300.so.  There is no fallback: if the library was not built, or the
+CUDA runtime cannot create a context, every call raises."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import abi
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "libbsq_gb300.so")
+_lib = None
+
+
+class BsqError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"breseq_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def load():
+    """Load the in-tree library (build it first with breseq_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise BsqError(-1, f"{LIB_PATH} is missing: run `python -m breseq_gb300.build` (needs nvcc)")
+    L = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    L.bsq_create.argtypes = [P(C.c_void_p), C.c_int]
+    L.bsq_destroy.argtypes = [C.c_void_p]
+    L.bsq_destroy.restype = None
+    L.bsq_last_error.argtypes = [C.c_void_p]
+    L.bsq_last_error.restype = C.c_char_p
+    L.bsq_version.restype = C.c_char_p
+    L.bsq_load_sample.argtypes = [C.c_void_p, P(abi.Reference), P(abi.ReadSoA), P(C.c_int32)]
+    L.bsq_free_sample.argtypes = [C.c_void_p, C.c_int32]
+    L.bsq_sample_footprint.argtypes = [P(abi.Reference), P(abi.ReadSoA)]
+    L.bsq_sample_footprint.restype = C.c_uint64
+    L.bsq_error_count.argtypes = [C.c_void_p, C.c_int32, P(abi.EcParams), P(abi.EcResult)]
+    L.bsq_counts_to_log10_prob.argtypes = [P(C.c_uint64), C.c_uint32, C.c_uint32, P(C.c_double)]
+    L.bsq_identify_mutations.argtypes = [C.c_void_p, C.c_int32, P(abi.ImParams), P(C.c_double), P(abi.PositionArrays)]
+    L.bsq_im_result_counts.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_uint64), P(C.c_uint64)]
+    L.bsq_im_result_copy.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]
+    L.bsq_last_pass_stats.argtypes = [C.c_void_p, P(C.c_double), P(C.c_uint32), P(C.c_double)]
+    L.bsq_timer_start.argtypes = [C.c_void_p]
+    L.bsq_timer_stop.argtypes = [C.c_void_p, P(C.c_double)]
+    L.bsq_host_register.argtypes = [C.c_void_p, C.c_uint64]
+    L.bsq_host_unregister.argtypes = [C.c_void_p]
+    _lib = L
+    return L
+
+
+EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_load_sample", "bsq_free_sample",
+            "bsq_sample_footprint", "bsq_error_count", "bsq_counts_to_log10_prob", "bsq_identify_mutations",
+            "bsq_im_result_counts", "bsq_im_result_copy", "bsq_last_pass_stats", "bsq_timer_start",
+            "bsq_timer_stop", "bsq_host_register", "bsq_host_unregister")

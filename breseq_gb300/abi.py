@@ -1,0 +1,186 @@
+"""ctypes mirror of include/breseq_gb300.h (structs only; the function bindings live in _lib.py)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+P = C.POINTER
+
+
+class Reference(C.Structure):
+    _fields_ = [
+        ("n_targets", C.c_uint32),
+        ("target_offset", P(C.c_uint64)),
+        ("seq", C.c_char_p),
+        ("coverage_group", P(C.c_uint32)),
+        ("n_coverage_groups", C.c_uint32),
+        ("target_order", P(C.c_uint32)),
+        ("n_target_order", C.c_uint32),
+    ]
+
+
+class ReadSoA(C.Structure):
+    _fields_ = [
+        ("n_reads", C.c_uint64),
+        ("tid", P(C.c_int32)),
+        ("pos", P(C.c_int32)),
+        ("flag", P(C.c_uint16)),
+        ("mapq", P(C.c_uint8)),
+        ("x1", P(C.c_uint32)),
+        ("xl", P(C.c_int32)),
+        ("xr", P(C.c_int32)),
+        ("read_file", P(C.c_uint8)),
+        ("read_group", P(C.c_uint16)),
+        ("l_qseq", P(C.c_uint32)),
+        ("seq_off", P(C.c_uint64)),
+        ("cigar_off", P(C.c_uint64)),
+        ("n_cigar", P(C.c_uint16)),
+        ("cigar", P(C.c_uint32)),
+        ("seq", P(C.c_uint8)),
+        ("qual", P(C.c_uint8)),
+        ("n_cigar_total", C.c_uint64),
+        ("n_bases_total", C.c_uint64),
+    ]
+
+
+class EcParams(C.Structure):
+    _fields_ = [
+        ("n_read_files", C.c_uint32),
+        ("n_quality", C.c_uint32),
+        ("do_coverage", C.c_int32),
+        ("do_errors", C.c_int32),
+        ("preprocess_stage", C.c_int32),
+        ("unmatched_end_minimum_read_length", C.c_uint32),
+        ("unmatched_end_length_factor", C.c_double),
+    ]
+
+
+class EcResult(C.Structure):
+    _fields_ = [
+        ("counts", P(C.c_uint64)),
+        ("coverage_hist", P(C.c_uint64)),
+        ("hist_capacity", C.c_uint32),
+        ("hist_size", P(C.c_uint32)),
+        ("no_pos_hash_pr", P(C.c_double)),
+    ]
+
+
+class ImParams(C.Structure):
+    _fields_ = [
+        ("n_read_files", C.c_uint32),
+        ("n_quality", C.c_uint32),
+        ("base_quality_cutoff", C.c_uint32),
+        ("mutation_cutoff", C.c_double),
+        ("polymorphism_cutoff", C.c_double),
+        ("polymorphism_precision_decimal", C.c_double),
+        ("polymorphism_precision_places", C.c_uint32),
+        ("skip_missing_coverage_prediction", C.c_int32),
+        ("log10_ref_length", C.c_double),
+        ("deletion_propagation_cutoff", P(C.c_double)),
+        ("deletion_seed_cutoff", P(C.c_double)),
+        ("precision", C.c_int32),
+    ]
+
+
+class RaRecord(C.Structure):
+    _fields_ = [
+        ("tid", C.c_uint32), ("position", C.c_uint32), ("insert_position", C.c_uint32),
+        ("ref_base", C.c_char), ("new_base", C.c_char), ("major_base", C.c_char), ("minor_base", C.c_char),
+        ("score", C.c_double), ("consensus_score", C.c_double), ("f", C.c_double * 5),
+        ("major_frequency", C.c_double), ("frequency", C.c_double),
+        ("frequency_lower", C.c_double), ("frequency_upper", C.c_double),
+        ("fisher_strand_p", C.c_double), ("ks_quality_p", C.c_double),
+        ("ref_cov", C.c_int32 * 2), ("new_cov", C.c_int32 * 2), ("major_cov", C.c_int32 * 2),
+        ("minor_cov", C.c_int32 * 2), ("total_cov", C.c_int32 * 2),
+        ("n", C.c_uint32), ("passed_consensus", C.c_uint8), ("passed_polymorphism", C.c_uint8),
+        ("pad", C.c_uint8 * 2),
+    ]
+
+
+class McRecord(C.Structure):
+    _fields_ = [
+        ("tid", C.c_uint32), ("start", C.c_uint32), ("end", C.c_uint32), ("start_range", C.c_uint32),
+        ("end_range", C.c_uint32), ("pad", C.c_uint32),
+        ("left_outside_cov", C.c_double), ("left_inside_cov", C.c_double),
+        ("right_inside_cov", C.c_double), ("right_outside_cov", C.c_double),
+    ]
+
+
+class UnRecord(C.Structure):
+    _fields_ = [("tid", C.c_uint32), ("start", C.c_uint32), ("end", C.c_uint32)]
+
+
+class PositionArrays(C.Structure):
+    _fields_ = [
+        ("unique_top", P(C.c_uint32)), ("unique_bot", P(C.c_uint32)),
+        ("redundant_top", P(C.c_double)), ("redundant_bot", P(C.c_double)),
+        ("raw_redundant_top", P(C.c_uint32)), ("raw_redundant_bot", P(C.c_uint32)),
+        ("consensus_score", P(C.c_double)), ("best_base", P(C.c_uint8)), ("n_scored", P(C.c_uint32)),
+    ]
+
+
+def ptr(a: np.ndarray, ctype):
+    assert a.flags["C_CONTIGUOUS"], "arrays handed to the library must be contiguous"
+    return a.ctypes.data_as(P(ctype))
+
+
+class SampleView:
+    """Builds the Reference / ReadSoA structs over a synth.Sample (or any object with the same
+    array attributes) and keeps every array it points into alive."""
+
+    def __init__(self, s):
+        self._keep = []
+
+        def k(a, dt):
+            a = np.ascontiguousarray(a, dtype=dt)
+            self._keep.append(a)
+            return a
+
+        toff = k(s.target_offset, np.uint64)
+        seq = k(s.ref_seq, np.uint8)
+        cg = k(s.coverage_group, np.uint32)
+        order = k(s.target_order, np.uint32)
+        self.ref = Reference(
+            n_targets=len(toff) - 1, target_offset=ptr(toff, C.c_uint64),
+            seq=C.cast(seq.ctypes.data, C.c_char_p), coverage_group=ptr(cg, C.c_uint32),
+            n_coverage_groups=int(s.n_coverage_groups), target_order=ptr(order, C.c_uint32),
+            n_target_order=len(order))
+        fields = dict(tid=(np.int32, C.c_int32), pos=(np.int32, C.c_int32), flag=(np.uint16, C.c_uint16),
+                      mapq=(np.uint8, C.c_uint8), x1=(np.uint32, C.c_uint32), xl=(np.int32, C.c_int32),
+                      xr=(np.int32, C.c_int32), read_file=(np.uint8, C.c_uint8),
+                      read_group=(np.uint16, C.c_uint16), l_qseq=(np.uint32, C.c_uint32),
+                      seq_off=(np.uint64, C.c_uint64), cigar_off=(np.uint64, C.c_uint64),
+                      n_cigar=(np.uint16, C.c_uint16), cigar=(np.uint32, C.c_uint32),
+                      seq=(np.uint8, C.c_uint8), qual=(np.uint8, C.c_uint8))
+        kw = {}
+        for name, (dt, ct) in fields.items():
+            kw[name] = ptr(k(getattr(s, name), dt), ct)
+        self.reads = ReadSoA(n_reads=int(len(s.tid)), n_cigar_total=int(len(s.cigar)),
+                             n_bases_total=int(len(s.qual)), **kw)
+
+
+def ra_to_dicts(arr) -> list:
+    out = []
+    for r in arr:
+        out.append(dict(
+            tid=r.tid, position=r.position, insert_position=r.insert_position,
+            ref_base=r.ref_base.decode(), new_base=r.new_base.decode(), major_base=r.major_base.decode(),
+            minor_base=r.minor_base.decode(), score=r.score, consensus_score=r.consensus_score,
+            f=list(r.f), major_frequency=r.major_frequency, frequency=r.frequency,
+            frequency_lower=r.frequency_lower, frequency_upper=r.frequency_upper,
+            fisher_strand_p=r.fisher_strand_p, ks_quality_p=r.ks_quality_p,
+            ref_cov=tuple(r.ref_cov), new_cov=tuple(r.new_cov), major_cov=tuple(r.major_cov),
+            minor_cov=tuple(r.minor_cov), total_cov=tuple(r.total_cov), n=r.n,
+            passed_consensus=r.passed_consensus, passed_polymorphism=r.passed_polymorphism))
+    return out
+
+
+def mc_to_dicts(arr) -> list:
+    return [dict(tid=m.tid, start=m.start, end=m.end, start_range=m.start_range, end_range=m.end_range,
+                 left_outside_cov=m.left_outside_cov, left_inside_cov=m.left_inside_cov,
+                 right_inside_cov=m.right_inside_cov, right_outside_cov=m.right_outside_cov) for m in arr]
+
+
+def un_to_dicts(arr) -> list:
+    return [dict(tid=u.tid, start=u.start, end=u.end) for u in arr]

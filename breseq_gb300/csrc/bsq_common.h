@@ -1,0 +1,154 @@
+// Device-side layout of a resident sample and the argument blocks of the scoring kernels.
+//
+// Column space: every target t of a sample occupies padded columns [tpoff[t], tpoff[t] + len[t]),
+// tpoff[t] = target_offset[t] + t, followed by one separator column holding '\0'.  The separator
+// makes ref[c + 1] at a target's last base read as '\0', which is what breseq's NUL-terminated
+// reference buffer yields there (src/breseq/pileup_base.cpp:80-85; error_count.cpp:937-940 reads
+// one past the column), and it is never covered by a read.
+//
+// Tiles: 32 consecutive columns, one warp.  tile_range[t] = [lo, hi) is the range of (start-sorted)
+// reads that can cover any column of the tile: start > c0 - maxspan and start < c0 + 32.
+#pragma once
+#include <stdint.h>
+
+namespace bsq {
+
+// 32-byte read record, coordinate-sorted; one broadcast load per (read, warp).
+struct __align__(16) DevRead {
+  uint32_t start;      // padded column of the first reference-consuming CIGAR op
+  uint32_t end;        // exclusive end column
+  uint64_t seq_off;    // nibble index into seq[] and byte index into qual[]
+  uint32_t cigar_off;  // complex reads: offset into cigar[]
+  uint16_t len;        // l_qseq
+  uint16_t n_cigar;
+  uint16_t xl;         // XL trim, 0xFFFF when absent
+  uint16_t xr;         // XR trim, 0xFFFF when absent
+  uint8_t mapq_idx;    // index of this read's MAPQ among the sample's distinct values
+  uint8_t rfile;       // flat read-file index (k_read_set covariate)
+  uint8_t flags;       // kRev | kSimple | kRedundant | kSkip
+  uint8_t clip;        // simple reads: leading soft clip
+};
+static_assert(sizeof(DevRead) == 32, "DevRead must stay 32 bytes");
+
+enum : uint8_t { kRev = 1, kSimple = 2, kRedundant = 4, kSkip = 8 };
+constexpr uint16_t kNoTag = 0xFFFF;
+
+// Query bounds of complex reads (simple reads derive them from clip and span):
+// qs0/qe0 = query_start_0/query_end_0 (alignment.cpp:219-256), qbe = query_bounds_0().second
+// (alignment.cpp:113-196), qbs = its first.  Packed 4 x 16 bits.
+struct QBounds { uint16_t qs0, qe0, qbs, qbe; };
+
+struct DevSample {
+  const uint8_t* ref;         // padded reference chars
+  const DevRead* reads;
+  const uint32_t* x1;         // redundancy per read
+  const uint16_t* rg;         // read group per read
+  const QBounds* qb;          // per read (valid for complex reads)
+  const uint32_t* cigar;
+  const uint8_t* seq;         // packed 4-bit, high nibble first
+  const uint8_t* qual;
+  const uint2* tile_range;    // [n_tiles]
+  const uint32_t* tpoff;      // padded target offsets [n_targets + 1]
+  const uint32_t* tgt_group;  // coverage group per target
+  const uint8_t* tgt_called;  // 1 when the target is in the pileup set
+  const uint8_t* tgt_failed;  // pass 2: deletion propagation cutoff < 0 (coverage only)
+  uint32_t n_cols;            // padded columns
+  uint32_t n_tiles;
+  uint32_t n_reads;
+  uint32_t n_targets;
+  uint32_t maxspan;
+};
+
+// ----------------------------------------------------------------------------- pass 1
+struct EcArgs {
+  unsigned long long* counts;       // [R*25*Q]
+  unsigned long long* cov_hist;     // [G * hist_cap]
+  unsigned long long* found;        // [n_targets * 2] preprocess read-start tallies
+  uint32_t* err;                    // error word (bit set per kind)
+  uint32_t R, Q, hist_cap;
+  int do_errors, preprocess;
+  uint32_t unmatched_min_len;
+  float unmatched_factor;           // only used through floor(); double on host
+  double unmatched_factor_d;
+  uint32_t flush_tiles;             // shared histogram flush period (avoids u32 overflow)
+};
+
+// ----------------------------------------------------------------------------- pass 2
+// Likelihood class of a read base: (mapq_idx, read file, strand, quality, observed base).
+// For each class the host precomputes, exactly as fill_read_base_likelihoods does per read
+// (identify_mutations.cpp:3359-3384): log10 P(obs | b) for the five hypotheses, their maximum
+// and r[b] = 10^(lp[b] - max).
+struct ClassTable {
+  const double* lp64;     // [K][5]
+  const double* r64;      // [K][5]
+  const double* lpmax64;  // [K]
+  const float* lp32;      // [K][8]: lp[0..4] as float, [5] = 1 when obs-hypothesis is not the max
+  uint32_t K;
+  uint32_t R, Q, n_mapq;
+};
+
+// Per-column output of the column pass (insert position 0).
+struct ColCov {               // 32 bytes
+  uint32_t uniq_top, uniq_bot, rawred_top, rawred_bot;
+  double red_top, red_bot;
+};
+struct ColCall {              // 16 bytes
+  double score;               // consensus score (NaN when n == 0)
+  uint32_t n;
+  uint8_t best;               // 0..4, 5 = N
+  uint8_t flags;              // kBasePredicted | kUniqueOnly | kCandidate | kSlots | kRecompute
+  uint8_t pad[2];
+};
+enum : uint8_t { kBasePredicted = 1, kUniqueOnly = 2, kCandidate = 4, kSlots = 8, kRecompute = 16, kScored = 32 };
+
+struct ImArgs {
+  ColCov* cov;
+  ColCall* call;
+  uint32_t* err;
+  uint32_t base_quality_cutoff;
+  int precision;              // 0 = FP64 everywhere, 1 = FP32 compensated + screen
+  double log10_ref_len;
+  double mutation_cutoff;
+  double poly_cutoff;
+  float screen_margin;        // log10 units subtracted from the polymorphism cutoff for the screen
+  float guard;                // consensus guard band (log10 units) for FP64 recompute
+};
+
+// A scoring job for the candidate kernel: one reference column, all its insert slots.
+struct CandArgs {
+  const uint32_t* cand;       // candidate columns
+  uint32_t n_cand;
+  unsigned int* next;         // work counter (persistent warps)
+  ColCall* call;              // slot-0 consensus is rewritten for kRecompute columns
+  struct RaDev* ra;           // output records
+  unsigned int* n_ra;
+  uint32_t ra_cap;
+  uint4* scratch;             // per-warp gather buffer: [n_warps][scratch_per_warp]
+  uint32_t scratch_per_warp;
+  uint32_t* err;
+  uint32_t base_quality_cutoff;
+  double log10_ref_len;
+  double mutation_cutoff;
+  double poly_cutoff;
+  double precision_decimal;
+  uint32_t Qhist;             // quality histogram bins kept per RA (for the K-S test)
+  uint32_t* qhist;            // [ra_cap][2][Qhist] major / minor qualities
+};
+
+// Raw RA values written by the candidate kernel (host adds Fisher / K-S and formats).
+struct RaDev {
+  uint32_t col;               // padded column
+  uint32_t insert_position;
+  double score, consensus_score;
+  double f[5];
+  double lower, upper;
+  uint32_t pos_info[5][2];    // [base][top, bottom]
+  uint32_t n;
+  uint8_t ref_idx, var_idx, maj_idx, min_idx, passed_cons, passed_poly, pad[2];
+};
+
+// error word bits
+enum : uint32_t { kErrCovariate = 1, kErrBase = 2, kErrBounds = 4, kErrOrder = 8, kErrCigar = 16,
+                  kErrScratch = 32, kErrRaOverflow = 64, kErrX1 = 128 };
+
+}  // namespace bsq

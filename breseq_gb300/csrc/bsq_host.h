@@ -1,0 +1,47 @@
+// Host-side steps around the scoring kernels (bsq_host.cpp).
+#pragma once
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/breseq_gb300.h"
+#include "bsq_common.h"
+
+namespace bsq {
+namespace host {
+
+// counts_to_log10_prob + the 6-significant-digit text round trip of error_rates.tab
+// (src/breseq/error_count.cpp:629-690, 1005-1026).
+void counts_to_log10_prob(const uint64_t* counts, uint32_t R, uint32_t Q, double* out);
+
+struct ClassTableHost {
+  std::vector<double> lp64, r64, lpmax64;
+  std::vector<float> lp32;
+  uint32_t K = 0;
+};
+// Per likelihood class (mapq_idx, read file, strand, quality, observed base) the values that
+// fill_read_base_likelihoods computes per read (src/breseq/identify_mutations.cpp:3359-3384).
+void build_class_table(const double* log10_table, uint32_t R, uint32_t Q, const std::vector<uint8_t>& mapq_values,
+                       ClassTableHost& out);
+
+// fisher_exact_test_2x2 / ks_test_two_sample_less (src/breseq/stats.cpp:2144-2286)
+double fisher_2x2(uint32_t a, uint32_t b, uint32_t c, uint32_t d);
+// x, y given as quality histograms (value = bin index)
+double ks_less_hist(const uint32_t* xh, const uint32_t* yh, uint32_t bins);
+
+struct SampleLayout {
+  const std::vector<uint32_t>* tpoff;
+  const std::vector<uint64_t>* toff;
+  const std::vector<uint32_t>* order;
+};
+
+void assemble_ra(const std::vector<RaDev>& ra, const std::vector<uint32_t>& qhist, uint32_t Qh, const SampleLayout& L,
+                 std::vector<bsq_ra_record>& out);
+// MC and UN state machines in pileup order (identify_mutations.cpp:2107-2164, 2262-2344, 2972-3007)
+void intervals(const std::vector<ColCov>& cov, const std::vector<ColCall>& call, const SampleLayout& L,
+               const bsq_im_params* p, std::vector<bsq_mc_record>& mc, std::vector<bsq_un_record>& un);
+void fill_positions(const std::vector<ColCov>& cov, const std::vector<ColCall>& call, const SampleLayout& L,
+                    bsq_position_arrays* out);
+
+}  // namespace host
+}  // namespace bsq

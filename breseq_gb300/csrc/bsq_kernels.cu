@@ -1,0 +1,988 @@
+// CUDA kernels of the read-evidence scoring path (sm_103a).
+//
+// All column work is "tile-gather over start-sorted reads": a warp owns 32 consecutive reference
+// columns, walks the reads that can cover them in BAM order (one broadcast 32-byte record load per
+// read), and each lane resolves its own column inside the read.  Adjacent lanes therefore read
+// adjacent bytes of the same read: base and quality loads coalesce, every column sees its reads in
+// BAM order (the order htslib's pileup presents them, so per-column FP64 sums run in the reference's
+// order), and there is no global atomic per read base.
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "bsq_common.h"
+#include "bsq_kernels.h"
+
+namespace bsq {
+
+// ============================================================================ helpers
+__device__ __forceinline__ uint8_t nib_at(const uint8_t* seq, uint64_t nib) {
+  uint8_t b = __ldg(seq + (nib >> 1));
+  return (nib & 1) ? (b & 0xF) : (b >> 4);
+}
+// 4-bit BAM base -> index A,C,G,T = 0..3; N/others -> -1 (src/breseq/common.h:253-265)
+__device__ __forceinline__ int bam_idx(uint8_t b) {
+  return b == 1 ? 0 : b == 2 ? 1 : b == 4 ? 2 : b == 8 ? 3 : -1;
+}
+// reference char -> index, 'N' -> 5, other -> -1 (common.h:267-279)
+__device__ __forceinline__ int chr_idx(uint8_t c) {
+  return c == 'A' ? 0 : c == 'C' ? 1 : c == 'G' ? 2 : c == 'T' ? 3 : c == 'N' ? 5 : -1;
+}
+__device__ __forceinline__ bool op_ref(uint32_t op) { return op == 0 || op == 2 || op == 3 || op == 7 || op == 8; }
+__device__ __forceinline__ bool op_qm(uint32_t op) { return op == 0 || op == 7 || op == 8; }
+
+struct Pile { int qpos; int indel; bool del; };
+
+// htslib's per-column read state (bam_plp_auto / resolve_cigar2 semantics) for a CIGAR with more
+// than a single aligned block; c must lie in [start, end).
+__device__ bool resolve_cigar(const uint32_t* cig, int n, uint32_t start, uint32_t c, Pile& e) {
+  uint32_t x = start;
+  int y = 0;
+  for (int k = 0; k < n; k++) {
+    uint32_t w = __ldg(cig + k), op = w & 0xF, len = w >> 4;
+    if (op_ref(op)) {
+      if (c < x + len) {
+        if (op_qm(op)) { e.qpos = y + (int)(c - x); e.del = false; }
+        else { e.qpos = y; e.del = true; }
+        e.indel = 0;
+        if (c == x + len - 1 && k + 1 < n) {
+          uint32_t w2 = __ldg(cig + k + 1), op2 = w2 & 0xF;
+          if (op2 == 2 && op != 2) {
+            int d = -(int)(w2 >> 4);
+            for (int j = k + 2; j < n; j++) { uint32_t wj = __ldg(cig + j); if ((wj & 0xF) == 2) d -= (int)(wj >> 4); else break; }
+            e.indel = d;
+          } else if (op2 == 1) {
+            int d = (int)(w2 >> 4);
+            for (int j = k + 2; j < n; j++) {
+              uint32_t wj = __ldg(cig + j), o = wj & 0xF;
+              if (o == 1) d += (int)(wj >> 4); else if (o != 6) break;
+            }
+            e.indel = d;
+          } else if (op2 == 6 && k + 2 < n) {
+            int l3 = 0;
+            for (int j = k + 2; j < n; j++) {
+              uint32_t wj = __ldg(cig + j), o = wj & 0xF;
+              if (o == 1) l3 += (int)(wj >> 4); else if (op_ref(o)) break;
+            }
+            if (l3 > 0) e.indel = l3;
+          }
+        }
+        return true;
+      }
+      x += len;
+      if (op_qm(op)) y += (int)len;
+    } else if (op == 1 || op == 4) {
+      y += (int)len;
+    }
+  }
+  return false;
+}
+
+__device__ __forceinline__ void resolve(const DevSample& S, const DevRead& rd, uint32_t c, Pile& e) {
+  if (rd.flags & kSimple) { e.qpos = (int)(c - rd.start) + rd.clip; e.indel = 0; e.del = false; }
+  else if (!resolve_cigar(S.cigar + rd.cigar_off, rd.n_cigar, rd.start, c, e)) { e.qpos = 0; e.indel = 0; e.del = true; }
+}
+
+// pileup_wrapper::is_trimmed (src/breseq/alignment.h:389-411), unsigned arithmetic as there
+__device__ __forceinline__ bool is_trimmed(const DevRead& rd, int qpos, bool past_base) {
+  uint32_t qp1 = (uint32_t)(qpos + 1);
+  if (rd.xl != kNoTag && qp1 <= rd.xl) return true;
+  if (rd.xr != kNoTag) {
+    uint32_t len = rd.len;
+    if (len - qp1 + 1u <= rd.xr) return true;
+    if (past_base && (len - qp1 == rd.xr)) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ int query_end0(const DevSample& S, const DevRead& rd, uint32_t r) {
+  return (rd.flags & kSimple) ? (int)rd.clip + (int)(rd.end - rd.start) - 1 : (int)S.qb[r].qe0;
+}
+__device__ __forceinline__ int query_start0(const DevSample& S, const DevRead& rd, uint32_t r) {
+  return (rd.flags & kSimple) ? (int)rd.clip : (int)S.qb[r].qs0;
+}
+__device__ __forceinline__ int bounds_end0(const DevSample& S, const DevRead& rd, uint32_t r) {
+  return (rd.flags & kSimple) ? (int)rd.clip + (int)(rd.end - rd.start) - 1 : (int)S.qb[r].qbe;
+}
+
+__device__ __forceinline__ uint32_t target_of(const DevSample& S, uint32_t c) {
+  uint32_t lo = 0, hi = S.n_targets;  // largest t with tpoff[t] <= c
+  while (hi - lo > 1) { uint32_t mid = (lo + hi) >> 1; if (__ldg(S.tpoff + mid) <= c) lo = mid; else hi = mid; }
+  return lo;
+}
+
+// ============================================================================ pack + validate
+// One thread per record: builds the 32-byte DevRead, the query bounds of complex reads, checks the
+// record (sortedness, CIGAR, offsets) and gathers the sample statistics the tile kernels need.
+__global__ void pack_reads_kernel(RawSoA in, PackOut out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= in.n) return;
+  const int32_t tid = in.tid[i], pos = in.pos[i];
+  const uint16_t flag = in.flag[i];
+  uint32_t err = 0;
+  if (tid < 0 || (uint32_t)tid >= in.n_targets || pos < 0) { atomicOr(out.err, kErrOrder); return; }
+  if (i > 0) {
+    int32_t pt = in.tid[i - 1], pp = in.pos[i - 1];
+    if (pt > tid || (pt == tid && pp > pos)) err |= kErrOrder;
+  }
+  const uint32_t len = in.l_qseq[i];
+  const uint64_t so = in.seq_off[i];
+  const uint64_t co = in.cigar_off[i];
+  const uint32_t nc = in.n_cigar[i];
+  DevRead d;
+  d.seq_off = so;
+  d.len = (uint16_t)len;
+  d.n_cigar = (uint16_t)nc;
+  d.cigar_off = (uint32_t)co;
+  d.xl = in.xl[i] < 0 ? kNoTag : (uint16_t)in.xl[i];
+  d.xr = in.xr[i] < 0 ? kNoTag : (uint16_t)in.xr[i];
+  const uint8_t mq = in.mapq[i];
+  d.mapq_idx = 0;
+  d.rfile = in.read_file[i];
+  d.clip = 0;
+  uint8_t fl = 0;
+  if (flag & 0x10) fl |= kRev;
+  const uint32_t x1 = in.x1[i];
+  if (x1 == 0) err |= kErrX1;
+  if (x1 > 1) fl |= kRedundant;
+  const bool skip = (flag & 0x704) != 0;
+  if (skip) fl |= kSkip;
+  if (len > 65535 || (so & 1) || so + len > in.n_bases || co + nc > in.n_cigar_total) err |= kErrBounds;
+  if (in.xl[i] >= 65535 || in.xr[i] >= 65535) err |= kErrBounds;
+  uint32_t rlen = 0, qlen = 0, nblk = 0;
+  int32_t qs1 = 1, qe1 = 0, bs = 1, be = 0;
+  bool only_s_m = true;
+  uint32_t lead_s = 0;
+  if (!(err & kErrBounds)) {
+    const uint32_t* cg = in.cigar + co;
+    for (uint32_t k = 0; k < nc; k++) {
+      uint32_t op = cg[k] & 0xF, l = cg[k] >> 4;
+      if (op_ref(op)) rlen += l;
+      if (op == 0 || op == 1 || op == 4 || op == 7 || op == 8) qlen += l;
+      if (op == 0) nblk++;
+      else if (op == 4) { if (k == 0) lead_s = l; else if (k != nc - 1) only_s_m = false; }
+      else only_s_m = false;
+    }
+    for (uint32_t k = 0; k < nc; k++) { if ((cg[k] & 0xF) != 4) break; qs1 += (int32_t)(cg[k] >> 4); }
+    qe1 = (int32_t)qlen;
+    for (uint32_t k = nc - 1; k > 0 && k < nc; k--) { if ((cg[k] & 0xF) != 4) break; qe1 -= (int32_t)(cg[k] >> 4); }
+    be = (int32_t)qlen;
+    for (uint32_t k = 0; k < nc; k++) {
+      uint32_t op = cg[k] & 0xF;
+      if (op != 4 && op != 5 && op != 3) break;
+      if (op == 4) bs += (int32_t)(cg[k] >> 4);
+    }
+    for (uint32_t k = nc - 1; k > 0 && k < nc; k--) {
+      uint32_t op = cg[k] & 0xF;
+      if (op != 4 && op != 5 && op != 3) break;
+      if (op == 4) be -= (int32_t)(cg[k] >> 4);
+    }
+  }
+  const uint32_t tlen = in.tpoff[tid + 1] - in.tpoff[tid] - 1;
+  if (!skip && !(err & kErrBounds)) {
+    if (nc == 0 || rlen == 0 || qlen != len) err |= kErrCigar;
+    if ((uint64_t)pos + rlen > tlen) err |= kErrCigar;
+  }
+  if (rlen == 0) rlen = 1;
+  d.start = in.tpoff[tid] + (uint32_t)pos;
+  d.end = d.start + rlen;
+  if (only_s_m && nblk == 1 && lead_s < 256) { fl |= kSimple; d.clip = (uint8_t)lead_s; }
+  d.flags = fl;
+  QBounds qb;
+  qb.qs0 = (uint16_t)(qs1 - 1); qb.qe0 = (uint16_t)(qe1 - 1); qb.qbs = (uint16_t)(bs - 1); qb.qbe = (uint16_t)(be - 1);
+  out.reads[i] = d;
+  out.qb[i] = qb;
+  out.rstart[i] = d.start;
+  out.mapq[i] = mq;
+  if (err) atomicOr(out.err, err);
+  if (!skip) {
+    atomicMax(out.maxspan, rlen);
+    atomicOr(out.mapq_mask + (mq >> 5), 1u << (mq & 31));
+  }
+}
+
+// apply the host's MAPQ -> class index map
+__global__ void mapq_index_kernel(DevRead* reads, const uint8_t* mapq, const uint8_t* map, uint32_t n) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) reads[i].mapq_idx = map[mapq[i]];
+}
+
+// tile read ranges: reads with start in (c0 - maxspan, c0 + 32)
+__global__ void tile_range_kernel(const uint32_t* rstart, uint32_t n_reads, uint32_t n_tiles, uint32_t maxspan,
+                                  uint2* tile_range, uint32_t* max_tile_reads) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tiles) return;
+  uint32_t c0 = t * 32;
+  uint32_t lo_key = (c0 + 1 > maxspan) ? c0 + 1 - maxspan : 0;   // start >= c0 - maxspan + 1
+  uint32_t hi_key = c0 + 32;                                       // start < c0 + 32
+  uint32_t a = 0, b = n_reads;
+  while (a < b) { uint32_t m = (a + b) >> 1; if (__ldg(rstart + m) < lo_key) a = m + 1; else b = m; }
+  uint32_t lo = a;
+  b = n_reads;
+  while (a < b) { uint32_t m = (a + b) >> 1; if (__ldg(rstart + m) < hi_key) a = m + 1; else b = m; }
+  tile_range[t] = make_uint2(lo, a);
+  atomicMax(max_tile_reads, a - lo);
+}
+
+// ============================================================================ pass 1: error counts
+// error_count_pileup::pileup_callback (error_count.cpp:125-199) + count_alignment_position
+// (error_count.cpp:854-986).  Covariate events go to a block-private shared histogram; unique-only
+// coverage goes to the per-group histogram with one atomic per distinct value per warp.
+__global__ void __launch_bounds__(256) ec_kernel(DevSample S, EcArgs A) {
+  extern __shared__ uint32_t sh_hist[];
+  const uint32_t nbins = A.R * 25u * A.Q;
+  for (uint32_t i = threadIdx.x; i < nbins; i += blockDim.x) sh_hist[i] = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  uint32_t local_err = 0;
+  uint32_t tiles_done = 0;
+  // all warps of the block run the same number of loop trips so the periodic flush can sync
+  const uint32_t stride = gridDim.x * nwarps;
+  const uint32_t trips = (S.n_tiles + stride - 1) / stride;
+  for (uint32_t trip = 0; trip < trips; trip++) {
+    const uint32_t tile = trip * stride + blockIdx.x * nwarps + warp;
+    if (tile < S.n_tiles) {
+      const uint32_t c0 = tile * 32, c = c0 + lane;
+      const uint8_t refc = (c < S.n_cols) ? __ldg(S.ref + c) : 0;
+      const uint8_t refn = (c + 1 < S.n_cols) ? __ldg(S.ref + c + 1) : 0;
+      const uint32_t t = (c < S.n_cols) ? target_of(S, c) : 0;
+      const bool real = (c < S.n_cols) && refc != 0 && __ldg(S.tgt_called + t);
+      uint32_t uniq = 0;
+      bool red = false;
+      int hqs0 = 0, hqs1 = 0;
+      const uint2 rr = __ldg(S.tile_range + tile);
+      for (uint32_t r = rr.x; r < rr.y; r++) {
+        const DevRead rd = S.reads[r];
+        if ((rd.flags & kSkip) || rd.end <= c0) continue;
+        if (!(real && c >= rd.start && c < rd.end)) continue;
+        Pile e;
+        resolve(S, rd, c, e);
+        if (e.del) continue;
+        if (rd.flags & kRedundant) { red = true; continue; }
+        ++uniq;
+        const int rev = rd.flags & kRev;
+        if (A.preprocess) {
+          // Settings::required_junction_read_end_min_coordinate (settings.h:345-354)
+          int32_t umax = (int32_t)floor((double)((int32_t)rd.len - (int32_t)A.unmatched_min_len) * A.unmatched_factor_d);
+          uint32_t req = (umax <= 0) ? rd.len : rd.len - (uint32_t)umax;
+          uint32_t send1;
+          if (rd.flags & kSimple) {
+            uint32_t bs1 = rd.clip + 1, be1 = rd.clip + (rd.end - rd.start);
+            send1 = rev ? rd.len - bs1 + 1 : be1;
+          } else {
+            QBounds q = S.qb[r];
+            send1 = rev ? rd.len - (q.qbs + 1u) + 1 : q.qbe + 1u;
+          }
+          if (e.qpos == 0 && send1 >= req) { if (rev) hqs1 = 1; else hqs0 = 1; }
+        }
+        if (!A.do_errors) continue;
+        const uint32_t rs = rd.rfile;
+        const uint64_t so = rd.seq_off;
+        // (1) base substitution / match
+        {
+          const uint8_t ob = nib_at(S.seq, so + e.qpos);
+          if (ob != 15 && refc != 'N') {
+            int oi = bam_idx(ob), ri = chr_idx(refc);
+            if (oi < 0 || ri < 0 || ri > 3) { local_err |= kErrBase; }
+            else {
+              if (rev) { oi = 3 - oi; ri = 3 - ri; }
+              const uint32_t q = __ldg(S.qual + so + e.qpos);
+              if (q >= A.Q || rs >= A.R) local_err |= kErrCovariate;
+              else atomicAdd(&sh_hist[rs + A.R * (ri + 5u * (oi + 5u * q))], 1u);
+            }
+          }
+        }
+        if (e.indel == 0) {                         // (2a) '..'
+          if (e.qpos < query_end0(S, rd, r)) {
+            const int mq = e.qpos + 1 - rev;
+            const uint8_t ob = nib_at(S.seq, so + mq);
+            const uint8_t rc = rev ? refc : refn;
+            if (ob != 15 && rc != 'N') {
+              const uint32_t q = __ldg(S.qual + so + mq);
+              if (q >= A.Q || rs >= A.R) local_err |= kErrCovariate;
+              else atomicAdd(&sh_hist[rs + A.R * (4u + 5u * (4u + 5u * q))], 1u);
+            }
+          }
+        } else if (e.indel == -1) {                 // (2b) one deleted base follows
+          const int mq = e.qpos + 1 - rev;
+          if (mq < 0 || mq >= (int)rd.len) { local_err |= kErrBounds; }
+          else {
+            const uint8_t ob = nib_at(S.seq, so + mq);
+            if (ob != 15 && refn != 'N') {
+              int ri = chr_idx(refn);
+              if (ri < 0 || ri > 3) local_err |= kErrBase;
+              else {
+                if (rev) ri = 3 - ri;
+                const uint32_t q = __ldg(S.qual + so + mq);
+                if (q >= A.Q || rs >= A.R) local_err |= kErrCovariate;
+                else atomicAdd(&sh_hist[rs + A.R * (ri + 5u * (4u + 5u * q))], 1u);
+              }
+            }
+          }
+        } else if (e.indel == 1) {                  // (2c) one inserted base follows
+          const int mq = e.qpos + 1;
+          if (mq >= (int)rd.len) { local_err |= kErrBounds; }
+          else if (mq <= query_end0(S, rd, r) && mq >= query_start0(S, rd, r)) {
+            const uint8_t ob = nib_at(S.seq, so + mq);
+            if (ob != 15) {
+              int oi = bam_idx(ob);
+              if (oi < 0) local_err |= kErrBase;
+              else {
+                if (rev) oi = 3 - oi;
+                const uint32_t q = __ldg(S.qual + so + mq);
+                if (q >= A.Q || rs >= A.R) local_err |= kErrCovariate;
+                else atomicAdd(&sh_hist[rs + A.R * (4u + 5u * (oi + 5u * q))], 1u);
+              }
+            }
+          }
+        }
+      }
+      // unique-only coverage histogram (error_count.cpp:181-186), one atomic per distinct value
+      const bool rec = real && !red;
+      const uint32_t g = rec ? __ldg(S.tgt_group + t) : 0;
+      const uint32_t key = rec ? (g * A.hist_cap + min(uniq, A.hist_cap - 1)) : 0xFFFFFFFFu;
+      const unsigned active = __ballot_sync(0xFFFFFFFFu, rec);
+      if (rec) {
+        const unsigned peers = __match_any_sync(active, key);
+        if (lane == __ffs(peers) - 1) atomicAdd(A.cov_hist + key, (unsigned long long)__popc(peers));
+        if (uniq >= A.hist_cap) local_err |= kErrBounds;
+        if (A.preprocess) {
+          atomicAdd(A.found + 2 * t + hqs0, 1ull);
+          atomicAdd(A.found + 2 * t + hqs1, 1ull);
+        }
+      }
+    }
+    if (++tiles_done == A.flush_tiles) {   // keep the shared u32 counters far from overflow
+      tiles_done = 0;
+      __syncthreads();
+      for (uint32_t i = threadIdx.x; i < nbins; i += blockDim.x) {
+        uint32_t v = sh_hist[i];
+        if (v) { atomicAdd(A.counts + i, (unsigned long long)v); sh_hist[i] = 0; }
+      }
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < nbins; i += blockDim.x) {
+    uint32_t v = sh_hist[i];
+    if (v) atomicAdd(A.counts + i, (unsigned long long)v);
+  }
+  if (local_err) atomicOr(A.err, local_err);
+}
+
+// ============================================================================ pass 2: column pass
+// identify_mutations_pileup::pileup_callback at insert position 0 (identify_mutations.cpp:1359-1686)
+// for every column: coverage, the five summed log10 likelihoods, the pure-genotype call, and the
+// decision of which columns go on to the EM candidate kernel.
+template <bool FP64>
+__global__ void __launch_bounds__(256) im_column_kernel(DevSample S, ClassTable T, ImArgs A) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  uint32_t local_err = 0;
+  for (uint32_t tile = blockIdx.x * nwarps + warp; tile < S.n_tiles; tile += gridDim.x * nwarps) {
+    const uint32_t c0 = tile * 32, c = c0 + lane;
+    const bool inr = c < S.n_cols;
+    const uint8_t refc = inr ? __ldg(S.ref + c) : 0;
+    const uint32_t t = inr ? target_of(S, c) : 0;
+    const bool real = inr && refc != 0 && __ldg(S.tgt_called + t);
+    const bool failed = real && __ldg(S.tgt_failed + t);
+    const int ref_idx = chr_idx(refc) < 0 ? 5 : chr_idx(refc);
+    uint32_t utop = 0, ubot = 0, rtop = 0, rbot = 0, n = 0;
+    double redtop = 0.0, redbot = 0.0;
+    bool uonly = true, slots = false;
+    double S64[5] = {0, 0, 0, 0, 0};
+    float s32[5] = {0, 0, 0, 0, 0}, k32[5] = {0, 0, 0, 0, 0}, B[5] = {0, 0, 0, 0, 0};
+    const uint2 rr = __ldg(S.tile_range + tile);
+    for (uint32_t r = rr.x; r < rr.y; r++) {
+      const DevRead rd = S.reads[r];
+      if ((rd.flags & kSkip) || rd.end <= c0) continue;
+      if (!(real && c >= rd.start && c < rd.end)) continue;
+      Pile e;
+      resolve(S, rd, c, e);
+      const bool rev = rd.flags & kRev;
+      const bool red = rd.flags & kRedundant;
+      if (failed) {
+        // tabulate_position_coverage (identify_mutations.cpp:2218-2250)
+        if (e.del) continue;
+        if (nib_at(S.seq, rd.seq_off + e.qpos) == 15) continue;
+        if (!red) { if (rev) ++ubot; else ++utop; }
+        else { double w = 1.0 / (double)__ldg(S.x1 + r); if (rev) { redbot += w; ++rbot; } else { redtop += w; ++rtop; } }
+        continue;
+      }
+      const int obi = e.del ? -1 : max(e.indel, 0);
+      const uint8_t base = e.del ? (uint8_t)'.' : nib_at(S.seq, rd.seq_off + e.qpos);
+      if (base == 15) continue;
+      if (!red) {
+        if (rev) ++ubot; else ++utop;
+        if (obi > 0) slots = true;
+      } else {
+        uonly = false;
+        double w = 1.0 / (double)__ldg(S.x1 + r);
+        if (rev) { redbot += w; ++rbot; } else { redtop += w; ++rtop; }
+        continue;
+      }
+      if (is_trimmed(rd, e.qpos, e.del)) continue;
+      int qp = e.qpos;
+      if (e.del) {
+        qp += 1 - (int)rev;
+        if (qp >= (int)rd.len) continue;      // the reference asserts here; unusable base
+        if (nib_at(S.seq, rd.seq_off + qp) == 15) continue;
+      }
+      const int obs = e.del ? 4 : bam_idx(base);
+      if (obs < 0) { local_err |= kErrBase; continue; }
+      const uint32_t q = __ldg(S.qual + rd.seq_off + qp);
+      const uint32_t rs = rd.rfile;
+      if (q >= T.Q || rs >= T.R) { local_err |= kErrCovariate; continue; }
+      if (q < A.base_quality_cutoff) continue;
+      const uint32_t k = ((((uint32_t)rd.mapq_idx * T.R + rs) * 2u + (rev ? 1u : 0u)) * T.Q + q) * 5u + (uint32_t)obs;
+      ++n;
+      if (FP64) {
+        const double* lp = T.lp64 + (size_t)k * 5;
+#pragma unroll
+        for (int b = 0; b < 5; b++) S64[b] += __ldg(lp + b);
+      } else {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(T.lp32 + (size_t)k * 8));
+        const float2 w = __ldg(reinterpret_cast<const float2*>(T.lp32 + (size_t)k * 8 + 4));
+        const float lp[5] = {v.x, v.y, v.z, v.w, w.x};
+#pragma unroll
+        for (int b = 0; b < 5; b++) {        // Kahan-compensated FP32 sums
+          const float y = lp[b] - k32[b];
+          const float tt = s32[b] + y;
+          k32[b] = (tt - s32[b]) - y;
+          s32[b] = tt;
+        }
+        // screen bound  B_v = sum_i max(0, lp_i[v] - lp_i[ref]); zero unless the read's own
+        // base is not its most likely hypothesis or it differs from the reference
+        if (obs != ref_idx || w.y != 0.0f) {
+          const float lr = ref_idx == 0 ? lp[0] : ref_idx == 1 ? lp[1] : ref_idx == 2 ? lp[2] : ref_idx == 3 ? lp[3] : lp[4];
+#pragma unroll
+          for (int b = 0; b < 5; b++) B[b] += fmaxf(0.0f, lp[b] - lr);
+        }
+      }
+    }
+    if (!inr) continue;
+    ColCov cv;
+    cv.uniq_top = utop; cv.uniq_bot = ubot; cv.rawred_top = rtop; cv.rawred_bot = rbot;
+    cv.red_top = redtop; cv.red_bot = redbot;
+    ColCall cl;
+    cl.n = n; cl.best = 5; cl.score = __longlong_as_double(0x7ff8000000000000ll); cl.flags = 0;
+    cl.pad[0] = cl.pad[1] = 0;
+    if (real && !failed) {
+      if (uonly) cl.flags |= kUniqueOnly;
+      if (slots) cl.flags |= kSlots;
+      cl.flags |= kScored;
+      if (n > 0) {
+        // pure_genotype_call (identify_mutations.cpp:3398-3433) and the Bonferroni shift (:1680)
+        int best = 0;
+        double score;
+        if (FP64) {
+#pragma unroll
+          for (int b = 1; b < 5; b++) if (S64[b] > S64[best]) best = b;
+          double off = -DBL_MAX;
+#pragma unroll
+          for (int b = 0; b < 5; b++) if (b != best) off = fmax(off, S64[b]);
+          double te = 0;
+#pragma unroll
+          for (int b = 0; b < 5; b++) if (b != best) te += exp10(S64[b] - off);
+          score = S64[best] - (log10(te) + off) - A.log10_ref_len;
+          if (best != ref_idx && score > 0) cl.flags |= kCandidate;
+          cl.flags |= kCandidate;            // the plain form runs the EM wherever a base was scored
+        } else {
+          double tot[5];
+#pragma unroll
+          for (int b = 0; b < 5; b++) tot[b] = (double)s32[b] - (double)k32[b];
+#pragma unroll
+          for (int b = 1; b < 5; b++) if (tot[b] > tot[best]) best = b;
+          double d[5], off = -DBL_MAX;
+#pragma unroll
+          for (int b = 0; b < 5; b++) { d[b] = tot[b] - tot[best]; if (b != best) off = fmax(off, d[b]); }
+          float te = 0.0f;
+#pragma unroll
+          for (int b = 0; b < 5; b++) if (b != best) te += exp10f((float)(d[b] - off));
+          score = -(off + (double)log10f(te)) - A.log10_ref_len;
+          // guard band: FP32 sums are within ~n * 6e-7 of FP64; decisions closer than that are
+          // recomputed in FP64 by the candidate kernel
+          const double g = (double)A.guard * (1.0 + (double)n);
+          const bool near = fabs(score - A.mutation_cutoff) < g || (best != ref_idx && fabs(score) < g) || off > -g;
+          if (near) cl.flags |= kRecompute;
+          if (best != ref_idx && score > 0) cl.flags |= kCandidate;
+          float bmax = 0.0f;
+#pragma unroll
+          for (int b = 0; b < 5; b++) if (b != ref_idx) bmax = fmaxf(bmax, B[b]);
+          if (ref_idx == 5 || (double)bmax - A.log10_ref_len >= A.poly_cutoff - (double)A.screen_margin)
+            cl.flags |= kCandidate;
+        }
+        cl.best = (uint8_t)best;
+        cl.score = score;
+        if (score >= A.mutation_cutoff) cl.flags |= kBasePredicted;
+      }
+    }
+    A.cov[c] = cv;
+    A.call[c] = cl;
+  }
+  if (local_err) atomicOr(A.err, local_err);
+}
+
+// ============================================================================ candidate compaction
+// Deterministic stream compaction of the columns flagged for the candidate kernel, in column order.
+__global__ void cand_count_kernel(const ColCall* call, uint32_t n, uint32_t* block_counts) {
+  __shared__ uint32_t s;
+  if (threadIdx.x == 0) s = 0;
+  __syncthreads();
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool f = i < n && (call[i].flags & (kCandidate | kSlots | kRecompute));
+  uint32_t b = __popc(__ballot_sync(0xFFFFFFFFu, f));
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(&s, b);
+  __syncthreads();
+  if (threadIdx.x == 0) block_counts[blockIdx.x] = s;
+}
+
+__global__ void scan_kernel(uint32_t* v, uint32_t n, uint32_t* total) {  // single block, exclusive
+  __shared__ uint32_t carry;
+  __shared__ uint32_t warp_sums[32];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < n; base += blockDim.x) {
+    uint32_t i = base + threadIdx.x;
+    uint32_t x = i < n ? v[i] : 0;
+    uint32_t incl = x;
+    for (int o = 1; o < 32; o <<= 1) { uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o); if ((threadIdx.x & 31) >= o) incl += y; }
+    if ((threadIdx.x & 31) == 31) warp_sums[threadIdx.x >> 5] = incl;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      uint32_t ws = threadIdx.x < (blockDim.x >> 5) ? warp_sums[threadIdx.x] : 0;
+      for (int o = 1; o < 32; o <<= 1) { uint32_t y = __shfl_up_sync(0xFFFFFFFFu, ws, o); if (threadIdx.x >= o) ws += y; }
+      warp_sums[threadIdx.x] = ws;
+    }
+    __syncthreads();
+    uint32_t wpre = (threadIdx.x >> 5) ? warp_sums[(threadIdx.x >> 5) - 1] : 0;
+    uint32_t excl = carry + wpre + incl - x;
+    if (i < n) v[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = excl + x;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void cand_scatter_kernel(const ColCall* call, uint32_t n, const uint32_t* block_offsets, uint32_t* out) {
+  __shared__ uint32_t warp_base[32];
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool f = i < n && (call[i].flags & (kCandidate | kSlots | kRecompute));
+  unsigned m = __ballot_sync(0xFFFFFFFFu, f);
+  if ((threadIdx.x & 31) == 0) warp_base[threadIdx.x >> 5] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t acc = 0;
+    for (uint32_t w = 0; w < (blockDim.x >> 5); w++) { uint32_t x = warp_base[w]; warp_base[w] = acc; acc += x; }
+  }
+  __syncthreads();
+  if (f) out[block_offsets[blockIdx.x] + warp_base[threadIdx.x >> 5] + __popc(m & ((1u << (threadIdx.x & 31)) - 1))] = i;
+}
+
+// ============================================================================ pass 2: candidates
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  return v;
+}
+__device__ __forceinline__ uint32_t warp_sum_u(uint32_t v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+
+// Entries of the per-warp gather list (uint4): x = read index, y = qpos | (on_base_indel + 1) << 16,
+// z = likelihood class for the current slot (0xFFFFFFFF = not scored), w = obs | q << 8 | strand << 16.
+// E-step sweep of fit_allele_frequencies / profile_log10_likelihood: sum_w[b] over the reads at the
+// given frequencies (allowed alleles only).  Returns the per-warp totals in all lanes.
+__device__ void em_sweep(const uint4* ents, uint32_t m, const ClassTable& T, const double f[5], unsigned allowed,
+                         double sw[5]) {
+  double a[5] = {0, 0, 0, 0, 0};
+  for (uint32_t i = threadIdx.x & 31; i < m; i += 32) {
+    const uint32_t cls = ents[i].z;
+    if (cls == 0xFFFFFFFFu) continue;
+    const double* r = T.r64 + (size_t)cls * 5;
+    double p[5], s = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) { p[b] = ((allowed >> b) & 1) ? f[b] * __ldg(r + b) : 0.0; s += p[b]; }
+    if (s > 0.0) {
+      const double inv = 1.0 / s;
+#pragma unroll
+      for (int b = 0; b < 5; b++) a[b] += p[b] * inv;
+    } else {
+#pragma unroll
+      for (int b = 0; b < 5; b++) if ((allowed >> b) & 1) a[b] += f[b];
+    }
+  }
+#pragma unroll
+  for (int b = 0; b < 5; b++) sw[b] = warp_sum(a[b]);
+}
+
+__device__ double em_loglik(const uint4* ents, uint32_t m, const ClassTable& T, const double f[5], unsigned allowed) {
+  double ll = 0;
+  for (uint32_t i = threadIdx.x & 31; i < m; i += 32) {
+    const uint32_t cls = ents[i].z;
+    if (cls == 0xFFFFFFFFu) continue;
+    const double* r = T.r64 + (size_t)cls * 5;
+    double s = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) if ((allowed >> b) & 1) s += f[b] * __ldg(r + b);
+    if (s > 0.0) ll += log10(s) + __ldg(T.lpmax64 + cls);
+  }
+  return warp_sum(ll);
+}
+
+struct Fit { double f[5]; double ll; };
+
+// fit_allele_frequencies (identify_mutations.cpp:3241-3318).  The log-likelihood the reference
+// commits is the one evaluated at the frequencies entering the final iteration, so it is computed
+// once, after convergence, at those frequencies.
+__device__ Fit em_fit(const uint4* ents, uint32_t m, uint32_t n, const uint32_t obs_count[5], const ClassTable& T,
+                      unsigned allowed, double tol) {
+  Fit F;
+  double f[5] = {0, 0, 0, 0, 0}, fprev[5];
+  double tot = 0;
+#pragma unroll
+  for (int b = 0; b < 5; b++) if ((allowed >> b) & 1) { f[b] = 0.5 + (double)obs_count[b]; }
+#pragma unroll
+  for (int b = 0; b < 5; b++) tot += f[b];
+#pragma unroll
+  for (int b = 0; b < 5; b++) f[b] /= tot;
+  for (int it = 1; it <= 50; it++) {
+    double sw[5];
+    em_sweep(ents, m, T, f, allowed, sw);
+    double md = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) {
+      fprev[b] = f[b];
+      if (!((allowed >> b) & 1)) continue;
+      const double fn = sw[b] / (double)n;
+      md = fmax(md, fabs(fn - f[b]));
+      f[b] = fn;
+    }
+    if (md < tol) break;
+  }
+  F.ll = em_loglik(ents, m, T, fprev, allowed);
+#pragma unroll
+  for (int b = 0; b < 5; b++) F.f[b] = f[b];
+  return F;
+}
+
+// profile_log10_likelihood (identify_mutations.cpp:3094-3143)
+__device__ double em_profile(const uint4* ents, uint32_t m, const ClassTable& T, const double full[5], int v,
+                             double ff, double tol) {
+  double f[5], fprev[5], other = 0;
+#pragma unroll
+  for (int b = 0; b < 5; b++) if (b != v) other += full[b];
+#pragma unroll
+  for (int b = 0; b < 5; b++) f[b] = (b == v) ? ff : ((other > 0.0) ? (1.0 - ff) * full[b] / other : (1.0 - ff) / 4.0);
+  for (int it = 0; it < 50; it++) {
+    double sw[5];
+    em_sweep(ents, m, T, f, 31u, sw);
+    double others = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) if (b != v) others += sw[b];
+    double md = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) {
+      fprev[b] = f[b];
+      if (b == v) continue;
+      const double fn = (others > 0.0) ? (1.0 - ff) * sw[b] / others : (1.0 - ff) / 4.0;
+      md = fmax(md, fabs(fn - f[b]));
+      f[b] = fn;
+    }
+    if (md < tol) break;
+  }
+  return em_loglik(ents, m, T, fprev, 31u);
+}
+
+__device__ __forceinline__ int am_major(const double f[5], uint32_t n) {
+  if (n == 0) return 5;
+  int best = 0;
+  for (int b = 1; b < 5; b++) if (f[b] > f[best]) best = b;
+  return f[best] > 0.0 ? best : 5;
+}
+__device__ __forceinline__ int am_next(const double f[5], uint32_t n, int excl) {
+  if (n == 0) return 5;
+  const double thr = 0.5 / (double)n;
+  int best = 5;
+  for (int b = 0; b < 5; b++) {
+    if (b == excl || f[b] < thr) continue;
+    if (best == 5 || f[b] > f[best]) best = b;
+  }
+  return best;
+}
+
+// One warp per candidate column: gathers the column's reads in BAM order into a per-warp scratch
+// list, then for insert slot 0 (when flagged) and every insert slot that exists, scores the slot in
+// FP64: summed log10 likelihoods and pure-genotype call, the five-allele EM, the variant-presence
+// EM, and for emitted RA items the profile-likelihood bounds and the strand / quality tallies.
+__global__ void __launch_bounds__(128) im_candidate_kernel(DevSample S, ClassTable T, CandArgs A) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  uint4* ents = A.scratch + (size_t)gw * A.scratch_per_warp;
+  const uint32_t cap = A.scratch_per_warp;
+  for (;;) {
+    uint32_t idx = 0;
+    if (lane == 0) idx = atomicAdd(A.next, 1u);
+    idx = __shfl_sync(0xFFFFFFFFu, idx, 0);
+    if (idx >= A.n_cand) break;
+    const uint32_t c = A.cand[idx];
+    const ColCall cl0 = A.call[c];
+    // ---- gather covering reads in BAM order
+    const uint2 rr = __ldg(S.tile_range + (c >> 5));
+    uint32_t m = 0;
+    bool overflow = false;
+    for (uint32_t b0 = rr.x; b0 < rr.y; b0 += 32) {
+      const uint32_t r = b0 + lane;
+      bool ok = false;
+      Pile e;
+      DevRead rd;
+      if (r < rr.y) {
+        rd = S.reads[r];
+        ok = !(rd.flags & kSkip) && c >= rd.start && c < rd.end;
+        if (ok) resolve(S, rd, c, e);
+      }
+      const unsigned bal = __ballot_sync(0xFFFFFFFFu, ok);
+      const uint32_t slot = m + __popc(bal & ((1u << lane) - 1));
+      if (ok && slot < cap) {
+        const int obi = e.del ? -1 : max(e.indel, 0);
+        ents[slot] = make_uint4(r, (uint32_t)e.qpos | ((uint32_t)(obi + 1) << 16), 0xFFFFFFFFu, 0);
+      }
+      m += __popc(bal);
+    }
+    if (m > cap) { overflow = true; m = cap; }
+    if (overflow) { if (lane == 0) atomicOr(A.err, kErrScratch); continue; }
+    __syncwarp();
+    const bool do_slot0 = cl0.flags & (kCandidate | kRecompute);
+    int k = do_slot0 ? 0 : 1;
+    const uint8_t refc0 = __ldg(S.ref + c);
+    for (;; k++) {
+      // ---- build the slot's read bases (identify_mutations.cpp:1392-1658)
+      uint32_t pc[5][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+      uint32_t n_local = 0;
+      bool next_local = false;
+      double s64[5] = {0, 0, 0, 0, 0};
+      for (uint32_t i = lane; i < m; i += 32) {
+        uint4 en = ents[i];
+        en.z = 0xFFFFFFFFu;
+        const uint32_t r = en.x;
+        const DevRead rd = S.reads[r];
+        const int qpos = (int)(en.y & 0xFFFF);
+        const int obi = (int)(en.y >> 16) - 1;
+        const bool rev = rd.flags & kRev;
+        uint8_t base = '.';
+        bool past = true;
+        if (obi >= k) { base = nib_at(S.seq, rd.seq_off + qpos + k); past = false; }
+        if (base != 15) {
+          const bool red = rd.flags & kRedundant;
+          if (!red && obi > k) next_local = true;
+          if (!red && !is_trimmed(rd, qpos, past)) {
+            int qp = qpos;
+            bool ok = true;
+            if (obi == -1) {
+              qp += 1 - (int)rev;
+              if (qp >= (int)rd.len || nib_at(S.seq, rd.seq_off + qp) == 15) ok = false;
+            } else if (k > 0) {
+              int mo = k < obi ? k : obi;
+              qp += mo + 1 - (int)rev;
+              if (qp > bounds_end0(S, rd, r) || nib_at(S.seq, rd.seq_off + qp) == 15) ok = false;
+            }
+            if (ok) {
+              const int obs = (base == '.') ? 4 : bam_idx(base);
+              const uint32_t q = __ldg(S.qual + rd.seq_off + qp);
+              const uint32_t rs = rd.rfile;
+              if (obs < 0 || q >= T.Q || rs >= T.R) ok = false;
+              else if (q >= A.base_quality_cutoff) {
+                const uint32_t cls = ((((uint32_t)rd.mapq_idx * T.R + rs) * 2u + (rev ? 1u : 0u)) * T.Q + q) * 5u + (uint32_t)obs;
+                en.z = cls;
+                en.w = (uint32_t)obs | (q << 8) | ((rev ? 1u : 0u) << 16);
+                pc[obs][rev ? 1 : 0]++;
+                n_local++;
+                const double* lp = T.lp64 + (size_t)cls * 5;
+#pragma unroll
+                for (int b = 0; b < 5; b++) s64[b] += __ldg(lp + b);
+              }
+            }
+          }
+        }
+        ents[i] = en;
+      }
+      __syncwarp();
+      const uint32_t n = warp_sum_u(n_local);
+      const bool next_exists = __any_sync(0xFFFFFFFFu, next_local);
+      uint32_t cnt[5];
+      uint32_t pinfo[5][2];
+#pragma unroll
+      for (int b = 0; b < 5; b++) {
+        pinfo[b][0] = warp_sum_u(pc[b][0]);
+        pinfo[b][1] = warp_sum_u(pc[b][1]);
+        cnt[b] = pinfo[b][0] + pinfo[b][1];
+        s64[b] = warp_sum(s64[b]);
+      }
+      const uint8_t refc = (k == 0) ? refc0 : (uint8_t)'.';
+      const int ref_idx = (refc == '.') ? 4 : (chr_idx(refc) < 0 ? 5 : chr_idx(refc));
+      // ---- pure genotype call (identify_mutations.cpp:3398-3433)
+      int best = 5;
+      double cscore = __longlong_as_double(0x7ff8000000000000ll);
+      if (n > 0) {
+        best = 0;
+        for (int b = 1; b < 5; b++) if (s64[b] > s64[best]) best = b;
+        double off = -DBL_MAX;
+        for (int b = 0; b < 5; b++) if (b != best) off = fmax(off, s64[b]);
+        double te = 0;
+        for (int b = 0; b < 5; b++) if (b != best) te += exp10(s64[b] - off);
+        cscore = s64[best] - (log10(te) + off) - A.log10_ref_len;
+      }
+      if (k == 0 && (cl0.flags & kRecompute) && lane == 0) {
+        ColCall cl = cl0;
+        cl.best = (uint8_t)best;
+        cl.score = cscore;
+        cl.flags = (uint8_t)((cl.flags & ~kBasePredicted) | ((cscore >= A.mutation_cutoff) ? kBasePredicted : 0));
+        A.call[c] = cl;
+      }
+      const bool passed_cons = (best != ref_idx) && !isnan(cscore) && cscore > 0;
+      // ---- five-allele fit and variant presence (identify_mutations.cpp:1795-1821)
+      Fit full;
+      for (int b = 0; b < 5; b++) full.f[b] = 0;
+      full.ll = 0;
+      int maj = 5, mnr = 5, var = 5;
+      double vscore = __longlong_as_double(0x7ff8000000000000ll);
+      bool passed_poly = false;
+      if (n > 0) {
+        full = em_fit(ents, m, n, cnt, T, 31u, A.precision_decimal);
+        maj = am_major(full.f, n);
+        mnr = am_next(full.f, n, maj);
+        var = am_next(full.f, n, ref_idx);
+        if (var != 5) {
+          Fit nf = em_fit(ents, m, n, cnt, T, 31u & ~(1u << var), A.precision_decimal);
+          vscore = (full.ll - nf.ll) - A.log10_ref_len;
+          passed_poly = vscore >= A.poly_cutoff;
+        }
+      }
+      if (passed_cons || passed_poly) {
+        // ---- write_RA_frequency_bounds (identify_mutations.cpp:3175-3217)
+        double lower = 0.0, upper = 1.0;
+        if (n > 0 && var < 5) {
+          const double D = 0.587566;
+          const double fh = full.f[var];
+          const double tol = A.precision_decimal;
+          const double target = em_profile(ents, m, T, full.f, var, fh, tol) - D;
+          if (em_profile(ents, m, T, full.f, var, 0.0, tol) >= target) lower = 0.0;
+          else {
+            double lo = 0.0, hi = fh;
+            for (int i = 0; i < 40 && (hi - lo) > tol; i++) {
+              double mid = 0.5 * (lo + hi);
+              if (em_profile(ents, m, T, full.f, var, mid, tol) >= target) hi = mid; else lo = mid;
+            }
+            lower = hi;
+          }
+          if (em_profile(ents, m, T, full.f, var, 1.0, tol) >= target) upper = 1.0;
+          else {
+            double lo = fh, hi = 1.0;
+            for (int i = 0; i < 40 && (hi - lo) > tol; i++) {
+              double mid = 0.5 * (lo + hi);
+              if (em_profile(ents, m, T, full.f, var, mid, tol) >= target) lo = mid; else hi = mid;
+            }
+            upper = lo;
+          }
+        }
+        uint32_t slot = 0;
+        if (lane == 0) slot = atomicAdd(A.n_ra, 1u);
+        slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+        if (slot < A.ra_cap) {
+          if (lane == 0) {
+            RaDev o;
+            o.col = c; o.insert_position = (uint32_t)k;
+            o.score = vscore; o.consensus_score = cscore;
+            for (int b = 0; b < 5; b++) { o.f[b] = full.f[b]; o.pos_info[b][0] = pinfo[b][0]; o.pos_info[b][1] = pinfo[b][1]; }
+            o.lower = lower; o.upper = upper; o.n = n;
+            o.ref_idx = (uint8_t)ref_idx; o.var_idx = (uint8_t)var; o.maj_idx = (uint8_t)maj; o.min_idx = (uint8_t)mnr;
+            o.passed_cons = passed_cons; o.passed_poly = passed_poly; o.pad[0] = o.pad[1] = 0;
+            A.ra[slot] = o;
+          }
+          // qualities of the major and minor alleles' reads for the K-S test (:3009-3033)
+          uint32_t* qh = A.qhist + (size_t)slot * 2 * A.Qhist;
+          for (uint32_t i = lane; i < 2 * A.Qhist; i += 32) qh[i] = 0;
+          __syncwarp();
+          for (uint32_t i = lane; i < m; i += 32) {
+            const uint4 en = ents[i];
+            if (en.z == 0xFFFFFFFFu) continue;
+            const int obs = (int)(en.w & 0xFF);
+            const uint32_t q = (en.w >> 8) & 0xFF;
+            if (q >= A.Qhist) continue;
+            if (obs == maj) atomicAdd(qh + q, 1u);
+            if (obs == mnr) atomicAdd(qh + A.Qhist + q, 1u);
+          }
+        } else if (lane == 0) {
+          atomicOr(A.err, kErrRaOverflow);
+        }
+      }
+      if (!next_exists) break;
+      __syncwarp();
+    }
+    __syncwarp();
+  }
+}
+
+// ============================================================================ launch wrappers
+static int grid_for(uint32_t work, int per_block, int sms, int min_blocks_per_sm) {
+  long g = ((long)work + per_block - 1) / per_block;
+  long cap = (long)sms * min_blocks_per_sm;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st) {
+  if (in.n == 0) return cudaSuccess;
+  pack_reads_kernel<<<(in.n + 255) / 256, 256, 0, st>>>(in, out);
+  return cudaGetLastError();
+}
+cudaError_t launch_mapq_index(DevRead* reads, const uint8_t* mapq, const uint8_t* map, uint32_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  mapq_index_kernel<<<(n + 255) / 256, 256, 0, st>>>(reads, mapq, map, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t n_tiles, uint32_t maxspan,
+                              uint2* tile_range, uint32_t* max_tile_reads, cudaStream_t st) {
+  tile_range_kernel<<<(n_tiles + 255) / 256, 256, 0, st>>>(rstart, n_reads, n_tiles, maxspan, tile_range, max_tile_reads);
+  return cudaGetLastError();
+}
+cudaError_t launch_ec(const DevSample& S, const EcArgs& A, int sms, cudaStream_t st) {
+  const size_t smem = (size_t)A.R * 25 * A.Q * sizeof(uint32_t);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(ec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const int grid = grid_for(S.n_tiles, 8, sms, 8);
+  ec_kernel<<<grid, 256, smem, st>>>(S, A);
+  return cudaGetLastError();
+}
+cudaError_t launch_im_column(const DevSample& S, const ClassTable& T, const ImArgs& A, int sms, cudaStream_t st) {
+  const int grid = grid_for(S.n_tiles, 8, sms, 8);
+  if (A.precision == 0) im_column_kernel<true><<<grid, 256, 0, st>>>(S, T, A);
+  else im_column_kernel<false><<<grid, 256, 0, st>>>(S, T, A);
+  return cudaGetLastError();
+}
+cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_counts, uint32_t* total, uint32_t* out,
+                           cudaStream_t st) {
+  const uint32_t nb = (n + 255) / 256;
+  cand_count_kernel<<<nb, 256, 0, st>>>(call, n, block_counts);
+  scan_kernel<<<1, 1024, 0, st>>>(block_counts, nb, total);
+  cand_scatter_kernel<<<nb, 256, 0, st>>>(call, n, block_counts, out);
+  return cudaGetLastError();
+}
+cudaError_t launch_candidates(const DevSample& S, const ClassTable& T, const CandArgs& A, int n_warps, cudaStream_t st) {
+  const int blocks = (n_warps + 3) / 4;
+  im_candidate_kernel<<<blocks, 128, 0, st>>>(S, T, A);
+  return cudaGetLastError();
+}
+
+}  // namespace bsq

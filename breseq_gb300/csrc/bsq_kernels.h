@@ -1,0 +1,52 @@
+// Launch wrappers of the scoring kernels (bsq_kernels.cu) for the host orchestration (bsq_abi.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bsq_common.h"
+
+namespace bsq {
+
+// Raw record arrays as uploaded from the caller's bsq_read_soa (device pointers).
+struct RawSoA {
+  const int32_t* tid;
+  const int32_t* pos;
+  const uint16_t* flag;
+  const uint8_t* mapq;
+  const uint32_t* x1;
+  const int32_t* xl;
+  const int32_t* xr;
+  const uint8_t* read_file;
+  const uint32_t* l_qseq;
+  const uint64_t* seq_off;
+  const uint64_t* cigar_off;
+  const uint16_t* n_cigar;
+  const uint32_t* cigar;
+  const uint32_t* tpoff;     // padded target offsets
+  uint32_t n;
+  uint32_t n_targets;
+  uint64_t n_bases;
+  uint64_t n_cigar_total;
+};
+
+struct PackOut {
+  DevRead* reads;
+  QBounds* qb;
+  uint32_t* rstart;
+  uint8_t* mapq;
+  uint32_t* err;
+  uint32_t* maxspan;
+  uint32_t* mapq_mask;       // [8] presence bits of MAPQ values
+};
+
+cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st);
+cudaError_t launch_mapq_index(DevRead* reads, const uint8_t* mapq, const uint8_t* map, uint32_t n, cudaStream_t st);
+cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t n_tiles, uint32_t maxspan,
+                              uint2* tile_range, uint32_t* max_tile_reads, cudaStream_t st);
+cudaError_t launch_ec(const DevSample& S, const EcArgs& A, int sms, cudaStream_t st);
+cudaError_t launch_im_column(const DevSample& S, const ClassTable& T, const ImArgs& A, int sms, cudaStream_t st);
+cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_counts, uint32_t* total, uint32_t* out,
+                           cudaStream_t st);
+cudaError_t launch_candidates(const DevSample& S, const ClassTable& T, const CandArgs& A, int n_warps, cudaStream_t st);
+
+}  // namespace bsq

@@ -1,0 +1,459 @@
+"""Seeded synthetic genomes and aligned reads in the packed record layout of the library.
+
+There is no aligner and no public data set here, so reads are simulated together with their true
+alignment, the way breseq's own SIMULATE-READS command draws them (src/breseq/fastq.cpp:1301-1459)
+but with the quality law of the scoring benchmarks: Q_i ~ N(36 - 8 i / L, 4) rounded and clipped to
+[2, 41] in sequencing order, and a substitution to a uniformly chosen other base with probability
+10^(-Q/10).  Tags follow breseq's reference.bam conventions (src/breseq/alignment.cpp:915-945):
+X1 = number of equally good locations (reads inside repeat copies are written at every copy, with
+MAPQ 0), XL/XR trims present on every record, and the read group + mate flag giving the read file.
+
+Everything is numpy; generation is chunked so the 4.8 Mb x 200x workload stays within a few GB.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import dataclasses
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+BASES = np.frombuffer(b"ACGT", dtype=np.uint8)
+# ASCII -> 4-bit BAM code
+_ASCII2BAM = np.full(256, 15, dtype=np.uint8)
+for _c, _v in zip(b"ACGTN", (1, 2, 4, 8, 15)):
+    _ASCII2BAM[_c] = _v
+BAM_M, BAM_I, BAM_D, BAM_S = 0, 1, 2, 4
+FLAG_PAIRED, FLAG_PROPER, FLAG_REVERSE, FLAG_MREVERSE, FLAG_READ1, FLAG_READ2 = 0x1, 0x2, 0x10, 0x20, 0x40, 0x80
+
+
+@dataclass
+class ReadFileSet:
+    """One read group: single-end (one read file) or paired-end (two files, R1 then R2)."""
+    coverage: float            # fold coverage contributed by EACH file of the set
+    read_length: int
+    paired: bool = False
+    insert_mean: float = 350.0
+    insert_sd: float = 50.0
+
+
+@dataclass
+class SimConfig:
+    seed: int = 1
+    target_lengths: tuple = (48502,)
+    target_names: tuple | None = None
+    gc: float = 0.5
+    n_snps: int = 25
+    n_indels: int = 5
+    max_indel: int = 1
+    # population mode: variant frequencies log-uniform in [freq_min, 1]; clonal when None
+    freq_min: float | None = None
+    repeat_copies: int = 0
+    repeat_length: int = 1300
+    read_sets: tuple = (ReadFileSet(coverage=125.0, read_length=101),)
+    strand_bias_sites: int = 0
+    low_quality_sites: int = 0
+    # rates of features that exercise the rarer branches of the scoring path
+    trim_fraction: float = 0.0      # reads with non-zero XL/XR
+    softclip_fraction: float = 0.0  # reads with a soft clip at one end
+    n_base_rate: float = 0.0        # read bases replaced by N (quality 2)
+    low_mapq_fraction: float = 0.0  # unique reads with MAPQ drawn in [20, 41]
+    chunk_reads: int = 400_000
+
+
+@dataclass
+class Sample:
+    """Reference + coordinate-sorted records, in the bsq_reference / bsq_read_soa layout."""
+    ref_seq: np.ndarray            # uint8 ASCII, all targets concatenated
+    target_offset: np.ndarray      # uint64 [T+1]
+    target_names: list
+    coverage_group: np.ndarray     # uint32 [T]
+    n_coverage_groups: int
+    target_order: np.ndarray       # uint32: lexicographic seq_id order
+    tid: np.ndarray
+    pos: np.ndarray
+    flag: np.ndarray
+    mapq: np.ndarray
+    x1: np.ndarray
+    xl: np.ndarray
+    xr: np.ndarray
+    read_file: np.ndarray
+    read_group: np.ndarray
+    l_qseq: np.ndarray
+    seq_off: np.ndarray
+    cigar_off: np.ndarray
+    n_cigar: np.ndarray
+    cigar: np.ndarray
+    seq: np.ndarray                # packed 4-bit, high nibble first
+    qual: np.ndarray
+    n_read_files: int
+    n_quality: int
+    variants: list = field(default_factory=list)
+
+    @property
+    def n_reads(self) -> int:
+        return int(self.tid.shape[0])
+
+    def aligned_bases(self) -> int:
+        """Aligned read-bases (M/=/X + I lengths) over records the pileup keeps: the unit of work."""
+        ops = self.cigar & 0xF
+        lens = (self.cigar >> 4).astype(np.int64)
+        keep = (self.flag & 0x704) == 0
+        per_op = np.where((ops == 0) | (ops == 1) | (ops == 7) | (ops == 8), lens, 0)
+        owner = np.repeat(np.arange(self.n_reads), self.n_cigar.astype(np.int64))
+        return int(per_op[keep[owner]].sum())
+
+    def total_length(self) -> int:
+        return int(self.target_offset[-1])
+
+
+def _lexicographic_order(names):
+    return np.array(sorted(range(len(names)), key=lambda i: names[i]), dtype=np.uint32)
+
+
+_ERR_LUT = np.power(10.0, -np.arange(256, dtype=np.float64) / 10.0).astype(np.float32)
+_CODE2BAM = np.array([1, 2, 4, 8], dtype=np.uint8)
+
+
+def _quality_table(L):
+    """[L, 65536] inverse-CDF tables: quality at read position i for a uniform 16-bit draw, following
+    Q_i ~ N(36 - 8 i / L, 4) rounded to the nearest integer and clipped to [2, 41]."""
+    from math import erf, sqrt
+    qs = np.arange(2, 42)
+    u = (np.arange(65536) + 0.5) / 65536.0
+    tab = np.empty((L, 65536), dtype=np.uint8)
+    for i in range(L):
+        mu = 36.0 - 8.0 * i / L
+        # P(round(X) <= q) = Phi((q + 0.5 - mu) / 4); clipping moves the tails onto 2 and 41
+        cdf = np.array([0.5 * (1 + erf((q + 0.5 - mu) / (4.0 * sqrt(2.0)))) for q in qs])
+        cdf[-1] = 1.0
+        tab[i] = qs[np.searchsorted(cdf, u, side="right").clip(0, len(qs) - 1)]
+    return tab
+
+
+def simulate(cfg: SimConfig) -> Sample:
+    rng = np.random.default_rng(cfg.seed)
+    T = len(cfg.target_lengths)
+    names = list(cfg.target_names) if cfg.target_names else [f"seq{t + 1}" for t in range(T)]
+    lens = np.array(cfg.target_lengths, dtype=np.int64)
+    toff = np.zeros(T + 1, dtype=np.uint64)
+    toff[1:] = np.cumsum(lens)
+    total = int(toff[-1])
+    # ---------------------------------------------------------------- reference
+    probs = np.array([(1 - cfg.gc) / 2, cfg.gc / 2, cfg.gc / 2, (1 - cfg.gc) / 2])
+    ref = BASES[rng.choice(4, size=total, p=probs)]
+    repeat_spans = []
+    if cfg.repeat_copies > 1:
+        L0 = int(lens[0])
+        seg = BASES[rng.choice(4, size=cfg.repeat_length, p=probs)]
+        slots = np.sort(rng.choice(L0 // (cfg.repeat_length * 3), size=cfg.repeat_copies, replace=False))
+        for s in slots:
+            p0 = int(s) * cfg.repeat_length * 3 + cfg.repeat_length
+            ref[p0:p0 + cfg.repeat_length] = seg
+            repeat_spans.append((0, p0, p0 + cfg.repeat_length))
+    # ---------------------------------------------------------------- variants
+    def _in_repeat(t, p, margin):
+        return any(t == rt and rs - margin <= p < re + margin for rt, rs, re in repeat_spans)
+
+    variants = []   # dict(tid, pos, kind, alt/len, freq, artifact)
+    taken = set()
+    def _pick_site(margin=8):
+        for _ in range(10000):
+            t = int(rng.choice(T, p=lens / lens.sum()))
+            p = int(rng.integers(200, max(201, int(lens[t]) - 400)))
+            if _in_repeat(t, p, 200) or any((t, q) in taken for q in range(p - margin, p + margin)):
+                continue
+            taken.add((t, p))
+            return t, p
+        raise RuntimeError("no free site")
+
+    def _freq():
+        if cfg.freq_min is None:
+            return 1.0
+        return float(np.exp(rng.uniform(np.log(cfg.freq_min), 0.0)))
+
+    for _ in range(cfg.n_snps):
+        t, p = _pick_site()
+        r = ref[toff[t] + p]
+        alt = BASES[rng.choice([b for b in range(4) if BASES[b] != r])]
+        variants.append(dict(tid=t, pos=p, kind="snp", alt=int(alt), freq=_freq()))
+    for _ in range(cfg.n_indels):
+        t, p = _pick_site(margin=8 + cfg.max_indel)
+        k = int(rng.integers(1, cfg.max_indel + 1))
+        if rng.random() < 0.5:
+            variants.append(dict(tid=t, pos=p, kind="del", length=k, freq=_freq()))
+        else:
+            ins = BASES[rng.integers(0, 4, size=k)]
+            variants.append(dict(tid=t, pos=p, kind="ins", seq=ins, freq=_freq()))
+    for _ in range(cfg.strand_bias_sites):
+        t, p = _pick_site()
+        r = ref[toff[t] + p]
+        alt = BASES[rng.choice([b for b in range(4) if BASES[b] != r])]
+        variants.append(dict(tid=t, pos=p, kind="strand_bias", alt=int(alt), freq=0.15, strand=int(rng.integers(0, 2))))
+    for _ in range(cfg.low_quality_sites):
+        t, p = _pick_site()
+        r = ref[toff[t] + p]
+        alt = BASES[rng.choice([b for b in range(4) if BASES[b] != r])]
+        variants.append(dict(tid=t, pos=p, kind="low_quality", alt=int(alt), freq=0.10))
+
+    # ---------------------------------------------------------------- read placement
+    recs = {k: [] for k in ("tid", "pos", "flag", "rfile", "rg", "L", "clipL", "clipR", "x1", "group")}
+    rfile_base = 0
+    max_indel_span = cfg.max_indel + 1
+    group_counter = 0
+    for gi, rs in enumerate(cfg.read_sets):
+        L = rs.read_length
+        n_frag = int(round(rs.coverage * total / L))
+        tids = rng.choice(T, size=n_frag, p=lens / lens.sum())
+        if rs.paired:
+            ins = np.clip(np.rint(rng.normal(rs.insert_mean, rs.insert_sd, n_frag)), L, None).astype(np.int64)
+        else:
+            ins = np.full(n_frag, L, dtype=np.int64)
+        hi = lens[tids] - ins - max_indel_span
+        start = (rng.random(n_frag) * np.maximum(hi, 1)).astype(np.int64)
+        fwd = rng.random(n_frag) < 0.5
+        mates = [(start, ~fwd, 0)] if not rs.paired else [(start, ~fwd, 0), (start + ins - L, fwd, 1)]
+        for p_arr, rev, mate in mates:
+            # in a pair, mate 0 takes the fragment's strand, mate 1 the opposite
+            flag = np.where(rev, FLAG_REVERSE, 0).astype(np.uint16)
+            if rs.paired:
+                flag |= FLAG_PAIRED | FLAG_PROPER | (FLAG_READ1 if mate == 0 else FLAG_READ2)
+                flag |= np.where(~rev, FLAG_MREVERSE, 0).astype(np.uint16)
+            recs["tid"].append(tids); recs["pos"].append(p_arr); recs["flag"].append(flag)
+            recs["rfile"].append(np.full(n_frag, rfile_base + mate, dtype=np.uint8))
+            recs["rg"].append(np.full(n_frag, gi, dtype=np.uint16))
+            recs["L"].append(np.full(n_frag, L, dtype=np.int64))
+            recs["group"].append(np.arange(group_counter, group_counter + n_frag))
+            group_counter += n_frag
+        rfile_base += 2 if rs.paired else 1
+    tid = np.concatenate(recs["tid"]).astype(np.int32)
+    pos = np.concatenate(recs["pos"]).astype(np.int64)
+    flag = np.concatenate(recs["flag"])
+    rfile = np.concatenate(recs["rfile"])
+    rg = np.concatenate(recs["rg"])
+    L_arr = np.concatenate(recs["L"])
+    n = tid.shape[0]
+    mapq = np.full(n, 42, dtype=np.uint8)
+    if cfg.low_mapq_fraction > 0:
+        m = rng.random(n) < cfg.low_mapq_fraction
+        mapq[m] = rng.integers(20, 42, size=int(m.sum())).astype(np.uint8)
+    x1 = np.ones(n, dtype=np.uint32)
+    clip_l = np.zeros(n, dtype=np.int64)
+    clip_r = np.zeros(n, dtype=np.int64)
+    if cfg.softclip_fraction > 0:
+        m = rng.random(n) < cfg.softclip_fraction
+        k = rng.integers(1, 11, size=n)
+        left = rng.random(n) < 0.5
+        clip_l[m & left] = k[m & left]
+        clip_r[m & ~left] = k[m & ~left]
+    # reads fully inside a repeat copy map equally well to every copy
+    src_index = np.arange(n)
+    if repeat_spans:
+        inside = np.zeros(n, dtype=bool)
+        which = np.full(n, -1)
+        for ci, (rt, rs0, re0) in enumerate(repeat_spans):
+            m = (tid == rt) & (pos >= rs0) & (pos + L_arr <= re0)
+            inside |= m
+            which[m] = ci
+        idx = np.nonzero(inside)[0]
+        ncp = len(repeat_spans)
+        x1[idx] = ncp
+        mapq[idx] = 0
+        extra_src = np.repeat(idx, ncp - 1)
+        extra_pos = []
+        for i0 in idx:
+            off = pos[i0] - repeat_spans[which[i0]][1]
+            for cj, (rt, rs0, re0) in enumerate(repeat_spans):
+                if cj != which[i0]:
+                    extra_pos.append(rs0 + off)
+        extra_pos = np.array(extra_pos, dtype=np.int64)
+        clip_l[idx] = 0
+        clip_r[idx] = 0
+
+        def ext(a, v=None):
+            return np.concatenate([a, a[extra_src] if v is None else v])
+        tid = ext(tid); flag = ext(flag); rfile = ext(rfile); rg = ext(rg); L_arr = ext(L_arr)
+        mapq = ext(mapq); x1 = ext(x1); clip_l = ext(clip_l); clip_r = ext(clip_r)
+        pos = ext(pos, extra_pos)
+        src_index = np.concatenate([src_index, extra_src])
+        n = tid.shape[0]
+    # soft clipped reads start later on the reference by the left clip
+    pos = pos + clip_l
+    order = np.lexsort((pos, tid))
+    tid, pos, flag, rfile, rg, L_arr = tid[order], pos[order], flag[order], rfile[order], rg[order], L_arr[order]
+    mapq, x1, clip_l, clip_r, src_index = mapq[order], x1[order], clip_l[order], clip_r[order], src_index[order]
+    xl = np.zeros(n, dtype=np.int32)
+    xr = np.zeros(n, dtype=np.int32)
+    if cfg.trim_fraction > 0:
+        m = rng.random(n) < cfg.trim_fraction
+        xl[m] = rng.integers(0, 6, size=int(m.sum()))
+        xr[m] = rng.integers(0, 6, size=int(m.sum()))
+    xl = xl + clip_l.astype(np.int32)
+    xr = xr + clip_r.astype(np.int32)
+
+    # ---------------------------------------------------------------- read content
+    Lp = L_arr + (L_arr & 1)
+    seq_off = np.zeros(n, dtype=np.uint64)
+    seq_off[1:] = np.cumsum(Lp[:-1]).astype(np.uint64)
+    n_bases = int(Lp.sum())
+    qual = np.zeros(n_bases, dtype=np.uint8)
+    nib = np.zeros(n_bases, dtype=np.uint8)   # unpacked 4-bit codes
+    gpos = toff[tid].astype(np.int64) + pos
+    ref_code = np.searchsorted(BASES, ref).astype(np.uint8)          # A,C,G,T -> 0..3
+    chunk_seeds = np.random.SeedSequence([cfg.seed, 7]).spawn((n + cfg.chunk_reads - 1) // cfg.chunk_reads + 1)
+    qtabs = {}
+
+    def fill(ci):
+        c0 = ci * cfg.chunk_reads
+        c1 = min(n, c0 + cfg.chunk_reads)
+        crng = np.random.default_rng(chunk_seeds[ci])
+        for L in np.unique(L_arr[c0:c1]):
+            sel = np.nonzero(L_arr[c0:c1] == L)[0] + c0
+            m = len(sel)
+            L = int(L)
+            aligned = L - clip_l[sel] - clip_r[sel]
+            col = np.arange(L, dtype=np.int64)[None, :] - clip_l[sel][:, None]
+            inref = (col >= 0) & (col < aligned[:, None])
+            gidx = np.minimum(gpos[sel][:, None] + np.maximum(col, 0), total - 1)
+            code = ref_code[gidx]
+            rnd = crng.integers(0, 4, size=(m, L), dtype=np.uint8)
+            code = np.where(inref, code, rnd)
+            q = qtabs[L][np.arange(L)[None, :], crng.integers(0, 65536, size=(m, L), dtype=np.uint16)]
+            rev = (flag[sel] & FLAG_REVERSE) != 0
+            q[rev] = q[rev, ::-1]            # sequencing order runs right to left on the reverse strand
+            err = crng.random((m, L), dtype=np.float32) < _ERR_LUT[q]
+            shift = crng.integers(1, 4, size=(m, L), dtype=np.uint8)
+            code = np.where(err, (code + shift) & 3, code)
+            codes = _CODE2BAM[code]
+            if cfg.n_base_rate > 0:
+                nm = crng.random((m, L), dtype=np.float32) < cfg.n_base_rate
+                codes[nm] = 15
+                q[nm] = 2
+            off = seq_off[sel].astype(np.int64)[:, None] + np.arange(L)[None, :]
+            qual[off] = q
+            nib[off] = codes
+
+    for L in np.unique(L_arr):
+        qtabs[int(L)] = _quality_table(int(L))
+    n_chunks = (n + cfg.chunk_reads - 1) // cfg.chunk_reads
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        list(ex.map(fill, range(n_chunks)))
+    # ---------------------------------------------------------------- variants in reads
+    cigar_list = [None] * n
+    starts_sorted = gpos
+    reads_end = gpos + L_arr - clip_l - clip_r
+    for v in variants:
+        gp = int(toff[v["tid"]]) + v["pos"]
+        lo = np.searchsorted(starts_sorted, gp - int(L_arr.max()) - 4, side="left")
+        hi = np.searchsorted(starts_sorted, gp, side="right")
+        cand = np.arange(lo, hi)
+        cand = cand[(reads_end[cand] > gp) & (x1[cand] == 1)]
+        if cand.size == 0:
+            continue
+        kind = v["kind"]
+        if kind in ("snp", "strand_bias", "low_quality"):
+            carry = rng.random(cand.size) < v["freq"]
+            if kind == "strand_bias":
+                carry &= ((flag[cand] & FLAG_REVERSE) != 0) == bool(v["strand"])
+            cand = cand[carry]
+            qoff = gp - gpos[cand] + clip_l[cand]
+            idx = seq_off[cand].astype(np.int64) + qoff
+            nib[idx] = _ASCII2BAM[v["alt"]]
+            if kind == "low_quality":
+                qual[idx] = rng.integers(2, 16, size=cand.size).astype(np.uint8)
+            continue
+        # indels: rebuild each carrying read with its gapped alignment
+        for r in cand:
+            if clip_l[r] or clip_r[r] or rng.random() >= v["freq"]:
+                continue
+            L = int(L_arr[r])
+            a = gp - int(gpos[r])
+            o = int(seq_off[r])
+            if kind == "del":
+                k = v["length"]
+                if a < 1 or a > L - 1:
+                    continue
+                tail = ref[gp + k: gp + k + (L - a)]
+                nib[o + a: o + L] = _ASCII2BAM[tail]
+                cigar_list[r] = [(a << 4) | BAM_M, (k << 4) | BAM_D, ((L - a) << 4) | BAM_M]
+            else:
+                k = len(v["seq"])
+                if a < 1 or a > L - k - 1:
+                    continue
+                tail = np.concatenate([v["seq"], ref[gp: gp + (L - a - k)]])
+                nib[o + a: o + L] = _ASCII2BAM[tail]
+                cigar_list[r] = [(a << 4) | BAM_M, (k << 4) | BAM_I, ((L - a - k) << 4) | BAM_M]
+    # identical content for every copy of a redundant read
+    if repeat_spans:
+        first = {}
+        for r in np.nonzero(x1 > 1)[0]:
+            s = int(src_index[r])
+            if s in first:
+                f = first[s]
+                L = int(L_arr[r])
+                nib[int(seq_off[r]): int(seq_off[r]) + L] = nib[int(seq_off[f]): int(seq_off[f]) + L]
+                qual[int(seq_off[r]): int(seq_off[r]) + L] = qual[int(seq_off[f]): int(seq_off[f]) + L]
+            else:
+                first[s] = r
+    # ---------------------------------------------------------------- CIGARs
+    n_cigar = np.ones(n, dtype=np.uint16)
+    n_cigar[(clip_l > 0) | (clip_r > 0)] = 2
+    special = [r for r in range(n) if cigar_list[r] is not None]
+    for r in special:
+        n_cigar[r] = len(cigar_list[r])
+    cigar_off = np.zeros(n, dtype=np.uint64)
+    cigar_off[1:] = np.cumsum(n_cigar[:-1].astype(np.uint64))
+    cigar = np.zeros(int(n_cigar.astype(np.int64).sum()), dtype=np.uint32)
+    simple = n_cigar == 1
+    cigar[cigar_off[simple].astype(np.int64)] = (L_arr[simple].astype(np.uint32) << 4) | BAM_M
+    for side, arr in (("l", clip_l), ("r", clip_r)):
+        m = (arr > 0) & (n_cigar == 2)
+        o = cigar_off[m].astype(np.int64)
+        aligned = (L_arr[m] - arr[m]).astype(np.uint32)
+        if side == "l":
+            cigar[o] = (arr[m].astype(np.uint32) << 4) | BAM_S
+            cigar[o + 1] = (aligned << 4) | BAM_M
+        else:
+            cigar[o] = (aligned << 4) | BAM_M
+            cigar[o + 1] = (arr[m].astype(np.uint32) << 4) | BAM_S
+    for r in special:
+        o = int(cigar_off[r])
+        cigar[o:o + len(cigar_list[r])] = cigar_list[r]
+    # ---------------------------------------------------------------- pack nibbles
+    seq = ((nib[0::2] << 4) | nib[1::2]).astype(np.uint8)
+    n_read_files = sum(2 if rs.paired else 1 for rs in cfg.read_sets)
+    return Sample(
+        ref_seq=ref, target_offset=toff, target_names=names,
+        coverage_group=np.arange(T, dtype=np.uint32), n_coverage_groups=T,
+        target_order=_lexicographic_order(names),
+        tid=tid, pos=pos.astype(np.int32), flag=flag.astype(np.uint16), mapq=mapq, x1=x1,
+        xl=xl, xr=xr, read_file=rfile.astype(np.uint8), read_group=rg.astype(np.uint16),
+        l_qseq=L_arr.astype(np.uint32), seq_off=seq_off, cigar_off=cigar_off, n_cigar=n_cigar,
+        cigar=cigar, seq=seq, qual=qual, n_read_files=n_read_files, n_quality=42, variants=variants)
+
+
+# ------------------------------------------------------------------ benchmark workloads
+def config_clonal_small(seed=11) -> SimConfig:
+    """48,502-bp reference, 25 SNPs + 5 single-base indels, 60,000 single-end 101-bp reads (~125x)."""
+    return SimConfig(seed=seed, target_lengths=(48502,), gc=0.5, n_snps=25, n_indels=5, max_indel=1,
+                     read_sets=(ReadFileSet(coverage=60000 * 101 / 48502, read_length=101),))
+
+
+def config_ecoli(seed=21, scale=1.0, coverage=100.0) -> SimConfig:
+    """4.63 Mb chromosome + 100 kb + 60 kb plasmids, 50.8% GC, five 1.3-kb repeat copies, 300 SNPs and
+    40 indels of length <= 3, paired-end 150-bp reads (two read files, `coverage` x each)."""
+    lens = tuple(max(2000, int(x * scale)) for x in (4_630_000, 100_000, 60_000))
+    return SimConfig(seed=seed, target_lengths=lens, target_names=("chromosome", "plasmid1", "plasmid2"),
+                     gc=0.508, n_snps=max(3, int(300 * scale)), n_indels=max(2, int(40 * scale)), max_indel=3,
+                     repeat_copies=5, repeat_length=1300,
+                     read_sets=(ReadFileSet(coverage=coverage, read_length=150, paired=True),))
+
+
+def config_population(seed=31, scale=1.0, coverage=500.0) -> SimConfig:
+    """Same genome in polymorphism mode: 1000x paired-end 150 (500x per file), 400 variants at
+    frequencies log-uniform in [0.01, 1], 50 strand-biased and 50 low-quality-skewed sites."""
+    c = config_ecoli(seed=seed, scale=scale, coverage=coverage)
+    return dataclasses.replace(c, n_snps=max(4, int(360 * scale)), n_indels=max(2, int(40 * scale)),
+                               freq_min=0.01, strand_bias_sites=max(1, int(50 * scale)),
+                               low_quality_sites=max(1, int(50 * scale)))

@@ -1,0 +1,247 @@
+/*
+ * breseq_gb300.h -- C ABI of the GB300 read-evidence scoring library (libbsq_gb300.so).
+ *
+ * The library replaces the three passes of breseq's read-evidence scoring path:
+ *
+ *   error_count pileup      breseq: src/breseq/error_count.cpp:50-68 (error_count)
+ *                                   src/breseq/error_count.cpp:125-199 (error_count_pileup::pileup_callback)
+ *                                   src/breseq/error_count.cpp:854-986 (cErrorTable::count_alignment_position)
+ *   identify_mutations      breseq: src/breseq/identify_mutations.cpp:48-88 (identify_mutations)
+ *                                   src/breseq/identify_mutations.cpp:1309-2022 (pileup_callback)
+ *   coverage counts         breseq: src/breseq/error_count.cpp:239-253 (unique-only coverage histogram)
+ *                                   src/breseq/identify_mutations.cpp:2173-2250 (coverage table rows)
+ *
+ * The reference exposes these passes as two C++ free functions that read a BAM/FASTA pair.  Here the
+ * host decodes the alignments once into the struct-of-arrays record set `bsq_read_soa`, the library
+ * keeps it resident in device memory, and each pass is one call.  Every function returns BSQ_OK (0)
+ * or a negative status; the message is available from bsq_last_error().  No function exits the
+ * process or traps the device (the reference calls exit(1) from ASSERT, src/breseq/common.h:111-193;
+ * the C++ wrappers in breseq_gb300/csrc/bsq_host.hpp keep that convention for drop-in callers).
+ *
+ * A context is single-threaded.  Buffers passed in are borrowed for the duration of the call only.
+ */
+#ifndef BRESEQ_GB300_H
+#define BRESEQ_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define BSQ_OK               0
+#define BSQ_ERR_INVALID     -1   /* bad argument / unsorted records / malformed CIGAR            */
+#define BSQ_ERR_CUDA        -2   /* a CUDA runtime call failed                                    */
+#define BSQ_ERR_DATA        -3   /* data outside the table (covariate >= max, non-ACGTN base ...) */
+#define BSQ_ERR_NOMEM       -4   /* device memory exhausted / admission budget exceeded           */
+#define BSQ_ERR_SIZE        -5   /* caller buffer too small; required size returned               */
+#define BSQ_ERR_NOSAMPLE    -6   /* unknown sample id                                             */
+
+/* ---------------------------------------------------------------- BAM constants used by the path */
+#define BSQ_FLAG_PAIRED      0x1
+#define BSQ_FLAG_UNMAP       0x4
+#define BSQ_FLAG_REVERSE     0x10
+#define BSQ_FLAG_READ2       0x80
+#define BSQ_FLAG_SECONDARY   0x100
+#define BSQ_FLAG_QCFAIL      0x200
+#define BSQ_FLAG_DUP         0x400
+/* htslib's default pileup filter (BAM_DEF_MASK); breseq never overrides it
+ * (src/breseq/pileup_base.cpp:333-339). */
+#define BSQ_PILEUP_SKIP_MASK (BSQ_FLAG_UNMAP | BSQ_FLAG_SECONDARY | BSQ_FLAG_QCFAIL | BSQ_FLAG_DUP)
+
+/* ---------------------------------------------------------------- inputs */
+
+/* Reference sequences.  Replaces the FASTA/faidx load of pileup_base::pileup_base
+ * (src/breseq/pileup_base.cpp:61-88).  `seq` holds every target's bases, upper-case A/C/G/T/N,
+ * concatenated in BAM header order; target t occupies seq[target_offset[t] .. target_offset[t+1]). */
+typedef struct bsq_reference {
+    uint32_t        n_targets;
+    const uint64_t* target_offset;    /* n_targets + 1 */
+    const char*     seq;
+    /* coverage group of each target (Settings::seq_id_to_coverage_group, src/breseq/settings.cpp:224-258) */
+    const uint32_t* coverage_group;
+    uint32_t        n_coverage_groups;
+    /* targets to pile up, in processing order: the reference walks
+     * Settings::call_mutations_seq_id_set(), a std::set<string>, i.e. lexicographic seq_id order
+     * (src/breseq/pileup_base.cpp:364-385).  Targets not listed are not scored. */
+    const uint32_t* target_order;
+    uint32_t        n_target_order;
+} bsq_reference;
+
+/* Decoded alignments, one entry per BAM record, coordinate-sorted (tid, pos) in BAM order.
+ * Fields mirror the accessors of alignment_wrapper / pileup_wrapper (src/breseq/alignment.h:43-416).
+ * Read i's bases are the 4-bit BAM codes at nibble index seq_off[i] + q of `seq` (high nibble first,
+ * as in BAM), its qualities are qual[seq_off[i] + q]; seq_off[i] must be even.  CIGAR ops are the
+ * BAM encoding (len << 4 | op) at cigar[cigar_off[i] ..]. */
+typedef struct bsq_read_soa {
+    uint64_t        n_reads;
+    const int32_t*  tid;
+    const int32_t*  pos;           /* 0-based leftmost reference position                        */
+    const uint16_t* flag;
+    const uint8_t*  mapq;
+    const uint32_t* x1;            /* X1:i redundancy, 1 when the tag is absent (alignment.cpp:52-57) */
+    const int32_t*  xl;            /* XL:i left trim,  -1 when absent (alignment.h:389-411)        */
+    const int32_t*  xr;            /* XR:i right trim, -1 when absent                              */
+    const uint8_t*  read_file;     /* flat read-file index: read group + mate (alignment.h:576-592)*/
+    const uint16_t* read_group;    /* dense @RG index (alignment.h:533-573)                        */
+    const uint32_t* l_qseq;
+    const uint64_t* seq_off;
+    const uint64_t* cigar_off;
+    const uint16_t* n_cigar;
+    const uint32_t* cigar;
+    const uint8_t*  seq;
+    const uint8_t*  qual;
+    uint64_t        n_cigar_total;
+    uint64_t        n_bases_total;   /* length of qual[] (and 2 x length of seq[])               */
+} bsq_read_soa;
+
+/* ---------------------------------------------------------------- pass 1: error counts */
+
+/* Parameters of error_count() (src/breseq/error_count.h:44-56).  The covariate string the pipeline
+ * uses is "read_set=R,obs_base,ref_base,quality=Q" (src/breseq/breseq_cmdline.cpp:2304), giving the
+ * table index  idx = rs + R*(ref + 5*(obs + 5*q))  (src/breseq/error_count.cpp:477-497). */
+typedef struct bsq_ec_params {
+    uint32_t n_read_files;           /* R */
+    uint32_t n_quality;              /* Q = max_qual + 1 */
+    int32_t  do_coverage;
+    int32_t  do_errors;
+    int32_t  preprocess_stage;
+    /* Settings::required_junction_read_end_min_coordinate (src/breseq/settings.h:345-354) */
+    uint32_t unmatched_end_minimum_read_length;
+    double   unmatched_end_length_factor;
+} bsq_ec_params;
+
+/* Caller-owned outputs of pass 1. */
+typedef struct bsq_ec_result {
+    uint64_t* counts;          /* [R*5*5*Q] covariate counts                                 */
+    uint64_t* coverage_hist;   /* [n_coverage_groups * hist_capacity]                        */
+    uint32_t  hist_capacity;   /* bins per group supplied by the caller                      */
+    uint32_t* hist_size;       /* [n_coverage_groups] out: reference vector size (max cov + 1) */
+    double*   no_pos_hash_pr;  /* [n_targets] preprocess only (may be NULL)                  */
+} bsq_ec_result;
+
+/* ---------------------------------------------------------------- pass 2: identify mutations */
+
+#define BSQ_PRECISION_FP64   0   /* plain form: FP64 sums and the EM at every column            */
+#define BSQ_PRECISION_FP32C  1   /* FP32 Kahan-compensated sums, candidate screen, FP64 EM       */
+
+typedef struct bsq_im_params {
+    uint32_t n_read_files;                 /* R of the error table                               */
+    uint32_t n_quality;                    /* Q of the error table                               */
+    uint32_t base_quality_cutoff;          /* Settings::base_quality_cutoff (default 3)          */
+    double   mutation_cutoff;              /* consensus score cutoff (mutation_log10_e_value_cutoff) */
+    double   polymorphism_cutoff;          /* polymorphism_log10_e_value_cutoff                  */
+    double   polymorphism_precision_decimal;
+    uint32_t polymorphism_precision_places;
+    int32_t  skip_missing_coverage_prediction;
+    double   log10_ref_length;             /* log10 of the summed BAM target lengths (identify_mutations.cpp:848-852) */
+    const double* deletion_propagation_cutoff;  /* [n_targets] */
+    const double* deletion_seed_cutoff;         /* [n_targets] */
+    int32_t  precision;                    /* BSQ_PRECISION_* */
+} bsq_im_params;
+
+/* One RA evidence item with raw (unformatted) values; identify_mutations.cpp:1836-1910. */
+typedef struct bsq_ra_record {
+    uint32_t tid;
+    uint32_t position;          /* 1-based */
+    uint32_t insert_position;
+    char     ref_base, new_base, major_base, minor_base;
+    double   score;             /* variant presence score, NaN when there is no variant allele */
+    double   consensus_score;   /* pure-genotype score minus log10(reference length)         */
+    double   f[5];              /* fitted allele frequencies A,C,G,T,'.'                      */
+    double   major_frequency;   /* reported (floored) frequency of the major allele          */
+    double   frequency;         /* reported frequency of the variant allele                  */
+    double   frequency_lower;
+    double   frequency_upper;
+    double   fisher_strand_p;
+    double   ks_quality_p;
+    int32_t  ref_cov[2], new_cov[2], major_cov[2], minor_cov[2], total_cov[2];   /* top, bottom */
+    uint32_t n;                 /* read bases in the fit */
+    uint8_t  passed_consensus;
+    uint8_t  passed_polymorphism;
+    uint8_t  pad[2];
+} bsq_ra_record;
+
+/* MC (missing coverage) item; identify_mutations.cpp:2262-2344, 2140-2159. */
+typedef struct bsq_mc_record {
+    uint32_t tid, start, end, start_range, end_range;
+    uint32_t pad;
+    double   left_outside_cov, left_inside_cov, right_inside_cov, right_outside_cov;  /* NaN = NA */
+} bsq_mc_record;
+
+/* UN (unknown base) interval; identify_mutations.cpp:2972-3007. */
+typedef struct bsq_un_record {
+    uint32_t tid, start, end;
+} bsq_un_record;
+
+/* Per-position outputs (insert position 0) for the coverage table and checks.  Arrays of length
+ * total reference length, indexed by the global column target_offset[t] + position_0. */
+typedef struct bsq_position_arrays {
+    uint32_t* unique_top;       /* may be NULL */
+    uint32_t* unique_bot;
+    double*   redundant_top;
+    double*   redundant_bot;
+    uint32_t* raw_redundant_top;
+    uint32_t* raw_redundant_bot;
+    double*   consensus_score;  /* NaN where no read base scored */
+    uint8_t*  best_base;        /* 0..4 = A,C,G,T,'.'; 5 = N */
+    uint32_t* n_scored;
+} bsq_position_arrays;
+
+/* ---------------------------------------------------------------- context API */
+
+typedef struct bsq_ctx bsq_ctx;
+
+/* Create a context on CUDA device `device`.  Fails with BSQ_ERR_CUDA when no device is present. */
+int         bsq_create(bsq_ctx** out, int device);
+void        bsq_destroy(bsq_ctx* ctx);
+const char* bsq_last_error(const bsq_ctx* ctx);
+const char* bsq_version(void);
+
+/* Upload a sample (reference + records) to device memory and keep it resident.  Records are
+ * validated (sorted, CIGAR consumes the reference, offsets inside the arrays).  Replaces the BAM/BAI/
+ * FASTA open of pileup_base::pileup_base (src/breseq/pileup_base.cpp:61-88). */
+int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* reads, int32_t* sample_id);
+int bsq_free_sample(bsq_ctx* ctx, int32_t sample_id);
+/* Device bytes a sample of this shape occupies (for admission by HBM footprint). */
+uint64_t bsq_sample_footprint(const bsq_reference* ref, const bsq_read_soa* reads);
+
+/* Pass 1.  Replaces error_count() (src/breseq/error_count.cpp:50-68) minus its file writers, which
+ * are bsq_write_error_rates / bsq_write_coverage_distribution below. */
+int bsq_error_count(bsq_ctx* ctx, int32_t sample_id, const bsq_ec_params* p, bsq_ec_result* out);
+
+/* Convert pass-1 counts into the log10 probability table exactly as breseq round-trips it through
+ * error_rates.tab: counts_to_log10_prob (error_count.cpp:1005-1026), printed with 6 significant
+ * digits (write_log10_prob_table, :660-690) and parsed back (read_log10_prob_table, :629-654).
+ * log10_prob must hold R*5*5*Q doubles. */
+int bsq_counts_to_log10_prob(const uint64_t* counts, uint32_t n_read_files, uint32_t n_quality, double* log10_prob);
+
+/* Pass 2.  Replaces identify_mutations() (src/breseq/identify_mutations.cpp:48-88) for RA, MC, UN
+ * and the coverage table.  Results are kept in the context until the next call and read with
+ * bsq_im_result_counts / bsq_im_result_copy.  `pos_out` may be NULL. */
+int bsq_identify_mutations(bsq_ctx* ctx, int32_t sample_id, const bsq_im_params* p,
+                           const double* log10_prob_table, bsq_position_arrays* pos_out);
+int bsq_im_result_counts(const bsq_ctx* ctx, uint64_t* n_ra, uint64_t* n_mc, uint64_t* n_un);
+int bsq_im_result_copy(const bsq_ctx* ctx, bsq_ra_record* ra, uint64_t ra_cap,
+                       bsq_mc_record* mc, uint64_t mc_cap, bsq_un_record* un, uint64_t un_cap);
+
+/* Timing of the last pass on the device (CUDA events around the kernels, milliseconds) and the
+ * number of kernels launched by it. */
+int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_launches,
+                        double* main_kernel_ms);
+
+/* Device-timeline timer on the context's stream: CUDA events recorded where the passes launch
+ * their kernels, so the interval covers exactly the work issued in between (and any idle gaps). */
+int bsq_timer_start(bsq_ctx* ctx);
+int bsq_timer_stop(bsq_ctx* ctx, double* elapsed_ms);
+
+/* Page-lock caller memory (cudaHostRegister) so sample uploads run at full host-to-device speed. */
+int bsq_host_register(void* ptr, uint64_t bytes);
+int bsq_host_unregister(void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BRESEQ_GB300_H */

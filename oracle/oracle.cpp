@@ -1,0 +1,1020 @@
+/*
+ * oracle.cpp -- CPU restatement of breseq's read-evidence scoring path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA path: only tests/, the smoke test
+ * and the CPU-baseline leg of bench.py load it.  Nothing in the breseq_gb300 package links or calls it.
+ *
+ * Parity status: UNPINNED against the reference binary.  breseq cannot be built here (it needs
+ * htslib 1.23.1 and miniz 3.1.1, external libraries absent from the image, plus autotools), and its
+ * tests' RA goldens need inputs that are not in the tree.  The statistics helpers are pinned to
+ * R-equivalent implementations (scipy) by tests/test_oracle_stats.py, as the reference documents
+ * them to be R-equivalent (src/breseq/stats.cpp:2130-2143, 2206-2219).
+ *
+ * What is restated, with the reference lines each part follows:
+ *   - the pileup column iterator of htslib 1.23.1 (bam_plp_auto / resolve_cigar2, a third-party
+ *     dependency not present under the reference tree), as breseq drives it from
+ *     src/breseq/pileup_base.cpp:141-210, 308-385: per column, the covering reads in BAM order, with
+ *     qpos, is_del (D and N ops) and indel (length of an I/D op that follows this aligned base).
+ *     On a deletion column qpos is the query index of the next aligned base (htslib sets it to the
+ *     query bases consumed so far);
+ *   - error_count_pileup::pileup_callback      src/breseq/error_count.cpp:125-199
+ *   - cErrorTable::count_alignment_position    src/breseq/error_count.cpp:854-986
+ *   - covariates_to_index / counts_to_log10_prob  src/breseq/error_count.cpp:477-497, 1005-1026
+ *   - identify_mutations_pileup::pileup_callback  src/breseq/identify_mutations.cpp:1309-2022
+ *   - alignment_position_to_covariates         src/breseq/error_count.cpp:1049-1105
+ *   - fill_read_base_likelihoods               src/breseq/identify_mutations.cpp:3359-3384
+ *   - pure_genotype_call                       src/breseq/identify_mutations.cpp:3398-3433
+ *   - fit_allele_frequencies / variant_presence_score   :3241-3318, :3329-3344
+ *   - profile_log10_likelihood / write_RA_frequency_bounds  :3094-3143, :3175-3217
+ *   - annotate_polymorphism_statistics          :3009-3033
+ *   - fisher_exact_test_2x2 / ks_test_two_sample_less   src/breseq/stats.cpp:2144-2286
+ *   - check_deletion_completion / update_unknown_intervals / at_target_end  :2262-2344, :2972-3007, :2107-2164
+ *   - alignment accessors (query bounds, trims, redundancy)  src/breseq/alignment.cpp:44-290, alignment.h:355-411
+ *
+ * One deliberate divergence: where the reference would index a read past its end (a deletion that is
+ * followed by a single aligned base, error_count.cpp:1073), it aborts on an assert; here the base is
+ * treated as unusable.  The CUDA path does the same.
+ */
+#include "../include/breseq_gb300.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+const double kNaN = std::numeric_limits<double>::quiet_NaN();
+const uint32_t kUndef = 0xFFFFFFFFu;
+
+// ----------------------------------------------------------------------------- encodings
+// src/breseq/common.h:195-318
+inline bool bam_is_N(uint8_t b) { return b == 0x0f; }
+inline uint8_t compl_bam(uint8_t b) {
+  switch (b) { case 1: return 8; case 2: return 4; case 4: return 2; case 8: return 1; default: return b; }
+}
+inline char compl_char(char c) {
+  switch (c) { case 'A': return 'T'; case 'C': return 'G'; case 'G': return 'C'; case 'T': return 'A'; default: return c; }
+}
+inline int bam2index(uint8_t b) {  // '.' -> 4, unrecognised -> -1 (reference ASSERTs)
+  switch (b) { case 1: return 0; case 2: return 1; case 4: return 2; case 8: return 3; case '.': return 4; default: return -1; }
+}
+inline int char2index(char c) {
+  switch (c) { case 'A': return 0; case 'C': return 1; case 'G': return 2; case 'T': return 3; case '.': return 4; case 'N': return 5; default: return -1; }
+}
+inline int compl_index(int b) { return (b >= 0 && b <= 3) ? 3 - b : 4; }
+const char kBaseChars[6] = {'A', 'C', 'G', 'T', '.', 'N'};
+
+inline bool op_ref(uint32_t op) { return op == 0 || op == 2 || op == 3 || op == 7 || op == 8; }
+inline bool op_qmatch(uint32_t op) { return op == 0 || op == 7 || op == 8; }
+enum { OP_M = 0, OP_I = 1, OP_D = 2, OP_N = 3, OP_S = 4, OP_H = 5, OP_P = 6, OP_EQ = 7, OP_X = 8 };
+
+struct ReadInfo {
+  int64_t pos, endpos;
+  uint32_t len;
+  int32_t qs0, qe0;    // query_start_0 / query_end_0       (alignment.cpp:219-256)
+  int32_t qb0s, qb0e;  // query_bounds_0(min_qual = 0)       (alignment.cpp:113-196)
+  uint32_t stranded_end1;  // query_stranded_end_1             (alignment.cpp:201-214)
+  bool rev, skip;
+};
+
+struct Pile { int32_t qpos; bool is_del; int32_t indel; };
+
+struct Data {
+  const bsq_reference* ref;
+  const bsq_read_soa* rd;
+  std::vector<ReadInfo> info;
+  std::vector<uint64_t> tgt_begin, tgt_end;  // read index range per target
+  std::vector<int64_t> tgt_maxspan;
+  std::string err;
+};
+
+inline uint8_t base_at(const bsq_read_soa* rd, uint64_t r, int64_t q) {
+  uint64_t nib = rd->seq_off[r] + (uint64_t)q;
+  uint8_t byte = rd->seq[nib >> 1];
+  return (nib & 1) ? (byte & 0xf) : (byte >> 4);
+}
+inline uint8_t qual_at(const bsq_read_soa* rd, uint64_t r, int64_t q) { return rd->qual[rd->seq_off[r] + (uint64_t)q]; }
+
+// htslib resolve_cigar2 restated from scratch for one column (see header comment).
+bool resolve(const bsq_read_soa* rd, uint64_t r, int64_t col, Pile& e) {
+  const uint32_t* cig = rd->cigar + rd->cigar_off[r];
+  const int n = rd->n_cigar[r];
+  int64_t x = rd->pos[r];
+  int32_t y = 0;
+  for (int k = 0; k < n; k++) {
+    uint32_t op = cig[k] & 0xf, len = cig[k] >> 4;
+    if (op_ref(op)) {
+      if (col < x + (int64_t)len) {
+        if (op_qmatch(op)) { e.qpos = y + (int32_t)(col - x); e.is_del = false; }
+        else { e.qpos = y; e.is_del = true; }
+        e.indel = 0;
+        if (col == x + (int64_t)len - 1 && k + 1 < n) {
+          uint32_t op2 = cig[k + 1] & 0xf, l2 = cig[k + 1] >> 4;
+          if (op2 == OP_D && op != OP_D) {
+            e.indel = -(int32_t)l2;
+            for (int j = k + 2; j < n; j++) { if ((cig[j] & 0xf) == OP_D) e.indel -= (int32_t)(cig[j] >> 4); else break; }
+          } else if (op2 == OP_I) {
+            e.indel = (int32_t)l2;
+            for (int j = k + 2; j < n; j++) {
+              uint32_t o = cig[j] & 0xf;
+              if (o == OP_I) e.indel += (int32_t)(cig[j] >> 4); else if (o != OP_P) break;
+            }
+          } else if (op2 == OP_P && k + 2 < n) {
+            int32_t l3 = 0;
+            for (int j = k + 2; j < n; j++) {
+              uint32_t o = cig[j] & 0xf;
+              if (o == OP_I) l3 += (int32_t)(cig[j] >> 4); else if (op_ref(o)) break;
+            }
+            if (l3 > 0) e.indel = l3;
+          }
+        }
+        return true;
+      }
+      x += len;
+      if (op_qmatch(op)) y += (int32_t)len;
+    } else if (op == OP_I || op == OP_S) {
+      y += (int32_t)len;
+    }
+  }
+  return false;
+}
+
+int prepare(Data& d) {
+  const bsq_read_soa* rd = d.rd;
+  const bsq_reference* ref = d.ref;
+  const uint64_t n = rd->n_reads;
+  d.info.resize(n);
+  d.tgt_begin.assign(ref->n_targets, 0);
+  d.tgt_end.assign(ref->n_targets, 0);
+  d.tgt_maxspan.assign(ref->n_targets, 1);
+  int32_t last_tid = -1;
+  int64_t last_pos = -1;
+  for (uint64_t r = 0; r < n; r++) {
+    ReadInfo& ri = d.info[r];
+    int32_t tid = rd->tid[r];
+    if (tid < 0 || (uint32_t)tid >= ref->n_targets) { d.err = "read with invalid tid"; return BSQ_ERR_INVALID; }
+    if (tid < last_tid || (tid == last_tid && rd->pos[r] < last_pos)) { d.err = "records not coordinate-sorted"; return BSQ_ERR_INVALID; }
+    last_tid = tid; last_pos = rd->pos[r];
+    ri.skip = (rd->flag[r] & BSQ_PILEUP_SKIP_MASK) != 0;
+    ri.rev = (rd->flag[r] & BSQ_FLAG_REVERSE) != 0;
+    ri.pos = rd->pos[r];
+    ri.len = rd->l_qseq[r];
+    const uint32_t* cig = rd->cigar + rd->cigar_off[r];
+    const int nc = rd->n_cigar[r];
+    int64_t rlen = 0; uint32_t qlen = 0;
+    for (int k = 0; k < nc; k++) {
+      uint32_t op = cig[k] & 0xf, len = cig[k] >> 4;
+      if (op_ref(op)) rlen += len;
+      if (op == OP_M || op == OP_I || op == OP_S || op == OP_EQ || op == OP_X) qlen += len;
+    }
+    if (ri.skip) { ri.endpos = ri.pos + (rlen > 0 ? rlen : 1); continue; }
+    if (nc == 0 || rlen == 0) { d.err = "mapped read without reference-consuming CIGAR op"; return BSQ_ERR_INVALID; }
+    if (qlen != ri.len) { d.err = "CIGAR query length differs from read length"; return BSQ_ERR_INVALID; }
+    ri.endpos = ri.pos + rlen;
+    if ((uint64_t)ri.endpos > ref->target_offset[tid + 1] - ref->target_offset[tid]) { d.err = "read extends past target end"; return BSQ_ERR_INVALID; }
+    d.tgt_maxspan[tid] = std::max<int64_t>(d.tgt_maxspan[tid], rlen);
+    // query_start_1 (alignment.cpp:219-236)
+    int32_t qs1 = 1;
+    for (int k = 0; k < nc; k++) { if ((cig[k] & 0xf) != OP_S) break; qs1 += (int32_t)(cig[k] >> 4); }
+    // query_end_1 (alignment.cpp:239-256)
+    int32_t qe1 = (int32_t)qlen;
+    for (int k = nc - 1; k > 0; k--) { if ((cig[k] & 0xf) != OP_S) break; qe1 -= (int32_t)(cig[k] >> 4); }
+    ri.qs0 = qs1 - 1; ri.qe0 = qe1 - 1;
+    // query_bounds_1 with min_qual = 0 (alignment.cpp:113-196): skips S/H/N, only S moves
+    int32_t bs = 1, be = (int32_t)qlen;
+    for (int k = 0; k < nc; k++) {
+      uint32_t op = cig[k] & 0xf;
+      if (op != OP_S && op != OP_H && op != OP_N) break;
+      if (op == OP_S) bs += (int32_t)(cig[k] >> 4);
+    }
+    for (int k = nc - 1; k > 0; k--) {
+      uint32_t op = cig[k] & 0xf;
+      if (op != OP_S && op != OP_H && op != OP_N) break;
+      if (op == OP_S) be -= (int32_t)(cig[k] >> 4);
+    }
+    ri.qb0s = bs - 1; ri.qb0e = be - 1;
+    ri.stranded_end1 = ri.rev ? (uint32_t)((int32_t)ri.len - bs + 1) : (uint32_t)be;
+  }
+  // read index range of each target (records are sorted by tid)
+  for (uint32_t t = 0; t < ref->n_targets; t++) {
+    d.tgt_begin[t] = std::lower_bound(rd->tid, rd->tid + n, (int32_t)t) - rd->tid;
+    d.tgt_end[t] = std::lower_bound(rd->tid, rd->tid + n, (int32_t)t + 1) - rd->tid;
+  }
+  return BSQ_OK;
+}
+
+// Active-window walk over columns [c0, c1) of target t: calls fn(col, active_reads) per column.
+template <class F>
+void walk_columns(const Data& d, uint32_t t, int64_t c0, int64_t c1, F&& fn) {
+  const bsq_read_soa* rd = d.rd;
+  uint64_t rb = d.tgt_begin[t], re = d.tgt_end[t];
+  // first read that may still cover c0
+  int64_t lo_pos = c0 - d.tgt_maxspan[t];
+  uint64_t r = std::lower_bound(rd->pos + rb, rd->pos + re, (int32_t)std::max<int64_t>(lo_pos, -1)) - rd->pos;
+  std::vector<uint64_t> active;
+  for (; r < re && rd->pos[r] < c0; r++) {
+    if (!d.info[r].skip && d.info[r].endpos > c0) active.push_back(r);
+  }
+  for (int64_t c = c0; c < c1; c++) {
+    for (; r < re && rd->pos[r] <= c; r++) if (!d.info[r].skip) active.push_back(r);
+    size_t w = 0;
+    for (size_t i = 0; i < active.size(); i++) if (d.info[active[i]].endpos > c) active[w++] = active[i];
+    active.resize(w);
+    fn(c, active);
+  }
+}
+
+template <class F>
+void parallel_chunks(int64_t n, int n_threads, F&& fn) {
+  if (n_threads <= 1 || n < 4096) { fn(0, n, 0); return; }
+  int64_t chunk = std::max<int64_t>(1024, (n + n_threads * 4 - 1) / (n_threads * 4));
+  std::atomic<int64_t> next(0);
+  std::vector<std::thread> th;
+  for (int i = 0; i < n_threads; i++) {
+    th.emplace_back([&, i]() {
+      for (;;) {
+        int64_t s = next.fetch_add(chunk);
+        if (s >= n) break;
+        fn(s, std::min(n, s + chunk), i);
+      }
+    });
+  }
+  for (auto& x : th) x.join();
+}
+
+// ============================================================================ pass 1
+struct EcPartial {
+  std::vector<uint64_t> counts;
+  std::vector<std::vector<uint64_t>> hist;   // per coverage group
+  uint64_t found[2] = {0, 0};
+  int err = 0;
+};
+
+// cErrorTable::count_alignment_position (error_count.cpp:854-986)
+inline int count_events(const Data& d, uint64_t r, const Pile& e, int64_t ref_pos, const char* ref_seq, int64_t tlen,
+                        uint32_t R, uint32_t Q, std::vector<uint64_t>& counts) {
+  const bsq_read_soa* rd = d.rd;
+  const ReadInfo& ri = d.info[r];
+  const int rev = ri.rev ? 1 : 0;
+  const uint32_t rs = rd->read_file[r];
+  const int32_t qpos = e.qpos, qlen = (int32_t)ri.len;
+  auto ref_at = [&](int64_t p) -> char { return (p >= 0 && p < tlen) ? ref_seq[p] : '\0'; };
+  auto add = [&](uint32_t ref_i, uint32_t obs_i, uint32_t q) -> int {
+    if (rs >= R || q >= Q) return BSQ_ERR_DATA;
+    counts[rs + R * (ref_i + 5 * (obs_i + 5 * q))] += 1;
+    return 0;
+  };
+  {  // (1) base substitution or match at this column
+    uint8_t obs = base_at(rd, r, qpos);
+    char refc = ref_at(ref_pos);
+    if (!bam_is_N(obs) && refc != 'N') {
+      if (rev) { obs = compl_bam(obs); refc = compl_char(refc); }
+      int oi = bam2index(obs), ri2 = char2index(refc);
+      if (oi < 0 || ri2 < 0 || ri2 > 4) return BSQ_ERR_DATA;
+      if (add(ri2, oi, qual_at(rd, r, qpos))) return BSQ_ERR_DATA;
+    }
+  }
+  if (e.indel == 0) {  // (2a) next base also aligned: '..'
+    if (qpos < ri.qe0) {
+      int32_t mq = qpos + 1 - rev;
+      if (mq < 0 || mq >= qlen) return BSQ_ERR_DATA;
+      uint8_t obs = base_at(rd, r, mq);
+      char refc = ref_at(ref_pos + 1 - rev);
+      if (!bam_is_N(obs) && refc != 'N') { if (add(4, 4, qual_at(rd, r, mq))) return BSQ_ERR_DATA; }
+    }
+  } else if (e.indel == -1) {  // (2b) exactly one deleted base follows
+    int32_t mq = qpos + 1 - rev;
+    if (mq < 0 || mq >= qlen) return BSQ_ERR_DATA;
+    uint8_t obs = base_at(rd, r, mq);
+    char refc = ref_at(ref_pos + 1);
+    if (!bam_is_N(obs) && refc != 'N') {
+      if (rev) refc = compl_char(refc);
+      int ri2 = char2index(refc);
+      if (ri2 < 0 || ri2 > 4) return BSQ_ERR_DATA;
+      if (add(ri2, 4, qual_at(rd, r, mq))) return BSQ_ERR_DATA;
+    }
+  } else if (e.indel == 1) {  // (2c) exactly one inserted base follows
+    int32_t mq = qpos + 1;
+    if (mq >= qlen) return BSQ_ERR_DATA;
+    if (mq <= ri.qe0 && mq >= ri.qs0) {
+      uint8_t obs = base_at(rd, r, mq);
+      if (!bam_is_N(obs)) {
+        if (rev) obs = compl_bam(obs);
+        int oi = bam2index(obs);
+        if (oi < 0) return BSQ_ERR_DATA;
+        if (add(4, oi, qual_at(rd, r, mq))) return BSQ_ERR_DATA;
+      }
+    }
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ============================================================================ exported: pass 1
+extern "C" int oracle_error_count(const bsq_reference* ref, const bsq_read_soa* rd, const bsq_ec_params* p,
+                                  bsq_ec_result* out, int n_threads, char* errbuf, int errcap) {
+  Data d; d.ref = ref; d.rd = rd;
+  int rc = prepare(d);
+  if (rc) { if (errbuf) snprintf(errbuf, errcap, "%s", d.err.c_str()); return rc; }
+  const uint32_t R = p->n_read_files, Q = p->n_quality;
+  const uint32_t G = ref->n_coverage_groups;
+  const size_t nbins = (size_t)R * 25 * Q;
+  std::vector<uint64_t> counts(nbins, 0);
+  std::vector<std::vector<uint64_t>> hist(G);
+  if (out->no_pos_hash_pr) for (uint32_t t = 0; t < ref->n_targets; t++) out->no_pos_hash_pr[t] = 1.0;
+
+  for (uint32_t oi = 0; oi < ref->n_target_order; oi++) {
+    const uint32_t t = ref->target_order[oi];
+    const char* tseq = ref->seq + ref->target_offset[t];
+    const int64_t tlen = (int64_t)(ref->target_offset[t + 1] - ref->target_offset[t]);
+    const uint32_t g = ref->coverage_group[t];
+    int nth = std::max(1, n_threads);
+    std::vector<EcPartial> parts(nth);
+    for (auto& pp : parts) { pp.counts.assign(p->do_errors ? nbins : 0, 0); pp.hist.assign(1, {}); }
+    parallel_chunks(tlen, nth, [&](int64_t c0, int64_t c1, int th) {
+      EcPartial& P = parts[th];
+      walk_columns(d, t, c0, c1, [&](int64_t c, const std::vector<uint64_t>& act) {
+        size_t unique = 0;
+        bool has_red = false;
+        int hqs[2] = {0, 0};
+        for (uint64_t r : act) {
+          Pile e;
+          if (!resolve(rd, r, c, e)) continue;
+          if (e.is_del) continue;
+          if (rd->x1[r] > 1) { has_red = true; continue; }
+          ++unique;
+          const ReadInfo& ri = d.info[r];
+          if (p->preprocess_stage) {
+            // Settings::required_junction_read_end_min_coordinate (settings.h:345-354)
+            int32_t umax = (int32_t)std::floor((double)((int32_t)ri.len - (int32_t)p->unmatched_end_minimum_read_length) *
+                                               p->unmatched_end_length_factor);
+            uint32_t req = (umax <= 0) ? ri.len : ri.len - (uint32_t)umax;
+            if (e.qpos + 1 == 1 && ri.stranded_end1 >= req) hqs[ri.rev ? 1 : 0] = 1;
+          }
+          if (!p->do_errors) continue;
+          int er = count_events(d, r, e, c, tseq, tlen, R, Q, P.counts);
+          if (er) P.err = er;
+        }
+        if (!has_red) {
+          if (P.hist[0].size() <= unique) P.hist[0].resize(unique + 1, 0);
+          P.hist[0][unique]++;
+          if (p->preprocess_stage) { P.found[hqs[0]]++; P.found[hqs[1]]++; }
+        }
+      });
+    });
+    uint64_t found[2] = {0, 0};
+    for (auto& P : parts) {
+      if (P.err) { if (errbuf) snprintf(errbuf, errcap, "covariate outside the error table"); return P.err; }
+      if (p->do_errors) for (size_t i = 0; i < nbins; i++) counts[i] += P.counts[i];
+      if (hist[g].size() < P.hist[0].size()) hist[g].resize(P.hist[0].size(), 0);
+      for (size_t i = 0; i < P.hist[0].size(); i++) hist[g][i] += P.hist[0][i];
+      found[0] += P.found[0]; found[1] += P.found[1];
+    }
+    if (p->preprocess_stage && out->no_pos_hash_pr) {
+      double total = (double)(found[0] + found[1]);
+      out->no_pos_hash_pr[t] = (total != 0) ? (double)found[0] / total : 1.0;
+    }
+  }
+  if (out->counts) for (size_t i = 0; i < nbins; i++) out->counts[i] = counts[i];
+  for (uint32_t g = 0; g < G; g++) {
+    if (out->hist_size) out->hist_size[g] = (uint32_t)hist[g].size();
+    if (out->coverage_hist) {
+      for (uint32_t i = 0; i < out->hist_capacity; i++)
+        out->coverage_hist[(size_t)g * out->hist_capacity + i] = (i < hist[g].size()) ? hist[g][i] : 0;
+      if (hist[g].size() > out->hist_capacity) { if (errbuf) snprintf(errbuf, errcap, "histogram capacity"); return BSQ_ERR_SIZE; }
+    }
+  }
+  return BSQ_OK;
+}
+
+// counts_to_log10_prob (error_count.cpp:1005-1026) followed by the 6-significant-digit text round trip
+// of write_log10_prob_table / read_log10_prob_table (error_count.cpp:629-690).
+extern "C" int oracle_counts_to_log10_prob(const uint64_t* counts, uint32_t R, uint32_t Q, double* out) {
+  for (uint32_t q = 0; q < Q; q++)
+    for (uint32_t ref = 0; ref < 5; ref++)
+      for (uint32_t rs = 0; rs < R; rs++) {
+        double sum = 0;
+        for (uint32_t obs = 0; obs < 5; obs++) sum += (double)counts[rs + R * (ref + 5 * (obs + 5 * q))];
+        for (uint32_t obs = 0; obs < 5; obs++) {
+          size_t i = rs + R * (ref + 5 * (obs + 5 * q));
+          double v = log10((double)(counts[i] + 1)) - log10(sum + 1 * 5);
+          char buf[64];
+          snprintf(buf, sizeof buf, "%.6g", v);
+          out[i] = strtod(buf, nullptr);
+        }
+      }
+  return BSQ_OK;
+}
+
+// ============================================================================ pass 2
+namespace {
+
+struct PData {
+  uint8_t obs;      // 0..4 (obs in top-strand space)
+  uint8_t quality;
+  int8_t strand;
+  double lp[5], r[5], lpmax;
+};
+
+struct AlleleModel {
+  double f[5] = {0, 0, 0, 0, 0};
+  double log10_likelihood = 0;
+  double sum_w[5] = {0, 0, 0, 0, 0};
+  uint32_t n = 0, iterations = 0;
+  double reported(int b) const {
+    if (n == 0 || b < 0 || b >= 5) return 0.0;
+    return (f[b] < 0.5 / (double)n) ? 0.0 : f[b];
+  }
+  int major() const {
+    if (n == 0) return 5;
+    int best = 0;
+    for (int b = 1; b < 5; b++) if (f[b] > f[best]) best = b;
+    return (f[best] > 0.0) ? best : 5;
+  }
+  int next(int excl) const {
+    if (n == 0) return 5;
+    double thr = 0.5 / (double)n;
+    int best = 5;
+    for (int b = 0; b < 5; b++) {
+      if (b == excl) continue;
+      if (f[b] < thr) continue;
+      if (best == 5 || f[b] > f[best]) best = b;
+    }
+    return best;
+  }
+};
+
+struct Pass2 {
+  const Data& d;
+  const bsq_im_params* p;
+  std::vector<double> prob;  // pow(10, log10 table) (error_count.cpp:1032-1040)
+  uint32_t R, Q;
+  Pass2(const Data& dd, const bsq_im_params* pp, const double* table) : d(dd), p(pp) {
+    R = p->n_read_files; Q = p->n_quality;
+    prob.resize((size_t)R * 25 * Q);
+    for (size_t i = 0; i < prob.size(); i++) prob[i] = pow(10, table[i]);
+  }
+
+  // fill_read_base_likelihoods (identify_mutations.cpp:3359-3384)
+  void fill(PData& pd, uint32_t rs, int obs_idx, uint32_t q, int mapq) const {
+    const double inc = pow(10, -(double)mapq / 10);
+    const double cor = 1 - inc;
+    const double uni = 1.0 / 5.0;
+    const bool top = pd.strand == 1;
+    int o = top ? obs_idx : compl_index(obs_idx);
+    pd.lpmax = -std::numeric_limits<double>::max();
+    for (int b = 0; b < 5; b++) {
+      int refb = top ? b : compl_index(b);
+      double pr = cor * prob[rs + R * (refb + 5 * (o + 5 * q))] + inc * uni;
+      if (pr < 0.0) pr = 0.0;
+      pd.lp[b] = log10(pr);
+      pd.lpmax = std::max(pd.lpmax, pd.lp[b]);
+    }
+    for (int b = 0; b < 5; b++) pd.r[b] = pow(10, pd.lp[b] - pd.lpmax);
+  }
+
+  // fit_allele_frequencies (identify_mutations.cpp:3241-3318)
+  AlleleModel fit(const std::vector<PData>& pd, const bool allowed[5]) const {
+    AlleleModel m;
+    m.n = (uint32_t)pd.size();
+    if (m.n == 0) return m;
+    uint32_t na = 0;
+    for (int b = 0; b < 5; b++) if (allowed[b]) { na++; m.f[b] = 0.5; }
+    if (na == 0) return m;
+    for (auto& x : pd) if (x.obs < 5 && allowed[x.obs]) m.f[x.obs] += 1.0;
+    double tot = 0;
+    for (int b = 0; b < 5; b++) tot += m.f[b];
+    for (int b = 0; b < 5; b++) m.f[b] /= tot;
+    const double tol = p->polymorphism_precision_decimal;
+    for (m.iterations = 1; m.iterations <= 50; m.iterations++) {
+      double sw[5] = {0, 0, 0, 0, 0};
+      double ll = 0;
+      for (auto& x : pd) {
+        double s = 0;
+        for (int b = 0; b < 5; b++) if (allowed[b]) s += m.f[b] * x.r[b];
+        if (s > 0.0) {
+          ll += log10(s) + x.lpmax;
+          for (int b = 0; b < 5; b++) if (allowed[b]) sw[b] += m.f[b] * x.r[b] / s;
+        } else {
+          for (int b = 0; b < 5; b++) if (allowed[b]) sw[b] += m.f[b];
+        }
+      }
+      double md = 0;
+      for (int b = 0; b < 5; b++) {
+        if (!allowed[b]) continue;
+        double fn = sw[b] / (double)m.n;
+        md = std::max(md, fabs(fn - m.f[b]));
+        m.f[b] = fn;
+      }
+      for (int b = 0; b < 5; b++) m.sum_w[b] = sw[b];
+      m.log10_likelihood = ll;
+      if (md < tol) break;
+    }
+    if (m.iterations > 50) m.iterations = 50;
+    return m;
+  }
+
+  // variant_presence_score (identify_mutations.cpp:3329-3344)
+  double presence(const std::vector<PData>& pd, const AlleleModel& full, int v) const {
+    if (full.n == 0 || v >= 5) return kNaN;
+    bool without[5];
+    for (int b = 0; b < 5; b++) without[b] = (b != v);
+    AlleleModel nf = fit(pd, without);
+    return (full.log10_likelihood - nf.log10_likelihood) - p->log10_ref_length;
+  }
+
+  // profile_log10_likelihood (identify_mutations.cpp:3094-3143)
+  double profile(const std::vector<PData>& pd, const AlleleModel& full, int v, double ff) const {
+    if (full.n == 0 || v >= 5) return 0.0;
+    double f[5], other = 0;
+    for (int b = 0; b < 5; b++) if (b != v) other += full.f[b];
+    for (int b = 0; b < 5; b++) {
+      if (b == v) f[b] = ff;
+      else f[b] = (other > 0.0) ? (1.0 - ff) * full.f[b] / other : (1.0 - ff) / 4.0;
+    }
+    double ll = 0;
+    for (uint32_t it = 0; it < 50; it++) {
+      double sw[5] = {0, 0, 0, 0, 0};
+      ll = 0;
+      for (auto& x : pd) {
+        double s = 0;
+        for (int b = 0; b < 5; b++) s += f[b] * x.r[b];
+        if (s > 0.0) {
+          ll += log10(s) + x.lpmax;
+          for (int b = 0; b < 5; b++) sw[b] += f[b] * x.r[b] / s;
+        } else {
+          for (int b = 0; b < 5; b++) sw[b] += f[b];
+        }
+      }
+      double others = 0;
+      for (int b = 0; b < 5; b++) if (b != v) others += sw[b];
+      double md = 0;
+      for (int b = 0; b < 5; b++) {
+        if (b == v) continue;
+        double fn = (others > 0.0) ? (1.0 - ff) * sw[b] / others : (1.0 - ff) / 4.0;
+        md = std::max(md, fabs(fn - f[b]));
+        f[b] = fn;
+      }
+      if (md < p->polymorphism_precision_decimal) break;
+    }
+    return ll;
+  }
+
+  // write_RA_frequency_bounds (identify_mutations.cpp:3175-3217)
+  void bounds(const std::vector<PData>& pd, const AlleleModel& am, int v, double& lower, double& upper) const {
+    lower = 0.0; upper = 1.0;
+    if (am.n > 0 && v < 5) {
+      const double D = 0.587566;
+      const double fh = am.f[v];
+      const double plmax = profile(pd, am, v, fh);
+      const double target = plmax - D;
+      const double prec = p->polymorphism_precision_decimal;
+      if (profile(pd, am, v, 0.0) >= target) lower = 0.0;
+      else {
+        double lo = 0.0, hi = fh;
+        for (uint32_t i = 0; i < 40 && (hi - lo) > prec; i++) {
+          double mid = 0.5 * (lo + hi);
+          if (profile(pd, am, v, mid) >= target) hi = mid; else lo = mid;
+        }
+        lower = hi;
+      }
+      if (profile(pd, am, v, 1.0) >= target) upper = 1.0;
+      else {
+        double lo = fh, hi = 1.0;
+        for (uint32_t i = 0; i < 40 && (hi - lo) > prec; i++) {
+          double mid = 0.5 * (lo + hi);
+          if (profile(pd, am, v, mid) >= target) lo = mid; else hi = mid;
+        }
+        upper = lo;
+      }
+    }
+  }
+};
+
+// log-gamma based helpers for stats.cpp:2074-2078 (log_choose)
+inline double log_choose(double n, double k) { return lgamma(n + 1) - lgamma(k + 1) - lgamma(n - k + 1); }
+
+}  // namespace
+
+// fisher_exact_test_2x2 (stats.cpp:2144-2169)
+extern "C" double oracle_fisher_2x2(uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  uint32_t row1 = a + b, row2 = c + d, col1 = a + c, col2 = b + d, n = row1 + row2;
+  uint32_t amin = (row1 > col2) ? (row1 - col2) : 0;
+  uint32_t amax = std::min(row1, col1);
+  double ld = log_choose(n, row1);
+  double lpo = log_choose(col1, a) + log_choose(col2, row1 - a) - ld;
+  const double lre = log(1.0 + 1e-7);
+  double tot = 0;
+  for (uint32_t ai = amin; ai <= amax; ai++) {
+    double lp = log_choose(col1, ai) + log_choose(col2, row1 - ai) - ld;
+    if (lp <= lpo + lre) tot += exp(lp);
+  }
+  return std::min(tot, 1.0);
+}
+
+// ks_test_two_sample_less (stats.cpp:2180-2286)
+extern "C" double oracle_ks_less(const double* x, uint32_t nx, const double* y, uint32_t ny) {
+  if (nx == 0 || ny == 0) return kNaN;
+  std::vector<std::pair<double, bool>> comb;
+  comb.reserve(nx + ny);
+  for (uint32_t i = 0; i < nx; i++) comb.push_back({x[i], true});
+  for (uint32_t i = 0; i < ny; i++) comb.push_back({y[i], false});
+  std::sort(comb.begin(), comb.end());
+  uint32_t cx = 0, cy = 0, bx = 0, by = 0;
+  double minz = 0; bool have = false;
+  std::vector<char> boundary(nx + ny + 1, 1);
+  size_t i = 0;
+  while (i < comb.size()) {
+    double v = comb[i].first;
+    size_t gs = i;
+    while (i < comb.size() && comb[i].first == v) { if (comb[i].second) cx++; else cy++; i++; }
+    for (size_t k = gs + 1; k < i; k++) boundary[k] = 0;
+    double z = (double)cx / nx - (double)cy / ny;
+    if (!have || z < minz) { minz = z; have = true; bx = cx; by = cy; }
+  }
+  double stat = -minz;
+  if ((double)nx * ny < 10000) {
+    uint32_t m = ny, n = nx;
+    int64_t thr = (int64_t)by * n - (int64_t)bx * m;
+    std::vector<double> u((size_t)(m + 1) * (n + 1), 0.0);
+    for (uint32_t a = 0; a <= m; a++)
+      for (uint32_t b = 0; b <= n; b++) {
+        double val;
+        if (a == 0 && b == 0) val = 1.0;
+        else val = (a > 0 ? u[(size_t)(a - 1) * (n + 1) + b] : 0.0) + (b > 0 ? u[(size_t)a * (n + 1) + b - 1] : 0.0);
+        int64_t lev = (int64_t)a * n - (int64_t)b * m;
+        if (boundary[a + b] && lev >= thr) val = 0.0;
+        u[(size_t)a * (n + 1) + b] = val;
+      }
+    double allowed = u[(size_t)m * (n + 1) + n];
+    double total = exp(log_choose(m + n, m));
+    double pv = 1.0 - allowed / total;
+    return std::min(std::max(pv, 0.0), 1.0);
+  }
+  double neff = ((double)nx * ny) / (nx + ny);
+  return exp(-2.0 * stat * stat * neff);
+}
+
+namespace {
+
+struct ColumnOut {   // insert position 0 of one reference column
+  double unique[3], redundant[3];
+  int raw_redundant[3];
+  int total;
+  bool base_predicted, unique_only;
+  double consensus;
+  uint8_t best;
+  uint32_t n;
+};
+
+struct ImOut {
+  std::vector<bsq_ra_record> ra;
+  std::vector<bsq_mc_record> mc;
+  std::vector<bsq_un_record> un;
+};
+
+// One (column, insert slot) of identify_mutations_pileup::pileup_callback (identify_mutations.cpp:1359-1910)
+struct SlotScorer {
+  const Pass2& P;
+  const Data& d;
+  SlotScorer(const Pass2& p, const Data& dd) : P(p), d(dd) {}
+
+  // returns next_insert_count_exists
+  bool score(uint32_t t, int64_t c, int insert_count, const std::vector<uint64_t>& act, const std::vector<Pile>& piles,
+             char ref_base_char, ColumnOut* col, std::vector<bsq_ra_record>& ra_out, int& err) const {
+    const bsq_read_soa* rd = d.rd;
+    const bsq_im_params* p = P.p;
+    bool next_exists = false;
+    uint32_t pos_info[6][3];
+    memset(pos_info, 0, sizeof pos_info);
+    double cov_unique[3] = {0, 0, 0}, cov_red[3] = {0, 0, 0};
+    int cov_raw[3] = {0, 0, 0};
+    bool unique_only = true;
+    std::vector<PData> pdata;
+    double lps[5] = {0, 0, 0, 0, 0};
+    for (size_t ii = 0; ii < act.size(); ii++) {
+      const uint64_t r = act[ii];
+      const Pile& e = piles[ii];
+      const ReadInfo& ri = d.info[r];
+      int indel = e.indel;
+      if (indel < 0) indel = 0;
+      if (e.is_del) indel = -1;
+      uint8_t read_base = '.';
+      bool past_base = true;
+      if (indel >= insert_count) {
+        int32_t qq = e.qpos + insert_count;
+        if (qq < 0 || qq >= (int32_t)ri.len) { err = BSQ_ERR_DATA; return false; }
+        read_base = base_at(rd, r, qq);
+        past_base = false;
+      }
+      if (bam_is_N(read_base)) continue;
+      const uint32_t red = rd->x1[r];
+      const int strand = ri.rev ? -1 : 1;
+      // is_trimmed (alignment.h:389-411), unsigned arithmetic as in the reference
+      bool trimmed = false;
+      {
+        uint32_t qp1 = (uint32_t)(e.qpos + 1);
+        if (rd->xl[r] >= 0 && qp1 <= (uint32_t)rd->xl[r]) trimmed = true;
+        if (!trimmed && rd->xr[r] >= 0) {
+          if (ri.len - qp1 + 1 <= (uint32_t)rd->xr[r]) trimmed = true;
+          else if (past_base && (ri.len - qp1 == (uint32_t)rd->xr[r])) trimmed = true;
+        }
+      }
+      if (red == 1) {
+        ++cov_unique[1 + strand];
+        if (indel > insert_count) next_exists = true;
+      } else {
+        unique_only = false;
+        cov_red[1 + strand] += 1.0 / red;
+        ++cov_raw[1 + strand];
+      }
+      if (red > 1) continue;
+      if (trimmed) continue;
+      // alignment_position_to_covariates (error_count.cpp:1049-1105)
+      int obi = e.is_del ? -1 : std::max(e.indel, 0);
+      uint8_t rb;
+      {
+        if (obi < insert_count) rb = '.';
+        else rb = base_at(rd, r, e.qpos + insert_count);
+      }
+      if (bam_is_N(rb)) continue;
+      int64_t qp = e.qpos;
+      if (obi == -1) {
+        qp += 1 - (ri.rev ? 1 : 0);
+        if (qp < 0 || qp >= (int64_t)ri.len) continue;  // reference asserts here; treated as unusable
+        if (bam_is_N(base_at(rd, r, qp))) continue;
+      } else if (insert_count > 0) {
+        int32_t mo = insert_count;
+        if (obi < mo) mo = obi;
+        qp += mo + 1 - (ri.rev ? 1 : 0);
+        if (qp > ri.qb0e) continue;
+        if (bam_is_N(base_at(rd, r, qp))) continue;
+      }
+      int oi = bam2index(rb);
+      if (oi < 0) { err = BSQ_ERR_DATA; return false; }
+      uint32_t q = qual_at(rd, r, qp);
+      uint32_t rs = rd->read_file[r];
+      if (q >= P.Q || rs >= P.R) { err = BSQ_ERR_DATA; return false; }
+      if (q < p->base_quality_cutoff) continue;
+      ++pos_info[oi][1 + strand];
+      PData pd;
+      pd.obs = (uint8_t)oi; pd.quality = (uint8_t)q; pd.strand = (int8_t)strand;
+      P.fill(pd, rs, oi, q, rd->mapq[r]);
+      for (int b = 0; b < 5; b++) lps[b] += pd.lp[b];
+      pdata.push_back(pd);
+    }
+    cov_unique[1] = cov_unique[0] + cov_unique[2];
+    cov_red[1] = cov_red[0] + cov_red[2];
+    cov_raw[1] = cov_raw[0] + cov_raw[2];
+    int total = (int)round(cov_unique[1]) + (int)round(cov_red[1]);
+
+    // pure_genotype_call (identify_mutations.cpp:3398-3433)
+    const uint32_t n = (uint32_t)pdata.size();
+    uint8_t best = 5;
+    double cscore = kNaN;
+    if (n > 0) {
+      int bb = 0;
+      for (int b = 1; b < 5; b++) if (lps[b] > lps[bb]) bb = b;
+      double off = -std::numeric_limits<double>::max();
+      for (int b = 0; b < 5; b++) if (b != bb) off = std::max(off, lps[b]);
+      double te = 0;
+      for (int b = 0; b < 5; b++) if (b != bb) te += pow(10, lps[b] - off);
+      double lte = log10(te) + off;
+      best = (uint8_t)bb;
+      cscore = (lps[bb] - lte) - p->log10_ref_length;
+    }
+    const char best_char = kBaseChars[best];
+    const bool base_predicted = cscore >= p->mutation_cutoff;
+    if (col) {
+      for (int k = 0; k < 3; k++) { col->unique[k] = cov_unique[k]; col->redundant[k] = cov_red[k]; col->raw_redundant[k] = cov_raw[k]; }
+      col->total = total; col->base_predicted = base_predicted; col->unique_only = unique_only;
+      col->consensus = cscore; col->best = best; col->n = n;
+    }
+    int total_cov[3] = {0, 0, 0};
+    for (int j = 0; j < 5; j++) { total_cov[2] += (int)pos_info[j][2]; total_cov[0] += (int)pos_info[j][0]; }
+
+    const bool passed_cons = (best_char != ref_base_char) && !std::isnan(cscore) && cscore > 0;
+    bool all[5] = {true, true, true, true, true};
+    AlleleModel am = P.fit(pdata, all);
+    const int ref_idx = (ref_base_char == 'N') ? 5 : char2index(ref_base_char);
+    const int maj = am.major();
+    const int minr = am.next(maj);
+    const int var = am.next(ref_idx);
+    double vscore = kNaN;
+    bool passed_poly = false;
+    if (var != 5) {
+      vscore = P.presence(pdata, am, var);
+      if (vscore >= p->polymorphism_cutoff) passed_poly = true;
+    }
+    if (passed_cons || passed_poly) {
+      bsq_ra_record ra;
+      memset(&ra, 0, sizeof ra);
+      ra.tid = t; ra.position = (uint32_t)(c + 1); ra.insert_position = (uint32_t)insert_count;
+      ra.ref_base = ref_base_char; ra.new_base = kBaseChars[var];
+      ra.major_base = kBaseChars[maj]; ra.minor_base = kBaseChars[minr];
+      ra.score = vscore; ra.consensus_score = cscore;
+      for (int b = 0; b < 5; b++) ra.f[b] = am.f[b];
+      ra.major_frequency = am.reported(maj);
+      ra.frequency = am.reported(var);
+      P.bounds(pdata, am, var, ra.frequency_lower, ra.frequency_upper);
+      // annotate_polymorphism_statistics (identify_mutations.cpp:3009-3033)
+      const int majc = maj, minc = minr;  // 5 == 'N': no reads carry it
+      std::vector<double> mq, nq;
+      for (auto& x : pdata) {
+        if (x.obs == majc) mq.push_back(x.quality);
+        if (x.obs == minc) nq.push_back(x.quality);
+      }
+      ra.ks_quality_p = 1.0;
+      if (!mq.empty() && !nq.empty()) ra.ks_quality_p = oracle_ks_less(nq.data(), (uint32_t)nq.size(), mq.data(), (uint32_t)mq.size());
+      ra.fisher_strand_p = oracle_fisher_2x2(pos_info[minc][2], pos_info[minc][0], pos_info[majc][2], pos_info[majc][0]);
+      auto covpair = [&](int idx, int32_t out[2]) { out[0] = (int32_t)pos_info[idx][2]; out[1] = (int32_t)pos_info[idx][0]; };
+      covpair(ref_idx, ra.ref_cov); covpair(var, ra.new_cov); covpair(maj, ra.major_cov); covpair(minr, ra.minor_cov);
+      ra.total_cov[0] = total_cov[2]; ra.total_cov[1] = total_cov[0];
+      ra.n = n;
+      ra.passed_consensus = passed_cons; ra.passed_polymorphism = passed_poly;
+      ra_out.push_back(ra);
+    }
+    return next_exists;
+  }
+};
+
+}  // namespace
+
+struct oracle_im_result { ImOut o; std::vector<ColumnOut> cols; std::vector<uint64_t> col_base; };
+
+extern "C" int oracle_identify(const bsq_reference* ref, const bsq_read_soa* rd, const bsq_im_params* p,
+                               const double* log10_table, oracle_im_result** res_out, int n_threads,
+                               char* errbuf, int errcap) {
+  Data d; d.ref = ref; d.rd = rd;
+  int rc = prepare(d);
+  if (rc) { if (errbuf) snprintf(errbuf, errcap, "%s", d.err.c_str()); return rc; }
+  Pass2 P(d, p, log10_table);
+  SlotScorer S(P, d);
+  oracle_im_result* res = new oracle_im_result();
+  const uint64_t total_len = ref->target_offset[ref->n_targets];
+  res->cols.resize(total_len);
+  int nth = std::max(1, n_threads);
+
+  // MC / UN state (identify_mutations_pileup members; some persist across targets)
+  uint32_t last_del_start = kUndef, last_del_end = kUndef, last_red_start = kUndef, last_red_end = kUndef;
+  uint32_t last_un_start = kUndef;
+  bool reaches_seed = false, red_zero = false;
+  ColumnOut nan_col;
+  for (int k = 0; k < 3; k++) { nan_col.unique[k] = kNaN; nan_col.redundant[k] = kNaN; nan_col.raw_redundant[k] = 0; }
+  nan_col.total = 0;
+  ColumnOut last_cov = nan_col, left_out = nan_col, left_in = nan_col;
+  double prop_cut = 0, seed_cut = 0;
+
+  auto check_deletion = [&](uint32_t t, uint32_t position, const ColumnOut& cov) {
+    if (position == 1) last_cov = nan_col;
+    if (cov.unique[1] <= prop_cut) {
+      if (last_del_start == kUndef) { last_del_start = position; left_out = last_cov; left_in = cov; }
+    }
+    if (!std::isnan(cov.unique[1]) && (double)cov.total <= seed_cut) reaches_seed = true;
+    if (last_del_start != kUndef && (std::isnan(cov.unique[1]) || cov.unique[1] > prop_cut)) {
+      if (reaches_seed) {
+        last_del_end = position - 1;
+        if (last_red_end == kUndef) last_red_end = last_del_end;
+        if (last_red_start == kUndef) last_red_start = last_del_start;
+        bsq_mc_record mc;
+        memset(&mc, 0, sizeof mc);
+        mc.tid = t; mc.start = last_del_start; mc.end = last_del_end;
+        mc.start_range = last_red_start - last_del_start; mc.end_range = last_del_end - last_red_end;
+        mc.left_outside_cov = left_out.unique[1]; mc.left_inside_cov = left_in.unique[1];
+        mc.right_inside_cov = last_cov.unique[1]; mc.right_outside_cov = cov.unique[1];
+        res->o.mc.push_back(mc);
+      }
+      reaches_seed = false; red_zero = false;
+      last_del_start = kUndef; last_del_end = kUndef; last_red_start = kUndef; last_red_end = kUndef;
+    }
+    if (last_del_start != kUndef) {
+      if (cov.redundant[1] == 0) { red_zero = true; last_red_end = kUndef; }
+      else if (cov.redundant[1] > 0) {
+        if (!red_zero) last_red_start = position;
+        else if (last_red_end == kUndef) last_red_end = position;
+      }
+    }
+    last_cov = cov;
+  };
+  auto update_unknown = [&](uint32_t t, uint32_t position, bool base_predicted) {
+    if (!base_predicted) {
+      if (last_un_start == kUndef) last_un_start = position;
+    } else if (last_un_start != kUndef) {
+      bsq_un_record un; un.tid = t; un.start = last_un_start; un.end = position - 1;
+      res->o.un.push_back(un);
+      last_un_start = kUndef;
+    }
+  };
+
+  for (uint32_t oi = 0; oi < ref->n_target_order; oi++) {
+    const uint32_t t = ref->target_order[oi];
+    const char* tseq = ref->seq + ref->target_offset[t];
+    const int64_t tlen = (int64_t)(ref->target_offset[t + 1] - ref->target_offset[t]);
+    const uint64_t cbase = ref->target_offset[t];
+    const bool failed = p->deletion_propagation_cutoff[t] < 0.0;
+    std::vector<std::vector<bsq_ra_record>> ra_parts((size_t)((tlen + 1023) / 1024) + 1);
+    std::atomic<int> err(0);
+    parallel_chunks(tlen, nth, [&](int64_t c0, int64_t c1, int) {
+      std::vector<Pile> piles;
+      std::vector<bsq_ra_record> local;
+      walk_columns(d, t, c0, c1, [&](int64_t c, const std::vector<uint64_t>& act) {
+        piles.resize(act.size());
+        for (size_t i = 0; i < act.size(); i++) resolve(rd, act[i], c, piles[i]);
+        ColumnOut& co = res->cols[cbase + c];
+        int e = 0;
+        if (failed) {
+          // tabulate_position_coverage (identify_mutations.cpp:2218-2250): coverage only
+          ColumnOut x;
+          for (int k = 0; k < 3; k++) { x.unique[k] = 0; x.redundant[k] = 0; x.raw_redundant[k] = 0; }
+          for (size_t i = 0; i < act.size(); i++) {
+            if (piles[i].is_del) continue;
+            if (bam_is_N(base_at(rd, act[i], piles[i].qpos))) continue;
+            int strand = d.info[act[i]].rev ? -1 : 1;
+            uint32_t red = rd->x1[act[i]];
+            if (red == 1) ++x.unique[1 + strand];
+            else { x.redundant[1 + strand] += 1.0 / red; ++x.raw_redundant[1 + strand]; }
+          }
+          x.unique[1] = x.unique[0] + x.unique[2]; x.redundant[1] = x.redundant[0] + x.redundant[2];
+          x.raw_redundant[1] = x.raw_redundant[0] + x.raw_redundant[2];
+          x.total = (int)round(x.unique[1]) + (int)round(x.redundant[1]);
+          x.base_predicted = false; x.unique_only = true; x.consensus = kNaN; x.best = 5; x.n = 0;
+          co = x;
+          return;
+        }
+        int insert_count = -1;
+        bool next = true;
+        while (next) {
+          ++insert_count;
+          char refc = insert_count == 0 ? tseq[c] : '.';
+          next = S.score(t, c, insert_count, act, piles, refc, insert_count == 0 ? &co : nullptr, local, e);
+          if (e) { err = e; return; }
+        }
+      });
+      // chunks are processed in any order; keep results keyed by chunk start
+      if (!local.empty()) {
+        std::vector<bsq_ra_record>& dst = ra_parts[(size_t)(c0 / 1024)];
+        dst = std::move(local);
+      }
+    });
+    if (err) { delete res; if (errbuf) snprintf(errbuf, errcap, "data outside the error table"); return err; }
+    // RA items in column order
+    for (auto& v : ra_parts) for (auto& x : v) res->o.ra.push_back(x);
+
+    // sequential state machines in column order (at_target_start / per position / at_target_end)
+    last_del_start = last_del_end = last_red_start = last_red_end = kUndef;
+    last_un_start = kUndef;
+    prop_cut = p->deletion_propagation_cutoff[t];
+    seed_cut = p->deletion_seed_cutoff[t];
+    if (!failed) {
+      for (int64_t c = 0; c < tlen; c++) {
+        const ColumnOut& co = res->cols[cbase + c];
+        if (!p->skip_missing_coverage_prediction) check_deletion(t, (uint32_t)(c + 1), co);
+        update_unknown(t, (uint32_t)(c + 1), co.base_predicted);
+      }
+    }
+    if (!p->skip_missing_coverage_prediction) check_deletion(t, (uint32_t)(tlen + 1), nan_col);
+    update_unknown(t, (uint32_t)(tlen + 1), true);
+    if (!p->skip_missing_coverage_prediction && failed) {
+      bsq_mc_record mc;
+      memset(&mc, 0, sizeof mc);
+      mc.tid = t; mc.start = 1; mc.end = (uint32_t)tlen; mc.start_range = 0; mc.end_range = 0;
+      mc.left_outside_cov = kNaN; mc.left_inside_cov = 0.0; mc.right_inside_cov = 0.0; mc.right_outside_cov = kNaN;
+      res->o.mc.push_back(mc);
+    }
+  }
+  *res_out = res;
+  return BSQ_OK;
+}
+
+extern "C" void oracle_im_counts(const oracle_im_result* r, uint64_t* n_ra, uint64_t* n_mc, uint64_t* n_un) {
+  *n_ra = r->o.ra.size(); *n_mc = r->o.mc.size(); *n_un = r->o.un.size();
+}
+extern "C" void oracle_im_copy(const oracle_im_result* r, bsq_ra_record* ra, bsq_mc_record* mc, bsq_un_record* un) {
+  if (ra) std::copy(r->o.ra.begin(), r->o.ra.end(), ra);
+  if (mc) std::copy(r->o.mc.begin(), r->o.mc.end(), mc);
+  if (un) std::copy(r->o.un.begin(), r->o.un.end(), un);
+}
+extern "C" void oracle_im_positions(const oracle_im_result* r, bsq_position_arrays* pa) {
+  const size_t n = r->cols.size();
+  for (size_t i = 0; i < n; i++) {
+    const ColumnOut& c = r->cols[i];
+    if (pa->unique_top) pa->unique_top[i] = (uint32_t)c.unique[2];
+    if (pa->unique_bot) pa->unique_bot[i] = (uint32_t)c.unique[0];
+    if (pa->redundant_top) pa->redundant_top[i] = c.redundant[2];
+    if (pa->redundant_bot) pa->redundant_bot[i] = c.redundant[0];
+    if (pa->raw_redundant_top) pa->raw_redundant_top[i] = (uint32_t)c.raw_redundant[2];
+    if (pa->raw_redundant_bot) pa->raw_redundant_bot[i] = (uint32_t)c.raw_redundant[0];
+    if (pa->consensus_score) pa->consensus_score[i] = c.consensus;
+    if (pa->best_base) pa->best_base[i] = c.best;
+    if (pa->n_scored) pa->n_scored[i] = c.n;
+  }
+}
+extern "C" void oracle_im_free(oracle_im_result* r) { delete r; }

@@ -1,0 +1,140 @@
+"""ctypes front end of the CPU oracle (test infrastructure only: tests/, the smoke test and the CPU
+baseline leg of bench.py use it to check and time the CUDA path)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from breseq_gb300 import abi
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.OUT
+        if not os.path.exists(path):
+            path = _build.build()
+        L = C.CDLL(path)
+        L.oracle_error_count.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.POINTER(abi.EcParams),
+                                         C.POINTER(abi.EcResult), C.c_int, C.c_char_p, C.c_int]
+        L.oracle_counts_to_log10_prob.argtypes = [C.POINTER(C.c_uint64), C.c_uint32, C.c_uint32, C.POINTER(C.c_double)]
+        L.oracle_identify.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.POINTER(abi.ImParams),
+                                      C.POINTER(C.c_double), C.POINTER(C.c_void_p), C.c_int, C.c_char_p, C.c_int]
+        L.oracle_im_counts.argtypes = [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.oracle_im_copy.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_im_positions.argtypes = [C.c_void_p, C.POINTER(abi.PositionArrays)]
+        L.oracle_im_free.argtypes = [C.c_void_p]
+        L.oracle_fisher_2x2.argtypes = [C.c_uint32] * 4
+        L.oracle_fisher_2x2.restype = C.c_double
+        L.oracle_ks_less.argtypes = [C.POINTER(C.c_double), C.c_uint32, C.POINTER(C.c_double), C.c_uint32]
+        L.oracle_ks_less.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def error_count(sample, n_threads=os.cpu_count() or 1, do_coverage=True, do_errors=True, preprocess=False,
+                hist_capacity=None, n_quality=None):
+    view = abi.SampleView(sample)
+    R, Q = sample.n_read_files, n_quality or sample.n_quality
+    G = sample.n_coverage_groups
+    cap = hist_capacity or 4096
+    counts = np.zeros(R * 25 * Q, dtype=np.uint64)
+    hist = np.zeros(G * cap, dtype=np.uint64)
+    hsize = np.zeros(G, dtype=np.uint32)
+    pr = np.zeros(len(sample.target_offset) - 1, dtype=np.float64)
+    p = abi.EcParams(n_read_files=R, n_quality=Q, do_coverage=int(do_coverage), do_errors=int(do_errors),
+                     preprocess_stage=int(preprocess), unmatched_end_minimum_read_length=50,
+                     unmatched_end_length_factor=0.1)
+    out = abi.EcResult(counts=abi.ptr(counts, C.c_uint64), coverage_hist=abi.ptr(hist, C.c_uint64),
+                       hist_capacity=cap, hist_size=abi.ptr(hsize, C.c_uint32), no_pos_hash_pr=abi.ptr(pr, C.c_double))
+    err = C.create_string_buffer(256)
+    rc = lib().oracle_error_count(C.byref(view.ref), C.byref(view.reads), C.byref(p), C.byref(out), n_threads, err, 256)
+    if rc != 0:
+        raise OracleError(f"oracle_error_count failed ({rc}): {err.value.decode()}")
+    return dict(counts=counts, hist=hist.reshape(G, cap), hist_size=hsize, no_pos_hash_pr=pr)
+
+
+def counts_to_log10_prob(counts, R, Q):
+    out = np.zeros(R * 25 * Q, dtype=np.float64)
+    c = np.ascontiguousarray(counts, dtype=np.uint64)
+    lib().oracle_counts_to_log10_prob(abi.ptr(c, C.c_uint64), R, Q, abi.ptr(out, C.c_double))
+    return out
+
+
+def default_im_params(sample, polymorphism_mode=False, prop_cutoff=None, seed_cutoff=None):
+    """Settings defaults of breseq (src/breseq/settings.cpp:857-950, 1335)."""
+    T = len(sample.target_offset) - 1
+    total = float(sample.target_offset[-1])
+    prop = np.broadcast_to(np.asarray(5.0 if prop_cutoff is None else prop_cutoff, dtype=np.float64), (T,)).copy()
+    seed = np.broadcast_to(np.asarray(0.0 if seed_cutoff is None else seed_cutoff, dtype=np.float64), (T,)).copy()
+    return dict(n_read_files=sample.n_read_files, n_quality=sample.n_quality, base_quality_cutoff=3,
+                mutation_cutoff=10.0, polymorphism_cutoff=2.0 if polymorphism_mode else 10.0,
+                polymorphism_precision_decimal=1e-6,
+                polymorphism_precision_places=8 if polymorphism_mode else 3,
+                skip_missing_coverage_prediction=0, log10_ref_length=float(np.log10(total)),
+                deletion_propagation_cutoff=np.ascontiguousarray(prop, dtype=np.float64),
+                deletion_seed_cutoff=np.ascontiguousarray(seed, dtype=np.float64), precision=0)
+
+
+def make_im_params(d):
+    keep = [d["deletion_propagation_cutoff"], d["deletion_seed_cutoff"]]
+    p = abi.ImParams(**{k: v for k, v in d.items() if k not in ("deletion_propagation_cutoff", "deletion_seed_cutoff")},
+                     deletion_propagation_cutoff=abi.ptr(keep[0], C.c_double),
+                     deletion_seed_cutoff=abi.ptr(keep[1], C.c_double))
+    return p, keep
+
+
+def identify(sample, log10_table, params: dict, n_threads=os.cpu_count() or 1, positions=True):
+    view = abi.SampleView(sample)
+    p, keep = make_im_params(params)
+    tab = np.ascontiguousarray(log10_table, dtype=np.float64)
+    handle = C.c_void_p()
+    err = C.create_string_buffer(256)
+    rc = lib().oracle_identify(C.byref(view.ref), C.byref(view.reads), C.byref(p), abi.ptr(tab, C.c_double),
+                               C.byref(handle), n_threads, err, 256)
+    if rc != 0:
+        raise OracleError(f"oracle_identify failed ({rc}): {err.value.decode()}")
+    try:
+        n_ra, n_mc, n_un = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        lib().oracle_im_counts(handle, C.byref(n_ra), C.byref(n_mc), C.byref(n_un))
+        ra = (abi.RaRecord * max(1, n_ra.value))()
+        mc = (abi.McRecord * max(1, n_mc.value))()
+        un = (abi.UnRecord * max(1, n_un.value))()
+        lib().oracle_im_copy(handle, C.cast(ra, C.c_void_p), C.cast(mc, C.c_void_p), C.cast(un, C.c_void_p))
+        out = dict(ra=abi.ra_to_dicts(ra[:n_ra.value]), mc=abi.mc_to_dicts(mc[:n_mc.value]),
+                   un=abi.un_to_dicts(un[:n_un.value]))
+        if positions:
+            n = int(sample.target_offset[-1])
+            arrs = dict(unique_top=np.zeros(n, np.uint32), unique_bot=np.zeros(n, np.uint32),
+                        redundant_top=np.zeros(n, np.float64), redundant_bot=np.zeros(n, np.float64),
+                        raw_redundant_top=np.zeros(n, np.uint32), raw_redundant_bot=np.zeros(n, np.uint32),
+                        consensus_score=np.zeros(n, np.float64), best_base=np.zeros(n, np.uint8),
+                        n_scored=np.zeros(n, np.uint32))
+            ctypes_map = dict(unique_top=C.c_uint32, unique_bot=C.c_uint32, redundant_top=C.c_double,
+                              redundant_bot=C.c_double, raw_redundant_top=C.c_uint32, raw_redundant_bot=C.c_uint32,
+                              consensus_score=C.c_double, best_base=C.c_uint8, n_scored=C.c_uint32)
+            pa = abi.PositionArrays(**{k: abi.ptr(v, ctypes_map[k]) for k, v in arrs.items()})
+            lib().oracle_im_positions(handle, C.byref(pa))
+            out["positions"] = arrs
+        return out
+    finally:
+        lib().oracle_im_free(handle)
+
+
+def fisher_2x2(a, b, c, d):
+    return lib().oracle_fisher_2x2(a, b, c, d)
+
+
+def ks_less(x, y):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    return lib().oracle_ks_less(abi.ptr(x, C.c_double), len(x), abi.ptr(y, C.c_double), len(y))
