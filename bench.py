@@ -160,7 +160,7 @@ def run_reference(args, world, rank, pg):
 def run_ours(args, world, rank, local, pg):
     from breseq_gb300 import abi
     from breseq_gb300.api import ImSettings, Scorer
-    s = _workload(seed=21 + rank)
+    s = _workload(seed=21 + rank, scale=args.scale)
     bases = s.aligned_bases()
     n_cols = s.total_length() + len(s.target_offset) - 1
     sc = Scorer(local)
@@ -245,7 +245,7 @@ def run_ours(args, world, rank, local, pg):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32c+f64" if prec == 1 else "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "genome_bp": s.total_length(), "reads": n_reads, "read_bases_per_step": bases,
+        "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD} scaled x{args.scale:g}", "genome_bp": s.total_length(), "reads": n_reads, "read_bases_per_step": bases,
                    "precision": args.precision, "l2": "inputs (%.2f GB) larger than L2" % ((s.qual.nbytes + s.seq.nbytes) / 1e9)},
         "e2e": {"value": world * bases / (e2e_ms_max / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
@@ -277,6 +277,7 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-scale", type=float, default=0.05)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0, help="genome length scale of the workload (profiling cases)")
     args = ap.parse_args()
     world, rank, local, pg = _dist()
     if args.impl == "reference":
