@@ -46,6 +46,8 @@ def load():
     L.bsq_timer_stop.argtypes = [C.c_void_p, P(C.c_double)]
     L.bsq_host_register.argtypes = [C.c_void_p, C.c_uint64]
     L.bsq_host_unregister.argtypes = [C.c_void_p]
+    L.bsq_score_positions_noalloc.argtypes = [C.c_void_p, C.c_int32, P(abi.ImParams), P(C.c_double), C.c_void_p,
+                                              C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
     _lib = L
     return L
 
@@ -53,4 +55,4 @@ def load():
 EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_load_sample", "bsq_free_sample",
             "bsq_sample_footprint", "bsq_error_count", "bsq_counts_to_log10_prob", "bsq_identify_mutations",
             "bsq_im_result_counts", "bsq_im_result_copy", "bsq_last_pass_stats", "bsq_timer_start",
-            "bsq_timer_stop", "bsq_host_register", "bsq_host_unregister")
+            "bsq_timer_stop", "bsq_host_register", "bsq_host_unregister", "bsq_score_positions_noalloc")

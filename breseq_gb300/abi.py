@@ -98,6 +98,16 @@ class RaRecord(C.Structure):
     ]
 
 
+class RaRaw(C.Structure):
+    _fields_ = [
+        ("column", C.c_uint32), ("insert_position", C.c_uint32), ("score", C.c_double),
+        ("consensus_score", C.c_double), ("f", C.c_double * 5), ("frequency_lower", C.c_double),
+        ("frequency_upper", C.c_double), ("pos_info", (C.c_uint32 * 2) * 5), ("n", C.c_uint32),
+        ("ref_idx", C.c_uint8), ("var_idx", C.c_uint8), ("major_idx", C.c_uint8), ("minor_idx", C.c_uint8),
+        ("passed_consensus", C.c_uint8), ("passed_polymorphism", C.c_uint8), ("pad", C.c_uint8 * 2),
+    ]
+
+
 class McRecord(C.Structure):
     _fields_ = [
         ("tid", C.c_uint32), ("start", C.c_uint32), ("end", C.c_uint32), ("start_range", C.c_uint32),

@@ -17,6 +17,7 @@
 #include "bsq_common.h"
 #include "bsq_host.h"
 #include "bsq_kernels.h"
+#include "bsq_noalloc.h"
 
 using namespace bsq;
 
@@ -522,6 +523,50 @@ int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_
   if (device_ms) *device_ms = ctx->last_ms;
   if (kernel_launches) *kernel_launches = ctx->launches;
   if (main_kernel_ms) *main_kernel_ms = ctx->main_ms;
+  return BSQ_OK;
+}
+
+int bsq_score_positions_noalloc(bsq_ctx* ctx, int32_t sid, const bsq_im_params* p, const double* table,
+                                const uint32_t* d_tid, const uint32_t* d_pos0, uint32_t n_positions, bsq_ra_raw* d_ra,
+                                uint32_t ra_capacity, uint32_t* d_n_ra, uint32_t* d_qhist) {
+  if (!ctx || !p || !table || !d_n_ra || (n_positions && (!d_tid || !d_pos0)) || (ra_capacity && (!d_ra || !d_qhist)))
+    return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  SampleDev* s = find_sample(ctx, sid);
+  if (!s) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
+  if (!p->deletion_propagation_cutoff) return fail(ctx, BSQ_ERR_INVALID, "missing deletion cutoffs");
+  const uint32_t R = p->n_read_files, Q = p->n_quality;
+  if (R == 0 || Q == 0 || R > 255 || Q > 256) return fail(ctx, BSQ_ERR_INVALID, "error table dimensions out of range");
+  if ((uint64_t)R * 25 * Q > kNoAllocMaxTable)
+    return fail(ctx, BSQ_ERR_SIZE, "error table larger than the no-allocation limit (R x 25 x Q <= 32768)");
+  const uint64_t K = (uint64_t)s->mapq_values.size() * R * 2 * Q * 5;
+  if (K > kNoAllocMaxClasses)
+    return fail(ctx, BSQ_ERR_SIZE, "more likelihood classes than the no-allocation limit (32768)");
+  const uint32_t per_warp = std::max<uint32_t>(32, s->max_tile_reads);
+  const uint64_t fit = kNoAllocGatherEntries / per_warp;
+  if (fit == 0) return fail(ctx, BSQ_ERR_SIZE, "a column is covered by more reads than the no-allocation scratch holds");
+  CK(cudaSetDevice(ctx->device));
+  void* scratch = nullptr;
+  CK(noalloc_scratch_setup(ctx->device, &scratch));
+  cudaStream_t st = ctx->stream;
+  for (uint32_t t = 0; t < s->n_targets; t++)
+    CK(cudaMemsetAsync(s->tgt_failed.as<uint8_t>() + t, p->deletion_propagation_cutoff[t] < 0.0 ? 1 : 0, 1, st));
+  NoAllocJob J;
+  J.log10_table = table; J.R = R; J.Q = Q;
+  J.mapq_values = s->mapq_values.data(); J.n_mapq = (uint32_t)s->mapq_values.size();
+  J.tid = d_tid; J.pos0 = d_pos0; J.n_positions = n_positions; J.failed = s->tgt_failed.as<uint8_t>();
+  J.ra = d_ra; J.ra_cap = ra_capacity; J.n_ra = d_n_ra; J.qhist = d_qhist;
+  J.base_quality_cutoff = p->base_quality_cutoff; J.log10_ref_len = p->log10_ref_length;
+  J.mutation_cutoff = p->mutation_cutoff; J.poly_cutoff = p->polymorphism_cutoff;
+  J.precision_decimal = p->polymorphism_precision_decimal;
+  J.per_warp = per_warp;
+  J.n_warps = (uint32_t)std::min<uint64_t>((uint64_t)ctx->sms * 16, fit);
+  uint32_t err = 0;
+  CK(launch_noalloc_positions(scratch, make_dev_sample(*s), J, st, &err));
+  err &= ~kErrRaOverflow;
+  if (err) return fail(ctx, BSQ_ERR_DATA, "score_positions_noalloc: " + err_text(err));
+  uint32_t n_ra = 0;
+  CK(cudaMemcpy(&n_ra, d_n_ra, sizeof n_ra, cudaMemcpyDeviceToHost));
+  if (n_ra > ra_capacity) return fail(ctx, BSQ_ERR_SIZE, "more passing RA items than ra_capacity");
   return BSQ_OK;
 }
 

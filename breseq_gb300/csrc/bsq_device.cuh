@@ -1,0 +1,465 @@
+// Device code shared by the scoring kernels (bsq_kernels.cu) and the no-allocation variant
+// (bsq_noalloc.cu): pileup state of a read at a column, encodings, warp reductions, the FP64 EM of
+// fit_allele_frequencies / profile_log10_likelihood, and the per-column candidate scoring.
+#pragma once
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "bsq_common.h"
+
+namespace bsq {
+namespace {
+
+__device__ __forceinline__ uint8_t nib_at(const uint8_t* seq, uint64_t nib) {
+  uint8_t b = __ldg(seq + (nib >> 1));
+  return (nib & 1) ? (b & 0xF) : (b >> 4);
+}
+// 4-bit BAM base -> index A,C,G,T = 0..3; N/others -> -1 (src/breseq/common.h:253-265)
+__device__ __forceinline__ int bam_idx(uint8_t b) {
+  return b == 1 ? 0 : b == 2 ? 1 : b == 4 ? 2 : b == 8 ? 3 : -1;
+}
+// reference char -> index, 'N' -> 5, other -> -1 (common.h:267-279)
+__device__ __forceinline__ int chr_idx(uint8_t c) {
+  return c == 'A' ? 0 : c == 'C' ? 1 : c == 'G' ? 2 : c == 'T' ? 3 : c == 'N' ? 5 : -1;
+}
+__device__ __forceinline__ bool op_ref(uint32_t op) { return op == 0 || op == 2 || op == 3 || op == 7 || op == 8; }
+__device__ __forceinline__ bool op_qm(uint32_t op) { return op == 0 || op == 7 || op == 8; }
+
+struct Pile { int qpos; int indel; bool del; };
+
+// htslib's per-column read state (bam_plp_auto / resolve_cigar2 semantics) for a CIGAR with more
+// than a single aligned block; c must lie in [start, end).
+__device__ bool resolve_cigar(const uint32_t* cig, int n, uint32_t start, uint32_t c, Pile& e) {
+  uint32_t x = start;
+  int y = 0;
+  for (int k = 0; k < n; k++) {
+    uint32_t w = __ldg(cig + k), op = w & 0xF, len = w >> 4;
+    if (op_ref(op)) {
+      if (c < x + len) {
+        if (op_qm(op)) { e.qpos = y + (int)(c - x); e.del = false; }
+        else { e.qpos = y; e.del = true; }
+        e.indel = 0;
+        if (c == x + len - 1 && k + 1 < n) {
+          uint32_t w2 = __ldg(cig + k + 1), op2 = w2 & 0xF;
+          if (op2 == 2 && op != 2) {
+            int d = -(int)(w2 >> 4);
+            for (int j = k + 2; j < n; j++) { uint32_t wj = __ldg(cig + j); if ((wj & 0xF) == 2) d -= (int)(wj >> 4); else break; }
+            e.indel = d;
+          } else if (op2 == 1) {
+            int d = (int)(w2 >> 4);
+            for (int j = k + 2; j < n; j++) {
+              uint32_t wj = __ldg(cig + j), o = wj & 0xF;
+              if (o == 1) d += (int)(wj >> 4); else if (o != 6) break;
+            }
+            e.indel = d;
+          } else if (op2 == 6 && k + 2 < n) {
+            int l3 = 0;
+            for (int j = k + 2; j < n; j++) {
+              uint32_t wj = __ldg(cig + j), o = wj & 0xF;
+              if (o == 1) l3 += (int)(wj >> 4); else if (op_ref(o)) break;
+            }
+            if (l3 > 0) e.indel = l3;
+          }
+        }
+        return true;
+      }
+      x += len;
+      if (op_qm(op)) y += (int)len;
+    } else if (op == 1 || op == 4) {
+      y += (int)len;
+    }
+  }
+  return false;
+}
+
+__device__ __forceinline__ void resolve(const DevSample& S, const DevRead& rd, uint32_t c, Pile& e) {
+  if (rd.flags & kSimple) { e.qpos = (int)(c - rd.start) + rd.clip; e.indel = 0; e.del = false; }
+  else if (!resolve_cigar(S.cigar + rd.cigar_off, rd.n_cigar, rd.start, c, e)) { e.qpos = 0; e.indel = 0; e.del = true; }
+}
+
+// pileup_wrapper::is_trimmed (src/breseq/alignment.h:389-411), unsigned arithmetic as there
+__device__ __forceinline__ bool is_trimmed(const DevRead& rd, int qpos, bool past_base) {
+  uint32_t qp1 = (uint32_t)(qpos + 1);
+  if (rd.xl != kNoTag && qp1 <= rd.xl) return true;
+  if (rd.xr != kNoTag) {
+    uint32_t len = rd.len;
+    if (len - qp1 + 1u <= rd.xr) return true;
+    if (past_base && (len - qp1 == rd.xr)) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ int query_end0(const DevSample& S, const DevRead& rd, uint32_t r) {
+  return (rd.flags & kSimple) ? (int)rd.clip + (int)(rd.end - rd.start) - 1 : (int)S.qb[r].qe0;
+}
+__device__ __forceinline__ int query_start0(const DevSample& S, const DevRead& rd, uint32_t r) {
+  return (rd.flags & kSimple) ? (int)rd.clip : (int)S.qb[r].qs0;
+}
+__device__ __forceinline__ int bounds_end0(const DevSample& S, const DevRead& rd, uint32_t r) {
+  return (rd.flags & kSimple) ? (int)rd.clip + (int)(rd.end - rd.start) - 1 : (int)S.qb[r].qbe;
+}
+
+__device__ __forceinline__ uint32_t target_of(const DevSample& S, uint32_t c) {
+  uint32_t lo = 0, hi = S.n_targets;  // largest t with tpoff[t] <= c
+  while (hi - lo > 1) { uint32_t mid = (lo + hi) >> 1; if (__ldg(S.tpoff + mid) <= c) lo = mid; else hi = mid; }
+  return lo;
+}
+
+// ============================================================================ candidate scoring
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  return v;
+}
+__device__ __forceinline__ uint32_t warp_sum_u(uint32_t v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+
+// Entries of the per-warp gather list (uint4): x = read index, y = qpos | (on_base_indel + 1) << 16,
+// z = likelihood class for the current slot (0xFFFFFFFF = not scored), w = obs | q << 8 | strand << 16.
+// E-step sweep of fit_allele_frequencies / profile_log10_likelihood: sum_w[b] over the reads at the
+// given frequencies (allowed alleles only).  Returns the per-warp totals in all lanes.
+__device__ void em_sweep(const uint4* ents, uint32_t m, const ClassTable& T, const double f[5], unsigned allowed,
+                         double sw[5]) {
+  double a[5] = {0, 0, 0, 0, 0};
+  for (uint32_t i = threadIdx.x & 31; i < m; i += 32) {
+    const uint32_t cls = ents[i].z;
+    if (cls == 0xFFFFFFFFu) continue;
+    const double* r = T.r64 + (size_t)cls * 5;
+    double p[5], s = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) { p[b] = ((allowed >> b) & 1) ? f[b] * __ldg(r + b) : 0.0; s += p[b]; }
+    if (s > 0.0) {
+      const double inv = 1.0 / s;
+#pragma unroll
+      for (int b = 0; b < 5; b++) a[b] += p[b] * inv;
+    } else {
+#pragma unroll
+      for (int b = 0; b < 5; b++) if ((allowed >> b) & 1) a[b] += f[b];
+    }
+  }
+#pragma unroll
+  for (int b = 0; b < 5; b++) sw[b] = warp_sum(a[b]);
+}
+
+__device__ double em_loglik(const uint4* ents, uint32_t m, const ClassTable& T, const double f[5], unsigned allowed) {
+  double ll = 0;
+  for (uint32_t i = threadIdx.x & 31; i < m; i += 32) {
+    const uint32_t cls = ents[i].z;
+    if (cls == 0xFFFFFFFFu) continue;
+    const double* r = T.r64 + (size_t)cls * 5;
+    double s = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) if ((allowed >> b) & 1) s += f[b] * __ldg(r + b);
+    if (s > 0.0) ll += log10(s) + __ldg(T.lpmax64 + cls);
+  }
+  return warp_sum(ll);
+}
+
+struct Fit { double f[5]; double ll; };
+
+// fit_allele_frequencies (identify_mutations.cpp:3241-3318).  The log-likelihood the reference
+// commits is the one evaluated at the frequencies entering the final iteration, so it is computed
+// once, after convergence, at those frequencies.
+__device__ Fit em_fit(const uint4* ents, uint32_t m, uint32_t n, const uint32_t obs_count[5], const ClassTable& T,
+                      unsigned allowed, double tol) {
+  Fit F;
+  double f[5] = {0, 0, 0, 0, 0}, fprev[5];
+  double tot = 0;
+#pragma unroll
+  for (int b = 0; b < 5; b++) if ((allowed >> b) & 1) { f[b] = 0.5 + (double)obs_count[b]; }
+#pragma unroll
+  for (int b = 0; b < 5; b++) tot += f[b];
+#pragma unroll
+  for (int b = 0; b < 5; b++) f[b] /= tot;
+  for (int it = 1; it <= 50; it++) {
+    double sw[5];
+    em_sweep(ents, m, T, f, allowed, sw);
+    double md = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) {
+      fprev[b] = f[b];
+      if (!((allowed >> b) & 1)) continue;
+      const double fn = sw[b] / (double)n;
+      md = fmax(md, fabs(fn - f[b]));
+      f[b] = fn;
+    }
+    if (md < tol) break;
+  }
+  F.ll = em_loglik(ents, m, T, fprev, allowed);
+#pragma unroll
+  for (int b = 0; b < 5; b++) F.f[b] = f[b];
+  return F;
+}
+
+// profile_log10_likelihood (identify_mutations.cpp:3094-3143)
+__device__ double em_profile(const uint4* ents, uint32_t m, const ClassTable& T, const double full[5], int v,
+                             double ff, double tol) {
+  double f[5], fprev[5], other = 0;
+#pragma unroll
+  for (int b = 0; b < 5; b++) if (b != v) other += full[b];
+#pragma unroll
+  for (int b = 0; b < 5; b++) f[b] = (b == v) ? ff : ((other > 0.0) ? (1.0 - ff) * full[b] / other : (1.0 - ff) / 4.0);
+  for (int it = 0; it < 50; it++) {
+    double sw[5];
+    em_sweep(ents, m, T, f, 31u, sw);
+    double others = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) if (b != v) others += sw[b];
+    double md = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) {
+      fprev[b] = f[b];
+      if (b == v) continue;
+      const double fn = (others > 0.0) ? (1.0 - ff) * sw[b] / others : (1.0 - ff) / 4.0;
+      md = fmax(md, fabs(fn - f[b]));
+      f[b] = fn;
+    }
+    if (md < tol) break;
+  }
+  return em_loglik(ents, m, T, fprev, 31u);
+}
+
+__device__ __forceinline__ int am_major(const double f[5], uint32_t n) {
+  if (n == 0) return 5;
+  int best = 0;
+  for (int b = 1; b < 5; b++) if (f[b] > f[best]) best = b;
+  return f[best] > 0.0 ? best : 5;
+}
+__device__ __forceinline__ int am_next(const double f[5], uint32_t n, int excl) {
+  if (n == 0) return 5;
+  const double thr = 0.5 / (double)n;
+  int best = 5;
+  for (int b = 0; b < 5; b++) {
+    if (b == excl || f[b] < thr) continue;
+    if (best == 5 || f[b] > f[best]) best = b;
+  }
+  return best;
+}
+
+// Where a scored column's RA items go, and the thresholds of the slot decisions.
+struct CandOut {
+  RaDev* ra;
+  unsigned int* n_ra;
+  uint32_t ra_cap;
+  uint32_t* qhist;
+  uint32_t Qhist;
+  uint32_t* err;
+  uint32_t base_quality_cutoff;
+  double log10_ref_len, mutation_cutoff, poly_cutoff, precision_decimal;
+};
+
+// Scores one reference column (called by a whole warp): gathers the reads covering column c in BAM
+// order into the warp's list `ents` (capacity `cap`), then for insert slot 0 (when do_slot0) and every
+// insert slot that exists, scores the slot in FP64: summed log10 likelihoods and pure-genotype call,
+// the five-allele EM, the variant-presence EM, and for emitted RA items the profile-likelihood
+// bounds and the strand / quality tallies (identify_mutations.cpp:1359-1910).  When `recompute`,
+// the slot-0 consensus call is written back to call[c].
+__device__ void score_candidate_column(const DevSample& S, const ClassTable& T, const CandOut& A, uint32_t c,
+                                       bool do_slot0, bool recompute, ColCall cl0, ColCall* call, uint4* ents,
+                                       uint32_t cap) {
+  const int lane = threadIdx.x & 31;
+  // ---- gather covering reads in BAM order
+  const uint2 rr = __ldg(S.tile_range + (c >> 5));
+  uint32_t m = 0;
+  bool overflow = false;
+  for (uint32_t b0 = rr.x; b0 < rr.y; b0 += 32) {
+    const uint32_t r = b0 + lane;
+    bool ok = false;
+    Pile e;
+    DevRead rd;
+    if (r < rr.y) {
+      rd = S.reads[r];
+      ok = !(rd.flags & kSkip) && c >= rd.start && c < rd.end;
+      if (ok) resolve(S, rd, c, e);
+    }
+    const unsigned bal = __ballot_sync(0xFFFFFFFFu, ok);
+    const uint32_t slot = m + __popc(bal & ((1u << lane) - 1));
+    if (ok && slot < cap) {
+      const int obi = e.del ? -1 : max(e.indel, 0);
+      ents[slot] = make_uint4(r, (uint32_t)e.qpos | ((uint32_t)(obi + 1) << 16), 0xFFFFFFFFu, 0);
+    }
+    m += __popc(bal);
+  }
+  if (m > cap) { overflow = true; m = cap; }
+  if (overflow) { if (lane == 0) atomicOr(A.err, kErrScratch); return; }
+  __syncwarp();
+  int k = do_slot0 ? 0 : 1;
+  const uint8_t refc0 = __ldg(S.ref + c);
+  for (;; k++) {
+    // ---- build the slot's read bases (identify_mutations.cpp:1392-1658)
+    uint32_t pc[5][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    uint32_t n_local = 0;
+    bool next_local = false;
+    double s64[5] = {0, 0, 0, 0, 0};
+    for (uint32_t i = lane; i < m; i += 32) {
+      uint4 en = ents[i];
+      en.z = 0xFFFFFFFFu;
+      const uint32_t r = en.x;
+      const DevRead rd = S.reads[r];
+      const int qpos = (int)(en.y & 0xFFFF);
+      const int obi = (int)(en.y >> 16) - 1;
+      const bool rev = rd.flags & kRev;
+      uint8_t base = '.';
+      bool past = true;
+      if (obi >= k) { base = nib_at(S.seq, rd.seq_off + qpos + k); past = false; }
+      if (base != 15) {
+        const bool red = rd.flags & kRedundant;
+        if (!red && obi > k) next_local = true;
+        if (!red && !is_trimmed(rd, qpos, past)) {
+          int qp = qpos;
+          bool ok = true;
+          if (obi == -1) {
+            qp += 1 - (int)rev;
+            if (qp >= (int)rd.len || nib_at(S.seq, rd.seq_off + qp) == 15) ok = false;
+          } else if (k > 0) {
+            int mo = k < obi ? k : obi;
+            qp += mo + 1 - (int)rev;
+            if (qp > bounds_end0(S, rd, r) || nib_at(S.seq, rd.seq_off + qp) == 15) ok = false;
+          }
+          if (ok) {
+            const int obs = (base == '.') ? 4 : bam_idx(base);
+            const uint32_t q = __ldg(S.qual + rd.seq_off + qp);
+            const uint32_t rs = rd.rfile;
+            if (obs < 0 || q >= T.Q || rs >= T.R) ok = false;
+            else if (q >= A.base_quality_cutoff) {
+              const uint32_t cls = ((((uint32_t)rd.mapq_idx * T.R + rs) * 2u + (rev ? 1u : 0u)) * T.Q + q) * 5u + (uint32_t)obs;
+              en.z = cls;
+              en.w = (uint32_t)obs | (q << 8) | ((rev ? 1u : 0u) << 16);
+              pc[obs][rev ? 1 : 0]++;
+              n_local++;
+              const double* lp = T.lp64 + (size_t)cls * 5;
+#pragma unroll
+              for (int b = 0; b < 5; b++) s64[b] += __ldg(lp + b);
+            }
+          }
+        }
+      }
+      ents[i] = en;
+    }
+    __syncwarp();
+    const uint32_t n = warp_sum_u(n_local);
+    const bool next_exists = __any_sync(0xFFFFFFFFu, next_local);
+    uint32_t cnt[5];
+    uint32_t pinfo[5][2];
+#pragma unroll
+    for (int b = 0; b < 5; b++) {
+      pinfo[b][0] = warp_sum_u(pc[b][0]);
+      pinfo[b][1] = warp_sum_u(pc[b][1]);
+      cnt[b] = pinfo[b][0] + pinfo[b][1];
+      s64[b] = warp_sum(s64[b]);
+    }
+    const uint8_t refc = (k == 0) ? refc0 : (uint8_t)'.';
+    const int ref_idx = (refc == '.') ? 4 : (chr_idx(refc) < 0 ? 5 : chr_idx(refc));
+    // ---- pure genotype call (identify_mutations.cpp:3398-3433)
+    int best = 5;
+    double cscore = __longlong_as_double(0x7ff8000000000000ll);
+    if (n > 0) {
+      best = 0;
+      for (int b = 1; b < 5; b++) if (s64[b] > s64[best]) best = b;
+      double off = -DBL_MAX;
+      for (int b = 0; b < 5; b++) if (b != best) off = fmax(off, s64[b]);
+      double te = 0;
+      for (int b = 0; b < 5; b++) if (b != best) te += exp10(s64[b] - off);
+      cscore = s64[best] - (log10(te) + off) - A.log10_ref_len;
+    }
+    if (k == 0 && recompute && call != nullptr && lane == 0) {
+      ColCall cl = cl0;
+      cl.best = (uint8_t)best;
+      cl.score = cscore;
+      cl.flags = (uint8_t)((cl.flags & ~kBasePredicted) | ((cscore >= A.mutation_cutoff) ? kBasePredicted : 0));
+      call[c] = cl;
+    }
+    const bool passed_cons = (best != ref_idx) && !isnan(cscore) && cscore > 0;
+    // ---- five-allele fit and variant presence (identify_mutations.cpp:1795-1821)
+    Fit full;
+    for (int b = 0; b < 5; b++) full.f[b] = 0;
+    full.ll = 0;
+    int maj = 5, mnr = 5, var = 5;
+    double vscore = __longlong_as_double(0x7ff8000000000000ll);
+    bool passed_poly = false;
+    if (n > 0) {
+      full = em_fit(ents, m, n, cnt, T, 31u, A.precision_decimal);
+      maj = am_major(full.f, n);
+      mnr = am_next(full.f, n, maj);
+      var = am_next(full.f, n, ref_idx);
+      if (var != 5) {
+        Fit nf = em_fit(ents, m, n, cnt, T, 31u & ~(1u << var), A.precision_decimal);
+        vscore = (full.ll - nf.ll) - A.log10_ref_len;
+        passed_poly = vscore >= A.poly_cutoff;
+      }
+    }
+    if (passed_cons || passed_poly) {
+      // ---- write_RA_frequency_bounds (identify_mutations.cpp:3175-3217)
+      double lower = 0.0, upper = 1.0;
+      if (n > 0 && var < 5) {
+        const double D = 0.587566;
+        const double fh = full.f[var];
+        const double tol = A.precision_decimal;
+        const double target = em_profile(ents, m, T, full.f, var, fh, tol) - D;
+        if (em_profile(ents, m, T, full.f, var, 0.0, tol) >= target) lower = 0.0;
+        else {
+          double lo = 0.0, hi = fh;
+          for (int i = 0; i < 40 && (hi - lo) > tol; i++) {
+            double mid = 0.5 * (lo + hi);
+            if (em_profile(ents, m, T, full.f, var, mid, tol) >= target) hi = mid; else lo = mid;
+          }
+          lower = hi;
+        }
+        if (em_profile(ents, m, T, full.f, var, 1.0, tol) >= target) upper = 1.0;
+        else {
+          double lo = fh, hi = 1.0;
+          for (int i = 0; i < 40 && (hi - lo) > tol; i++) {
+            double mid = 0.5 * (lo + hi);
+            if (em_profile(ents, m, T, full.f, var, mid, tol) >= target) lo = mid; else hi = mid;
+          }
+          upper = lo;
+        }
+      }
+      uint32_t slot = 0;
+      if (lane == 0) slot = atomicAdd(A.n_ra, 1u);
+      slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+      if (slot < A.ra_cap) {
+        if (lane == 0) {
+          RaDev o;
+          o.col = c; o.insert_position = (uint32_t)k;
+          o.score = vscore; o.consensus_score = cscore;
+          for (int b = 0; b < 5; b++) { o.f[b] = full.f[b]; o.pos_info[b][0] = pinfo[b][0]; o.pos_info[b][1] = pinfo[b][1]; }
+          o.lower = lower; o.upper = upper; o.n = n;
+          o.ref_idx = (uint8_t)ref_idx; o.var_idx = (uint8_t)var; o.maj_idx = (uint8_t)maj; o.min_idx = (uint8_t)mnr;
+          o.passed_cons = passed_cons; o.passed_poly = passed_poly; o.pad[0] = o.pad[1] = 0;
+          A.ra[slot] = o;
+        }
+        // qualities of the major and minor alleles' reads for the K-S test (:3009-3033)
+        uint32_t* qh = A.qhist + (size_t)slot * 2 * A.Qhist;
+        for (uint32_t i = lane; i < 2 * A.Qhist; i += 32) qh[i] = 0;
+        __syncwarp();
+        for (uint32_t i = lane; i < m; i += 32) {
+          const uint4 en = ents[i];
+          if (en.z == 0xFFFFFFFFu) continue;
+          const int obs = (int)(en.w & 0xFF);
+          const uint32_t q = (en.w >> 8) & 0xFF;
+          if (q >= A.Qhist) continue;
+          if (obs == maj) atomicAdd(qh + q, 1u);
+          if (obs == mnr) atomicAdd(qh + A.Qhist + q, 1u);
+        }
+      } else if (lane == 0) {
+        atomicOr(A.err, kErrRaOverflow);
+      }
+    }
+    if (!next_exists) break;
+    __syncwarp();
+  }
+}
+
+}  // namespace
+}  // namespace bsq

@@ -232,6 +232,48 @@ int bsq_im_result_copy(const bsq_ctx* ctx, bsq_ra_record* ra, uint64_t ra_cap,
 int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_launches,
                         double* main_kernel_ms);
 
+/* ---------------------------------------------------------------- scoring without allocation */
+
+/* Raw values of one RA item as the scoring kernel writes them (device memory).  `column` is the
+ * target's padded column: target_offset[tid] + tid + (position - 1).  Base indices are 0..4 =
+ * A,C,G,T,'.', 5 = N; pos_info is [base][top, bottom] strand coverage of the scored read bases. */
+typedef struct bsq_ra_raw {
+    uint32_t column;
+    uint32_t insert_position;
+    double   score, consensus_score;
+    double   f[5];
+    double   frequency_lower, frequency_upper;
+    uint32_t pos_info[5][2];
+    uint32_t n;
+    uint8_t  ref_idx, var_idx, major_idx, minor_idx, passed_consensus, passed_polymorphism, pad[2];
+} bsq_ra_raw;
+
+/* Score the given reference positions (all of their insert slots) of a resident sample and write the
+ * RA items that pass into caller-owned device memory, allocating nothing.  It has no counterpart in
+ * the reference, which scores every position of every target in one pileup.  It is for callers that
+ * cannot call cudaMalloc while they run: a serving loop with jobs in flight on other streams, where
+ * cudaMalloc/cudaFree may synchronize the device and stall them, or a program that has handed all
+ * of HBM to its own arena.  The scoring is the same as bsq_identify_mutations' candidate scoring.
+ *
+ * d_tid / d_pos0 (0-based positions) are device arrays of n_positions entries.  d_ra (ra_capacity
+ * records), d_n_ra (one counter, set by the call) and d_qhist (ra_capacity x 2 x n_quality counters:
+ * the qualities of the major- and minor-allele read bases of each record) are device memory the
+ * caller owns.  Records appear in completion order, not position order.  Targets whose deletion
+ * propagation cutoff is negative are skipped, as bsq_identify_mutations skips them.
+ *
+ * Scratch: one fixed 20 MiB device array in the library, held by every GPU that loads it until the
+ * process exits.  Limits: n_read_files x 25 x n_quality <= 32768, (distinct MAPQ values) x
+ * n_read_files x 2 x n_quality x 5 <= 32768 likelihood classes; larger tables are rejected with
+ * BSQ_ERR_SIZE.  The first call on a device fetches the array's device address (cudaGetSymbolAddress),
+ * so make that first call before any stream capture.  All calls share the array and each clears its
+ * counters on entry: calls that overlap on the GPU (other threads, other contexts on the same device)
+ * race on it and must be serialized by the caller.  Returns BSQ_ERR_SIZE, with *d_n_ra holding the
+ * number of passing items, when more than ra_capacity pass. */
+int bsq_score_positions_noalloc(bsq_ctx* ctx, int32_t sample_id, const bsq_im_params* p,
+                                const double* log10_prob_table, const uint32_t* d_tid, const uint32_t* d_pos0,
+                                uint32_t n_positions, bsq_ra_raw* d_ra, uint32_t ra_capacity, uint32_t* d_n_ra,
+                                uint32_t* d_qhist);
+
 /* Device-timeline timer on the context's stream: CUDA events recorded where the passes launch
  * their kernels, so the interval covers exactly the work issued in between (and any idle gaps). */
 int bsq_timer_start(bsq_ctx* ctx);
