@@ -23,19 +23,23 @@ using namespace bsq;
 
 namespace {
 
+// Device buffer from the device's stream-ordered pool: the context keeps the pool's memory instead of
+// returning it to the driver, so loading and freeing samples per job costs no cudaMalloc/cudaFree.
 struct DevMem {
   void* p = nullptr;
   size_t bytes = 0;
+  cudaStream_t st = nullptr;
   DevMem() = default;
   DevMem(const DevMem&) = delete;
   DevMem& operator=(const DevMem&) = delete;
   ~DevMem() { release(); }
-  void release() { if (p) cudaFree(p); p = nullptr; bytes = 0; }
-  cudaError_t alloc(size_t n) {
+  void release() { if (p) cudaFreeAsync(p, st); p = nullptr; bytes = 0; }
+  cudaError_t alloc(size_t n, cudaStream_t stream) {
     if (n == 0) n = 16;
     if (p && bytes >= n) return cudaSuccess;
     release();
-    cudaError_t e = cudaMalloc(&p, n);
+    st = stream;
+    cudaError_t e = cudaMallocAsync(&p, n, stream);
     if (e == cudaSuccess) bytes = n;
     return e;
   }
@@ -65,6 +69,7 @@ struct bsq_ctx {
   int32_t next_id = 1;
   // working memory reused across calls
   DevMem cov, call, blk, total, cand, next, ra, n_ra, qhist, scratch, errw, lp64, r64, lpmax64, lp32, stats;
+  DevMem keep, kcol, kcov, kcall, d_prop, d_seed;
   DevMem counts, hist, found;
   std::vector<bsq_ra_record> res_ra;
   std::vector<bsq_mc_record> res_mc;
@@ -99,7 +104,7 @@ static std::string err_text(uint32_t e) {
 
 template <class T>
 static cudaError_t upload(DevMem& m, const T* src, uint64_t n, cudaStream_t st) {
-  cudaError_t e = m.alloc(n * sizeof(T) + 16);
+  cudaError_t e = m.alloc(n * sizeof(T) + 16, st);
   if (e != cudaSuccess) return e;
   if (n) e = cudaMemcpyAsync(m.p, src, n * sizeof(T), cudaMemcpyHostToDevice, st);
   return e;
@@ -150,6 +155,11 @@ int bsq_create(bsq_ctx** out, int device) {
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return BSQ_ERR_CUDA;
   c->sms = prop.multiProcessorCount;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return BSQ_ERR_CUDA;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;   // keep freed blocks in this process's pool for the next sample
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       cudaEventCreate(&c->evm0) != cudaSuccess || cudaEventCreate(&c->evm1) != cudaSuccess ||
       cudaEventCreate(&c->evt0) != cudaSuccess || cudaEventCreate(&c->evt1) != cudaSuccess)
@@ -163,6 +173,13 @@ void bsq_destroy(bsq_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->samples.clear();
+  // pool blocks are returned on the context's stream, so before it goes
+  for (DevMem* m : {&ctx->cov, &ctx->call, &ctx->blk, &ctx->total, &ctx->cand, &ctx->next, &ctx->ra, &ctx->n_ra,
+                    &ctx->qhist, &ctx->scratch, &ctx->errw, &ctx->lp64, &ctx->r64, &ctx->lpmax64, &ctx->lp32,
+                    &ctx->stats, &ctx->counts, &ctx->hist, &ctx->found, &ctx->keep, &ctx->kcol, &ctx->kcov,
+                    &ctx->kcall, &ctx->d_prop, &ctx->d_seed})
+    m->release();
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   cudaEventDestroy(ctx->ev0); cudaEventDestroy(ctx->ev1); cudaEventDestroy(ctx->evm0); cudaEventDestroy(ctx->evm1);
   cudaEventDestroy(ctx->evt0); cudaEventDestroy(ctx->evt1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -222,7 +239,7 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   }
   cudaStream_t st = ctx->stream;
   // reference, one '\0' separator after each target
-  CK(s->ref.alloc(s->n_cols + 64));
+  CK(s->ref.alloc(s->n_cols + 64, st));
   CK(cudaMemsetAsync(s->ref.p, 0, s->n_cols + 64, st));
   for (uint32_t t = 0; t < T; t++) {
     const uint64_t len = s->toff[t + 1] - s->toff[t];
@@ -231,7 +248,7 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   CK(upload(s->d_tpoff, s->tpoff.data(), T + 1, st));
   CK(upload(s->tgt_group, s->group.data(), T, st));
   CK(upload(s->tgt_called, called.data(), T, st));
-  CK(s->tgt_failed.alloc(T + 16));
+  CK(s->tgt_failed.alloc(T + 16, st));
   CK(cudaMemsetAsync(s->tgt_failed.p, 0, T, st));
   // records: raw arrays -> packed 32-byte records on the device
   const uint64_t n = rd->n_reads;
@@ -252,10 +269,10 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   CK(upload(s->cigar, rd->cigar, rd->n_cigar_total, st));
   CK(upload(s->seq, rd->seq, (rd->n_bases_total + 1) / 2, st));
   CK(upload(s->qual, rd->qual, rd->n_bases_total, st));
-  CK(s->reads.alloc(n * sizeof(DevRead) + 64));
-  CK(s->qb.alloc(n * sizeof(QBounds) + 64));
-  CK(s->rstart.alloc(n * 4 + 64));
-  CK(ctx->stats.alloc(64));
+  CK(s->reads.alloc(n * sizeof(DevRead) + 64, st));
+  CK(s->qb.alloc(n * sizeof(QBounds) + 64, st));
+  CK(s->rstart.alloc(n * 4 + 64, st));
+  CK(ctx->stats.alloc(64, st));
   CK(cudaMemsetAsync(ctx->stats.p, 0, 64, st));
   uint32_t* stats = ctx->stats.as<uint32_t>();  // [0] err, [1] maxspan, [2..9] mapq mask, [10] max tile reads
   RawSoA in;
@@ -283,7 +300,7 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   DevMem dmap;
   CK(upload(dmap, map, 256, st));
   CK(launch_mapq_index(s->reads.as<DevRead>(), s->mapq.as<uint8_t>(), dmap.as<uint8_t>(), (uint32_t)n, st));
-  CK(s->tile_range.alloc((size_t)s->n_tiles * sizeof(uint2) + 16));
+  CK(s->tile_range.alloc((size_t)s->n_tiles * sizeof(uint2) + 16, st));
   CK(cudaMemsetAsync(stats + 10, 0, 4, st));
   CK(launch_tile_range(s->rstart.as<uint32_t>(), (uint32_t)n, s->n_tiles, s->maxspan, s->tile_range.as<uint2>(), stats + 10, st));
   CK(cudaMemcpyAsync(h + 10, stats + 10, 4, cudaMemcpyDeviceToHost, st));
@@ -317,10 +334,10 @@ int bsq_error_count(bsq_ctx* ctx, int32_t sid, const bsq_ec_params* p, bsq_ec_re
   const uint32_t R = p->n_read_files, Q = p->n_quality, G = s->n_groups;
   const size_t nbins = (size_t)R * 25 * Q;
   const uint32_t cap = s->max_tile_reads + 2;
-  CK(ctx->counts.alloc(nbins * 8));
-  CK(ctx->hist.alloc((size_t)G * cap * 8));
-  CK(ctx->found.alloc((size_t)s->n_targets * 16 + 16));
-  CK(ctx->errw.alloc(16));
+  CK(ctx->counts.alloc(nbins * 8, st));
+  CK(ctx->hist.alloc((size_t)G * cap * 8, st));
+  CK(ctx->found.alloc((size_t)s->n_targets * 16 + 16, st));
+  CK(ctx->errw.alloc(16, st));
   CK(cudaMemsetAsync(ctx->counts.p, 0, nbins * 8, st));
   CK(cudaMemsetAsync(ctx->hist.p, 0, (size_t)G * cap * 8, st));
   CK(cudaMemsetAsync(ctx->found.p, 0, (size_t)s->n_targets * 16 + 16, st));
@@ -413,15 +430,15 @@ int bsq_identify_mutations(bsq_ctx* ctx, int32_t sid, const bsq_im_params* p, co
   for (uint32_t t = 0; t < s->n_targets; t++) failed[t] = p->deletion_propagation_cutoff[t] < 0.0;
   CK(cudaMemcpyAsync(s->tgt_failed.p, failed.data(), s->n_targets, cudaMemcpyHostToDevice, st));
   const uint32_t ncol = s->n_cols;
-  CK(ctx->cov.alloc((size_t)ncol * sizeof(ColCov)));
-  CK(ctx->call.alloc((size_t)ncol * sizeof(ColCall)));
+  CK(ctx->cov.alloc((size_t)ncol * sizeof(ColCov), st));
+  CK(ctx->call.alloc((size_t)ncol * sizeof(ColCall), st));
   const uint32_t nblk = (ncol + 255) / 256;
-  CK(ctx->blk.alloc((size_t)nblk * 4 + 16));
-  CK(ctx->total.alloc(16));
-  CK(ctx->cand.alloc((size_t)ncol * 4 + 16));
-  CK(ctx->next.alloc(16));
-  CK(ctx->n_ra.alloc(16));
-  CK(ctx->errw.alloc(16));
+  CK(ctx->blk.alloc((size_t)nblk * 4 + 16, st));
+  CK(ctx->total.alloc(16, st));
+  CK(ctx->cand.alloc((size_t)ncol * 4 + 16, st));
+  CK(ctx->next.alloc(16, st));
+  CK(ctx->n_ra.alloc(16, st));
+  CK(ctx->errw.alloc(16, st));
   CK(cudaMemsetAsync(ctx->errw.p, 0, 16, st));
   DevSample S = make_dev_sample(*s);
   ImArgs A;
@@ -445,13 +462,13 @@ int bsq_identify_mutations(bsq_ctx* ctx, int32_t sid, const bsq_im_params* p, co
   // ---- candidate columns: FP64 EM, presence score, bounds
   const int n_warps = ctx->sms * 16;
   const uint32_t per_warp = std::max<uint32_t>(32, s->max_tile_reads);
-  CK(ctx->scratch.alloc((size_t)n_warps * per_warp * sizeof(uint4)));
+  CK(ctx->scratch.alloc((size_t)n_warps * cand_warp_stride(per_warp) * sizeof(uint4), st));
   uint32_t ra_cap = n_cand * 2 + 1024;
   const uint32_t Qh = p->n_quality;
   uint32_t n_ra = 0;
   for (int attempt = 0; attempt < 4; attempt++) {
-    CK(ctx->ra.alloc((size_t)ra_cap * sizeof(RaDev)));
-    CK(ctx->qhist.alloc((size_t)ra_cap * 2 * Qh * 4));
+    CK(ctx->ra.alloc((size_t)ra_cap * sizeof(RaDev), st));
+    CK(ctx->qhist.alloc((size_t)ra_cap * 2 * Qh * 4, st));
     CK(cudaMemsetAsync(ctx->next.p, 0, 16, st));
     CK(cudaMemsetAsync(ctx->n_ra.p, 0, 16, st));
     CandArgs C;
@@ -473,29 +490,63 @@ int bsq_identify_mutations(bsq_ctx* ctx, int32_t sid, const bsq_im_params* p, co
   }
   std::vector<RaDev> ra(n_ra);
   std::vector<uint32_t> qh((size_t)n_ra * 2 * Qh);
-  std::vector<ColCov> cov(ncol);
-  std::vector<ColCall> call(ncol);
   uint32_t err = 0;
   if (n_ra) {
     CK(cudaMemcpyAsync(ra.data(), ctx->ra.p, (size_t)n_ra * sizeof(RaDev), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(qh.data(), ctx->qhist.p, qh.size() * 4, cudaMemcpyDeviceToHost, st));
   }
-  CK(cudaMemcpyAsync(cov.data(), ctx->cov.p, (size_t)ncol * sizeof(ColCov), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(call.data(), ctx->call.p, (size_t)ncol * sizeof(ColCall), cudaMemcpyDeviceToHost, st));
+  host::SampleLayout L;
+  L.tpoff = &s->tpoff; L.toff = &s->toff; L.order = &s->order;
+  std::vector<ColCov> cov;
+  std::vector<ColCall> call;
+  std::vector<uint32_t> kept;
+  if (pos_out) {
+    // every column comes back: per-position arrays were asked for
+    cov.resize(ncol);
+    call.resize(ncol);
+    CK(cudaMemcpyAsync(cov.data(), ctx->cov.p, (size_t)ncol * sizeof(ColCov), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(call.data(), ctx->call.p, (size_t)ncol * sizeof(ColCall), cudaMemcpyDeviceToHost, st));
+  } else {
+    // only the columns where the MC / UN state machines can change state
+    CK(upload(ctx->d_prop, p->deletion_propagation_cutoff, s->n_targets, st));
+    CK(upload(ctx->d_seed, p->deletion_seed_cutoff, s->n_targets, st));
+    CK(ctx->keep.alloc(ncol + 16, st));
+    CK(ctx->kcol.alloc((size_t)ncol * 4 + 16, st));
+    CK(ctx->kcov.alloc((size_t)ncol * sizeof(ColCov) + 16, st));
+    CK(ctx->kcall.alloc((size_t)ncol * sizeof(ColCall) + 16, st));
+    CK(launch_intervals(ctx->cov.as<ColCov>(), ctx->call.as<ColCall>(), ncol, s->d_tpoff.as<uint32_t>(), s->n_targets,
+                        s->tgt_called.as<uint8_t>(), s->tgt_failed.as<uint8_t>(), ctx->d_prop.as<double>(),
+                        ctx->d_seed.as<double>(), ctx->keep.as<uint8_t>(), ctx->blk.as<uint32_t>(),
+                        ctx->total.as<uint32_t>(), ctx->kcol.as<uint32_t>(), ctx->kcov.as<ColCov>(),
+                        ctx->kcall.as<ColCall>(), st));
+    uint32_t nk = 0;
+    CK(cudaMemcpyAsync(&nk, ctx->total.p, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    kept.resize(nk);
+    cov.resize(nk);
+    call.resize(nk);
+    if (nk) {
+      CK(cudaMemcpyAsync(kept.data(), ctx->kcol.p, (size_t)nk * 4, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(cov.data(), ctx->kcov.p, (size_t)nk * sizeof(ColCov), cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(call.data(), ctx->kcall.p, (size_t)nk * sizeof(ColCall), cudaMemcpyDeviceToHost, st));
+    }
+  }
   CK(cudaMemcpyAsync(&err, ctx->errw.p, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaEventRecord(ctx->ev1, st));
   CK(cudaStreamSynchronize(st));
   float ms = 0, mms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   cudaEventElapsedTime(&mms, ctx->evm0, ctx->evm1);
-  ctx->last_ms = ms; ctx->main_ms = mms; ctx->launches = 4 + (n_cand ? 1 : 0);
+  ctx->last_ms = ms; ctx->main_ms = mms; ctx->launches = 4 + (n_cand ? 1 : 0) + (pos_out ? 0 : 4);
   if (err) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(err));
   // ---- host assembly
-  host::SampleLayout L;
-  L.tpoff = &s->tpoff; L.toff = &s->toff; L.order = &s->order;
   host::assemble_ra(ra, qh, Qh, L, ctx->res_ra);
-  host::intervals(cov, call, L, p, ctx->res_mc, ctx->res_un);
-  if (pos_out) host::fill_positions(cov, call, L, pos_out);
+  if (pos_out) {
+    host::intervals(cov, call, L, p, ctx->res_mc, ctx->res_un);
+    host::fill_positions(cov, call, L, pos_out);
+  } else {
+    host::intervals_sparse(kept, cov, call, L, p, ctx->res_mc, ctx->res_un);
+  }
   return BSQ_OK;
 }
 
@@ -542,7 +593,7 @@ int bsq_score_positions_noalloc(bsq_ctx* ctx, int32_t sid, const bsq_im_params* 
   if (K > kNoAllocMaxClasses)
     return fail(ctx, BSQ_ERR_SIZE, "more likelihood classes than the no-allocation limit (32768)");
   const uint32_t per_warp = std::max<uint32_t>(32, s->max_tile_reads);
-  const uint64_t fit = kNoAllocGatherEntries / per_warp;
+  const uint64_t fit = kNoAllocGatherEntries / cand_warp_stride(per_warp);
   if (fit == 0) return fail(ctx, BSQ_ERR_SIZE, "a column is covered by more reads than the no-allocation scratch holds");
   CK(cudaSetDevice(ctx->device));
   void* scratch = nullptr;

@@ -147,6 +147,10 @@ struct RaDev {
   uint8_t ref_idx, var_idx, maj_idx, min_idx, passed_cons, passed_poly, pad[2];
 };
 
+// Per-warp scratch of the candidate kernels, in uint4 units: `cap` gather entries followed by `cap`
+// (class, multiplicity) pairs.
+inline __host__ __device__ uint64_t cand_warp_stride(uint32_t cap) { return (uint64_t)cap + (cap + 1) / 2; }
+
 // error word bits
 enum : uint32_t { kErrCovariate = 1, kErrBase = 2, kErrBounds = 4, kErrOrder = 8, kErrCigar = 16,
                   kErrScratch = 32, kErrRaOverflow = 64, kErrX1 = 128 };

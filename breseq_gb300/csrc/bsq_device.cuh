@@ -126,43 +126,68 @@ __device__ __forceinline__ uint32_t warp_sum_u(uint32_t v) {
 
 // Entries of the per-warp gather list (uint4): x = read index, y = qpos | (on_base_indel + 1) << 16,
 // z = likelihood class for the current slot (0xFFFFFFFF = not scored), w = obs | q << 8 | strand << 16.
-// E-step sweep of fit_allele_frequencies / profile_log10_likelihood: sum_w[b] over the reads at the
-// given frequencies (allowed alleles only).  Returns the per-warp totals in all lanes.
-__device__ void em_sweep(const uint4* ents, uint32_t m, const ClassTable& T, const double f[5], unsigned allowed,
-                         double sw[5]) {
+constexpr uint32_t kNoClass = 0xFFFFFFFFu;
+// Likelihood classes up to this many get a per-warp shared-memory histogram, so the EM runs over
+// distinct classes instead of reads.
+constexpr uint32_t kEmHistMax = 2048;
+
+// The slot's scored read bases as (likelihood class, multiplicity) pairs.  Reads of one class add
+// identical terms to every sum of fit_allele_frequencies / profile_log10_likelihood
+// (identify_mutations.cpp:3241-3318, 3094-3143), so each sum runs over distinct classes with weights.
+struct EmList { const uint2* e; uint32_t m; };
+
+// One E-step sweep: g[b] = sum_i r_i(b) / s_i (the gradient of ln L in f[b]) over allowed alleles;
+// the E-step sums are sum_w[b] = f[b] g[b].  With `ll` the sweep also returns an FP32 estimate of
+// sum_i log10 s_i (error well below 1e-3 for a few thousand reads).
+__device__ void em_sweep(const EmList& L, const ClassTable& T, const double f[5], unsigned allowed, double g[5],
+                         float* ll) {
   double a[5] = {0, 0, 0, 0, 0};
-  for (uint32_t i = threadIdx.x & 31; i < m; i += 32) {
-    const uint32_t cls = ents[i].z;
-    if (cls == 0xFFFFFFFFu) continue;
-    const double* r = T.r64 + (size_t)cls * 5;
-    double p[5], s = 0;
+  float lls = 0.0f;
+  for (uint32_t i = threadIdx.x & 31; i < L.m; i += 32) {
+    const uint2 e = L.e[i];
+    const double cnt = (double)e.y;
+    const double* r = T.r64 + (size_t)e.x * 5;
+    double rv[5], s = 0;
 #pragma unroll
-    for (int b = 0; b < 5; b++) { p[b] = ((allowed >> b) & 1) ? f[b] * __ldg(r + b) : 0.0; s += p[b]; }
+    for (int b = 0; b < 5; b++) { rv[b] = __ldg(r + b); if ((allowed >> b) & 1) s += f[b] * rv[b]; }
     if (s > 0.0) {
-      const double inv = 1.0 / s;
+      const double w = cnt / s;
 #pragma unroll
-      for (int b = 0; b < 5; b++) a[b] += p[b] * inv;
+      for (int b = 0; b < 5; b++) a[b] += rv[b] * w;
+      if (ll) lls += (float)e.y * log10f((float)s);
     } else {
+      // the reference's fallback keeps sum_w = n exact: each read adds f[b] to sum_w[b], i.e. 1 to g[b]
 #pragma unroll
-      for (int b = 0; b < 5; b++) if ((allowed >> b) & 1) a[b] += f[b];
+      for (int b = 0; b < 5; b++) a[b] += cnt;
     }
   }
 #pragma unroll
-  for (int b = 0; b < 5; b++) sw[b] = warp_sum(a[b]);
+  for (int b = 0; b < 5; b++) g[b] = warp_sum(((allowed >> b) & 1) ? a[b] : 0.0);
+  if (ll) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lls += __shfl_xor_sync(0xFFFFFFFFu, lls, o);
+    *ll = lls;
+  }
 }
 
-__device__ double em_loglik(const uint4* ents, uint32_t m, const ClassTable& T, const double f[5], unsigned allowed) {
+// sum_i (log10 s_i + max_i) in FP64 at frequencies f, as the reference accumulates its likelihood
+__device__ double em_loglik(const EmList& L, const ClassTable& T, const double f[5], unsigned allowed) {
   double ll = 0;
-  for (uint32_t i = threadIdx.x & 31; i < m; i += 32) {
-    const uint32_t cls = ents[i].z;
-    if (cls == 0xFFFFFFFFu) continue;
-    const double* r = T.r64 + (size_t)cls * 5;
+  for (uint32_t i = threadIdx.x & 31; i < L.m; i += 32) {
+    const uint2 e = L.e[i];
+    const double* r = T.r64 + (size_t)e.x * 5;
     double s = 0;
 #pragma unroll
     for (int b = 0; b < 5; b++) if ((allowed >> b) & 1) s += f[b] * __ldg(r + b);
-    if (s > 0.0) ll += log10(s) + __ldg(T.lpmax64 + cls);
+    if (s > 0.0) ll += (double)e.y * (log10(s) + __ldg(T.lpmax64 + e.x));
   }
   return warp_sum(ll);
+}
+
+__device__ double em_maxsum(const EmList& L, const ClassTable& T) {   // sum_i max_i, constant over iterations
+  double v = 0;
+  for (uint32_t i = threadIdx.x & 31; i < L.m; i += 32) v += (double)L.e[i].y * __ldg(T.lpmax64 + L.e[i].x);
+  return warp_sum(v);
 }
 
 struct Fit { double f[5]; double ll; };
@@ -170,7 +195,7 @@ struct Fit { double f[5]; double ll; };
 // fit_allele_frequencies (identify_mutations.cpp:3241-3318).  The log-likelihood the reference
 // commits is the one evaluated at the frequencies entering the final iteration, so it is computed
 // once, after convergence, at those frequencies.
-__device__ Fit em_fit(const uint4* ents, uint32_t m, uint32_t n, const uint32_t obs_count[5], const ClassTable& T,
+__device__ Fit em_fit(const EmList& L, uint32_t n, const uint32_t obs_count[5], const ClassTable& T,
                       unsigned allowed, double tol) {
   Fit F;
   double f[5] = {0, 0, 0, 0, 0}, fprev[5];
@@ -182,51 +207,89 @@ __device__ Fit em_fit(const uint4* ents, uint32_t m, uint32_t n, const uint32_t 
 #pragma unroll
   for (int b = 0; b < 5; b++) f[b] /= tot;
   for (int it = 1; it <= 50; it++) {
-    double sw[5];
-    em_sweep(ents, m, T, f, allowed, sw);
+    double g[5];
+    em_sweep(L, T, f, allowed, g, nullptr);
     double md = 0;
 #pragma unroll
     for (int b = 0; b < 5; b++) {
       fprev[b] = f[b];
       if (!((allowed >> b) & 1)) continue;
-      const double fn = sw[b] / (double)n;
+      const double fn = f[b] * g[b] / (double)n;
       md = fmax(md, fabs(fn - f[b]));
       f[b] = fn;
     }
     if (md < tol) break;
   }
-  F.ll = em_loglik(ents, m, T, fprev, allowed);
+  F.ll = em_loglik(L, T, fprev, allowed);
 #pragma unroll
   for (int b = 0; b < 5; b++) F.f[b] = f[b];
   return F;
 }
 
-// profile_log10_likelihood (identify_mutations.cpp:3094-3143)
-__device__ double em_profile(const uint4* ents, uint32_t m, const ClassTable& T, const double full[5], int v,
-                             double ff, double tol) {
-  double f[5], fprev[5], other = 0;
+// profile_log10_likelihood (identify_mutations.cpp:3094-3143): the EM with f[v] pinned at ff and the
+// other alleles renormalized, warm-started from the free fit.
+__device__ void em_profile_init(const double full[5], int v, double ff, double f[5]) {
+  double other = 0;
 #pragma unroll
   for (int b = 0; b < 5; b++) if (b != v) other += full[b];
 #pragma unroll
   for (int b = 0; b < 5; b++) f[b] = (b == v) ? ff : ((other > 0.0) ? (1.0 - ff) * full[b] / other : (1.0 - ff) / 4.0);
-  for (int it = 0; it < 50; it++) {
-    double sw[5];
-    em_sweep(ents, m, T, f, 31u, sw);
-    double others = 0;
+}
+
+// One profile M-step; returns max |delta f|.
+__device__ __forceinline__ double em_profile_step(double f[5], double fprev[5], const double g[5], int v, double ff) {
+  double sw[5], others = 0;
 #pragma unroll
-    for (int b = 0; b < 5; b++) if (b != v) others += sw[b];
-    double md = 0;
+  for (int b = 0; b < 5; b++) { sw[b] = f[b] * g[b]; if (b != v) others += sw[b]; }
+  double md = 0;
 #pragma unroll
-    for (int b = 0; b < 5; b++) {
-      fprev[b] = f[b];
-      if (b == v) continue;
-      const double fn = (others > 0.0) ? (1.0 - ff) * sw[b] / others : (1.0 - ff) / 4.0;
-      md = fmax(md, fabs(fn - f[b]));
-      f[b] = fn;
-    }
-    if (md < tol) break;
+  for (int b = 0; b < 5; b++) {
+    fprev[b] = f[b];
+    if (b == v) continue;
+    const double fn = (others > 0.0) ? (1.0 - ff) * sw[b] / others : (1.0 - ff) / 4.0;
+    md = fmax(md, fabs(fn - f[b]));
+    f[b] = fn;
   }
-  return em_loglik(ents, m, T, fprev, 31u);
+  return md;
+}
+
+__device__ double em_profile(const EmList& L, const ClassTable& T, const double full[5], int v, double ff, double tol) {
+  double f[5], fprev[5];
+  em_profile_init(full, v, ff, f);
+  for (int it = 0; it < 50; it++) {
+    double g[5];
+    em_sweep(L, T, f, 31u, g, nullptr);
+    if (em_profile_step(f, fprev, g, v, ff) < tol) break;
+  }
+  return em_loglik(L, T, fprev, 31u);
+}
+
+// profile_log10_likelihood(ff) >= target, decided with two early exits that cannot change the answer.
+// EM never decreases the likelihood, and the reference's value is the likelihood at the start of its
+// last iteration, so once an iterate clears the target the reference's value does too.  The
+// log-likelihood is concave in f, so its maximum over the feasible set is at most
+//   ln L(f) + (1 - ff) max_{b != v} g_b - sum_{b != v} f_b g_b
+// and once that bound falls short of the target the reference's value does too.  Both tests use the
+// FP32 estimate with a margin that covers its error; anything closer runs the exact FP64 evaluation.
+__device__ bool em_profile_ge(const EmList& L, const ClassTable& T, const double full[5], int v, double ff,
+                              double tol, double target, double maxsum, uint32_t n) {
+  const double margin = 1e-3 + 2e-6 * (double)n;
+  double f[5], fprev[5];
+  em_profile_init(full, v, ff, f);
+  for (int it = 0; it < 50; it++) {
+    double g[5];
+    float llf;
+    em_sweep(L, T, f, 31u, g, &llf);
+    const double ll = maxsum + (double)llf;
+    if (ll - margin >= target) return true;
+    double gmax = -DBL_MAX, dot = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) if (b != v) { gmax = fmax(gmax, g[b]); dot += f[b] * g[b]; }
+    const double upper = ll + ((1.0 - ff) * gmax - dot) / 2.302585092994046;
+    if (upper + margin < target) return false;
+    if (em_profile_step(f, fprev, g, v, ff) < tol) break;
+  }
+  return em_loglik(L, T, fprev, 31u) >= target;
 }
 
 __device__ __forceinline__ int am_major(const double f[5], uint32_t n) {
@@ -266,8 +329,9 @@ struct CandOut {
 // the slot-0 consensus call is written back to call[c].
 __device__ void score_candidate_column(const DevSample& S, const ClassTable& T, const CandOut& A, uint32_t c,
                                        bool do_slot0, bool recompute, ColCall cl0, ColCall* call, uint4* ents,
-                                       uint32_t cap) {
+                                       uint32_t cap, uint32_t* hist) {
   const int lane = threadIdx.x & 31;
+  uint2* list = reinterpret_cast<uint2*>(ents + cap);   // the warp's (class, multiplicity) list
   // ---- gather covering reads in BAM order
   const uint2 rr = __ldg(S.tile_range + (c >> 5));
   uint32_t m = 0;
@@ -380,6 +444,35 @@ __device__ void score_candidate_column(const DevSample& S, const ClassTable& T, 
       call[c] = cl;
     }
     const bool passed_cons = (best != ref_idx) && !isnan(cscore) && cscore > 0;
+    // ---- distinct likelihood classes of the slot, in class order (or read order without a histogram)
+    EmList L;
+    L.e = list;
+    {
+      uint32_t outn = 0;
+      if (hist != nullptr) {
+        for (uint32_t i = lane; i < T.K; i += 32) hist[i] = 0;
+        __syncwarp();
+        for (uint32_t i = lane; i < m; i += 32) { const uint32_t cls = ents[i].z; if (cls != kNoClass) atomicAdd(hist + cls, 1u); }
+        __syncwarp();
+        for (uint32_t b0 = 0; b0 < T.K; b0 += 32) {
+          const uint32_t i = b0 + lane;
+          const uint32_t cnt = i < T.K ? hist[i] : 0u;
+          const unsigned bal = __ballot_sync(0xFFFFFFFFu, cnt != 0);
+          if (cnt) list[outn + __popc(bal & ((1u << lane) - 1))] = make_uint2(i, cnt);
+          outn += __popc(bal);
+        }
+      } else {
+        for (uint32_t b0 = 0; b0 < m; b0 += 32) {
+          const uint32_t i = b0 + lane;
+          const uint32_t cls = i < m ? ents[i].z : kNoClass;
+          const unsigned bal = __ballot_sync(0xFFFFFFFFu, cls != kNoClass);
+          if (cls != kNoClass) list[outn + __popc(bal & ((1u << lane) - 1))] = make_uint2(cls, 1u);
+          outn += __popc(bal);
+        }
+      }
+      L.m = outn;
+      __syncwarp();
+    }
     // ---- five-allele fit and variant presence (identify_mutations.cpp:1795-1821)
     Fit full;
     for (int b = 0; b < 5; b++) full.f[b] = 0;
@@ -388,39 +481,41 @@ __device__ void score_candidate_column(const DevSample& S, const ClassTable& T, 
     double vscore = __longlong_as_double(0x7ff8000000000000ll);
     bool passed_poly = false;
     if (n > 0) {
-      full = em_fit(ents, m, n, cnt, T, 31u, A.precision_decimal);
+      full = em_fit(L, n, cnt, T, 31u, A.precision_decimal);
       maj = am_major(full.f, n);
       mnr = am_next(full.f, n, maj);
       var = am_next(full.f, n, ref_idx);
       if (var != 5) {
-        Fit nf = em_fit(ents, m, n, cnt, T, 31u & ~(1u << var), A.precision_decimal);
+        Fit nf = em_fit(L, n, cnt, T, 31u & ~(1u << var), A.precision_decimal);
         vscore = (full.ll - nf.ll) - A.log10_ref_len;
         passed_poly = vscore >= A.poly_cutoff;
       }
     }
     if (passed_cons || passed_poly) {
-      // ---- write_RA_frequency_bounds (identify_mutations.cpp:3175-3217)
+      // ---- write_RA_frequency_bounds (identify_mutations.cpp:3175-3217): the same bisection, with
+      // each "profile >= target" test decided by em_profile_ge
       double lower = 0.0, upper = 1.0;
       if (n > 0 && var < 5) {
         const double D = 0.587566;
         const double fh = full.f[var];
         const double tol = A.precision_decimal;
-        const double target = em_profile(ents, m, T, full.f, var, fh, tol) - D;
-        if (em_profile(ents, m, T, full.f, var, 0.0, tol) >= target) lower = 0.0;
+        const double maxsum = em_maxsum(L, T);
+        const double target = em_profile(L, T, full.f, var, fh, tol) - D;
+        if (em_profile_ge(L, T, full.f, var, 0.0, tol, target, maxsum, n)) lower = 0.0;
         else {
           double lo = 0.0, hi = fh;
           for (int i = 0; i < 40 && (hi - lo) > tol; i++) {
             double mid = 0.5 * (lo + hi);
-            if (em_profile(ents, m, T, full.f, var, mid, tol) >= target) hi = mid; else lo = mid;
+            if (em_profile_ge(L, T, full.f, var, mid, tol, target, maxsum, n)) hi = mid; else lo = mid;
           }
           lower = hi;
         }
-        if (em_profile(ents, m, T, full.f, var, 1.0, tol) >= target) upper = 1.0;
+        if (em_profile_ge(L, T, full.f, var, 1.0, tol, target, maxsum, n)) upper = 1.0;
         else {
           double lo = fh, hi = 1.0;
           for (int i = 0; i < 40 && (hi - lo) > tol; i++) {
             double mid = 0.5 * (lo + hi);
-            if (em_profile(ents, m, T, full.f, var, mid, tol) >= target) lo = mid; else hi = mid;
+            if (em_profile_ge(L, T, full.f, var, mid, tol, target, maxsum, n)) lo = mid; else hi = mid;
           }
           upper = lo;
         }

@@ -197,16 +197,23 @@ void assemble_ra(const std::vector<RaDev>& ra, const std::vector<uint32_t>& qh, 
 
 namespace {
 struct Cov1 { double unique1, red1; int total; };
-}
 
-void intervals(const std::vector<ColCov>& cov, const std::vector<ColCall>& call, const SampleLayout& L,
-               const bsq_im_params* p, std::vector<bsq_mc_record>& mc, std::vector<bsq_un_record>& un) {
+// check_deletion_completion / update_unknown_intervals / at_target_end of identify_mutations_pileup
+// (identify_mutations.cpp:2107-2164, 2262-2344, 2972-3007).  Some of the state deliberately carries
+// over from one target to the next, as it does there.
+struct IntervalMachine {
+  const bsq_im_params* p;
+  std::vector<bsq_mc_record>& mc;
+  std::vector<bsq_un_record>& un;
   uint32_t del_start = kUndef, del_end = kUndef, red_start = kUndef, red_end = kUndef, un_start = kUndef;
   bool reaches_seed = false, red_zero = false;
-  const Cov1 nan_cov = {kNaN, kNaN, 0};
+  Cov1 nan_cov = {kNaN, kNaN, 0};
   Cov1 last = nan_cov, left_out = nan_cov, left_in = nan_cov;
   double prop = 0, seed = 0;
-  auto check = [&](uint32_t t, uint32_t position, const Cov1& c) {
+
+  IntervalMachine(const bsq_im_params* pp, std::vector<bsq_mc_record>& m, std::vector<bsq_un_record>& u) : p(pp), mc(m), un(u) {}
+
+  void check(uint32_t t, uint32_t position, const Cov1& c) {
     if (position == 1) last = nan_cov;
     if (c.unique1 <= prop && del_start == kUndef) { del_start = position; left_out = last; left_in = c; }
     if (!std::isnan(c.unique1) && (double)c.total <= seed) reaches_seed = true;
@@ -234,8 +241,8 @@ void intervals(const std::vector<ColCov>& cov, const std::vector<ColCall>& call,
       }
     }
     last = c;
-  };
-  auto unknown = [&](uint32_t t, uint32_t position, bool predicted) {
+  }
+  void unknown(uint32_t t, uint32_t position, bool predicted) {
     if (!predicted) {
       if (un_start == kUndef) un_start = position;
     } else if (un_start != kUndef) {
@@ -243,27 +250,22 @@ void intervals(const std::vector<ColCov>& cov, const std::vector<ColCall>& call,
       un.push_back(u);
       un_start = kUndef;
     }
-  };
-  const std::vector<uint32_t>& tp = *L.tpoff;
-  for (uint32_t t : *L.order) {
-    const uint32_t len = tp[t + 1] - tp[t] - 1;
-    const bool failed = p->deletion_propagation_cutoff[t] < 0.0;
+  }
+  void target_start(uint32_t t) {
     del_start = del_end = red_start = red_end = kUndef;
     un_start = kUndef;
     prop = p->deletion_propagation_cutoff[t];
     seed = p->deletion_seed_cutoff[t];
-    if (!failed) {
-      for (uint32_t i = 0; i < len; i++) {
-        const ColCov& cv = cov[tp[t] + i];
-        const ColCall& cl = call[tp[t] + i];
-        Cov1 c;
-        c.unique1 = (double)cv.uniq_bot + (double)cv.uniq_top;
-        c.red1 = cv.red_bot + cv.red_top;
-        c.total = (int)std::round(c.unique1) + (int)std::round(c.red1);
-        if (!p->skip_missing_coverage_prediction) check(t, i + 1, c);
-        unknown(t, i + 1, (cl.flags & kBasePredicted) != 0);
-      }
-    }
+  }
+  void position(uint32_t t, uint32_t pos1, const ColCov& cv, const ColCall& cl) {
+    Cov1 c;
+    c.unique1 = (double)cv.uniq_bot + (double)cv.uniq_top;
+    c.red1 = cv.red_bot + cv.red_top;
+    c.total = (int)std::round(c.unique1) + (int)std::round(c.red1);
+    if (!p->skip_missing_coverage_prediction) check(t, pos1, c);
+    unknown(t, pos1, (cl.flags & kBasePredicted) != 0);
+  }
+  void target_end(uint32_t t, uint32_t len, bool failed) {
     if (!p->skip_missing_coverage_prediction) check(t, len + 1, nan_cov);
     unknown(t, len + 1, true);
     if (!p->skip_missing_coverage_prediction && failed) {
@@ -273,6 +275,41 @@ void intervals(const std::vector<ColCov>& cov, const std::vector<ColCall>& call,
       m.left_outside_cov = kNaN; m.left_inside_cov = 0.0; m.right_inside_cov = 0.0; m.right_outside_cov = kNaN;
       mc.push_back(m);
     }
+  }
+};
+}  // namespace
+
+void intervals(const std::vector<ColCov>& cov, const std::vector<ColCall>& call, const SampleLayout& L,
+               const bsq_im_params* p, std::vector<bsq_mc_record>& mc, std::vector<bsq_un_record>& un) {
+  IntervalMachine M(p, mc, un);
+  const std::vector<uint32_t>& tp = *L.tpoff;
+  for (uint32_t t : *L.order) {
+    const uint32_t len = tp[t + 1] - tp[t] - 1;
+    const bool failed = p->deletion_propagation_cutoff[t] < 0.0;
+    M.target_start(t);
+    if (!failed)
+      for (uint32_t i = 0; i < len; i++) M.position(t, i + 1, cov[tp[t] + i], call[tp[t] + i]);
+    M.target_end(t, len, failed);
+  }
+}
+
+void intervals_sparse(const std::vector<uint32_t>& cols, const std::vector<ColCov>& cov, const std::vector<ColCall>& call,
+                      const SampleLayout& L, const bsq_im_params* p, std::vector<bsq_mc_record>& mc,
+                      std::vector<bsq_un_record>& un) {
+  IntervalMachine M(p, mc, un);
+  const std::vector<uint32_t>& tp = *L.tpoff;
+  for (uint32_t t : *L.order) {
+    const uint32_t len = tp[t + 1] - tp[t] - 1;
+    const bool failed = p->deletion_propagation_cutoff[t] < 0.0;
+    M.target_start(t);
+    if (!failed) {
+      auto it = std::lower_bound(cols.begin(), cols.end(), tp[t]);
+      for (; it != cols.end() && *it < tp[t] + len; ++it) {
+        const size_t k = (size_t)(it - cols.begin());
+        M.position(t, *it - tp[t] + 1, cov[k], call[k]);
+      }
+    }
+    M.target_end(t, len, failed);
   }
 }
 

@@ -40,6 +40,10 @@ void assemble_ra(const std::vector<RaDev>& ra, const std::vector<uint32_t>& qhis
 // MC and UN state machines in pileup order (identify_mutations.cpp:2107-2164, 2262-2344, 2972-3007)
 void intervals(const std::vector<ColCov>& cov, const std::vector<ColCall>& call, const SampleLayout& L,
                const bsq_im_params* p, std::vector<bsq_mc_record>& mc, std::vector<bsq_un_record>& un);
+// The same state machines over the marked columns only (padded column indices, ascending).
+void intervals_sparse(const std::vector<uint32_t>& cols, const std::vector<ColCov>& cov, const std::vector<ColCall>& call,
+                      const SampleLayout& L, const bsq_im_params* p, std::vector<bsq_mc_record>& mc,
+                      std::vector<bsq_un_record>& un);
 void fill_positions(const std::vector<ColCov>& cov, const std::vector<ColCall>& call, const SampleLayout& L,
                     bsq_position_arrays* out);
 

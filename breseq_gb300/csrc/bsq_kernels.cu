@@ -485,12 +485,75 @@ __global__ void cand_scatter_kernel(const ColCall* call, uint32_t n, const uint3
   if (f) out[block_offsets[blockIdx.x] + warp_base[threadIdx.x >> 5] + __popc(m & ((1u << (threadIdx.x & 31)) - 1))] = i;
 }
 
+// ============================================================================ sparse MC / UN input
+// The MC and UN state machines (identify_mutations.cpp:2262-2344, 2972-3007) change state only at a
+// column that is not base-predicted, has unique coverage at or below the target's propagation cutoff,
+// or total coverage at or below its seed cutoff; the column after such a column closes what it
+// opened, and the column before it supplies the left-outside coverage.  Those columns are marked and
+// the host replays the state machines over them alone.
+__global__ void interval_mark_kernel(const ColCov* cov, const ColCall* call, uint32_t n_cols, const uint32_t* tpoff,
+                                     uint32_t n_targets, const uint8_t* called, const uint8_t* failed,
+                                     const double* prop, const double* seed, uint8_t* keep) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cols) return;
+  if (!(call[c].flags & kScored)) return;
+  uint32_t lo = 0, hi = n_targets;
+  while (hi - lo > 1) { uint32_t mid = (lo + hi) >> 1; if (tpoff[mid] <= c) lo = mid; else hi = mid; }
+  const uint32_t t = lo;
+  if (!called[t] || failed[t]) return;
+  const ColCov v = cov[c];
+  const double u1 = (double)v.uniq_bot + (double)v.uniq_top;
+  const double r1 = v.red_bot + v.red_top;
+  const double total = (double)((int)rint(u1) + (int)rint(r1));
+  const bool interesting = !(call[c].flags & kBasePredicted) || u1 <= prop[t] || total <= seed[t];
+  if (!interesting) return;
+  keep[c] = 1;
+  if (c > tpoff[t]) keep[c - 1] = 1;
+  if (c + 1 < tpoff[t + 1] - 1) keep[c + 1] = 1;
+}
+
+__global__ void flag_count_kernel(const uint8_t* keep, uint32_t n, uint32_t* block_counts) {
+  __shared__ uint32_t s;
+  if (threadIdx.x == 0) s = 0;
+  __syncthreads();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool f = i < n && keep[i];
+  const uint32_t b = __popc(__ballot_sync(0xFFFFFFFFu, f));
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(&s, b);
+  __syncthreads();
+  if (threadIdx.x == 0) block_counts[blockIdx.x] = s;
+}
+
+// scatter the kept columns in column order, with their coverage and call
+__global__ void flag_gather_kernel(const uint8_t* keep, uint32_t n, const uint32_t* block_offsets, const ColCov* cov,
+                                   const ColCall* call, uint32_t* out_col, ColCov* out_cov, ColCall* out_call) {
+  __shared__ uint32_t warp_base[32];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool f = i < n && keep[i];
+  const unsigned m = __ballot_sync(0xFFFFFFFFu, f);
+  if ((threadIdx.x & 31) == 0) warp_base[threadIdx.x >> 5] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t acc = 0;
+    for (uint32_t w = 0; w < (blockDim.x >> 5); w++) { const uint32_t x = warp_base[w]; warp_base[w] = acc; acc += x; }
+  }
+  __syncthreads();
+  if (f) {
+    const uint32_t o = block_offsets[blockIdx.x] + warp_base[threadIdx.x >> 5] + __popc(m & ((1u << (threadIdx.x & 31)) - 1));
+    out_col[o] = i;
+    out_cov[o] = cov[i];
+    out_call[o] = call[i];
+  }
+}
+
 // One warp per candidate column (persistent warps pulling from a work counter); the scoring itself is
 // score_candidate_column (bsq_device.cuh).
 __global__ void __launch_bounds__(128) im_candidate_kernel(DevSample S, ClassTable T, CandArgs A) {
+  extern __shared__ uint32_t sh_hist[];
   const int lane = threadIdx.x & 31;
   const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  uint4* ents = A.scratch + (size_t)gw * A.scratch_per_warp;
+  uint4* ents = A.scratch + (size_t)gw * cand_warp_stride(A.scratch_per_warp);
+  uint32_t* hist = (T.K <= kEmHistMax) ? sh_hist + (threadIdx.x >> 5) * T.K : nullptr;
   CandOut out;
   out.ra = A.ra; out.n_ra = A.n_ra; out.ra_cap = A.ra_cap; out.qhist = A.qhist; out.Qhist = A.Qhist; out.err = A.err;
   out.base_quality_cutoff = A.base_quality_cutoff; out.log10_ref_len = A.log10_ref_len;
@@ -503,7 +566,7 @@ __global__ void __launch_bounds__(128) im_candidate_kernel(DevSample S, ClassTab
     const uint32_t c = A.cand[idx];
     const ColCall cl0 = A.call[c];
     score_candidate_column(S, T, out, c, (cl0.flags & (kCandidate | kRecompute)) != 0, (cl0.flags & kRecompute) != 0,
-                           cl0, A.call, ents, A.scratch_per_warp);
+                           cl0, A.call, ents, A.scratch_per_warp, hist);
     __syncwarp();
   }
 }
@@ -556,9 +619,24 @@ cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_coun
   cand_scatter_kernel<<<nb, 256, 0, st>>>(call, n, block_counts, out);
   return cudaGetLastError();
 }
+cudaError_t launch_intervals(const ColCov* cov, const ColCall* call, uint32_t n_cols, const uint32_t* tpoff,
+                             uint32_t n_targets, const uint8_t* called, const uint8_t* failed, const double* prop,
+                             const double* seed, uint8_t* keep, uint32_t* block_counts, uint32_t* total,
+                             uint32_t* out_col, ColCov* out_cov, ColCall* out_call, cudaStream_t st) {
+  const uint32_t nb = (n_cols + 255) / 256;
+  cudaError_t e = cudaMemsetAsync(keep, 0, n_cols, st);
+  if (e != cudaSuccess) return e;
+  interval_mark_kernel<<<nb, 256, 0, st>>>(cov, call, n_cols, tpoff, n_targets, called, failed, prop, seed, keep);
+  flag_count_kernel<<<nb, 256, 0, st>>>(keep, n_cols, block_counts);
+  scan_kernel<<<1, 1024, 0, st>>>(block_counts, nb, total);
+  flag_gather_kernel<<<nb, 256, 0, st>>>(keep, n_cols, block_counts, cov, call, out_col, out_cov, out_call);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_candidates(const DevSample& S, const ClassTable& T, const CandArgs& A, int n_warps, cudaStream_t st) {
   const int blocks = (n_warps + 3) / 4;
-  im_candidate_kernel<<<blocks, 128, 0, st>>>(S, T, A);
+  const size_t smem = (T.K <= kEmHistMax) ? (size_t)4 * T.K * sizeof(uint32_t) : 0;
+  im_candidate_kernel<<<blocks, 128, smem, st>>>(S, T, A);
   return cudaGetLastError();
 }
 

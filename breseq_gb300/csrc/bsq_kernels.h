@@ -47,6 +47,10 @@ cudaError_t launch_ec(const DevSample& S, const EcArgs& A, int sms, cudaStream_t
 cudaError_t launch_im_column(const DevSample& S, const ClassTable& T, const ImArgs& A, int sms, cudaStream_t st);
 cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_counts, uint32_t* total, uint32_t* out,
                            cudaStream_t st);
+cudaError_t launch_intervals(const ColCov* cov, const ColCall* call, uint32_t n_cols, const uint32_t* tpoff,
+                             uint32_t n_targets, const uint8_t* called, const uint8_t* failed, const double* prop,
+                             const double* seed, uint8_t* keep, uint32_t* block_counts, uint32_t* total,
+                             uint32_t* out_col, ColCov* out_cov, ColCall* out_call, cudaStream_t st);
 cudaError_t launch_candidates(const DevSample& S, const ClassTable& T, const CandArgs& A, int n_warps, cudaStream_t st);
 
 }  // namespace bsq

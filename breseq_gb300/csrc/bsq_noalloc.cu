@@ -91,10 +91,12 @@ __global__ void noalloc_class_kernel(ClassArgs A) {
 
 // One warp per requested position, persistent warps over the shared work counter.
 __global__ void __launch_bounds__(128) noalloc_positions_kernel(DevSample S, ClassTable T, CandOut out, NoAllocArgs A) {
+  extern __shared__ uint32_t sh_hist[];
   const int lane = threadIdx.x & 31;
   const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (gw >= A.n_warps) return;
-  uint4* ents = A.gather + (size_t)gw * A.per_warp;
+  uint4* ents = A.gather + (size_t)gw * cand_warp_stride(A.per_warp);
+  uint32_t* hist = (T.K <= kEmHistMax) ? sh_hist + (threadIdx.x >> 5) * T.K : nullptr;
   ColCall none;
   none.score = 0; none.n = 0; none.best = 5; none.flags = 0; none.pad[0] = none.pad[1] = 0;
   for (;;) {
@@ -108,7 +110,7 @@ __global__ void __launch_bounds__(128) noalloc_positions_kernel(DevSample S, Cla
       continue;
     }
     if (A.failed[t]) continue;
-    score_candidate_column(S, T, out, S.tpoff[t] + p0, true, false, none, nullptr, ents, A.per_warp);
+    score_candidate_column(S, T, out, S.tpoff[t] + p0, true, false, none, nullptr, ents, A.per_warp, hist);
     __syncwarp();
   }
 }
@@ -157,7 +159,8 @@ cudaError_t launch_noalloc_positions(void* scratch, const DevSample& S, const No
   A.gather = reinterpret_cast<uint4*>(base); A.per_warp = J.per_warp; A.n_warps = J.n_warps;
   const uint32_t warps = J.n_warps;
   if (J.n_positions) {
-    noalloc_positions_kernel<<<(warps + 3) / 4, 128, 0, st>>>(S, T, out, A);
+    const size_t smem = (T.K <= kEmHistMax) ? (size_t)4 * T.K * sizeof(uint32_t) : 0;
+    noalloc_positions_kernel<<<(warps + 3) / 4, 128, smem, st>>>(S, T, out, A);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   if ((e = cudaMemcpyAsync(err_host, counters + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;

@@ -59,6 +59,8 @@ class SimConfig:
     softclip_fraction: float = 0.0  # reads with a soft clip at one end
     n_base_rate: float = 0.0        # read bases replaced by N (quality 2)
     low_mapq_fraction: float = 0.0  # unique reads with MAPQ drawn in [20, 41]
+    large_deletions: int = 0        # regions of the reference missing from the sample (MC evidence)
+    large_deletion_length: int = 800
     chunk_reads: int = 400_000
 
 
@@ -197,6 +199,11 @@ def simulate(cfg: SimConfig) -> Sample:
         alt = BASES[rng.choice([b for b in range(4) if BASES[b] != r])]
         variants.append(dict(tid=t, pos=p, kind="low_quality", alt=int(alt), freq=0.10))
 
+    deleted = []   # (tid, start, end) regions absent from the sample: no read covers them
+    for _ in range(cfg.large_deletions):
+        t, p = _pick_site(margin=cfg.large_deletion_length + 300)
+        deleted.append((t, p, p + cfg.large_deletion_length))
+        variants.append(dict(tid=t, pos=p, kind="large_del", length=cfg.large_deletion_length, freq=1.0))
     # ---------------------------------------------------------------- read placement
     recs = {k: [] for k in ("tid", "pos", "flag", "rfile", "rg", "L", "clipL", "clipR", "x1", "group")}
     rfile_base = 0
@@ -233,6 +240,11 @@ def simulate(cfg: SimConfig) -> Sample:
     rfile = np.concatenate(recs["rfile"])
     rg = np.concatenate(recs["rg"])
     L_arr = np.concatenate(recs["L"])
+    if deleted:
+        keep = np.ones(tid.shape[0], dtype=bool)
+        for t, a, b in deleted:
+            keep &= ~((tid == t) & (pos < b) & (pos + L_arr + max_indel_span > a))
+        tid, pos, flag, rfile, rg, L_arr = tid[keep], pos[keep], flag[keep], rfile[keep], rg[keep], L_arr[keep]
     n = tid.shape[0]
     mapq = np.full(n, 42, dtype=np.uint8)
     if cfg.low_mapq_fraction > 0:

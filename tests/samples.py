@@ -16,7 +16,8 @@ def ecoli_small():
     """Three targets with five repeat copies (X1 = 5 reads), PE150 in two read files, indels up to 3 bp,
     plus trims, soft clips, N bases and mixed MAPQ to exercise the rarer branches."""
     c = synth.config_ecoli(seed=21, scale=0.02, coverage=30.0)
-    c = dataclasses.replace(c, trim_fraction=0.05, softclip_fraction=0.02, n_base_rate=0.002, low_mapq_fraction=0.05)
+    c = dataclasses.replace(c, trim_fraction=0.05, softclip_fraction=0.02, n_base_rate=0.002, low_mapq_fraction=0.05,
+                            large_deletions=2)
     return synth.simulate(c)
 
 

@@ -55,16 +55,20 @@ def test_log10_table_round_trip(scorer, oracle_results, name):
     assert np.array_equal(tab_g, tab_o)
 
 
+@pytest.mark.parametrize("positions", [True, False], ids=["dense", "sparse"])
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32c"])
 @pytest.mark.parametrize("name", list(samples.ALL))
-def test_identify_mutations_parity(scorer, loaded, oracle_results, name, precision):
+def test_identify_mutations_parity(scorer, loaded, oracle_results, name, precision, positions):
+    """RA items, MC/UN intervals and (dense) per-position arrays against the oracle.  The sparse run
+    returns no per-position arrays, and its MC/UN come from the marked columns only."""
     from breseq_gb300.api import ImSettings
     _, tab, im_o = oracle_results[name]
     im_g = scorer.identify_mutations(loaded[name], tab, ImSettings(polymorphism_prediction=name in POLY),
-                                     precision=precision, positions=True)
+                                     precision=precision, positions=positions)
     problems = compare.compare_ra(im_g["ra"], im_o["ra"])
     problems += compare.compare_intervals(im_g, im_o)
-    problems += compare.compare_positions(im_g["positions"], im_o["positions"])
+    if positions:
+        problems += compare.compare_positions(im_g["positions"], im_o["positions"])
     assert not problems, "\n".join(problems[:20])
     assert len(im_o["ra"]) > 0
 
@@ -85,9 +89,27 @@ def test_failed_coverage_fit_target(scorer, loaded, oracle_results):
     prop = np.array([5.0, -1.0, 5.0])
     p = po.default_im_params(s, prop_cutoff=prop)
     im_o = po.identify(s, tab, p)
-    im_g = scorer.identify_mutations(loaded["ecoli_small"], tab, ImSettings(), deletion_propagation_cutoff=prop,
-                                     precision=1, positions=True)
-    problems = compare.compare_ra(im_g["ra"], im_o["ra"]) + compare.compare_intervals(im_g, im_o)
-    problems += compare.compare_positions(im_g["positions"], im_o["positions"])
-    assert not problems, "\n".join(problems[:20])
-    assert any(m["tid"] == 1 and m["start"] == 1 for m in im_g["mc"])
+    for positions in (True, False):
+        im_g = scorer.identify_mutations(loaded["ecoli_small"], tab, ImSettings(), deletion_propagation_cutoff=prop,
+                                         precision=1, positions=positions)
+        problems = compare.compare_ra(im_g["ra"], im_o["ra"]) + compare.compare_intervals(im_g, im_o)
+        if positions:
+            problems += compare.compare_positions(im_g["positions"], im_o["positions"])
+        assert not problems, "\n".join(problems[:20])
+        assert any(m["tid"] == 1 and m["start"] == 1 for m in im_g["mc"])
+
+
+@pytest.mark.parametrize("prop_cutoff,seed_cutoff", [(12.0, 2.0), (25.0, 8.0)])
+def test_intervals_with_deletion_cutoffs(scorer, loaded, oracle_results, prop_cutoff, seed_cutoff):
+    """Higher deletion cutoffs open many MC candidates (30x sample), exercising the MC state machine
+    (redundant-coverage ranges, seed reached or not) on both interval paths."""
+    from breseq_gb300.api import ImSettings
+    s = samples.ecoli_small()
+    _, tab, _ = oracle_results["ecoli_small"]
+    im_o = po.identify(s, tab, po.default_im_params(s, prop_cutoff=prop_cutoff, seed_cutoff=seed_cutoff))
+    assert len(im_o["mc"]) > 5
+    for positions in (True, False):
+        im_g = scorer.identify_mutations(loaded["ecoli_small"], tab, ImSettings(), deletion_propagation_cutoff=prop_cutoff,
+                                         deletion_seed_cutoff=seed_cutoff, precision=1, positions=positions)
+        problems = compare.compare_intervals(im_g, im_o) + compare.compare_ra(im_g["ra"], im_o["ra"])
+        assert not problems, "\n".join(problems[:20])
