@@ -71,6 +71,13 @@ struct EcArgs {
   float unmatched_factor;           // only used through floor(); double on host
   double unmatched_factor_d;
   uint32_t flush_tiles;             // shared histogram flush period (avoids u32 overflow)
+  // read-parallel form: per-column difference arrays of unique / redundant coverage and the
+  // preprocess read-start flags, turned into coverage by a scan afterwards
+  int32_t* diff_u;                  // [n_cols + 1]
+  int32_t* diff_r;                  // [n_cols + 1]
+  uint8_t* qs_flag;                 // [2][n_cols]: a read starts at this column (forward, reverse)
+  uint32_t* blk_u;                  // per 1024-column block: sums of diff_u / diff_r
+  uint32_t* blk_r;
 };
 
 // ----------------------------------------------------------------------------- pass 2

@@ -51,7 +51,8 @@ __global__ void pack_reads_kernel(RawSoA in, PackOut out) {
   const uint32_t x1 = in.x1[i];
   if (x1 == 0) err |= kErrX1;
   if (x1 > 1) fl |= kRedundant;
-  const bool skip = (flag & 0x704) != 0;
+  // filtered like htslib's pileup does by default, or on a target the pileup never visits
+  const bool skip = (flag & 0x704) != 0 || !in.called[tid];
   if (skip) fl |= kSkip;
   if (len > 65535 || (so & 1) || so + len > in.n_bases || co + nc > in.n_cigar_total) err |= kErrBounds;
   if (in.xl[i] >= 65535 || in.xr[i] >= 65535) err |= kErrBounds;
@@ -131,158 +132,260 @@ __global__ void tile_range_kernel(const uint32_t* rstart, uint32_t n_reads, uint
 }
 
 // ============================================================================ pass 1: error counts
-// error_count_pileup::pileup_callback (error_count.cpp:125-199) + count_alignment_position
-// (error_count.cpp:854-986).  Covariate events go to a block-private shared histogram; unique-only
-// coverage goes to the per-group histogram with one atomic per distinct value per warp.
-__global__ void __launch_bounds__(256) ec_kernel(DevSample S, EcArgs A) {
+// error_count_pileup::pileup_callback (error_count.cpp:125-199) with count_alignment_position
+// (error_count.cpp:854-986), read-parallel: a warp walks one read at a time, lanes over its aligned
+// bases (the column a base sits on and its htslib pileup state follow from the CIGAR walk), so every
+// (read, column) incidence is one lane-iteration.  Covariate events go to a block-private shared
+// histogram with one atomic per distinct bin per warp; the per-column unique / redundant read counts
+// the coverage histogram needs are +1/-1 difference arrays over each aligned block, scanned later.
+
+// Both events of one unique read base (error_count.cpp:888-984).
+__device__ __forceinline__ void ec_events(const DevSample& S, const EcArgs& A, uint32_t* hist,
+                                          bool on, const DevRead& rd, uint32_t r, uint32_t c, int qpos, int indel,
+                                          uint32_t& err) {
+  const int rev = rd.flags & kRev;
+  const uint32_t rs = rd.rfile;
+  const uint64_t so = rd.seq_off;
+  uint32_t bin1 = 0xFFFFFFFFu, bin2 = 0xFFFFFFFFu;
+  if (on) {
+    const uint8_t refc = __ldg(S.ref + c);
+    // (1) base substitution / match at this column
+    const uint8_t ob = nib_at(S.seq, so + qpos);
+    if (ob != 15 && refc != 'N') {
+      int oi = bam_idx(ob), ri = chr_idx(refc);
+      if (oi < 0 || ri < 0 || ri > 3) err |= kErrBase;
+      else {
+        if (rev) { oi = 3 - oi; ri = 3 - ri; }
+        const uint32_t q = __ldg(S.qual + so + qpos);
+        if (q >= A.Q || rs >= A.R) err |= kErrCovariate;
+        else bin1 = rs + A.R * (ri + 5u * (oi + 5u * q));
+      }
+    }
+    if (indel == 0) {                          // (2a) '..': the next base also aligned
+      if (qpos < query_end0(S, rd, r)) {
+        const int mq = qpos + 1 - rev;
+        const uint8_t ob2 = nib_at(S.seq, so + mq);
+        const uint8_t rc2 = rev ? refc : __ldg(S.ref + c + 1);
+        if (ob2 != 15 && rc2 != 'N') {
+          const uint32_t q = __ldg(S.qual + so + mq);
+          if (q >= A.Q || rs >= A.R) err |= kErrCovariate;
+          else bin2 = rs + A.R * (4u + 5u * (4u + 5u * q));
+        }
+      }
+    } else if (indel == -1) {                  // (2b) one deleted base follows
+      const int mq = qpos + 1 - rev;
+      if (mq < 0 || mq >= (int)rd.len) err |= kErrBounds;
+      else {
+        const uint8_t ob2 = nib_at(S.seq, so + mq);
+        const uint8_t rn = __ldg(S.ref + c + 1);
+        if (ob2 != 15 && rn != 'N') {
+          int ri = chr_idx(rn);
+          if (ri < 0 || ri > 3) err |= kErrBase;
+          else {
+            if (rev) ri = 3 - ri;
+            const uint32_t q = __ldg(S.qual + so + mq);
+            if (q >= A.Q || rs >= A.R) err |= kErrCovariate;
+            else bin2 = rs + A.R * (ri + 5u * (4u + 5u * q));
+          }
+        }
+      }
+    } else if (indel == 1) {                   // (2c) one inserted base follows
+      const int mq = qpos + 1;
+      if (mq >= (int)rd.len) err |= kErrBounds;
+      else if (mq <= query_end0(S, rd, r) && mq >= query_start0(S, rd, r)) {
+        const uint8_t ob2 = nib_at(S.seq, so + mq);
+        if (ob2 != 15) {
+          int oi = bam_idx(ob2);
+          if (oi < 0) err |= kErrBase;
+          else {
+            if (rev) oi = 3 - oi;
+            const uint32_t q = __ldg(S.qual + so + mq);
+            if (q >= A.Q || rs >= A.R) err |= kErrCovariate;
+            else bin2 = rs + A.R * (4u + 5u * (oi + 5u * q));
+          }
+        }
+      }
+    }
+  }
+  if (bin1 != 0xFFFFFFFFu) atomicAdd(hist + bin1, 1u);
+  if (bin2 != 0xFFFFFFFFu) atomicAdd(hist + bin2, 1u);
+}
+
+// required_junction_read_end_min_coordinate test of the preprocess stage (settings.h:345-354)
+__device__ __forceinline__ bool read_start_counts(const EcArgs& A, const DevRead& rd, uint32_t bs1, uint32_t be1) {
+  const int32_t umax = (int32_t)floor((double)((int32_t)rd.len - (int32_t)A.unmatched_min_len) * A.unmatched_factor_d);
+  const uint32_t req = (umax <= 0) ? rd.len : rd.len - (uint32_t)umax;
+  const uint32_t send1 = (rd.flags & kRev) ? rd.len - bs1 + 1 : be1;
+  return send1 >= req;
+}
+
+__global__ void __launch_bounds__(256) ec_read_kernel(DevSample S, EcArgs A) {
   extern __shared__ uint32_t sh_hist[];
   const uint32_t nbins = A.R * 25u * A.Q;
   for (uint32_t i = threadIdx.x; i < nbins; i += blockDim.x) sh_hist[i] = 0;
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  uint32_t local_err = 0;
-  uint32_t tiles_done = 0;
-  // all warps of the block run the same number of loop trips so the periodic flush can sync
-  const uint32_t stride = gridDim.x * nwarps;
-  const uint32_t trips = (S.n_tiles + stride - 1) / stride;
-  for (uint32_t trip = 0; trip < trips; trip++) {
-    const uint32_t tile = trip * stride + blockIdx.x * nwarps + warp;
-    if (tile < S.n_tiles) {
-      const uint32_t c0 = tile * 32, c = c0 + lane;
-      const uint8_t refc = (c < S.n_cols) ? __ldg(S.ref + c) : 0;
-      const uint8_t refn = (c + 1 < S.n_cols) ? __ldg(S.ref + c + 1) : 0;
-      const uint32_t t = (c < S.n_cols) ? target_of(S, c) : 0;
-      const bool real = (c < S.n_cols) && refc != 0 && __ldg(S.tgt_called + t);
-      uint32_t uniq = 0;
-      bool red = false;
-      int hqs0 = 0, hqs1 = 0;
-      const uint2 rr = __ldg(S.tile_range + tile);
-      for (uint32_t r = rr.x; r < rr.y; r++) {
-        const DevRead rd = S.reads[r];
-        if ((rd.flags & kSkip) || rd.end <= c0) continue;
-        if (!(real && c >= rd.start && c < rd.end)) continue;
-        Pile e;
-        resolve(S, rd, c, e);
-        if (e.del) continue;
-        if (rd.flags & kRedundant) { red = true; continue; }
-        ++uniq;
-        const int rev = rd.flags & kRev;
-        if (A.preprocess) {
-          // Settings::required_junction_read_end_min_coordinate (settings.h:345-354)
-          int32_t umax = (int32_t)floor((double)((int32_t)rd.len - (int32_t)A.unmatched_min_len) * A.unmatched_factor_d);
-          uint32_t req = (umax <= 0) ? rd.len : rd.len - (uint32_t)umax;
-          uint32_t send1;
-          if (rd.flags & kSimple) {
-            uint32_t bs1 = rd.clip + 1, be1 = rd.clip + (rd.end - rd.start);
-            send1 = rev ? rd.len - bs1 + 1 : be1;
-          } else {
-            QBounds q = S.qb[r];
-            send1 = rev ? rd.len - (q.qbs + 1u) + 1 : q.qbe + 1u;
-          }
-          if (e.qpos == 0 && send1 >= req) { if (rev) hqs1 = 1; else hqs0 = 1; }
-        }
-        if (!A.do_errors) continue;
-        const uint32_t rs = rd.rfile;
-        const uint64_t so = rd.seq_off;
-        // (1) base substitution / match
-        {
-          const uint8_t ob = nib_at(S.seq, so + e.qpos);
-          if (ob != 15 && refc != 'N') {
-            int oi = bam_idx(ob), ri = chr_idx(refc);
-            if (oi < 0 || ri < 0 || ri > 3) { local_err |= kErrBase; }
-            else {
-              if (rev) { oi = 3 - oi; ri = 3 - ri; }
-              const uint32_t q = __ldg(S.qual + so + e.qpos);
-              if (q >= A.Q || rs >= A.R) local_err |= kErrCovariate;
-              else atomicAdd(&sh_hist[rs + A.R * (ri + 5u * (oi + 5u * q))], 1u);
-            }
-          }
-        }
-        if (e.indel == 0) {                         // (2a) '..'
-          if (e.qpos < query_end0(S, rd, r)) {
-            const int mq = e.qpos + 1 - rev;
-            const uint8_t ob = nib_at(S.seq, so + mq);
-            const uint8_t rc = rev ? refc : refn;
-            if (ob != 15 && rc != 'N') {
-              const uint32_t q = __ldg(S.qual + so + mq);
-              if (q >= A.Q || rs >= A.R) local_err |= kErrCovariate;
-              else atomicAdd(&sh_hist[rs + A.R * (4u + 5u * (4u + 5u * q))], 1u);
-            }
-          }
-        } else if (e.indel == -1) {                 // (2b) one deleted base follows
-          const int mq = e.qpos + 1 - rev;
-          if (mq < 0 || mq >= (int)rd.len) { local_err |= kErrBounds; }
-          else {
-            const uint8_t ob = nib_at(S.seq, so + mq);
-            if (ob != 15 && refn != 'N') {
-              int ri = chr_idx(refn);
-              if (ri < 0 || ri > 3) local_err |= kErrBase;
-              else {
-                if (rev) ri = 3 - ri;
-                const uint32_t q = __ldg(S.qual + so + mq);
-                if (q >= A.Q || rs >= A.R) local_err |= kErrCovariate;
-                else atomicAdd(&sh_hist[rs + A.R * (ri + 5u * (4u + 5u * q))], 1u);
+  const int lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  uint32_t err = 0;
+  uint32_t done = 0;
+  for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < S.n_reads; r += nwarps) {
+    const DevRead rd = S.reads[r];
+    if (rd.flags & kSkip) continue;      // filtered by flag, or on a target outside the pileup set
+    const bool red = rd.flags & kRedundant;
+    int32_t* diff = red ? A.diff_r : A.diff_u;
+    if (rd.flags & kSimple) {
+      const uint32_t span = rd.end - rd.start;
+      if (lane == 0) {
+        atomicAdd(diff + rd.start, 1);
+        atomicAdd(diff + rd.end, -1);
+        if (A.preprocess && !red && rd.clip == 0 && read_start_counts(A, rd, 1u, span))
+          A.qs_flag[(size_t)(rd.flags & kRev) * S.n_cols + rd.start] = 1;
+      }
+      if (red || !A.do_errors) continue;
+      // two bases per lane per trip keep two independent load chains in flight
+      for (uint32_t i = lane; i < span; i += 64) {
+        ec_events(S, A, sh_hist, true, rd, r, rd.start + i, (int)rd.clip + (int)i, 0, err);
+        if (i + 32 < span) ec_events(S, A, sh_hist, true, rd, r, rd.start + i + 32, (int)rd.clip + (int)i + 32, 0, err);
+      }
+      done += span;
+    } else {
+      // the CIGAR walk of htslib's pileup (resolve_cigar2): M/=/X blocks carry their read bases, the
+      // last base of a block sees the I / D run that follows it as its indel
+      const uint32_t* cg = S.cigar + rd.cigar_off;
+      const int nc = rd.n_cigar;
+      uint32_t x = rd.start;
+      int y = 0;
+      const QBounds qb = S.qb[r];
+      for (int k = 0; k < nc; k++) {
+        const uint32_t w = __ldg(cg + k), op = w & 0xF, len = w >> 4;
+        if (op_qm(op)) {
+          int ind = 0;
+          if (k + 1 < nc) {
+            const uint32_t w2 = __ldg(cg + k + 1), op2 = w2 & 0xF;
+            if (op2 == 2) {
+              ind = -(int)(w2 >> 4);
+              for (int j = k + 2; j < nc; j++) { const uint32_t wj = __ldg(cg + j); if ((wj & 0xF) == 2) ind -= (int)(wj >> 4); else break; }
+            } else if (op2 == 1) {
+              ind = (int)(w2 >> 4);
+              for (int j = k + 2; j < nc; j++) {
+                const uint32_t wj = __ldg(cg + j), o = wj & 0xF;
+                if (o == 1) ind += (int)(wj >> 4); else if (o != 6) break;
               }
-            }
-          }
-        } else if (e.indel == 1) {                  // (2c) one inserted base follows
-          const int mq = e.qpos + 1;
-          if (mq >= (int)rd.len) { local_err |= kErrBounds; }
-          else if (mq <= query_end0(S, rd, r) && mq >= query_start0(S, rd, r)) {
-            const uint8_t ob = nib_at(S.seq, so + mq);
-            if (ob != 15) {
-              int oi = bam_idx(ob);
-              if (oi < 0) local_err |= kErrBase;
-              else {
-                if (rev) oi = 3 - oi;
-                const uint32_t q = __ldg(S.qual + so + mq);
-                if (q >= A.Q || rs >= A.R) local_err |= kErrCovariate;
-                else atomicAdd(&sh_hist[rs + A.R * (4u + 5u * (oi + 5u * q))], 1u);
+            } else if (op2 == 6 && k + 2 < nc) {
+              int l3 = 0;
+              for (int j = k + 2; j < nc; j++) {
+                const uint32_t wj = __ldg(cg + j), o = wj & 0xF;
+                if (o == 1) l3 += (int)(wj >> 4); else if (op_ref(o)) break;
               }
+              if (l3 > 0) ind = l3;
             }
           }
+          if (lane == 0) {
+            atomicAdd(diff + x, 1);
+            atomicAdd(diff + x + len, -1);
+            if (A.preprocess && !red && y == 0 && read_start_counts(A, rd, (uint32_t)qb.qbs + 1u, (uint32_t)qb.qbe + 1u))
+              A.qs_flag[(size_t)(rd.flags & kRev) * S.n_cols + x] = 1;
+          }
+          if (!red && A.do_errors) {
+            for (uint32_t i = lane; i < len; i += 32)
+              ec_events(S, A, sh_hist, true, rd, r, x + i, y + (int)i, (i == len - 1) ? ind : 0, err);
+            done += len;
+          }
+          x += len;
+          y += (int)len;
+        } else if (op_ref(op)) {
+          x += len;                      // D / N columns: deletions, skipped by error counting
+        } else if (op == 1 || op == 4) {
+          y += (int)len;
         }
       }
-      // unique-only coverage histogram (error_count.cpp:181-186), one atomic per distinct value
-      const bool rec = real && !red;
-      const uint32_t g = rec ? __ldg(S.tgt_group + t) : 0;
-      const uint32_t key = rec ? (g * A.hist_cap + min(uniq, A.hist_cap - 1)) : 0xFFFFFFFFu;
-      const unsigned active = __ballot_sync(0xFFFFFFFFu, rec);
-      if (rec) {
-        const unsigned peers = __match_any_sync(active, key);
-        if (lane == __ffs(peers) - 1) atomicAdd(A.cov_hist + key, (unsigned long long)__popc(peers));
-        if (uniq >= A.hist_cap) local_err |= kErrBounds;
-        if (A.preprocess) {
-          atomicAdd(A.found + 2 * t + hqs0, 1ull);
-          atomicAdd(A.found + 2 * t + hqs1, 1ull);
-        }
-      }
-    }
-    if (++tiles_done == A.flush_tiles) {   // keep the shared u32 counters far from overflow
-      tiles_done = 0;
-      __syncthreads();
-      for (uint32_t i = threadIdx.x; i < nbins; i += blockDim.x) {
-        uint32_t v = sh_hist[i];
-        if (v) { atomicAdd(A.counts + i, (unsigned long long)v); sh_hist[i] = 0; }
-      }
-      __syncthreads();
     }
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < nbins; i += blockDim.x) {
-    uint32_t v = sh_hist[i];
+    const uint32_t v = sh_hist[i];
     if (v) atomicAdd(A.counts + i, (unsigned long long)v);
   }
-  if (local_err) atomicOr(A.err, local_err);
+  if (err) atomicOr(A.err, err);
+  (void)done;
+}
+
+// Block-wide inclusive scan of (a, b) pairs, 1024 threads.
+__device__ __forceinline__ void block_scan2(int& a, int& b, int* sh_a, int* sh_b) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int ya = __shfl_up_sync(0xFFFFFFFFu, a, o), yb = __shfl_up_sync(0xFFFFFFFFu, b, o);
+    if (lane >= o) { a += ya; b += yb; }
+  }
+  if (lane == 31) { sh_a[w] = a; sh_b[w] = b; }
+  __syncthreads();
+  if (w == 0) {
+    int va = sh_a[lane], vb = sh_b[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int ya = __shfl_up_sync(0xFFFFFFFFu, va, o), yb = __shfl_up_sync(0xFFFFFFFFu, vb, o);
+      if (lane >= o) { va += ya; vb += yb; }
+    }
+    sh_a[lane] = va; sh_b[lane] = vb;
+  }
+  __syncthreads();
+  if (w > 0) { a += sh_a[w - 1]; b += sh_b[w - 1]; }
+}
+
+__global__ void __launch_bounds__(1024) cov_blocksum_kernel(const int32_t* du, const int32_t* dr, uint32_t n,
+                                                            uint32_t* bu, uint32_t* br) {
+  __shared__ int sa[32], sb[32];
+  const uint32_t c = blockIdx.x * 1024 + threadIdx.x;
+  int a = c < n ? du[c] : 0, b = c < n ? dr[c] : 0;
+  block_scan2(a, b, sa, sb);
+  if (threadIdx.x == 1023) { bu[blockIdx.x] = (uint32_t)a; br[blockIdx.x] = (uint32_t)b; }
+}
+
+// Unique-only coverage histogram (error_count.cpp:176-191): a column counts when no redundant read
+// covers it; preprocess adds the read-start tallies of the same columns.
+__global__ void __launch_bounds__(1024) cov_hist_kernel(DevSample S, EcArgs A) {
+  __shared__ int sa[32], sb[32];
+  const uint32_t c = blockIdx.x * 1024 + threadIdx.x;
+  int a = c < S.n_cols ? A.diff_u[c] : 0, b = c < S.n_cols ? A.diff_r[c] : 0;
+  block_scan2(a, b, sa, sb);
+  a += (int)A.blk_u[blockIdx.x];
+  b += (int)A.blk_r[blockIdx.x];
+  bool rec = false;
+  uint32_t t = 0, key = 0xFFFFFFFFu;
+  if (c < S.n_cols && __ldg(S.ref + c) != 0) {
+    t = target_of(S, c);
+    if (__ldg(S.tgt_called + t) && b == 0) {
+      rec = true;
+      const uint32_t u = (uint32_t)a;
+      if (u >= A.hist_cap) atomicOr(A.err, kErrBounds);
+      key = __ldg(S.tgt_group + t) * A.hist_cap + min(u, A.hist_cap - 1);
+    }
+  }
+  const unsigned active = __ballot_sync(0xFFFFFFFFu, rec);
+  if (rec) {
+    const unsigned peers = __match_any_sync(active, key);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(A.cov_hist + key, (unsigned long long)__popc(peers));
+    if (A.preprocess) {
+      atomicAdd(A.found + 2 * t + A.qs_flag[c], 1ull);
+      atomicAdd(A.found + 2 * t + A.qs_flag[(size_t)S.n_cols + c], 1ull);
+    }
+  }
 }
 
 // ============================================================================ pass 2: column pass
 // identify_mutations_pileup::pileup_callback at insert position 0 (identify_mutations.cpp:1359-1686)
 // for every column: coverage, the five summed log10 likelihoods, the pure-genotype call, and the
-// decision of which columns go on to the EM candidate kernel.
+// decision of which columns go on to the EM candidate kernel.  The warp stages the records of each
+// 32-read batch in shared memory and walks only those that reach its tile, in BAM order, with the
+// base and quality loads of two reads in flight before either is consumed.
+constexpr uint32_t kColumnWarps = 8;
+
 template <bool FP64>
-__global__ void __launch_bounds__(256) im_column_kernel(DevSample S, ClassTable T, ImArgs A) {
+__global__ void __launch_bounds__(256, 4) im_column_kernel(DevSample S, ClassTable T, ImArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  DevRead* sh_rd = reinterpret_cast<DevRead*>(smem) + warp * 32;
   uint32_t local_err = 0;
   for (uint32_t tile = blockIdx.x * nwarps + warp; tile < S.n_tiles; tile += gridDim.x * nwarps) {
     const uint32_t c0 = tile * 32, c = c0 + lane;
@@ -298,47 +401,61 @@ __global__ void __launch_bounds__(256) im_column_kernel(DevSample S, ClassTable 
     double S64[5] = {0, 0, 0, 0, 0};
     float s32[5] = {0, 0, 0, 0, 0}, k32[5] = {0, 0, 0, 0, 0}, B[5] = {0, 0, 0, 0, 0};
     const uint2 rr = __ldg(S.tile_range + tile);
-    for (uint32_t r = rr.x; r < rr.y; r++) {
-      const DevRead rd = S.reads[r];
-      if ((rd.flags & kSkip) || rd.end <= c0) continue;
-      if (!(real && c >= rd.start && c < rd.end)) continue;
-      Pile e;
-      resolve(S, rd, c, e);
+    // One read of the batch as this lane sees it: pileup state at column c and the base / quality
+    // loads, issued for two reads before either is consumed.
+    struct Pend { uint32_t r; bool cov; Pile e; uint8_t base; uint8_t q; };
+    auto prep = [&](const DevRead& rd, uint32_t r, Pend& P) {
+      P.r = r;
+      P.cov = real && c >= rd.start && c < rd.end;
+      P.base = 15; P.q = 0;
+      if (!P.cov) return;
+      if (rd.flags & kSimple) { P.e.qpos = (int)(c - rd.start) + rd.clip; P.e.indel = 0; P.e.del = false; }
+      else resolve(S, rd, c, P.e);
+      const bool rev = rd.flags & kRev;
+      int qp = P.e.qpos;
+      if (P.e.del) qp += 1 - (int)rev;
+      if (qp < (int)rd.len) {
+        P.base = nib_at(S.seq, rd.seq_off + qp);            // the base itself, or the one checked for a deletion
+        P.q = __ldg(S.qual + rd.seq_off + qp);
+      }
+    };
+    auto consume = [&](const DevRead& rd, const Pend& P) {
+      if (!P.cov) return;
+      const Pile& e = P.e;
       const bool rev = rd.flags & kRev;
       const bool red = rd.flags & kRedundant;
       if (failed) {
         // tabulate_position_coverage (identify_mutations.cpp:2218-2250)
-        if (e.del) continue;
-        if (nib_at(S.seq, rd.seq_off + e.qpos) == 15) continue;
+        if (e.del || P.base == 15) return;
         if (!red) { if (rev) ++ubot; else ++utop; }
-        else { double w = 1.0 / (double)__ldg(S.x1 + r); if (rev) { redbot += w; ++rbot; } else { redtop += w; ++rtop; } }
-        continue;
+        else { double w = 1.0 / (double)__ldg(S.x1 + P.r); if (rev) { redbot += w; ++rbot; } else { redtop += w; ++rtop; } }
+        return;
       }
-      const int obi = e.del ? -1 : max(e.indel, 0);
-      const uint8_t base = e.del ? (uint8_t)'.' : nib_at(S.seq, rd.seq_off + e.qpos);
-      if (base == 15) continue;
-      if (!red) {
-        if (rev) ++ubot; else ++utop;
-        if (obi > 0) slots = true;
-      } else {
+      if (!e.del && P.base == 15) return;                     // N read base: not counted at all
+      if (red) {
         uonly = false;
-        double w = 1.0 / (double)__ldg(S.x1 + r);
+        const double w = 1.0 / (double)__ldg(S.x1 + P.r);
         if (rev) { redbot += w; ++rbot; } else { redtop += w; ++rtop; }
-        continue;
+        return;
       }
-      if (is_trimmed(rd, e.qpos, e.del)) continue;
-      int qp = e.qpos;
+      if (rev) ++ubot; else ++utop;
+      if (e.indel > 0 && !e.del) slots = true;
+      // trims: a read with XL and XR both absent or 0 is never trimmed except at a deletion column
+      if ((e.del || (rd.xl != kNoTag && rd.xl != 0) || (rd.xr != kNoTag && rd.xr != 0)) && is_trimmed(rd, e.qpos, e.del))
+        return;
       if (e.del) {
-        qp += 1 - (int)rev;
-        if (qp >= (int)rd.len) continue;      // the reference asserts here; unusable base
-        if (nib_at(S.seq, rd.seq_off + qp) == 15) continue;
+        // the quality comes from the next base; the reference asserts if there is none
+        if (e.qpos + 1 - (int)rev >= (int)rd.len || P.base == 15) return;
       }
-      const int obs = e.del ? 4 : bam_idx(base);
-      if (obs < 0) { local_err |= kErrBase; continue; }
-      const uint32_t q = __ldg(S.qual + rd.seq_off + qp);
+      int obs = 4;
+      if (!e.del) {
+        if (P.base & (P.base - 1)) { local_err |= kErrBase; return; }   // not one of A, C, G, T
+        obs = __ffs(P.base) - 1;
+      }
+      const uint32_t q = P.q;
       const uint32_t rs = rd.rfile;
-      if (q >= T.Q || rs >= T.R) { local_err |= kErrCovariate; continue; }
-      if (q < A.base_quality_cutoff) continue;
+      if (q >= T.Q || rs >= T.R) { local_err |= kErrCovariate; return; }
+      if (q < A.base_quality_cutoff) return;
       const uint32_t k = ((((uint32_t)rd.mapq_idx * T.R + rs) * 2u + (rev ? 1u : 0u)) * T.Q + q) * 5u + (uint32_t)obs;
       ++n;
       if (FP64) {
@@ -350,7 +467,7 @@ __global__ void __launch_bounds__(256) im_column_kernel(DevSample S, ClassTable 
         const float2 w = __ldg(reinterpret_cast<const float2*>(T.lp32 + (size_t)k * 8 + 4));
         const float lp[5] = {v.x, v.y, v.z, v.w, w.x};
 #pragma unroll
-        for (int b = 0; b < 5; b++) {        // Kahan-compensated FP32 sums
+        for (int b = 0; b < 5; b++) {          // Kahan-compensated FP32 sums
           const float y = lp[b] - k32[b];
           const float tt = s32[b] + y;
           k32[b] = (tt - s32[b]) - y;
@@ -364,66 +481,95 @@ __global__ void __launch_bounds__(256) im_column_kernel(DevSample S, ClassTable 
           for (int b = 0; b < 5; b++) B[b] += fmaxf(0.0f, lp[b] - lr);
         }
       }
-    }
-    if (!inr) continue;
-    ColCov cv;
-    cv.uniq_top = utop; cv.uniq_bot = ubot; cv.rawred_top = rtop; cv.rawred_bot = rbot;
-    cv.red_top = redtop; cv.red_bot = redbot;
-    ColCall cl;
-    cl.n = n; cl.best = 5; cl.score = __longlong_as_double(0x7ff8000000000000ll); cl.flags = 0;
-    cl.pad[0] = cl.pad[1] = 0;
-    if (real && !failed) {
-      if (uonly) cl.flags |= kUniqueOnly;
-      if (slots) cl.flags |= kSlots;
-      cl.flags |= kScored;
-      if (n > 0) {
-        // pure_genotype_call (identify_mutations.cpp:3398-3433) and the Bonferroni shift (:1680)
-        int best = 0;
-        double score;
-        if (FP64) {
-#pragma unroll
-          for (int b = 1; b < 5; b++) if (S64[b] > S64[best]) best = b;
-          double off = -DBL_MAX;
-#pragma unroll
-          for (int b = 0; b < 5; b++) if (b != best) off = fmax(off, S64[b]);
-          double te = 0;
-#pragma unroll
-          for (int b = 0; b < 5; b++) if (b != best) te += exp10(S64[b] - off);
-          score = S64[best] - (log10(te) + off) - A.log10_ref_len;
-          if (best != ref_idx && score > 0) cl.flags |= kCandidate;
-          cl.flags |= kCandidate;            // the plain form runs the EM wherever a base was scored
-        } else {
-          double tot[5];
-#pragma unroll
-          for (int b = 0; b < 5; b++) tot[b] = (double)s32[b] - (double)k32[b];
-#pragma unroll
-          for (int b = 1; b < 5; b++) if (tot[b] > tot[best]) best = b;
-          double d[5], off = -DBL_MAX;
-#pragma unroll
-          for (int b = 0; b < 5; b++) { d[b] = tot[b] - tot[best]; if (b != best) off = fmax(off, d[b]); }
-          float te = 0.0f;
-#pragma unroll
-          for (int b = 0; b < 5; b++) if (b != best) te += exp10f((float)(d[b] - off));
-          score = -(off + (double)log10f(te)) - A.log10_ref_len;
-          // guard band: FP32 sums are within ~n * 6e-7 of FP64; decisions closer than that are
-          // recomputed in FP64 by the candidate kernel
-          const double g = (double)A.guard * (1.0 + (double)n);
-          const bool near = fabs(score - A.mutation_cutoff) < g || (best != ref_idx && fabs(score) < g) || off > -g;
-          if (near) cl.flags |= kRecompute;
-          if (best != ref_idx && score > 0) cl.flags |= kCandidate;
-          float bmax = 0.0f;
-#pragma unroll
-          for (int b = 0; b < 5; b++) if (b != ref_idx) bmax = fmaxf(bmax, B[b]);
-          if (ref_idx == 5 || (double)bmax - A.log10_ref_len >= A.poly_cutoff - (double)A.screen_margin)
-            cl.flags |= kCandidate;
-        }
-        cl.best = (uint8_t)best;
-        cl.score = score;
-        if (score >= A.mutation_cutoff) cl.flags |= kBasePredicted;
+    };
+    for (uint32_t b0 = rr.x; b0 < rr.y; b0 += 32) {
+      const uint32_t rl = b0 + lane;
+      bool rel = false;
+      if (rl < rr.y) {
+        const DevRead mine = S.reads[rl];
+        rel = !(mine.flags & kSkip) && mine.end > c0;
+        sh_rd[lane] = mine;
       }
+      unsigned mask = __ballot_sync(0xFFFFFFFFu, rel);
+      __syncwarp();
+      while (mask) {                                  // reads in BAM order, two at a time
+        const int j1 = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int j2 = mask ? __ffs(mask) - 1 : -1;
+        if (j2 >= 0) mask &= mask - 1;
+        const DevRead rd1 = sh_rd[j1];
+        Pend P1, P2;
+        prep(rd1, b0 + j1, P1);
+        if (j2 >= 0) {
+          const DevRead rd2 = sh_rd[j2];
+          prep(rd2, b0 + j2, P2);
+          consume(rd1, P1);
+          consume(rd2, P2);
+        } else {
+          consume(rd1, P1);
+        }
+      }
+      __syncwarp();
     }
-    A.cov[c] = cv;
-    A.call[c] = cl;
+    if (inr) {
+      ColCov cv;
+      cv.uniq_top = utop; cv.uniq_bot = ubot; cv.rawred_top = rtop; cv.rawred_bot = rbot;
+      cv.red_top = redtop; cv.red_bot = redbot;
+      ColCall cl;
+      cl.n = n; cl.best = 5; cl.score = __longlong_as_double(0x7ff8000000000000ll); cl.flags = 0;
+      cl.pad[0] = cl.pad[1] = 0;
+      if (real && !failed) {
+        if (uonly) cl.flags |= kUniqueOnly;
+        if (slots) cl.flags |= kSlots;
+        cl.flags |= kScored;
+        if (n > 0) {
+          // pure_genotype_call (identify_mutations.cpp:3398-3433) and the Bonferroni shift (:1680)
+          int best = 0;
+          double score;
+          if (FP64) {
+#pragma unroll
+            for (int b = 1; b < 5; b++) if (S64[b] > S64[best]) best = b;
+            double off = -DBL_MAX;
+#pragma unroll
+            for (int b = 0; b < 5; b++) if (b != best) off = fmax(off, S64[b]);
+            double te = 0;
+#pragma unroll
+            for (int b = 0; b < 5; b++) if (b != best) te += exp10(S64[b] - off);
+            score = S64[best] - (log10(te) + off) - A.log10_ref_len;
+            cl.flags |= kCandidate;            // the plain form runs the EM wherever a base was scored
+          } else {
+            double tot[5];
+#pragma unroll
+            for (int b = 0; b < 5; b++) tot[b] = (double)s32[b] - (double)k32[b];
+#pragma unroll
+            for (int b = 1; b < 5; b++) if (tot[b] > tot[best]) best = b;
+            double d[5], off = -DBL_MAX;
+#pragma unroll
+            for (int b = 0; b < 5; b++) { d[b] = tot[b] - tot[best]; if (b != best) off = fmax(off, d[b]); }
+            float te = 0.0f;
+#pragma unroll
+            for (int b = 0; b < 5; b++) if (b != best) te += exp10f((float)(d[b] - off));
+            score = -(off + (double)log10f(te)) - A.log10_ref_len;
+            // guard band: FP32 sums are within ~n * 6e-7 of FP64; decisions closer than that are
+            // recomputed in FP64 by the candidate kernel
+            const double g = (double)A.guard * (1.0 + (double)n);
+            const bool near = fabs(score - A.mutation_cutoff) < g || (best != ref_idx && fabs(score) < g) || off > -g;
+            if (near) cl.flags |= kRecompute;
+            if (best != ref_idx && score > 0) cl.flags |= kCandidate;
+            float bmax = 0.0f;
+#pragma unroll
+            for (int b = 0; b < 5; b++) if (b != ref_idx) bmax = fmaxf(bmax, B[b]);
+            if (ref_idx == 5 || (double)bmax - A.log10_ref_len >= A.poly_cutoff - (double)A.screen_margin)
+              cl.flags |= kCandidate;
+          }
+          cl.best = (uint8_t)best;
+          cl.score = score;
+          if (score >= A.mutation_cutoff) cl.flags |= kBasePredicted;
+        }
+      }
+      A.cov[c] = cv;
+      A.call[c] = cl;
+    }
   }
   if (local_err) atomicOr(A.err, local_err);
 }
@@ -595,20 +741,28 @@ cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t
   tile_range_kernel<<<(n_tiles + 255) / 256, 256, 0, st>>>(rstart, n_reads, n_tiles, maxspan, tile_range, max_tile_reads);
   return cudaGetLastError();
 }
-cudaError_t launch_ec(const DevSample& S, const EcArgs& A, int sms, cudaStream_t st) {
+cudaError_t launch_ec(const DevSample& S, const EcArgs& A, int sms, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1) {
   const size_t smem = (size_t)A.R * 25 * A.Q * sizeof(uint32_t);
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(ec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(ec_read_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  const int grid = grid_for(S.n_tiles, 8, sms, 8);
-  ec_kernel<<<grid, 256, smem, st>>>(S, A);
+  const int grid = grid_for(S.n_reads / 8 + 1, 8, sms, 8);
+  if (main0) cudaEventRecord(main0, st);
+  ec_read_kernel<<<grid, 256, smem, st>>>(S, A);
+  if (main1) cudaEventRecord(main1, st);
+  const uint32_t nb = (S.n_cols + 1023) / 1024;
+  cov_blocksum_kernel<<<nb, 1024, 0, st>>>(A.diff_u, A.diff_r, S.n_cols, A.blk_u, A.blk_r);
+  scan_kernel<<<1, 1024, 0, st>>>(A.blk_u, nb, A.blk_u + nb);
+  scan_kernel<<<1, 1024, 0, st>>>(A.blk_r, nb, A.blk_r + nb);
+  cov_hist_kernel<<<nb, 1024, 0, st>>>(S, A);
   return cudaGetLastError();
 }
 cudaError_t launch_im_column(const DevSample& S, const ClassTable& T, const ImArgs& A, int sms, cudaStream_t st) {
   const int grid = grid_for(S.n_tiles, 8, sms, 8);
-  if (A.precision == 0) im_column_kernel<true><<<grid, 256, 0, st>>>(S, T, A);
-  else im_column_kernel<false><<<grid, 256, 0, st>>>(S, T, A);
+  const size_t smem = kColumnWarps * 32 * sizeof(DevRead);
+  if (A.precision == 0) im_column_kernel<true><<<grid, 32 * kColumnWarps, smem, st>>>(S, T, A);
+  else im_column_kernel<false><<<grid, 32 * kColumnWarps, smem, st>>>(S, T, A);
   return cudaGetLastError();
 }
 cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_counts, uint32_t* total, uint32_t* out,

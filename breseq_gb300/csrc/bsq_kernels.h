@@ -23,6 +23,7 @@ struct RawSoA {
   const uint16_t* n_cigar;
   const uint32_t* cigar;
   const uint32_t* tpoff;     // padded target offsets
+  const uint8_t* called;     // per target: in the pileup set
   uint32_t n;
   uint32_t n_targets;
   uint64_t n_bases;
@@ -43,7 +44,8 @@ cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st);
 cudaError_t launch_mapq_index(DevRead* reads, const uint8_t* mapq, const uint8_t* map, uint32_t n, cudaStream_t st);
 cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t n_tiles, uint32_t maxspan,
                               uint2* tile_range, uint32_t* max_tile_reads, cudaStream_t st);
-cudaError_t launch_ec(const DevSample& S, const EcArgs& A, int sms, cudaStream_t st);
+cudaError_t launch_ec(const DevSample& S, const EcArgs& A, int sms, cudaStream_t st, cudaEvent_t main0,
+                      cudaEvent_t main1);
 cudaError_t launch_im_column(const DevSample& S, const ClassTable& T, const ImArgs& A, int sms, cudaStream_t st);
 cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_counts, uint32_t* total, uint32_t* out,
                            cudaStream_t st);
