@@ -48,6 +48,15 @@ def load():
     L.bsq_host_unregister.argtypes = [C.c_void_p]
     L.bsq_score_positions_noalloc.argtypes = [C.c_void_p, C.c_int32, P(abi.ImParams), P(C.c_double), C.c_void_p,
                                               C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+    L.bsq_default_ra_settings.argtypes = [C.c_int, P(abi.RaSettings)]
+    L.bsq_test_ra_evidence.argtypes = [C.c_void_p, C.c_uint64, P(abi.RaSettings), P(abi.Reference), P(C.c_char_p), C.c_void_p]
+    L.bsq_write_error_rates.argtypes = [C.c_char_p, P(C.c_uint64), C.c_uint32, C.c_uint32]
+    L.bsq_write_base_qual_error_prob.argtypes = [C.c_char_p, P(C.c_char_p), P(C.c_uint64), C.c_uint32, C.c_uint32]
+    L.bsq_write_coverage_distribution.argtypes = [C.c_char_p, P(C.c_uint64), C.c_uint32]
+    L.bsq_write_coverage_table.argtypes = [C.c_char_p, C.c_char_p, P(abi.Reference), C.c_uint32, P(abi.PositionArrays)]
+    L.bsq_format_ra.argtypes = [C.c_void_p, C.c_char_p, C.c_uint32, C.c_char_p, C.c_uint64]
+    L.bsq_write_gd.argtypes = [C.c_char_p, P(abi.Reference), P(C.c_char_p), P(C.c_double), C.c_uint32, C.c_void_p,
+                               C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]
     _lib = L
     return L
 
@@ -55,4 +64,6 @@ def load():
 EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_load_sample", "bsq_free_sample",
             "bsq_sample_footprint", "bsq_error_count", "bsq_counts_to_log10_prob", "bsq_identify_mutations",
             "bsq_im_result_counts", "bsq_im_result_copy", "bsq_last_pass_stats", "bsq_timer_start",
-            "bsq_timer_stop", "bsq_host_register", "bsq_host_unregister", "bsq_score_positions_noalloc")
+            "bsq_timer_stop", "bsq_host_register", "bsq_host_unregister", "bsq_score_positions_noalloc",
+            "bsq_default_ra_settings", "bsq_test_ra_evidence", "bsq_write_error_rates", "bsq_write_base_qual_error_prob",
+            "bsq_write_coverage_distribution", "bsq_write_coverage_table", "bsq_format_ra", "bsq_write_gd")

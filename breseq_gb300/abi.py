@@ -108,6 +108,31 @@ class RaRaw(C.Structure):
     ]
 
 
+class RaSettings(C.Structure):
+    _fields_ = [
+        ("polymorphism_prediction", C.c_int32), ("polymorphism_precision_places", C.c_uint32),
+        ("mutation_log10_e_value_cutoff", C.c_double), ("consensus_frequency_cutoff", C.c_double),
+        ("consensus_minimum_variant_coverage", C.c_double), ("consensus_minimum_total_coverage", C.c_double),
+        ("consensus_minimum_variant_coverage_each_strand", C.c_double),
+        ("consensus_minimum_total_coverage_each_strand", C.c_double),
+        ("consensus_reject_indel_homopolymer_length", C.c_uint32),
+        ("consensus_reject_surrounding_homopolymer_length", C.c_uint32),
+        ("polymorphism_log10_e_value_cutoff", C.c_double), ("polymorphism_frequency_cutoff", C.c_double),
+        ("polymorphism_minimum_variant_coverage", C.c_double), ("polymorphism_minimum_total_coverage", C.c_double),
+        ("polymorphism_minimum_variant_coverage_each_strand", C.c_double),
+        ("polymorphism_minimum_total_coverage_each_strand", C.c_double),
+        ("polymorphism_reject_indel_homopolymer_length", C.c_uint32),
+        ("polymorphism_reject_surrounding_homopolymer_length", C.c_uint32),
+        ("polymorphism_fisher_strand_p_value_cutoff", C.c_double),
+        ("polymorphism_ks_quality_p_value_cutoff", C.c_double), ("polymorphism_no_indels", C.c_int32),
+    ]
+
+
+class RaCall(C.Structure):
+    _fields_ = [("prediction", C.c_char * 16), ("reject", C.c_char * 96), ("consensus_reject", C.c_char * 96),
+                ("polymorphism_reject", C.c_char * 96), ("deleted", C.c_uint8), ("pad", C.c_uint8 * 7)]
+
+
 class McRecord(C.Structure):
     _fields_ = [
         ("tid", C.c_uint32), ("start", C.c_uint32), ("end", C.c_uint32), ("start_range", C.c_uint32),
@@ -184,6 +209,39 @@ def ra_to_dicts(arr) -> list:
             minor_cov=tuple(r.minor_cov), total_cov=tuple(r.total_cov), n=r.n,
             passed_consensus=r.passed_consensus, passed_polymorphism=r.passed_polymorphism))
     return out
+
+
+def ra_from_dicts(recs):
+    arr = (RaRecord * max(1, len(recs)))()
+    for i, d in enumerate(recs):
+        r = arr[i]
+        for k in ("tid", "position", "insert_position", "score", "consensus_score", "major_frequency", "frequency",
+                  "frequency_lower", "frequency_upper", "fisher_strand_p", "ks_quality_p", "n",
+                  "passed_consensus", "passed_polymorphism"):
+            setattr(r, k, d[k])
+        for k in ("ref_base", "new_base", "major_base", "minor_base"):
+            setattr(r, k, d[k].encode())
+        for b in range(5):
+            r.f[b] = d["f"][b]
+        for k in ("ref_cov", "new_cov", "major_cov", "minor_cov", "total_cov"):
+            getattr(r, k)[0], getattr(r, k)[1] = d[k]
+    return arr
+
+
+def mc_from_dicts(recs):
+    arr = (McRecord * max(1, len(recs)))()
+    for i, d in enumerate(recs):
+        for k, v in d.items():
+            setattr(arr[i], k, v)
+    return arr
+
+
+def un_from_dicts(recs):
+    arr = (UnRecord * max(1, len(recs)))()
+    for i, d in enumerate(recs):
+        for k, v in d.items():
+            setattr(arr[i], k, v)
+    return arr
 
 
 def mc_to_dicts(arr) -> list:

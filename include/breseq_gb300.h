@@ -190,6 +190,73 @@ typedef struct bsq_position_arrays {
     uint32_t* n_scored;
 } bsq_position_arrays;
 
+/* ---------------------------------------------------------------- RA classification */
+
+/* The Settings fields test_RA_evidence reads (src/breseq/identify_mutations.cpp:143-749); defaults from
+ * bsq_default_ra_settings (src/breseq/settings.cpp:857-950).  A cutoff of 0 switches its test off. */
+typedef struct bsq_ra_settings {
+    int32_t  polymorphism_prediction;
+    uint32_t polymorphism_precision_places;
+    double   mutation_log10_e_value_cutoff;
+    double   consensus_frequency_cutoff;
+    double   consensus_minimum_variant_coverage;
+    double   consensus_minimum_total_coverage;
+    double   consensus_minimum_variant_coverage_each_strand;
+    double   consensus_minimum_total_coverage_each_strand;
+    uint32_t consensus_reject_indel_homopolymer_length;
+    uint32_t consensus_reject_surrounding_homopolymer_length;
+    double   polymorphism_log10_e_value_cutoff;
+    double   polymorphism_frequency_cutoff;
+    double   polymorphism_minimum_variant_coverage;
+    double   polymorphism_minimum_total_coverage;
+    double   polymorphism_minimum_variant_coverage_each_strand;
+    double   polymorphism_minimum_total_coverage_each_strand;
+    uint32_t polymorphism_reject_indel_homopolymer_length;
+    uint32_t polymorphism_reject_surrounding_homopolymer_length;
+    double   polymorphism_fisher_strand_p_value_cutoff;
+    double   polymorphism_ks_quality_p_value_cutoff;
+    int32_t  polymorphism_no_indels;
+} bsq_ra_settings;
+
+/* Outcome of test_RA_evidence for one RA item. */
+typedef struct bsq_ra_call {
+    char    prediction[16];            /* "consensus" / "polymorphism" / "" */
+    char    reject[96];                /* comma-separated reasons                  */
+    char    consensus_reject[96];
+    char    polymorphism_reject[96];
+    uint8_t deleted;                   /* the reference drops the item             */
+    uint8_t pad[7];
+} bsq_ra_call;
+
+int bsq_default_ra_settings(int polymorphism_prediction, bsq_ra_settings* s);
+
+/* test_RA_evidence (src/breseq/identify_mutations.cpp:687-749) on RA items as they would be written to
+ * and read back from the GenomeDiff (values formatted with the reference's precision first). */
+int bsq_test_ra_evidence(const bsq_ra_record* ra, uint64_t n, const bsq_ra_settings* s, const bsq_reference* ref,
+                         const char* const* target_names, bsq_ra_call* out);
+
+/* ---------------------------------------------------------------- output files */
+
+/* error_rates.tab: counts_to_log10_prob + write_log10_prob_table (src/breseq/error_count.cpp:660-690, 1005-1026) */
+int bsq_write_error_rates(const char* path, const uint64_t* counts, uint32_t n_read_files, uint32_t n_quality);
+/* base_qual_error_prob.#.tab, '#' replaced by each read file's name (error_count.cpp:697-785) */
+int bsq_write_base_qual_error_prob(const char* path_pattern, const char* const* read_file_names, const uint64_t* counts,
+                                   uint32_t n_read_files, uint32_t n_quality);
+/* <group>.unique_only_coverage_distribution.tab (error_count.cpp:239-253); size = hist_size of the group */
+int bsq_write_coverage_distribution(const char* path, const uint64_t* hist, uint32_t size);
+/* <seq_id>.coverage.tsv aggregate columns from per-position arrays (identify_mutations.cpp:2028-2052, 2173-2204) */
+int bsq_write_coverage_table(const char* path, const char* seq_id, const bsq_reference* ref, uint32_t tid,
+                             const bsq_position_arrays* positions);
+/* One RA item as its GenomeDiff fields (tab-separated, no type / id / evidence columns). */
+int bsq_format_ra(const bsq_ra_record* ra, const char* seq_id, uint32_t precision_places, char* buf, uint64_t cap);
+/* ra_mc_evidence.gd: RA / MC / UN lines with ids in the pileup's add order and cGenomeDiff's sort order
+ * (src/breseq/genome_diff.cpp:685-760, genome_diff_entry.cpp:570-660).  `calls` (may be NULL) adds the
+ * test_RA_evidence fields and leaves out deleted items. */
+int bsq_write_gd(const char* path, const bsq_reference* ref, const char* const* target_names,
+                 const double* deletion_propagation_cutoff, uint32_t precision_places,
+                 const bsq_ra_record* ra, uint64_t n_ra, const bsq_ra_call* calls,
+                 const bsq_mc_record* mc, uint64_t n_mc, const bsq_un_record* un, uint64_t n_un);
+
 /* ---------------------------------------------------------------- context API */
 
 typedef struct bsq_ctx bsq_ctx;
