@@ -37,6 +37,12 @@ def load():
     L.bsq_sample_footprint.argtypes = [P(abi.Reference), P(abi.ReadSoA)]
     L.bsq_sample_footprint.restype = C.c_uint64
     L.bsq_error_count.argtypes = [C.c_void_p, C.c_int32, P(abi.EcParams), P(abi.EcResult)]
+    L.bsq_error_count_batch.argtypes = [C.c_void_p, C.c_uint32, P(C.c_int32), P(abi.EcParams), P(abi.EcResult)]
+    L.bsq_identify_mutations_batch.argtypes = [C.c_void_p, C.c_uint32, P(C.c_int32), P(abi.ImParams),
+                                               P(P(C.c_double)), P(P(abi.PositionArrays))]
+    L.bsq_im_batch_result_counts.argtypes = [C.c_void_p, C.c_uint32, P(C.c_uint64), P(C.c_uint64), P(C.c_uint64)]
+    L.bsq_im_batch_result_copy.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
+                                           C.c_void_p, C.c_uint64]
     L.bsq_counts_to_log10_prob.argtypes = [P(C.c_uint64), C.c_uint32, C.c_uint32, P(C.c_double)]
     L.bsq_identify_mutations.argtypes = [C.c_void_p, C.c_int32, P(abi.ImParams), P(C.c_double), P(abi.PositionArrays)]
     L.bsq_im_result_counts.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_uint64), P(C.c_uint64)]
@@ -57,13 +63,35 @@ def load():
     L.bsq_format_ra.argtypes = [C.c_void_p, C.c_char_p, C.c_uint32, C.c_char_p, C.c_uint64]
     L.bsq_write_gd.argtypes = [C.c_char_p, P(abi.Reference), P(C.c_char_p), P(C.c_double), C.c_uint32, C.c_void_p,
                                C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]
+    L.bsq_job_footprint.argtypes = [P(abi.Reference), P(abi.ReadSoA)]
+    L.bsq_job_footprint.restype = C.c_uint64
+    L.bsq_server_create.argtypes = [P(C.c_void_p), C.c_int, C.c_uint64, C.c_uint32, C.c_int32]
+    L.bsq_server_destroy.argtypes = [C.c_void_p]
+    L.bsq_server_destroy.restype = None
+    L.bsq_server_last_error.argtypes = [C.c_void_p]
+    L.bsq_server_last_error.restype = C.c_char_p
+    L.bsq_server_submit.argtypes = [C.c_void_p, P(abi.Job), P(C.c_uint64)]
+    L.bsq_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_int64, P(abi.JobInfo)]
+    L.bsq_server_job_info.argtypes = [C.c_void_p, C.c_uint64, P(abi.JobInfo)]
+    L.bsq_server_job_error.argtypes = [C.c_void_p, C.c_uint64]
+    L.bsq_server_job_error.restype = C.c_char_p
+    L.bsq_server_error_counts.argtypes = [C.c_void_p, C.c_uint64, P(C.c_uint64), P(C.c_uint64), P(C.c_uint32)]
+    L.bsq_server_results.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
+                                     C.c_void_p, C.c_uint64]
+    L.bsq_server_release.argtypes = [C.c_void_p, C.c_uint64]
+    L.bsq_server_get_stats.argtypes = [C.c_void_p, P(abi.ServerStats)]
     _lib = L
     return L
 
 
 EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_load_sample", "bsq_free_sample",
             "bsq_sample_footprint", "bsq_error_count", "bsq_counts_to_log10_prob", "bsq_identify_mutations",
-            "bsq_im_result_counts", "bsq_im_result_copy", "bsq_last_pass_stats", "bsq_timer_start",
+            "bsq_im_result_counts", "bsq_im_result_copy",
+            "bsq_error_count_batch", "bsq_identify_mutations_batch", "bsq_im_batch_result_counts",
+            "bsq_im_batch_result_copy", "bsq_job_footprint", "bsq_server_create", "bsq_server_destroy",
+            "bsq_server_last_error", "bsq_server_submit", "bsq_server_wait", "bsq_server_job_info",
+            "bsq_server_job_error", "bsq_server_error_counts", "bsq_server_results", "bsq_server_release",
+            "bsq_server_get_stats", "bsq_last_pass_stats", "bsq_timer_start",
             "bsq_timer_stop", "bsq_host_register", "bsq_host_unregister", "bsq_score_positions_noalloc",
             "bsq_default_ra_settings", "bsq_test_ra_evidence", "bsq_write_error_rates", "bsq_write_base_qual_error_prob",
             "bsq_write_coverage_distribution", "bsq_write_coverage_table", "bsq_format_ra", "bsq_write_gd")

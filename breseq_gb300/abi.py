@@ -160,6 +160,23 @@ def ptr(a: np.ndarray, ctype):
     return a.ctypes.data_as(P(ctype))
 
 
+class Job(C.Structure):
+    _fields_ = [("ref", C.POINTER(Reference)), ("reads", C.POINTER(ReadSoA)), ("ec", EcParams), ("im", ImParams),
+                ("hist_capacity", C.c_uint32)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("round_jobs", C.c_uint32), ("footprint", C.c_uint64), ("n_ra", C.c_uint64),
+                ("n_mc", C.c_uint64), ("n_un", C.c_uint64), ("read_bases", C.c_uint64), ("submit_ms", C.c_double),
+                ("admit_ms", C.c_double), ("ready_ms", C.c_double), ("start_ms", C.c_double), ("done_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("jobs_done", C.c_uint64), ("rounds", C.c_uint64), ("budget", C.c_uint64), ("in_use", C.c_uint64),
+                ("peak_in_use", C.c_uint64), ("max_round_jobs", C.c_uint32), ("max_resident_jobs", C.c_uint32),
+                ("gpu_busy_ms", C.c_double)]
+
+
 class SampleView:
     """Builds the Reference / ReadSoA structs over a synth.Sample (or any object with the same
     array attributes) and keeps every array it points into alive."""

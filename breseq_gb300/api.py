@@ -41,6 +41,28 @@ class ImSettings:
         return poly, places
 
 
+def im_params(s, st: ImSettings, deletion_propagation_cutoff=None, deletion_seed_cutoff=None, precision=PRECISION_FP32C,
+              n_read_files=None, n_quality=None):
+    """bsq_im_params for sample `s`; returns (params, arrays the params point into)."""
+    poly, places = st.resolved()
+    T = len(s.target_offset) - 1
+    keep = dict(
+        prop=np.broadcast_to(np.asarray(5.0 if deletion_propagation_cutoff is None else deletion_propagation_cutoff,
+                                        dtype=np.float64), (T,)).copy(),
+        seed=np.broadcast_to(np.asarray(0.0 if deletion_seed_cutoff is None else deletion_seed_cutoff,
+                                        dtype=np.float64), (T,)).copy())
+    p = abi.ImParams(n_read_files=n_read_files or s.n_read_files, n_quality=n_quality or s.n_quality,
+                     base_quality_cutoff=st.base_quality_cutoff,
+                     mutation_cutoff=st.mutation_log10_e_value_cutoff, polymorphism_cutoff=poly,
+                     polymorphism_precision_decimal=st.polymorphism_precision_decimal,
+                     polymorphism_precision_places=places,
+                     skip_missing_coverage_prediction=int(st.skip_missing_coverage_prediction),
+                     log10_ref_length=float(np.log10(float(s.target_offset[-1]))),
+                     deletion_propagation_cutoff=abi.ptr(keep["prop"], C.c_double),
+                     deletion_seed_cutoff=abi.ptr(keep["seed"], C.c_double), precision=precision)
+    return p, keep
+
+
 class Scorer:
     """One library context on one GPU; samples stay resident until freed."""
 
@@ -83,26 +105,41 @@ class Scorer:
         return self._views[sid][0]
 
     # ------------------------------------------------------------------ pass 1
-    def error_count(self, sid: int, n_read_files=None, n_quality=None, do_coverage=True, do_errors=True,
-                    preprocess=False, unmatched_end_minimum_read_length=50, unmatched_end_length_factor=0.1,
-                    hist_capacity=8192):
+    def _ec_job(self, sid, n_read_files, n_quality, do_coverage, do_errors, preprocess,
+                unmatched_end_minimum_read_length, unmatched_end_length_factor, hist_capacity):
         s = self.sample(sid)
         R = n_read_files or s.n_read_files
         Q = n_quality or s.n_quality
         G = s.n_coverage_groups
-        counts = np.zeros(R * 25 * Q, dtype=np.uint64)
-        hist = np.zeros(G * hist_capacity, dtype=np.uint64)
-        hsize = np.zeros(G, dtype=np.uint32)
-        pr = np.zeros(len(s.target_offset) - 1, dtype=np.float64)
+        res = dict(counts=np.zeros(R * 25 * Q, dtype=np.uint64), hist=np.zeros((G, hist_capacity), dtype=np.uint64),
+                   hist_size=np.zeros(G, dtype=np.uint32),
+                   no_pos_hash_pr=np.zeros(len(s.target_offset) - 1, dtype=np.float64))
         p = abi.EcParams(n_read_files=R, n_quality=Q, do_coverage=int(do_coverage), do_errors=int(do_errors),
                          preprocess_stage=int(preprocess),
                          unmatched_end_minimum_read_length=unmatched_end_minimum_read_length,
                          unmatched_end_length_factor=unmatched_end_length_factor)
-        out = abi.EcResult(counts=abi.ptr(counts, C.c_uint64), coverage_hist=abi.ptr(hist, C.c_uint64),
-                           hist_capacity=hist_capacity, hist_size=abi.ptr(hsize, C.c_uint32),
-                           no_pos_hash_pr=abi.ptr(pr, C.c_double))
-        self._check(self.L.bsq_error_count(self.ctx, sid, C.byref(p), C.byref(out)))
-        return dict(counts=counts, hist=hist.reshape(G, hist_capacity), hist_size=hsize, no_pos_hash_pr=pr)
+        out = abi.EcResult(counts=abi.ptr(res["counts"], C.c_uint64), coverage_hist=abi.ptr(res["hist"], C.c_uint64),
+                           hist_capacity=hist_capacity, hist_size=abi.ptr(res["hist_size"], C.c_uint32),
+                           no_pos_hash_pr=abi.ptr(res["no_pos_hash_pr"], C.c_double))
+        return p, out, res
+
+    def error_count_batch(self, sids, n_read_files=None, n_quality=None, do_coverage=True, do_errors=True,
+                          preprocess=False, unmatched_end_minimum_read_length=50, unmatched_end_length_factor=0.1,
+                          hist_capacity=8192):
+        """Pass 1 over several resident samples in one launch; one result dict per sample."""
+        sids = list(sids)
+        n = len(sids)
+        jobs = [self._ec_job(sid, n_read_files, n_quality, do_coverage, do_errors, preprocess,
+                             unmatched_end_minimum_read_length, unmatched_end_length_factor, hist_capacity)
+                for sid in sids]
+        ids = (C.c_int32 * n)(*sids)
+        ps = (abi.EcParams * n)(*[j[0] for j in jobs])
+        outs = (abi.EcResult * n)(*[j[1] for j in jobs])
+        self._check(self.L.bsq_error_count_batch(self.ctx, n, ids, ps, outs))
+        return [j[2] for j in jobs]
+
+    def error_count(self, sid: int, **kw):
+        return self.error_count_batch([sid], **kw)[0]
 
     def counts_to_log10_prob(self, counts, R, Q):
         out = np.zeros(R * 25 * Q, dtype=np.float64)
@@ -111,29 +148,12 @@ class Scorer:
         return out
 
     # ------------------------------------------------------------------ pass 2
-    def identify_mutations(self, sid: int, log10_table, settings: ImSettings | None = None,
-                           deletion_propagation_cutoff=None, deletion_seed_cutoff=None,
-                           precision=PRECISION_FP32C, positions=False, n_read_files=None, n_quality=None):
+    def _im_job(self, sid, log10_table, st, deletion_propagation_cutoff, deletion_seed_cutoff, precision, positions,
+                n_read_files, n_quality):
         s = self.sample(sid)
-        st = settings or ImSettings()
-        poly, places = st.resolved()
-        T = len(s.target_offset) - 1
-        prop = np.broadcast_to(np.asarray(5.0 if deletion_propagation_cutoff is None else deletion_propagation_cutoff,
-                                          dtype=np.float64), (T,)).copy()
-        seed = np.broadcast_to(np.asarray(0.0 if deletion_seed_cutoff is None else deletion_seed_cutoff,
-                                          dtype=np.float64), (T,)).copy()
-        tab = np.ascontiguousarray(log10_table, dtype=np.float64)
-        p = abi.ImParams(n_read_files=n_read_files or s.n_read_files, n_quality=n_quality or s.n_quality,
-                         base_quality_cutoff=st.base_quality_cutoff,
-                         mutation_cutoff=st.mutation_log10_e_value_cutoff, polymorphism_cutoff=poly,
-                         polymorphism_precision_decimal=st.polymorphism_precision_decimal,
-                         polymorphism_precision_places=places,
-                         skip_missing_coverage_prediction=int(st.skip_missing_coverage_prediction),
-                         log10_ref_length=float(np.log10(float(s.target_offset[-1]))),
-                         deletion_propagation_cutoff=abi.ptr(prop, C.c_double),
-                         deletion_seed_cutoff=abi.ptr(seed, C.c_double), precision=precision)
-        arrs = None
-        pa = None
+        p, keep = im_params(s, st, deletion_propagation_cutoff, deletion_seed_cutoff, precision, n_read_files, n_quality)
+        keep["tab"] = np.ascontiguousarray(log10_table, dtype=np.float64)
+        arrs = pa = None
         if positions:
             n = int(s.target_offset[-1])
             arrs = dict(unique_top=np.zeros(n, np.uint32), unique_bot=np.zeros(n, np.uint32),
@@ -145,20 +165,48 @@ class Scorer:
                       raw_redundant_top=C.c_uint32, raw_redundant_bot=C.c_uint32, consensus_score=C.c_double,
                       best_base=C.c_uint8, n_scored=C.c_uint32)
             pa = abi.PositionArrays(**{k: abi.ptr(v, cm[k]) for k, v in arrs.items()})
-        self._check(self.L.bsq_identify_mutations(self.ctx, sid, C.byref(p), abi.ptr(tab, C.c_double),
-                                                  C.byref(pa) if pa is not None else None))
-        n_ra, n_mc, n_un = C.c_uint64(), C.c_uint64(), C.c_uint64()
-        self._check(self.L.bsq_im_result_counts(self.ctx, C.byref(n_ra), C.byref(n_mc), C.byref(n_un)))
-        ra = (abi.RaRecord * max(1, n_ra.value))()
-        mc = (abi.McRecord * max(1, n_mc.value))()
-        un = (abi.UnRecord * max(1, n_un.value))()
-        self._check(self.L.bsq_im_result_copy(self.ctx, C.cast(ra, C.c_void_p), n_ra.value, C.cast(mc, C.c_void_p),
-                                              n_mc.value, C.cast(un, C.c_void_p), n_un.value))
-        out = dict(ra=abi.ra_to_dicts(ra[:n_ra.value]), mc=abi.mc_to_dicts(mc[:n_mc.value]),
-                   un=abi.un_to_dicts(un[:n_un.value]))
-        if arrs is not None:
-            out["positions"] = arrs
-        return out
+        return p, pa, arrs, keep
+
+    def identify_mutations_batch(self, sids, log10_tables, settings: ImSettings | None = None,
+                                 deletion_propagation_cutoff=None, deletion_seed_cutoff=None,
+                                 precision=PRECISION_FP32C, positions=False, n_read_files=None, n_quality=None):
+        """Pass 2 over several resident samples in one launch per kernel.  `log10_tables`, `settings`
+        and the deletion cutoffs are per sample (a list) or shared (one value)."""
+        sids = list(sids)
+        n = len(sids)
+
+        def per(x, j):
+            return x[j] if isinstance(x, (list, tuple)) else x
+
+        jobs = [self._im_job(sid, per(log10_tables, j), per(settings, j) or ImSettings(), per(deletion_propagation_cutoff, j),
+                             per(deletion_seed_cutoff, j), precision, positions, n_read_files, n_quality)
+                for j, sid in enumerate(sids)]
+        ids = (C.c_int32 * n)(*sids)
+        ps = (abi.ImParams * n)(*[j[0] for j in jobs])
+        tabs = (C.POINTER(C.c_double) * n)(*[abi.ptr(j[3]["tab"], C.c_double) for j in jobs])
+        pas = None
+        if positions:
+            pas = (C.POINTER(abi.PositionArrays) * n)(*[C.pointer(j[1]) for j in jobs])
+        self._check(self.L.bsq_identify_mutations_batch(self.ctx, n, ids, ps, tabs, pas))
+        outs = []
+        for j in range(n):
+            n_ra, n_mc, n_un = C.c_uint64(), C.c_uint64(), C.c_uint64()
+            self._check(self.L.bsq_im_batch_result_counts(self.ctx, j, C.byref(n_ra), C.byref(n_mc), C.byref(n_un)))
+            ra = (abi.RaRecord * max(1, n_ra.value))()
+            mc = (abi.McRecord * max(1, n_mc.value))()
+            un = (abi.UnRecord * max(1, n_un.value))()
+            self._check(self.L.bsq_im_batch_result_copy(self.ctx, j, C.cast(ra, C.c_void_p), n_ra.value,
+                                                        C.cast(mc, C.c_void_p), n_mc.value, C.cast(un, C.c_void_p),
+                                                        n_un.value))
+            out = dict(ra=abi.ra_to_dicts(ra[:n_ra.value]), mc=abi.mc_to_dicts(mc[:n_mc.value]),
+                       un=abi.un_to_dicts(un[:n_un.value]))
+            if jobs[j][2] is not None:
+                out["positions"] = jobs[j][2]
+            outs.append(out)
+        return outs
+
+    def identify_mutations(self, sid: int, log10_table, settings: ImSettings | None = None, **kw):
+        return self.identify_mutations_batch([sid], [log10_table], settings, **kw)[0]
 
     def timer_start(self):
         self._check(self.L.bsq_timer_start(self.ctx))
@@ -186,3 +234,96 @@ def identify_mutations(sample, log10_table, device=0, **kw):
     with Scorer(device) as sc:
         sid = sc.load_sample(sample)
         return sc.identify_mutations(sid, log10_table, **kw)
+
+
+class Server:
+    """Continuous-batching scoring server (bsq_server_*): jobs are admitted by HBM footprint,
+    uploaded while earlier jobs run, and every GPU round runs both passes over all resident jobs as
+    one batch per pass.  A job is one sample through error_count, the error-table round trip and
+    identify_mutations."""
+
+    def __init__(self, device: int = 0, hbm_budget: float = 150e9, max_batch_jobs: int = 64,
+                 precision: int = PRECISION_FP32C):
+        self.L = _lib.load()
+        self.srv = C.c_void_p()
+        rc = self.L.bsq_server_create(C.byref(self.srv), device, int(hbm_budget), max_batch_jobs, precision)
+        if rc != 0:
+            raise _lib.BsqError(rc, "bsq_server_create failed")
+        self._jobs = {}
+
+    def submit(self, sample, settings: ImSettings | None = None, deletion_propagation_cutoff=None,
+               deletion_seed_cutoff=None, hist_capacity=8192, n_read_files=None, n_quality=None,
+               view=None) -> int:
+        """Queue one job; `sample` (or the prepared abi.SampleView `view`) stays referenced until
+        the job is released."""
+        view = view or abi.SampleView(sample)
+        R = n_read_files or sample.n_read_files
+        Q = n_quality or sample.n_quality
+        ec = abi.EcParams(n_read_files=R, n_quality=Q, do_coverage=1, do_errors=1, preprocess_stage=0,
+                          unmatched_end_minimum_read_length=50, unmatched_end_length_factor=0.1)
+        im, keep = im_params(sample, settings or ImSettings(), deletion_propagation_cutoff, deletion_seed_cutoff,
+                             PRECISION_FP32C, R, Q)
+        job = abi.Job(ref=C.pointer(view.ref), reads=C.pointer(view.reads), ec=ec, im=im, hist_capacity=hist_capacity)
+        jid = C.c_uint64()
+        rc = self.L.bsq_server_submit(self.srv, C.byref(job), C.byref(jid))
+        if rc != 0:
+            raise _lib.BsqError(rc, self.L.bsq_server_last_error(self.srv).decode())
+        self._jobs[jid.value] = (sample, view, keep, job, R, Q, hist_capacity)
+        return jid.value
+
+    @staticmethod
+    def _info(i: abi.JobInfo) -> dict:
+        return {k: getattr(i, k) for k, _ in abi.JobInfo._fields_}
+
+    def wait(self, jid: int, timeout_ms: int = -1) -> dict:
+        info = abi.JobInfo()
+        rc = self.L.bsq_server_wait(self.srv, jid, timeout_ms, C.byref(info))
+        if rc != 0:
+            raise _lib.BsqError(rc, "wait failed")
+        d = self._info(info)
+        if d["state"] < 0:
+            raise _lib.BsqError(d["state"], self.L.bsq_server_job_error(self.srv, jid).decode())
+        return d
+
+    def result(self, jid: int) -> dict:
+        """Pass-1 and pass-2 results of a finished job (waits for it)."""
+        info = self.wait(jid)
+        sample, _, _, _, R, Q, cap = self._jobs[jid]
+        G = sample.n_coverage_groups
+        counts = np.zeros(R * 25 * Q, dtype=np.uint64)
+        hist = np.zeros((G, cap), dtype=np.uint64)
+        hsize = np.zeros(G, dtype=np.uint32)
+        rc = self.L.bsq_server_error_counts(self.srv, jid, abi.ptr(counts, C.c_uint64), abi.ptr(hist, C.c_uint64),
+                                            abi.ptr(hsize, C.c_uint32))
+        if rc != 0:
+            raise _lib.BsqError(rc, "error counts unavailable")
+        ra = (abi.RaRecord * max(1, info["n_ra"]))()
+        mc = (abi.McRecord * max(1, info["n_mc"]))()
+        un = (abi.UnRecord * max(1, info["n_un"]))()
+        rc = self.L.bsq_server_results(self.srv, jid, C.cast(ra, C.c_void_p), info["n_ra"], C.cast(mc, C.c_void_p),
+                                       info["n_mc"], C.cast(un, C.c_void_p), info["n_un"])
+        if rc != 0:
+            raise _lib.BsqError(rc, "results unavailable")
+        return dict(counts=counts, hist=hist, hist_size=hsize, ra=abi.ra_to_dicts(ra[:info["n_ra"]]),
+                    mc=abi.mc_to_dicts(mc[:info["n_mc"]]), un=abi.un_to_dicts(un[:info["n_un"]]), info=info)
+
+    def release(self, jid: int):
+        self.L.bsq_server_release(self.srv, jid)
+        self._jobs.pop(jid, None)
+
+    def stats(self) -> dict:
+        st = abi.ServerStats()
+        self.L.bsq_server_get_stats(self.srv, C.byref(st))
+        return {k: getattr(st, k) for k, _ in abi.ServerStats._fields_}
+
+    def close(self):
+        if self.srv:
+            self.L.bsq_server_destroy(self.srv)
+            self.srv = C.c_void_p()
+            self._jobs.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

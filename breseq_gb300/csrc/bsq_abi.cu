@@ -10,6 +10,7 @@
 #include <limits>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -57,30 +58,41 @@ struct SampleDev {
   std::vector<uint8_t> mapq_values; // distinct MAPQ values, index = mapq_idx
 };
 
+// Per-job device buffers of pass 1 and pass 2, kept across calls (pool-backed).
+struct EcBufs { DevMem counts, hist, found, diff_u, diff_r, qs_flag, blk_u, blk_r, err; };
+struct ImBufs { DevMem lp64, r64, lpmax64, lp32, prop, seed, failed, err; };
+
 }  // namespace
 
 struct bsq_ctx {
   int device = 0;
   int sms = 1;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;        // the passes
+  cudaStream_t load_stream = nullptr;   // sample uploads: a loader thread runs them beside the passes
+  std::mutex mu;                        // guards `samples` and `next_id`
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm0 = nullptr, evm1 = nullptr, evt0 = nullptr, evt1 = nullptr;
-  std::string err;
   std::map<int32_t, std::unique_ptr<SampleDev>> samples;
   int32_t next_id = 1;
   // working memory reused across calls
-  DevMem cov, call, blk, total, cand, next, ra, n_ra, qhist, scratch, errw, lp64, r64, lpmax64, lp32, stats;
-  DevMem keep, kcol, kcov, kcall, d_prop, d_seed;
-  DevMem counts, hist, found, diff_u, diff_r, qs_flag, blk_u, blk_r;
-  std::vector<bsq_ra_record> res_ra;
-  std::vector<bsq_mc_record> res_mc;
-  std::vector<bsq_un_record> res_un;
+  DevMem cov, call, blk, total, cand, next, ra, n_ra, qhist, scratch, errw, stats;
+  DevMem keep, kcol, kcov, kcall;
+  DevMem d_chunks;
+  std::vector<std::unique_ptr<EcBufs>> ecb;
+  std::vector<std::unique_ptr<ImBufs>> imb;
+  std::vector<std::vector<bsq_ra_record>> res_ra;
+  std::vector<std::vector<bsq_mc_record>> res_mc;
+  std::vector<std::vector<bsq_un_record>> res_un;
   double last_ms = 0, main_ms = 0;
   uint32_t launches = 0;
   uint64_t last_candidates = 0;
 };
 
-static int fail(bsq_ctx* c, int code, const std::string& msg) {
-  if (c) c->err = msg;
+// The message of the last failed call, per calling thread: a loader thread and the pass thread can
+// share one context without overwriting each other's message.
+static thread_local std::string t_err;
+
+static int fail(bsq_ctx*, int code, const std::string& msg) {
+  t_err = msg;
   return code;
 }
 #define CK(call)                                                                                          \
@@ -134,6 +146,7 @@ static DevSample make_dev_sample(const SampleDev& s) {
 }
 
 static SampleDev* find_sample(bsq_ctx* ctx, int32_t id) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
   auto it = ctx->samples.find(id);
   return it == ctx->samples.end() ? nullptr : it->second.get();
 }
@@ -155,6 +168,7 @@ int bsq_create(bsq_ctx** out, int device) {
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return BSQ_ERR_CUDA;
   c->sms = prop.multiProcessorCount;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return BSQ_ERR_CUDA;
+  if (cudaStreamCreateWithFlags(&c->load_stream, cudaStreamNonBlocking) != cudaSuccess) return BSQ_ERR_CUDA;
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
     uint64_t keep = UINT64_MAX;   // keep freed blocks in this process's pool for the next sample
@@ -172,22 +186,25 @@ void bsq_destroy(bsq_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->load_stream) cudaStreamSynchronize(ctx->load_stream);
   ctx->samples.clear();
   // pool blocks are returned on the context's stream, so before it goes
   for (DevMem* m : {&ctx->cov, &ctx->call, &ctx->blk, &ctx->total, &ctx->cand, &ctx->next, &ctx->ra, &ctx->n_ra,
-                    &ctx->qhist, &ctx->scratch, &ctx->errw, &ctx->lp64, &ctx->r64, &ctx->lpmax64, &ctx->lp32,
-                    &ctx->stats, &ctx->counts, &ctx->hist, &ctx->found, &ctx->diff_u, &ctx->diff_r, &ctx->qs_flag,
-                    &ctx->blk_u, &ctx->blk_r, &ctx->keep, &ctx->kcol, &ctx->kcov,
-                    &ctx->kcall, &ctx->d_prop, &ctx->d_seed})
+                    &ctx->qhist, &ctx->scratch, &ctx->errw, &ctx->stats, &ctx->keep, &ctx->kcol, &ctx->kcov, &ctx->kcall,
+                    &ctx->d_chunks})
     m->release();
+  ctx->ecb.clear();
+  ctx->imb.clear();
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   cudaEventDestroy(ctx->ev0); cudaEventDestroy(ctx->ev1); cudaEventDestroy(ctx->evm0); cudaEventDestroy(ctx->evm1);
   cudaEventDestroy(ctx->evt0); cudaEventDestroy(ctx->evt1);
+  if (ctx->load_stream) cudaStreamSynchronize(ctx->load_stream);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->load_stream) cudaStreamDestroy(ctx->load_stream);
   delete ctx;
 }
 
-const char* bsq_last_error(const bsq_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+const char* bsq_last_error(const bsq_ctx* ctx) { return ctx ? t_err.c_str() : "null context"; }
 
 uint64_t bsq_sample_footprint(const bsq_reference* ref, const bsq_read_soa* rd) {
   if (!ref || !rd) return 0;
@@ -238,7 +255,7 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
     if (ch != 'A' && ch != 'C' && ch != 'G' && ch != 'T' && ch != 'N')
       return fail(ctx, BSQ_ERR_DATA, "reference base outside A/C/G/T/N");
   }
-  cudaStream_t st = ctx->stream;
+  cudaStream_t st = ctx->load_stream;
   // reference, one '\0' separator after each target
   CK(s->ref.alloc(s->n_cols + 64, st));
   CK(cudaMemsetAsync(s->ref.p, 0, s->n_cols + 64, st));
@@ -273,9 +290,10 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   CK(s->reads.alloc(n * sizeof(DevRead) + 64, st));
   CK(s->qb.alloc(n * sizeof(QBounds) + 64, st));
   CK(s->rstart.alloc(n * 4 + 64, st));
-  CK(ctx->stats.alloc(64, st));
-  CK(cudaMemsetAsync(ctx->stats.p, 0, 64, st));
-  uint32_t* stats = ctx->stats.as<uint32_t>();  // [0] err, [1] maxspan, [2..9] mapq mask, [10] max tile reads
+  DevMem dstats;
+  CK(dstats.alloc(64, st));
+  CK(cudaMemsetAsync(dstats.p, 0, 64, st));
+  uint32_t* stats = dstats.as<uint32_t>();  // [0] err, [1] maxspan, [2..9] mapq mask, [10] max tile reads
   RawSoA in;
   in.tid = tid.as<int32_t>(); in.pos = pos.as<int32_t>(); in.flag = flag.as<uint16_t>(); in.mapq = s->mapq.as<uint8_t>();
   in.x1 = s->x1.as<uint32_t>(); in.xl = xl.as<int32_t>(); in.xr = xr.as<int32_t>(); in.read_file = rfile.as<uint8_t>();
@@ -307,6 +325,7 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   CK(cudaMemcpyAsync(h + 10, stats + 10, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   s->max_tile_reads = h[10];
+  std::lock_guard<std::mutex> lk(ctx->mu);
   const int32_t id = ctx->next_id++;
   ctx->samples[id] = std::move(s);
   *sample_id = id;
@@ -315,96 +334,155 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
 
 int bsq_free_sample(bsq_ctx* ctx, int32_t id) {
   if (!ctx) return BSQ_ERR_INVALID;
-  auto it = ctx->samples.find(id);
-  if (it == ctx->samples.end()) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
+  std::unique_ptr<SampleDev> victim;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->samples.find(id);
+    if (it == ctx->samples.end()) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
+    victim = std::move(it->second);
+    ctx->samples.erase(it);
+  }
   cudaSetDevice(ctx->device);
-  cudaStreamSynchronize(ctx->stream);
-  ctx->samples.erase(it);
+  cudaStreamSynchronize(ctx->stream);   // no pass still reads it; its blocks go back on the load stream
+  victim.reset();
   return BSQ_OK;
 }
 
 // ============================================================================ pass 1
-int bsq_error_count(bsq_ctx* ctx, int32_t sid, const bsq_ec_params* p, bsq_ec_result* out) {
-  if (!ctx || !p || !out) return fail(ctx, BSQ_ERR_INVALID, "null argument");
-  SampleDev* s = find_sample(ctx, sid);
-  if (!s) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
-  if (p->n_read_files == 0 || p->n_read_files > 255 || p->n_quality == 0 || p->n_quality > 256)
-    return fail(ctx, BSQ_ERR_INVALID, "covariate dimensions out of range");
+static constexpr uint32_t kReadChunk = 1024;   // reads per pass-1 work unit
+
+// One group of at most kBatchJobs samples: one launch per kernel of pass 1.
+static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_params* P, bsq_ec_result* out) {
+  std::vector<SampleDev*> smp(n);
+  for (uint32_t j = 0; j < n; j++) {
+    smp[j] = find_sample(ctx, ids[j]);
+    if (!smp[j]) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
+    if (P[j].n_read_files == 0 || P[j].n_read_files > 255 || P[j].n_quality == 0 || P[j].n_quality > 256)
+      return fail(ctx, BSQ_ERR_INVALID, "covariate dimensions out of range");
+  }
   CK(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
-  const uint32_t R = p->n_read_files, Q = p->n_quality, G = s->n_groups;
-  const size_t nbins = (size_t)R * 25 * Q;
-  const uint32_t cap = s->max_tile_reads + 2;
-  CK(ctx->counts.alloc(nbins * 8, st));
-  CK(ctx->hist.alloc((size_t)G * cap * 8, st));
-  CK(ctx->found.alloc((size_t)s->n_targets * 16 + 16, st));
-  CK(ctx->errw.alloc(16, st));
-  CK(cudaMemsetAsync(ctx->counts.p, 0, nbins * 8, st));
-  CK(cudaMemsetAsync(ctx->hist.p, 0, (size_t)G * cap * 8, st));
-  CK(cudaMemsetAsync(ctx->found.p, 0, (size_t)s->n_targets * 16 + 16, st));
-  CK(cudaMemsetAsync(ctx->errw.p, 0, 16, st));
-  const uint32_t ncb = (s->n_cols + 1023) / 1024;
-  CK(ctx->diff_u.alloc((size_t)(s->n_cols + 16) * 4, st));
-  CK(ctx->diff_r.alloc((size_t)(s->n_cols + 16) * 4, st));
-  CK(ctx->qs_flag.alloc((size_t)2 * s->n_cols + 16, st));
-  CK(ctx->blk_u.alloc((size_t)(ncb + 16) * 4, st));
-  CK(ctx->blk_r.alloc((size_t)(ncb + 16) * 4, st));
-  CK(cudaMemsetAsync(ctx->diff_u.p, 0, (size_t)(s->n_cols + 16) * 4, st));
-  CK(cudaMemsetAsync(ctx->diff_r.p, 0, (size_t)(s->n_cols + 16) * 4, st));
-  if (p->preprocess_stage) CK(cudaMemsetAsync(ctx->qs_flag.p, 0, (size_t)2 * s->n_cols + 16, st));
-  DevSample S = make_dev_sample(*s);
-  EcArgs A;
-  A.diff_u = ctx->diff_u.as<int32_t>(); A.diff_r = ctx->diff_r.as<int32_t>(); A.qs_flag = ctx->qs_flag.as<uint8_t>();
-  A.blk_u = ctx->blk_u.as<uint32_t>(); A.blk_r = ctx->blk_r.as<uint32_t>();
-  A.counts = ctx->counts.as<unsigned long long>();
-  A.cov_hist = ctx->hist.as<unsigned long long>();
-  A.found = ctx->found.as<unsigned long long>();
-  A.err = ctx->errw.as<uint32_t>();
-  A.R = R; A.Q = Q; A.hist_cap = cap;
-  A.do_errors = p->do_errors; A.preprocess = p->preprocess_stage;
-  A.unmatched_min_len = p->unmatched_end_minimum_read_length;
-  A.unmatched_factor = (float)p->unmatched_end_length_factor;
-  A.unmatched_factor_d = p->unmatched_end_length_factor;
-  const uint64_t per_tile = 64ull * std::max<uint32_t>(1, s->max_tile_reads) * 8;
-  A.flush_tiles = (uint32_t)std::max<uint64_t>(1, (1ull << 31) / per_tile);
+  while (ctx->ecb.size() < n) ctx->ecb.emplace_back(new EcBufs());
+  std::vector<DevJob> jobs(n);
+  std::vector<uint32_t> cblk(n + 1, 0);
+  std::vector<uint4> chunks;
+  uint32_t max_bins = 0;
+  for (uint32_t j = 0; j < n; j++) {
+    SampleDev* s = smp[j];
+    EcBufs& E = *ctx->ecb[j];
+    const uint32_t R = P[j].n_read_files, Q = P[j].n_quality, G = s->n_groups;
+    const size_t nbins = (size_t)R * 25 * Q;
+    const uint32_t cap = s->max_tile_reads + 2;
+    const uint32_t ncb = (s->n_cols + 1023) / 1024;
+    max_bins = std::max<uint32_t>(max_bins, (uint32_t)nbins);
+    CK(E.counts.alloc(nbins * 8, st));
+    CK(E.hist.alloc((size_t)G * cap * 8, st));
+    CK(E.found.alloc((size_t)s->n_targets * 16 + 16, st));
+    CK(E.err.alloc(16, st));
+    CK(E.diff_u.alloc((size_t)(s->n_cols + 16) * 4, st));
+    CK(E.diff_r.alloc((size_t)(s->n_cols + 16) * 4, st));
+    CK(E.qs_flag.alloc((size_t)2 * s->n_cols + 16, st));
+    CK(E.blk_u.alloc((size_t)(ncb + 16) * 4, st));
+    CK(E.blk_r.alloc((size_t)(ncb + 16) * 4, st));
+    CK(cudaMemsetAsync(E.counts.p, 0, nbins * 8, st));
+    CK(cudaMemsetAsync(E.hist.p, 0, (size_t)G * cap * 8, st));
+    CK(cudaMemsetAsync(E.found.p, 0, (size_t)s->n_targets * 16 + 16, st));
+    CK(cudaMemsetAsync(E.err.p, 0, 16, st));
+    CK(cudaMemsetAsync(E.diff_u.p, 0, (size_t)(s->n_cols + 16) * 4, st));
+    CK(cudaMemsetAsync(E.diff_r.p, 0, (size_t)(s->n_cols + 16) * 4, st));
+    if (P[j].preprocess_stage) CK(cudaMemsetAsync(E.qs_flag.p, 0, (size_t)2 * s->n_cols + 16, st));
+    DevJob& J = jobs[j];
+    memset(&J, 0, sizeof J);
+    J.S = make_dev_sample(*s);
+    EcArgs& A = J.E;
+    A.counts = E.counts.as<unsigned long long>(); A.cov_hist = E.hist.as<unsigned long long>();
+    A.found = E.found.as<unsigned long long>(); A.err = E.err.as<uint32_t>();
+    A.R = R; A.Q = Q; A.hist_cap = cap;
+    A.do_errors = P[j].do_errors; A.preprocess = P[j].preprocess_stage;
+    A.unmatched_min_len = P[j].unmatched_end_minimum_read_length;
+    A.unmatched_factor = (float)P[j].unmatched_end_length_factor;
+    A.unmatched_factor_d = P[j].unmatched_end_length_factor;
+    A.flush_tiles = 1;
+    A.diff_u = E.diff_u.as<int32_t>(); A.diff_r = E.diff_r.as<int32_t>(); A.qs_flag = E.qs_flag.as<uint8_t>();
+    A.blk_u = E.blk_u.as<uint32_t>(); A.blk_r = E.blk_r.as<uint32_t>();
+    cblk[j + 1] = cblk[j] + ncb;
+    for (uint32_t r0 = 0; r0 < s->n_reads; r0 += kReadChunk)
+      chunks.push_back(make_uint4(j, r0, std::min<uint32_t>(s->n_reads, r0 + kReadChunk), 0));
+  }
+  CK(upload(ctx->d_chunks, chunks.data(), chunks.size(), st));
+  CK(ctx->next.alloc(16, st));
+  std::unique_ptr<Batch> Bp(new Batch());
+  Batch& B = *Bp;
+  memset(&B, 0, sizeof B);
+  B.n_jobs = n;
+  B.total_cblk = cblk[n];
+  for (uint32_t j = 0; j < n; j++) B.jobs[j] = jobs[j];
+  for (uint32_t j = 0; j <= n; j++) B.cblk_begin[j] = cblk[j];
   CK(cudaEventRecord(ctx->ev0, st));
-  CK(launch_ec(S, A, ctx->sms, st, ctx->evm0, ctx->evm1));
-  std::vector<unsigned long long> counts(nbins), hist((size_t)G * cap), found((size_t)s->n_targets * 2);
-  uint32_t err = 0;
-  CK(cudaMemcpyAsync(counts.data(), ctx->counts.p, nbins * 8, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(hist.data(), ctx->hist.p, (size_t)G * cap * 8, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(found.data(), ctx->found.p, found.size() * 8, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(&err, ctx->errw.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(launch_ec(B, ctx->d_chunks.as<uint4>(), (uint32_t)chunks.size(), ctx->next.as<unsigned int>(), max_bins, ctx->sms, st,
+               ctx->evm0, ctx->evm1));
+  std::vector<std::vector<unsigned long long>> counts(n), hist(n), found(n);
+  std::vector<uint32_t> err(n, 0);
+  for (uint32_t j = 0; j < n; j++) {
+    EcBufs& E = *ctx->ecb[j];
+    counts[j].resize((size_t)P[j].n_read_files * 25 * P[j].n_quality);
+    hist[j].resize((size_t)smp[j]->n_groups * (smp[j]->max_tile_reads + 2));
+    found[j].resize((size_t)smp[j]->n_targets * 2);
+    CK(cudaMemcpyAsync(counts[j].data(), E.counts.p, counts[j].size() * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hist[j].data(), E.hist.p, hist[j].size() * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(found[j].data(), E.found.p, found[j].size() * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&err[j], E.err.p, 4, cudaMemcpyDeviceToHost, st));
+  }
   CK(cudaEventRecord(ctx->ev1, st));
   CK(cudaStreamSynchronize(st));
   float ms = 0, mms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   cudaEventElapsedTime(&mms, ctx->evm0, ctx->evm1);
-  ctx->last_ms = ms; ctx->main_ms = mms; ctx->launches = 5;
-  if (err) return fail(ctx, BSQ_ERR_DATA, "error_count: " + err_text(err));
-  if (out->counts) for (size_t i = 0; i < nbins; i++) out->counts[i] = p->do_errors ? counts[i] : 0;
+  ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 4;
   int rc = BSQ_OK;
-  for (uint32_t g = 0; g < G; g++) {
-    uint32_t size = 0;
-    for (uint32_t i = 0; i < cap; i++) if (hist[(size_t)g * cap + i]) size = i + 1;
-    if (!p->do_coverage) size = 0;
-    if (out->hist_size) out->hist_size[g] = size;
-    if (out->coverage_hist) {
-      for (uint32_t i = 0; i < out->hist_capacity; i++)
-        out->coverage_hist[(size_t)g * out->hist_capacity + i] = (i < size) ? hist[(size_t)g * cap + i] : 0;
-      if (size > out->hist_capacity) rc = BSQ_ERR_SIZE;
-    }
-  }
-  if (out->no_pos_hash_pr) {
-    for (uint32_t t = 0; t < s->n_targets; t++) out->no_pos_hash_pr[t] = 1.0;
-    if (p->preprocess_stage)
-      for (uint32_t t : s->order) {
-        const double tot = (double)(found[2 * t] + found[2 * t + 1]);
-        out->no_pos_hash_pr[t] = (tot != 0) ? (double)found[2 * t] / tot : 1.0;
+  for (uint32_t j = 0; j < n; j++) {
+    if (err[j]) return fail(ctx, BSQ_ERR_DATA, "error_count: " + err_text(err[j]));
+    SampleDev* s = smp[j];
+    bsq_ec_result* o = &out[j];
+    const size_t nbins = counts[j].size();
+    if (o->counts) for (size_t i = 0; i < nbins; i++) o->counts[i] = P[j].do_errors ? counts[j][i] : 0;
+    const uint32_t cap = s->max_tile_reads + 2;
+    for (uint32_t g = 0; g < s->n_groups; g++) {
+      uint32_t size = 0;
+      for (uint32_t i = 0; i < cap; i++) if (hist[j][(size_t)g * cap + i]) size = i + 1;
+      if (!P[j].do_coverage) size = 0;
+      if (o->hist_size) o->hist_size[g] = size;
+      if (o->coverage_hist) {
+        for (uint32_t i = 0; i < o->hist_capacity; i++)
+          o->coverage_hist[(size_t)g * o->hist_capacity + i] = (i < size) ? hist[j][(size_t)g * cap + i] : 0;
+        if (size > o->hist_capacity) rc = BSQ_ERR_SIZE;
       }
+    }
+    if (o->no_pos_hash_pr) {
+      for (uint32_t t = 0; t < s->n_targets; t++) o->no_pos_hash_pr[t] = 1.0;
+      if (P[j].preprocess_stage)
+        for (uint32_t t : s->order) {
+          const double tot = (double)(found[j][2 * t] + found[j][2 * t + 1]);
+          o->no_pos_hash_pr[t] = (tot != 0) ? (double)found[j][2 * t] / tot : 1.0;
+        }
+    }
   }
   if (rc == BSQ_ERR_SIZE) return fail(ctx, rc, "coverage histogram larger than hist_capacity; see hist_size");
   return BSQ_OK;
+}
+
+int bsq_error_count_batch(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_params* P, bsq_ec_result* out) {
+  if (!ctx || !ids || !P || !out || n == 0) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  ctx->last_ms = 0; ctx->main_ms = 0; ctx->launches = 0;
+  for (uint32_t g = 0; g < n; g += kBatchJobs) {
+    const int rc = ec_group(ctx, std::min(kBatchJobs, n - g), ids + g, P + g, out + g);
+    if (rc != BSQ_OK) return rc;
+  }
+  return BSQ_OK;
+}
+
+int bsq_error_count(bsq_ctx* ctx, int32_t sid, const bsq_ec_params* p, bsq_ec_result* out) {
+  return bsq_error_count_batch(ctx, 1, &sid, p, out);
 }
 
 int bsq_counts_to_log10_prob(const uint64_t* counts, uint32_t R, uint32_t Q, double* out) {
@@ -414,81 +492,111 @@ int bsq_counts_to_log10_prob(const uint64_t* counts, uint32_t R, uint32_t Q, dou
 }
 
 // ============================================================================ pass 2
-int bsq_identify_mutations(bsq_ctx* ctx, int32_t sid, const bsq_im_params* p, const double* table,
-                           bsq_position_arrays* pos_out) {
-  if (!ctx || !p || !table) return fail(ctx, BSQ_ERR_INVALID, "null argument");
-  SampleDev* s = find_sample(ctx, sid);
-  if (!s) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
-  if (!p->deletion_propagation_cutoff || !p->deletion_seed_cutoff) return fail(ctx, BSQ_ERR_INVALID, "missing deletion cutoffs");
-  if (p->n_read_files == 0 || p->n_read_files > 255 || p->n_quality == 0 || p->n_quality > 256)
-    return fail(ctx, BSQ_ERR_INVALID, "error table dimensions out of range");
+// One group of at most kBatchJobs samples; results go to res_*[job0 + j].
+static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_params* P,
+                    const double* const* tables, bsq_position_arrays* const* pos_out, uint32_t job0) {
+  std::vector<SampleDev*> smp(n);
+  for (uint32_t j = 0; j < n; j++) {
+    smp[j] = find_sample(ctx, ids[j]);
+    if (!smp[j]) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
+    if (!tables[j] || !P[j].deletion_propagation_cutoff || !P[j].deletion_seed_cutoff)
+      return fail(ctx, BSQ_ERR_INVALID, "missing error table or deletion cutoffs");
+    if (P[j].n_read_files == 0 || P[j].n_read_files > 255 || P[j].n_quality == 0 || P[j].n_quality > 256)
+      return fail(ctx, BSQ_ERR_INVALID, "error table dimensions out of range");
+    if (P[j].precision != P[0].precision) return fail(ctx, BSQ_ERR_INVALID, "one precision per batch");
+  }
   CK(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
-  ctx->res_ra.clear(); ctx->res_mc.clear(); ctx->res_un.clear();
-  // ---- likelihood classes, computed on the host exactly as fill_read_base_likelihoods does
-  host::ClassTableHost ct;
-  host::build_class_table(table, p->n_read_files, p->n_quality, s->mapq_values, ct);
-  CK(upload(ctx->lp64, ct.lp64.data(), ct.lp64.size(), st));
-  CK(upload(ctx->r64, ct.r64.data(), ct.r64.size(), st));
-  CK(upload(ctx->lpmax64, ct.lpmax64.data(), ct.lpmax64.size(), st));
-  CK(upload(ctx->lp32, ct.lp32.data(), ct.lp32.size(), st));
-  ClassTable T;
-  T.lp64 = ctx->lp64.as<double>(); T.r64 = ctx->r64.as<double>(); T.lpmax64 = ctx->lpmax64.as<double>();
-  T.lp32 = ctx->lp32.as<float>(); T.K = ct.K; T.R = p->n_read_files; T.Q = p->n_quality;
-  T.n_mapq = (uint32_t)s->mapq_values.size();
-  std::vector<uint8_t> failed(s->n_targets);
-  for (uint32_t t = 0; t < s->n_targets; t++) failed[t] = p->deletion_propagation_cutoff[t] < 0.0;
-  CK(cudaMemcpyAsync(s->tgt_failed.p, failed.data(), s->n_targets, cudaMemcpyHostToDevice, st));
-  const uint32_t ncol = s->n_cols;
-  CK(ctx->cov.alloc((size_t)ncol * sizeof(ColCov), st));
-  CK(ctx->call.alloc((size_t)ncol * sizeof(ColCall), st));
-  const uint32_t nblk = (ncol + 255) / 256;
+  while (ctx->imb.size() < n) ctx->imb.emplace_back(new ImBufs());
+  std::vector<DevJob> jobs(n);
+  std::vector<uint32_t> tile_b(n + 1, 0), col_b(n + 1, 0);
+  uint32_t max_K = 0, per_warp = 32, Qh = 0;
+  for (uint32_t j = 0; j < n; j++) {
+    SampleDev* s = smp[j];
+    ImBufs& I = *ctx->imb[j];
+    // likelihood classes, computed on the host exactly as fill_read_base_likelihoods does
+    host::ClassTableHost ct;
+    host::build_class_table(tables[j], P[j].n_read_files, P[j].n_quality, s->mapq_values, ct);
+    CK(upload(I.lp64, ct.lp64.data(), ct.lp64.size(), st));
+    CK(upload(I.r64, ct.r64.data(), ct.r64.size(), st));
+    CK(upload(I.lpmax64, ct.lpmax64.data(), ct.lpmax64.size(), st));
+    CK(upload(I.lp32, ct.lp32.data(), ct.lp32.size(), st));
+    CK(upload(I.prop, P[j].deletion_propagation_cutoff, s->n_targets, st));
+    CK(upload(I.seed, P[j].deletion_seed_cutoff, s->n_targets, st));
+    CK(I.err.alloc(16, st));
+    CK(cudaMemsetAsync(I.err.p, 0, 16, st));
+    // per job, not per sample: one sample may sit in a batch twice with different cutoffs
+    std::vector<uint8_t> failed(s->n_targets);
+    for (uint32_t t = 0; t < s->n_targets; t++) failed[t] = P[j].deletion_propagation_cutoff[t] < 0.0;
+    CK(upload(I.failed, failed.data(), s->n_targets, st));
+    DevJob& J = jobs[j];
+    memset(&J, 0, sizeof J);
+    J.S = make_dev_sample(*s);
+    J.S.tgt_failed = I.failed.as<uint8_t>();
+    J.T.lp64 = I.lp64.as<double>(); J.T.r64 = I.r64.as<double>(); J.T.lpmax64 = I.lpmax64.as<double>();
+    J.T.lp32 = I.lp32.as<float>(); J.T.K = ct.K; J.T.R = P[j].n_read_files; J.T.Q = P[j].n_quality;
+    J.T.n_mapq = (uint32_t)s->mapq_values.size();
+    J.prop = I.prop.as<double>(); J.seed = I.seed.as<double>();
+    J.col_begin = col_b[j]; J.tile_begin = tile_b[j];
+    col_b[j + 1] = col_b[j] + s->n_cols;
+    tile_b[j + 1] = tile_b[j] + s->n_tiles;
+    max_K = std::max(max_K, ct.K);
+    per_warp = std::max<uint32_t>(per_warp, s->max_tile_reads);
+    Qh = std::max(Qh, P[j].n_quality);
+  }
+  const uint32_t total_cols = col_b[n];
+  CK(ctx->cov.alloc((size_t)total_cols * sizeof(ColCov), st));
+  CK(ctx->call.alloc((size_t)total_cols * sizeof(ColCall), st));
+  for (uint32_t j = 0; j < n; j++) {
+    ImArgs& A = jobs[j].I;
+    A.cov = ctx->cov.as<ColCov>() + col_b[j]; A.call = ctx->call.as<ColCall>() + col_b[j];
+    A.err = ctx->imb[j]->err.as<uint32_t>();
+    A.base_quality_cutoff = P[j].base_quality_cutoff;
+    A.precision = P[j].precision;
+    A.log10_ref_len = P[j].log10_ref_length;
+    A.mutation_cutoff = P[j].mutation_cutoff;
+    A.poly_cutoff = P[j].polymorphism_cutoff;
+    A.screen_margin = 1.0f;
+    A.guard = 2e-6f;
+    A.precision_decimal = P[j].polymorphism_precision_decimal;
+  }
+  std::unique_ptr<Batch> Bp(new Batch());
+  Batch& B = *Bp;
+  memset(&B, 0, sizeof B);
+  B.n_jobs = n;
+  B.total_tiles = tile_b[n]; B.total_cols = total_cols;
+  for (uint32_t j = 0; j < n; j++) B.jobs[j] = jobs[j];
+  for (uint32_t j = 0; j <= n; j++) { B.tile_begin[j] = tile_b[j]; B.col_begin[j] = col_b[j]; }
+  const uint32_t nblk = (total_cols + 255) / 256;
   CK(ctx->blk.alloc((size_t)nblk * 4 + 16, st));
   CK(ctx->total.alloc(16, st));
-  CK(ctx->cand.alloc((size_t)ncol * 4 + 16, st));
+  CK(ctx->cand.alloc((size_t)total_cols * 4 + 16, st));
   CK(ctx->next.alloc(16, st));
   CK(ctx->n_ra.alloc(16, st));
   CK(ctx->errw.alloc(16, st));
   CK(cudaMemsetAsync(ctx->errw.p, 0, 16, st));
-  DevSample S = make_dev_sample(*s);
-  ImArgs A;
-  A.cov = ctx->cov.as<ColCov>(); A.call = ctx->call.as<ColCall>(); A.err = ctx->errw.as<uint32_t>();
-  A.base_quality_cutoff = p->base_quality_cutoff;
-  A.precision = p->precision;
-  A.log10_ref_len = p->log10_ref_length;
-  A.mutation_cutoff = p->mutation_cutoff;
-  A.poly_cutoff = p->polymorphism_cutoff;
-  A.screen_margin = 1.0f;
-  A.guard = 2e-6f;
+  const int n_warps = ctx->sms * 16;
+  CK(ctx->scratch.alloc((size_t)n_warps * cand_warp_stride(per_warp) * sizeof(uint4), st));
+  uint32_t ra_cap = 4096 + total_cols / 64;
   CK(cudaEventRecord(ctx->ev0, st));
   CK(cudaEventRecord(ctx->evm0, st));
-  CK(launch_im_column(S, T, A, ctx->sms, st));
+  CK(launch_im_column(B, P[0].precision, ctx->sms, st));
   CK(cudaEventRecord(ctx->evm1, st));
-  CK(launch_compact(ctx->call.as<ColCall>(), ncol, ctx->blk.as<uint32_t>(), ctx->total.as<uint32_t>(), ctx->cand.as<uint32_t>(), st));
-  uint32_t n_cand = 0;
-  CK(cudaMemcpyAsync(&n_cand, ctx->total.p, 4, cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  ctx->last_candidates = n_cand;
-  // ---- candidate columns: FP64 EM, presence score, bounds
-  const int n_warps = ctx->sms * 16;
-  const uint32_t per_warp = std::max<uint32_t>(32, s->max_tile_reads);
-  CK(ctx->scratch.alloc((size_t)n_warps * cand_warp_stride(per_warp) * sizeof(uint4), st));
-  uint32_t ra_cap = n_cand * 2 + 1024;
-  const uint32_t Qh = p->n_quality;
+  CK(launch_compact(ctx->call.as<ColCall>(), total_cols, ctx->blk.as<uint32_t>(), ctx->total.as<uint32_t>(),
+                    ctx->cand.as<uint32_t>(), st));
+  // ---- candidate columns: FP64 EM, presence score, bounds (the count stays on the device)
   uint32_t n_ra = 0;
   for (int attempt = 0; attempt < 4; attempt++) {
     CK(ctx->ra.alloc((size_t)ra_cap * sizeof(RaDev), st));
     CK(ctx->qhist.alloc((size_t)ra_cap * 2 * Qh * 4, st));
-    CK(cudaMemsetAsync(ctx->next.p, 0, 16, st));
     CK(cudaMemsetAsync(ctx->n_ra.p, 0, 16, st));
     CandArgs C;
-    C.cand = ctx->cand.as<uint32_t>(); C.n_cand = n_cand; C.next = ctx->next.as<unsigned int>();
-    C.call = ctx->call.as<ColCall>(); C.ra = ctx->ra.as<RaDev>(); C.n_ra = ctx->n_ra.as<unsigned int>(); C.ra_cap = ra_cap;
+    memset(&C, 0, sizeof C);
+    C.cand = ctx->cand.as<uint32_t>(); C.n_cand_dev = ctx->total.as<uint32_t>(); C.next = ctx->next.as<unsigned int>();
+    C.ra = ctx->ra.as<RaDev>(); C.n_ra = ctx->n_ra.as<unsigned int>(); C.ra_cap = ra_cap;
     C.scratch = ctx->scratch.as<uint4>(); C.scratch_per_warp = per_warp; C.err = ctx->errw.as<uint32_t>();
-    C.base_quality_cutoff = p->base_quality_cutoff; C.log10_ref_len = p->log10_ref_length;
-    C.mutation_cutoff = p->mutation_cutoff; C.poly_cutoff = p->polymorphism_cutoff;
-    C.precision_decimal = p->polymorphism_precision_decimal; C.Qhist = Qh; C.qhist = ctx->qhist.as<uint32_t>();
-    if (n_cand) CK(launch_candidates(S, T, C, n_warps, st));
+    C.Qhist = Qh; C.qhist = ctx->qhist.as<uint32_t>();
+    CK(launch_candidates(B, C, max_K, n_warps, st));
     CK(cudaMemcpyAsync(&n_ra, ctx->n_ra.p, 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (n_ra <= ra_cap) break;
@@ -498,85 +606,139 @@ int bsq_identify_mutations(bsq_ctx* ctx, int32_t sid, const bsq_im_params* p, co
     CK(cudaMemcpy(ctx->errw.p, &e, 4, cudaMemcpyHostToDevice));
     ra_cap = n_ra + 1024;
   }
+  uint32_t n_cand = 0;
+  CK(cudaMemcpyAsync(&n_cand, ctx->total.p, 4, cudaMemcpyDeviceToHost, st));
   std::vector<RaDev> ra(n_ra);
   std::vector<uint32_t> qh((size_t)n_ra * 2 * Qh);
-  uint32_t err = 0;
   if (n_ra) {
     CK(cudaMemcpyAsync(ra.data(), ctx->ra.p, (size_t)n_ra * sizeof(RaDev), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(qh.data(), ctx->qhist.p, qh.size() * 4, cudaMemcpyDeviceToHost, st));
   }
-  host::SampleLayout L;
-  L.tpoff = &s->tpoff; L.toff = &s->toff; L.order = &s->order;
-  std::vector<ColCov> cov;
-  std::vector<ColCall> call;
-  std::vector<uint32_t> kept;
-  if (pos_out) {
-    // every column comes back: per-position arrays were asked for
-    cov.resize(ncol);
-    call.resize(ncol);
-    CK(cudaMemcpyAsync(cov.data(), ctx->cov.p, (size_t)ncol * sizeof(ColCov), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(call.data(), ctx->call.p, (size_t)ncol * sizeof(ColCall), cudaMemcpyDeviceToHost, st));
-  } else {
-    // only the columns where the MC / UN state machines can change state
-    CK(upload(ctx->d_prop, p->deletion_propagation_cutoff, s->n_targets, st));
-    CK(upload(ctx->d_seed, p->deletion_seed_cutoff, s->n_targets, st));
-    CK(ctx->keep.alloc(ncol + 16, st));
-    CK(ctx->kcol.alloc((size_t)ncol * 4 + 16, st));
-    CK(ctx->kcov.alloc((size_t)ncol * sizeof(ColCov) + 16, st));
-    CK(ctx->kcall.alloc((size_t)ncol * sizeof(ColCall) + 16, st));
-    CK(launch_intervals(ctx->cov.as<ColCov>(), ctx->call.as<ColCall>(), ncol, s->d_tpoff.as<uint32_t>(), s->n_targets,
-                        s->tgt_called.as<uint8_t>(), s->tgt_failed.as<uint8_t>(), ctx->d_prop.as<double>(),
-                        ctx->d_seed.as<double>(), ctx->keep.as<uint8_t>(), ctx->blk.as<uint32_t>(),
-                        ctx->total.as<uint32_t>(), ctx->kcol.as<uint32_t>(), ctx->kcov.as<ColCov>(),
-                        ctx->kcall.as<ColCall>(), st));
-    uint32_t nk = 0;
-    CK(cudaMemcpyAsync(&nk, ctx->total.p, 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    kept.resize(nk);
-    cov.resize(nk);
-    call.resize(nk);
-    if (nk) {
-      CK(cudaMemcpyAsync(kept.data(), ctx->kcol.p, (size_t)nk * 4, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(cov.data(), ctx->kcov.p, (size_t)nk * sizeof(ColCov), cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(call.data(), ctx->kcall.p, (size_t)nk * sizeof(ColCall), cudaMemcpyDeviceToHost, st));
-    }
+  // ---- MC / UN input: the columns where the state machines can change state, all jobs at once
+  CK(ctx->keep.alloc(total_cols + 16, st));
+  CK(ctx->kcol.alloc((size_t)total_cols * 4 + 16, st));
+  CK(ctx->kcov.alloc((size_t)total_cols * sizeof(ColCov) + 16, st));
+  CK(ctx->kcall.alloc((size_t)total_cols * sizeof(ColCall) + 16, st));
+  CK(launch_intervals(B, ctx->cov.as<ColCov>(), ctx->call.as<ColCall>(), ctx->keep.as<uint8_t>(), ctx->blk.as<uint32_t>(),
+                      ctx->total.as<uint32_t>() + 1, ctx->kcol.as<uint32_t>(), ctx->kcov.as<ColCov>(),
+                      ctx->kcall.as<ColCall>(), st));
+  uint32_t nk = 0;
+  CK(cudaMemcpyAsync(&nk, ctx->total.as<uint32_t>() + 1, 4, cudaMemcpyDeviceToHost, st));
+  std::vector<uint32_t> err(n, 0);
+  for (uint32_t j = 0; j < n; j++) CK(cudaMemcpyAsync(&err[j], ctx->imb[j]->err.p, 4, cudaMemcpyDeviceToHost, st));
+  uint32_t cerr = 0;
+  CK(cudaMemcpyAsync(&cerr, ctx->errw.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::vector<uint32_t> kept(nk);
+  std::vector<ColCov> kcov(nk);
+  std::vector<ColCall> kcall(nk);
+  if (nk) {
+    CK(cudaMemcpyAsync(kept.data(), ctx->kcol.p, (size_t)nk * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(kcov.data(), ctx->kcov.p, (size_t)nk * sizeof(ColCov), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(kcall.data(), ctx->kcall.p, (size_t)nk * sizeof(ColCall), cudaMemcpyDeviceToHost, st));
   }
-  CK(cudaMemcpyAsync(&err, ctx->errw.p, 4, cudaMemcpyDeviceToHost, st));
+  // per-position arrays only where they were asked for
+  std::vector<std::vector<ColCov>> pcov(n);
+  std::vector<std::vector<ColCall>> pcall(n);
+  for (uint32_t j = 0; j < n; j++) {
+    if (!pos_out || !pos_out[j]) continue;
+    const uint32_t nc = smp[j]->n_cols;
+    pcov[j].resize(nc);
+    pcall[j].resize(nc);
+    CK(cudaMemcpyAsync(pcov[j].data(), ctx->cov.as<ColCov>() + col_b[j], (size_t)nc * sizeof(ColCov), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(pcall[j].data(), ctx->call.as<ColCall>() + col_b[j], (size_t)nc * sizeof(ColCall), cudaMemcpyDeviceToHost, st));
+  }
   CK(cudaEventRecord(ctx->ev1, st));
   CK(cudaStreamSynchronize(st));
   float ms = 0, mms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   cudaEventElapsedTime(&mms, ctx->evm0, ctx->evm1);
-  ctx->last_ms = ms; ctx->main_ms = mms; ctx->launches = 4 + (n_cand ? 1 : 0) + (pos_out ? 0 : 4);
-  if (err) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(err));
-  // ---- host assembly
-  host::assemble_ra(ra, qh, Qh, L, ctx->res_ra);
-  if (pos_out) {
-    host::intervals(cov, call, L, p, ctx->res_mc, ctx->res_un);
-    host::fill_positions(cov, call, L, pos_out);
-  } else {
-    host::intervals_sparse(kept, cov, call, L, p, ctx->res_mc, ctx->res_un);
+  ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 9;
+  ctx->last_candidates += n_cand;
+  if (cerr & ~kErrRaOverflow) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(cerr));
+  for (uint32_t j = 0; j < n; j++)
+    if (err[j]) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(err[j]));
+  // ---- host assembly, per job
+  std::vector<std::vector<RaDev>> jra(n);
+  std::vector<std::vector<uint32_t>> jqh(n);
+  for (uint32_t i = 0; i < n_ra; i++) {
+    const uint32_t j = (uint32_t)(std::upper_bound(col_b.begin(), col_b.end(), ra[i].col) - col_b.begin()) - 1;
+    RaDev d = ra[i];
+    d.col -= col_b[j];
+    jra[j].push_back(d);
+    jqh[j].insert(jqh[j].end(), qh.begin() + (size_t)i * 2 * Qh, qh.begin() + (size_t)(i + 1) * 2 * Qh);
+  }
+  size_t kp = 0;
+  for (uint32_t j = 0; j < n; j++) {
+    SampleDev* s = smp[j];
+    host::SampleLayout L;
+    L.tpoff = &s->tpoff; L.toff = &s->toff; L.order = &s->order;
+    host::assemble_ra(jra[j], jqh[j], Qh, L, ctx->res_ra[job0 + j]);
+    std::vector<uint32_t> kc;
+    std::vector<ColCov> kv;
+    std::vector<ColCall> kl;
+    for (; kp < nk && kept[kp] < col_b[j + 1]; kp++) {
+      kc.push_back(kept[kp] - col_b[j]);
+      kv.push_back(kcov[kp]);
+      kl.push_back(kcall[kp]);
+    }
+    if (pos_out && pos_out[j]) {   // dense arrays fetched anyway: run the state machines over every column
+      host::intervals(pcov[j], pcall[j], L, &P[j], ctx->res_mc[job0 + j], ctx->res_un[job0 + j]);
+      host::fill_positions(pcov[j], pcall[j], L, pos_out[j]);
+    } else {
+      host::intervals_sparse(kc, kv, kl, L, &P[j], ctx->res_mc[job0 + j], ctx->res_un[job0 + j]);
+    }
   }
   return BSQ_OK;
 }
 
-int bsq_im_result_counts(const bsq_ctx* ctx, uint64_t* n_ra, uint64_t* n_mc, uint64_t* n_un) {
-  if (!ctx) return BSQ_ERR_INVALID;
-  if (n_ra) *n_ra = ctx->res_ra.size();
-  if (n_mc) *n_mc = ctx->res_mc.size();
-  if (n_un) *n_un = ctx->res_un.size();
+int bsq_identify_mutations_batch(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_params* P,
+                                 const double* const* tables, bsq_position_arrays* const* pos_out) {
+  if (!ctx || !ids || !P || !tables || n == 0) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  ctx->res_ra.assign(n, {}); ctx->res_mc.assign(n, {}); ctx->res_un.assign(n, {});
+  ctx->last_ms = 0; ctx->main_ms = 0; ctx->launches = 0; ctx->last_candidates = 0;
+  for (uint32_t g = 0; g < n; g += kBatchJobs) {
+    const int rc = im_group(ctx, std::min(kBatchJobs, n - g), ids + g, P + g, tables + g,
+                            pos_out ? pos_out + g : nullptr, g);
+    if (rc != BSQ_OK) { ctx->res_ra.clear(); ctx->res_mc.clear(); ctx->res_un.clear(); return rc; }
+  }
   return BSQ_OK;
+}
+
+int bsq_identify_mutations(bsq_ctx* ctx, int32_t sid, const bsq_im_params* p, const double* table,
+                           bsq_position_arrays* pos_out) {
+  bsq_position_arrays* po[1] = {pos_out};
+  return bsq_identify_mutations_batch(ctx, 1, &sid, p, &table, pos_out ? po : nullptr);
+}
+
+int bsq_im_batch_result_counts(const bsq_ctx* ctx, uint32_t job, uint64_t* n_ra, uint64_t* n_mc, uint64_t* n_un) {
+  if (!ctx || job >= ctx->res_ra.size()) return BSQ_ERR_INVALID;
+  if (n_ra) *n_ra = ctx->res_ra[job].size();
+  if (n_mc) *n_mc = ctx->res_mc[job].size();
+  if (n_un) *n_un = ctx->res_un[job].size();
+  return BSQ_OK;
+}
+
+int bsq_im_batch_result_copy(const bsq_ctx* ctx, uint32_t job, bsq_ra_record* ra, uint64_t ra_cap, bsq_mc_record* mc,
+                             uint64_t mc_cap, bsq_un_record* un, uint64_t un_cap) {
+  if (!ctx || job >= ctx->res_ra.size()) return BSQ_ERR_INVALID;
+  const auto &R = ctx->res_ra[job];
+  const auto &M = ctx->res_mc[job];
+  const auto &U = ctx->res_un[job];
+  if ((ra && ra_cap < R.size()) || (mc && mc_cap < M.size()) || (un && un_cap < U.size())) return BSQ_ERR_SIZE;
+  if (ra) std::copy(R.begin(), R.end(), ra);
+  if (mc) std::copy(M.begin(), M.end(), mc);
+  if (un) std::copy(U.begin(), U.end(), un);
+  return BSQ_OK;
+}
+
+int bsq_im_result_counts(const bsq_ctx* ctx, uint64_t* n_ra, uint64_t* n_mc, uint64_t* n_un) {
+  return bsq_im_batch_result_counts(ctx, 0, n_ra, n_mc, n_un);
 }
 
 int bsq_im_result_copy(const bsq_ctx* ctx, bsq_ra_record* ra, uint64_t ra_cap, bsq_mc_record* mc, uint64_t mc_cap,
                        bsq_un_record* un, uint64_t un_cap) {
-  if (!ctx) return BSQ_ERR_INVALID;
-  if ((ra && ra_cap < ctx->res_ra.size()) || (mc && mc_cap < ctx->res_mc.size()) || (un && un_cap < ctx->res_un.size()))
-    return BSQ_ERR_SIZE;
-  if (ra) std::copy(ctx->res_ra.begin(), ctx->res_ra.end(), ra);
-  if (mc) std::copy(ctx->res_mc.begin(), ctx->res_mc.end(), mc);
-  if (un) std::copy(ctx->res_un.begin(), ctx->res_un.end(), un);
-  return BSQ_OK;
+  return bsq_im_batch_result_copy(ctx, 0, ra, ra_cap, mc, mc_cap, un, un_cap);
 }
 
 int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_launches, double* main_kernel_ms) {

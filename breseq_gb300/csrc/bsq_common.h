@@ -119,25 +119,20 @@ struct ImArgs {
   double poly_cutoff;
   float screen_margin;        // log10 units subtracted from the polymorphism cutoff for the screen
   float guard;                // consensus guard band (log10 units) for FP64 recompute
+  double precision_decimal;   // EM convergence tolerance (polymorphism_precision_decimal)
 };
 
 // A scoring job for the candidate kernel: one reference column, all its insert slots.
 struct CandArgs {
-  const uint32_t* cand;       // candidate columns
-  uint32_t n_cand;
+  const uint32_t* cand;       // candidate columns (batch column space)
+  const uint32_t* n_cand_dev; // number of candidates, written by the compaction on the device
   unsigned int* next;         // work counter (persistent warps)
-  ColCall* call;              // slot-0 consensus is rewritten for kRecompute columns
   struct RaDev* ra;           // output records
   unsigned int* n_ra;
   uint32_t ra_cap;
   uint4* scratch;             // per-warp gather buffer: [n_warps][scratch_per_warp]
   uint32_t scratch_per_warp;
   uint32_t* err;
-  uint32_t base_quality_cutoff;
-  double log10_ref_len;
-  double mutation_cutoff;
-  double poly_cutoff;
-  double precision_decimal;
   uint32_t Qhist;             // quality histogram bins kept per RA (for the K-S test)
   uint32_t* qhist;            // [ra_cap][2][Qhist] major / minor qualities
 };
@@ -152,6 +147,40 @@ struct RaDev {
   uint32_t pos_info[5][2];    // [base][top, bottom]
   uint32_t n;
   uint8_t ref_idx, var_idx, maj_idx, min_idx, passed_cons, passed_poly, pad[2];
+};
+
+// ----------------------------------------------------------------------------- batches
+// One sample of a batch with everything its passes read and write.  Pass-2 per-column outputs of all
+// jobs live in one array (the batch column space); I.cov / I.call point at this job's part of it.
+struct DevJob {
+  DevSample S;
+  ClassTable T;
+  EcArgs E;
+  ImArgs I;
+  const double* prop;       // per target deletion propagation cutoff (pass 2)
+  const double* seed;       // per target deletion seed cutoff (pass 2)
+  uint32_t col_begin;       // first column of this job in the batch column space
+  uint32_t tile_begin;      // first tile of this job in the batch tile space
+  uint32_t cblk_begin;      // first 1024-column coverage block of this job
+  uint32_t pad;
+};
+
+// Kernel argument describing a batch: the jobs and the prefix sums that map a batch-wide tile /
+// column / coverage block back to its job.  Passed by value as a __grid_constant__ parameter, so
+// the job fields are read from the constant bank (and re-read there instead of being held in
+// registers); 64 jobs keep it under the 32 KB kernel-parameter limit.  Larger batches run as
+// consecutive groups of kBatchJobs.
+constexpr uint32_t kBatchJobs = 64;
+struct Batch {
+  uint32_t n_jobs;
+  uint32_t total_tiles;
+  uint32_t total_cols;
+  uint32_t total_cblk;
+  uint32_t tile_begin[kBatchJobs + 1];
+  uint32_t col_begin[kBatchJobs + 1];
+  uint32_t cblk_begin[kBatchJobs + 1];
+  uint32_t pad;
+  DevJob jobs[kBatchJobs];
 };
 
 // Per-warp scratch of the candidate kernels, in uint4 units: `cap` gather entries followed by `cap`

@@ -101,6 +101,14 @@ __device__ __forceinline__ int bounds_end0(const DevSample& S, const DevRead& rd
   return (rd.flags & kSimple) ? (int)rd.clip + (int)(rd.end - rd.start) - 1 : (int)S.qb[r].qbe;
 }
 
+// Index j with prefix[j] <= g < prefix[j + 1] (prefix ascending, n + 1 entries).
+// prefix lives in kernel-parameter space: plain loads, no __ldg
+__device__ __forceinline__ uint32_t job_of(const uint32_t* prefix, uint32_t n, uint32_t g) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) { const uint32_t mid = (lo + hi) >> 1; if (prefix[mid] <= g) lo = mid; else hi = mid; }
+  return lo;
+}
+
 __device__ __forceinline__ uint32_t target_of(const DevSample& S, uint32_t c) {
   uint32_t lo = 0, hi = S.n_targets;  // largest t with tpoff[t] <= c
   while (hi - lo > 1) { uint32_t mid = (lo + hi) >> 1; if (__ldg(S.tpoff + mid) <= c) lo = mid; else hi = mid; }
@@ -319,6 +327,7 @@ struct CandOut {
   uint32_t* err;
   uint32_t base_quality_cutoff;
   double log10_ref_len, mutation_cutoff, poly_cutoff, precision_decimal;
+  uint32_t col_offset;        // added to the column reported in each RA item
 };
 
 // Scores one reference column (called by a whole warp): gathers the reads covering column c in BAM
@@ -526,7 +535,7 @@ __device__ void score_candidate_column(const DevSample& S, const ClassTable& T, 
       if (slot < A.ra_cap) {
         if (lane == 0) {
           RaDev o;
-          o.col = c; o.insert_position = (uint32_t)k;
+          o.col = c + A.col_offset; o.insert_position = (uint32_t)k;
           o.score = vscore; o.consensus_score = cscore;
           for (int b = 0; b < 5; b++) { o.f[b] = full.f[b]; o.pos_info[b][0] = pinfo[b][0]; o.pos_info[b][1] = pinfo[b][1]; }
           o.lower = lower; o.upper = upper; o.n = n;

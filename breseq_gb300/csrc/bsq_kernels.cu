@@ -219,16 +219,26 @@ __device__ __forceinline__ bool read_start_counts(const EcArgs& A, const DevRead
   return send1 >= req;
 }
 
-__global__ void __launch_bounds__(256) ec_read_kernel(DevSample S, EcArgs A) {
+// Work units are chunks of one job's reads, pulled by whole blocks from a shared counter; the block's
+// shared histogram belongs to the chunk's job and is flushed at the chunk's end.
+__global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Batch B, const uint4* chunks, uint32_t n_chunks, unsigned int* next) {
   extern __shared__ uint32_t sh_hist[];
+  __shared__ uint32_t sh_chunk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (;;) {
+  if (threadIdx.x == 0) sh_chunk = atomicAdd(next, 1u);
+  __syncthreads();
+  const uint32_t ci = sh_chunk;
+  if (ci >= n_chunks) break;
+  const uint4 ch = chunks[ci];                 // x = job, y = first read, z = end read
+  const DevSample& S = B.jobs[ch.x].S;
+  const EcArgs& A = B.jobs[ch.x].E;
   const uint32_t nbins = A.R * 25u * A.Q;
   for (uint32_t i = threadIdx.x; i < nbins; i += blockDim.x) sh_hist[i] = 0;
   __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   uint32_t err = 0;
   uint32_t done = 0;
-  for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < S.n_reads; r += nwarps) {
+  for (uint32_t r = ch.y + warp; r < ch.z; r += nwarps) {
     const DevRead rd = S.reads[r];
     if (rd.flags & kSkip) continue;      // filtered by flag, or on a target outside the pileup set
     const bool red = rd.flags & kRedundant;
@@ -308,6 +318,8 @@ __global__ void __launch_bounds__(256) ec_read_kernel(DevSample S, EcArgs A) {
   }
   if (err) atomicOr(A.err, err);
   (void)done;
+  __syncthreads();
+  }
 }
 
 // Block-wide inclusive scan of (a, b) pairs, 1024 threads.
@@ -333,24 +345,31 @@ __device__ __forceinline__ void block_scan2(int& a, int& b, int* sh_a, int* sh_b
   if (w > 0) { a += sh_a[w - 1]; b += sh_b[w - 1]; }
 }
 
-__global__ void __launch_bounds__(1024) cov_blocksum_kernel(const int32_t* du, const int32_t* dr, uint32_t n,
-                                                            uint32_t* bu, uint32_t* br) {
+__global__ void __launch_bounds__(1024) cov_blocksum_kernel(const __grid_constant__ Batch B) {
   __shared__ int sa[32], sb[32];
-  const uint32_t c = blockIdx.x * 1024 + threadIdx.x;
-  int a = c < n ? du[c] : 0, b = c < n ? dr[c] : 0;
+  const uint32_t job = job_of(B.cblk_begin, B.n_jobs, blockIdx.x);
+  const uint32_t lb = blockIdx.x - B.cblk_begin[job];
+  const EcArgs& A = B.jobs[job].E;
+  const uint32_t n = B.jobs[job].S.n_cols;
+  const uint32_t c = lb * 1024 + threadIdx.x;
+  int a = c < n ? A.diff_u[c] : 0, b = c < n ? A.diff_r[c] : 0;
   block_scan2(a, b, sa, sb);
-  if (threadIdx.x == 1023) { bu[blockIdx.x] = (uint32_t)a; br[blockIdx.x] = (uint32_t)b; }
+  if (threadIdx.x == 1023) { A.blk_u[lb] = (uint32_t)a; A.blk_r[lb] = (uint32_t)b; }
 }
 
 // Unique-only coverage histogram (error_count.cpp:176-191): a column counts when no redundant read
 // covers it; preprocess adds the read-start tallies of the same columns.
-__global__ void __launch_bounds__(1024) cov_hist_kernel(DevSample S, EcArgs A) {
+__global__ void __launch_bounds__(1024) cov_hist_kernel(const __grid_constant__ Batch B) {
   __shared__ int sa[32], sb[32];
-  const uint32_t c = blockIdx.x * 1024 + threadIdx.x;
+  const uint32_t job = job_of(B.cblk_begin, B.n_jobs, blockIdx.x);
+  const uint32_t lb = blockIdx.x - B.cblk_begin[job];
+  const DevSample& S = B.jobs[job].S;
+  const EcArgs& A = B.jobs[job].E;
+  const uint32_t c = lb * 1024 + threadIdx.x;
   int a = c < S.n_cols ? A.diff_u[c] : 0, b = c < S.n_cols ? A.diff_r[c] : 0;
   block_scan2(a, b, sa, sb);
-  a += (int)A.blk_u[blockIdx.x];
-  b += (int)A.blk_r[blockIdx.x];
+  a += (int)A.blk_u[lb];
+  b += (int)A.blk_r[lb];
   bool rec = false;
   uint32_t t = 0, key = 0xFFFFFFFFu;
   if (c < S.n_cols && __ldg(S.ref + c) != 0) {
@@ -382,12 +401,17 @@ __global__ void __launch_bounds__(1024) cov_hist_kernel(DevSample S, EcArgs A) {
 constexpr uint32_t kColumnWarps = 8;
 
 template <bool FP64>
-__global__ void __launch_bounds__(256, 4) im_column_kernel(DevSample S, ClassTable T, ImArgs A) {
+__global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant__ Batch Bt) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   DevRead* sh_rd = reinterpret_cast<DevRead*>(smem) + warp * 32;
   uint32_t local_err = 0;
-  for (uint32_t tile = blockIdx.x * nwarps + warp; tile < S.n_tiles; tile += gridDim.x * nwarps) {
+  for (uint32_t gt = blockIdx.x * nwarps + warp; gt < Bt.total_tiles; gt += gridDim.x * nwarps) {
+    const uint32_t job = job_of(Bt.tile_begin, Bt.n_jobs, gt);
+    const uint32_t tile = gt - Bt.tile_begin[job];
+    const DevSample& S = Bt.jobs[job].S;
+    const ClassTable& T = Bt.jobs[job].T;
+    const ImArgs& A = Bt.jobs[job].I;
     const uint32_t c0 = tile * 32, c = c0 + lane;
     const bool inr = c < S.n_cols;
     const uint8_t refc = inr ? __ldg(S.ref + c) : 0;
@@ -570,8 +594,8 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(DevSample S, ClassTab
       A.cov[c] = cv;
       A.call[c] = cl;
     }
+    if (local_err) { atomicOr(A.err, local_err); local_err = 0; }
   }
-  if (local_err) atomicOr(A.err, local_err);
 }
 
 // ============================================================================ candidate compaction
@@ -588,7 +612,8 @@ __global__ void cand_count_kernel(const ColCall* call, uint32_t n, uint32_t* blo
   if (threadIdx.x == 0) block_counts[blockIdx.x] = s;
 }
 
-__global__ void scan_kernel(uint32_t* v, uint32_t n, uint32_t* total) {  // single block, exclusive
+// Exclusive scan of v[0..n) in place by one block of 1024 threads; the sum goes to *total.
+__device__ void block_exclusive_scan(uint32_t* v, uint32_t n, uint32_t* total) {
   __shared__ uint32_t carry;
   __shared__ uint32_t warp_sums[32];
   if (threadIdx.x == 0) carry = 0;
@@ -614,6 +639,18 @@ __global__ void scan_kernel(uint32_t* v, uint32_t n, uint32_t* total) {  // sing
     __syncthreads();
   }
   if (threadIdx.x == 0) *total = carry;
+  __syncthreads();
+}
+
+__global__ void scan_kernel(uint32_t* v, uint32_t n, uint32_t* total) { block_exclusive_scan(v, n, total); }
+
+// the coverage block sums of every job, one block per job
+__global__ void scan_jobs_kernel(const __grid_constant__ Batch B) {
+  const uint32_t job = blockIdx.x;
+  const uint32_t nb = B.cblk_begin[job + 1] - B.cblk_begin[job];
+  const EcArgs& A = B.jobs[job].E;
+  block_exclusive_scan(A.blk_u, nb, A.blk_u + nb);
+  block_exclusive_scan(A.blk_r, nb, A.blk_r + nb);
 }
 
 __global__ void cand_scatter_kernel(const ColCall* call, uint32_t n, const uint32_t* block_offsets, uint32_t* out) {
@@ -637,25 +674,27 @@ __global__ void cand_scatter_kernel(const ColCall* call, uint32_t n, const uint3
 // or total coverage at or below its seed cutoff; the column after such a column closes what it
 // opened, and the column before it supplies the left-outside coverage.  Those columns are marked and
 // the host replays the state machines over them alone.
-__global__ void interval_mark_kernel(const ColCov* cov, const ColCall* call, uint32_t n_cols, const uint32_t* tpoff,
-                                     uint32_t n_targets, const uint8_t* called, const uint8_t* failed,
-                                     const double* prop, const double* seed, uint8_t* keep) {
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n_cols) return;
-  if (!(call[c].flags & kScored)) return;
-  uint32_t lo = 0, hi = n_targets;
+__global__ void interval_mark_kernel(const __grid_constant__ Batch B, const ColCov* cov, const ColCall* call, uint8_t* keep) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= B.total_cols) return;
+  if (!(call[g].flags & kScored)) return;
+  const uint32_t job = job_of(B.col_begin, B.n_jobs, g);
+  const uint32_t c = g - B.col_begin[job];
+  const DevJob& J = B.jobs[job];
+  const uint32_t* tpoff = J.S.tpoff;
+  uint32_t lo = 0, hi = J.S.n_targets;
   while (hi - lo > 1) { uint32_t mid = (lo + hi) >> 1; if (tpoff[mid] <= c) lo = mid; else hi = mid; }
   const uint32_t t = lo;
-  if (!called[t] || failed[t]) return;
-  const ColCov v = cov[c];
+  if (!J.S.tgt_called[t] || J.S.tgt_failed[t]) return;
+  const ColCov v = cov[g];
   const double u1 = (double)v.uniq_bot + (double)v.uniq_top;
   const double r1 = v.red_bot + v.red_top;
   const double total = (double)((int)rint(u1) + (int)rint(r1));
-  const bool interesting = !(call[c].flags & kBasePredicted) || u1 <= prop[t] || total <= seed[t];
+  const bool interesting = !(call[g].flags & kBasePredicted) || u1 <= J.prop[t] || total <= J.seed[t];
   if (!interesting) return;
-  keep[c] = 1;
-  if (c > tpoff[t]) keep[c - 1] = 1;
-  if (c + 1 < tpoff[t + 1] - 1) keep[c + 1] = 1;
+  keep[g] = 1;
+  if (c > tpoff[t]) keep[g - 1] = 1;
+  if (c + 1 < tpoff[t + 1] - 1) keep[g + 1] = 1;
 }
 
 __global__ void flag_count_kernel(const uint8_t* keep, uint32_t n, uint32_t* block_counts) {
@@ -694,25 +733,33 @@ __global__ void flag_gather_kernel(const uint8_t* keep, uint32_t n, const uint32
 
 // One warp per candidate column (persistent warps pulling from a work counter); the scoring itself is
 // score_candidate_column (bsq_device.cuh).
-__global__ void __launch_bounds__(128) im_candidate_kernel(DevSample S, ClassTable T, CandArgs A) {
+__global__ void __launch_bounds__(128) im_candidate_kernel(const __grid_constant__ Batch B, CandArgs A, uint32_t hist_cap) {
   extern __shared__ uint32_t sh_hist[];
   const int lane = threadIdx.x & 31;
   const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   uint4* ents = A.scratch + (size_t)gw * cand_warp_stride(A.scratch_per_warp);
-  uint32_t* hist = (T.K <= kEmHistMax) ? sh_hist + (threadIdx.x >> 5) * T.K : nullptr;
-  CandOut out;
-  out.ra = A.ra; out.n_ra = A.n_ra; out.ra_cap = A.ra_cap; out.qhist = A.qhist; out.Qhist = A.Qhist; out.err = A.err;
-  out.base_quality_cutoff = A.base_quality_cutoff; out.log10_ref_len = A.log10_ref_len;
-  out.mutation_cutoff = A.mutation_cutoff; out.poly_cutoff = A.poly_cutoff; out.precision_decimal = A.precision_decimal;
+  const uint32_t n_cand = *A.n_cand_dev;
   for (;;) {
     uint32_t idx = 0;
     if (lane == 0) idx = atomicAdd(A.next, 1u);
     idx = __shfl_sync(0xFFFFFFFFu, idx, 0);
-    if (idx >= A.n_cand) break;
-    const uint32_t c = A.cand[idx];
-    const ColCall cl0 = A.call[c];
+    if (idx >= n_cand) break;
+    const uint32_t g = A.cand[idx];
+    const uint32_t job = job_of(B.col_begin, B.n_jobs, g);
+    const uint32_t col0 = B.col_begin[job];
+    const uint32_t c = g - col0;
+    const DevJob& J = B.jobs[job];
+    const DevSample& S = J.S;
+    const ClassTable& T = J.T;
+    uint32_t* hist = (T.K <= hist_cap) ? sh_hist + (threadIdx.x >> 5) * hist_cap : nullptr;
+    CandOut out;
+    out.ra = A.ra; out.n_ra = A.n_ra; out.ra_cap = A.ra_cap; out.qhist = A.qhist; out.Qhist = A.Qhist; out.err = A.err;
+    out.base_quality_cutoff = J.I.base_quality_cutoff; out.log10_ref_len = J.I.log10_ref_len;
+    out.mutation_cutoff = J.I.mutation_cutoff; out.poly_cutoff = J.I.poly_cutoff;
+    out.precision_decimal = J.I.precision_decimal; out.col_offset = col0;
+    const ColCall cl0 = J.I.call[c];
     score_candidate_column(S, T, out, c, (cl0.flags & (kCandidate | kRecompute)) != 0, (cl0.flags & kRecompute) != 0,
-                           cl0, A.call, ents, A.scratch_per_warp, hist);
+                           cl0, J.I.call, ents, A.scratch_per_warp, hist);
     __syncwarp();
   }
 }
@@ -741,28 +788,29 @@ cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t
   tile_range_kernel<<<(n_tiles + 255) / 256, 256, 0, st>>>(rstart, n_reads, n_tiles, maxspan, tile_range, max_tile_reads);
   return cudaGetLastError();
 }
-cudaError_t launch_ec(const DevSample& S, const EcArgs& A, int sms, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1) {
-  const size_t smem = (size_t)A.R * 25 * A.Q * sizeof(uint32_t);
+cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, unsigned int* next, uint32_t max_bins,
+                      int sms, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1) {
+  const size_t smem = (size_t)max_bins * sizeof(uint32_t);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(ec_read_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  const int grid = grid_for(S.n_reads / 8 + 1, 8, sms, 8);
+  cudaError_t e = cudaMemsetAsync(next, 0, sizeof(unsigned int), st);
+  if (e != cudaSuccess) return e;
+  const int grid = grid_for(n_chunks, 1, sms, 8);
   if (main0) cudaEventRecord(main0, st);
-  ec_read_kernel<<<grid, 256, smem, st>>>(S, A);
+  ec_read_kernel<<<grid, 256, smem, st>>>(B, chunks, n_chunks, next);
   if (main1) cudaEventRecord(main1, st);
-  const uint32_t nb = (S.n_cols + 1023) / 1024;
-  cov_blocksum_kernel<<<nb, 1024, 0, st>>>(A.diff_u, A.diff_r, S.n_cols, A.blk_u, A.blk_r);
-  scan_kernel<<<1, 1024, 0, st>>>(A.blk_u, nb, A.blk_u + nb);
-  scan_kernel<<<1, 1024, 0, st>>>(A.blk_r, nb, A.blk_r + nb);
-  cov_hist_kernel<<<nb, 1024, 0, st>>>(S, A);
+  cov_blocksum_kernel<<<B.total_cblk, 1024, 0, st>>>(B);
+  scan_jobs_kernel<<<B.n_jobs, 1024, 0, st>>>(B);
+  cov_hist_kernel<<<B.total_cblk, 1024, 0, st>>>(B);
   return cudaGetLastError();
 }
-cudaError_t launch_im_column(const DevSample& S, const ClassTable& T, const ImArgs& A, int sms, cudaStream_t st) {
-  const int grid = grid_for(S.n_tiles, 8, sms, 8);
+cudaError_t launch_im_column(const Batch& B, int precision, int sms, cudaStream_t st) {
+  const int grid = grid_for(B.total_tiles, 8, sms, 8);
   const size_t smem = kColumnWarps * 32 * sizeof(DevRead);
-  if (A.precision == 0) im_column_kernel<true><<<grid, 32 * kColumnWarps, smem, st>>>(S, T, A);
-  else im_column_kernel<false><<<grid, 32 * kColumnWarps, smem, st>>>(S, T, A);
+  if (precision == 0) im_column_kernel<true><<<grid, 32 * kColumnWarps, smem, st>>>(B);
+  else im_column_kernel<false><<<grid, 32 * kColumnWarps, smem, st>>>(B);
   return cudaGetLastError();
 }
 cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_counts, uint32_t* total, uint32_t* out,
@@ -773,24 +821,27 @@ cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_coun
   cand_scatter_kernel<<<nb, 256, 0, st>>>(call, n, block_counts, out);
   return cudaGetLastError();
 }
-cudaError_t launch_intervals(const ColCov* cov, const ColCall* call, uint32_t n_cols, const uint32_t* tpoff,
-                             uint32_t n_targets, const uint8_t* called, const uint8_t* failed, const double* prop,
-                             const double* seed, uint8_t* keep, uint32_t* block_counts, uint32_t* total,
-                             uint32_t* out_col, ColCov* out_cov, ColCall* out_call, cudaStream_t st) {
-  const uint32_t nb = (n_cols + 255) / 256;
-  cudaError_t e = cudaMemsetAsync(keep, 0, n_cols, st);
+cudaError_t launch_intervals(const Batch& B, const ColCov* cov, const ColCall* call, uint8_t* keep, uint32_t* block_counts,
+                             uint32_t* total, uint32_t* out_col, ColCov* out_cov, ColCall* out_call, cudaStream_t st) {
+  const uint32_t n = B.total_cols;
+  const uint32_t nb = (n + 255) / 256;
+  cudaError_t e = cudaMemsetAsync(keep, 0, n, st);
   if (e != cudaSuccess) return e;
-  interval_mark_kernel<<<nb, 256, 0, st>>>(cov, call, n_cols, tpoff, n_targets, called, failed, prop, seed, keep);
-  flag_count_kernel<<<nb, 256, 0, st>>>(keep, n_cols, block_counts);
+  interval_mark_kernel<<<nb, 256, 0, st>>>(B, cov, call, keep);
+  flag_count_kernel<<<nb, 256, 0, st>>>(keep, n, block_counts);
   scan_kernel<<<1, 1024, 0, st>>>(block_counts, nb, total);
-  flag_gather_kernel<<<nb, 256, 0, st>>>(keep, n_cols, block_counts, cov, call, out_col, out_cov, out_call);
+  flag_gather_kernel<<<nb, 256, 0, st>>>(keep, n, block_counts, cov, call, out_col, out_cov, out_call);
   return cudaGetLastError();
 }
 
-cudaError_t launch_candidates(const DevSample& S, const ClassTable& T, const CandArgs& A, int n_warps, cudaStream_t st) {
-  const int blocks = (n_warps + 3) / 4;
-  const size_t smem = (T.K <= kEmHistMax) ? (size_t)4 * T.K * sizeof(uint32_t) : 0;
-  im_candidate_kernel<<<blocks, 128, smem, st>>>(S, T, A);
+cudaError_t launch_candidates(const Batch& B, const CandArgs& A, uint32_t max_K, int n_warps, cudaStream_t st) {
+  // each job compresses by class when its own K fits, so a job's summation order (and its
+  // results) do not depend on the other jobs of the batch
+  const uint32_t hist_cap = max_K < kEmHistMax ? max_K : kEmHistMax;
+  const size_t smem = (size_t)4 * hist_cap * sizeof(uint32_t);
+  cudaError_t e = cudaMemsetAsync(A.next, 0, sizeof(unsigned int), st);
+  if (e != cudaSuccess) return e;
+  im_candidate_kernel<<<(n_warps + 3) / 4, 128, smem, st>>>(B, A, hist_cap);
   return cudaGetLastError();
 }
 

@@ -44,15 +44,13 @@ cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st);
 cudaError_t launch_mapq_index(DevRead* reads, const uint8_t* mapq, const uint8_t* map, uint32_t n, cudaStream_t st);
 cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t n_tiles, uint32_t maxspan,
                               uint2* tile_range, uint32_t* max_tile_reads, cudaStream_t st);
-cudaError_t launch_ec(const DevSample& S, const EcArgs& A, int sms, cudaStream_t st, cudaEvent_t main0,
-                      cudaEvent_t main1);
-cudaError_t launch_im_column(const DevSample& S, const ClassTable& T, const ImArgs& A, int sms, cudaStream_t st);
+cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, unsigned int* next, uint32_t max_bins,
+                      int sms, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1);
+cudaError_t launch_im_column(const Batch& B, int precision, int sms, cudaStream_t st);
 cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_counts, uint32_t* total, uint32_t* out,
                            cudaStream_t st);
-cudaError_t launch_intervals(const ColCov* cov, const ColCall* call, uint32_t n_cols, const uint32_t* tpoff,
-                             uint32_t n_targets, const uint8_t* called, const uint8_t* failed, const double* prop,
-                             const double* seed, uint8_t* keep, uint32_t* block_counts, uint32_t* total,
-                             uint32_t* out_col, ColCov* out_cov, ColCall* out_call, cudaStream_t st);
-cudaError_t launch_candidates(const DevSample& S, const ClassTable& T, const CandArgs& A, int n_warps, cudaStream_t st);
+cudaError_t launch_intervals(const Batch& B, const ColCov* cov, const ColCall* call, uint8_t* keep, uint32_t* block_counts,
+                             uint32_t* total, uint32_t* out_col, ColCov* out_cov, ColCall* out_call, cudaStream_t st);
+cudaError_t launch_candidates(const Batch& B, const CandArgs& A, uint32_t max_K, int n_warps, cudaStream_t st);
 
 }  // namespace bsq

@@ -154,6 +154,7 @@ cudaError_t launch_noalloc_positions(void* scratch, const DevSample& S, const No
   out.ra = reinterpret_cast<RaDev*>(J.ra); out.n_ra = J.n_ra; out.ra_cap = J.ra_cap; out.qhist = J.qhist; out.Qhist = J.Q;
   out.err = counters + 1; out.base_quality_cutoff = J.base_quality_cutoff; out.log10_ref_len = J.log10_ref_len;
   out.mutation_cutoff = J.mutation_cutoff; out.poly_cutoff = J.poly_cutoff; out.precision_decimal = J.precision_decimal;
+  out.col_offset = 0;
   NoAllocArgs A;
   A.tid = J.tid; A.pos0 = J.pos0; A.n = J.n_positions; A.next = counters; A.failed = J.failed;
   A.gather = reinterpret_cast<uint4*>(base); A.per_warp = J.per_warp; A.n_warps = J.n_warps;

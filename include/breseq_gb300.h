@@ -294,6 +294,22 @@ int bsq_im_result_counts(const bsq_ctx* ctx, uint64_t* n_ra, uint64_t* n_mc, uin
 int bsq_im_result_copy(const bsq_ctx* ctx, bsq_ra_record* ra, uint64_t ra_cap,
                        bsq_mc_record* mc, uint64_t mc_cap, bsq_un_record* un, uint64_t un_cap);
 
+/* Batch forms: n samples scored by one launch per kernel of the pass (every sample's reads or
+ * column tiles are units of one persistent grid).  Element j of each array belongs to sample_ids[j];
+ * the results of each sample equal those of the single-sample call.  breseq runs error_count and
+ * identify_mutations once per sample (src/breseq/breseq_cmdline.cpp:1969, :2293); a caller scoring
+ * many samples issues one batch call instead.  The single-sample functions above are batches of one.
+ * All samples of one bsq_identify_mutations_batch call use the same `precision`.  Results of the
+ * identify batch are read per job index j (0..n-1) until the next pass-2 call.  `pos_out` may be
+ * NULL, and so may any pos_out[j]. */
+int bsq_error_count_batch(bsq_ctx* ctx, uint32_t n, const int32_t* sample_ids, const bsq_ec_params* p,
+                          bsq_ec_result* out);
+int bsq_identify_mutations_batch(bsq_ctx* ctx, uint32_t n, const int32_t* sample_ids, const bsq_im_params* p,
+                                 const double* const* log10_prob_tables, bsq_position_arrays* const* pos_out);
+int bsq_im_batch_result_counts(const bsq_ctx* ctx, uint32_t job, uint64_t* n_ra, uint64_t* n_mc, uint64_t* n_un);
+int bsq_im_batch_result_copy(const bsq_ctx* ctx, uint32_t job, bsq_ra_record* ra, uint64_t ra_cap,
+                             bsq_mc_record* mc, uint64_t mc_cap, bsq_un_record* un, uint64_t un_cap);
+
 /* Timing of the last pass on the device (CUDA events around the kernels, milliseconds) and the
  * number of kernels launched by it. */
 int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_launches,
@@ -349,6 +365,79 @@ int bsq_timer_stop(bsq_ctx* ctx, double* elapsed_ms);
 /* Page-lock caller memory (cudaHostRegister) so sample uploads run at full host-to-device speed. */
 int bsq_host_register(void* ptr, uint64_t bytes);
 int bsq_host_unregister(void* ptr);
+
+/* ---------------------------------------------------------------- serving
+ *
+ * A scoring server over one context: jobs (one sample's reads + reference, both passes) are
+ * submitted from any thread and admitted while the sum of the footprints of admitted jobs stays
+ * within an HBM budget.  An admission thread uploads each admitted job on the context's load
+ * stream while the GPU thread runs the jobs already resident; every round the GPU thread takes all
+ * resident jobs (up to max_batch_jobs) and runs pass 1, the log10 table of each job
+ * (bsq_counts_to_log10_prob) and pass 2 as one batch call per pass.  Jobs that arrive while a round
+ * runs join the next round (continuous batching).  A job's results are the same as those of the
+ * single-sample calls on the same inputs.  breseq itself has no server: this replaces its
+ * per-sample sequence error_count -> error_rates.tab -> identify_mutations
+ * (src/breseq/breseq_cmdline.cpp:2293-2318, :2471) for a caller that scores many samples. */
+
+#define BSQ_ERR_TIMEOUT     -7   /* bsq_server_wait: the job did not finish within the timeout  */
+
+#define BSQ_JOB_QUEUED   0       /* waiting for HBM budget                                     */
+#define BSQ_JOB_LOADING  1       /* admitted, upload in progress                               */
+#define BSQ_JOB_READY    2       /* resident, waiting for the next GPU round                   */
+#define BSQ_JOB_RUNNING  3       /* in the GPU round now                                       */
+#define BSQ_JOB_DONE     4       /* results available; negative = error code                   */
+
+typedef struct bsq_server bsq_server;
+
+typedef struct bsq_job {
+    const bsq_reference* ref;    /* borrowed until the job is done                               */
+    const bsq_read_soa* reads;   /* borrowed until the job is done                               */
+    bsq_ec_params ec;
+    bsq_im_params im;            /* deletion cutoff arrays borrowed until done; precision is the server's */
+    uint32_t hist_capacity;      /* coverage-histogram bins kept per coverage group               */
+} bsq_job;
+
+typedef struct bsq_job_info {
+    int32_t  state;              /* BSQ_JOB_*, or a negative error code                         */
+    uint32_t round_jobs;         /* jobs in the GPU round this job ran in                        */
+    uint64_t footprint;          /* bytes charged against the HBM budget                        */
+    uint64_t n_ra, n_mc, n_un;
+    uint64_t read_bases;         /* aligned read bases of the sample (one pass)                  */
+    double   submit_ms, admit_ms, ready_ms, start_ms, done_ms;   /* since server creation    */
+} bsq_job_info;
+
+typedef struct bsq_server_stats {
+    uint64_t jobs_done, rounds, budget, in_use, peak_in_use;
+    uint32_t max_round_jobs, max_resident_jobs;
+    double   gpu_busy_ms;        /* summed wall time of the GPU rounds                           */
+} bsq_server_stats;
+
+/* Bytes one job holds on the device while admitted: the resident sample plus both passes'
+ * per-column working set. */
+uint64_t bsq_job_footprint(const bsq_reference* ref, const bsq_read_soa* reads);
+
+int  bsq_server_create(bsq_server** out, int device, uint64_t hbm_budget_bytes, uint32_t max_batch_jobs,
+                       int32_t precision);
+/* Waits for every submitted job, then stops the threads. */
+void bsq_server_destroy(bsq_server* srv);
+const char* bsq_server_last_error(const bsq_server* srv);
+/* BSQ_ERR_NOMEM when the job alone exceeds the budget. */
+int  bsq_server_submit(bsq_server* srv, const bsq_job* job, uint64_t* job_id);
+/* Blocks until the job is done or failed (BSQ_OK, info filled) or timeout_ms passes
+ * (BSQ_ERR_TIMEOUT; timeout_ms < 0 waits without limit). */
+int  bsq_server_wait(bsq_server* srv, uint64_t job_id, int64_t timeout_ms, bsq_job_info* info);
+int  bsq_server_job_info(bsq_server* srv, uint64_t job_id, bsq_job_info* info);
+const char* bsq_server_job_error(bsq_server* srv, uint64_t job_id);
+/* Pass-1 results of a done job: counts [R*25*Q], coverage_hist [groups * hist_capacity], hist_size
+ * [groups]; any may be NULL. */
+int  bsq_server_error_counts(bsq_server* srv, uint64_t job_id, uint64_t* counts, uint64_t* coverage_hist,
+                             uint32_t* hist_size);
+/* Pass-2 records of a done job (sizes in bsq_job_info). */
+int  bsq_server_results(bsq_server* srv, uint64_t job_id, bsq_ra_record* ra, uint64_t ra_cap, bsq_mc_record* mc,
+                        uint64_t mc_cap, bsq_un_record* un, uint64_t un_cap);
+/* Forget a done job and its results. */
+int  bsq_server_release(bsq_server* srv, uint64_t job_id);
+int  bsq_server_get_stats(bsq_server* srv, bsq_server_stats* out);
 
 #ifdef __cplusplus
 }

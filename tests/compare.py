@@ -87,3 +87,18 @@ def compare_positions(g, r, exact_scores=False):
         bad = np.nonzero(g["best_base"] != r["best_base"])[0]
         out.append(f"best base differs at {len(bad)} positions, first {bad[:5]}")
     return out
+
+
+def _same(a, b):
+    if isinstance(a, float) and isinstance(b, float):
+        return a == b or (math.isnan(a) and math.isnan(b))
+    if isinstance(a, (list, tuple)) and isinstance(b, (list, tuple)):
+        return len(a) == len(b) and all(_same(x, y) for x, y in zip(a, b))
+    if isinstance(a, dict) and isinstance(b, dict):
+        return a.keys() == b.keys() and all(_same(a[k], b[k]) for k in a)
+    return a == b
+
+
+def identical(a, b):
+    """Exact equality of record lists (bit-identical floats, NaN equal to NaN)."""
+    return _same(a, b)

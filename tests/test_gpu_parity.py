@@ -113,3 +113,50 @@ def test_intervals_with_deletion_cutoffs(scorer, loaded, oracle_results, prop_cu
                                          deletion_seed_cutoff=seed_cutoff, precision=1, positions=positions)
         problems = compare.compare_intervals(im_g, im_o) + compare.compare_ra(im_g["ra"], im_o["ra"])
         assert not problems, "\n".join(problems[:20])
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32c"])
+def test_batch_equals_single_calls(scorer, loaded, oracle_results, precision):
+    """Every sample scored in one batch (one launch per kernel over all samples' tiles) gets the
+    results it gets alone, in both passes, and the oracle's."""
+    from breseq_gb300.api import ImSettings
+    names = list(samples.ALL) + ["clonal_small"]          # a sample may appear twice in one batch
+    sids = [loaded[n] for n in names]
+    cap = max(oracle_results[n][0]["hist"].shape[1] for n in names)
+    ecs = scorer.error_count_batch(sids, hist_capacity=cap)
+    for n, ec in zip(names, ecs):
+        alone = scorer.error_count(loaded[n], hist_capacity=cap)
+        for k in ("counts", "hist", "hist_size"):
+            assert np.array_equal(ec[k], alone[k]), (n, k)
+        assert np.array_equal(ec["counts"], oracle_results[n][0]["counts"])
+    tabs = [oracle_results[n][1] for n in names]
+    sets = [ImSettings(polymorphism_prediction=n in POLY) for n in names]
+    ims = scorer.identify_mutations_batch(sids, tabs, sets, precision=precision, positions=False)
+    for n, im, tab, st in zip(names, ims, tabs, sets):
+        alone = scorer.identify_mutations(loaded[n], tab, st, precision=precision, positions=False)
+        assert all(compare.identical(im[k], alone[k]) for k in ("ra", "mc", "un")), n
+        problems = compare.compare_ra(im["ra"], oracle_results[n][2]["ra"]) + compare.compare_intervals(im, oracle_results[n][2])
+        assert not problems, "\n".join(problems[:20])
+    dense = scorer.identify_mutations_batch(sids[:2], tabs[:2], sets[:2], precision=precision, positions=True)
+    for n, im in zip(names[:2], dense):
+        assert not compare.compare_positions(im["positions"], oracle_results[n][2]["positions"])
+
+
+def test_batch_larger_than_one_launch_group(scorer, loaded, oracle_results):
+    """More samples than one launch carries (64 jobs per kernel parameter block) run as consecutive
+    groups; every job still gets the single-call result."""
+    from breseq_gb300.api import ImSettings
+    names = ["clonal_small", "population_small"] * 35
+    sids = [loaded[n] for n in names]
+    ecs = scorer.error_count_batch(sids)
+    tabs = [oracle_results[n][1] for n in names]
+    sets = [ImSettings(polymorphism_prediction=n in POLY) for n in names]
+    ims = scorer.identify_mutations_batch(sids, tabs, sets, precision=1)
+    for n in set(names):
+        alone_ec = scorer.error_count(loaded[n])
+        alone = scorer.identify_mutations(loaded[n], oracle_results[n][1], ImSettings(polymorphism_prediction=n in POLY),
+                                          precision=1)
+        for i in [i for i, m in enumerate(names) if m == n]:
+            assert np.array_equal(ecs[i]["counts"], alone_ec["counts"]), i
+            assert np.array_equal(ecs[i]["hist"], alone_ec["hist"]), i
+            assert all(compare.identical(ims[i][k], alone[k]) for k in ("ra", "mc", "un")), i
