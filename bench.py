@@ -10,6 +10,14 @@ sample resident in HBM; `e2e` runs the same step through the C ABI from pinned h
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
+Two more legs on rank 0 report the batched and served forms on a mix of samples of uneven shape
+(genome length log-uniform in [40 kb, 6 Mb], 20-500x, reads of 36/101/150 bp, SE/PE, consensus and
+polymorphism modes), drawn from a pool of distinct seeded samples:
+  "batched": all jobs resident, both passes as one batch call per pass (one launch per kernel per
+             64 jobs), against the plain FP64 form run one sample per call;
+  "served":  open-loop Poisson arrivals at 0.5/1/2x the batched capacity into the scoring server
+             (HBM-footprint admission, continuous batching), with p50/p99 job latency.
+
 Under torchrun each rank scores its own sample (weak scaling, no collective in the data path); the
 timed region is bracketed by barriers and the slowest rank's time is used.
 """
@@ -121,17 +129,28 @@ def _workload(seed: int, scale: float = 1.0):
     return synth.simulate(synth.config_ecoli(seed=seed, scale=scale))
 
 
-def _cpu_reference(sample_scale: float, threads: int):
-    """The oracle port of the reference algorithm on a bounded sample of the same workload."""
+_CPU_SAMPLE = {}
+
+
+def _cpu_reference(sample_scale: float, threads: int, min_seconds: float = 0.0):
+    """The oracle port of the reference algorithm on a bounded sample of the same workload, repeated
+    until at least `min_seconds` of CPU work were timed."""
     from oracle import pyoracle as po
-    s = _workload(seed=21, scale=sample_scale)
+    if sample_scale not in _CPU_SAMPLE:
+        _CPU_SAMPLE[sample_scale] = _workload(seed=21, scale=sample_scale)
+    s = _CPU_SAMPLE[sample_scale]
     bases = s.aligned_bases()
+    reps = 0
     t0 = time.perf_counter()
-    ec = po.error_count(s, n_threads=threads)
-    tab = po.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
-    po.identify(s, tab, po.default_im_params(s), n_threads=threads, positions=False)
+    while True:
+        ec = po.error_count(s, n_threads=threads)
+        tab = po.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
+        po.identify(s, tab, po.default_im_params(s), n_threads=threads, positions=False)
+        reps += 1
+        if time.perf_counter() - t0 >= min_seconds:
+            break
     dt = time.perf_counter() - t0
-    return bases / dt, bases, dt, s.total_length()
+    return reps * bases / dt, reps * bases, dt, s.total_length(), reps
 
 
 def run_reference(args, world, rank, pg):
@@ -141,7 +160,7 @@ def run_reference(args, world, rank, pg):
     times = []
     rate = bases = ln = None
     for i in range(args.warmup + args.steps):
-        rate, bases, dt, ln = _cpu_reference(args.cpu_scale, threads)
+        rate, bases, dt, ln, _ = _cpu_reference(args.cpu_scale, threads)
         if i >= args.warmup:
             times.append(dt)
     ms = 1000.0 * statistics.mean(times)
@@ -259,12 +278,120 @@ def run_ours(args, world, rank, local, pg):
         "ra_items": len(im["ra"]),
     }
     if rank == 0 and not args.no_cpu:
-        rate, cb, dt, ln = _cpu_reference(args.cpu_scale, os.cpu_count() or 1)
+        rate, cb, dt, ln, reps = _cpu_reference(args.cpu_scale, os.cpu_count() or 1, args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": f"same workload at {args.cpu_scale:g} x genome length ({ln} bp, {cb} read-bases), {dt:.1f} s"}
+                                "sample": f"same workload at {args.cpu_scale:g} x genome length ({ln} bp), "
+                                          f"{reps} runs, {cb} read-bases in {dt:.1f} s"}
     sc.close()
+    if rank == 0 and args.batch_jobs > 0:
+        line["batched"], line["served"] = run_mix(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def _pool(args):
+    """Distinct seeded samples of the mixed-shape distribution; job i uses pool[i % len(pool)]."""
+    from breseq_gb300 import synth
+    cfgs = synth.config_batch(seed=41, n_samples=max(args.batch_jobs, args.batch_pool), scale=args.batch_scale)
+    return [(synth.simulate(c), poly) for c, poly in cfgs[:args.batch_pool]]
+
+
+def _calls(im):
+    return [(r["tid"], r["position"], r["insert_position"], r["new_base"]) for r in im["ra"]]
+
+
+def run_mix(args, device):
+    from breseq_gb300 import abi
+    from breseq_gb300.api import ImSettings, Scorer, Server
+    pool = _pool(args)
+    P = len(pool)
+    views = [abi.SampleView(s) for s, _ in pool]
+    sc = Scorer(device)
+    pinned = []
+    for v in views:                        # page-locked once: every job's upload is a DMA copy
+        for a in v._keep:
+            if a.nbytes >= 1 << 16 and sc.L.bsq_host_register(a.ctypes.data, a.nbytes) == 0:
+                pinned.append(a)
+    jobs = [i % P for i in range(args.batch_jobs)]
+    sets = [ImSettings(polymorphism_prediction=pool[k][1]) for k in range(P)]
+    pool_bases = [s.aligned_bases() for s, _ in pool]
+    job_bases = sum(pool_bases[k] for k in jobs)
+    cfg = {"workload": "mixed_shapes_genome40k-6Mb_cov20-500_L36/101/150_se/pe_consensus/polymorphism",
+           "jobs": len(jobs), "distinct_samples": P, "genome_scale": args.batch_scale,
+           "genome_bp": [int(s.total_length()) for s, _ in pool], "read_bases_per_step": job_bases}
+    # ---- batched: every job resident, one batch call per pass
+    sids = [sc.load_sample(pool[k][0]) for k in jobs]
+
+    def batch_step():
+        ecs = sc.error_count_batch(sids)
+        tabs = [sc.counts_to_log10_prob(ec["counts"], pool[k][0].n_read_files, pool[k][0].n_quality)
+                for ec, k in zip(ecs, jobs)]
+        return sc.identify_mutations_batch(sids, tabs, [sets[k] for k in jobs], precision=1)
+
+    for _ in range(max(1, args.warmup)):
+        ims = batch_step()
+    sc.timer_start()
+    for _ in range(args.batch_steps):
+        ims = batch_step()
+    batch_ms = sc.timer_stop() / args.batch_steps
+    for sid in sids:
+        sc.free_sample(sid)
+    # ---- plain FP64, one sample per call, each distinct sample once
+    plain_ms = 0.0
+    same = True
+    for k, (s, _) in enumerate(pool):
+        sid = sc.load_sample(s)
+        sc.timer_start()
+        ec = sc.error_count(sid)
+        tab = sc.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
+        im = sc.identify_mutations(sid, tab, sets[k], precision=0)
+        plain_ms += sc.timer_stop()
+        sc.free_sample(sid)
+        same &= _calls(im) == _calls(ims[k])
+    plain_rate = sum(pool_bases) / (plain_ms / 1000.0)
+    batched = {"config": cfg, "ms_per_step": batch_ms, "value": job_bases / (batch_ms / 1000.0), "unit": UNIT,
+               "plain_fp64": {"value": plain_rate, "ms_per_pool_pass": plain_ms,
+                              "batched_over_plain": job_bases / (batch_ms / 1000.0) / plain_rate},
+               "identical_calls": bool(same)}
+    sc.close()
+    # ---- served: open-loop Poisson arrivals into the scoring server
+    cap = len(jobs) / (batch_ms / 1000.0)     # jobs/s the batched form sustains
+    levels = []
+    rng = np.random.default_rng(7)
+    for rho in (0.5, 1.0, 2.0):
+        lam = rho * cap
+        n = args.served_jobs
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, size=n))
+        with Server(device, hbm_budget=args.budget_gb * 1e9, max_batch_jobs=64) as srv:
+            ids = []
+            t0 = time.perf_counter()
+            for i in range(n):
+                d = arrivals[i] - (time.perf_counter() - t0)
+                if d > 0:
+                    time.sleep(d)
+                k = i % P
+                ids.append((srv.submit(pool[k][0], sets[k], view=views[k]), k))
+            infos = [srv.wait(j) for j, _ in ids]
+            st = srv.stats()
+        lat = np.array([i["done_ms"] - i["submit_ms"] for i in infos])
+        stage = {k: float(np.mean([i[b] - i[a] for i in infos])) for k, a, b in
+                 (("queue_ms", "submit_ms", "admit_ms"), ("upload_ms", "admit_ms", "ready_ms"),
+                  ("wait_gpu_ms", "ready_ms", "start_ms"), ("round_ms", "start_ms", "done_ms"))}
+        span = (max(i["done_ms"] for i in infos) - min(i["submit_ms"] for i in infos)) / 1000.0
+        bases = sum(pool_bases[k] for _, k in ids)
+        levels.append({"load": rho, "arrival_rate_jobs_s": lam, "jobs": n, "p50_ms": float(np.percentile(lat, 50)),
+                       "p99_ms": float(np.percentile(lat, 99)), "value": bases / span, "unit": UNIT,
+                       "served_over_plain": bases / span / plain_rate, "max_round_jobs": st["max_round_jobs"],
+                       "max_resident_jobs": st["max_resident_jobs"], "peak_hbm_gb": st["peak_in_use"] / 1e9,
+                       "rounds": st["rounds"], "gpu_busy_frac": st["gpu_busy_ms"] / 1000.0 / span,
+                       "mean_stage_ms": stage})
+    from breseq_gb300 import _lib
+    L = _lib.load()
+    for a in pinned:
+        L.bsq_host_unregister(a.ctypes.data)
+    served = {"capacity_jobs_s": cap, "budget_gb": args.budget_gb, "levels": levels,
+              "p50_ms": levels[1]["p50_ms"], "p99_ms": levels[1]["p99_ms"], "plain_fp64_value": plain_rate}
+    return batched, served
 
 
 def main():
@@ -278,6 +405,13 @@ def main():
     ap.add_argument("--cpu-scale", type=float, default=0.05)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0, help="genome length scale of the workload (profiling cases)")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="minimum CPU work timed for cpu_baseline")
+    ap.add_argument("--batch-jobs", type=int, default=96, help="jobs of the batched / served legs (0: skip them)")
+    ap.add_argument("--batch-pool", type=int, default=16, help="distinct samples the jobs are drawn from")
+    ap.add_argument("--batch-scale", type=float, default=0.25, help="genome length scale of the mixed samples")
+    ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--served-jobs", type=int, default=96)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
     args = ap.parse_args()
     world, rank, local, pg = _dist()
     if args.impl == "reference":

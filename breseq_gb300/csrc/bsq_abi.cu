@@ -9,6 +9,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <atomic>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -68,7 +69,11 @@ struct bsq_ctx {
   int device = 0;
   int sms = 1;
   cudaStream_t stream = nullptr;        // the passes
-  cudaStream_t load_stream = nullptr;   // sample uploads: a loader thread runs them beside the passes
+  // sample uploads run on their own streams, beside the passes; concurrent loads (loader threads)
+  // take the streams round robin
+  static constexpr int kLoadStreams = 4;
+  cudaStream_t load_streams[kLoadStreams] = {};
+  std::atomic<uint32_t> load_rr{0};
   std::mutex mu;                        // guards `samples` and `next_id`
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm0 = nullptr, evm1 = nullptr, evt0 = nullptr, evt1 = nullptr;
   std::map<int32_t, std::unique_ptr<SampleDev>> samples;
@@ -168,7 +173,8 @@ int bsq_create(bsq_ctx** out, int device) {
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return BSQ_ERR_CUDA;
   c->sms = prop.multiProcessorCount;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return BSQ_ERR_CUDA;
-  if (cudaStreamCreateWithFlags(&c->load_stream, cudaStreamNonBlocking) != cudaSuccess) return BSQ_ERR_CUDA;
+  for (cudaStream_t& ls : c->load_streams)
+    if (cudaStreamCreateWithFlags(&ls, cudaStreamNonBlocking) != cudaSuccess) return BSQ_ERR_CUDA;
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
     uint64_t keep = UINT64_MAX;   // keep freed blocks in this process's pool for the next sample
@@ -186,7 +192,7 @@ void bsq_destroy(bsq_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  if (ctx->load_stream) cudaStreamSynchronize(ctx->load_stream);
+  for (cudaStream_t ls : ctx->load_streams) if (ls) cudaStreamSynchronize(ls);
   ctx->samples.clear();
   // pool blocks are returned on the context's stream, so before it goes
   for (DevMem* m : {&ctx->cov, &ctx->call, &ctx->blk, &ctx->total, &ctx->cand, &ctx->next, &ctx->ra, &ctx->n_ra,
@@ -198,9 +204,9 @@ void bsq_destroy(bsq_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   cudaEventDestroy(ctx->ev0); cudaEventDestroy(ctx->ev1); cudaEventDestroy(ctx->evm0); cudaEventDestroy(ctx->evm1);
   cudaEventDestroy(ctx->evt0); cudaEventDestroy(ctx->evt1);
-  if (ctx->load_stream) cudaStreamSynchronize(ctx->load_stream);
+  for (cudaStream_t ls : ctx->load_streams) if (ls) cudaStreamSynchronize(ls);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
-  if (ctx->load_stream) cudaStreamDestroy(ctx->load_stream);
+  for (cudaStream_t ls : ctx->load_streams) if (ls) cudaStreamDestroy(ls);
   delete ctx;
 }
 
@@ -255,7 +261,7 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
     if (ch != 'A' && ch != 'C' && ch != 'G' && ch != 'T' && ch != 'N')
       return fail(ctx, BSQ_ERR_DATA, "reference base outside A/C/G/T/N");
   }
-  cudaStream_t st = ctx->load_stream;
+  cudaStream_t st = ctx->load_streams[ctx->load_rr.fetch_add(1) % bsq_ctx::kLoadStreams];
   // reference, one '\0' separator after each target
   CK(s->ref.alloc(s->n_cols + 64, st));
   CK(cudaMemsetAsync(s->ref.p, 0, s->n_cols + 64, st));

@@ -1,5 +1,5 @@
-// Scoring server: HBM-budget admission, uploads beside the running GPU round, and continuous
-// batching of both passes over the resident jobs.  Built only on the library's C ABI.
+// Scoring server: HBM-budget admission, uploads (several at once) beside the running GPU round,
+// and continuous batching of both passes over the resident jobs.  Built only on the library's C ABI.
 //
 // breseq scores one sample per process, one pass after the other (error_count at
 // src/breseq/breseq_cmdline.cpp:2293, identify_mutations at :2471); a job here is that sequence for
@@ -80,7 +80,9 @@ struct bsq_server {
   double gpu_busy_ms = 0;
   bool stop = false;
   std::string err;
-  std::thread admitter, gpu;
+  static constexpr int kLoaders = 4;   // uploads in flight at once (each on its own load stream)
+  std::vector<std::thread> admitters;
+  std::thread gpu;
 
   double ms(Clock::time_point t) const { return std::chrono::duration<double, std::milli>(t - t0).count(); }
 
@@ -257,7 +259,7 @@ int bsq_server_create(bsq_server** out, int device, uint64_t budget, uint32_t ma
   s->precision = precision;
   s->t0 = Clock::now();
   bsq_server* p = s.get();
-  s->admitter = std::thread([p] { p->admit_loop(); });
+  for (int i = 0; i < bsq_server::kLoaders; i++) s->admitters.emplace_back([p] { p->admit_loop(); });
   s->gpu = std::thread([p] { p->gpu_loop(); });
   *out = s.release();
   return BSQ_OK;
@@ -278,7 +280,7 @@ void bsq_server_destroy(bsq_server* s) {
   }
   s->cv_admit.notify_all();
   s->cv_ready.notify_all();
-  s->admitter.join();
+  for (std::thread& t : s->admitters) t.join();
   s->gpu.join();
   bsq_destroy(s->ctx);
   delete s;

@@ -469,3 +469,31 @@ def config_population(seed=31, scale=1.0, coverage=500.0) -> SimConfig:
     return dataclasses.replace(c, n_snps=max(4, int(360 * scale)), n_indels=max(2, int(40 * scale)),
                                freq_min=0.01, strand_bias_sites=max(1, int(50 * scale)),
                                low_quality_sites=max(1, int(50 * scale)))
+
+
+def config_batch(seed=41, n_samples=96, scale=1.0):
+    """Many samples of uneven shape: genome length log-uniform in [40 kb, 6 Mb], total coverage
+    uniform in [20, 500]x, read length from {36, 101, 150}, single- or paired-end, consensus or
+    polymorphism mode; each sample uses the clonal (planted SNPs and short indels, repeats on
+    genomes of 1 Mb and more) or population (variant frequencies log-uniform in [0.01, 1],
+    strand-biased and low-quality sites) variant model.  `scale` multiplies every genome length
+    (profiling and quick runs).  Returns [(SimConfig, polymorphism_mode)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_samples):
+        g = max(5000, int(np.exp(rng.uniform(np.log(40e3), np.log(6e6))) * scale))
+        cov = float(rng.uniform(20.0, 500.0))
+        L = int(rng.choice([36, 101, 150]))
+        paired = bool(rng.random() < 0.5)
+        poly = bool(rng.random() < 0.5)
+        mb = g / 1e6
+        rs = ReadFileSet(coverage=cov / 2 if paired else cov, read_length=L, paired=paired)
+        c = SimConfig(seed=seed * 1000 + i, target_lengths=(g,), target_names=(f"sample{i}_chr",), gc=0.5,
+                      n_snps=max(5, int(65 * mb)), n_indels=max(2, int(9 * mb)), max_indel=3,
+                      repeat_copies=5 if g >= 1_000_000 else 0, repeat_length=1300, read_sets=(rs,),
+                      chunk_reads=16_000)
+        if poly:
+            c = dataclasses.replace(c, freq_min=0.01, strand_bias_sites=max(1, int(11 * mb)),
+                                    low_quality_sites=max(1, int(11 * mb)))
+        out.append((c, poly))
+    return out
