@@ -40,6 +40,8 @@ sys.path.insert(0, ROOT)
 METRIC = "read-bases/s scored, served vs plain on same GPU (identical calls); p50/p99 ms"
 UNIT = "read-bases/s"
 WORKLOAD = "ecoli_clonal_4.79Mb_pe150_2x100x"
+# the plain FP64 form: same kernels, FP64 everywhere, one sample per call, launched without graphs
+PLAIN_TUNING = dict(ec_read_chunk=1024, ec_blocks_per_sm=8, col_blocks_per_sm=8, cand_warps_per_sm=16, use_graphs=0)
 
 
 def _peaks():
@@ -199,6 +201,9 @@ def run_ours(args, world, rank, local, pg):
             ps = sc.last_pass_stats(); kstats["im"].append(ps["main_kernel_ms"]); launches[0] += ps["kernel_launches"]
         return im
 
+    ec0 = sc.error_count(sid)
+    tab0 = sc.counts_to_log10_prob(ec0["counts"], s.n_read_files, s.n_quality)
+    tuning = sc.autotune([sid], [tab0], st, precision=prec) if not args.no_tune else sc.tuning()
     for _ in range(args.warmup):
         ref_im = step(sid)
     clocks = ClockSampler(local)
@@ -212,7 +217,8 @@ def run_ours(args, world, rank, local, pg):
     clk = clocks.stop()
     ms_max = _max_over_ranks(pg, ms)
     value = world * bases / (ms_max / 1000.0)
-    # ---- plain FP64 form on the same sample (the spec comparison), same calls
+    # ---- plain FP64 form on the same sample, same calls: default launch shapes, no graphs
+    sc.set_tuning(**PLAIN_TUNING)
     t_plain = []
     for i in range(1 + args.plain_steps):
         sc.timer_start()
@@ -226,6 +232,7 @@ def run_ours(args, world, rank, local, pg):
     same_calls = [(r["tid"], r["position"], r["insert_position"], r["new_base"]) for r in im_plain["ra"]] == \
                  [(r["tid"], r["position"], r["insert_position"], r["new_base"]) for r in im["ra"]]
     plain_ms = statistics.mean(t_plain) if t_plain else None
+    sc.set_tuning(**tuning)
     # ---- end to end through the C ABI from pinned host buffers
     view = abi.SampleView(s)
     pinned = []
@@ -275,6 +282,7 @@ def run_ours(args, world, rank, local, pg):
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind},
         "clocks": clk,
+        "tuning": tuning,
         "ra_items": len(im["ra"]),
     }
     if rank == 0 and not args.no_cpu:
@@ -328,6 +336,13 @@ def run_mix(args, device):
                 for ec, k in zip(ecs, jobs)]
         return sc.identify_mutations_batch(sids, tabs, [sets[k] for k in jobs], precision=1)
 
+    if not args.no_tune:
+        ecs = sc.error_count_batch(sids)
+        tabs = [sc.counts_to_log10_prob(ec["counts"], pool[k][0].n_read_files, pool[k][0].n_quality)
+                for ec, k in zip(ecs, jobs)]
+        tuning = sc.autotune(sids, tabs, [sets[k] for k in jobs], precision=1)
+    else:
+        tuning = sc.tuning()
     for _ in range(max(1, args.warmup)):
         ims = batch_step()
     sc.timer_start()
@@ -336,7 +351,8 @@ def run_mix(args, device):
     batch_ms = sc.timer_stop() / args.batch_steps
     for sid in sids:
         sc.free_sample(sid)
-    # ---- plain FP64, one sample per call, each distinct sample once
+    # ---- plain FP64, one sample per call, each distinct sample once, default shapes, no graphs
+    sc.set_tuning(**PLAIN_TUNING)
     plain_ms = 0.0
     same = True
     for k, (s, _) in enumerate(pool):
@@ -352,7 +368,7 @@ def run_mix(args, device):
     batched = {"config": cfg, "ms_per_step": batch_ms, "value": job_bases / (batch_ms / 1000.0), "unit": UNIT,
                "plain_fp64": {"value": plain_rate, "ms_per_pool_pass": plain_ms,
                               "batched_over_plain": job_bases / (batch_ms / 1000.0) / plain_rate},
-               "identical_calls": bool(same)}
+               "identical_calls": bool(same), "tuning": tuning}
     sc.close()
     # ---- served: open-loop Poisson arrivals into the scoring server
     cap = len(jobs) / (batch_ms / 1000.0)     # jobs/s the batched form sustains
@@ -412,6 +428,7 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--served-jobs", type=int, default=96)
     ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     args = ap.parse_args()
     world, rank, local, pg = _dist()
     if args.impl == "reference":

@@ -63,6 +63,10 @@ def load():
     L.bsq_format_ra.argtypes = [C.c_void_p, C.c_char_p, C.c_uint32, C.c_char_p, C.c_uint64]
     L.bsq_write_gd.argtypes = [C.c_char_p, P(abi.Reference), P(C.c_char_p), P(C.c_double), C.c_uint32, C.c_void_p,
                                C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]
+    L.bsq_get_tuning.argtypes = [C.c_void_p, P(abi.Tuning)]
+    L.bsq_set_tuning.argtypes = [C.c_void_p, P(abi.Tuning)]
+    L.bsq_autotune.argtypes = [C.c_void_p, C.c_uint32, P(C.c_int32), P(abi.EcParams), P(abi.ImParams),
+                               P(P(C.c_double)), P(abi.Tuning)]
     L.bsq_job_footprint.argtypes = [P(abi.Reference), P(abi.ReadSoA)]
     L.bsq_job_footprint.restype = C.c_uint64
     L.bsq_server_create.argtypes = [P(C.c_void_p), C.c_int, C.c_uint64, C.c_uint32, C.c_int32]
@@ -88,7 +92,8 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_sample_footprint", "bsq_error_count", "bsq_counts_to_log10_prob", "bsq_identify_mutations",
             "bsq_im_result_counts", "bsq_im_result_copy",
             "bsq_error_count_batch", "bsq_identify_mutations_batch", "bsq_im_batch_result_counts",
-            "bsq_im_batch_result_copy", "bsq_job_footprint", "bsq_server_create", "bsq_server_destroy",
+            "bsq_im_batch_result_copy", "bsq_get_tuning", "bsq_set_tuning", "bsq_autotune",
+            "bsq_job_footprint", "bsq_server_create", "bsq_server_destroy",
             "bsq_server_last_error", "bsq_server_submit", "bsq_server_wait", "bsq_server_job_info",
             "bsq_server_job_error", "bsq_server_error_counts", "bsq_server_results", "bsq_server_release",
             "bsq_server_get_stats", "bsq_last_pass_stats", "bsq_timer_start",

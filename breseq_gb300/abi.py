@@ -160,6 +160,11 @@ def ptr(a: np.ndarray, ctype):
     return a.ctypes.data_as(P(ctype))
 
 
+class Tuning(C.Structure):
+    _fields_ = [("ec_read_chunk", C.c_uint32), ("ec_blocks_per_sm", C.c_uint32), ("col_blocks_per_sm", C.c_uint32),
+                ("cand_warps_per_sm", C.c_uint32), ("use_graphs", C.c_int32)]
+
+
 class Job(C.Structure):
     _fields_ = [("ref", C.POINTER(Reference)), ("reads", C.POINTER(ReadSoA)), ("ec", EcParams), ("im", ImParams),
                 ("hist_capacity", C.c_uint32)]

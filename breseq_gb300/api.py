@@ -208,6 +208,35 @@ class Scorer:
     def identify_mutations(self, sid: int, log10_table, settings: ImSettings | None = None, **kw):
         return self.identify_mutations_batch([sid], [log10_table], settings, **kw)[0]
 
+    # ------------------------------------------------------------------ launch shapes
+    def tuning(self) -> dict:
+        t = abi.Tuning()
+        self._check(self.L.bsq_get_tuning(self.ctx, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in abi.Tuning._fields_}
+
+    def set_tuning(self, **kw):
+        t = abi.Tuning(**{**self.tuning(), **kw})
+        self._check(self.L.bsq_set_tuning(self.ctx, C.byref(t)))
+
+    def autotune(self, sids, log10_tables, settings=None, precision=PRECISION_FP32C) -> dict:
+        """Pick the fastest launch shapes for these resident samples (results are unaffected)."""
+        sids = list(sids)
+        n = len(sids)
+
+        def per(x, j):
+            return x[j] if isinstance(x, (list, tuple)) else x
+
+        ec = [self._ec_job(sid, None, None, True, True, False, 50, 0.1, 8)[0] for sid in sids]
+        im = [self._im_job(sid, per(log10_tables, j), per(settings, j) or ImSettings(), None, None, precision, False,
+                           None, None) for j, sid in enumerate(sids)]
+        ids = (C.c_int32 * n)(*sids)
+        eps = (abi.EcParams * n)(*ec)
+        ips = (abi.ImParams * n)(*[j[0] for j in im])
+        tabs = (C.POINTER(C.c_double) * n)(*[abi.ptr(j[3]["tab"], C.c_double) for j in im])
+        t = abi.Tuning()
+        self._check(self.L.bsq_autotune(self.ctx, n, ids, eps, ips, tabs, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in abi.Tuning._fields_}
+
     def timer_start(self):
         self._check(self.L.bsq_timer_start(self.ctx))
 

@@ -59,9 +59,29 @@ struct SampleDev {
   std::vector<uint8_t> mapq_values; // distinct MAPQ values, index = mapq_idx
 };
 
-// Per-job device buffers of pass 1 and pass 2, kept across calls (pool-backed).
-struct EcBufs { DevMem counts, hist, found, diff_u, diff_r, qs_flag, blk_u, blk_r, err; };
-struct ImBufs { DevMem lp64, r64, lpmax64, lp32, prop, seed, failed, err; };
+// Page-locked host staging: a pass's inputs go to the device in one copy and its small results come
+// back in one copy, both graph-capturable.
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  ~PinnedBuf() { if (p) cudaFreeHost(p); }
+  cudaError_t reserve(size_t n) {
+    if (p && bytes >= n) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    const size_t want = n + n / 4 + 4096;
+    cudaError_t e = cudaMallocHost(&p, want);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+  unsigned char* at(size_t off) const { return static_cast<unsigned char*>(p) + off; }
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 }  // namespace
 
@@ -79,11 +99,13 @@ struct bsq_ctx {
   std::map<int32_t, std::unique_ptr<SampleDev>> samples;
   int32_t next_id = 1;
   // working memory reused across calls
-  DevMem cov, call, blk, total, cand, next, ra, n_ra, qhist, scratch, errw, stats;
+  DevMem cov, call, blk, cand, next, ra, qhist, scratch;
   DevMem keep, kcol, kcov, kcall;
-  DevMem d_chunks;
-  std::vector<std::unique_ptr<EcBufs>> ecb;
-  std::vector<std::unique_ptr<ImBufs>> imb;
+  DevMem d_chunks, ec_arena, im_arena, ctl;
+  PinnedBuf pin_in, pin_out;
+  bsq_tuning tune = {1024, 8, 8, 16, 1};
+  cudaGraphExec_t exec_ec = nullptr, exec_im = nullptr;
+  uint64_t graph_instantiations = 0, graph_updates = 0;
   std::vector<std::vector<bsq_ra_record>> res_ra;
   std::vector<std::vector<bsq_mc_record>> res_mc;
   std::vector<std::vector<bsq_un_record>> res_un;
@@ -156,6 +178,62 @@ static SampleDev* find_sample(bsq_ctx* ctx, int32_t id) {
   return it == ctx->samples.end() ? nullptr : it->second.get();
 }
 
+// Runs `enqueue` on the context's stream.  With graphs on, the work is captured and launched as one
+// CUDA graph; the executable graph is kept and updated in place for the next call of the same shape
+// (the node list of a pass does not depend on the number of jobs), else instantiated anew.
+// Timing event inside a pass: recorded as an event node when the pass is captured (a plain record
+// in a capture only orders the capture and is never recorded).
+static cudaError_t record(cudaEvent_t ev, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+    return cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal);
+  return cudaEventRecord(ev, st);
+}
+
+// Device time between two events of the last pass, 0 when unavailable.
+static float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) { cudaGetLastError(); ms = 0; }
+  return ms;
+}
+
+template <class F>
+static cudaError_t run_pass(bsq_ctx* ctx, cudaGraphExec_t& exec, F&& enqueue, std::string& where) {
+  cudaGetLastError();   // a launch reports through cudaGetLastError: start from a clean slate
+  if (!ctx->tune.use_graphs) { where = "launch"; return enqueue(); }
+  cudaStream_t st = ctx->stream;
+  where = "begin capture";
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  const cudaError_t ee = enqueue();
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(st, &g);
+  if (ee != cudaSuccess || e != cudaSuccess) {
+    where = ee != cudaSuccess ? "capture" : "end capture";
+    if (g) cudaGraphDestroy(g);
+    return ee != cudaSuccess ? ee : e;
+  }
+  if (exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(exec, g, &info) == cudaSuccess) {
+      ctx->graph_updates++;
+    } else {
+      cudaGetLastError();
+      cudaGraphExecDestroy(exec);
+      exec = nullptr;
+    }
+  }
+  if (!exec) {
+    where = "instantiate";
+    e = cudaGraphInstantiate(&exec, g, 0);
+    if (e != cudaSuccess) { exec = nullptr; cudaGraphDestroy(g); return e; }
+    ctx->graph_instantiations++;
+  }
+  cudaGraphDestroy(g);
+  where = "graph launch";
+  return cudaGraphLaunch(exec, st);
+}
+
 extern "C" {
 
 const char* bsq_version(void) { return "breseq_gb300 0.1 (sm_103a)"; }
@@ -195,12 +273,12 @@ void bsq_destroy(bsq_ctx* ctx) {
   for (cudaStream_t ls : ctx->load_streams) if (ls) cudaStreamSynchronize(ls);
   ctx->samples.clear();
   // pool blocks are returned on the context's stream, so before it goes
-  for (DevMem* m : {&ctx->cov, &ctx->call, &ctx->blk, &ctx->total, &ctx->cand, &ctx->next, &ctx->ra, &ctx->n_ra,
-                    &ctx->qhist, &ctx->scratch, &ctx->errw, &ctx->stats, &ctx->keep, &ctx->kcol, &ctx->kcov, &ctx->kcall,
-                    &ctx->d_chunks})
+  for (DevMem* m : {&ctx->cov, &ctx->call, &ctx->blk, &ctx->cand, &ctx->next, &ctx->ra,
+                    &ctx->qhist, &ctx->scratch, &ctx->keep, &ctx->kcol, &ctx->kcov, &ctx->kcall,
+                    &ctx->d_chunks, &ctx->ec_arena, &ctx->im_arena, &ctx->ctl})
     m->release();
-  ctx->ecb.clear();
-  ctx->imb.clear();
+  if (ctx->exec_ec) cudaGraphExecDestroy(ctx->exec_ec);
+  if (ctx->exec_im) cudaGraphExecDestroy(ctx->exec_im);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   cudaEventDestroy(ctx->ev0); cudaEventDestroy(ctx->ev1); cudaEventDestroy(ctx->evm0); cudaEventDestroy(ctx->evm1);
   cudaEventDestroy(ctx->evt0); cudaEventDestroy(ctx->evt1);
@@ -355,9 +433,10 @@ int bsq_free_sample(bsq_ctx* ctx, int32_t id) {
 }
 
 // ============================================================================ pass 1
-static constexpr uint32_t kReadChunk = 1024;   // reads per pass-1 work unit
-
 // One group of at most kBatchJobs samples: one launch per kernel of pass 1.
+//   device arena: [results of every job: counts | coverage hist | read-start tallies | error word]
+//                 [work of every job: coverage difference arrays, read-start flags, block sums]
+// zeroed by one memset; the result part comes back in one copy.
 static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_params* P, bsq_ec_result* out) {
   std::vector<SampleDev*> smp(n);
   for (uint32_t j = 0; j < n; j++) {
@@ -365,102 +444,117 @@ static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_p
     if (!smp[j]) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
     if (P[j].n_read_files == 0 || P[j].n_read_files > 255 || P[j].n_quality == 0 || P[j].n_quality > 256)
       return fail(ctx, BSQ_ERR_INVALID, "covariate dimensions out of range");
+    if ((size_t)P[j].n_read_files * 25 * P[j].n_quality * 4 > kEcMaxHistBytes)
+      return fail(ctx, BSQ_ERR_SIZE, "covariate table larger than the shared-memory histogram of the pass-1 kernel");
   }
   CK(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
-  while (ctx->ecb.size() < n) ctx->ecb.emplace_back(new EcBufs());
-  std::vector<DevJob> jobs(n);
+  const bsq_tuning& tn = ctx->tune;
+  struct Lay { size_t counts, hist, found, err, diff_u, diff_r, qs, blk_u, blk_r; uint32_t cap; };
+  std::vector<Lay> lay(n);
   std::vector<uint32_t> cblk(n + 1, 0);
-  std::vector<uint4> chunks;
+  size_t off = 0;
   uint32_t max_bins = 0;
   for (uint32_t j = 0; j < n; j++) {
-    SampleDev* s = smp[j];
-    EcBufs& E = *ctx->ecb[j];
-    const uint32_t R = P[j].n_read_files, Q = P[j].n_quality, G = s->n_groups;
-    const size_t nbins = (size_t)R * 25 * Q;
-    const uint32_t cap = s->max_tile_reads + 2;
-    const uint32_t ncb = (s->n_cols + 1023) / 1024;
+    const SampleDev* s = smp[j];
+    const size_t nbins = (size_t)P[j].n_read_files * 25 * P[j].n_quality;
     max_bins = std::max<uint32_t>(max_bins, (uint32_t)nbins);
-    CK(E.counts.alloc(nbins * 8, st));
-    CK(E.hist.alloc((size_t)G * cap * 8, st));
-    CK(E.found.alloc((size_t)s->n_targets * 16 + 16, st));
-    CK(E.err.alloc(16, st));
-    CK(E.diff_u.alloc((size_t)(s->n_cols + 16) * 4, st));
-    CK(E.diff_r.alloc((size_t)(s->n_cols + 16) * 4, st));
-    CK(E.qs_flag.alloc((size_t)2 * s->n_cols + 16, st));
-    CK(E.blk_u.alloc((size_t)(ncb + 16) * 4, st));
-    CK(E.blk_r.alloc((size_t)(ncb + 16) * 4, st));
-    CK(cudaMemsetAsync(E.counts.p, 0, nbins * 8, st));
-    CK(cudaMemsetAsync(E.hist.p, 0, (size_t)G * cap * 8, st));
-    CK(cudaMemsetAsync(E.found.p, 0, (size_t)s->n_targets * 16 + 16, st));
-    CK(cudaMemsetAsync(E.err.p, 0, 16, st));
-    CK(cudaMemsetAsync(E.diff_u.p, 0, (size_t)(s->n_cols + 16) * 4, st));
-    CK(cudaMemsetAsync(E.diff_r.p, 0, (size_t)(s->n_cols + 16) * 4, st));
-    if (P[j].preprocess_stage) CK(cudaMemsetAsync(E.qs_flag.p, 0, (size_t)2 * s->n_cols + 16, st));
-    DevJob& J = jobs[j];
-    memset(&J, 0, sizeof J);
-    J.S = make_dev_sample(*s);
-    EcArgs& A = J.E;
-    A.counts = E.counts.as<unsigned long long>(); A.cov_hist = E.hist.as<unsigned long long>();
-    A.found = E.found.as<unsigned long long>(); A.err = E.err.as<uint32_t>();
-    A.R = R; A.Q = Q; A.hist_cap = cap;
-    A.do_errors = P[j].do_errors; A.preprocess = P[j].preprocess_stage;
-    A.unmatched_min_len = P[j].unmatched_end_minimum_read_length;
-    A.unmatched_factor = (float)P[j].unmatched_end_length_factor;
-    A.unmatched_factor_d = P[j].unmatched_end_length_factor;
-    A.flush_tiles = 1;
-    A.diff_u = E.diff_u.as<int32_t>(); A.diff_r = E.diff_r.as<int32_t>(); A.qs_flag = E.qs_flag.as<uint8_t>();
-    A.blk_u = E.blk_u.as<uint32_t>(); A.blk_r = E.blk_r.as<uint32_t>();
-    cblk[j + 1] = cblk[j] + ncb;
-    for (uint32_t r0 = 0; r0 < s->n_reads; r0 += kReadChunk)
-      chunks.push_back(make_uint4(j, r0, std::min<uint32_t>(s->n_reads, r0 + kReadChunk), 0));
+    lay[j].cap = s->max_tile_reads + 2;
+    lay[j].counts = off; off = align256(off + nbins * 8);
+    lay[j].hist = off; off = align256(off + (size_t)s->n_groups * lay[j].cap * 8);
+    lay[j].found = off; off = align256(off + (size_t)s->n_targets * 16);
+    lay[j].err = off; off = align256(off + 8);
   }
-  CK(upload(ctx->d_chunks, chunks.data(), chunks.size(), st));
+  const size_t res_bytes = off;
+  for (uint32_t j = 0; j < n; j++) {
+    const SampleDev* s = smp[j];
+    const uint32_t ncb = (s->n_cols + 1023) / 1024;
+    lay[j].diff_u = off; off = align256(off + (size_t)(s->n_cols + 16) * 4);
+    lay[j].diff_r = off; off = align256(off + (size_t)(s->n_cols + 16) * 4);
+    lay[j].qs = off; off = align256(off + (size_t)2 * s->n_cols + 16);
+    lay[j].blk_u = off; off = align256(off + (size_t)(ncb + 16) * 4);
+    lay[j].blk_r = off; off = align256(off + (size_t)(ncb + 16) * 4);
+    cblk[j + 1] = cblk[j] + ncb;
+  }
+  const size_t arena_bytes = off;
+  CK(ctx->ec_arena.alloc(arena_bytes, st));
+  unsigned char* A0 = ctx->ec_arena.as<unsigned char>();
+  // work units: chunks of reads, tuned size
+  const uint32_t chunk = std::max<uint32_t>(64, tn.ec_read_chunk);
+  size_t n_chunks = 0;
+  for (uint32_t j = 0; j < n; j++) n_chunks += (smp[j]->n_reads + chunk - 1) / chunk;
+  CK(ctx->pin_in.reserve(std::max<size_t>(16, n_chunks * sizeof(uint4))));
+  CK(ctx->pin_out.reserve(res_bytes));
+  CK(ctx->d_chunks.alloc(std::max<size_t>(16, n_chunks * sizeof(uint4)), st));
   CK(ctx->next.alloc(16, st));
+  uint4* ch = reinterpret_cast<uint4*>(ctx->pin_in.p);
+  size_t c = 0;
   std::unique_ptr<Batch> Bp(new Batch());
   Batch& B = *Bp;
   memset(&B, 0, sizeof B);
   B.n_jobs = n;
   B.total_cblk = cblk[n];
-  for (uint32_t j = 0; j < n; j++) B.jobs[j] = jobs[j];
-  for (uint32_t j = 0; j <= n; j++) B.cblk_begin[j] = cblk[j];
-  CK(cudaEventRecord(ctx->ev0, st));
-  CK(launch_ec(B, ctx->d_chunks.as<uint4>(), (uint32_t)chunks.size(), ctx->next.as<unsigned int>(), max_bins, ctx->sms, st,
-               ctx->evm0, ctx->evm1));
-  std::vector<std::vector<unsigned long long>> counts(n), hist(n), found(n);
-  std::vector<uint32_t> err(n, 0);
   for (uint32_t j = 0; j < n; j++) {
-    EcBufs& E = *ctx->ecb[j];
-    counts[j].resize((size_t)P[j].n_read_files * 25 * P[j].n_quality);
-    hist[j].resize((size_t)smp[j]->n_groups * (smp[j]->max_tile_reads + 2));
-    found[j].resize((size_t)smp[j]->n_targets * 2);
-    CK(cudaMemcpyAsync(counts[j].data(), E.counts.p, counts[j].size() * 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(hist[j].data(), E.hist.p, hist[j].size() * 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(found[j].data(), E.found.p, found[j].size() * 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&err[j], E.err.p, 4, cudaMemcpyDeviceToHost, st));
+    const SampleDev* s = smp[j];
+    for (uint32_t r0 = 0; r0 < s->n_reads; r0 += chunk) ch[c++] = make_uint4(j, r0, std::min<uint32_t>(s->n_reads, r0 + chunk), 0);
+    DevJob& J = B.jobs[j];
+    J.S = make_dev_sample(*s);
+    EcArgs& E = J.E;
+    E.counts = reinterpret_cast<unsigned long long*>(A0 + lay[j].counts);
+    E.cov_hist = reinterpret_cast<unsigned long long*>(A0 + lay[j].hist);
+    E.found = reinterpret_cast<unsigned long long*>(A0 + lay[j].found);
+    E.err = reinterpret_cast<uint32_t*>(A0 + lay[j].err);
+    E.R = P[j].n_read_files; E.Q = P[j].n_quality; E.hist_cap = lay[j].cap;
+    E.do_errors = P[j].do_errors; E.preprocess = P[j].preprocess_stage;
+    E.unmatched_min_len = P[j].unmatched_end_minimum_read_length;
+    E.unmatched_factor = (float)P[j].unmatched_end_length_factor;
+    E.unmatched_factor_d = P[j].unmatched_end_length_factor;
+    E.flush_tiles = 1;
+    E.diff_u = reinterpret_cast<int32_t*>(A0 + lay[j].diff_u);
+    E.diff_r = reinterpret_cast<int32_t*>(A0 + lay[j].diff_r);
+    E.qs_flag = A0 + lay[j].qs;
+    E.blk_u = reinterpret_cast<uint32_t*>(A0 + lay[j].blk_u);
+    E.blk_r = reinterpret_cast<uint32_t*>(A0 + lay[j].blk_r);
   }
-  CK(cudaEventRecord(ctx->ev1, st));
+  for (uint32_t j = 0; j <= n; j++) B.cblk_begin[j] = cblk[j];
+  CK(prepare_ec(max_bins));
+  const int grid = ec_grid((uint32_t)n_chunks, ctx->sms, tn.ec_blocks_per_sm);
+  std::string where, step;
+  const cudaError_t pe = run_pass(ctx, ctx->exec_ec, [&]() -> cudaError_t {
+    cudaError_t e;
+    if ((e = record(ctx->ev0, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(ctx->d_chunks.p, ctx->pin_in.p, std::max<size_t>(16, n_chunks * sizeof(uint4)),
+                             cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(A0, 0, arena_bytes, st)) != cudaSuccess) return e;
+    if ((e = launch_ec(B, ctx->d_chunks.as<uint4>(), (uint32_t)n_chunks, ctx->next.as<unsigned int>(), max_bins, grid, st,
+                       ctx->evm0, ctx->evm1)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(ctx->pin_out.p, A0, res_bytes, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    return record(ctx->ev1, st);
+  }, where);
+  if (pe != cudaSuccess) return fail(ctx, BSQ_ERR_CUDA, "error_count pass (" + where + "): " + cudaGetErrorString(pe));
   CK(cudaStreamSynchronize(st));
-  float ms = 0, mms = 0;
-  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-  cudaEventElapsedTime(&mms, ctx->evm0, ctx->evm1);
+  const float ms = elapsed(ctx->ev0, ctx->ev1), mms = elapsed(ctx->evm0, ctx->evm1);
   ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 4;
   int rc = BSQ_OK;
   for (uint32_t j = 0; j < n; j++) {
-    if (err[j]) return fail(ctx, BSQ_ERR_DATA, "error_count: " + err_text(err[j]));
-    SampleDev* s = smp[j];
+    const uint32_t err = *reinterpret_cast<const uint32_t*>(ctx->pin_out.at(lay[j].err));
+    if (err) return fail(ctx, BSQ_ERR_DATA, "error_count: " + err_text(err));
+    const SampleDev* s = smp[j];
+    const uint64_t* counts = reinterpret_cast<const uint64_t*>(ctx->pin_out.at(lay[j].counts));
+    const uint64_t* hist = reinterpret_cast<const uint64_t*>(ctx->pin_out.at(lay[j].hist));
+    const uint64_t* found = reinterpret_cast<const uint64_t*>(ctx->pin_out.at(lay[j].found));
     bsq_ec_result* o = &out[j];
-    const size_t nbins = counts[j].size();
-    if (o->counts) for (size_t i = 0; i < nbins; i++) o->counts[i] = P[j].do_errors ? counts[j][i] : 0;
-    const uint32_t cap = s->max_tile_reads + 2;
+    const size_t nbins = (size_t)P[j].n_read_files * 25 * P[j].n_quality;
+    if (o->counts) for (size_t i = 0; i < nbins; i++) o->counts[i] = P[j].do_errors ? counts[i] : 0;
+    const uint32_t cap = lay[j].cap;
     for (uint32_t g = 0; g < s->n_groups; g++) {
       uint32_t size = 0;
-      for (uint32_t i = 0; i < cap; i++) if (hist[j][(size_t)g * cap + i]) size = i + 1;
+      for (uint32_t i = 0; i < cap; i++) if (hist[(size_t)g * cap + i]) size = i + 1;
       if (!P[j].do_coverage) size = 0;
       if (o->hist_size) o->hist_size[g] = size;
       if (o->coverage_hist) {
         for (uint32_t i = 0; i < o->hist_capacity; i++)
-          o->coverage_hist[(size_t)g * o->hist_capacity + i] = (i < size) ? hist[j][(size_t)g * cap + i] : 0;
+          o->coverage_hist[(size_t)g * o->hist_capacity + i] = (i < size) ? hist[(size_t)g * cap + i] : 0;
         if (size > o->hist_capacity) rc = BSQ_ERR_SIZE;
       }
     }
@@ -468,8 +562,8 @@ static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_p
       for (uint32_t t = 0; t < s->n_targets; t++) o->no_pos_hash_pr[t] = 1.0;
       if (P[j].preprocess_stage)
         for (uint32_t t : s->order) {
-          const double tot = (double)(found[j][2 * t] + found[j][2 * t + 1]);
-          o->no_pos_hash_pr[t] = (tot != 0) ? (double)found[j][2 * t] / tot : 1.0;
+          const double tot = (double)(found[2 * t] + found[2 * t + 1]);
+          o->no_pos_hash_pr[t] = (tot != 0) ? (double)found[2 * t] / tot : 1.0;
         }
     }
   }
@@ -498,7 +592,12 @@ int bsq_counts_to_log10_prob(const uint64_t* counts, uint32_t R, uint32_t Q, dou
 }
 
 // ============================================================================ pass 2
+// Control words of pass 2, written on the device and read back in one copy.
+enum : uint32_t { kCtlCand = 0, kCtlKept = 1, kCtlRa = 2, kCtlCandErr = 3, kCtlJobErr = 8, kCtlWords = 8 + kBatchJobs };
+
 // One group of at most kBatchJobs samples; results go to res_*[job0 + j].
+//   device arena: per job the likelihood-class table (lp64 | r64 | lpmax64 | lp32) and the per-target
+//   deletion cutoffs and failed-fit flags, staged on the host and sent in one copy.
 static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_params* P,
                     const double* const* tables, bsq_position_arrays* const* pos_out, uint32_t job0) {
   std::vector<SampleDev*> smp(n);
@@ -513,50 +612,85 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
   }
   CK(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
-  while (ctx->imb.size() < n) ctx->imb.emplace_back(new ImBufs());
-  std::vector<DevJob> jobs(n);
+  const bsq_tuning& tn = ctx->tune;
+  // likelihood classes, computed on the host exactly as fill_read_base_likelihoods does
+  std::vector<host::ClassTableHost> ct(n);
+  struct Lay { size_t lp64, r64, lpmax64, lp32, prop, seed, failed; };
+  std::vector<Lay> lay(n);
   std::vector<uint32_t> tile_b(n + 1, 0), col_b(n + 1, 0);
   uint32_t max_K = 0, per_warp = 32, Qh = 0;
+  size_t off = 0;
   for (uint32_t j = 0; j < n; j++) {
-    SampleDev* s = smp[j];
-    ImBufs& I = *ctx->imb[j];
-    // likelihood classes, computed on the host exactly as fill_read_base_likelihoods does
-    host::ClassTableHost ct;
-    host::build_class_table(tables[j], P[j].n_read_files, P[j].n_quality, s->mapq_values, ct);
-    CK(upload(I.lp64, ct.lp64.data(), ct.lp64.size(), st));
-    CK(upload(I.r64, ct.r64.data(), ct.r64.size(), st));
-    CK(upload(I.lpmax64, ct.lpmax64.data(), ct.lpmax64.size(), st));
-    CK(upload(I.lp32, ct.lp32.data(), ct.lp32.size(), st));
-    CK(upload(I.prop, P[j].deletion_propagation_cutoff, s->n_targets, st));
-    CK(upload(I.seed, P[j].deletion_seed_cutoff, s->n_targets, st));
-    CK(I.err.alloc(16, st));
-    CK(cudaMemsetAsync(I.err.p, 0, 16, st));
-    // per job, not per sample: one sample may sit in a batch twice with different cutoffs
-    std::vector<uint8_t> failed(s->n_targets);
-    for (uint32_t t = 0; t < s->n_targets; t++) failed[t] = P[j].deletion_propagation_cutoff[t] < 0.0;
-    CK(upload(I.failed, failed.data(), s->n_targets, st));
-    DevJob& J = jobs[j];
-    memset(&J, 0, sizeof J);
-    J.S = make_dev_sample(*s);
-    J.S.tgt_failed = I.failed.as<uint8_t>();
-    J.T.lp64 = I.lp64.as<double>(); J.T.r64 = I.r64.as<double>(); J.T.lpmax64 = I.lpmax64.as<double>();
-    J.T.lp32 = I.lp32.as<float>(); J.T.K = ct.K; J.T.R = P[j].n_read_files; J.T.Q = P[j].n_quality;
-    J.T.n_mapq = (uint32_t)s->mapq_values.size();
-    J.prop = I.prop.as<double>(); J.seed = I.seed.as<double>();
-    J.col_begin = col_b[j]; J.tile_begin = tile_b[j];
+    const SampleDev* s = smp[j];
+    host::build_class_table(tables[j], P[j].n_read_files, P[j].n_quality, s->mapq_values, ct[j]);
+    lay[j].lp64 = off; off = align256(off + ct[j].lp64.size() * 8);
+    lay[j].r64 = off; off = align256(off + ct[j].r64.size() * 8);
+    lay[j].lpmax64 = off; off = align256(off + ct[j].lpmax64.size() * 8);
+    lay[j].lp32 = off; off = align256(off + ct[j].lp32.size() * 4);
+    lay[j].prop = off; off = align256(off + (size_t)s->n_targets * 8);
+    lay[j].seed = off; off = align256(off + (size_t)s->n_targets * 8);
+    lay[j].failed = off; off = align256(off + s->n_targets);
     col_b[j + 1] = col_b[j] + s->n_cols;
     tile_b[j + 1] = tile_b[j] + s->n_tiles;
-    max_K = std::max(max_K, ct.K);
+    max_K = std::max(max_K, ct[j].K);
     per_warp = std::max<uint32_t>(per_warp, s->max_tile_reads);
     Qh = std::max(Qh, P[j].n_quality);
   }
+  const size_t arena_bytes = std::max<size_t>(off, 256);
   const uint32_t total_cols = col_b[n];
+  // ---- every device buffer before anything is enqueued (nothing allocates inside a capture)
+  CK(ctx->pin_in.reserve(arena_bytes));
+  CK(ctx->pin_out.reserve(kCtlWords * 4));
+  CK(ctx->im_arena.alloc(arena_bytes, st));
+  CK(ctx->ctl.alloc(kCtlWords * 4, st));
   CK(ctx->cov.alloc((size_t)total_cols * sizeof(ColCov), st));
   CK(ctx->call.alloc((size_t)total_cols * sizeof(ColCall), st));
+  const uint32_t nblk = (total_cols + 255) / 256;
+  CK(ctx->blk.alloc((size_t)nblk * 4 + 16, st));
+  CK(ctx->cand.alloc((size_t)total_cols * 4 + 16, st));
+  CK(ctx->next.alloc(16, st));
+  const int n_warps = ctx->sms * (int)std::max<uint32_t>(1, tn.cand_warps_per_sm);
+  CK(ctx->scratch.alloc((size_t)n_warps * cand_warp_stride(per_warp) * sizeof(uint4), st));
+  uint32_t ra_cap = 4096 + total_cols / 64;
+  CK(ctx->ra.alloc((size_t)ra_cap * sizeof(RaDev), st));
+  CK(ctx->qhist.alloc((size_t)ra_cap * 2 * Qh * 4, st));
+  CK(ctx->keep.alloc(total_cols + 16, st));
+  CK(ctx->kcol.alloc((size_t)total_cols * 4 + 16, st));
+  CK(ctx->kcov.alloc((size_t)total_cols * sizeof(ColCov) + 16, st));
+  CK(ctx->kcall.alloc((size_t)total_cols * sizeof(ColCall) + 16, st));
+  unsigned char* A0 = ctx->im_arena.as<unsigned char>();
+  uint32_t* ctl = ctx->ctl.as<uint32_t>();
+  std::unique_ptr<Batch> Bp(new Batch());
+  Batch& B = *Bp;
+  memset(&B, 0, sizeof B);
+  B.n_jobs = n;
+  B.total_tiles = tile_b[n]; B.total_cols = total_cols;
+  for (uint32_t j = 0; j <= n; j++) { B.tile_begin[j] = tile_b[j]; B.col_begin[j] = col_b[j]; }
   for (uint32_t j = 0; j < n; j++) {
-    ImArgs& A = jobs[j].I;
+    const SampleDev* s = smp[j];
+    memcpy(ctx->pin_in.at(lay[j].lp64), ct[j].lp64.data(), ct[j].lp64.size() * 8);
+    memcpy(ctx->pin_in.at(lay[j].r64), ct[j].r64.data(), ct[j].r64.size() * 8);
+    memcpy(ctx->pin_in.at(lay[j].lpmax64), ct[j].lpmax64.data(), ct[j].lpmax64.size() * 8);
+    memcpy(ctx->pin_in.at(lay[j].lp32), ct[j].lp32.data(), ct[j].lp32.size() * 4);
+    memcpy(ctx->pin_in.at(lay[j].prop), P[j].deletion_propagation_cutoff, (size_t)s->n_targets * 8);
+    memcpy(ctx->pin_in.at(lay[j].seed), P[j].deletion_seed_cutoff, (size_t)s->n_targets * 8);
+    // per job, not per sample: one sample may sit in a batch twice with different cutoffs
+    for (uint32_t t = 0; t < s->n_targets; t++) ctx->pin_in.at(lay[j].failed)[t] = P[j].deletion_propagation_cutoff[t] < 0.0;
+    DevJob& J = B.jobs[j];
+    J.S = make_dev_sample(*s);
+    J.S.tgt_failed = A0 + lay[j].failed;
+    J.T.lp64 = reinterpret_cast<const double*>(A0 + lay[j].lp64);
+    J.T.r64 = reinterpret_cast<const double*>(A0 + lay[j].r64);
+    J.T.lpmax64 = reinterpret_cast<const double*>(A0 + lay[j].lpmax64);
+    J.T.lp32 = reinterpret_cast<const float*>(A0 + lay[j].lp32);
+    J.T.K = ct[j].K; J.T.R = P[j].n_read_files; J.T.Q = P[j].n_quality;
+    J.T.n_mapq = (uint32_t)s->mapq_values.size();
+    J.prop = reinterpret_cast<const double*>(A0 + lay[j].prop);
+    J.seed = reinterpret_cast<const double*>(A0 + lay[j].seed);
+    J.col_begin = col_b[j]; J.tile_begin = tile_b[j];
+    ImArgs& A = J.I;
     A.cov = ctx->cov.as<ColCov>() + col_b[j]; A.call = ctx->call.as<ColCall>() + col_b[j];
-    A.err = ctx->imb[j]->err.as<uint32_t>();
+    A.err = ctl + kCtlJobErr + j;
     A.base_quality_cutoff = P[j].base_quality_cutoff;
     A.precision = P[j].precision;
     A.log10_ref_len = P[j].log10_ref_length;
@@ -566,75 +700,73 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
     A.guard = 2e-6f;
     A.precision_decimal = P[j].polymorphism_precision_decimal;
   }
-  std::unique_ptr<Batch> Bp(new Batch());
-  Batch& B = *Bp;
-  memset(&B, 0, sizeof B);
-  B.n_jobs = n;
-  B.total_tiles = tile_b[n]; B.total_cols = total_cols;
-  for (uint32_t j = 0; j < n; j++) B.jobs[j] = jobs[j];
-  for (uint32_t j = 0; j <= n; j++) { B.tile_begin[j] = tile_b[j]; B.col_begin[j] = col_b[j]; }
-  const uint32_t nblk = (total_cols + 255) / 256;
-  CK(ctx->blk.alloc((size_t)nblk * 4 + 16, st));
-  CK(ctx->total.alloc(16, st));
-  CK(ctx->cand.alloc((size_t)total_cols * 4 + 16, st));
-  CK(ctx->next.alloc(16, st));
-  CK(ctx->n_ra.alloc(16, st));
-  CK(ctx->errw.alloc(16, st));
-  CK(cudaMemsetAsync(ctx->errw.p, 0, 16, st));
-  const int n_warps = ctx->sms * 16;
-  CK(ctx->scratch.alloc((size_t)n_warps * cand_warp_stride(per_warp) * sizeof(uint4), st));
-  uint32_t ra_cap = 4096 + total_cols / 64;
-  CK(cudaEventRecord(ctx->ev0, st));
-  CK(cudaEventRecord(ctx->evm0, st));
-  CK(launch_im_column(B, P[0].precision, ctx->sms, st));
-  CK(cudaEventRecord(ctx->evm1, st));
-  CK(launch_compact(ctx->call.as<ColCall>(), total_cols, ctx->blk.as<uint32_t>(), ctx->total.as<uint32_t>(),
-                    ctx->cand.as<uint32_t>(), st));
-  // ---- candidate columns: FP64 EM, presence score, bounds (the count stays on the device)
-  uint32_t n_ra = 0;
-  for (int attempt = 0; attempt < 4; attempt++) {
+  CandArgs C;
+  memset(&C, 0, sizeof C);
+  C.cand = ctx->cand.as<uint32_t>(); C.n_cand_dev = ctl + kCtlCand; C.next = ctx->next.as<unsigned int>();
+  C.ra = ctx->ra.as<RaDev>(); C.n_ra = ctl + kCtlRa; C.ra_cap = ra_cap;
+  C.scratch = ctx->scratch.as<uint4>(); C.scratch_per_warp = per_warp; C.err = ctl + kCtlCandErr;
+  C.Qhist = Qh; C.qhist = ctx->qhist.as<uint32_t>();
+  const int col_grid = column_grid(B.total_tiles, ctx->sms, tn.col_blocks_per_sm);
+  const uint32_t* ctl_host = reinterpret_cast<const uint32_t*>(ctx->pin_out.p);
+  // ---- the device part of the pass: column scores -> candidates -> EM -> interval marks
+  std::string where, step;
+  const cudaError_t pe = run_pass(ctx, ctx->exec_im, [&]() -> cudaError_t {
+    cudaError_t e;
+    step = "ev0";
+    if ((e = record(ctx->ev0, st)) != cudaSuccess) return e;
+    step = "arena copy";
+    if ((e = cudaMemcpyAsync(A0, ctx->pin_in.p, arena_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    step = "control words";
+    if ((e = cudaMemsetAsync(ctl, 0, kCtlWords * 4, st)) != cudaSuccess) return e;
+    if ((e = record(ctx->evm0, st)) != cudaSuccess) return e;
+    step = "column kernel";
+    if ((e = launch_im_column(B, P[0].precision, col_grid, st)) != cudaSuccess) return e;
+    if ((e = record(ctx->evm1, st)) != cudaSuccess) return e;
+    step = "compaction";
+    if ((e = launch_compact(ctx->call.as<ColCall>(), total_cols, ctx->blk.as<uint32_t>(), ctl + kCtlCand,
+                            ctx->cand.as<uint32_t>(), st)) != cudaSuccess) return e;
+    step = "candidate kernel";
+    if ((e = launch_candidates(B, C, max_K, n_warps, st)) != cudaSuccess) return e;
+    step = "interval kernels";
+    if ((e = launch_intervals(B, ctx->cov.as<ColCov>(), ctx->call.as<ColCall>(), ctx->keep.as<uint8_t>(),
+                              ctx->blk.as<uint32_t>(), ctl + kCtlKept, ctx->kcol.as<uint32_t>(), ctx->kcov.as<ColCov>(),
+                              ctx->kcall.as<ColCall>(), st)) != cudaSuccess) return e;
+    step = "control copy";
+    if ((e = cudaMemcpyAsync(ctx->pin_out.p, ctl, kCtlWords * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    step = "ev1";
+    return record(ctx->ev1, st);
+  }, where);
+  if (pe != cudaSuccess)
+    return fail(ctx, BSQ_ERR_CUDA, "identify_mutations pass (" + where + (where == "capture" ? ": " + step : "") +
+                                       "): " + cudaGetErrorString(pe));
+  CK(cudaStreamSynchronize(st));
+  const float ms = elapsed(ctx->ev0, ctx->ev1), mms = elapsed(ctx->evm0, ctx->evm1);
+  // more RA items than the buffer holds: rerun the candidate kernel alone with room for all
+  for (int attempt = 0; attempt < 3 && ctl_host[kCtlRa] > ra_cap; attempt++) {
+    ra_cap = ctl_host[kCtlRa] + 1024;
     CK(ctx->ra.alloc((size_t)ra_cap * sizeof(RaDev), st));
     CK(ctx->qhist.alloc((size_t)ra_cap * 2 * Qh * 4, st));
-    CK(cudaMemsetAsync(ctx->n_ra.p, 0, 16, st));
-    CandArgs C;
-    memset(&C, 0, sizeof C);
-    C.cand = ctx->cand.as<uint32_t>(); C.n_cand_dev = ctx->total.as<uint32_t>(); C.next = ctx->next.as<unsigned int>();
-    C.ra = ctx->ra.as<RaDev>(); C.n_ra = ctx->n_ra.as<unsigned int>(); C.ra_cap = ra_cap;
-    C.scratch = ctx->scratch.as<uint4>(); C.scratch_per_warp = per_warp; C.err = ctx->errw.as<uint32_t>();
-    C.Qhist = Qh; C.qhist = ctx->qhist.as<uint32_t>();
+    C.ra = ctx->ra.as<RaDev>(); C.ra_cap = ra_cap; C.qhist = ctx->qhist.as<uint32_t>();
+    CK(cudaMemsetAsync(ctl + kCtlRa, 0, 8, st));   // RA count and the candidate error word
     CK(launch_candidates(B, C, max_K, n_warps, st));
-    CK(cudaMemcpyAsync(&n_ra, ctx->n_ra.p, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(ctx->pin_out.p, ctl, kCtlWords * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (n_ra <= ra_cap) break;
-    uint32_t e = 0;
-    CK(cudaMemcpy(&e, ctx->errw.p, 4, cudaMemcpyDeviceToHost));
-    e &= ~kErrRaOverflow;
-    CK(cudaMemcpy(ctx->errw.p, &e, 4, cudaMemcpyHostToDevice));
-    ra_cap = n_ra + 1024;
   }
-  uint32_t n_cand = 0;
-  CK(cudaMemcpyAsync(&n_cand, ctx->total.p, 4, cudaMemcpyDeviceToHost, st));
+  const uint32_t n_cand = ctl_host[kCtlCand], nk = ctl_host[kCtlKept], n_ra = ctl_host[kCtlRa];
+  const uint32_t cerr = ctl_host[kCtlCandErr];
+  ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 9;
+  ctx->last_candidates += n_cand;
+  if (n_ra > ra_cap) return fail(ctx, BSQ_ERR_NOMEM, "identify_mutations: RA buffer overflow");
+  if (cerr & ~kErrRaOverflow) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(cerr));
+  for (uint32_t j = 0; j < n; j++)
+    if (ctl_host[kCtlJobErr + j]) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(ctl_host[kCtlJobErr + j]));
+  // ---- variable-size results
   std::vector<RaDev> ra(n_ra);
   std::vector<uint32_t> qh((size_t)n_ra * 2 * Qh);
   if (n_ra) {
     CK(cudaMemcpyAsync(ra.data(), ctx->ra.p, (size_t)n_ra * sizeof(RaDev), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(qh.data(), ctx->qhist.p, qh.size() * 4, cudaMemcpyDeviceToHost, st));
   }
-  // ---- MC / UN input: the columns where the state machines can change state, all jobs at once
-  CK(ctx->keep.alloc(total_cols + 16, st));
-  CK(ctx->kcol.alloc((size_t)total_cols * 4 + 16, st));
-  CK(ctx->kcov.alloc((size_t)total_cols * sizeof(ColCov) + 16, st));
-  CK(ctx->kcall.alloc((size_t)total_cols * sizeof(ColCall) + 16, st));
-  CK(launch_intervals(B, ctx->cov.as<ColCov>(), ctx->call.as<ColCall>(), ctx->keep.as<uint8_t>(), ctx->blk.as<uint32_t>(),
-                      ctx->total.as<uint32_t>() + 1, ctx->kcol.as<uint32_t>(), ctx->kcov.as<ColCov>(),
-                      ctx->kcall.as<ColCall>(), st));
-  uint32_t nk = 0;
-  CK(cudaMemcpyAsync(&nk, ctx->total.as<uint32_t>() + 1, 4, cudaMemcpyDeviceToHost, st));
-  std::vector<uint32_t> err(n, 0);
-  for (uint32_t j = 0; j < n; j++) CK(cudaMemcpyAsync(&err[j], ctx->imb[j]->err.p, 4, cudaMemcpyDeviceToHost, st));
-  uint32_t cerr = 0;
-  CK(cudaMemcpyAsync(&cerr, ctx->errw.p, 4, cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
   std::vector<uint32_t> kept(nk);
   std::vector<ColCov> kcov(nk);
   std::vector<ColCall> kcall(nk);
@@ -654,16 +786,7 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
     CK(cudaMemcpyAsync(pcov[j].data(), ctx->cov.as<ColCov>() + col_b[j], (size_t)nc * sizeof(ColCov), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(pcall[j].data(), ctx->call.as<ColCall>() + col_b[j], (size_t)nc * sizeof(ColCall), cudaMemcpyDeviceToHost, st));
   }
-  CK(cudaEventRecord(ctx->ev1, st));
   CK(cudaStreamSynchronize(st));
-  float ms = 0, mms = 0;
-  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-  cudaEventElapsedTime(&mms, ctx->evm0, ctx->evm1);
-  ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 9;
-  ctx->last_candidates += n_cand;
-  if (cerr & ~kErrRaOverflow) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(cerr));
-  for (uint32_t j = 0; j < n; j++)
-    if (err[j]) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(err[j]));
   // ---- host assembly, per job
   std::vector<std::vector<RaDev>> jra(n);
   std::vector<std::vector<uint32_t>> jqh(n);
@@ -752,6 +875,65 @@ int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_
   if (device_ms) *device_ms = ctx->last_ms;
   if (kernel_launches) *kernel_launches = ctx->launches;
   if (main_kernel_ms) *main_kernel_ms = ctx->main_ms;
+  return BSQ_OK;
+}
+
+int bsq_get_tuning(const bsq_ctx* ctx, bsq_tuning* out) {
+  if (!ctx || !out) return BSQ_ERR_INVALID;
+  *out = ctx->tune;
+  return BSQ_OK;
+}
+
+int bsq_set_tuning(bsq_ctx* ctx, const bsq_tuning* t) {
+  if (!ctx || !t) return BSQ_ERR_INVALID;
+  if (t->ec_read_chunk < 64 || t->ec_read_chunk > (1u << 20) || t->ec_blocks_per_sm < 1 || t->ec_blocks_per_sm > 64 ||
+      t->col_blocks_per_sm < 1 || t->col_blocks_per_sm > 64 || t->cand_warps_per_sm < 1 || t->cand_warps_per_sm > 64)
+    return fail(ctx, BSQ_ERR_INVALID, "tuning value out of range");
+  ctx->tune = *t;
+  return BSQ_OK;
+}
+
+int bsq_autotune(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_params* ec, const bsq_im_params* im,
+                 const double* const* tables, bsq_tuning* chosen) {
+  if (!ctx || !ids || !ec || !im || !tables || n == 0) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  std::vector<bsq_ec_result> eo(n);
+  memset(eo.data(), 0, n * sizeof(bsq_ec_result));
+  auto time_ec = [&](double& ms) -> int {
+    const int rc = bsq_error_count_batch(ctx, n, ids, ec, eo.data());
+    ms = ctx->last_ms;
+    return rc;
+  };
+  auto time_im = [&](double& ms) -> int {
+    const int rc = bsq_identify_mutations_batch(ctx, n, ids, im, tables, nullptr);
+    ms = ctx->last_ms;
+    return rc;
+  };
+  // coordinate search: each knob over its candidates with the others held, fastest kept
+  auto search = [&](uint32_t bsq_tuning::*knob, std::initializer_list<uint32_t> values, bool pass1) -> int {
+    bsq_tuning best = ctx->tune;
+    double best_ms = 1e300;
+    for (uint32_t v : values) {
+      bsq_tuning t = best;
+      t.*knob = v;
+      ctx->tune = t;
+      double ms = 0;
+      const int rc = pass1 ? time_ec(ms) : time_im(ms);
+      if (rc != BSQ_OK) return rc;
+      if (ms < best_ms) { best_ms = ms; best = t; }
+    }
+    ctx->tune = best;
+    return BSQ_OK;
+  };
+  const bsq_tuning start = ctx->tune;
+  double warm = 0;
+  int rc = time_ec(warm);                           // first use: allocations and graph instantiation
+  if (rc == BSQ_OK) rc = time_im(warm);
+  if (rc == BSQ_OK) rc = search(&bsq_tuning::ec_read_chunk, {256, 512, 1024, 2048, 4096}, true);
+  if (rc == BSQ_OK) rc = search(&bsq_tuning::ec_blocks_per_sm, {2, 4, 6, 8, 12}, true);
+  if (rc == BSQ_OK) rc = search(&bsq_tuning::col_blocks_per_sm, {2, 3, 4, 6, 8, 12}, false);
+  if (rc == BSQ_OK) rc = search(&bsq_tuning::cand_warps_per_sm, {4, 8, 16, 32}, false);
+  if (rc != BSQ_OK) { ctx->tune = start; return rc; }
+  if (chosen) *chosen = ctx->tune;
   return BSQ_OK;
 }
 

@@ -788,26 +788,39 @@ cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t
   tile_range_kernel<<<(n_tiles + 255) / 256, 256, 0, st>>>(rstart, n_reads, n_tiles, maxspan, tile_range, max_tile_reads);
   return cudaGetLastError();
 }
-cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, unsigned int* next, uint32_t max_bins,
-                      int sms, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1) {
+// An event recorded inside a stream capture becomes an event node only with the external flag.
+static cudaError_t record_event(cudaEvent_t ev, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+    return cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal);
+  return cudaEventRecord(ev, st);
+}
+
+int ec_grid(uint32_t n_chunks, int sms, uint32_t blocks_per_sm) {
+  return grid_for(n_chunks, 1, sms, (int)std::max<uint32_t>(1, blocks_per_sm));
+}
+int column_grid(uint32_t total_tiles, int sms, uint32_t blocks_per_sm) {
+  return grid_for(total_tiles, kColumnWarps, sms, (int)std::max<uint32_t>(1, blocks_per_sm));
+}
+cudaError_t prepare_ec(uint32_t max_bins) {
   const size_t smem = (size_t)max_bins * sizeof(uint32_t);
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(ec_read_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
+  if (smem <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(ec_read_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, unsigned int* next, uint32_t max_bins,
+                      int grid, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1) {
+  const size_t smem = (size_t)max_bins * sizeof(uint32_t);
   cudaError_t e = cudaMemsetAsync(next, 0, sizeof(unsigned int), st);
   if (e != cudaSuccess) return e;
-  const int grid = grid_for(n_chunks, 1, sms, 8);
-  if (main0) cudaEventRecord(main0, st);
+  if (main0 && (e = record_event(main0, st)) != cudaSuccess) return e;
   ec_read_kernel<<<grid, 256, smem, st>>>(B, chunks, n_chunks, next);
-  if (main1) cudaEventRecord(main1, st);
-  cov_blocksum_kernel<<<B.total_cblk, 1024, 0, st>>>(B);
+  if (main1 && (e = record_event(main1, st)) != cudaSuccess) return e;
+  cov_blocksum_kernel<<<std::max<uint32_t>(1, B.total_cblk), 1024, 0, st>>>(B);
   scan_jobs_kernel<<<B.n_jobs, 1024, 0, st>>>(B);
-  cov_hist_kernel<<<B.total_cblk, 1024, 0, st>>>(B);
+  cov_hist_kernel<<<std::max<uint32_t>(1, B.total_cblk), 1024, 0, st>>>(B);
   return cudaGetLastError();
 }
-cudaError_t launch_im_column(const Batch& B, int precision, int sms, cudaStream_t st) {
-  const int grid = grid_for(B.total_tiles, 8, sms, 8);
+cudaError_t launch_im_column(const Batch& B, int precision, int grid, cudaStream_t st) {
   const size_t smem = kColumnWarps * 32 * sizeof(DevRead);
   if (precision == 0) im_column_kernel<true><<<grid, 32 * kColumnWarps, smem, st>>>(B);
   else im_column_kernel<false><<<grid, 32 * kColumnWarps, smem, st>>>(B);

@@ -44,9 +44,17 @@ cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st);
 cudaError_t launch_mapq_index(DevRead* reads, const uint8_t* mapq, const uint8_t* map, uint32_t n, cudaStream_t st);
 cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t n_tiles, uint32_t maxspan,
                               uint2* tile_range, uint32_t* max_tile_reads, cudaStream_t st);
+// Largest covariate table the pass-1 kernel keeps in shared memory (R*25*Q 32-bit bins).
+constexpr size_t kEcMaxHistBytes = 200 * 1024;
+
+// Grid sizes from the tuning knobs (resident blocks per SM, capped by the work).
+int ec_grid(uint32_t n_chunks, int sms, uint32_t blocks_per_sm);
+int column_grid(uint32_t total_tiles, int sms, uint32_t blocks_per_sm);
+// Attribute setup that must precede a stream capture of launch_ec.
+cudaError_t prepare_ec(uint32_t max_bins);
 cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, unsigned int* next, uint32_t max_bins,
-                      int sms, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1);
-cudaError_t launch_im_column(const Batch& B, int precision, int sms, cudaStream_t st);
+                      int grid, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1);
+cudaError_t launch_im_column(const Batch& B, int precision, int grid, cudaStream_t st);
 cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_counts, uint32_t* total, uint32_t* out,
                            cudaStream_t st);
 cudaError_t launch_intervals(const Batch& B, const ColCov* cov, const ColCall* call, uint8_t* keep, uint32_t* block_counts,

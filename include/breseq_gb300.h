@@ -310,6 +310,23 @@ int bsq_im_batch_result_counts(const bsq_ctx* ctx, uint32_t job, uint64_t* n_ra,
 int bsq_im_batch_result_copy(const bsq_ctx* ctx, uint32_t job, bsq_ra_record* ra, uint64_t ra_cap,
                              bsq_mc_record* mc, uint64_t mc_cap, bsq_un_record* un, uint64_t un_cap);
 
+/* Launch shape of the passes.  None of the knobs changes a result: every count is an integer sum
+ * and every column and candidate is scored by one warp whatever the grid. */
+typedef struct bsq_tuning {
+    uint32_t ec_read_chunk;       /* reads per pass-1 work unit (default 1024)                  */
+    uint32_t ec_blocks_per_sm;    /* pass-1 blocks per SM (default 8)                            */
+    uint32_t col_blocks_per_sm;   /* column-pass blocks of 8 warps per SM (default 8)            */
+    uint32_t cand_warps_per_sm;   /* candidate-kernel warps per SM (default 16)                  */
+    int32_t  use_graphs;          /* capture each pass as one CUDA graph, updated in place (default 1) */
+} bsq_tuning;
+int bsq_get_tuning(const bsq_ctx* ctx, bsq_tuning* out);
+int bsq_set_tuning(bsq_ctx* ctx, const bsq_tuning* t);
+/* Times the passes over the given resident samples under candidate launch shapes (one knob at a
+ * time, CUDA events around each pass), keeps the fastest in the context and returns it in *chosen.
+ * Runs both passes several times; the samples' results are not kept. */
+int bsq_autotune(bsq_ctx* ctx, uint32_t n, const int32_t* sample_ids, const bsq_ec_params* ec,
+                 const bsq_im_params* im, const double* const* log10_prob_tables, bsq_tuning* chosen);
+
 /* Timing of the last pass on the device (CUDA events around the kernels, milliseconds) and the
  * number of kernels launched by it. */
 int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_launches,

@@ -160,3 +160,40 @@ def test_batch_larger_than_one_launch_group(scorer, loaded, oracle_results):
             assert np.array_equal(ecs[i]["counts"], alone_ec["counts"]), i
             assert np.array_equal(ecs[i]["hist"], alone_ec["hist"]), i
             assert all(compare.identical(ims[i][k], alone[k]) for k in ("ra", "mc", "un")), i
+
+
+def test_graphs_and_launch_shapes_do_not_change_results(scorer, loaded, oracle_results):
+    """Graph capture on/off, several launch shapes and the autotuner's pick give bit-identical
+    results (integer counts; every column and candidate is scored by one warp whatever the grid)."""
+    from breseq_gb300.api import ImSettings
+    names = list(samples.ALL)
+    sids = [loaded[n] for n in names]
+    tabs = [oracle_results[n][1] for n in names]
+    sets = [ImSettings(polymorphism_prediction=n in POLY) for n in names]
+    default = scorer.tuning()
+
+    def run():
+        ecs = scorer.error_count_batch(sids)
+        ims = scorer.identify_mutations_batch(sids, tabs, sets, precision=1)
+        return ecs, ims
+
+    base_ec, base_im = run()
+    shapes = [dict(use_graphs=0), dict(use_graphs=1),
+              dict(ec_read_chunk=256, ec_blocks_per_sm=2, col_blocks_per_sm=3, cand_warps_per_sm=4),
+              dict(ec_read_chunk=4096, ec_blocks_per_sm=12, col_blocks_per_sm=12, cand_warps_per_sm=32, use_graphs=0)]
+    try:
+        for sh in shapes:
+            scorer.set_tuning(**sh)
+            for _ in range(2):           # the second call updates the kept graph in place
+                ecs, ims = run()
+                for a, b in zip(ecs, base_ec):
+                    assert np.array_equal(a["counts"], b["counts"]) and np.array_equal(a["hist"], b["hist"]), sh
+                for a, b in zip(ims, base_im):
+                    assert all(compare.identical(a[k], b[k]) for k in ("ra", "mc", "un")), sh
+        chosen = scorer.autotune(sids, tabs, sets)
+        assert chosen == scorer.tuning()
+        ecs, ims = run()
+        for a, b in zip(ims, base_im):
+            assert all(compare.identical(a[k], b[k]) for k in ("ra", "mc", "un"))
+    finally:
+        scorer.set_tuning(**default)
