@@ -40,6 +40,11 @@ sys.path.insert(0, ROOT)
 METRIC = "read-bases/s scored, served vs plain on same GPU (identical calls); p50/p99 ms"
 UNIT = "read-bases/s"
 WORKLOAD = "ecoli_clonal_4.79Mb_pe150_2x100x"
+# DRAM bytes (read + write) per aligned read-base of one launch, from an ncu capture of the same
+# workload at 0.25x genome length (profiles/im_column_kernel_ecoli_clonal_x0.25.md,
+# profiles/ec_read_kernel_ecoli_clonal_x0.25.md), scaled linearly with read-bases
+IM_COLUMN_DRAM_PER_BASE = 0.5668e9 / 0.2441e9
+EC_READ_DRAM_PER_BASE = 0.4250e9 / 0.2441e9
 # the plain FP64 form: same kernels, FP64 everywhere, one sample per call, launched without graphs
 PLAIN_TUNING = dict(ec_read_chunk=1024, ec_blocks_per_sm=8, col_blocks_per_sm=8, cand_warps_per_sm=16, use_graphs=0)
 
@@ -263,9 +268,9 @@ def run_ours(args, world, rank, local, pg):
     bytes_ec = bases * 1.5 + n_reads * 20 + n_cols * 0.25
     bytes_im = bytes_ec + n_cols * 48
     if im_ms >= ec_ms:
-        kname, kms, kbytes = "im_column_kernel", im_ms, bytes_im
+        kname, kms, kbytes, dram_per_base = "im_column_kernel", im_ms, bytes_im, IM_COLUMN_DRAM_PER_BASE
     else:
-        kname, kms, kbytes = "ec_kernel", ec_ms, bytes_ec
+        kname, kms, kbytes, dram_per_base = "ec_read_kernel", ec_ms, bytes_ec, EC_READ_DRAM_PER_BASE
     achieved = kbytes / (kms / 1000.0) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -280,7 +285,8 @@ def run_ours(args, world, rank, local, pg):
                        "served_over_plain": (plain_ms / ms) if plain_ms else None, "identical_calls": same_calls},
         "passes_ms": {"error_count_kernel": ec_ms, "im_column_kernel": im_ms},
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind},
+                     "frac": achieved / hbm, "traffic": dram_per_base * bases, "traffic_unit": "bytes per launch",
+                     "algorithmic_bytes": kbytes, "peak_kind": peak_kind},
         "clocks": clk,
         "tuning": tuning,
         "ra_items": len(im["ra"]),
