@@ -162,7 +162,7 @@ def ptr(a: np.ndarray, ctype):
 
 class Tuning(C.Structure):
     _fields_ = [("ec_read_chunk", C.c_uint32), ("ec_blocks_per_sm", C.c_uint32), ("col_blocks_per_sm", C.c_uint32),
-                ("cand_warps_per_sm", C.c_uint32), ("use_graphs", C.c_int32)]
+                ("cand_warps_per_sm", C.c_uint32), ("bound_warps_per_sm", C.c_uint32), ("use_graphs", C.c_int32)]
 
 
 class Job(C.Structure):

@@ -99,11 +99,11 @@ struct bsq_ctx {
   std::map<int32_t, std::unique_ptr<SampleDev>> samples;
   int32_t next_id = 1;
   // working memory reused across calls
-  DevMem cov, call, blk, cand, next, ra, qhist, scratch;
+  DevMem cov, call, blk, cand, next, ra, qhist, scratch, bq, pool;
   DevMem keep, kcol, kcov, kcall;
   DevMem d_chunks, ec_arena, im_arena, ctl;
   PinnedBuf pin_in, pin_out;
-  bsq_tuning tune = {1024, 8, 8, 16, 1};
+  bsq_tuning tune = {1024, 8, 8, 16, 4, 1};
   cudaGraphExec_t exec_ec = nullptr, exec_im = nullptr;
   uint64_t graph_instantiations = 0, graph_updates = 0;
   std::vector<std::vector<bsq_ra_record>> res_ra;
@@ -273,7 +273,7 @@ void bsq_destroy(bsq_ctx* ctx) {
   for (cudaStream_t ls : ctx->load_streams) if (ls) cudaStreamSynchronize(ls);
   ctx->samples.clear();
   // pool blocks are returned on the context's stream, so before it goes
-  for (DevMem* m : {&ctx->cov, &ctx->call, &ctx->blk, &ctx->cand, &ctx->next, &ctx->ra,
+  for (DevMem* m : {&ctx->cov, &ctx->call, &ctx->blk, &ctx->cand, &ctx->next, &ctx->ra, &ctx->bq, &ctx->pool,
                     &ctx->qhist, &ctx->scratch, &ctx->keep, &ctx->kcol, &ctx->kcov, &ctx->kcall,
                     &ctx->d_chunks, &ctx->ec_arena, &ctx->im_arena, &ctx->ctl})
     m->release();
@@ -593,7 +593,9 @@ int bsq_counts_to_log10_prob(const uint64_t* counts, uint32_t R, uint32_t Q, dou
 
 // ============================================================================ pass 2
 // Control words of pass 2, written on the device and read back in one copy.
-enum : uint32_t { kCtlCand = 0, kCtlKept = 1, kCtlRa = 2, kCtlCandErr = 3, kCtlJobErr = 8, kCtlWords = 8 + kBatchJobs };
+enum : uint32_t { kCtlCand = 0, kCtlCand2 = 1, kCtlKept = 2, kCtlRa = 3, kCtlCandErr = 4, kCtlBq = 5, kCtlPool = 6,
+                  kCtlBqNext = 7, kCtlJobErr = 8, kCtlWords = 8 + kBatchJobs };
+constexpr uint32_t kBoundPool = 4u << 20;   // (class, multiplicity) entries for deferred bounds: 32 MiB
 
 // One group of at most kBatchJobs samples; results go to res_*[job0 + j].
 //   device arena: per job the likelihood-class table (lp64 | r64 | lpmax64 | lp32) and the per-target
@@ -654,6 +656,8 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
   uint32_t ra_cap = 4096 + total_cols / 64;
   CK(ctx->ra.alloc((size_t)ra_cap * sizeof(RaDev), st));
   CK(ctx->qhist.alloc((size_t)ra_cap * 2 * Qh * 4, st));
+  CK(ctx->bq.alloc((size_t)2 * ra_cap * sizeof(BoundJob), st));
+  CK(ctx->pool.alloc((size_t)kBoundPool * sizeof(uint2), st));
   CK(ctx->keep.alloc(total_cols + 16, st));
   CK(ctx->kcol.alloc((size_t)total_cols * 4 + 16, st));
   CK(ctx->kcov.alloc((size_t)total_cols * sizeof(ColCov) + 16, st));
@@ -706,6 +710,8 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
   C.ra = ctx->ra.as<RaDev>(); C.n_ra = ctl + kCtlRa; C.ra_cap = ra_cap;
   C.scratch = ctx->scratch.as<uint4>(); C.scratch_per_warp = per_warp; C.err = ctl + kCtlCandErr;
   C.Qhist = Qh; C.qhist = ctx->qhist.as<uint32_t>();
+  C.bq = ctx->bq.as<BoundJob>(); C.n_bq = ctl + kCtlBq; C.bq_cap = 2 * ra_cap;
+  C.pool = ctx->pool.as<uint2>(); C.pool_used = ctl + kCtlPool; C.pool_cap = kBoundPool;
   const int col_grid = column_grid(B.total_tiles, ctx->sms, tn.col_blocks_per_sm);
   const uint32_t* ctl_host = reinterpret_cast<const uint32_t*>(ctx->pin_out.p);
   // ---- the device part of the pass: column scores -> candidates -> EM -> interval marks
@@ -727,6 +733,8 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
                             ctx->cand.as<uint32_t>(), st)) != cudaSuccess) return e;
     step = "candidate kernel";
     if ((e = launch_candidates(B, C, max_K, n_warps, st)) != cudaSuccess) return e;
+    step = "bounds kernel";
+    if ((e = launch_bounds(B, C, ctl + kCtlBqNext, ctx->sms, tn.bound_warps_per_sm, st)) != cudaSuccess) return e;
     step = "interval kernels";
     if ((e = launch_intervals(B, ctx->cov.as<ColCov>(), ctx->call.as<ColCall>(), ctx->keep.as<uint8_t>(),
                               ctx->blk.as<uint32_t>(), ctl + kCtlKept, ctx->kcol.as<uint32_t>(), ctx->kcov.as<ColCov>(),
@@ -746,15 +754,18 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
     ra_cap = ctl_host[kCtlRa] + 1024;
     CK(ctx->ra.alloc((size_t)ra_cap * sizeof(RaDev), st));
     CK(ctx->qhist.alloc((size_t)ra_cap * 2 * Qh * 4, st));
+    CK(ctx->bq.alloc((size_t)2 * ra_cap * sizeof(BoundJob), st));
     C.ra = ctx->ra.as<RaDev>(); C.ra_cap = ra_cap; C.qhist = ctx->qhist.as<uint32_t>();
-    CK(cudaMemsetAsync(ctl + kCtlRa, 0, 8, st));   // RA count and the candidate error word
+    C.bq = ctx->bq.as<BoundJob>(); C.bq_cap = 2 * ra_cap;
+    CK(cudaMemsetAsync(ctl + kCtlRa, 0, (kCtlBqNext + 1 - kCtlRa) * 4, st));   // RA, error, bound-job counters
     CK(launch_candidates(B, C, max_K, n_warps, st));
+    CK(launch_bounds(B, C, ctl + kCtlBqNext, ctx->sms, tn.bound_warps_per_sm, st));
     CK(cudaMemcpyAsync(ctx->pin_out.p, ctl, kCtlWords * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
   }
-  const uint32_t n_cand = ctl_host[kCtlCand], nk = ctl_host[kCtlKept], n_ra = ctl_host[kCtlRa];
+  const uint32_t n_cand = ctl_host[kCtlCand] + ctl_host[kCtlCand2], nk = ctl_host[kCtlKept], n_ra = ctl_host[kCtlRa];
   const uint32_t cerr = ctl_host[kCtlCandErr];
-  ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 9;
+  ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 13;
   ctx->last_candidates += n_cand;
   if (n_ra > ra_cap) return fail(ctx, BSQ_ERR_NOMEM, "identify_mutations: RA buffer overflow");
   if (cerr & ~kErrRaOverflow) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(cerr));
@@ -887,7 +898,8 @@ int bsq_get_tuning(const bsq_ctx* ctx, bsq_tuning* out) {
 int bsq_set_tuning(bsq_ctx* ctx, const bsq_tuning* t) {
   if (!ctx || !t) return BSQ_ERR_INVALID;
   if (t->ec_read_chunk < 64 || t->ec_read_chunk > (1u << 20) || t->ec_blocks_per_sm < 1 || t->ec_blocks_per_sm > 64 ||
-      t->col_blocks_per_sm < 1 || t->col_blocks_per_sm > 64 || t->cand_warps_per_sm < 1 || t->cand_warps_per_sm > 64)
+      t->col_blocks_per_sm < 1 || t->col_blocks_per_sm > 64 || t->cand_warps_per_sm < 1 || t->cand_warps_per_sm > 64 ||
+      t->bound_warps_per_sm < 1 || t->bound_warps_per_sm > 8)
     return fail(ctx, BSQ_ERR_INVALID, "tuning value out of range");
   ctx->tune = *t;
   return BSQ_OK;
@@ -932,6 +944,7 @@ int bsq_autotune(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_para
   if (rc == BSQ_OK) rc = search(&bsq_tuning::ec_blocks_per_sm, {2, 4, 6, 8, 12}, true);
   if (rc == BSQ_OK) rc = search(&bsq_tuning::col_blocks_per_sm, {2, 3, 4, 6, 8, 12}, false);
   if (rc == BSQ_OK) rc = search(&bsq_tuning::cand_warps_per_sm, {4, 8, 16, 32}, false);
+  if (rc == BSQ_OK) rc = search(&bsq_tuning::bound_warps_per_sm, {1, 2, 3, 4, 6, 8}, false);
   if (rc != BSQ_OK) { ctx->tune = start; return rc; }
   if (chosen) *chosen = ctx->tune;
   return BSQ_OK;

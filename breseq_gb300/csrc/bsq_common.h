@@ -106,7 +106,8 @@ struct ColCall {              // 16 bytes
   uint8_t flags;              // kBasePredicted | kUniqueOnly | kCandidate | kSlots | kRecompute
   uint8_t pad[2];
 };
-enum : uint8_t { kBasePredicted = 1, kUniqueOnly = 2, kCandidate = 4, kSlots = 8, kRecompute = 16, kScored = 32 };
+enum : uint8_t { kBasePredicted = 1, kUniqueOnly = 2, kCandidate = 4, kSlots = 8, kRecompute = 16, kScored = 32,
+                 kLikelyRa = 64 };   // best base differs from the reference: queued first (longest work)
 
 struct ImArgs {
   ColCov* cov;
@@ -125,7 +126,7 @@ struct ImArgs {
 // A scoring job for the candidate kernel: one reference column, all its insert slots.
 struct CandArgs {
   const uint32_t* cand;       // candidate columns (batch column space)
-  const uint32_t* n_cand_dev; // number of candidates, written by the compaction on the device
+  const uint32_t* n_cand_dev; // [2] candidates queued first (likely RA items) and the rest, from the compaction
   unsigned int* next;         // work counter (persistent warps)
   struct RaDev* ra;           // output records
   unsigned int* n_ra;
@@ -135,6 +136,27 @@ struct CandArgs {
   uint32_t* err;
   uint32_t Qhist;             // quality histogram bins kept per RA (for the K-S test)
   uint32_t* qhist;            // [ra_cap][2][Qhist] major / minor qualities
+  // deferred frequency bounds (may be null: bounds are then computed inline)
+  struct BoundJob* bq;        // [bq_cap] one bisection each
+  unsigned int* n_bq;
+  uint32_t bq_cap;
+  uint2* pool;                // [pool_cap] (class, multiplicity) lists the bound jobs read
+  unsigned int* pool_used;
+  uint32_t pool_cap;
+};
+
+// One deferred profile-likelihood bound of an RA item (write_RA_frequency_bounds,
+// identify_mutations.cpp:3175-3217): the lower or the upper bisection, run on its own warp by the
+// bounds kernel.  The two bisections of an item are independent (each test restarts from the free
+// fit), so splitting them changes no arithmetic.
+struct BoundJob {
+  double full[5];             // free-fit frequencies
+  double target, maxsum, fh, tol;
+  uint32_t slot;              // RA record to complete
+  uint32_t pool_off, m;       // the item's class list in the pool
+  uint32_t n;                 // scored read bases
+  uint32_t col;               // batch column (job lookup)
+  uint8_t var, side, pad[2];  // variant allele; side 0 = lower, 1 = upper
 };
 
 // Raw RA values written by the candidate kernel (host adds Fisher / K-S and formats).

@@ -121,6 +121,33 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
   return v;
 }
+// Sums of five values over the warp, returned to every lane, with 8 FP64 adds per lane instead of
+// the 25 of five butterflies: each exchange step halves the values a lane keeps (xor 16: 3 of 5,
+// xor 8: 2 or 1, xor 4: 1), the last two steps add single values, and five shuffles broadcast the
+// sums.  FP64 issue is the scarce resource of the EM on this part.
+__device__ __forceinline__ void warp_sum5(const double in[5], double out[5]) {
+  const int lane = threadIdx.x & 31;
+  const bool hi = lane & 16, b3 = lane & 8, b2 = lane & 4;
+  // xor 16: the low half keeps sums 0,1,2 and the high half 3,4
+  const double k0 = (hi ? in[3] : in[0]) + __shfl_xor_sync(0xFFFFFFFFu, hi ? in[0] : in[3], 16);
+  const double k1 = (hi ? in[4] : in[1]) + __shfl_xor_sync(0xFFFFFFFFu, hi ? in[1] : in[4], 16);
+  const double k2 = (hi ? 0.0 : in[2]) + __shfl_xor_sync(0xFFFFFFFFu, hi ? in[2] : 0.0, 16);
+  // xor 8: low/low keeps 0,1; low/high keeps 2; high/low keeps 3; high/high keeps 4
+  const double m0 = (hi ? (b3 ? k1 : k0) : (b3 ? k2 : k0)) +
+                    __shfl_xor_sync(0xFFFFFFFFu, hi ? (b3 ? k0 : k1) : (b3 ? k0 : k2), 8);
+  const double m1 = ((!hi && !b3) ? k1 : 0.0) + __shfl_xor_sync(0xFFFFFFFFu, (!hi && b3) ? k1 : 0.0, 8);
+  // xor 4: the lanes holding 0,1 split them; every other lane keeps its one value
+  const bool pair = !hi && !b3;
+  double u = (pair ? (b2 ? m1 : m0) : m0) + __shfl_xor_sync(0xFFFFFFFFu, pair ? (b2 ? m0 : m1) : m0, 4);
+  u += __shfl_xor_sync(0xFFFFFFFFu, u, 2);
+  u += __shfl_xor_sync(0xFFFFFFFFu, u, 1);
+  out[0] = __shfl_sync(0xFFFFFFFFu, u, 0);
+  out[1] = __shfl_sync(0xFFFFFFFFu, u, 4);
+  out[2] = __shfl_sync(0xFFFFFFFFu, u, 8);
+  out[3] = __shfl_sync(0xFFFFFFFFu, u, 16);
+  out[4] = __shfl_sync(0xFFFFFFFFu, u, 24);
+}
+
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
@@ -147,31 +174,46 @@ struct EmList { const uint2* e; uint32_t m; };
 // One E-step sweep: g[b] = sum_i r_i(b) / s_i (the gradient of ln L in f[b]) over allowed alleles;
 // the E-step sums are sum_w[b] = f[b] g[b].  With `ll` the sweep also returns an FP32 estimate of
 // sum_i log10 s_i (error well below 1e-3 for a few thousand reads).
+__device__ __forceinline__ void em_class(const EmList& L, const ClassTable& T, const double f[5], uint32_t i,
+                                         double a[5], float& lls, bool want_ll) {
+  const uint2 e = L.e[i];
+  const double cnt = (double)e.y;
+  const double* r = T.r64 + (size_t)e.x * 5;
+  double rv[5];
+#pragma unroll
+  for (int b = 0; b < 5; b++) rv[b] = __ldg(r + b);
+  // f[b] is exactly 0 for an allele outside the allowed set, so the unmasked sum equals the masked one
+  const double s = (f[0] * rv[0] + f[1] * rv[1]) + (f[2] * rv[2] + f[3] * rv[3]) + f[4] * rv[4];
+  if (s > 0.0) {
+    const double w = cnt / s;
+#pragma unroll
+    for (int b = 0; b < 5; b++) a[b] += rv[b] * w;
+    if (want_ll) lls += (float)e.y * log10f((float)s);
+  } else {
+    // the reference's fallback keeps sum_w = n exact: each read adds f[b] to sum_w[b], i.e. 1 to g[b]
+#pragma unroll
+    for (int b = 0; b < 5; b++) a[b] += cnt;
+  }
+}
+
 __device__ void em_sweep(const EmList& L, const ClassTable& T, const double f[5], unsigned allowed, double g[5],
                          float* ll) {
-  double a[5] = {0, 0, 0, 0, 0};
-  float lls = 0.0f;
-  for (uint32_t i = threadIdx.x & 31; i < L.m; i += 32) {
-    const uint2 e = L.e[i];
-    const double cnt = (double)e.y;
-    const double* r = T.r64 + (size_t)e.x * 5;
-    double rv[5], s = 0;
-#pragma unroll
-    for (int b = 0; b < 5; b++) { rv[b] = __ldg(r + b); if ((allowed >> b) & 1) s += f[b] * rv[b]; }
-    if (s > 0.0) {
-      const double w = cnt / s;
-#pragma unroll
-      for (int b = 0; b < 5; b++) a[b] += rv[b] * w;
-      if (ll) lls += (float)e.y * log10f((float)s);
-    } else {
-      // the reference's fallback keeps sum_w = n exact: each read adds f[b] to sum_w[b], i.e. 1 to g[b]
-#pragma unroll
-      for (int b = 0; b < 5; b++) a[b] += cnt;
-    }
+  // two classes per lane in flight: the FP64 chains of a class are short and latency-bound
+  double a0[5] = {0, 0, 0, 0, 0}, a1[5] = {0, 0, 0, 0, 0};
+  float l0 = 0.0f, l1 = 0.0f;
+  const bool want = ll != nullptr;
+  uint32_t i = threadIdx.x & 31;
+  for (; i + 32 < L.m; i += 64) {
+    em_class(L, T, f, i, a0, l0, want);
+    em_class(L, T, f, i + 32, a1, l1, want);
   }
+  if (i < L.m) em_class(L, T, f, i, a0, l0, want);
+  double a[5];
 #pragma unroll
-  for (int b = 0; b < 5; b++) g[b] = warp_sum(((allowed >> b) & 1) ? a[b] : 0.0);
+  for (int b = 0; b < 5; b++) a[b] = ((allowed >> b) & 1) ? a0[b] + a1[b] : 0.0;
+  warp_sum5(a, g);
   if (ll) {
+    float lls = l0 + l1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lls += __shfl_xor_sync(0xFFFFFFFFu, lls, o);
     *ll = lls;
@@ -214,6 +256,7 @@ __device__ Fit em_fit(const EmList& L, uint32_t n, const uint32_t obs_count[5], 
   for (int b = 0; b < 5; b++) tot += f[b];
 #pragma unroll
   for (int b = 0; b < 5; b++) f[b] /= tot;
+  const double inv_n = 1.0 / (double)n;
   for (int it = 1; it <= 50; it++) {
     double g[5];
     em_sweep(L, T, f, allowed, g, nullptr);
@@ -222,7 +265,7 @@ __device__ Fit em_fit(const EmList& L, uint32_t n, const uint32_t obs_count[5], 
     for (int b = 0; b < 5; b++) {
       fprev[b] = f[b];
       if (!((allowed >> b) & 1)) continue;
-      const double fn = f[b] * g[b] / (double)n;
+      const double fn = f[b] * g[b] * inv_n;
       md = fmax(md, fabs(fn - f[b]));
       f[b] = fn;
     }
@@ -250,11 +293,12 @@ __device__ __forceinline__ double em_profile_step(double f[5], double fprev[5], 
 #pragma unroll
   for (int b = 0; b < 5; b++) { sw[b] = f[b] * g[b]; if (b != v) others += sw[b]; }
   double md = 0;
+  const double scale = (others > 0.0) ? (1.0 - ff) / others : 0.0, even = (1.0 - ff) * 0.25;
 #pragma unroll
   for (int b = 0; b < 5; b++) {
     fprev[b] = f[b];
     if (b == v) continue;
-    const double fn = (others > 0.0) ? (1.0 - ff) * sw[b] / others : (1.0 - ff) / 4.0;
+    const double fn = (others > 0.0) ? scale * sw[b] : even;
     md = fmax(md, fabs(fn - f[b]));
     f[b] = fn;
   }
@@ -293,7 +337,7 @@ __device__ bool em_profile_ge(const EmList& L, const ClassTable& T, const double
     double gmax = -DBL_MAX, dot = 0;
 #pragma unroll
     for (int b = 0; b < 5; b++) if (b != v) { gmax = fmax(gmax, g[b]); dot += f[b] * g[b]; }
-    const double upper = ll + ((1.0 - ff) * gmax - dot) / 2.302585092994046;
+    const double upper = ll + ((1.0 - ff) * gmax - dot) * 0.43429448190325176;   // 1 / ln 10
     if (upper + margin < target) return false;
     if (em_profile_step(f, fprev, g, v, ff) < tol) break;
   }
@@ -328,7 +372,36 @@ struct CandOut {
   uint32_t base_quality_cutoff;
   double log10_ref_len, mutation_cutoff, poly_cutoff, precision_decimal;
   uint32_t col_offset;        // added to the column reported in each RA item
+  BoundJob* bq;               // deferred bounds (null: computed inline)
+  unsigned int* n_bq;
+  uint32_t bq_cap;
+  uint2* pool;
+  unsigned int* pool_used;
+  uint32_t pool_cap;
 };
+
+// write_RA_frequency_bounds (identify_mutations.cpp:3175-3217): the reference's bisections, with each
+// "profile >= target" test decided by em_profile_ge.  Used inline and by the bounds kernel.
+__device__ double ra_lower_bound(const EmList& L, const ClassTable& T, const double full[5], int var, double fh,
+                                 double tol, double target, double maxsum, uint32_t n) {
+  if (em_profile_ge(L, T, full, var, 0.0, tol, target, maxsum, n)) return 0.0;
+  double lo = 0.0, hi = fh;
+  for (int i = 0; i < 40 && (hi - lo) > tol; i++) {
+    const double mid = 0.5 * (lo + hi);
+    if (em_profile_ge(L, T, full, var, mid, tol, target, maxsum, n)) hi = mid; else lo = mid;
+  }
+  return hi;
+}
+__device__ double ra_upper_bound(const EmList& L, const ClassTable& T, const double full[5], int var, double fh,
+                                 double tol, double target, double maxsum, uint32_t n) {
+  if (em_profile_ge(L, T, full, var, 1.0, tol, target, maxsum, n)) return 1.0;
+  double lo = fh, hi = 1.0;
+  for (int i = 0; i < 40 && (hi - lo) > tol; i++) {
+    const double mid = 0.5 * (lo + hi);
+    if (em_profile_ge(L, T, full, var, mid, tol, target, maxsum, n)) lo = mid; else hi = mid;
+  }
+  return lo;
+}
 
 // Scores one reference column (called by a whole warp): gathers the reads covering column c in BAM
 // order into the warp's list `ents` (capacity `cap`), then for insert slot 0 (when do_slot0) and every
@@ -501,8 +574,11 @@ __device__ void score_candidate_column(const DevSample& S, const ClassTable& T, 
       }
     }
     if (passed_cons || passed_poly) {
-      // ---- write_RA_frequency_bounds (identify_mutations.cpp:3175-3217): the same bisection, with
-      // each "profile >= target" test decided by em_profile_ge
+      uint32_t slot = 0;
+      if (lane == 0) slot = atomicAdd(A.n_ra, 1u);
+      slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+      // ---- frequency bounds (identify_mutations.cpp:3175-3217): deferred to the bounds kernel as two
+      // independent bisections when there is room, else computed here
       double lower = 0.0, upper = 1.0;
       if (n > 0 && var < 5) {
         const double D = 0.587566;
@@ -510,28 +586,30 @@ __device__ void score_candidate_column(const DevSample& S, const ClassTable& T, 
         const double tol = A.precision_decimal;
         const double maxsum = em_maxsum(L, T);
         const double target = em_profile(L, T, full.f, var, fh, tol) - D;
-        if (em_profile_ge(L, T, full.f, var, 0.0, tol, target, maxsum, n)) lower = 0.0;
-        else {
-          double lo = 0.0, hi = fh;
-          for (int i = 0; i < 40 && (hi - lo) > tol; i++) {
-            double mid = 0.5 * (lo + hi);
-            if (em_profile_ge(L, T, full.f, var, mid, tol, target, maxsum, n)) hi = mid; else lo = mid;
+        bool deferred = false;
+        if (A.bq != nullptr && slot < A.ra_cap) {
+          uint32_t off = 0, jb = 0;
+          if (lane == 0) { off = atomicAdd(A.pool_used, L.m); jb = atomicAdd(A.n_bq, 2u); }
+          off = __shfl_sync(0xFFFFFFFFu, off, 0);
+          jb = __shfl_sync(0xFFFFFFFFu, jb, 0);
+          if ((uint64_t)off + L.m <= A.pool_cap && (uint64_t)jb + 2 <= A.bq_cap) {
+            for (uint32_t i = lane; i < L.m; i += 32) A.pool[off + i] = L.e[i];
+            if (lane < 2) {
+              BoundJob b;
+              for (int q = 0; q < 5; q++) b.full[q] = full.f[q];
+              b.target = target; b.maxsum = maxsum; b.fh = fh; b.tol = tol;
+              b.slot = slot; b.pool_off = off; b.m = L.m; b.n = n; b.col = c + A.col_offset;
+              b.var = (uint8_t)var; b.side = (uint8_t)lane; b.pad[0] = b.pad[1] = 0;
+              A.bq[jb + lane] = b;
+            }
+            deferred = true;
           }
-          lower = hi;
         }
-        if (em_profile_ge(L, T, full.f, var, 1.0, tol, target, maxsum, n)) upper = 1.0;
-        else {
-          double lo = fh, hi = 1.0;
-          for (int i = 0; i < 40 && (hi - lo) > tol; i++) {
-            double mid = 0.5 * (lo + hi);
-            if (em_profile_ge(L, T, full.f, var, mid, tol, target, maxsum, n)) lo = mid; else hi = mid;
-          }
-          upper = lo;
+        if (!deferred) {
+          lower = ra_lower_bound(L, T, full.f, var, fh, tol, target, maxsum, n);
+          upper = ra_upper_bound(L, T, full.f, var, fh, tol, target, maxsum, n);
         }
       }
-      uint32_t slot = 0;
-      if (lane == 0) slot = atomicAdd(A.n_ra, 1u);
-      slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
       if (slot < A.ra_cap) {
         if (lane == 0) {
           RaDev o;

@@ -561,6 +561,7 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
             for (int b = 0; b < 5; b++) if (b != best) te += exp10(S64[b] - off);
             score = S64[best] - (log10(te) + off) - A.log10_ref_len;
             cl.flags |= kCandidate;            // the plain form runs the EM wherever a base was scored
+            if (best != ref_idx && score > 0) cl.flags |= kLikelyRa;
           } else {
             double tot[5];
 #pragma unroll
@@ -579,7 +580,7 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
             const double g = (double)A.guard * (1.0 + (double)n);
             const bool near = fabs(score - A.mutation_cutoff) < g || (best != ref_idx && fabs(score) < g) || off > -g;
             if (near) cl.flags |= kRecompute;
-            if (best != ref_idx && score > 0) cl.flags |= kCandidate;
+            if (best != ref_idx && score > 0) cl.flags |= kCandidate | kLikelyRa;
             float bmax = 0.0f;
 #pragma unroll
             for (int b = 0; b < 5; b++) if (b != ref_idx) bmax = fmaxf(bmax, B[b]);
@@ -600,12 +601,18 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
 
 // ============================================================================ candidate compaction
 // Deterministic stream compaction of the columns flagged for the candidate kernel, in column order.
-__global__ void cand_count_kernel(const ColCall* call, uint32_t n, uint32_t* block_counts) {
+// The candidate queue puts the columns likely to emit an RA item (their bounds are the longest
+// work) first, the others after them, each part in column order.  `part` 0 / 1 selects which.
+__device__ __forceinline__ bool cand_pick(const ColCall& cl, int part) {
+  if (!(cl.flags & (kCandidate | kSlots | kRecompute))) return false;
+  return ((cl.flags & kLikelyRa) != 0) == (part == 0);
+}
+__global__ void cand_count_kernel(const ColCall* call, uint32_t n, uint32_t* block_counts, int part) {
   __shared__ uint32_t s;
   if (threadIdx.x == 0) s = 0;
   __syncthreads();
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  bool f = i < n && (call[i].flags & (kCandidate | kSlots | kRecompute));
+  bool f = i < n && cand_pick(call[i], part);
   uint32_t b = __popc(__ballot_sync(0xFFFFFFFFu, f));
   if ((threadIdx.x & 31) == 0 && b) atomicAdd(&s, b);
   __syncthreads();
@@ -653,10 +660,12 @@ __global__ void scan_jobs_kernel(const __grid_constant__ Batch B) {
   block_exclusive_scan(A.blk_r, nb, A.blk_r + nb);
 }
 
-__global__ void cand_scatter_kernel(const ColCall* call, uint32_t n, const uint32_t* block_offsets, uint32_t* out) {
+__global__ void cand_scatter_kernel(const ColCall* call, uint32_t n, const uint32_t* block_offsets, uint32_t* out,
+                                    int part, const uint32_t* base) {
   __shared__ uint32_t warp_base[32];
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  bool f = i < n && (call[i].flags & (kCandidate | kSlots | kRecompute));
+  bool f = i < n && cand_pick(call[i], part);
+  if (base) out += *base;
   unsigned m = __ballot_sync(0xFFFFFFFFu, f);
   if ((threadIdx.x & 31) == 0) warp_base[threadIdx.x >> 5] = __popc(m);
   __syncthreads();
@@ -738,7 +747,7 @@ __global__ void __launch_bounds__(128) im_candidate_kernel(const __grid_constant
   const int lane = threadIdx.x & 31;
   const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   uint4* ents = A.scratch + (size_t)gw * cand_warp_stride(A.scratch_per_warp);
-  const uint32_t n_cand = *A.n_cand_dev;
+  const uint32_t n_cand = A.n_cand_dev[0] + A.n_cand_dev[1];
   for (;;) {
     uint32_t idx = 0;
     if (lane == 0) idx = atomicAdd(A.next, 1u);
@@ -757,9 +766,39 @@ __global__ void __launch_bounds__(128) im_candidate_kernel(const __grid_constant
     out.base_quality_cutoff = J.I.base_quality_cutoff; out.log10_ref_len = J.I.log10_ref_len;
     out.mutation_cutoff = J.I.mutation_cutoff; out.poly_cutoff = J.I.poly_cutoff;
     out.precision_decimal = J.I.precision_decimal; out.col_offset = col0;
+    out.bq = A.bq; out.n_bq = A.n_bq; out.bq_cap = A.bq_cap;
+    out.pool = A.pool; out.pool_used = A.pool_used; out.pool_cap = A.pool_cap;
     const ColCall cl0 = J.I.call[c];
     score_candidate_column(S, T, out, c, (cl0.flags & (kCandidate | kRecompute)) != 0, (cl0.flags & kRecompute) != 0,
                            cl0, J.I.call, ents, A.scratch_per_warp, hist);
+    __syncwarp();
+  }
+}
+
+// ============================================================================ deferred bounds
+// One warp per bound job: the lower or upper bisection of one RA item, written into its record.
+__global__ void __launch_bounds__(256) im_bounds_kernel(const __grid_constant__ Batch B, CandArgs A, unsigned int* next) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t n_jobs = min(*A.n_bq, A.bq_cap);
+  for (;;) {
+    uint32_t idx = 0;
+    if (lane == 0) idx = atomicAdd(next, 1u);
+    idx = __shfl_sync(0xFFFFFFFFu, idx, 0);
+    if (idx >= n_jobs) break;
+    // jobs are written in (lower, upper) pairs; take every lower bisection first, the longer ones
+    // for consensus calls (their upper test at f = 1 passes at once)
+    const uint32_t half = (n_jobs + 1) / 2;
+    const BoundJob J = A.bq[idx < half ? 2 * idx : 2 * (idx - half) + 1];
+    const uint32_t job = job_of(B.col_begin, B.n_jobs, J.col);
+    const ClassTable& T = B.jobs[job].T;
+    EmList L;
+    L.e = A.pool + J.pool_off;
+    L.m = J.m;
+    const double v = J.side == 0 ? ra_lower_bound(L, T, J.full, J.var, J.fh, J.tol, J.target, J.maxsum, J.n)
+                                 : ra_upper_bound(L, T, J.full, J.var, J.fh, J.tol, J.target, J.maxsum, J.n);
+    if (lane == 0) {
+      if (J.side == 0) A.ra[J.slot].lower = v; else A.ra[J.slot].upper = v;
+    }
     __syncwarp();
   }
 }
@@ -829,9 +868,11 @@ cudaError_t launch_im_column(const Batch& B, int precision, int grid, cudaStream
 cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_counts, uint32_t* total, uint32_t* out,
                            cudaStream_t st) {
   const uint32_t nb = (n + 255) / 256;
-  cand_count_kernel<<<nb, 256, 0, st>>>(call, n, block_counts);
-  scan_kernel<<<1, 1024, 0, st>>>(block_counts, nb, total);
-  cand_scatter_kernel<<<nb, 256, 0, st>>>(call, n, block_counts, out);
+  for (int part = 0; part < 2; part++) {
+    cand_count_kernel<<<nb, 256, 0, st>>>(call, n, block_counts, part);
+    scan_kernel<<<1, 1024, 0, st>>>(block_counts, nb, total + part);
+    cand_scatter_kernel<<<nb, 256, 0, st>>>(call, n, block_counts, out, part, part ? total : nullptr);
+  }
   return cudaGetLastError();
 }
 cudaError_t launch_intervals(const Batch& B, const ColCov* cov, const ColCall* call, uint8_t* keep, uint32_t* block_counts,
@@ -855,6 +896,16 @@ cudaError_t launch_candidates(const Batch& B, const CandArgs& A, uint32_t max_K,
   cudaError_t e = cudaMemsetAsync(A.next, 0, sizeof(unsigned int), st);
   if (e != cudaSuccess) return e;
   im_candidate_kernel<<<(n_warps + 3) / 4, 128, smem, st>>>(B, A, hist_cap);
+  return cudaGetLastError();
+}
+cudaError_t launch_bounds(const Batch& B, const CandArgs& A, unsigned int* next, int sms, uint32_t warps_per_sm,
+                          cudaStream_t st) {
+  if (A.bq == nullptr) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(next, 0, sizeof(unsigned int), st);
+  if (e != cudaSuccess) return e;
+  // one block per SM: a few bisections share an SM's FP64 pipe and the SMs pull jobs as they free up
+  const uint32_t w = std::min<uint32_t>(8, std::max<uint32_t>(1, warps_per_sm));
+  im_bounds_kernel<<<sms, 32 * w, 0, st>>>(B, A, next);
   return cudaGetLastError();
 }
 

@@ -55,10 +55,14 @@ cudaError_t prepare_ec(uint32_t max_bins);
 cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, unsigned int* next, uint32_t max_bins,
                       int grid, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1);
 cudaError_t launch_im_column(const Batch& B, int precision, int grid, cudaStream_t st);
+// Candidate columns in queue order (likely RA items first); total[0], total[1] = the two part sizes.
 cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_counts, uint32_t* total, uint32_t* out,
                            cudaStream_t st);
 cudaError_t launch_intervals(const Batch& B, const ColCov* cov, const ColCall* call, uint8_t* keep, uint32_t* block_counts,
                              uint32_t* total, uint32_t* out_col, ColCov* out_cov, ColCall* out_call, cudaStream_t st);
 cudaError_t launch_candidates(const Batch& B, const CandArgs& A, uint32_t max_K, int n_warps, cudaStream_t st);
+// The deferred frequency bounds the candidate kernel queued (no-op when A.bq is null).
+cudaError_t launch_bounds(const Batch& B, const CandArgs& A, unsigned int* next, int sms, uint32_t warps_per_sm,
+                          cudaStream_t st);
 
 }  // namespace bsq

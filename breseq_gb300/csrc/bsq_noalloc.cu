@@ -155,6 +155,8 @@ cudaError_t launch_noalloc_positions(void* scratch, const DevSample& S, const No
   out.err = counters + 1; out.base_quality_cutoff = J.base_quality_cutoff; out.log10_ref_len = J.log10_ref_len;
   out.mutation_cutoff = J.mutation_cutoff; out.poly_cutoff = J.poly_cutoff; out.precision_decimal = J.precision_decimal;
   out.col_offset = 0;
+  out.bq = nullptr; out.n_bq = nullptr; out.bq_cap = 0;     // bounds inline: no extra device memory
+  out.pool = nullptr; out.pool_used = nullptr; out.pool_cap = 0;
   NoAllocArgs A;
   A.tid = J.tid; A.pos0 = J.pos0; A.n = J.n_positions; A.next = counters; A.failed = J.failed;
   A.gather = reinterpret_cast<uint4*>(base); A.per_warp = J.per_warp; A.n_warps = J.n_warps;

@@ -317,6 +317,7 @@ typedef struct bsq_tuning {
     uint32_t ec_blocks_per_sm;    /* pass-1 blocks per SM (default 8)                            */
     uint32_t col_blocks_per_sm;   /* column-pass blocks of 8 warps per SM (default 8)            */
     uint32_t cand_warps_per_sm;   /* candidate-kernel warps per SM (default 16)                  */
+    uint32_t bound_warps_per_sm;  /* frequency-bound bisections in flight per SM, 1-8 (default 4) */
     int32_t  use_graphs;          /* capture each pass as one CUDA graph, updated in place (default 1) */
 } bsq_tuning;
 int bsq_get_tuning(const bsq_ctx* ctx, bsq_tuning* out);

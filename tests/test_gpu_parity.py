@@ -179,8 +179,9 @@ def test_graphs_and_launch_shapes_do_not_change_results(scorer, loaded, oracle_r
 
     base_ec, base_im = run()
     shapes = [dict(use_graphs=0), dict(use_graphs=1),
-              dict(ec_read_chunk=256, ec_blocks_per_sm=2, col_blocks_per_sm=3, cand_warps_per_sm=4),
-              dict(ec_read_chunk=4096, ec_blocks_per_sm=12, col_blocks_per_sm=12, cand_warps_per_sm=32, use_graphs=0)]
+              dict(ec_read_chunk=256, ec_blocks_per_sm=2, col_blocks_per_sm=3, cand_warps_per_sm=4, bound_warps_per_sm=1),
+              dict(ec_read_chunk=4096, ec_blocks_per_sm=12, col_blocks_per_sm=12, cand_warps_per_sm=32,
+                   bound_warps_per_sm=8, use_graphs=0)]
     try:
         for sh in shapes:
             scorer.set_tuning(**sh)
