@@ -221,6 +221,70 @@ __device__ __forceinline__ bool read_start_counts(const EcArgs& A, const DevRead
 
 // Work units are chunks of one job's reads, pulled by whole blocks from a shared counter; the block's
 // shared histogram belongs to the chunk's job and is flushed at the chunk's end.
+// count_alignment_position for a read with one aligned block (soft clips allowed): its bases are
+// consecutive query positions on consecutive columns and no base has an indel, so each base has
+// event (1) and, below the query end, event (2a).  Lanes take consecutive bases; a forward read's
+// (2a) event uses the next base, the next quality and the next column's reference, which the next
+// lane already holds.  Reference characters are A/C/G/T/N (checked when the sample is loaded).
+__device__ __forceinline__ uint32_t ref_code(uint32_t ch) {   // A,C,G,T -> 0..3 (N handled by the caller)
+  const uint32_t x = (ch >> 1) & 3u;                          // A 0, C 1, G 3, T 2
+  return x ^ (x >> 1);
+}
+__device__ __forceinline__ void ec_simple_read(const DevSample& S, const EcArgs& A, uint32_t* hist, const DevRead& rd,
+                                               uint32_t span, int lane, uint32_t& err) {
+  const bool rev = rd.flags & kRev;
+  const uint32_t rs = rd.rfile, R = A.R, Q = A.Q;
+  if (rs >= R) { err |= kErrCovariate; return; }
+  const uint8_t* bp = S.seq + (rd.seq_off >> 1);   // seq_off is even: the read starts on a byte
+  const uint8_t* qp = S.qual + rd.seq_off;
+  const uint8_t* rp = S.ref + rd.start;
+  const int clip = rd.clip;
+  const int qend = clip + (int)span - 1;
+  for (uint32_t i0 = 0; i0 < span; i0 += 32) {
+    const uint32_t i = i0 + lane;
+    const bool act = i < span;
+    const int qpos = clip + (int)i;
+    uint32_t ob = 15, q = 0, rc = 'N';
+    if (act) {
+      const uint32_t byte = __ldg(bp + (qpos >> 1));
+      ob = (qpos & 1) ? (byte & 15u) : (byte >> 4);
+      q = __ldg(qp + qpos);
+      rc = __ldg(rp + i);
+    }
+    uint32_t ob_n = __shfl_down_sync(0xFFFFFFFFu, ob, 1);
+    uint32_t q_n = __shfl_down_sync(0xFFFFFFFFu, q, 1);
+    uint32_t rc_n = __shfl_down_sync(0xFFFFFFFFu, rc, 1);
+    if (!act) continue;
+    if (lane == 31 && !rev && qpos < qend) {       // its next base belongs to the next trip
+      const uint32_t byte = __ldg(bp + ((qpos + 1) >> 1));
+      ob_n = ((qpos + 1) & 1) ? (byte & 15u) : (byte >> 4);
+      q_n = __ldg(qp + qpos + 1);
+      rc_n = __ldg(rp + i + 1);
+    }
+    uint32_t bin1 = 0xFFFFFFFFu, bin2 = 0xFFFFFFFFu;
+    // (1) the base at this column
+    if (ob != 15 && rc != 'N') {
+      if (__popc(ob) != 1) err |= kErrBase;
+      else {
+        uint32_t oi = __ffs(ob) - 1, ri = ref_code(rc);
+        if (rev) { oi = 3 - oi; ri = 3 - ri; }
+        if (q >= Q) err |= kErrCovariate;
+        else bin1 = rs + R * (ri + 5u * (oi + 5u * q));
+      }
+    }
+    // (2a) '..': the next base (forward) or this base again (reverse) with its quality
+    if (qpos < qend) {
+      const uint32_t ob2 = rev ? ob : ob_n, q2 = rev ? q : q_n, rc2 = rev ? rc : rc_n;
+      if (ob2 != 15 && rc2 != 'N') {
+        if (q2 >= Q) err |= kErrCovariate;
+        else bin2 = rs + R * (4u + 5u * (4u + 5u * q2));
+      }
+    }
+    if (bin1 != 0xFFFFFFFFu) atomicAdd(hist + bin1, 1u);
+    if (bin2 != 0xFFFFFFFFu) atomicAdd(hist + bin2, 1u);
+  }
+}
+
 __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Batch B, const uint4* chunks, uint32_t n_chunks, unsigned int* next) {
   extern __shared__ uint32_t sh_hist[];
   __shared__ uint32_t sh_chunk;
@@ -252,11 +316,7 @@ __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Ba
           A.qs_flag[(size_t)(rd.flags & kRev) * S.n_cols + rd.start] = 1;
       }
       if (red || !A.do_errors) continue;
-      // two bases per lane per trip keep two independent load chains in flight
-      for (uint32_t i = lane; i < span; i += 64) {
-        ec_events(S, A, sh_hist, true, rd, r, rd.start + i, (int)rd.clip + (int)i, 0, err);
-        if (i + 32 < span) ec_events(S, A, sh_hist, true, rd, r, rd.start + i + 32, (int)rd.clip + (int)i + 32, 0, err);
-      }
+      ec_simple_read(S, A, sh_hist, rd, span, lane, err);
       done += span;
     } else {
       // the CIGAR walk of htslib's pileup (resolve_cigar2): M/=/X blocks carry their read bases, the
@@ -401,7 +461,7 @@ __global__ void __launch_bounds__(1024) cov_hist_kernel(const __grid_constant__ 
 constexpr uint32_t kColumnWarps = 8;
 
 template <bool FP64>
-__global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant__ Batch Bt) {
+__global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant__ Batch Bt) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   DevRead* sh_rd = reinterpret_cast<DevRead*>(smem) + warp * 32;
@@ -425,6 +485,34 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
     double S64[5] = {0, 0, 0, 0, 0};
     float s32[5] = {0, 0, 0, 0, 0}, k32[5] = {0, 0, 0, 0, 0}, B[5] = {0, 0, 0, 0, 0};
     const uint2 rr = __ldg(S.tile_range + tile);
+    const bool tile_fast = __all_sync(0xFFFFFFFFu, !failed);
+    // one scored read base of likelihood class k (identify_mutations.cpp:1640-1658)
+    auto accumulate = [&](uint32_t k, int obs) {
+      ++n;
+      if (FP64) {
+        const double* lp = T.lp64 + (size_t)k * 5;
+#pragma unroll
+        for (int b = 0; b < 5; b++) S64[b] += __ldg(lp + b);
+      } else {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(T.lp32 + (size_t)k * 8));
+        const float2 w = __ldg(reinterpret_cast<const float2*>(T.lp32 + (size_t)k * 8 + 4));
+        const float lp[5] = {v.x, v.y, v.z, v.w, w.x};
+#pragma unroll
+        for (int b = 0; b < 5; b++) {          // Kahan-compensated FP32 sums
+          const float y = lp[b] - k32[b];
+          const float tt = s32[b] + y;
+          k32[b] = (tt - s32[b]) - y;
+          s32[b] = tt;
+        }
+        // screen bound  B_v = sum_i max(0, lp_i[v] - lp_i[ref]); zero unless the read's own
+        // base is not its most likely hypothesis or it differs from the reference
+        if (obs != ref_idx || w.y != 0.0f) {
+          const float lr = ref_idx == 0 ? lp[0] : ref_idx == 1 ? lp[1] : ref_idx == 2 ? lp[2] : ref_idx == 3 ? lp[3] : lp[4];
+#pragma unroll
+          for (int b = 0; b < 5; b++) B[b] += fmaxf(0.0f, lp[b] - lr);
+        }
+      }
+    };
     // One read of the batch as this lane sees it: pileup state at column c and the base / quality
     // loads, issued for two reads before either is consumed.
     struct Pend { uint32_t r; bool cov; Pile e; uint8_t base; uint8_t q; };
@@ -473,7 +561,7 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       }
       int obs = 4;
       if (!e.del) {
-        if (P.base & (P.base - 1)) { local_err |= kErrBase; return; }   // not one of A, C, G, T
+        if (__popc(P.base) != 1) { local_err |= kErrBase; return; }     // not one of A, C, G, T
         obs = __ffs(P.base) - 1;
       }
       const uint32_t q = P.q;
@@ -481,30 +569,36 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       if (q >= T.Q || rs >= T.R) { local_err |= kErrCovariate; return; }
       if (q < A.base_quality_cutoff) return;
       const uint32_t k = ((((uint32_t)rd.mapq_idx * T.R + rs) * 2u + (rev ? 1u : 0u)) * T.Q + q) * 5u + (uint32_t)obs;
-      ++n;
-      if (FP64) {
-        const double* lp = T.lp64 + (size_t)k * 5;
-#pragma unroll
-        for (int b = 0; b < 5; b++) S64[b] += __ldg(lp + b);
-      } else {
-        const float4 v = __ldg(reinterpret_cast<const float4*>(T.lp32 + (size_t)k * 8));
-        const float2 w = __ldg(reinterpret_cast<const float2*>(T.lp32 + (size_t)k * 8 + 4));
-        const float lp[5] = {v.x, v.y, v.z, v.w, w.x};
-#pragma unroll
-        for (int b = 0; b < 5; b++) {          // Kahan-compensated FP32 sums
-          const float y = lp[b] - k32[b];
-          const float tt = s32[b] + y;
-          k32[b] = (tt - s32[b]) - y;
-          s32[b] = tt;
-        }
-        // screen bound  B_v = sum_i max(0, lp_i[v] - lp_i[ref]); zero unless the read's own
-        // base is not its most likely hypothesis or it differs from the reference
-        if (obs != ref_idx || w.y != 0.0f) {
-          const float lr = ref_idx == 0 ? lp[0] : ref_idx == 1 ? lp[1] : ref_idx == 2 ? lp[2] : ref_idx == 3 ? lp[3] : lp[4];
-#pragma unroll
-          for (int b = 0; b < 5; b++) B[b] += fmaxf(0.0f, lp[b] - lr);
-        }
+      accumulate(k, obs);
+    };
+    // the reads a lane sees on the common path: one aligned block, unique, untrimmed, a known read
+    // file, in a tile with no failed-fit target column
+    auto fast_read = [&](const DevRead& rd) {
+      return (rd.flags & (kSimple | kRedundant)) == kSimple && (rd.xl == kNoTag || rd.xl == 0) &&
+             (rd.xr == kNoTag || rd.xr == 0) && rd.rfile < T.R;
+    };
+    struct FastPend { bool cov; int qpos; uint32_t byte, q; };
+    auto fast_prep = [&](const DevRead& rd, FastPend& F) {
+      F.cov = real && c >= rd.start && c < rd.end;
+      F.qpos = (int)(c - rd.start) + rd.clip;
+      F.byte = 0; F.q = 0;
+      if (F.cov) {
+        F.byte = __ldg(S.seq + (rd.seq_off >> 1) + (F.qpos >> 1));
+        F.q = __ldg(S.qual + rd.seq_off + F.qpos);
       }
+    };
+    auto fast_consume = [&](const DevRead& rd, const FastPend& F) {
+      if (!F.cov) return;
+      const uint32_t base = (F.qpos & 1) ? (F.byte & 15u) : (F.byte >> 4);
+      if (base == 15) return;                                // N read base: not counted at all
+      const bool rev = rd.flags & kRev;
+      if (rev) ++ubot; else ++utop;
+      if (__popc(base) != 1) { local_err |= kErrBase; return; }
+      const int obs = __ffs(base) - 1;
+      if (F.q >= T.Q) { local_err |= kErrCovariate; return; }
+      if (F.q < A.base_quality_cutoff) return;
+      const uint32_t k = ((((uint32_t)rd.mapq_idx * T.R + rd.rfile) * 2u + (rev ? 1u : 0u)) * T.Q + F.q) * 5u + (uint32_t)obs;
+      accumulate(k, obs);
     };
     for (uint32_t b0 = rr.x; b0 < rr.y; b0 += 32) {
       const uint32_t rl = b0 + lane;
@@ -522,15 +616,25 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
         const int j2 = mask ? __ffs(mask) - 1 : -1;
         if (j2 >= 0) mask &= mask - 1;
         const DevRead rd1 = sh_rd[j1];
-        Pend P1, P2;
-        prep(rd1, b0 + j1, P1);
-        if (j2 >= 0) {
-          const DevRead rd2 = sh_rd[j2];
-          prep(rd2, b0 + j2, P2);
-          consume(rd1, P1);
-          consume(rd2, P2);
+        const DevRead rd2 = sh_rd[j2 >= 0 ? j2 : j1];
+        // warp-uniform choice: both reads on the common path, or the general pileup state
+        const bool f1 = tile_fast && fast_read(rd1), f2 = (j2 < 0) || (tile_fast && fast_read(rd2));
+        if (f1 && f2) {
+          FastPend F1, F2;
+          fast_prep(rd1, F1);
+          if (j2 >= 0) fast_prep(rd2, F2);
+          fast_consume(rd1, F1);
+          if (j2 >= 0) fast_consume(rd2, F2);
         } else {
-          consume(rd1, P1);
+          Pend P1, P2;
+          prep(rd1, b0 + j1, P1);
+          if (j2 >= 0) {
+            prep(rd2, b0 + j2, P2);
+            consume(rd1, P1);
+            consume(rd2, P2);
+          } else {
+            consume(rd1, P1);
+          }
         }
       }
       __syncwarp();
