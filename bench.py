@@ -157,6 +157,14 @@ def _cpu_reference(sample_scale: float, threads: int, min_seconds: float = 0.0):
     return reps * bases / dt, reps * bases, dt, s.total_length(), reps
 
 
+def _calls(im):
+    """The call set of a result (RA records as dicts or as a structured array)."""
+    def b(x):
+        return x.decode() if isinstance(x, bytes) else str(x)
+    return [(int(r["tid"]), int(r["position"]), int(r["insert_position"]), b(r["new_base"]),
+             bool(r["passed_consensus"]), bool(r["passed_polymorphism"])) for r in im["ra"]]
+
+
 def run_reference(args, world, rank, pg):
     if rank != 0:
         return
@@ -198,7 +206,7 @@ def run_ours(args, world, rank, local, pg):
         if record:
             ps = sc.last_pass_stats(); kstats["ec"].append(ps["main_kernel_ms"]); launches[0] += ps["kernel_launches"]
         tab = sc.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
-        im = sc.identify_mutations(sample_id, tab, st, precision=prec)
+        im = sc.identify_mutations(sample_id, tab, st, precision=prec, as_dicts=False)
         if record:
             ps = sc.last_pass_stats(); kstats["im"].append(ps["main_kernel_ms"]); launches[0] += ps["kernel_launches"]
         return im
@@ -226,13 +234,12 @@ def run_ours(args, world, rank, local, pg):
         sc.timer_start()
         ec = sc.error_count(sid)
         tab = sc.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
-        im_plain = sc.identify_mutations(sid, tab, st, precision=0)
+        im_plain = sc.identify_mutations(sid, tab, st, precision=0, as_dicts=False)
         if i > 0:
             t_plain.append(sc.timer_stop())
         else:
             sc.timer_stop()
-    same_calls = [(r["tid"], r["position"], r["insert_position"], r["new_base"]) for r in im_plain["ra"]] == \
-                 [(r["tid"], r["position"], r["insert_position"], r["new_base"]) for r in im["ra"]]
+    same_calls = _calls(im_plain) == _calls(im)
     plain_ms = statistics.mean(t_plain) if t_plain else None
     sc.set_tuning(**tuning)
     # ---- end to end through the C ABI from pinned host buffers
@@ -243,16 +250,31 @@ def run_ours(args, world, rank, local, pg):
             pinned.append(a)
     h2d = int(sum(a.nbytes for a in view._keep))
     e2e_ms = []
-    d2h = 0
+    phases = {"load": [], "pass1": [], "table": [], "pass2": [], "free": []}
+    xfer = {"h2d": 0, "d2h": 0}
     for i in range(args.warmup + args.steps):
         sc.timer_start()
+        t0 = time.perf_counter()
         sid2 = sc.load_sample(s)
-        im2 = step(sid2)
+        t1 = time.perf_counter()
+        ec2 = sc.error_count(sid2)
+        b1 = sc.last_pass_bytes()
+        t2 = time.perf_counter()
+        tab2 = sc.counts_to_log10_prob(ec2["counts"], s.n_read_files, s.n_quality)
+        t3 = time.perf_counter()
+        im2 = sc.identify_mutations(sid2, tab2, st, precision=prec, as_dicts=False)
+        b2 = sc.last_pass_bytes()
+        t4 = time.perf_counter()
         sc.free_sample(sid2)
         t = sc.timer_stop()
+        t5 = time.perf_counter()
         if i >= args.warmup:
             e2e_ms.append(t)
-    d2h = n_cols * 48 + len(im2["ra"]) * 200 + s.n_read_files * 25 * s.n_quality * 8
+            for k, a, b in (("load", t0, t1), ("pass1", t1, t2), ("table", t2, t3), ("pass2", t3, t4), ("free", t4, t5)):
+                phases[k].append(1e3 * (b - a))
+            xfer = {"h2d": b1["h2d"] + b2["h2d"], "d2h": b1["d2h"] + b2["d2h"]}
+    h2d += xfer["h2d"]
+    d2h = xfer["d2h"]
     for a in pinned:
         sc.L.bsq_host_unregister(a.ctypes.data)
     e2e_ms_max = _max_over_ranks(pg, statistics.mean(e2e_ms))
@@ -276,7 +298,8 @@ def run_ours(args, world, rank, local, pg):
         "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD} scaled x{args.scale:g}", "genome_bp": s.total_length(), "reads": n_reads, "read_bases_per_step": bases,
                    "precision": args.precision, "l2": "inputs (%.2f GB) larger than L2" % ((s.qual.nbytes + s.seq.nbytes) / 1e9)},
         "e2e": {"value": world * bases / (e2e_ms_max / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_max,
+                "host_ms_by_phase": {k: statistics.mean(v) for k, v in phases.items()}},
         "gpu_launches": launches[0],
         "plain_fp64": {"ms_per_step": plain_ms, "value": (bases / (plain_ms / 1000.0)) if plain_ms else None,
                        "served_over_plain": (plain_ms / ms) if plain_ms else None, "identical_calls": same_calls},
@@ -307,10 +330,6 @@ def _pool(args):
     return [(synth.simulate(c), poly) for c, poly in cfgs[:args.batch_pool]]
 
 
-def _calls(im):
-    return [(r["tid"], r["position"], r["insert_position"], r["new_base"]) for r in im["ra"]]
-
-
 def run_mix(args, device):
     from breseq_gb300 import abi
     from breseq_gb300.api import ImSettings, Scorer, Server
@@ -337,7 +356,7 @@ def run_mix(args, device):
         ecs = sc.error_count_batch(sids)
         tabs = [sc.counts_to_log10_prob(ec["counts"], pool[k][0].n_read_files, pool[k][0].n_quality)
                 for ec, k in zip(ecs, jobs)]
-        return sc.identify_mutations_batch(sids, tabs, [sets[k] for k in jobs], precision=1)
+        return sc.identify_mutations_batch(sids, tabs, [sets[k] for k in jobs], precision=1, as_dicts=False)
 
     if not args.no_tune:
         ecs = sc.error_count_batch(sids)
@@ -363,7 +382,7 @@ def run_mix(args, device):
         sc.timer_start()
         ec = sc.error_count(sid)
         tab = sc.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
-        im = sc.identify_mutations(sid, tab, sets[k], precision=0)
+        im = sc.identify_mutations(sid, tab, sets[k], precision=0, as_dicts=False)
         plain_ms += sc.timer_stop()
         sc.free_sample(sid)
         same &= _calls(im) == _calls(ims[k])

@@ -169,9 +169,11 @@ class Scorer:
 
     def identify_mutations_batch(self, sids, log10_tables, settings: ImSettings | None = None,
                                  deletion_propagation_cutoff=None, deletion_seed_cutoff=None,
-                                 precision=PRECISION_FP32C, positions=False, n_read_files=None, n_quality=None):
+                                 precision=PRECISION_FP32C, positions=False, n_read_files=None, n_quality=None,
+                                 as_dicts=True):
         """Pass 2 over several resident samples in one launch per kernel.  `log10_tables`, `settings`
-        and the deletion cutoffs are per sample (a list) or shared (one value)."""
+        and the deletion cutoffs are per sample (a list) or shared (one value).  With as_dicts=False
+        the RA / MC / UN records come back as numpy structured arrays of the C structs."""
         sids = list(sids)
         n = len(sids)
 
@@ -198,15 +200,19 @@ class Scorer:
             self._check(self.L.bsq_im_batch_result_copy(self.ctx, j, C.cast(ra, C.c_void_p), n_ra.value,
                                                         C.cast(mc, C.c_void_p), n_mc.value, C.cast(un, C.c_void_p),
                                                         n_un.value))
-            out = dict(ra=abi.ra_to_dicts(ra[:n_ra.value]), mc=abi.mc_to_dicts(mc[:n_mc.value]),
-                       un=abi.un_to_dicts(un[:n_un.value]))
+            if as_dicts:
+                out = dict(ra=abi.ra_to_dicts(ra[:n_ra.value]), mc=abi.mc_to_dicts(mc[:n_mc.value]),
+                           un=abi.un_to_dicts(un[:n_un.value]))
+            else:   # the C records as numpy structured arrays (no per-item Python objects)
+                out = dict(ra=np.ctypeslib.as_array(ra)[:n_ra.value], mc=np.ctypeslib.as_array(mc)[:n_mc.value],
+                           un=np.ctypeslib.as_array(un)[:n_un.value])
             if jobs[j][2] is not None:
                 out["positions"] = jobs[j][2]
             outs.append(out)
         return outs
 
     def identify_mutations(self, sid: int, log10_table, settings: ImSettings | None = None, **kw):
-        return self.identify_mutations_batch([sid], [log10_table], settings, **kw)[0]
+        return self.identify_mutations_batch([sid], [log10_table], [settings], **kw)[0]
 
     # ------------------------------------------------------------------ launch shapes
     def tuning(self) -> dict:
@@ -244,6 +250,11 @@ class Scorer:
         ms = C.c_double()
         self._check(self.L.bsq_timer_stop(self.ctx, C.byref(ms)))
         return ms.value
+
+    def last_pass_bytes(self):
+        h, d = C.c_uint64(), C.c_uint64()
+        self._check(self.L.bsq_last_pass_bytes(self.ctx, C.byref(h), C.byref(d)))
+        return dict(h2d=h.value, d2h=d.value)
 
     def last_pass_stats(self):
         ms, launches, main = C.c_double(), C.c_uint32(), C.c_double()

@@ -111,6 +111,7 @@ struct bsq_ctx {
   std::vector<std::vector<bsq_un_record>> res_un;
   double last_ms = 0, main_ms = 0;
   uint32_t launches = 0;
+  uint64_t last_h2d = 0, last_d2h = 0;   // bytes the last pass call copied each way
   uint64_t last_candidates = 0;
 };
 
@@ -334,11 +335,6 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
     if (t >= T) return fail(ctx, BSQ_ERR_INVALID, "target_order entry out of range");
     called[t] = 1;
   }
-  for (uint64_t i = 0; i < total; i++) {
-    const char ch = ref->seq[i];
-    if (ch != 'A' && ch != 'C' && ch != 'G' && ch != 'T' && ch != 'N')
-      return fail(ctx, BSQ_ERR_DATA, "reference base outside A/C/G/T/N");
-  }
   cudaStream_t st = ctx->load_streams[ctx->load_rr.fetch_add(1) % bsq_ctx::kLoadStreams];
   // reference, one '\0' separator after each target
   CK(s->ref.alloc(s->n_cols + 64, st));
@@ -388,9 +384,12 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   po.reads = s->reads.as<DevRead>(); po.qb = s->qb.as<QBounds>(); po.rstart = s->rstart.as<uint32_t>();
   po.mapq = s->mapq.as<uint8_t>(); po.err = stats; po.maxspan = stats + 1; po.mapq_mask = stats + 2;
   CK(launch_pack(in, po, st));
+  // the reference checked on the device: [11] bytes outside A/C/G/T/N, [12] zero bytes (separators)
+  CK(launch_ref_check(s->ref.as<uint8_t>(), s->n_cols, stats + 11, stats + 12, ctx->sms, st));
   uint32_t h[16];
   CK(cudaMemcpyAsync(h, stats, 16 * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  if (h[11] || h[12] != T) return fail(ctx, BSQ_ERR_DATA, "reference base outside A/C/G/T/N");
   if (h[0]) return fail(ctx, (h[0] & (kErrOrder | kErrCigar | kErrBounds | kErrX1)) ? BSQ_ERR_INVALID : BSQ_ERR_DATA,
                         "invalid records: " + err_text(h[0]));
   s->maxspan = std::max<uint32_t>(1, h[1]);
@@ -535,6 +534,8 @@ static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_p
   CK(cudaStreamSynchronize(st));
   const float ms = elapsed(ctx->ev0, ctx->ev1), mms = elapsed(ctx->evm0, ctx->evm1);
   ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 4;
+  ctx->last_h2d += std::max<size_t>(16, n_chunks * sizeof(uint4));
+  ctx->last_d2h += res_bytes;
   int rc = BSQ_OK;
   for (uint32_t j = 0; j < n; j++) {
     const uint32_t err = *reinterpret_cast<const uint32_t*>(ctx->pin_out.at(lay[j].err));
@@ -573,7 +574,7 @@ static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_p
 
 int bsq_error_count_batch(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_params* P, bsq_ec_result* out) {
   if (!ctx || !ids || !P || !out || n == 0) return fail(ctx, BSQ_ERR_INVALID, "null argument");
-  ctx->last_ms = 0; ctx->main_ms = 0; ctx->launches = 0;
+  ctx->last_ms = 0; ctx->main_ms = 0; ctx->launches = 0; ctx->last_h2d = 0; ctx->last_d2h = 0;
   for (uint32_t g = 0; g < n; g += kBatchJobs) {
     const int rc = ec_group(ctx, std::min(kBatchJobs, n - g), ids + g, P + g, out + g);
     if (rc != BSQ_OK) return rc;
@@ -766,6 +767,11 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
   const uint32_t n_cand = ctl_host[kCtlCand] + ctl_host[kCtlCand2], nk = ctl_host[kCtlKept], n_ra = ctl_host[kCtlRa];
   const uint32_t cerr = ctl_host[kCtlCandErr];
   ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 13;
+  ctx->last_h2d += arena_bytes;
+  ctx->last_d2h += (uint64_t)kCtlWords * 4 + (uint64_t)n_ra * (sizeof(RaDev) + 2 * Qh * 4) +
+                   (uint64_t)nk * (4 + sizeof(ColCov) + sizeof(ColCall));
+  for (uint32_t j = 0; j < n; j++)
+    if (pos_out && pos_out[j]) ctx->last_d2h += (uint64_t)smp[j]->n_cols * (sizeof(ColCov) + sizeof(ColCall));
   ctx->last_candidates += n_cand;
   if (n_ra > ra_cap) return fail(ctx, BSQ_ERR_NOMEM, "identify_mutations: RA buffer overflow");
   if (cerr & ~kErrRaOverflow) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(cerr));
@@ -836,7 +842,7 @@ int bsq_identify_mutations_batch(bsq_ctx* ctx, uint32_t n, const int32_t* ids, c
                                  const double* const* tables, bsq_position_arrays* const* pos_out) {
   if (!ctx || !ids || !P || !tables || n == 0) return fail(ctx, BSQ_ERR_INVALID, "null argument");
   ctx->res_ra.assign(n, {}); ctx->res_mc.assign(n, {}); ctx->res_un.assign(n, {});
-  ctx->last_ms = 0; ctx->main_ms = 0; ctx->launches = 0; ctx->last_candidates = 0;
+  ctx->last_ms = 0; ctx->main_ms = 0; ctx->launches = 0; ctx->last_candidates = 0; ctx->last_h2d = 0; ctx->last_d2h = 0;
   for (uint32_t g = 0; g < n; g += kBatchJobs) {
     const int rc = im_group(ctx, std::min(kBatchJobs, n - g), ids + g, P + g, tables + g,
                             pos_out ? pos_out + g : nullptr, g);
@@ -886,6 +892,13 @@ int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_
   if (device_ms) *device_ms = ctx->last_ms;
   if (kernel_launches) *kernel_launches = ctx->launches;
   if (main_kernel_ms) *main_kernel_ms = ctx->main_ms;
+  return BSQ_OK;
+}
+
+int bsq_last_pass_bytes(const bsq_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes) {
+  if (!ctx) return BSQ_ERR_INVALID;
+  if (h2d_bytes) *h2d_bytes = ctx->last_h2d;
+  if (d2h_bytes) *d2h_bytes = ctx->last_d2h;
   return BSQ_OK;
 }
 

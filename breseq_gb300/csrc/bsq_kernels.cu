@@ -20,9 +20,31 @@ namespace bsq {
 // ============================================================================ pack + validate
 // One thread per record: builds the 32-byte DevRead, the query bounds of complex reads, checks the
 // record (sortedness, CIGAR, offsets) and gathers the sample statistics the tile kernels need.
-__global__ void pack_reads_kernel(RawSoA in, PackOut out) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= in.n) return;
+// Per-block accumulation of the sample-wide maximum reference span and MAPQ presence bits: one
+// global atomic per block instead of one per read (a read-per-thread atomic on a single word
+// serialises in L2).
+__device__ __forceinline__ void pack_flush(uint32_t span, uint8_t mq, bool has, const PackOut& out) {
+  __shared__ uint32_t sh_span, sh_mask[8];
+  if (threadIdx.x == 0) sh_span = 0;
+  if (threadIdx.x < 8) sh_mask[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t wspan = __reduce_max_sync(0xFFFFFFFFu, has ? span : 0u);
+  uint32_t wmask[8];
+#pragma unroll
+  for (int w = 0; w < 8; w++) wmask[w] = __reduce_or_sync(0xFFFFFFFFu, (has && (mq >> 5) == w) ? (1u << (mq & 31)) : 0u);
+  if ((threadIdx.x & 31) == 0) {
+    if (wspan) atomicMax(&sh_span, wspan);
+#pragma unroll
+    for (int w = 0; w < 8; w++) if (wmask[w]) atomicOr(&sh_mask[w], wmask[w]);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && sh_span) atomicMax(out.maxspan, sh_span);
+  if (threadIdx.x < 8 && sh_mask[threadIdx.x]) atomicOr(out.mapq_mask + threadIdx.x, sh_mask[threadIdx.x]);
+}
+
+// Validates and packs record i; returns its reference span and MAPQ when the pileup keeps it.
+__device__ __forceinline__ void pack_one(const RawSoA& in, const PackOut& out, uint32_t i, uint32_t& span_out,
+                                         uint8_t& mq_out, bool& kept) {
   const int32_t tid = in.tid[i], pos = in.pos[i];
   const uint16_t flag = in.flag[i];
   uint32_t err = 0;
@@ -102,10 +124,18 @@ __global__ void pack_reads_kernel(RawSoA in, PackOut out) {
   out.rstart[i] = d.start;
   out.mapq[i] = mq;
   if (err) atomicOr(out.err, err);
-  if (!skip) {
-    atomicMax(out.maxspan, rlen);
-    atomicOr(out.mapq_mask + (mq >> 5), 1u << (mq & 31));
-  }
+  span_out = rlen;
+  mq_out = mq;
+  kept = !skip;
+}
+
+__global__ void pack_reads_kernel(RawSoA in, PackOut out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t span = 0;
+  uint8_t mq = 0;
+  bool kept = false;
+  if (i < in.n) pack_one(in, out, i, span, mq, kept);
+  pack_flush(span, mq, kept, out);   // every thread of the block, from this one place
 }
 
 // apply the host's MAPQ -> class index map
@@ -916,6 +946,29 @@ static int grid_for(uint32_t work, int per_block, int sms, int min_blocks_per_sm
   return (int)g;
 }
 
+// Reference characters of the padded column space: every byte of a target is one of A/C/G/T/N and
+// the only zero bytes are the one separator after each target.  Counts both kinds for the host.
+__global__ void ref_check_kernel(const uint8_t* ref, uint32_t n_cols, uint32_t* bad, uint32_t* zeros) {
+  uint32_t nb = 0, nz = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_cols; i += gridDim.x * blockDim.x) {
+    const uint8_t ch = __ldg(ref + i);
+    nz += ch == 0;
+    nb += !(ch == 0 || ch == 'A' || ch == 'C' || ch == 'G' || ch == 'T' || ch == 'N');
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    nb += __shfl_xor_sync(0xFFFFFFFFu, nb, o);
+    nz += __shfl_xor_sync(0xFFFFFFFFu, nz, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (nb) atomicAdd(bad, nb);
+    if (nz) atomicAdd(zeros, nz);
+  }
+}
+cudaError_t launch_ref_check(const uint8_t* ref, uint32_t n_cols, uint32_t* bad, uint32_t* zeros, int sms, cudaStream_t st) {
+  ref_check_kernel<<<sms * 4, 256, 0, st>>>(ref, n_cols, bad, zeros);
+  return cudaGetLastError();
+}
 cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st) {
   if (in.n == 0) return cudaSuccess;
   pack_reads_kernel<<<(in.n + 255) / 256, 256, 0, st>>>(in, out);

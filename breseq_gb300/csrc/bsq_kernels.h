@@ -41,6 +41,8 @@ struct PackOut {
 };
 
 cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st);
+// Counts reference bytes outside A/C/G/T/N/separator into *bad and zero bytes into *zeros.
+cudaError_t launch_ref_check(const uint8_t* ref, uint32_t n_cols, uint32_t* bad, uint32_t* zeros, int sms, cudaStream_t st);
 cudaError_t launch_mapq_index(DevRead* reads, const uint8_t* mapq, const uint8_t* map, uint32_t n, cudaStream_t st);
 cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t n_tiles, uint32_t maxspan,
                               uint2* tile_range, uint32_t* max_tile_reads, cudaStream_t st);

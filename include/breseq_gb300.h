@@ -333,6 +333,9 @@ int bsq_autotune(bsq_ctx* ctx, uint32_t n, const int32_t* sample_ids, const bsq_
 int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_launches,
                         double* main_kernel_ms);
 
+/* Bytes the last pass call copied host-to-device and device-to-host (staged inputs, results). */
+int bsq_last_pass_bytes(const bsq_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
+
 /* ---------------------------------------------------------------- scoring without allocation */
 
 /* Raw values of one RA item as the scoring kernel writes them (device memory).  `column` is the

@@ -198,3 +198,17 @@ def test_graphs_and_launch_shapes_do_not_change_results(scorer, loaded, oracle_r
             assert all(compare.identical(a[k], b[k]) for k in ("ra", "mc", "un"))
     finally:
         scorer.set_tuning(**default)
+
+
+@pytest.mark.parametrize("bad", [b"X", b"\0", b"a"])
+def test_reference_characters_checked_at_load(scorer, bad):
+    """A reference byte outside A/C/G/T/N (including a NUL inside a target, or lower case) is a
+    data error at load; the sample is not kept."""
+    import dataclasses
+    from breseq_gb300 import _lib
+    s = samples.clonal_small()
+    ref = s.ref_seq.copy()
+    ref[1000] = bad[0]
+    with pytest.raises(_lib.BsqError) as e:
+        scorer.load_sample(dataclasses.replace(s, ref_seq=ref))
+    assert e.value.code == -3
