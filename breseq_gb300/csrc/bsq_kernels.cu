@@ -256,6 +256,20 @@ __device__ __forceinline__ bool read_start_counts(const EcArgs& A, const DevRead
 // event (1) and, below the query end, event (2a).  Lanes take consecutive bases; a forward read's
 // (2a) event uses the next base, the next quality and the next column's reference, which the next
 // lane already holds.  Reference characters are A/C/G/T/N (checked when the sample is loaded).
+// Packed pairs of FP32 values (element 0 in the low word): Blackwell's two-wide FP32 add / sub.
+__device__ __forceinline__ unsigned long long f32x2_add(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ unsigned long long f32x2_sub(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ float f32x2_lo(unsigned long long x) { return __uint_as_float((uint32_t)x); }
+__device__ __forceinline__ float f32x2_hi(unsigned long long x) { return __uint_as_float((uint32_t)(x >> 32)); }
+
 __device__ __forceinline__ uint32_t ref_code(uint32_t ch) {   // A,C,G,T -> 0..3 (N handled by the caller)
   const uint32_t x = (ch >> 1) & 3u;                          // A 0, C 1, G 3, T 2
   return x ^ (x >> 1);
@@ -265,6 +279,8 @@ __device__ __forceinline__ void ec_simple_read(const DevSample& S, const EcArgs&
   const bool rev = rd.flags & kRev;
   const uint32_t rs = rd.rfile, R = A.R, Q = A.Q;
   if (rs >= R) { err |= kErrCovariate; return; }
+  const uint32_t flip = rev ? 3u : 0u;              // 3 - x == x ^ 3 for x in 0..3
+  const uint32_t nbins = R * 25u * Q;               // slots nbins + lane absorb events that do not count
   const uint8_t* bp = S.seq + (rd.seq_off >> 1);   // seq_off is even: the read starts on a byte
   const uint8_t* qp = S.qual + rd.seq_off;
   const uint8_t* rp = S.ref + rd.start;
@@ -281,37 +297,34 @@ __device__ __forceinline__ void ec_simple_read(const DevSample& S, const EcArgs&
       q = __ldg(qp + qpos);
       rc = __ldg(rp + i);
     }
-    uint32_t ob_n = __shfl_down_sync(0xFFFFFFFFu, ob, 1);
-    uint32_t q_n = __shfl_down_sync(0xFFFFFFFFu, q, 1);
-    uint32_t rc_n = __shfl_down_sync(0xFFFFFFFFu, rc, 1);
-    if (!act) continue;
-    if (lane == 31 && !rev && qpos < qend) {       // its next base belongs to the next trip
-      const uint32_t byte = __ldg(bp + ((qpos + 1) >> 1));
-      ob_n = ((qpos + 1) & 1) ? (byte & 15u) : (byte >> 4);
-      q_n = __ldg(qp + qpos + 1);
-      rc_n = __ldg(rp + i + 1);
+    // the base after this trip's last one, read by every lane from one address
+    uint32_t ob32 = 15, q32 = 0, rc32 = 'N';
+    if (i0 + 32 < span) {
+      const int qn = clip + (int)i0 + 32;
+      const uint32_t byte = __ldg(bp + (qn >> 1));
+      ob32 = (qn & 1) ? (byte & 15u) : (byte >> 4);
+      q32 = __ldg(qp + qn);
+      rc32 = __ldg(rp + i0 + 32);
     }
-    uint32_t bin1 = 0xFFFFFFFFu, bin2 = 0xFFFFFFFFu;
+    const uint32_t sob = __shfl_down_sync(0xFFFFFFFFu, ob, 1);
+    const uint32_t sq = __shfl_down_sync(0xFFFFFFFFu, q, 1);
+    const uint32_t src = __shfl_down_sync(0xFFFFFFFFu, rc, 1);
+    const uint32_t ob_n = lane == 31 ? ob32 : sob, q_n = lane == 31 ? q32 : sq, rc_n = lane == 31 ? rc32 : src;
     // (1) the base at this column
-    if (ob != 15 && rc != 'N') {
-      if (__popc(ob) != 1) err |= kErrBase;
-      else {
-        uint32_t oi = __ffs(ob) - 1, ri = ref_code(rc);
-        if (rev) { oi = 3 - oi; ri = 3 - ri; }
-        if (q >= Q) err |= kErrCovariate;
-        else bin1 = rs + R * (ri + 5u * (oi + 5u * q));
-      }
-    }
+    const bool ev1 = act && ob != 15 && rc != 'N';
+    const bool base_ok = __popc(ob) == 1;
+    const bool q_ok = q < Q;
+    err |= (ev1 && !base_ok) ? kErrBase : 0u;
+    err |= (ev1 && base_ok && !q_ok) ? kErrCovariate : 0u;
+    const uint32_t oi = (uint32_t)(__ffs(ob) - 1) ^ flip, ri = ref_code(rc) ^ flip;
+    const uint32_t bin1 = (ev1 && base_ok && q_ok) ? rs + R * (ri + 5u * (oi + 5u * q)) : nbins + (uint32_t)lane;
     // (2a) '..': the next base (forward) or this base again (reverse) with its quality
-    if (qpos < qend) {
-      const uint32_t ob2 = rev ? ob : ob_n, q2 = rev ? q : q_n, rc2 = rev ? rc : rc_n;
-      if (ob2 != 15 && rc2 != 'N') {
-        if (q2 >= Q) err |= kErrCovariate;
-        else bin2 = rs + R * (4u + 5u * (4u + 5u * q2));
-      }
-    }
-    if (bin1 != 0xFFFFFFFFu) atomicAdd(hist + bin1, 1u);
-    if (bin2 != 0xFFFFFFFFu) atomicAdd(hist + bin2, 1u);
+    const uint32_t ob2 = rev ? ob : ob_n, q2 = rev ? q : q_n, rc2 = rev ? rc : rc_n;
+    const bool ev2 = act && qpos < qend && ob2 != 15 && rc2 != 'N';
+    err |= (ev2 && q2 >= Q) ? kErrCovariate : 0u;
+    const uint32_t bin2 = (ev2 && q2 < Q) ? rs + R * (24u + 25u * q2) : nbins + (uint32_t)lane;
+    atomicAdd(hist + bin1, 1u);
+    atomicAdd(hist + bin2, 1u);
   }
 }
 
@@ -328,7 +341,7 @@ __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Ba
   const DevSample& S = B.jobs[ch.x].S;
   const EcArgs& A = B.jobs[ch.x].E;
   const uint32_t nbins = A.R * 25u * A.Q;
-  for (uint32_t i = threadIdx.x; i < nbins; i += blockDim.x) sh_hist[i] = 0;
+  for (uint32_t i = threadIdx.x; i < nbins + 32; i += blockDim.x) sh_hist[i] = 0;
   __syncthreads();
   uint32_t err = 0;
   uint32_t done = 0;
@@ -513,7 +526,10 @@ __global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant
     double redtop = 0.0, redbot = 0.0;
     bool uonly = true, slots = false;
     double S64[5] = {0, 0, 0, 0, 0};
-    float s32[5] = {0, 0, 0, 0, 0}, k32[5] = {0, 0, 0, 0, 0}, B[5] = {0, 0, 0, 0, 0};
+    // Kahan sums of hypotheses 0-1 and 2-3 as packed FP32 pairs (one f32x2 instruction per step for
+    // two sums, the same IEEE operations per element), hypothesis 4 scalar
+    unsigned long long s01 = 0, s23 = 0, k01 = 0, k23 = 0;
+    float s4 = 0.0f, k4 = 0.0f, B[5] = {0, 0, 0, 0, 0};
     const uint2 rr = __ldg(S.tile_range + tile);
     const bool tile_fast = __all_sync(0xFFFFFFFFu, !failed);
     // one scored read base of likelihood class k (identify_mutations.cpp:1640-1658)
@@ -524,19 +540,22 @@ __global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant
 #pragma unroll
         for (int b = 0; b < 5; b++) S64[b] += __ldg(lp + b);
       } else {
-        const float4 v = __ldg(reinterpret_cast<const float4*>(T.lp32 + (size_t)k * 8));
+        const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(T.lp32 + (size_t)k * 8));
         const float2 w = __ldg(reinterpret_cast<const float2*>(T.lp32 + (size_t)k * 8 + 4));
-        const float lp[5] = {v.x, v.y, v.z, v.w, w.x};
-#pragma unroll
-        for (int b = 0; b < 5; b++) {          // Kahan-compensated FP32 sums
-          const float y = lp[b] - k32[b];
-          const float tt = s32[b] + y;
-          k32[b] = (tt - s32[b]) - y;
-          s32[b] = tt;
+        {                                       // Kahan-compensated FP32 sums
+          const unsigned long long y01 = f32x2_sub(v.x, k01), y23 = f32x2_sub(v.y, k23);
+          const unsigned long long t01 = f32x2_add(s01, y01), t23 = f32x2_add(s23, y23);
+          k01 = f32x2_sub(f32x2_sub(t01, s01), y01);
+          k23 = f32x2_sub(f32x2_sub(t23, s23), y23);
+          s01 = t01; s23 = t23;
+          const float y4 = w.x - k4, t4 = s4 + y4;
+          k4 = (t4 - s4) - y4;
+          s4 = t4;
         }
         // screen bound  B_v = sum_i max(0, lp_i[v] - lp_i[ref]); zero unless the read's own
         // base is not its most likely hypothesis or it differs from the reference
         if (obs != ref_idx || w.y != 0.0f) {
+          const float lp[5] = {f32x2_lo(v.x), f32x2_hi(v.x), f32x2_lo(v.y), f32x2_hi(v.y), w.x};
           const float lr = ref_idx == 0 ? lp[0] : ref_idx == 1 ? lp[1] : ref_idx == 2 ? lp[2] : ref_idx == 3 ? lp[3] : lp[4];
 #pragma unroll
           for (int b = 0; b < 5; b++) B[b] += fmaxf(0.0f, lp[b] - lr);
@@ -697,6 +716,8 @@ __global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant
             cl.flags |= kCandidate;            // the plain form runs the EM wherever a base was scored
             if (best != ref_idx && score > 0) cl.flags |= kLikelyRa;
           } else {
+            const float s32[5] = {f32x2_lo(s01), f32x2_hi(s01), f32x2_lo(s23), f32x2_hi(s23), s4};
+            const float k32[5] = {f32x2_lo(k01), f32x2_hi(k01), f32x2_lo(k23), f32x2_hi(k23), k4};
             double tot[5];
 #pragma unroll
             for (int b = 0; b < 5; b++) tot[b] = (double)s32[b] - (double)k32[b];
@@ -999,13 +1020,13 @@ int column_grid(uint32_t total_tiles, int sms, uint32_t blocks_per_sm) {
   return grid_for(total_tiles, kColumnWarps, sms, (int)std::max<uint32_t>(1, blocks_per_sm));
 }
 cudaError_t prepare_ec(uint32_t max_bins) {
-  const size_t smem = (size_t)max_bins * sizeof(uint32_t);
+  const size_t smem = (size_t)(max_bins + 32) * sizeof(uint32_t);
   if (smem <= 48 * 1024) return cudaSuccess;
   return cudaFuncSetAttribute(ec_read_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, unsigned int* next, uint32_t max_bins,
                       int grid, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1) {
-  const size_t smem = (size_t)max_bins * sizeof(uint32_t);
+  const size_t smem = (size_t)(max_bins + 32) * sizeof(uint32_t);   // + one discard slot per lane
   cudaError_t e = cudaMemsetAsync(next, 0, sizeof(unsigned int), st);
   if (e != cudaSuccess) return e;
   if (main0 && (e = record_event(main0, st)) != cudaSuccess) return e;
