@@ -12,6 +12,7 @@
 #include <atomic>
 #include <memory>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -182,6 +183,23 @@ static SampleDev* find_sample(bsq_ctx* ctx, int32_t id) {
 // Runs `enqueue` on the context's stream.  With graphs on, the work is captured and launched as one
 // CUDA graph; the executable graph is kept and updated in place for the next call of the same shape
 // (the node list of a pass does not depend on the number of jobs), else instantiated anew.
+// f(0..n-1) on up to 16 host threads (the calling thread included); items are independent.
+template <class F>
+static void parallel_for(uint32_t n, F&& f) {
+  const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const uint32_t nt = std::min<uint32_t>(n, std::min<uint32_t>(hw, 16));
+  if (nt <= 1) {
+    for (uint32_t i = 0; i < n; i++) f(i);
+    return;
+  }
+  std::atomic<uint32_t> next{0};
+  auto work = [&]() { for (uint32_t i; (i = next.fetch_add(1)) < n;) f(i); };
+  std::vector<std::thread> th;
+  for (uint32_t t = 1; t < nt; t++) th.emplace_back(work);
+  work();
+  for (std::thread& t : th) t.join();
+}
+
 // Timing event inside a pass: recorded as an event node when the pass is captured (a plain record
 // in a capture only orders the capture and is never recorded).
 static cudaError_t record(cudaEvent_t ev, cudaStream_t st) {
@@ -623,9 +641,11 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
   std::vector<uint32_t> tile_b(n + 1, 0), col_b(n + 1, 0);
   uint32_t max_K = 0, per_warp = 32, Qh = 0;
   size_t off = 0;
+  parallel_for(n, [&](uint32_t j) {
+    host::build_class_table(tables[j], P[j].n_read_files, P[j].n_quality, smp[j]->mapq_values, ct[j]);
+  });
   for (uint32_t j = 0; j < n; j++) {
     const SampleDev* s = smp[j];
-    host::build_class_table(tables[j], P[j].n_read_files, P[j].n_quality, s->mapq_values, ct[j]);
     lay[j].lp64 = off; off = align256(off + ct[j].lp64.size() * 8);
     lay[j].r64 = off; off = align256(off + ct[j].r64.size() * 8);
     lay[j].lpmax64 = off; off = align256(off + ct[j].lpmax64.size() * 8);

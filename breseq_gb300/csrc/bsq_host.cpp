@@ -17,6 +17,32 @@ static const double kNaN = std::numeric_limits<double>::quiet_NaN();
 static const uint32_t kUndef = 0xFFFFFFFFu;
 static const char kChars[6] = {'A', 'C', 'G', 'T', '.', 'N'};
 
+// printf("%.6g") followed by strtod, without the text: for |x| in [1e-17, 1e6) the six significant
+// digits are m = round(|x| * 10^k) with k = 5 - floor(log10|x|) and 10^k exact, and the parsed value is
+// the correctly rounded quotient m / 10^k, which one IEEE division gives.  The product |x| * 10^k is
+// within one ulp of exact, so a fraction within 1e-7 of one half (a possible tie or misrounding), an
+// exponent estimate that lands outside [1e5, 1e6), and every other case take the text route.
+static double round_sig6_text(double x) {
+  char txt[48];
+  snprintf(txt, sizeof txt, "%.6g", x);
+  return strtod(txt, nullptr);
+}
+double round_sig6(double x) {
+  static const double p10[23] = {1e0, 1e1, 1e2, 1e3, 1e4, 1e5, 1e6, 1e7, 1e8, 1e9, 1e10, 1e11,
+                                 1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+  const double ax = fabs(x);
+  if (!(ax >= 1e-17 && ax < 1e6)) return round_sig6_text(x);
+  const int k = 5 - (int)floor(log10(ax));
+  if (k < 0 || k > 22) return round_sig6_text(x);
+  const double y = ax * p10[k];
+  if (!(y >= 100000.0 && y < 999999.5)) return round_sig6_text(x);
+  const double fl = floor(y), fr = y - fl;
+  if (fabs(fr - 0.5) < 1e-7) return round_sig6_text(x);
+  const double m = fr > 0.5 ? fl + 1.0 : fl;
+  const double v = m / p10[k];
+  return x < 0 ? -v : v;
+}
+
 void counts_to_log10_prob(const uint64_t* counts, uint32_t R, uint32_t Q, double* out) {
   for (uint32_t q = 0; q < Q; q++)
     for (uint32_t ref = 0; ref < 5; ref++)
@@ -27,9 +53,7 @@ void counts_to_log10_prob(const uint64_t* counts, uint32_t R, uint32_t Q, double
         const double denom = log10(total + 5.0);
         for (uint32_t obs = 0; obs < 5; obs++) {
           const size_t i = base + (size_t)R * 5 * obs;
-          char txt[48];
-          snprintf(txt, sizeof txt, "%.6g", log10((double)(counts[i] + 1)) - denom);
-          out[i] = strtod(txt, nullptr);
+          out[i] = round_sig6(log10((double)(counts[i] + 1)) - denom);
         }
       }
 }

@@ -13,6 +13,8 @@ namespace host {
 // counts_to_log10_prob + the 6-significant-digit text round trip of error_rates.tab
 // (src/breseq/error_count.cpp:629-690, 1005-1026).
 void counts_to_log10_prob(const uint64_t* counts, uint32_t R, uint32_t Q, double* out);
+// x as printf("%.6g") then strtod give it back (bit-exact).
+double round_sig6(double x);
 
 struct ClassTableHost {
   std::vector<double> lp64, r64, lpmax64;

@@ -5,6 +5,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 from breseq_gb300 import _lib, abi
 
@@ -35,12 +36,16 @@ def test_version_and_no_device_error(built_lib):
         L.bsq_destroy(ctx)
 
 
-def test_counts_to_log10_prob_matches_oracle(built_lib, oracle_lib):
+@pytest.mark.parametrize("seed", range(12))
+def test_counts_to_log10_prob_matches_oracle(built_lib, oracle_lib, seed):
+    """The library rounds to six significant digits without text; the oracle prints with %.6g and
+    parses back.  Bit-exact over tables from sparse to 10^12-deep counts."""
     from oracle import pyoracle as po
-    rng = np.random.default_rng(3)
-    R, Q = 2, 42
-    counts = rng.integers(0, 10**7, size=R * 25 * Q).astype(np.uint64)
-    counts[::7] = 0
+    rng = np.random.default_rng(seed)
+    R, Q = (1, 42) if seed % 3 == 0 else (2, 64)
+    top = [10**3, 10**7, 10**12][seed % 3]
+    counts = rng.integers(0, top, size=R * 25 * Q).astype(np.uint64)
+    counts[rng.random(counts.size) < 0.3] = 0
     out = np.zeros(R * 25 * Q)
     L = _lib.load()
     assert L.bsq_counts_to_log10_prob(abi.ptr(counts, C.c_uint64), R, Q, abi.ptr(out, C.c_double)) == 0
