@@ -354,8 +354,8 @@ def run_mix(args, device):
 
     def batch_step():
         ecs = sc.error_count_batch(sids)
-        tabs = [sc.counts_to_log10_prob(ec["counts"], pool[k][0].n_read_files, pool[k][0].n_quality)
-                for ec, k in zip(ecs, jobs)]
+        tabs = sc.counts_to_log10_prob_batch([ec["counts"] for ec in ecs], [pool[k][0].n_read_files for k in jobs],
+                                             [pool[k][0].n_quality for k in jobs])
         return sc.identify_mutations_batch(sids, tabs, [sets[k] for k in jobs], precision=1, as_dicts=False)
 
     if not args.no_tune:

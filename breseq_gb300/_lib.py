@@ -63,6 +63,8 @@ def load():
     L.bsq_format_ra.argtypes = [C.c_void_p, C.c_char_p, C.c_uint32, C.c_char_p, C.c_uint64]
     L.bsq_write_gd.argtypes = [C.c_char_p, P(abi.Reference), P(C.c_char_p), P(C.c_double), C.c_uint32, C.c_void_p,
                                C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64]
+    L.bsq_counts_to_log10_prob_batch.argtypes = [C.c_uint32, P(P(C.c_uint64)), P(C.c_uint32), P(C.c_uint32),
+                                                 P(P(C.c_double))]
     L.bsq_last_pass_bytes.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_uint64)]
     L.bsq_get_tuning.argtypes = [C.c_void_p, P(abi.Tuning)]
     L.bsq_set_tuning.argtypes = [C.c_void_p, P(abi.Tuning)]
@@ -93,7 +95,7 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_sample_footprint", "bsq_error_count", "bsq_counts_to_log10_prob", "bsq_identify_mutations",
             "bsq_im_result_counts", "bsq_im_result_copy",
             "bsq_error_count_batch", "bsq_identify_mutations_batch", "bsq_im_batch_result_counts",
-            "bsq_im_batch_result_copy", "bsq_last_pass_bytes", "bsq_get_tuning", "bsq_set_tuning", "bsq_autotune",
+            "bsq_im_batch_result_copy", "bsq_counts_to_log10_prob_batch", "bsq_last_pass_bytes", "bsq_get_tuning", "bsq_set_tuning", "bsq_autotune",
             "bsq_job_footprint", "bsq_server_create", "bsq_server_destroy",
             "bsq_server_last_error", "bsq_server_submit", "bsq_server_wait", "bsq_server_job_info",
             "bsq_server_job_error", "bsq_server_error_counts", "bsq_server_results", "bsq_server_release",

@@ -147,6 +147,16 @@ class Scorer:
         self._check(self.L.bsq_counts_to_log10_prob(abi.ptr(c, C.c_uint64), R, Q, abi.ptr(out, C.c_double)))
         return out
 
+    def counts_to_log10_prob_batch(self, counts_list, Rs, Qs):
+        """Tables of several samples at once (host threads); per-sample R, Q lists."""
+        n = len(counts_list)
+        cs = [np.ascontiguousarray(c, dtype=np.uint64) for c in counts_list]
+        outs = [np.zeros(int(R) * 25 * int(Q), dtype=np.float64) for R, Q in zip(Rs, Qs)]
+        self._check(self.L.bsq_counts_to_log10_prob_batch(
+            n, (C.POINTER(C.c_uint64) * n)(*[abi.ptr(c, C.c_uint64) for c in cs]), (C.c_uint32 * n)(*Rs),
+            (C.c_uint32 * n)(*Qs), (C.POINTER(C.c_double) * n)(*[abi.ptr(o, C.c_double) for o in outs])))
+        return outs
+
     # ------------------------------------------------------------------ pass 2
     def _im_job(self, sid, log10_table, st, deletion_propagation_cutoff, deletion_seed_cutoff, precision, positions,
                 n_read_files, n_quality):

@@ -610,6 +610,15 @@ int bsq_counts_to_log10_prob(const uint64_t* counts, uint32_t R, uint32_t Q, dou
   return BSQ_OK;
 }
 
+int bsq_counts_to_log10_prob_batch(uint32_t n, const uint64_t* const* counts, const uint32_t* R, const uint32_t* Q,
+                                   double* const* out) {
+  if (!counts || !R || !Q || !out) return BSQ_ERR_INVALID;
+  for (uint32_t j = 0; j < n; j++)
+    if (!counts[j] || !out[j] || R[j] == 0 || Q[j] == 0) return BSQ_ERR_INVALID;
+  parallel_for(n, [&](uint32_t j) { host::counts_to_log10_prob(counts[j], R[j], Q[j], out[j]); });
+  return BSQ_OK;
+}
+
 // ============================================================================ pass 2
 // Control words of pass 2, written on the device and read back in one copy.
 enum : uint32_t { kCtlCand = 0, kCtlCand2 = 1, kCtlKept = 2, kCtlRa = 3, kCtlCandErr = 4, kCtlBq = 5, kCtlPool = 6,
@@ -834,27 +843,27 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
     jra[j].push_back(d);
     jqh[j].insert(jqh[j].end(), qh.begin() + (size_t)i * 2 * Qh, qh.begin() + (size_t)(i + 1) * 2 * Qh);
   }
-  size_t kp = 0;
-  for (uint32_t j = 0; j < n; j++) {
+  // the kept columns of each job: a range of the (column-sorted) compacted list
+  std::vector<size_t> kb(n + 1, 0);
+  for (uint32_t j = 0; j < n; j++)
+    kb[j + 1] = (size_t)(std::lower_bound(kept.begin(), kept.end(), col_b[j + 1]) - kept.begin());
+  parallel_for(n, [&](uint32_t j) {
     SampleDev* s = smp[j];
     host::SampleLayout L;
     L.tpoff = &s->tpoff; L.toff = &s->toff; L.order = &s->order;
     host::assemble_ra(jra[j], jqh[j], Qh, L, ctx->res_ra[job0 + j]);
-    std::vector<uint32_t> kc;
-    std::vector<ColCov> kv;
-    std::vector<ColCall> kl;
-    for (; kp < nk && kept[kp] < col_b[j + 1]; kp++) {
-      kc.push_back(kept[kp] - col_b[j]);
-      kv.push_back(kcov[kp]);
-      kl.push_back(kcall[kp]);
-    }
     if (pos_out && pos_out[j]) {   // dense arrays fetched anyway: run the state machines over every column
       host::intervals(pcov[j], pcall[j], L, &P[j], ctx->res_mc[job0 + j], ctx->res_un[job0 + j]);
       host::fill_positions(pcov[j], pcall[j], L, pos_out[j]);
     } else {
+      std::vector<uint32_t> kc;
+      kc.reserve(kb[j + 1] - kb[j]);
+      for (size_t i = kb[j]; i < kb[j + 1]; i++) kc.push_back(kept[i] - col_b[j]);
+      const std::vector<ColCov> kv(kcov.begin() + kb[j], kcov.begin() + kb[j + 1]);
+      const std::vector<ColCall> kl(kcall.begin() + kb[j], kcall.begin() + kb[j + 1]);
       host::intervals_sparse(kc, kv, kl, L, &P[j], ctx->res_mc[job0 + j], ctx->res_un[job0 + j]);
     }
-  }
+  });
   return BSQ_OK;
 }
 

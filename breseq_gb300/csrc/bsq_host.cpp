@@ -99,7 +99,9 @@ void build_class_table(const double* tab, uint32_t R, uint32_t Q, const std::vec
   }
 }
 
-static double log_choose(double n, double k) { return lgamma(n + 1) - lgamma(k + 1) - lgamma(n - k + 1); }
+// lgamma_r: the reentrant form (lgamma writes the global signgam), so batches assemble in parallel
+static double lg(double x) { int sign; return lgamma_r(x, &sign); }
+static double log_choose(double n, double k) { return lg(n + 1) - lg(k + 1) - lg(n - k + 1); }
 
 double fisher_2x2(uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   const uint32_t row1 = a + b, row2 = c + d, col1 = a + c, col2 = b + d, n = row1 + row2;

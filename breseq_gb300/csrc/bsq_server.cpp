@@ -160,17 +160,21 @@ struct bsq_server {
     if (rc != BSQ_OK) { e = std::string("error_count: ") + bsq_last_error(ctx); return rc; }
     std::vector<bsq_im_params> ip(n);
     std::vector<const double*> tabs(n);
+    std::vector<const uint64_t*> cptr(n);
+    std::vector<double*> tptr(n);
+    std::vector<uint32_t> Rs(n), Qs(n);
     for (uint32_t i = 0; i < n; i++) {
       Job* j = js[i];
       const uint32_t R = j->desc.im.n_read_files, Q = j->desc.im.n_quality;
       if (R != ep[i].n_read_files || Q != ep[i].n_quality) { e = "error table dimensions differ between passes"; return BSQ_ERR_INVALID; }
       j->table.assign((size_t)R * 25 * Q, 0.0);
-      rc = bsq_counts_to_log10_prob(j->counts.data(), R, Q, j->table.data());
-      if (rc != BSQ_OK) { e = "counts_to_log10_prob failed"; return rc; }
+      cptr[i] = j->counts.data(); tptr[i] = j->table.data(); Rs[i] = R; Qs[i] = Q;
       ip[i] = j->desc.im;
       ip[i].precision = precision;
       tabs[i] = j->table.data();
     }
+    rc = bsq_counts_to_log10_prob_batch(n, cptr.data(), Rs.data(), Qs.data(), tptr.data());
+    if (rc != BSQ_OK) { e = "counts_to_log10_prob failed"; return rc; }
     rc = bsq_identify_mutations_batch(ctx, n, ids.data(), ip.data(), tabs.data(), nullptr);
     if (rc != BSQ_OK) { e = std::string("identify_mutations: ") + bsq_last_error(ctx); return rc; }
     for (uint32_t i = 0; i < n; i++) {

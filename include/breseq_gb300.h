@@ -284,6 +284,9 @@ int bsq_error_count(bsq_ctx* ctx, int32_t sample_id, const bsq_ec_params* p, bsq
  * digits (write_log10_prob_table, :660-690) and parsed back (read_log10_prob_table, :629-654).
  * log10_prob must hold R*5*5*Q doubles. */
 int bsq_counts_to_log10_prob(const uint64_t* counts, uint32_t n_read_files, uint32_t n_quality, double* log10_prob);
+/* The same for n tables at once (host threads). */
+int bsq_counts_to_log10_prob_batch(uint32_t n, const uint64_t* const* counts, const uint32_t* n_read_files,
+                                   const uint32_t* n_quality, double* const* log10_prob);
 
 /* Pass 2.  Replaces identify_mutations() (src/breseq/identify_mutations.cpp:48-88) for RA, MC, UN
  * and the coverage table.  Results are kept in the context until the next call and read with

@@ -56,3 +56,20 @@ def test_struct_sizes_match_header():
     # bsq_ra_record layout shared by the library, the oracle and the bindings
     assert C.sizeof(abi.RaRecord) == 4 * 3 + 4 + 8 * 2 + 8 * 5 + 8 * 6 + 4 * 10 + 4 + 4
     assert C.sizeof(abi.McRecord) == 6 * 4 + 4 * 8
+
+
+def test_counts_to_log10_prob_batch_equals_single(built_lib):
+    rng = np.random.default_rng(11)
+    L = _lib.load()
+    shapes = [(1, 42), (2, 42), (2, 64), (3, 30)]
+    counts = [rng.integers(0, 10**6, size=R * 25 * Q).astype(np.uint64) for R, Q in shapes]
+    outs = [np.zeros(R * 25 * Q) for R, Q in shapes]
+    n = len(shapes)
+    rc = L.bsq_counts_to_log10_prob_batch(n, (C.POINTER(C.c_uint64) * n)(*[abi.ptr(c, C.c_uint64) for c in counts]),
+                                          (C.c_uint32 * n)(*[R for R, _ in shapes]), (C.c_uint32 * n)(*[Q for _, Q in shapes]),
+                                          (C.POINTER(C.c_double) * n)(*[abi.ptr(o, C.c_double) for o in outs]))
+    assert rc == 0
+    for (R, Q), c, o in zip(shapes, counts, outs):
+        single = np.zeros(R * 25 * Q)
+        assert L.bsq_counts_to_log10_prob(abi.ptr(c, C.c_uint64), R, Q, abi.ptr(single, C.c_double)) == 0
+        assert np.array_equal(o, single)
