@@ -503,11 +503,38 @@ __global__ void __launch_bounds__(1024) cov_hist_kernel(const __grid_constant__ 
 // base and quality loads of two reads in flight before either is consumed.
 constexpr uint32_t kColumnWarps = 8;
 
+// Per-thread shared-memory accumulators of the column pass, structure of arrays (thread t's values at
+// index t of each array: no bank conflicts): the screen bound B[5] and the redundant-read counts and
+// 1/X1 weights per strand.
+struct ColRare {
+  float* b;          // [5][256]
+  uint32_t* cnt;     // [2][256]
+  double* w;         // [2][256]
+  uint32_t t;
+  __device__ ColRare(unsigned char* base, uint32_t tid)
+      : b(reinterpret_cast<float*>(base)), cnt(reinterpret_cast<uint32_t*>(base + 5 * 256 * 4)),
+        w(reinterpret_cast<double*>(base + 7 * 256 * 4)), t(tid) {}
+  __device__ void clear() {
+#pragma unroll
+    for (int i = 0; i < 5; i++) b[i * 256 + t] = 0.0f;
+    cnt[t] = cnt[256 + t] = 0;
+    w[t] = w[256 + t] = 0.0;
+  }
+  __device__ float& B(int i) { return b[i * 256 + t]; }
+  __device__ void redundant(bool rev, double weight) { cnt[rev * 256 + t] += 1; w[rev * 256 + t] += weight; }
+  __device__ uint32_t raw(bool rev) const { return cnt[rev * 256 + t]; }
+  __device__ double weight(bool rev) const { return w[rev * 256 + t]; }
+};
+constexpr size_t kColRareBytes = 256 * (5 * 4 + 2 * 4 + 2 * 8);
+
 template <bool FP64>
-__global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant__ Batch Bt) {
+__global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant__ Batch Bt) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   DevRead* sh_rd = reinterpret_cast<DevRead*>(smem) + warp * 32;
+  // accumulators only rare reads touch (mismatching or low-likelihood bases, redundant reads): one
+  // shared-memory slot per thread, column by column, instead of registers held for the whole tile
+  ColRare rare(smem + kColumnWarps * 32 * sizeof(DevRead), threadIdx.x);
   uint32_t local_err = 0;
   for (uint32_t gt = blockIdx.x * nwarps + warp; gt < Bt.total_tiles; gt += gridDim.x * nwarps) {
     const uint32_t job = job_of(Bt.tile_begin, Bt.n_jobs, gt);
@@ -522,14 +549,14 @@ __global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant
     const bool real = inr && refc != 0 && __ldg(S.tgt_called + t);
     const bool failed = real && __ldg(S.tgt_failed + t);
     const int ref_idx = chr_idx(refc) < 0 ? 5 : chr_idx(refc);
-    uint32_t utop = 0, ubot = 0, rtop = 0, rbot = 0, n = 0;
-    double redtop = 0.0, redbot = 0.0;
+    uint32_t utop = 0, ubot = 0, n = 0;
+    rare.clear();
     bool uonly = true, slots = false;
     double S64[5] = {0, 0, 0, 0, 0};
     // Kahan sums of hypotheses 0-1 and 2-3 as packed FP32 pairs (one f32x2 instruction per step for
     // two sums, the same IEEE operations per element), hypothesis 4 scalar
     unsigned long long s01 = 0, s23 = 0, k01 = 0, k23 = 0;
-    float s4 = 0.0f, k4 = 0.0f, B[5] = {0, 0, 0, 0, 0};
+    float s4 = 0.0f, k4 = 0.0f;
     const uint2 rr = __ldg(S.tile_range + tile);
     const bool tile_fast = __all_sync(0xFFFFFFFFu, !failed);
     // one scored read base of likelihood class k (identify_mutations.cpp:1640-1658)
@@ -558,7 +585,7 @@ __global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant
           const float lp[5] = {f32x2_lo(v.x), f32x2_hi(v.x), f32x2_lo(v.y), f32x2_hi(v.y), w.x};
           const float lr = ref_idx == 0 ? lp[0] : ref_idx == 1 ? lp[1] : ref_idx == 2 ? lp[2] : ref_idx == 3 ? lp[3] : lp[4];
 #pragma unroll
-          for (int b = 0; b < 5; b++) B[b] += fmaxf(0.0f, lp[b] - lr);
+          for (int b = 0; b < 5; b++) rare.B(b) += fmaxf(0.0f, lp[b] - lr);
         }
       }
     };
@@ -589,14 +616,14 @@ __global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant
         // tabulate_position_coverage (identify_mutations.cpp:2218-2250)
         if (e.del || P.base == 15) return;
         if (!red) { if (rev) ++ubot; else ++utop; }
-        else { double w = 1.0 / (double)__ldg(S.x1 + P.r); if (rev) { redbot += w; ++rbot; } else { redtop += w; ++rtop; } }
+        else rare.redundant(rev, 1.0 / (double)__ldg(S.x1 + P.r));
         return;
       }
       if (!e.del && P.base == 15) return;                     // N read base: not counted at all
       if (red) {
         uonly = false;
         const double w = 1.0 / (double)__ldg(S.x1 + P.r);
-        if (rev) { redbot += w; ++rbot; } else { redtop += w; ++rtop; }
+        rare.redundant(rev, w);
         return;
       }
       if (rev) ++ubot; else ++utop;
@@ -659,7 +686,7 @@ __global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant
       }
       unsigned mask = __ballot_sync(0xFFFFFFFFu, rel);
       __syncwarp();
-      while (mask) {                                  // reads in BAM order, two at a time
+      while (mask) {                                  // reads in BAM order, up to four at a time
         const int j1 = __ffs(mask) - 1;
         mask &= mask - 1;
         const int j2 = mask ? __ffs(mask) - 1 : -1;
@@ -668,6 +695,30 @@ __global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant
         const DevRead rd2 = sh_rd[j2 >= 0 ? j2 : j1];
         // warp-uniform choice: both reads on the common path, or the general pileup state
         const bool f1 = tile_fast && fast_read(rd1), f2 = (j2 < 0) || (tile_fast && fast_read(rd2));
+        if (f1 && f2 && j2 >= 0 && mask) {
+          // two more common-path reads: four reads' base and quality loads in flight
+          const int j3 = __ffs(mask) - 1;
+          const unsigned rest = mask & (mask - 1);
+          const int j4 = rest ? __ffs(rest) - 1 : -1;
+          // records read in place from shared memory: four register copies would spill
+          const DevRead& r1 = sh_rd[j1];
+          const DevRead& r2 = sh_rd[j2];
+          const DevRead& r3 = sh_rd[j3];
+          const DevRead& r4 = sh_rd[j4 >= 0 ? j4 : j3];
+          if (fast_read(r3) && (j4 < 0 || fast_read(r4))) {
+            mask = j4 >= 0 ? (rest & (rest - 1)) : rest;
+            FastPend F1, F2, F3, F4;
+            fast_prep(r1, F1);
+            fast_prep(r2, F2);
+            fast_prep(r3, F3);
+            if (j4 >= 0) fast_prep(r4, F4);
+            fast_consume(r1, F1);
+            fast_consume(r2, F2);
+            fast_consume(r3, F3);
+            if (j4 >= 0) fast_consume(r4, F4);
+            continue;
+          }
+        }
         if (f1 && f2) {
           FastPend F1, F2;
           fast_prep(rd1, F1);
@@ -690,8 +741,8 @@ __global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant
     }
     if (inr) {
       ColCov cv;
-      cv.uniq_top = utop; cv.uniq_bot = ubot; cv.rawred_top = rtop; cv.rawred_bot = rbot;
-      cv.red_top = redtop; cv.red_bot = redbot;
+      cv.uniq_top = utop; cv.uniq_bot = ubot; cv.rawred_top = rare.raw(false); cv.rawred_bot = rare.raw(true);
+      cv.red_top = rare.weight(false); cv.red_bot = rare.weight(true);
       ColCall cl;
       cl.n = n; cl.best = 5; cl.score = __longlong_as_double(0x7ff8000000000000ll); cl.flags = 0;
       cl.pad[0] = cl.pad[1] = 0;
@@ -738,7 +789,7 @@ __global__ void __launch_bounds__(256, 3) im_column_kernel(const __grid_constant
             if (best != ref_idx && score > 0) cl.flags |= kCandidate | kLikelyRa;
             float bmax = 0.0f;
 #pragma unroll
-            for (int b = 0; b < 5; b++) if (b != ref_idx) bmax = fmaxf(bmax, B[b]);
+            for (int b = 0; b < 5; b++) if (b != ref_idx) bmax = fmaxf(bmax, rare.B(b));
             if (ref_idx == 5 || (double)bmax - A.log10_ref_len >= A.poly_cutoff - (double)A.screen_margin)
               cl.flags |= kCandidate;
           }
@@ -1038,7 +1089,7 @@ cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, un
   return cudaGetLastError();
 }
 cudaError_t launch_im_column(const Batch& B, int precision, int grid, cudaStream_t st) {
-  const size_t smem = kColumnWarps * 32 * sizeof(DevRead);
+  const size_t smem = kColumnWarps * 32 * sizeof(DevRead) + kColRareBytes;
   if (precision == 0) im_column_kernel<true><<<grid, 32 * kColumnWarps, smem, st>>>(B);
   else im_column_kernel<false><<<grid, 32 * kColumnWarps, smem, st>>>(B);
   return cudaGetLastError();
