@@ -175,7 +175,7 @@ struct EmList { const uint2* e; uint32_t m; };
 // the E-step sums are sum_w[b] = f[b] g[b].  With `ll` the sweep also returns an FP32 estimate of
 // sum_i log10 s_i (error well below 1e-3 for a few thousand reads).
 __device__ __forceinline__ void em_class(const EmList& L, const ClassTable& T, const double f[5], uint32_t i,
-                                         double a[5], float& lls, bool want_ll) {
+                                         double a[5], float& lls, float& las, bool want_ll) {
   const uint2 e = L.e[i];
   const double cnt = (double)e.y;
   const double* r = T.r64 + (size_t)e.x * 5;
@@ -188,7 +188,11 @@ __device__ __forceinline__ void em_class(const EmList& L, const ClassTable& T, c
     const double w = cnt / s;
 #pragma unroll
     for (int b = 0; b < 5; b++) a[b] += rv[b] * w;
-    if (want_ll) lls += (float)e.y * log10f((float)s);
+    if (want_ll) {
+      const float lg = log10f((float)s);
+      lls += (float)e.y * lg;
+      las += (float)e.y * fabsf(lg);
+    }
   } else {
     // the reference's fallback keeps sum_w = n exact: each read adds f[b] to sum_w[b], i.e. 1 to g[b]
 #pragma unroll
@@ -197,27 +201,42 @@ __device__ __forceinline__ void em_class(const EmList& L, const ClassTable& T, c
 }
 
 __device__ void em_sweep(const EmList& L, const ClassTable& T, const double f[5], unsigned allowed, double g[5],
-                         float* ll) {
+                         float* ll, float* la = nullptr) {
   // two classes per lane in flight: the FP64 chains of a class are short and latency-bound
   double a0[5] = {0, 0, 0, 0, 0}, a1[5] = {0, 0, 0, 0, 0};
-  float l0 = 0.0f, l1 = 0.0f;
+  float l0 = 0.0f, l1 = 0.0f, m0 = 0.0f, m1 = 0.0f;
   const bool want = ll != nullptr;
   uint32_t i = threadIdx.x & 31;
   for (; i + 32 < L.m; i += 64) {
-    em_class(L, T, f, i, a0, l0, want);
-    em_class(L, T, f, i + 32, a1, l1, want);
+    em_class(L, T, f, i, a0, l0, m0, want);
+    em_class(L, T, f, i + 32, a1, l1, m1, want);
   }
-  if (i < L.m) em_class(L, T, f, i, a0, l0, want);
+  if (i < L.m) em_class(L, T, f, i, a0, l0, m0, want);
   double a[5];
 #pragma unroll
   for (int b = 0; b < 5; b++) a[b] = ((allowed >> b) & 1) ? a0[b] + a1[b] : 0.0;
   warp_sum5(a, g);
   if (ll) {
-    float lls = l0 + l1;
+    float lls = l0 + l1, las = m0 + m1;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) lls += __shfl_xor_sync(0xFFFFFFFFu, lls, o);
+    for (int o = 16; o > 0; o >>= 1) {
+      lls += __shfl_xor_sync(0xFFFFFFFFu, lls, o);
+      las += __shfl_xor_sync(0xFFFFFFFFu, las, o);
+    }
     *ll = lls;
+    if (la) *la = las;
   }
+}
+
+// A bound on |FP32 estimate - exact FP64 value| of sum_i cnt_i log10 s_i from one sweep: s_i rounded to
+// float (2^-24 relative: 2.6e-8 absolute in log10), log10f (at most 2 ulp), the product with cnt_i
+// (2^-24 relative) and the FP32 accumulation, a chain of at most m/64 + 1 adds per lane accumulator
+// plus one join and five shuffle levels, each adding 2^-24 of the running magnitude, which never
+// exceeds A = sum_i cnt_i |log10 s_i|.  Doubled, plus 1e-9 for the difference between this EM's FP64
+// trajectory and the reference's.
+__device__ __forceinline__ double ll_margin(uint32_t n, uint32_t m, float A) {
+  const double chain = (double)(m / 64 + 8);
+  return 2.0 * (3.0e-8 * (double)n + (2.5e-7 + chain * 6.0e-8) * (double)A) + 1e-9;
 }
 
 // sum_i (log10 s_i + max_i) in FP64 at frequencies f, as the reference accumulates its likelihood
@@ -325,13 +344,13 @@ __device__ double em_profile(const EmList& L, const ClassTable& T, const double 
 // FP32 estimate with a margin that covers its error; anything closer runs the exact FP64 evaluation.
 __device__ bool em_profile_ge(const EmList& L, const ClassTable& T, const double full[5], int v, double ff,
                               double tol, double target, double maxsum, uint32_t n) {
-  const double margin = 1e-3 + 2e-6 * (double)n;
   double f[5], fprev[5];
   em_profile_init(full, v, ff, f);
   for (int it = 0; it < 50; it++) {
     double g[5];
-    float llf;
-    em_sweep(L, T, f, 31u, g, &llf);
+    float llf, la;
+    em_sweep(L, T, f, 31u, g, &llf, &la);
+    const double margin = ll_margin(n, L.m, la);
     const double ll = maxsum + (double)llf;
     if (ll - margin >= target) return true;
     double gmax = -DBL_MAX, dot = 0;
