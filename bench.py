@@ -275,9 +275,31 @@ def run_ours(args, world, rank, local, pg):
             xfer = {"h2d": b1["h2d"] + b2["h2d"], "d2h": b1["d2h"] + b2["d2h"]}
     h2d += xfer["h2d"]
     d2h = xfer["d2h"]
+    # ---- end to end as a stream of samples: the next step's upload (its own load stream) runs while
+    # this step's passes do; every step's host-to-device copy and result read stay inside the timed
+    # region, which starts with the first step's upload and ends after the last step's free
+    import concurrent.futures as cf
+
+    def run_stream(k):
+        with cf.ThreadPoolExecutor(1) as ex:
+            sc.timer_start()
+            fut = ex.submit(sc.load_sample, s)
+            for i in range(k):
+                sid_i = fut.result()
+                if i + 1 < k:
+                    fut = ex.submit(sc.load_sample, s)
+                ec_i = sc.error_count(sid_i)
+                tab_i = sc.counts_to_log10_prob(ec_i["counts"], s.n_read_files, s.n_quality)
+                sc.identify_mutations(sid_i, tab_i, st, precision=prec, as_dicts=False)
+                sc.free_sample(sid_i)
+            return sc.timer_stop()
+
+    run_stream(args.warmup)
+    stream_ms = run_stream(args.steps) / args.steps
     for a in pinned:
         sc.L.bsq_host_unregister(a.ctypes.data)
-    e2e_ms_max = _max_over_ranks(pg, statistics.mean(e2e_ms))
+    e2e_seq_ms = _max_over_ranks(pg, statistics.mean(e2e_ms))
+    e2e_ms_max = _max_over_ranks(pg, stream_ms)
     # ---- roofline of the dominant kernel
     hbm, peak_kind = _peaks()
     ec_ms = statistics.mean(kstats["ec"]); im_ms = statistics.mean(kstats["im"])
@@ -299,7 +321,9 @@ def run_ours(args, world, rank, local, pg):
                    "precision": args.precision, "l2": "inputs (%.2f GB) larger than L2" % ((s.qual.nbytes + s.seq.nbytes) / 1e9)},
         "e2e": {"value": world * bases / (e2e_ms_max / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_max,
-                "host_ms_by_phase": {k: statistics.mean(v) for k, v in phases.items()}},
+                "mode": "stream: step i+1's upload overlaps step i's passes",
+                "sequential": {"value": world * bases / (e2e_seq_ms / 1000.0), "ms_per_step": e2e_seq_ms,
+                               "host_ms_by_phase": {k: statistics.mean(v) for k, v in phases.items()}}},
         "gpu_launches": launches[0],
         "plain_fp64": {"ms_per_step": plain_ms, "value": (bases / (plain_ms / 1000.0)) if plain_ms else None,
                        "served_over_plain": (plain_ms / ms) if plain_ms else None, "identical_calls": same_calls},
