@@ -43,8 +43,8 @@ WORKLOAD = "ecoli_clonal_4.79Mb_pe150_2x100x"
 # DRAM bytes (read + write) per aligned read-base of one launch, from an ncu capture of the same
 # workload at 0.25x genome length (profiles/im_column_kernel_ecoli_clonal_x0.25.md,
 # profiles/ec_read_kernel_ecoli_clonal_x0.25.md), scaled linearly with read-bases
-IM_COLUMN_DRAM_PER_BASE = 0.5668e9 / 0.2441e9
-EC_READ_DRAM_PER_BASE = 0.4250e9 / 0.2441e9
+IM_COLUMN_DRAM_PER_BASE = 0.5843e9 / 0.2441e9
+EC_READ_DRAM_PER_BASE = 0.4251e9 / 0.2441e9
 # the plain FP64 form: same kernels, FP64 everywhere, one sample per call, launched without graphs
 PLAIN_TUNING = dict(ec_read_chunk=1024, ec_blocks_per_sm=8, col_blocks_per_sm=8, cand_warps_per_sm=16,
                     bound_warps_per_sm=4, use_graphs=0)
