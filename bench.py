@@ -75,7 +75,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                                          "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
@@ -214,10 +214,10 @@ def run_ours(args, world, rank, local, pg):
     ec0 = sc.error_count(sid)
     tab0 = sc.counts_to_log10_prob(ec0["counts"], s.n_read_files, s.n_quality)
     tuning = sc.autotune([sid], [tab0], st, precision=prec) if not args.no_tune else sc.tuning()
+    clocks = ClockSampler(local)   # sampling from the warm-up on, so the short timed region is covered
+    clocks.start()
     for _ in range(args.warmup):
         ref_im = step(sid)
-    clocks = ClockSampler(local)
-    clocks.start()
     _barrier(pg)
     sc.timer_start()
     for _ in range(args.steps):
