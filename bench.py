@@ -472,7 +472,7 @@ def main():
     ap.add_argument("--batch-pool", type=int, default=16, help="distinct samples the jobs are drawn from")
     ap.add_argument("--batch-scale", type=float, default=0.25, help="genome length scale of the mixed samples")
     ap.add_argument("--batch-steps", type=int, default=3)
-    ap.add_argument("--served-jobs", type=int, default=96)
+    ap.add_argument("--served-jobs", type=int, default=288)
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     args = ap.parse_args()

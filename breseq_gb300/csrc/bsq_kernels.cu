@@ -158,7 +158,9 @@ __global__ void tile_range_kernel(const uint32_t* rstart, uint32_t n_reads, uint
   b = n_reads;
   while (a < b) { uint32_t m = (a + b) >> 1; if (__ldg(rstart + m) < hi_key) a = m + 1; else b = m; }
   tile_range[t] = make_uint2(lo, a);
-  atomicMax(max_tile_reads, a - lo);
+  const unsigned act = __activemask();
+  const uint32_t wmax = __reduce_max_sync(act, a - lo);   // one atomic per warp
+  if ((threadIdx.x & 31) == __ffs(act) - 1) atomicMax(max_tile_reads, wmax);
 }
 
 // ============================================================================ pass 1: error counts
