@@ -416,8 +416,17 @@ def run_mix(args, device):
                               "batched_over_plain": job_bases / (batch_ms / 1000.0) / plain_rate},
                "identical_calls": bool(same), "tuning": tuning}
     sc.close()
-    # ---- served: open-loop Poisson arrivals into the scoring server
-    cap = len(jobs) / (batch_ms / 1000.0)     # jobs/s the batched form sustains
+    # ---- served: the server's own capacity (every job submitted at once, completions per second),
+    # then open-loop Poisson arrivals at 0.5 / 1 / 2 x that capacity
+    batched_cap = len(jobs) / (batch_ms / 1000.0)     # jobs/s the batched form sustains
+    n_sat = args.served_jobs
+    with Server(device, hbm_budget=args.budget_gb * 1e9, max_batch_jobs=64) as srv:
+        srv.set_tuning(**tuning)
+        sat_ids = [(srv.submit(pool[i % P][0], sets[i % P], view=views[i % P]), i % P) for i in range(n_sat)]
+        sat_infos = [srv.wait(j) for j, _ in sat_ids]
+    sat_span = (max(i["done_ms"] for i in sat_infos) - min(i["submit_ms"] for i in sat_infos)) / 1000.0
+    cap = n_sat / sat_span
+    sat_value = sum(pool_bases[k] for _, k in sat_ids) / sat_span
     levels = []
     rng = np.random.default_rng(7)
     for rho in (0.5, 1.0, 2.0):
@@ -425,6 +434,7 @@ def run_mix(args, device):
         n = args.served_jobs
         arrivals = np.cumsum(rng.exponential(1.0 / lam, size=n))
         with Server(device, hbm_budget=args.budget_gb * 1e9, max_batch_jobs=64) as srv:
+            srv.set_tuning(**tuning)   # the batched leg's autotuned launch shapes
             ids = []
             t0 = time.perf_counter()
             for i in range(n):
@@ -446,12 +456,14 @@ def run_mix(args, device):
                        "served_over_plain": bases / span / plain_rate, "max_round_jobs": st["max_round_jobs"],
                        "max_resident_jobs": st["max_resident_jobs"], "peak_hbm_gb": st["peak_in_use"] / 1e9,
                        "rounds": st["rounds"], "gpu_busy_frac": st["gpu_busy_ms"] / 1000.0 / span,
+                       "round_phase_ms": st["phase_ms"],
                        "mean_stage_ms": stage})
     from breseq_gb300 import _lib
     L = _lib.load()
     for a in pinned:
         L.bsq_host_unregister(a.ctypes.data)
-    served = {"capacity_jobs_s": cap, "budget_gb": args.budget_gb, "levels": levels,
+    served = {"capacity_jobs_s": cap, "capacity_value": sat_value, "batched_capacity_jobs_s": batched_cap,
+              "budget_gb": args.budget_gb, "levels": levels,
               "p50_ms": levels[1]["p50_ms"], "p99_ms": levels[1]["p99_ms"], "plain_fp64_value": plain_rate}
     return batched, served
 

@@ -87,6 +87,7 @@ def load():
                                      C.c_void_p, C.c_uint64]
     L.bsq_server_release.argtypes = [C.c_void_p, C.c_uint64]
     L.bsq_server_get_stats.argtypes = [C.c_void_p, P(abi.ServerStats)]
+    L.bsq_server_set_tuning.argtypes = [C.c_void_p, P(abi.Tuning)]
     _lib = L
     return L
 
@@ -99,7 +100,7 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_job_footprint", "bsq_server_create", "bsq_server_destroy",
             "bsq_server_last_error", "bsq_server_submit", "bsq_server_wait", "bsq_server_job_info",
             "bsq_server_job_error", "bsq_server_error_counts", "bsq_server_results", "bsq_server_release",
-            "bsq_server_get_stats", "bsq_last_pass_stats", "bsq_timer_start",
+            "bsq_server_get_stats", "bsq_server_set_tuning", "bsq_last_pass_stats", "bsq_timer_start",
             "bsq_timer_stop", "bsq_host_register", "bsq_host_unregister", "bsq_score_positions_noalloc",
             "bsq_default_ra_settings", "bsq_test_ra_evidence", "bsq_write_error_rates", "bsq_write_base_qual_error_prob",
             "bsq_write_coverage_distribution", "bsq_write_coverage_table", "bsq_format_ra", "bsq_write_gd")

@@ -179,7 +179,7 @@ class JobInfo(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("jobs_done", C.c_uint64), ("rounds", C.c_uint64), ("budget", C.c_uint64), ("in_use", C.c_uint64),
                 ("peak_in_use", C.c_uint64), ("max_round_jobs", C.c_uint32), ("max_resident_jobs", C.c_uint32),
-                ("gpu_busy_ms", C.c_double)]
+                ("gpu_busy_ms", C.c_double), ("phase_ms", C.c_double * 5)]
 
 
 class SampleView:

@@ -361,10 +361,19 @@ class Server:
         self.L.bsq_server_release(self.srv, jid)
         self._jobs.pop(jid, None)
 
+    def set_tuning(self, **kw):
+        """Launch shapes for the server's passes (keys of abi.Tuning); applied before the next round."""
+        t = abi.Tuning(**kw)
+        rc = self.L.bsq_server_set_tuning(self.srv, C.byref(t))
+        if rc != 0:
+            raise _lib.BsqError(rc, "bsq_server_set_tuning failed")
+
     def stats(self) -> dict:
         st = abi.ServerStats()
         self.L.bsq_server_get_stats(self.srv, C.byref(st))
-        return {k: getattr(st, k) for k, _ in abi.ServerStats._fields_}
+        out = {k: getattr(st, k) for k, _ in abi.ServerStats._fields_}
+        out["phase_ms"] = dict(zip(("pass1", "tables", "pass2", "results", "free"), list(st.phase_ms)))
+        return out
 
     def close(self):
         if self.srv:

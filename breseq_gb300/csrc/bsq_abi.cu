@@ -92,7 +92,7 @@ struct bsq_ctx {
   cudaStream_t stream = nullptr;        // the passes
   // sample uploads run on their own streams, beside the passes; concurrent loads (loader threads)
   // take the streams round robin
-  static constexpr int kLoadStreams = 4;
+  static constexpr int kLoadStreams = 8;
   cudaStream_t load_streams[kLoadStreams] = {};
   std::atomic<uint32_t> load_rr{0};
   std::mutex mu;                        // guards `samples` and `next_id`

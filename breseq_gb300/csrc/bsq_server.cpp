@@ -78,9 +78,12 @@ struct bsq_server {
   uint32_t max_round_jobs = 0, resident = 0, max_resident = 0;
   uint32_t pending = 0;             // submitted and not finished
   double gpu_busy_ms = 0;
+  bool tune_pending = false;
+  bsq_tuning tune{};                      // applied by the GPU thread before its next round
+  double phase_ms[5] = {0, 0, 0, 0, 0};   // pass 1, tables, pass 2, result copies, frees (summed over rounds)
   bool stop = false;
   std::string err;
-  static constexpr int kLoaders = 4;   // uploads in flight at once (each on its own load stream)
+  static constexpr int kLoaders = 8;   // uploads in flight at once (each on its own load stream)
   std::vector<std::thread> admitters;
   std::thread gpu;
 
@@ -156,8 +159,17 @@ struct bsq_server {
       eo[i].hist_capacity = j->desc.hist_capacity;
       eo[i].hist_size = j->hist_size.data();
     }
+    auto tick = [](Clock::time_point& t) {
+      const Clock::time_point now = Clock::now();
+      const double d = std::chrono::duration<double, std::milli>(now - t).count();
+      t = now;
+      return d;
+    };
+    Clock::time_point tp = Clock::now();
+    double ph[4] = {0, 0, 0, 0};
     int rc = bsq_error_count_batch(ctx, n, ids.data(), ep.data(), eo.data());
     if (rc != BSQ_OK) { e = std::string("error_count: ") + bsq_last_error(ctx); return rc; }
+    ph[0] = tick(tp);
     std::vector<bsq_im_params> ip(n);
     std::vector<const double*> tabs(n);
     std::vector<const uint64_t*> cptr(n);
@@ -175,8 +187,10 @@ struct bsq_server {
     }
     rc = bsq_counts_to_log10_prob_batch(n, cptr.data(), Rs.data(), Qs.data(), tptr.data());
     if (rc != BSQ_OK) { e = "counts_to_log10_prob failed"; return rc; }
+    ph[1] = tick(tp);
     rc = bsq_identify_mutations_batch(ctx, n, ids.data(), ip.data(), tabs.data(), nullptr);
     if (rc != BSQ_OK) { e = std::string("identify_mutations: ") + bsq_last_error(ctx); return rc; }
+    ph[2] = tick(tp);
     for (uint32_t i = 0; i < n; i++) {
       Job* j = js[i];
       uint64_t a = 0, b = 0, c = 0;
@@ -185,6 +199,9 @@ struct bsq_server {
       rc = bsq_im_batch_result_copy(ctx, i, j->ra.data(), a, j->mc.data(), b, j->un.data(), c);
       if (rc != BSQ_OK) { e = "result copy failed"; return rc; }
     }
+    ph[3] = tick(tp);
+    std::lock_guard<std::mutex> lk(mu);
+    for (int k = 0; k < 4; k++) phase_ms[k] += ph[k];
     return BSQ_OK;
   }
 
@@ -193,6 +210,7 @@ struct bsq_server {
     for (;;) {
       cv_ready.wait(lk, [&] { return !ready.empty() || (stop && pending == 0); });
       if (ready.empty()) return;
+      if (tune_pending) { bsq_set_tuning(ctx, &tune); tune_pending = false; }
       std::vector<Job*> js;
       while (!ready.empty() && js.size() < max_batch) { js.push_back(ready.front()); ready.pop_front(); }
       const Clock::time_point ts = Clock::now();
@@ -209,9 +227,11 @@ struct bsq_server {
           rcs[i] = run_round(one, es[i]);
         }
       }
+      const Clock::time_point tf = Clock::now();
       for (Job* j : js) bsq_free_sample(ctx, j->sample);
       const Clock::time_point te = Clock::now();
       lk.lock();
+      phase_ms[4] += std::chrono::duration<double, std::milli>(te - tf).count();
       gpu_busy_ms += std::chrono::duration<double, std::milli>(te - ts).count();
       rounds++;
       for (size_t i = 0; i < js.size(); i++) {
@@ -374,6 +394,14 @@ int bsq_server_release(bsq_server* s, uint64_t id) {
   return BSQ_OK;
 }
 
+int bsq_server_set_tuning(bsq_server* s, const bsq_tuning* t) {
+  if (!s || !t) return BSQ_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->tune = *t;
+  s->tune_pending = true;
+  return BSQ_OK;
+}
+
 int bsq_server_get_stats(bsq_server* s, bsq_server_stats* o) {
   if (!s || !o) return BSQ_ERR_INVALID;
   std::lock_guard<std::mutex> lk(s->mu);
@@ -381,6 +409,7 @@ int bsq_server_get_stats(bsq_server* s, bsq_server_stats* o) {
   o->jobs_done = s->jobs_done; o->rounds = s->rounds; o->budget = s->budget; o->in_use = s->in_use;
   o->peak_in_use = s->peak_in_use; o->max_round_jobs = s->max_round_jobs; o->max_resident_jobs = s->max_resident;
   o->gpu_busy_ms = s->gpu_busy_ms;
+  for (int k = 0; k < 5; k++) o->phase_ms[k] = s->phase_ms[k];
   return BSQ_OK;
 }
 

@@ -434,6 +434,7 @@ typedef struct bsq_server_stats {
     uint64_t jobs_done, rounds, budget, in_use, peak_in_use;
     uint32_t max_round_jobs, max_resident_jobs;
     double   gpu_busy_ms;        /* summed wall time of the GPU rounds                           */
+    double   phase_ms[5];        /* of which: pass 1, table conversion, pass 2, result copies, frees */
 } bsq_server_stats;
 
 /* Bytes one job holds on the device while admitted: the resident sample plus both passes'
@@ -462,6 +463,9 @@ int  bsq_server_results(bsq_server* srv, uint64_t job_id, bsq_ra_record* ra, uin
 /* Forget a done job and its results. */
 int  bsq_server_release(bsq_server* srv, uint64_t job_id);
 int  bsq_server_get_stats(bsq_server* srv, bsq_server_stats* out);
+/* Launch shapes for the server's passes (e.g. from bsq_autotune on representative samples); the GPU
+ * thread applies them before its next round.  Results do not depend on them. */
+int  bsq_server_set_tuning(bsq_server* srv, const bsq_tuning* t);
 
 #ifdef __cplusplus
 }
