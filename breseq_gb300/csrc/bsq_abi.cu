@@ -74,7 +74,9 @@ struct PinnedBuf {
     if (p) cudaFreeHost(p);
     p = nullptr;
     bytes = 0;
-    const size_t want = n + n / 4 + 4096;
+    // geometric growth: a pinned allocation can wait behind other threads' transfers, so it
+    // should happen rarely
+    const size_t want = std::max<size_t>(n + n / 4 + 4096, std::max<size_t>(2 * bytes, size_t(8) << 20));
     cudaError_t e = cudaMallocHost(&p, want);
     if (e == cudaSuccess) bytes = want;
     return e;
@@ -269,14 +271,19 @@ int bsq_create(bsq_ctx** out, int device) {
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return BSQ_ERR_CUDA;
   c->sms = prop.multiProcessorCount;
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return BSQ_ERR_CUDA;
+  // the passes' stream first in line for SMs; uploads (copies plus small packing kernels) behind it
+  int prio_low = 0, prio_high = 0;
+  if (cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high) != cudaSuccess) prio_low = prio_high = 0;
+  if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_high) != cudaSuccess) return BSQ_ERR_CUDA;
   for (cudaStream_t& ls : c->load_streams)
-    if (cudaStreamCreateWithFlags(&ls, cudaStreamNonBlocking) != cudaSuccess) return BSQ_ERR_CUDA;
+    if (cudaStreamCreateWithPriority(&ls, cudaStreamNonBlocking, prio_low) != cudaSuccess) return BSQ_ERR_CUDA;
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
     uint64_t keep = UINT64_MAX;   // keep freed blocks in this process's pool for the next sample
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
+  // pinned staging reserved now, before any upload runs beside it (see PinnedBuf::reserve)
+  if (c->pin_in.reserve(8u << 20) != cudaSuccess || c->pin_out.reserve(8u << 20) != cudaSuccess) return BSQ_ERR_CUDA;
   if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       cudaEventCreate(&c->evm0) != cudaSuccess || cudaEventCreate(&c->evm1) != cudaSuccess ||
       cudaEventCreate(&c->evt0) != cudaSuccess || cudaEventCreate(&c->evt1) != cudaSuccess)

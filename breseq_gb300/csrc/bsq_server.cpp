@@ -210,7 +210,14 @@ struct bsq_server {
     for (;;) {
       cv_ready.wait(lk, [&] { return !ready.empty() || (stop && pending == 0); });
       if (ready.empty()) return;
-      if (tune_pending) { bsq_set_tuning(ctx, &tune); tune_pending = false; }
+      if (tune_pending) {
+        // passes run without graph capture here: captures were measured to wait behind the
+        // admission threads' uploads (tens of ms), and rounds are large enough not to need graphs
+        bsq_tuning t = tune;
+        t.use_graphs = 0;
+        bsq_set_tuning(ctx, &t);
+        tune_pending = false;
+      }
       std::vector<Job*> js;
       while (!ready.empty() && js.size() < max_batch) { js.push_back(ready.front()); ready.pop_front(); }
       const Clock::time_point ts = Clock::now();
@@ -282,6 +289,8 @@ int bsq_server_create(bsq_server** out, int device, uint64_t budget, uint32_t ma
   s->max_batch = max_batch_jobs ? max_batch_jobs : 64;
   s->precision = precision;
   s->t0 = Clock::now();
+  bsq_get_tuning(s->ctx, &s->tune);
+  s->tune_pending = true;   // graph capture off from the first round (see gpu_loop)
   bsq_server* p = s.get();
   for (int i = 0; i < bsq_server::kLoaders; i++) s->admitters.emplace_back([p] { p->admit_loop(); });
   s->gpu = std::thread([p] { p->gpu_loop(); });

@@ -464,7 +464,8 @@ int  bsq_server_results(bsq_server* srv, uint64_t job_id, bsq_ra_record* ra, uin
 int  bsq_server_release(bsq_server* srv, uint64_t job_id);
 int  bsq_server_get_stats(bsq_server* srv, bsq_server_stats* out);
 /* Launch shapes for the server's passes (e.g. from bsq_autotune on representative samples); the GPU
- * thread applies them before its next round.  Results do not depend on them. */
+ * thread applies them before its next round, always with use_graphs = 0 (a stream capture waits
+ * behind concurrent uploads).  Results do not depend on them. */
 int  bsq_server_set_tuning(bsq_server* srv, const bsq_tuning* t);
 
 #ifdef __cplusplus
