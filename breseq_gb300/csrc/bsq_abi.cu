@@ -457,6 +457,23 @@ int bsq_free_sample(bsq_ctx* ctx, int32_t id) {
 }
 
 // ============================================================================ pass 1
+// How many of the next samples form one launch group: at most kBatchJobs, and at most 2^31 columns
+// and 2^31 reads in total so that batch-wide column, tile and read indices stay 32-bit.  A single
+// sample is always a group of its own (its sizes were checked at load).  0 for an unknown id.
+static uint32_t group_size(bsq_ctx* ctx, uint32_t left, const int32_t* ids) {
+  uint64_t cols = 0, reads = 0;
+  uint32_t k = 0;
+  while (k < left && k < kBatchJobs) {
+    const SampleDev* s = find_sample(ctx, ids[k]);
+    if (!s) return k;   // the group stops before it; the pass reports the unknown id
+    if (k > 0 && (cols + s->n_cols > (1ull << 31) || reads + s->n_reads > (1ull << 31))) break;
+    cols += s->n_cols;
+    reads += s->n_reads;
+    k++;
+  }
+  return k;
+}
+
 // One group of at most kBatchJobs samples: one launch per kernel of pass 1.
 //   device arena: [results of every job: counts | coverage hist | read-start tallies | error word]
 //                 [work of every job: coverage difference arrays, read-start flags, block sums]
@@ -600,9 +617,12 @@ static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_p
 int bsq_error_count_batch(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_params* P, bsq_ec_result* out) {
   if (!ctx || !ids || !P || !out || n == 0) return fail(ctx, BSQ_ERR_INVALID, "null argument");
   ctx->last_ms = 0; ctx->main_ms = 0; ctx->launches = 0; ctx->last_h2d = 0; ctx->last_d2h = 0;
-  for (uint32_t g = 0; g < n; g += kBatchJobs) {
-    const int rc = ec_group(ctx, std::min(kBatchJobs, n - g), ids + g, P + g, out + g);
+  for (uint32_t g = 0; g < n;) {
+    const uint32_t k = group_size(ctx, n - g, ids + g);
+    if (k == 0) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
+    const int rc = ec_group(ctx, k, ids + g, P + g, out + g);
     if (rc != BSQ_OK) return rc;
+    g += k;
   }
   return BSQ_OK;
 }
@@ -879,10 +899,12 @@ int bsq_identify_mutations_batch(bsq_ctx* ctx, uint32_t n, const int32_t* ids, c
   if (!ctx || !ids || !P || !tables || n == 0) return fail(ctx, BSQ_ERR_INVALID, "null argument");
   ctx->res_ra.assign(n, {}); ctx->res_mc.assign(n, {}); ctx->res_un.assign(n, {});
   ctx->last_ms = 0; ctx->main_ms = 0; ctx->launches = 0; ctx->last_candidates = 0; ctx->last_h2d = 0; ctx->last_d2h = 0;
-  for (uint32_t g = 0; g < n; g += kBatchJobs) {
-    const int rc = im_group(ctx, std::min(kBatchJobs, n - g), ids + g, P + g, tables + g,
-                            pos_out ? pos_out + g : nullptr, g);
+  for (uint32_t g = 0; g < n;) {
+    const uint32_t k = group_size(ctx, n - g, ids + g);
+    if (k == 0) { ctx->res_ra.clear(); ctx->res_mc.clear(); ctx->res_un.clear(); return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id"); }
+    const int rc = im_group(ctx, k, ids + g, P + g, tables + g, pos_out ? pos_out + g : nullptr, g);
     if (rc != BSQ_OK) { ctx->res_ra.clear(); ctx->res_mc.clear(); ctx->res_un.clear(); return rc; }
+    g += k;
   }
   return BSQ_OK;
 }
