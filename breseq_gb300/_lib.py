@@ -88,6 +88,11 @@ def load():
     L.bsq_server_release.argtypes = [C.c_void_p, C.c_uint64]
     L.bsq_server_get_stats.argtypes = [C.c_void_p, P(abi.ServerStats)]
     L.bsq_server_set_tuning.argtypes = [C.c_void_p, P(abi.Tuning)]
+    L.bsq_default_sc_params.argtypes = [P(abi.ScParams)]
+    L.bsq_soft_clipping.argtypes = [C.c_void_p, C.c_int32, P(abi.ScParams), P(abi.ScSummary)]
+    L.bsq_sc_result_copy.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
+    L.bsq_write_soft_clipping_counts.argtypes = [C.c_char_p, P(C.c_char_p), P(abi.ScParams), P(abi.ScSummary),
+                                                 C.c_void_p, C.c_uint64]
     _lib = L
     return L
 
@@ -103,4 +108,5 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_server_get_stats", "bsq_server_set_tuning", "bsq_last_pass_stats", "bsq_timer_start",
             "bsq_timer_stop", "bsq_host_register", "bsq_host_unregister", "bsq_score_positions_noalloc",
             "bsq_default_ra_settings", "bsq_test_ra_evidence", "bsq_write_error_rates", "bsq_write_base_qual_error_prob",
-            "bsq_write_coverage_distribution", "bsq_write_coverage_table", "bsq_format_ra", "bsq_write_gd")
+            "bsq_write_coverage_distribution", "bsq_write_coverage_table", "bsq_format_ra", "bsq_write_gd",
+            "bsq_default_sc_params", "bsq_soft_clipping", "bsq_sc_result_copy", "bsq_write_soft_clipping_counts")

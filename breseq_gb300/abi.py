@@ -41,6 +41,48 @@ class ReadSoA(C.Structure):
         ("qual", P(C.c_uint8)),
         ("n_cigar_total", C.c_uint64),
         ("n_bases_total", C.c_uint64),
+        ("xj", P(C.c_uint8)),
+    ]
+
+
+class ScParams(C.Structure):
+    _fields_ = [
+        ("minimum_clipped_bases", C.c_uint32),
+        ("consensus_base_fraction", C.c_double),
+        ("dispersion_trim_frequency", C.c_double),
+        ("maximum_dispersion", C.c_double),
+        ("minimum_rate", C.c_double),
+        ("target_name_order", P(C.c_uint32)),
+    ]
+
+
+class ScSummary(C.Structure):
+    _fields_ = [
+        ("total_spanning_read_bases", C.c_uint64),
+        ("total_clipped_read_ends", C.c_uint64),
+        ("total_agreeing_clipped_read_ends", C.c_uint64),
+        ("soft_clipping_rate", C.c_double),
+        ("null_rate", C.c_double),
+        ("null_rate_raw", C.c_double),
+        ("dispersion", C.c_double),
+        ("dispersion_raw", C.c_double),
+        ("pearson_phi", C.c_double),
+        ("tested_positions", C.c_uint64),
+        ("trimmed_positions", C.c_uint64),
+        ("mean_tested_reads", C.c_double),
+        ("n_positions", C.c_uint64),
+    ]
+
+
+class ScPosition(C.Structure):
+    _fields_ = [
+        ("target", C.c_uint32),
+        ("position", C.c_uint32),
+        ("direction", C.c_int32),
+        ("clipped_count", C.c_uint32),
+        ("total_count", C.c_uint32),
+        ("agree_count", C.c_uint32),
+        ("clipped_sequence", C.c_char * 24),
     ]
 
 
@@ -213,8 +255,28 @@ class SampleView:
         kw = {}
         for name, (dt, ct) in fields.items():
             kw[name] = ptr(k(getattr(s, name), dt), ct)
+        xj = getattr(s, "xj", None)
+        if xj is not None:
+            kw["xj"] = ptr(k(xj, np.uint8), C.c_uint8)
         self.reads = ReadSoA(n_reads=int(len(s.tid)), n_cigar_total=int(len(s.cigar)),
                              n_bases_total=int(len(s.qual)), **kw)
+
+
+def sc_summary_dict(s: ScSummary) -> dict:
+    return {name: getattr(s, name) for name, _ in ScSummary._fields_}
+
+
+SC_ROW_DTYPE = np.dtype([("target", np.uint32), ("position", np.uint32), ("direction", np.int32),
+                         ("clipped_count", np.uint32), ("total_count", np.uint32), ("agree_count", np.uint32),
+                         ("clipped_sequence", "S24")])
+
+
+def sc_rows_array(rows, n: int) -> np.ndarray:
+    """The first n bsq_sc_position entries of a ctypes array as a numpy structured array."""
+    assert SC_ROW_DTYPE.itemsize == C.sizeof(ScPosition)
+    if n == 0:
+        return np.zeros(0, dtype=SC_ROW_DTYPE)
+    return np.frombuffer(bytes(memoryview(rows).cast("B")[:n * C.sizeof(ScPosition)]), dtype=SC_ROW_DTYPE).copy()
 
 
 def ra_to_dicts(arr) -> list:

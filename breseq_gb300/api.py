@@ -1,7 +1,8 @@
-"""Host API over the C ABI, mirroring breseq's two entry points of the scoring path.
+"""Host API over the C ABI, mirroring breseq's entry points of the scoring path.
 
     error_count(...)         <- breseq::error_count          (src/breseq/error_count.h:44-56)
     identify_mutations(...)  <- breseq::identify_mutations   (src/breseq/identify_mutations.h:46-60)
+    soft_clipping(...)       <- breseq::tabulate_soft_clipping_counts (src/breseq/soft_clipping.h)
 
 Both take a decoded sample (breseq_gb300.synth.Sample or anything with the same record arrays)
 instead of BAM/FASTA file names, and return what breseq writes to its output files: the covariate
@@ -18,6 +19,26 @@ from . import _lib, abi
 
 PRECISION_FP64 = 0
 PRECISION_FP32C = 1
+
+
+@dataclass
+class ScSettings:
+    """Soft-clipping settings with breseq's defaults (src/breseq/settings.cpp:1369-1374)."""
+    minimum_clipped_bases: int = 12
+    consensus_base_fraction: float = 0.95
+    dispersion_trim_frequency: float = 0.25
+    maximum_dispersion: float = 0.005
+    minimum_rate: float = 1e-5
+
+
+def sc_params(sample, st: ScSettings):
+    """bsq_sc_params for a sample; rows follow the std::string order of its target names."""
+    names = list(sample.target_names)
+    order = np.array(sorted(range(len(names)), key=lambda t: names[t].encode()), dtype=np.uint32)
+    p = abi.ScParams(minimum_clipped_bases=st.minimum_clipped_bases, consensus_base_fraction=st.consensus_base_fraction,
+                     dispersion_trim_frequency=st.dispersion_trim_frequency, maximum_dispersion=st.maximum_dispersion,
+                     minimum_rate=st.minimum_rate, target_name_order=abi.ptr(order, C.c_uint32))
+    return p, order
 
 
 @dataclass
@@ -223,6 +244,17 @@ class Scorer:
 
     def identify_mutations(self, sid: int, log10_table, settings: ImSettings | None = None, **kw):
         return self.identify_mutations_batch([sid], [log10_table], [settings], **kw)[0]
+
+    # ------------------------------------------------------------------ soft clipping
+    def soft_clipping(self, sid: int, settings: ScSettings | None = None) -> dict:
+        """tabulate_soft_clipping_counts over a resident sample: the summary (Summary::soft_clipping)
+        and the rows of soft_clipping_counts.tab as a structured array."""
+        p, keep = sc_params(self.sample(sid), settings or ScSettings())
+        s = abi.ScSummary()
+        self._check(self.L.bsq_soft_clipping(self.ctx, sid, C.byref(p), C.byref(s)))
+        rows = (abi.ScPosition * max(1, s.n_positions))()
+        self._check(self.L.bsq_sc_result_copy(self.ctx, rows, s.n_positions))
+        return dict(summary=abi.sc_summary_dict(s), rows=abi.sc_rows_array(rows, s.n_positions))
 
     # ------------------------------------------------------------------ launch shapes
     def tuning(self) -> dict:

@@ -21,6 +21,7 @@
 #include "bsq_host.h"
 #include "bsq_kernels.h"
 #include "bsq_noalloc.h"
+#include "bsq_softclip.h"
 
 using namespace bsq;
 
@@ -112,6 +113,9 @@ struct bsq_ctx {
   std::vector<std::vector<bsq_ra_record>> res_ra;
   std::vector<std::vector<bsq_mc_record>> res_mc;
   std::vector<std::vector<bsq_un_record>> res_un;
+  // soft-clipping tabulation: working buffers and the rows of the last call
+  DevMem sc_diff, sc_cnt, sc_blk, sc_tot, sc_rows, sc_outs, sc_tails;
+  std::vector<bsq_sc_position> sc_res;
   double last_ms = 0, main_ms = 0;
   uint32_t launches = 0;
   uint64_t last_h2d = 0, last_d2h = 0;   // bytes the last pass call copied each way
@@ -301,7 +305,8 @@ void bsq_destroy(bsq_ctx* ctx) {
   // pool blocks are returned on the context's stream, so before it goes
   for (DevMem* m : {&ctx->cov, &ctx->call, &ctx->blk, &ctx->cand, &ctx->next, &ctx->ra, &ctx->bq, &ctx->pool,
                     &ctx->qhist, &ctx->scratch, &ctx->keep, &ctx->kcol, &ctx->kcov, &ctx->kcall,
-                    &ctx->d_chunks, &ctx->ec_arena, &ctx->im_arena, &ctx->ctl})
+                    &ctx->d_chunks, &ctx->ec_arena, &ctx->im_arena, &ctx->ctl, &ctx->sc_diff, &ctx->sc_cnt,
+                    &ctx->sc_blk, &ctx->sc_tot, &ctx->sc_rows, &ctx->sc_outs, &ctx->sc_tails})
     m->release();
   if (ctx->exec_ec) cudaGraphExecDestroy(ctx->exec_ec);
   if (ctx->exec_im) cudaGraphExecDestroy(ctx->exec_im);
@@ -392,6 +397,8 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   CK(upload(s->cigar, rd->cigar, rd->n_cigar_total, st));
   CK(upload(s->seq, rd->seq, (rd->n_bases_total + 1) / 2, st));
   CK(upload(s->qual, rd->qual, rd->n_bases_total, st));
+  DevMem xj;
+  if (rd->xj) CK(upload(xj, rd->xj, n, st));
   CK(s->reads.alloc(n * sizeof(DevRead) + 64, st));
   CK(s->qb.alloc(n * sizeof(QBounds) + 64, st));
   CK(s->rstart.alloc(n * 4 + 64, st));
@@ -404,6 +411,7 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   in.x1 = s->x1.as<uint32_t>(); in.xl = xl.as<int32_t>(); in.xr = xr.as<int32_t>(); in.read_file = rfile.as<uint8_t>();
   in.l_qseq = lq.as<uint32_t>(); in.seq_off = soff.as<uint64_t>(); in.cigar_off = coff.as<uint64_t>();
   in.n_cigar = nc.as<uint16_t>(); in.cigar = s->cigar.as<uint32_t>(); in.tpoff = s->d_tpoff.as<uint32_t>(); in.called = s->tgt_called.as<uint8_t>();
+  in.xj = rd->xj ? xj.as<uint8_t>() : nullptr;
   in.n = (uint32_t)n; in.n_targets = T; in.n_bases = rd->n_bases_total; in.n_cigar_total = rd->n_cigar_total;
   PackOut po;
   po.reads = s->reads.as<DevRead>(); po.qb = s->qb.as<QBounds>(); po.rstart = s->rstart.as<uint32_t>();
@@ -943,6 +951,109 @@ int bsq_im_result_counts(const bsq_ctx* ctx, uint64_t* n_ra, uint64_t* n_mc, uin
 int bsq_im_result_copy(const bsq_ctx* ctx, bsq_ra_record* ra, uint64_t ra_cap, bsq_mc_record* mc, uint64_t mc_cap,
                        bsq_un_record* un, uint64_t un_cap) {
   return bsq_im_batch_result_copy(ctx, 0, ra, ra_cap, mc, mc_cap, un, un_cap);
+}
+
+// tabulate_soft_clipping_counts (src/breseq/soft_clipping.cpp:285-666): the device walks the records
+// and the columns (bsq_softclip.cu); the rows come back in (direction, column) order and the host
+// puts them in the reference's order and fits the null model.
+int bsq_soft_clipping(bsq_ctx* ctx, int32_t sample_id, const bsq_sc_params* p, bsq_sc_summary* summary) {
+  if (!ctx || !p || !summary) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  // the ranges Settings enforces when it parses the options (src/breseq/settings.cpp:766-779)
+  if (!(p->consensus_base_fraction >= 0.0 && p->consensus_base_fraction <= 1.0) ||
+      !(p->dispersion_trim_frequency >= 0.0 && p->dispersion_trim_frequency <= 1.0) ||
+      !(p->maximum_dispersion >= 0.0 && p->maximum_dispersion < 1.0) ||
+      !(p->minimum_rate >= 0.0 && p->minimum_rate < 1.0))
+    return fail(ctx, BSQ_ERR_INVALID, "soft-clipping setting out of range");
+  SampleDev* s = find_sample(ctx, sample_id);
+  if (!s) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
+  CK(cudaSetDevice(ctx->device));
+  const uint32_t T = s->n_targets;
+  std::vector<uint32_t> order(T);
+  if (p->target_name_order) {
+    std::vector<uint8_t> seen(T, 0);
+    for (uint32_t i = 0; i < T; i++) {
+      const uint32_t t = p->target_name_order[i];
+      if (t >= T || seen[t]) return fail(ctx, BSQ_ERR_INVALID, "target_name_order is not a permutation of the targets");
+      seen[t] = 1;
+      order[i] = t;
+    }
+  } else {
+    for (uint32_t i = 0; i < T; i++) order[i] = i;
+  }
+  cudaStream_t st = ctx->stream;
+  cudaGetLastError();
+  const uint32_t nb = (s->n_cols + kScBlockCols - 1) / kScBlockCols;
+  const uint64_t cstride = (uint64_t)nb * kScBlockCols;
+  CK(ctx->sc_diff.alloc(cstride * 4, st));
+  CK(ctx->sc_cnt.alloc(cstride * 8, st));
+  CK(ctx->sc_blk.alloc((uint64_t)nb * 5 * 8, st));
+  CK(ctx->sc_tot.alloc(128, st));
+  CK(record(ctx->ev0, st));
+  CK(cudaMemsetAsync(ctx->sc_diff.p, 0, cstride * 4, st));
+  CK(cudaMemsetAsync(ctx->sc_cnt.p, 0, cstride * 8, st));
+  CK(cudaMemsetAsync(ctx->sc_tot.p, 0, 128, st));
+  ScArgs A;
+  memset(&A, 0, sizeof A);
+  A.reads = s->reads.as<DevRead>();
+  A.qb = s->qb.as<QBounds>();
+  A.seq = s->seq.as<uint8_t>();
+  A.tpoff = s->d_tpoff.as<uint32_t>();
+  A.n_reads = s->n_reads;
+  A.n_targets = T;
+  A.n_cols = s->n_cols;
+  A.n_blocks = nb;
+  A.cstride = cstride;
+  A.m = p->minimum_clipped_bases;
+  A.K = std::min(p->minimum_clipped_bases, kScMaxConsensus);
+  A.base_fraction = p->consensus_base_fraction;
+  A.diff = ctx->sc_diff.as<int32_t>();
+  A.cnt = ctx->sc_cnt.as<uint32_t>();
+  A.blk = ctx->sc_blk.as<long long>();
+  A.tot = ctx->sc_tot.as<unsigned long long>();
+  A.err = reinterpret_cast<uint32_t*>(ctx->sc_tot.as<unsigned char>() + 64);
+  CK(sc_launch_count(A, ctx->sms, st));
+  CK(ctx->pin_out.reserve(128));
+  CK(cudaMemcpyAsync(ctx->pin_out.p, ctx->sc_tot.p, 128, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  uint64_t tot[8];
+  memcpy(tot, ctx->pin_out.p, sizeof tot);
+  const uint32_t err = *reinterpret_cast<const uint32_t*>(ctx->pin_out.at(64));
+  if (err) return fail(ctx, BSQ_ERR_INVALID, "invalid records: " + err_text(err));
+  const uint64_t n_rows = tot[0] + tot[2], n_tails = tot[1] + tot[3];
+  if (n_tails >= 0xFFFFFFFFull) return fail(ctx, BSQ_ERR_SIZE, "more than 2^32 - 1 clip events in one sample");
+  CK(ctx->sc_rows.alloc(n_rows * sizeof(ScRowDev), st));
+  CK(ctx->sc_outs.alloc(n_rows * sizeof(ScOutDev), st));
+  CK(ctx->sc_tails.alloc(n_tails * 8, st));
+  A.rows = ctx->sc_rows.as<ScRowDev>();
+  A.outs = ctx->sc_outs.as<ScOutDev>();
+  A.tails = ctx->sc_tails.as<unsigned long long>();
+  CK(sc_launch_rows(A, (uint32_t)n_rows, ctx->sms, st));
+  const size_t rows_bytes = n_rows * sizeof(ScRowDev), outs_bytes = n_rows * sizeof(ScOutDev);
+  CK(ctx->pin_out.reserve(128 + rows_bytes + outs_bytes));
+  unsigned char* h = ctx->pin_out.at(0);
+  CK(cudaMemcpyAsync(h, ctx->sc_tot.p, 64, cudaMemcpyDeviceToHost, st));
+  if (n_rows) {
+    CK(cudaMemcpyAsync(h + 128, ctx->sc_rows.p, rows_bytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h + 128 + rows_bytes, ctx->sc_outs.p, outs_bytes, cudaMemcpyDeviceToHost, st));
+  }
+  CK(record(ctx->ev1, st));
+  CK(cudaStreamSynchronize(st));
+  ctx->last_ms = elapsed(ctx->ev0, ctx->ev1);
+  ctx->main_ms = 0;
+  ctx->launches = n_rows ? (s->n_reads ? 7 : 5) : (s->n_reads ? 4 : 3);
+  ctx->last_h2d = 0;
+  ctx->last_d2h = 128 + 64 + rows_bytes + outs_bytes;
+  memcpy(tot, h, 64);
+  host::sc_assemble(reinterpret_cast<const ScRowDev*>(h + 128), reinterpret_cast<const ScOutDev*>(h + 128 + rows_bytes),
+                    tot[0], tot[2], s->tpoff, order, A.K, *p, n_tails, tot[4], tot[5], ctx->sc_res, *summary);
+  return BSQ_OK;
+}
+
+int bsq_sc_result_copy(const bsq_ctx* ctx, bsq_sc_position* rows, uint64_t capacity) {
+  if (!ctx || (!rows && capacity)) return BSQ_ERR_INVALID;
+  if (capacity < ctx->sc_res.size()) return BSQ_ERR_SIZE;
+  std::copy(ctx->sc_res.begin(), ctx->sc_res.end(), rows);
+  return BSQ_OK;
 }
 
 int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_launches, double* main_kernel_ms) {

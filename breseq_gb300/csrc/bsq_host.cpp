@@ -362,5 +362,88 @@ void fill_positions(const std::vector<ColCov>& cov, const std::vector<ColCall>& 
   }
 }
 
+void sc_assemble(const ScRowDev* rows, const ScOutDev* outs, uint64_t rows_neg, uint64_t rows_pos,
+                 const std::vector<uint32_t>& tpoff, const std::vector<uint32_t>& name_order, uint32_t K,
+                 const bsq_sc_params& p, uint64_t total_clipped, uint64_t total_spanning, uint64_t tested_spanning,
+                 std::vector<bsq_sc_position>& out, bsq_sc_summary& s) {
+  out.clear();
+  out.reserve(rows_neg + rows_pos);
+  uint64_t total_agreeing = 0, tested = tested_spanning;
+  for (int dir = -1; dir <= 1; dir += 2) {
+    const ScRowDev* R = dir < 0 ? rows : rows + rows_neg;
+    const ScOutDev* O = dir < 0 ? outs : outs + rows_neg;
+    const uint64_t n = dir < 0 ? rows_neg : rows_pos;
+    for (uint32_t t : name_order) {
+      const uint32_t c0 = tpoff[t], c1 = tpoff[t + 1];
+      uint64_t i = std::lower_bound(R, R + n, c0, [](const ScRowDev& r, uint32_t c) { return r.col < c; }) - R;
+      for (; i < n && R[i].col < c1; i++) {
+        bsq_sc_position w;
+        memset(&w, 0, sizeof w);
+        w.target = t;
+        w.position = R[i].col - c0 + 1;
+        w.direction = dir;
+        w.clipped_count = R[i].clipped;
+        w.total_count = R[i].clipped + R[i].read_through;
+        w.agree_count = O[i].agree;
+        if (O[i].informative > 0) {
+          // columns run outward from the clip wall; a leading clip's tail is stored reference-forward
+          for (uint32_t k = 0; k < K; k++) {
+            const uint32_t code = (uint32_t)(O[i].cons >> (3 * k)) & 7u;
+            w.clipped_sequence[dir < 0 ? K - 1 - k : k] = code < 4 ? "ACGT"[code] : 'N';
+          }
+        }
+        total_agreeing += w.agree_count;
+        if (R[i].read_through == 0) tested++;
+        out.push_back(w);
+      }
+    }
+  }
+  memset(&s, 0, sizeof s);
+  const uint64_t total_opp = total_clipped + total_spanning;
+  s.total_spanning_read_bases = total_spanning;
+  s.total_clipped_read_ends = total_clipped;
+  s.total_agreeing_clipped_read_ends = total_agreeing;
+  s.soft_clipping_rate = total_opp > 0 ? (double)total_clipped / (double)total_opp : 0.0;
+  const double p0_raw = total_opp > 0 ? (double)total_agreeing / (double)total_opp : 0.0;
+  double p0 = p0_raw;
+  if (p.minimum_rate > 0.0 && p0 < p.minimum_rate) p0 = p.minimum_rate;
+  // Pearson chi-square of the quasi-binomial over the untrimmed rows, in row order
+  double S_k = 0.0, S_k2_over_n = 0.0, S_n_trimmed = 0.0;
+  uint64_t trimmed = 0;
+  for (const bsq_sc_position& w : out) {
+    if (w.total_count == 0) continue;
+    const double k = (double)w.agree_count, n = (double)w.total_count;
+    if (p.dispersion_trim_frequency > 0.0 && k / n >= p.dispersion_trim_frequency) {
+      trimmed++;
+      S_n_trimmed += n;
+      continue;
+    }
+    S_k += k;
+    S_k2_over_n += k * k / n;
+  }
+  const uint64_t N_prime = tested > trimmed ? tested - trimmed : 0;
+  const double S_n_prime = (double)total_opp - S_n_trimmed;
+  const double mean_n = N_prime > 0 ? S_n_prime / (double)N_prime : 0.0;
+  double phi = 0.0, rho = 0.0;
+  if (N_prime > 1 && mean_n > 1.0 && p0 > 0.0 && p0 < 1.0) {
+    const double chi2 = (S_k2_over_n - 2.0 * p0 * S_k + p0 * p0 * S_n_prime) / (p0 * (1.0 - p0));
+    phi = chi2 / (double)(N_prime - 1);
+    rho = (phi - 1.0) / (mean_n - 1.0);
+  }
+  const double rho_raw = rho;
+  if (!std::isfinite(rho) || rho < 0.0) rho = 0.0;   // degenerate: plain binomial
+  if (p.maximum_dispersion > 0.0 && rho > p.maximum_dispersion) rho = p.maximum_dispersion;
+  if (rho < 1e-6) rho = 0.0;
+  s.null_rate = p0;
+  s.null_rate_raw = p0_raw;
+  s.dispersion = rho;
+  s.dispersion_raw = rho_raw;
+  s.pearson_phi = phi;
+  s.tested_positions = N_prime;
+  s.trimmed_positions = trimmed;
+  s.mean_tested_reads = mean_n;
+  s.n_positions = out.size();
+}
+
 }  // namespace host
 }  // namespace bsq

@@ -6,6 +6,7 @@
 
 #include "../../include/breseq_gb300.h"
 #include "bsq_common.h"
+#include "bsq_softclip.h"
 
 namespace bsq {
 namespace host {
@@ -48,6 +49,15 @@ void intervals_sparse(const std::vector<uint32_t>& cols, const std::vector<ColCo
                       std::vector<bsq_un_record>& un);
 void fill_positions(const std::vector<ColCov>& cov, const std::vector<ColCall>& call, const SampleLayout& L,
                     bsq_position_arrays* out);
+
+// Soft-clipping rows in the reference's order (direction -1 then +1, targets in seq_id order,
+// positions ascending; soft_clipping.cpp:500-545) and the genome-wide totals and dispersion fit
+// (:547-623).  rows / outs hold the device's rows: direction -1 in column order, then direction +1.
+// tested_spanning = 2 x the testable positions with spanning reads.
+void sc_assemble(const ScRowDev* rows, const ScOutDev* outs, uint64_t rows_neg, uint64_t rows_pos,
+                 const std::vector<uint32_t>& tpoff, const std::vector<uint32_t>& name_order, uint32_t K,
+                 const bsq_sc_params& p, uint64_t total_clipped, uint64_t total_spanning, uint64_t tested_spanning,
+                 std::vector<bsq_sc_position>& out, bsq_sc_summary& s);
 
 }  // namespace host
 }  // namespace bsq

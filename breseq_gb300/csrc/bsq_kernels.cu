@@ -108,10 +108,12 @@ __device__ __forceinline__ void pack_one(const RawSoA& in, const PackOut& out, u
     }
   }
   const uint32_t tlen = in.tpoff[tid + 1] - in.tpoff[tid] - 1;
-  if (!skip && !(err & kErrBounds)) {
-    if (nc == 0 || rlen == 0 || qlen != len) err |= kErrCigar;
-    if ((uint64_t)pos + rlen > tlen) err |= kErrCigar;
-  }
+  const bool bad_cigar = (err & kErrBounds) || nc == 0 || rlen == 0 || qlen != len || (uint64_t)pos + rlen > tlen;
+  if (!skip && !(err & kErrBounds) && bad_cigar) err |= kErrCigar;
+  // soft-clipping tabulation: every mapped record on a non-empty target except XJ-tagged ones
+  // (soft_clipping.cpp:373-393); X1 > 1 is kRedundant
+  if ((flag & 0x4) || (in.xj && in.xj[i]) || tlen == 0) fl |= kScSkip;
+  else if (bad_cigar) fl |= kScBad;
   if (rlen == 0) rlen = 1;
   d.start = in.tpoff[tid] + (uint32_t)pos;
   d.end = d.start + rlen;

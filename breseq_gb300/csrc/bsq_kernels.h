@@ -22,6 +22,7 @@ struct RawSoA {
   const uint64_t* cigar_off;
   const uint16_t* n_cigar;
   const uint32_t* cigar;
+  const uint8_t* xj;         // XJ tag present (may be null: no record has one)
   const uint32_t* tpoff;     // padded target offsets
   const uint8_t* called;     // per target: in the pileup set
   uint32_t n;

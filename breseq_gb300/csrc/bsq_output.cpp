@@ -513,4 +513,35 @@ int bsq_write_gd(const char* path, const bsq_reference* ref, const char* const* 
   return out ? BSQ_OK : BSQ_ERR_INVALID;
 }
 
+int bsq_default_sc_params(bsq_sc_params* p) {
+  if (!p) return BSQ_ERR_INVALID;
+  // Settings defaults (src/breseq/settings.cpp:1369-1374)
+  p->minimum_clipped_bases = 12;
+  p->consensus_base_fraction = 0.95;
+  p->dispersion_trim_frequency = 0.25;
+  p->maximum_dispersion = 0.005;
+  p->minimum_rate = 1e-5;
+  p->target_name_order = nullptr;
+  return BSQ_OK;
+}
+
+int bsq_write_soft_clipping_counts(const char* path, const char* const* target_names, const bsq_sc_params* p,
+                                   const bsq_sc_summary* s, const bsq_sc_position* rows, uint64_t n) {
+  if (!path || !target_names || !p || !s || (n && !rows)) return BSQ_ERR_INVALID;
+  std::ofstream out(path);
+  if (!out) return BSQ_ERR_INVALID;
+  // soft_clipping.cpp:630-646: a parameter line (default ostream formatting of the doubles), the
+  // column names, and one row per (position, direction) with clip events; "." for no sequence
+  out << "#sc_format=2\tsoft_clipping_minimum_bases=" << p->minimum_clipped_bases
+      << "\tconsensus_base_fraction=" << fmt_default(p->consensus_base_fraction)
+      << "\tnull_rate=" << fmt_default(s->null_rate) << "\tdispersion=" << fmt_default(s->dispersion) << "\n";
+  out << "seq_id\tposition\tdirection\tclipped_count\ttotal_count\tagree_count\tclipped_sequence\n";
+  for (uint64_t i = 0; i < n; i++) {
+    const bsq_sc_position& r = rows[i];
+    out << target_names[r.target] << "\t" << r.position << "\t" << r.direction << "\t" << r.clipped_count << "\t"
+        << r.total_count << "\t" << r.agree_count << "\t" << (r.clipped_sequence[0] ? r.clipped_sequence : ".") << "\n";
+  }
+  return out ? BSQ_OK : BSQ_ERR_INVALID;
+}
+
 }  // extern "C"

@@ -61,6 +61,11 @@ class SimConfig:
     low_mapq_fraction: float = 0.0  # unique reads with MAPQ drawn in [20, 41]
     large_deletions: int = 0        # regions of the reference missing from the sample (MC evidence)
     large_deletion_length: int = 800
+    # soft-clip evidence: junctions whose crossing reads are clipped at the junction with one donor
+    # sequence each, longer clips of random bases, and records tagged XJ
+    breakpoints: int = 0
+    long_clip_fraction: float = 0.0  # unique reads clipped by 12-40 random bases at one end
+    xj_fraction: float = 0.0
     chunk_reads: int = 400_000
 
 
@@ -92,6 +97,7 @@ class Sample:
     n_read_files: int
     n_quality: int
     variants: list = field(default_factory=list)
+    xj: np.ndarray | None = None   # uint8, XJ tag present; None when no record has one
 
     @property
     def n_reads(self) -> int:
@@ -290,11 +296,43 @@ def simulate(cfg: SimConfig) -> Sample:
         pos = ext(pos, extra_pos)
         src_index = np.concatenate([src_index, extra_src])
         n = tid.shape[0]
+    # junction breakpoints: a share of the unique reads crossing the junction is clipped there, the
+    # clipped bases taken from the breakpoint's donor sequence (outward from the junction)
+    donor = np.full(n, -1, dtype=np.int64)
+    donors = []
+    if cfg.breakpoints > 0:
+        Lmax = int(L_arr.max())
+        for b in range(cfg.breakpoints):
+            t, p = _pick_site(margin=Lmax + 50)
+            d = -1 if rng.random() < 0.5 else 1
+            f = float(np.exp(rng.uniform(np.log(0.02), 0.0)))   # low-frequency ones stay in the null fit
+            donors.append(rng.integers(0, 4, size=Lmax).astype(np.uint8))
+            variants.append(dict(tid=t, pos=p, kind="breakpoint", direction=d, freq=f))
+            cand = np.nonzero((tid == t) & (x1 == 1) & (pos < p) & (pos + L_arr > p) & (donor < 0))[0]
+            a = np.where(d > 0, p - pos[cand], pos[cand] + L_arr[cand] - p)   # aligned bases kept
+            cand = cand[(a >= 20) & (a <= L_arr[cand] - 1)]
+            cand = cand[rng.random(cand.size) < f]
+            donor[cand] = b
+            if d > 0:
+                clip_r[cand] = L_arr[cand] - (p - pos[cand])
+                clip_l[cand] = 0
+            else:
+                clip_l[cand] = p - pos[cand]
+                clip_r[cand] = 0
+    if cfg.long_clip_fraction > 0:
+        m = (rng.random(n) < cfg.long_clip_fraction) & (x1 == 1) & (donor < 0)
+        k = np.minimum(rng.integers(12, 41, size=n), L_arr - 20)
+        left = rng.random(n) < 0.5
+        clip_l[m & left] = k[m & left]
+        clip_r[m & left] = 0
+        clip_r[m & ~left] = k[m & ~left]
+        clip_l[m & ~left] = 0
     # soft clipped reads start later on the reference by the left clip
     pos = pos + clip_l
     order = np.lexsort((pos, tid))
     tid, pos, flag, rfile, rg, L_arr = tid[order], pos[order], flag[order], rfile[order], rg[order], L_arr[order]
     mapq, x1, clip_l, clip_r, src_index = mapq[order], x1[order], clip_l[order], clip_r[order], src_index[order]
+    donor = donor[order]
     xl = np.zeros(n, dtype=np.int32)
     xr = np.zeros(n, dtype=np.int32)
     if cfg.trim_fraction > 0:
@@ -351,6 +389,18 @@ def simulate(cfg: SimConfig) -> Sample:
     n_chunks = (n + cfg.chunk_reads - 1) // cfg.chunk_reads
     with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
         list(ex.map(fill, range(n_chunks)))
+    for r in np.nonzero(donor >= 0)[0]:
+        D = donors[donor[r]]
+        o = int(seq_off[r])
+        k = int(clip_l[r] or clip_r[r])
+        tail = D[:k].copy()
+        e = rng.random(k) < 0.01     # sequencing errors in the donor part as well
+        tail[e] = (tail[e] + rng.integers(1, 4, size=int(e.sum()))) & 3
+        if clip_l[r]:
+            nib[o: o + k] = _CODE2BAM[tail[::-1]]
+        else:
+            L = int(L_arr[r])
+            nib[o + L - k: o + L] = _CODE2BAM[tail]
     # ---------------------------------------------------------------- variants in reads
     cigar_list = [None] * n
     starts_sorted = gpos
@@ -364,6 +414,8 @@ def simulate(cfg: SimConfig) -> Sample:
         if cand.size == 0:
             continue
         kind = v["kind"]
+        if kind == "breakpoint":
+            continue
         if kind in ("snp", "strand_bias", "low_quality"):
             carry = rng.random(cand.size) < v["freq"]
             if kind == "strand_bias":
@@ -442,7 +494,8 @@ def simulate(cfg: SimConfig) -> Sample:
         tid=tid, pos=pos.astype(np.int32), flag=flag.astype(np.uint16), mapq=mapq, x1=x1,
         xl=xl, xr=xr, read_file=rfile.astype(np.uint8), read_group=rg.astype(np.uint16),
         l_qseq=L_arr.astype(np.uint32), seq_off=seq_off, cigar_off=cigar_off, n_cigar=n_cigar,
-        cigar=cigar, seq=seq, qual=qual, n_read_files=n_read_files, n_quality=42, variants=variants)
+        cigar=cigar, seq=seq, qual=qual, n_read_files=n_read_files, n_quality=42, variants=variants,
+        xj=(rng.random(n) < cfg.xj_fraction).astype(np.uint8) if cfg.xj_fraction > 0 else None)
 
 
 # ------------------------------------------------------------------ benchmark workloads

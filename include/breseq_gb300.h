@@ -10,13 +10,14 @@
  *                                   src/breseq/identify_mutations.cpp:1309-2022 (pileup_callback)
  *   coverage counts         breseq: src/breseq/error_count.cpp:239-253 (unique-only coverage histogram)
  *                                   src/breseq/identify_mutations.cpp:2173-2250 (coverage table rows)
+ *   soft-clip tabulation    breseq: src/breseq/soft_clipping.cpp:285-666 (tabulate_soft_clipping_counts)
  *
  * The reference exposes these passes as two C++ free functions that read a BAM/FASTA pair.  Here the
  * host decodes the alignments once into the struct-of-arrays record set `bsq_read_soa`, the library
  * keeps it resident in device memory, and each pass is one call.  Every function returns BSQ_OK (0)
  * or a negative status; the message is available from bsq_last_error().  No function exits the
  * process or traps the device (the reference calls exit(1) from ASSERT, src/breseq/common.h:111-193;
- * the C++ wrappers in breseq_gb300/csrc/bsq_host.hpp keep that convention for drop-in callers).
+ * a drop-in caller's wrappers with the reference signatures keep that convention on their side).
  *
  * A context is single-threaded.  Buffers passed in are borrowed for the duration of the call only.
  */
@@ -95,6 +96,9 @@ typedef struct bsq_read_soa {
     const uint8_t*  qual;
     uint64_t        n_cigar_total;
     uint64_t        n_bases_total;   /* length of qual[] (and 2 x length of seq[])               */
+    /* non-zero when the record carries an XJ:i tag (one side of a junction match); NULL when no
+     * record does.  Only the soft-clipping tabulation reads it (src/breseq/soft_clipping.cpp:382-384). */
+    const uint8_t*  xj;
 } bsq_read_soa;
 
 /* ---------------------------------------------------------------- pass 1: error counts */
@@ -312,6 +316,62 @@ int bsq_identify_mutations_batch(bsq_ctx* ctx, uint32_t n, const int32_t* sample
 int bsq_im_batch_result_counts(const bsq_ctx* ctx, uint32_t job, uint64_t* n_ra, uint64_t* n_mc, uint64_t* n_un);
 int bsq_im_batch_result_copy(const bsq_ctx* ctx, uint32_t job, bsq_ra_record* ra, uint64_t ra_cap,
                              bsq_mc_record* mc, uint64_t mc_cap, bsq_un_record* un, uint64_t un_cap);
+
+/* ---------------------------------------------------------------- soft-clipping tabulation */
+
+/* Settings of tabulate_soft_clipping_counts (src/breseq/soft_clipping.cpp:285-666), which breseq runs
+ * in the error-calibration step over the same BAM (src/breseq/breseq_cmdline.cpp:2307-2318) when
+ * --predict-soft-clipping is given.  Defaults: src/breseq/settings.cpp:1369-1374 (bsq_default_sc_params). */
+typedef struct bsq_sc_params {
+    uint32_t minimum_clipped_bases;      /* soft_clipping_minimum_bases (12)               */
+    double   consensus_base_fraction;    /* soft_clipping_consensus_base_fraction (0.95)   */
+    double   dispersion_trim_frequency;  /* soft_clipping_dispersion_trim_frequency (0.25) */
+    double   maximum_dispersion;         /* soft_clipping_maximum_dispersion (0.005)       */
+    double   minimum_rate;               /* soft_clipping_minimum_rate (1e-5)              */
+    /* every target once, in std::string order of the seq_ids: the order of the rows (the reference
+     * keys its tallies by seq_id in std::map).  NULL = target index order. */
+    const uint32_t* target_name_order;
+} bsq_sc_params;
+
+/* Summary::soft_clipping (src/breseq/summary.h:333-364), plus the unclamped values the reference
+ * prints and the number of rows. */
+typedef struct bsq_sc_summary {
+    uint64_t total_spanning_read_bases;
+    uint64_t total_clipped_read_ends;
+    uint64_t total_agreeing_clipped_read_ends;
+    double   soft_clipping_rate;
+    double   null_rate;                  /* p0 used: agreeing rate after the minimum-rate floor */
+    double   null_rate_raw;
+    double   dispersion;                 /* rho used; 0 = plain binomial */
+    double   dispersion_raw;
+    double   pearson_phi;
+    uint64_t tested_positions;           /* N': (position, direction) pairs entering the fit */
+    uint64_t trimmed_positions;
+    double   mean_tested_reads;
+    uint64_t n_positions;                /* rows: (position, direction) pairs with clip events */
+} bsq_sc_summary;
+
+/* One row of soft_clipping_counts.tab (soft_clipping.cpp:520-545, 639-646). */
+typedef struct bsq_sc_position {
+    uint32_t target;
+    uint32_t position;                   /* 1-based */
+    int32_t  direction;                  /* -1: leading clip at reference_start_1; +1: trailing clip at reference_end_1 */
+    uint32_t clipped_count;
+    uint32_t total_count;                /* clipped reads + reads spanning the position */
+    uint32_t agree_count;
+    char     clipped_sequence[24];       /* consensus tail, reference-forward, NUL-terminated; "" = none */
+} bsq_sc_position;
+
+int bsq_default_sc_params(bsq_sc_params* p);
+/* Tabulates the clip events of a resident sample.  Every mapped record counts except X1 > 1 and
+ * XJ-tagged ones (the pileup's flag filter does not apply).  Rows are kept in the context until
+ * the next call; read them with bsq_sc_result_copy (summary->n_positions rows, in the reference's
+ * order: direction -1 then +1, targets in target_name_order, positions ascending). */
+int bsq_soft_clipping(bsq_ctx* ctx, int32_t sample_id, const bsq_sc_params* p, bsq_sc_summary* summary);
+int bsq_sc_result_copy(const bsq_ctx* ctx, bsq_sc_position* rows, uint64_t capacity);
+/* soft_clipping_counts.tab (soft_clipping.cpp:625-646). */
+int bsq_write_soft_clipping_counts(const char* path, const char* const* target_names, const bsq_sc_params* p,
+                                   const bsq_sc_summary* s, const bsq_sc_position* rows, uint64_t n);
 
 /* Launch shape of the passes.  None of the knobs changes a result: every count is an integer sum
  * and every column and candidate is scored by one warp whatever the grid. */

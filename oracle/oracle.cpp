@@ -44,6 +44,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <string>
 #include <thread>
 #include <vector>
@@ -1018,3 +1019,236 @@ extern "C" void oracle_im_positions(const oracle_im_result* r, bsq_position_arra
   }
 }
 extern "C" void oracle_im_free(oracle_im_result* r) { delete r; }
+
+// ============================================================================ soft-clipping tabulation
+// tabulate_soft_clipping_counts (src/breseq/soft_clipping.cpp:285-666), restated over the decoded
+// records with the reference's containers: tallies keyed by seq_id in std::map (which fixes the row
+// order), tails packed 3 bits per base, the spanning denominator as a difference array.  Records the
+// reference would walk past their own arrays (no CIGAR, no reference-consuming op, a CIGAR query
+// length other than l_qseq, an alignment past the target's end) are reported as invalid instead.
+namespace {
+
+const uint32_t kScMaxConsensusBases = 21;   // soft_clipping.cpp:37
+
+// base_to_code over BAM 4-bit codes (soft_clipping.cpp:41-50): only A/C/G/T get 0..3
+inline uint32_t sc_code(uint8_t bam) {
+  switch (bam) { case 1: return 0; case 2: return 1; case 4: return 2; case 8: return 3; default: return 4; }
+}
+
+// sc_position_is_testable (soft_clipping.cpp:162-169)
+bool sc_testable(uint32_t p, uint32_t seq_length, uint32_t m) {
+  if (seq_length == 0) return false;
+  const uint32_t margin = m > 1 ? m : 1;
+  if (p <= margin) return false;
+  if ((uint64_t)p + margin > seq_length) return false;
+  return true;
+}
+
+// compute_clipped_tail_consensus (soft_clipping.cpp:98-147)
+void sc_consensus(const std::vector<uint64_t>& tails, uint32_t K, double base_fraction, std::string& cons,
+                  uint32_t& agree) {
+  cons.clear();
+  agree = (uint32_t)tails.size();
+  if (tails.empty() || base_fraction <= 0.0) return;
+  cons.assign(K, 'N');
+  std::vector<uint32_t> code(K, 4);
+  uint32_t informative = 0;
+  for (uint32_t col = 0; col < K; col++) {
+    uint32_t tally[4] = {0, 0, 0, 0};
+    for (uint64_t t : tails) { uint32_t c = (uint32_t)((t >> (3 * col)) & 7); if (c < 4) tally[c]++; }
+    uint32_t best = 4, best_n = 0;
+    for (uint32_t c = 0; c < 4; c++) if (tally[c] > best_n) { best_n = tally[c]; best = c; }
+    code[col] = best;
+    cons[col] = best < 4 ? "ACGT"[best] : 'N';
+    if (best < 4) informative++;
+  }
+  if (informative == 0) { cons.clear(); agree = 0; return; }
+  uint32_t required = (uint32_t)std::floor(base_fraction * (double)informative);
+  if (required < 1) required = 1;
+  agree = 0;
+  for (uint64_t t : tails) {
+    uint32_t matches = 0;
+    for (uint32_t col = 0; col < K; col++) {
+      if (code[col] >= 4) continue;
+      if (((t >> (3 * col)) & 7) == code[col]) matches++;
+    }
+    if (matches >= required) agree++;
+  }
+}
+
+struct ScRow { uint32_t target, position; int32_t direction; uint32_t clipped, total, agree; std::string tail; };
+
+}  // namespace
+
+struct oracle_sc_result { bsq_sc_summary s; std::vector<ScRow> rows; };
+
+extern "C" int oracle_soft_clipping(const bsq_reference* ref, const bsq_read_soa* rd, const char* const* names,
+                                    const bsq_sc_params* p, oracle_sc_result** res_out, char* errbuf, int errcap) {
+  const uint32_t m = p->minimum_clipped_bases;
+  const uint32_t T = ref->n_targets;
+  std::map<std::string, uint32_t> seq_lengths, tid_of;      // soft_clipping.cpp:296-300
+  for (uint32_t t = 0; t < T; t++) {
+    seq_lengths[names[t]] = (uint32_t)(ref->target_offset[t + 1] - ref->target_offset[t]);
+    tid_of[names[t]] = t;
+  }
+  std::map<std::string, std::map<uint32_t, uint32_t>> clipped_neg, clipped_pos;
+  std::map<std::string, std::map<uint32_t, std::vector<uint64_t>>> tails_neg, tails_pos;
+  std::map<std::string, std::vector<int32_t>> spanning_diff;
+  const uint32_t K = std::min(m, kScMaxConsensusBases);
+  uint64_t total_clipped = 0, total_agreeing = 0, total_tested = 0;
+  for (uint64_t r = 0; r < rd->n_reads; r++) {                // soft_clipping.cpp:366-453
+    if (rd->flag[r] & BSQ_FLAG_UNMAP) continue;
+    if (rd->x1[r] > 1) continue;
+    if (rd->xj && rd->xj[r]) continue;
+    const std::string seq_id = names[rd->tid[r]];
+    const uint32_t seq_length = seq_lengths[seq_id];
+    if (seq_length == 0) continue;
+    // bam_cigar2qlen / bam_endpos / query_start_1 / query_end_1 (alignment.cpp:248-290)
+    const uint32_t* cg = rd->cigar + rd->cigar_off[r];
+    const uint32_t nc = rd->n_cigar[r];
+    uint64_t qlen = 0, rlen = 0;
+    for (uint32_t k = 0; k < nc; k++) {
+      const uint32_t op = cg[k] & 0xf, len = cg[k] >> 4;
+      if (op == OP_M || op == OP_I || op == OP_S || op == OP_EQ || op == OP_X) qlen += len;
+      if (op_ref(op)) rlen += len;
+    }
+    if (nc == 0 || rlen == 0 || qlen != rd->l_qseq[r] || (uint64_t)rd->pos[r] + rlen > seq_length) {
+      if (errbuf) snprintf(errbuf, errcap, "record %llu: CIGAR does not match the read or runs past the target",
+                           (unsigned long long)r);
+      return BSQ_ERR_INVALID;
+    }
+    uint32_t qs1 = 1;
+    for (uint32_t k = 0; k < nc; k++) { if ((cg[k] & 0xf) != OP_S) break; qs1 += cg[k] >> 4; }
+    uint32_t qe1 = (uint32_t)qlen;
+    for (uint32_t k = nc - 1; k > 0; k--) { if ((cg[k] & 0xf) != OP_S) break; qe1 -= cg[k] >> 4; }
+    const uint32_t read_length = (uint32_t)qlen;
+    const uint32_t lead = qs1 - 1, trail = read_length - qe1;
+    const uint32_t ref_start = (uint32_t)rd->pos[r] + 1, ref_end = (uint32_t)(rd->pos[r] + rlen);
+    std::vector<int32_t>& sd = spanning_diff[seq_id];
+    if (sd.empty()) sd.resize(seq_length + 2, 0);
+    if ((uint64_t)ref_end >= (uint64_t)ref_start + 2ull * m) {
+      sd[ref_start + m] += 1;
+      sd[ref_end - m + 1] -= 1;
+    }
+    if (lead >= m && sc_testable(ref_start, seq_length, m)) {
+      clipped_neg[seq_id][ref_start]++;
+      total_clipped++;
+      uint64_t packed = 0;
+      for (uint32_t col = 0; col < K; col++)
+        packed |= (uint64_t)sc_code(base_at(rd, r, (int64_t)qs1 - 2 - col)) << (3 * col);
+      tails_neg[seq_id][ref_start].push_back(packed);
+    }
+    if (trail >= m && sc_testable(ref_end, seq_length, m)) {
+      clipped_pos[seq_id][ref_end]++;
+      total_clipped++;
+      uint64_t packed = 0;
+      for (uint32_t col = 0; col < K; col++)
+        packed |= (uint64_t)sc_code(base_at(rd, r, (int64_t)qe1 + col)) << (3 * col);
+      tails_pos[seq_id][ref_end].push_back(packed);
+    }
+  }
+  // prefix sums of the difference arrays (soft_clipping.cpp:455-490)
+  std::map<std::string, std::vector<uint32_t>> spanning;
+  uint64_t total_spanning = 0;
+  for (auto& kv : seq_lengths) {
+    auto it = spanning_diff.find(kv.first);
+    if (it == spanning_diff.end()) continue;
+    std::vector<int32_t>& sd = it->second;
+    std::vector<uint32_t>& sp = spanning[kv.first];
+    sp.assign(sd.size(), 0);
+    int32_t running = 0;
+    for (uint32_t q = 1; q < sd.size(); q++) {
+      running += sd[q];
+      sp[q] = running > 0 ? (uint32_t)running : 0;
+      if (sc_testable(q, kv.second, m)) {
+        total_spanning += 2ull * sp[q];
+        if (sp[q] > 0) total_tested += 2;
+      }
+    }
+  }
+  // rows with their tail consensus (soft_clipping.cpp:500-545)
+  oracle_sc_result* res = new oracle_sc_result();
+  for (int32_t dir = -1; dir <= 1; dir += 2) {
+    auto& clipped = dir < 0 ? clipped_neg : clipped_pos;
+    auto& tails = dir < 0 ? tails_neg : tails_pos;
+    for (auto& sk : clipped) {
+      const std::vector<uint32_t>& cov = spanning[sk.first];
+      for (auto& pk : sk.second) {
+        ScRow row;
+        row.target = tid_of[sk.first];
+        row.position = pk.first;
+        row.direction = dir;
+        row.clipped = pk.second;
+        const uint32_t read_through = pk.first < cov.size() ? cov[pk.first] : 0;
+        row.total = row.clipped + read_through;
+        sc_consensus(tails[sk.first][pk.first], K, p->consensus_base_fraction, row.tail, row.agree);
+        if (dir < 0) std::reverse(row.tail.begin(), row.tail.end());
+        total_agreeing += row.agree;
+        if (read_through == 0) total_tested++;
+        res->rows.push_back(row);
+      }
+    }
+  }
+  // genome-wide totals and the dispersion fit (soft_clipping.cpp:547-623)
+  bsq_sc_summary& s = res->s;
+  memset(&s, 0, sizeof s);
+  const uint64_t total_opp = total_clipped + total_spanning;
+  s.total_spanning_read_bases = total_spanning;
+  s.total_clipped_read_ends = total_clipped;
+  s.total_agreeing_clipped_read_ends = total_agreeing;
+  s.soft_clipping_rate = total_opp > 0 ? (double)total_clipped / (double)total_opp : 0.0;
+  const double p0_raw = total_opp > 0 ? (double)total_agreeing / (double)total_opp : 0.0;
+  double p0 = p0_raw;
+  if (p->minimum_rate > 0.0 && p0 < p->minimum_rate) p0 = p->minimum_rate;
+  double S_k = 0.0, S_k2_over_n = 0.0, S_n_trimmed = 0.0;
+  const double S_n = (double)total_opp;
+  uint64_t trimmed = 0;
+  for (const ScRow& row : res->rows) {
+    if (row.total == 0) continue;
+    const double k = (double)row.agree, n = (double)row.total;
+    if (p->dispersion_trim_frequency > 0.0 && k / n >= p->dispersion_trim_frequency) {
+      trimmed++;
+      S_n_trimmed += n;
+      continue;
+    }
+    S_k += k;
+    S_k2_over_n += k * k / n;
+  }
+  const uint64_t N_prime = total_tested > trimmed ? total_tested - trimmed : 0;
+  const double S_n_prime = S_n - S_n_trimmed;
+  const double mean_n_prime = N_prime > 0 ? S_n_prime / (double)N_prime : 0.0;
+  double phi = 0.0, rho = 0.0;
+  if (N_prime > 1 && mean_n_prime > 1.0 && p0 > 0.0 && p0 < 1.0) {
+    const double chi2 = (S_k2_over_n - 2.0 * p0 * S_k + p0 * p0 * S_n_prime) / (p0 * (1.0 - p0));
+    phi = chi2 / (double)(N_prime - 1);
+    rho = (phi - 1.0) / (mean_n_prime - 1.0);
+  }
+  const double rho_raw = rho;
+  if (!std::isfinite(rho) || rho < 0.0) rho = 0.0;
+  if (p->maximum_dispersion > 0.0 && rho > p->maximum_dispersion) rho = p->maximum_dispersion;
+  if (rho < 1e-6) rho = 0.0;
+  s.null_rate = p0;
+  s.null_rate_raw = p0_raw;
+  s.dispersion = rho;
+  s.dispersion_raw = rho_raw;
+  s.pearson_phi = phi;
+  s.tested_positions = N_prime;
+  s.trimmed_positions = trimmed;
+  s.mean_tested_reads = mean_n_prime;
+  s.n_positions = res->rows.size();
+  *res_out = res;
+  return BSQ_OK;
+}
+
+extern "C" void oracle_sc_summary(const oracle_sc_result* r, bsq_sc_summary* s) { *s = r->s; }
+extern "C" void oracle_sc_rows(const oracle_sc_result* r, bsq_sc_position* out) {
+  for (size_t i = 0; i < r->rows.size(); i++) {
+    const ScRow& w = r->rows[i];
+    bsq_sc_position& o = out[i];
+    memset(&o, 0, sizeof o);
+    o.target = w.target; o.position = w.position; o.direction = w.direction;
+    o.clipped_count = w.clipped; o.total_count = w.total; o.agree_count = w.agree;
+    snprintf(o.clipped_sequence, sizeof o.clipped_sequence, "%s", w.tail.c_str());
+  }
+}
+extern "C" void oracle_sc_free(oracle_sc_result* r) { delete r; }

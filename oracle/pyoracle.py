@@ -33,6 +33,11 @@ def lib():
         L.oracle_fisher_2x2.restype = C.c_double
         L.oracle_ks_less.argtypes = [C.POINTER(C.c_double), C.c_uint32, C.POINTER(C.c_double), C.c_uint32]
         L.oracle_ks_less.restype = C.c_double
+        L.oracle_soft_clipping.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.POINTER(C.c_char_p),
+                                           C.POINTER(abi.ScParams), C.POINTER(C.c_void_p), C.c_char_p, C.c_int]
+        L.oracle_sc_summary.argtypes = [C.c_void_p, C.POINTER(abi.ScSummary)]
+        L.oracle_sc_rows.argtypes = [C.c_void_p, C.c_void_p]
+        L.oracle_sc_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -138,3 +143,27 @@ def ks_less(x, y):
     x = np.ascontiguousarray(x, dtype=np.float64)
     y = np.ascontiguousarray(y, dtype=np.float64)
     return lib().oracle_ks_less(abi.ptr(x, C.c_double), len(x), abi.ptr(y, C.c_double), len(y))
+
+
+def soft_clipping(sample, minimum_clipped_bases=12, consensus_base_fraction=0.95, dispersion_trim_frequency=0.25,
+                  maximum_dispersion=0.005, minimum_rate=1e-5):
+    """tabulate_soft_clipping_counts restated on the CPU: dict(summary, rows) in the library's format.
+    The row order comes from the oracle's own std::map over the target names."""
+    view = abi.SampleView(sample)
+    names = (C.c_char_p * len(sample.target_names))(*[n.encode() for n in sample.target_names])
+    p = abi.ScParams(minimum_clipped_bases=minimum_clipped_bases, consensus_base_fraction=consensus_base_fraction,
+                     dispersion_trim_frequency=dispersion_trim_frequency, maximum_dispersion=maximum_dispersion,
+                     minimum_rate=minimum_rate)
+    h = C.c_void_p()
+    err = C.create_string_buffer(256)
+    rc = lib().oracle_soft_clipping(C.byref(view.ref), C.byref(view.reads), names, C.byref(p), C.byref(h), err, 256)
+    if rc != 0:
+        raise OracleError(f"oracle_soft_clipping failed ({rc}): {err.value.decode()}")
+    try:
+        s = abi.ScSummary()
+        lib().oracle_sc_summary(h, C.byref(s))
+        rows = (abi.ScPosition * max(1, s.n_positions))()
+        lib().oracle_sc_rows(h, rows)
+        return dict(summary=abi.sc_summary_dict(s), rows=abi.sc_rows_array(rows, s.n_positions))
+    finally:
+        lib().oracle_sc_free(h)
