@@ -18,6 +18,10 @@ polymorphism modes), drawn from a pool of distinct seeded samples:
   "served":  open-loop Poisson arrivals at 0.5/1/2x the batched capacity into the scoring server
              (HBM-footprint admission, continuous batching), with p50/p99 job latency.
 
+A "soft_clipping" leg times the soft-clipping tabulation (tabulate_soft_clipping_counts) on a sample
+of the same shape with 50 junction breakpoints and 1% of reads clipped by 12-40 random bases, against
+the oracle's CPU tabulation of the same sample.
+
 Under torchrun each rank scores its own sample (weak scaling, no collective in the data path); the
 timed region is bracketed by barriers and the slowest rank's time is used.
 """
@@ -131,6 +135,73 @@ def _max_over_ranks(pg, v: float) -> float:
 def _workload(seed: int, scale: float = 1.0):
     from breseq_gb300 import synth
     return synth.simulate(synth.config_ecoli(seed=seed, scale=scale))
+
+
+SC_WORKLOAD = "ecoli_4.79Mb_pe150_2x100x_50breakpoints_1pct_long_clips"
+# count pass of the tabulation: one 32-byte record per read and one 4-byte difference-array entry per
+# column (DRAM bytes per launch measured in profiles/sc_reads_kernel_ecoli_breakpoints.md)
+SC_READS_DRAM_PER_READ = None
+
+
+def run_softclip(args, device):
+    """tabulate_soft_clipping_counts on a resident sample: device time of the call, its read pass
+    (the dominant kernel), the end-to-end call from host buffers, and the oracle on the CPU."""
+    import dataclasses
+    from breseq_gb300 import abi, synth
+    from breseq_gb300.api import Scorer, ScSettings
+    from oracle import pyoracle as po
+    c = synth.config_ecoli(seed=23, scale=args.scale)
+    s = synth.simulate(dataclasses.replace(c, breakpoints=50, long_clip_fraction=0.01, softclip_fraction=0.02))
+    n_cols = s.total_length() + len(s.target_offset) - 1
+    with Scorer(device) as sc:
+        sid = sc.load_sample(s)
+        for _ in range(args.warmup):
+            g = sc.soft_clipping(sid)
+        dev, main, wall = [], [], []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            g = sc.soft_clipping(sid)
+            wall.append(1e3 * (time.perf_counter() - t0))
+            st = sc.last_pass_stats()
+            dev.append(st["device_ms"]); main.append(st["main_kernel_ms"])
+        launches = st["kernel_launches"]
+        sc.free_sample(sid)
+        # end to end: upload from pinned host buffers, tabulation, rows back, free
+        view = abi.SampleView(s)
+        pinned = [a for a in view._keep if a.nbytes >= 1 << 16 and sc.L.bsq_host_register(a.ctypes.data, a.nbytes) == 0]
+        e2e = []
+        for i in range(args.warmup + args.steps):
+            sc.timer_start()
+            sid2 = sc.load_sample(s)
+            sc.soft_clipping(sid2)
+            sc.free_sample(sid2)
+            t = sc.timer_stop()
+            if i >= args.warmup:
+                e2e.append(t)
+        for a in pinned:
+            sc.L.bsq_host_unregister(a.ctypes.data)
+    t0 = time.perf_counter()
+    o = po.soft_clipping(s)
+    cpu_s = time.perf_counter() - t0
+    same = g["summary"] == o["summary"] and np.array_equal(g["rows"], o["rows"])
+    ms, kms = statistics.mean(dev), statistics.mean(main)
+    hbm, peak_kind = _peaks()
+    kbytes = 32 * s.n_reads + 4 * n_cols
+    out = {"workload": SC_WORKLOAD if args.scale == 1.0 else f"{SC_WORKLOAD} scaled x{args.scale:g}",
+           "reads": s.n_reads, "genome_bp": s.total_length(), "rows": int(g["summary"]["n_positions"]),
+           "clip_events": int(g["summary"]["total_clipped_read_ends"]),
+           "device_ms": ms, "wall_ms": statistics.mean(wall), "kernel_launches": launches,
+           "value": s.n_reads / (ms / 1e3), "unit": "records/s",
+           "e2e": {"ms": statistics.mean(e2e), "value": s.n_reads / (statistics.mean(e2e) / 1e3), "unit": "records/s",
+                   "h2d_bytes": int(sum(a.nbytes for a in view._keep))},
+           "roofline": {"bound": "hbm", "kernel": "sc_reads_kernel", "achieved": kbytes / (kms / 1e3) / 1e9,
+                        "peak": hbm, "unit": "GB/s", "frac": kbytes / (kms / 1e3) / 1e9 / hbm, "kernel_ms": kms,
+                        "algorithmic_bytes": kbytes, "peak_kind": peak_kind,
+                        "traffic": SC_READS_DRAM_PER_READ * s.n_reads if SC_READS_DRAM_PER_READ else None},
+           "identical_to_oracle": bool(same),
+           "cpu_baseline": {"value": s.n_reads / cpu_s, "unit": "records/s", "cores": 1, "kind": "port",
+                            "sample": f"the same sample, one run ({cpu_s:.2f} s)"}}
+    return out
 
 
 _CPU_SAMPLE = {}
@@ -343,6 +414,8 @@ def run_ours(args, world, rank, local, pg):
     sc.close()
     if rank == 0 and args.batch_jobs > 0:
         line["batched"], line["served"] = run_mix(args, local)
+    if rank == 0 and not args.no_softclip:
+        line["soft_clipping"] = run_softclip(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -487,6 +560,7 @@ def main():
     ap.add_argument("--served-jobs", type=int, default=288)
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--no-softclip", action="store_true", help="skip the soft-clipping leg")
     args = ap.parse_args()
     world, rank, local, pg = _dist()
     if args.impl == "reference":

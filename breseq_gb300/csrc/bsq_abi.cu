@@ -114,7 +114,7 @@ struct bsq_ctx {
   std::vector<std::vector<bsq_mc_record>> res_mc;
   std::vector<std::vector<bsq_un_record>> res_un;
   // soft-clipping tabulation: working buffers and the rows of the last call
-  DevMem sc_diff, sc_cnt, sc_blk, sc_tot, sc_rows, sc_outs, sc_tails;
+  DevMem sc_diff, sc_cnt, sc_blk, sc_tot, sc_rows, sc_outs, sc_tails, sc_ev, sc_ev_n;
   std::vector<bsq_sc_position> sc_res;
   double last_ms = 0, main_ms = 0;
   uint32_t launches = 0;
@@ -306,7 +306,8 @@ void bsq_destroy(bsq_ctx* ctx) {
   for (DevMem* m : {&ctx->cov, &ctx->call, &ctx->blk, &ctx->cand, &ctx->next, &ctx->ra, &ctx->bq, &ctx->pool,
                     &ctx->qhist, &ctx->scratch, &ctx->keep, &ctx->kcol, &ctx->kcov, &ctx->kcall,
                     &ctx->d_chunks, &ctx->ec_arena, &ctx->im_arena, &ctx->ctl, &ctx->sc_diff, &ctx->sc_cnt,
-                    &ctx->sc_blk, &ctx->sc_tot, &ctx->sc_rows, &ctx->sc_outs, &ctx->sc_tails})
+                    &ctx->sc_blk, &ctx->sc_tot, &ctx->sc_rows, &ctx->sc_outs, &ctx->sc_tails, &ctx->sc_ev,
+                    &ctx->sc_ev_n})
     m->release();
   if (ctx->exec_ec) cudaGraphExecDestroy(ctx->exec_ec);
   if (ctx->exec_im) cudaGraphExecDestroy(ctx->exec_im);
@@ -982,16 +983,6 @@ int bsq_soft_clipping(bsq_ctx* ctx, int32_t sample_id, const bsq_sc_params* p, b
   }
   cudaStream_t st = ctx->stream;
   cudaGetLastError();
-  const uint32_t nb = (s->n_cols + kScBlockCols - 1) / kScBlockCols;
-  const uint64_t cstride = (uint64_t)nb * kScBlockCols;
-  CK(ctx->sc_diff.alloc(cstride * 4, st));
-  CK(ctx->sc_cnt.alloc(cstride * 8, st));
-  CK(ctx->sc_blk.alloc((uint64_t)nb * 5 * 8, st));
-  CK(ctx->sc_tot.alloc(128, st));
-  CK(record(ctx->ev0, st));
-  CK(cudaMemsetAsync(ctx->sc_diff.p, 0, cstride * 4, st));
-  CK(cudaMemsetAsync(ctx->sc_cnt.p, 0, cstride * 8, st));
-  CK(cudaMemsetAsync(ctx->sc_tot.p, 0, 128, st));
   ScArgs A;
   memset(&A, 0, sizeof A);
   A.reads = s->reads.as<DevRead>();
@@ -1001,8 +992,21 @@ int bsq_soft_clipping(bsq_ctx* ctx, int32_t sample_id, const bsq_sc_params* p, b
   A.n_reads = s->n_reads;
   A.n_targets = T;
   A.n_cols = s->n_cols;
-  A.n_blocks = nb;
-  A.cstride = cstride;
+  sc_plan(A, ctx->sms);
+  const uint32_t nb = A.n_blocks;
+  const uint64_t cstride = A.cstride;
+  CK(ctx->sc_diff.alloc(cstride * 4, st));
+  CK(ctx->sc_cnt.alloc(cstride * 8, st));
+  CK(ctx->sc_blk.alloc((uint64_t)nb * 5 * 8, st));
+  CK(ctx->sc_tot.alloc(128, st));
+  CK(ctx->sc_ev.alloc((uint64_t)s->n_reads * 4, st));
+  CK(ctx->sc_ev_n.alloc((uint64_t)A.ev_blocks * 4, st));
+  CK(record(ctx->ev0, st));
+  CK(cudaMemsetAsync(ctx->sc_diff.p, 0, cstride * 4, st));
+  CK(cudaMemsetAsync(ctx->sc_cnt.p, 0, cstride * 8, st));
+  CK(cudaMemsetAsync(ctx->sc_tot.p, 0, 128, st));
+  A.ev = ctx->sc_ev.as<uint32_t>();
+  A.ev_n = ctx->sc_ev_n.as<uint32_t>();
   A.m = p->minimum_clipped_bases;
   A.K = std::min(p->minimum_clipped_bases, kScMaxConsensus);
   A.base_fraction = p->consensus_base_fraction;
@@ -1011,7 +1015,7 @@ int bsq_soft_clipping(bsq_ctx* ctx, int32_t sample_id, const bsq_sc_params* p, b
   A.blk = ctx->sc_blk.as<long long>();
   A.tot = ctx->sc_tot.as<unsigned long long>();
   A.err = reinterpret_cast<uint32_t*>(ctx->sc_tot.as<unsigned char>() + 64);
-  CK(sc_launch_count(A, ctx->sms, st));
+  CK(sc_launch_count(A, ctx->sms, st, ctx->evm0, ctx->evm1));
   CK(ctx->pin_out.reserve(128));
   CK(cudaMemcpyAsync(ctx->pin_out.p, ctx->sc_tot.p, 128, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -1039,8 +1043,8 @@ int bsq_soft_clipping(bsq_ctx* ctx, int32_t sample_id, const bsq_sc_params* p, b
   CK(record(ctx->ev1, st));
   CK(cudaStreamSynchronize(st));
   ctx->last_ms = elapsed(ctx->ev0, ctx->ev1);
-  ctx->main_ms = 0;
-  ctx->launches = n_rows ? (s->n_reads ? 7 : 5) : (s->n_reads ? 4 : 3);
+  ctx->main_ms = elapsed(ctx->evm0, ctx->evm1);   // the read pass that counts the events
+  ctx->launches = n_rows ? 7 : 4;
   ctx->last_h2d = 0;
   ctx->last_d2h = 128 + 64 + rows_bytes + outs_bytes;
   memcpy(tot, h, 64);

@@ -6,8 +6,8 @@
 //      into per-column counters, one array per direction;
 //   2. column scan: spanning coverage, the testable totals, and the rows (columns with events) in
 //      (direction, column) order with each row's slice of the tail array;
-//   3. read pass (scatter): each clip event packs its tail (3 bits a base, outward from the clip
-//      wall) into its row's slice;
+//   3. scatter: the reads the count pass listed (those with clip events) pack each tail (3 bits a
+//      base, outward from the clip wall) into its row's slice;
 //   4. consensus: one warp per row tallies the tails column by column and counts agreeing tails.
 // The dispersion fit is O(rows) scalar arithmetic and runs on the host in the reference's row order.
 #pragma once
@@ -19,7 +19,8 @@
 namespace bsq {
 
 constexpr uint32_t kScMaxConsensus = 21;     // soft_clipping.cpp:37 (3 bits a base in 64)
-constexpr uint32_t kScBlockCols = 1024;      // columns per scan block (256 threads x 4)
+constexpr uint32_t kScBlockCols = 2048;      // columns per scan block (256 threads x 8)
+constexpr uint32_t kScSmallRow = 4;          // rows with at most this many tails: one lane each
 
 // A (position, direction) with clip events.
 struct ScRowDev {
@@ -51,13 +52,21 @@ struct ScArgs {
   long long* blk;                  // [5 * n_blocks] per-block sums, then their exclusive scan
   unsigned long long* tot;         // [8]: rows(-1), tails(-1), rows(+1), tails(+1), spanning read bases, tested positions
   uint32_t* err;                   // kErrCigar: a kept record whose CIGAR does not fit
+  // the count pass gives block b the reads [b * ev_per_block, (b + 1) * ev_per_block) and lists
+  // those with clip events at ev[b * ev_per_block ..], ev_n[b] of them
+  uint32_t* ev;                    // [n_reads]
+  uint32_t* ev_n;                  // [ev_blocks]
+  uint32_t ev_blocks, ev_per_block;
   ScRowDev* rows;                  // [rows(-1) + rows(+1)]
   ScOutDev* outs;
   unsigned long long* tails;       // [tails(-1) + tails(+1)]
 };
 
+// Grid shapes: n_blocks, cstride, ev_blocks and ev_per_block from n_reads and n_cols.
+void sc_plan(ScArgs& A, int sms);
 // Read pass (count), block sums and their scan: afterwards tot[0..3] hold the row and tail totals.
-cudaError_t sc_launch_count(const ScArgs& A, int sms, cudaStream_t st);
+// main0 / main1 (may be null) are recorded around the read pass.
+cudaError_t sc_launch_count(const ScArgs& A, int sms, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1);
 // Rows and cursors, tail scatter and consensus, once rows / outs / tails are allocated.
 cudaError_t sc_launch_rows(const ScArgs& A, uint32_t n_rows, int sms, cudaStream_t st);
 

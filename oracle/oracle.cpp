@@ -30,6 +30,10 @@
  *   - fisher_exact_test_2x2 / ks_test_two_sample_less   src/breseq/stats.cpp:2144-2286
  *   - check_deletion_completion / update_unknown_intervals / at_target_end  :2262-2344, :2972-3007, :2107-2164
  *   - alignment accessors (query bounds, trims, redundancy)  src/breseq/alignment.cpp:44-290, alignment.h:355-411
+ *   - tabulate_soft_clipping_counts / compute_clipped_tail_consensus / sc_position_is_testable
+ *                                               src/breseq/soft_clipping.cpp:98-169, 285-666
+ *     (pinned by hand-worked answers and the rules the reference states in its comments; see
+ *     tests/test_softclip.py)
  *
  * One deliberate divergence: where the reference would index a read past its end (a deletion that is
  * followed by a single aligned base, error_count.cpp:1073), it aborts on an assert; here the base is
