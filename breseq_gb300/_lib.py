@@ -93,6 +93,10 @@ def load():
     L.bsq_sc_result_copy.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
     L.bsq_write_soft_clipping_counts.argtypes = [C.c_char_p, P(C.c_char_p), P(abi.ScParams), P(abi.ScSummary),
                                                  C.c_void_p, C.c_uint64]
+    L.bsq_coverage_columns.argtypes = [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32, C.c_uint32, P(abi.CovColumns),
+                                       P(C.c_uint32)]
+    L.bsq_write_coverage_region.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, C.c_uint32, C.c_uint32,
+                                            C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_double)]
     _lib = L
     return L
 
@@ -109,4 +113,5 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_timer_stop", "bsq_host_register", "bsq_host_unregister", "bsq_score_positions_noalloc",
             "bsq_default_ra_settings", "bsq_test_ra_evidence", "bsq_write_error_rates", "bsq_write_base_qual_error_prob",
             "bsq_write_coverage_distribution", "bsq_write_coverage_table", "bsq_format_ra", "bsq_write_gd",
-            "bsq_default_sc_params", "bsq_soft_clipping", "bsq_sc_result_copy", "bsq_write_soft_clipping_counts")
+            "bsq_default_sc_params", "bsq_soft_clipping", "bsq_sc_result_copy", "bsq_write_soft_clipping_counts",
+            "bsq_coverage_columns", "bsq_write_coverage_region")

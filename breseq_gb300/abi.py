@@ -266,6 +266,27 @@ def sc_summary_dict(s: ScSummary) -> dict:
     return {name: getattr(s, name) for name, _ in ScSummary._fields_}
 
 
+class CovColumns(C.Structure):
+    _fields_ = [
+        ("unique_top", P(C.c_uint32)),
+        ("unique_bot", P(C.c_uint32)),
+        ("redundant_top", P(C.c_double)),
+        ("redundant_bot", P(C.c_double)),
+        ("raw_redundant_top", P(C.c_uint32)),
+        ("raw_redundant_bot", P(C.c_uint32)),
+        ("unique_top_begin", P(C.c_uint32)),
+        ("unique_bot_begin", P(C.c_uint32)),
+    ]
+
+
+def cov_columns(n: int):
+    """Numpy arrays for one region of n positions and the bsq_cov_columns struct pointing at them."""
+    arrs = {name: np.zeros(n, dtype=np.float64 if "redundant_" in name and "raw" not in name else np.uint32)
+            for name, _ in CovColumns._fields_}
+    st = CovColumns(**{k: ptr(v, C.c_double if v.dtype == np.float64 else C.c_uint32) for k, v in arrs.items()})
+    return arrs, st
+
+
 SC_ROW_DTYPE = np.dtype([("target", np.uint32), ("position", np.uint32), ("direction", np.int32),
                          ("clipped_count", np.uint32), ("total_count", np.uint32), ("agree_count", np.uint32),
                          ("clipped_sequence", "S24")])

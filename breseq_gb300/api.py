@@ -256,6 +256,25 @@ class Scorer:
         self._check(self.L.bsq_sc_result_copy(self.ctx, rows, s.n_positions))
         return dict(summary=abi.sc_summary_dict(s), rows=abi.sc_rows_array(rows, s.n_positions))
 
+    # ------------------------------------------------------------------ BAM2COV coverage table
+    def coverage_columns(self, sid: int, tid: int, start: int, end: int) -> dict:
+        """Per-position coverage of positions start..end (1-based) of target tid as `breseq BAM2COV`
+        tabulates it, and the pileup's last column ("last")."""
+        arrs, st = abi.cov_columns(end - start + 1)
+        last = C.c_uint32()
+        self._check(self.L.bsq_coverage_columns(self.ctx, sid, tid, start, end, C.byref(st), C.byref(last)))
+        arrs["last"] = last.value
+        return arrs
+
+    def write_coverage_region(self, sid: int, path: str, tid: int, start: int, end: int, resolution: int = 600,
+                              total_only: bool = False, csv: bool = False, reference_average=None):
+        """`breseq BAM2COV --format TSV|CSV -r seq:start-end --resolution N` into path."""
+        s = self.sample(sid)
+        flags = (1 if total_only else 0) | (2 if csv else 0)
+        avg = C.byref(C.c_double(reference_average)) if reference_average is not None else None
+        self._check(self.L.bsq_write_coverage_region(self.ctx, sid, path.encode(), s.target_names[tid].encode(), tid,
+                                                     start, end, resolution, flags, avg))
+
     # ------------------------------------------------------------------ launch shapes
     def tuning(self) -> dict:
         t = abi.Tuning()

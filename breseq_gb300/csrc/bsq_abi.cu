@@ -22,6 +22,7 @@
 #include "bsq_kernels.h"
 #include "bsq_noalloc.h"
 #include "bsq_softclip.h"
+#include "bsq_covtable.h"
 
 using namespace bsq;
 
@@ -115,6 +116,8 @@ struct bsq_ctx {
   std::vector<std::vector<bsq_un_record>> res_un;
   // soft-clipping tabulation: working buffers and the rows of the last call
   DevMem sc_diff, sc_cnt, sc_blk, sc_tot, sc_rows, sc_outs, sc_tails, sc_ev, sc_ev_n;
+  // coverage table of a region
+  DevMem ct_diff, ct_blk, ct_counts, ct_red, ct_stat, ct_ref;
   std::vector<bsq_sc_position> sc_res;
   double last_ms = 0, main_ms = 0;
   uint32_t launches = 0;
@@ -307,7 +310,8 @@ void bsq_destroy(bsq_ctx* ctx) {
                     &ctx->qhist, &ctx->scratch, &ctx->keep, &ctx->kcol, &ctx->kcov, &ctx->kcall,
                     &ctx->d_chunks, &ctx->ec_arena, &ctx->im_arena, &ctx->ctl, &ctx->sc_diff, &ctx->sc_cnt,
                     &ctx->sc_blk, &ctx->sc_tot, &ctx->sc_rows, &ctx->sc_outs, &ctx->sc_tails, &ctx->sc_ev,
-                    &ctx->sc_ev_n})
+                    &ctx->sc_ev_n, &ctx->ct_diff, &ctx->ct_blk, &ctx->ct_counts, &ctx->ct_red, &ctx->ct_stat,
+                    &ctx->ct_ref})
     m->release();
   if (ctx->exec_ec) cudaGraphExecDestroy(ctx->exec_ec);
   if (ctx->exec_im) cudaGraphExecDestroy(ctx->exec_im);
@@ -1050,6 +1054,109 @@ int bsq_soft_clipping(bsq_ctx* ctx, int32_t sample_id, const bsq_sc_params* p, b
   memcpy(tot, h, 64);
   host::sc_assemble(reinterpret_cast<const ScRowDev*>(h + 128), reinterpret_cast<const ScOutDev*>(h + 128 + rows_bytes),
                     tot[0], tot[2], s->tpoff, order, A.K, *p, n_tails, tot[4], tot[5], ctx->sc_res, *summary);
+  return BSQ_OK;
+}
+
+// Coverage columns of one region (coverage_output::pileup_callback, coverage_output.cpp:307-470):
+// bsq_covtable.cu on the device; the counts, weights and reference characters come back in one
+// pinned buffer.  Layout of the host copy: [6][n] u32 counts | [2][n] f64 weights | stat | the
+// target's reference characters up to end_1.
+struct CovRegion {
+  const uint32_t* counts;
+  const double* red;
+  const char* ref;
+  uint32_t n, last;
+};
+static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start, uint32_t end, CovRegion& out) {
+  SampleDev* s = find_sample(ctx, sample_id);
+  if (!s) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
+  if (tid >= s->n_targets) return fail(ctx, BSQ_ERR_INVALID, "target index out of range");
+  const uint32_t tlen = s->tpoff[tid + 1] - s->tpoff[tid] - 1;
+  if (start < 1 || start > end || end > tlen) return fail(ctx, BSQ_ERR_INVALID, "region outside the target");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  cudaGetLastError();
+  const uint32_t n = end - start + 1;
+  CovTabArgs A;
+  memset(&A, 0, sizeof A);
+  A.reads = s->reads.as<DevRead>();
+  A.cigar = s->cigar.as<uint32_t>();
+  A.x1 = s->x1.as<uint32_t>();
+  A.rstart = s->rstart.as<uint32_t>();
+  A.n_reads = s->n_reads;
+  A.t0 = s->tpoff[tid];
+  A.c0 = A.t0 + start - 1;
+  A.n = n;
+  A.n_blocks = (uint32_t)(((uint64_t)n + 1 + kCtBlockCols - 1) / kCtBlockCols);
+  A.stride = (uint64_t)A.n_blocks * kCtBlockCols;
+  CK(ctx->ct_diff.alloc(A.stride * 16, st));
+  CK(ctx->ct_blk.alloc((uint64_t)A.n_blocks * 32, st));
+  CK(ctx->ct_counts.alloc((uint64_t)n * 24, st));
+  CK(ctx->ct_red.alloc((uint64_t)n * 16, st));
+  CK(ctx->ct_stat.alloc(64, st));
+  A.diff = ctx->ct_diff.as<int32_t>();
+  A.blk = ctx->ct_blk.as<long long>();
+  A.counts = ctx->ct_counts.as<uint32_t>();
+  A.red = ctx->ct_red.as<double>();
+  A.stat = ctx->ct_stat.as<uint32_t>();
+  CK(record(ctx->ev0, st));
+  CK(cudaMemsetAsync(A.diff, 0, A.stride * 16, st));
+  CK(cudaMemsetAsync(A.counts + 4ull * n, 0, (uint64_t)n * 8, st));
+  CK(cudaMemsetAsync(A.stat, 0, 64, st));
+  CK(record(ctx->evm0, st));
+  CK(ct_launch(A, ctx->sms, st));
+  CK(record(ctx->evm1, st));
+  const size_t cbytes = (size_t)n * 24, rbytes = (size_t)n * 16;
+  CK(ctx->pin_out.reserve(cbytes + rbytes + 64 + end + 16));
+  unsigned char* h = ctx->pin_out.at(0);
+  CK(cudaMemcpyAsync(h, A.counts, cbytes, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h + cbytes, A.red, rbytes, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h + cbytes + rbytes, A.stat, 64, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h + cbytes + rbytes + 64, s->ref.as<uint8_t>() + A.t0, end, cudaMemcpyDeviceToHost, st));
+  CK(record(ctx->ev1, st));
+  CK(cudaStreamSynchronize(st));
+  ctx->last_ms = elapsed(ctx->ev0, ctx->ev1);
+  ctx->main_ms = elapsed(ctx->evm0, ctx->evm1);
+  ctx->launches = 6;
+  ctx->last_h2d = 0;
+  ctx->last_d2h = cbytes + rbytes + 64 + end;
+  const uint32_t* stat = reinterpret_cast<const uint32_t*>(h + cbytes + rbytes);
+  if (stat[2]) return fail(ctx, BSQ_ERR_INVALID, "invalid records: " + err_text(stat[2]));
+  out.counts = reinterpret_cast<const uint32_t*>(h);
+  out.red = reinterpret_cast<const double*>(h + cbytes);
+  out.ref = reinterpret_cast<const char*>(h + cbytes + rbytes + 64);
+  out.n = n;
+  out.last = stat[0];
+  return BSQ_OK;
+}
+
+int bsq_coverage_columns(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start_1, uint32_t end_1,
+                         bsq_cov_columns* out, uint32_t* last_column_1) {
+  if (!ctx || !out) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  CovRegion R;
+  const int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, R);
+  if (rc != BSQ_OK) return rc;
+  uint32_t* const u32[6] = {out->unique_top, out->unique_bot, out->raw_redundant_top, out->raw_redundant_bot,
+                            out->unique_top_begin, out->unique_bot_begin};
+  for (int q = 0; q < 6; q++)
+    if (u32[q]) memcpy(u32[q], R.counts + (size_t)q * R.n, (size_t)R.n * 4);
+  if (out->redundant_top) memcpy(out->redundant_top, R.red, (size_t)R.n * 8);
+  if (out->redundant_bot) memcpy(out->redundant_bot, R.red + R.n, (size_t)R.n * 8);
+  if (last_column_1) *last_column_1 = R.last;
+  return BSQ_OK;
+}
+
+int bsq_write_coverage_region(bsq_ctx* ctx, int32_t sample_id, const char* path, const char* seq_id, uint32_t tid,
+                              uint32_t start_1, uint32_t end_1, uint32_t resolution, uint32_t flags,
+                              const double* reference_average) {
+  if (!ctx || !path) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  CovRegion R;
+  const int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, R);
+  if (rc != BSQ_OK) return rc;
+  (void)seq_id;   // the table has no seq_id column; the name is part of the caller's file name
+  host::CoverageRegion H{R.counts, R.red, R.ref, start_1, end_1, R.last};
+  if (!host::write_coverage_region(path, H, resolution, flags, reference_average))
+    return fail(ctx, BSQ_ERR_INVALID, std::string("cannot write ") + path);
   return BSQ_OK;
 }
 

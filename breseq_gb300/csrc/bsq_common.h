@@ -25,16 +25,18 @@ struct __align__(16) DevRead {
   uint16_t xr;         // XR trim, 0xFFFF when absent
   uint8_t mapq_idx;    // index of this read's MAPQ among the sample's distinct values
   uint8_t rfile;       // flat read-file index (k_read_set covariate)
-  uint8_t flags;       // kRev | kSimple | kRedundant | kSkip | kScSkip | kScBad
+  uint8_t flags;       // kRev | kSimple | kRedundant | kSkip | kScSkip | kBadCigar | kFiltered
   uint8_t clip;        // simple reads: leading soft clip
 };
 static_assert(sizeof(DevRead) == 32, "DevRead must stay 32 bytes");
 
-// kSkip: the pileup leaves the record out (flag filter or a target outside the pileup set).
-// kScSkip: the soft-clipping tabulation leaves it out (unmapped, XJ-tagged, or on an empty target).
-// kScBad: a record the tabulation keeps whose CIGAR does not fit the read or the target (the load
-// rejects such records only when the pileup keeps them).
-enum : uint8_t { kRev = 1, kSimple = 2, kRedundant = 4, kSkip = 8, kScSkip = 16, kScBad = 32 };
+// kSkip: the pileup of the scoring passes leaves the record out (flag filter, or a target outside
+// the pileup set).  kFiltered: the flag filter alone (UNMAP | SECONDARY | QCFAIL | DUP), which the
+// coverage table applies on every target.  kScSkip: the soft-clipping tabulation leaves it out
+// (unmapped, XJ-tagged, or on an empty target).  kBadCigar: the CIGAR does not fit the read or the
+// target; the load rejects such a record when the scoring pileup keeps it, the other passes report
+// it when they keep it.
+enum : uint8_t { kRev = 1, kSimple = 2, kRedundant = 4, kSkip = 8, kScSkip = 16, kBadCigar = 32, kFiltered = 64 };
 constexpr uint16_t kNoTag = 0xFFFF;
 
 // Query bounds of complex reads (simple reads derive them from clip and span):

@@ -50,6 +50,21 @@ void intervals_sparse(const std::vector<uint32_t>& cols, const std::vector<ColCo
 void fill_positions(const std::vector<ColCov>& cov, const std::vector<ColCall>& call, const SampleLayout& L,
                     bsq_position_arrays* out);
 
+// One region's coverage columns as bsq_covtable.cu produces them: counts [6][n] (unique top/bottom,
+// raw redundant top/bottom, begin top/bottom), redundant weights [2][n], the target's reference
+// characters from position 1 to end, and the pileup's last column.
+struct CoverageRegion {
+  const uint32_t* counts;
+  const double* red;
+  const char* ref;
+  uint32_t start, end, last;
+};
+// coverage_output::table (src/breseq/coverage_output.cpp:190-284) with the rows the pileup driver
+// produces for the region (pileup_base.cpp:130-133, 141-210, 308-355).  False if the file cannot be
+// written.
+bool write_coverage_region(const char* path, const CoverageRegion& R, uint32_t resolution, uint32_t flags,
+                           const double* reference_average);
+
 // Soft-clipping rows in the reference's order (direction -1 then +1, targets in seq_id order,
 // positions ascending; soft_clipping.cpp:500-545) and the genome-wide totals and dispersion fit
 // (:547-623).  rows / outs hold the device's rows: direction -1 in column order, then direction +1.

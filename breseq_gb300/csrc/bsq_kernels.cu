@@ -113,7 +113,8 @@ __device__ __forceinline__ void pack_one(const RawSoA& in, const PackOut& out, u
   // soft-clipping tabulation: every mapped record on a non-empty target except XJ-tagged ones
   // (soft_clipping.cpp:373-393); X1 > 1 is kRedundant
   if ((flag & 0x4) || (in.xj && in.xj[i]) || tlen == 0) fl |= kScSkip;
-  else if (bad_cigar) fl |= kScBad;
+  if (bad_cigar) fl |= kBadCigar;
+  if (flag & 0x704) fl |= kFiltered;
   if (rlen == 0) rlen = 1;
   d.start = in.tpoff[tid] + (uint32_t)pos;
   d.end = d.start + rlen;

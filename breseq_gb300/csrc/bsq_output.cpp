@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/breseq_gb300.h"
+#include "bsq_host.h"
 
 namespace {
 
@@ -272,6 +273,77 @@ void copy_str(char* dst, size_t cap, const std::string& s) {
 }
 
 }  // namespace
+
+namespace bsq {
+namespace host {
+
+bool write_coverage_region(const char* path, const CoverageRegion& R, uint32_t resolution, uint32_t flags,
+                           const double* reference_average) {
+  const bool total_only = flags & BSQ_COV_TOTAL_ONLY;
+  const char* d = (flags & BSQ_COV_CSV) ? "," : "\t";
+  const uint32_t n = R.end - R.start + 1;
+  // --resolution: downsample = floor(size / resolution), at least 1 (coverage_output.cpp:203-209);
+  // handle_position keeps (position + start) % downsample == 0 inside the region (pileup_base.cpp:130-133)
+  uint32_t downsample = 1;
+  if (resolution != 0) downsample = std::max<uint32_t>(1, (uint32_t)std::floor((double)n / (double)resolution));
+  auto handled = [&](uint32_t p) { return p >= R.start && p <= R.end && (p + R.start) % downsample == 0; };
+  std::ofstream out(path);
+  if (!out) return false;
+  out << "position" << d << "ref_base";
+  static const char* kFull[8] = {"unique_top_cov", "unique_bot_cov", "redundant_top_cov", "redundant_bot_cov",
+                                 "raw_redundant_top_cov", "raw_redundant_bot_cov", "unique_top_begin", "unique_bot_begin"};
+  static const char* kTotal[3] = {"unique_cov", "redundant_cov", "total_cov"};
+  const int ncols = total_only ? 3 : 8;
+  for (int c = 0; c < ncols; c++) out << d << (total_only ? kTotal[c] : kFull[c]);
+  out << "\n";
+  double sum_unique = 0, sum_repeat = 0, sum_all = 0;
+  uint32_t rows = 0;
+  // a row for position p (coverage_output.cpp:436-451): zero coverage outside the region's columns
+  auto row = [&](uint32_t p) {
+    uint32_t c[6] = {0, 0, 0, 0, 0, 0};
+    double r0 = 0, r1 = 0;
+    if (p >= R.start && p <= R.end) {
+      const uint32_t i = p - R.start;
+      for (int q = 0; q < 6; q++) c[q] = R.counts[(size_t)q * n + i];
+      r0 = R.red[i];
+      r1 = R.red[(size_t)n + i];
+    }
+    rows++;
+    sum_unique += c[0] + c[1];
+    sum_repeat += r0 + r1;
+    sum_all += c[0] + c[1] + r0 + r1;
+    out << p << d << R.ref[p - 1] << d;
+    if (total_only) out << (c[0] + c[1]) << d << fmt_default(r0 + r1) << d << fmt_default(c[0] + c[1] + r0 + r1);
+    else out << c[0] << d << c[1] << d << fmt_default(r0) << d << fmt_default(r1) << d << c[2] << d << c[3] << d << c[4] << d << c[5];
+    out << "\n";
+  };
+  // Up to the pileup's last column the driver moves its cursor through every position and the
+  // handled ones get a row.  Past it only handled positions move the cursor, and each of them first
+  // prints the positions skipped since the cursor as zero rows (coverage_output.cpp:318-327,
+  // pileup_base.cpp:345-351).
+  for (uint32_t p = R.start; p <= std::min(R.last, R.end); p++) if (handled(p)) row(p);
+  uint32_t cursor = R.last;
+  for (uint32_t q = std::max(R.last + 1, R.start); q <= R.end; q++) {
+    if (!handled(q)) continue;
+    for (uint32_t i = cursor + 1; i < q; i++) {
+      out << i << d << R.ref[i - 1];
+      for (int c = 0; c < ncols; c++) out << d << 0;
+      out << "\n";
+      rows++;
+    }
+    row(q);
+    cursor = q;
+  }
+  if (reference_average) out << "#" << d << "reference_unique_average_cov" << d << fmt_default(*reference_average) << "\n";
+  out << "#" << d << "region_unique_average_cov" << d << fmt_default(sum_unique / rows) << "\n";
+  out << "#" << d << "region_repeat_average_cov" << d << fmt_default(sum_repeat / rows) << "\n";
+  out << "#" << d << "region_average_cov" << d << fmt_default(sum_all / rows) << "\n";
+  out << "#" << d << "number_of_positions" << d << rows << "\n";
+  return (bool)out;
+}
+
+}  // namespace host
+}  // namespace bsq
 
 extern "C" {
 

@@ -34,7 +34,7 @@ struct ScRead {
 __device__ __forceinline__ uint32_t sc_classify(const ScArgs& A, const DevRead& rd, uint32_t r, uint32_t margin,
                                                 ScRead& e) {
   if (rd.flags & (kScSkip | kRedundant)) return 0;   // unmapped, X1 > 1, XJ, empty target (:373-393)
-  if (rd.flags & kScBad) return 8;
+  if (rd.flags & kBadCigar) return 8;
   // the record lies inside one target: start .. end - 1 are its columns
   uint32_t lo = 0, hi = A.n_targets;
   while (hi - lo > 1) { const uint32_t mid = (lo + hi) >> 1; if (__ldg(A.tpoff + mid) <= rd.start) lo = mid; else hi = mid; }

@@ -373,6 +373,38 @@ int bsq_sc_result_copy(const bsq_ctx* ctx, bsq_sc_position* rows, uint64_t capac
 int bsq_write_soft_clipping_counts(const char* path, const char* const* target_names, const bsq_sc_params* p,
                                    const bsq_sc_summary* s, const bsq_sc_position* rows, uint64_t n);
 
+/* ---------------------------------------------------------------- BAM2COV coverage table */
+
+/* Per-position coverage of one region as `breseq BAM2COV --format TSV` tabulates it
+ * (coverage_output::pileup_callback, src/breseq/coverage_output.cpp:307-470; command at
+ * src/breseq/breseq_cmdline.cpp:294): over the records htslib's pileup keeps (flag filter only, on
+ * every target), deletion entries skipped, N bases counted.  Each array holds end_1 - start_1 + 1
+ * entries, position start_1 first; any may be NULL. */
+typedef struct bsq_cov_columns {
+    uint32_t* unique_top;                /* X1 = 1 records, forward strand              */
+    uint32_t* unique_bot;
+    double*   redundant_top;             /* sum of 1/X1 over X1 > 1 records, in BAM order */
+    double*   redundant_bot;
+    uint32_t* raw_redundant_top;
+    uint32_t* raw_redundant_bot;
+    uint32_t* unique_top_begin;          /* unique records whose first sequenced base is here */
+    uint32_t* unique_bot_begin;
+} bsq_cov_columns;
+/* last_column_1 (may be NULL) gets the last reference position any kept record overlapping the
+ * region reaches (the pileup's last column; 0 when there is none). */
+int bsq_coverage_columns(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start_1, uint32_t end_1,
+                         bsq_cov_columns* out, uint32_t* last_column_1);
+
+#define BSQ_COV_TOTAL_ONLY  1   /* --total-only: unique_cov, redundant_cov, total_cov */
+#define BSQ_COV_CSV         2   /* --format CSV (comma-separated) instead of TSV       */
+/* coverage_output::table (coverage_output.cpp:190-284) for the region seq_id:start_1-end_1 with
+ * --resolution (0 = every position), including the pileup driver's row selection
+ * (pileup_base.cpp:130-133, 141-210, 308-355).  reference_average (may be NULL) adds the
+ * reference_unique_average_cov line of --show-average. */
+int bsq_write_coverage_region(bsq_ctx* ctx, int32_t sample_id, const char* path, const char* seq_id, uint32_t tid,
+                              uint32_t start_1, uint32_t end_1, uint32_t resolution, uint32_t flags,
+                              const double* reference_average);
+
 /* Launch shape of the passes.  None of the knobs changes a result: every count is an integer sum
  * and every column and candidate is scored by one warp whatever the grid. */
 typedef struct bsq_tuning {

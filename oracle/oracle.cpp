@@ -49,6 +49,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <sstream>
 #include <string>
 #include <thread>
 #include <vector>
@@ -1256,3 +1257,153 @@ extern "C" void oracle_sc_rows(const oracle_sc_result* r, bsq_sc_position* out) 
   }
 }
 extern "C" void oracle_sc_free(oracle_sc_result* r) { delete r; }
+
+// ============================================================================ BAM2COV coverage table
+// coverage_output::pileup_callback (src/breseq/coverage_output.cpp:307-470) over htslib's pileup of one
+// region, as pileup_base::do_pileup drives it (src/breseq/pileup_base.cpp:130-133, 141-210, 308-355),
+// and coverage_output::table (coverage_output.cpp:190-284).
+namespace {
+
+struct CovCol { uint32_t u[2] = {0, 0}, raw[2] = {0, 0}, beg[2] = {0, 0}; double red[2] = {0.0, 0.0}; };
+
+int cov_columns(Data& d, uint32_t t, uint32_t start, uint32_t end, std::vector<CovCol>& cols, uint32_t& last) {
+  const bsq_read_soa* rd = d.rd;
+  cols.assign(end - start + 1, CovCol());
+  // the pileup column entries in BAM order: deletions skipped, redundancy from X1
+  walk_columns(d, t, (int64_t)start - 1, (int64_t)end, [&](int64_t c, const std::vector<uint64_t>& active) {
+    CovCol& x = cols[c - ((int64_t)start - 1)];
+    for (uint64_t r : active) {
+      Pile e;
+      if (!resolve(rd, r, c, e) || e.is_del) continue;
+      const int rev = d.info[r].rev ? 1 : 0;
+      const uint32_t redundancy = rd->x1[r];
+      // first sequenced base: query position 1 on the top strand, read_length on the bottom
+      const bool first = rev ? (e.qpos + 1 == (int32_t)d.info[r].len) : (e.qpos == 0);
+      if (redundancy == 1) {
+        x.u[rev]++;
+        if (first) x.beg[rev]++;
+      } else {
+        x.raw[rev]++;
+        x.red[rev] += 1.0 / redundancy;
+      }
+    }
+  });
+  // the pileup's last column: the furthest end of a kept record the region query returns
+  last = 0;
+  for (uint64_t r = d.tgt_begin[t]; r < d.tgt_end[t]; r++) {
+    if (d.info[r].skip) continue;
+    if (d.info[r].pos < (int64_t)end && d.info[r].endpos > (int64_t)start - 1)
+      last = std::max<uint32_t>(last, (uint32_t)d.info[r].endpos);
+  }
+  return BSQ_OK;
+}
+
+std::string fmt_double(double v) {   // default ostream formatting, as the reference writes
+  std::ostringstream o;
+  o << v;
+  return o.str();
+}
+
+}  // namespace
+
+extern "C" int oracle_coverage_columns(const bsq_reference* ref, const bsq_read_soa* rd, uint32_t tid, uint32_t start,
+                                       uint32_t end, bsq_cov_columns* out, uint32_t* last_out, char* errbuf, int errcap) {
+  Data d; d.ref = ref; d.rd = rd;
+  int rc = prepare(d);
+  if (rc) { if (errbuf) snprintf(errbuf, errcap, "%s", d.err.c_str()); return rc; }
+  std::vector<CovCol> cols;
+  uint32_t last = 0;
+  cov_columns(d, tid, start, end, cols, last);
+  for (size_t i = 0; i < cols.size(); i++) {
+    if (out->unique_top) out->unique_top[i] = cols[i].u[0];
+    if (out->unique_bot) out->unique_bot[i] = cols[i].u[1];
+    if (out->redundant_top) out->redundant_top[i] = cols[i].red[0];
+    if (out->redundant_bot) out->redundant_bot[i] = cols[i].red[1];
+    if (out->raw_redundant_top) out->raw_redundant_top[i] = cols[i].raw[0];
+    if (out->raw_redundant_bot) out->raw_redundant_bot[i] = cols[i].raw[1];
+    if (out->unique_top_begin) out->unique_top_begin[i] = cols[i].beg[0];
+    if (out->unique_bot_begin) out->unique_bot_begin[i] = cols[i].beg[1];
+  }
+  if (last_out) *last_out = last;
+  return BSQ_OK;
+}
+
+extern "C" int oracle_write_coverage_region(const bsq_reference* ref, const bsq_read_soa* rd, const char* path,
+                                            const char* seq_id, uint32_t tid, uint32_t start, uint32_t end,
+                                            uint32_t resolution, uint32_t flags, const double* ref_average,
+                                            char* errbuf, int errcap) {
+  Data d; d.ref = ref; d.rd = rd;
+  int rc = prepare(d);
+  if (rc) { if (errbuf) snprintf(errbuf, errcap, "%s", d.err.c_str()); return rc; }
+  (void)seq_id;
+  std::vector<CovCol> cols;
+  uint32_t last = 0;
+  cov_columns(d, tid, start, end, cols, last);
+  const char* refseq = ref->seq + ref->target_offset[tid];
+  const bool total_only = flags & BSQ_COV_TOTAL_ONLY;
+  const std::string dl = (flags & BSQ_COV_CSV) ? "," : "\t";
+  // resolution -> downsampling (coverage_output.cpp:203-209) and the position filter of
+  // pileup_base::handle_position (pileup_base.cpp:130-133)
+  const uint32_t size = end - start + 1;
+  uint32_t downsample = 1;
+  if (resolution != 0) {
+    downsample = (uint32_t)std::floor((double)size / (double)resolution);
+    if (downsample < 1) downsample = 1;
+  }
+  auto handled = [&](uint32_t p) { return p >= start && p <= end && (p + start) % downsample == 0; };
+  std::ostringstream o;
+  o << "position" << dl << "ref_base";
+  const char* names8[8] = {"unique_top_cov", "unique_bot_cov", "redundant_top_cov", "redundant_bot_cov",
+                           "raw_redundant_top_cov", "raw_redundant_bot_cov", "unique_top_begin", "unique_bot_begin"};
+  const char* names3[3] = {"unique_cov", "redundant_cov", "total_cov"};
+  for (int c = 0; c < (total_only ? 3 : 8); c++) o << dl << (total_only ? names3[c] : names8[c]);
+  o << "\n";
+  double sum_u = 0, sum_r = 0, sum_all = 0;
+  uint32_t n_pos = 0;
+  auto zero_row = [&](uint32_t i) {
+    o << i << dl << refseq[i - 1];
+    for (int c = 0; c < (total_only ? 3 : 8); c++) o << dl << 0;
+    o << "\n";
+    n_pos++;
+  };
+  auto row = [&](uint32_t p) {
+    CovCol x;
+    if (p >= start && p <= end) x = cols[p - start];
+    n_pos++;
+    sum_u += x.u[0] + x.u[1];
+    sum_r += x.red[0] + x.red[1];
+    sum_all += x.u[0] + x.u[1] + x.red[0] + x.red[1];
+    o << p << dl << refseq[p - 1] << dl;
+    if (total_only) {
+      o << (x.u[0] + x.u[1]) << dl << fmt_double(x.red[0] + x.red[1]) << dl
+        << fmt_double(x.u[0] + x.u[1] + x.red[0] + x.red[1]);
+    } else {
+      o << x.u[0] << dl << x.u[1] << dl << fmt_double(x.red[0]) << dl << fmt_double(x.red[1]) << dl << x.raw[0] << dl
+        << x.raw[1] << dl << x.beg[0] << dl << x.beg[1];
+    }
+    o << "\n";
+  };
+  // the pileup's columns and the gaps between them: every position up to the last column is
+  // visited, the handled ones print
+  for (uint32_t p = 1; p <= last; p++) if (handled(p)) row(p);
+  // past the last column only handled positions move the cursor, so each one first prints the
+  // positions skipped since the previous one (coverage_output.cpp:318-327, pileup_base.cpp:345-351)
+  uint32_t cursor = last;
+  for (uint32_t q = last + 1; q <= end; q++) {
+    if (!handled(q)) continue;
+    for (uint32_t i = cursor + 1; i < q; i++) zero_row(i);
+    row(q);
+    cursor = q;
+  }
+  if (ref_average) o << "#" << dl << "reference_unique_average_cov" << dl << fmt_double(*ref_average) << "\n";
+  o << "#" << dl << "region_unique_average_cov" << dl << fmt_double(sum_u / n_pos) << "\n";
+  o << "#" << dl << "region_repeat_average_cov" << dl << fmt_double(sum_r / n_pos) << "\n";
+  o << "#" << dl << "region_average_cov" << dl << fmt_double(sum_all / n_pos) << "\n";
+  o << "#" << dl << "number_of_positions" << dl << n_pos << "\n";
+  FILE* f = fopen(path, "w");
+  if (!f) { if (errbuf) snprintf(errbuf, errcap, "cannot write %s", path); return BSQ_ERR_INVALID; }
+  const std::string txt = o.str();
+  fwrite(txt.data(), 1, txt.size(), f);
+  fclose(f);
+  return BSQ_OK;
+}

@@ -38,6 +38,12 @@ def lib():
         L.oracle_sc_summary.argtypes = [C.c_void_p, C.POINTER(abi.ScSummary)]
         L.oracle_sc_rows.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_sc_free.argtypes = [C.c_void_p]
+        L.oracle_coverage_columns.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.c_uint32, C.c_uint32,
+                                              C.c_uint32, C.POINTER(abi.CovColumns), C.POINTER(C.c_uint32), C.c_char_p,
+                                              C.c_int]
+        L.oracle_write_coverage_region.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.c_char_p,
+                                                   C.c_char_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                                   C.c_uint32, C.POINTER(C.c_double), C.c_char_p, C.c_int]
         _lib = L
     return _lib
 
@@ -167,3 +173,30 @@ def soft_clipping(sample, minimum_clipped_bases=12, consensus_base_fraction=0.95
         return dict(summary=abi.sc_summary_dict(s), rows=abi.sc_rows_array(rows, s.n_positions))
     finally:
         lib().oracle_sc_free(h)
+
+
+def coverage_columns(sample, tid, start, end):
+    """coverage_output::pileup_callback restated on the CPU for positions start..end of target tid."""
+    view = abi.SampleView(sample)
+    arrs, st = abi.cov_columns(end - start + 1)
+    last = C.c_uint32()
+    err = C.create_string_buffer(256)
+    rc = lib().oracle_coverage_columns(C.byref(view.ref), C.byref(view.reads), tid, start, end, C.byref(st),
+                                       C.byref(last), err, 256)
+    if rc != 0:
+        raise OracleError(f"oracle_coverage_columns failed ({rc}): {err.value.decode()}")
+    arrs["last"] = last.value
+    return arrs
+
+
+def write_coverage_region(sample, path, tid, start, end, resolution=600, total_only=False, csv=False,
+                          reference_average=None):
+    view = abi.SampleView(sample)
+    flags = (1 if total_only else 0) | (2 if csv else 0)
+    avg = C.byref(C.c_double(reference_average)) if reference_average is not None else None
+    err = C.create_string_buffer(256)
+    rc = lib().oracle_write_coverage_region(C.byref(view.ref), C.byref(view.reads), path.encode(),
+                                            sample.target_names[tid].encode(), tid, start, end, resolution, flags,
+                                            avg, err, 256)
+    if rc != 0:
+        raise OracleError(f"oracle_write_coverage_region failed ({rc}): {err.value.decode()}")

@@ -1,0 +1,55 @@
+"""BAM2COV coverage table (coverage_output.cpp:190-470) restated on the CPU, pinned by hand-worked
+values on hand-made records and by the rows the reference's pileup driver produces."""
+import numpy as np
+
+from oracle import pyoracle as po
+from tests import samples
+
+
+def test_columns_known_answers():
+    s, _ = samples.softclip_known()
+    c = po.coverage_columns(s, 0, 1, 60)
+    assert c["last"] == 60
+    # position 21: R1 R2 R3 R4, the XJ-tagged R7 (the pileup ignores XJ), R9 R10 C1; R8 is secondary
+    # and R5 unmapped (filtered), R6 has X1 = 2 (redundant weight 1/2)
+    assert c["unique_top"][20] == 8 and c["raw_redundant_top"][20] == 1 and c["redundant_top"][20] == 0.5
+    # C1 (10M2I5M3D10M5S at 13) has deleted bases at 28-30: deletion entries are not counted
+    assert list(c["unique_top"][26:31]) == [8, 7, 7, 7, 8]
+    # first sequenced bases aligned: R9 and R10 at 11, C1 at 13, R12 at 51; R11 starts with a clip
+    assert np.nonzero(c["unique_top_begin"])[0].tolist() == [10, 12, 50]
+    assert c["unique_top_begin"][10] == 2
+    assert not c["unique_bot"].any() and not c["unique_bot_begin"].any()
+
+
+def _rows(path):
+    return [l.split("\t") for l in open(path).read().splitlines() if not l.startswith(("#", "position"))]
+
+
+def test_driver_rows_with_downsampling(tmp_path):
+    s, _ = samples.softclip_known()
+    p = str(tmp_path / "a.tsv")
+    # 60 positions at resolution 7: downsample floor(60/7) = 8, rows where (position + 1) % 8 == 0;
+    # the pileup's last column is 60, so there is no tail
+    po.write_coverage_region(s, p, 0, 1, 60, resolution=7)
+    assert [int(r[0]) for r in _rows(p)] == [7, 15, 23, 31, 39, 47, 55]
+    # s0 (40 bp) has one record, on 11-30; downsample 10 keeps 9, 19, 29, 39.  Past the last column
+    # (30) only handled positions move the cursor, so position 39 first prints 31-38 as zero rows
+    po.write_coverage_region(s, p, 1, 1, 40, resolution=4)
+    rows = _rows(p)
+    assert [int(r[0]) for r in rows] == [9, 19, 29] + list(range(31, 40))
+    assert rows[0][2] == "0" and rows[1][2] == "1" and all(r[2] == "0" for r in rows[3:])
+    assert open(p).read().splitlines()[-1] == "#\tnumber_of_positions\t12"
+    # no record overlaps 35-40: the cursor stays at 0 and position 35 prints 1-34 first
+    po.write_coverage_region(s, p, 1, 35, 40, resolution=0)
+    assert [int(r[0]) for r in _rows(p)] == list(range(1, 41))
+
+
+def test_total_only_csv_and_average(tmp_path):
+    s, _ = samples.softclip_known()
+    p = str(tmp_path / "b.csv")
+    po.write_coverage_region(s, p, 0, 20, 22, resolution=0, total_only=True, csv=True, reference_average=7.25)
+    lines = open(p).read().splitlines()
+    assert lines[0] == "position,ref_base,unique_cov,redundant_cov,total_cov"
+    assert lines[2].split(",")[2:] == ["8", "0.5", "8.5"]
+    assert lines[4] == "#,reference_unique_average_cov,7.25"
+    assert lines[-1] == "#,number_of_positions,3"
