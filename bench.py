@@ -18,6 +18,9 @@ polymorphism modes), drawn from a pool of distinct seeded samples:
   "served":  open-loop Poisson arrivals at 0.5/1/2x the batched capacity into the scoring server
              (HBM-footprint admission, continuous batching), with p50/p99 job latency.
 
+A "coverage_table" leg times the BAM2COV coverage columns of the workload's chromosome (every position)
+and the table at BAM2COV's default resolution, against the oracle on a 200 kb region.
+
 A "soft_clipping" leg times the soft-clipping tabulation (tabulate_soft_clipping_counts) on a sample
 of the same shape with 50 junction breakpoints and 1% of reads clipped by 12-40 random bases, against
 the oracle's CPU tabulation of the same sample.
@@ -138,9 +141,62 @@ def _workload(seed: int, scale: float = 1.0):
 
 
 SC_WORKLOAD = "ecoli_4.79Mb_pe150_2x100x_50breakpoints_1pct_long_clips"
-# count pass of the tabulation: one 32-byte record per read and one 4-byte difference-array entry per
-# column (DRAM bytes per launch measured in profiles/sc_reads_kernel_ecoli_breakpoints.md)
-SC_READS_DRAM_PER_READ = None
+# DRAM bytes (read + write) of one launch of the tabulation's count pass per record, from the ncu
+# capture of the same workload (profiles/sc_kernels_ecoli_breakpoints_4.79Mb.md)
+SC_READS_DRAM_PER_READ = (230.080768e6 + 14.4256e6) / 6416810
+# DRAM bytes of the four main coverage-table kernels over their algorithmic bytes, from the ncu capture
+# of the same chromosome (profiles/coverage_table_kernels_ecoli_chromosome_4.63Mb.md)
+COV_TABLE_DRAM_OVER_ALGORITHMIC = 580.482284e6 / (32 * 6206454 + 80 * 4630000)
+
+
+COV_COLUMNS = ("unique_top", "unique_bot", "redundant_top", "redundant_bot", "raw_redundant_top",
+               "raw_redundant_bot", "unique_top_begin", "unique_bot_begin")
+
+
+def run_coverage(args, sc, sid, s):
+    """BAM2COV coverage columns of target 0 (all positions) on the resident sample: device time of
+    the kernels, the call, the written table at resolution 600, and the oracle on a bounded region."""
+    from oracle import pyoracle as po
+    L = int(s.target_offset[1] - s.target_offset[0])
+    reads = int(np.count_nonzero(s.tid == 0))
+    for _ in range(args.warmup):
+        sc.coverage_columns(sid, 0, 1, L)
+    dev, main, wall = [], [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        c = sc.coverage_columns(sid, 0, 1, L)
+        wall.append(1e3 * (time.perf_counter() - t0))
+        st = sc.last_pass_stats()
+        dev.append(st["device_ms"]); main.append(st["main_kernel_ms"])
+    with tempfile.TemporaryDirectory() as d:
+        table = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            sc.write_coverage_region(sid, os.path.join(d, "c.tsv"), 0, 1, L, resolution=600)
+            if i >= args.warmup:
+                table.append(1e3 * (time.perf_counter() - t0))
+        table_ms = statistics.mean(table)
+    n_cpu = min(L, 200_000)
+    t0 = time.perf_counter()
+    o = po.coverage_columns(s, 0, 1, n_cpu)
+    cpu_s = time.perf_counter() - t0
+    same = all(np.array_equal(c[k][:n_cpu], o[k]) for k in COV_COLUMNS)
+    ms, kms = statistics.mean(dev), statistics.mean(main)
+    hbm, peak_kind = _peaks()
+    # 32 B per record; per position the difference arrays read twice (32 B), the counts written and
+    # re-read (32 B) and the two weights written (16 B)
+    kbytes = 32 * reads + 80 * L
+    return {"workload": f"{WORKLOAD}: chromosome, {L} positions", "positions": L, "records": reads,
+            "device_ms": ms, "kernels_ms": kms, "wall_ms": statistics.mean(wall), "kernel_launches": st["kernel_launches"],
+            "value": L / (ms / 1e3), "unit": "positions/s",
+            "table_ms_resolution_600": table_ms,
+            "roofline": {"bound": "hbm", "kernel": "coverage-table kernels (all six)", "achieved": kbytes / (kms / 1e3) / 1e9,
+                         "peak": hbm, "unit": "GB/s", "frac": kbytes / (kms / 1e3) / 1e9 / hbm,
+                         "algorithmic_bytes": kbytes, "peak_kind": peak_kind,
+                         "traffic": COV_TABLE_DRAM_OVER_ALGORITHMIC * kbytes, "traffic_unit": "bytes per call"},
+            "identical_to_oracle": bool(same),
+            "cpu_baseline": {"value": n_cpu / cpu_s, "unit": "positions/s", "cores": 1, "kind": "port",
+                             "sample": f"positions 1-{n_cpu} of the same chromosome ({cpu_s:.2f} s)"}}
 
 
 def run_softclip(args, device):
@@ -194,7 +250,7 @@ def run_softclip(args, device):
            "value": s.n_reads / (ms / 1e3), "unit": "records/s",
            "e2e": {"ms": statistics.mean(e2e), "value": s.n_reads / (statistics.mean(e2e) / 1e3), "unit": "records/s",
                    "h2d_bytes": int(sum(a.nbytes for a in view._keep))},
-           "roofline": {"bound": "hbm", "kernel": "sc_reads_kernel", "achieved": kbytes / (kms / 1e3) / 1e9,
+           "roofline": {"bound": "hbm", "kernel": "sc_count_kernel", "achieved": kbytes / (kms / 1e3) / 1e9,
                         "peak": hbm, "unit": "GB/s", "frac": kbytes / (kms / 1e3) / 1e9 / hbm, "kernel_ms": kms,
                         "algorithmic_bytes": kbytes, "peak_kind": peak_kind,
                         "traffic": SC_READS_DRAM_PER_READ * s.n_reads if SC_READS_DRAM_PER_READ else None},
@@ -406,6 +462,8 @@ def run_ours(args, world, rank, local, pg):
         "tuning": tuning,
         "ra_items": len(im["ra"]),
     }
+    if rank == 0 and not args.no_coverage:
+        line["coverage_table"] = run_coverage(args, sc, sid, s)
     if rank == 0 and not args.no_cpu:
         rate, cb, dt, ln, reps = _cpu_reference(args.cpu_scale, os.cpu_count() or 1, args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
@@ -561,6 +619,7 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--no-softclip", action="store_true", help="skip the soft-clipping leg")
+    ap.add_argument("--no-coverage", action="store_true", help="skip the coverage-table leg")
     args = ap.parse_args()
     world, rank, local, pg = _dist()
     if args.impl == "reference":

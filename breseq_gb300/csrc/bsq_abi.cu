@@ -117,7 +117,7 @@ struct bsq_ctx {
   // soft-clipping tabulation: working buffers and the rows of the last call
   DevMem sc_diff, sc_cnt, sc_blk, sc_tot, sc_rows, sc_outs, sc_tails, sc_ev, sc_ev_n;
   // coverage table of a region
-  DevMem ct_diff, ct_blk, ct_counts, ct_red, ct_stat, ct_ref;
+  DevMem ct_diff, ct_blk, ct_counts, ct_red, ct_stat, ct_gather;
   std::vector<bsq_sc_position> sc_res;
   double last_ms = 0, main_ms = 0;
   uint32_t launches = 0;
@@ -311,7 +311,7 @@ void bsq_destroy(bsq_ctx* ctx) {
                     &ctx->d_chunks, &ctx->ec_arena, &ctx->im_arena, &ctx->ctl, &ctx->sc_diff, &ctx->sc_cnt,
                     &ctx->sc_blk, &ctx->sc_tot, &ctx->sc_rows, &ctx->sc_outs, &ctx->sc_tails, &ctx->sc_ev,
                     &ctx->sc_ev_n, &ctx->ct_diff, &ctx->ct_blk, &ctx->ct_counts, &ctx->ct_red, &ctx->ct_stat,
-                    &ctx->ct_ref})
+                    &ctx->ct_gather})
     m->release();
   if (ctx->exec_ec) cudaGraphExecDestroy(ctx->exec_ec);
   if (ctx->exec_im) cudaGraphExecDestroy(ctx->exec_im);
@@ -1058,16 +1058,11 @@ int bsq_soft_clipping(bsq_ctx* ctx, int32_t sample_id, const bsq_sc_params* p, b
 }
 
 // Coverage columns of one region (coverage_output::pileup_callback, coverage_output.cpp:307-470):
-// bsq_covtable.cu on the device; the counts, weights and reference characters come back in one
-// pinned buffer.  Layout of the host copy: [6][n] u32 counts | [2][n] f64 weights | stat | the
-// target's reference characters up to end_1.
-struct CovRegion {
-  const uint32_t* counts;
-  const double* red;
-  const char* ref;
-  uint32_t n, last;
-};
-static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start, uint32_t end, CovRegion& out) {
+// bsq_covtable.cu on the device.  The columns at positions start + k * step (k < m; step 1 = every
+// position) come back in one pinned buffer with the reference characters: [6][m] u32 counts |
+// [2][m] f64 weights | stat | the target's reference characters up to end_1.
+static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start, uint32_t end,
+                           uint32_t first, uint32_t step, host::CoverageRegion& out) {
   SampleDev* s = find_sample(ctx, sample_id);
   if (!s) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
   if (tid >= s->n_targets) return fail(ctx, BSQ_ERR_INVALID, "target index out of range");
@@ -1094,6 +1089,8 @@ static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32
   CK(ctx->ct_counts.alloc((uint64_t)n * 24, st));
   CK(ctx->ct_red.alloc((uint64_t)n * 16, st));
   CK(ctx->ct_stat.alloc(64, st));
+  const uint32_t m = first <= end ? (end - first) / step + 1 : 0;
+  if (step > 1) CK(ctx->ct_gather.alloc((uint64_t)m * 40 + 16, st));
   A.diff = ctx->ct_diff.as<int32_t>();
   A.blk = ctx->ct_blk.as<long long>();
   A.counts = ctx->ct_counts.as<uint32_t>();
@@ -1105,19 +1102,30 @@ static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32
   CK(cudaMemsetAsync(A.stat, 0, 64, st));
   CK(record(ctx->evm0, st));
   CK(ct_launch(A, ctx->sms, st));
+  const uint32_t* counts_src = A.counts;
+  const double* red_src = A.red;
+  if (step > 1) {
+    uint32_t* gc = ctx->ct_gather.as<uint32_t>();
+    double* gr = reinterpret_cast<double*>(ctx->ct_gather.as<unsigned char>() + (size_t)m * 24);
+    CK(ct_launch_gather(A, first - start, step, m, gc, gr, ctx->sms, st));
+    counts_src = gc;
+    red_src = gr;
+  }
   CK(record(ctx->evm1, st));
-  const size_t cbytes = (size_t)n * 24, rbytes = (size_t)n * 16;
+  const size_t cbytes = (size_t)m * 24, rbytes = (size_t)m * 16;
   CK(ctx->pin_out.reserve(cbytes + rbytes + 64 + end + 16));
   unsigned char* h = ctx->pin_out.at(0);
-  CK(cudaMemcpyAsync(h, A.counts, cbytes, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(h + cbytes, A.red, rbytes, cudaMemcpyDeviceToHost, st));
+  if (m) {
+    CK(cudaMemcpyAsync(h, counts_src, cbytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h + cbytes, red_src, rbytes, cudaMemcpyDeviceToHost, st));
+  }
   CK(cudaMemcpyAsync(h + cbytes + rbytes, A.stat, 64, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(h + cbytes + rbytes + 64, s->ref.as<uint8_t>() + A.t0, end, cudaMemcpyDeviceToHost, st));
   CK(record(ctx->ev1, st));
   CK(cudaStreamSynchronize(st));
   ctx->last_ms = elapsed(ctx->ev0, ctx->ev1);
   ctx->main_ms = elapsed(ctx->evm0, ctx->evm1);
-  ctx->launches = 6;
+  ctx->launches = step > 1 && m ? 7 : 6;
   ctx->last_h2d = 0;
   ctx->last_d2h = cbytes + rbytes + 64 + end;
   const uint32_t* stat = reinterpret_cast<const uint32_t*>(h + cbytes + rbytes);
@@ -1125,23 +1133,27 @@ static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32
   out.counts = reinterpret_cast<const uint32_t*>(h);
   out.red = reinterpret_cast<const double*>(h + cbytes);
   out.ref = reinterpret_cast<const char*>(h + cbytes + rbytes + 64);
-  out.n = n;
+  out.start = start;
+  out.end = end;
   out.last = stat[0];
+  out.first = first;
+  out.step = step;
+  out.m = m;
   return BSQ_OK;
 }
 
 int bsq_coverage_columns(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start_1, uint32_t end_1,
                          bsq_cov_columns* out, uint32_t* last_column_1) {
   if (!ctx || !out) return fail(ctx, BSQ_ERR_INVALID, "null argument");
-  CovRegion R;
-  const int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, R);
+  host::CoverageRegion R;
+  const int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, start_1, 1, R);
   if (rc != BSQ_OK) return rc;
   uint32_t* const u32[6] = {out->unique_top, out->unique_bot, out->raw_redundant_top, out->raw_redundant_bot,
                             out->unique_top_begin, out->unique_bot_begin};
   for (int q = 0; q < 6; q++)
-    if (u32[q]) memcpy(u32[q], R.counts + (size_t)q * R.n, (size_t)R.n * 4);
-  if (out->redundant_top) memcpy(out->redundant_top, R.red, (size_t)R.n * 8);
-  if (out->redundant_bot) memcpy(out->redundant_bot, R.red + R.n, (size_t)R.n * 8);
+    if (u32[q]) memcpy(u32[q], R.counts + (size_t)q * R.m, (size_t)R.m * 4);
+  if (out->redundant_top) memcpy(out->redundant_top, R.red, (size_t)R.m * 8);
+  if (out->redundant_bot) memcpy(out->redundant_bot, R.red + R.m, (size_t)R.m * 8);
   if (last_column_1) *last_column_1 = R.last;
   return BSQ_OK;
 }
@@ -1150,12 +1162,14 @@ int bsq_write_coverage_region(bsq_ctx* ctx, int32_t sample_id, const char* path,
                               uint32_t start_1, uint32_t end_1, uint32_t resolution, uint32_t flags,
                               const double* reference_average) {
   if (!ctx || !path) return fail(ctx, BSQ_ERR_INVALID, "null argument");
-  CovRegion R;
-  const int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, R);
+  if (start_1 < 1 || start_1 > end_1) return fail(ctx, BSQ_ERR_INVALID, "region outside the target");
+  // only the positions the table can show a count for come back: the handled ones
+  const uint32_t ds = host::coverage_downsample(start_1, end_1, resolution);
+  host::CoverageRegion R;
+  const int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, host::coverage_first_handled(start_1, ds), ds, R);
   if (rc != BSQ_OK) return rc;
   (void)seq_id;   // the table has no seq_id column; the name is part of the caller's file name
-  host::CoverageRegion H{R.counts, R.red, R.ref, start_1, end_1, R.last};
-  if (!host::write_coverage_region(path, H, resolution, flags, reference_average))
+  if (!host::write_coverage_region(path, R, resolution, flags, reference_average))
     return fail(ctx, BSQ_ERR_INVALID, std::string("cannot write ") + path);
   return BSQ_OK;
 }

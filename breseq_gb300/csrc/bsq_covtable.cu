@@ -37,14 +37,20 @@ __global__ void ct_range_kernel(const CovTabArgs A) {
 // a record are its aligned bases (M/=/X); deletions and N are entries too but this table skips them.
 __global__ void __launch_bounds__(256) ct_reads_kernel(const CovTabArgs A) {
   const uint32_t end_col = A.c0 + A.n;
+  // block b walks its own contiguous share of the records: neighbouring threads add to
+  // neighbouring columns
   const uint32_t r_lo = A.stat[3], r_hi = A.stat[4];
-  for (uint32_t r = r_lo + blockIdx.x * blockDim.x + threadIdx.x; r < r_hi; r += gridDim.x * blockDim.x) {
+  const uint32_t per = (uint32_t)(((uint64_t)(r_hi - r_lo) + gridDim.x - 1) / gridDim.x);
+  const uint32_t b_lo = (uint32_t)min((uint64_t)r_hi, (uint64_t)r_lo + (uint64_t)blockIdx.x * per);
+  const uint32_t b_hi = (uint32_t)min((uint64_t)r_hi, (uint64_t)b_lo + per);
+  uint32_t last = 0, span = 0;                          // maxima, reduced per warp at the end
+  for (uint32_t r = b_lo + threadIdx.x; r < b_hi; r += blockDim.x) {
     const DevRead rd = A.reads[r];
     if (rd.flags & kFiltered) continue;                 // htslib's default pileup mask
     if (rd.end <= A.c0) continue;                       // ends before the region: not fetched
     if (rd.flags & kBadCigar) { atomicOr(A.stat + 2, kErrCigar); continue; }
-    atomicMax(A.stat, rd.end - A.t0);                   // last column (1-based) of the pileup
-    atomicMax(A.stat + 1, rd.end - rd.start);
+    last = max(last, rd.end - A.t0);                    // last column (1-based) of the pileup
+    span = max(span, rd.end - rd.start);
     const int rev = (rd.flags & kRev) ? 1 : 0;
     const bool unique = __ldg(A.x1 + r) == 1;
     const int k = (unique ? 0 : 2) + rev;
@@ -76,6 +82,12 @@ __global__ void __launch_bounds__(256) ct_reads_kernel(const CovTabArgs A) {
       if (rev && unique && (last_q_op == 0 || last_q_op == 7 || last_q_op == 8)) first_col = last_q_end - 1;
     }
     if (first_col >= A.c0 && first_col < end_col) atomicAdd(A.counts + (uint64_t)(4 + rev) * A.n + (first_col - A.c0), 1u);
+  }
+  last = __reduce_max_sync(kFull, last);
+  span = __reduce_max_sync(kFull, span);
+  if ((threadIdx.x & 31) == 0 && last) {
+    atomicMax(A.stat, last);
+    atomicMax(A.stat + 1, span);
   }
 }
 
@@ -196,30 +208,73 @@ __global__ void __launch_bounds__(256) ct_apply_kernel(const CovTabArgs A) {
   }
 }
 
-// Redundant weights: 1/X1 summed over the covering redundant records in record order, at the
-// columns that have any (coverage_output.cpp:418-426).
+// Redundant weights (coverage_output.cpp:418-426): 1/X1 summed over the covering redundant records
+// in record order.  One warp per 32-column tile with any redundant coverage, lane k on column k: the
+// warp loads the tile's candidate records 32 at a time (one per lane, which also computes the record's
+// weight 1.0 / X1), then walks them in record order by shuffle, each lane adding the weight when the
+// record covers its column with an aligned base.  Each lane's sum is the reference's sequential sum.
 __global__ void __launch_bounds__(256) ct_redundant_kernel(const CovTabArgs A) {
+  const int lane = threadIdx.x & 31;
   const uint32_t maxspan = A.stat[1];
   const uint32_t r_lo = A.stat[3], r_hi = A.stat[4];
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+  const uint32_t n_tiles = (A.n + 31) / 32;
+  // consecutive tiles go to different blocks: tiles with redundant coverage come in runs (repeat
+  // copies), and a run on one block would queue on one SM
+  const uint32_t warp0 = (threadIdx.x >> 5) * gridDim.x + blockIdx.x, n_warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t tile = warp0; tile < n_tiles; tile += n_warps) {
+    const uint32_t i = tile * 32 + lane;
+    const bool in = i < A.n;
+    const uint32_t raw = in ? A.counts[2ull * A.n + i] + A.counts[3ull * A.n + i] : 0;
     double top = 0.0, bot = 0.0;
-    if (A.counts[2ull * A.n + i] + A.counts[3ull * A.n + i] > 0) {
-      const uint32_t col = A.c0 + i;
-      const uint32_t key = col + 1 > maxspan ? col + 1 - maxspan : 0;   // start > col - maxspan
-      for (uint32_t r = first_start_at(A, r_lo, r_hi, key); r < r_hi && __ldg(A.rstart + r) <= col; r++) {
-        const DevRead rd = A.reads[r];
-        if (rd.flags & (kFiltered | kBadCigar)) continue;
-        const uint32_t redundancy = __ldg(A.x1 + r);
-        if (redundancy == 1 || rd.end <= col) continue;
-        if (!(rd.flags & kSimple)) {
-          Pile e;
-          if (!resolve_cigar(A.cigar + rd.cigar_off, rd.n_cigar, rd.start, col, e) || e.del) continue;
+    if (__ballot_sync(kFull, raw > 0)) {
+      const uint32_t col0 = A.c0 + tile * 32, col = col0 + lane;
+      const uint32_t key = col0 + 1 > maxspan ? col0 + 1 - maxspan : 0;   // start > col0 - maxspan
+      const uint32_t lo = first_start_at(A, r_lo, r_hi, key);
+      const uint32_t hi = first_start_at(A, lo, r_hi, col0 + 32);          // start < tile end
+      for (uint32_t base = lo; base < hi; base += 32) {
+        const uint32_t r = base + lane;
+        uint32_t start = 0, end = 0, coff = 0, fl_nc = kFiltered;   // flags | n_cigar << 8
+        double w = 0.0;
+        if (r < hi) {
+          const DevRead rd = A.reads[r];
+          const uint32_t redundancy = __ldg(A.x1 + r);
+          start = rd.start;
+          end = rd.end;
+          coff = rd.cigar_off;
+          fl_nc = rd.flags | ((uint32_t)rd.n_cigar << 8);
+          if (redundancy == 1 || (rd.flags & (kFiltered | kBadCigar))) end = 0;   // never covers
+          else w = 1.0 / redundancy;
         }
-        if (rd.flags & kRev) bot += 1.0 / redundancy; else top += 1.0 / redundancy;
+        const uint32_t cnt = min(32u, hi - base);
+        for (uint32_t j = 0; j < cnt; j++) {
+          const uint32_t s_start = __shfl_sync(kFull, start, j), s_end = __shfl_sync(kFull, end, j);
+          const uint32_t s_fl = __shfl_sync(kFull, fl_nc, j), s_coff = __shfl_sync(kFull, coff, j);
+          const double s_w = __shfl_sync(kFull, w, j);
+          bool covers = in && s_start <= col && s_end > col;
+          if (covers && !(s_fl & kSimple)) {
+            Pile e;
+            covers = resolve_cigar(A.cigar + s_coff, (int)(s_fl >> 8), s_start, col, e) && !e.del;
+          }
+          if (covers) { if (s_fl & kRev) bot += s_w; else top += s_w; }
+        }
       }
     }
-    A.red[i] = top;
-    A.red[(uint64_t)A.n + i] = bot;
+    if (in) {
+      A.red[i] = top;
+      A.red[(uint64_t)A.n + i] = bot;
+    }
+  }
+}
+
+// The handled positions first + k * step of the region, k < m, into the compact arrays.
+__global__ void __launch_bounds__(256) ct_gather_kernel(const CovTabArgs A, uint32_t first, uint32_t step, uint32_t m,
+                                                        uint32_t* counts_out, double* red_out) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    const uint64_t src = (uint64_t)first + (uint64_t)k * step;
+#pragma unroll
+    for (int q = 0; q < 6; q++) counts_out[(uint64_t)q * m + k] = A.counts[(uint64_t)q * A.n + src];
+    red_out[k] = A.red[src];
+    red_out[(uint64_t)m + k] = A.red[(uint64_t)A.n + src];
   }
 }
 
@@ -236,7 +291,13 @@ cudaError_t ct_launch(const CovTabArgs& A, int sms, cudaStream_t st) {
   ct_block_sums_kernel<<<A.n_blocks, 256, 0, st>>>(A);
   ct_block_scan_kernel<<<1, 1024, 0, st>>>(A);
   ct_apply_kernel<<<A.n_blocks, 256, 0, st>>>(A);
-  ct_redundant_kernel<<<grid_for(A.n, 256, sms, 8), 256, 0, st>>>(A);
+  ct_redundant_kernel<<<grid_for(((uint64_t)A.n + 31) / 32 * 32, 256, sms, 8), 256, 0, st>>>(A);
+  return cudaGetLastError();
+}
+
+cudaError_t ct_launch_gather(const CovTabArgs& A, uint32_t first, uint32_t step, uint32_t m, uint32_t* counts_out,
+                             double* red_out, int sms, cudaStream_t st) {
+  if (m) ct_gather_kernel<<<grid_for(m, 256, sms, 8), 256, 0, st>>>(A, first, step, m, counts_out, red_out);
   return cudaGetLastError();
 }
 

@@ -6,8 +6,8 @@
 //      difference array (unique or raw-redundant, per strand) and its first sequenced base, when
 //      aligned, to a begin counter; the pileup's last column and the longest span are maxima;
 //   2. scan: the difference arrays become counts (block sums, one sweep over them, apply);
-//   3. redundant weights: at columns with redundant coverage, one thread sums 1/X1 over the
-//      covering records in record (BAM) order, as the pileup does, so the doubles are exact.
+//   3. redundant weights: at columns with redundant coverage a warp sums 1/X1 over the covering
+//      records in record (BAM) order, as the pileup does, so the doubles are exact.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -39,5 +39,8 @@ struct CovTabArgs {
 
 // Read pass, scan and redundant weights.  counts[4..5], diff and stat must be zeroed first.
 cudaError_t ct_launch(const CovTabArgs& A, int sms, cudaStream_t st);
+// Region offsets first + k * step, k < m, of the counts and weights into [6][m] / [2][m] arrays.
+cudaError_t ct_launch_gather(const CovTabArgs& A, uint32_t first, uint32_t step, uint32_t m, uint32_t* counts_out,
+                             double* red_out, int sms, cudaStream_t st);
 
 }  // namespace bsq

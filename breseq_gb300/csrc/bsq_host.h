@@ -50,15 +50,22 @@ void intervals_sparse(const std::vector<uint32_t>& cols, const std::vector<ColCo
 void fill_positions(const std::vector<ColCov>& cov, const std::vector<ColCall>& call, const SampleLayout& L,
                     bsq_position_arrays* out);
 
-// One region's coverage columns as bsq_covtable.cu produces them: counts [6][n] (unique top/bottom,
-// raw redundant top/bottom, begin top/bottom), redundant weights [2][n], the target's reference
-// characters from position 1 to end, and the pileup's last column.
+// One region's coverage columns as bsq_covtable.cu produces them, at the positions first + k * step,
+// k < m: counts [6][m] (unique top/bottom, raw redundant top/bottom, begin top/bottom), redundant
+// weights [2][m]; the target's reference characters from position 1 to end, and the pileup's last
+// column.
 struct CoverageRegion {
   const uint32_t* counts;
   const double* red;
   const char* ref;
   uint32_t start, end, last;
+  uint32_t first, step, m;
 };
+// The table's downsampling for a region and --resolution (coverage_output.cpp:203-209) and the first
+// position pileup_base::handle_position keeps, (position + start) % downsample == 0
+// (pileup_base.cpp:130-133).
+uint32_t coverage_downsample(uint32_t start, uint32_t end, uint32_t resolution);
+uint32_t coverage_first_handled(uint32_t start, uint32_t downsample);
 // coverage_output::table (src/breseq/coverage_output.cpp:190-284) with the rows the pileup driver
 // produces for the region (pileup_base.cpp:130-133, 141-210, 308-355).  False if the file cannot be
 // written.

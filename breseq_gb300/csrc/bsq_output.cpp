@@ -277,16 +277,22 @@ void copy_str(char* dst, size_t cap, const std::string& s) {
 namespace bsq {
 namespace host {
 
+uint32_t coverage_downsample(uint32_t start, uint32_t end, uint32_t resolution) {
+  if (resolution == 0) return 1;
+  return std::max<uint32_t>(1, (uint32_t)std::floor((double)(end - start + 1) / (double)resolution));
+}
+uint32_t coverage_first_handled(uint32_t start, uint32_t downsample) {
+  return start + (uint32_t)((downsample - ((uint64_t)start * 2) % downsample) % downsample);
+}
+
 bool write_coverage_region(const char* path, const CoverageRegion& R, uint32_t resolution, uint32_t flags,
                            const double* reference_average) {
   const bool total_only = flags & BSQ_COV_TOTAL_ONLY;
   const char* d = (flags & BSQ_COV_CSV) ? "," : "\t";
-  const uint32_t n = R.end - R.start + 1;
-  // --resolution: downsample = floor(size / resolution), at least 1 (coverage_output.cpp:203-209);
-  // handle_position keeps (position + start) % downsample == 0 inside the region (pileup_base.cpp:130-133)
-  uint32_t downsample = 1;
-  if (resolution != 0) downsample = std::max<uint32_t>(1, (uint32_t)std::floor((double)n / (double)resolution));
-  auto handled = [&](uint32_t p) { return p >= R.start && p <= R.end && (p + R.start) % downsample == 0; };
+  const uint32_t downsample = coverage_downsample(R.start, R.end, resolution);
+  const uint32_t first_handled = coverage_first_handled(R.start, downsample);
+  if (downsample % R.step != 0 || R.first > first_handled || (first_handled - R.first) % R.step != 0)
+    return false;   // the columns do not include every handled position
   std::ofstream out(path);
   if (!out) return false;
   out << "position" << d << "ref_base";
@@ -302,11 +308,11 @@ bool write_coverage_region(const char* path, const CoverageRegion& R, uint32_t r
   auto row = [&](uint32_t p) {
     uint32_t c[6] = {0, 0, 0, 0, 0, 0};
     double r0 = 0, r1 = 0;
-    if (p >= R.start && p <= R.end) {
-      const uint32_t i = p - R.start;
-      for (int q = 0; q < 6; q++) c[q] = R.counts[(size_t)q * n + i];
+    if (p >= R.first && p <= R.end && (p - R.first) % R.step == 0) {
+      const uint32_t i = (p - R.first) / R.step;
+      for (int q = 0; q < 6; q++) c[q] = R.counts[(size_t)q * R.m + i];
       r0 = R.red[i];
-      r1 = R.red[(size_t)n + i];
+      r1 = R.red[(size_t)R.m + i];
     }
     rows++;
     sum_unique += c[0] + c[1];
@@ -321,18 +327,19 @@ bool write_coverage_region(const char* path, const CoverageRegion& R, uint32_t r
   // handled ones get a row.  Past it only handled positions move the cursor, and each of them first
   // prints the positions skipped since the cursor as zero rows (coverage_output.cpp:318-327,
   // pileup_base.cpp:345-351).
-  for (uint32_t p = R.start; p <= std::min(R.last, R.end); p++) if (handled(p)) row(p);
+  const uint32_t covered_end = std::min(R.last, R.end);
+  uint64_t q = first_handled;
+  for (; q <= covered_end; q += downsample) row((uint32_t)q);
   uint32_t cursor = R.last;
-  for (uint32_t q = std::max(R.last + 1, R.start); q <= R.end; q++) {
-    if (!handled(q)) continue;
+  for (; q <= R.end; q += downsample) {
     for (uint32_t i = cursor + 1; i < q; i++) {
       out << i << d << R.ref[i - 1];
       for (int c = 0; c < ncols; c++) out << d << 0;
       out << "\n";
       rows++;
     }
-    row(q);
-    cursor = q;
+    row((uint32_t)q);
+    cursor = (uint32_t)q;
   }
   if (reference_average) out << "#" << d << "reference_unique_average_cov" << d << fmt_default(*reference_average) << "\n";
   out << "#" << d << "region_unique_average_cov" << d << fmt_default(sum_unique / rows) << "\n";
