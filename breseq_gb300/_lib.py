@@ -97,6 +97,14 @@ def load():
                                        P(C.c_uint32)]
     L.bsq_write_coverage_region.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, C.c_uint32, C.c_uint32,
                                             C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_double)]
+    L.bsq_bam_open.argtypes = [C.c_void_p, C.c_char_p, C.c_uint64, P(C.c_void_p)]
+    L.bsq_bam_close.argtypes = [C.c_void_p]
+    L.bsq_bam_close.restype = None
+    L.bsq_bam_header.argtypes = [C.c_void_p, P(C.c_char_p), P(C.c_uint64), P(C.c_uint32), P(P(C.c_char_p)),
+                                 P(P(C.c_uint32))]
+    L.bsq_bam_decode.argtypes = [C.c_void_p, C.c_void_p, P(abi.BamGroups), P(C.c_uint64), P(C.c_uint64), P(C.c_uint64)]
+    L.bsq_bam_copy_records.argtypes = [C.c_void_p, C.c_void_p, P(abi.ReadArrays)]
+    L.bsq_bam_load.argtypes = [C.c_void_p, C.c_void_p, P(abi.Reference), P(C.c_int32)]
     _lib = L
     return L
 
@@ -114,4 +122,5 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_default_ra_settings", "bsq_test_ra_evidence", "bsq_write_error_rates", "bsq_write_base_qual_error_prob",
             "bsq_write_coverage_distribution", "bsq_write_coverage_table", "bsq_format_ra", "bsq_write_gd",
             "bsq_default_sc_params", "bsq_soft_clipping", "bsq_sc_result_copy", "bsq_write_soft_clipping_counts",
-            "bsq_coverage_columns", "bsq_write_coverage_region")
+            "bsq_coverage_columns", "bsq_write_coverage_region", "bsq_bam_open", "bsq_bam_close", "bsq_bam_header",
+            "bsq_bam_decode", "bsq_bam_copy_records", "bsq_bam_load")

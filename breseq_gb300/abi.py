@@ -266,6 +266,34 @@ def sc_summary_dict(s: ScSummary) -> dict:
     return {name: getattr(s, name) for name, _ in ScSummary._fields_}
 
 
+class BamGroups(C.Structure):
+    _fields_ = [
+        ("n_groups", C.c_uint32),
+        ("ids", P(C.c_char_p)),
+        ("file_base", P(C.c_uint32)),
+        ("file_count", P(C.c_uint32)),
+    ]
+
+
+READ_ARRAY_FIELDS = (("tid", np.int32), ("pos", np.int32), ("flag", np.uint16), ("mapq", np.uint8), ("x1", np.uint32),
+                     ("xl", np.int32), ("xr", np.int32), ("read_file", np.uint8), ("read_group", np.uint16),
+                     ("l_qseq", np.uint32), ("seq_off", np.uint64), ("cigar_off", np.uint64), ("n_cigar", np.uint16),
+                     ("cigar", np.uint32), ("seq", np.uint8), ("qual", np.uint8), ("xj", np.uint8))
+_CT = {np.int32: C.c_int32, np.uint16: C.c_uint16, np.uint8: C.c_uint8, np.uint32: C.c_uint32, np.uint64: C.c_uint64}
+
+
+class ReadArrays(C.Structure):
+    _fields_ = [(name, P(_CT[dt])) for name, dt in READ_ARRAY_FIELDS]
+
+
+def read_arrays(n: int, n_cigar: int, n_bases: int):
+    """Numpy arrays for decoded records and the bsq_read_arrays struct pointing at them."""
+    size = {"cigar": n_cigar, "seq": n_bases // 2, "qual": n_bases}
+    arrs = {name: np.zeros(max(1, size.get(name, n)), dtype=dt) for name, dt in READ_ARRAY_FIELDS}
+    st = ReadArrays(**{name: ptr(arrs[name], _CT[dt]) for name, dt in READ_ARRAY_FIELDS})
+    return arrs, st
+
+
 class CovColumns(C.Structure):
     _fields_ = [
         ("unique_top", P(C.c_uint32)),

@@ -256,6 +256,20 @@ class Scorer:
         self._check(self.L.bsq_sc_result_copy(self.ctx, rows, s.n_positions))
         return dict(summary=abi.sc_summary_dict(s), rows=abi.sc_rows_array(rows, s.n_positions))
 
+    # ------------------------------------------------------------------ BAM input
+    def open_bam(self, data: bytes) -> "Bam":
+        """Uploads a BAM file's bytes and inflates every BGZF block on the device."""
+        h = C.c_void_p()
+        self._check(self.L.bsq_bam_open(self.ctx, data, len(data), C.byref(h)))
+        return Bam(self, h)
+
+    def load_bam(self, data: bytes, reference_sample, groups=None) -> int:
+        """BAM bytes -> resident sample: inflate, decode and pack on the device.  reference_sample
+        supplies the reference (any object with the bsq_reference arrays, e.g. a synth.Sample)."""
+        with self.open_bam(data) as bam:
+            bam.decode(groups)
+            return bam.load(reference_sample)
+
     # ------------------------------------------------------------------ BAM2COV coverage table
     def coverage_columns(self, sid: int, tid: int, start: int, end: int) -> dict:
         """Per-position coverage of positions start..end (1-based) of target tid as `breseq BAM2COV`
@@ -431,6 +445,63 @@ class Server:
             self.L.bsq_server_destroy(self.srv)
             self.srv = C.c_void_p()
             self._jobs.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Bam:
+    """An uploaded, inflated BAM file (bsq_bam_open); decode() and load() make it a sample."""
+
+    def __init__(self, scorer: Scorer, handle):
+        self.sc, self.h = scorer, handle
+        self.counts = None
+
+    def header(self) -> dict:
+        text, tl, n = C.c_char_p(), C.c_uint64(), C.c_uint32()
+        names, lens = C.POINTER(C.c_char_p)(), C.POINTER(C.c_uint32)()
+        self.sc._check(self.sc.L.bsq_bam_header(self.h, C.byref(text), C.byref(tl), C.byref(n), C.byref(names),
+                                                C.byref(lens)))
+        return dict(text=C.string_at(text, tl.value).decode(), names=[names[i].decode() for i in range(n.value)],
+                    lengths=[lens[i] for i in range(n.value)])
+
+    def decode(self, groups=None):
+        """groups: (ids, file_base, file_count) as breseq resolves read groups, or None."""
+        g, keep = None, []
+        if groups is not None:
+            ids, base, count = groups
+            arr_ids = (C.c_char_p * len(ids))(*[x.encode() for x in ids])
+            b = np.ascontiguousarray(base, dtype=np.uint32)
+            c = np.ascontiguousarray(count, dtype=np.uint32)
+            keep = [arr_ids, b, c]
+            g = abi.BamGroups(n_groups=len(ids), ids=arr_ids, file_base=abi.ptr(b, C.c_uint32),
+                              file_count=abi.ptr(c, C.c_uint32))
+        n, nc, nb = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self.sc._check(self.sc.L.bsq_bam_decode(self.sc.ctx, self.h, C.byref(g) if g is not None else None,
+                                                C.byref(n), C.byref(nc), C.byref(nb)))
+        self.counts = (n.value, nc.value, nb.value)
+        return self.counts
+
+    def records(self) -> dict:
+        """The decoded records as numpy arrays in the bsq_read_soa layout."""
+        arrs, st = abi.read_arrays(*self.counts)
+        self.sc._check(self.sc.L.bsq_bam_copy_records(self.sc.ctx, self.h, C.byref(st)))
+        return arrs
+
+    def load(self, reference_sample) -> int:
+        view = abi.SampleView(reference_sample)
+        sid = C.c_int32()
+        self.sc._check(self.sc.L.bsq_bam_load(self.sc.ctx, self.h, C.byref(view.ref), C.byref(sid)))
+        self.sc._views[sid.value] = (reference_sample, view)
+        return sid.value
+
+    def close(self):
+        if self.h:
+            self.sc.L.bsq_bam_close(self.h)
+            self.h = None
 
     def __enter__(self):
         return self

@@ -23,6 +23,7 @@
 #include "bsq_noalloc.h"
 #include "bsq_softclip.h"
 #include "bsq_covtable.h"
+#include "bsq_bam.h"
 
 using namespace bsq;
 
@@ -336,19 +337,31 @@ uint64_t bsq_sample_footprint(const bsq_reference* ref, const bsq_read_soa* rd) 
          rd->n_bases_total + tiles * 8 + upload_tmp;
 }
 
-int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* rd, int32_t* sample_id) {
-  if (!ctx || !ref || !rd || !sample_id) return fail(ctx, BSQ_ERR_INVALID, "null argument");
-  CK(cudaSetDevice(ctx->device));
+}  // extern "C"
+
+// The record arrays of a sample on the device, in the bsq_read_soa layout, before packing.
+struct RecordsDev {
+  DevMem tid, pos, flag, mapq, x1, xl, xr, rfile, rg, lq, soff, coff, nc, cigar, seq, qual, xj;
+  uint64_t n = 0, n_cigar_total = 0, n_bases_total = 0;
+  bool has_xj = false;
+};
+
+static void take(DevMem& to, DevMem& from) {
+  to.release();
+  to.p = from.p; to.bytes = from.bytes; to.st = from.st;
+  from.p = nullptr; from.bytes = 0;
+}
+
+// A new sample's reference side: target offsets, coverage groups, the pileup set, and the padded
+// reference uploaded on stream st.
+static int new_sample(bsq_ctx* ctx, const bsq_reference* ref, uint64_t n_reads, std::unique_ptr<SampleDev>& out,
+                      cudaStream_t st) {
   const uint32_t T = ref->n_targets;
   if (T == 0 || !ref->target_offset || !ref->seq || !ref->coverage_group || !ref->target_order)
     return fail(ctx, BSQ_ERR_INVALID, "reference without targets");
   const uint64_t total = ref->target_offset[T];
   if (total + T >= 0xFFFFFF00ull) return fail(ctx, BSQ_ERR_INVALID, "reference longer than 2^32 - 256 columns");
-  if (rd->n_reads >= 0xFFFFFFFFull) return fail(ctx, BSQ_ERR_INVALID, "more than 2^32 - 1 records in one sample");
-  if (rd->n_reads && (!rd->tid || !rd->pos || !rd->flag || !rd->mapq || !rd->x1 || !rd->xl || !rd->xr ||
-                      !rd->read_file || !rd->read_group || !rd->l_qseq || !rd->seq_off || !rd->cigar_off ||
-                      !rd->n_cigar || !rd->cigar || !rd->seq || !rd->qual))
-    return fail(ctx, BSQ_ERR_INVALID, "null record array");
+  if (n_reads >= 0xFFFFFFFFull) return fail(ctx, BSQ_ERR_INVALID, "more than 2^32 - 1 records in one sample");
   std::unique_ptr<SampleDev> s(new SampleDev());
   s->n_targets = T;
   s->toff.assign(ref->target_offset, ref->target_offset + T + 1);
@@ -359,7 +372,7 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   }
   s->n_cols = s->tpoff[T];
   s->n_tiles = (s->n_cols + 31) / 32;
-  s->n_reads = (uint32_t)rd->n_reads;
+  s->n_reads = (uint32_t)n_reads;
   s->group.assign(ref->coverage_group, ref->coverage_group + T);
   s->n_groups = ref->n_coverage_groups;
   for (uint32_t t = 0; t < T; t++)
@@ -370,7 +383,6 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
     if (t >= T) return fail(ctx, BSQ_ERR_INVALID, "target_order entry out of range");
     called[t] = 1;
   }
-  cudaStream_t st = ctx->load_streams[ctx->load_rr.fetch_add(1) % bsq_ctx::kLoadStreams];
   // reference, one '\0' separator after each target
   CK(s->ref.alloc(s->n_cols + 64, st));
   CK(cudaMemsetAsync(s->ref.p, 0, s->n_cols + 64, st));
@@ -383,27 +395,22 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   CK(upload(s->tgt_called, called.data(), T, st));
   CK(s->tgt_failed.alloc(T + 16, st));
   CK(cudaMemsetAsync(s->tgt_failed.p, 0, T, st));
-  // records: raw arrays -> packed 32-byte records on the device
-  const uint64_t n = rd->n_reads;
-  DevMem tid, pos, flag, xl, xr, rfile, lq, soff, coff, nc;
-  CK(upload(tid, rd->tid, n, st));
-  CK(upload(pos, rd->pos, n, st));
-  CK(upload(flag, rd->flag, n, st));
-  CK(upload(s->mapq, rd->mapq, n, st));
-  CK(upload(s->x1, rd->x1, n, st));
-  CK(upload(xl, rd->xl, n, st));
-  CK(upload(xr, rd->xr, n, st));
-  CK(upload(rfile, rd->read_file, n, st));
-  CK(upload(s->rg, rd->read_group, n, st));
-  CK(upload(lq, rd->l_qseq, n, st));
-  CK(upload(soff, rd->seq_off, n, st));
-  CK(upload(coff, rd->cigar_off, n, st));
-  CK(upload(nc, rd->n_cigar, n, st));
-  CK(upload(s->cigar, rd->cigar, rd->n_cigar_total, st));
-  CK(upload(s->seq, rd->seq, (rd->n_bases_total + 1) / 2, st));
-  CK(upload(s->qual, rd->qual, rd->n_bases_total, st));
-  DevMem xj;
-  if (rd->xj) CK(upload(xj, rd->xj, n, st));
+  out = std::move(s);
+  return BSQ_OK;
+}
+
+// Packs and validates the records (sorted, CIGAR consumes the reference, offsets inside the arrays),
+// checks the reference characters, builds the MAPQ classes and tile read ranges, and registers the
+// sample.  The arrays the passes keep move into the sample.
+static int pack_sample(bsq_ctx* ctx, std::unique_ptr<SampleDev>& s, RecordsDev& R, cudaStream_t st, int32_t* sample_id) {
+  const uint32_t T = s->n_targets;
+  const uint64_t n = R.n;
+  take(s->mapq, R.mapq);
+  take(s->x1, R.x1);
+  take(s->rg, R.rg);
+  take(s->cigar, R.cigar);
+  take(s->seq, R.seq);
+  take(s->qual, R.qual);
   CK(s->reads.alloc(n * sizeof(DevRead) + 64, st));
   CK(s->qb.alloc(n * sizeof(QBounds) + 64, st));
   CK(s->rstart.alloc(n * 4 + 64, st));
@@ -412,12 +419,12 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   CK(cudaMemsetAsync(dstats.p, 0, 64, st));
   uint32_t* stats = dstats.as<uint32_t>();  // [0] err, [1] maxspan, [2..9] mapq mask, [10] max tile reads
   RawSoA in;
-  in.tid = tid.as<int32_t>(); in.pos = pos.as<int32_t>(); in.flag = flag.as<uint16_t>(); in.mapq = s->mapq.as<uint8_t>();
-  in.x1 = s->x1.as<uint32_t>(); in.xl = xl.as<int32_t>(); in.xr = xr.as<int32_t>(); in.read_file = rfile.as<uint8_t>();
-  in.l_qseq = lq.as<uint32_t>(); in.seq_off = soff.as<uint64_t>(); in.cigar_off = coff.as<uint64_t>();
-  in.n_cigar = nc.as<uint16_t>(); in.cigar = s->cigar.as<uint32_t>(); in.tpoff = s->d_tpoff.as<uint32_t>(); in.called = s->tgt_called.as<uint8_t>();
-  in.xj = rd->xj ? xj.as<uint8_t>() : nullptr;
-  in.n = (uint32_t)n; in.n_targets = T; in.n_bases = rd->n_bases_total; in.n_cigar_total = rd->n_cigar_total;
+  in.tid = R.tid.as<int32_t>(); in.pos = R.pos.as<int32_t>(); in.flag = R.flag.as<uint16_t>(); in.mapq = s->mapq.as<uint8_t>();
+  in.x1 = s->x1.as<uint32_t>(); in.xl = R.xl.as<int32_t>(); in.xr = R.xr.as<int32_t>(); in.read_file = R.rfile.as<uint8_t>();
+  in.l_qseq = R.lq.as<uint32_t>(); in.seq_off = R.soff.as<uint64_t>(); in.cigar_off = R.coff.as<uint64_t>();
+  in.n_cigar = R.nc.as<uint16_t>(); in.cigar = s->cigar.as<uint32_t>(); in.tpoff = s->d_tpoff.as<uint32_t>(); in.called = s->tgt_called.as<uint8_t>();
+  in.xj = R.has_xj ? R.xj.as<uint8_t>() : nullptr;
+  in.n = (uint32_t)n; in.n_targets = T; in.n_bases = R.n_bases_total; in.n_cigar_total = R.n_cigar_total;
   PackOut po;
   po.reads = s->reads.as<DevRead>(); po.qb = s->qb.as<QBounds>(); po.rstart = s->rstart.as<uint32_t>();
   po.mapq = s->mapq.as<uint8_t>(); po.err = stats; po.maxspan = stats + 1; po.mapq_mask = stats + 2;
@@ -451,6 +458,48 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   ctx->samples[id] = std::move(s);
   *sample_id = id;
   return BSQ_OK;
+}
+
+extern "C" {
+
+int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* rd, int32_t* sample_id) {
+  if (!ctx || !ref || !rd || !sample_id) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  if (rd->n_reads && (!rd->tid || !rd->pos || !rd->flag || !rd->mapq || !rd->x1 || !rd->xl || !rd->xr ||
+                      !rd->read_file || !rd->read_group || !rd->l_qseq || !rd->seq_off || !rd->cigar_off ||
+                      !rd->n_cigar || !rd->cigar || !rd->seq || !rd->qual))
+    return fail(ctx, BSQ_ERR_INVALID, "null record array");
+  cudaStream_t st = ctx->load_streams[ctx->load_rr.fetch_add(1) % bsq_ctx::kLoadStreams];
+  std::unique_ptr<SampleDev> s;
+  int rc = new_sample(ctx, ref, rd->n_reads, s, st);
+  if (rc != BSQ_OK) return rc;
+  // records: raw arrays -> packed 32-byte records on the device
+  const uint64_t n = rd->n_reads;
+  RecordsDev R;
+  R.n = n;
+  R.n_cigar_total = rd->n_cigar_total;
+  R.n_bases_total = rd->n_bases_total;
+  CK(upload(R.tid, rd->tid, n, st));
+  CK(upload(R.pos, rd->pos, n, st));
+  CK(upload(R.flag, rd->flag, n, st));
+  CK(upload(R.mapq, rd->mapq, n, st));
+  CK(upload(R.x1, rd->x1, n, st));
+  CK(upload(R.xl, rd->xl, n, st));
+  CK(upload(R.xr, rd->xr, n, st));
+  CK(upload(R.rfile, rd->read_file, n, st));
+  CK(upload(R.rg, rd->read_group, n, st));
+  CK(upload(R.lq, rd->l_qseq, n, st));
+  CK(upload(R.soff, rd->seq_off, n, st));
+  CK(upload(R.coff, rd->cigar_off, n, st));
+  CK(upload(R.nc, rd->n_cigar, n, st));
+  CK(upload(R.cigar, rd->cigar, rd->n_cigar_total, st));
+  CK(upload(R.seq, rd->seq, (rd->n_bases_total + 1) / 2, st));
+  CK(upload(R.qual, rd->qual, rd->n_bases_total, st));
+  if (rd->xj) {
+    CK(upload(R.xj, rd->xj, n, st));
+    R.has_xj = true;
+  }
+  return pack_sample(ctx, s, R, st, sample_id);
 }
 
 int bsq_free_sample(bsq_ctx* ctx, int32_t id) {
@@ -1327,6 +1376,318 @@ int bsq_host_register(void* ptr, uint64_t bytes) {
 int bsq_host_unregister(void* ptr) {
   if (!ptr) return BSQ_ERR_INVALID;
   return cudaHostUnregister(ptr) == cudaSuccess ? BSQ_OK : BSQ_ERR_CUDA;
+}
+
+
+// ============================================================================ BAM input
+// The BGZF block table comes from the block headers on the host (each gives its compressed size, so
+// no inflating is needed to find them; SAM/BAM specification §4.1); the device does the rest.
+}  // extern "C"
+
+struct bsq_bam {
+  bsq_ctx* ctx = nullptr;
+  DevMem file, stream, blocks, scratch;
+  std::vector<BgzfBlock> hblocks;
+  uint64_t stream_len = 0, records_begin = 0;
+  std::string text;
+  std::vector<std::string> names;
+  std::vector<const char*> name_ptrs;
+  std::vector<uint32_t> lengths;
+  std::unique_ptr<RecordsDev> rec;   // the decoded records until they move into a sample
+  bool decoded = false;
+};
+
+static bool parse_bgzf(const uint8_t* d, uint64_t size, std::vector<BgzfBlock>& out, uint64_t& stream_len, std::string& why) {
+  out.clear();
+  uint64_t pos = 0, opos = 0;
+  auto u16 = [&](uint64_t o) { return (uint32_t)d[o] | ((uint32_t)d[o + 1] << 8); };
+  auto u32 = [&](uint64_t o) { return u16(o) | (u16(o + 2) << 16); };
+  while (pos < size) {
+    if (size - pos < 18) { why = "truncated BGZF block header"; return false; }
+    if (d[pos] != 31 || d[pos + 1] != 139 || d[pos + 2] != 8 || !(d[pos + 3] & 4)) { why = "not a BGZF block"; return false; }
+    const uint32_t xlen = u16(pos + 10);
+    if (size - pos < 12ull + xlen) { why = "truncated BGZF extra field"; return false; }
+    uint32_t bsize = 0;
+    bool found = false;
+    for (uint64_t x = pos + 12; x + 4 <= pos + 12 + xlen;) {
+      const uint32_t slen = u16(x + 2);
+      if (d[x] == 66 && d[x + 1] == 67 && slen == 2 && x + 6 <= pos + 12 + xlen) { bsize = u16(x + 4); found = true; }
+      x += 4 + slen;
+    }
+    if (!found) { why = "BGZF block without a BC field"; return false; }
+    const uint64_t total = (uint64_t)bsize + 1;
+    if (total < 12ull + xlen + 8 || total > size - pos) { why = "BGZF block size out of range"; return false; }
+    BgzfBlock b;
+    b.in_off = pos + 12 + xlen;
+    b.in_len = (uint32_t)(total - 12 - xlen - 8);
+    b.crc = u32(pos + total - 8);
+    b.isize = u32(pos + total - 4);
+    b.out_off = opos;
+    b.pad = 0;
+    if (b.isize > 65536) { why = "BGZF block larger than 64 KiB"; return false; }
+    out.push_back(b);
+    opos += b.isize;
+    pos += total;
+  }
+  stream_len = opos;
+  return true;
+}
+
+// The BAM header from the start of the inflated stream: magic, text, reference names and lengths.
+// Returns 0 when complete, 1 when more of the stream is needed, -1 when malformed.
+static int parse_bam_header(const uint8_t* h, uint64_t n, bsq_bam& B) {
+  auto i32 = [&](uint64_t o) { return (int32_t)((uint32_t)h[o] | ((uint32_t)h[o + 1] << 8) | ((uint32_t)h[o + 2] << 16) | ((uint32_t)h[o + 3] << 24)); };
+  if (n < 8) return 1;
+  if (memcmp(h, "BAM\1", 4) != 0) return -1;
+  const int32_t l_text = i32(4);
+  if (l_text < 0) return -1;
+  uint64_t o = 8 + (uint64_t)l_text;
+  if (n < o + 4) return 1;
+  const int32_t n_ref = i32(o);
+  if (n_ref < 0) return -1;
+  o += 4;
+  std::vector<std::string> names;
+  std::vector<uint32_t> lens;
+  for (int32_t r = 0; r < n_ref; r++) {
+    if (n < o + 4) return 1;
+    const int32_t l_name = i32(o);
+    if (l_name < 1) return -1;
+    if (n < o + 4 + (uint64_t)l_name + 4) return 1;
+    names.emplace_back(reinterpret_cast<const char*>(h + o + 4), strnlen(reinterpret_cast<const char*>(h + o + 4), (size_t)l_name));
+    const int32_t l_ref = i32(o + 4 + (uint64_t)l_name);
+    if (l_ref < 0) return -1;
+    lens.push_back((uint32_t)l_ref);
+    o += 4 + (uint64_t)l_name + 4;
+  }
+  B.text.assign(reinterpret_cast<const char*>(h + 8), (size_t)l_text);
+  B.names = std::move(names);
+  B.lengths = std::move(lens);
+  B.name_ptrs.clear();
+  for (auto& x : B.names) B.name_ptrs.push_back(x.c_str());
+  B.records_begin = o;
+  return 0;
+}
+
+static std::string bam_err_text(uint32_t e) {
+  std::string s;
+  if (e & kBamInflate) s += "BGZF block does not inflate; ";
+  if (e & kBamCrc) s += "BGZF block CRC-32 mismatch; ";
+  if (e & kBamSpan) s += "a record spans BGZF blocks or its size is invalid; ";
+  if (e & kBamRecord) s += "record fields out of range; ";
+  if (e & kBamAux) s += "malformed aux field; ";
+  if (e & kBamOrder) s += "unplaced records before placed ones; ";
+  return s;
+}
+
+extern "C" {
+
+int bsq_bam_open(bsq_ctx* ctx, const uint8_t* data, uint64_t size, bsq_bam** out) {
+  if (!ctx || !data || !out) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  std::unique_ptr<bsq_bam> B(new bsq_bam());
+  B->ctx = ctx;
+  std::string why;
+  if (!parse_bgzf(data, size, B->hblocks, B->stream_len, why)) return fail(ctx, BSQ_ERR_INVALID, why);
+  cudaStream_t st = ctx->stream;
+  const uint32_t nb = (uint32_t)B->hblocks.size();
+  CK(B->file.alloc(size + 16, st));
+  CK(cudaMemcpyAsync(B->file.p, data, size, cudaMemcpyHostToDevice, st));
+  CK(upload(B->blocks, B->hblocks.data(), nb, st));
+  CK(B->stream.alloc(B->stream_len + 64, st));
+  CK(B->scratch.alloc(64, st));
+  uint32_t* w = B->scratch.as<uint32_t>();
+  CK(cudaMemsetAsync(w, 0, 4, st));
+  CK(cudaMemsetAsync(w + 1, 0xFF, 4, st));
+  CK(record(ctx->ev0, st));
+  CK(bam_inflate(B->file.as<uint8_t>(), B->blocks.as<BgzfBlock>(), nb, B->stream.as<uint8_t>(), w, w + 1, ctx->sms, st));
+  CK(record(ctx->ev1, st));
+  uint32_t h[2];
+  CK(cudaMemcpyAsync(h, w, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  ctx->last_ms = ctx->main_ms = elapsed(ctx->ev0, ctx->ev1);
+  ctx->launches = nb ? 1 : 0;
+  ctx->last_h2d = size;
+  if (h[0]) return fail(ctx, BSQ_ERR_DATA, bam_err_text(h[0]) + "first failing block " + std::to_string(h[1]));
+  // the header: fetch a growing prefix of the stream until it parses
+  std::vector<uint8_t> pre;
+  for (uint64_t want = std::min<uint64_t>(B->stream_len, 1 << 16);; want = std::min<uint64_t>(B->stream_len, want * 4)) {
+    pre.resize(want);
+    CK(cudaMemcpy(pre.data(), B->stream.p, want, cudaMemcpyDeviceToHost));
+    const int r = parse_bam_header(pre.data(), want, *B);
+    if (r == 0) break;
+    if (r < 0 || want == B->stream_len) return fail(ctx, BSQ_ERR_INVALID, "malformed BAM header");
+  }
+  *out = B.release();
+  return BSQ_OK;
+}
+
+void bsq_bam_close(bsq_bam* bam) {
+  if (!bam) return;
+  cudaSetDevice(bam->ctx->device);
+  cudaStreamSynchronize(bam->ctx->stream);
+  delete bam;
+}
+
+int bsq_bam_header(const bsq_bam* bam, const char** text, uint64_t* text_len, uint32_t* n_ref,
+                   const char* const** ref_names, const uint32_t** ref_lengths) {
+  if (!bam) return BSQ_ERR_INVALID;
+  if (text) *text = bam->text.c_str();
+  if (text_len) *text_len = bam->text.size();
+  if (n_ref) *n_ref = (uint32_t)bam->names.size();
+  if (ref_names) *ref_names = bam->name_ptrs.data();
+  if (ref_lengths) *ref_lengths = bam->lengths.data();
+  return BSQ_OK;
+}
+
+int bsq_bam_decode(bsq_ctx* ctx, bsq_bam* bam, const bsq_bam_groups* groups, uint64_t* n_records,
+                   uint64_t* n_cigar_total, uint64_t* n_bases_total) {
+  if (!ctx || !bam || bam->ctx != ctx) return fail(ctx, BSQ_ERR_INVALID, "null argument or another context's BAM");
+  CK(cudaSetDevice(ctx->device));
+  BamGroups G;
+  memset(&G, 0, sizeof G);
+  std::string ids;
+  if (groups && groups->n_groups) {
+    if (groups->n_groups > (uint32_t)kBamMaxGroups || !groups->ids)
+      return fail(ctx, BSQ_ERR_INVALID, "more than 64 read groups, or no IDs");
+    G.n = groups->n_groups;
+    for (uint32_t g = 0; g < G.n; g++) {
+      G.id_off[g] = (uint32_t)ids.size();
+      ids += groups->ids[g];
+      G.file_base[g] = groups->file_base ? groups->file_base[g] : 0;
+      G.file_count[g] = (groups->file_base && groups->file_count) ? groups->file_count[g] : 0;
+    }
+    G.id_off[G.n] = (uint32_t)ids.size();
+  }
+  cudaStream_t st = ctx->stream;
+  cudaGetLastError();
+  const uint32_t nb = (uint32_t)bam->hblocks.size();
+  uint32_t* w = bam->scratch.as<uint32_t>();
+  CK(record(ctx->ev0, st));
+  CK(cudaMemsetAsync(w, 0, 16, st));
+  CK(cudaMemsetAsync(w + 1, 0xFF, 4, st));
+  // records per block, then their offsets
+  DevMem counts, base;
+  CK(counts.alloc((uint64_t)nb * 4 + 16, st));
+  CK(bam_walk(bam->stream.as<uint8_t>(), bam->blocks.as<BgzfBlock>(), nb, bam->records_begin, counts.as<uint32_t>(),
+              nullptr, nullptr, w, ctx->sms, st));
+  std::vector<uint32_t> hc(nb);
+  uint32_t herr = 0;
+  if (nb) CK(cudaMemcpyAsync(hc.data(), counts.p, (uint64_t)nb * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&herr, w, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (herr) return fail(ctx, BSQ_ERR_INVALID, bam_err_text(herr));
+  std::vector<uint64_t> hb(nb);
+  uint64_t n = 0;
+  for (uint32_t b = 0; b < nb; b++) { hb[b] = n; n += hc[b]; }
+  if (n >= 0xFFFFFFFFull) return fail(ctx, BSQ_ERR_INVALID, "more than 2^32 - 1 records");
+  DevMem offsets;
+  CK(upload(base, hb.data(), nb, st));
+  CK(offsets.alloc(n * 8 + 16, st));
+  CK(bam_walk(bam->stream.as<uint8_t>(), bam->blocks.as<BgzfBlock>(), nb, bam->records_begin, nullptr,
+              base.as<uint64_t>(), offsets.as<uint64_t>(), w, ctx->sms, st));
+  // fixed fields and tags
+  bam->rec.reset(new RecordsDev());
+  bam->decoded = false;
+  RecordsDev& R = *bam->rec;
+  CK(R.tid.alloc(n * 4 + 16, st)); CK(R.pos.alloc(n * 4 + 16, st)); CK(R.flag.alloc(n * 2 + 16, st));
+  CK(R.mapq.alloc(n + 16, st)); CK(R.x1.alloc(n * 4 + 16, st)); CK(R.xl.alloc(n * 4 + 16, st));
+  CK(R.xr.alloc(n * 4 + 16, st)); CK(R.rfile.alloc(n + 16, st)); CK(R.rg.alloc(n * 2 + 16, st));
+  CK(R.lq.alloc(n * 4 + 16, st)); CK(R.soff.alloc(n * 8 + 16, st)); CK(R.coff.alloc(n * 8 + 16, st));
+  CK(R.nc.alloc(n * 2 + 16, st)); CK(R.xj.alloc(n + 16, st));
+  DevMem ncig32, nib, tmp, ids_dev;
+  CK(ncig32.alloc(n * 4 + 16, st));
+  CK(nib.alloc(n * 4 + 16, st));
+  CK(tmp.alloc((n / 1024 + 4) * 8 + 64, st));
+  CK(upload(ids_dev, ids.data(), ids.size() + 1, st));
+  BamRecordsDev D;
+  D.tid = R.tid.as<int32_t>(); D.pos = R.pos.as<int32_t>(); D.flag = R.flag.as<uint16_t>(); D.mapq = R.mapq.as<uint8_t>();
+  D.x1 = R.x1.as<uint32_t>(); D.xl = R.xl.as<int32_t>(); D.xr = R.xr.as<int32_t>(); D.read_file = R.rfile.as<uint8_t>();
+  D.read_group = R.rg.as<uint16_t>(); D.l_qseq = R.lq.as<uint32_t>(); D.seq_off = R.soff.as<uint64_t>();
+  D.cigar_off = R.coff.as<uint64_t>(); D.n_cigar = R.nc.as<uint16_t>(); D.xj = R.xj.as<uint8_t>();
+  D.cigar = nullptr; D.seq = nullptr; D.qual = nullptr;
+  CK(bam_fields(bam->stream.as<uint8_t>(), offsets.as<uint64_t>(), n, (uint32_t)bam->names.size(), G,
+                ids_dev.as<char>(), D, ncig32.as<uint32_t>(), nib.as<uint32_t>(), w, ctx->sms, st));
+  // CIGAR and base offsets
+  uint64_t* tot = reinterpret_cast<uint64_t*>(w + 4);   // [0] CIGAR ops, [1] nibbles
+  CK(scan_u32(ncig32.as<uint32_t>(), D.cigar_off, n, tmp.as<uint64_t>(), tot, st));
+  CK(scan_u32(nib.as<uint32_t>(), D.seq_off, n, tmp.as<uint64_t>(), tot + 1, st));
+  uint32_t hw[8];
+  CK(cudaMemcpyAsync(hw, w, 32, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (hw[0]) return fail(ctx, BSQ_ERR_INVALID, bam_err_text(hw[0]));
+  uint64_t totals[2];
+  memcpy(totals, hw + 4, 16);
+  // unplaced records: all after the placed ones; they are dropped
+  uint64_t used = n;
+  if (hw[1] != 0xFFFFFFFFu) {
+    if (hw[2] > hw[1]) return fail(ctx, BSQ_ERR_INVALID, bam_err_text(kBamOrder));
+    used = hw[1];
+  }
+  CK(R.cigar.alloc(totals[0] * 4 + 16, st));
+  CK(R.seq.alloc(totals[1] / 2 + 16, st));
+  CK(R.qual.alloc(totals[1] + 16, st));
+  D.cigar = R.cigar.as<uint32_t>(); D.seq = R.seq.as<uint8_t>(); D.qual = R.qual.as<uint8_t>();
+  CK(bam_copy(bam->stream.as<uint8_t>(), offsets.as<uint64_t>(), n, D, ctx->sms, st));
+  CK(record(ctx->ev1, st));
+  CK(cudaStreamSynchronize(st));
+  ctx->last_ms = ctx->main_ms = elapsed(ctx->ev0, ctx->ev1);
+  ctx->launches = 9;
+  // the dropped unplaced records are the last ones: their CIGARs and bases are at the arrays' ends
+  R.n = used;
+  if (used < n) {
+    uint64_t off[2];
+    CK(cudaMemcpy(&off[0], D.cigar_off + used, 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&off[1], D.seq_off + used, 8, cudaMemcpyDeviceToHost));
+    R.n_cigar_total = off[0];
+    R.n_bases_total = off[1];
+  } else {
+    R.n_cigar_total = totals[0];
+    R.n_bases_total = totals[1];
+  }
+  R.has_xj = true;
+  bam->decoded = true;
+  if (n_records) *n_records = R.n;
+  if (n_cigar_total) *n_cigar_total = R.n_cigar_total;
+  if (n_bases_total) *n_bases_total = R.n_bases_total;
+  return BSQ_OK;
+}
+
+int bsq_bam_copy_records(bsq_ctx* ctx, const bsq_bam* bam, const bsq_read_arrays* out) {
+  if (!ctx || !bam || !out) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  if (!bam->decoded) return fail(ctx, BSQ_ERR_INVALID, "BAM not decoded");
+  CK(cudaSetDevice(ctx->device));
+  const RecordsDev& R = *bam->rec;
+  const uint64_t n = R.n;
+  struct Item { void* dst; const DevMem* src; uint64_t bytes; };
+  const Item items[] = {
+      {out->tid, &R.tid, n * 4}, {out->pos, &R.pos, n * 4}, {out->flag, &R.flag, n * 2}, {out->mapq, &R.mapq, n},
+      {out->x1, &R.x1, n * 4}, {out->xl, &R.xl, n * 4}, {out->xr, &R.xr, n * 4}, {out->read_file, &R.rfile, n},
+      {out->read_group, &R.rg, n * 2}, {out->l_qseq, &R.lq, n * 4}, {out->seq_off, &R.soff, n * 8},
+      {out->cigar_off, &R.coff, n * 8}, {out->n_cigar, &R.nc, n * 2}, {out->xj, &R.xj, n},
+      {out->cigar, &R.cigar, R.n_cigar_total * 4}, {out->seq, &R.seq, R.n_bases_total / 2},
+      {out->qual, &R.qual, R.n_bases_total}};
+  for (const Item& it : items)
+    if (it.dst && it.bytes) CK(cudaMemcpyAsync(it.dst, it.src->p, it.bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return BSQ_OK;
+}
+
+int bsq_bam_load(bsq_ctx* ctx, bsq_bam* bam, const bsq_reference* ref, int32_t* sample_id) {
+  if (!ctx || !bam || !ref || !sample_id || bam->ctx != ctx) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  if (!bam->decoded) return fail(ctx, BSQ_ERR_INVALID, "BAM not decoded");
+  CK(cudaSetDevice(ctx->device));
+  if (ref->n_targets != bam->names.size()) return fail(ctx, BSQ_ERR_INVALID, "reference and BAM header differ in targets");
+  for (uint32_t t = 0; t < ref->n_targets; t++)
+    if (ref->target_offset[t + 1] - ref->target_offset[t] != bam->lengths[t])
+      return fail(ctx, BSQ_ERR_INVALID, "reference and BAM header differ in target length");
+  cudaStream_t st = ctx->stream;
+  std::unique_ptr<SampleDev> s;
+  int rc = new_sample(ctx, ref, bam->rec->n, s, st);
+  if (rc != BSQ_OK) return rc;
+  rc = pack_sample(ctx, s, *bam->rec, st, sample_id);
+  bam->rec.reset();
+  bam->decoded = false;
+  return rc;
 }
 
 }  // extern "C"

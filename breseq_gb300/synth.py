@@ -550,3 +550,114 @@ def config_batch(seed=41, n_samples=96, scale=1.0):
                                     low_quality_sites=max(1, int(11 * mb)))
         out.append((c, poly))
     return out
+
+
+# ------------------------------------------------------------------ BAM bytes of a sample
+BGZF_EOF = bytes.fromhex("1f8b08040000000000ff0600424302001b0003000000000000000000")
+
+
+def _reg2bin(beg: int, end: int) -> int:
+    """BAM bin of a 0-based half-open interval (SAM/BAM specification §5.3)."""
+    end -= 1
+    for shift, off in ((14, 4681), (17, 585), (20, 73), (23, 9), (26, 1)):
+        if beg >> shift == end >> shift:
+            return off + (beg >> shift)
+    return 0
+
+
+def _bgzf_block(payload: bytes, level: int) -> bytes:
+    import struct
+    import zlib
+    co = zlib.compressobj(level, zlib.DEFLATED, -15)
+    cdata = co.compress(payload) + co.flush()
+    bsize = 12 + 6 + len(cdata) + 8 - 1
+    head = struct.pack("<BBBBIBBHBBHH", 31, 139, 8, 4, 0, 0, 255, 6, 66, 67, 2, bsize)
+    return head + cdata + struct.pack("<II", zlib.crc32(payload) & 0xFFFFFFFF, len(payload))
+
+
+def bam_groups(s: Sample):
+    """The read groups the BAM of bam_bytes() declares: IDs, and each group's first read-file index
+    and file count, from the sample's read files."""
+    groups = sorted(set(int(g) for g in np.unique(s.read_group)))
+    n = max(groups) + 1 if groups else 1
+    ids = [f"rg{g}" for g in range(n)]
+    base, count = [], []
+    for g in range(n):
+        f = s.read_file[s.read_group == g]
+        lo = int(f.min()) if f.size else 0
+        hi = int(f.max()) if f.size else 0
+        base.append(lo)
+        count.append(hi - lo + 1)
+    return ids, base, count
+
+
+def bam_bytes(s: Sample, level: int = 6, block_payload: int = 0xFF00, seed: int = 0, rg_tags: bool = True) -> bytes:
+    """The sample as a coordinate-sorted BAM (SAM/BAM specification §4.2), compressed in BGZF blocks
+    the way htslib writes them: the header in its own blocks, a record never split across blocks
+    (a block is closed before a record would overflow block_payload bytes), an EOF block at the end.
+    Tags: X1 when the redundancy is not 1, XL / XR when present, XJ when set, RG when the sample has
+    several read groups (or always, with rg_tags); integer tags in varying BAM integer types."""
+    import struct
+    rng = np.random.default_rng(seed)
+    ids, _, _ = bam_groups(s)
+    T = len(s.target_names)
+    text = "@HD\tVN:1.6\tSO:coordinate\n"
+    for t in range(T):
+        text += f"@SQ\tSN:{s.target_names[t]}\tLN:{int(s.target_offset[t + 1] - s.target_offset[t])}\n"
+    for g in ids:
+        text += f"@RG\tID:{g}\tLB:{g}\tSM:sample\n"
+    head = b"BAM\1" + struct.pack("<i", len(text)) + text.encode() + struct.pack("<i", T)
+    for t in range(T):
+        name = s.target_names[t].encode() + b"\0"
+        head += struct.pack("<i", len(name)) + name + struct.pack("<i", int(s.target_offset[t + 1] - s.target_offset[t]))
+    out = [_bgzf_block(head[i:i + block_payload], level) for i in range(0, len(head), block_payload)]
+    int_types = [("C", "<B", 0, 255), ("S", "<H", 0, 65535), ("i", "<i", -2**31, 2**31 - 1), ("I", "<I", 0, 2**32 - 1),
+                 ("c", "<b", -128, 127), ("s", "<h", -32768, 32767)]
+
+    def int_tag(tag, v):
+        ok = [t for t in int_types if t[2] <= v <= t[3]]
+        code, fmt, _, _ = ok[int(rng.integers(0, len(ok)))]
+        return tag.encode() + code.encode() + struct.pack(fmt, v)
+
+    buf = bytearray()
+    for i in range(s.n_reads):
+        L = int(s.l_qseq[i])
+        nc = int(s.n_cigar[i])
+        co = int(s.cigar_off[i])
+        cig = s.cigar[co:co + nc]
+        ops, lens = cig & 0xF, cig >> 4
+        rlen = int(lens[(ops == 0) | (ops == 2) | (ops == 3) | (ops == 7) | (ops == 8)].sum())
+        pos = int(s.pos[i])
+        name = f"r{i}".encode() + b"\0"
+        so = int(s.seq_off[i])
+        seq = s.seq[so // 2: so // 2 + (L + 1) // 2].tobytes()
+        if L & 1 and seq:   # the spare low nibble of an odd-length read is zero in BAM
+            seq = seq[:-1] + bytes([seq[-1] & 0xF0])
+        qual = s.qual[so: so + L].tobytes()
+        aux = b""
+        if int(s.x1[i]) != 1:
+            aux += int_tag("X1", int(s.x1[i]))
+        if int(s.xl[i]) >= 0:
+            aux += int_tag("XL", int(s.xl[i]))
+        if int(s.xr[i]) >= 0:
+            aux += int_tag("XR", int(s.xr[i]))
+        if rng.random() < 0.3:
+            aux += b"NMi" + struct.pack("<i", int(rng.integers(0, 5)))
+        if s.xj is not None and s.xj[i]:
+            aux += int_tag("XJ", 1)
+        if rg_tags or len(ids) > 1:
+            aux += b"RGZ" + ids[int(s.read_group[i])].encode() + b"\0"
+        if rng.random() < 0.1:
+            aux += b"ZBBs" + struct.pack("<I", 3) + struct.pack("<3h", 1, -2, 3)
+        body = struct.pack("<iiBBHHHiiii", int(s.tid[i]), pos, len(name), int(s.mapq[i]), _reg2bin(pos, pos + max(rlen, 1)),
+                           nc, int(s.flag[i]), L, -1, -1, 0)
+        rec = body + name + cig.astype("<u4").tobytes() + seq + qual + aux
+        rec = struct.pack("<i", len(rec)) + rec
+        if len(buf) + len(rec) > block_payload and buf:
+            out.append(_bgzf_block(bytes(buf), level))
+            buf = bytearray()
+        buf += rec
+    if buf:
+        out.append(_bgzf_block(bytes(buf), level))
+    out.append(BGZF_EOF)
+    return b"".join(out)

@@ -373,6 +373,65 @@ int bsq_sc_result_copy(const bsq_ctx* ctx, bsq_sc_position* rows, uint64_t capac
 int bsq_write_soft_clipping_counts(const char* path, const char* const* target_names, const bsq_sc_params* p,
                                    const bsq_sc_summary* s, const bsq_sc_position* rows, uint64_t n);
 
+/* ---------------------------------------------------------------- BAM input on the device */
+
+/* breseq reads reference.bam through htslib on the host (src/breseq/pileup_base.cpp:61-88,
+ * 232-235): BGZF inflate, then record decode.  Here the file's bytes are uploaded once, every BGZF
+ * block is inflated on the device by its own thread (its CRC-32 checked), and the records are
+ * decoded there into the bsq_read_soa layout.  Records must not span BGZF blocks, which htslib's
+ * writer guarantees for records under 64 KiB; a file that breaks this is refused (BSQ_ERR_INVALID).
+ * Unplaced records (refID -1), which a coordinate-sorted file keeps last, are dropped. */
+typedef struct bsq_bam bsq_bam;
+int  bsq_bam_open(bsq_ctx* ctx, const uint8_t* data, uint64_t size, bsq_bam** out);
+void bsq_bam_close(bsq_bam* bam);
+/* The header text and the reference sequences it names (valid until bsq_bam_close). */
+int bsq_bam_header(const bsq_bam* bam, const char** text, uint64_t* text_len, uint32_t* n_ref,
+                   const char* const** ref_names, const uint32_t** ref_lengths);
+
+/* Read groups as breseq resolves them: the @RG IDs in header order (read_group_index_map,
+ * src/breseq/alignment.h:533-560: a record without RG, with an unknown ID, or in a header with at
+ * most one group gets group 0) and each group's first flat read-file index and file count
+ * (read_file_partition, :569-607).  file_base / file_count NULL: no read file sets, every record's
+ * read file is 0. */
+typedef struct bsq_bam_groups {
+    uint32_t           n_groups;      /* at most 64 */
+    const char* const* ids;
+    const uint32_t*    file_base;
+    const uint32_t*    file_count;
+} bsq_bam_groups;
+
+/* Decodes the records on the device; the counts size the arrays of bsq_bam_copy_records. */
+int bsq_bam_decode(bsq_ctx* ctx, bsq_bam* bam, const bsq_bam_groups* groups, uint64_t* n_records,
+                   uint64_t* n_cigar_total, uint64_t* n_bases_total);
+
+/* Writable arrays in the bsq_read_soa layout (sizes: n_records, n_cigar_total, n_bases_total and
+ * n_bases_total / 2 for seq). */
+typedef struct bsq_read_arrays {
+    int32_t*  tid;
+    int32_t*  pos;
+    uint16_t* flag;
+    uint8_t*  mapq;
+    uint32_t* x1;
+    int32_t*  xl;
+    int32_t*  xr;
+    uint8_t*  read_file;
+    uint16_t* read_group;
+    uint32_t* l_qseq;
+    uint64_t* seq_off;
+    uint64_t* cigar_off;
+    uint16_t* n_cigar;
+    uint32_t* cigar;
+    uint8_t*  seq;
+    uint8_t*  qual;
+    uint8_t*  xj;
+} bsq_read_arrays;
+int bsq_bam_copy_records(bsq_ctx* ctx, const bsq_bam* bam, const bsq_read_arrays* out);
+
+/* Makes the decoded records a resident sample with the given reference (whose targets must be the
+ * header's, in order and length), as bsq_load_sample does with host arrays.  The decoded arrays move
+ * into the sample; decode again to load another copy. */
+int bsq_bam_load(bsq_ctx* ctx, bsq_bam* bam, const bsq_reference* ref, int32_t* sample_id);
+
 /* ---------------------------------------------------------------- BAM2COV coverage table */
 
 /* Per-position coverage of one region as `breseq BAM2COV --format TSV` tabulates it
