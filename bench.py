@@ -18,6 +18,11 @@ polymorphism modes), drawn from a pool of distinct seeded samples:
   "served":  open-loop Poisson arrivals at 0.5/1/2x the batched capacity into the scoring server
              (HBM-footprint admission, continuous batching), with p50/p99 job latency.
 
+A "bam_input" leg runs the same step from the workload's BAM bytes (written by the vectorised
+synthetic writer, zlib level 6, htslib's record-aligned blocks): upload of the compressed file, BGZF
+inflate and record decode on the device, sample load, both passes; against zlib inflating the same
+blocks on all host cores.
+
 A "coverage_table" leg times the BAM2COV coverage columns of the workload's chromosome (every position)
 and the table at BAM2COV's default resolution, against the oracle on a 200 kb region.
 
@@ -151,6 +156,85 @@ COV_TABLE_DRAM_OVER_ALGORITHMIC = 580.482284e6 / (32 * 6206454 + 80 * 4630000)
 
 COV_COLUMNS = ("unique_top", "unique_bot", "redundant_top", "redundant_bot", "raw_redundant_top",
                "raw_redundant_bot", "unique_top_begin", "unique_bot_begin")
+
+
+def _cpu_inflate(data: bytes, threads: int):
+    """zlib inflating every BGZF block of data on `threads` host threads: seconds, output bytes."""
+    import concurrent.futures as cf
+    import struct
+    import zlib
+    blocks, pos = [], 0
+    while pos < len(data):
+        xlen = struct.unpack_from("<H", data, pos + 10)[0]
+        bsize = struct.unpack_from("<H", data, pos + 16)[0]
+        blocks.append(data[pos + 12 + xlen: pos + bsize + 1 - 8])
+        pos += bsize + 1
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        out = sum(len(x) for x in ex.map(lambda c: zlib.decompress(c, -15), blocks, chunksize=64))
+    return time.perf_counter() - t0, out
+
+
+def run_bam(args, device, s):
+    """The step from BAM bytes: open (upload + inflate), decode, load, pass 1, table, pass 2, free."""
+    from breseq_gb300 import synth
+    from breseq_gb300.api import ImSettings, Scorer
+    t0 = time.perf_counter()
+    data = synth.bam_bytes_fast(s)
+    gen_s = time.perf_counter() - t0
+    groups = synth.bam_groups(s)
+    arr = np.frombuffer(bytearray(data), dtype=np.uint8)
+    bases = s.aligned_bases()
+    prec = 1 if args.precision == "fp32c" else 0
+    st = ImSettings()
+    with Scorer(device) as sc:
+        pinned = sc.L.bsq_host_register(arr.ctypes.data, arr.nbytes) == 0
+        steps, phases = [], {"open": [], "decode": [], "load": [], "passes": []}
+        kern = {"inflate": [], "decode": []}
+        for i in range(args.warmup + args.steps):
+            sc.timer_start()
+            t0 = time.perf_counter()
+            bam = sc.open_bam(arr)
+            k_inf = sc.last_pass_stats()["main_kernel_ms"]
+            t1 = time.perf_counter()
+            bam.decode(groups)
+            k_dec = sc.last_pass_stats()["device_ms"]
+            t2 = time.perf_counter()
+            sid = bam.load(s)
+            bam.close()
+            t3 = time.perf_counter()
+            ec = sc.error_count(sid)
+            tab = sc.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
+            sc.identify_mutations(sid, tab, st, precision=prec, as_dicts=False)
+            sc.free_sample(sid)
+            t = sc.timer_stop()
+            t4 = time.perf_counter()
+            if i >= args.warmup:
+                steps.append(t)
+                for k, a, b in (("open", t0, t1), ("decode", t1, t2), ("load", t2, t3), ("passes", t3, t4)):
+                    phases[k].append(1e3 * (b - a))
+                kern["inflate"].append(k_inf)
+                kern["decode"].append(k_dec)
+        if pinned:
+            sc.L.bsq_host_unregister(arr.ctypes.data)
+    cpu_s, out_bytes = _cpu_inflate(data, os.cpu_count() or 1)
+    ms = statistics.mean(steps)
+    inf_ms = statistics.mean(kern["inflate"])
+    hbm, peak_kind = _peaks()
+    return {"workload": f"{WORKLOAD} as BAM (zlib level 6, {len(data) / 1e6:.0f} MB compressed)",
+            "compressed_bytes": len(data), "inflated_bytes": out_bytes, "records": s.n_reads,
+            "value": bases / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "e2e": {"value": bases / (ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": len(data),
+                    "mode": "sequential: open, decode, load, both passes, free per step"},
+            "host_ms_by_phase": {k: statistics.mean(v) for k, v in phases.items()},
+            "inflate_kernel_ms": inf_ms, "decode_device_ms": statistics.mean(kern["decode"]),
+            "roofline": {"bound": "latency (one thread decodes a block's Huffman stream serially)", "kernel": "bgzf_inflate_kernel",
+                         "achieved": (len(data) + out_bytes) / (inf_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": (len(data) + out_bytes) / (inf_ms / 1e3) / 1e9 / hbm, "peak_kind": peak_kind,
+                         "algorithmic_bytes": len(data) + out_bytes, "traffic": None},
+            "writer_seconds": gen_s,
+            "cpu_baseline": {"value": out_bytes / cpu_s, "unit": "inflated bytes/s", "cores": os.cpu_count() or 1,
+                             "kind": "port", "sample": f"zlib inflating all {len(data) / 1e6:.0f} MB of blocks ({cpu_s:.2f} s)"}}
 
 
 def run_coverage(args, sc, sid, s):
@@ -470,6 +554,8 @@ def run_ours(args, world, rank, local, pg):
                                 "sample": f"same workload at {args.cpu_scale:g} x genome length ({ln} bp), "
                                           f"{reps} runs, {cb} read-bases in {dt:.1f} s"}
     sc.close()
+    if rank == 0 and not args.no_bam:
+        line["bam_input"] = run_bam(args, local, s)
     if rank == 0 and args.batch_jobs > 0:
         line["batched"], line["served"] = run_mix(args, local)
     if rank == 0 and not args.no_softclip:
@@ -620,6 +706,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--no-softclip", action="store_true", help="skip the soft-clipping leg")
     ap.add_argument("--no-coverage", action="store_true", help="skip the coverage-table leg")
+    ap.add_argument("--no-bam", action="store_true", help="skip the BAM-input leg")
     args = ap.parse_args()
     world, rank, local, pg = _dist()
     if args.impl == "reference":

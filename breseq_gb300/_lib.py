@@ -97,7 +97,7 @@ def load():
                                        P(C.c_uint32)]
     L.bsq_write_coverage_region.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, C.c_uint32, C.c_uint32,
                                             C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_double)]
-    L.bsq_bam_open.argtypes = [C.c_void_p, C.c_char_p, C.c_uint64, P(C.c_void_p)]
+    L.bsq_bam_open.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, P(C.c_void_p)]
     L.bsq_bam_close.argtypes = [C.c_void_p]
     L.bsq_bam_close.restype = None
     L.bsq_bam_header.argtypes = [C.c_void_p, P(C.c_char_p), P(C.c_uint64), P(C.c_uint32), P(P(C.c_char_p)),

@@ -257,10 +257,15 @@ class Scorer:
         return dict(summary=abi.sc_summary_dict(s), rows=abi.sc_rows_array(rows, s.n_positions))
 
     # ------------------------------------------------------------------ BAM input
-    def open_bam(self, data: bytes) -> "Bam":
-        """Uploads a BAM file's bytes and inflates every BGZF block on the device."""
+    def open_bam(self, data) -> "Bam":
+        """Uploads a BAM file's bytes (bytes, or a uint8 numpy array, e.g. page-locked) and inflates
+        every BGZF block on the device."""
         h = C.c_void_p()
-        self._check(self.L.bsq_bam_open(self.ctx, data, len(data), C.byref(h)))
+        if isinstance(data, np.ndarray):
+            addr, size = data.ctypes.data, data.nbytes
+        else:
+            addr, size = C.cast(C.c_char_p(data), C.c_void_p).value, len(data)
+        self._check(self.L.bsq_bam_open(self.ctx, addr, size, C.byref(h)))
         return Bam(self, h)
 
     def load_bam(self, data: bytes, reference_sample, groups=None) -> int:

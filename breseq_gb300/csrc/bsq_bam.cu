@@ -23,33 +23,97 @@ __device__ __forceinline__ uint32_t rd32(const uint8_t* p) {
   return p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
 }
 
-// One thread per BGZF block: inflate, then the CRC-32 of the output (reflected polynomial 0xEDB88320,
-// as gzip defines it), from a table each thread block builds in shared memory.
-__global__ void __launch_bounds__(128) bgzf_inflate_kernel(const uint8_t* file, const BgzfBlock* blocks, uint32_t n,
-                                                           uint8_t* out, uint32_t* err, uint32_t* first_bad) {
+// One warp per BGZF block.  Lane 0 runs the resumable decoder (bsq_inflate.cuh) from a 1 KiB
+// shared-memory window of the compressed block into the warp's 4 KiB shared-memory ring; whenever
+// it pauses the whole warp moves the new output bytes to global memory and, when the decoder runs
+// low, stages the next window of input.  Then every lane takes the CRC-32 of a 1/32 slice of the
+// block, and the slices are combined in order.
+constexpr int kInfWarps = 4;
+constexpr uint32_t kInWin = 1024;
+struct InflateWarp {
+  inflate::Tables T;
+  uint8_t ring[inflate::kRing];
+  uint8_t win[kInWin];
+};
+
+__global__ void __launch_bounds__(kInfWarps * 32) bgzf_inflate_kernel(const uint8_t* file, const BgzfBlock* blocks,
+                                                                      uint32_t n, uint8_t* out, uint32_t* err,
+                                                                      uint32_t* first_bad) {
   __shared__ uint32_t crc_table[256];
+  __shared__ InflateWarp W[kInfWarps];
   for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) {
     uint32_t c = i;
-    for (int k = 0; k < 8; k++) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+    for (int k = 0; k < 8; k++) c = (c & 1) ? inflate::kCrcPoly ^ (c >> 1) : c >> 1;
     crc_table[i] = c;
   }
   __syncthreads();
-  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= n) return;
-  const BgzfBlock B = blocks[b];
-  uint32_t got = 0;
-  const int rc = inflate::inflate_raw(file + B.in_off, B.in_len, out + B.out_off, B.isize, &got);
-  if (rc != inflate::kOk || got != B.isize) {
-    atomicOr(err, kBamInflate);
-    atomicMin(first_bad, b);
-    return;
-  }
-  uint32_t c = 0xFFFFFFFFu;
-  const uint8_t* o = out + B.out_off;
-  for (uint32_t k = 0; k < B.isize; k++) c = crc_table[(c ^ o[k]) & 0xFF] ^ (c >> 8);
-  if ((c ^ 0xFFFFFFFFu) != B.crc) {
-    atomicOr(err, kBamCrc);
-    atomicMin(first_bad, b);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  InflateWarp& S = W[w];
+  for (uint32_t b = blockIdx.x * kInfWarps + w; b < n; b += gridDim.x * kInfWarps) {
+    const BgzfBlock B = blocks[b];
+    uint8_t* o = out + B.out_off;
+    const uint8_t* in = file + B.in_off;
+    inflate::Inflater z;
+    inflate::Codes K;
+    if (lane == 0) {
+      inflate::inflater_init(z, B.in_len, B.isize);
+      z.win = S.win;
+    }
+    uint32_t flushed = 0, pos = 0, win_hi = 0;
+    int status = 0;
+    for (;;) {
+      // stage the next window of input when the decoder is low on it (and at the start)
+      if (win_hi < B.in_len && pos + inflate::kInMargin > win_hi) {
+        const uint32_t lo = pos, hi = min(B.in_len, pos + kInWin);
+        for (uint32_t k = lo + lane; k < hi; k += 32) S.win[k - lo] = in[k];
+        win_hi = hi;
+        if (lane == 0) { z.win_lo = lo; z.win_hi = hi; }
+      }
+      __syncwarp();
+      uint32_t produced = 0;
+      if (lane == 0) {
+        inflate::z_run(z, S.T, K, S.ring, o);
+        produced = z.n;
+        pos = z.pos;
+        status = z.err ? 2 : (z.state == 3 ? 1 : 0);
+      }
+      __syncwarp();
+      produced = __shfl_sync(kFull, produced, 0);
+      pos = __shfl_sync(kFull, pos, 0);
+      status = __shfl_sync(kFull, status, 0);
+      for (uint32_t p = flushed + lane; p < produced; p += 32) o[p] = S.ring[p & (inflate::kRing - 1)];
+      __syncwarp();
+      flushed = produced;
+      if (lane == 0) z.flushed = produced;
+      if (status) break;
+    }
+    if (status == 2 || flushed != B.isize) {
+      if (lane == 0) {
+        atomicOr(err, kBamInflate);
+        atomicMin(first_bad, b);
+      }
+      continue;
+    }
+    // CRC-32 of each lane's slice, then combined in order
+    const uint32_t slice = (B.isize + 31) / 32;
+    const uint32_t a0 = min(B.isize, lane * slice), a1 = min(B.isize, a0 + slice);
+    uint32_t c = 0xFFFFFFFFu;
+    for (uint32_t k = a0; k < a1; k++) c = crc_table[(c ^ o[k]) & 0xFF] ^ (c >> 8);
+    c ^= 0xFFFFFFFFu;
+    uint32_t total = __shfl_sync(kFull, c, 0);
+    // every lane walks the combination, so the shuffles stay warp-wide
+    const uint32_t shift_full = inflate::gf2_x8n(slice);
+    for (int j = 1; j < 32; j++) {
+      const uint32_t cj = __shfl_sync(kFull, c, j);
+      const uint32_t bj0 = min(B.isize, (uint32_t)j * slice), bj1 = min(B.isize, bj0 + slice);
+      const uint32_t lj = bj1 - bj0;
+      if (lj == 0) continue;
+      total = inflate::gf2_mulmod(lj == slice ? shift_full : inflate::gf2_x8n(lj), total) ^ cj;
+    }
+    if (lane == 0 && total != B.crc) {
+      atomicOr(err, kBamCrc);
+      atomicMin(first_bad, b);
+    }
   }
 }
 
@@ -317,8 +381,8 @@ __global__ void __launch_bounds__(256) scan_apply_kernel(const uint32_t* in, uin
 
 cudaError_t bam_inflate(const uint8_t* file, const BgzfBlock* blocks, uint32_t n_blocks, uint8_t* out, uint32_t* err,
                         uint32_t* first_bad, int sms, cudaStream_t st) {
-  (void)sms;
-  if (n_blocks) bgzf_inflate_kernel<<<(n_blocks + 127) / 128, 128, 0, st>>>(file, blocks, n_blocks, out, err, first_bad);
+  if (n_blocks)
+    bgzf_inflate_kernel<<<grid_for(n_blocks, kInfWarps, sms, 8), kInfWarps * 32, 0, st>>>(file, blocks, n_blocks, out, err, first_bad);
   return cudaGetLastError();
 }
 

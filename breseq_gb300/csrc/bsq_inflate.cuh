@@ -236,3 +236,322 @@ BSQ_HD int inflate_raw(const uint8_t* in, uint32_t in_len, uint8_t* out, uint32_
 
 }  // namespace inflate
 }  // namespace bsq
+
+namespace bsq {
+namespace inflate {
+
+// ----------------------------------------------------------------------------- resumable decoder
+// The same format, decoded with lookup tables (9 bits for literal/length codes, 8 for distances; a
+// code longer than the table falls back to the canonical bit-by-bit decode) and suspended whenever
+// the staged output reaches a threshold or the staged input runs low, so a caller can move output
+// out of a small ring buffer and move more input in.  Output: positions [n - kRing, n) are in
+// ring[p & (kRing - 1)], everything before `flushed` is in out[] already, at most kRing bytes are
+// unflushed.  Input: bytes [win_lo, win_hi) of the compressed data are in win[]; decoding pauses
+// at a step boundary when fewer than kInMargin bytes remain staged, more than any one step (a
+// dynamic block header, or a symbol with its extra bits) reads.
+
+constexpr int kLitBits = 9, kDistBits = 8;
+constexpr uint32_t kRing = 4096;
+constexpr uint32_t kSuspend = kRing - 258 - 1;   // unflushed bytes at which decoding pauses
+constexpr uint32_t kInMargin = 640;              // staged input bytes below which decoding pauses
+
+// The lookup tables and code lengths of the current block (the device keeps them in shared memory)
+struct Tables {
+  uint16_t lit[1 << kLitBits];    // (length << 9) | symbol, 0 = not in the table
+  uint16_t dist[1 << kDistBits];  // (length << 9) | symbol
+  uint8_t lengths[288 + 32];
+};
+// The canonical codes, for building the tables and for codes longer than them (per thread)
+struct Codes {
+  Code lit_code, dist_code;
+};
+
+struct Inflater {
+  const uint8_t* win;             // staged input: bytes [win_lo, win_hi) of the compressed data
+  uint32_t win_lo, win_hi;
+  uint32_t in_len, pos;
+  uint64_t buf;
+  int cnt;
+  uint32_t n, flushed, cap;       // produced, moved to out, output capacity
+  int state;                      // 0 block header, 1 stored bytes, 2 Huffman symbols, 3 done
+  int last;
+  uint32_t stored_left;
+  int err;
+};
+
+BSQ_HD void inflater_init(Inflater& z, uint32_t in_len, uint32_t cap) {
+  z.win = nullptr; z.win_lo = 0; z.win_hi = 0;
+  z.in_len = in_len; z.pos = 0; z.buf = 0; z.cnt = 0;
+  z.n = 0; z.flushed = 0; z.cap = cap; z.state = 0; z.last = 0; z.stored_left = 0; z.err = kOk;
+}
+
+BSQ_HD void z_refill(Inflater& z) {
+  while (z.cnt <= 56 && z.pos < z.win_hi) {
+    z.buf |= (uint64_t)z.win[z.pos - z.win_lo] << z.cnt;
+    z.pos++;
+    z.cnt += 8;
+  }
+}
+
+// More input must be staged before the next step.
+BSQ_HD bool z_input_low(const Inflater& z) { return z.win_hi < z.in_len && z.pos + kInMargin > z.win_hi; }
+
+BSQ_HD uint32_t z_bits(Inflater& z, int k) {   // k <= 32
+  if (k == 0) return 0;
+  if (z.cnt < k) { z_refill(z); if (z.cnt < k) { z.err = kErrInput; return 0; } }
+  const uint32_t v = (uint32_t)(z.buf & ((1ull << k) - 1));
+  z.buf >>= k;
+  z.cnt -= k;
+  return v;
+}
+
+// Canonical codes of the lengths (RFC 1951 §3.2.2), bit-reversed into a k-bit lookup table.
+BSQ_HD void table_build(uint16_t* table, int k, const uint8_t* lengths, int nsym, const Code& c) {
+  for (int i = 0; i < (1 << k); i++) table[i] = 0;
+  // first code of each length; unused symbols (length 0) take no codes
+  uint32_t next[kMaxBits + 2];
+  uint32_t code = 0;
+  next[0] = 0;
+  for (int l = 1; l <= kMaxBits; l++) {
+    code = (code + (l > 1 ? c.count[l - 1] : 0u)) << 1;
+    next[l] = code;
+  }
+  for (int s = 0; s < nsym; s++) {
+    const int l = lengths[s];
+    if (l == 0) continue;
+    const uint32_t cd = next[l]++;
+    if (l > k) continue;
+    uint32_t rev = 0;
+    for (int b = 0; b < l; b++) rev |= ((cd >> b) & 1u) << (l - 1 - b);
+    for (uint32_t f = rev; f < (1u << k); f += 1u << l) table[f] = (uint16_t)((l << 9) | s);
+  }
+}
+
+// One symbol: the table when the code is short enough, else the canonical decode.
+BSQ_HD int z_symbol(Inflater& z, const uint16_t* table, int k, const Code& c) {
+  if (z.cnt < kMaxBits) z_refill(z);
+  const uint16_t e = table[z.buf & ((1u << k) - 1)];
+  if (e) {
+    const int l = e >> 9;
+    if (l > z.cnt) { z.err = kErrInput; return -1; }
+    z.buf >>= l;
+    z.cnt -= l;
+    return e & 511;
+  }
+  int code = 0, first = 0, index = 0;
+  for (int l = 1; l <= kMaxBits; l++) {
+    code |= (int)z_bits(z, 1);
+    if (z.err) return -1;
+    const int count = c.count[l];
+    if (code - first < count) return c.symbol[index + (code - first)];
+    index += count;
+    first += count;
+    first <<= 1;
+    code <<= 1;
+  }
+  z.err = kErrCode;
+  return -1;
+}
+
+// Reads one block header; builds the block's tables.
+BSQ_HD void z_header(Inflater& z, Tables& T, Codes& K) {
+  z.last = (int)z_bits(z, 1);
+  const uint32_t type = z_bits(z, 2);
+  if (z.err) return;
+  if (type == 0) {
+    // the rest of the current byte is skipped: whole bytes still buffered are given back
+    const int drop = z.cnt & 7;
+    z.buf >>= drop;
+    z.cnt -= drop;
+    const uint32_t len = z_bits(z, 16), nlen = z_bits(z, 16);
+    if (z.err) return;
+    if (len != (~nlen & 0xFFFFu)) { z.err = kErrStored; return; }
+    z.stored_left = len;
+    z.state = 1;
+  } else if (type == 1) {
+    for (int s = 0; s < 144; s++) T.lengths[s] = 8;
+    for (int s = 144; s < 256; s++) T.lengths[s] = 9;
+    for (int s = 256; s < 280; s++) T.lengths[s] = 7;
+    for (int s = 280; s < 288; s++) T.lengths[s] = 8;
+    for (int s = 0; s < 30; s++) T.lengths[288 + s] = 5;
+    code_build(K.lit_code, T.lengths, 288);
+    code_build(K.dist_code, T.lengths + 288, 30);
+    table_build(T.lit, kLitBits, T.lengths, 288, K.lit_code);
+    table_build(T.dist, kDistBits, T.lengths + 288, 30, K.dist_code);
+    z.state = 2;
+  } else if (type == 2) {
+    const int nlen = (int)z_bits(z, 5) + 257, ndist = (int)z_bits(z, 5) + 1, ncode = (int)z_bits(z, 4) + 4;
+    if (z.err) return;
+    if (nlen > 286 || ndist > 30) { z.err = kErrCode; return; }
+    const uint8_t order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+    for (int k = 0; k < 19; k++) T.lengths[k] = 0;
+    for (int k = 0; k < ncode; k++) T.lengths[order[k]] = (uint8_t)z_bits(z, 3);
+    if (z.err) return;
+    // the code-length code lives in dist_code while the lengths are read
+    if (!code_build(K.dist_code, T.lengths, 19)) { z.err = kErrCode; return; }
+    table_build(T.dist, kDistBits, T.lengths, 19, K.dist_code);
+    int k = 0;
+    while (k < nlen + ndist) {
+      const int sym = z_symbol(z, T.dist, kDistBits, K.dist_code);
+      if (sym < 0) { if (!z.err) z.err = kErrCode; return; }
+      if (sym < 16) { T.lengths[k++] = (uint8_t)sym; continue; }
+      uint8_t v = 0;
+      int rep;
+      if (sym == 16) {
+        if (k == 0) { z.err = kErrCode; return; }
+        v = T.lengths[k - 1];
+        rep = 3 + (int)z_bits(z, 2);
+      } else if (sym == 17) {
+        rep = 3 + (int)z_bits(z, 3);
+      } else {
+        rep = 11 + (int)z_bits(z, 7);
+      }
+      if (z.err) return;
+      if (k + rep > nlen + ndist) { z.err = kErrCode; return; }
+      while (rep--) T.lengths[k++] = v;
+    }
+    if (T.lengths[256] == 0) { z.err = kErrCode; return; }
+    if (!code_build(K.lit_code, T.lengths, nlen) || !code_build(K.dist_code, T.lengths + nlen, ndist)) {
+      z.err = kErrCode;
+      return;
+    }
+    table_build(T.lit, kLitBits, T.lengths, nlen, K.lit_code);
+    table_build(T.dist, kDistBits, T.lengths + nlen, ndist, K.dist_code);
+    z.state = 2;
+  } else {
+    z.err = kErrBlockType;
+  }
+}
+
+// Decodes until kSuspend bytes are unflushed, the stream ends (state 3) or an error.  ring holds the
+// recent output; out is read for back-references older than the ring.
+BSQ_HD void z_run(Inflater& z, Tables& T, Codes& K, uint8_t* ring, const uint8_t* out) {
+  while (z.err == kOk && z.state != 3 && z.n - z.flushed < kSuspend && !z_input_low(z)) {
+    if (z.state == 0) {
+      z_header(z, T, K);
+    } else if (z.state == 1) {
+      // stored bytes: whole buffered bytes first, then the input
+      if (z.stored_left == 0) { z.state = z.last ? 3 : 0; continue; }
+      if (z.n >= z.cap) { z.err = kErrOutput; return; }
+      uint8_t byte;
+      if (z.cnt >= 8) {
+        byte = (uint8_t)(z.buf & 0xFF);
+        z.buf >>= 8;
+        z.cnt -= 8;
+      } else {
+        if (z.pos >= z.win_hi) { z.err = kErrInput; return; }
+        byte = z.win[z.pos - z.win_lo];
+        z.pos++;
+      }
+      ring[z.n & (kRing - 1)] = byte;
+      z.n++;
+      z.stored_left--;
+    } else {
+      const int sym = z_symbol(z, T.lit, kLitBits, K.lit_code);
+      if (sym < 0) { if (!z.err) z.err = kErrCode; return; }
+      if (sym < 256) {
+        if (z.n >= z.cap) { z.err = kErrOutput; return; }
+        ring[z.n & (kRing - 1)] = (uint8_t)sym;
+        z.n++;
+      } else if (sym == 256) {
+        z.state = z.last ? 3 : 0;
+      } else {
+        const int li = sym - 257;
+        if (li >= 29) { z.err = kErrSymbol; return; }
+        const uint32_t len = length_base(li) + z_bits(z, length_extra(li));
+        const int ds = z_symbol(z, T.dist, kDistBits, K.dist_code);
+        if (ds < 0) { if (!z.err) z.err = kErrCode; return; }
+        if (ds >= 30) { z.err = kErrSymbol; return; }
+        const uint32_t d = dist_base(ds) + z_bits(z, dist_extra(ds));
+        if (z.err) return;
+        if (d > z.n) { z.err = kErrDistance; return; }
+        if (len > z.cap - z.n) { z.err = kErrOutput; return; }
+        if (d <= kRing) {
+          // the source is in the ring; an overlapping copy (d < len) repeats the bytes just written
+          for (uint32_t k = 0; k < len; k++) {
+            ring[z.n & (kRing - 1)] = ring[(z.n - d) & (kRing - 1)];
+            z.n++;
+          }
+        } else {
+          // farther than the ring: flushed output, read 16 bytes at a time so the loads overlap
+          const uint8_t* src = out + (z.n - d);
+          uint32_t k = 0;
+          for (; k + 16 <= len; k += 16) {
+            uint8_t v[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) v[j] = src[k + j];
+#pragma unroll
+            for (int j = 0; j < 16; j++) ring[(z.n + j) & (kRing - 1)] = v[j];
+            z.n += 16;
+          }
+          for (; k < len; k++) {
+            ring[z.n & (kRing - 1)] = src[k];
+            z.n++;
+          }
+        }
+      }
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------- CRC-32
+// gzip's CRC-32 (reflected, polynomial 0xEDB88320).  Two CRCs combine as crc(AB) =
+// crc(A) * x^(8 |B|) + crc(B) over GF(2) modulo the polynomial, the products taken in the
+// reflected representation (bit 31 is x^0).
+constexpr uint32_t kCrcPoly = 0xEDB88320u;
+
+BSQ_HD uint32_t gf2_mulmod(uint32_t a, uint32_t b) {
+  uint32_t p = 0;
+  for (int i = 0; i < 32; i++) {
+    if (a & (0x80000000u >> i)) p ^= b;
+    b = (b & 1) ? (b >> 1) ^ kCrcPoly : b >> 1;
+  }
+  return p;
+}
+
+// x^(8 n) modulo the polynomial
+BSQ_HD uint32_t gf2_x8n(uint64_t n) {
+  uint32_t p = 0x80000000u;            // x^0
+  uint32_t sq = 0x00800000u;           // x^8
+  while (n) {
+    if (n & 1) p = gf2_mulmod(sq, p);
+    sq = gf2_mulmod(sq, sq);
+    n >>= 1;
+  }
+  return p;
+}
+
+BSQ_HD uint32_t crc_combine(uint32_t crc_a, uint32_t crc_b, uint64_t len_b) {
+  return gf2_mulmod(gf2_x8n(len_b), crc_a) ^ crc_b;
+}
+
+}  // namespace inflate
+}  // namespace bsq
+
+namespace bsq {
+namespace inflate {
+
+// Host-side driver of the resumable decoder: whenever it pauses the ring is flushed into out and a
+// window of win_size input bytes from the current position is staged in win.
+inline int inflate_ring_host(const uint8_t* in, uint32_t in_len, uint8_t* out, uint32_t cap, uint32_t* out_len,
+                             Tables& T, uint8_t* ring, uint8_t* win, uint32_t win_size) {
+  Codes K;
+  Inflater z;
+  inflater_init(z, in_len, cap);
+  z.win = win;
+  while (z.err == kOk && z.state != 3) {
+    if (z.win_hi < z.in_len && z.pos + kInMargin > z.win_hi) {
+      z.win_lo = z.pos;
+      z.win_hi = z.pos + win_size < in_len ? z.pos + win_size : in_len;
+      for (uint32_t k = z.win_lo; k < z.win_hi; k++) win[k - z.win_lo] = in[k];
+    }
+    z_run(z, T, K, ring, out);
+    for (uint32_t p = z.flushed; p < z.n; p++) out[p] = ring[p & (kRing - 1)];
+    z.flushed = z.n;
+  }
+  *out_len = z.n;
+  return z.err;
+}
+
+}  // namespace inflate
+}  // namespace bsq

@@ -661,3 +661,141 @@ def bam_bytes(s: Sample, level: int = 6, block_payload: int = 0xFF00, seed: int 
         out.append(_bgzf_block(bytes(buf), level))
     out.append(BGZF_EOF)
     return b"".join(out)
+
+
+def bam_bytes_fast(s: Sample, level: int = 6, block_payload: int = 0xFF00, threads: int = 16,
+                   chunk: int = 65536) -> bytes:
+    """bam_bytes() for large samples: records assembled with numpy gathers, chunk by chunk, and the
+    BGZF blocks compressed on host threads.  Read names r0000000000.., tags X1:I when the redundancy
+    is not 1, XL:i / XR:i when present, XJ:C when set, RG:Z always."""
+    import struct
+    n = s.n_reads
+    ids, _, _ = bam_groups(s)
+    T = len(s.target_names)
+    text = "@HD\tVN:1.6\tSO:coordinate\n"
+    for t in range(T):
+        text += f"@SQ\tSN:{s.target_names[t]}\tLN:{int(s.target_offset[t + 1] - s.target_offset[t])}\n"
+    for g in ids:
+        text += f"@RG\tID:{g}\tLB:{g}\tSM:sample\n"
+    head = b"BAM\1" + struct.pack("<i", len(text)) + text.encode() + struct.pack("<i", T)
+    for t in range(T):
+        name = s.target_names[t].encode() + b"\0"
+        head += struct.pack("<i", len(name)) + name + struct.pack("<i", int(s.target_offset[t + 1] - s.target_offset[t]))
+    rg_str = [g.encode() + b"\0" for g in ids]
+    rg_bytes = np.frombuffer(b"".join(rg_str), dtype=np.uint8)
+    rg_off_tab = np.concatenate([[0], np.cumsum([len(x) for x in rg_str])]).astype(np.int64)
+    rg_len_tab = np.array([len(x) for x in rg_str], dtype=np.int64)
+    LNAME = 12   # "r" + 10 digits + NUL
+
+    def build(a, b):
+        """The records a..b-1 as bytes."""
+        m = b - a
+        L = s.l_qseq[a:b].astype(np.int64)
+        nc = s.n_cigar[a:b].astype(np.int64)
+        co = s.cigar_off[a:b].astype(np.int64)
+        so = s.seq_off[a:b].astype(np.int64)
+        nb = (L + 1) // 2
+        has_x1 = s.x1[a:b] != 1
+        has_xl = s.xl[a:b] >= 0
+        has_xr = s.xr[a:b] >= 0
+        has_xj = (s.xj[a:b] != 0) if s.xj is not None else np.zeros(m, bool)
+        rg = s.read_group[a:b].astype(np.int64)
+        rg_len = rg_len_tab[rg]
+        rec_len = 36 + LNAME + 4 * nc + nb + L + has_x1 * 7 + has_xl * 7 + has_xr * 7 + has_xj * 4 + 3 + rg_len
+        off = np.zeros(m + 1, dtype=np.int64)
+        off[1:] = np.cumsum(rec_len)
+        buf = np.zeros(int(off[-1]), dtype=np.uint8)
+
+        def put(dst, src, src_start, length):
+            tot = int(length.sum())
+            if tot == 0:
+                return
+            rep = np.repeat(np.arange(m), length)
+            k = np.arange(tot) - np.repeat(np.cumsum(length) - length, length)
+            buf[dst[rep] + k] = src[src_start[rep] + k]
+
+        def put_rows(dst, rows):
+            w = rows.shape[1]
+            buf[(dst[:, None] + np.arange(w)[None, :]).ravel()] = rows.ravel()
+
+        # bin (SAM/BAM specification §5.3) from the reference span
+        cig = s.cigar[co[0]: co[-1] + nc[-1]] if m else s.cigar[:0]
+        ops, lens = cig & 0xF, (cig >> 4).astype(np.int64)
+        refc = ((ops == 0) | (ops == 2) | (ops == 3) | (ops == 7) | (ops == 8)) * lens
+        starts = co - co[0]
+        rlen = np.add.reduceat(refc, starts) if len(refc) else np.zeros(m, np.int64)
+        rlen = np.where(nc > 0, rlen, 0)
+        pos = s.pos[a:b].astype(np.int64)
+        last = pos + np.maximum(rlen, 1) - 1
+        binv = np.zeros(m, dtype=np.int64)
+        done = np.zeros(m, bool)
+        for shift, o in ((14, 4681), (17, 585), (20, 73), (23, 9), (26, 1)):
+            hit = ~done & ((pos >> shift) == (last >> shift))
+            binv[hit] = o + (pos[hit] >> shift)
+            done |= hit
+        fixed = np.zeros(m, dtype=[("bs", "<i4"), ("ref", "<i4"), ("pos", "<i4"), ("ln", "u1"), ("mq", "u1"),
+                                   ("bin", "<u2"), ("nc", "<u2"), ("flag", "<u2"), ("ls", "<i4"), ("nref", "<i4"),
+                                   ("npos", "<i4"), ("tlen", "<i4")])
+        fixed["bs"] = rec_len - 4
+        fixed["ref"] = s.tid[a:b]
+        fixed["pos"] = s.pos[a:b]
+        fixed["ln"] = LNAME
+        fixed["mq"] = s.mapq[a:b]
+        fixed["bin"] = binv
+        fixed["nc"] = nc
+        fixed["flag"] = s.flag[a:b]
+        fixed["ls"] = L
+        fixed["nref"] = -1
+        fixed["npos"] = -1
+        cur = off[:-1].copy()
+        put_rows(cur, fixed.view(np.uint8).reshape(m, 36))
+        cur += 36
+        idx = np.arange(a, b, dtype=np.int64)
+        digits = np.zeros((m, LNAME), dtype=np.uint8)
+        digits[:, 0] = ord("r")
+        for d in range(10):
+            digits[:, 10 - d] = (idx // 10 ** d) % 10 + 48
+        put_rows(cur, digits)
+        cur += LNAME
+        put(cur, s.cigar.astype("<u4").view(np.uint8), co * 4, nc * 4)
+        cur += 4 * nc
+        seq = s.seq[so[0] // 2: (so[-1] + L[-1] + 1) // 2 + 1].copy() if m else s.seq[:0]
+        base = so[0] // 2 if m else 0
+        odd = np.nonzero((L & 1) == 1)[0]
+        seq[so[odd] // 2 + nb[odd] - 1 - base] &= 0xF0
+        put(cur, seq, so // 2 - base, nb)
+        cur += nb
+        put(cur, s.qual, so, L)
+        cur += L
+        for tag, has, fmt, vals in ((b"X1I", has_x1, "<u4", s.x1[a:b]), (b"XLi", has_xl, "<i4", s.xl[a:b]),
+                                    (b"XRi", has_xr, "<i4", s.xr[a:b])):
+            w = np.nonzero(has)[0]
+            if len(w):
+                v = np.zeros(len(w), dtype=[("t", "S3"), ("v", fmt)])
+                v["t"] = tag
+                v["v"] = vals[w]
+                put_rows(cur[w], v.view(np.uint8).reshape(len(w), 7))
+            cur += has * 7
+        w = np.nonzero(has_xj)[0]
+        if len(w):
+            put_rows(cur[w], np.tile(np.frombuffer(b"XJC\1", np.uint8), (len(w), 1)))
+        cur += has_xj * 4
+        put_rows(cur, np.tile(np.frombuffer(b"RGZ", np.uint8), (m, 1)))
+        cur += 3
+        put(cur, rg_bytes, rg_off_tab[rg], rg_len)
+        # record-aligned blocks of at most block_payload bytes
+        pieces, first = [], 0
+        while first < m:
+            j = int(np.searchsorted(off, off[first] + block_payload, side="right")) - 1
+            j = max(j, first + 1)
+            pieces.append(_bgzf_block(bytes(buf[off[first]:off[j]]), level))
+            first = j
+        return pieces
+
+    bounds = [(a, min(n, a + chunk)) for a in range(0, n, chunk)]
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        parts = list(ex.map(lambda ab: build(*ab), bounds))
+    out = [_bgzf_block(head[i:i + block_payload], level) for i in range(0, len(head), block_payload)]
+    for p in parts:
+        out += p
+    return b"".join(out + [BGZF_EOF])

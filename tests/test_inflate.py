@@ -1,4 +1,5 @@
-"""The library's DEFLATE decoder (breseq_gb300/csrc/bsq_inflate.cuh), compiled for the host, against
+"""The library's DEFLATE decoders (breseq_gb300/csrc/bsq_inflate.cuh: the bit-by-bit one and the
+resumable table-driven one the device uses, driven here through a 4 KiB ring), compiled for the host, against
 zlib (the inflater htslib uses under breseq) on random, repetitive and sequence-like data at every
 compression level and strategy, and on truncated or corrupted input, which must fail cleanly."""
 import ctypes as C
@@ -20,6 +21,9 @@ def lib():
     subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", SRC, "-o", OUT])
     L = C.CDLL(OUT)
     L.host_inflate.argtypes = [C.c_char_p, C.c_uint32, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)]
+    L.host_inflate_ring.argtypes = L.host_inflate.argtypes + [C.c_uint32]
+    L.host_crc_combine.argtypes = [C.c_uint32, C.c_uint32, C.c_uint64]
+    L.host_crc_combine.restype = C.c_uint32
     return L
 
 
@@ -41,9 +45,18 @@ def deflate(raw, level, strategy):
 STRATEGIES = [zlib.Z_DEFAULT_STRATEGY, zlib.Z_FIXED, zlib.Z_HUFFMAN_ONLY, zlib.Z_RLE]
 
 
+def run(lib, fn, comp, out, cap, got):
+    if fn == "host_inflate":
+        return lib.host_inflate(comp, len(comp), out, cap, C.byref(got))
+    # the ring decoder with the device's 2 KiB input window, and with a window barely above the margin
+    win = 2048 if fn == "ring" else 700
+    return lib.host_inflate_ring(comp, len(comp), out, cap, C.byref(got), win)
+
+
+@pytest.mark.parametrize("fn", ["host_inflate", "ring", "ring_small_window"])
 @pytest.mark.parametrize("level", [0, 1, 6, 9])
 @pytest.mark.parametrize("strategy", STRATEGIES, ids=["default", "fixed", "huffman", "rle"])
-def test_matches_zlib(lib, level, strategy):
+def test_matches_zlib(lib, fn, level, strategy):
     rng = random.Random(level * 10 + strategy)
     for n in [0, 1, 7, 300, 5000, 65536]:
         for kind in range(4):
@@ -51,7 +64,7 @@ def test_matches_zlib(lib, level, strategy):
             comp = deflate(raw, level, strategy)
             out = C.create_string_buffer(max(1, n))
             got = C.c_uint32()
-            assert lib.host_inflate(comp, len(comp), out, n, C.byref(got)) == 0
+            assert run(lib, fn, comp, out, n, got) == 0
             assert got.value == n and out.raw[:n] == raw
 
 
@@ -75,3 +88,26 @@ def test_bad_input_fails_cleanly(lib):
         for _ in range(2):
             b[rng.randrange(len(b))] ^= 1 << rng.randrange(8)
         assert lib.host_inflate(bytes(b), len(b), out, 65536, C.byref(got)) in range(0, 8)
+
+
+def test_ring_decoder_bad_input(lib):
+    rng = random.Random(9)
+    raw = payload(rng, 30000, 3)
+    comp = deflate(raw, 6, zlib.Z_DEFAULT_STRATEGY)
+    out = C.create_string_buffer(65536)
+    got = C.c_uint32()
+    assert run(lib, "ring", comp[: len(comp) // 2], out, 65536, got) != 0
+    assert run(lib, "ring", comp, out, 1000, got) == 5
+    for _ in range(200):
+        b = bytearray(comp)
+        b[rng.randrange(len(b))] ^= 1 << rng.randrange(8)
+        assert run(lib, "ring_small_window", bytes(b), out, 65536, got) in range(0, 8)
+
+
+def test_crc_combine(lib):
+    # crc(AB) from crc(A), crc(B) and |B|, as the device combines the 32 lanes' slices
+    rng = random.Random(3)
+    for _ in range(200):
+        a = payload(rng, rng.randrange(0, 3000), rng.randrange(4))
+        b = payload(rng, rng.randrange(0, 3000), rng.randrange(4))
+        assert lib.host_crc_combine(zlib.crc32(a), zlib.crc32(b), len(b)) == zlib.crc32(a + b)
