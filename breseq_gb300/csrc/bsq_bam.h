@@ -3,7 +3,8 @@
 // breseq opens reference.bam through htslib (src/breseq/pileup_base.cpp:61-88, 232-235): BGZF
 // blocks are inflated and the BAM records decoded on the host.  Here the file's bytes go to the
 // device and:
-//   1. every BGZF block is inflated by one thread (bsq_inflate.cuh) and its CRC-32 checked;
+//   1. every BGZF block is inflated by one warp (bsq_inflate.cuh): one lane decodes through a
+//      shared-memory ring that the warp flushes, and the 32 lanes check its CRC-32;
 //   2. one thread per block walks the records of its block (htslib's BAM writer starts a new block
 //      rather than split a record, so every block after the header starts at a record) and counts
 //      them; a second walk writes each record's offset;

@@ -109,26 +109,14 @@ BSQ_HD int code_decode(Bits& b, const Code& c) {
   return -1;
 }
 
-// Length symbols 257..285 and distance symbols 0..29: base values and extra bits (RFC 1951 §3.2.5).
+// Length symbols 257..285 and distance symbols 0..29: base values and extra bits (RFC 1951 §3.2.5),
+// from the tables' closed forms (a table in a function would be rebuilt at every call on the device).
+BSQ_HD int length_extra(int i) { return (i < 8 || i == 28) ? 0 : (i - 4) >> 2; }
 BSQ_HD uint32_t length_base(int i) {
-  const uint16_t t[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27, 31, 35, 43, 51, 59,
-                          67, 83, 99, 115, 131, 163, 195, 227, 258};
-  return t[i];
+  return i == 28 ? 258u : (i < 8 ? 3u + i : ((4u + (i & 3)) << length_extra(i)) + 3u);
 }
-BSQ_HD int length_extra(int i) {
-  const uint8_t t[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
-  return t[i];
-}
-BSQ_HD uint32_t dist_base(int i) {
-  const uint16_t t[30] = {1, 2, 3, 4, 5, 7, 9, 13, 17, 25, 33, 49, 65, 97, 129, 193, 257, 385, 513, 769,
-                          1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
-  return t[i];
-}
-BSQ_HD int dist_extra(int i) {
-  const uint8_t t[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11,
-                         12, 12, 13, 13};
-  return t[i];
-}
+BSQ_HD int dist_extra(int i) { return i < 4 ? 0 : (i - 2) >> 1; }
+BSQ_HD uint32_t dist_base(int i) { return i < 4 ? 1u + i : ((2u + (i & 1)) << dist_extra(i)) + 1u; }
 
 // Literal/length and distance symbols of one Huffman block until the end-of-block symbol.
 BSQ_HD int decode_symbols(Bits& b, const Code& lit, const Code& dist, uint8_t* out, uint32_t cap, uint32_t& n) {
@@ -241,7 +229,7 @@ namespace bsq {
 namespace inflate {
 
 // ----------------------------------------------------------------------------- resumable decoder
-// The same format, decoded with lookup tables (9 bits for literal/length codes, 8 for distances; a
+// The same format, decoded with lookup tables (10 bits for literal/length codes, 8 for distances; a
 // code longer than the table falls back to the canonical bit-by-bit decode) and suspended whenever
 // the staged output reaches a threshold or the staged input runs low, so a caller can move output
 // out of a small ring buffer and move more input in.  Output: positions [n - kRing, n) are in
@@ -250,7 +238,7 @@ namespace inflate {
 // at a step boundary when fewer than kInMargin bytes remain staged, more than any one step (a
 // dynamic block header, or a symbol with its extra bits) reads.
 
-constexpr int kLitBits = 9, kDistBits = 8;
+constexpr int kLitBits = 10, kDistBits = 8;
 constexpr uint32_t kRing = 4096;
 constexpr uint32_t kSuspend = kRing - 258 - 1;   // unflushed bytes at which decoding pauses
 constexpr uint32_t kInMargin = 640;              // staged input bytes below which decoding pauses
@@ -425,7 +413,7 @@ BSQ_HD void z_header(Inflater& z, Tables& T, Codes& K) {
 
 // Decodes until kSuspend bytes are unflushed, the stream ends (state 3) or an error.  ring holds the
 // recent output; out is read for back-references older than the ring.
-BSQ_HD void z_run(Inflater& z, Tables& T, Codes& K, uint8_t* ring, const uint8_t* out) {
+BSQ_HD void z_run_body(Inflater& z, Tables& T, Codes& K, uint8_t* ring, const uint8_t* out) {
   while (z.err == kOk && z.state != 3 && z.n - z.flushed < kSuspend && !z_input_low(z)) {
     if (z.state == 0) {
       z_header(z, T, K);
@@ -447,6 +435,21 @@ BSQ_HD void z_run(Inflater& z, Tables& T, Codes& K, uint8_t* ring, const uint8_t
       z.n++;
       z.stored_left--;
     } else {
+      // runs of literals whose codes are in the table, without the per-step checks above; the
+      // run stops where a step must (output or input low, a longer code, anything but a literal)
+      for (;;) {
+        if (z.cnt < kMaxBits) z_refill(z);
+        const uint16_t e = T.lit[z.buf & ((1u << kLitBits) - 1)];
+        const int l = e >> 9;
+        if (e == 0 || l > z.cnt || (e & 511) >= 256) break;
+        if (z.n >= z.cap) { z.err = kErrOutput; return; }
+        z.buf >>= l;
+        z.cnt -= l;
+        ring[z.n & (kRing - 1)] = (uint8_t)(e & 511);
+        z.n++;
+        if (z.n - z.flushed >= kSuspend || z_input_low(z)) break;
+      }
+      if (z.n - z.flushed >= kSuspend || z_input_low(z)) continue;
       const int sym = z_symbol(z, T.lit, kLitBits, K.lit_code);
       if (sym < 0) { if (!z.err) z.err = kErrCode; return; }
       if (sym < 256) {
@@ -492,6 +495,13 @@ BSQ_HD void z_run(Inflater& z, Tables& T, Codes& K, uint8_t* ring, const uint8_t
       }
     }
   }
+}
+
+// The decoder state is copied into a local for the run, so that it stays in registers.
+BSQ_HD void z_run(Inflater& state, Tables& T, Codes& K, uint8_t* ring, const uint8_t* out) {
+  Inflater z = state;
+  z_run_body(z, T, K, ring, out);
+  state = z;
 }
 
 // ----------------------------------------------------------------------------- CRC-32

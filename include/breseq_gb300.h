@@ -377,7 +377,7 @@ int bsq_write_soft_clipping_counts(const char* path, const char* const* target_n
 
 /* breseq reads reference.bam through htslib on the host (src/breseq/pileup_base.cpp:61-88,
  * 232-235): BGZF inflate, then record decode.  Here the file's bytes are uploaded once, every BGZF
- * block is inflated on the device by its own thread (its CRC-32 checked), and the records are
+ * block is inflated on the device by its own warp (its CRC-32 checked), and the records are
  * decoded there into the bsq_read_soa layout.  Records must not span BGZF blocks, which htslib's
  * writer guarantees for records under 64 KiB; a file that breaks this is refused (BSQ_ERR_INVALID).
  * Unplaced records (refID -1), which a coordinate-sorted file keeps last, are dropped. */
