@@ -283,6 +283,39 @@ def run_coverage(args, sc, sid, s):
                              "sample": f"positions 1-{n_cpu} of the same chromosome ({cpu_s:.2f} s)"}}
 
 
+def run_covfit(args, ec, s):
+    """The coverage-distribution fit (host threads) of every coverage group's unique-only histogram
+    from pass 1, against the oracle's sequential restatement."""
+    from breseq_gb300.api import fit_coverage_distribution
+    from oracle import pyoracle as po
+    groups = []
+    for g in range(s.n_coverage_groups):
+        h = np.ascontiguousarray(ec["hist"][g, : int(ec["hist_size"][g])])
+        length = int(sum(s.target_offset[t + 1] - s.target_offset[t] for t in range(len(s.target_offset) - 1)
+                         if s.coverage_group[t] == g))
+        groups.append((h, 0.05 / np.sqrt(float(length))))
+    for _ in range(args.warmup):
+        fits = [fit_coverage_distribution(h, deletion_propagation_pr_cutoff=pr) for h, pr in groups]
+    wall = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        fits = [fit_coverage_distribution(h, deletion_propagation_pr_cutoff=pr) for h, pr in groups]
+        wall.append(1e3 * (time.perf_counter() - t0))
+    t0 = time.perf_counter()
+    ofits = [po.fit_coverage_distribution(h, pr) for h, pr in groups]
+    cpu_s = time.perf_counter() - t0
+    same = all(a == b for a, b in zip(fits, ofits))
+    ms = statistics.mean(wall)
+    return {"workload": f"{WORKLOAD}: unique-only coverage histogram of each coverage group from pass 1",
+            "groups": len(groups), "host_threads": os.cpu_count(), "wall_ms": ms, "value": len(groups) / (ms / 1e3),
+            "unit": "fits/s",
+            "fits": [{k: f[k] for k in ("nbinom_mean", "nbinom_size", "deletion_coverage_propagation_cutoff",
+                                        "censor_start", "censor_end", "restarts_converged")} for f in fits],
+            "identical_to_oracle": bool(same),
+            "cpu_baseline": {"value": len(groups) / cpu_s, "unit": "fits/s", "cores": 1, "kind": "port",
+                             "sample": f"the same histograms, one sequential run ({cpu_s * 1e3:.0f} ms)"}}
+
+
 def run_softclip(args, device):
     """tabulate_soft_clipping_counts on a resident sample: device time of the call, its read pass
     (the dominant kernel), the end-to-end call from host buffers, and the oracle on the CPU."""
@@ -548,6 +581,7 @@ def run_ours(args, world, rank, local, pg):
     }
     if rank == 0 and not args.no_coverage:
         line["coverage_table"] = run_coverage(args, sc, sid, s)
+        line["coverage_fit"] = run_covfit(args, ec0, s)
     if rank == 0 and not args.no_cpu:
         rate, cb, dt, ln, reps = _cpu_reference(args.cpu_scale, os.cpu_count() or 1, args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",

@@ -105,6 +105,13 @@ def load():
     L.bsq_bam_decode.argtypes = [C.c_void_p, C.c_void_p, P(abi.BamGroups), P(C.c_uint64), P(C.c_uint64), P(C.c_uint64)]
     L.bsq_bam_copy_records.argtypes = [C.c_void_p, C.c_void_p, P(abi.ReadArrays)]
     L.bsq_bam_load.argtypes = [C.c_void_p, C.c_void_p, P(abi.Reference), P(C.c_int32)]
+    L.bsq_fit_coverage_distribution.argtypes = [P(C.c_uint64), C.c_uint32, C.c_double, C.c_int, P(abi.CoverageFit)]
+    L.bsq_fit_negative_binomial.argtypes = [P(C.c_double), C.c_uint32, C.c_int, P(C.c_double), P(C.c_double)]
+    L.bsq_nbinom_pmf.argtypes = [C.c_double, C.c_double, C.c_double]
+    L.bsq_nbinom_pmf.restype = C.c_double
+    L.bsq_nbinom_cdf.argtypes = [C.c_double, C.c_double, C.c_double]
+    L.bsq_nbinom_cdf.restype = C.c_double
+    L.bsq_nbinom_quantile.argtypes = [C.c_double, C.c_double, C.c_double, P(C.c_uint64)]
     _lib = L
     return L
 
@@ -123,4 +130,5 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_write_coverage_distribution", "bsq_write_coverage_table", "bsq_format_ra", "bsq_write_gd",
             "bsq_default_sc_params", "bsq_soft_clipping", "bsq_sc_result_copy", "bsq_write_soft_clipping_counts",
             "bsq_coverage_columns", "bsq_write_coverage_region", "bsq_bam_open", "bsq_bam_close", "bsq_bam_header",
-            "bsq_bam_decode", "bsq_bam_copy_records", "bsq_bam_load")
+            "bsq_bam_decode", "bsq_bam_copy_records", "bsq_bam_load", "bsq_fit_coverage_distribution",
+            "bsq_fit_negative_binomial", "bsq_nbinom_pmf", "bsq_nbinom_cdf", "bsq_nbinom_quantile")

@@ -315,6 +315,29 @@ def cov_columns(n: int):
     return arrs, st
 
 
+class CoverageFit(C.Structure):
+    _fields_ = [
+        ("nbinom_size", C.c_double),
+        ("nbinom_mean", C.c_double),
+        ("nbinom_prob", C.c_double),
+        ("nbinom_variance", C.c_double),
+        ("nbinom_relative_variance", C.c_double),
+        ("average", C.c_double),
+        ("variance", C.c_double),
+        ("relative_variance", C.c_double),
+        ("deletion_coverage_propagation_cutoff", C.c_double),
+        ("nbinom_scale", C.c_double),
+        ("censor_start", C.c_uint32),
+        ("censor_end", C.c_uint32),
+        ("restarts_converged", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
+def coverage_fit_dict(f: CoverageFit) -> dict:
+    return {name: getattr(f, name) for name, _ in CoverageFit._fields_ if name != "reserved"}
+
+
 SC_ROW_DTYPE = np.dtype([("target", np.uint32), ("position", np.uint32), ("direction", np.int32),
                          ("clipped_count", np.uint32), ("total_count", np.uint32), ("agree_count", np.uint32),
                          ("clipped_sequence", "S24")])

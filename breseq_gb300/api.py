@@ -356,6 +356,25 @@ def identify_mutations(sample, log10_table, device=0, **kw):
         return sc.identify_mutations(sid, log10_table, **kw)
 
 
+def fit_coverage_distribution(hist, sequence_length: int | None = None, deletion_propagation_pr_cutoff=None,
+                              n_threads: int = 0) -> dict:
+    """CoverageDistribution::fit + analyze_unique_coverage_distribution (src/breseq/coverage_distribution.cpp:
+    437-505, 519-588) on one coverage group's unique-only histogram, as error_count returns it
+    (hist[0 .. hist_size-1]).  The cutoff probability is breseq's 0.05 / sqrt(group length) unless given.
+    Host code; needs no GPU."""
+    h = np.ascontiguousarray(hist, dtype=np.uint64)
+    if deletion_propagation_pr_cutoff is None:
+        if not sequence_length:
+            raise ValueError("give sequence_length or deletion_propagation_pr_cutoff")
+        deletion_propagation_pr_cutoff = 0.05 / np.sqrt(float(sequence_length))
+    out = abi.CoverageFit()
+    rc = _lib.load().bsq_fit_coverage_distribution(abi.ptr(h, C.c_uint64), h.size, float(deletion_propagation_pr_cutoff),
+                                                  int(n_threads), C.byref(out))
+    if rc != 0:
+        raise RuntimeError(f"bsq_fit_coverage_distribution failed ({rc})")
+    return abi.coverage_fit_dict(out)
+
+
 class Server:
     """Continuous-batching scoring server (bsq_server_*): jobs are admitted by HBM footprint,
     uploaded while earlier jobs run, and every GPU round runs both passes over all resident jobs as

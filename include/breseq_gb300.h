@@ -1,7 +1,7 @@
 /*
  * breseq_gb300.h -- C ABI of the GB300 read-evidence scoring library (libbsq_gb300.so).
  *
- * The library replaces the three passes of breseq's read-evidence scoring path:
+ * The library replaces these parts of breseq's read-evidence scoring path:
  *
  *   error_count pileup      breseq: src/breseq/error_count.cpp:50-68 (error_count)
  *                                   src/breseq/error_count.cpp:125-199 (error_count_pileup::pileup_callback)
@@ -11,6 +11,9 @@
  *   coverage counts         breseq: src/breseq/error_count.cpp:239-253 (unique-only coverage histogram)
  *                                   src/breseq/identify_mutations.cpp:2173-2250 (coverage table rows)
  *   soft-clip tabulation    breseq: src/breseq/soft_clipping.cpp:285-666 (tabulate_soft_clipping_counts)
+ *   coverage fit (host)     breseq: src/breseq/coverage_distribution.cpp:115-505 (CoverageDistribution::fit)
+ *   BAM2COV table           breseq: src/breseq/coverage_output.cpp:190-470
+ *   BAM input               breseq: src/breseq/pileup_base.cpp:61-88, 232-235 (htslib decode)
  *
  * The reference exposes these passes as two C++ free functions that read a BAM/FASTA pair.  Here the
  * host decodes the alignments once into the struct-of-arrays record set `bsq_read_soa`, the library
@@ -260,6 +263,48 @@ int bsq_write_gd(const char* path, const bsq_reference* ref, const char* const* 
                  const double* deletion_propagation_cutoff, uint32_t precision_places,
                  const bsq_ra_record* ra, uint64_t n_ra, const bsq_ra_call* calls,
                  const bsq_mc_record* mc, uint64_t n_mc, const bsq_un_record* un, uint64_t n_un);
+
+/* ---------------------------------------------------------------- coverage-distribution fit */
+
+/* The negative-binomial fit of a coverage group's unique-only coverage histogram and the deletion-
+ * propagation cutoff breseq derives from it (CoverageDistribution::fit and
+ * analyze_unique_coverage_distribution, src/breseq/coverage_distribution.cpp:115-396, 437-505,
+ * 566-588).  Host code: 48 Nelder-Mead restarts on host threads, the result independent of their
+ * number.  Fields named after the Summary's unique_coverage entries; the nbinom_* parameters stay 0
+ * when the fit fails (nbinom_mean == 0). */
+typedef struct bsq_coverage_fit {
+    double   nbinom_size;               /* nbinom_size_parameter */
+    double   nbinom_mean;               /* nbinom_mean_parameter */
+    double   nbinom_prob;               /* size / (mean + size) */
+    double   nbinom_variance;           /* mean + mean^2 / size */
+    double   nbinom_relative_variance;  /* variance / mean */
+    double   average;                   /* histogram mean over coverage >= 1 */
+    double   variance;                  /* sample variance */
+    double   relative_variance;
+    double   deletion_coverage_propagation_cutoff;   /* -1: the sequences themselves are deleted */
+    double   nbinom_scale;              /* scales dnbinom to the histogram's counts (the plot's curve) */
+    uint32_t censor_start;              /* fitting window [censor_start, censor_end]; equal: no fit */
+    uint32_t censor_end;
+    uint32_t restarts_converged;        /* of the 48 restarts */
+    uint32_t reserved;
+} bsq_coverage_fit;
+
+/* hist / hist_size as bsq_ec_result gives them (the .tab file's rows 1 .. hist_size-1).
+ * deletion_propagation_pr_cutoff: breseq uses 0.05 / sqrt(total length of the group's sequences)
+ * (coverage_distribution.cpp:545).  n_threads <= 0: one per host core, at most 48.
+ * BSQ_ERR_DATA where the reference would stop on an assertion (a probability mass function evaluated
+ * at mean or size 0). */
+int bsq_fit_coverage_distribution(const uint64_t* hist, uint32_t hist_size, double deletion_propagation_pr_cutoff,
+                                  int n_threads, bsq_coverage_fit* out);
+/* fit_negative_binomial_histogram (coverage_distribution.cpp:402-409): n[0..max_index], n[0] ignored.
+ * Returns 1 when size and mu are both positive, 0 when the fit failed, < 0 on error. */
+int bsq_fit_negative_binomial(const double* n, uint32_t max_index, int n_threads, double* size, double* mu);
+/* The negative-binomial functions of src/breseq/stats.h:92-105 / stats.cpp:982-990, 2047-2072:
+ * R's dnbinom(k, size, mu=mu), the CDF P(X <= k) with success probability p (Cephes nbdtr), and
+ * qnbinom(target, size, mu=mu). */
+double bsq_nbinom_pmf(double k, double size, double mu);
+double bsq_nbinom_cdf(double k, double size, double p);
+int    bsq_nbinom_quantile(double target_pr, double size, double mu, uint64_t* k);
 
 /* ---------------------------------------------------------------- context API */
 

@@ -47,6 +47,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <map>
 #include <sstream>
@@ -1407,3 +1408,418 @@ extern "C" int oracle_write_coverage_region(const bsq_reference* ref, const bsq_
   fclose(f);
   return BSQ_OK;
 }
+
+// ======================================================================================= coverage fit
+// The censored negative-binomial fit of a unique-only coverage histogram and its deletion-propagation
+// cutoff, restated in the reference's own shape: per-bin dnbinom_mu calls, a std::function objective,
+// vector vertices ordered by std::sort, the 48 restarts in sequence.
+//   fit_censored_negative_binomial          src/breseq/coverage_distribution.cpp:115-319
+//   fit_coverage_distribution               src/breseq/coverage_distribution.cpp:341-396
+//   summary parameters                      src/breseq/coverage_distribution.cpp:566-588
+//   nelder_mead_minimize                    src/breseq/stats.cpp:2289-2381
+//   dnbinom_mu / qnbinom_mu / nbdtr         src/breseq/stats.h:92-100, stats.cpp:2047-2072, 982-990
+//   lngamma (ALGLIB form of Cephes lgam)    src/breseq/stats.cpp:534-650
+//   lgam / gamma / stirf / incbet / incbcf / incbd / pseries (Cephes 2.8)   stats.cpp:277-500, 1385-1700
+namespace ofit {
+
+const double MACHEP = 1.11022302462515654042E-16, MAXLOG = 7.09782712893383996732E2,
+             MINLOG = -7.451332191019412076235E2, MAXGAM = 171.624376956302725, BIG = 4.503599627370496e15,
+             BIGINV = 2.22044604925031308085e-16;
+
+double polevl(double x, const double* c, int n) {
+  double a = c[0];
+  for (int i = 1; i <= n; i++) a = a * x + c[i];
+  return a;
+}
+double p1evl(double x, const double* c, int n) {
+  double a = x + c[0];
+  for (int i = 1; i < n; i++) a = a * x + c[i];
+  return a;
+}
+
+double lngamma(double x) {   // x > 0
+  double z, p, u, q, a, b, c;
+  if (x < 13) {
+    z = 1; p = 0; u = x;
+    while (u >= 3) { p = p - 1; u = x + p; z = z * u; }
+    while (u < 2) { z = z / u; p = p + 1; u = x + p; }
+    if (u == 2) return log(z);
+    p = p - 2; x = x + p;
+    b = -1378.25152569120859100;
+    b = -38801.6315134637840924 + x * b;
+    b = -331612.992738871184744 + x * b;
+    b = -1162370.97492762307383 + x * b;
+    b = -1721737.00820839662146 + x * b;
+    b = -853555.664245765465627 + x * b;
+    c = 1;
+    c = -351.815701436523470549 + x * c;
+    c = -17064.2106651881159223 + x * c;
+    c = -220528.590553854454839 + x * c;
+    c = -1139334.44367982507207 + x * c;
+    c = -2532523.07177582951285 + x * c;
+    c = -2018891.41433532773231 + x * c;
+    p = x * b / c;
+    return log(z) + p;
+  }
+  q = (x - 0.5) * log(x) - x + 0.91893853320467274178;
+  if (x > 100000000) return q;
+  p = 1 / (x * x);
+  if (x >= 1000.0) return q + ((7.9365079365079365079365 * 0.0001 * p - 2.7777777777777777777778 * 0.001) * p +
+                               0.0833333333333333333333) / x;
+  a = 8.11614167470508450300 * 0.0001;
+  a = -5.95061904284301438324 * 0.0001 + p * a;
+  a = 7.93650340457716943945 * 0.0001 + p * a;
+  a = -2.77777777730099687205 * 0.001 + p * a;
+  a = 8.33333333333331927722 * 0.01 + p * a;
+  return q + a / x;
+}
+
+const double LA[] = {8.11614167470508450300E-4, -5.95061904284301438324E-4, 7.93650340457716943945E-4,
+                     -2.77777777730099687205E-3, 8.33333333333331927722E-2};
+const double LB[] = {-1.37825152569120859100E3, -3.88016315134637840924E4, -3.31612992738871184744E5,
+                     -1.16237097492762307383E6, -1.72173700820839662146E6, -8.53555664245765465627E5};
+const double LC[] = {-3.51815701436523470549E2, -1.70642106651881159223E4, -2.20528590553854454839E5,
+                     -1.13933444367982507207E6, -2.53252307177582951285E6, -2.01889141433532773231E6};
+double lgam(double x) {   // x > 0
+  double p, q, u, z;
+  if (x < 13.0) {
+    z = 1.0; p = 0.0; u = x;
+    while (u >= 3.0) { p -= 1.0; u = x + p; z *= u; }
+    while (u < 2.0) { z /= u; p += 1.0; u = x + p; }
+    if (u == 2.0) return log(z);
+    p -= 2.0; x = x + p;
+    p = x * polevl(x, LB, 5) / p1evl(x, LC, 6);
+    return log(z) + p;
+  }
+  if (x > 2.556348e305) return INFINITY;
+  q = (x - 0.5) * log(x) - x + 0.91893853320467274178;
+  if (x > 1.0e8) return q;
+  p = 1.0 / (x * x);
+  if (x >= 1000.0)
+    q += ((7.9365079365079365079365e-4 * p - 2.7777777777777777777778e-3) * p + 0.0833333333333333333333) / x;
+  else
+    q += polevl(p, LA, 4) / x;
+  return q;
+}
+
+const double GP[] = {1.60119522476751861407E-4, 1.19135147006586384913E-3, 1.04213797561761569935E-2,
+                     4.76367800457137231464E-2, 2.07448227648435975150E-1, 4.94214826801497100753E-1,
+                     9.99999999999999996796E-1};
+const double GQ[] = {-2.31581873324120129819E-5, 5.39605580493303397842E-4, -4.45641913851797240494E-3,
+                     1.18139785222060435552E-2, 3.58236398605498653373E-2, -2.34591795718243348568E-1,
+                     7.14304917030273074085E-2, 1.00000000000000000320E0};
+const double STIR[] = {7.87311395793093628397E-4, -2.29549961613378126380E-4, -2.68132617805781232825E-3,
+                       3.47222221605458667310E-3, 8.33333333333482257126E-2};
+double stirf(double x) {
+  double w = 1.0 / x;
+  w = 1.0 + w * polevl(w, STIR, 4);
+  double y = exp(x);
+  if (x > 143.01608) {
+    double v = pow(x, 0.5 * x - 0.25);
+    y = v * (v / y);
+  } else {
+    y = pow(x, x - 0.5) / y;
+  }
+  return 2.50662827463100050242E0 * y * w;
+}
+double gamma_(double x) {   // x > 0
+  if (x > 33.0) return 1 * stirf(x);
+  double z = 1.0;
+  while (x >= 3.0) { x -= 1.0; z *= x; }
+  while (x < 2.0) {
+    if (x < 1.e-9) goto small;
+    z /= x;
+    x += 1.0;
+  }
+  if (x == 2.0) return z;
+  x -= 2.0;
+  return z * polevl(x, GP, 6) / polevl(x, GQ, 7);
+small:
+  if (x == 0.0) return INFINITY;
+  return z / ((1.0 + 0.5772156649015329 * x) * x);
+}
+
+double incbcf(double a, double b, double x) {
+  double xk, pk, pkm1, pkm2, qk, qkm1, qkm2, k1, k2, k3, k4, k5, k6, k7, k8, r, t, ans, thresh;
+  int n;
+  k1 = a; k2 = a + b; k3 = a; k4 = a + 1.0; k5 = 1.0; k6 = b - 1.0; k7 = k4; k8 = a + 2.0;
+  pkm2 = 0.0; qkm2 = 1.0; pkm1 = 1.0; qkm1 = 1.0; ans = 1.0; r = 1.0; n = 0; thresh = 3.0 * MACHEP;
+  do {
+    xk = -(x * k1 * k2) / (k3 * k4);
+    pk = pkm1 + pkm2 * xk; qk = qkm1 + qkm2 * xk;
+    pkm2 = pkm1; pkm1 = pk; qkm2 = qkm1; qkm1 = qk;
+    xk = (x * k5 * k6) / (k7 * k8);
+    pk = pkm1 + pkm2 * xk; qk = qkm1 + qkm2 * xk;
+    pkm2 = pkm1; pkm1 = pk; qkm2 = qkm1; qkm1 = qk;
+    if (qk != 0) r = pk / qk;
+    if (r != 0) { t = fabs((ans - r) / r); ans = r; } else t = 1.0;
+    if (t < thresh) return ans;
+    k1 += 1.0; k2 += 1.0; k3 += 2.0; k4 += 2.0; k5 += 1.0; k6 -= 1.0; k7 += 2.0; k8 += 2.0;
+    if ((fabs(qk) + fabs(pk)) > BIG) { pkm2 *= BIGINV; pkm1 *= BIGINV; qkm2 *= BIGINV; qkm1 *= BIGINV; }
+    if ((fabs(qk) < BIGINV) || (fabs(pk) < BIGINV)) { pkm2 *= BIG; pkm1 *= BIG; qkm2 *= BIG; qkm1 *= BIG; }
+  } while (++n < 300);
+  return ans;
+}
+double incbd(double a, double b, double x) {
+  double xk, pk, pkm1, pkm2, qk, qkm1, qkm2, k1, k2, k3, k4, k5, k6, k7, k8, r, t, ans, z, thresh;
+  int n;
+  k1 = a; k2 = b - 1.0; k3 = a; k4 = a + 1.0; k5 = 1.0; k6 = a + b; k7 = a + 1.0; k8 = a + 2.0;
+  pkm2 = 0.0; qkm2 = 1.0; pkm1 = 1.0; qkm1 = 1.0; z = x / (1.0 - x); ans = 1.0; r = 1.0; n = 0;
+  thresh = 3.0 * MACHEP;
+  do {
+    xk = -(z * k1 * k2) / (k3 * k4);
+    pk = pkm1 + pkm2 * xk; qk = qkm1 + qkm2 * xk;
+    pkm2 = pkm1; pkm1 = pk; qkm2 = qkm1; qkm1 = qk;
+    xk = (z * k5 * k6) / (k7 * k8);
+    pk = pkm1 + pkm2 * xk; qk = qkm1 + qkm2 * xk;
+    pkm2 = pkm1; pkm1 = pk; qkm2 = qkm1; qkm1 = qk;
+    if (qk != 0) r = pk / qk;
+    if (r != 0) { t = fabs((ans - r) / r); ans = r; } else t = 1.0;
+    if (t < thresh) return ans;
+    k1 += 1.0; k2 -= 1.0; k3 += 2.0; k4 += 2.0; k5 += 1.0; k6 += 1.0; k7 += 2.0; k8 += 2.0;
+    if ((fabs(qk) + fabs(pk)) > BIG) { pkm2 *= BIGINV; pkm1 *= BIGINV; qkm2 *= BIGINV; qkm1 *= BIGINV; }
+    if ((fabs(qk) < BIGINV) || (fabs(pk) < BIGINV)) { pkm2 *= BIG; pkm1 *= BIG; qkm2 *= BIG; qkm1 *= BIG; }
+  } while (++n < 300);
+  return ans;
+}
+double pseries(double a, double b, double x) {
+  double s, t, u, v, n, t1, z, ai;
+  ai = 1.0 / a; u = (1.0 - b) * x; v = u / (a + 1.0); t1 = v; t = u; n = 2.0; s = 0.0; z = MACHEP * ai;
+  while (fabs(v) > z) { u = (n - b) * x / n; t *= u; v = t / (a + n); s += v; n += 1.0; }
+  s += t1;
+  s += ai;
+  u = a * log(x);
+  if ((a + b) < MAXGAM && fabs(u) < MAXLOG) {
+    t = gamma_(a + b) / (gamma_(a) * gamma_(b));
+    s = s * t * pow(x, a);
+  } else {
+    t = lgam(a + b) - lgam(a) - lgam(b) + u + log(s);
+    if (t < MINLOG) s = 0.0; else s = exp(t);
+  }
+  return s;
+}
+double incbet(double aa, double bb, double xx) {
+  double a, b, t, x, xc, w, y;
+  int flag;
+  if (aa <= 0.0 || bb <= 0.0) return 0.0;
+  if ((xx <= 0.0) || (xx >= 1.0)) {
+    if (xx == 0.0) return 0.0;
+    if (xx == 1.0) return 1.0;
+    return 0.0;
+  }
+  flag = 0;
+  if ((bb * xx) <= 1.0 && xx <= 0.95) { t = pseries(aa, bb, xx); goto done; }
+  w = 1.0 - xx;
+  if (xx > (aa / (aa + bb))) { flag = 1; a = bb; b = aa; xc = xx; x = w; }
+  else { a = aa; b = bb; xc = w; x = xx; }
+  if (flag == 1 && (b * x) <= 1.0 && x <= 0.95) { t = pseries(a, b, x); goto done; }
+  y = x * (a + b - 2.0) - (a - 1.0);
+  if (y < 0.0) w = incbcf(a, b, x); else w = incbd(a, b, x) / xc;
+  y = a * log(x);
+  t = b * log(xc);
+  if ((a + b) < MAXGAM && fabs(y) < MAXLOG && fabs(t) < MAXLOG) {
+    t = pow(xc, b); t *= pow(x, a); t /= a; t *= w;
+    t *= gamma_(a + b) / (gamma_(a) * gamma_(b));
+    goto done;
+  }
+  y += t + lgam(a + b) - lgam(a) - lgam(b);
+  y += log(w / a);
+  if (y < MINLOG) t = 0.0; else t = exp(y);
+done:
+  if (flag == 1) { if (t <= MACHEP) t = 1.0 - MACHEP; else t = 1.0 - t; }
+  return t;
+}
+double nbdtr(double k, double n, double p) { return incbet(n, k + 1, p); }
+double dnbinom_mu(double k, double size, double mu) {
+  double p = size / (size + mu);
+  double log_pmf = lngamma(k + size) - lngamma(size) - lngamma(k + 1) + size * log(p) + k * log(1.0 - p);
+  return exp(log_pmf);
+}
+uint32_t qnbinom_mu(double target_pr, double size, double mu) {
+  double p = size / (size + mu);
+  if (target_pr <= 0.0) return 0;
+  uint64_t hi = 1;
+  while (nbdtr((double)hi, size, p) < target_pr) hi *= 2;
+  uint64_t lo = hi / 2;
+  while (lo < hi) {
+    uint64_t mid = lo + (hi - lo) / 2;
+    if (nbdtr((double)mid, size, p) < target_pr) lo = mid + 1; else hi = mid;
+  }
+  return (uint32_t)lo;
+}
+
+struct NM { std::vector<double> estimate; bool converged; };
+NM nelder_mead(const std::function<double(const std::vector<double>&)>& f, const std::vector<double>& init) {
+  const size_t n = init.size();
+  const uint32_t max_iterations = 1000;
+  const double tolerance = 1e-8;
+  std::vector<std::vector<double>> simplex(n + 1, init);
+  for (size_t i = 0; i < n; i++) simplex[i + 1][i] += (init[i] != 0.0) ? 0.05 * fabs(init[i]) : 0.00025;
+  std::vector<double> values(n + 1);
+  for (size_t i = 0; i <= n; i++) values[i] = f(simplex[i]);
+  bool converged = false;
+  for (uint32_t iter = 0; iter < max_iterations; iter++) {
+    std::vector<size_t> order(n + 1);
+    for (size_t i = 0; i <= n; i++) order[i] = i;
+    std::sort(order.begin(), order.end(), [&values](size_t l, size_t r) { return values[l] < values[r]; });
+    std::vector<std::vector<double>> ss(n + 1);
+    std::vector<double> sv(n + 1);
+    for (size_t i = 0; i <= n; i++) { ss[i] = simplex[order[i]]; sv[i] = values[order[i]]; }
+    simplex = ss;
+    values = sv;
+    if ((values[n] - values[0]) < tolerance) { converged = true; break; }
+    std::vector<double> c(n, 0.0);
+    for (size_t i = 0; i < n; i++) for (size_t j = 0; j < n; j++) c[j] += simplex[i][j];
+    for (size_t j = 0; j < n; j++) c[j] /= (double)n;
+    std::vector<double> r(n);
+    for (size_t j = 0; j < n; j++) r[j] = c[j] + 1.0 * (c[j] - simplex[n][j]);
+    double fr = f(r);
+    if (fr < values[0]) {
+      std::vector<double> e(n);
+      for (size_t j = 0; j < n; j++) e[j] = c[j] + 2.0 * (r[j] - c[j]);
+      double fe = f(e);
+      if (fe < fr) { simplex[n] = e; values[n] = fe; } else { simplex[n] = r; values[n] = fr; }
+    } else if (fr < values[n - 1]) {
+      simplex[n] = r; values[n] = fr;
+    } else {
+      std::vector<double> k(n);
+      for (size_t j = 0; j < n; j++) k[j] = c[j] + 0.5 * (simplex[n][j] - c[j]);
+      double fk = f(k);
+      if (fk < values[n]) { simplex[n] = k; values[n] = fk; }
+      else {
+        for (size_t i = 1; i <= n; i++) {
+          for (size_t j = 0; j < n; j++) simplex[i][j] = simplex[0][j] + 0.5 * (simplex[i][j] - simplex[0][j]);
+          values[i] = f(simplex[i]);
+        }
+      }
+    }
+  }
+  size_t best = 0;
+  for (size_t i = 1; i <= n; i++) if (values[i] < values[best]) best = i;
+  return NM{simplex[best], converged && std::isfinite(values[best])};
+}
+
+}  // namespace ofit
+
+extern "C" int oracle_fit_coverage_distribution(const uint64_t* hist, uint32_t hist_size, double cutoff_pr,
+                                                bsq_coverage_fit* out) {
+  using namespace ofit;
+  memset(out, 0, sizeof(*out));
+  const uint32_t N = hist_size ? hist_size - 1 : 0;
+  std::vector<double> n((size_t)N + 1, 0.0);
+  for (uint32_t i = 1; i <= N; i++) n[i] = (double)hist[i];
+  double nb_mu = 0, nb_size = 0, m = 0, v = 0, scale = 0;
+  uint32_t cs = 0, ce = 0, n_conv = 0;
+  [&]() {
+    double total_positions = 0;
+    for (uint32_t i = 1; i <= N; i++) total_positions += n[i];
+    if (total_positions == 0) return;
+    for (uint32_t i = 1; i <= N; i++) m += i * n[i];
+    m /= total_positions;
+    if (total_positions > 1) {
+      for (uint32_t i = 1; i <= N; i++) v += n[i] * (i - m) * (i - m);
+      v /= (total_positions - 1);
+    }
+    std::vector<double> ma(N + 1, 0.0);
+    std::vector<bool> ma_valid(N + 1, false);
+    if (N >= 5) {
+      for (uint32_t i = 3; i <= N - 2; i++) { ma[i] = (n[i - 2] + n[i - 1] + n[i] + n[i + 1] + n[i + 2]) / 5.0; ma_valid[i] = true; }
+    } else {
+      for (uint32_t i = 1; i <= N; i++) { ma[i] = n[i]; ma_valid[i] = true; }
+    }
+    uint32_t min_i = std::max((uint32_t)(m / 4.0), (uint32_t)1);
+    double max_n = 0;
+    uint32_t max_i = 0;
+    for (uint32_t i = min_i; i <= N; i++) if (ma_valid[i] && ma[i] > max_n) { max_n = ma[i]; max_i = i; }
+    uint32_t start_i = std::max((uint32_t)floor(max_i * 0.5), (uint32_t)1);
+    uint32_t end_i = std::min((uint32_t)ceil(max_i * 1.5), N);
+    if (start_i == end_i) return;
+    cs = start_i;
+    ce = end_i;
+    uint32_t npb = (end_i - start_i) / 1000;
+    std::vector<double> x;
+    uint32_t s0, e0;
+    if (npb > 1) {
+      s0 = start_i / npb;
+      e0 = (uint32_t)ceil((double)end_i / npb);
+      x.assign(e0 + 1, 0.0);
+      for (uint32_t i = s0; i <= e0; i++)
+        for (uint32_t j = 1; j <= npb; j++) { uint32_t idx = i * npb + j; if (idx <= N) x[i] += n[idx]; }
+    } else {
+      npb = 1; s0 = start_i; e0 = end_i;
+      x.assign(e0 + 1, 0.0);
+      for (uint32_t i = 1; i <= e0; i++) x[i] = n[i];
+    }
+    double inner_total = 0;
+    for (uint32_t i = s0; i <= e0; i++) inner_total += x[i];
+    double num = 0, den = 0;
+    for (uint32_t i = 1; i <= e0; i++) { num += i * x[i]; den += x[i]; }
+    double mean_estimate = num / den;
+    auto f_nb = [&](const std::vector<double>& par) -> double {
+      double mu = exp(par[0]), size = exp(par[1]);
+      if (!std::isfinite(mu) || !std::isfinite(size)) return 1e10;
+      std::vector<double> dist(e0 + 1, 0.0);
+      double total = 0;
+      for (uint32_t i = s0; i <= e0; i++) { dist[i] = dnbinom_mu((double)i, size, mu); total += dist[i]; }
+      if (!(total > 0) || !std::isfinite(total)) return 1e10;
+      double l = 0;
+      for (uint32_t i = s0; i <= e0; i++) { double d = (x[i] / inner_total) - (dist[i] / total); l += d * d; }
+      return std::isfinite(l) ? l : 1e10;
+    };
+    std::vector<double> tm = {mean_estimate, (double)e0, (double)s0, 1.0 * (e0 + s0) / 4.0, 2.0 * (e0 + s0) / 4.0,
+                              3.0 * (e0 + s0) / 4.0};
+    double best = HUGE_VAL;
+    for (double mean : tm) {
+      double ts = 100000;
+      for (int k = 0; k < 8; k++) {
+        ts /= 10.0;
+        NM r = nelder_mead(f_nb, {log(mean), log(ts)});
+        if (!r.converged) continue;
+        n_conv++;
+        double obj = f_nb(r.estimate);
+        if (obj < best) { best = obj; nb_mu = exp(r.estimate[0]); nb_size = exp(r.estimate[1]); }
+      }
+    }
+    if (!(best < HUGE_VAL)) nb_mu = nb_size = 0;
+    double inc = 0;
+    if (nb_mu > 0) {
+      double p = nb_size / (nb_size + nb_mu);
+      inc = nbdtr((double)e0, nb_size, p) - nbdtr((double)s0, nb_size, p);
+      if (inc >= 0.01 && npb > 1) nb_mu = nb_mu * npb;
+    }
+    if (inc < 0.01) nb_mu = nb_size = 0;
+    if (nb_mu > 0) scale = inner_total / inc;
+  }();
+  double dpc;
+  if (nb_mu > 0) {
+    dpc = (double)qnbinom_mu(cutoff_pr, nb_size, nb_mu);
+  } else {
+    double se = (1.0 / (v - m)) * m * m;
+    dpc = ((se > 0) && std::isfinite(se)) ? (double)qnbinom_mu(cutoff_pr, se, m) : -1;
+    if (!(dpc >= 1)) dpc = m * 0.1;
+  }
+  if (dpc < 1) dpc = 1;
+  if ((nb_mu <= 3) && (m <= 3)) dpc = -1;
+  out->nbinom_size = nb_size;
+  out->nbinom_mean = nb_mu;
+  if (nb_mu != 0) {
+    out->nbinom_prob = nb_size / (nb_mu + nb_size);
+    out->nbinom_variance = nb_mu + pow(nb_mu, 2) / nb_size;
+    out->nbinom_relative_variance = out->nbinom_variance / nb_mu;
+  }
+  out->average = m;
+  out->variance = v;
+  out->relative_variance = (m > 0) ? v / m : 0.0;
+  out->deletion_coverage_propagation_cutoff = dpc;
+  out->nbinom_scale = scale;
+  out->censor_start = cs;
+  out->censor_end = ce;
+  out->restarts_converged = n_conv;
+  return BSQ_OK;
+}
+
+extern "C" double oracle_nbinom_pmf(double k, double size, double mu) { return ofit::dnbinom_mu(k, size, mu); }
+extern "C" double oracle_nbinom_cdf(double k, double size, double p) { return ofit::nbdtr(k, size, p); }
+extern "C" double oracle_lgam(double x) { return ofit::lgam(x); }
+extern "C" double oracle_lngamma(double x) { return ofit::lngamma(x); }
+extern "C" double oracle_gamma(double x) { return ofit::gamma_(x); }

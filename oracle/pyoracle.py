@@ -38,6 +38,12 @@ def lib():
         L.oracle_sc_summary.argtypes = [C.c_void_p, C.POINTER(abi.ScSummary)]
         L.oracle_sc_rows.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_sc_free.argtypes = [C.c_void_p]
+        L.oracle_fit_coverage_distribution.argtypes = [C.POINTER(C.c_uint64), C.c_uint32, C.c_double,
+                                                       C.POINTER(abi.CoverageFit)]
+        for name, n in (("oracle_nbinom_pmf", 3), ("oracle_nbinom_cdf", 3), ("oracle_lgam", 1), ("oracle_lngamma", 1),
+                        ("oracle_gamma", 1)):
+            getattr(L, name).argtypes = [C.c_double] * n
+            getattr(L, name).restype = C.c_double
         L.oracle_coverage_columns.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.c_uint32, C.c_uint32,
                                               C.c_uint32, C.POINTER(abi.CovColumns), C.POINTER(C.c_uint32), C.c_char_p,
                                               C.c_int]
@@ -200,3 +206,17 @@ def write_coverage_region(sample, path, tid, start, end, resolution=600, total_o
                                             avg, err, 256)
     if rc != 0:
         raise OracleError(f"oracle_write_coverage_region failed ({rc}): {err.value.decode()}")
+
+
+def fit_coverage_distribution(hist, deletion_propagation_pr_cutoff):
+    """CoverageDistribution::fit on a unique-only histogram hist[0 .. size-1] (single-threaded)."""
+    h = np.ascontiguousarray(hist, dtype=np.uint64)
+    out = abi.CoverageFit()
+    lib().oracle_fit_coverage_distribution(abi.ptr(h, C.c_uint64), h.size, float(deletion_propagation_pr_cutoff),
+                                           C.byref(out))
+    return abi.coverage_fit_dict(out)
+
+
+def special(name, *args):
+    """nbinom_pmf / nbinom_cdf / lgam / lngamma / gamma of the restatement."""
+    return getattr(lib(), "oracle_" + name)(*[float(a) for a in args])
