@@ -316,6 +316,53 @@ def run_covfit(args, ec, s):
                              "sample": f"the same histograms, one sequential run ({cpu_s * 1e3:.0f} ms)"}}
 
 
+def run_pairs(args, device, s):
+    """Discordant-pair and missing-pair candidate scans (bsq_pair_candidates) on the headline sample
+    with pair annotations (discordant and mate-unmapped pairs planted near breakpoints and at a
+    background rate): device time, the classification pass over every read (the dominant kernel),
+    the host replay, and the oracle's position-by-position walk on the CPU."""
+    from breseq_gb300 import synth
+    from breseq_gb300.api import PairSettings, Scorer
+    from oracle import pyoracle as po
+    sp = synth.with_pairs(s, seed=31, discordant_sites=40, unmapped_sites=40)
+    st = PairSettings(dp_group=tuple([0] * (int(sp.read_group.max()) + 1)), window_width=(462.75,),
+                      predict_missing_pairs=True)
+    with Scorer(device) as sc:
+        sid = sc.load_sample(sp)
+        for _ in range(args.warmup):
+            r = sc.pair_candidates(sid, st)
+        dev, main, wall = [], [], []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            r = sc.pair_candidates(sid, st)
+            wall.append(1e3 * (time.perf_counter() - t0))
+            ps = sc.last_pass_stats()
+            dev.append(ps["device_ms"]); main.append(ps["main_kernel_ms"])
+        launches = ps["kernel_launches"]
+        with tempfile.TemporaryDirectory() as d:
+            dp, mp, odp, omp = (os.path.join(d, f) for f in ("dp", "mp", "odp", "omp"))
+            sc.write_pair_candidates(r, dp, mp, sp.target_names)
+            t0 = time.perf_counter()
+            po.pair_candidates(sp, st, odp, omp)
+            cpu_s = time.perf_counter() - t0
+            same = open(dp).read() == open(odp).read() and open(mp).read() == open(omp).read()
+        sc.free_sample(sid)
+    n = sp.n_reads
+    ms, kms = statistics.mean(dev), statistics.mean(main)
+    hbm, peak_kind = _peaks()
+    kbytes = 47 * n   # per read: 32-byte record, flag, XP, read group read; code, group, two selections written
+    return {"workload": f"{WORKLOAD} with pair annotations", "reads": n, "dp_regions": len(r["dp"]),
+            "mp_regions": len(r["mp"]), "device_ms": ms, "wall_ms": statistics.mean(wall),
+            "host_replay_ms": statistics.mean(wall) - ms, "kernel_launches": launches,
+            "value": n / (statistics.mean(wall) / 1e3), "unit": "records/s",
+            "roofline": {"bound": "hbm", "kernel": "pair_classify_kernel", "achieved": kbytes / (kms / 1e3) / 1e9,
+                         "peak": hbm, "unit": "GB/s", "frac": kbytes / (kms / 1e3) / 1e9 / hbm, "kernel_ms": kms,
+                         "algorithmic_bytes": kbytes, "peak_kind": peak_kind, "traffic": None},
+            "identical_to_oracle": bool(same),
+            "cpu_baseline": {"value": n / cpu_s, "unit": "records/s", "cores": 1, "kind": "port",
+                             "sample": f"the same sample, one position-by-position walk ({cpu_s:.2f} s)"}}
+
+
 def run_softclip(args, device):
     """tabulate_soft_clipping_counts on a resident sample: device time of the call, its read pass
     (the dominant kernel), the end-to-end call from host buffers, and the oracle on the CPU."""
@@ -595,6 +642,8 @@ def run_ours(args, world, rank, local, pg):
         line["bam_input"] = run_bam(args, local, s)
     if rank == 0 and not args.no_softclip:
         line["soft_clipping"] = run_softclip(args, local)
+    if rank == 0 and not args.no_pairs:
+        line["pair_scans"] = run_pairs(args, local, s)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -742,6 +791,7 @@ def main():
     ap.add_argument("--no-softclip", action="store_true", help="skip the soft-clipping leg")
     ap.add_argument("--no-coverage", action="store_true", help="skip the coverage-table leg")
     ap.add_argument("--no-bam", action="store_true", help="skip the BAM-input leg")
+    ap.add_argument("--no-pairs", action="store_true", help="skip the discordant / missing-pair leg")
     args = ap.parse_args()
     world, rank, local, pg = _dist()
     if args.impl == "reference":

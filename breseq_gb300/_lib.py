@@ -105,6 +105,13 @@ def load():
     L.bsq_bam_decode.argtypes = [C.c_void_p, C.c_void_p, P(abi.BamGroups), P(C.c_uint64), P(C.c_uint64), P(C.c_uint64)]
     L.bsq_bam_copy_records.argtypes = [C.c_void_p, C.c_void_p, P(abi.ReadArrays)]
     L.bsq_bam_load.argtypes = [C.c_void_p, C.c_void_p, P(abi.Reference), P(C.c_int32)]
+    L.bsq_bam_name_bytes.argtypes = [C.c_void_p, C.c_void_p, P(C.c_uint64)]
+    L.bsq_pair_candidates.argtypes = [C.c_void_p, C.c_int32, P(abi.PairParams), P(C.c_uint64), P(C.c_uint64),
+                                      P(C.c_uint64)]
+    L.bsq_pair_result_copy.argtypes = [C.c_void_p, P(abi.PairRegion), C.c_uint64, P(abi.PairRegion), C.c_uint64,
+                                       C.c_char_p, C.c_uint64]
+    for fn in (L.bsq_write_dp_candidate_regions, L.bsq_write_mp_candidate_regions):
+        fn.argtypes = [C.c_char_p, P(C.c_char_p), P(abi.PairRegion), C.c_uint64, C.c_char_p]
     L.bsq_fit_coverage_distribution.argtypes = [P(C.c_uint64), C.c_uint32, C.c_double, C.c_int, P(abi.CoverageFit)]
     L.bsq_fit_negative_binomial.argtypes = [P(C.c_double), C.c_uint32, C.c_int, P(C.c_double), P(C.c_double)]
     L.bsq_nbinom_pmf.argtypes = [C.c_double, C.c_double, C.c_double]
@@ -131,4 +138,6 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_default_sc_params", "bsq_soft_clipping", "bsq_sc_result_copy", "bsq_write_soft_clipping_counts",
             "bsq_coverage_columns", "bsq_write_coverage_region", "bsq_bam_open", "bsq_bam_close", "bsq_bam_header",
             "bsq_bam_decode", "bsq_bam_copy_records", "bsq_bam_load", "bsq_fit_coverage_distribution",
-            "bsq_fit_negative_binomial", "bsq_nbinom_pmf", "bsq_nbinom_cdf", "bsq_nbinom_quantile")
+            "bsq_fit_negative_binomial", "bsq_nbinom_pmf", "bsq_nbinom_cdf", "bsq_nbinom_quantile",
+            "bsq_bam_name_bytes", "bsq_pair_candidates", "bsq_pair_result_copy", "bsq_write_dp_candidate_regions",
+            "bsq_write_mp_candidate_regions")

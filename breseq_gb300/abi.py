@@ -42,6 +42,46 @@ class ReadSoA(C.Structure):
         ("n_cigar_total", C.c_uint64),
         ("n_bases_total", C.c_uint64),
         ("xj", P(C.c_uint8)),
+        ("isize", P(C.c_int32)),
+        ("xp", P(C.c_uint8)),
+        ("qname_off", P(C.c_uint64)),
+        ("qname", C.c_void_p),
+    ]
+
+
+XP_CODES = {"FR": 0, "RF": 1, "FF": 2}
+XP_NONE = 3
+
+
+class PairParams(C.Structure):
+    _fields_ = [
+        ("n_read_groups", C.c_uint32),
+        ("dp_group", P(C.c_int32)),
+        ("n_dp_groups", C.c_uint32),
+        ("window_width", P(C.c_double)),
+        ("r1_name_prefix", P(C.c_uint32)),
+        ("r2_name_prefix", P(C.c_uint32)),
+        ("discordant_pair_seed", C.c_int32),
+        ("predict_missing_pairs", C.c_int32),
+        ("missing_pair_seed", C.c_int32),
+        ("missing_pair_seed_fraction", C.c_double),
+        ("deletion_propagation_cutoff", P(C.c_double)),
+    ]
+
+
+class PairRegion(C.Structure):
+    _fields_ = [
+        ("target", C.c_uint32),
+        ("start", C.c_uint32),
+        ("end", C.c_uint32),
+        ("strand", C.c_char),
+        ("orientation", C.c_char * 3),
+        ("max_count", C.c_uint32),
+        ("max_total", C.c_uint32),
+        ("redundant", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("text_off", C.c_uint64),
+        ("text_len", C.c_uint64),
     ]
 
 
@@ -258,6 +298,12 @@ class SampleView:
         xj = getattr(s, "xj", None)
         if xj is not None:
             kw["xj"] = ptr(k(xj, np.uint8), C.c_uint8)
+        if getattr(s, "xp", None) is not None:
+            kw["isize"] = ptr(k(s.isize, np.int32), C.c_int32)
+            kw["xp"] = ptr(k(s.xp, np.uint8), C.c_uint8)
+            kw["qname_off"] = ptr(k(s.qname_off, np.uint64), C.c_uint64)
+            kw["qname"] = k(np.frombuffer(bytes(s.qname), dtype=np.uint8) if not isinstance(s.qname, np.ndarray)
+                            else s.qname, np.uint8).ctypes.data
         self.reads = ReadSoA(n_reads=int(len(s.tid)), n_cigar_total=int(len(s.cigar)),
                              n_bases_total=int(len(s.qual)), **kw)
 
@@ -278,7 +324,8 @@ class BamGroups(C.Structure):
 READ_ARRAY_FIELDS = (("tid", np.int32), ("pos", np.int32), ("flag", np.uint16), ("mapq", np.uint8), ("x1", np.uint32),
                      ("xl", np.int32), ("xr", np.int32), ("read_file", np.uint8), ("read_group", np.uint16),
                      ("l_qseq", np.uint32), ("seq_off", np.uint64), ("cigar_off", np.uint64), ("n_cigar", np.uint16),
-                     ("cigar", np.uint32), ("seq", np.uint8), ("qual", np.uint8), ("xj", np.uint8))
+                     ("cigar", np.uint32), ("seq", np.uint8), ("qual", np.uint8), ("xj", np.uint8),
+                     ("isize", np.int32), ("xp", np.uint8), ("qname_off", np.uint64), ("qname", np.uint8))
 _CT = {np.int32: C.c_int32, np.uint16: C.c_uint16, np.uint8: C.c_uint8, np.uint32: C.c_uint32, np.uint64: C.c_uint64}
 
 
@@ -286,9 +333,9 @@ class ReadArrays(C.Structure):
     _fields_ = [(name, P(_CT[dt])) for name, dt in READ_ARRAY_FIELDS]
 
 
-def read_arrays(n: int, n_cigar: int, n_bases: int):
+def read_arrays(n: int, n_cigar: int, n_bases: int, n_name_bytes: int = 0):
     """Numpy arrays for decoded records and the bsq_read_arrays struct pointing at them."""
-    size = {"cigar": n_cigar, "seq": n_bases // 2, "qual": n_bases}
+    size = {"cigar": n_cigar, "seq": n_bases // 2, "qual": n_bases, "qname_off": n + 1, "qname": n_name_bytes}
     arrs = {name: np.zeros(max(1, size.get(name, n)), dtype=dt) for name, dt in READ_ARRAY_FIELDS}
     st = ReadArrays(**{name: ptr(arrs[name], _CT[dt]) for name, dt in READ_ARRAY_FIELDS})
     return arrs, st

@@ -42,6 +42,38 @@ def sc_params(sample, st: ScSettings):
 
 
 @dataclass
+class PairSettings:
+    """Discordant / missing-pair scan settings with breseq's defaults (src/breseq/settings.cpp:376-392).
+    dp_group: DP group of each read group (-1 none); window_width, r1_prefix, r2_prefix: per DP group."""
+    dp_group: tuple = (0,)
+    window_width: tuple = (400.0,)
+    r1_prefix: tuple = (1,)
+    r2_prefix: tuple = (2,)
+    discordant_pair_seed: int = 3
+    predict_missing_pairs: bool = False
+    missing_pair_seed: int = 3
+    missing_pair_seed_fraction: float = 0.25
+
+
+def pair_params(sample, st: PairSettings, deletion_propagation_cutoff=None):
+    """bsq_pair_params for a sample; returns (params, arrays they point into)."""
+    T = len(sample.target_offset) - 1
+    keep = dict(dpg=np.ascontiguousarray(st.dp_group, dtype=np.int32),
+                w=np.ascontiguousarray(st.window_width, dtype=np.float64),
+                r1=np.ascontiguousarray(st.r1_prefix, dtype=np.uint32),
+                r2=np.ascontiguousarray(st.r2_prefix, dtype=np.uint32),
+                cut=np.broadcast_to(np.asarray(5.0 if deletion_propagation_cutoff is None else deletion_propagation_cutoff,
+                                               dtype=np.float64), (T,)).copy())
+    p = abi.PairParams(n_read_groups=len(keep["dpg"]), dp_group=abi.ptr(keep["dpg"], C.c_int32),
+                       n_dp_groups=len(keep["w"]), window_width=abi.ptr(keep["w"], C.c_double),
+                       r1_name_prefix=abi.ptr(keep["r1"], C.c_uint32), r2_name_prefix=abi.ptr(keep["r2"], C.c_uint32),
+                       discordant_pair_seed=st.discordant_pair_seed, predict_missing_pairs=int(st.predict_missing_pairs),
+                       missing_pair_seed=st.missing_pair_seed, missing_pair_seed_fraction=st.missing_pair_seed_fraction,
+                       deletion_propagation_cutoff=abi.ptr(keep["cut"], C.c_double))
+    return p, keep
+
+
+@dataclass
 class ImSettings:
     """The Settings fields identify_mutations reads, with breseq's defaults."""
     polymorphism_prediction: bool = False
@@ -257,6 +289,32 @@ class Scorer:
         return dict(summary=abi.sc_summary_dict(s), rows=abi.sc_rows_array(rows, s.n_positions))
 
     # ------------------------------------------------------------------ BAM input
+    def pair_candidates(self, sid: int, settings: PairSettings | None = None, deletion_propagation_cutoff=None) -> dict:
+        """Discordant-pair and missing-pair candidate regions (bsq_pair_candidates): the regions as
+        structured arrays in detection order and the descriptor text they index."""
+        s = self.sample(sid)
+        p, keep = pair_params(s, settings or PairSettings(), deletion_propagation_cutoff)
+        nd, nm, nt = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self._check(self.L.bsq_pair_candidates(self.ctx, sid, C.byref(p), C.byref(nd), C.byref(nm), C.byref(nt)))
+        dp = (abi.PairRegion * max(1, nd.value))()
+        mp = (abi.PairRegion * max(1, nm.value))()
+        text = C.create_string_buffer(max(1, nt.value))
+        self._check(self.L.bsq_pair_result_copy(self.ctx, dp, nd.value, mp, nm.value, text, nt.value))
+        return dict(dp=list(dp)[: nd.value], mp=list(mp)[: nm.value], text=text.raw[: nt.value])
+
+    def write_pair_candidates(self, result: dict, dp_path: str | None, mp_path: str | None, target_names):
+        """dp_candidate_regions.csv / mp_candidate_regions.csv from a pair_candidates() result."""
+        names = (C.c_char_p * len(target_names))(*[n.encode() for n in target_names])
+        text = C.create_string_buffer(result["text"], max(1, len(result["text"])))
+        for path, key, fn in ((dp_path, "dp", self.L.bsq_write_dp_candidate_regions),
+                              (mp_path, "mp", self.L.bsq_write_mp_candidate_regions)):
+            if path is None:
+                continue
+            regs = (abi.PairRegion * max(1, len(result[key])))(*result[key])
+            rc = fn(path.encode(), names, regs, len(result[key]), text)
+            if rc != 0:
+                raise _lib.BsqError(rc, f"cannot write {path}")
+
     def open_bam(self, data) -> "Bam":
         """Uploads a BAM file's bytes (bytes, or a uint8 numpy array, e.g. page-locked) and inflates
         every BGZF block on the device."""
@@ -511,8 +569,11 @@ class Bam:
 
     def records(self) -> dict:
         """The decoded records as numpy arrays in the bsq_read_soa layout."""
-        arrs, st = abi.read_arrays(*self.counts)
+        nb = C.c_uint64()
+        self.sc._check(self.sc.L.bsq_bam_name_bytes(self.sc.ctx, self.h, C.byref(nb)))
+        arrs, st = abi.read_arrays(*self.counts, nb.value)
         self.sc._check(self.sc.L.bsq_bam_copy_records(self.sc.ctx, self.h, C.byref(st)))
+        arrs["qname"] = arrs["qname"][: nb.value]
         return arrs
 
     def load(self, reference_sample) -> int:

@@ -24,6 +24,7 @@
 #include "bsq_softclip.h"
 #include "bsq_covtable.h"
 #include "bsq_bam.h"
+#include "bsq_pairs.h"
 
 using namespace bsq;
 
@@ -54,6 +55,9 @@ struct DevMem {
 
 struct SampleDev {
   DevMem ref, reads, x1, rg, qb, cigar, seq, qual, tile_range, d_tpoff, tgt_group, tgt_called, tgt_failed, rstart, mapq;
+  // pair annotations for the discordant / missing-pair scans: raw flags, XP codes, TLEN, names
+  DevMem pflag, pxp, pisize, pqoff, pqname;
+  bool has_pairs = false;
   uint32_t n_targets = 0, n_cols = 0, n_tiles = 0, n_reads = 0, maxspan = 1, max_tile_reads = 0;
   uint32_t n_groups = 0;
   std::vector<uint64_t> toff;       // caller's target offsets
@@ -119,6 +123,10 @@ struct bsq_ctx {
   DevMem sc_diff, sc_cnt, sc_blk, sc_tot, sc_rows, sc_outs, sc_tails, sc_ev, sc_ev_n;
   // coverage table of a region
   DevMem ct_diff, ct_blk, ct_counts, ct_red, ct_stat, ct_gather;
+  // discordant / missing-pair scans
+  DevMem pr_code, pr_group, pr_sel, pr_mem, pr_evoff, pr_memoff, pr_tmp, pr_tot, pr_map, pr_ev, pr_names, pr_mstart,
+      pr_mkey;
+  host::PairReplayResult pair_res;
   std::vector<bsq_sc_position> sc_res;
   double last_ms = 0, main_ms = 0;
   uint32_t launches = 0;
@@ -312,7 +320,9 @@ void bsq_destroy(bsq_ctx* ctx) {
                     &ctx->d_chunks, &ctx->ec_arena, &ctx->im_arena, &ctx->ctl, &ctx->sc_diff, &ctx->sc_cnt,
                     &ctx->sc_blk, &ctx->sc_tot, &ctx->sc_rows, &ctx->sc_outs, &ctx->sc_tails, &ctx->sc_ev,
                     &ctx->sc_ev_n, &ctx->ct_diff, &ctx->ct_blk, &ctx->ct_counts, &ctx->ct_red, &ctx->ct_stat,
-                    &ctx->ct_gather})
+                    &ctx->ct_gather, &ctx->pr_code, &ctx->pr_group, &ctx->pr_sel, &ctx->pr_mem, &ctx->pr_evoff,
+                    &ctx->pr_memoff, &ctx->pr_tmp, &ctx->pr_tot, &ctx->pr_map, &ctx->pr_ev, &ctx->pr_names,
+                    &ctx->pr_mstart, &ctx->pr_mkey})
     m->release();
   if (ctx->exec_ec) cudaGraphExecDestroy(ctx->exec_ec);
   if (ctx->exec_im) cudaGraphExecDestroy(ctx->exec_im);
@@ -333,8 +343,12 @@ uint64_t bsq_sample_footprint(const bsq_reference* ref, const bsq_read_soa* rd) 
   const uint64_t tiles = (cols + 31) / 32;
   const uint64_t per_read = sizeof(DevRead) + 4 + 2 + sizeof(QBounds) + 4 + 1;
   const uint64_t upload_tmp = rd->n_reads * 48;  // raw arrays, freed after packing
+  // pair annotations stay resident: flag, XP, TLEN, name offsets and names
+  const uint64_t pairs = (rd->xp && rd->isize && rd->qname_off && rd->qname)
+                             ? rd->n_reads * 15 + 8 + (rd->n_reads ? rd->qname_off[rd->n_reads] : 0)
+                             : 0;
   return cols + 64 + rd->n_reads * per_read + rd->n_cigar_total * 4 + rd->n_bases_total / 2 + 16 +
-         rd->n_bases_total + tiles * 8 + upload_tmp;
+         rd->n_bases_total + tiles * 8 + upload_tmp + pairs;
 }
 
 }  // extern "C"
@@ -342,8 +356,9 @@ uint64_t bsq_sample_footprint(const bsq_reference* ref, const bsq_read_soa* rd) 
 // The record arrays of a sample on the device, in the bsq_read_soa layout, before packing.
 struct RecordsDev {
   DevMem tid, pos, flag, mapq, x1, xl, xr, rfile, rg, lq, soff, coff, nc, cigar, seq, qual, xj;
+  DevMem isize, xp, qoff, qname;   // pair annotations (has_pairs)
   uint64_t n = 0, n_cigar_total = 0, n_bases_total = 0;
-  bool has_xj = false;
+  bool has_xj = false, has_pairs = false;
 };
 
 static void take(DevMem& to, DevMem& from) {
@@ -453,6 +468,14 @@ static int pack_sample(bsq_ctx* ctx, std::unique_ptr<SampleDev>& s, RecordsDev& 
   CK(cudaMemcpyAsync(h + 10, stats + 10, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   s->max_tile_reads = h[10];
+  if (R.has_pairs) {
+    take(s->pflag, R.flag);
+    take(s->pxp, R.xp);
+    take(s->pisize, R.isize);
+    take(s->pqoff, R.qoff);
+    take(s->pqname, R.qname);
+    s->has_pairs = true;
+  }
   std::lock_guard<std::mutex> lk(ctx->mu);
   const int32_t id = ctx->next_id++;
   ctx->samples[id] = std::move(s);
@@ -498,6 +521,18 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
   if (rd->xj) {
     CK(upload(R.xj, rd->xj, n, st));
     R.has_xj = true;
+  }
+  if (rd->isize || rd->xp || rd->qname_off || rd->qname) {
+    if (!rd->isize || !rd->xp || !rd->qname_off || !rd->qname)
+      return fail(ctx, BSQ_ERR_INVALID, "pair annotations need isize, xp, qname_off and qname together");
+    for (uint64_t i = 0; i < n; i++)
+      if (rd->qname_off[i + 1] < rd->qname_off[i] || rd->qname_off[i + 1] - rd->qname_off[i] > 254)
+        return fail(ctx, BSQ_ERR_INVALID, "read name offsets decreasing or a name longer than 254 bytes");
+    CK(upload(R.isize, rd->isize, n, st));
+    CK(upload(R.xp, rd->xp, n, st));
+    CK(upload(R.qoff, rd->qname_off, n + 1, st));
+    CK(upload(R.qname, rd->qname, rd->qname_off[n], st));
+    R.has_pairs = true;
   }
   return pack_sample(ctx, s, R, st, sample_id);
 }
@@ -1106,6 +1141,139 @@ int bsq_soft_clipping(bsq_ctx* ctx, int32_t sample_id, const bsq_sc_params* p, b
   return BSQ_OK;
 }
 
+// Discordant-pair / missing-pair candidate regions: the reads are classified and the window entries
+// compacted on the device (bsq_pairs.cu); the sliding windows are replayed on the host over the
+// compacted reads (bsq_pairs_host.cpp).
+int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* p, uint64_t* n_dp, uint64_t* n_mp,
+                        uint64_t* text_bytes) {
+  if (!ctx || !p || !n_dp || !n_mp || !text_bytes) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  SampleDev* s = find_sample(ctx, sample_id);
+  if (!s) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
+  if (!s->has_pairs) return fail(ctx, BSQ_ERR_INVALID, "sample loaded without pair annotations (isize, xp, qname)");
+  const uint32_t T = s->n_targets, G = p->n_dp_groups, NRG = p->n_read_groups;
+  if (G > 255) return fail(ctx, BSQ_ERR_INVALID, "more than 255 DP groups");
+  if ((NRG && !p->dp_group) || (G && (!p->window_width || !p->r1_name_prefix || !p->r2_name_prefix)) ||
+      !p->deletion_propagation_cutoff)
+    return fail(ctx, BSQ_ERR_INVALID, "null parameter array");
+  for (uint32_t r = 0; r < NRG; r++)
+    if (p->dp_group[r] < -1 || p->dp_group[r] >= (int32_t)G) return fail(ctx, BSQ_ERR_INVALID, "DP group out of range");
+  for (uint32_t g = 0; g < G; g++)
+    if (!(p->window_width[g] > 0.0) || !std::isfinite(p->window_width[g]))
+      return fail(ctx, BSQ_ERR_INVALID, "window width must be positive and finite");
+  // the ranges Settings enforces (src/breseq/settings.cpp:719-735)
+  if (p->discordant_pair_seed < 0 || (p->predict_missing_pairs && (p->missing_pair_seed < 0 ||
+      !(p->missing_pair_seed_fraction >= 0.0 && p->missing_pair_seed_fraction <= 1.0))))
+    return fail(ctx, BSQ_ERR_INVALID, "seed setting out of range");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  cudaGetLastError();
+  const uint64_t n = s->n_reads;
+  const bool mp = p->predict_missing_pairs && G > 0;
+  host::PairReplayInput in;
+  in.tpoff = s->tpoff;
+  in.order = s->order;
+  in.piled.assign(T, 0);
+  for (uint32_t t : s->order) in.piled[t] = p->deletion_propagation_cutoff[t] >= 0.0 ? 1 : 0;
+  in.window_width.assign(p->window_width, p->window_width + G);
+  in.r1_prefix.assign(p->r1_name_prefix, p->r1_name_prefix + G);
+  in.r2_prefix.assign(p->r2_name_prefix, p->r2_name_prefix + G);
+  in.dp_seed = p->discordant_pair_seed;
+  in.mp_seed = p->missing_pair_seed;
+  in.mp_seed_fraction = p->missing_pair_seed_fraction;
+  in.mp = mp;
+  CK(record(ctx->ev0, st));
+  CK(ctx->pr_code.alloc(n + 16, st));
+  CK(ctx->pr_group.alloc(n + 16, st));
+  CK(ctx->pr_sel.alloc(n * 4 + 16, st));
+  CK(ctx->pr_evoff.alloc(n * 8 + 16, st));
+  if (mp) {
+    CK(ctx->pr_mem.alloc(n * 4 + 16, st));
+    CK(ctx->pr_memoff.alloc(n * 8 + 16, st));
+  }
+  CK(ctx->pr_tmp.alloc((n / 1024 + 4) * 8 + 64, st));
+  CK(ctx->pr_tot.alloc(64, st));
+  CK(upload(ctx->pr_map, p->dp_group, NRG, st));
+  PairArgs A;
+  memset(&A, 0, sizeof A);
+  A.reads = s->reads.as<DevRead>();
+  A.flag = s->pflag.as<uint16_t>();
+  A.xp = s->pxp.as<uint8_t>();
+  A.isize = s->pisize.as<int32_t>();
+  A.qoff = s->pqoff.as<uint64_t>();
+  A.qname = s->pqname.as<char>();
+  A.x1 = s->x1.as<uint32_t>();
+  A.rg = s->rg.as<uint16_t>();
+  A.rg_map = ctx->pr_map.as<int32_t>();
+  A.n_rg = NRG;
+  A.n = (uint32_t)n;
+  A.mp = mp ? 1 : 0;
+  A.code = ctx->pr_code.as<uint8_t>();
+  A.group = ctx->pr_group.as<uint8_t>();
+  A.sel = ctx->pr_sel.as<uint32_t>();
+  A.mem = mp ? ctx->pr_mem.as<uint32_t>() : nullptr;
+  uint64_t* tot = ctx->pr_tot.as<uint64_t>();
+  CK(record(ctx->evm0, st));
+  CK(pair_classify(A, ctx->sms, st));
+  CK(record(ctx->evm1, st));
+  CK(scan_u32(A.sel, ctx->pr_evoff.as<uint64_t>(), n, ctx->pr_tmp.as<uint64_t>(), tot, st));
+  if (mp) CK(scan_u32(A.mem, ctx->pr_memoff.as<uint64_t>(), n, ctx->pr_tmp.as<uint64_t>(), tot + 1, st));
+  CK(ctx->pin_out.reserve(64));
+  CK(cudaMemcpyAsync(ctx->pin_out.p, tot, 16, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  uint64_t counts[2];
+  memcpy(counts, ctx->pin_out.p, 16);
+  const uint64_t n_ev = counts[0], n_mem = mp ? counts[1] : 0;
+  CK(ctx->pr_ev.alloc(n_ev * sizeof(PairEvent) + 16, st));
+  CK(ctx->pr_names.alloc(n_ev * kPairNameSlot + 16, st));
+  CK(ctx->pr_mstart.alloc(n_mem * 4 + 16, st));
+  CK(ctx->pr_mkey.alloc(n_mem * 2 + 16, st));
+  CK(pair_scatter(A, ctx->pr_evoff.as<uint64_t>(), mp ? ctx->pr_memoff.as<uint64_t>() : nullptr,
+                  ctx->pr_ev.as<PairEvent>(), ctx->pr_names.as<char>(), ctx->pr_mstart.as<uint32_t>(),
+                  ctx->pr_mkey.as<uint16_t>(), ctx->sms, st));
+  const uint64_t b_ev = n_ev * sizeof(PairEvent), b_nm = n_ev * kPairNameSlot, b_ms = n_mem * 4, b_mk = n_mem * 2;
+  const uint64_t o_nm = align256(b_ev), o_ms = o_nm + align256(b_nm), o_mk = o_ms + align256(b_ms);
+  CK(ctx->pin_out.reserve(o_mk + b_mk + 64));
+  unsigned char* h = ctx->pin_out.at(0);
+  if (b_ev) CK(cudaMemcpyAsync(h, ctx->pr_ev.p, b_ev, cudaMemcpyDeviceToHost, st));
+  if (b_nm) CK(cudaMemcpyAsync(h + o_nm, ctx->pr_names.p, b_nm, cudaMemcpyDeviceToHost, st));
+  if (b_ms) CK(cudaMemcpyAsync(h + o_ms, ctx->pr_mstart.p, b_ms, cudaMemcpyDeviceToHost, st));
+  if (b_mk) CK(cudaMemcpyAsync(h + o_mk, ctx->pr_mkey.p, b_mk, cudaMemcpyDeviceToHost, st));
+  CK(record(ctx->ev1, st));
+  CK(cudaStreamSynchronize(st));
+  ctx->last_ms = elapsed(ctx->ev0, ctx->ev1);
+  ctx->main_ms = elapsed(ctx->evm0, ctx->evm1);   // the classification pass over every read
+  ctx->launches = 1 + 3 + (mp ? 3 : 0) + 1;
+  ctx->last_h2d = (uint64_t)NRG * 4;
+  ctx->last_d2h = 16 + b_ev + b_nm + b_ms + b_mk;
+  in.ev = reinterpret_cast<const PairEvent*>(h);
+  in.n_ev = n_ev;
+  in.names = reinterpret_cast<const char*>(h + o_nm);
+  in.mem_start = reinterpret_cast<const uint32_t*>(h + o_ms);
+  in.mem_key = reinterpret_cast<const uint16_t*>(h + o_mk);
+  in.n_mem = n_mem;
+  ctx->pair_res = host::PairReplayResult();
+  const int rc = host::pair_replay(in, ctx->pair_res);
+  if (rc != BSQ_OK) return fail(ctx, rc, "inconsistent pair events");
+  *n_dp = ctx->pair_res.dp.size();
+  *n_mp = ctx->pair_res.mp.size();
+  *text_bytes = ctx->pair_res.text.size();
+  return BSQ_OK;
+}
+
+int bsq_pair_result_copy(bsq_ctx* ctx, bsq_pair_region* dp, uint64_t n_dp, bsq_pair_region* mp, uint64_t n_mp,
+                         char* text, uint64_t text_bytes) {
+  if (!ctx) return BSQ_ERR_INVALID;
+  const host::PairReplayResult& r = ctx->pair_res;
+  if (n_dp < r.dp.size() || n_mp < r.mp.size() || text_bytes < r.text.size())
+    return fail(ctx, BSQ_ERR_SIZE, "result buffers too small");
+  if ((r.dp.size() && !dp) || (r.mp.size() && !mp) || (r.text.size() && !text))
+    return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  if (r.dp.size()) memcpy(dp, r.dp.data(), r.dp.size() * sizeof(bsq_pair_region));
+  if (r.mp.size()) memcpy(mp, r.mp.data(), r.mp.size() * sizeof(bsq_pair_region));
+  if (r.text.size()) memcpy(text, r.text.data(), r.text.size());
+  return BSQ_OK;
+}
+
 // Coverage columns of one region (coverage_output::pileup_callback, coverage_output.cpp:307-470):
 // bsq_covtable.cu on the device.  The columns at positions start + k * step (k < m; step 1 = every
 // position) come back in one pinned buffer with the reference characters: [6][m] u32 counts |
@@ -1594,9 +1762,11 @@ int bsq_bam_decode(bsq_ctx* ctx, bsq_bam* bam, const bsq_bam_groups* groups, uin
   CK(R.xr.alloc(n * 4 + 16, st)); CK(R.rfile.alloc(n + 16, st)); CK(R.rg.alloc(n * 2 + 16, st));
   CK(R.lq.alloc(n * 4 + 16, st)); CK(R.soff.alloc(n * 8 + 16, st)); CK(R.coff.alloc(n * 8 + 16, st));
   CK(R.nc.alloc(n * 2 + 16, st)); CK(R.xj.alloc(n + 16, st));
-  DevMem ncig32, nib, tmp, ids_dev;
+  CK(R.isize.alloc(n * 4 + 16, st)); CK(R.xp.alloc(n + 16, st)); CK(R.qoff.alloc(n * 8 + 24, st));
+  DevMem ncig32, nib, nlen, tmp, ids_dev;
   CK(ncig32.alloc(n * 4 + 16, st));
   CK(nib.alloc(n * 4 + 16, st));
+  CK(nlen.alloc(n * 4 + 16, st));
   CK(tmp.alloc((n / 1024 + 4) * 8 + 64, st));
   CK(upload(ids_dev, ids.data(), ids.size() + 1, st));
   BamRecordsDev D;
@@ -1604,19 +1774,22 @@ int bsq_bam_decode(bsq_ctx* ctx, bsq_bam* bam, const bsq_bam_groups* groups, uin
   D.x1 = R.x1.as<uint32_t>(); D.xl = R.xl.as<int32_t>(); D.xr = R.xr.as<int32_t>(); D.read_file = R.rfile.as<uint8_t>();
   D.read_group = R.rg.as<uint16_t>(); D.l_qseq = R.lq.as<uint32_t>(); D.seq_off = R.soff.as<uint64_t>();
   D.cigar_off = R.coff.as<uint64_t>(); D.n_cigar = R.nc.as<uint16_t>(); D.xj = R.xj.as<uint8_t>();
-  D.cigar = nullptr; D.seq = nullptr; D.qual = nullptr;
+  D.isize = R.isize.as<int32_t>(); D.xp = R.xp.as<uint8_t>(); D.qoff = R.qoff.as<uint64_t>();
+  D.cigar = nullptr; D.seq = nullptr; D.qual = nullptr; D.qname = nullptr;
   CK(bam_fields(bam->stream.as<uint8_t>(), offsets.as<uint64_t>(), n, (uint32_t)bam->names.size(), G,
-                ids_dev.as<char>(), D, ncig32.as<uint32_t>(), nib.as<uint32_t>(), w, ctx->sms, st));
-  // CIGAR and base offsets
-  uint64_t* tot = reinterpret_cast<uint64_t*>(w + 4);   // [0] CIGAR ops, [1] nibbles
+                ids_dev.as<char>(), D, ncig32.as<uint32_t>(), nib.as<uint32_t>(), nlen.as<uint32_t>(), w, ctx->sms, st));
+  // CIGAR, base and read-name offsets
+  uint64_t* tot = reinterpret_cast<uint64_t*>(w + 4);   // [0] CIGAR ops, [1] nibbles, [2] name bytes
   CK(scan_u32(ncig32.as<uint32_t>(), D.cigar_off, n, tmp.as<uint64_t>(), tot, st));
   CK(scan_u32(nib.as<uint32_t>(), D.seq_off, n, tmp.as<uint64_t>(), tot + 1, st));
-  uint32_t hw[8];
-  CK(cudaMemcpyAsync(hw, w, 32, cudaMemcpyDeviceToHost, st));
+  CK(scan_u32(nlen.as<uint32_t>(), D.qoff, n, tmp.as<uint64_t>(), tot + 2, st));
+  CK(cudaMemcpyAsync(D.qoff + n, tot + 2, 8, cudaMemcpyDeviceToDevice, st));
+  uint32_t hw[12];
+  CK(cudaMemcpyAsync(hw, w, 48, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (hw[0]) return fail(ctx, BSQ_ERR_INVALID, bam_err_text(hw[0]));
-  uint64_t totals[2];
-  memcpy(totals, hw + 4, 16);
+  uint64_t totals[3];
+  memcpy(totals, hw + 4, 24);
   // unplaced records: all after the placed ones; they are dropped
   uint64_t used = n;
   if (hw[1] != 0xFFFFFFFFu) {
@@ -1626,12 +1799,14 @@ int bsq_bam_decode(bsq_ctx* ctx, bsq_bam* bam, const bsq_bam_groups* groups, uin
   CK(R.cigar.alloc(totals[0] * 4 + 16, st));
   CK(R.seq.alloc(totals[1] / 2 + 16, st));
   CK(R.qual.alloc(totals[1] + 16, st));
+  CK(R.qname.alloc(totals[2] + 16, st));
   D.cigar = R.cigar.as<uint32_t>(); D.seq = R.seq.as<uint8_t>(); D.qual = R.qual.as<uint8_t>();
+  D.qname = R.qname.as<char>();
   CK(bam_copy(bam->stream.as<uint8_t>(), offsets.as<uint64_t>(), n, D, ctx->sms, st));
   CK(record(ctx->ev1, st));
   CK(cudaStreamSynchronize(st));
   ctx->last_ms = ctx->main_ms = elapsed(ctx->ev0, ctx->ev1);
-  ctx->launches = 9;
+  ctx->launches = 12;
   // the dropped unplaced records are the last ones: their CIGARs and bases are at the arrays' ends
   R.n = used;
   if (used < n) {
@@ -1645,6 +1820,7 @@ int bsq_bam_decode(bsq_ctx* ctx, bsq_bam* bam, const bsq_bam_groups* groups, uin
     R.n_bases_total = totals[1];
   }
   R.has_xj = true;
+  R.has_pairs = true;
   bam->decoded = true;
   if (n_records) *n_records = R.n;
   if (n_cigar_total) *n_cigar_total = R.n_cigar_total;
@@ -1665,10 +1841,25 @@ int bsq_bam_copy_records(bsq_ctx* ctx, const bsq_bam* bam, const bsq_read_arrays
       {out->read_group, &R.rg, n * 2}, {out->l_qseq, &R.lq, n * 4}, {out->seq_off, &R.soff, n * 8},
       {out->cigar_off, &R.coff, n * 8}, {out->n_cigar, &R.nc, n * 2}, {out->xj, &R.xj, n},
       {out->cigar, &R.cigar, R.n_cigar_total * 4}, {out->seq, &R.seq, R.n_bases_total / 2},
-      {out->qual, &R.qual, R.n_bases_total}};
+      {out->qual, &R.qual, R.n_bases_total}, {out->isize, &R.isize, n * 4}, {out->xp, &R.xp, n},
+      {out->qname_off, &R.qoff, (n + 1) * 8}};
   for (const Item& it : items)
     if (it.dst && it.bytes) CK(cudaMemcpyAsync(it.dst, it.src->p, it.bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  if (out->qname) {
+    uint64_t nb = 0;
+    CK(cudaMemcpyAsync(&nb, R.qoff.as<uint64_t>() + n, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (nb) CK(cudaMemcpyAsync(out->qname, R.qname.p, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  }
   CK(cudaStreamSynchronize(ctx->stream));
+  return BSQ_OK;
+}
+
+int bsq_bam_name_bytes(bsq_ctx* ctx, const bsq_bam* bam, uint64_t* bytes) {
+  if (!ctx || !bam || !bytes) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  if (!bam->decoded) return fail(ctx, BSQ_ERR_INVALID, "BAM not decoded");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpy(bytes, bam->rec->qoff.as<uint64_t>() + bam->rec->n, 8, cudaMemcpyDeviceToHost));
   return BSQ_OK;
 }
 

@@ -215,14 +215,14 @@ __device__ __forceinline__ int64_t aux_size(const uint8_t* p, const uint8_t* end
 __global__ void __launch_bounds__(256) bam_fields_kernel(const uint8_t* stream, const uint64_t* offsets, uint64_t n,
                                                          uint32_t n_ref, const __grid_constant__ BamGroups G,
                                                          const char* ids, BamRecordsDev R, uint32_t* ncig32,
-                                                         uint32_t* nib, uint32_t* err) {
+                                                         uint32_t* nib, uint32_t* nlen, uint32_t* err) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const RecordView v = view_record(stream, offsets[i]);
     uint32_t e = 0;
     if (!v.ok || v.ref_id < -1 || v.ref_id >= (int32_t)n_ref) e |= kBamRecord;
     int64_t x1 = 1, xl = -1, xr = -1;
-    bool has_x1 = false, has_xl = false, has_xr = false, has_xj = false, has_rg = false;
-    uint32_t group = 0;
+    bool has_x1 = false, has_xl = false, has_xr = false, has_xj = false, has_rg = false, has_xp = false;
+    uint32_t group = 0, xp = 3;   // BSQ_XP_NONE
     if (v.ok) {
       const uint8_t* q = stream + v.aux;
       const uint8_t* end = stream + v.end;
@@ -236,6 +236,15 @@ __global__ void __launch_bounds__(256) bam_fields_kernel(const uint8_t* stream, 
         else if (t0 == 'X' && t1 == 'L' && !has_xl) { has_xl = true; xl = aux_int(q, type); }
         else if (t0 == 'X' && t1 == 'R' && !has_xr) { has_xr = true; xr = aux_int(q, type); }
         else if (t0 == 'X' && t1 == 'J') { has_xj = true; }
+        else if (t0 == 'X' && t1 == 'P' && !has_xp) {
+          // the pair orientation breseq writes as XP:Z (FR, RF or FF); read as bam_aux2Z does
+          has_xp = true;
+          if ((type == 'Z' || type == 'H') && sz == 3 && q[2] == 0) {
+            if (q[0] == 'F' && q[1] == 'R') xp = 0;
+            else if (q[0] == 'R' && q[1] == 'F') xp = 1;
+            else if (q[0] == 'F' && q[1] == 'F') xp = 2;
+          }
+        }
         else if (t0 == 'R' && t1 == 'G' && !has_rg) {
           has_rg = true;
           // bam_aux2Z: Z and H strings only; one group or none resolves to 0 without a lookup
@@ -270,6 +279,8 @@ __global__ void __launch_bounds__(256) bam_fields_kernel(const uint8_t* stream, 
     R.xl[i] = (int32_t)xl;
     R.xr[i] = (int32_t)xr;
     R.xj[i] = has_xj ? 1 : 0;
+    R.xp[i] = (uint8_t)xp;
+    R.isize[i] = (int32_t)rd32(stream + offsets[i] + 32);   // TLEN: inside the 32 fixed bytes the walk checked
     R.read_group[i] = (uint16_t)group;
     uint32_t file = 0;
     if (G.n > 0 && group < G.n && G.file_count[group] > 0)
@@ -280,6 +291,7 @@ __global__ void __launch_bounds__(256) bam_fields_kernel(const uint8_t* stream, 
     R.n_cigar[i] = (uint16_t)(v.ok ? v.n_cigar : 0);
     ncig32[i] = v.ok ? v.n_cigar : 0;
     nib[i] = ls + (ls & 1);
+    nlen[i] = v.ok ? v.l_read_name - 1 : 0;
   }
 }
 
@@ -301,6 +313,10 @@ __global__ void __launch_bounds__(256) bam_copy_kernel(const uint8_t* stream, co
     uint8_t* ql = R.qual + so;
     for (uint32_t j = lane; j < (uint32_t)v.l_seq; j += 32) ql[j] = stream[v.qual + j];
     if ((v.l_seq & 1) && lane == 0) ql[v.l_seq] = 0;   // the padding position of an odd-length read
+    if (R.qname) {
+      char* nm = R.qname + R.qoff[i];
+      for (uint32_t j = lane; j + 1 < v.l_read_name; j += 32) nm[j] = (char)stream[v.off + 36 + j];
+    }
   }
 }
 
@@ -395,9 +411,10 @@ cudaError_t bam_walk(const uint8_t* stream, const BgzfBlock* blocks, uint32_t n_
 }
 
 cudaError_t bam_fields(const uint8_t* stream, const uint64_t* offsets, uint64_t n, uint32_t n_ref, const BamGroups& groups,
-                       const char* ids, const BamRecordsDev& R, uint32_t* ncig32, uint32_t* nib, uint32_t* err, int sms,
-                       cudaStream_t st) {
-  if (n) bam_fields_kernel<<<grid_for(n, 256, sms, 8), 256, 0, st>>>(stream, offsets, n, n_ref, groups, ids, R, ncig32, nib, err);
+                       const char* ids, const BamRecordsDev& R, uint32_t* ncig32, uint32_t* nib, uint32_t* nlen,
+                       uint32_t* err, int sms, cudaStream_t st) {
+  if (n) bam_fields_kernel<<<grid_for(n, 256, sms, 8), 256, 0, st>>>(stream, offsets, n, n_ref, groups, ids, R, ncig32, nib,
+                                                                       nlen, err);
   return cudaGetLastError();
 }
 

@@ -61,6 +61,10 @@ struct BamRecordsDev {
   uint32_t* cigar;
   uint8_t* seq;
   uint8_t* qual;
+  int32_t* isize;        // TLEN
+  uint8_t* xp;           // XP:Z orientation code (BSQ_XP_*)
+  uint64_t* qoff;        // [n + 1] read-name offsets
+  char* qname;           // names without terminators; null until their total is known
 };
 
 cudaError_t bam_inflate(const uint8_t* file, const BgzfBlock* blocks, uint32_t n_blocks, uint8_t* out, uint32_t* err,
@@ -70,16 +74,16 @@ cudaError_t bam_inflate(const uint8_t* file, const BgzfBlock* blocks, uint32_t n
 cudaError_t bam_walk(const uint8_t* stream, const BgzfBlock* blocks, uint32_t n_blocks, uint64_t records_begin,
                      uint32_t* counts, const uint64_t* base, uint64_t* offsets, uint32_t* err, int sms, cudaStream_t st);
 // Fixed fields and tags of each record, and the per-record counts the scans turn into offsets: CIGAR
-// ops and nibbles (l_seq rounded up to even).  n_ref: references in the header.  err[0] gets error
-// bits, err[1] the first unplaced record (initialise to 0xFFFFFFFF), err[2] one past the last placed
-// record (initialise to 0).
+// ops, nibbles (l_seq rounded up to even) and read-name bytes.  n_ref: references in the header.
+// err[0] gets error bits, err[1] the first unplaced record (initialise to 0xFFFFFFFF), err[2] one past
+// the last placed record (initialise to 0).
 cudaError_t bam_fields(const uint8_t* stream, const uint64_t* offsets, uint64_t n, uint32_t n_ref, const BamGroups& groups,
-                       const char* ids, const BamRecordsDev& R, uint32_t* ncig32, uint32_t* nib, uint32_t* err, int sms,
-                       cudaStream_t st);
+                       const char* ids, const BamRecordsDev& R, uint32_t* ncig32, uint32_t* nib, uint32_t* nlen,
+                       uint32_t* err, int sms, cudaStream_t st);
 // Exclusive scan of n 32-bit counts into 64-bit offsets; total[0] gets the sum.  tmp holds
 // 8 * (n / 1024 + 2) bytes.
 cudaError_t scan_u32(const uint32_t* in, uint64_t* out, uint64_t n, uint64_t* tmp, uint64_t* total, cudaStream_t st);
-// CIGAR words, bases and qualities of every record into the arrays.
+// CIGAR words, bases, qualities and read names of every record into the arrays.
 cudaError_t bam_copy(const uint8_t* stream, const uint64_t* offsets, uint64_t n, const BamRecordsDev& R, int sms,
                      cudaStream_t st);
 

@@ -2,10 +2,12 @@
 #pragma once
 #include <stdint.h>
 
+#include <string>
 #include <vector>
 
 #include "../../include/breseq_gb300.h"
 #include "bsq_common.h"
+#include "bsq_pairs.h"
 #include "bsq_softclip.h"
 
 namespace bsq {
@@ -80,6 +82,31 @@ void sc_assemble(const ScRowDev* rows, const ScOutDev* outs, uint64_t rows_neg, 
                  const std::vector<uint32_t>& tpoff, const std::vector<uint32_t>& name_order, uint32_t K,
                  const bsq_sc_params& p, uint64_t total_clipped, uint64_t total_spanning, uint64_t tested_spanning,
                  std::vector<bsq_sc_position>& out, bsq_sc_summary& s);
+
+// Discordant / missing-pair candidate regions (bsq_pairs_host.cpp) from the reads the device
+// compacted: events in BAM order with their names in 256-byte slots, and the MP window-total
+// members' start columns with keys group * 2 + strand.  piled[t]: target t is in the pileup set and
+// its deletion propagation cutoff is not below 0.
+struct PairReplayInput {
+  std::vector<uint32_t> tpoff, order;
+  std::vector<uint8_t> piled;
+  std::vector<double> window_width;
+  std::vector<uint32_t> r1_prefix, r2_prefix;
+  int32_t dp_seed = 3, mp_seed = 3;
+  double mp_seed_fraction = 0.25;
+  bool mp = false;
+  const PairEvent* ev = nullptr;
+  uint64_t n_ev = 0;
+  const char* names = nullptr;
+  const uint32_t* mem_start = nullptr;
+  const uint16_t* mem_key = nullptr;
+  uint64_t n_mem = 0;
+};
+struct PairReplayResult {
+  std::vector<bsq_pair_region> dp, mp;
+  std::string text;
+};
+int pair_replay(const PairReplayInput& in, PairReplayResult& out);
 
 }  // namespace host
 }  // namespace bsq

@@ -1,0 +1,296 @@
+// Discordant-pair (DP) and missing-pair (MP) candidate regions: the sliding-window replay on the host
+// over the reads the device compacted (bsq_pairs.cu), and the two CSV writers.
+//
+// breseq advances every window at every reference position of a piled-up target
+// (check_discordant_completion / check_missing_pair_completion, src/breseq/identify_mutations.cpp:
+// 2358-2437, 2439-2522, called per column at :1758-1767 and once past the end at :2131-2137).  A DP
+// window count only changes where a read enters (its start) or leaves (start + ceil(width)), so the
+// replay visits those positions only; an MP region also depends on the window total of all reads of
+// the strand, which changes almost everywhere, so where the MP count reaches the seed every position
+// is evaluated, the total coming from binary searches over the members' start positions.  Region
+// contents, their order and every count are those of the per-position walk.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <deque>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "../../include/breseq_gb300.h"
+#include "bsq_host.h"
+#include "bsq_pairs.h"
+
+namespace bsq {
+namespace host {
+namespace {
+
+constexpr uint32_t kUndefPos = 0xFFFFFFFFu;
+const char* const kOrient[3] = {"FR", "RF", "FF"};
+
+struct Ev {
+  uint32_t start1, end1;   // 1-based aligned extent
+  uint32_t group;
+  bool redundant;
+  uint64_t idx;            // index into the compacted events
+};
+
+std::string dp_key(const PairEvent& e, const char* name, uint32_t r1_prefix, uint32_t r2_prefix) {
+  // <read1_name>__<read2_name>__<r1_insert_size> (identify_mutations.cpp:1418-1436)
+  const std::string fname(name, e.name_len);
+  const bool focal_is_r1 = !(e.code & kPairRead2);
+  const size_t colon = fname.find(':');
+  std::string r1, r2;
+  if (colon != std::string::npos) {
+    const std::string counter = fname.substr(colon + 1);
+    r1 = std::to_string(r1_prefix) + ":" + counter;
+    r2 = std::to_string(r2_prefix) + ":" + counter;
+  } else {
+    r1 = focal_is_r1 ? fname : "";
+    r2 = focal_is_r1 ? "" : fname;
+  }
+  const int32_t r1_insert = focal_is_r1 ? e.isize : (int32_t)(0u - (uint32_t)e.isize);
+  return r1 + "__" + r2 + "__" + std::to_string(r1_insert);
+}
+
+// One bin's open region.
+struct Region {
+  uint32_t start = kUndefPos, max_count = 0, max_total = 0, redundant = 0;
+  std::vector<uint64_t> reads;   // indices into the descriptor strings, in region order
+};
+
+struct Ctx {
+  const PairReplayInput& in;
+  PairReplayResult& out;
+  std::vector<std::string> desc;   // descriptor of each compacted event
+};
+
+void close_region(Ctx& c, Region& r, uint32_t tid, uint32_t end, char strand, const char* orient, bool mp) {
+  bsq_pair_region x;
+  memset(&x, 0, sizeof x);
+  x.target = tid;
+  x.start = r.start;
+  x.end = end;
+  x.strand = strand;
+  if (orient) { x.orientation[0] = orient[0]; x.orientation[1] = orient[1]; }
+  x.max_count = r.max_count;
+  x.max_total = mp ? r.max_total : 0;
+  x.redundant = (2 * (uint64_t)r.redundant > r.reads.size()) ? 1 : 0;
+  x.text_off = c.out.text.size();
+  for (size_t k = 0; k < r.reads.size(); k++) {
+    if (k) c.out.text += ';';
+    c.out.text += c.desc[r.reads[k]];
+  }
+  x.text_len = c.out.text.size() - x.text_off;
+  (mp ? c.out.mp : c.out.dp).push_back(x);
+  r = Region();
+}
+
+// The windows of one bin over one target.  ev: the bin's reads in BAM order.  totals: MP only,
+// members[g] = sorted start positions of the strand's window-total members of DP group g.
+void replay_bin(Ctx& c, uint32_t tid, uint32_t len, const std::vector<Ev>& ev, int bin, bool mp,
+                const std::vector<std::vector<uint32_t>>* members) {
+  const PairReplayInput& in = c.in;
+  const uint32_t G = (uint32_t)in.window_width.size();
+  const int32_t seed = mp ? in.mp_seed : in.dp_seed;
+  // positions where the window count can change: entries, exits inside the target, and the flush
+  std::vector<uint32_t> pos;
+  pos.reserve(2 * ev.size() + 1);
+  for (const Ev& e : ev) {
+    pos.push_back(e.start1);
+    const double w = ceil(in.window_width[e.group]);
+    if ((double)e.start1 + w <= (double)len) pos.push_back(e.start1 + (uint32_t)w);
+  }
+  if (len >= 1) pos.push_back(1);   // a seed of 0 is reached before any read enters
+  pos.push_back(len + 1);
+  std::sort(pos.begin(), pos.end());
+  pos.erase(std::unique(pos.begin(), pos.end()), pos.end());
+
+  std::vector<std::deque<size_t>> win(G);
+  int32_t metric = 0;
+  size_t next = 0;
+  Region r;
+  const char strand = mp ? (bin == 0 ? 'F' : 'R') : (bin / 3 == 0 ? 'F' : 'R');
+  const char* orient = mp ? nullptr : kOrient[bin % 3];
+
+  auto total_at = [&](uint32_t p) -> int64_t {
+    int64_t t = 0;
+    for (uint32_t g = 0; g < G; g++) {
+      const std::vector<uint32_t>& s = (*members)[g];
+      if (s.empty()) continue;
+      const int64_t lo = (int64_t)p - (int64_t)ceil(in.window_width[g]);   // in window: start > lo
+      const auto hi_it = std::upper_bound(s.begin(), s.end(), p);
+      const auto lo_it = lo < 0 ? s.begin() : std::upper_bound(s.begin(), hi_it, (uint32_t)std::min<int64_t>(lo, 0xFFFFFFFFll));
+      t += hi_it - lo_it;
+    }
+    return t;
+  };
+  // the per-position test and region bookkeeping, after the position's entries and exits
+  auto check = [&](uint32_t p) {
+    bool above;
+    int64_t total = 0;
+    if (mp) {
+      total = total_at(p);
+      const bool enriched = (total > 0) && ((double)metric >= in.mp_seed_fraction * (double)total);
+      above = (metric >= seed) && enriched && (p <= len);
+    } else {
+      above = (metric >= seed) && (p <= len);
+    }
+    if (above) {
+      if (r.start == kUndefPos) {
+        r.start = p;
+        r.max_count = (uint32_t)metric;
+        r.max_total = (uint32_t)total;
+        r.reads.clear();
+        r.redundant = 0;
+        for (uint32_t g = 0; g < G; g++)
+          for (size_t k : win[g]) {
+            r.reads.push_back(ev[k].idx);
+            if (ev[k].redundant) r.redundant++;
+          }
+      } else if ((uint32_t)metric > r.max_count) {
+        r.max_count = (uint32_t)metric;
+        r.max_total = (uint32_t)total;
+      }
+    } else if (r.start != kUndefPos) {
+      close_region(c, r, tid, p - 1, strand, orient, mp);
+    }
+  };
+
+  for (size_t pi = 0; pi < pos.size(); pi++) {
+    const uint32_t p = pos[pi];
+    // entries at p, in BAM order; an open region takes them at once
+    while (next < ev.size() && ev[next].start1 == p) {
+      win[ev[next].group].push_back(next);
+      metric++;
+      if (r.start != kUndefPos) {
+        r.reads.push_back(ev[next].idx);
+        if (ev[next].redundant) r.redundant++;
+      }
+      next++;
+    }
+    // exits
+    for (uint32_t g = 0; g < G; g++)
+      while (!win[g].empty() && ((double)p - (double)ev[win[g].front()].start1 >= in.window_width[g])) {
+        win[g].pop_front();
+        metric--;
+      }
+    check(p);
+    // MP: between this position and the next event the count is fixed, but the total is not
+    if (mp && metric >= seed && pi + 1 < pos.size())
+      for (uint32_t q = p + 1; q < pos[pi + 1] && q <= len; q++) check(q);
+  }
+}
+
+}  // namespace
+
+int pair_replay(const PairReplayInput& in, PairReplayResult& out) {
+  Ctx c{in, out, {}};
+  const uint32_t G = (uint32_t)in.window_width.size();
+  // descriptors of every compacted event
+  c.desc.resize(in.n_ev);
+  std::vector<uint32_t> ev_tid(in.n_ev);
+  for (uint64_t k = 0; k < in.n_ev; k++) {
+    const PairEvent& e = in.ev[k];
+    const uint32_t t = (uint32_t)(std::upper_bound(in.tpoff.begin(), in.tpoff.end(), e.start) - in.tpoff.begin()) - 1;
+    ev_tid[k] = t;
+    const uint32_t s1 = e.start - in.tpoff[t] + 1, e1 = e.end - in.tpoff[t];
+    if ((e.code & kPairDpBinMask) != kPairNoBin) {
+      if (e.group >= G) return BSQ_ERR_INVALID;
+      c.desc[k] = dp_key(e, in.names + k * kPairNameSlot, in.r1_prefix[e.group], in.r2_prefix[e.group]) + "__" +
+                  std::to_string(s1) + "__" + std::to_string(e1);
+    } else {
+      c.desc[k] = std::to_string(s1) + "__" + std::to_string(e1);
+    }
+  }
+  for (uint32_t t : in.order) {
+    const uint32_t len = in.tpoff[t + 1] - in.tpoff[t] - 1;
+    const uint32_t c0 = in.tpoff[t], c1 = in.tpoff[t] + len;
+    // this target's events and members (both in BAM order, so contiguous and start-sorted)
+    auto ev_lo = std::lower_bound(in.ev, in.ev + in.n_ev, c0, [](const PairEvent& e, uint32_t v) { return e.start < v; });
+    auto ev_hi = std::lower_bound(ev_lo, in.ev + in.n_ev, c1 + 1, [](const PairEvent& e, uint32_t v) { return e.start < v; });
+    if (!in.piled[t]) continue;
+    std::vector<Ev> dp[6], mpe[2];
+    for (auto it = ev_lo; it != ev_hi; ++it) {
+      const uint64_t k = it - in.ev;
+      Ev x{it->start - c0 + 1, it->end - c0, it->group, it->redundant != 0, k};
+      const int bin = it->code & kPairDpBinMask;
+      if (bin != kPairNoBin) dp[bin].push_back(x);
+      if (in.mp && (it->code & kPairMpUnmapped)) mpe[(it->code & kPairRev) ? 1 : 0].push_back(x);
+    }
+    if (G) for (int b = 0; b < 6; b++) replay_bin(c, t, len, dp[b], b, false, nullptr);
+    if (in.mp && G) {
+      std::vector<std::vector<uint32_t>> members[2] = {std::vector<std::vector<uint32_t>>(G),
+                                                       std::vector<std::vector<uint32_t>>(G)};
+      const uint32_t* ms = in.mem_start;
+      const uint64_t lo = std::lower_bound(ms, ms + in.n_mem, c0) - ms;
+      const uint64_t hi = std::lower_bound(ms + lo, ms + in.n_mem, c1 + 1) - ms;
+      for (uint64_t k = lo; k < hi; k++) {
+        const uint32_t key = in.mem_key[k];
+        if (key / 2 >= G) return BSQ_ERR_INVALID;
+        members[key & 1][key / 2].push_back(ms[k] - c0 + 1);
+      }
+      for (int b = 0; b < 2; b++) replay_bin(c, t, len, mpe[b], b, true, &members[b]);
+    }
+  }
+  return BSQ_OK;
+}
+
+}  // namespace host
+}  // namespace bsq
+
+namespace {
+
+template <class Less>
+int write_regions(const char* path, const char* const* names, const bsq_pair_region* regions, uint64_t n,
+                  const char* text, bool mp, Less less) {
+  if (!path || (n && (!regions || !names || !text))) return BSQ_ERR_INVALID;
+  std::vector<const bsq_pair_region*> v(n);
+  for (uint64_t i = 0; i < n; i++) v[i] = regions + i;
+  std::sort(v.begin(), v.end(), [&](const bsq_pair_region* a, const bsq_pair_region* b) { return less(*a, *b); });
+  std::ofstream out(path);
+  if (!out) return BSQ_ERR_INVALID;
+  if (mp)
+    out << "seq_id,start,end,strand,length,max_unpaired_count,max_window_total_count,redundant,unpaired_reads\n";
+  else
+    out << "seq_id,start,end,strand,orientation,length,max_discordant_count,redundant,discordant_pairs\n";
+  for (const bsq_pair_region* r : v) {
+    out << names[r->target] << "," << r->start << "," << r->end << "," << r->strand << ",";
+    if (!mp) out << std::string(r->orientation, strnlen(r->orientation, 3)) << ",";
+    out << (r->end - r->start + 1) << "," << r->max_count << ",";
+    if (mp) out << r->max_total << ",";
+    out << (r->redundant ? 1 : 0) << "," << std::string(text + r->text_off, r->text_len) << "\n";
+  }
+  return out ? BSQ_OK : BSQ_ERR_INVALID;
+}
+
+}  // namespace
+
+extern "C" int bsq_write_dp_candidate_regions(const char* path, const char* const* target_names,
+                                              const bsq_pair_region* regions, uint64_t n, const char* text) {
+  // sorted by (seq_id, start, strand, orientation): identify_mutations.cpp:2553-2560
+  return write_regions(path, target_names, regions, n, text, false,
+                       [&](const bsq_pair_region& a, const bsq_pair_region& b) {
+                         const std::string sa = target_names[a.target], sb = target_names[b.target];
+                         if (sa != sb) return sa < sb;
+                         if (a.start != b.start) return a.start < b.start;
+                         if (a.strand != b.strand) return a.strand < b.strand;
+                         return std::string(a.orientation, strnlen(a.orientation, 3)) <
+                                std::string(b.orientation, strnlen(b.orientation, 3));
+                       });
+}
+
+extern "C" int bsq_write_mp_candidate_regions(const char* path, const char* const* target_names,
+                                              const bsq_pair_region* regions, uint64_t n, const char* text) {
+  // sorted by (seq_id, start, strand): identify_mutations.cpp:2527-2533
+  return write_regions(path, target_names, regions, n, text, true,
+                       [&](const bsq_pair_region& a, const bsq_pair_region& b) {
+                         const std::string sa = target_names[a.target], sb = target_names[b.target];
+                         if (sa != sb) return sa < sb;
+                         if (a.start != b.start) return a.start < b.start;
+                         return a.strand < b.strand;
+                       });
+}

@@ -15,7 +15,7 @@ from __future__ import annotations
 import concurrent.futures as cf
 import dataclasses
 import os
-from dataclasses import dataclass, field
+from dataclasses import dataclass, field, replace
 
 import numpy as np
 
@@ -98,6 +98,11 @@ class Sample:
     n_quality: int
     variants: list = field(default_factory=list)
     xj: np.ndarray | None = None   # uint8, XJ tag present; None when no record has one
+    # pair annotations (with_pairs): TLEN, XP orientation code (0 FR, 1 RF, 2 FF, 3 none), read names
+    isize: np.ndarray | None = None
+    xp: np.ndarray | None = None
+    qname_off: np.ndarray | None = None
+    qname: np.ndarray | None = None
 
     @property
     def n_reads(self) -> int:
@@ -591,6 +596,66 @@ def bam_groups(s: Sample):
     return ids, base, count
 
 
+def with_pairs(s: Sample, seed: int = 0, discordant_sites: int = 6, unmapped_sites: int = 6, site_span: int = 250,
+               site_fraction: float = 0.6, background_discordant: float = 0.002, background_unmapped: float = 0.004,
+               no_xp_fraction: float = 0.0, supplementary_fraction: float = 0.001) -> Sample:
+    """Pair annotations for a sample, as breseq's alignment resolution leaves them
+    (src/breseq/resolve_alignments.cpp:1255-1300): read names <read file + 1>:<fragment>, TLEN, and the
+    XP orientation of every pair with both mates mapped.  Paired reads are proper pairs with XP FR,
+    except near `discordant_sites` breakpoints (and a background rate), where pairs are discordant
+    (not proper, XP FR / RF / FF, long TLEN), and near `unmapped_sites` insertions (and a background
+    rate), where the mate is unmapped (0x8, no XP, TLEN 0).  no_xp_fraction of the discordant reads
+    lose their XP tag.  The scoring passes read none of these fields (the flag filter is 0x704), so
+    their results do not change."""
+    rng = np.random.default_rng(seed)
+    n = s.n_reads
+    flag = s.flag.astype(np.uint16).copy()
+    paired = (flag & FLAG_PAIRED) != 0
+    col = s.target_offset[s.tid].astype(np.int64) + s.pos.astype(np.int64)
+    total = int(s.target_offset[-1])
+    near = lambda sites: np.isin(col // site_span, (rng.integers(0, max(1, total), sites) // site_span)) \
+        if sites else np.zeros(n, bool)
+    disc = paired & ((near(discordant_sites) & (rng.random(n) < site_fraction)) | (rng.random(n) < background_discordant))
+    unm = paired & ~disc & ((near(unmapped_sites) & (rng.random(n) < site_fraction)) | (rng.random(n) < background_unmapped))
+    flag[disc | unm] &= np.uint16(~FLAG_PROPER & 0xFFFF)
+    flag[unm] |= np.uint16(0x8)
+    flag[unm] &= np.uint16(~FLAG_MREVERSE & 0xFFFF)
+    flag[rng.random(n) < supplementary_fraction] |= np.uint16(0x800)
+    xp = np.where(paired, 0, 3).astype(np.uint8)
+    xp[disc] = rng.integers(0, 3, int(disc.sum())).astype(np.uint8)
+    xp[unm] = 3
+    xp[disc & (rng.random(n) < no_xp_fraction)] = 3
+    isize = np.zeros(n, dtype=np.int32)
+    mag = rng.integers(250, 450, n)
+    isize[paired] = np.where(rng.random(int(paired.sum())) < 0.5, 1, -1) * mag[paired]
+    isize[disc] = rng.integers(-60000, 60000, int(disc.sum()))
+    isize[unm] = 0
+    # names "<read file + 1>:<fragment>", assembled digit by digit
+    a = s.read_file.astype(np.int64) + 1
+    b = np.arange(n, dtype=np.int64) // 2
+    nd_a = np.maximum(1, np.floor(np.log10(np.maximum(a, 1))).astype(np.int64) + 1)
+    nd_b = np.maximum(1, np.floor(np.log10(np.maximum(b, 1))).astype(np.int64) + 1)
+    ln = nd_a + 1 + nd_b
+    qname_off = np.zeros(n + 1, dtype=np.uint64)
+    qname_off[1:] = np.cumsum(ln)
+    qname = np.zeros(int(qname_off[-1]), dtype=np.uint8)
+    o = qname_off[:-1].astype(np.int64)
+    for d in range(int(nd_a.max()) if n else 0):
+        k = d < nd_a
+        qname[o[k] + nd_a[k] - 1 - d] = (a[k] // 10 ** d) % 10 + 48
+    qname[o + nd_a] = ord(":")
+    for d in range(int(nd_b.max()) if n else 0):
+        k = d < nd_b
+        qname[o[k] + nd_a[k] + nd_b[k] - d] = (b[k] // 10 ** d) % 10 + 48
+    if n and no_xp_fraction > 0:   # a name without ':' takes the fallback key
+        i = int(rng.integers(0, n))
+        names = [qname[int(qname_off[j]):int(qname_off[j + 1])].tobytes() for j in range(n)]
+        names[i] = b"plainname"
+        qname_off[1:] = np.cumsum([len(x) for x in names])
+        qname = np.frombuffer(b"".join(names), dtype=np.uint8).copy()
+    return replace(s, flag=flag, isize=isize, xp=xp, qname_off=qname_off, qname=qname)
+
+
 def bam_bytes(s: Sample, level: int = 6, block_payload: int = 0xFF00, seed: int = 0, rg_tags: bool = True) -> bytes:
     """The sample as a coordinate-sorted BAM (SAM/BAM specification §4.2), compressed in BGZF blocks
     the way htslib writes them: the header in its own blocks, a record never split across blocks
@@ -628,7 +693,10 @@ def bam_bytes(s: Sample, level: int = 6, block_payload: int = 0xFF00, seed: int 
         ops, lens = cig & 0xF, cig >> 4
         rlen = int(lens[(ops == 0) | (ops == 2) | (ops == 3) | (ops == 7) | (ops == 8)].sum())
         pos = int(s.pos[i])
-        name = f"r{i}".encode() + b"\0"
+        if s.qname is not None:
+            name = s.qname[int(s.qname_off[i]): int(s.qname_off[i + 1])].tobytes() + b"\0"
+        else:
+            name = f"r{i}".encode() + b"\0"
         so = int(s.seq_off[i])
         seq = s.seq[so // 2: so // 2 + (L + 1) // 2].tobytes()
         if L & 1 and seq:   # the spare low nibble of an odd-length read is zero in BAM
@@ -649,8 +717,14 @@ def bam_bytes(s: Sample, level: int = 6, block_payload: int = 0xFF00, seed: int 
             aux += b"RGZ" + ids[int(s.read_group[i])].encode() + b"\0"
         if rng.random() < 0.1:
             aux += b"ZBBs" + struct.pack("<I", 3) + struct.pack("<3h", 1, -2, 3)
+        if s.xp is not None:
+            if s.xp[i] <= 2:
+                aux += b"XPZ" + (b"FR", b"RF", b"FF")[int(s.xp[i])] + b"\0"
+            elif rng.random() < 0.2:
+                aux += b"XPZRR\0"    # an XP value other than FR / RF / FF: no orientation
+        tlen = int(s.isize[i]) if s.isize is not None else 0
         body = struct.pack("<iiBBHHHiiii", int(s.tid[i]), pos, len(name), int(s.mapq[i]), _reg2bin(pos, pos + max(rlen, 1)),
-                           nc, int(s.flag[i]), L, -1, -1, 0)
+                           nc, int(s.flag[i]), L, -1, -1, tlen)
         rec = body + name + cig.astype("<u4").tobytes() + seq + qual + aux
         rec = struct.pack("<i", len(rec)) + rec
         if len(buf) + len(rec) > block_payload and buf:

@@ -45,12 +45,15 @@ extern "C" {
 
 /* ---------------------------------------------------------------- BAM constants used by the path */
 #define BSQ_FLAG_PAIRED      0x1
+#define BSQ_FLAG_PROPER      0x2
 #define BSQ_FLAG_UNMAP       0x4
+#define BSQ_FLAG_MUNMAP      0x8
 #define BSQ_FLAG_REVERSE     0x10
 #define BSQ_FLAG_READ2       0x80
 #define BSQ_FLAG_SECONDARY   0x100
 #define BSQ_FLAG_QCFAIL      0x200
 #define BSQ_FLAG_DUP         0x400
+#define BSQ_FLAG_SUPPLEMENTARY 0x800
 /* htslib's default pileup filter (BAM_DEF_MASK); breseq never overrides it
  * (src/breseq/pileup_base.cpp:333-339). */
 #define BSQ_PILEUP_SKIP_MASK (BSQ_FLAG_UNMAP | BSQ_FLAG_SECONDARY | BSQ_FLAG_QCFAIL | BSQ_FLAG_DUP)
@@ -102,7 +105,21 @@ typedef struct bsq_read_soa {
     /* non-zero when the record carries an XJ:i tag (one side of a junction match); NULL when no
      * record does.  Only the soft-clipping tabulation reads it (src/breseq/soft_clipping.cpp:382-384). */
     const uint8_t*  xj;
+    /* Pair annotations, read only by the discordant / missing-pair scans (bsq_pair_candidates);
+     * NULL when absent.  isize: TLEN.  xp: the XP:Z pair orientation breseq writes
+     * (src/breseq/resolve_alignments.cpp:1255-1273) as BSQ_XP_FR / _RF / _FF, BSQ_XP_NONE when the
+     * tag is absent or holds anything else.  qname: read names concatenated without terminators,
+     * read i at [qname_off[i], qname_off[i+1]), at most 254 bytes each (the BAM limit). */
+    const int32_t*  isize;
+    const uint8_t*  xp;
+    const uint64_t* qname_off;
+    const char*     qname;
 } bsq_read_soa;
+
+#define BSQ_XP_FR   0
+#define BSQ_XP_RF   1
+#define BSQ_XP_FF   2
+#define BSQ_XP_NONE 3
 
 /* ---------------------------------------------------------------- pass 1: error counts */
 
@@ -469,8 +486,16 @@ typedef struct bsq_read_arrays {
     uint8_t*  seq;
     uint8_t*  qual;
     uint8_t*  xj;
+    /* pair annotations, each optional (NULL: not copied): isize [n_records], xp [n_records],
+     * qname_off [n_records + 1], qname [bsq_bam_name_bytes] */
+    int32_t*  isize;
+    uint8_t*  xp;
+    uint64_t* qname_off;
+    char*     qname;
 } bsq_read_arrays;
 int bsq_bam_copy_records(bsq_ctx* ctx, const bsq_bam* bam, const bsq_read_arrays* out);
+/* Bytes of the decoded records' read names (no terminators). */
+int bsq_bam_name_bytes(bsq_ctx* ctx, const bsq_bam* bam, uint64_t* bytes);
 
 /* Makes the decoded records a resident sample with the given reference (whose targets must be the
  * header's, in order and length), as bsq_load_sample does with host arrays.  The decoded arrays move
@@ -534,6 +559,60 @@ int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_
 
 /* Bytes the last pass call copied host-to-device and device-to-host (staged inputs, results). */
 int bsq_last_pass_bytes(const bsq_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
+
+/* ---------------------------------------------------------------- discordant / missing-pair scans */
+
+/* The discordant-pair (DP) and missing-pair (MP) candidate-region scans that breseq runs inside the
+ * identify_mutations pileup (identify_mutations.cpp:1395-1493 enter steps, 2358-2437 and 2439-2522
+ * sliding windows, 2524-2586 writers; groups at :883-913).  Read groups map to DP groups: a paired
+ * read-file set with a fitted paired-mapping distance, window width median + 2.42 * MAD.  Per bin
+ * (focal strand x XP orientation for DP, strand for MP) a region is a maximal run of positions where
+ * the reads that started within the window reach the seed; MP also needs the mate-unmapped reads to
+ * be at least missing_pair_seed_fraction of all primary mapped reads of that strand in the window. */
+typedef struct bsq_pair_params {
+    uint32_t        n_read_groups;       /* entries of dp_group (the sample's read-group indices) */
+    const int32_t*  dp_group;            /* per read group: its DP group, -1 when none */
+    uint32_t        n_dp_groups;         /* at most 255 */
+    const double*   window_width;        /* per DP group: median + 2.42 * MAD */
+    const uint32_t* r1_name_prefix;      /* per DP group: m_id + 1 of the set's R1 / R2 read file */
+    const uint32_t* r2_name_prefix;
+    int32_t         discordant_pair_seed;          /* --discordant-pair-seed, default 3 */
+    int32_t         predict_missing_pairs;         /* --predict-missing-pairs */
+    int32_t         missing_pair_seed;             /* --missing-pair-seed, default 3 */
+    double          missing_pair_seed_fraction;    /* --missing-pair-seed-fraction, default 0.25 */
+    /* per target: identify_mutations' deletion propagation cutoff; a target below 0 is not piled up
+     * (pileup_callback returns at once, identify_mutations.cpp:1318-1329) */
+    const double*   deletion_propagation_cutoff;
+} bsq_pair_params;
+
+/* One candidate region.  Text fields are in the result's text buffer at [text_off, text_off +
+ * text_len): DP "<read1>__<read2>__<r1_insert_size>__<read_start>__<read_end>" per read, MP
+ * "<read_start>__<read_end>", joined by ';'. */
+typedef struct bsq_pair_region {
+    uint32_t target;
+    uint32_t start;
+    uint32_t end;
+    char     strand;            /* 'F' or 'R' */
+    char     orientation[3];    /* DP: "FR", "RF" or "FF"; MP: "" */
+    uint32_t max_count;         /* max_discordant_count / max_unpaired_count */
+    uint32_t max_total;         /* MP: max_window_total_count; DP: 0 */
+    uint32_t redundant;         /* a majority of the region's reads have X1 > 1 */
+    uint32_t reserved;
+    uint64_t text_off;
+    uint64_t text_len;
+} bsq_pair_region;
+
+/* Runs the scans on a resident sample (needs the pair annotations of bsq_read_soa or a BAM load).
+ * Regions are in detection order; the writers sort them as breseq does. */
+int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* params, uint64_t* n_dp,
+                        uint64_t* n_mp, uint64_t* text_bytes);
+int bsq_pair_result_copy(bsq_ctx* ctx, bsq_pair_region* dp, uint64_t n_dp, bsq_pair_region* mp, uint64_t n_mp,
+                         char* text, uint64_t text_bytes);
+/* dp_candidate_regions.csv / mp_candidate_regions.csv (identify_mutations.cpp:2524-2586) */
+int bsq_write_dp_candidate_regions(const char* path, const char* const* target_names, const bsq_pair_region* regions,
+                                   uint64_t n, const char* text);
+int bsq_write_mp_candidate_regions(const char* path, const char* const* target_names, const bsq_pair_region* regions,
+                                   uint64_t n, const char* text);
 
 /* ---------------------------------------------------------------- scoring without allocation */
 

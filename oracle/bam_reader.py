@@ -62,13 +62,14 @@ def read_bam(data: bytes, groups=None):
         o += 8 + l_name
     ids, base, count = groups if groups is not None else ([], None, None)
     cols = {k: [] for k in ("tid", "pos", "flag", "mapq", "x1", "xl", "xr", "read_file", "read_group", "l_qseq",
-                            "n_cigar", "xj")}
-    cig, seq, qual = [], [], []
+                            "n_cigar", "xj", "isize", "xp")}
+    cig, seq, qual, qnames = [], [], [], []
     seen_unplaced = False
     int_fmt = {"c": "<b", "C": "<B", "s": "<h", "S": "<H", "i": "<i", "I": "<I"}
     fixed = {"A": 1, "c": 1, "C": 1, "s": 2, "S": 2, "i": 4, "I": 4, "f": 4}
     while o < len(stream):
         bs = struct.unpack_from("<i", stream, o)[0]
+        o_rec = o
         end = o + 4 + bs
         ref_id, pos, l_name, mapq, _bin, n_cig, flag, l_seq = struct.unpack_from("<iiBBHHHi", stream, o + 4)
         c0 = o + 36 + l_name
@@ -111,18 +112,26 @@ def read_bam(data: bytes, groups=None):
         rfile = 0
         if ids and base is not None and group < len(ids) and count[group] > 0:
             rfile = base[group] + (1 if (flag & 0x80) and count[group] > 1 else 0)
+        # XP: the pair orientation breseq writes as a Z string (resolve_alignments.cpp:1255-1273); anything
+        # else, or no tag, is no orientation (3)
+        xp = 3
+        if "XP" in tags and tags["XP"][0] in "ZH":
+            xp = {b"FR\0": 0, b"RF\0": 1, b"FF\0": 2}.get(bytes(tags["XP"][1]), 3)
+        tlen = struct.unpack_from("<i", stream, o_rec + 32)[0]
         for k, v in (("tid", ref_id), ("pos", pos), ("flag", flag), ("mapq", mapq),
                      ("x1", as_int("X1", 1) & 0xFFFFFFFF), ("xl", as_int("XL", -1)), ("xr", as_int("XR", -1)),
                      ("read_file", rfile), ("read_group", group), ("l_qseq", l_seq), ("n_cigar", n_cig),
-                     ("xj", 1 if "XJ" in tags else 0)):
+                     ("xj", 1 if "XJ" in tags else 0), ("isize", tlen), ("xp", xp)):
             cols[k].append(v)
+        qnames.append(stream[o_rec + 36:o_rec + 36 + l_name - 1])
         cig.append(np.frombuffer(stream[c0:s0], dtype="<u4"))
         sq = stream[s0:q0]
         ql = stream[q0:q0 + l_seq] + (b"\0" if l_seq & 1 else b"")
         seq.append(np.frombuffer(sq, dtype=np.uint8))
         qual.append(np.frombuffer(ql, dtype=np.uint8))
     dts = dict(tid=np.int32, pos=np.int32, flag=np.uint16, mapq=np.uint8, x1=np.uint32, xl=np.int32, xr=np.int32,
-               read_file=np.uint8, read_group=np.uint16, l_qseq=np.uint32, n_cigar=np.uint16, xj=np.uint8)
+               read_file=np.uint8, read_group=np.uint16, l_qseq=np.uint32, n_cigar=np.uint16, xj=np.uint8,
+               isize=np.int32, xp=np.uint8)
     rec = {k: np.array(v, dtype=dts[k]) for k, v in cols.items()}
     nc = rec["n_cigar"].astype(np.uint64)
     rec["cigar_off"] = np.concatenate([[0], np.cumsum(nc)[:-1]]).astype(np.uint64) if len(nc) else np.zeros(0, np.uint64)
@@ -131,4 +140,6 @@ def read_bam(data: bytes, groups=None):
     rec["cigar"] = np.concatenate(cig).astype(np.uint32) if cig else np.zeros(0, np.uint32)
     rec["seq"] = np.concatenate(seq) if seq else np.zeros(0, np.uint8)
     rec["qual"] = np.concatenate(qual) if qual else np.zeros(0, np.uint8)
+    rec["qname_off"] = np.concatenate([[0], np.cumsum([len(x) for x in qnames])]).astype(np.uint64)
+    rec["qname"] = np.frombuffer(b"".join(qnames), dtype=np.uint8).copy()
     return dict(header=dict(text=text, names=names, lengths=lengths), records=rec)

@@ -47,6 +47,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <functional>
 #include <limits>
 #include <map>
@@ -1823,3 +1824,227 @@ extern "C" double oracle_nbinom_cdf(double k, double size, double p) { return of
 extern "C" double oracle_lgam(double x) { return ofit::lgam(x); }
 extern "C" double oracle_lngamma(double x) { return ofit::lngamma(x); }
 extern "C" double oracle_gamma(double x) { return ofit::gamma_(x); }
+
+// ======================================================================================= pair scans
+// The discordant-pair (DP) and missing-pair (MP) candidate-region scans, walked position by position
+// as the identify_mutations pileup does:
+//   groups / window widths                 src/breseq/identify_mutations.cpp:883-913
+//   per-read enter steps (insert slot 0, at the read's start column)   :1395-1493
+//   check_discordant_completion            :2358-2437
+//   check_missing_pair_completion          :2439-2522
+//   at_target_start / at_target_end        :2028-2100, :2117-2137
+//   write_mp / write_dp_candidate_regions  :2524-2586
+// A target whose deletion propagation cutoff is below 0 is not walked (pileup_callback returns at
+// once, :1318-1329).
+namespace opair {
+
+struct DpRead { uint32_t start, end; std::string key; bool redundant; };
+struct MpRead { uint32_t start, end; bool redundant; };
+struct Group {
+  double w;
+  uint32_t r1, r2;
+  std::deque<DpRead> reads[6];
+  std::deque<MpRead> mp_reads[2];
+  std::deque<uint32_t> mp_all[2];
+};
+struct DpRegion { std::string seq_id; uint32_t start, end; char strand; std::string orientation; uint32_t max_count; bool redundant; std::string pairs; };
+struct MpRegion { std::string seq_id; uint32_t start, end; char strand; uint32_t max_count, max_total; bool redundant; std::string reads; };
+
+std::string dp_desc(const DpRead& r) { return r.key + "__" + std::to_string(r.start) + "__" + std::to_string(r.end); }
+std::string mp_desc(const MpRead& r) { return std::to_string(r.start) + "__" + std::to_string(r.end); }
+
+}  // namespace opair
+
+extern "C" int oracle_pair_candidates(const bsq_reference* ref, const bsq_read_soa* rd, const bsq_pair_params* prm,
+                                      const char* const* target_names, const char* dp_path, const char* mp_path,
+                                      char* errbuf, int errcap) {
+  using namespace opair;
+  Data d;
+  d.ref = ref;
+  d.rd = rd;
+  int rc = prepare(d);
+  if (rc != BSQ_OK) { if (errbuf) snprintf(errbuf, errcap, "%s", d.err.c_str()); return rc; }
+  const uint32_t G = prm->n_dp_groups;
+  std::vector<Group> groups(G);
+  for (uint32_t g = 0; g < G; g++) { groups[g].w = prm->window_width[g]; groups[g].r1 = prm->r1_name_prefix[g]; groups[g].r2 = prm->r2_name_prefix[g]; }
+  const bool dp_on = G > 0, mp_on = prm->predict_missing_pairs && G > 0;
+  static const char* kOrientName[3] = {"FR", "RF", "FF"};
+  int32_t dp_metric[6], mp_metric[2], mp_total[2];
+  uint32_t dp_start[6], dp_max[6], dp_red[6], mp_start[2], mp_max[2], mp_maxt[2], mp_red[2];
+  std::vector<std::string> dp_desc_v[6], mp_desc_v[2];
+  std::vector<DpRegion> dp_regions;
+  std::vector<MpRegion> mp_regions;
+  for (uint32_t t : std::vector<uint32_t>(ref->target_order, ref->target_order + ref->n_target_order)) {
+    if (prm->deletion_propagation_cutoff[t] < 0.0) continue;
+    const uint32_t len = (uint32_t)(ref->target_offset[t + 1] - ref->target_offset[t]);
+    const std::string seq_id = target_names[t];
+    // at_target_start
+    for (int b = 0; b < 6; b++) {
+      for (Group& g : groups) g.reads[b].clear();
+      dp_metric[b] = 0; dp_start[b] = kUndef; dp_max[b] = 0; dp_red[b] = 0; dp_desc_v[b].clear();
+    }
+    for (int b = 0; b < 2; b++) {
+      for (Group& g : groups) { g.mp_reads[b].clear(); g.mp_all[b].clear(); }
+      mp_metric[b] = 0; mp_total[b] = 0; mp_start[b] = kUndef; mp_max[b] = 0; mp_maxt[b] = 0; mp_red[b] = 0;
+      mp_desc_v[b].clear();
+    }
+    auto check_dp = [&](uint32_t position) {
+      for (int bin = 0; bin < 6; bin++) {
+        for (Group& g : groups)
+          while (!g.reads[bin].empty() && ((double)position - (double)g.reads[bin].front().start >= g.w)) {
+            g.reads[bin].pop_front();
+            --dp_metric[bin];
+          }
+        const bool above = (dp_metric[bin] >= prm->discordant_pair_seed) && (position <= len);
+        if (above) {
+          if (dp_start[bin] == kUndef) {
+            dp_start[bin] = position;
+            dp_max[bin] = (uint32_t)dp_metric[bin];
+            dp_desc_v[bin].clear();
+            dp_red[bin] = 0;
+            for (Group& g : groups)
+              for (const DpRead& r : g.reads[bin]) { dp_desc_v[bin].push_back(dp_desc(r)); if (r.redundant) ++dp_red[bin]; }
+          } else if ((uint32_t)dp_metric[bin] > dp_max[bin]) {
+            dp_max[bin] = (uint32_t)dp_metric[bin];
+          }
+        } else if (dp_start[bin] != kUndef) {
+          DpRegion x;
+          x.seq_id = seq_id; x.start = dp_start[bin]; x.end = position - 1;
+          x.strand = (bin / 3 == 0) ? 'F' : 'R'; x.orientation = kOrientName[bin % 3]; x.max_count = dp_max[bin];
+          x.redundant = (2 * dp_red[bin] > dp_desc_v[bin].size());
+          for (size_t k = 0; k < dp_desc_v[bin].size(); k++) { if (k) x.pairs += ";"; x.pairs += dp_desc_v[bin][k]; }
+          dp_regions.push_back(x);
+          dp_start[bin] = kUndef; dp_max[bin] = 0; dp_desc_v[bin].clear(); dp_red[bin] = 0;
+        }
+      }
+    };
+    auto check_mp = [&](uint32_t position) {
+      for (int bin = 0; bin < 2; bin++) {
+        for (Group& g : groups) {
+          while (!g.mp_reads[bin].empty() && ((double)position - (double)g.mp_reads[bin].front().start >= g.w)) {
+            g.mp_reads[bin].pop_front();
+            --mp_metric[bin];
+          }
+          while (!g.mp_all[bin].empty() && ((double)position - (double)g.mp_all[bin].front() >= g.w)) {
+            g.mp_all[bin].pop_front();
+            --mp_total[bin];
+          }
+        }
+        const bool enriched = (mp_total[bin] > 0) &&
+                              ((double)mp_metric[bin] >= prm->missing_pair_seed_fraction * (double)mp_total[bin]);
+        const bool above = (mp_metric[bin] >= prm->missing_pair_seed) && enriched && (position <= len);
+        if (above) {
+          if (mp_start[bin] == kUndef) {
+            mp_start[bin] = position;
+            mp_max[bin] = (uint32_t)mp_metric[bin];
+            mp_maxt[bin] = (uint32_t)mp_total[bin];
+            mp_desc_v[bin].clear();
+            mp_red[bin] = 0;
+            for (Group& g : groups)
+              for (const MpRead& r : g.mp_reads[bin]) { mp_desc_v[bin].push_back(mp_desc(r)); if (r.redundant) ++mp_red[bin]; }
+          } else if ((uint32_t)mp_metric[bin] > mp_max[bin]) {
+            mp_max[bin] = (uint32_t)mp_metric[bin];
+            mp_maxt[bin] = (uint32_t)mp_total[bin];
+          }
+        } else if (mp_start[bin] != kUndef) {
+          MpRegion x;
+          x.seq_id = seq_id; x.start = mp_start[bin]; x.end = position - 1; x.strand = (bin == 0) ? 'F' : 'R';
+          x.max_count = mp_max[bin]; x.max_total = mp_maxt[bin];
+          x.redundant = (2 * mp_red[bin] > mp_desc_v[bin].size());
+          for (size_t k = 0; k < mp_desc_v[bin].size(); k++) { if (k) x.reads += ";"; x.reads += mp_desc_v[bin][k]; }
+          mp_regions.push_back(x);
+          mp_start[bin] = kUndef; mp_max[bin] = 0; mp_maxt[bin] = 0; mp_desc_v[bin].clear(); mp_red[bin] = 0;
+        }
+      }
+    };
+    uint64_t r = d.tgt_begin[t];
+    const uint64_t r_end = d.tgt_end[t];
+    for (uint32_t position = 1; position <= len; position++) {
+      // the pileup's reads that start at this column, in BAM order
+      for (; r < r_end && (uint64_t)rd->pos[r] + 1 <= position; r++) {
+        if ((uint64_t)rd->pos[r] + 1 < position) continue;
+        const ReadInfo& ri = d.info[r];
+        if (ri.skip) continue;
+        const uint32_t f = rd->flag[r];
+        const uint32_t rg = rd->read_group[r];
+        const int gi = rg < prm->n_read_groups ? prm->dp_group[rg] : -1;
+        const uint32_t end1 = (uint32_t)ri.endpos;
+        const bool redundant = rd->x1[r] > 1;
+        if (dp_on && (f & BSQ_FLAG_PAIRED) && !(f & BSQ_FLAG_UNMAP) && !(f & BSQ_FLAG_PROPER) &&
+            !(f & (BSQ_FLAG_SECONDARY | BSQ_FLAG_SUPPLEMENTARY | BSQ_FLAG_MUNMAP)) && gi >= 0) {
+          const Group& g = groups[gi];
+          const int s = ri.rev ? 1 : 0;
+          const int o = rd->xp[r] <= 2 ? rd->xp[r] : -1;
+          if (o < 0) continue;   // no usable orientation: the rest of this read's processing is skipped
+          const int bin = s * 3 + o;
+          const bool focal_is_r1 = !(f & BSQ_FLAG_READ2);
+          const std::string fname(rd->qname + rd->qname_off[r], rd->qname_off[r + 1] - rd->qname_off[r]);
+          const size_t colon = fname.find(':');
+          std::string read1_name, read2_name;
+          if (colon != std::string::npos) {
+            const std::string counter = fname.substr(colon + 1);
+            read1_name = std::to_string(g.r1) + ":" + counter;
+            read2_name = std::to_string(g.r2) + ":" + counter;
+          } else {
+            read1_name = focal_is_r1 ? fname : "";
+            read2_name = focal_is_r1 ? "" : fname;
+          }
+          const int32_t r1_insert_size = focal_is_r1 ? rd->isize[r] : -rd->isize[r];
+          DpRead dr{position, end1, read1_name + "__" + read2_name + "__" + std::to_string(r1_insert_size), redundant};
+          groups[gi].reads[bin].push_back(dr);
+          ++dp_metric[bin];
+          if (dp_start[bin] != kUndef) { dp_desc_v[bin].push_back(dp_desc(dr)); if (dr.redundant) ++dp_red[bin]; }
+        }
+        if (mp_on && !(f & BSQ_FLAG_UNMAP) && !(f & (BSQ_FLAG_SECONDARY | BSQ_FLAG_SUPPLEMENTARY)) && gi >= 0) {
+          const int bin = ri.rev ? 1 : 0;
+          groups[gi].mp_all[bin].push_back(position);
+          ++mp_total[bin];
+          if ((f & BSQ_FLAG_PAIRED) && (f & BSQ_FLAG_MUNMAP)) {
+            MpRead mr{position, end1, redundant};
+            groups[gi].mp_reads[bin].push_back(mr);
+            ++mp_metric[bin];
+            if (mp_start[bin] != kUndef) { mp_desc_v[bin].push_back(mp_desc(mr)); if (mr.redundant) ++mp_red[bin]; }
+          }
+        }
+      }
+      if (dp_on) check_dp(position);
+      if (mp_on) check_mp(position);
+    }
+    if (dp_on) check_dp(len + 1);
+    if (mp_on) check_mp(len + 1);
+  }
+  if (dp_path) {
+    std::sort(dp_regions.begin(), dp_regions.end(), [](const DpRegion& a, const DpRegion& b) {
+      if (a.seq_id != b.seq_id) return a.seq_id < b.seq_id;
+      if (a.start != b.start) return a.start < b.start;
+      if (a.strand != b.strand) return a.strand < b.strand;
+      return a.orientation < b.orientation;
+    });
+    std::ostringstream o;
+    o << "seq_id,start,end,strand,orientation,length,max_discordant_count,redundant,discordant_pairs\n";
+    for (const DpRegion& x : dp_regions)
+      o << x.seq_id << "," << x.start << "," << x.end << "," << x.strand << "," << x.orientation << ","
+        << (x.end - x.start + 1) << "," << x.max_count << "," << (x.redundant ? 1 : 0) << "," << x.pairs << "\n";
+    FILE* f = fopen(dp_path, "w");
+    if (!f) return BSQ_ERR_INVALID;
+    fwrite(o.str().data(), 1, o.str().size(), f);
+    fclose(f);
+  }
+  if (mp_path) {
+    std::sort(mp_regions.begin(), mp_regions.end(), [](const MpRegion& a, const MpRegion& b) {
+      if (a.seq_id != b.seq_id) return a.seq_id < b.seq_id;
+      if (a.start != b.start) return a.start < b.start;
+      return a.strand < b.strand;
+    });
+    std::ostringstream o;
+    o << "seq_id,start,end,strand,length,max_unpaired_count,max_window_total_count,redundant,unpaired_reads\n";
+    for (const MpRegion& x : mp_regions)
+      o << x.seq_id << "," << x.start << "," << x.end << "," << x.strand << "," << (x.end - x.start + 1) << ","
+        << x.max_count << "," << x.max_total << "," << (x.redundant ? 1 : 0) << "," << x.reads << "\n";
+    FILE* f = fopen(mp_path, "w");
+    if (!f) return BSQ_ERR_INVALID;
+    fwrite(o.str().data(), 1, o.str().size(), f);
+    fclose(f);
+  }
+  return BSQ_OK;
+}

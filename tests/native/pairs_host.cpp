@@ -1,0 +1,91 @@
+// Test driver: the library's discordant / missing-pair scan with the device steps done on the host.
+// pair_classify_one (bsq_pairs.h, shared with the classification kernel) classifies every read; the
+// window entries and MP window-total members are compacted in BAM order exactly as the scatter
+// kernel lays them out; host::pair_replay (bsq_pairs_host.cpp, the library's own replay) and the
+// library's CSV writers produce the files.  Compared with the oracle's position-by-position walk by
+// tests/test_pairs.py.
+#include <cuda_runtime.h>   // vector types and alignment macros of the shared headers; nothing is called
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+#include "../../breseq_gb300/csrc/bsq_host.h"
+#include "../../breseq_gb300/csrc/bsq_pairs.h"
+
+using namespace bsq;
+
+extern "C" int host_pair_candidates(const bsq_reference* ref, const bsq_read_soa* rd, const bsq_pair_params* p,
+                                    const char* const* target_names, const char* dp_path, const char* mp_path) {
+  const uint32_t T = ref->n_targets;
+  std::vector<uint32_t> tpoff(T + 1);
+  for (uint32_t t = 0; t <= T; t++) tpoff[t] = (uint32_t)(ref->target_offset[t] + t);
+  std::vector<uint8_t> called(T, 0);
+  for (uint32_t i = 0; i < ref->n_target_order; i++) called[ref->target_order[i]] = 1;
+  const bool mp = p->predict_missing_pairs && p->n_dp_groups > 0;
+  std::vector<PairEvent> ev;
+  std::vector<char> names;
+  std::vector<uint32_t> mem_start;
+  std::vector<uint16_t> mem_key;
+  for (uint64_t i = 0; i < rd->n_reads; i++) {
+    const uint32_t t = (uint32_t)rd->tid[i];
+    uint32_t rlen = 0;
+    for (uint32_t k = 0; k < rd->n_cigar[i]; k++) {
+      const uint32_t w = rd->cigar[rd->cigar_off[i] + k], op = w & 0xF;
+      if (op == 0 || op == 2 || op == 3 || op == 7 || op == 8) rlen += w >> 4;
+    }
+    uint32_t dflags = 0;
+    if ((rd->flag[i] & BSQ_PILEUP_SKIP_MASK) || !called[t]) dflags |= kSkip;
+    if (rd->flag[i] & BSQ_FLAG_REVERSE) dflags |= kRev;
+    const uint32_t g = rd->read_group[i];
+    const int32_t gi = g < p->n_read_groups ? p->dp_group[g] : -1;
+    uint8_t code, grp;
+    uint32_t sel, mem;
+    pair_classify_one(dflags, rd->flag[i], rd->xp[i], gi, mp, code, grp, sel, mem);
+    const uint32_t start = tpoff[t] + (uint32_t)rd->pos[i];
+    if (sel) {
+      PairEvent x;
+      x.rec = (uint32_t)i;
+      x.start = start;
+      x.end = start + rlen;
+      x.isize = rd->isize[i];
+      x.code = code;
+      x.group = grp;
+      x.redundant = rd->x1[i] > 1;
+      const uint64_t len = rd->qname_off[i + 1] - rd->qname_off[i];
+      x.name_len = (uint8_t)len;
+      ev.push_back(x);
+      names.resize(ev.size() * kPairNameSlot, 0);
+      memcpy(names.data() + (ev.size() - 1) * kPairNameSlot, rd->qname + rd->qname_off[i], len);
+    }
+    if (mem) {
+      mem_start.push_back(start);
+      mem_key.push_back((uint16_t)(grp * 2 + ((code & kPairRev) ? 1 : 0)));
+    }
+  }
+  host::PairReplayInput in;
+  in.tpoff = tpoff;
+  in.order.assign(ref->target_order, ref->target_order + ref->n_target_order);
+  in.piled.assign(T, 0);
+  for (uint32_t t : in.order) in.piled[t] = p->deletion_propagation_cutoff[t] >= 0.0 ? 1 : 0;
+  in.window_width.assign(p->window_width, p->window_width + p->n_dp_groups);
+  in.r1_prefix.assign(p->r1_name_prefix, p->r1_name_prefix + p->n_dp_groups);
+  in.r2_prefix.assign(p->r2_name_prefix, p->r2_name_prefix + p->n_dp_groups);
+  in.dp_seed = p->discordant_pair_seed;
+  in.mp_seed = p->missing_pair_seed;
+  in.mp_seed_fraction = p->missing_pair_seed_fraction;
+  in.mp = mp;
+  in.ev = ev.data();
+  in.n_ev = ev.size();
+  in.names = names.data();
+  in.mem_start = mem_start.data();
+  in.mem_key = mem_key.data();
+  in.n_mem = mem_start.size();
+  host::PairReplayResult out;
+  int rc = host::pair_replay(in, out);
+  if (rc != BSQ_OK) return rc;
+  if (dp_path) rc = bsq_write_dp_candidate_regions(dp_path, target_names, out.dp.data(), out.dp.size(), out.text.data());
+  if (rc == BSQ_OK && mp_path)
+    rc = bsq_write_mp_candidate_regions(mp_path, target_names, out.mp.data(), out.mp.size(), out.text.data());
+  return rc;
+}

@@ -12,7 +12,7 @@ from tests import bam_cases, compare, samples
 pytestmark = pytest.mark.gpu
 
 FIELDS = ("tid", "pos", "flag", "mapq", "x1", "xl", "xr", "read_file", "read_group", "l_qseq", "n_cigar", "cigar_off",
-          "seq_off", "cigar", "seq", "qual", "xj")
+          "seq_off", "cigar", "seq", "qual", "xj", "isize", "xp", "qname_off", "qname")
 
 
 @pytest.fixture(scope="module")
@@ -35,7 +35,7 @@ def check(sc, data, groups):
     hdr, (n, nc, nb), g = gpu_decode(sc, data, groups)
     o = bam_reader.read_bam(data, groups)
     assert hdr == o["header"]
-    size = {"cigar": nc, "seq": nb // 2, "qual": nb}
+    size = {"cigar": nc, "seq": nb // 2, "qual": nb, "qname_off": n + 1, "qname": len(o["records"]["qname"])}
     assert n == len(o["records"]["tid"])
     for k in FIELDS:
         assert np.array_equal(g[k][:size.get(k, n)], o["records"][k]), k

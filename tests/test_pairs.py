@@ -1,0 +1,140 @@
+"""Discordant-pair / missing-pair candidate regions on the CPU: the library's classification
+(pair_classify_one) and sliding-window replay (host::pair_replay), driven on the host by
+tests/native/pairs_host.cpp, against the oracle's position-by-position walk of the reference's
+windows; the written CSV files must be identical.  The device path is checked against the same
+oracle by tests/test_gpu_pairs.py."""
+import ctypes as C
+import dataclasses
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from breseq_gb300 import abi, synth
+from breseq_gb300.api import PairSettings, pair_params
+from oracle import pyoracle as po
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRCS = [os.path.join(ROOT, "tests", "native", "pairs_host.cpp"),
+        os.path.join(ROOT, "breseq_gb300", "csrc", "bsq_pairs_host.cpp")]
+DEPS = SRCS + [os.path.join(ROOT, "breseq_gb300", "csrc", f) for f in ("bsq_pairs.h", "bsq_host.h", "bsq_common.h")]
+OUT = os.path.join(ROOT, "tests", "native", "_build", "libpairs_host.so")
+
+
+@pytest.fixture(scope="module")
+def host():
+    if not os.path.exists(OUT) or os.path.getmtime(OUT) < max(os.path.getmtime(d) for d in DEPS):
+        os.makedirs(os.path.dirname(OUT), exist_ok=True)
+        cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off", "-I" + cuda_inc]
+                              + SRCS + ["-o", OUT])
+    L = C.CDLL(OUT)
+    L.host_pair_candidates.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.POINTER(abi.PairParams),
+                                       C.POINTER(C.c_char_p), C.c_char_p, C.c_char_p]
+    return L
+
+
+def run_both(host, s, st, tmp_path, cutoff=None):
+    view = abi.SampleView(s)
+    p, keep = pair_params(s, st, cutoff)
+    names = (C.c_char_p * len(s.target_names))(*[n.encode() for n in s.target_names])
+    paths = {k: str(tmp_path / f"{k}.csv") for k in ("dp", "mp", "odp", "omp")}
+    rc = host.host_pair_candidates(C.byref(view.ref), C.byref(view.reads), C.byref(p), names,
+                                   paths["dp"].encode(), paths["mp"].encode())
+    assert rc == 0
+    po.pair_candidates(s, st, paths["odp"], paths["omp"], cutoff)
+    got = [open(paths[k]).read() for k in ("dp", "mp")]
+    exp = [open(paths[k]).read() for k in ("odp", "omp")]
+    return got, exp
+
+
+def ecoli_pairs(scale=0.03, seed=5, **kw):
+    return synth.with_pairs(synth.simulate(synth.config_ecoli(seed=seed, scale=scale)), seed=seed, **kw)
+
+
+def two_groups(seed=3):
+    cfg = synth.SimConfig(seed=seed, target_lengths=(30_000, 6_000, 2_500), target_names=("chrA", "plasmid", "chrB"),
+                          n_snps=10, n_indels=3, max_indel=2,
+                          read_sets=(synth.ReadFileSet(coverage=40, read_length=101, paired=True, insert_mean=300),
+                                     synth.ReadFileSet(coverage=25, read_length=150, paired=True, insert_mean=500)))
+    return synth.with_pairs(synth.simulate(cfg), seed=seed, discordant_sites=4, unmapped_sites=4,
+                            background_discordant=0.02, background_unmapped=0.03, no_xp_fraction=0.1)
+
+
+def test_pairs_ecoli_matches_oracle(host, tmp_path):
+    s = ecoli_pairs()
+    st = PairSettings(dp_group=(0,), window_width=(462.75,), predict_missing_pairs=True)
+    got, exp = run_both(host, s, st, tmp_path)
+    assert got == exp
+    assert got[0].count("\n") > 5 and got[1].count("\n") > 3   # regions were found on both scans
+
+
+def test_pairs_skip_without_orientation(host, tmp_path):
+    # DP-eligible reads without a usable XP are skipped at their start column, MP included
+    s = ecoli_pairs(scale=0.02, seed=8, no_xp_fraction=0.3, background_discordant=0.01)
+    st = PairSettings(dp_group=(0,), window_width=(400.0,), predict_missing_pairs=True, missing_pair_seed=2,
+                      missing_pair_seed_fraction=0.1)
+    got, exp = run_both(host, s, st, tmp_path)
+    assert got == exp
+
+
+@pytest.mark.parametrize("dp_group,widths", [((0, 1), (300.5, 520.0)), ((-1, 0), (37.25,)), ((0, 0), (1.0,)),
+                                             ((1, 0), (0.5, 2000.0))])
+@pytest.mark.parametrize("seeds", [(3, 3, 0.25), (1, 2, 0.0), (0, 0, 0.5), (6, 4, 1.0)])
+def test_pairs_groups_and_seeds(host, tmp_path, dp_group, widths, seeds):
+    s = two_groups()
+    G = len(widths)
+    st = PairSettings(dp_group=dp_group, window_width=widths, r1_prefix=tuple(1 + 2 * g for g in range(G)),
+                      r2_prefix=tuple(2 + 2 * g for g in range(G)), discordant_pair_seed=seeds[0],
+                      predict_missing_pairs=True, missing_pair_seed=seeds[1], missing_pair_seed_fraction=seeds[2])
+    got, exp = run_both(host, s, st, tmp_path)
+    assert got == exp
+
+
+def test_pairs_targets_skipped(host, tmp_path):
+    # a target below the deletion propagation cutoff is not walked; one outside the pileup set neither
+    s = two_groups(seed=4)
+    s = dataclasses.replace(s, target_order=np.array([0, 2], dtype=np.uint32))
+    st = PairSettings(dp_group=(0, 1), window_width=(350.0, 600.0), r1_prefix=(1, 3), r2_prefix=(2, 4),
+                      predict_missing_pairs=True)
+    got, exp = run_both(host, s, st, tmp_path, cutoff=np.array([5.0, 5.0, -1.0]))
+    assert got == exp
+    assert "chrB" not in got[0] + got[1] and "plasmid" not in got[0] + got[1]
+
+
+def test_pairs_mp_off_and_no_groups(host, tmp_path):
+    s = two_groups(seed=6)
+    got, exp = run_both(host, s, PairSettings(dp_group=(0, 1), window_width=(400.0, 400.0), r1_prefix=(1, 3),
+                                              r2_prefix=(2, 4)), tmp_path)
+    assert got == exp and got[1].count("\n") == 1       # MP off: header only
+    got, exp = run_both(host, s, PairSettings(dp_group=(-1, -1), window_width=(), r1_prefix=(), r2_prefix=(),
+                                              predict_missing_pairs=True), tmp_path)
+    assert got == exp and got[0].count("\n") == 1 and got[1].count("\n") == 1
+
+
+def test_pairs_hand_worked(host, tmp_path):
+    """Three discordant FR reads starting at 101, 151, 201 (window 100, seed 2) on one 1000-bp target:
+    two are in the window at 151 (101 <= 151 < 201) and at 201 the first leaves (201 - 101 >= 100) as the
+    third enters, so the count is 2 from 151 to 250; at 251 the second leaves.  Region 151-250, maximum
+    2, all three reads listed (two in the snapshot at 151, one appended at 201)."""
+    seq = np.frombuffer(b"ACGT" * 250, dtype=np.uint8).copy()
+    n = 3
+    pos = np.array([100, 150, 200], dtype=np.int32)
+    cig = np.array([(50 << 4) | 0] * n, dtype=np.uint32)
+    s = synth.Sample(ref_seq=seq, target_offset=np.array([0, 1000], dtype=np.uint64), target_names=["t"],
+                     coverage_group=np.zeros(1, np.uint32), n_coverage_groups=1, target_order=np.zeros(1, np.uint32),
+                     tid=np.zeros(n, np.int32), pos=pos, flag=np.array([0x1 | 0x40, 0x1 | 0x80, 0x1 | 0x40], np.uint16),
+                     mapq=np.full(n, 40, np.uint8), x1=np.array([1, 2, 1], np.uint32), xl=np.full(n, -1, np.int32),
+                     xr=np.full(n, -1, np.int32), read_file=np.zeros(n, np.uint8), read_group=np.zeros(n, np.uint16),
+                     l_qseq=np.full(n, 50, np.uint32), seq_off=np.arange(n, dtype=np.uint64) * 50,
+                     cigar_off=np.arange(n, dtype=np.uint64), n_cigar=np.ones(n, np.uint16), cigar=cig,
+                     seq=np.full(n * 25, 0x12, np.uint8), qual=np.full(n * 50, 30, np.uint8), n_read_files=2,
+                     n_quality=42, isize=np.array([900, 800, -700], np.int32), xp=np.zeros(n, np.uint8),
+                     qname_off=np.array([0, 3, 6, 9], np.uint64), qname=np.frombuffer(b"1:71:82:9", np.uint8).copy())
+    st = PairSettings(dp_group=(0,), window_width=(100.0,), r1_prefix=(5,), r2_prefix=(6,), discordant_pair_seed=2)
+    got, exp = run_both(host, s, st, tmp_path)
+    assert got == exp
+    want = ("seq_id,start,end,strand,orientation,length,max_discordant_count,redundant,discordant_pairs\n"
+            "t,151,250,F,FR,100,2,0,5:7__6:7__900__101__150;5:8__6:8__-800__151__200;5:9__6:9__-700__201__250\n")
+    assert got[0] == want
