@@ -15,9 +15,11 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <deque>
 #include <fstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/breseq_gb300.h"
@@ -65,7 +67,7 @@ struct Region {
 struct Ctx {
   const PairReplayInput& in;
   PairReplayResult& out;
-  std::vector<std::string> desc;   // descriptor of each compacted event
+  const std::vector<std::string>& desc;   // descriptor of each compacted event
 };
 
 void close_region(Ctx& c, Region& r, uint32_t tid, uint32_t end, char strand, const char* orient, bool mp) {
@@ -89,10 +91,16 @@ void close_region(Ctx& c, Region& r, uint32_t tid, uint32_t end, char strand, co
   r = Region();
 }
 
-// The windows of one bin over one target.  ev: the bin's reads in BAM order.  totals: MP only,
-// members[g] = sorted start positions of the strand's window-total members of DP group g.
+// Start positions of one strand's MP window-total members, per DP group: group g's sorted starts are
+// start[off[g] .. off[g + 1]).
+struct Members {
+  std::vector<uint32_t> start;
+  std::vector<uint64_t> off;
+};
+
+// The windows of one bin over one target.  ev: the bin's reads in BAM order.  members: MP only.
 void replay_bin(Ctx& c, uint32_t tid, uint32_t len, const std::vector<Ev>& ev, int bin, bool mp,
-                const std::vector<std::vector<uint32_t>>* members) {
+                const Members* members) {
   const PairReplayInput& in = c.in;
   const uint32_t G = (uint32_t)in.window_width.size();
   const int32_t seed = mp ? in.mp_seed : in.dp_seed;
@@ -116,15 +124,22 @@ void replay_bin(Ctx& c, uint32_t tid, uint32_t len, const std::vector<Ev>& ev, i
   const char strand = mp ? (bin == 0 ? 'F' : 'R') : (bin / 3 == 0 ? 'F' : 'R');
   const char* orient = mp ? nullptr : kOrient[bin % 3];
 
+  // the window total at p: members with p - ceil(width) < start <= p.  Positions only increase
+  // within a bin, so two cursors per group advance through the sorted starts.
+  std::vector<uint64_t> lo_i(G), hi_i(G);
+  std::vector<int64_t> wceil(G);
+  for (uint32_t g = 0; g < G; g++) {
+    wceil[g] = (int64_t)ceil(in.window_width[g]);
+    if (members) lo_i[g] = hi_i[g] = members->off[g];
+  }
   auto total_at = [&](uint32_t p) -> int64_t {
     int64_t t = 0;
     for (uint32_t g = 0; g < G; g++) {
-      const std::vector<uint32_t>& s = (*members)[g];
-      if (s.empty()) continue;
-      const int64_t lo = (int64_t)p - (int64_t)ceil(in.window_width[g]);   // in window: start > lo
-      const auto hi_it = std::upper_bound(s.begin(), s.end(), p);
-      const auto lo_it = lo < 0 ? s.begin() : std::upper_bound(s.begin(), hi_it, (uint32_t)std::min<int64_t>(lo, 0xFFFFFFFFll));
-      t += hi_it - lo_it;
+      const uint64_t end = members->off[g + 1];
+      while (hi_i[g] < end && members->start[hi_i[g]] <= p) hi_i[g]++;
+      const int64_t lo = (int64_t)p - wceil[g];
+      while (lo_i[g] < hi_i[g] && (int64_t)members->start[lo_i[g]] <= lo) lo_i[g]++;
+      t += (int64_t)(hi_i[g] - lo_i[g]);
     }
     return t;
   };
@@ -188,53 +203,99 @@ void replay_bin(Ctx& c, uint32_t tid, uint32_t len, const std::vector<Ev>& ev, i
 }  // namespace
 
 int pair_replay(const PairReplayInput& in, PairReplayResult& out) {
-  Ctx c{in, out, {}};
   const uint32_t G = (uint32_t)in.window_width.size();
   // descriptors of every compacted event
-  c.desc.resize(in.n_ev);
-  std::vector<uint32_t> ev_tid(in.n_ev);
+  std::vector<std::string> desc(in.n_ev);
   for (uint64_t k = 0; k < in.n_ev; k++) {
     const PairEvent& e = in.ev[k];
     const uint32_t t = (uint32_t)(std::upper_bound(in.tpoff.begin(), in.tpoff.end(), e.start) - in.tpoff.begin()) - 1;
-    ev_tid[k] = t;
     const uint32_t s1 = e.start - in.tpoff[t] + 1, e1 = e.end - in.tpoff[t];
     if ((e.code & kPairDpBinMask) != kPairNoBin) {
       if (e.group >= G) return BSQ_ERR_INVALID;
-      c.desc[k] = dp_key(e, in.names + k * kPairNameSlot, in.r1_prefix[e.group], in.r2_prefix[e.group]) + "__" +
-                  std::to_string(s1) + "__" + std::to_string(e1);
+      desc[k] = dp_key(e, in.names + k * kPairNameSlot, in.r1_prefix[e.group], in.r2_prefix[e.group]) + "__" +
+                std::to_string(s1) + "__" + std::to_string(e1);
     } else {
-      c.desc[k] = std::to_string(s1) + "__" + std::to_string(e1);
+      desc[k] = std::to_string(s1) + "__" + std::to_string(e1);
     }
   }
+  for (uint64_t k = 0; k < in.n_mem; k++)
+    if (in.mem_key[k] / 2 >= G) return BSQ_ERR_INVALID;
+  if (!G) return BSQ_OK;
+  // independent tasks: per piled target, the six DP bins, and each MP strand; merged in this order
+  struct Task { uint32_t t; int kind; PairReplayResult res; };
+  std::vector<Task> tasks;
+  // MP window-total members of each piled target, split by strand and group with one counting pass
+  // (BAM order keeps each group's starts sorted)
+  std::vector<Members> members(in.mp ? 2 * (size_t)in.tpoff.size() : 0);
   for (uint32_t t : in.order) {
+    if (!in.piled[t]) continue;
+    tasks.push_back({t, 0, {}});
+    if (!in.mp) continue;
+    tasks.push_back({t, 1, {}});
+    tasks.push_back({t, 2, {}});
+    const uint32_t c0 = in.tpoff[t], c1 = in.tpoff[t + 1] - 1;
+    const uint32_t* ms = in.mem_start;
+    const uint64_t lo = std::lower_bound(ms, ms + in.n_mem, c0) - ms;
+    const uint64_t hi = std::lower_bound(ms + lo, ms + in.n_mem, c1) - ms;
+    std::vector<uint64_t> cnt(2 * G, 0);
+    for (uint64_t k = lo; k < hi; k++) cnt[in.mem_key[k]]++;
+    std::vector<uint64_t> fill(2 * G);
+    for (int b = 0; b < 2; b++) {
+      Members& m = members[2 * t + b];
+      m.off.assign(G + 1, 0);
+      for (uint32_t g = 0; g < G; g++) m.off[g + 1] = m.off[g] + cnt[2 * g + b];
+      m.start.resize(m.off[G]);
+      for (uint32_t g = 0; g < G; g++) fill[2 * g + b] = m.off[g];
+    }
+    uint32_t* dst[2] = {members[2 * t].start.data(), members[2 * t + 1].start.data()};
+    for (uint64_t k = lo; k < hi; k++) {
+      const uint32_t key = in.mem_key[k];
+      dst[key & 1][fill[key]++] = ms[k] - c0 + 1;
+    }
+  }
+  auto run = [&](Task& task) {
+    const uint32_t t = task.t;
     const uint32_t len = in.tpoff[t + 1] - in.tpoff[t] - 1;
     const uint32_t c0 = in.tpoff[t], c1 = in.tpoff[t] + len;
+    Ctx c{in, task.res, desc};
     // this target's events and members (both in BAM order, so contiguous and start-sorted)
     auto ev_lo = std::lower_bound(in.ev, in.ev + in.n_ev, c0, [](const PairEvent& e, uint32_t v) { return e.start < v; });
     auto ev_hi = std::lower_bound(ev_lo, in.ev + in.n_ev, c1 + 1, [](const PairEvent& e, uint32_t v) { return e.start < v; });
-    if (!in.piled[t]) continue;
-    std::vector<Ev> dp[6], mpe[2];
-    for (auto it = ev_lo; it != ev_hi; ++it) {
-      const uint64_t k = it - in.ev;
-      Ev x{it->start - c0 + 1, it->end - c0, it->group, it->redundant != 0, k};
-      const int bin = it->code & kPairDpBinMask;
-      if (bin != kPairNoBin) dp[bin].push_back(x);
-      if (in.mp && (it->code & kPairMpUnmapped)) mpe[(it->code & kPairRev) ? 1 : 0].push_back(x);
-    }
-    if (G) for (int b = 0; b < 6; b++) replay_bin(c, t, len, dp[b], b, false, nullptr);
-    if (in.mp && G) {
-      std::vector<std::vector<uint32_t>> members[2] = {std::vector<std::vector<uint32_t>>(G),
-                                                       std::vector<std::vector<uint32_t>>(G)};
-      const uint32_t* ms = in.mem_start;
-      const uint64_t lo = std::lower_bound(ms, ms + in.n_mem, c0) - ms;
-      const uint64_t hi = std::lower_bound(ms + lo, ms + in.n_mem, c1 + 1) - ms;
-      for (uint64_t k = lo; k < hi; k++) {
-        const uint32_t key = in.mem_key[k];
-        if (key / 2 >= G) return BSQ_ERR_INVALID;
-        members[key & 1][key / 2].push_back(ms[k] - c0 + 1);
+    if (task.kind == 0) {
+      std::vector<Ev> dp[6];
+      for (auto it = ev_lo; it != ev_hi; ++it) {
+        const int bin = it->code & kPairDpBinMask;
+        if (bin != kPairNoBin) dp[bin].push_back(Ev{it->start - c0 + 1, it->end - c0, it->group, it->redundant != 0,
+                                                    (uint64_t)(it - in.ev)});
       }
-      for (int b = 0; b < 2; b++) replay_bin(c, t, len, mpe[b], b, true, &members[b]);
+      for (int b = 0; b < 6; b++) replay_bin(c, t, len, dp[b], b, false, nullptr);
+      return;
     }
+    const int b = task.kind - 1;
+    std::vector<Ev> mpe;
+    for (auto it = ev_lo; it != ev_hi; ++it)
+      if ((it->code & kPairMpUnmapped) && ((it->code & kPairRev) ? 1 : 0) == b)
+        mpe.push_back(Ev{it->start - c0 + 1, it->end - c0, it->group, it->redundant != 0, (uint64_t)(it - in.ev)});
+    replay_bin(c, t, len, mpe, b, true, &members[2 * t + b]);
+  };
+  const unsigned hw = std::thread::hardware_concurrency();
+  const size_t n_threads = std::min<size_t>(tasks.size(), hw ? hw : 1);
+  if (n_threads <= 1) {
+    for (Task& task : tasks) run(task);
+  } else {
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    for (size_t i = 0; i < n_threads; i++)
+      pool.emplace_back([&]() {
+        for (size_t k; (k = next.fetch_add(1)) < tasks.size();) run(tasks[k]);
+      });
+    for (std::thread& th : pool) th.join();
+  }
+  for (Task& task : tasks) {
+    const uint64_t base = out.text.size();
+    out.text += task.res.text;
+    for (bsq_pair_region r : task.res.dp) { r.text_off += base; out.dp.push_back(r); }
+    for (bsq_pair_region r : task.res.mp) { r.text_off += base; out.mp.push_back(r); }
   }
   return BSQ_OK;
 }

@@ -603,7 +603,8 @@ typedef struct bsq_pair_region {
 } bsq_pair_region;
 
 /* Runs the scans on a resident sample (needs the pair annotations of bsq_read_soa or a BAM load).
- * Regions are in detection order; the writers sort them as breseq does. */
+ * Regions come per target (pileup order): DP bins 0-5, then MP strands, each by position; the writers
+ * sort them as breseq does. */
 int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* params, uint64_t* n_dp,
                         uint64_t* n_mp, uint64_t* text_bytes);
 int bsq_pair_result_copy(bsq_ctx* ctx, bsq_pair_region* dp, uint64_t n_dp, bsq_pair_region* mp, uint64_t n_mp,
