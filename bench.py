@@ -30,6 +30,13 @@ A "soft_clipping" leg times the soft-clipping tabulation (tabulate_soft_clipping
 of the same shape with 50 junction breakpoints and 1% of reads clipped by 12-40 random bases, against
 the oracle's CPU tabulation of the same sample.
 
+A "coverage_fit" leg times the coverage-distribution fit (host threads) of each coverage group's
+histogram from pass 1, against the oracle's sequential restatement.
+
+A "pair_scans" leg times the discordant-pair and missing-pair candidate scans on the workload with
+pair annotations (discordant and mate-unmapped pairs planted at 40 sites each and at background
+rates), against the oracle's position-by-position walk.
+
 Under torchrun each rank scores its own sample (weak scaling, no collective in the data path); the
 timed region is bracketed by barriers and the slowest rank's time is used.
 """
@@ -152,6 +159,9 @@ SC_READS_DRAM_PER_READ = (230.080768e6 + 14.4256e6) / 6416810
 # DRAM bytes of the four main coverage-table kernels over their algorithmic bytes, from the ncu capture
 # of the same chromosome (profiles/coverage_table_kernels_ecoli_chromosome_4.63Mb.md)
 COV_TABLE_DRAM_OVER_ALGORITHMIC = 580.482284e6 / (32 * 6206454 + 80 * 4630000)
+# DRAM bytes of one pair-classification launch per record, from the ncu capture of the same workload at
+# half the genome length, timed call (profiles/pair_scan_kernels_ecoli_pairs_x0.5.md)
+PAIR_CLASSIFY_DRAM_PER_READ = (116.804608e6 + 10.306816e6) / 3223958
 
 
 COV_COLUMNS = ("unique_top", "unique_bot", "redundant_top", "redundant_bot", "raw_redundant_top",
@@ -357,7 +367,8 @@ def run_pairs(args, device, s):
             "value": n / (statistics.mean(wall) / 1e3), "unit": "records/s",
             "roofline": {"bound": "hbm", "kernel": "pair_classify_kernel", "achieved": kbytes / (kms / 1e3) / 1e9,
                          "peak": hbm, "unit": "GB/s", "frac": kbytes / (kms / 1e3) / 1e9 / hbm, "kernel_ms": kms,
-                         "algorithmic_bytes": kbytes, "peak_kind": peak_kind, "traffic": None},
+                         "algorithmic_bytes": kbytes, "peak_kind": peak_kind,
+                         "traffic": PAIR_CLASSIFY_DRAM_PER_READ * n},
             "identical_to_oracle": bool(same),
             "cpu_baseline": {"value": n / cpu_s, "unit": "records/s", "cores": 1, "kind": "port",
                              "sample": f"the same sample, one position-by-position walk ({cpu_s:.2f} s)"}}
