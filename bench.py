@@ -327,16 +327,18 @@ def run_covfit(args, ec, s):
 
 
 def run_pairs(args, device, s):
-    """Discordant-pair and missing-pair candidate scans (bsq_pair_candidates) on the headline sample
-    with pair annotations (discordant and mate-unmapped pairs planted near breakpoints and at a
-    background rate): device time, the classification pass over every read (the dominant kernel),
-    the host replay, and the oracle's position-by-position walk on the CPU."""
+    """Discordant-pair, missing-pair and pair-distance candidate scans (bsq_pair_candidates) on the
+    headline sample with pair annotations (discordant and mate-unmapped pairs planted near breakpoints
+    and at a background rate, longer pairs near 40 deletion-like sites): device time, the
+    classification pass over every read, the host replay, and the oracle's position-by-position walk
+    on the CPU."""
     from breseq_gb300 import synth
     from breseq_gb300.api import PairSettings, Scorer
     from oracle import pyoracle as po
-    sp = synth.with_pairs(s, seed=31, discordant_sites=40, unmapped_sites=40)
+    sp = synth.with_pairs(s, seed=31, discordant_sites=40, unmapped_sites=40, distance_sites=40)
     st = PairSettings(dp_group=tuple([0] * (int(sp.read_group.max()) + 1)), window_width=(462.75,),
-                      predict_missing_pairs=True)
+                      predict_missing_pairs=True, predict_pair_distance=True, pd_cdf=(synth.pd_null(sp),),
+                      pd_orientation=("FR",), pd_max_span=1500, pd_z_seed=2.5, pd_mean_covering_gap=137.5)
     with Scorer(device) as sc:
         sid = sc.load_sample(sp)
         for _ in range(args.warmup):
@@ -350,19 +352,19 @@ def run_pairs(args, device, s):
             dev.append(ps["device_ms"]); main.append(ps["main_kernel_ms"])
         launches = ps["kernel_launches"]
         with tempfile.TemporaryDirectory() as d:
-            dp, mp, odp, omp = (os.path.join(d, f) for f in ("dp", "mp", "odp", "omp"))
-            sc.write_pair_candidates(r, dp, mp, sp.target_names)
+            dp, mp, pd, odp, omp, opd = (os.path.join(d, f) for f in ("dp", "mp", "pd", "odp", "omp", "opd"))
+            sc.write_pair_candidates(r, dp, mp, sp.target_names, pd)
             t0 = time.perf_counter()
-            po.pair_candidates(sp, st, odp, omp)
+            po.pair_candidates(sp, st, odp, omp, None, opd)
             cpu_s = time.perf_counter() - t0
-            same = open(dp).read() == open(odp).read() and open(mp).read() == open(omp).read()
+            same = all(open(a).read() == open(b).read() for a, b in ((dp, odp), (mp, omp), (pd, opd)))
         sc.free_sample(sid)
     n = sp.n_reads
     ms, kms = statistics.mean(dev), statistics.mean(main)
     hbm, peak_kind = _peaks()
     kbytes = 47 * n   # per read: 32-byte record, flag, XP, read group read; code, group, two selections written
     return {"workload": f"{WORKLOAD} with pair annotations", "reads": n, "dp_regions": len(r["dp"]),
-            "mp_regions": len(r["mp"]), "device_ms": ms, "wall_ms": statistics.mean(wall),
+            "mp_regions": len(r["mp"]), "pd_regions": len(r["pd"]), "device_ms": ms, "wall_ms": statistics.mean(wall),
             "host_replay_ms": statistics.mean(wall) - ms, "kernel_launches": launches,
             "value": n / (statistics.mean(wall) / 1e3), "unit": "records/s",
             "roofline": {"bound": "hbm", "kernel": "pair_classify_kernel", "achieved": kbytes / (kms / 1e3) / 1e9,

@@ -110,6 +110,9 @@ def load():
                                       P(C.c_uint64)]
     L.bsq_pair_result_copy.argtypes = [C.c_void_p, P(abi.PairRegion), C.c_uint64, P(abi.PairRegion), C.c_uint64,
                                        C.c_char_p, C.c_uint64]
+    L.bsq_pd_result.argtypes = [C.c_void_p, P(C.c_uint64), P(abi.PdRegion), C.c_uint64, P(abi.PdSummary)]
+    L.bsq_write_pd_candidate_regions.argtypes = [C.c_char_p, P(C.c_char_p), P(abi.PdRegion), C.c_uint64,
+                                                 P(abi.PdSummary)]
     for fn in (L.bsq_write_dp_candidate_regions, L.bsq_write_mp_candidate_regions):
         fn.argtypes = [C.c_char_p, P(C.c_char_p), P(abi.PairRegion), C.c_uint64, C.c_char_p]
     L.bsq_fit_coverage_distribution.argtypes = [P(C.c_uint64), C.c_uint32, C.c_double, C.c_int, P(abi.CoverageFit)]
@@ -140,4 +143,5 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_bam_decode", "bsq_bam_copy_records", "bsq_bam_load", "bsq_fit_coverage_distribution",
             "bsq_fit_negative_binomial", "bsq_nbinom_pmf", "bsq_nbinom_cdf", "bsq_nbinom_quantile",
             "bsq_bam_name_bytes", "bsq_pair_candidates", "bsq_pair_result_copy", "bsq_write_dp_candidate_regions",
-            "bsq_write_mp_candidate_regions")
+            "bsq_write_mp_candidate_regions", "bsq_pd_result",
+            "bsq_write_pd_candidate_regions")

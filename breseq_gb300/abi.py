@@ -46,6 +46,8 @@ class ReadSoA(C.Structure):
         ("xp", P(C.c_uint8)),
         ("qname_off", P(C.c_uint64)),
         ("qname", C.c_void_p),
+        ("mtid", P(C.c_int32)),
+        ("mpos", P(C.c_int32)),
     ]
 
 
@@ -66,6 +68,48 @@ class PairParams(C.Structure):
         ("missing_pair_seed", C.c_int32),
         ("missing_pair_seed_fraction", C.c_double),
         ("deletion_propagation_cutoff", P(C.c_double)),
+        ("predict_pair_distance", C.c_int32),
+        ("pd_cdf", P(P(C.c_int64))),
+        ("pd_cdf_len", P(C.c_uint32)),
+        ("pd_orientation", P(C.c_uint8)),
+        ("pd_max_span", C.c_int32),
+        ("pd_z_seed", C.c_double),
+        ("pair_distance_seed", C.c_int32),
+        ("pair_distance_tail_quantile", C.c_double),
+        ("pd_mean_covering_gap", C.c_double),
+        ("total_reference_length", C.c_uint64),
+    ]
+
+
+class PdRegion(C.Structure):
+    _fields_ = [
+        ("target", C.c_uint32),
+        ("start", C.c_uint32),
+        ("end", C.c_uint32),
+        ("direction", C.c_char),
+        ("reserved", C.c_char * 3),
+        ("peak_position", C.c_uint32),
+        ("peak_covering", C.c_int32),
+        ("peak_tail", C.c_int32),
+        ("reserved2", C.c_uint32),
+        ("peak_z", C.c_double),
+    ]
+
+
+class PdSummary(C.Structure):
+    _fields_ = [
+        ("mean_covering_gap", C.c_double),
+        ("n_effective_tests", C.c_double),
+        ("seed_z_used", C.c_double),
+        ("z_iqr_inflation", C.c_double),
+        ("region_tail_fit_ok", C.c_int32),
+        ("reserved", C.c_int32),
+        ("region_tail_log_intercept", C.c_double),
+        ("region_tail_sigma", C.c_double),
+        ("region_tail_fit_lo", C.c_double),
+        ("region_tail_fit_hi", C.c_double),
+        ("ladder", C.c_uint64 * 21),
+        ("regions_seeded", C.c_uint64),
     ]
 
 
@@ -304,6 +348,9 @@ class SampleView:
             kw["qname_off"] = ptr(k(s.qname_off, np.uint64), C.c_uint64)
             kw["qname"] = k(np.frombuffer(bytes(s.qname), dtype=np.uint8) if not isinstance(s.qname, np.ndarray)
                             else s.qname, np.uint8).ctypes.data
+        if getattr(s, "mtid", None) is not None:
+            kw["mtid"] = ptr(k(s.mtid, np.int32), C.c_int32)
+            kw["mpos"] = ptr(k(s.mpos, np.int32), C.c_int32)
         self.reads = ReadSoA(n_reads=int(len(s.tid)), n_cigar_total=int(len(s.cigar)),
                              n_bases_total=int(len(s.qual)), **kw)
 
@@ -325,7 +372,8 @@ READ_ARRAY_FIELDS = (("tid", np.int32), ("pos", np.int32), ("flag", np.uint16), 
                      ("xl", np.int32), ("xr", np.int32), ("read_file", np.uint8), ("read_group", np.uint16),
                      ("l_qseq", np.uint32), ("seq_off", np.uint64), ("cigar_off", np.uint64), ("n_cigar", np.uint16),
                      ("cigar", np.uint32), ("seq", np.uint8), ("qual", np.uint8), ("xj", np.uint8),
-                     ("isize", np.int32), ("xp", np.uint8), ("qname_off", np.uint64), ("qname", np.uint8))
+                     ("isize", np.int32), ("xp", np.uint8), ("qname_off", np.uint64), ("qname", np.uint8),
+                     ("mtid", np.int32), ("mpos", np.int32))
 _CT = {np.int32: C.c_int32, np.uint16: C.c_uint16, np.uint8: C.c_uint8, np.uint32: C.c_uint32, np.uint64: C.c_uint64}
 
 

@@ -53,6 +53,17 @@ class PairSettings:
     predict_missing_pairs: bool = False
     missing_pair_seed: int = 3
     missing_pair_seed_fraction: float = 0.25
+    # pair distance: per DP group the null (pd_build_cdf's mid-CDF in 2^20 fixed point, None: none) and
+    # its orientation ("FR", "RF" or "" for any); the span and seed z as the pileup constructor derives them
+    predict_pair_distance: bool = False
+    pd_cdf: tuple = ()
+    pd_orientation: tuple = ()
+    pd_max_span: int = 0
+    pd_z_seed: float = 2.5
+    pair_distance_seed: int = 3
+    pair_distance_tail_quantile: float = 0.05
+    pd_mean_covering_gap: float = 0.0
+    total_reference_length: int = 0
 
 
 def pair_params(sample, st: PairSettings, deletion_propagation_cutoff=None):
@@ -64,12 +75,26 @@ def pair_params(sample, st: PairSettings, deletion_propagation_cutoff=None):
                 r2=np.ascontiguousarray(st.r2_prefix, dtype=np.uint32),
                 cut=np.broadcast_to(np.asarray(5.0 if deletion_propagation_cutoff is None else deletion_propagation_cutoff,
                                                dtype=np.float64), (T,)).copy())
+    G = len(keep["w"])
+    cdfs = [np.ascontiguousarray(st.pd_cdf[g] if g < len(st.pd_cdf) and st.pd_cdf[g] is not None else [], dtype=np.int64)
+            for g in range(G)]
+    keep["cdfs"] = cdfs
+    keep["cdf_ptrs"] = (C.POINTER(C.c_int64) * max(1, G))(*[abi.ptr(c, C.c_int64) for c in cdfs])
+    keep["cdf_len"] = np.array([len(c) for c in cdfs] or [0], dtype=np.uint32)
+    keep["orient"] = np.array([abi.XP_CODES.get(st.pd_orientation[g], abi.XP_NONE) if g < len(st.pd_orientation)
+                               else abi.XP_NONE for g in range(G)] or [3], dtype=np.uint8)
     p = abi.PairParams(n_read_groups=len(keep["dpg"]), dp_group=abi.ptr(keep["dpg"], C.c_int32),
                        n_dp_groups=len(keep["w"]), window_width=abi.ptr(keep["w"], C.c_double),
                        r1_name_prefix=abi.ptr(keep["r1"], C.c_uint32), r2_name_prefix=abi.ptr(keep["r2"], C.c_uint32),
                        discordant_pair_seed=st.discordant_pair_seed, predict_missing_pairs=int(st.predict_missing_pairs),
                        missing_pair_seed=st.missing_pair_seed, missing_pair_seed_fraction=st.missing_pair_seed_fraction,
-                       deletion_propagation_cutoff=abi.ptr(keep["cut"], C.c_double))
+                       deletion_propagation_cutoff=abi.ptr(keep["cut"], C.c_double),
+                       predict_pair_distance=int(st.predict_pair_distance), pd_cdf=keep["cdf_ptrs"],
+                       pd_cdf_len=abi.ptr(keep["cdf_len"], C.c_uint32), pd_orientation=abi.ptr(keep["orient"], C.c_uint8),
+                       pd_max_span=st.pd_max_span, pd_z_seed=st.pd_z_seed, pair_distance_seed=st.pair_distance_seed,
+                       pair_distance_tail_quantile=st.pair_distance_tail_quantile,
+                       pd_mean_covering_gap=st.pd_mean_covering_gap,
+                       total_reference_length=int(st.total_reference_length or sample.target_offset[-1]))
     return p, keep
 
 
@@ -300,10 +325,17 @@ class Scorer:
         mp = (abi.PairRegion * max(1, nm.value))()
         text = C.create_string_buffer(max(1, nt.value))
         self._check(self.L.bsq_pair_result_copy(self.ctx, dp, nd.value, mp, nm.value, text, nt.value))
-        return dict(dp=list(dp)[: nd.value], mp=list(mp)[: nm.value], text=text.raw[: nt.value])
+        npd = C.c_uint64()
+        summ = abi.PdSummary()
+        self._check(self.L.bsq_pd_result(self.ctx, C.byref(npd), None, 0, C.byref(summ)))
+        pd = (abi.PdRegion * max(1, npd.value))()
+        self._check(self.L.bsq_pd_result(self.ctx, C.byref(npd), pd, npd.value, None))
+        return dict(dp=list(dp)[: nd.value], mp=list(mp)[: nm.value], text=text.raw[: nt.value],
+                    pd=list(pd)[: npd.value], pd_summary=summ)
 
-    def write_pair_candidates(self, result: dict, dp_path: str | None, mp_path: str | None, target_names):
-        """dp_candidate_regions.csv / mp_candidate_regions.csv from a pair_candidates() result."""
+    def write_pair_candidates(self, result: dict, dp_path: str | None, mp_path: str | None, target_names,
+                              pd_path: str | None = None):
+        """dp / mp / pd_candidate_regions.csv from a pair_candidates() result."""
         names = (C.c_char_p * len(target_names))(*[n.encode() for n in target_names])
         text = C.create_string_buffer(result["text"], max(1, len(result["text"])))
         for path, key, fn in ((dp_path, "dp", self.L.bsq_write_dp_candidate_regions),
@@ -314,6 +346,12 @@ class Scorer:
             rc = fn(path.encode(), names, regs, len(result[key]), text)
             if rc != 0:
                 raise _lib.BsqError(rc, f"cannot write {path}")
+        if pd_path is not None:
+            regs = (abi.PdRegion * max(1, len(result["pd"])))(*result["pd"])
+            rc = self.L.bsq_write_pd_candidate_regions(pd_path.encode(), names, regs, len(result["pd"]),
+                                                       C.byref(result["pd_summary"]))
+            if rc != 0:
+                raise _lib.BsqError(rc, f"cannot write {pd_path}")
 
     def open_bam(self, data) -> "Bam":
         """Uploads a BAM file's bytes (bytes, or a uint8 numpy array, e.g. page-locked) and inflates

@@ -56,8 +56,8 @@ struct DevMem {
 struct SampleDev {
   DevMem ref, reads, x1, rg, qb, cigar, seq, qual, tile_range, d_tpoff, tgt_group, tgt_called, tgt_failed, rstart, mapq;
   // pair annotations for the discordant / missing-pair scans: raw flags, XP codes, TLEN, names
-  DevMem pflag, pxp, pisize, pqoff, pqname;
-  bool has_pairs = false;
+  DevMem pflag, pxp, pisize, pqoff, pqname, pmtid, pmpos;
+  bool has_pairs = false, has_mates = false;
   uint32_t n_targets = 0, n_cols = 0, n_tiles = 0, n_reads = 0, maxspan = 1, max_tile_reads = 0;
   uint32_t n_groups = 0;
   std::vector<uint64_t> toff;       // caller's target offsets
@@ -127,6 +127,9 @@ struct bsq_ctx {
   DevMem pr_code, pr_group, pr_sel, pr_mem, pr_evoff, pr_memoff, pr_tmp, pr_tot, pr_map, pr_ev, pr_names, pr_mstart,
       pr_mkey;
   host::PairReplayResult pair_res;
+  DevMem pd_diff, pd_blk, pd_mask, pd_hist, pd_ladder, pd_above, pd_cnt, pd_cdf, pd_cdfoff, pd_cdflen, pd_orient,
+      pd_piled;
+  host::PdResult pd_res;
   std::vector<bsq_sc_position> sc_res;
   double last_ms = 0, main_ms = 0;
   uint32_t launches = 0;
@@ -322,7 +325,9 @@ void bsq_destroy(bsq_ctx* ctx) {
                     &ctx->sc_ev_n, &ctx->ct_diff, &ctx->ct_blk, &ctx->ct_counts, &ctx->ct_red, &ctx->ct_stat,
                     &ctx->ct_gather, &ctx->pr_code, &ctx->pr_group, &ctx->pr_sel, &ctx->pr_mem, &ctx->pr_evoff,
                     &ctx->pr_memoff, &ctx->pr_tmp, &ctx->pr_tot, &ctx->pr_map, &ctx->pr_ev, &ctx->pr_names,
-                    &ctx->pr_mstart, &ctx->pr_mkey})
+                    &ctx->pr_mstart, &ctx->pr_mkey, &ctx->pd_diff, &ctx->pd_blk, &ctx->pd_mask, &ctx->pd_hist,
+                    &ctx->pd_ladder, &ctx->pd_above, &ctx->pd_cnt, &ctx->pd_cdf, &ctx->pd_cdfoff, &ctx->pd_cdflen,
+                    &ctx->pd_orient, &ctx->pd_piled})
     m->release();
   if (ctx->exec_ec) cudaGraphExecDestroy(ctx->exec_ec);
   if (ctx->exec_im) cudaGraphExecDestroy(ctx->exec_im);
@@ -357,8 +362,9 @@ uint64_t bsq_sample_footprint(const bsq_reference* ref, const bsq_read_soa* rd) 
 struct RecordsDev {
   DevMem tid, pos, flag, mapq, x1, xl, xr, rfile, rg, lq, soff, coff, nc, cigar, seq, qual, xj;
   DevMem isize, xp, qoff, qname;   // pair annotations (has_pairs)
+  DevMem mtid, mpos;               // mate positions (has_mates)
   uint64_t n = 0, n_cigar_total = 0, n_bases_total = 0;
-  bool has_xj = false, has_pairs = false;
+  bool has_xj = false, has_pairs = false, has_mates = false;
 };
 
 static void take(DevMem& to, DevMem& from) {
@@ -476,6 +482,11 @@ static int pack_sample(bsq_ctx* ctx, std::unique_ptr<SampleDev>& s, RecordsDev& 
     take(s->pqname, R.qname);
     s->has_pairs = true;
   }
+  if (R.has_mates) {
+    take(s->pmtid, R.mtid);
+    take(s->pmpos, R.mpos);
+    s->has_mates = true;
+  }
   std::lock_guard<std::mutex> lk(ctx->mu);
   const int32_t id = ctx->next_id++;
   ctx->samples[id] = std::move(s);
@@ -533,6 +544,12 @@ int bsq_load_sample(bsq_ctx* ctx, const bsq_reference* ref, const bsq_read_soa* 
     CK(upload(R.qoff, rd->qname_off, n + 1, st));
     CK(upload(R.qname, rd->qname, rd->qname_off[n], st));
     R.has_pairs = true;
+  }
+  if (rd->mtid || rd->mpos) {
+    if (!rd->mtid || !rd->mpos) return fail(ctx, BSQ_ERR_INVALID, "mate positions need mtid and mpos together");
+    CK(upload(R.mtid, rd->mtid, n, st));
+    CK(upload(R.mpos, rd->mpos, n, st));
+    R.has_mates = true;
   }
   return pack_sample(ctx, s, R, st, sample_id);
 }
@@ -1164,6 +1181,16 @@ int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* 
   if (p->discordant_pair_seed < 0 || (p->predict_missing_pairs && (p->missing_pair_seed < 0 ||
       !(p->missing_pair_seed_fraction >= 0.0 && p->missing_pair_seed_fraction <= 1.0))))
     return fail(ctx, BSQ_ERR_INVALID, "seed setting out of range");
+  const bool pd = p->predict_pair_distance != 0;
+  if (pd) {
+    if (!s->has_mates) return fail(ctx, BSQ_ERR_INVALID, "pair-distance scan needs the records' mtid and mpos");
+    if (G && (!p->pd_cdf || !p->pd_cdf_len || !p->pd_orientation))
+      return fail(ctx, BSQ_ERR_INVALID, "null pair-distance parameter array");
+    if (!(p->pair_distance_tail_quantile >= 0.0 && p->pair_distance_tail_quantile <= 1.0) || !std::isfinite(p->pd_z_seed))
+      return fail(ctx, BSQ_ERR_INVALID, "pair-distance setting out of range");
+    for (uint32_t g = 0; g < G; g++)
+      if (p->pd_cdf_len[g] && !p->pd_cdf[g]) return fail(ctx, BSQ_ERR_INVALID, "null pair-distance null");
+  }
   CK(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
   cudaGetLastError();
@@ -1230,21 +1257,105 @@ int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* 
   CK(pair_scatter(A, ctx->pr_evoff.as<uint64_t>(), mp ? ctx->pr_memoff.as<uint64_t>() : nullptr,
                   ctx->pr_ev.as<PairEvent>(), ctx->pr_names.as<char>(), ctx->pr_mstart.as<uint32_t>(),
                   ctx->pr_mkey.as<uint16_t>(), ctx->sms, st));
+  // pair distance: gaps into difference arrays, every position's statistics, the ladder edges
+  bool pd_on = false;
+  uint32_t pd_launches = 0;
+  host::PdAssembleInput pdin;
+  if (pd) {
+    std::vector<int64_t> cdf;
+    std::vector<uint64_t> cdf_off(G + 1, 0);
+    std::vector<uint32_t> cdf_len(G + 1, 0);
+    std::vector<uint8_t> orient(G + 1, 3);
+    bool usable = false;
+    for (uint32_t g = 0; g < G; g++) {
+      cdf_off[g] = cdf.size();
+      cdf_len[g] = p->pd_cdf_len[g];
+      orient[g] = p->pd_orientation[g];
+      if (cdf_len[g]) { cdf.insert(cdf.end(), p->pd_cdf[g], p->pd_cdf[g] + cdf_len[g]); usable = true; }
+    }
+    pd_on = usable && p->pd_max_span > 0 && G > 0;
+    pdin.tpoff = s->tpoff;
+    pdin.enabled = pd_on;
+    pdin.z_seed = p->pd_z_seed;
+    pdin.mean_covering_gap = p->pd_mean_covering_gap;
+    pdin.total_reference_length = p->total_reference_length;
+    if (G) pdin.hist.assign(kPdHistBins, 0);
+    if (pd_on) {
+      const uint64_t cols = s->n_cols;
+      const uint32_t nb = (uint32_t)((cols + kPdScanCols - 1) / kPdScanCols);
+      std::vector<uint8_t> piled(T, 0);
+      for (uint32_t t : s->order) piled[t] = p->deletion_propagation_cutoff[t] >= 0.0 ? 1 : 0;
+      CK(upload(ctx->pd_cdf, cdf.data(), cdf.size(), st));
+      CK(upload(ctx->pd_cdfoff, cdf_off.data(), G + 1, st));
+      CK(upload(ctx->pd_cdflen, cdf_len.data(), G + 1, st));
+      CK(upload(ctx->pd_orient, orient.data(), G + 1, st));
+      CK(upload(ctx->pd_piled, piled.data(), T, st));
+      CK(ctx->pd_diff.alloc(cols * 32 + 64, st));
+      CK(ctx->pd_blk.alloc((uint64_t)nb * 32 + 64, st));
+      CK(ctx->pd_mask.alloc(cols * 8 + 64, st));
+      CK(ctx->pd_hist.alloc(kPdHistBins * 8 + 64, st));
+      CK(ctx->pd_ladder.alloc(2 * kPdLadderSteps * 8 + 64, st));
+      CK(ctx->pd_above.alloc(cols * sizeof(PdAbove) + 64, st));
+      CK(ctx->pd_cnt.alloc(64, st));
+      CK(cudaMemsetAsync(ctx->pd_diff.p, 0, cols * 32, st));
+      CK(cudaMemsetAsync(ctx->pd_hist.p, 0, kPdHistBins * 8, st));
+      CK(cudaMemsetAsync(ctx->pd_ladder.p, 0, 2 * kPdLadderSteps * 8, st));
+      CK(cudaMemsetAsync(ctx->pd_cnt.p, 0, 16, st));
+      PdArgs D;
+      memset(&D, 0, sizeof D);
+      D.reads = s->reads.as<DevRead>(); D.flag = s->pflag.as<uint16_t>(); D.code = A.code; D.group = A.group;
+      D.x1 = A.x1; D.isize = A.isize; D.mtid = s->pmtid.as<int32_t>(); D.mpos = s->pmpos.as<int32_t>();
+      D.tpoff = s->d_tpoff.as<uint32_t>(); D.piled = ctx->pd_piled.as<uint8_t>(); D.cdf = ctx->pd_cdf.as<int64_t>();
+      D.cdf_off = ctx->pd_cdfoff.as<uint64_t>(); D.cdf_len = ctx->pd_cdflen.as<uint32_t>();
+      D.orient = ctx->pd_orient.as<uint8_t>(); D.n = (uint32_t)n; D.n_targets = T; D.n_cols = (uint32_t)cols;
+      D.max_span = p->pd_max_span; D.seed = p->pair_distance_seed;
+      D.lower_tail = static_cast<int64_t>(p->pair_distance_tail_quantile * static_cast<double>(kPdUScale));
+      D.z_seed = p->pd_z_seed; D.diff = ctx->pd_diff.as<long long>(); D.blk = ctx->pd_blk.as<long long>();
+      D.mask = ctx->pd_mask.as<uint64_t>(); D.hist = ctx->pd_hist.as<unsigned long long>();
+      D.ladder = ctx->pd_ladder.as<unsigned long long>(); D.above = ctx->pd_above.as<PdAbove>();
+      D.n_above = ctx->pd_cnt.as<unsigned int>(); D.above_cap = (uint32_t)cols;
+      CK(pd_launch(D, ctx->sms, st));
+      pd_launches = 5;
+    }
+  }
   const uint64_t b_ev = n_ev * sizeof(PairEvent), b_nm = n_ev * kPairNameSlot, b_ms = n_mem * 4, b_mk = n_mem * 2;
   const uint64_t o_nm = align256(b_ev), o_ms = o_nm + align256(b_nm), o_mk = o_ms + align256(b_ms);
-  CK(ctx->pin_out.reserve(o_mk + b_mk + 64));
+  const uint64_t o_pd = align256(o_mk + b_mk), b_pd = 64 + (kPdHistBins + 2 * kPdLadderSteps) * 8;
+  CK(ctx->pin_out.reserve(o_pd + b_pd + 64));
   unsigned char* h = ctx->pin_out.at(0);
+  if (pd_on) {
+    CK(cudaMemcpyAsync(h + o_pd, ctx->pd_cnt.p, 16, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h + o_pd + 64, ctx->pd_hist.p, kPdHistBins * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h + o_pd + 64 + kPdHistBins * 8, ctx->pd_ladder.p, 2 * kPdLadderSteps * 8,
+                       cudaMemcpyDeviceToHost, st));
+  }
   if (b_ev) CK(cudaMemcpyAsync(h, ctx->pr_ev.p, b_ev, cudaMemcpyDeviceToHost, st));
   if (b_nm) CK(cudaMemcpyAsync(h + o_nm, ctx->pr_names.p, b_nm, cudaMemcpyDeviceToHost, st));
   if (b_ms) CK(cudaMemcpyAsync(h + o_ms, ctx->pr_mstart.p, b_ms, cudaMemcpyDeviceToHost, st));
   if (b_mk) CK(cudaMemcpyAsync(h + o_mk, ctx->pr_mkey.p, b_mk, cudaMemcpyDeviceToHost, st));
+  uint64_t b_above = 0;
+  if (pd_on) {
+    CK(cudaStreamSynchronize(st));
+    uint32_t cnt[2];
+    memcpy(cnt, h + o_pd, 8);
+    if (cnt[1])
+      return fail(ctx, BSQ_ERR_DATA, "a pair's gap runs outside the pair-distance window (TLEN shorter than the gap, "
+                                     "or the mate outside its target)");
+    pdin.above.resize(cnt[0]);
+    b_above = (uint64_t)cnt[0] * sizeof(PdAbove);
+    if (cnt[0]) CK(cudaMemcpyAsync(pdin.above.data(), ctx->pd_above.p, b_above, cudaMemcpyDeviceToHost, st));
+    memcpy(pdin.hist.data(), h + o_pd + 64, kPdHistBins * 8);
+    memcpy(pdin.ladder, h + o_pd + 64 + kPdHistBins * 8, 2 * kPdLadderSteps * 8);
+  }
   CK(record(ctx->ev1, st));
   CK(cudaStreamSynchronize(st));
   ctx->last_ms = elapsed(ctx->ev0, ctx->ev1);
   ctx->main_ms = elapsed(ctx->evm0, ctx->evm1);   // the classification pass over every read
-  ctx->launches = 1 + 3 + (mp ? 3 : 0) + 1;
+  ctx->launches = 1 + 3 + (mp ? 3 : 0) + 1 + pd_launches;
   ctx->last_h2d = (uint64_t)NRG * 4;
-  ctx->last_d2h = 16 + b_ev + b_nm + b_ms + b_mk;
+  ctx->last_d2h = 16 + b_ev + b_nm + b_ms + b_mk + (pd_on ? b_pd + b_above : 0);
+  ctx->pd_res = host::PdResult();
+  if (pd) host::pd_assemble(pdin, ctx->pd_res);
   in.ev = reinterpret_cast<const PairEvent*>(h);
   in.n_ev = n_ev;
   in.names = reinterpret_cast<const char*>(h + o_nm);
@@ -1257,6 +1368,17 @@ int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* 
   *n_dp = ctx->pair_res.dp.size();
   *n_mp = ctx->pair_res.mp.size();
   *text_bytes = ctx->pair_res.text.size();
+  return BSQ_OK;
+}
+
+int bsq_pd_result(bsq_ctx* ctx, uint64_t* n_regions, bsq_pd_region* regions, uint64_t capacity, bsq_pd_summary* summary) {
+  if (!ctx || !n_regions) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  const host::PdResult& r = ctx->pd_res;
+  *n_regions = r.regions.size();
+  if (summary) *summary = r.summary;
+  if (!regions) return BSQ_OK;
+  if (capacity < r.regions.size()) return fail(ctx, BSQ_ERR_SIZE, "region buffer too small");
+  if (r.regions.size()) memcpy(regions, r.regions.data(), r.regions.size() * sizeof(bsq_pd_region));
   return BSQ_OK;
 }
 
@@ -1763,6 +1885,7 @@ int bsq_bam_decode(bsq_ctx* ctx, bsq_bam* bam, const bsq_bam_groups* groups, uin
   CK(R.lq.alloc(n * 4 + 16, st)); CK(R.soff.alloc(n * 8 + 16, st)); CK(R.coff.alloc(n * 8 + 16, st));
   CK(R.nc.alloc(n * 2 + 16, st)); CK(R.xj.alloc(n + 16, st));
   CK(R.isize.alloc(n * 4 + 16, st)); CK(R.xp.alloc(n + 16, st)); CK(R.qoff.alloc(n * 8 + 24, st));
+  CK(R.mtid.alloc(n * 4 + 16, st)); CK(R.mpos.alloc(n * 4 + 16, st));
   DevMem ncig32, nib, nlen, tmp, ids_dev;
   CK(ncig32.alloc(n * 4 + 16, st));
   CK(nib.alloc(n * 4 + 16, st));
@@ -1775,6 +1898,7 @@ int bsq_bam_decode(bsq_ctx* ctx, bsq_bam* bam, const bsq_bam_groups* groups, uin
   D.read_group = R.rg.as<uint16_t>(); D.l_qseq = R.lq.as<uint32_t>(); D.seq_off = R.soff.as<uint64_t>();
   D.cigar_off = R.coff.as<uint64_t>(); D.n_cigar = R.nc.as<uint16_t>(); D.xj = R.xj.as<uint8_t>();
   D.isize = R.isize.as<int32_t>(); D.xp = R.xp.as<uint8_t>(); D.qoff = R.qoff.as<uint64_t>();
+  D.mtid = R.mtid.as<int32_t>(); D.mpos = R.mpos.as<int32_t>();
   D.cigar = nullptr; D.seq = nullptr; D.qual = nullptr; D.qname = nullptr;
   CK(bam_fields(bam->stream.as<uint8_t>(), offsets.as<uint64_t>(), n, (uint32_t)bam->names.size(), G,
                 ids_dev.as<char>(), D, ncig32.as<uint32_t>(), nib.as<uint32_t>(), nlen.as<uint32_t>(), w, ctx->sms, st));
@@ -1821,6 +1945,7 @@ int bsq_bam_decode(bsq_ctx* ctx, bsq_bam* bam, const bsq_bam_groups* groups, uin
   }
   R.has_xj = true;
   R.has_pairs = true;
+  R.has_mates = true;
   bam->decoded = true;
   if (n_records) *n_records = R.n;
   if (n_cigar_total) *n_cigar_total = R.n_cigar_total;
@@ -1842,7 +1967,7 @@ int bsq_bam_copy_records(bsq_ctx* ctx, const bsq_bam* bam, const bsq_read_arrays
       {out->cigar_off, &R.coff, n * 8}, {out->n_cigar, &R.nc, n * 2}, {out->xj, &R.xj, n},
       {out->cigar, &R.cigar, R.n_cigar_total * 4}, {out->seq, &R.seq, R.n_bases_total / 2},
       {out->qual, &R.qual, R.n_bases_total}, {out->isize, &R.isize, n * 4}, {out->xp, &R.xp, n},
-      {out->qname_off, &R.qoff, (n + 1) * 8}};
+      {out->qname_off, &R.qoff, (n + 1) * 8}, {out->mtid, &R.mtid, n * 4}, {out->mpos, &R.mpos, n * 4}};
   for (const Item& it : items)
     if (it.dst && it.bytes) CK(cudaMemcpyAsync(it.dst, it.src->p, it.bytes, cudaMemcpyDeviceToHost, ctx->stream));
   if (out->qname) {

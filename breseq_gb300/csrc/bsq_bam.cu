@@ -281,6 +281,8 @@ __global__ void __launch_bounds__(256) bam_fields_kernel(const uint8_t* stream, 
     R.xj[i] = has_xj ? 1 : 0;
     R.xp[i] = (uint8_t)xp;
     R.isize[i] = (int32_t)rd32(stream + offsets[i] + 32);   // TLEN: inside the 32 fixed bytes the walk checked
+    R.mtid[i] = (int32_t)rd32(stream + offsets[i] + 24);    // RNEXT
+    R.mpos[i] = (int32_t)rd32(stream + offsets[i] + 28);    // PNEXT
     R.read_group[i] = (uint16_t)group;
     uint32_t file = 0;
     if (G.n > 0 && group < G.n && G.file_count[group] > 0)

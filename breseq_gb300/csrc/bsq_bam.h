@@ -65,6 +65,8 @@ struct BamRecordsDev {
   uint8_t* xp;           // XP:Z orientation code (BSQ_XP_*)
   uint64_t* qoff;        // [n + 1] read-name offsets
   char* qname;           // names without terminators; null until their total is known
+  int32_t* mtid;         // RNEXT
+  int32_t* mpos;         // PNEXT
 };
 
 cudaError_t bam_inflate(const uint8_t* file, const BgzfBlock* blocks, uint32_t n_blocks, uint8_t* out, uint32_t* err,

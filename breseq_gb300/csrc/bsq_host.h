@@ -108,5 +108,22 @@ struct PairReplayResult {
 };
 int pair_replay(const PairReplayInput& in, PairReplayResult& out);
 
+// Pair-distance regions and calibration (bsq_pairs_host.cpp) from the device's positions above a seed,
+// its z histogram and ladder counts.
+struct PdAssembleInput {
+  std::vector<uint32_t> tpoff;
+  std::vector<PdAbove> above;        // any order
+  std::vector<uint64_t> hist;        // kPdHistBins; empty when the scan was not set up
+  uint64_t ladder[2][kPdLadderSteps] = {};
+  bool enabled = false;
+  double z_seed = 0, mean_covering_gap = 0;
+  uint64_t total_reference_length = 0;
+};
+struct PdResult {
+  std::vector<bsq_pd_region> regions;   // capped and in the writer's order
+  bsq_pd_summary summary;
+};
+void pd_assemble(PdAssembleInput& in, PdResult& out);
+
 }  // namespace host
 }  // namespace bsq

@@ -4,6 +4,7 @@
 // host's sliding-window replay (bsq_pairs_host.cpp).
 #pragma once
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 #include "bsq_common.h"
@@ -78,6 +79,119 @@ BSQ_PAIR_HD void pair_classify_one(uint32_t dflags, uint32_t f, uint32_t xp, int
     }
   }
 }
+
+// ------------------------------------------------------------------ pair distance (PD)
+constexpr int64_t kPdUScale = 1048576;          // quantiles in 2^20 fixed point
+constexpr int kPdLadderSteps = 21;              // seed ladder |z| >= 1 + 0.25 k
+constexpr int kPdHistPerUnit = 50, kPdHistLimit = 40;
+constexpr int kPdHistBins = 2 * kPdHistLimit * kPdHistPerUnit + 1;
+constexpr int32_t kPdHistMinCovering = 4;
+constexpr int kPdBitLadder = 2;                 // mask bits: 0 above L, 1 above S, 2.. rungs L, 2 + 21.. rungs S
+
+// The PD enter test of one read (identify_mutations.cpp:1514-1555): a normally oriented pair with
+// both mates on this target, TLEN > 0, X1 <= 1, in a DP group whose null it matches; its unsequenced
+// gap [lo, hi] (between-base positions, lo = the read's aligned end, hi = the mate's start - 1) is
+// added with its distance quantile u and tail bin (0 long, 1 short, -1 neither).  bad: the interval
+// breaks the reference's ring-buffer assertion (:2590-2593), where breseq stops.
+struct PdInterval {
+  int32_t lo, hi;
+  int64_t u;
+  int bin;
+  bool ok, bad;
+};
+BSQ_PAIR_HD void pd_interval_one(uint32_t dflags, uint32_t f, bool xp_skip, int32_t gi, uint32_t x1, int32_t tid,
+                                 int32_t mtid, int32_t isize, uint32_t start1, uint32_t end1, int32_t mpos,
+                                 const int64_t* cdf, uint32_t cdf_len, uint32_t orient, int32_t max_span,
+                                 int64_t lower_tail, PdInterval& out) {
+  out.ok = false;
+  out.bad = false;
+  if ((dflags & kSkip) || xp_skip || gi < 0) return;
+  if (!(f & 0x1) || (f & 0x4) || (f & (0x100 | 0x800 | 0x8))) return;
+  const bool rev = (dflags & kRev) != 0, mrev = (f & 0x20) != 0;
+  if (mtid != tid || isize <= 0 || rev == mrev || x1 > 1) return;
+  if (orient == 0 && rev) return;                 // the group's null is FR
+  if (orient == 1 && !rev) return;                // RF
+  const int32_t lo = (int32_t)end1, hi = mpos;    // mate_start_1 - 1
+  if (!(hi >= lo) || cdf_len == 0 || isize > max_span) return;
+  const int64_t u = (uint32_t)isize < cdf_len ? cdf[isize] : kPdUScale;
+  out.bin = (u >= kPdUScale - lower_tail) ? 0 : (u <= lower_tail ? 1 : -1);
+  out.lo = lo;
+  out.hi = hi;
+  out.u = u;
+  out.ok = true;
+  out.bad = !(lo >= (int32_t)start1 && (int64_t)hi + 1 <= (int64_t)start1 + max_span);
+}
+
+// The per-position PD statistics (identify_mutations.cpp:2660-2706) from the covering counts: the
+// rank-sum z, the z histogram bin (-1 when n < 4), and the mask of seed tests (above per direction,
+// and each ladder rung per direction).  in_seq: the position is inside the target (not the flush).
+BSQ_PAIR_HD void pd_eval_one(int64_t n, int64_t nlong, int64_t nshort, int64_t u, bool in_seq, double z_seed,
+                             int32_t seed, double& z, int& hist_bin, uint64_t& mask) {
+  z = 0.0;
+  hist_bin = -1;
+  if (n > 0) {
+    const double mean_offset = ((double)u - (double)n * (double)kPdUScale / 2.0) / (double)kPdUScale;
+    z = mean_offset * sqrt(12.0 / (double)n);
+    if (n >= kPdHistMinCovering) {
+      int b = (int)floor(z * kPdHistPerUnit) + kPdHistLimit * kPdHistPerUnit;
+      if (b < 0) b = 0;
+      if (b >= kPdHistBins) b = kPdHistBins - 1;
+      hist_bin = b;
+    }
+  }
+  mask = 0;
+  for (int bin = 0; bin < 2; bin++) {
+    const int64_t tail = bin == 0 ? nlong : nshort;
+    const bool right_way = bin == 0 ? (z >= z_seed) : (z <= -z_seed);
+    const bool tail_ok = (tail >= seed) && in_seq;
+    if (tail_ok && right_way) mask |= 1ull << bin;
+    const double directed = bin == 0 ? z : -z;
+    if (tail_ok)
+      for (int k = 0; k < kPdLadderSteps; k++)
+        if (directed >= 1.0 + 0.25 * (double)k) mask |= 1ull << (kPdBitLadder + bin * kPdLadderSteps + k);
+  }
+}
+
+// One position where a PD direction is above its seed, for the host's region assembly.
+struct PdAbove {
+  uint32_t col;
+  uint32_t bits;     // bit 0: L, bit 1: S
+  int32_t n, nlong, nshort, pad;
+  double z;
+};
+static_assert(sizeof(PdAbove) == 32, "PdAbove layout");
+
+struct PdArgs {
+  const DevRead* reads;
+  const uint16_t* flag;
+  const uint8_t* code;        // pair classification (kPairXpSkip)
+  const uint8_t* group;       // DP group per read (0xFF none)
+  const uint32_t* x1;
+  const int32_t* isize;
+  const int32_t* mtid;
+  const int32_t* mpos;
+  const uint32_t* tpoff;      // [n_targets + 1]
+  const uint8_t* piled;       // [n_targets]
+  const int64_t* cdf;         // all groups' nulls, group g at cdf_off[g]
+  const uint64_t* cdf_off;
+  const uint32_t* cdf_len;
+  const uint8_t* orient;
+  uint32_t n, n_targets, n_cols;
+  int32_t max_span, seed;
+  int64_t lower_tail;
+  double z_seed;
+  long long* diff;            // [n_cols][4]: covering, long, short, quantile sum
+  long long* blk;             // [blocks][4]
+  uint64_t* mask;             // [n_cols]
+  unsigned long long* hist;   // [kPdHistBins]
+  unsigned long long* ladder; // [2][kPdLadderSteps]
+  PdAbove* above;
+  unsigned int* n_above;      // [0] count, [1] ring-assertion violations
+  uint32_t above_cap;
+};
+constexpr int kPdScanCols = 2048;               // columns per scan block (256 threads x 8)
+
+cudaError_t pd_launch(const PdArgs& a, int sms, cudaStream_t st);
 
 struct PairArgs {
   const DevRead* reads;

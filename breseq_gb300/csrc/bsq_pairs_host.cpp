@@ -18,6 +18,8 @@
 #include <atomic>
 #include <deque>
 #include <fstream>
+#include <iomanip>
+#include <sstream>
 #include <string>
 #include <thread>
 #include <vector>
@@ -300,6 +302,144 @@ int pair_replay(const PairReplayInput& in, PairReplayResult& out) {
   return BSQ_OK;
 }
 
+// identify_mutations_pileup::pd_z_inflation (identify_mutations.cpp:2758-2786): the spread of the
+// per-position z over the genome, as the interquartile range of its histogram over 1.34898038.
+static double pd_z_inflation(const std::vector<uint64_t>& hist) {
+  if (hist.empty()) return 1.0;
+  uint64_t total = 0;
+  for (uint64_t h : hist) total += h;
+  if (total < 1000) return 1.0;
+  const uint64_t want_lo = total / 4, want_hi = (total * 3) / 4;
+  double q_lo = 0.0, q_hi = 0.0;
+  uint64_t run = 0;
+  bool have_lo = false, have_hi = false;
+  for (size_t i = 0; i < hist.size(); i++) {
+    run += hist[i];
+    const double centre = (static_cast<double>(i) + 0.5) / kPdHistPerUnit - kPdHistLimit;
+    if (!have_lo && (run >= want_lo)) { q_lo = centre; have_lo = true; }
+    if (!have_hi && (run >= want_hi)) { q_hi = centre; have_hi = true; break; }
+  }
+  if (!have_lo || !have_hi) return 1.0;
+  const double sd = (q_hi - q_lo) / 1.34898038;
+  if (!(sd > 1.0)) return 1.0;
+  return sd;
+}
+
+static double pd_ladder_z(int i) { return 1.0 + 0.25 * static_cast<double>(i); }
+
+// pd_fit_region_tail (identify_mutations.cpp:2788-2850): a weighted least-squares fit of
+// log(count) against t^2 over the ladder rungs with enough regions and past the bulk.
+static bool pd_fit_region_tail(const uint64_t (&ladder)[2][kPdLadderSteps], bool enabled, double& out_log_intercept,
+                               double& out_sigma, double& out_fit_lo, double& out_fit_hi) {
+  out_log_intercept = 0.0;
+  out_sigma = 1.0;
+  out_fit_lo = 0.0;
+  out_fit_hi = 0.0;
+  if (!enabled) return false;
+  const uint64_t kMinRegions = 20, kTailFactor = 3;
+  const int kMinRungs = 3;
+  uint64_t max_count = 0;
+  for (int step = 0; step < kPdLadderSteps; step++) max_count = std::max(max_count, ladder[0][step] + ladder[1][step]);
+  double sw = 0.0, swx = 0.0, swy = 0.0, swxx = 0.0, swxy = 0.0;
+  int rungs = 0;
+  for (int step = 0; step < kPdLadderSteps; step++) {
+    const uint64_t count = ladder[0][step] + ladder[1][step];
+    if (count < kMinRegions) continue;
+    if (count * kTailFactor > max_count) continue;
+    const double t = pd_ladder_z(step);
+    const double x = t * t;
+    const double y = log(static_cast<double>(count));
+    const double w = static_cast<double>(count);
+    sw += w; swx += w * x; swy += w * y; swxx += w * x * x; swxy += w * x * y;
+    if (rungs == 0) out_fit_lo = t;
+    out_fit_hi = t;
+    rungs++;
+  }
+  if (rungs < kMinRungs) return false;
+  const double denom = sw * swxx - swx * swx;
+  if (!(fabs(denom) > 0.0)) return false;
+  const double slope = (sw * swxy - swx * swy) / denom;
+  const double intercept = (swy - slope * swx) / sw;
+  if (!(slope < 0.0)) return false;
+  const double sigma = sqrt(-1.0 / (2.0 * slope));
+  if (!(sigma > 0.0) || !std::isfinite(sigma)) return false;
+  out_log_intercept = intercept;
+  out_sigma = sigma;
+  return true;
+}
+
+void pd_assemble(PdAssembleInput& in, PdResult& out) {
+  // regions: maximal runs of consecutive positions above a direction's seed; the peak is the first
+  // position of largest |z| (identify_mutations.cpp:2708-2742)
+  std::sort(in.above.begin(), in.above.end(), [](const PdAbove& a, const PdAbove& b) { return a.col < b.col; });
+  std::vector<bsq_pd_region> regions;
+  for (int bin = 0; bin < 2; bin++) {
+    bool open = false;
+    uint32_t last = 0;
+    bsq_pd_region r;
+    auto close = [&]() {
+      const uint32_t t = (uint32_t)(std::upper_bound(in.tpoff.begin(), in.tpoff.end(), last) - in.tpoff.begin()) - 1;
+      r.end = last - in.tpoff[t] + 1;
+      regions.push_back(r);
+      open = false;
+    };
+    for (const PdAbove& a : in.above) {
+      if (!(a.bits & (1u << bin))) continue;
+      if (open && a.col != last + 1) close();
+      if (!open) {
+        const uint32_t t = (uint32_t)(std::upper_bound(in.tpoff.begin(), in.tpoff.end(), a.col) - in.tpoff.begin()) - 1;
+        memset(&r, 0, sizeof r);
+        r.target = t;
+        r.start = a.col - in.tpoff[t] + 1;
+        r.direction = bin == 0 ? 'L' : 'S';
+        r.peak_position = r.start;
+        r.peak_covering = a.n;
+        r.peak_tail = bin == 0 ? a.nlong : a.nshort;
+        r.peak_z = a.z;
+        open = true;
+      } else if (fabs(a.z) > fabs(r.peak_z)) {
+        r.peak_position = a.col - in.tpoff[r.target] + 1;
+        r.peak_covering = a.n;
+        r.peak_tail = bin == 0 ? a.nlong : a.nshort;
+        r.peak_z = a.z;
+      }
+      last = a.col;
+    }
+    if (open) close();
+  }
+  // calibration (fill_pd_summary, :2852-2862)
+  bsq_pd_summary& c = out.summary;
+  memset(&c, 0, sizeof c);
+  c.mean_covering_gap = in.mean_covering_gap;
+  c.n_effective_tests =
+      (in.mean_covering_gap > 0.0) ? static_cast<double>(in.total_reference_length) / in.mean_covering_gap : 0.0;
+  c.seed_z_used = in.z_seed;
+  c.z_iqr_inflation = pd_z_inflation(in.hist);
+  c.regions_seeded = regions.size();
+  c.region_tail_fit_ok = pd_fit_region_tail(in.ladder, in.enabled, c.region_tail_log_intercept, c.region_tail_sigma,
+                                            c.region_tail_fit_lo, c.region_tail_fit_hi) ? 1 : 0;
+  for (int step = 0; step < kPdLadderSteps; step++) c.ladder[step] = in.ladder[0][step] + in.ladder[1][step];
+  // the rescan budget: raise the seed to the first rung at or above it with at most 3000 regions
+  // (write_pd_candidate_regions, :2875-2904)
+  const uint64_t kMaxCandidateRegions = 3000;
+  double capped_z = c.seed_z_used;
+  for (int step = 0; step < kPdLadderSteps; step++) {
+    const double t = pd_ladder_z(step);
+    if (t < c.seed_z_used) continue;
+    capped_z = t;
+    if (c.ladder[step] <= kMaxCandidateRegions) break;
+  }
+  if (capped_z > c.seed_z_used) {
+    std::vector<bsq_pd_region> kept;
+    for (const bsq_pd_region& r : regions)
+      if (fabs(r.peak_z) >= capped_z) kept.push_back(r);
+    regions.swap(kept);
+    c.seed_z_used = capped_z;
+    c.regions_seeded = regions.size();
+  }
+  out.regions = std::move(regions);
+}
+
 }  // namespace host
 }  // namespace bsq
 
@@ -354,4 +494,44 @@ extern "C" int bsq_write_mp_candidate_regions(const char* path, const char* cons
                          if (a.start != b.start) return a.start < b.start;
                          return a.strand < b.strand;
                        });
+}
+
+extern "C" int bsq_write_pd_candidate_regions(const char* path, const char* const* target_names,
+                                              const bsq_pd_region* regions, uint64_t n, const bsq_pd_summary* c) {
+  // identify_mutations.cpp:2906-2957: calibration lines, the ladder, then the regions sorted by
+  // (seq_id, start, direction)
+  if (!path || !c || (n && (!regions || !target_names))) return BSQ_ERR_INVALID;
+  std::vector<const bsq_pd_region*> v(n);
+  for (uint64_t i = 0; i < n; i++) v[i] = regions + i;
+  std::sort(v.begin(), v.end(), [&](const bsq_pd_region* a, const bsq_pd_region* b) {
+    const std::string sa = target_names[a->target], sb = target_names[b->target];
+    if (sa != sb) return sa < sb;
+    if (a->start != b->start) return a->start < b->start;
+    return a->direction < b->direction;
+  });
+  std::ofstream out(path);
+  if (!out) return BSQ_ERR_INVALID;
+  out << std::fixed << std::setprecision(6);
+  out << "#mean_covering_gap=" << c->mean_covering_gap << "\n";
+  out << "#n_effective_tests=" << c->n_effective_tests << "\n";
+  out << "#seed_z=" << c->seed_z_used << "\n";
+  out << "#z_iqr_inflation=" << c->z_iqr_inflation << "\n";
+  out << "#region_tail_fit_ok=" << (c->region_tail_fit_ok ? 1 : 0) << "\n";
+  out << "#region_tail_log_intercept=" << c->region_tail_log_intercept << "\n";
+  out << "#region_tail_sigma=" << c->region_tail_sigma << "\n";
+  out << "#region_tail_fit_lo=" << c->region_tail_fit_lo << "\n";
+  out << "#region_tail_fit_hi=" << c->region_tail_fit_hi << "\n";
+  out << "#region_ladder=";
+  for (int step = 0; step < bsq::kPdLadderSteps; step++) {
+    if (step) out << ";";
+    out << std::setprecision(2) << (1.0 + 0.25 * static_cast<double>(step)) << ":" << c->ladder[step];
+  }
+  out << "\n";
+  out << "seq_id,start,end,direction,length,peak_position,peak_covering_count,peak_tail_count,peak_z\n";
+  out << std::setprecision(4);
+  for (const bsq_pd_region* r : v)
+    out << target_names[r->target] << "," << r->start << "," << r->end << "," << r->direction << ","
+        << (r->end - r->start + 1) << "," << r->peak_position << "," << r->peak_covering << "," << r->peak_tail
+        << "," << r->peak_z << "\n";
+  return out ? BSQ_OK : BSQ_ERR_INVALID;
 }

@@ -103,6 +103,8 @@ class Sample:
     xp: np.ndarray | None = None
     qname_off: np.ndarray | None = None
     qname: np.ndarray | None = None
+    mtid: np.ndarray | None = None     # mate reference id and 0-based position (RNEXT / PNEXT)
+    mpos: np.ndarray | None = None
 
     @property
     def n_reads(self) -> int:
@@ -598,15 +600,18 @@ def bam_groups(s: Sample):
 
 def with_pairs(s: Sample, seed: int = 0, discordant_sites: int = 6, unmapped_sites: int = 6, site_span: int = 250,
                site_fraction: float = 0.6, background_discordant: float = 0.002, background_unmapped: float = 0.004,
-               no_xp_fraction: float = 0.0, supplementary_fraction: float = 0.001) -> Sample:
+               no_xp_fraction: float = 0.0, supplementary_fraction: float = 0.001, distance_sites: int = 0,
+               distance_shift: int = 300) -> Sample:
     """Pair annotations for a sample, as breseq's alignment resolution leaves them
     (src/breseq/resolve_alignments.cpp:1255-1300): read names <read file + 1>:<fragment>, TLEN, and the
     XP orientation of every pair with both mates mapped.  Paired reads are proper pairs with XP FR,
     except near `discordant_sites` breakpoints (and a background rate), where pairs are discordant
     (not proper, XP FR / RF / FF, long TLEN), and near `unmapped_sites` insertions (and a background
     rate), where the mate is unmapped (0x8, no XP, TLEN 0).  no_xp_fraction of the discordant reads
-    lose their XP tag.  The scoring passes read none of these fields (the flag filter is 0x704), so
-    their results do not change."""
+    lose their XP tag.  Mate positions follow TLEN (a positive TLEN puts the mate's end there); near
+    `distance_sites` points the pairs starting up to 450 bases before it are `distance_shift` longer.
+    The scoring passes read none of these fields (the flag filter is 0x704), so their results do not
+    change."""
     rng = np.random.default_rng(seed)
     n = s.n_reads
     flag = s.flag.astype(np.uint16).copy()
@@ -630,6 +635,24 @@ def with_pairs(s: Sample, seed: int = 0, discordant_sites: int = 6, unmapped_sit
     isize[paired] = np.where(rng.random(int(paired.sum())) < 0.5, 1, -1) * mag[paired]
     isize[disc] = rng.integers(-60000, 60000, int(disc.sum()))
     isize[unm] = 0
+    tlen_t = (s.target_offset[s.tid + 1] - s.target_offset[s.tid]).astype(np.int64)
+    pos64 = s.pos.astype(np.int64)
+    if distance_sites:
+        sites = rng.integers(0, max(1, total), distance_sites)
+        near_site = np.zeros(n, bool)
+        for c in sites:
+            near_site |= (col > c - 450) & (col <= c)
+        shift = paired & ~disc & ~unm & (isize > 0) & near_site
+        isize[shift] += distance_shift
+    # mates: a positive TLEN ends the mate there, a negative one starts it |TLEN| before this read's end
+    L = s.l_qseq.astype(np.int64)
+    mpos = np.where(isize > 0, pos64 + isize - L, pos64 + L + isize)
+    mpos = np.clip(mpos, 0, tlen_t - 1)
+    mpos[unm] = pos64[unm]
+    mpos[~paired] = -1
+    mtid = np.where(paired, s.tid, -1).astype(np.int32)
+    keep_in = (isize > 0) & (pos64 + isize > tlen_t)
+    isize[keep_in] = (tlen_t - pos64)[keep_in].astype(np.int32)   # mates stay on the target
     # names "<read file + 1>:<fragment>", assembled digit by digit
     a = s.read_file.astype(np.int64) + 1
     b = np.arange(n, dtype=np.int64) // 2
@@ -653,7 +676,23 @@ def with_pairs(s: Sample, seed: int = 0, discordant_sites: int = 6, unmapped_sit
         names[i] = b"plainname"
         qname_off[1:] = np.cumsum([len(x) for x in names])
         qname = np.frombuffer(b"".join(names), dtype=np.uint8).copy()
-    return replace(s, flag=flag, isize=isize, xp=xp, qname_off=qname_off, qname=qname)
+    return replace(s, flag=flag, isize=isize, xp=xp, qname_off=qname_off, qname=qname, mtid=mtid,
+                   mpos=mpos.astype(np.int32))
+
+
+def pd_null(s: Sample, max_distance: int = 2000) -> np.ndarray:
+    """A pair-distance null for tests: the mid-CDF (G(d-1) + G(d)) / 2 of the positive TLENs of proper
+    pairs in 2^20 fixed point, indexed by distance, as identify_mutations' pd_build_cdf scales it.  Each
+    distance is weighted by the gap its pairs leave between two reads (d - 2 x read length), the number
+    of positions a pair of that distance covers, so the null is that of the covering pairs."""
+    d = s.isize[((s.flag & 0x3) == 0x3) & (s.isize > 0)].astype(np.int64)
+    trunc = 2 * int(np.median(s.l_qseq)) if s.n_reads else 0
+    w = np.bincount(np.clip(d, 0, max_distance), minlength=max_distance + 1).astype(np.float64)
+    w *= np.maximum(np.arange(max_distance + 1) - trunc, 0)
+    total = w.sum()
+    below = np.concatenate([[0.0], np.cumsum(w)[:-1]])
+    mid = (below + 0.5 * w) / total
+    return np.clip((mid * 1048576 + 0.5).astype(np.int64), 0, 1048576)
 
 
 def bam_bytes(s: Sample, level: int = 6, block_payload: int = 0xFF00, seed: int = 0, rg_tags: bool = True) -> bytes:
@@ -723,8 +762,10 @@ def bam_bytes(s: Sample, level: int = 6, block_payload: int = 0xFF00, seed: int 
             elif rng.random() < 0.2:
                 aux += b"XPZRR\0"    # an XP value other than FR / RF / FF: no orientation
         tlen = int(s.isize[i]) if s.isize is not None else 0
+        mt = int(s.mtid[i]) if s.mtid is not None else -1
+        mp = int(s.mpos[i]) if s.mpos is not None else -1
         body = struct.pack("<iiBBHHHiiii", int(s.tid[i]), pos, len(name), int(s.mapq[i]), _reg2bin(pos, pos + max(rlen, 1)),
-                           nc, int(s.flag[i]), L, -1, -1, tlen)
+                           nc, int(s.flag[i]), L, mt, mp, tlen)
         rec = body + name + cig.astype("<u4").tobytes() + seq + qual + aux
         rec = struct.pack("<i", len(rec)) + rec
         if len(buf) + len(rec) > block_payload and buf:

@@ -49,6 +49,7 @@ extern "C" {
 #define BSQ_FLAG_UNMAP       0x4
 #define BSQ_FLAG_MUNMAP      0x8
 #define BSQ_FLAG_REVERSE     0x10
+#define BSQ_FLAG_MREVERSE    0x20
 #define BSQ_FLAG_READ2       0x80
 #define BSQ_FLAG_SECONDARY   0x100
 #define BSQ_FLAG_QCFAIL      0x200
@@ -114,6 +115,10 @@ typedef struct bsq_read_soa {
     const uint8_t*  xp;
     const uint64_t* qname_off;
     const char*     qname;
+    /* mate reference id and 0-based position (RNEXT / PNEXT), read only by the pair-distance scan;
+     * NULL when absent */
+    const int32_t*  mtid;
+    const int32_t*  mpos;
 } bsq_read_soa;
 
 #define BSQ_XP_FR   0
@@ -492,6 +497,8 @@ typedef struct bsq_read_arrays {
     uint8_t*  xp;
     uint64_t* qname_off;
     char*     qname;
+    int32_t*  mtid;
+    int32_t*  mpos;
 } bsq_read_arrays;
 int bsq_bam_copy_records(bsq_ctx* ctx, const bsq_bam* bam, const bsq_read_arrays* out);
 /* Bytes of the decoded records' read names (no terminators). */
@@ -583,7 +590,52 @@ typedef struct bsq_pair_params {
     /* per target: identify_mutations' deletion propagation cutoff; a target below 0 is not piled up
      * (pileup_callback returns at once, identify_mutations.cpp:1318-1329) */
     const double*   deletion_propagation_cutoff;
+    /* Pair-distance (PD) scan (--predict-pair-distance; identify_mutations.cpp:920-1006 setup,
+     * :1514-1555 enter step, :2588-2757 windows, :2758-2967 calibration and writer).  Needs the
+     * records' mtid / mpos.  Per DP group: the null as pd_build_cdf builds it (:112-141: the mid-CDF
+     * of the length-bias-corrected distance histogram in 2^20 fixed point, indexed by distance; length
+     * 0 = no null for the group) and the majority orientation the null was built from. */
+    int32_t                predict_pair_distance;
+    const int64_t* const*  pd_cdf;
+    const uint32_t*        pd_cdf_len;
+    const uint8_t*         pd_orientation;      /* BSQ_XP_FR, BSQ_XP_RF, or BSQ_XP_NONE for "" (any) */
+    int32_t                pd_max_span;         /* _pd_max_span as the constructor derives it */
+    double                 pd_z_seed;           /* _pd_z_seed as the constructor derives it */
+    int32_t                pair_distance_seed;  /* --pair-distance-seed */
+    double                 pair_distance_tail_quantile;
+    double                 pd_mean_covering_gap;     /* the largest group's covering gap (header line) */
+    uint64_t               total_reference_length;   /* for n_effective_tests */
 } bsq_pair_params;
+
+/* One PD candidate region (identify_mutations.cpp:2713-2730) and the calibration lines of
+ * pd_candidate_regions.csv (:2852-2862). */
+typedef struct bsq_pd_region {
+    uint32_t target;
+    uint32_t start;
+    uint32_t end;
+    char     direction;         /* 'L' (pairs farther apart) or 'S' */
+    char     reserved[3];
+    uint32_t peak_position;
+    int32_t  peak_covering;
+    int32_t  peak_tail;
+    uint32_t reserved2;
+    double   peak_z;
+} bsq_pd_region;
+
+typedef struct bsq_pd_summary {
+    double   mean_covering_gap;
+    double   n_effective_tests;
+    double   seed_z_used;
+    double   z_iqr_inflation;
+    int32_t  region_tail_fit_ok;
+    int32_t  reserved;
+    double   region_tail_log_intercept;
+    double   region_tail_sigma;
+    double   region_tail_fit_lo;
+    double   region_tail_fit_hi;
+    uint64_t ladder[21];        /* seeded regions at |z| >= 1 + 0.25 k, both directions */
+    uint64_t regions_seeded;
+} bsq_pd_summary;
 
 /* One candidate region.  Text fields are in the result's text buffer at [text_off, text_off +
  * text_len): DP "<read1>__<read2>__<r1_insert_size>__<read_start>__<read_end>" per read, MP
@@ -609,6 +661,13 @@ int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* 
                         uint64_t* n_mp, uint64_t* text_bytes);
 int bsq_pair_result_copy(bsq_ctx* ctx, bsq_pair_region* dp, uint64_t n_dp, bsq_pair_region* mp, uint64_t n_mp,
                          char* text, uint64_t text_bytes);
+/* The PD result of the last bsq_pair_candidates call: regions in the order the writer prints them
+ * (after its rescan-budget cap, identify_mutations.cpp:2875-2904) and the calibration. */
+int bsq_pd_result(bsq_ctx* ctx, uint64_t* n_regions, bsq_pd_region* regions, uint64_t capacity,
+                  bsq_pd_summary* summary);
+/* pd_candidate_regions.csv (identify_mutations.cpp:2864-2967) */
+int bsq_write_pd_candidate_regions(const char* path, const char* const* target_names, const bsq_pd_region* regions,
+                                   uint64_t n, const bsq_pd_summary* summary);
 /* dp_candidate_regions.csv / mp_candidate_regions.csv (identify_mutations.cpp:2524-2586) */
 int bsq_write_dp_candidate_regions(const char* path, const char* const* target_names, const bsq_pair_region* regions,
                                    uint64_t n, const char* text);

@@ -62,7 +62,7 @@ def read_bam(data: bytes, groups=None):
         o += 8 + l_name
     ids, base, count = groups if groups is not None else ([], None, None)
     cols = {k: [] for k in ("tid", "pos", "flag", "mapq", "x1", "xl", "xr", "read_file", "read_group", "l_qseq",
-                            "n_cigar", "xj", "isize", "xp")}
+                            "n_cigar", "xj", "isize", "xp", "mtid", "mpos")}
     cig, seq, qual, qnames = [], [], [], []
     seen_unplaced = False
     int_fmt = {"c": "<b", "C": "<B", "s": "<h", "S": "<H", "i": "<i", "I": "<I"}
@@ -117,11 +117,11 @@ def read_bam(data: bytes, groups=None):
         xp = 3
         if "XP" in tags and tags["XP"][0] in "ZH":
             xp = {b"FR\0": 0, b"RF\0": 1, b"FF\0": 2}.get(bytes(tags["XP"][1]), 3)
-        tlen = struct.unpack_from("<i", stream, o_rec + 32)[0]
+        mtid, mpos, tlen = struct.unpack_from("<iii", stream, o_rec + 24)
         for k, v in (("tid", ref_id), ("pos", pos), ("flag", flag), ("mapq", mapq),
                      ("x1", as_int("X1", 1) & 0xFFFFFFFF), ("xl", as_int("XL", -1)), ("xr", as_int("XR", -1)),
                      ("read_file", rfile), ("read_group", group), ("l_qseq", l_seq), ("n_cigar", n_cig),
-                     ("xj", 1 if "XJ" in tags else 0), ("isize", tlen), ("xp", xp)):
+                     ("xj", 1 if "XJ" in tags else 0), ("isize", tlen), ("xp", xp), ("mtid", mtid), ("mpos", mpos)):
             cols[k].append(v)
         qnames.append(stream[o_rec + 36:o_rec + 36 + l_name - 1])
         cig.append(np.frombuffer(stream[c0:s0], dtype="<u4"))
@@ -131,7 +131,7 @@ def read_bam(data: bytes, groups=None):
         qual.append(np.frombuffer(ql, dtype=np.uint8))
     dts = dict(tid=np.int32, pos=np.int32, flag=np.uint16, mapq=np.uint8, x1=np.uint32, xl=np.int32, xr=np.int32,
                read_file=np.uint8, read_group=np.uint16, l_qseq=np.uint32, n_cigar=np.uint16, xj=np.uint8,
-               isize=np.int32, xp=np.uint8)
+               isize=np.int32, xp=np.uint8, mtid=np.int32, mpos=np.int32)
     rec = {k: np.array(v, dtype=dts[k]) for k, v in cols.items()}
     nc = rec["n_cigar"].astype(np.uint64)
     rec["cigar_off"] = np.concatenate([[0], np.cumsum(nc)[:-1]]).astype(np.uint64) if len(nc) else np.zeros(0, np.uint64)

@@ -49,6 +49,7 @@
 #include <cstring>
 #include <deque>
 #include <functional>
+#include <iomanip>
 #include <limits>
 #include <map>
 #include <sstream>
@@ -1857,7 +1858,7 @@ std::string mp_desc(const MpRead& r) { return std::to_string(r.start) + "__" + s
 
 extern "C" int oracle_pair_candidates(const bsq_reference* ref, const bsq_read_soa* rd, const bsq_pair_params* prm,
                                       const char* const* target_names, const char* dp_path, const char* mp_path,
-                                      char* errbuf, int errcap) {
+                                      const char* pd_path, char* errbuf, int errcap) {
   using namespace opair;
   Data d;
   d.ref = ref;
@@ -1874,7 +1875,30 @@ extern "C" int oracle_pair_candidates(const bsq_reference* ref, const bsq_read_s
   std::vector<std::string> dp_desc_v[6], mp_desc_v[2];
   std::vector<DpRegion> dp_regions;
   std::vector<MpRegion> mp_regions;
-  for (uint32_t t : std::vector<uint32_t>(ref->target_order, ref->target_order + ref->n_target_order)) {
+  // pair distance (identify_mutations.cpp:920-1006, 1514-1555, 2588-2757)
+  const int64_t kS = 1048576;
+  bool pd_usable = false;
+  for (uint32_t g = 0; g < G && prm->predict_pair_distance; g++) if (prm->pd_cdf_len[g]) pd_usable = true;
+  const bool pd_on = prm->predict_pair_distance && G > 0 && pd_usable && prm->pd_max_span > 0;
+  const int32_t ring_w = prm->pd_max_span + 2;
+  std::vector<int32_t> ring_n, ring_long, ring_short;
+  std::vector<int64_t> ring_u;
+  std::vector<uint64_t> z_hist;
+  if (prm->predict_pair_distance && G > 0) z_hist.assign(4001, 0);
+  int32_t pd_n = 0, pd_long = 0, pd_short = 0;
+  int64_t pd_u = 0;
+  uint32_t pd_last_b = 0;
+  uint32_t pd_start[2];
+  uint32_t pd_peak_pos[2];
+  int32_t pd_peak_cov[2], pd_peak_tail[2];
+  double pd_peak_z[2];
+  bool ladder_open[2][21];
+  uint64_t ladder_count[2][21] = {};
+  struct PdRegion { std::string seq_id; uint32_t start, end; char direction; uint32_t peak_position; int32_t peak_covering, peak_tail; double peak_z; };
+  std::vector<PdRegion> pd_regions;
+  bool pd_bad = false;
+  for (uint32_t oi = 0; oi < ref->n_target_order; oi++) {
+    const uint32_t t = ref->target_order[oi];
     if (prm->deletion_propagation_cutoff[t] < 0.0) continue;
     const uint32_t len = (uint32_t)(ref->target_offset[t + 1] - ref->target_offset[t]);
     const std::string seq_id = target_names[t];
@@ -1888,6 +1912,60 @@ extern "C" int oracle_pair_candidates(const bsq_reference* ref, const bsq_read_s
       mp_metric[b] = 0; mp_total[b] = 0; mp_start[b] = kUndef; mp_max[b] = 0; mp_maxt[b] = 0; mp_red[b] = 0;
       mp_desc_v[b].clear();
     }
+    if (pd_on) {
+      ring_n.assign(ring_w, 0); ring_long.assign(ring_w, 0); ring_short.assign(ring_w, 0); ring_u.assign(ring_w, 0);
+      pd_n = pd_long = pd_short = 0; pd_u = 0; pd_last_b = 0;
+      for (int b = 0; b < 2; b++) {
+        pd_start[b] = kUndef; pd_peak_pos[b] = 0; pd_peak_cov[b] = 0; pd_peak_tail[b] = 0; pd_peak_z[b] = 0.0;
+        for (int k = 0; k < 21; k++) ladder_open[b][k] = false;
+      }
+    }
+    auto check_pd = [&](uint32_t position) {
+      for (uint32_t b = pd_last_b + 1; b <= position; b++) {
+        const int32_t i = (int32_t)(b % (uint32_t)ring_w);
+        pd_n += ring_n[i]; ring_n[i] = 0;
+        pd_long += ring_long[i]; ring_long[i] = 0;
+        pd_short += ring_short[i]; ring_short[i] = 0;
+        pd_u += ring_u[i]; ring_u[i] = 0;
+      }
+      pd_last_b = position;
+      double z = 0.0;
+      if (pd_n > 0) {
+        double mean_offset = ((double)pd_u - (double)pd_n * (double)kS / 2.0) / (double)kS;
+        z = mean_offset * sqrt(12.0 / (double)pd_n);
+        if (pd_n >= 4) {
+          int bin = (int)floor(z * 50) + 40 * 50;
+          if (bin < 0) bin = 0;
+          if (bin >= 4001) bin = 4000;
+          z_hist[bin]++;
+        }
+      }
+      for (int bin = 0; bin < 2; bin++) {
+        const int32_t tail = bin == 0 ? pd_long : pd_short;
+        const bool right_way = bin == 0 ? (z >= prm->pd_z_seed) : (z <= -prm->pd_z_seed);
+        const bool above = (tail >= prm->pair_distance_seed) && right_way && (position <= len);
+        const bool in_sequence = position <= len;
+        const bool tail_ok = (tail >= prm->pair_distance_seed) && in_sequence;
+        const double directed_z = bin == 0 ? z : -z;
+        for (int step = 0; step < 21; step++) {
+          const bool rung = tail_ok && (directed_z >= 1.0 + 0.25 * (double)step);
+          if (rung) ladder_open[bin][step] = true;
+          else if (ladder_open[bin][step]) { ladder_count[bin][step]++; ladder_open[bin][step] = false; }
+        }
+        if (above) {
+          if (pd_start[bin] == kUndef) {
+            pd_start[bin] = position; pd_peak_pos[bin] = position; pd_peak_cov[bin] = pd_n; pd_peak_tail[bin] = tail;
+            pd_peak_z[bin] = z;
+          } else if (fabs(z) > fabs(pd_peak_z[bin])) {
+            pd_peak_pos[bin] = position; pd_peak_cov[bin] = pd_n; pd_peak_tail[bin] = tail; pd_peak_z[bin] = z;
+          }
+        } else if (pd_start[bin] != kUndef) {
+          pd_regions.push_back(PdRegion{seq_id, pd_start[bin], position - 1, bin == 0 ? 'L' : 'S', pd_peak_pos[bin],
+                                        pd_peak_cov[bin], pd_peak_tail[bin], pd_peak_z[bin]});
+          pd_start[bin] = kUndef; pd_peak_pos[bin] = 0; pd_peak_cov[bin] = 0; pd_peak_tail[bin] = 0; pd_peak_z[bin] = 0.0;
+        }
+      }
+    };
     auto check_dp = [&](uint32_t position) {
       for (int bin = 0; bin < 6; bin++) {
         for (Group& g : groups)
@@ -2006,13 +2084,41 @@ extern "C" int oracle_pair_candidates(const bsq_reference* ref, const bsq_read_s
             if (mp_start[bin] != kUndef) { mp_desc_v[bin].push_back(mp_desc(mr)); if (mr.redundant) ++mp_red[bin]; }
           }
         }
+        if (pd_on && (f & BSQ_FLAG_PAIRED) && !(f & BSQ_FLAG_UNMAP) &&
+            !(f & (BSQ_FLAG_SECONDARY | BSQ_FLAG_SUPPLEMENTARY | BSQ_FLAG_MUNMAP)) && rd->mtid[r] == (int32_t)t &&
+            rd->isize[r] > 0 && (ri.rev != ((f & BSQ_FLAG_MREVERSE) != 0)) && rd->x1[r] <= 1 && gi >= 0) {
+          const uint8_t o = prm->pd_orientation[gi];
+          const bool match = (o == BSQ_XP_FR) ? !ri.rev : (o == BSQ_XP_RF) ? ri.rev : true;
+          if (match) {
+            const int32_t d = rd->isize[r];
+            const int32_t lo = (int32_t)end1, hi = rd->mpos[r] + 1 - 1;
+            const uint32_t clen = prm->pd_cdf_len[gi];
+            if ((hi >= lo) && clen && (d <= prm->pd_max_span)) {
+              const int64_t u = ((uint32_t)d < clen) ? prm->pd_cdf[gi][d] : kS;
+              const int64_t lower_tail = (int64_t)(prm->pair_distance_tail_quantile * (double)kS);
+              int bin = -1;
+              if (u >= kS - lower_tail) bin = 0;
+              else if (u <= lower_tail) bin = 1;
+              const int32_t next_b = (int32_t)pd_last_b + 1;
+              if (!((lo >= next_b) && (hi + 1 <= next_b + prm->pd_max_span))) { pd_bad = true; continue; }
+              const int32_t i_lo = lo % ring_w, i_hi = (hi + 1) % ring_w;
+              ring_n[i_lo] += 1; ring_n[i_hi] -= 1;
+              ring_u[i_lo] += u; ring_u[i_hi] -= u;
+              if (bin == 0) { ring_long[i_lo] += 1; ring_long[i_hi] -= 1; }
+              else if (bin == 1) { ring_short[i_lo] += 1; ring_short[i_hi] -= 1; }
+            }
+          }
+        }
       }
       if (dp_on) check_dp(position);
       if (mp_on) check_mp(position);
+      if (pd_on) check_pd(position);
     }
     if (dp_on) check_dp(len + 1);
     if (mp_on) check_mp(len + 1);
+    if (pd_on) check_pd(len + 1);
   }
+  if (pd_bad) { if (errbuf) snprintf(errbuf, errcap, "pair-distance ring write out of range"); return BSQ_ERR_DATA; }
   if (dp_path) {
     std::sort(dp_regions.begin(), dp_regions.end(), [](const DpRegion& a, const DpRegion& b) {
       if (a.seq_id != b.seq_id) return a.seq_id < b.seq_id;
@@ -2026,6 +2132,100 @@ extern "C" int oracle_pair_candidates(const bsq_reference* ref, const bsq_read_s
       o << x.seq_id << "," << x.start << "," << x.end << "," << x.strand << "," << x.orientation << ","
         << (x.end - x.start + 1) << "," << x.max_count << "," << (x.redundant ? 1 : 0) << "," << x.pairs << "\n";
     FILE* f = fopen(dp_path, "w");
+    if (!f) return BSQ_ERR_INVALID;
+    fwrite(o.str().data(), 1, o.str().size(), f);
+    fclose(f);
+  }
+  if (pd_path) {
+    // calibration (fill_pd_summary / pd_z_inflation / pd_fit_region_tail, :2758-2862), the rescan cap
+    // and the file (:2864-2967)
+    double infl = 1.0;
+    if (!z_hist.empty()) {
+      uint64_t total = 0;
+      for (uint64_t h : z_hist) total += h;
+      if (total >= 1000) {
+        uint64_t want_lo = total / 4, want_hi = (total * 3) / 4, run = 0;
+        double q_lo = 0, q_hi = 0;
+        bool hl = false, hh = false;
+        for (size_t i = 0; i < z_hist.size(); i++) {
+          run += z_hist[i];
+          double centre = ((double)i + 0.5) / 50 - 40;
+          if (!hl && run >= want_lo) { q_lo = centre; hl = true; }
+          if (!hh && run >= want_hi) { q_hi = centre; hh = true; break; }
+        }
+        if (hl && hh) { double sd = (q_hi - q_lo) / 1.34898038; if (sd > 1.0) infl = sd; }
+      }
+    }
+    uint64_t ladder[21];
+    for (int k = 0; k < 21; k++) ladder[k] = ladder_count[0][k] + ladder_count[1][k];
+    bool fit_ok = false;
+    double li = 0.0, sigma = 1.0, flo = 0.0, fhi = 0.0;
+    if (pd_on) {
+      uint64_t maxc = 0;
+      for (int k = 0; k < 21; k++) maxc = std::max(maxc, ladder[k]);
+      double sw = 0, swx = 0, swy = 0, swxx = 0, swxy = 0;
+      int rungs = 0;
+      double lo_t = 0, hi_t = 0;
+      for (int k = 0; k < 21; k++) {
+        if (ladder[k] < 20) continue;
+        if (ladder[k] * 3 > maxc) continue;
+        double t = 1.0 + 0.25 * (double)k, x = t * t, y = log((double)ladder[k]), w = (double)ladder[k];
+        sw += w; swx += w * x; swy += w * y; swxx += w * x * x; swxy += w * x * y;
+        if (rungs == 0) lo_t = t;
+        hi_t = t;
+        rungs++;
+      }
+      flo = lo_t; fhi = hi_t;
+      if (rungs >= 3) {
+        double denom = sw * swxx - swx * swx;
+        if (fabs(denom) > 0.0) {
+          double slope = (sw * swxy - swx * swy) / denom, intercept = (swy - slope * swx) / sw;
+          if (slope < 0.0) {
+            double sg = sqrt(-1.0 / (2.0 * slope));
+            if (sg > 0.0 && std::isfinite(sg)) { fit_ok = true; li = intercept; sigma = sg; }
+          }
+        }
+      }
+    }
+    double seed_z = prm->pd_z_seed, capped = seed_z;
+    for (int k = 0; k < 21; k++) {
+      double t = 1.0 + 0.25 * (double)k;
+      if (t < seed_z) continue;
+      capped = t;
+      if (ladder[k] <= 3000) break;
+    }
+    if (capped > seed_z) {
+      std::vector<PdRegion> kept;
+      for (const PdRegion& x : pd_regions) if (fabs(x.peak_z) >= capped) kept.push_back(x);
+      pd_regions.swap(kept);
+      seed_z = capped;
+    }
+    std::sort(pd_regions.begin(), pd_regions.end(), [](const PdRegion& a, const PdRegion& b) {
+      if (a.seq_id != b.seq_id) return a.seq_id < b.seq_id;
+      if (a.start != b.start) return a.start < b.start;
+      return a.direction < b.direction;
+    });
+    const double gap = prm->pd_mean_covering_gap;
+    std::ostringstream o;
+    o << std::fixed << std::setprecision(6);
+    o << "#mean_covering_gap=" << gap << "\n";
+    o << "#n_effective_tests=" << (gap > 0.0 ? (double)prm->total_reference_length / gap : 0.0) << "\n";
+    o << "#seed_z=" << seed_z << "\n";
+    o << "#z_iqr_inflation=" << infl << "\n";
+    o << "#region_tail_fit_ok=" << (fit_ok ? 1 : 0) << "\n";
+    o << "#region_tail_log_intercept=" << (fit_ok ? li : 0.0) << "\n";
+    o << "#region_tail_sigma=" << (fit_ok ? sigma : 1.0) << "\n";
+    o << "#region_tail_fit_lo=" << (pd_on ? flo : 0.0) << "\n";
+    o << "#region_tail_fit_hi=" << (pd_on ? fhi : 0.0) << "\n";
+    o << "#region_ladder=";
+    for (int k = 0; k < 21; k++) { if (k) o << ";"; o << std::setprecision(2) << (1.0 + 0.25 * (double)k) << ":" << ladder[k]; }
+    o << "\n";
+    o << "seq_id,start,end,direction,length,peak_position,peak_covering_count,peak_tail_count,peak_z\n";
+    o << std::setprecision(4);
+    for (const PdRegion& x : pd_regions)
+      o << x.seq_id << "," << x.start << "," << x.end << "," << x.direction << "," << (x.end - x.start + 1) << ","
+        << x.peak_position << "," << x.peak_covering << "," << x.peak_tail << "," << x.peak_z << "\n";
+    FILE* f = fopen(pd_path, "w");
     if (!f) return BSQ_ERR_INVALID;
     fwrite(o.str().data(), 1, o.str().size(), f);
     fclose(f);

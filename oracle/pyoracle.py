@@ -39,7 +39,8 @@ def lib():
         L.oracle_sc_rows.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_sc_free.argtypes = [C.c_void_p]
         L.oracle_pair_candidates.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.POINTER(abi.PairParams),
-                                             C.POINTER(C.c_char_p), C.c_char_p, C.c_char_p, C.c_char_p, C.c_int]
+                                             C.POINTER(C.c_char_p), C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
+                                             C.c_int]
         L.oracle_fit_coverage_distribution.argtypes = [C.POINTER(C.c_uint64), C.c_uint32, C.c_double,
                                                        C.POINTER(abi.CoverageFit)]
         for name, n in (("oracle_nbinom_pmf", 3), ("oracle_nbinom_cdf", 3), ("oracle_lgam", 1), ("oracle_lngamma", 1),
@@ -224,7 +225,7 @@ def special(name, *args):
     return getattr(lib(), "oracle_" + name)(*[float(a) for a in args])
 
 
-def pair_candidates(sample, settings, dp_path, mp_path, deletion_propagation_cutoff=None):
+def pair_candidates(sample, settings, dp_path, mp_path, deletion_propagation_cutoff=None, pd_path=None):
     """The DP / MP candidate-region files of a sample with pair annotations (breseq_gb300.synth.with_pairs);
     settings: a breseq_gb300.api.PairSettings."""
     from breseq_gb300.api import pair_params
@@ -234,6 +235,6 @@ def pair_candidates(sample, settings, dp_path, mp_path, deletion_propagation_cut
     err = C.create_string_buffer(256)
     rc = lib().oracle_pair_candidates(C.byref(view.ref), C.byref(view.reads), C.byref(p), names,
                                       dp_path.encode() if dp_path else None, mp_path.encode() if mp_path else None,
-                                      err, 256)
+                                      pd_path.encode() if pd_path else None, err, 256)
     if rc != 0:
         raise RuntimeError(f"oracle_pair_candidates failed: {err.value.decode()}")

@@ -12,7 +12,7 @@ from tests import bam_cases, compare, samples
 pytestmark = pytest.mark.gpu
 
 FIELDS = ("tid", "pos", "flag", "mapq", "x1", "xl", "xr", "read_file", "read_group", "l_qseq", "n_cigar", "cigar_off",
-          "seq_off", "cigar", "seq", "qual", "xj", "isize", "xp", "qname_off", "qname")
+          "seq_off", "cigar", "seq", "qual", "xj", "isize", "xp", "qname_off", "qname", "mtid", "mpos")
 
 
 @pytest.fixture(scope="module")

@@ -9,7 +9,7 @@ import pytest
 from breseq_gb300 import _lib, synth
 from breseq_gb300.api import PairSettings
 from oracle import pyoracle as po
-from tests.test_pairs import ecoli_pairs, two_groups
+from tests.test_pairs import ecoli_pairs, pd_settings, two_groups
 
 pytestmark = pytest.mark.gpu
 
@@ -24,15 +24,17 @@ def scorer(built_lib):
 
 def gpu_files(sc, sid, s, st, tmp_path, cutoff=None):
     r = sc.pair_candidates(sid, st, cutoff)
-    dp, mp = str(tmp_path / "dp.csv"), str(tmp_path / "mp.csv")
-    sc.write_pair_candidates(r, dp, mp, s.target_names)
-    return [open(dp).read(), open(mp).read()], r
+    f = [str(tmp_path / x) for x in ("dp.csv", "mp.csv", "pd.csv")]
+    pd = st.predict_pair_distance
+    sc.write_pair_candidates(r, f[0], f[1], s.target_names, f[2] if pd else None)
+    return [open(x).read() for x in (f if pd else f[:2])], r
 
 
 def oracle_files(s, st, tmp_path, cutoff=None):
-    dp, mp = str(tmp_path / "odp.csv"), str(tmp_path / "omp.csv")
-    po.pair_candidates(s, st, dp, mp, cutoff)
-    return [open(dp).read(), open(mp).read()]
+    f = [str(tmp_path / x) for x in ("odp.csv", "omp.csv", "opd.csv")]
+    pd = st.predict_pair_distance
+    po.pair_candidates(s, st, f[0], f[1], cutoff, f[2] if pd else None)
+    return [open(x).read() for x in (f if pd else f[:2])]
 
 
 def test_pairs_ecoli(scorer, tmp_path):
@@ -95,3 +97,37 @@ def test_pairs_need_annotations(scorer):
     bad = bad.__class__(**{**bad.__dict__, "qname_off": bad.qname_off[::-1].copy()})
     with pytest.raises(_lib.BsqError):
         scorer.load_sample(bad)
+
+
+def test_pd_ecoli(scorer, tmp_path):
+    s = ecoli_pairs(seed=9, distance_sites=25)
+    st = pd_settings(s)
+    sid = scorer.load_sample(s)
+    got, r = gpu_files(scorer, sid, s, st, tmp_path)
+    scorer.free_sample(sid)
+    assert got == oracle_files(s, st, tmp_path)
+    assert len(r["pd"]) > 2
+
+
+@pytest.mark.parametrize("kw", [dict(pd_z_seed=1.0, pair_distance_seed=1), dict(pd_z_seed=2.6),
+                                dict(pd_orientation=("",)), dict(pd_cdf=(None,))])
+def test_pd_settings(scorer, tmp_path, kw):
+    s = ecoli_pairs(scale=0.02, seed=10, distance_sites=10)
+    st = pd_settings(s, **kw)
+    sid = scorer.load_sample(s)
+    got, _ = gpu_files(scorer, sid, s, st, tmp_path)
+    scorer.free_sample(sid)
+    assert got == oracle_files(s, st, tmp_path)
+
+
+def test_pd_from_bam_two_groups(scorer, tmp_path):
+    import dataclasses
+    s = two_groups(seed=11)
+    s = dataclasses.replace(s, target_order=np.array([0, 2], dtype=np.uint32))
+    s = synth.with_pairs(s, seed=11, distance_sites=6, no_xp_fraction=0.2, background_discordant=0.02)
+    st = pd_settings(s, pd_cdf=(synth.pd_null(s), None), window_width=(300.5, 520.0), pd_z_seed=1.5)
+    cut = np.array([5.0, 5.0, -1.0])
+    sid = scorer.load_bam(synth.bam_bytes(s), s, synth.bam_groups(s))
+    got, _ = gpu_files(scorer, sid, s, st, tmp_path, cut)
+    scorer.free_sample(sid)
+    assert got == oracle_files(s, st, tmp_path, cut)

@@ -27,11 +27,12 @@ def host():
     if not os.path.exists(OUT) or os.path.getmtime(OUT) < max(os.path.getmtime(d) for d in DEPS):
         os.makedirs(os.path.dirname(OUT), exist_ok=True)
         cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
-        subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off", "-I" + cuda_inc]
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-pthread", "-ffp-contract=off",
+                               "-I" + cuda_inc]
                               + SRCS + ["-o", OUT])
     L = C.CDLL(OUT)
     L.host_pair_candidates.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.POINTER(abi.PairParams),
-                                       C.POINTER(C.c_char_p), C.c_char_p, C.c_char_p]
+                                       C.POINTER(C.c_char_p), C.c_char_p, C.c_char_p, C.c_char_p]
     return L
 
 
@@ -39,14 +40,27 @@ def run_both(host, s, st, tmp_path, cutoff=None):
     view = abi.SampleView(s)
     p, keep = pair_params(s, st, cutoff)
     names = (C.c_char_p * len(s.target_names))(*[n.encode() for n in s.target_names])
-    paths = {k: str(tmp_path / f"{k}.csv") for k in ("dp", "mp", "odp", "omp")}
+    paths = {k: str(tmp_path / f"{k}.csv") for k in ("dp", "mp", "pd", "odp", "omp", "opd")}
+    pd = st.predict_pair_distance
     rc = host.host_pair_candidates(C.byref(view.ref), C.byref(view.reads), C.byref(p), names,
-                                   paths["dp"].encode(), paths["mp"].encode())
+                                   paths["dp"].encode(), paths["mp"].encode(), paths["pd"].encode() if pd else None)
     assert rc == 0
-    po.pair_candidates(s, st, paths["odp"], paths["omp"], cutoff)
-    got = [open(paths[k]).read() for k in ("dp", "mp")]
-    exp = [open(paths[k]).read() for k in ("odp", "omp")]
+    po.pair_candidates(s, st, paths["odp"], paths["omp"], cutoff, paths["opd"] if pd else None)
+    keys = ("dp", "mp", "pd") if pd else ("dp", "mp")
+    got = [open(paths[k]).read() for k in keys]
+    exp = [open(paths["o" + k]).read() for k in keys]
     return got, exp
+
+
+def pd_settings(s, **kw):
+    """Pair-distance settings over a sample's null (one DP group per read group)."""
+    G = int(s.read_group.max()) + 1
+    base = dict(dp_group=tuple(range(G)), window_width=(400.0,) * G, r1_prefix=tuple(1 + 2 * g for g in range(G)),
+                r2_prefix=tuple(2 + 2 * g for g in range(G)), predict_missing_pairs=True, predict_pair_distance=True,
+                pd_cdf=(synth.pd_null(s),) * G, pd_orientation=("FR",) * G, pd_max_span=1500, pd_z_seed=2.5,
+                pd_mean_covering_gap=137.5)
+    base.update(kw)
+    return PairSettings(**base)
 
 
 def ecoli_pairs(scale=0.03, seed=5, **kw):
@@ -138,3 +152,33 @@ def test_pairs_hand_worked(host, tmp_path):
     want = ("seq_id,start,end,strand,orientation,length,max_discordant_count,redundant,discordant_pairs\n"
             "t,151,250,F,FR,100,2,0,5:7__6:7__900__101__150;5:8__6:8__-800__151__200;5:9__6:9__-700__201__250\n")
     assert got[0] == want
+
+
+def test_pd_ecoli_matches_oracle(host, tmp_path):
+    s = ecoli_pairs(seed=9, distance_sites=25)
+    got, exp = run_both(host, s, pd_settings(s), tmp_path)
+    assert got == exp
+    lines = got[2].splitlines()
+    assert lines[0].startswith("#mean_covering_gap=137.500000") and len(lines) > 14   # regions found
+
+
+@pytest.mark.parametrize("kw", [dict(pd_z_seed=1.0, pair_distance_seed=1), dict(pd_z_seed=2.6),
+                                dict(pd_orientation=("",)), dict(pd_orientation=("RF",), pd_max_span=600),
+                                dict(pair_distance_tail_quantile=0.25, pair_distance_seed=5),
+                                dict(pd_cdf=(None,)), dict(pd_max_span=0)])
+def test_pd_settings(host, tmp_path, kw):
+    # a low seed seeds many regions (the ladder and tail fit see hundreds), 2.6 is raised to the next
+    # rung, an empty orientation takes any opposite-strand pair, no null or no span disables the scan
+    s = ecoli_pairs(scale=0.02, seed=10, distance_sites=10)
+    got, exp = run_both(host, s, pd_settings(s, **kw), tmp_path)
+    assert got == exp
+
+
+def test_pd_two_groups_and_skips(host, tmp_path):
+    import dataclasses
+    s = two_groups(seed=11)
+    s = dataclasses.replace(s, target_order=np.array([0, 2], dtype=np.uint32))
+    s = synth.with_pairs(s, seed=11, distance_sites=6, no_xp_fraction=0.2, background_discordant=0.02)
+    st = pd_settings(s, pd_cdf=(synth.pd_null(s), None), window_width=(300.5, 520.0), pd_z_seed=1.5)
+    got, exp = run_both(host, s, st, tmp_path, cutoff=np.array([5.0, 5.0, -1.0]))
+    assert got == exp
