@@ -1,7 +1,8 @@
-// Device side of the discordant-pair (DP) and missing-pair (MP) candidate-region scans
-// (bsq_pairs.cu), used by bsq_abi.cu.  The reads are classified in parallel; the few that enter a
-// DP or MP window, and the start columns of the MP window totals, are compacted in BAM order for the
-// host's sliding-window replay (bsq_pairs_host.cpp).
+// Device side of the discordant-pair (DP), missing-pair (MP) and pair-distance (PD) candidate-region
+// scans (bsq_pairs.cu), used by bsq_abi.cu.  The reads are classified in parallel; the few that enter
+// a DP or MP window, and the start columns of the MP window totals, are compacted in BAM order for
+// the host's sliding-window replay (bsq_pairs_host.cpp).  PD's gaps go into difference arrays whose
+// scan evaluates every position on the device; the host assembles the regions and the calibration.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>

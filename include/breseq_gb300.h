@@ -14,6 +14,7 @@
  *   coverage fit (host)     breseq: src/breseq/coverage_distribution.cpp:115-505 (CoverageDistribution::fit)
  *   BAM2COV table           breseq: src/breseq/coverage_output.cpp:190-470
  *   BAM input               breseq: src/breseq/pileup_base.cpp:61-88, 232-235 (htslib decode)
+ *   DP / MP / PD scans      breseq: src/breseq/identify_mutations.cpp:1395-1555, 2358-2967
  *
  * The reference exposes these passes as two C++ free functions that read a BAM/FASTA pair.  Here the
  * host decodes the alignments once into the struct-of-arrays record set `bsq_read_soa`, the library
@@ -567,7 +568,7 @@ int bsq_last_pass_stats(const bsq_ctx* ctx, double* device_ms, uint32_t* kernel_
 /* Bytes the last pass call copied host-to-device and device-to-host (staged inputs, results). */
 int bsq_last_pass_bytes(const bsq_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
 
-/* ---------------------------------------------------------------- discordant / missing-pair scans */
+/* ---------------------------------------------------------------- discordant / missing-pair / pair-distance scans */
 
 /* The discordant-pair (DP) and missing-pair (MP) candidate-region scans that breseq runs inside the
  * identify_mutations pileup (identify_mutations.cpp:1395-1493 enter steps, 2358-2437 and 2439-2522
@@ -575,7 +576,9 @@ int bsq_last_pass_bytes(const bsq_ctx* ctx, uint64_t* h2d_bytes, uint64_t* d2h_b
  * read-file set with a fitted paired-mapping distance, window width median + 2.42 * MAD.  Per bin
  * (focal strand x XP orientation for DP, strand for MP) a region is a maximal run of positions where
  * the reads that started within the window reach the seed; MP also needs the mate-unmapped reads to
- * be at least missing_pair_seed_fraction of all primary mapped reads of that strand in the window. */
+ * be at least missing_pair_seed_fraction of all primary mapped reads of that strand in the window.
+ * PD: per position, the rank-sum z of the distance quantiles of the concordant pairs whose
+ * unsequenced gap covers it, and the count of those in the long or short tail. */
 typedef struct bsq_pair_params {
     uint32_t        n_read_groups;       /* entries of dp_group (the sample's read-group indices) */
     const int32_t*  dp_group;            /* per read group: its DP group, -1 when none */
