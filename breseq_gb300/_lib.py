@@ -97,6 +97,10 @@ def load():
                                        P(C.c_uint32)]
     L.bsq_write_coverage_region.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, C.c_uint32, C.c_uint32,
                                             C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_double)]
+    L.bsq_coverage_columns_rg.argtypes = [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32,
+                                          P(abi.CovColumns), P(C.c_uint32)]
+    L.bsq_write_coverage_region_rg.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, C.c_uint32, C.c_uint32,
+                                               C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_double), C.c_uint32]
     L.bsq_bam_open.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, P(C.c_void_p)]
     L.bsq_bam_close.argtypes = [C.c_void_p]
     L.bsq_bam_close.restype = None
@@ -144,4 +148,4 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_fit_negative_binomial", "bsq_nbinom_pmf", "bsq_nbinom_cdf", "bsq_nbinom_quantile",
             "bsq_bam_name_bytes", "bsq_pair_candidates", "bsq_pair_result_copy", "bsq_write_dp_candidate_regions",
             "bsq_write_mp_candidate_regions", "bsq_pd_result",
-            "bsq_write_pd_candidate_regions")
+            "bsq_write_pd_candidate_regions", "bsq_coverage_columns_rg", "bsq_write_coverage_region_rg")

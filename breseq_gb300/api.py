@@ -372,23 +372,29 @@ class Scorer:
             return bam.load(reference_sample)
 
     # ------------------------------------------------------------------ BAM2COV coverage table
-    def coverage_columns(self, sid: int, tid: int, start: int, end: int) -> dict:
+    def coverage_columns(self, sid: int, tid: int, start: int, end: int, read_group: int = -1) -> dict:
         """Per-position coverage of positions start..end (1-based) of target tid as `breseq BAM2COV`
-        tabulates it, and the pileup's last column ("last")."""
+        tabulates it (of one read group's records when read_group >= 0), and the pileup's last column
+        ("last")."""
         arrs, st = abi.cov_columns(end - start + 1)
         last = C.c_uint32()
-        self._check(self.L.bsq_coverage_columns(self.ctx, sid, tid, start, end, C.byref(st), C.byref(last)))
+        self._check(self.L.bsq_coverage_columns_rg(self.ctx, sid, tid, start, end, read_group, C.byref(st),
+                                                   C.byref(last)))
         arrs["last"] = last.value
         return arrs
 
     def write_coverage_region(self, sid: int, path: str, tid: int, start: int, end: int, resolution: int = 600,
-                              total_only: bool = False, csv: bool = False, reference_average=None):
-        """`breseq BAM2COV --format TSV|CSV -r seq:start-end --resolution N` into path."""
+                              total_only: bool = False, csv: bool = False, reference_average=None,
+                              per_read_group: bool = False, n_read_groups: int | None = None):
+        """`breseq BAM2COV --format TSV|CSV -r seq:start-end --resolution N [--per-read-group]` into path;
+        n_read_groups: the BAM header's @RG count (default: the sample's highest read group + 1)."""
         s = self.sample(sid)
-        flags = (1 if total_only else 0) | (2 if csv else 0)
+        flags = (1 if total_only else 0) | (2 if csv else 0) | (4 if per_read_group else 0)
         avg = C.byref(C.c_double(reference_average)) if reference_average is not None else None
-        self._check(self.L.bsq_write_coverage_region(self.ctx, sid, path.encode(), s.target_names[tid].encode(), tid,
-                                                     start, end, resolution, flags, avg))
+        if n_read_groups is None:
+            n_read_groups = int(np.max(s.read_group)) + 1 if len(s.read_group) else 1
+        self._check(self.L.bsq_write_coverage_region_rg(self.ctx, sid, path.encode(), s.target_names[tid].encode(), tid,
+                                                        start, end, resolution, flags, avg, n_read_groups))
 
     # ------------------------------------------------------------------ launch shapes
     def tuning(self) -> dict:

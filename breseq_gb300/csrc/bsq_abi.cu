@@ -1401,7 +1401,7 @@ int bsq_pair_result_copy(bsq_ctx* ctx, bsq_pair_region* dp, uint64_t n_dp, bsq_p
 // position) come back in one pinned buffer with the reference characters: [6][m] u32 counts |
 // [2][m] f64 weights | stat | the target's reference characters up to end_1.
 static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start, uint32_t end,
-                           uint32_t first, uint32_t step, host::CoverageRegion& out) {
+                           uint32_t first, uint32_t step, host::CoverageRegion& out, int32_t rg_only = -1) {
   SampleDev* s = find_sample(ctx, sample_id);
   if (!s) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
   if (tid >= s->n_targets) return fail(ctx, BSQ_ERR_INVALID, "target index out of range");
@@ -1417,6 +1417,8 @@ static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32
   A.cigar = s->cigar.as<uint32_t>();
   A.x1 = s->x1.as<uint32_t>();
   A.rstart = s->rstart.as<uint32_t>();
+  A.rg = s->rg.as<uint16_t>();
+  A.rg_only = rg_only;
   A.n_reads = s->n_reads;
   A.t0 = s->tpoff[tid];
   A.c0 = A.t0 + start - 1;
@@ -1483,9 +1485,14 @@ static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32
 
 int bsq_coverage_columns(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start_1, uint32_t end_1,
                          bsq_cov_columns* out, uint32_t* last_column_1) {
+  return bsq_coverage_columns_rg(ctx, sample_id, tid, start_1, end_1, -1, out, last_column_1);
+}
+
+int bsq_coverage_columns_rg(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start_1, uint32_t end_1,
+                            int32_t read_group, bsq_cov_columns* out, uint32_t* last_column_1) {
   if (!ctx || !out) return fail(ctx, BSQ_ERR_INVALID, "null argument");
   host::CoverageRegion R;
-  const int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, start_1, 1, R);
+  const int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, start_1, 1, R, read_group < 0 ? -1 : read_group);
   if (rc != BSQ_OK) return rc;
   uint32_t* const u32[6] = {out->unique_top, out->unique_bot, out->raw_redundant_top, out->raw_redundant_bot,
                             out->unique_top_begin, out->unique_bot_begin};
@@ -1500,15 +1507,36 @@ int bsq_coverage_columns(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t
 int bsq_write_coverage_region(bsq_ctx* ctx, int32_t sample_id, const char* path, const char* seq_id, uint32_t tid,
                               uint32_t start_1, uint32_t end_1, uint32_t resolution, uint32_t flags,
                               const double* reference_average) {
+  return bsq_write_coverage_region_rg(ctx, sample_id, path, seq_id, tid, start_1, end_1, resolution,
+                                      flags & ~(uint32_t)BSQ_COV_PER_READ_GROUP, reference_average, 0);
+}
+
+int bsq_write_coverage_region_rg(bsq_ctx* ctx, int32_t sample_id, const char* path, const char* seq_id, uint32_t tid,
+                                 uint32_t start_1, uint32_t end_1, uint32_t resolution, uint32_t flags,
+                                 const double* reference_average, uint32_t n_read_groups) {
   if (!ctx || !path) return fail(ctx, BSQ_ERR_INVALID, "null argument");
   if (start_1 < 1 || start_1 > end_1) return fail(ctx, BSQ_ERR_INVALID, "region outside the target");
+  if (n_read_groups > 0xFFFF) return fail(ctx, BSQ_ERR_INVALID, "more read groups than a record can name");
   // only the positions the table can show a count for come back: the handled ones
   const uint32_t ds = host::coverage_downsample(start_1, end_1, resolution);
+  const uint32_t first = host::coverage_first_handled(start_1, ds);
   host::CoverageRegion R;
-  const int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, host::coverage_first_handled(start_1, ds), ds, R);
+  int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, first, ds, R);
   if (rc != BSQ_OK) return rc;
+  R.own();
+  // --per-read-group: the same columns over each group's records (num_read_group_columns() =
+  // max(read groups, 1), coverage_output.h:143-152)
+  std::vector<host::CoverageRegion> per_rg;
+  if (flags & BSQ_COV_PER_READ_GROUP) {
+    per_rg.resize(std::max<uint32_t>(n_read_groups, 1));
+    for (uint32_t g = 0; g < per_rg.size(); g++) {
+      rc = coverage_region(ctx, sample_id, tid, start_1, end_1, first, ds, per_rg[g], (int32_t)g);
+      if (rc != BSQ_OK) return rc;
+      per_rg[g].own();
+    }
+  }
   (void)seq_id;   // the table has no seq_id column; the name is part of the caller's file name
-  if (!host::write_coverage_region(path, R, resolution, flags, reference_average))
+  if (!host::write_coverage_region(path, R, resolution, flags, reference_average, per_rg))
     return fail(ctx, BSQ_ERR_INVALID, std::string("cannot write ") + path);
   return BSQ_OK;
 }

@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(256) ct_reads_kernel(const CovTabArgs A) {
     if (rd.flags & kFiltered) continue;                 // htslib's default pileup mask
     if (rd.end <= A.c0) continue;                       // ends before the region: not fetched
     if (rd.flags & kBadCigar) { atomicOr(A.stat + 2, kErrCigar); continue; }
+    if (A.rg_only >= 0 && (int32_t)__ldg(A.rg + r) != A.rg_only) continue;   // another read group's record
     last = max(last, rd.end - A.t0);                    // last column (1-based) of the pileup
     span = max(span, rd.end - rd.start);
     const int rev = (rd.flags & kRev) ? 1 : 0;
@@ -242,7 +243,9 @@ __global__ void __launch_bounds__(256) ct_redundant_kernel(const CovTabArgs A) {
           end = rd.end;
           coff = rd.cigar_off;
           fl_nc = rd.flags | ((uint32_t)rd.n_cigar << 8);
-          if (redundancy == 1 || (rd.flags & (kFiltered | kBadCigar))) end = 0;   // never covers
+          if (redundancy == 1 || (rd.flags & (kFiltered | kBadCigar)) ||
+              (A.rg_only >= 0 && (int32_t)__ldg(A.rg + r) != A.rg_only))
+            end = 0;   // never covers
           else w = 1.0 / redundancy;
         }
         const uint32_t cnt = min(32u, hi - base);

@@ -35,6 +35,8 @@ struct CovTabArgs {
   double* red;                 // [2][n]
   uint32_t* stat;              // [0] last column (1-based), [1] longest span, [2] error word,
                                // [3] [4] the records of the target that start before the region ends
+  const uint16_t* rg;          // read group per record
+  int32_t rg_only;             // >= 0: only this read group's records (--per-read-group columns)
 };
 
 // Read pass, scan and redundant weights.  counts[4..5], diff and stat must be zeroed first.

@@ -62,6 +62,18 @@ struct CoverageRegion {
   const char* ref;
   uint32_t start, end, last;
   uint32_t first, step, m;
+  // own(): copies the arrays out of the staging buffer the next call reuses
+  std::vector<uint32_t> own_counts;
+  std::vector<double> own_red;
+  std::string own_ref;
+  void own() {
+    own_counts.assign(counts, counts + (size_t)6 * m);
+    own_red.assign(red, red + (size_t)2 * m);
+    own_ref.assign(ref, end);
+    counts = own_counts.data();
+    red = own_red.data();
+    ref = own_ref.data();
+  }
 };
 // The table's downsampling for a region and --resolution (coverage_output.cpp:203-209) and the first
 // position pileup_base::handle_position keeps, (position + start) % downsample == 0
@@ -71,8 +83,9 @@ uint32_t coverage_first_handled(uint32_t start, uint32_t downsample);
 // coverage_output::table (src/breseq/coverage_output.cpp:190-284) with the rows the pileup driver
 // produces for the region (pileup_base.cpp:130-133, 141-210, 308-355).  False if the file cannot be
 // written.
+// per_rg: with BSQ_COV_PER_READ_GROUP, each read group's columns at the same positions.
 bool write_coverage_region(const char* path, const CoverageRegion& R, uint32_t resolution, uint32_t flags,
-                           const double* reference_average);
+                           const double* reference_average, const std::vector<CoverageRegion>& per_rg);
 
 // Soft-clipping rows in the reference's order (direction -1 then +1, targets in seq_id order,
 // positions ascending; soft_clipping.cpp:500-545) and the genome-wide totals and dispersion fit

@@ -286,7 +286,7 @@ uint32_t coverage_first_handled(uint32_t start, uint32_t downsample) {
 }
 
 bool write_coverage_region(const char* path, const CoverageRegion& R, uint32_t resolution, uint32_t flags,
-                           const double* reference_average) {
+                           const double* reference_average, const std::vector<CoverageRegion>& per_rg) {
   const bool total_only = flags & BSQ_COV_TOTAL_ONLY;
   const char* d = (flags & BSQ_COV_CSV) ? "," : "\t";
   const uint32_t downsample = coverage_downsample(R.start, R.end, resolution);
@@ -300,27 +300,50 @@ bool write_coverage_region(const char* path, const CoverageRegion& R, uint32_t r
                                  "raw_redundant_top_cov", "raw_redundant_bot_cov", "unique_top_begin", "unique_bot_begin"};
   static const char* kTotal[3] = {"unique_cov", "redundant_cov", "total_cov"};
   const int ncols = total_only ? 3 : 8;
+  const bool by_rg = (flags & BSQ_COV_PER_READ_GROUP) != 0;
+  const size_t n_rg = by_rg ? per_rg.size() : 0;
   for (int c = 0; c < ncols; c++) out << d << (total_only ? kTotal[c] : kFull[c]);
+  // per read group, after the aggregate columns, prefixed "RG-<g>_" (coverage_output.cpp:236-247)
+  for (size_t g = 0; g < n_rg; g++)
+    for (int c = 0; c < ncols; c++) out << d << "RG-" << g << "_" << (total_only ? kTotal[c] : kFull[c]);
   out << "\n";
   double sum_unique = 0, sum_repeat = 0, sum_all = 0;
+  std::vector<double> rg_unique(n_rg, 0.0), rg_repeat(n_rg, 0.0), rg_all(n_rg, 0.0);
   uint32_t rows = 0;
-  // a row for position p (coverage_output.cpp:436-451): zero coverage outside the region's columns
-  auto row = [&](uint32_t p) {
-    uint32_t c[6] = {0, 0, 0, 0, 0, 0};
-    double r0 = 0, r1 = 0;
-    if (p >= R.first && p <= R.end && (p - R.first) % R.step == 0) {
-      const uint32_t i = (p - R.first) / R.step;
-      for (int q = 0; q < 6; q++) c[q] = R.counts[(size_t)q * R.m + i];
-      r0 = R.red[i];
-      r1 = R.red[(size_t)R.m + i];
+  // the columns of one region at position p: zero coverage outside its columns
+  auto cells = [&](const CoverageRegion& X, uint32_t p, uint32_t (&c)[6], double& r0, double& r1) {
+    for (int q = 0; q < 6; q++) c[q] = 0;
+    r0 = r1 = 0;
+    if (p >= X.first && p <= X.end && (p - X.first) % X.step == 0) {
+      const uint32_t i = (p - X.first) / X.step;
+      for (int q = 0; q < 6; q++) c[q] = X.counts[(size_t)q * X.m + i];
+      r0 = X.red[i];
+      r1 = X.red[(size_t)X.m + i];
     }
+  };
+  auto print = [&](const uint32_t (&c)[6], double r0, double r1) {
+    if (total_only) out << (c[0] + c[1]) << d << fmt_default(r0 + r1) << d << fmt_default(c[0] + c[1] + r0 + r1);
+    else out << c[0] << d << c[1] << d << fmt_default(r0) << d << fmt_default(r1) << d << c[2] << d << c[3] << d << c[4] << d << c[5];
+  };
+  // a row for position p (coverage_output.cpp:436-500)
+  auto row = [&](uint32_t p) {
+    uint32_t c[6];
+    double r0, r1;
+    cells(R, p, c, r0, r1);
     rows++;
     sum_unique += c[0] + c[1];
     sum_repeat += r0 + r1;
     sum_all += c[0] + c[1] + r0 + r1;
     out << p << d << R.ref[p - 1] << d;
-    if (total_only) out << (c[0] + c[1]) << d << fmt_default(r0 + r1) << d << fmt_default(c[0] + c[1] + r0 + r1);
-    else out << c[0] << d << c[1] << d << fmt_default(r0) << d << fmt_default(r1) << d << c[2] << d << c[3] << d << c[4] << d << c[5];
+    print(c, r0, r1);
+    for (size_t g = 0; g < n_rg; g++) {
+      cells(per_rg[g], p, c, r0, r1);
+      out << d;
+      print(c, r0, r1);
+      rg_unique[g] += c[0] + c[1];
+      rg_repeat[g] += r0 + r1;
+      rg_all[g] += c[0] + c[1] + r0 + r1;
+    }
     out << "\n";
   };
   // Up to the pileup's last column the driver moves its cursor through every position and the
@@ -334,7 +357,7 @@ bool write_coverage_region(const char* path, const CoverageRegion& R, uint32_t r
   for (; q <= R.end; q += downsample) {
     for (uint32_t i = cursor + 1; i < q; i++) {
       out << i << d << R.ref[i - 1];
-      for (int c = 0; c < ncols; c++) out << d << 0;
+      for (size_t c = 0; c < (size_t)ncols * (1 + n_rg); c++) out << d << 0;
       out << "\n";
       rows++;
     }
@@ -346,6 +369,11 @@ bool write_coverage_region(const char* path, const CoverageRegion& R, uint32_t r
   out << "#" << d << "region_repeat_average_cov" << d << fmt_default(sum_repeat / rows) << "\n";
   out << "#" << d << "region_average_cov" << d << fmt_default(sum_all / rows) << "\n";
   out << "#" << d << "number_of_positions" << d << rows << "\n";
+  for (size_t g = 0; g < n_rg; g++) {
+    out << "#" << d << "RG-" << g << "_region_unique_average_cov" << d << fmt_default(rg_unique[g] / rows) << "\n";
+    out << "#" << d << "RG-" << g << "_region_repeat_average_cov" << d << fmt_default(rg_repeat[g] / rows) << "\n";
+    out << "#" << d << "RG-" << g << "_region_average_cov" << d << fmt_default(rg_all[g] / rows) << "\n";
+  }
   return (bool)out;
 }
 

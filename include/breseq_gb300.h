@@ -534,6 +534,7 @@ int bsq_coverage_columns(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t
 
 #define BSQ_COV_TOTAL_ONLY  1   /* --total-only: unique_cov, redundant_cov, total_cov */
 #define BSQ_COV_CSV         2   /* --format CSV (comma-separated) instead of TSV       */
+#define BSQ_COV_PER_READ_GROUP 4   /* --per-read-group (bsq_write_coverage_region_rg)  */
 /* coverage_output::table (coverage_output.cpp:190-284) for the region seq_id:start_1-end_1 with
  * --resolution (0 = every position), including the pileup driver's row selection
  * (pileup_base.cpp:130-133, 141-210, 308-355).  reference_average (may be NULL) adds the
@@ -541,6 +542,16 @@ int bsq_coverage_columns(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t
 int bsq_write_coverage_region(bsq_ctx* ctx, int32_t sample_id, const char* path, const char* seq_id, uint32_t tid,
                               uint32_t start_1, uint32_t end_1, uint32_t resolution, uint32_t flags,
                               const double* reference_average);
+/* The same with BSQ_COV_PER_READ_GROUP honoured: after the aggregate columns, the columns of each read
+ * group 0 .. max(n_read_groups, 1) - 1 prefixed "RG-<g>_" (the header's @RG count; a record's group is
+ * its read_group), and per group the three region averages after number_of_positions
+ * (coverage_output.cpp:236-247, 270-278, 364-500). */
+int bsq_write_coverage_region_rg(bsq_ctx* ctx, int32_t sample_id, const char* path, const char* seq_id, uint32_t tid,
+                                 uint32_t start_1, uint32_t end_1, uint32_t resolution, uint32_t flags,
+                                 const double* reference_average, uint32_t n_read_groups);
+/* The columns of one read group's records (read_group < 0: all records, as bsq_coverage_columns). */
+int bsq_coverage_columns_rg(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start_1, uint32_t end_1,
+                            int32_t read_group, bsq_cov_columns* out, uint32_t* last_column_1);
 
 /* Launch shape of the passes.  None of the knobs changes a result: every count is an integer sum
  * and every column and candidate is scored by one warp whatever the grid. */

@@ -1269,13 +1269,16 @@ namespace {
 
 struct CovCol { uint32_t u[2] = {0, 0}, raw[2] = {0, 0}, beg[2] = {0, 0}; double red[2] = {0.0, 0.0}; };
 
-int cov_columns(Data& d, uint32_t t, uint32_t start, uint32_t end, std::vector<CovCol>& cols, uint32_t& last) {
+int cov_columns(Data& d, uint32_t t, uint32_t start, uint32_t end, std::vector<CovCol>& cols, uint32_t& last,
+                int32_t rg_only = -1) {
   const bsq_read_soa* rd = d.rd;
   cols.assign(end - start + 1, CovCol());
   // the pileup column entries in BAM order: deletions skipped, redundancy from X1
   walk_columns(d, t, (int64_t)start - 1, (int64_t)end, [&](int64_t c, const std::vector<uint64_t>& active) {
     CovCol& x = cols[c - ((int64_t)start - 1)];
     for (uint64_t r : active) {
+      // --per-read-group: the entries of one read group (read_group_index, coverage_output.cpp:383)
+      if (rg_only >= 0 && (int32_t)rd->read_group[r] != rg_only) continue;
       Pile e;
       if (!resolve(rd, r, c, e) || e.is_del) continue;
       const int rev = d.info[r].rev ? 1 : 0;
@@ -1331,10 +1334,10 @@ extern "C" int oracle_coverage_columns(const bsq_reference* ref, const bsq_read_
   return BSQ_OK;
 }
 
-extern "C" int oracle_write_coverage_region(const bsq_reference* ref, const bsq_read_soa* rd, const char* path,
-                                            const char* seq_id, uint32_t tid, uint32_t start, uint32_t end,
-                                            uint32_t resolution, uint32_t flags, const double* ref_average,
-                                            char* errbuf, int errcap) {
+extern "C" int oracle_write_coverage_region_rg(const bsq_reference* ref, const bsq_read_soa* rd, const char* path,
+                                               const char* seq_id, uint32_t tid, uint32_t start, uint32_t end,
+                                               uint32_t resolution, uint32_t flags, const double* ref_average,
+                                               uint32_t n_read_groups, char* errbuf, int errcap) {
   Data d; d.ref = ref; d.rd = rd;
   int rc = prepare(d);
   if (rc) { if (errbuf) snprintf(errbuf, errcap, "%s", d.err.c_str()); return rc; }
@@ -1342,6 +1345,11 @@ extern "C" int oracle_write_coverage_region(const bsq_reference* ref, const bsq_
   std::vector<CovCol> cols;
   uint32_t last = 0;
   cov_columns(d, tid, start, end, cols, last);
+  // --per-read-group: num_read_group_columns() = max(read groups, 1) (coverage_output.h:143-152)
+  const uint32_t n_rg = (flags & BSQ_COV_PER_READ_GROUP) ? std::max<uint32_t>(n_read_groups, 1) : 0;
+  std::vector<std::vector<CovCol>> rg_cols(n_rg);
+  for (uint32_t g = 0; g < n_rg; g++) { uint32_t l2; cov_columns(d, tid, start, end, rg_cols[g], l2, (int32_t)g); }
+  std::vector<double> rg_u(n_rg, 0.0), rg_r(n_rg, 0.0), rg_all(n_rg, 0.0);
   const char* refseq = ref->seq + ref->target_offset[tid];
   const bool total_only = flags & BSQ_COV_TOTAL_ONLY;
   const std::string dl = (flags & BSQ_COV_CSV) ? "," : "\t";
@@ -1360,12 +1368,15 @@ extern "C" int oracle_write_coverage_region(const bsq_reference* ref, const bsq_
                            "raw_redundant_top_cov", "raw_redundant_bot_cov", "unique_top_begin", "unique_bot_begin"};
   const char* names3[3] = {"unique_cov", "redundant_cov", "total_cov"};
   for (int c = 0; c < (total_only ? 3 : 8); c++) o << dl << (total_only ? names3[c] : names8[c]);
+  for (uint32_t g = 0; g < n_rg; g++)
+    for (int c = 0; c < (total_only ? 3 : 8); c++)
+      o << dl << "RG-" << g << "_" << (total_only ? names3[c] : names8[c]);
   o << "\n";
   double sum_u = 0, sum_r = 0, sum_all = 0;
   uint32_t n_pos = 0;
   auto zero_row = [&](uint32_t i) {
     o << i << dl << refseq[i - 1];
-    for (int c = 0; c < (total_only ? 3 : 8); c++) o << dl << 0;
+    for (uint32_t c = 0; c < (total_only ? 3u : 8u) * (1 + n_rg); c++) o << dl << 0;
     o << "\n";
     n_pos++;
   };
@@ -1383,6 +1394,19 @@ extern "C" int oracle_write_coverage_region(const bsq_reference* ref, const bsq_
     } else {
       o << x.u[0] << dl << x.u[1] << dl << fmt_double(x.red[0]) << dl << fmt_double(x.red[1]) << dl << x.raw[0] << dl
         << x.raw[1] << dl << x.beg[0] << dl << x.beg[1];
+    }
+    for (uint32_t g = 0; g < n_rg; g++) {
+      CovCol y;
+      if (p >= start && p <= end) y = rg_cols[g][p - start];
+      if (total_only)
+        o << dl << (y.u[0] + y.u[1]) << dl << fmt_double(y.red[0] + y.red[1]) << dl
+          << fmt_double(y.u[0] + y.u[1] + y.red[0] + y.red[1]);
+      else
+        o << dl << y.u[0] << dl << y.u[1] << dl << fmt_double(y.red[0]) << dl << fmt_double(y.red[1]) << dl << y.raw[0]
+          << dl << y.raw[1] << dl << y.beg[0] << dl << y.beg[1];
+      rg_u[g] += y.u[0] + y.u[1];
+      rg_r[g] += y.red[0] + y.red[1];
+      rg_all[g] += y.u[0] + y.u[1] + y.red[0] + y.red[1];
     }
     o << "\n";
   };
@@ -1403,6 +1427,12 @@ extern "C" int oracle_write_coverage_region(const bsq_reference* ref, const bsq_
   o << "#" << dl << "region_repeat_average_cov" << dl << fmt_double(sum_r / n_pos) << "\n";
   o << "#" << dl << "region_average_cov" << dl << fmt_double(sum_all / n_pos) << "\n";
   o << "#" << dl << "number_of_positions" << dl << n_pos << "\n";
+  for (uint32_t g = 0; g < n_rg; g++) {
+    const std::string pre = "RG-" + std::to_string(g) + "_";
+    o << "#" << dl << pre << "region_unique_average_cov" << dl << fmt_double(rg_u[g] / n_pos) << "\n";
+    o << "#" << dl << pre << "region_repeat_average_cov" << dl << fmt_double(rg_r[g] / n_pos) << "\n";
+    o << "#" << dl << pre << "region_average_cov" << dl << fmt_double(rg_all[g] / n_pos) << "\n";
+  }
   FILE* f = fopen(path, "w");
   if (!f) { if (errbuf) snprintf(errbuf, errcap, "cannot write %s", path); return BSQ_ERR_INVALID; }
   const std::string txt = o.str();
@@ -2247,4 +2277,12 @@ extern "C" int oracle_pair_candidates(const bsq_reference* ref, const bsq_read_s
     fclose(f);
   }
   return BSQ_OK;
+}
+
+extern "C" int oracle_write_coverage_region(const bsq_reference* ref, const bsq_read_soa* rd, const char* path,
+                                            const char* seq_id, uint32_t tid, uint32_t start, uint32_t end,
+                                            uint32_t resolution, uint32_t flags, const double* ref_average,
+                                            char* errbuf, int errcap) {
+  return oracle_write_coverage_region_rg(ref, rd, path, seq_id, tid, start, end, resolution,
+                                         flags & ~(uint32_t)BSQ_COV_PER_READ_GROUP, ref_average, 0, errbuf, errcap);
 }

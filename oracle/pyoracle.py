@@ -53,6 +53,10 @@ def lib():
         L.oracle_write_coverage_region.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.c_char_p,
                                                    C.c_char_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                                    C.c_uint32, C.POINTER(C.c_double), C.c_char_p, C.c_int]
+        L.oracle_write_coverage_region_rg.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.c_char_p,
+                                                      C.c_char_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                                      C.c_uint32, C.POINTER(C.c_double), C.c_uint32, C.c_char_p,
+                                                      C.c_int]
         _lib = L
     return _lib
 
@@ -199,14 +203,16 @@ def coverage_columns(sample, tid, start, end):
 
 
 def write_coverage_region(sample, path, tid, start, end, resolution=600, total_only=False, csv=False,
-                          reference_average=None):
+                          reference_average=None, per_read_group=False, n_read_groups=None):
     view = abi.SampleView(sample)
-    flags = (1 if total_only else 0) | (2 if csv else 0)
+    flags = (1 if total_only else 0) | (2 if csv else 0) | (4 if per_read_group else 0)
     avg = C.byref(C.c_double(reference_average)) if reference_average is not None else None
+    if n_read_groups is None:
+        n_read_groups = int(np.max(sample.read_group)) + 1 if len(sample.read_group) else 1
     err = C.create_string_buffer(256)
-    rc = lib().oracle_write_coverage_region(C.byref(view.ref), C.byref(view.reads), path.encode(),
-                                            sample.target_names[tid].encode(), tid, start, end, resolution, flags,
-                                            avg, err, 256)
+    rc = lib().oracle_write_coverage_region_rg(C.byref(view.ref), C.byref(view.reads), path.encode(),
+                                               sample.target_names[tid].encode(), tid, start, end, resolution, flags,
+                                               avg, n_read_groups, err, 256)
     if rc != 0:
         raise OracleError(f"oracle_write_coverage_region failed ({rc}): {err.value.decode()}")
 

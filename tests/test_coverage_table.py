@@ -53,3 +53,31 @@ def test_total_only_csv_and_average(tmp_path):
     assert lines[2].split(",")[2:] == ["8", "0.5", "8.5"]
     assert lines[4] == "#,reference_unique_average_cov,7.25"
     assert lines[-1] == "#,number_of_positions,3"
+
+
+def test_per_read_group_columns_add_up(tmp_path):
+    # the oracle's --per-read-group columns: integer columns of the groups sum to the aggregate, the
+    # redundant weights to within rounding; header and average lines per group
+    from breseq_gb300 import synth
+    cfg = synth.SimConfig(seed=13, target_lengths=(8_000,), n_snps=3, n_indels=1, max_indel=1, repeat_copies=2,
+                          repeat_length=300, read_sets=(synth.ReadFileSet(coverage=20, read_length=101, paired=True),
+                                                        synth.ReadFileSet(coverage=15, read_length=150)))
+    s = synth.simulate(cfg)
+    path = str(tmp_path / "rg.tsv")
+    po.write_coverage_region(s, path, 0, 1, 8_000, resolution=0, per_read_group=True, n_read_groups=3)
+    lines = open(path).read().splitlines()
+    head = lines[0].split("\t")
+    assert head[2:10] == ["unique_top_cov", "unique_bot_cov", "redundant_top_cov", "redundant_bot_cov",
+                          "raw_redundant_top_cov", "raw_redundant_bot_cov", "unique_top_begin", "unique_bot_begin"]
+    assert head[10] == "RG-0_unique_top_cov" and head[-1] == "RG-2_unique_bot_begin" and len(head) == 2 + 8 * 4
+    rows = [x.split("\t") for x in lines[1:] if not x.startswith("#")]
+    for r in rows[::97]:
+        v = [float(x) for x in r[2:]]
+        agg, per = v[:8], [v[8 + 8 * g: 16 + 8 * g] for g in range(3)]
+        for c in (0, 1, 4, 5, 6, 7):
+            assert agg[c] == sum(p[c] for p in per)
+        for c in (2, 3):
+            assert abs(agg[c] - sum(p[c] for p in per)) < 1e-9 * max(1.0, agg[c])
+        assert per[2] == [0.0] * 8     # a group no record names
+    tail = [x for x in lines if x.startswith("#")]
+    assert tail[-9].split("\t")[1] == "RG-0_region_unique_average_cov" and len(tail) == 4 + 9

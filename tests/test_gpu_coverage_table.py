@@ -114,3 +114,48 @@ def test_region_errors(scorer):
                 scorer.coverage_columns(sid, t, a, b)
     finally:
         scorer.free_sample(sid)
+
+
+def two_read_groups():
+    from breseq_gb300 import synth
+    cfg = synth.SimConfig(seed=13, target_lengths=(20_000, 3_000), target_names=("chrA", "chrB"), n_snps=5,
+                          n_indels=2, max_indel=2, repeat_copies=3, repeat_length=400,
+                          read_sets=(synth.ReadFileSet(coverage=30, read_length=101, paired=True),
+                                     synth.ReadFileSet(coverage=20, read_length=150)))
+    return synth.simulate(cfg)
+
+
+RG_TABLES = [dict(resolution=0), dict(resolution=600, total_only=True), dict(resolution=7, csv=True),
+             dict(resolution=0, n_read_groups=4)]
+
+
+@pytest.mark.parametrize("kw", RG_TABLES, ids=[",".join(f"{k}={v}" for k, v in d.items()) for d in RG_TABLES])
+def test_per_read_group_tables(scorer, tmp_path, kw):
+    # --per-read-group: each read group's columns and averages after the aggregate ones; a header with
+    # more groups than the records use prints zero columns for the others
+    s = two_read_groups()
+    sid = scorer.load_sample(s)
+    try:
+        for i, (t, a, b) in enumerate([(0, 1, 20_000), (0, 5_000, 9_000), (1, 1, 3_000)]):
+            pg, po_ = str(tmp_path / f"g{i}.tsv"), str(tmp_path / f"o{i}.tsv")
+            scorer.write_coverage_region(sid, pg, t, a, b, per_read_group=True, **kw)
+            po.write_coverage_region(s, po_, t, a, b, per_read_group=True, **kw)
+            assert open(pg).read() == open(po_).read(), (t, a, b)
+    finally:
+        scorer.free_sample(sid)
+
+
+def test_per_read_group_columns(scorer):
+    s = two_read_groups()
+    sid = scorer.load_sample(s)
+    try:
+        for g in (0, 1):
+            got = scorer.coverage_columns(sid, 0, 1, 20_000, read_group=g)
+            keep = (s.read_group == g) | (s.tid != 0)
+            import dataclasses
+            o = po.coverage_columns(dataclasses.replace(s, flag=np.where(keep, s.flag, s.flag | 0x400).astype(np.uint16)),
+                                    0, 1, 20_000)
+            for k in COLS:
+                assert np.array_equal(got[k], o[k]), (g, k)
+    finally:
+        scorer.free_sample(sid)
