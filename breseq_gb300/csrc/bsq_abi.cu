@@ -1214,8 +1214,8 @@ int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* 
   CK(ctx->pr_sel.alloc(n * 4 + 16, st));
   CK(ctx->pr_evoff.alloc(n * 8 + 16, st));
   if (mp) {
-    CK(ctx->pr_mem.alloc(n * 4 + 16, st));
-    CK(ctx->pr_memoff.alloc(n * 8 + 16, st));
+    CK(ctx->pr_mem.alloc(2 * n * 4 + 16, st));
+    CK(ctx->pr_memoff.alloc(2 * n * 8 + 16, st));
   }
   CK(ctx->pr_tmp.alloc((n / 1024 + 4) * 8 + 64, st));
   CK(ctx->pr_tot.alloc(64, st));
@@ -1237,26 +1237,33 @@ int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* 
   A.code = ctx->pr_code.as<uint8_t>();
   A.group = ctx->pr_group.as<uint8_t>();
   A.sel = ctx->pr_sel.as<uint32_t>();
-  A.mem = mp ? ctx->pr_mem.as<uint32_t>() : nullptr;
+  A.mem0 = mp ? ctx->pr_mem.as<uint32_t>() : nullptr;
+  A.mem1 = mp ? ctx->pr_mem.as<uint32_t>() + n : nullptr;
   uint64_t* tot = ctx->pr_tot.as<uint64_t>();
   CK(record(ctx->evm0, st));
   CK(pair_classify(A, ctx->sms, st));
   CK(record(ctx->evm1, st));
   CK(scan_u32(A.sel, ctx->pr_evoff.as<uint64_t>(), n, ctx->pr_tmp.as<uint64_t>(), tot, st));
-  if (mp) CK(scan_u32(A.mem, ctx->pr_memoff.as<uint64_t>(), n, ctx->pr_tmp.as<uint64_t>(), tot + 1, st));
+  uint64_t* off0 = ctx->pr_memoff.as<uint64_t>();
+  uint64_t* off1 = off0 + n;
+  if (mp) {
+    CK(scan_u32(A.mem0, off0, n, ctx->pr_tmp.as<uint64_t>(), tot + 1, st));
+    CK(scan_u32(A.mem1, off1, n, ctx->pr_tmp.as<uint64_t>(), tot + 2, st));
+  }
   CK(ctx->pin_out.reserve(64));
-  CK(cudaMemcpyAsync(ctx->pin_out.p, tot, 16, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(ctx->pin_out.p, tot, 24, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  uint64_t counts[2];
-  memcpy(counts, ctx->pin_out.p, 16);
-  const uint64_t n_ev = counts[0], n_mem = mp ? counts[1] : 0;
+  uint64_t counts[3];
+  memcpy(counts, ctx->pin_out.p, 24);
+  const uint64_t n_ev = counts[0], n_m0 = mp ? counts[1] : 0, n_m1 = mp ? counts[2] : 0, n_mem = n_m0 + n_m1;
   CK(ctx->pr_ev.alloc(n_ev * sizeof(PairEvent) + 16, st));
   CK(ctx->pr_names.alloc(n_ev * kPairNameSlot + 16, st));
   CK(ctx->pr_mstart.alloc(n_mem * 4 + 16, st));
-  CK(ctx->pr_mkey.alloc(n_mem * 2 + 16, st));
-  CK(pair_scatter(A, ctx->pr_evoff.as<uint64_t>(), mp ? ctx->pr_memoff.as<uint64_t>() : nullptr,
-                  ctx->pr_ev.as<PairEvent>(), ctx->pr_names.as<char>(), ctx->pr_mstart.as<uint32_t>(),
-                  ctx->pr_mkey.as<uint16_t>(), ctx->sms, st));
+  CK(ctx->pr_mkey.alloc(n_mem + 16, st));
+  uint32_t* ms = ctx->pr_mstart.as<uint32_t>();
+  uint8_t* mg = ctx->pr_mkey.as<uint8_t>();
+  CK(pair_scatter(A, ctx->pr_evoff.as<uint64_t>(), mp ? off0 : nullptr, mp ? off1 : nullptr, ctx->pr_ev.as<PairEvent>(),
+                  ctx->pr_names.as<char>(), ms, ms + n_m0, mg, mg + n_m0, ctx->sms, st));
   // pair distance: gaps into difference arrays, every position's statistics, the ladder edges
   bool pd_on = false;
   uint32_t pd_launches = 0;
@@ -1318,7 +1325,7 @@ int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* 
       pd_launches = 5;
     }
   }
-  const uint64_t b_ev = n_ev * sizeof(PairEvent), b_nm = n_ev * kPairNameSlot, b_ms = n_mem * 4, b_mk = n_mem * 2;
+  const uint64_t b_ev = n_ev * sizeof(PairEvent), b_nm = n_ev * kPairNameSlot, b_ms = n_mem * 4, b_mk = n_mem;
   const uint64_t o_nm = align256(b_ev), o_ms = o_nm + align256(b_nm), o_mk = o_ms + align256(b_ms);
   const uint64_t o_pd = align256(o_mk + b_mk), b_pd = 64 + (kPdHistBins + 2 * kPdLadderSteps) * 8;
   CK(ctx->pin_out.reserve(o_pd + b_pd + 64));
@@ -1351,7 +1358,7 @@ int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* 
   CK(cudaStreamSynchronize(st));
   ctx->last_ms = elapsed(ctx->ev0, ctx->ev1);
   ctx->main_ms = elapsed(ctx->evm0, ctx->evm1);   // the classification pass over every read
-  ctx->launches = 1 + 3 + (mp ? 3 : 0) + 1 + pd_launches;
+  ctx->launches = 1 + 3 + (mp ? 6 : 0) + 1 + pd_launches;
   ctx->last_h2d = (uint64_t)NRG * 4;
   ctx->last_d2h = 16 + b_ev + b_nm + b_ms + b_mk + (pd_on ? b_pd + b_above : 0);
   ctx->pd_res = host::PdResult();
@@ -1359,9 +1366,12 @@ int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* 
   in.ev = reinterpret_cast<const PairEvent*>(h);
   in.n_ev = n_ev;
   in.names = reinterpret_cast<const char*>(h + o_nm);
-  in.mem_start = reinterpret_cast<const uint32_t*>(h + o_ms);
-  in.mem_key = reinterpret_cast<const uint16_t*>(h + o_mk);
-  in.n_mem = n_mem;
+  in.mem_start[0] = reinterpret_cast<const uint32_t*>(h + o_ms);
+  in.mem_start[1] = in.mem_start[0] + n_m0;
+  in.mem_group[0] = reinterpret_cast<const uint8_t*>(h + o_mk);
+  in.mem_group[1] = in.mem_group[0] + n_m0;
+  in.n_mem[0] = n_m0;
+  in.n_mem[1] = n_m1;
   ctx->pair_res = host::PairReplayResult();
   const int rc = host::pair_replay(in, ctx->pair_res);
   if (rc != BSQ_OK) return fail(ctx, rc, "inconsistent pair events");

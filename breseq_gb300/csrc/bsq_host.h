@@ -97,8 +97,8 @@ void sc_assemble(const ScRowDev* rows, const ScOutDev* outs, uint64_t rows_neg, 
                  std::vector<bsq_sc_position>& out, bsq_sc_summary& s);
 
 // Discordant / missing-pair candidate regions (bsq_pairs_host.cpp) from the reads the device
-// compacted: events in BAM order with their names in 256-byte slots, and the MP window-total
-// members' start columns with keys group * 2 + strand.  piled[t]: target t is in the pileup set and
+// compacted: events in BAM order with their names in 256-byte slots, and per strand the MP
+// window-total members' start columns (BAM order, so sorted) with their DP groups.  piled[t]: target t is in the pileup set and
 // its deletion propagation cutoff is not below 0.
 struct PairReplayInput {
   std::vector<uint32_t> tpoff, order;
@@ -111,9 +111,9 @@ struct PairReplayInput {
   const PairEvent* ev = nullptr;
   uint64_t n_ev = 0;
   const char* names = nullptr;
-  const uint32_t* mem_start = nullptr;
-  const uint16_t* mem_key = nullptr;
-  uint64_t n_mem = 0;
+  const uint32_t* mem_start[2] = {nullptr, nullptr};
+  const uint8_t* mem_group[2] = {nullptr, nullptr};
+  uint64_t n_mem[2] = {0, 0};
 };
 struct PairReplayResult {
   std::vector<bsq_pair_region> dp, mp;

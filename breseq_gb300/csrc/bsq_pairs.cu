@@ -27,13 +27,18 @@ __global__ void __launch_bounds__(256) pair_classify_kernel(PairArgs a) {
     a.code[i] = code;
     a.group[i] = grp;
     a.sel[i] = sel;
-    if (a.mem) a.mem[i] = mem;
+    if (a.mem0) {
+      const bool rev = (code & kPairRev) != 0;
+      a.mem0[i] = mem && !rev;
+      a.mem1[i] = mem && rev;
+    }
   }
 }
 
-__global__ void __launch_bounds__(256) pair_scatter_kernel(PairArgs a, const uint64_t* ev_off, const uint64_t* mem_off,
-                                                           PairEvent* ev, char* names, uint32_t* mem_start,
-                                                           uint16_t* mem_key) {
+__global__ void __launch_bounds__(256) pair_scatter_kernel(PairArgs a, const uint64_t* ev_off, const uint64_t* off0,
+                                                           const uint64_t* off1, PairEvent* ev, char* names,
+                                                           uint32_t* start0, uint32_t* start1, uint8_t* group0,
+                                                           uint8_t* group1) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
     if (a.sel[i]) {
       const DevRead r = a.reads[i];
@@ -54,10 +59,13 @@ __global__ void __launch_bounds__(256) pair_scatter_kernel(PairArgs a, const uin
       char* dst = names + e * kPairNameSlot;
       for (uint32_t k = 0; k < len; k++) dst[k] = a.qname[q0 + k];
     }
-    if (a.mem && a.mem[i]) {
-      const uint64_t m = mem_off[i];
-      mem_start[m] = a.reads[i].start;
-      mem_key[m] = (uint16_t)(a.group[i] * 2 + ((a.code[i] & kPairRev) ? 1 : 0));
+    if (a.mem0 && a.mem0[i]) {
+      start0[off0[i]] = a.reads[i].start;
+      group0[off0[i]] = a.group[i];
+    }
+    if (a.mem1 && a.mem1[i]) {
+      start1[off1[i]] = a.reads[i].start;
+      group1[off1[i]] = a.group[i];
     }
   }
 }
@@ -283,9 +291,12 @@ cudaError_t pair_classify(const PairArgs& a, int sms, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t pair_scatter(const PairArgs& a, const uint64_t* ev_off, const uint64_t* mem_off, PairEvent* ev, char* names,
-                         uint32_t* mem_start, uint16_t* mem_key, int sms, cudaStream_t st) {
-  if (a.n) pair_scatter_kernel<<<grid_of(a.n, sms), 256, 0, st>>>(a, ev_off, mem_off, ev, names, mem_start, mem_key);
+cudaError_t pair_scatter(const PairArgs& a, const uint64_t* ev_off, const uint64_t* off0, const uint64_t* off1,
+                         PairEvent* ev, char* names, uint32_t* start0, uint32_t* start1, uint8_t* group0,
+                         uint8_t* group1, int sms, cudaStream_t st) {
+  if (a.n)
+    pair_scatter_kernel<<<grid_of(a.n, sms), 256, 0, st>>>(a, ev_off, off0, off1, ev, names, start0, start1, group0,
+                                                           group1);
   return cudaGetLastError();
 }
 

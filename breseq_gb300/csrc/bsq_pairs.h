@@ -210,13 +210,15 @@ struct PairArgs {
   uint8_t* code;             // [n]
   uint8_t* group;            // [n]
   uint32_t* sel;             // [n] 1: DP or MP-unmapped event
-  uint32_t* mem;             // [n] 1: MP window-total member (mp only)
+  uint32_t* mem0;            // [n] 1: MP window-total member on the forward strand (mp only)
+  uint32_t* mem1;            // [n] the same on the reverse strand
 };
 
 cudaError_t pair_classify(const PairArgs& a, int sms, cudaStream_t st);
-// Writes the events at their scanned offsets (ev_off), names into names[e * kPairNameSlot], and the
-// MP members' start columns and keys group * 2 + strand at mem_off.
-cudaError_t pair_scatter(const PairArgs& a, const uint64_t* ev_off, const uint64_t* mem_off, PairEvent* ev, char* names,
-                         uint32_t* mem_start, uint16_t* mem_key, int sms, cudaStream_t st);
+// Writes the events at their scanned offsets (ev_off), names into names[e * kPairNameSlot], and per
+// strand the MP members' start columns and DP groups at off0 / off1.
+cudaError_t pair_scatter(const PairArgs& a, const uint64_t* ev_off, const uint64_t* off0, const uint64_t* off1,
+                         PairEvent* ev, char* names, uint32_t* start0, uint32_t* start1, uint8_t* group0,
+                         uint8_t* group1, int sms, cudaStream_t st);
 
 }  // namespace bsq

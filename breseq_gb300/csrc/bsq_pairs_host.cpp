@@ -93,11 +93,12 @@ void close_region(Ctx& c, Region& r, uint32_t tid, uint32_t end, char strand, co
   r = Region();
 }
 
-// Start positions of one strand's MP window-total members, per DP group: group g's sorted starts are
-// start[off[g] .. off[g + 1]).
+// Start columns of one strand's MP window-total members on one target, per DP group: group g's sorted
+// columns are col[off[g] .. off[g + 1]).  With one group col points at the device's array itself.
 struct Members {
-  std::vector<uint32_t> start;
+  const uint32_t* col = nullptr;
   std::vector<uint64_t> off;
+  std::vector<uint32_t> own;
 };
 
 // The windows of one bin over one target.  ev: the bin's reads in BAM order.  members: MP only.
@@ -126,8 +127,10 @@ void replay_bin(Ctx& c, uint32_t tid, uint32_t len, const std::vector<Ev>& ev, i
   const char strand = mp ? (bin == 0 ? 'F' : 'R') : (bin / 3 == 0 ? 'F' : 'R');
   const char* orient = mp ? nullptr : kOrient[bin % 3];
 
-  // the window total at p: members with p - ceil(width) < start <= p.  Positions only increase
-  // within a bin, so two cursors per group advance through the sorted starts.
+  // the window total at p: members with p - ceil(width) < start <= p, compared as columns (position
+  // p is column c0 + p - 1).  Positions only increase within a bin, so two cursors per group advance
+  // through the sorted columns.
+  const int64_t c0m1 = (int64_t)in.tpoff[tid] - 1;
   std::vector<uint64_t> lo_i(G), hi_i(G);
   std::vector<int64_t> wceil(G);
   for (uint32_t g = 0; g < G; g++) {
@@ -136,11 +139,12 @@ void replay_bin(Ctx& c, uint32_t tid, uint32_t len, const std::vector<Ev>& ev, i
   }
   auto total_at = [&](uint32_t p) -> int64_t {
     int64_t t = 0;
+    const int64_t cp = c0m1 + p;
     for (uint32_t g = 0; g < G; g++) {
       const uint64_t end = members->off[g + 1];
-      while (hi_i[g] < end && members->start[hi_i[g]] <= p) hi_i[g]++;
-      const int64_t lo = (int64_t)p - wceil[g];
-      while (lo_i[g] < hi_i[g] && (int64_t)members->start[lo_i[g]] <= lo) lo_i[g]++;
+      while (hi_i[g] < end && (int64_t)members->col[hi_i[g]] <= cp) hi_i[g]++;
+      const int64_t lo = cp - wceil[g];
+      while (lo_i[g] < hi_i[g] && (int64_t)members->col[lo_i[g]] <= lo) lo_i[g]++;
       t += (int64_t)(hi_i[g] - lo_i[g]);
     }
     return t;
@@ -220,14 +224,15 @@ int pair_replay(const PairReplayInput& in, PairReplayResult& out) {
       desc[k] = std::to_string(s1) + "__" + std::to_string(e1);
     }
   }
-  for (uint64_t k = 0; k < in.n_mem; k++)
-    if (in.mem_key[k] / 2 >= G) return BSQ_ERR_INVALID;
+  for (int b = 0; b < 2; b++)
+    for (uint64_t k = 0; k < in.n_mem[b]; k++)
+      if (in.mem_group[b][k] >= G) return BSQ_ERR_INVALID;
   if (!G) return BSQ_OK;
   // independent tasks: per piled target, the six DP bins, and each MP strand; merged in this order
   struct Task { uint32_t t; int kind; PairReplayResult res; };
   std::vector<Task> tasks;
-  // MP window-total members of each piled target, split by strand and group with one counting pass
-  // (BAM order keeps each group's starts sorted)
+  // MP window-total members of each piled target and strand; with several DP groups they are split by
+  // group with a counting pass (BAM order keeps each group's columns sorted)
   std::vector<Members> members(in.mp ? 2 * (size_t)in.tpoff.size() : 0);
   for (uint32_t t : in.order) {
     if (!in.piled[t]) continue;
@@ -236,23 +241,23 @@ int pair_replay(const PairReplayInput& in, PairReplayResult& out) {
     tasks.push_back({t, 1, {}});
     tasks.push_back({t, 2, {}});
     const uint32_t c0 = in.tpoff[t], c1 = in.tpoff[t + 1] - 1;
-    const uint32_t* ms = in.mem_start;
-    const uint64_t lo = std::lower_bound(ms, ms + in.n_mem, c0) - ms;
-    const uint64_t hi = std::lower_bound(ms + lo, ms + in.n_mem, c1) - ms;
-    std::vector<uint64_t> cnt(2 * G, 0);
-    for (uint64_t k = lo; k < hi; k++) cnt[in.mem_key[k]]++;
-    std::vector<uint64_t> fill(2 * G);
     for (int b = 0; b < 2; b++) {
+      const uint32_t* ms = in.mem_start[b];
+      const uint64_t lo = std::lower_bound(ms, ms + in.n_mem[b], c0) - ms;
+      const uint64_t hi = std::lower_bound(ms + lo, ms + in.n_mem[b], c1) - ms;
       Members& m = members[2 * t + b];
+      if (G == 1) {
+        m.col = ms;
+        m.off = {lo, hi};
+        continue;
+      }
       m.off.assign(G + 1, 0);
-      for (uint32_t g = 0; g < G; g++) m.off[g + 1] = m.off[g] + cnt[2 * g + b];
-      m.start.resize(m.off[G]);
-      for (uint32_t g = 0; g < G; g++) fill[2 * g + b] = m.off[g];
-    }
-    uint32_t* dst[2] = {members[2 * t].start.data(), members[2 * t + 1].start.data()};
-    for (uint64_t k = lo; k < hi; k++) {
-      const uint32_t key = in.mem_key[k];
-      dst[key & 1][fill[key]++] = ms[k] - c0 + 1;
+      for (uint64_t k = lo; k < hi; k++) m.off[in.mem_group[b][k] + 1]++;
+      for (uint32_t g = 0; g < G; g++) m.off[g + 1] += m.off[g];
+      m.own.resize(m.off[G]);
+      std::vector<uint64_t> fill(m.off.begin(), m.off.end() - 1);
+      for (uint64_t k = lo; k < hi; k++) m.own[fill[in.mem_group[b][k]]++] = ms[k];
+      m.col = m.own.data();
     }
   }
   auto run = [&](Task& task) {

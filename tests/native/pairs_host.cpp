@@ -27,8 +27,8 @@ extern "C" int host_pair_candidates(const bsq_reference* ref, const bsq_read_soa
   std::vector<PairEvent> ev;
   std::vector<uint8_t> codes(rd->n_reads), groups(rd->n_reads);
   std::vector<char> names;
-  std::vector<uint32_t> mem_start;
-  std::vector<uint16_t> mem_key;
+  std::vector<uint32_t> mem_start[2];
+  std::vector<uint8_t> mem_group[2];
   for (uint64_t i = 0; i < rd->n_reads; i++) {
     const uint32_t t = (uint32_t)rd->tid[i];
     uint32_t rlen = 0;
@@ -63,8 +63,9 @@ extern "C" int host_pair_candidates(const bsq_reference* ref, const bsq_read_soa
       memcpy(names.data() + (ev.size() - 1) * kPairNameSlot, rd->qname + rd->qname_off[i], len);
     }
     if (mem) {
-      mem_start.push_back(start);
-      mem_key.push_back((uint16_t)(grp * 2 + ((code & kPairRev) ? 1 : 0)));
+      const int b = (code & kPairRev) ? 1 : 0;
+      mem_start[b].push_back(start);
+      mem_group[b].push_back(grp);
     }
   }
   host::PairReplayInput in;
@@ -82,9 +83,11 @@ extern "C" int host_pair_candidates(const bsq_reference* ref, const bsq_read_soa
   in.ev = ev.data();
   in.n_ev = ev.size();
   in.names = names.data();
-  in.mem_start = mem_start.data();
-  in.mem_key = mem_key.data();
-  in.n_mem = mem_start.size();
+  for (int b = 0; b < 2; b++) {
+    in.mem_start[b] = mem_start[b].data();
+    in.mem_group[b] = mem_group[b].data();
+    in.n_mem[b] = mem_start[b].size();
+  }
   host::PairReplayResult out;
   int rc = host::pair_replay(in, out);
   if (rc != BSQ_OK) return rc;
