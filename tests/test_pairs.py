@@ -182,3 +182,24 @@ def test_pd_two_groups_and_skips(host, tmp_path):
     st = pd_settings(s, pd_cdf=(synth.pd_null(s), None), window_width=(300.5, 520.0), pd_z_seed=1.5)
     got, exp = run_both(host, s, st, tmp_path, cutoff=np.array([5.0, 5.0, -1.0]))
     assert got == exp
+
+
+def test_writers_without_regions_and_bad_arguments(built_lib, tmp_path):
+    # the library's writers need no GPU: an empty result gives the header (and for PD the calibration)
+    from breseq_gb300 import _lib
+    L = _lib.load()
+    names = (C.c_char_p * 1)(b"chr")
+    dp, mp, pd = (str(tmp_path / f) for f in ("dp.csv", "mp.csv", "pd.csv"))
+    assert L.bsq_write_dp_candidate_regions(dp.encode(), names, None, 0, b"") == 0
+    assert L.bsq_write_mp_candidate_regions(mp.encode(), names, None, 0, b"") == 0
+    assert open(dp).read() == ("seq_id,start,end,strand,orientation,length,max_discordant_count,redundant,"
+                               "discordant_pairs\n")
+    assert open(mp).read().startswith("seq_id,start,end,strand,length,max_unpaired_count,max_window_total_count")
+    summ = abi.PdSummary(seed_z_used=2.5, z_iqr_inflation=1.0, region_tail_sigma=1.0)
+    assert L.bsq_write_pd_candidate_regions(pd.encode(), names, None, 0, C.byref(summ)) == 0
+    lines = open(pd).read().splitlines()
+    assert lines[2] == "#seed_z=2.500000" and lines[9].startswith("#region_ladder=1.00:0;1.25:0")
+    assert lines[10].startswith("seq_id,start,end,direction") and len(lines) == 11
+    assert L.bsq_write_pd_candidate_regions(pd.encode(), names, None, 0, None) != 0
+    regs = (abi.PairRegion * 1)()
+    assert L.bsq_write_dp_candidate_regions(dp.encode(), None, regs, 1, b"") != 0
