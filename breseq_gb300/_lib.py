@@ -117,6 +117,14 @@ def load():
     L.bsq_pd_result.argtypes = [C.c_void_p, P(C.c_uint64), P(abi.PdRegion), C.c_uint64, P(abi.PdSummary)]
     L.bsq_write_pd_candidate_regions.argtypes = [C.c_char_p, P(C.c_char_p), P(abi.PdRegion), C.c_uint64,
                                                  P(abi.PdSummary)]
+    L.bsq_pd_build_null.argtypes = [P(C.c_int32), P(C.c_double), C.c_uint64, C.c_int32, C.c_int32, P(C.c_int64),
+                                    C.c_uint32, P(C.c_uint32), P(C.c_double)]
+    L.bsq_pd_max_span.argtypes = [C.c_int32, P(C.c_double), C.c_uint32]
+    L.bsq_pd_max_span.restype = C.c_int32
+    L.bsq_pd_seed_z.argtypes = [C.c_double, C.c_double, C.c_uint64]
+    L.bsq_pd_seed_z.restype = C.c_double
+    L.bsq_ndtri.argtypes = [C.c_double]
+    L.bsq_ndtri.restype = C.c_double
     for fn in (L.bsq_write_dp_candidate_regions, L.bsq_write_mp_candidate_regions):
         fn.argtypes = [C.c_char_p, P(C.c_char_p), P(abi.PairRegion), C.c_uint64, C.c_char_p]
     L.bsq_fit_coverage_distribution.argtypes = [P(C.c_uint64), C.c_uint32, C.c_double, C.c_int, P(abi.CoverageFit)]
@@ -148,4 +156,5 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_fit_negative_binomial", "bsq_nbinom_pmf", "bsq_nbinom_cdf", "bsq_nbinom_quantile",
             "bsq_bam_name_bytes", "bsq_pair_candidates", "bsq_pair_result_copy", "bsq_write_dp_candidate_regions",
             "bsq_write_mp_candidate_regions", "bsq_pd_result",
-            "bsq_write_pd_candidate_regions", "bsq_coverage_columns_rg", "bsq_write_coverage_region_rg")
+            "bsq_write_pd_candidate_regions", "bsq_coverage_columns_rg", "bsq_write_coverage_region_rg",
+            "bsq_pd_build_null", "bsq_pd_max_span", "bsq_pd_seed_z", "bsq_ndtri")

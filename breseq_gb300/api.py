@@ -66,6 +66,26 @@ class PairSettings:
     total_reference_length: int = 0
 
 
+def pd_null_from_histogram(distance, count, trunc: int, max_distance: int):
+    """bsq_pd_build_null: a read-file set's PD null (mid-CDF in 2^20 fixed point) and its mean covering
+    gap from the rows of its paired-mapping distance histogram; (None, 0.0) when it has no usable weight."""
+    d = np.ascontiguousarray(distance, dtype=np.int32)
+    n = np.ascontiguousarray(count, dtype=np.float64)
+    L = _lib.load()
+    cap = int(max(d.max(initial=0), 0)) + 1
+    out = np.zeros(cap, dtype=np.int64)
+    ln, gap = C.c_uint32(), C.c_double()
+    rc = L.bsq_pd_build_null(abi.ptr(d, C.c_int32), abi.ptr(n, C.c_double), len(d), trunc, max_distance,
+                             abi.ptr(out, C.c_int64), cap, C.byref(ln), C.byref(gap))
+    if rc != 0:
+        raise RuntimeError(f"bsq_pd_build_null failed ({rc})")
+    return (out[: ln.value].copy() if ln.value else None), gap.value
+
+
+def pd_seed_z(pair_distance_seed_z: float, mean_covering_gap: float, total_reference_length: int) -> float:
+    return _lib.load().bsq_pd_seed_z(float(pair_distance_seed_z), float(mean_covering_gap), int(total_reference_length))
+
+
 def pair_params(sample, st: PairSettings, deletion_propagation_cutoff=None):
     """bsq_pair_params for a sample; returns (params, arrays they point into)."""
     T = len(sample.target_offset) - 1

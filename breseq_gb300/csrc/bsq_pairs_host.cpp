@@ -540,3 +540,135 @@ extern "C" int bsq_write_pd_candidate_regions(const char* path, const char* cons
         << "," << r->peak_z << "\n";
   return out ? BSQ_OK : BSQ_ERR_INVALID;
 }
+
+// ------------------------------------------------------------------ pair-distance setup (host)
+namespace {
+
+// Cephes ndtri (S. L. Moshier, Cephes Math Library 2.8; src/breseq/stats.cpp:1747-1791): the inverse
+// of the standard normal CDF, with breseq's coefficients and order of operations.
+const double kNdP0[5] = {-5.99633501014107895267E1, 9.80010754185999661536E1, -5.66762857469070293439E1,
+                         1.39312609387279679503E1, -1.23916583867381258016E0};
+const double kNdQ0[8] = {1.95448858338141759834E0, 4.67627912898881538453E0, 8.63602421390890590575E1,
+                         -2.25462687854119370527E2, 2.00260212380060660359E2, -8.20372256168333339912E1,
+                         1.59056225126211695515E1, -1.18331621121330003142E0};
+const double kNdP1[9] = {4.05544892305962419923E0, 3.15251094599893866154E1, 5.71628192246421288162E1,
+                         4.40805073893200834700E1, 1.46849561928858024014E1, 2.18663306850790267539E0,
+                         -1.40256079171354495875E-1, -3.50424626827848203418E-2, -8.57456785154685413611E-4};
+const double kNdQ1[8] = {1.57799883256466749731E1, 4.53907635128879210584E1, 4.13172038254672030440E1,
+                         1.50425385692907503408E1, 2.50464946208309415979E0, -1.42182922854787788574E-1,
+                         -3.80806407691578277194E-2, -9.33259480895457427372E-4};
+const double kNdP2[9] = {3.23774891776946035970E0, 6.91522889068984211695E0, 3.93881025292474443415E0,
+                         1.33303460815807542389E0, 2.01485389549179081538E-1, 1.23716634817820021358E-2,
+                         3.01581553508235416007E-4, 2.65806974686737550832E-6, 6.23974539184983293730E-9};
+const double kNdQ2[8] = {6.02427039364742014255E0, 3.67983563856160859403E0, 1.37702099489081330271E0,
+                         2.16236993594496635890E-1, 1.34204006088543189037E-2, 3.28014464682127739104E-4,
+                         2.89247864745380683936E-6, 6.79019408009981274425E-9};
+
+double horner(double x, const double* c, int n) {     // c[0] x^n + ... + c[n]
+  double r = c[0];
+  for (int i = 1; i <= n; i++) r = r * x + c[i];
+  return r;
+}
+double horner1(double x, const double* c, int n) {    // x^n + c[0] x^(n-1) + ... + c[n-1]
+  double r = x + c[0];
+  for (int i = 1; i < n; i++) r = r * x + c[i];
+  return r;
+}
+
+double ndtri(double y0) {
+  const double kMaxNum = 1.79769313486231570815E308, kS2Pi = 2.50662827463100050242E0;
+  if (y0 <= 0.0) return -kMaxNum;
+  if (y0 >= 1.0) return kMaxNum;
+  int code = 1;
+  double y = y0;
+  if (y > (1.0 - 0.13533528323661269189)) {   // exp(-2)
+    y = 1.0 - y;
+    code = 0;
+  }
+  if (y > 0.13533528323661269189) {
+    y = y - 0.5;
+    const double y2 = y * y;
+    double x = y + y * (y2 * horner(y2, kNdP0, 4) / horner1(y2, kNdQ0, 8));
+    x = x * kS2Pi;
+    return x;
+  }
+  double x = sqrt(-2.0 * log(y));
+  const double x0 = x - log(x) / x;
+  const double z = 1.0 / x;
+  const double x1 = x < 8.0 ? z * horner(z, kNdP1, 8) / horner1(z, kNdQ1, 8)
+                            : z * horner(z, kNdP2, 8) / horner1(z, kNdQ2, 8);
+  x = x0 - x1;
+  if (code != 0) x = -x;
+  return x;
+}
+
+}  // namespace
+
+extern "C" int bsq_pd_build_null(const int32_t* distance, const double* count, uint64_t n_rows, int32_t trunc,
+                                 int32_t max_distance, int64_t* cdf, uint32_t capacity, uint32_t* cdf_len,
+                                 double* mean_covering_gap) {
+  if ((n_rows && (!distance || !count)) || !cdf_len || !mean_covering_gap) return BSQ_ERR_INVALID;
+  // pd_load_weighted_histogram (src/breseq/pd_evidence.cpp:56-97): each distance weighted by its gap
+  // d - trunc, rows past max_distance (when > 0) and gapless rows dropped; a repeated distance keeps
+  // its last row's weight while the total takes every row
+  std::vector<double> weighted;
+  double total = 0.0;
+  for (uint64_t i = 0; i < n_rows; i++) {
+    const int32_t d = distance[i];
+    const double n = count[i];
+    if ((d < 0) || (n <= 0.0)) continue;
+    if ((max_distance > 0) && (d > max_distance)) continue;
+    const double weight = static_cast<double>(d - trunc);
+    if (weight <= 0.0) continue;
+    if (static_cast<int32_t>(weighted.size()) <= d) weighted.resize((size_t)d + 1, 0.0);
+    weighted[d] = n * weight;
+    total += weighted[d];
+  }
+  *cdf_len = 0;
+  *mean_covering_gap = 0.0;
+  if (total <= 0.0) return BSQ_OK;   // no usable weight: no null, PD skips the group
+  if (weighted.size() > capacity) {
+    *cdf_len = (uint32_t)weighted.size();
+    return BSQ_ERR_SIZE;
+  }
+  // pd_build_cdf (src/breseq/identify_mutations.cpp:112-141): the mid-CDF in 2^20 fixed point and the
+  // mean gap of a covering pair
+  double below = 0.0, gap_sum = 0.0;
+  for (size_t d = 0; d < weighted.size(); d++) {
+    const double mid = (below + 0.5 * weighted[d]) / total;
+    below += weighted[d];
+    gap_sum += weighted[d] * (static_cast<double>(d) - static_cast<double>(trunc));
+    int64_t scaled = static_cast<int64_t>(mid * static_cast<double>(bsq::kPdUScale) + 0.5);
+    if (scaled < 0) scaled = 0;
+    if (scaled > bsq::kPdUScale) scaled = bsq::kPdUScale;
+    cdf[d] = scaled;
+  }
+  *cdf_len = (uint32_t)weighted.size();
+  *mean_covering_gap = gap_sum / total;
+  return BSQ_OK;
+}
+
+extern "C" int32_t bsq_pd_max_span(int32_t pair_distance_maximum_span, const double* distance_cutoff,
+                                   uint32_t n_groups) {
+  // identify_mutations.cpp:928-941: twice the largest paired-mapping distance cutoff, unless given
+  double derived = 0.0;
+  for (uint32_t g = 0; g < n_groups; g++) derived = std::max(derived, 2.0 * distance_cutoff[g]);
+  return pair_distance_maximum_span > 0 ? pair_distance_maximum_span : static_cast<int32_t>(derived + 0.5);
+}
+
+extern "C" double bsq_pd_seed_z(double pair_distance_seed_z, double mean_covering_gap, uint64_t total_reference_length) {
+  // identify_mutations.cpp:979-994: the analytic one-sided threshold with the effective number of
+  // tests (reference length / covering gap), never above 2.5 nor below 1, unless given
+  if (pair_distance_seed_z > 0.0) return pair_distance_seed_z;
+  double alpha_half = 0.005;
+  if ((mean_covering_gap > 0.0) && (total_reference_length > 0))
+    alpha_half *= mean_covering_gap / static_cast<double>(total_reference_length);
+  if (alpha_half > 0.5) alpha_half = 0.5;
+  if (alpha_half < 1e-12) alpha_half = 1e-12;
+  const double analytic_z = ndtri(1.0 - alpha_half);
+  double z = std::min(analytic_z, 2.5);
+  if (z < 1.0) z = 1.0;
+  return z;
+}
+
+extern "C" double bsq_ndtri(double y) { return ndtri(y); }

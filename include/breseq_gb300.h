@@ -679,6 +679,21 @@ int bsq_pair_result_copy(bsq_ctx* ctx, bsq_pair_region* dp, uint64_t n_dp, bsq_p
  * (after its rescan-budget cap, identify_mutations.cpp:2875-2904) and the calibration. */
 int bsq_pd_result(bsq_ctx* ctx, uint64_t* n_regions, bsq_pd_region* regions, uint64_t capacity,
                   bsq_pd_summary* summary);
+/* The PD setup of identify_mutations_pileup (identify_mutations.cpp:920-995), host code:
+ *  - bsq_pd_build_null: one read-file set's null from the rows (distance, count) of its paired-mapping
+ *    distance histogram file, as pd_load_weighted_histogram (pd_evidence.cpp:56-97) weights them and
+ *    pd_build_cdf (identify_mutations.cpp:112-141) scales them; trunc = 2 x the rounded mean read
+ *    length, max_distance = the span when above trunc, else 0.  cdf_len 0: no usable weight (the group
+ *    has no null).  BSQ_ERR_SIZE with *cdf_len = the length needed when capacity is short.
+ *  - bsq_pd_max_span: --pair-distance-maximum-span, or twice the largest distance cutoff;
+ *  - bsq_pd_seed_z: --pair-distance-seed-z, or the analytic threshold over reference length /
+ *    covering gap tests, clamped to [1, 2.5] (Cephes ndtri, stats.cpp:1747-1791). */
+int     bsq_pd_build_null(const int32_t* distance, const double* count, uint64_t n_rows, int32_t trunc,
+                          int32_t max_distance, int64_t* cdf, uint32_t capacity, uint32_t* cdf_len,
+                          double* mean_covering_gap);
+int32_t bsq_pd_max_span(int32_t pair_distance_maximum_span, const double* distance_cutoff, uint32_t n_groups);
+double  bsq_pd_seed_z(double pair_distance_seed_z, double mean_covering_gap, uint64_t total_reference_length);
+double  bsq_ndtri(double y);
 /* pd_candidate_regions.csv (identify_mutations.cpp:2864-2967) */
 int bsq_write_pd_candidate_regions(const char* path, const char* const* target_names, const bsq_pd_region* regions,
                                    uint64_t n, const bsq_pd_summary* summary);

@@ -244,3 +244,96 @@ def pair_candidates(sample, settings, dp_path, mp_path, deletion_propagation_cut
                                       pd_path.encode() if pd_path else None, err, 256)
     if rc != 0:
         raise RuntimeError(f"oracle_pair_candidates failed: {err.value.decode()}")
+
+
+# ----------------------------------------------------------------- pair-distance setup, restated in Python
+# pd_load_weighted_histogram (src/breseq/pd_evidence.cpp:56-97), pd_build_cdf
+# (src/breseq/identify_mutations.cpp:112-141) and Cephes ndtri (src/breseq/stats.cpp:1747-1791); Python
+# floats are IEEE doubles and math.log / math.sqrt are the C library's, so results are bit-identical.
+_ND_P0 = (-5.99633501014107895267E1, 9.80010754185999661536E1, -5.66762857469070293439E1, 1.39312609387279679503E1,
+          -1.23916583867381258016E0)
+_ND_Q0 = (1.95448858338141759834E0, 4.67627912898881538453E0, 8.63602421390890590575E1, -2.25462687854119370527E2,
+          2.00260212380060660359E2, -8.20372256168333339912E1, 1.59056225126211695515E1, -1.18331621121330003142E0)
+_ND_P1 = (4.05544892305962419923E0, 3.15251094599893866154E1, 5.71628192246421288162E1, 4.40805073893200834700E1,
+          1.46849561928858024014E1, 2.18663306850790267539E0, -1.40256079171354495875E-1, -3.50424626827848203418E-2,
+          -8.57456785154685413611E-4)
+_ND_Q1 = (1.57799883256466749731E1, 4.53907635128879210584E1, 4.13172038254672030440E1, 1.50425385692907503408E1,
+          2.50464946208309415979E0, -1.42182922854787788574E-1, -3.80806407691578277194E-2, -9.33259480895457427372E-4)
+_ND_P2 = (3.23774891776946035970E0, 6.91522889068984211695E0, 3.93881025292474443415E0, 1.33303460815807542389E0,
+          2.01485389549179081538E-1, 1.23716634817820021358E-2, 3.01581553508235416007E-4, 2.65806974686737550832E-6,
+          6.23974539184983293730E-9)
+_ND_Q2 = (6.02427039364742014255E0, 3.67983563856160859403E0, 1.37702099489081330271E0, 2.16236993594496635890E-1,
+          1.34204006088543189037E-2, 3.28014464682127739104E-4, 2.89247864745380683936E-6, 6.79019408009981274425E-9)
+
+
+def _polevl(x, c):
+    a = c[0]
+    for v in c[1:]:
+        a = a * x + v
+    return a
+
+
+def _p1evl(x, c):
+    a = x + c[0]
+    for v in c[1:]:
+        a = a * x + v
+    return a
+
+
+def ndtri(y0):
+    import math
+    if y0 <= 0.0:
+        return -1.79769313486231570815E308
+    if y0 >= 1.0:
+        return 1.79769313486231570815E308
+    code, y = 1, y0
+    if y > (1.0 - 0.13533528323661269189):
+        y, code = 1.0 - y, 0
+    if y > 0.13533528323661269189:
+        y = y - 0.5
+        y2 = y * y
+        x = y + y * (y2 * _polevl(y2, _ND_P0) / _p1evl(y2, _ND_Q0))
+        return x * 2.50662827463100050242E0
+    x = math.sqrt(-2.0 * math.log(y))
+    x0 = x - math.log(x) / x
+    z = 1.0 / x
+    x1 = z * _polevl(z, _ND_P1) / _p1evl(z, _ND_Q1) if x < 8.0 else z * _polevl(z, _ND_P2) / _p1evl(z, _ND_Q2)
+    x = x0 - x1
+    return -x if code != 0 else x
+
+
+def pd_build_null(distance, count, trunc, max_distance):
+    weighted, total = [], 0.0
+    for d, n in zip(distance, count):
+        d, n = int(d), float(n)
+        if d < 0 or n <= 0.0:
+            continue
+        if max_distance > 0 and d > max_distance:
+            continue
+        w = float(d - trunc)
+        if w <= 0.0:
+            continue
+        if len(weighted) <= d:
+            weighted += [0.0] * (d + 1 - len(weighted))
+        weighted[d] = n * w
+        total += weighted[d]
+    if total <= 0.0:
+        return None, 0.0
+    cdf, below, gap = [], 0.0, 0.0
+    for d, w in enumerate(weighted):
+        mid = (below + 0.5 * w) / total
+        below += w
+        gap += w * (float(d) - float(trunc))
+        scaled = min(max(int(mid * 1048576.0 + 0.5), 0), 1048576)
+        cdf.append(scaled)
+    return np.array(cdf, dtype=np.int64), gap / total
+
+
+def pd_seed_z(seed_z, gap, total_length):
+    if seed_z > 0.0:
+        return seed_z
+    a = 0.005
+    if gap > 0.0 and total_length > 0:
+        a *= gap / float(total_length)
+    a = min(max(a, 1e-12), 0.5)
+    return max(min(ndtri(1.0 - a), 2.5), 1.0)

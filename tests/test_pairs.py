@@ -203,3 +203,35 @@ def test_writers_without_regions_and_bad_arguments(built_lib, tmp_path):
     assert L.bsq_write_pd_candidate_regions(pd.encode(), names, None, 0, None) != 0
     regs = (abi.PairRegion * 1)()
     assert L.bsq_write_dp_candidate_regions(dp.encode(), None, regs, 1, b"") != 0
+
+
+def test_pd_setup_helpers(built_lib):
+    # the PD null, span and seed z as the pileup constructor derives them, against the Python
+    # restatement bit for bit and ndtri against scipy
+    from breseq_gb300 import _lib
+    from breseq_gb300.api import pd_null_from_histogram, pd_seed_z
+    L = _lib.load()
+    ys = np.concatenate([np.geomspace(1e-300, 0.135, 200), np.linspace(0.13, 0.87, 200), 1 - np.geomspace(1e-16, 0.135, 200)])
+    for y in ys:
+        assert L.bsq_ndtri(float(y)) == po.ndtri(float(y))
+    sp = pytest.importorskip("scipy.special")
+    for y in ys[(ys > 1e-200) & (ys < 1 - 1e-15)]:
+        assert L.bsq_ndtri(float(y)) == pytest.approx(float(sp.ndtri(y)), rel=1e-13, abs=1e-300)
+    rng = np.random.default_rng(4)
+    for _ in range(20):
+        n = int(rng.integers(1, 400))
+        d = rng.integers(-5, 1500, n)
+        c = rng.choice([0.0, 1.0, 3.0, 17.5, 1000.0], n)
+        d[: n // 10] = d[0]                       # repeated distances
+        trunc, maxd = int(rng.integers(0, 400)), int(rng.choice([0, 600, 1200]))
+        got, gap = pd_null_from_histogram(d, c, trunc, maxd)
+        exp, egap = po.pd_build_null(d, c, trunc, maxd)
+        assert (got is None) == (exp is None) and gap == egap
+        if got is not None:
+            assert np.array_equal(got, exp)
+    for args in [(0.0, 137.5, 4_790_000), (3.25, 137.5, 4_790_000), (0.0, 0.0, 0), (0.0, 2e6, 1000),
+                 (0.0, 400.0, 48_502)]:
+        assert pd_seed_z(*args) == po.pd_seed_z(*args)
+    assert pd_seed_z(0.0, 137.5, 4_790_000) == 2.5 and pd_seed_z(0.0, 2e6, 1000) == 1.0
+    cut = (C.c_double * 2)(300.4, 612.25)
+    assert L.bsq_pd_max_span(0, cut, 2) == 1225 and L.bsq_pd_max_span(900, cut, 2) == 900
