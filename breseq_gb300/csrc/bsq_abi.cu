@@ -1244,8 +1244,8 @@ int bsq_pair_candidates(bsq_ctx* ctx, int32_t sample_id, const bsq_pair_params* 
   CK(pair_classify(A, ctx->sms, st));
   CK(record(ctx->evm1, st));
   CK(scan_u32(A.sel, ctx->pr_evoff.as<uint64_t>(), n, ctx->pr_tmp.as<uint64_t>(), tot, st));
-  uint64_t* off0 = ctx->pr_memoff.as<uint64_t>();
-  uint64_t* off1 = off0 + n;
+  uint64_t* off0 = mp ? ctx->pr_memoff.as<uint64_t>() : nullptr;
+  uint64_t* off1 = mp ? off0 + n : nullptr;
   if (mp) {
     CK(scan_u32(A.mem0, off0, n, ctx->pr_tmp.as<uint64_t>(), tot + 1, st));
     CK(scan_u32(A.mem1, off1, n, ctx->pr_tmp.as<uint64_t>(), tot + 2, st));
