@@ -66,10 +66,31 @@ struct Region {
   std::vector<uint64_t> reads;   // indices into the descriptor strings, in region order
 };
 
+// Descriptors are built when a region that lists the read closes: most compacted reads never make one
+// (a read can be listed by more than one region of its bin, so each is kept once built).  A read
+// belongs to one bin, and one task replays a bin, so tasks fill disjoint entries.
+struct Descriptors {
+  const PairReplayInput& in;
+  std::vector<std::string> text;
+  const std::string& get(uint64_t k) {
+    std::string& d = text[k];
+    if (!d.empty()) return d;
+    const PairEvent& e = in.ev[k];
+    const uint32_t t = (uint32_t)(std::upper_bound(in.tpoff.begin(), in.tpoff.end(), e.start) - in.tpoff.begin()) - 1;
+    const uint32_t s1 = e.start - in.tpoff[t] + 1, e1 = e.end - in.tpoff[t];
+    if ((e.code & kPairDpBinMask) != kPairNoBin)
+      d = dp_key(e, in.names + k * kPairNameSlot, in.r1_prefix[e.group], in.r2_prefix[e.group]) + "__" +
+          std::to_string(s1) + "__" + std::to_string(e1);
+    else
+      d = std::to_string(s1) + "__" + std::to_string(e1);
+    return d;
+  }
+};
+
 struct Ctx {
   const PairReplayInput& in;
   PairReplayResult& out;
-  const std::vector<std::string>& desc;   // descriptor of each compacted event
+  Descriptors& desc;
 };
 
 void close_region(Ctx& c, Region& r, uint32_t tid, uint32_t end, char strand, const char* orient, bool mp) {
@@ -86,7 +107,7 @@ void close_region(Ctx& c, Region& r, uint32_t tid, uint32_t end, char strand, co
   x.text_off = c.out.text.size();
   for (size_t k = 0; k < r.reads.size(); k++) {
     if (k) c.out.text += ';';
-    c.out.text += c.desc[r.reads[k]];
+    c.out.text += c.desc.get(r.reads[k]);
   }
   x.text_len = c.out.text.size() - x.text_off;
   (mp ? c.out.mp : c.out.dp).push_back(x);
@@ -210,20 +231,9 @@ void replay_bin(Ctx& c, uint32_t tid, uint32_t len, const std::vector<Ev>& ev, i
 
 int pair_replay(const PairReplayInput& in, PairReplayResult& out) {
   const uint32_t G = (uint32_t)in.window_width.size();
-  // descriptors of every compacted event
-  std::vector<std::string> desc(in.n_ev);
-  for (uint64_t k = 0; k < in.n_ev; k++) {
-    const PairEvent& e = in.ev[k];
-    const uint32_t t = (uint32_t)(std::upper_bound(in.tpoff.begin(), in.tpoff.end(), e.start) - in.tpoff.begin()) - 1;
-    const uint32_t s1 = e.start - in.tpoff[t] + 1, e1 = e.end - in.tpoff[t];
-    if ((e.code & kPairDpBinMask) != kPairNoBin) {
-      if (e.group >= G) return BSQ_ERR_INVALID;
-      desc[k] = dp_key(e, in.names + k * kPairNameSlot, in.r1_prefix[e.group], in.r2_prefix[e.group]) + "__" +
-                std::to_string(s1) + "__" + std::to_string(e1);
-    } else {
-      desc[k] = std::to_string(s1) + "__" + std::to_string(e1);
-    }
-  }
+  for (uint64_t k = 0; k < in.n_ev; k++)
+    if ((in.ev[k].code & kPairDpBinMask) != kPairNoBin && in.ev[k].group >= G) return BSQ_ERR_INVALID;
+  Descriptors desc{in, std::vector<std::string>(in.n_ev)};
   for (int b = 0; b < 2; b++)
     for (uint64_t k = 0; k < in.n_mem[b]; k++)
       if (in.mem_group[b][k] >= G) return BSQ_ERR_INVALID;
