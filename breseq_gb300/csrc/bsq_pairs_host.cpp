@@ -122,6 +122,21 @@ struct Members {
   std::vector<uint32_t> own;
 };
 
+// The first index at or after i (below end) whose column is above v: a galloping search, so a cursor
+// that catches up over a long stretch (between the runs of positions an MP bin evaluates) costs a
+// logarithm rather than a scan.
+inline uint64_t advance_past(const uint32_t* col, uint64_t i, uint64_t end, int64_t v) {
+  if (i >= end || (int64_t)col[i] > v) return i;
+  uint64_t lo = i, step = 1;
+  while (lo + step < end && (int64_t)col[lo + step] <= v) {
+    lo += step;
+    step <<= 1;
+  }
+  const uint64_t hi = std::min(lo + step, end);
+  return (uint64_t)(std::upper_bound(col + lo + 1, col + hi, v,
+                                     [](int64_t x, uint32_t c) { return x < (int64_t)c; }) - col);
+}
+
 // The windows of one bin over one target.  ev: the bin's reads in BAM order.  members: MP only.
 void replay_bin(Ctx& c, uint32_t tid, uint32_t len, const std::vector<Ev>& ev, int bin, bool mp,
                 const Members* members) {
@@ -162,15 +177,26 @@ void replay_bin(Ctx& c, uint32_t tid, uint32_t len, const std::vector<Ev>& ev, i
     int64_t t = 0;
     const int64_t cp = c0m1 + p;
     for (uint32_t g = 0; g < G; g++) {
-      const uint64_t end = members->off[g + 1];
-      while (hi_i[g] < end && (int64_t)members->col[hi_i[g]] <= cp) hi_i[g]++;
-      const int64_t lo = cp - wceil[g];
-      while (lo_i[g] < hi_i[g] && (int64_t)members->col[lo_i[g]] <= lo) lo_i[g]++;
+      hi_i[g] = advance_past(members->col, hi_i[g], members->off[g + 1], cp);
+      lo_i[g] = advance_past(members->col, lo_i[g], hi_i[g], cp - wceil[g]);
       t += (int64_t)(hi_i[g] - lo_i[g]);
     }
     return t;
   };
   // the per-position test and region bookkeeping, after the position's entries and exits
+  // a region opens at p with the reads in the windows as its snapshot
+  auto open_region = [&](uint32_t p, int64_t total) {
+    r.start = p;
+    r.max_count = (uint32_t)metric;
+    r.max_total = (uint32_t)total;
+    r.reads.clear();
+    r.redundant = 0;
+    for (uint32_t g = 0; g < G; g++)
+      for (size_t k : win[g]) {
+        r.reads.push_back(ev[k].idx);
+        if (ev[k].redundant) r.redundant++;
+      }
+  };
   auto check = [&](uint32_t p) {
     bool above;
     int64_t total = 0;
@@ -183,16 +209,7 @@ void replay_bin(Ctx& c, uint32_t tid, uint32_t len, const std::vector<Ev>& ev, i
     }
     if (above) {
       if (r.start == kUndefPos) {
-        r.start = p;
-        r.max_count = (uint32_t)metric;
-        r.max_total = (uint32_t)total;
-        r.reads.clear();
-        r.redundant = 0;
-        for (uint32_t g = 0; g < G; g++)
-          for (size_t k : win[g]) {
-            r.reads.push_back(ev[k].idx);
-            if (ev[k].redundant) r.redundant++;
-          }
+        open_region(p, total);
       } else if ((uint32_t)metric > r.max_count) {
         r.max_count = (uint32_t)metric;
         r.max_total = (uint32_t)total;
@@ -221,9 +238,39 @@ void replay_bin(Ctx& c, uint32_t tid, uint32_t len, const std::vector<Ev>& ev, i
         metric--;
       }
     check(p);
-    // MP: between this position and the next event the count is fixed, but the total is not
-    if (mp && metric >= seed && pi + 1 < pos.size())
-      for (uint32_t q = p + 1; q < pos[pi + 1] && q <= len; q++) check(q);
+    // MP: between this position and the next event the count is fixed (so the region's maximum
+    // cannot move), but the total is not: only the enrichment test can open or close a region
+    if (mp && metric >= seed && pi + 1 < pos.size()) {
+      const uint32_t q_end = std::min<uint32_t>(pos[pi + 1] - 1, len);
+      const double m = (double)metric;
+      // one DP group: the two cursors in registers
+      const bool one = G == 1;
+      const uint32_t* col = one ? members->col : nullptr;
+      uint64_t lo1 = one ? lo_i[0] : 0, hi1 = one ? hi_i[0] : 0;
+      const uint64_t end1 = one ? members->off[1] : 0;
+      const int64_t wc1 = one ? wceil[0] : 0;
+      for (uint32_t q = p + 1; q <= q_end; q++) {
+        int64_t total;
+        if (one) {
+          const int64_t cp = c0m1 + q;
+          hi1 = advance_past(col, hi1, end1, cp);
+          lo1 = advance_past(col, lo1, hi1, cp - wc1);
+          total = (int64_t)(hi1 - lo1);
+        } else {
+          total = total_at(q);
+        }
+        const bool above = (total > 0) && (m >= in.mp_seed_fraction * (double)total);
+        if (above) {
+          if (r.start == kUndefPos) open_region(q, total);
+        } else if (r.start != kUndefPos) {
+          close_region(c, r, tid, q - 1, strand, orient, mp);
+        }
+      }
+      if (one) {
+        lo_i[0] = lo1;
+        hi_i[0] = hi1;
+      }
+    }
   }
 }
 
