@@ -45,3 +45,13 @@ def test_single_group_and_unplaced_order():
     assert r["read_group"].tolist() == [0] * 6 and r["read_file"].tolist() == [5] * 6
     with pytest.raises(bam_reader.BamError):
         bam_reader.read_bam(bam_cases.bam([recs[6]] + recs[:6]))
+
+
+def test_pair_annotations_round_trip():
+    # names, TLEN, RNEXT / PNEXT and XP (FR / RF / FF; none, or another value, reads as 3)
+    s = synth.with_pairs(synth.simulate(synth.config_ecoli(seed=5, scale=0.005)), seed=2, no_xp_fraction=0.3,
+                         distance_sites=3)
+    r = bam_reader.read_bam(synth.bam_bytes(s, level=1), synth.bam_groups(s))["records"]
+    for k in ("isize", "xp", "qname_off", "qname", "mtid", "mpos", "flag"):
+        assert np.array_equal(r[k], getattr(s, k)), k
+    assert set(np.unique(r["xp"])) <= {0, 1, 2, 3} and (r["xp"] == 3).any() and (r["xp"] < 3).any()
