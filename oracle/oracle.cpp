@@ -34,6 +34,13 @@
  *                                               src/breseq/soft_clipping.cpp:98-169, 285-666
  *     (pinned by hand-worked answers and the rules the reference states in its comments; see
  *     tests/test_softclip.py)
+ *   - coverage_output::table / pileup_callback, with --per-read-group
+ *                                               src/breseq/coverage_output.cpp:190-500
+ *   - fit_censored_negative_binomial / fit_coverage_distribution and the Cephes functions they use
+ *                                               src/breseq/coverage_distribution.cpp:115-396, stats.cpp
+ *     (special functions pinned against scipy; see tests/test_coverage_fit.py)
+ *   - the DP / MP / PD candidate-region scans walked position by position, and their writers
+ *                                               src/breseq/identify_mutations.cpp:883-1006, 1395-1555, 2358-2967
  *
  * One deliberate divergence: where the reference would index a read past its end (a deletion that is
  * followed by a single aligned base, error_count.cpp:1073), it aborts on an assert; here the base is
