@@ -235,3 +235,45 @@ def test_pd_setup_helpers(built_lib):
     assert pd_seed_z(0.0, 137.5, 4_790_000) == 2.5 and pd_seed_z(0.0, 2e6, 1000) == 1.0
     cut = (C.c_double * 2)(300.4, 612.25)
     assert L.bsq_pd_max_span(0, cut, 2) == 1225 and L.bsq_pd_max_span(900, cut, 2) == 900
+
+
+def test_pd_hand_worked(host, tmp_path):
+    """Four concordant FR pairs of 50-bp reads at 100, TLEN 500, mates at 550: each gap covers
+    positions 149..549 (the read's end to the mate's start - 1).  The null puts distance 500 at the
+    0.9 quantile, inside the long tail (quantile 0.15), so at every covered position n = 4, four tail
+    pairs and z = (4 u - 4 S / 2) / S * sqrt(12 / 4) with u = 0.9 S: one L region 149-549 peaking at its
+    first position, eight ladder rungs (z >= 1 .. 2.75) with one region each, 401 positions in the z
+    histogram (fewer than 1000: no inflation), no tail fit."""
+    import math
+    n, L = 4, 50
+    S = 1048576
+    u = int(0.9 * S)
+    cdf = np.full(1001, S // 2, dtype=np.int64)
+    cdf[500] = u
+    seq = np.frombuffer(b"ACGT" * 250, dtype=np.uint8).copy()
+    s = synth.Sample(ref_seq=seq, target_offset=np.array([0, 1000], dtype=np.uint64), target_names=["t"],
+                     coverage_group=np.zeros(1, np.uint32), n_coverage_groups=1, target_order=np.zeros(1, np.uint32),
+                     tid=np.zeros(n, np.int32), pos=np.full(n, 99, np.int32), flag=np.full(n, 0x1 | 0x2 | 0x20 | 0x40, np.uint16),
+                     mapq=np.full(n, 40, np.uint8), x1=np.ones(n, np.uint32), xl=np.full(n, -1, np.int32),
+                     xr=np.full(n, -1, np.int32), read_file=np.zeros(n, np.uint8), read_group=np.zeros(n, np.uint16),
+                     l_qseq=np.full(n, L, np.uint32), seq_off=np.arange(n, dtype=np.uint64) * L,
+                     cigar_off=np.arange(n, dtype=np.uint64), n_cigar=np.ones(n, np.uint16),
+                     cigar=np.full(n, (L << 4) | 0, np.uint32), seq=np.full(n * L // 2, 0x12, np.uint8),
+                     qual=np.full(n * L, 30, np.uint8), n_read_files=2, n_quality=42,
+                     isize=np.full(n, 500, np.int32), xp=np.zeros(n, np.uint8),
+                     qname_off=np.arange(n + 1, dtype=np.uint64) * 3,
+                     qname=np.frombuffer(b"1:01:11:21:3", np.uint8).copy(), mtid=np.zeros(n, np.int32),
+                     mpos=np.full(n, 549, np.int32))
+    st = PairSettings(dp_group=(0,), window_width=(400.0,), predict_pair_distance=True, pd_cdf=(cdf,),
+                      pd_orientation=("FR",), pd_max_span=1000, pd_z_seed=2.5, pair_distance_seed=3,
+                      pair_distance_tail_quantile=0.15, pd_mean_covering_gap=250.0)
+    got, exp = run_both(host, s, st, tmp_path)
+    assert got == exp
+    z = (float(n * u) - float(n) * float(S) / 2.0) / float(S) * math.sqrt(12.0 / float(n))
+    lines = got[2].splitlines()
+    assert lines[0] == "#mean_covering_gap=250.000000" and lines[1] == "#n_effective_tests=4.000000"
+    assert lines[2] == "#seed_z=2.500000" and lines[3] == "#z_iqr_inflation=1.000000"
+    assert lines[4] == "#region_tail_fit_ok=0"
+    ladder = ";".join(f"{1 + 0.25 * k:.2f}:{1 if 1 + 0.25 * k <= z else 0}" for k in range(21))
+    assert lines[9] == "#region_ladder=" + ladder
+    assert lines[11:] == [f"t,149,549,L,401,149,4,4,{z:.4f}"]
