@@ -277,3 +277,35 @@ def test_pd_hand_worked(host, tmp_path):
     ladder = ";".join(f"{1 + 0.25 * k:.2f}:{1 if 1 + 0.25 * k <= z else 0}" for k in range(21))
     assert lines[9] == "#region_ladder=" + ladder
     assert lines[11:] == [f"t,149,549,L,401,149,4,4,{z:.4f}"]
+
+
+def test_mp_hand_worked(host, tmp_path):
+    """Forward reads of 50 bases starting at 101, 111, 121 with their mates unmapped, and mapped pairs at
+    105 and 300 (window 100, seed 2, fraction 0.5).  At 111 two mate-unmapped reads of three in the
+    window: the region opens with 101 and 111; at 121 the count reaches 3 of 4 (the maximum, 121
+    appended); at 201 and 205 the first two leave (2 of 3, 2 of 2, still enriched); at 211 only one is
+    left and the region closes at 210."""
+    seq = np.frombuffer(b"ACGT" * 250, dtype=np.uint8).copy()
+    pos = np.array([100, 104, 110, 120, 299], dtype=np.int32)
+    n, L = len(pos), 50
+    unm = np.array([1, 0, 1, 1, 0], dtype=bool)
+    flag = np.where(unm, 0x1 | 0x8 | 0x40, 0x1 | 0x2 | 0x20 | 0x40).astype(np.uint16)
+    names = [f"1:{i}".encode() for i in range(n)]
+    s = synth.Sample(ref_seq=seq, target_offset=np.array([0, 1000], dtype=np.uint64), target_names=["t"],
+                     coverage_group=np.zeros(1, np.uint32), n_coverage_groups=1, target_order=np.zeros(1, np.uint32),
+                     tid=np.zeros(n, np.int32), pos=pos, flag=flag, mapq=np.full(n, 40, np.uint8),
+                     x1=np.ones(n, np.uint32), xl=np.full(n, -1, np.int32), xr=np.full(n, -1, np.int32),
+                     read_file=np.zeros(n, np.uint8), read_group=np.zeros(n, np.uint16), l_qseq=np.full(n, L, np.uint32),
+                     seq_off=np.arange(n, dtype=np.uint64) * L, cigar_off=np.arange(n, dtype=np.uint64),
+                     n_cigar=np.ones(n, np.uint16), cigar=np.full(n, (L << 4) | 0, np.uint32),
+                     seq=np.full(n * L // 2, 0x12, np.uint8), qual=np.full(n * L, 30, np.uint8), n_read_files=2,
+                     n_quality=42, isize=np.where(unm, 0, 300).astype(np.int32),
+                     xp=np.where(unm, 3, 0).astype(np.uint8),
+                     qname_off=np.concatenate([[0], np.cumsum([len(x) for x in names])]).astype(np.uint64),
+                     qname=np.frombuffer(b"".join(names), np.uint8).copy())
+    st = PairSettings(dp_group=(0,), window_width=(100.0,), predict_missing_pairs=True, missing_pair_seed=2,
+                      missing_pair_seed_fraction=0.5)
+    got, exp = run_both(host, s, st, tmp_path)
+    assert got == exp
+    assert got[1].splitlines()[1:] == ["t,111,210,F,100,3,4,0,101__150;111__160;121__170"]
+    assert got[0].count("\n") == 1    # no discordant pair
