@@ -402,6 +402,21 @@ class CovColumns(C.Structure):
     ]
 
 
+POSITION_CTYPES = dict(unique_top=C.c_uint32, unique_bot=C.c_uint32, redundant_top=C.c_double,
+                       redundant_bot=C.c_double, raw_redundant_top=C.c_uint32, raw_redundant_bot=C.c_uint32,
+                       consensus_score=C.c_double, best_base=C.c_uint8, n_scored=C.c_uint32)
+
+
+def position_arrays_view(arrs: dict):
+    """A PositionArrays over a dict of per-position arrays (keys of POSITION_CTYPES; absent ones stay NULL)
+    and the contiguous arrays it points into, which the caller keeps alive across the call."""
+    keep = {}
+    for k, t in POSITION_CTYPES.items():
+        if k in arrs and arrs[k] is not None:
+            keep[k] = np.ascontiguousarray(arrs[k], dtype=np.dtype(t))
+    return PositionArrays(**{k: ptr(v, POSITION_CTYPES[k]) for k, v in keep.items()}), keep
+
+
 def cov_columns(n: int):
     """Numpy arrays for one region of n positions and the bsq_cov_columns struct pointing at them."""
     arrs = {name: np.zeros(n, dtype=np.float64 if "redundant_" in name and "raw" not in name else np.uint32)

@@ -403,6 +403,32 @@ class Scorer:
         arrs["last"] = last.value
         return arrs
 
+    def im_coverage_columns(self, sid: int, tid: int, start: int, end: int, read_group: int = -1,
+                            coverage_fit_failed: bool = False) -> dict:
+        """identify_mutations' coverage tally at positions start..end (1-based) of target tid, of one read
+        group's records when read_group >= 0: deletions count and N read bases do not, or, for a target
+        whose coverage fit failed, neither counts."""
+        arrs, st = abi.cov_columns(end - start + 1)
+        self._check(self.L.bsq_im_coverage_columns_rg(self.ctx, sid, tid, start, end, read_group,
+                                                      1 if coverage_fit_failed else 0, C.byref(st)))
+        return arrs
+
+    def write_coverage_table(self, sid: int, path: str, tid: int, positions: dict, n_read_groups: int | None = None,
+                             coverage_fit_failed: bool = False):
+        """<seq_id>.coverage.tsv of identify_mutations into path: the aggregate columns from `positions`
+        (identify_mutations(..., positions=True)["positions"]) and, with more than one read group, each
+        group's columns tallied on the device.  n_read_groups: the BAM header's @RG count (default: the
+        sample's highest read group + 1)."""
+        s = self.sample(sid)
+        if n_read_groups is None:
+            n_read_groups = int(np.max(s.read_group)) + 1 if len(s.read_group) else 1
+        view = abi.SampleView(s)
+        pa, keep = abi.position_arrays_view(positions)
+        self._check(self.L.bsq_write_coverage_table_rg(self.ctx, sid, path.encode(), s.target_names[tid].encode(),
+                                                       C.byref(view.ref), tid, C.byref(pa), n_read_groups,
+                                                       1 if coverage_fit_failed else 0))
+        del keep
+
     def write_coverage_region(self, sid: int, path: str, tid: int, start: int, end: int, resolution: int = 600,
                               total_only: bool = False, csv: bool = False, reference_average=None,
                               per_read_group: bool = False, n_read_groups: int | None = None):

@@ -1411,7 +1411,8 @@ int bsq_pair_result_copy(bsq_ctx* ctx, bsq_pair_region* dp, uint64_t n_dp, bsq_p
 // position) come back in one pinned buffer with the reference characters: [6][m] u32 counts |
 // [2][m] f64 weights | stat | the target's reference characters up to end_1.
 static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start, uint32_t end,
-                           uint32_t first, uint32_t step, host::CoverageRegion& out, int32_t rg_only = -1) {
+                           uint32_t first, uint32_t step, host::CoverageRegion& out, int32_t rg_only = -1,
+                           uint32_t mode = kCtBam2cov) {
   SampleDev* s = find_sample(ctx, sample_id);
   if (!s) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
   if (tid >= s->n_targets) return fail(ctx, BSQ_ERR_INVALID, "target index out of range");
@@ -1429,6 +1430,8 @@ static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32
   A.rstart = s->rstart.as<uint32_t>();
   A.rg = s->rg.as<uint16_t>();
   A.rg_only = rg_only;
+  A.seq = s->seq.as<uint8_t>();
+  A.mode = mode;
   A.n_reads = s->n_reads;
   A.t0 = s->tpoff[tid];
   A.c0 = A.t0 + start - 1;
@@ -1548,6 +1551,47 @@ int bsq_write_coverage_region_rg(bsq_ctx* ctx, int32_t sample_id, const char* pa
   (void)seq_id;   // the table has no seq_id column; the name is part of the caller's file name
   if (!host::write_coverage_region(path, R, resolution, flags, reference_average, per_rg))
     return fail(ctx, BSQ_ERR_INVALID, std::string("cannot write ") + path);
+  return BSQ_OK;
+}
+
+int bsq_im_coverage_columns_rg(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start_1, uint32_t end_1,
+                               int32_t read_group, int coverage_fit_failed, bsq_cov_columns* out) {
+  if (!ctx || !out) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  host::CoverageRegion R;
+  const int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, start_1, 1, R, read_group < 0 ? -1 : read_group,
+                                 coverage_fit_failed ? kCtImTabulate : kCtImPileup);
+  if (rc != BSQ_OK) return rc;
+  uint32_t* const u32[4] = {out->unique_top, out->unique_bot, out->raw_redundant_top, out->raw_redundant_bot};
+  for (int q = 0; q < 4; q++)
+    if (u32[q]) memcpy(u32[q], R.counts + (size_t)q * R.m, (size_t)R.m * 4);
+  if (out->unique_top_begin) memset(out->unique_top_begin, 0, (size_t)R.m * 4);
+  if (out->unique_bot_begin) memset(out->unique_bot_begin, 0, (size_t)R.m * 4);
+  if (out->redundant_top) memcpy(out->redundant_top, R.red, (size_t)R.m * 8);
+  if (out->redundant_bot) memcpy(out->redundant_bot, R.red + R.m, (size_t)R.m * 8);
+  return BSQ_OK;
+}
+
+int bsq_write_coverage_table_rg(bsq_ctx* ctx, int32_t sample_id, const char* path, const char* seq_id,
+                                const bsq_reference* ref, uint32_t tid, const bsq_position_arrays* positions,
+                                uint32_t n_read_groups, int coverage_fit_failed) {
+  if (!ctx || !path || !ref || !positions) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  if (tid >= ref->n_targets) return fail(ctx, BSQ_ERR_INVALID, "target index out of range");
+  if (n_read_groups > 0xFFFF) return fail(ctx, BSQ_ERR_INVALID, "more read groups than a record can name");
+  const uint32_t len = (uint32_t)(ref->target_offset[tid + 1] - ref->target_offset[tid]);
+  // _print_read_group_coverage: only with more than one read group (identify_mutations.cpp:862)
+  std::vector<host::CoverageRegion> per_rg;
+  if (n_read_groups > 1 && len > 0) {
+    per_rg.resize(n_read_groups);
+    for (uint32_t g = 0; g < n_read_groups; g++) {
+      const int rc = coverage_region(ctx, sample_id, tid, 1, len, 1, 1, per_rg[g], (int32_t)g,
+                                     coverage_fit_failed ? kCtImTabulate : kCtImPileup);
+      if (rc != BSQ_OK) return rc;
+      per_rg[g].own();
+    }
+  }
+  (void)seq_id;
+  const int rc = host::write_im_coverage_table(path, ref, tid, positions, per_rg);
+  if (rc != BSQ_OK) return fail(ctx, rc, std::string("cannot write ") + path);
   return BSQ_OK;
 }
 

@@ -20,6 +20,20 @@ __device__ __forceinline__ void add_block(const CovTabArgs& A, int k, uint32_t a
   atomicAdd(A.diff + (uint64_t)k * A.stride + (hi - A.c0), -1);
 }
 
+// The identify_mutations tallies leave out each entry whose aligned base is N: -1 at that column.
+// Query positions q .. q + len - 1 are aligned to columns x .. x + len - 1.
+__device__ __forceinline__ void drop_n_bases(const CovTabArgs& A, int k, const DevRead& rd, uint32_t x, uint32_t len,
+                                             uint32_t q) {
+  const uint32_t lo = max(x, A.c0), hi = min(x + len, A.c0 + A.n);
+  for (uint32_t c = lo; c < hi; c++) {
+    const uint32_t qp = q + (c - x);
+    if (qp < rd.len && nib_at(A.seq, rd.seq_off + qp) == 15) {
+      atomicAdd(A.diff + (uint64_t)k * A.stride + (c - A.c0), -1);
+      atomicAdd(A.diff + (uint64_t)k * A.stride + (c + 1 - A.c0), 1);
+    }
+  }
+}
+
 __device__ __forceinline__ uint32_t first_start_at(const CovTabArgs& A, uint32_t lo, uint32_t hi, uint32_t key) {
   while (lo < hi) { const uint32_t m = (lo + hi) >> 1; if (__ldg(A.rstart + m) < key) lo = m + 1; else hi = m; }
   return lo;
@@ -35,6 +49,7 @@ __global__ void ct_range_kernel(const CovTabArgs A) {
 
 // One thread per record of the target that starts before the region ends.  The pileup's entries of
 // a record are its aligned bases (M/=/X); deletions and N are entries too but this table skips them.
+template <uint32_t kMode>
 __global__ void __launch_bounds__(256) ct_reads_kernel(const CovTabArgs A) {
   const uint32_t end_col = A.c0 + A.n;
   // block b walks its own contiguous share of the records: neighbouring threads add to
@@ -59,24 +74,29 @@ __global__ void __launch_bounds__(256) ct_reads_kernel(const CovTabArgs A) {
     uint32_t first_col = 0xFFFFFFFFu;
     if (rd.flags & kSimple) {
       add_block(A, k, rd.start, rd.end);
+      if (kMode != kCtBam2cov) drop_n_bases(A, k, rd, rd.start, rd.end - rd.start, rd.clip);
       if (unique) {
         if (!rev && rd.clip == 0) first_col = rd.start;
         if (rev && (uint32_t)rd.clip + (rd.end - rd.start) == rd.len) first_col = rd.end - 1;
       }
     } else {
       const uint32_t* cg = A.cigar + rd.cigar_off;
-      uint32_t x = rd.start;
+      uint32_t x = rd.start, y = 0;                     // reference column, query position
       bool seen_query = false;
       uint32_t last_q_op = 0xFFu, last_q_end = 0;
+      // the identify_mutations pileup tally counts a read on every column it spans, deletions too
+      if (kMode == kCtImPileup) add_block(A, k, rd.start, rd.end);
       for (uint32_t j = 0; j < rd.n_cigar; j++) {
         const uint32_t op = __ldg(cg + j) & 0xF, len = __ldg(cg + j) >> 4;
         const bool aligned = op == 0 || op == 7 || op == 8;
         if (aligned) {
-          add_block(A, k, x, x + len);
+          if (kMode != kCtImPileup) add_block(A, k, x, x + len);
+          if (kMode != kCtBam2cov) drop_n_bases(A, k, rd, x, len, y);
           if (!seen_query && !rev && unique && len > 0) first_col = x;
         }
         if (aligned || op == 1 || op == 4) {            // consumes the query
           if (len > 0) { seen_query = true; last_q_op = op; last_q_end = x + len; }
+          y += len;
         }
         if (aligned || op == 2 || op == 3) x += len;    // consumes the reference
       }
@@ -214,6 +234,7 @@ __global__ void __launch_bounds__(256) ct_apply_kernel(const CovTabArgs A) {
 // warp loads the tile's candidate records 32 at a time (one per lane, which also computes the record's
 // weight 1.0 / X1), then walks them in record order by shuffle, each lane adding the weight when the
 // record covers its column with an aligned base.  Each lane's sum is the reference's sequential sum.
+template <uint32_t kMode>
 __global__ void __launch_bounds__(256) ct_redundant_kernel(const CovTabArgs A) {
   const int lane = threadIdx.x & 31;
   const uint32_t maxspan = A.stat[1];
@@ -235,6 +256,8 @@ __global__ void __launch_bounds__(256) ct_redundant_kernel(const CovTabArgs A) {
       for (uint32_t base = lo; base < hi; base += 32) {
         const uint32_t r = base + lane;
         uint32_t start = 0, end = 0, coff = 0, fl_nc = kFiltered;   // flags | n_cigar << 8
+        uint32_t clip = 0, len = 0;
+        uint64_t soff = 0;
         double w = 0.0;
         if (r < hi) {
           const DevRead rd = A.reads[r];
@@ -243,6 +266,9 @@ __global__ void __launch_bounds__(256) ct_redundant_kernel(const CovTabArgs A) {
           end = rd.end;
           coff = rd.cigar_off;
           fl_nc = rd.flags | ((uint32_t)rd.n_cigar << 8);
+          clip = rd.clip;
+          len = rd.len;
+          soff = rd.seq_off;
           if (redundancy == 1 || (rd.flags & (kFiltered | kBadCigar)) ||
               (A.rg_only >= 0 && (int32_t)__ldg(A.rg + r) != A.rg_only))
             end = 0;   // never covers
@@ -254,9 +280,23 @@ __global__ void __launch_bounds__(256) ct_redundant_kernel(const CovTabArgs A) {
           const uint32_t s_fl = __shfl_sync(kFull, fl_nc, j), s_coff = __shfl_sync(kFull, coff, j);
           const double s_w = __shfl_sync(kFull, w, j);
           bool covers = in && s_start <= col && s_end > col;
-          if (covers && !(s_fl & kSimple)) {
-            Pile e;
-            covers = resolve_cigar(A.cigar + s_coff, (int)(s_fl >> 8), s_start, col, e) && !e.del;
+          if (kMode == kCtBam2cov) {
+            if (covers && !(s_fl & kSimple)) {
+              Pile e;
+              covers = resolve_cigar(A.cigar + s_coff, (int)(s_fl >> 8), s_start, col, e) && !e.del;
+            }
+          } else {
+            const uint32_t s_clip = __shfl_sync(kFull, clip, j), s_len = __shfl_sync(kFull, len, j);
+            const uint64_t s_soff = __shfl_sync(kFull, soff, j);
+            if (covers) {
+              Pile e;
+              e.del = false;
+              e.qpos = (int)(col - s_start) + (int)s_clip;
+              if (!(s_fl & kSimple)) covers = resolve_cigar(A.cigar + s_coff, (int)(s_fl >> 8), s_start, col, e);
+              if (covers && e.del) covers = kMode == kCtImPileup;
+              else if (covers)
+                covers = (uint32_t)e.qpos < s_len && nib_at(A.seq, s_soff + (uint32_t)e.qpos) != 15;
+            }
           }
           if (covers) { if (s_fl & kRev) bot += s_w; else top += s_w; }
         }
@@ -290,11 +330,17 @@ int grid_for(uint64_t units, uint32_t per_block, int sms, int per_sm) {
 
 cudaError_t ct_launch(const CovTabArgs& A, int sms, cudaStream_t st) {
   ct_range_kernel<<<1, 32, 0, st>>>(A);
-  ct_reads_kernel<<<grid_for(A.n_reads, 256, sms, 8), 256, 0, st>>>(A);
+  const int g_reads = grid_for(A.n_reads, 256, sms, 8);
+  if (A.mode == kCtImPileup) ct_reads_kernel<kCtImPileup><<<g_reads, 256, 0, st>>>(A);
+  else if (A.mode == kCtImTabulate) ct_reads_kernel<kCtImTabulate><<<g_reads, 256, 0, st>>>(A);
+  else ct_reads_kernel<kCtBam2cov><<<g_reads, 256, 0, st>>>(A);
   ct_block_sums_kernel<<<A.n_blocks, 256, 0, st>>>(A);
   ct_block_scan_kernel<<<1, 1024, 0, st>>>(A);
   ct_apply_kernel<<<A.n_blocks, 256, 0, st>>>(A);
-  ct_redundant_kernel<<<grid_for(((uint64_t)A.n + 31) / 32 * 32, 256, sms, 8), 256, 0, st>>>(A);
+  const int g_red = grid_for(((uint64_t)A.n + 31) / 32 * 32, 256, sms, 8);
+  if (A.mode == kCtImPileup) ct_redundant_kernel<kCtImPileup><<<g_red, 256, 0, st>>>(A);
+  else if (A.mode == kCtImTabulate) ct_redundant_kernel<kCtImTabulate><<<g_red, 256, 0, st>>>(A);
+  else ct_redundant_kernel<kCtBam2cov><<<g_red, 256, 0, st>>>(A);
   return cudaGetLastError();
 }
 

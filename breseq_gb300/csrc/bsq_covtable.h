@@ -37,7 +37,16 @@ struct CovTabArgs {
                                // [3] [4] the records of the target that start before the region ends
   const uint16_t* rg;          // read group per record
   int32_t rg_only;             // >= 0: only this read group's records (--per-read-group columns)
+  const uint8_t* seq;          // packed 4-bit bases (kCtIm* modes read them)
+  uint32_t mode;               // kCtBam2cov, kCtImPileup or kCtImTabulate
 };
+
+// Which pileup entries a column counts.
+constexpr uint32_t kCtBam2cov = 0;     // coverage_output.cpp:373-376: every entry but deletions
+constexpr uint32_t kCtImPileup = 1;    // identify_mutations.cpp:1560-1610 at insert_count 0: deletions
+                                       // (read base '.') count, aligned N bases do not
+constexpr uint32_t kCtImTabulate = 2;  // tabulate_position_coverage (identify_mutations.cpp:2218-2250):
+                                       // neither deletions nor aligned N bases
 
 // Read pass, scan and redundant weights.  counts[4..5], diff and stat must be zeroed first.
 cudaError_t ct_launch(const CovTabArgs& A, int sms, cudaStream_t st);

@@ -75,6 +75,10 @@ struct CoverageRegion {
     ref = own_ref.data();
   }
 };
+// <seq_id>.coverage.tsv of identify_mutations (identify_mutations.cpp:2028-2052, 2173-2204): the
+// aggregate columns from pass 2's arrays, then each read group's (empty: none).  A BSQ_* status.
+int write_im_coverage_table(const char* path, const bsq_reference* ref, uint32_t tid, const bsq_position_arrays* pa,
+                            const std::vector<CoverageRegion>& per_rg);
 // The table's downsampling for a region and --resolution (coverage_output.cpp:203-209) and the first
 // position pileup_base::handle_position keeps, (position + start) % downsample == 0
 // (pileup_base.cpp:130-133).

@@ -380,6 +380,47 @@ bool write_coverage_region(const char* path, const CoverageRegion& R, uint32_t r
 }  // namespace host
 }  // namespace bsq
 
+namespace bsq {
+namespace host {
+
+// <seq_id>.coverage.tsv: the header and rows of identify_mutations.cpp:2028-2052, 2173-2204.  The
+// aggregate columns come from pass 2's per-position arrays (global columns); each read group's
+// columns, when given, from its region tally over positions 1..len (region offsets).  position_coverage
+// sums the strands bottom first (sum(), identify_mutations.h:99-126), and total_cov is the plain sum.
+int write_im_coverage_table(const char* path, const bsq_reference* ref, uint32_t tid, const bsq_position_arrays* pa,
+                            const std::vector<CoverageRegion>& per_rg) {
+  if (!path || !ref || !pa || tid >= ref->n_targets || !pa->unique_top || !pa->unique_bot || !pa->redundant_top ||
+      !pa->redundant_bot)
+    return BSQ_ERR_INVALID;
+  const uint64_t b = ref->target_offset[tid], e = ref->target_offset[tid + 1];
+  for (const CoverageRegion& R : per_rg)
+    if (R.m != e - b) return BSQ_ERR_INVALID;
+  std::ofstream out(path);
+  if (!out) return BSQ_ERR_INVALID;
+  static const char* const kCols[3] = {"unique_cov", "redundant_cov", "total_cov"};
+  out << "position\tref_base";
+  for (const char* c : kCols) out << "\t" << c;
+  for (size_t g = 0; g < per_rg.size(); g++)      // group-major, as coverage_output::table
+    for (const char* c : kCols) out << "\tRG-" << g << "_" << c;
+  out << "\n";
+  auto cols = [&](uint32_t ut, uint32_t ub, double rt, double rb) {
+    const double u = (double)ub + (double)ut;
+    const double rr = rb + rt;
+    out << "\t" << fmt_default(u) << "\t" << fmt_default(rr) << "\t" << fmt_default(u + rr);
+  };
+  for (uint64_t g = b; g < e; g++) {
+    out << (g - b + 1) << "\t" << ref->seq[g];
+    cols(pa->unique_top[g], pa->unique_bot[g], pa->redundant_top[g], pa->redundant_bot[g]);
+    const uint64_t i = g - b;
+    for (const CoverageRegion& R : per_rg) cols(R.counts[i], R.counts[R.m + i], R.red[i], R.red[R.m + i]);
+    out << "\n";
+  }
+  return out ? BSQ_OK : BSQ_ERR_INVALID;
+}
+
+}  // namespace host
+}  // namespace bsq
+
 extern "C" {
 
 int bsq_default_ra_settings(int polymorphism_prediction, bsq_ra_settings* s) {
@@ -503,21 +544,8 @@ int bsq_write_coverage_distribution(const char* path, const uint64_t* hist, uint
 
 int bsq_write_coverage_table(const char* path, const char* seq_id, const bsq_reference* ref, uint32_t tid,
                              const bsq_position_arrays* pa) {
-  if (!path || !ref || !pa || tid >= ref->n_targets || !pa->unique_top || !pa->unique_bot || !pa->redundant_top ||
-      !pa->redundant_bot)
-    return BSQ_ERR_INVALID;
   (void)seq_id;
-  std::ofstream out(path);     // identify_mutations.cpp:2028-2052, 2173-2204 (aggregate columns)
-  if (!out) return BSQ_ERR_INVALID;
-  out << "position\tref_base\tunique_cov\tredundant_cov\ttotal_cov\n";
-  const uint64_t b = ref->target_offset[tid], e = ref->target_offset[tid + 1];
-  for (uint64_t g = b; g < e; g++) {
-    const double u = (double)pa->unique_bot[g] + (double)pa->unique_top[g];
-    const double rr = pa->redundant_bot[g] + pa->redundant_top[g];
-    out << (g - b + 1) << "\t" << ref->seq[g] << "\t" << fmt_default(u) << "\t" << fmt_default(rr) << "\t"
-        << fmt_default(u + rr) << "\n";
-  }
-  return out ? BSQ_OK : BSQ_ERR_INVALID;
+  return bsq::host::write_im_coverage_table(path, ref, tid, pa, {});
 }
 
 int bsq_write_gd(const char* path, const bsq_reference* ref, const char* const* target_names,

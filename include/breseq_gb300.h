@@ -552,6 +552,20 @@ int bsq_write_coverage_region_rg(bsq_ctx* ctx, int32_t sample_id, const char* pa
 /* The columns of one read group's records (read_group < 0: all records, as bsq_coverage_columns). */
 int bsq_coverage_columns_rg(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start_1, uint32_t end_1,
                             int32_t read_group, bsq_cov_columns* out, uint32_t* last_column_1);
+/* identify_mutations' per-position coverage tally restricted to one read group's records (read_group < 0:
+ * all), positions start_1..end_1 of target tid: at insert position 0 every pileup entry whose read base
+ * is not N, deletions included (identify_mutations.cpp:1560-1610); where the target's coverage fit failed
+ * (coverage_fit_failed != 0) tabulate_position_coverage's, which leaves deletions out too (:2218-2250).
+ * Fills unique_*, raw_redundant_* and redundant_* of `out`; the begin counters are zeroed. */
+int bsq_im_coverage_columns_rg(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start_1, uint32_t end_1,
+                               int32_t read_group, int coverage_fit_failed, bsq_cov_columns* out);
+/* <seq_id>.coverage.tsv (identify_mutations.cpp:2028-2052, 2173-2250; written under --predict-copy-number):
+ * the aggregate columns from pass 2's per-position arrays, as bsq_write_coverage_table, and with more than
+ * one read group (:862) each group's unique_cov / redundant_cov / total_cov prefixed "RG-<g>_", tallied on
+ * the device by bsq_im_coverage_columns_rg over the resident sample. */
+int bsq_write_coverage_table_rg(bsq_ctx* ctx, int32_t sample_id, const char* path, const char* seq_id,
+                                const bsq_reference* ref, uint32_t tid, const bsq_position_arrays* positions,
+                                uint32_t n_read_groups, int coverage_fit_failed);
 
 /* Launch shape of the passes.  None of the knobs changes a result: every count is an integer sum
  * and every column and candidate is scored by one warp whatever the grid. */

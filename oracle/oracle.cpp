@@ -36,6 +36,9 @@
  *     tests/test_softclip.py)
  *   - coverage_output::table / pileup_callback, with --per-read-group
  *                                               src/breseq/coverage_output.cpp:190-500
+ *   - identify_mutations' coverage tally per read group and <seq_id>.coverage.tsv
+ *                                               src/breseq/identify_mutations.cpp:1560-1610, 2028-2052,
+ *                                               2173-2250
  *   - fit_censored_negative_binomial / fit_coverage_distribution and the Cephes functions they use
  *                                               src/breseq/coverage_distribution.cpp:115-396, stats.cpp
  *     (special functions pinned against scipy; see tests/test_coverage_fit.py)
@@ -1339,6 +1342,87 @@ extern "C" int oracle_coverage_columns(const bsq_reference* ref, const bsq_read_
   }
   if (last_out) *last_out = last;
   return BSQ_OK;
+}
+
+// identify_mutations' coverage tally of one read group's entries at insert position 0: the main loop
+// (src/breseq/identify_mutations.cpp:1560-1610), where a deletion's read base is '.' and so counts, and an
+// N read base does not; or tabulate_position_coverage (:2218-2250) for a target whose coverage fit failed,
+// which skips deletions as well.  Per strand: unique count, Σ 1/X1 in pileup order, raw redundant count.
+static void im_cov_columns(Data& d, uint32_t t, uint32_t start, uint32_t end, int32_t rg_only, bool failed,
+                           std::vector<CovCol>& cols) {
+  const bsq_read_soa* rd = d.rd;
+  cols.assign(end - start + 1, CovCol());
+  walk_columns(d, t, (int64_t)start - 1, (int64_t)end, [&](int64_t c, const std::vector<uint64_t>& active) {
+    CovCol& x = cols[c - ((int64_t)start - 1)];
+    for (uint64_t r : active) {
+      if (rg_only >= 0 && (int32_t)rd->read_group[r] != rg_only) continue;   // p.read_group_index(*i)
+      Pile e;
+      if (!resolve(rd, r, c, e)) continue;
+      if (failed && e.is_del) continue;
+      int indel = e.is_del ? -1 : std::max(e.indel, 0);
+      uint8_t read_base = '.';
+      if (indel >= 0) read_base = base_at(rd, r, e.qpos);
+      if (bam_is_N(read_base)) continue;
+      const int s = d.info[r].rev ? 1 : 0;
+      const uint32_t redundancy = rd->x1[r];
+      if (redundancy == 1) x.u[s]++;
+      else { x.red[s] += 1.0 / redundancy; x.raw[s]++; }
+    }
+  });
+}
+
+extern "C" int oracle_im_coverage_columns(const bsq_reference* ref, const bsq_read_soa* rd, uint32_t tid,
+                                          uint32_t start, uint32_t end, int32_t read_group, int coverage_fit_failed,
+                                          bsq_cov_columns* out, char* errbuf, int errcap) {
+  Data d; d.ref = ref; d.rd = rd;
+  int rc = prepare(d);
+  if (rc) { if (errbuf) snprintf(errbuf, errcap, "%s", d.err.c_str()); return rc; }
+  std::vector<CovCol> cols;
+  im_cov_columns(d, tid, start, end, read_group, coverage_fit_failed != 0, cols);
+  for (size_t i = 0; i < cols.size(); i++) {
+    if (out->unique_top) out->unique_top[i] = cols[i].u[0];
+    if (out->unique_bot) out->unique_bot[i] = cols[i].u[1];
+    if (out->redundant_top) out->redundant_top[i] = cols[i].red[0];
+    if (out->redundant_bot) out->redundant_bot[i] = cols[i].red[1];
+    if (out->raw_redundant_top) out->raw_redundant_top[i] = cols[i].raw[0];
+    if (out->raw_redundant_bot) out->raw_redundant_bot[i] = cols[i].raw[1];
+    if (out->unique_top_begin) out->unique_top_begin[i] = 0;
+    if (out->unique_bot_begin) out->unique_bot_begin[i] = 0;
+  }
+  return BSQ_OK;
+}
+
+// <seq_id>.coverage.tsv (identify_mutations.cpp:2028-2052, 2173-2216): the aggregate columns from the
+// given per-position arrays (pass 2's), then, with more than one read group (:862), each group's three
+// columns "RG-<g>_..." from im_cov_columns.  Strands are summed as position_coverage::sum does.
+extern "C" int oracle_write_coverage_table_rg(const bsq_reference* ref, const bsq_read_soa* rd, const char* path,
+                                              uint32_t tid, const bsq_position_arrays* pa, uint32_t n_read_groups,
+                                              int coverage_fit_failed, char* errbuf, int errcap) {
+  Data d; d.ref = ref; d.rd = rd;
+  int rc = prepare(d);
+  if (rc) { if (errbuf) snprintf(errbuf, errcap, "%s", d.err.c_str()); return rc; }
+  const uint64_t b = ref->target_offset[tid], len = ref->target_offset[tid + 1] - b;
+  std::vector<std::vector<CovCol>> rg(n_read_groups > 1 && len ? n_read_groups : 0);
+  for (uint32_t g = 0; g < rg.size(); g++) im_cov_columns(d, tid, 1, (uint32_t)len, (int32_t)g, coverage_fit_failed != 0, rg[g]);
+  FILE* f = fopen(path, "w");
+  if (!f) return BSQ_ERR_INVALID;
+  const char* names[3] = {"unique_cov", "redundant_cov", "total_cov"};
+  std::string line = "position\tref_base";
+  for (const char* n : names) line += std::string("\t") + n;
+  for (uint32_t g = 0; g < rg.size(); g++)
+    for (const char* n : names) line += "\tRG-" + std::to_string(g) + "_" + n;
+  fprintf(f, "%s\n", line.c_str());
+  auto three = [&](std::string& l, double ut, double ub, double rt, double rb) {
+    const double u = ub + ut, r = rb + rt;
+    l += "\t" + fmt_double(u) + "\t" + fmt_double(r) + "\t" + fmt_double(u + r);
+  };
+  for (uint64_t i = 0; i < len; i++) {
+    std::string l = std::to_string(i + 1) + "\t" + std::string(1, ref->seq[b + i]);
+    three(l, pa->unique_top[b + i], pa->unique_bot[b + i], pa->redundant_top[b + i], pa->redundant_bot[b + i]);
+    for (auto& cols : rg) three(l, cols[i].u[0], cols[i].u[1], cols[i].red[0], cols[i].red[1]);
+    fprintf(f, "%s\n", l.c_str());
+  }
+  return fclose(f) == 0 ? BSQ_OK : BSQ_ERR_INVALID;
 }
 
 extern "C" int oracle_write_coverage_region_rg(const bsq_reference* ref, const bsq_read_soa* rd, const char* path,

@@ -81,3 +81,97 @@ def test_per_read_group_columns_add_up(tmp_path):
         assert per[2] == [0.0] * 8     # a group no record names
     tail = [x for x in lines if x.startswith("#")]
     assert tail[-9].split("\t")[1] == "RG-0_region_unique_average_cov" and len(tail) == 4 + 9
+
+
+def im_read_groups():
+    """The ecoli_small sample (repeats, indels, N bases, trims) with its records spread over three read
+    groups: the read file, and a seeded tenth moved to group 2."""
+    import dataclasses
+    s = samples.ecoli_small()
+    rng = np.random.default_rng(5)
+    g = np.where(rng.random(len(s.read_group)) < 0.1, 2, s.read_file).astype(np.uint16)
+    return dataclasses.replace(s, read_group=g)
+
+
+IM_INT = ("unique_top", "unique_bot", "raw_redundant_top", "raw_redundant_bot")
+IM_RED = ("redundant_top", "redundant_bot")
+
+
+def test_im_coverage_tally_equals_pass_2(tmp_path):
+    # identify_mutations' coverage tally restated alone (all records) equals the per-position coverage
+    # the oracle's pass 2 keeps: deletions counted, N read bases not; with the coverage fit failed on
+    # one target, tabulate_position_coverage's (deletions left out too).  The groups' integer columns
+    # add up to it and their weights to within rounding.
+    s = im_read_groups()
+    ec = po.error_count(s)
+    tab = po.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
+    T = len(s.target_offset) - 1
+    p = po.default_im_params(s)
+    p["deletion_propagation_cutoff"][1] = -1.0
+    pos = po.identify(s, tab, p)["positions"]
+    more = fewer = False
+    for t in range(T):
+        b, e = int(s.target_offset[t]), int(s.target_offset[t + 1])
+        failed = t == 1
+        allc = po.im_coverage_columns(s, t, 1, e - b, coverage_fit_failed=failed)
+        for k in IM_INT + IM_RED:
+            assert np.array_equal(allc[k], pos[k][b:e]), (t, k)
+        per = [po.im_coverage_columns(s, t, 1, e - b, read_group=g, coverage_fit_failed=failed) for g in range(3)]
+        for k in IM_INT:
+            assert np.array_equal(sum(x[k].astype(np.int64) for x in per), allc[k].astype(np.int64)), (t, k)
+        for k in IM_RED:
+            assert np.allclose(sum(x[k] for x in per), allc[k], rtol=1e-12, atol=0), (t, k)
+        assert all(x["unique_top"].any() for x in per)
+        # the pass-2 tally differs from BAM2COV's exactly by the deletion entries (counted) and the
+        # aligned N bases (not counted)
+        if not failed:
+            bc = po.coverage_columns(s, t, 1, e - b)
+            d = allc["unique_top"].astype(np.int64) + allc["unique_bot"] - bc["unique_top"] - bc["unique_bot"]
+            more |= bool((d > 0).any())
+            fewer |= bool((d < 0).any())
+    assert more and fewer
+
+
+def test_im_coverage_table_read_group_columns(tmp_path):
+    s = im_read_groups()
+    ec = po.error_count(s)
+    tab = po.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
+    pos = po.identify(s, tab, po.default_im_params(s))["positions"]
+    path = str(tmp_path / "cov.tsv")
+    po.write_coverage_table(s, path, 2, pos, n_read_groups=3)
+    lines = open(path).read().splitlines()
+    head = lines[0].split("\t")
+    assert head[:5] == ["position", "ref_base", "unique_cov", "redundant_cov", "total_cov"]
+    assert head[5] == "RG-0_unique_cov" and head[-1] == "RG-2_total_cov" and len(head) == 5 + 9
+    b, e = int(s.target_offset[2]), int(s.target_offset[3])
+    assert len(lines) == 1 + (e - b)
+    for i in range(0, e - b, 37):
+        r = lines[1 + i].split("\t")
+        assert int(r[0]) == i + 1
+        u = float(pos["unique_top"][b + i]) + float(pos["unique_bot"][b + i])
+        assert float(r[2]) == u and sum(float(r[5 + 3 * g]) for g in range(3)) == u
+    # one read group: no per-group columns (identify_mutations.cpp:862)
+    po.write_coverage_table(s, path, 2, pos, n_read_groups=1)
+    assert open(path).readline().rstrip("\n").split("\t") == head[:5]
+
+
+def test_library_writer_matches_oracle(built_lib, tmp_path):
+    # the library's host writer of <seq_id>.coverage.tsv (aggregate columns, no device call) against the
+    # oracle's, on every target of a sample with a failed coverage fit on one of them
+    import ctypes as C
+    from breseq_gb300 import _lib, abi
+    s = im_read_groups()
+    ec = po.error_count(s)
+    tab = po.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
+    p = po.default_im_params(s)
+    p["deletion_propagation_cutoff"][1] = -1.0
+    pos = po.identify(s, tab, p)["positions"]
+    L = _lib.load()
+    view = abi.SampleView(s)
+    pa, keep = abi.position_arrays_view(pos)
+    for t in range(len(s.target_offset) - 1):
+        a, b = str(tmp_path / f"l{t}.tsv"), str(tmp_path / f"o{t}.tsv")
+        assert L.bsq_write_coverage_table(a.encode(), s.target_names[t].encode(), C.byref(view.ref), t, C.byref(pa)) == 0
+        po.write_coverage_table(s, b, t, pos, n_read_groups=1, coverage_fit_failed=t == 1)
+        assert open(a).read() == open(b).read(), t
+    del keep
