@@ -422,7 +422,7 @@ class Scorer:
         s = self.sample(sid)
         if n_read_groups is None:
             n_read_groups = int(np.max(s.read_group)) + 1 if len(s.read_group) else 1
-        view = abi.SampleView(s)
+        view = self._views[sid][1]
         pa, keep = abi.position_arrays_view(positions)
         self._check(self.L.bsq_write_coverage_table_rg(self.ctx, sid, path.encode(), s.target_names[tid].encode(),
                                                        C.byref(view.ref), tid, C.byref(pa), n_read_groups,
