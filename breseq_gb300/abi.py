@@ -206,6 +206,8 @@ class ImParams(C.Structure):
         ("deletion_propagation_cutoff", P(C.c_double)),
         ("deletion_seed_cutoff", P(C.c_double)),
         ("precision", C.c_int32),
+        ("n_read_groups", C.c_uint32),
+        ("dp_group", P(C.c_int32)),
     ]
 
 

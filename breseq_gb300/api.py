@@ -128,6 +128,11 @@ class ImSettings:
     polymorphism_precision_decimal: float = 1e-6
     polymorphism_precision_places: int | None = None          # 8 / 3
     skip_missing_coverage_prediction: bool = False
+    # DP group of each dense read group (-1: none), as identify_mutations_pileup builds it from the
+    # paired read-file sets with a paired-mapping-distance fit (identify_mutations.cpp:883-911); empty:
+    # no DP group.  A non-proper paired read of a DP group without a usable XP tag is left out of
+    # its first column (:1399-1416).
+    dp_group: tuple = ()
 
     def resolved(self):
         poly = self.polymorphism_log10_e_value_cutoff
@@ -148,7 +153,8 @@ def im_params(s, st: ImSettings, deletion_propagation_cutoff=None, deletion_seed
         prop=np.broadcast_to(np.asarray(5.0 if deletion_propagation_cutoff is None else deletion_propagation_cutoff,
                                         dtype=np.float64), (T,)).copy(),
         seed=np.broadcast_to(np.asarray(0.0 if deletion_seed_cutoff is None else deletion_seed_cutoff,
-                                        dtype=np.float64), (T,)).copy())
+                                        dtype=np.float64), (T,)).copy(),
+        dpg=np.ascontiguousarray(st.dp_group or [-1], dtype=np.int32))
     p = abi.ImParams(n_read_files=n_read_files or s.n_read_files, n_quality=n_quality or s.n_quality,
                      base_quality_cutoff=st.base_quality_cutoff,
                      mutation_cutoff=st.mutation_log10_e_value_cutoff, polymorphism_cutoff=poly,
@@ -157,7 +163,8 @@ def im_params(s, st: ImSettings, deletion_propagation_cutoff=None, deletion_seed
                      skip_missing_coverage_prediction=int(st.skip_missing_coverage_prediction),
                      log10_ref_length=float(np.log10(float(s.target_offset[-1]))),
                      deletion_propagation_cutoff=abi.ptr(keep["prop"], C.c_double),
-                     deletion_seed_cutoff=abi.ptr(keep["seed"], C.c_double), precision=precision)
+                     deletion_seed_cutoff=abi.ptr(keep["seed"], C.c_double), precision=precision,
+                     n_read_groups=len(st.dp_group), dp_group=abi.ptr(keep["dpg"], C.c_int32))
     return p, keep
 
 

@@ -54,7 +54,8 @@ struct DevMem {
 };
 
 struct SampleDev {
-  DevMem ref, reads, x1, rg, qb, cigar, seq, qual, tile_range, d_tpoff, tgt_group, tgt_called, tgt_failed, rstart, mapq;
+  DevMem ref, rcode, reads, x1, rg, qb, cigar, seq, qual, tile_range, d_tpoff, tgt_group, tgt_called, tgt_failed, rstart,
+      mapq;
   // pair annotations for the discordant / missing-pair scans: raw flags, XP codes, TLEN, names
   DevMem pflag, pxp, pisize, pqoff, pqname, pmtid, pmpos;
   bool has_pairs = false, has_mates = false;
@@ -175,6 +176,7 @@ static cudaError_t upload(DevMem& m, const T* src, uint64_t n, cudaStream_t st) 
 static DevSample make_dev_sample(const SampleDev& s) {
   DevSample S;
   S.ref = s.ref.as<uint8_t>();
+  S.rcode = s.rcode.as<uint8_t>();
   S.reads = s.reads.as<DevRead>();
   S.x1 = s.x1.as<uint32_t>();
   S.rg = s.rg.as<uint16_t>();
@@ -352,7 +354,7 @@ uint64_t bsq_sample_footprint(const bsq_reference* ref, const bsq_read_soa* rd) 
   const uint64_t pairs = (rd->xp && rd->isize && rd->qname_off && rd->qname)
                              ? rd->n_reads * 15 + 8 + (rd->n_reads ? rd->qname_off[rd->n_reads] : 0)
                              : 0;
-  return cols + 64 + rd->n_reads * per_read + rd->n_cigar_total * 4 + rd->n_bases_total / 2 + 16 +
+  return 2 * (cols + 64) + rd->n_reads * per_read + rd->n_cigar_total * 4 + rd->n_bases_total / 2 + 16 +
          rd->n_bases_total + tiles * 8 + upload_tmp + pairs;
 }
 
@@ -445,13 +447,15 @@ static int pack_sample(bsq_ctx* ctx, std::unique_ptr<SampleDev>& s, RecordsDev& 
   in.l_qseq = R.lq.as<uint32_t>(); in.seq_off = R.soff.as<uint64_t>(); in.cigar_off = R.coff.as<uint64_t>();
   in.n_cigar = R.nc.as<uint16_t>(); in.cigar = s->cigar.as<uint32_t>(); in.tpoff = s->d_tpoff.as<uint32_t>(); in.called = s->tgt_called.as<uint8_t>();
   in.xj = R.has_xj ? R.xj.as<uint8_t>() : nullptr;
+  in.xp = R.has_pairs ? R.xp.as<uint8_t>() : nullptr;
   in.n = (uint32_t)n; in.n_targets = T; in.n_bases = R.n_bases_total; in.n_cigar_total = R.n_cigar_total;
   PackOut po;
   po.reads = s->reads.as<DevRead>(); po.qb = s->qb.as<QBounds>(); po.rstart = s->rstart.as<uint32_t>();
   po.mapq = s->mapq.as<uint8_t>(); po.err = stats; po.maxspan = stats + 1; po.mapq_mask = stats + 2;
   CK(launch_pack(in, po, st));
   // the reference checked on the device: [11] bytes outside A/C/G/T/N, [12] zero bytes (separators)
-  CK(launch_ref_check(s->ref.as<uint8_t>(), s->n_cols, stats + 11, stats + 12, ctx->sms, st));
+  CK(s->rcode.alloc(s->n_cols + 64, st));
+  CK(launch_ref_check(s->ref.as<uint8_t>(), s->rcode.as<uint8_t>(), s->n_cols, stats + 11, stats + 12, ctx->sms, st));
   uint32_t h[16];
   CK(cudaMemcpyAsync(h, stats, 16 * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -769,6 +773,19 @@ constexpr uint32_t kBoundPool = 4u << 20;   // (class, multiplicity) entries for
 // One group of at most kBatchJobs samples; results go to res_*[job0 + j].
 //   device arena: per job the likelihood-class table (lp64 | r64 | lpmax64 | lp32) and the per-target
 //   deletion cutoffs and failed-fit flags, staged on the host and sent in one copy.
+// The discordant-pair read groups of pass-2 parameters as a 256-bit mask (identify_mutations.cpp:883-911).
+static int dp_mask(bsq_ctx* ctx, const bsq_im_params& p, uint32_t out[8]) {
+  for (int i = 0; i < 8; i++) out[i] = 0;
+  if (p.n_read_groups && !p.dp_group) return fail(ctx, BSQ_ERR_INVALID, "n_read_groups without dp_group");
+  for (uint32_t g = 0; g < p.n_read_groups; g++) {
+    if (p.dp_group[g] < -1) return fail(ctx, BSQ_ERR_INVALID, "DP group out of range");
+    if (p.dp_group[g] < 0) continue;
+    if (g >= 256) return fail(ctx, BSQ_ERR_INVALID, "discordant-pair groups on read groups beyond the first 256");
+    out[g >> 5] |= 1u << (g & 31);
+  }
+  return BSQ_OK;
+}
+
 static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_params* P,
                     const double* const* tables, bsq_position_arrays* const* pos_out, uint32_t job0) {
   std::vector<SampleDev*> smp(n);
@@ -780,6 +797,9 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
     if (P[j].n_read_files == 0 || P[j].n_read_files > 255 || P[j].n_quality == 0 || P[j].n_quality > 256)
       return fail(ctx, BSQ_ERR_INVALID, "error table dimensions out of range");
     if (P[j].precision != P[0].precision) return fail(ctx, BSQ_ERR_INVALID, "one precision per batch");
+    uint32_t m[8];
+    const int rc = dp_mask(ctx, P[j], m);
+    if (rc != BSQ_OK) return rc;
   }
   CK(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
@@ -874,6 +894,7 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
     A.screen_margin = 1.0f;
     A.guard = 2e-6f;
     A.precision_decimal = P[j].polymorphism_precision_decimal;
+    dp_mask(ctx, P[j], A.dp_rg);      // checked above
   }
   CandArgs C;
   memset(&C, 0, sizeof C);
@@ -1696,16 +1717,21 @@ int bsq_score_positions_noalloc(bsq_ctx* ctx, int32_t sid, const bsq_im_params* 
   const uint32_t per_warp = std::max<uint32_t>(32, s->max_tile_reads);
   const uint64_t fit = kNoAllocGatherEntries / cand_warp_stride(per_warp);
   if (fit == 0) return fail(ctx, BSQ_ERR_SIZE, "a column is covered by more reads than the no-allocation scratch holds");
+  if (s->n_targets > kNoAllocMaxTargets)
+    return fail(ctx, BSQ_ERR_SIZE, "more targets than the no-allocation limit (32768)");
+  NoAllocJob J;
+  {
+    const int rc = dp_mask(ctx, *p, J.dp_rg);
+    if (rc != BSQ_OK) return rc;
+  }
   CK(cudaSetDevice(ctx->device));
   void* scratch = nullptr;
   CK(noalloc_scratch_setup(ctx->device, &scratch));
   cudaStream_t st = ctx->stream;
-  for (uint32_t t = 0; t < s->n_targets; t++)
-    CK(cudaMemsetAsync(s->tgt_failed.as<uint8_t>() + t, p->deletion_propagation_cutoff[t] < 0.0 ? 1 : 0, 1, st));
-  NoAllocJob J;
   J.log10_table = table; J.R = R; J.Q = Q;
   J.mapq_values = s->mapq_values.data(); J.n_mapq = (uint32_t)s->mapq_values.size();
-  J.tid = d_tid; J.pos0 = d_pos0; J.n_positions = n_positions; J.failed = s->tgt_failed.as<uint8_t>();
+  J.tid = d_tid; J.pos0 = d_pos0; J.n_positions = n_positions;
+  J.prop_cutoff = p->deletion_propagation_cutoff; J.n_targets = s->n_targets;
   J.ra = d_ra; J.ra_cap = ra_capacity; J.n_ra = d_n_ra; J.qhist = d_qhist;
   J.base_quality_cutoff = p->base_quality_cutoff; J.log10_ref_len = p->log10_ref_length;
   J.mutation_cutoff = p->mutation_cutoff; J.poly_cutoff = p->polymorphism_cutoff;

@@ -35,8 +35,11 @@ static_assert(sizeof(DevRead) == 32, "DevRead must stay 32 bytes");
 // coverage table applies on every target.  kScSkip: the soft-clipping tabulation leaves it out
 // (unmapped, XJ-tagged, or on an empty target).  kBadCigar: the CIGAR does not fit the read or the
 // target; the load rejects such a record when the scoring pileup keeps it, the other passes report
-// it when they keep it.
-enum : uint8_t { kRev = 1, kSimple = 2, kRedundant = 4, kSkip = 8, kScSkip = 16, kBadCigar = 32, kFiltered = 64 };
+// it when they keep it.  kDpCand: a primary, mapped, paired record that is not a proper pair, has a
+// mapped mate and has no XP tag or one other than FR / RF / FF; pass 2 leaves it out of its first
+// column when its read group is a discordant-pair group (identify_mutations.cpp:1399-1416).
+enum : uint8_t { kRev = 1, kSimple = 2, kRedundant = 4, kSkip = 8, kScSkip = 16, kBadCigar = 32, kFiltered = 64,
+                 kDpCand = 128 };
 constexpr uint16_t kNoTag = 0xFFFF;
 
 // Query bounds of complex reads (simple reads derive them from clip and span):
@@ -46,6 +49,7 @@ struct QBounds { uint16_t qs0, qe0, qbs, qbe; };
 
 struct DevSample {
   const uint8_t* ref;         // padded reference chars
+  const uint8_t* rcode;       // the same columns as codes: A,C,G,T = 0..3, N = 4, separator = 5
   const DevRead* reads;
   const uint32_t* x1;         // redundancy per read
   const uint16_t* rg;         // read group per read
@@ -127,7 +131,14 @@ struct ImArgs {
   float screen_margin;        // log10 units subtracted from the polymorphism cutoff for the screen
   float guard;                // consensus guard band (log10 units) for FP64 recompute
   double precision_decimal;   // EM convergence tolerance (polymorphism_precision_decimal)
+  uint32_t dp_rg[8];          // bit g: read group g is a discordant-pair group (groups 0..255)
 };
+
+// Pass 2 leaves a kDpCand record of a discordant-pair read group out of its first column, insert
+// position 0 (identify_mutations.cpp:1399-1416).
+__host__ __device__ inline bool dp_group_member(const uint32_t* dp_rg, uint32_t rg) {
+  return rg < 256 && ((dp_rg[rg >> 5] >> (rg & 31)) & 1u);
+}
 
 // A scoring job for the candidate kernel: one reference column, all its insert slots.
 struct CandArgs {

@@ -397,6 +397,7 @@ struct CandOut {
   uint2* pool;
   unsigned int* pool_used;
   uint32_t pool_cap;
+  uint32_t dp_rg[8];          // discordant-pair read groups (ImArgs::dp_rg)
 };
 
 // write_RA_frequency_bounds (identify_mutations.cpp:3175-3217): the reference's bisections, with each
@@ -471,6 +472,10 @@ __device__ void score_candidate_column(const DevSample& S, const ClassTable& T, 
       en.z = 0xFFFFFFFFu;
       const uint32_t r = en.x;
       const DevRead rd = S.reads[r];
+      if (k == 0 && (rd.flags & kDpCand) && c == rd.start && dp_group_member(A.dp_rg, __ldg(S.rg + r))) {
+        ents[i] = en;                 // left out of its first column at insert position 0
+        continue;
+      }
       const int qpos = (int)(en.y & 0xFFFF);
       const int obi = (int)(en.y >> 16) - 1;
       const bool rev = rd.flags & kRev;

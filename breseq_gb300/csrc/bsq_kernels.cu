@@ -115,6 +115,10 @@ __device__ __forceinline__ void pack_one(const RawSoA& in, const PackOut& out, u
   if ((flag & 0x4) || (in.xj && in.xj[i]) || tlen == 0) fl |= kScSkip;
   if (bad_cigar) fl |= kBadCigar;
   if (flag & 0x704) fl |= kFiltered;
+  // the discordant-pair enter test of identify_mutations.cpp:1400-1415 that ends in `continue`:
+  // paired, mapped, not a proper pair, primary, mate mapped, XP absent or not FR / RF / FF
+  if ((flag & 0x1) && !(flag & 0x4) && !(flag & 0x2) && !(flag & (0x100 | 0x800 | 0x8)) && (!in.xp || in.xp[i] > 2))
+    fl |= kDpCand;
   if (rlen == 0) rlen = 1;
   d.start = in.tpoff[tid] + (uint32_t)pos;
   d.end = d.start + rlen;
@@ -256,11 +260,6 @@ __device__ __forceinline__ bool read_start_counts(const EcArgs& A, const DevRead
 
 // Work units are chunks of one job's reads, pulled by whole blocks from a shared counter; the block's
 // shared histogram belongs to the chunk's job and is flushed at the chunk's end.
-// count_alignment_position for a read with one aligned block (soft clips allowed): its bases are
-// consecutive query positions on consecutive columns and no base has an indel, so each base has
-// event (1) and, below the query end, event (2a).  Lanes take consecutive bases; a forward read's
-// (2a) event uses the next base, the next quality and the next column's reference, which the next
-// lane already holds.  Reference characters are A/C/G/T/N (checked when the sample is loaded).
 // Packed pairs of FP32 values (element 0 in the low word): Blackwell's two-wide FP32 add / sub.
 __device__ __forceinline__ unsigned long long f32x2_add(unsigned long long a, unsigned long long b) {
   unsigned long long d;
@@ -275,62 +274,46 @@ __device__ __forceinline__ unsigned long long f32x2_sub(unsigned long long a, un
 __device__ __forceinline__ float f32x2_lo(unsigned long long x) { return __uint_as_float((uint32_t)x); }
 __device__ __forceinline__ float f32x2_hi(unsigned long long x) { return __uint_as_float((uint32_t)(x >> 32)); }
 
-__device__ __forceinline__ uint32_t ref_code(uint32_t ch) {   // A,C,G,T -> 0..3 (N handled by the caller)
-  const uint32_t x = (ch >> 1) & 3u;                          // A 0, C 1, G 3, T 2
-  return x ^ (x >> 1);
-}
+// count_alignment_position (error_count.cpp:888-944) for a read with one aligned block (soft clips
+// allowed): its bases are consecutive query positions on consecutive columns and no base has an indel,
+// so base i has event (1) and, when i is not the block's last base, event (2a).  Event (2a) of base i
+// reads base, quality and reference at i + 1 - rev: for a forward read those of base i + 1, for a
+// reverse read its own.  Both events of base j therefore test only base j's own values: (1) always,
+// and (2a) on behalf of base j - 1 (forward, j >= 1) or of base j itself (reverse, j below the last).
+// One lane per base, no neighbour exchange; reference characters are A/C/G/T/N (checked at load).
 __device__ __forceinline__ void ec_simple_read(const DevSample& S, const EcArgs& A, uint32_t* hist, const DevRead& rd,
                                                uint32_t span, int lane, uint32_t& err) {
   const bool rev = rd.flags & kRev;
   const uint32_t rs = rd.rfile, R = A.R, Q = A.Q;
   if (rs >= R) { err |= kErrCovariate; return; }
   const uint32_t flip = rev ? 3u : 0u;              // 3 - x == x ^ 3 for x in 0..3
-  const uint32_t nbins = R * 25u * Q;               // slots nbins + lane absorb events that do not count
-  const uint8_t* bp = S.seq + (rd.seq_off >> 1);   // seq_off is even: the read starts on a byte
-  const uint8_t* qp = S.qual + rd.seq_off;
-  const uint8_t* rp = S.ref + rd.start;
-  const int clip = rd.clip;
-  const int qend = clip + (int)span - 1;
-  for (uint32_t i0 = 0; i0 < span; i0 += 32) {
-    const uint32_t i = i0 + lane;
-    const bool act = i < span;
-    const int qpos = clip + (int)i;
-    uint32_t ob = 15, q = 0, rc = 'N';
-    if (act) {
-      const uint32_t byte = __ldg(bp + (qpos >> 1));
-      ob = (qpos & 1) ? (byte & 15u) : (byte >> 4);
-      q = __ldg(qp + qpos);
-      rc = __ldg(rp + i);
-    }
-    // the base after this trip's last one, read by every lane from one address
-    uint32_t ob32 = 15, q32 = 0, rc32 = 'N';
-    if (i0 + 32 < span) {
-      const int qn = clip + (int)i0 + 32;
-      const uint32_t byte = __ldg(bp + (qn >> 1));
-      ob32 = (qn & 1) ? (byte & 15u) : (byte >> 4);
-      q32 = __ldg(qp + qn);
-      rc32 = __ldg(rp + i0 + 32);
-    }
-    const uint32_t sob = __shfl_down_sync(0xFFFFFFFFu, ob, 1);
-    const uint32_t sq = __shfl_down_sync(0xFFFFFFFFu, q, 1);
-    const uint32_t src = __shfl_down_sync(0xFFFFFFFFu, rc, 1);
-    const uint32_t ob_n = lane == 31 ? ob32 : sob, q_n = lane == 31 ? q32 : sq, rc_n = lane == 31 ? rc32 : src;
-    // (1) the base at this column
-    const bool ev1 = act && ob != 15 && rc != 'N';
-    const bool base_ok = __popc(ob) == 1;
+  const uint32_t clip = rd.clip;
+  // this lane's bases are i = lane + 32 k, whose query positions all have the parity of clip + lane:
+  // the nibble shift is the lane's for the whole read (high nibble first)
+  const uint32_t sh = ((clip + (uint32_t)lane) & 1u) ? 0u : 4u;
+  const uint8_t* bp = S.seq + (rd.seq_off >> 1) + ((clip + (uint32_t)lane) >> 1);   // seq_off is even
+  const uint8_t* qp = S.qual + rd.seq_off + clip + (uint32_t)lane;
+  const uint8_t* rp = S.rcode + rd.start + (uint32_t)lane;
+  const uint32_t lo2 = rev ? 0u : 1u, hi2 = rev ? span - 1u : span;   // bases carrying a (2a) event
+  bool bad_base = false, bad_q = false;
+#pragma unroll 2
+  for (uint32_t i = (uint32_t)lane; i < span; i += 32, bp += 16, qp += 32, rp += 32) {
+    const uint32_t ob = (__ldg(bp) >> sh) & 15u;
+    const uint32_t q = __ldg(qp);
+    const uint32_t rc = __ldg(rp);                   // A,C,G,T = 0..3, N = 4
+    const bool valid = ob != 15u && rc < 4u;          // neither the read base nor the reference is N
+    const bool base_ok = (0x116u >> ob) & 1u;        // one-hot: A, C, G or T
     const bool q_ok = q < Q;
-    err |= (ev1 && !base_ok) ? kErrBase : 0u;
-    err |= (ev1 && base_ok && !q_ok) ? kErrCovariate : 0u;
-    const uint32_t oi = (uint32_t)(__ffs(ob) - 1) ^ flip, ri = ref_code(rc) ^ flip;
-    const uint32_t bin1 = (ev1 && base_ok && q_ok) ? rs + R * (ri + 5u * (oi + 5u * q)) : nbins + (uint32_t)lane;
-    // (2a) '..': the next base (forward) or this base again (reverse) with its quality
-    const uint32_t ob2 = rev ? ob : ob_n, q2 = rev ? q : q_n, rc2 = rev ? rc : rc_n;
-    const bool ev2 = act && qpos < qend && ob2 != 15 && rc2 != 'N';
-    err |= (ev2 && q2 >= Q) ? kErrCovariate : 0u;
-    const uint32_t bin2 = (ev2 && q2 < Q) ? rs + R * (24u + 25u * q2) : nbins + (uint32_t)lane;
-    atomicAdd(hist + bin1, 1u);
-    atomicAdd(hist + bin2, 1u);
+    const bool in2 = i >= lo2 && i < hi2;
+    bad_base |= valid && !base_ok;
+    bad_q |= valid && !q_ok && (base_ok || in2);
+    const uint32_t oi = (31u - __clz(ob)) ^ flip, ri = rc ^ flip;
+    const uint32_t q25 = q * 25u;
+    if (valid && base_ok && q_ok) atomicAdd(hist + (q25 + oi * 5u + ri) * R + rs, 1u);   // (ref, obs, q)
+    if (valid && q_ok && in2) atomicAdd(hist + (q25 + 24u) * R + rs, 1u);                 // ('.', '.', q)
   }
+  if (bad_base) err |= kErrBase;
+  if (bad_q) err |= kErrCovariate;
 }
 
 __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Batch B, const uint4* chunks, uint32_t n_chunks, unsigned int* next) {
@@ -507,6 +490,7 @@ __global__ void __launch_bounds__(1024) cov_hist_kernel(const __grid_constant__ 
 // 32-read batch in shared memory and walks only those that reach its tile, in BAM order, with the
 // base and quality loads of two reads in flight before either is consumed.
 constexpr uint32_t kColumnWarps = 8;
+constexpr uint32_t kColumnIlp = 4;      // common-path reads whose loads are in flight together
 
 // Per-thread shared-memory accumulators of the column pass, structure of arrays (thread t's values at
 // index t of each array: no bank conflicts): the screen bound B[5] and the redundant-read counts and
@@ -532,11 +516,28 @@ struct ColRare {
 };
 constexpr size_t kColRareBytes = 256 * (5 * 4 + 2 * 4 + 2 * 8);
 
+// Staged record of a common-path read for one tile: one aligned block (soft clips allowed), unique,
+// untrimmed, a known read file, in a tile with no failed-fit column.  What depends on the read alone
+// (its likelihood-class base, the addresses of its bases and qualities, its span) is computed once
+// per (read, tile) by the lane that stages it, so a lane's work per read base is the coverage test,
+// two byte loads, the class lookup and the sums.
+struct __align__(16) FastRead {
+  uint64_t qual;       // address of qual[seq_off + clip - start]: the quality at column c is at qual + c
+  uint64_t seq;        // address of the read's first packed base byte (seq_off is even)
+  uint32_t start;      // first column
+  uint32_t span_clip;  // reference span (low 16 bits) | leading soft clip << 16
+  uint32_t kbase;      // likelihood class of (MAPQ, read file, strand) at quality 0, observed base 0
+  uint32_t rev;        // 1 for a reverse-strand read
+};
+static_assert(sizeof(FastRead) == sizeof(DevRead), "a staging slot holds either form");
+
 template <bool FP64>
 __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant__ Batch Bt) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  // one 32-byte slot per read of the staged batch: its FastRead on the common path, else its DevRead
   DevRead* sh_rd = reinterpret_cast<DevRead*>(smem) + warp * 32;
+  FastRead* sh_fr = reinterpret_cast<FastRead*>(smem) + warp * 32;
   // accumulators only rare reads touch (mismatching or low-likelihood bases, redundant reads): one
   // shared-memory slot per thread, column by column, instead of registers held for the whole tile
   ColRare rare(smem + kColumnWarps * 32 * sizeof(DevRead), threadIdx.x);
@@ -564,6 +565,25 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
     float s4 = 0.0f, k4 = 0.0f;
     const uint2 rr = __ldg(S.tile_range + tile);
     const bool tile_fast = __all_sync(0xFFFFFFFFu, !failed);
+    // Kahan-compensated FP32 sums of one class entry (hypotheses 0-1, 2-3 packed, 4 scalar)
+    auto kahan = [&](const ulonglong2& v, float x4) {
+      const unsigned long long y01 = f32x2_sub(v.x, k01), y23 = f32x2_sub(v.y, k23);
+      const unsigned long long t01 = f32x2_add(s01, y01), t23 = f32x2_add(s23, y23);
+      k01 = f32x2_sub(f32x2_sub(t01, s01), y01);
+      k23 = f32x2_sub(f32x2_sub(t23, s23), y23);
+      s01 = t01; s23 = t23;
+      const float y4 = x4 - k4, t4 = s4 + y4;
+      k4 = (t4 - s4) - y4;
+      s4 = t4;
+    };
+    // screen bound  B_v = sum_i max(0, lp_i[v] - lp_i[ref]); zero unless the read's own base is not
+    // its most likely hypothesis or it differs from the reference
+    auto screen = [&](const ulonglong2& v, float x4) {
+      const float lp[5] = {f32x2_lo(v.x), f32x2_hi(v.x), f32x2_lo(v.y), f32x2_hi(v.y), x4};
+      const float lr = ref_idx == 0 ? lp[0] : ref_idx == 1 ? lp[1] : ref_idx == 2 ? lp[2] : ref_idx == 3 ? lp[3] : lp[4];
+#pragma unroll
+      for (int b = 0; b < 5; b++) rare.B(b) += fmaxf(0.0f, lp[b] - lr);
+    };
     // one scored read base of likelihood class k (identify_mutations.cpp:1640-1658)
     auto accumulate = [&](uint32_t k, int obs) {
       ++n;
@@ -574,61 +594,38 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       } else {
         const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(T.lp32 + (size_t)k * 8));
         const float2 w = __ldg(reinterpret_cast<const float2*>(T.lp32 + (size_t)k * 8 + 4));
-        {                                       // Kahan-compensated FP32 sums
-          const unsigned long long y01 = f32x2_sub(v.x, k01), y23 = f32x2_sub(v.y, k23);
-          const unsigned long long t01 = f32x2_add(s01, y01), t23 = f32x2_add(s23, y23);
-          k01 = f32x2_sub(f32x2_sub(t01, s01), y01);
-          k23 = f32x2_sub(f32x2_sub(t23, s23), y23);
-          s01 = t01; s23 = t23;
-          const float y4 = w.x - k4, t4 = s4 + y4;
-          k4 = (t4 - s4) - y4;
-          s4 = t4;
-        }
-        // screen bound  B_v = sum_i max(0, lp_i[v] - lp_i[ref]); zero unless the read's own
-        // base is not its most likely hypothesis or it differs from the reference
-        if (obs != ref_idx || w.y != 0.0f) {
-          const float lp[5] = {f32x2_lo(v.x), f32x2_hi(v.x), f32x2_lo(v.y), f32x2_hi(v.y), w.x};
-          const float lr = ref_idx == 0 ? lp[0] : ref_idx == 1 ? lp[1] : ref_idx == 2 ? lp[2] : ref_idx == 3 ? lp[3] : lp[4];
-#pragma unroll
-          for (int b = 0; b < 5; b++) rare.B(b) += fmaxf(0.0f, lp[b] - lr);
-        }
+        kahan(v, w.x);
+        if (obs != ref_idx || w.y != 0.0f) screen(v, w.x);
       }
     };
-    // One read of the batch as this lane sees it: pileup state at column c and the base / quality
-    // loads, issued for two reads before either is consumed.
-    struct Pend { uint32_t r; bool cov; Pile e; uint8_t base; uint8_t q; };
-    auto prep = [&](const DevRead& rd, uint32_t r, Pend& P) {
-      P.r = r;
-      P.cov = real && c >= rd.start && c < rd.end;
-      P.base = 15; P.q = 0;
-      if (!P.cov) return;
-      if (rd.flags & kSimple) { P.e.qpos = (int)(c - rd.start) + rd.clip; P.e.indel = 0; P.e.del = false; }
-      else resolve(S, rd, c, P.e);
-      const bool rev = rd.flags & kRev;
-      int qp = P.e.qpos;
-      if (P.e.del) qp += 1 - (int)rev;
-      if (qp < (int)rd.len) {
-        P.base = nib_at(S.seq, rd.seq_off + qp);            // the base itself, or the one checked for a deletion
-        P.q = __ldg(S.qual + rd.seq_off + qp);
-      }
-    };
-    auto consume = [&](const DevRead& rd, const Pend& P) {
-      if (!P.cov) return;
-      const Pile& e = P.e;
+    // One read as this lane sees it in the general case: the pileup state at column c (CIGAR walk,
+    // trims, deletions, redundancy) and the base / quality that state selects.
+    auto general = [&](const DevRead& rd, uint32_t r) {
+      if (!(real && c >= rd.start && c < rd.end)) return;
+      Pile e;
+      resolve(S, rd, c, e);
       const bool rev = rd.flags & kRev;
       const bool red = rd.flags & kRedundant;
+      int qp = e.qpos;
+      if (e.del) qp += 1 - (int)rev;
+      uint8_t base = 15, qv = 0;
+      if (qp < (int)rd.len) {
+        base = nib_at(S.seq, rd.seq_off + qp);            // the base itself, or the one checked for a deletion
+        qv = __ldg(S.qual + rd.seq_off + qp);
+      }
       if (failed) {
         // tabulate_position_coverage (identify_mutations.cpp:2218-2250)
-        if (e.del || P.base == 15) return;
+        if (e.del || base == 15) return;
         if (!red) { if (rev) ++ubot; else ++utop; }
-        else rare.redundant(rev, 1.0 / (double)__ldg(S.x1 + P.r));
+        else rare.redundant(rev, 1.0 / (double)__ldg(S.x1 + r));
         return;
       }
-      if (!e.del && P.base == 15) return;                     // N read base: not counted at all
+      // a discordant-pair candidate without a usable XP tag, at its first column (:1399-1416)
+      if ((rd.flags & kDpCand) && c == rd.start && dp_group_member(A.dp_rg, __ldg(S.rg + r))) return;
+      if (!e.del && base == 15) return;                       // N read base: not counted at all
       if (red) {
         uonly = false;
-        const double w = 1.0 / (double)__ldg(S.x1 + P.r);
-        rare.redundant(rev, w);
+        rare.redundant(rev, 1.0 / (double)__ldg(S.x1 + r));
         return;
       }
       if (rev) ++ubot; else ++utop;
@@ -638,109 +635,110 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
         return;
       if (e.del) {
         // the quality comes from the next base; the reference asserts if there is none
-        if (e.qpos + 1 - (int)rev >= (int)rd.len || P.base == 15) return;
+        if (e.qpos + 1 - (int)rev >= (int)rd.len || base == 15) return;
       }
       int obs = 4;
       if (!e.del) {
-        if (__popc(P.base) != 1) { local_err |= kErrBase; return; }     // not one of A, C, G, T
-        obs = __ffs(P.base) - 1;
+        if (__popc(base) != 1) { local_err |= kErrBase; return; }     // not one of A, C, G, T
+        obs = __ffs(base) - 1;
       }
-      const uint32_t q = P.q;
+      const uint32_t q = qv;
       const uint32_t rs = rd.rfile;
       if (q >= T.Q || rs >= T.R) { local_err |= kErrCovariate; return; }
       if (q < A.base_quality_cutoff) return;
       const uint32_t k = ((((uint32_t)rd.mapq_idx * T.R + rs) * 2u + (rev ? 1u : 0u)) * T.Q + q) * 5u + (uint32_t)obs;
       accumulate(k, obs);
     };
-    // the reads a lane sees on the common path: one aligned block, unique, untrimmed, a known read
-    // file, in a tile with no failed-fit target column
-    auto fast_read = [&](const DevRead& rd) {
-      return (rd.flags & (kSimple | kRedundant)) == kSimple && (rd.xl == kNoTag || rd.xl == 0) &&
-             (rd.xr == kNoTag || rd.xr == 0) && rd.rfile < T.R;
-    };
-    struct FastPend { bool cov; int qpos; uint32_t byte, q; };
-    auto fast_prep = [&](const DevRead& rd, FastPend& F) {
-      F.cov = real && c >= rd.start && c < rd.end;
-      F.qpos = (int)(c - rd.start) + rd.clip;
-      F.byte = 0; F.q = 0;
-      if (F.cov) {
-        F.byte = __ldg(S.seq + (rd.seq_off >> 1) + (F.qpos >> 1));
-        F.q = __ldg(S.qual + rd.seq_off + F.qpos);
+    // A common-path read at this lane's column, without branches: a lane the read does not cover (or
+    // whose base is N) loads nothing and adds zeros, so the warp runs one instruction stream per read.
+    // Loads first, so the loads of all the reads in flight are issued before any is consumed.
+    struct FastLd { uint32_t q, byte, sh; };
+    auto fast_load = [&](const FastRead& f, bool have, FastLd& L) {
+      const uint32_t d = c - f.start;
+      const bool cov = have && real && d < (f.span_clip & 0xFFFFu);
+      const uint32_t qpos = d + (f.span_clip >> 16);
+      L.sh = (qpos & 1u) ? 0u : 4u;                                    // high nibble first
+      L.q = 0; L.byte = 0xFFu;
+      if (cov) {
+        L.q = __ldg(reinterpret_cast<const uint8_t*>(f.qual) + c);
+        L.byte = __ldg(reinterpret_cast<const uint8_t*>(f.seq) + (qpos >> 1));
       }
     };
-    auto fast_consume = [&](const DevRead& rd, const FastPend& F) {
-      if (!F.cov) return;
-      const uint32_t base = (F.qpos & 1) ? (F.byte & 15u) : (F.byte >> 4);
-      if (base == 15) return;                                // N read base: not counted at all
-      const bool rev = rd.flags & kRev;
-      if (rev) ++ubot; else ++utop;
-      if (__popc(base) != 1) { local_err |= kErrBase; return; }
-      const int obs = __ffs(base) - 1;
-      if (F.q >= T.Q) { local_err |= kErrCovariate; return; }
-      if (F.q < A.base_quality_cutoff) return;
-      const uint32_t k = ((((uint32_t)rd.mapq_idx * T.R + rd.rfile) * 2u + (rev ? 1u : 0u)) * T.Q + F.q) * 5u + (uint32_t)obs;
-      accumulate(k, obs);
+    bool bad_base = false, bad_q = false;
+    auto fast_use = [&](const FastRead& f, const FastLd& L) {
+      const uint32_t base = (L.byte >> L.sh) & 15u;
+      const bool counted = base != 15u;                               // covered, and not an N read base
+      utop += (counted && !f.rev) ? 1u : 0u;
+      ubot += (counted && f.rev) ? 1u : 0u;
+      const bool base_ok = (0x116u >> base) & 1u;                     // one-hot: A, C, G or T
+      const bool q_ok = L.q < T.Q;
+      bad_base |= counted && !base_ok;
+      bad_q |= counted && base_ok && !q_ok;
+      const bool use = counted && base_ok && q_ok && L.q >= A.base_quality_cutoff;
+      const uint32_t obs = 31u - __clz(base);
+      if (FP64) {
+        if (use) accumulate(f.kbase + L.q * 5u + obs, (int)obs);
+      } else {
+        // the class entry when the base is scored, zeros otherwise (a Kahan step adding zero)
+        ulonglong2 v = make_ulonglong2(0ull, 0ull);
+        float2 w = make_float2(0.0f, 0.0f);
+        const uint32_t k = f.kbase + L.q * 5u + obs;
+        if (use) {
+          v = __ldg(reinterpret_cast<const ulonglong2*>(T.lp32 + (size_t)k * 8));
+          w = __ldg(reinterpret_cast<const float2*>(T.lp32 + (size_t)k * 8 + 4));
+        }
+        n += use ? 1u : 0u;
+        kahan(v, w.x);
+        if (use && ((int)obs != ref_idx || w.y != 0.0f)) screen(v, w.x);
+      }
     };
     for (uint32_t b0 = rr.x; b0 < rr.y; b0 += 32) {
       const uint32_t rl = b0 + lane;
-      bool rel = false;
+      bool rel = false, fast = false;
       if (rl < rr.y) {
         const DevRead mine = S.reads[rl];
         rel = !(mine.flags & kSkip) && mine.end > c0;
-        sh_rd[lane] = mine;
-      }
-      unsigned mask = __ballot_sync(0xFFFFFFFFu, rel);
-      __syncwarp();
-      while (mask) {                                  // reads in BAM order, up to four at a time
-        const int j1 = __ffs(mask) - 1;
-        mask &= mask - 1;
-        const int j2 = mask ? __ffs(mask) - 1 : -1;
-        if (j2 >= 0) mask &= mask - 1;
-        const DevRead rd1 = sh_rd[j1];
-        const DevRead rd2 = sh_rd[j2 >= 0 ? j2 : j1];
-        // warp-uniform choice: both reads on the common path, or the general pileup state
-        const bool f1 = tile_fast && fast_read(rd1), f2 = (j2 < 0) || (tile_fast && fast_read(rd2));
-        if (f1 && f2 && j2 >= 0 && mask) {
-          // two more common-path reads: four reads' base and quality loads in flight
-          const int j3 = __ffs(mask) - 1;
-          const unsigned rest = mask & (mask - 1);
-          const int j4 = rest ? __ffs(rest) - 1 : -1;
-          // records read in place from shared memory: four register copies would spill
-          const DevRead& r1 = sh_rd[j1];
-          const DevRead& r2 = sh_rd[j2];
-          const DevRead& r3 = sh_rd[j3];
-          const DevRead& r4 = sh_rd[j4 >= 0 ? j4 : j3];
-          if (fast_read(r3) && (j4 < 0 || fast_read(r4))) {
-            mask = j4 >= 0 ? (rest & (rest - 1)) : rest;
-            FastPend F1, F2, F3, F4;
-            fast_prep(r1, F1);
-            fast_prep(r2, F2);
-            fast_prep(r3, F3);
-            if (j4 >= 0) fast_prep(r4, F4);
-            fast_consume(r1, F1);
-            fast_consume(r2, F2);
-            fast_consume(r3, F3);
-            if (j4 >= 0) fast_consume(r4, F4);
-            continue;
-          }
-        }
-        if (f1 && f2) {
-          FastPend F1, F2;
-          fast_prep(rd1, F1);
-          if (j2 >= 0) fast_prep(rd2, F2);
-          fast_consume(rd1, F1);
-          if (j2 >= 0) fast_consume(rd2, F2);
+        fast = rel && tile_fast && (mine.flags & (kSimple | kRedundant | kDpCand)) == kSimple &&
+               (mine.xl == kNoTag || mine.xl == 0) && (mine.xr == kNoTag || mine.xr == 0) && mine.rfile < T.R;
+        if (fast) {
+          FastRead f;
+          const uint32_t rev = mine.flags & kRev;
+          f.qual = (uint64_t)(uintptr_t)S.qual + mine.seq_off + mine.clip - mine.start;
+          f.seq = (uint64_t)(uintptr_t)S.seq + (mine.seq_off >> 1);
+          f.start = mine.start;
+          f.span_clip = (mine.end - mine.start) | ((uint32_t)mine.clip << 16);
+          f.kbase = (((uint32_t)mine.mapq_idx * T.R + mine.rfile) * 2u + rev) * T.Q * 5u;
+          f.rev = rev;
+          sh_fr[lane] = f;
         } else {
-          Pend P1, P2;
-          prep(rd1, b0 + j1, P1);
-          if (j2 >= 0) {
-            prep(rd2, b0 + j2, P2);
-            consume(rd1, P1);
-            consume(rd2, P2);
-          } else {
-            consume(rd1, P1);
-          }
+          sh_rd[lane] = mine;
         }
+      }
+      unsigned fmask = __ballot_sync(0xFFFFFFFFu, fast);
+      unsigned gmask = __ballot_sync(0xFFFFFFFFu, rel && !fast);
+      __syncwarp();
+      // common-path reads in BAM order, kColumnIlp at a time
+      while (fmask) {
+        int j[kColumnIlp];
+        bool have[kColumnIlp];
+#pragma unroll
+        for (int u = 0; u < (int)kColumnIlp; u++) {
+          have[u] = fmask != 0;
+          j[u] = have[u] ? __ffs(fmask) - 1 : 0;
+          fmask &= fmask - 1;
+        }
+        FastLd L[kColumnIlp];
+#pragma unroll
+        for (int u = 0; u < (int)kColumnIlp; u++) fast_load(sh_fr[j[u]], have[u], L[u]);
+#pragma unroll
+        for (int u = 0; u < (int)kColumnIlp; u++) fast_use(sh_fr[j[u]], L[u]);
+      }
+      // the other reads of the batch in BAM order (redundant reads keep BAM order among themselves,
+      // so the per-column 1/X1 sums run in the reference's order)
+      while (gmask) {
+        const int j = __ffs(gmask) - 1;
+        gmask &= gmask - 1;
+        general(sh_rd[j], b0 + j);
       }
       __syncwarp();
     }
@@ -760,15 +758,16 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
           int best = 0;
           double score;
           if (FP64) {
+            double sb = S64[0];                 // the best sum kept in a register (no indexed array)
 #pragma unroll
-            for (int b = 1; b < 5; b++) if (S64[b] > S64[best]) best = b;
+            for (int b = 1; b < 5; b++) if (S64[b] > sb) { sb = S64[b]; best = b; }
             double off = -DBL_MAX;
 #pragma unroll
             for (int b = 0; b < 5; b++) if (b != best) off = fmax(off, S64[b]);
             double te = 0;
 #pragma unroll
             for (int b = 0; b < 5; b++) if (b != best) te += exp10(S64[b] - off);
-            score = S64[best] - (log10(te) + off) - A.log10_ref_len;
+            score = sb - (log10(te) + off) - A.log10_ref_len;
             cl.flags |= kCandidate;            // the plain form runs the EM wherever a base was scored
             if (best != ref_idx && score > 0) cl.flags |= kLikelyRa;
           } else {
@@ -777,11 +776,12 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
             double tot[5];
 #pragma unroll
             for (int b = 0; b < 5; b++) tot[b] = (double)s32[b] - (double)k32[b];
+            double tb = tot[0];
 #pragma unroll
-            for (int b = 1; b < 5; b++) if (tot[b] > tot[best]) best = b;
+            for (int b = 1; b < 5; b++) if (tot[b] > tb) { tb = tot[b]; best = b; }
             double d[5], off = -DBL_MAX;
 #pragma unroll
-            for (int b = 0; b < 5; b++) { d[b] = tot[b] - tot[best]; if (b != best) off = fmax(off, d[b]); }
+            for (int b = 0; b < 5; b++) { d[b] = tot[b] - tb; if (b != best) off = fmax(off, d[b]); }
             float te = 0.0f;
 #pragma unroll
             for (int b = 0; b < 5; b++) if (b != best) te += exp10f((float)(d[b] - off));
@@ -806,6 +806,8 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       A.cov[c] = cv;
       A.call[c] = cl;
     }
+    if (bad_base) local_err |= kErrBase;
+    if (bad_q) local_err |= kErrCovariate;
     if (local_err) { atomicOr(A.err, local_err); local_err = 0; }
   }
 }
@@ -979,6 +981,8 @@ __global__ void __launch_bounds__(128) im_candidate_kernel(const __grid_constant
     out.precision_decimal = J.I.precision_decimal; out.col_offset = col0;
     out.bq = A.bq; out.n_bq = A.n_bq; out.bq_cap = A.bq_cap;
     out.pool = A.pool; out.pool_used = A.pool_used; out.pool_cap = A.pool_cap;
+#pragma unroll
+    for (int i = 0; i < 8; i++) out.dp_rg[i] = J.I.dp_rg[i];
     const ColCall cl0 = J.I.call[c];
     score_candidate_column(S, T, out, c, (cl0.flags & (kCandidate | kRecompute)) != 0, (cl0.flags & kRecompute) != 0,
                            cl0, J.I.call, ents, A.scratch_per_warp, hist);
@@ -1024,13 +1028,16 @@ static int grid_for(uint32_t work, int per_block, int sms, int min_blocks_per_sm
 }
 
 // Reference characters of the padded column space: every byte of a target is one of A/C/G/T/N and
-// the only zero bytes are the one separator after each target.  Counts both kinds for the host.
-__global__ void ref_check_kernel(const uint8_t* ref, uint32_t n_cols, uint32_t* bad, uint32_t* zeros) {
+// the only zero bytes are the one separator after each target.  Counts both kinds for the host and
+// writes the column codes the pass-1 kernel reads.
+__global__ void ref_check_kernel(const uint8_t* ref, uint8_t* rcode, uint32_t n_cols, uint32_t* bad, uint32_t* zeros) {
   uint32_t nb = 0, nz = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_cols; i += gridDim.x * blockDim.x) {
     const uint8_t ch = __ldg(ref + i);
     nz += ch == 0;
-    nb += !(ch == 0 || ch == 'A' || ch == 'C' || ch == 'G' || ch == 'T' || ch == 'N');
+    const uint8_t code = ch == 'A' ? 0 : ch == 'C' ? 1 : ch == 'G' ? 2 : ch == 'T' ? 3 : ch == 'N' ? 4 : ch == 0 ? 5 : 6;
+    nb += code == 6;
+    rcode[i] = code;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -1042,8 +1049,9 @@ __global__ void ref_check_kernel(const uint8_t* ref, uint32_t n_cols, uint32_t* 
     if (nz) atomicAdd(zeros, nz);
   }
 }
-cudaError_t launch_ref_check(const uint8_t* ref, uint32_t n_cols, uint32_t* bad, uint32_t* zeros, int sms, cudaStream_t st) {
-  ref_check_kernel<<<sms * 4, 256, 0, st>>>(ref, n_cols, bad, zeros);
+cudaError_t launch_ref_check(const uint8_t* ref, uint8_t* rcode, uint32_t n_cols, uint32_t* bad, uint32_t* zeros, int sms,
+                             cudaStream_t st) {
+  ref_check_kernel<<<sms * 4, 256, 0, st>>>(ref, rcode, n_cols, bad, zeros);
   return cudaGetLastError();
 }
 cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st) {

@@ -23,6 +23,7 @@ struct RawSoA {
   const uint16_t* n_cigar;
   const uint32_t* cigar;
   const uint8_t* xj;         // XJ tag present (may be null: no record has one)
+  const uint8_t* xp;         // BSQ_XP_* pair orientation (may be null: no record has an XP tag)
   const uint32_t* tpoff;     // padded target offsets
   const uint8_t* called;     // per target: in the pileup set
   uint32_t n;
@@ -42,8 +43,10 @@ struct PackOut {
 };
 
 cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st);
-// Counts reference bytes outside A/C/G/T/N/separator into *bad and zero bytes into *zeros.
-cudaError_t launch_ref_check(const uint8_t* ref, uint32_t n_cols, uint32_t* bad, uint32_t* zeros, int sms, cudaStream_t st);
+// Counts reference bytes outside A/C/G/T/N/separator into *bad and zero bytes into *zeros, and writes
+// each column's code (A,C,G,T = 0..3, N = 4, separator = 5, other = 6) to rcode.
+cudaError_t launch_ref_check(const uint8_t* ref, uint8_t* rcode, uint32_t n_cols, uint32_t* bad, uint32_t* zeros, int sms,
+                             cudaStream_t st);
 cudaError_t launch_mapq_index(DevRead* reads, const uint8_t* mapq, const uint8_t* map, uint32_t n, cudaStream_t st);
 cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t n_tiles, uint32_t maxspan,
                               uint2* tile_range, uint32_t* max_tile_reads, cudaStream_t st);

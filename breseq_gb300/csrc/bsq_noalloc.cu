@@ -9,6 +9,7 @@
 //     [0, 16 MiB)            per-warp gather lists of covering reads (uint4 each)
 //     [16 MiB, +2.75 MiB)    likelihood class table (lp[5], r[5], max per class; up to 32768 classes)
 //     [.., +256 KiB)         log10 error table (up to 32768 entries)
+//     [.., +256 KiB)         the caller's deletion propagation cutoffs (up to 32768 targets)
 //     [.., +256 B)           work counter and error word
 //
 // Host code must not take the array's name as a device address: the address is fetched with
@@ -16,7 +17,13 @@
 // on it.  Every call shares the array and finds the previous call's contents there; the counters are
 // cleared at the start of each call, and calls that overlap on the GPU (two streams, two threads)
 // race on it.
+//
+// The likelihood-class table is computed here on the device (CUDA's pow / log10, each within 2 ulp),
+// while bsq_identify_mutations computes it on the host with the C library's: the scores of the two
+// agree to ~1e-12, not bit for bit.
 #include <cuda_runtime.h>
+
+#include <atomic>
 
 #include "bsq_common.h"
 #include "bsq_device.cuh"
@@ -31,21 +38,25 @@ namespace {
 constexpr size_t kGatherBytes = 16u << 20;
 constexpr size_t kClassBytes = (size_t)kNoAllocMaxClasses * 11 * sizeof(double);
 constexpr size_t kTableBytes = (size_t)kNoAllocMaxTable * sizeof(double);
-constexpr size_t kCounterOff = kGatherBytes + kClassBytes + kTableBytes;
+constexpr size_t kCutOff = kGatherBytes + kClassBytes + kTableBytes;
+constexpr size_t kCutBytes = (size_t)kNoAllocMaxTargets * sizeof(double);
+constexpr size_t kCounterOff = kCutOff + kCutBytes;
 constexpr size_t kNoAllocBytes = 20u << 20;
 static_assert(kCounterOff + 256 <= kNoAllocBytes, "no-allocation scratch layout overflows its array");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kMaxDevices = 64;
-void* g_scratch_addr[kMaxDevices];  // device address of g_noalloc_scratch, per device
+// device address of g_noalloc_scratch, per device; several host threads may look it up at once
+std::atomic<void*> g_scratch_addr[kMaxDevices];
 
 struct NoAllocArgs {
   const uint32_t* tid;
   const uint32_t* pos0;
   uint32_t n;
   unsigned int* next;
-  const uint8_t* failed;      // per target: coverage fit failed, no RA scored there
+  const double* prop_cutoff;  // per target deletion propagation cutoff: < 0, the coverage fit failed and
+                              // no RA is scored there (identify_mutations.cpp:1317-1333)
   uint4* gather;
   uint32_t per_warp;
   uint32_t n_warps;           // warps that own a gather list; the launch may round up past it
@@ -109,7 +120,7 @@ __global__ void __launch_bounds__(128) noalloc_positions_kernel(DevSample S, Cla
       if (lane == 0) atomicOr(out.err, kErrBounds);
       continue;
     }
-    if (A.failed[t]) continue;
+    if (A.prop_cutoff[t] < 0.0) continue;
     score_candidate_column(S, T, out, S.tpoff[t] + p0, true, false, none, nullptr, ents, A.per_warp, hist);
     __syncwarp();
   }
@@ -119,13 +130,14 @@ __global__ void __launch_bounds__(128) noalloc_positions_kernel(DevSample S, Cla
 
 cudaError_t noalloc_scratch_setup(int device, void** addr) {
   if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
-  if (!g_scratch_addr[device]) {
-    void* p = nullptr;
+  void* p = g_scratch_addr[device].load(std::memory_order_acquire);
+  if (!p) {
+    // two threads may both look it up; they store the same address
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    g_scratch_addr[device] = p;
+    g_scratch_addr[device].store(p, std::memory_order_release);
   }
-  *addr = g_scratch_addr[device];
+  *addr = p;
   return cudaSuccess;
 }
 
@@ -138,8 +150,11 @@ cudaError_t launch_noalloc_positions(void* scratch, const DevSample& S, const No
   double* table = reinterpret_cast<double*>(base + kGatherBytes + kClassBytes);
   unsigned int* counters = reinterpret_cast<unsigned int*>(base + kCounterOff);   // [0] next, [1] err
   const size_t ntab = (size_t)J.R * 25 * J.Q;
+  double* cut = reinterpret_cast<double*>(base + kCutOff);
   cudaError_t e = cudaMemcpyAsync(table, J.log10_table, ntab * sizeof(double), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(cut, J.prop_cutoff, (size_t)J.n_targets * sizeof(double), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return e;
   if ((e = cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned int), st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(J.n_ra, 0, sizeof(unsigned int), st)) != cudaSuccess) return e;
   ClassArgs CA;
@@ -157,8 +172,9 @@ cudaError_t launch_noalloc_positions(void* scratch, const DevSample& S, const No
   out.col_offset = 0;
   out.bq = nullptr; out.n_bq = nullptr; out.bq_cap = 0;     // bounds inline: no extra device memory
   out.pool = nullptr; out.pool_used = nullptr; out.pool_cap = 0;
+  for (int i = 0; i < 8; i++) out.dp_rg[i] = J.dp_rg[i];
   NoAllocArgs A;
-  A.tid = J.tid; A.pos0 = J.pos0; A.n = J.n_positions; A.next = counters; A.failed = J.failed;
+  A.tid = J.tid; A.pos0 = J.pos0; A.n = J.n_positions; A.next = counters; A.prop_cutoff = cut;
   A.gather = reinterpret_cast<uint4*>(base); A.per_warp = J.per_warp; A.n_warps = J.n_warps;
   const uint32_t warps = J.n_warps;
   if (J.n_positions) {

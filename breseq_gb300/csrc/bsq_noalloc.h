@@ -11,6 +11,7 @@ namespace bsq {
 constexpr uint32_t kNoAllocMaxClasses = 32768;       // likelihood classes (MAPQ values x R x 2 x Q x 5)
 constexpr uint32_t kNoAllocMaxTable = 32768;         // R * 25 * Q error-table entries
 constexpr uint64_t kNoAllocGatherEntries = (16u << 20) / 16;   // uint4 gather entries shared by all warps
+constexpr uint32_t kNoAllocMaxTargets = 32768;       // deletion propagation cutoffs kept in the scratch
 
 struct NoAllocJob {
   const double* log10_table;    // host
@@ -20,7 +21,9 @@ struct NoAllocJob {
   const uint32_t* tid;          // device, caller's
   const uint32_t* pos0;         // device, caller's
   uint32_t n_positions;
-  const uint8_t* failed;        // device, per target
+  const double* prop_cutoff;    // host, caller's: per target deletion propagation cutoff (< 0: fit failed)
+  uint32_t n_targets;
+  uint32_t dp_rg[8];            // discordant-pair read groups (ImArgs::dp_rg)
   bsq_ra_raw* ra;               // device, caller's
   uint32_t ra_cap;
   unsigned int* n_ra;           // device, caller's

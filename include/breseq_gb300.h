@@ -170,6 +170,16 @@ typedef struct bsq_im_params {
     const double* deletion_propagation_cutoff;  /* [n_targets] */
     const double* deletion_seed_cutoff;         /* [n_targets] */
     int32_t  precision;                    /* BSQ_PRECISION_* */
+    /* Discordant-pair groups of the identify_mutations pileup (identify_mutations.cpp:883-911):
+     * dp_group[g] >= 0 for each dense read group g that is a paired read-file set with a paired
+     * mapping-distance fit, -1 otherwise; n_read_groups entries, at most 256 of them DP groups.
+     * 0 / NULL: no DP group.  At a read's first aligned column, insert position 0, breseq's
+     * per-read loop leaves out (`continue`, :1399-1416) a primary, mapped, paired read of a DP
+     * group that is not a proper pair, has a mapped mate, and has no XP tag or one other than
+     * FR / RF / FF; the passes do the same (the record's XP comes from bsq_read_soa.xp, none
+     * when that is NULL). */
+    uint32_t n_read_groups;
+    const int32_t* dp_group;
 } bsq_im_params;
 
 /* One RA evidence item with raw (unformatted) values; identify_mutations.cpp:1836-1910. */
@@ -738,7 +748,11 @@ typedef struct bsq_ra_raw {
  * the reference, which scores every position of every target in one pileup.  It is for callers that
  * cannot call cudaMalloc while they run: a serving loop with jobs in flight on other streams, where
  * cudaMalloc/cudaFree may synchronize the device and stall them, or a program that has handed all
- * of HBM to its own arena.  The scoring is the same as bsq_identify_mutations' candidate scoring.
+ * of HBM to its own arena.  The scoring is bsq_identify_mutations' candidate scoring (FP64 sums, EM,
+ * bounds), with one difference: the likelihood-class table is computed on the device with CUDA's pow
+ * and log10 (within 2 ulp) rather than on the host with the C library's, so scores and frequencies
+ * agree with bsq_identify_mutations' to about 1e-12, not bit for bit.  The call reads the deletion
+ * propagation cutoffs from `p` and changes nothing in the sample.
  *
  * d_tid / d_pos0 (0-based positions) are device arrays of n_positions entries.  d_ra (ra_capacity
  * records), d_n_ra (one counter, set by the call) and d_qhist (ra_capacity x 2 x n_quality counters:
@@ -748,8 +762,8 @@ typedef struct bsq_ra_raw {
  *
  * Scratch: one fixed 20 MiB device array in the library, held by every GPU that loads it until the
  * process exits.  Limits: n_read_files x 25 x n_quality <= 32768, (distinct MAPQ values) x
- * n_read_files x 2 x n_quality x 5 <= 32768 likelihood classes; larger tables are rejected with
- * BSQ_ERR_SIZE.  The first call on a device fetches the array's device address (cudaGetSymbolAddress),
+ * n_read_files x 2 x n_quality x 5 <= 32768 likelihood classes, at most 32768 targets; larger inputs
+ * are rejected with BSQ_ERR_SIZE.  The first call on a device fetches the array's device address (cudaGetSymbolAddress),
  * so make that first call before any stream capture.  All calls share the array and each clears its
  * counters on entry: calls that overlap on the GPU (other threads, other contexts on the same device)
  * race on it and must be serialized by the caller.  Returns BSQ_ERR_SIZE, with *d_n_ra holding the

@@ -471,6 +471,21 @@ struct AlleleModel {
   }
 };
 
+// The discordant-pair enter step of identify_mutations_pileup::pileup_callback
+// (identify_mutations.cpp:1399-1416) ends the per-read loop (`continue`) for a read at its first
+// column, insert position 0, when it is paired, mapped, not a proper pair, neither secondary nor
+// supplementary, with a mapped mate, in a read group that has a DP group, and has no XP tag or an
+// orientation other than FR / RF / FF.
+inline bool dp_skip_at(const bsq_read_soa* rd, const bsq_im_params* p, uint64_t r, int64_t col) {
+  if ((int64_t)rd->pos[r] != col) return false;
+  const uint16_t f = rd->flag[r];
+  if (!(f & 0x1) || (f & 0x4) || (f & 0x2) || (f & (0x100 | 0x800 | 0x8))) return false;
+  const uint32_t g = rd->read_group[r];
+  if (g >= p->n_read_groups || p->dp_group[g] < 0) return false;      // dp_group_for(p, *i) < 0
+  const uint8_t xp = rd->xp ? rd->xp[r] : (uint8_t)BSQ_XP_NONE;
+  return xp != BSQ_XP_FR && xp != BSQ_XP_RF && xp != BSQ_XP_FF;
+}
+
 struct Pass2 {
   const Data& d;
   const bsq_im_params* p;
@@ -723,6 +738,7 @@ struct SlotScorer {
       const uint64_t r = act[ii];
       const Pile& e = piles[ii];
       const ReadInfo& ri = d.info[r];
+      if (insert_count == 0 && dp_skip_at(rd, p, r, c)) continue;
       int indel = e.indel;
       if (indel < 0) indel = 0;
       if (e.is_del) indel = -1;

@@ -100,8 +100,9 @@ def counts_to_log10_prob(counts, R, Q):
     return out
 
 
-def default_im_params(sample, polymorphism_mode=False, prop_cutoff=None, seed_cutoff=None):
-    """Settings defaults of breseq (src/breseq/settings.cpp:857-950, 1335)."""
+def default_im_params(sample, polymorphism_mode=False, prop_cutoff=None, seed_cutoff=None, dp_group=()):
+    """Settings defaults of breseq (src/breseq/settings.cpp:857-950, 1335); dp_group: the DP group of
+    each read group (identify_mutations.cpp:883-911), empty for none."""
     T = len(sample.target_offset) - 1
     total = float(sample.target_offset[-1])
     prop = np.broadcast_to(np.asarray(5.0 if prop_cutoff is None else prop_cutoff, dtype=np.float64), (T,)).copy()
@@ -112,14 +113,18 @@ def default_im_params(sample, polymorphism_mode=False, prop_cutoff=None, seed_cu
                 polymorphism_precision_places=8 if polymorphism_mode else 3,
                 skip_missing_coverage_prediction=0, log10_ref_length=float(np.log10(total)),
                 deletion_propagation_cutoff=np.ascontiguousarray(prop, dtype=np.float64),
-                deletion_seed_cutoff=np.ascontiguousarray(seed, dtype=np.float64), precision=0)
+                deletion_seed_cutoff=np.ascontiguousarray(seed, dtype=np.float64), precision=0,
+                dp_group=np.ascontiguousarray(list(dp_group), dtype=np.int32))
 
 
 def make_im_params(d):
-    keep = [d["deletion_propagation_cutoff"], d["deletion_seed_cutoff"]]
-    p = abi.ImParams(**{k: v for k, v in d.items() if k not in ("deletion_propagation_cutoff", "deletion_seed_cutoff")},
+    dpg = np.ascontiguousarray(d.get("dp_group", np.zeros(0, np.int32)), dtype=np.int32)
+    keep = [d["deletion_propagation_cutoff"], d["deletion_seed_cutoff"], dpg if len(dpg) else np.full(1, -1, np.int32)]
+    skip = ("deletion_propagation_cutoff", "deletion_seed_cutoff", "dp_group")
+    p = abi.ImParams(**{k: v for k, v in d.items() if k not in skip},
                      deletion_propagation_cutoff=abi.ptr(keep[0], C.c_double),
-                     deletion_seed_cutoff=abi.ptr(keep[1], C.c_double))
+                     deletion_seed_cutoff=abi.ptr(keep[1], C.c_double),
+                     n_read_groups=len(dpg), dp_group=abi.ptr(keep[2], C.c_int32))
     return p, keep
 
 

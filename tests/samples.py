@@ -188,3 +188,23 @@ def softclip_known():
         ("t1", 40, 1, 3, 8, 2, "AGGT"),
     ]
     return from_records([("t1", t1), ("s0", s0)], reads), expected
+
+
+@functools.lru_cache(maxsize=None)
+def dp_skip_sample():
+    """Paired-end sample with discordant pairs at 10 sites and a 2% background, half of the discordant
+    reads without an XP tag: the reads breseq's identify_mutations pileup leaves out of their first
+    column when their read group has a discordant-pair group (identify_mutations.cpp:1399-1416)."""
+    c = synth.config_ecoli(seed=23, scale=0.01, coverage=30.0)
+    return synth.with_pairs(synth.simulate(c), seed=4, discordant_sites=10, background_discordant=0.02,
+                            no_xp_fraction=0.5)
+
+
+def dp_skip_reads(s, dp_group):
+    """Indices of the records the discordant-pair enter step ends at their first column."""
+    import numpy as np
+    f = s.flag.astype(np.int64)
+    rg = s.read_group.astype(np.int64)
+    member = np.array([g < len(dp_group) and dp_group[g] >= 0 for g in rg], dtype=bool)
+    cand = ((f & 0x1) != 0) & ((f & 0x4) == 0) & ((f & 0x2) == 0) & ((f & (0x100 | 0x800 | 0x8)) == 0)
+    return np.nonzero(cand & member & (s.xp > 2) & ((f & 0x704) == 0))[0]

@@ -212,3 +212,29 @@ def test_reference_characters_checked_at_load(scorer, bad):
     with pytest.raises(_lib.BsqError) as e:
         scorer.load_sample(dataclasses.replace(s, ref_seq=ref))
     assert e.value.code == -3
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32c"])
+def test_dp_group_first_column_skip(scorer, oracle_lib, precision):
+    """A non-proper paired read without a usable XP tag in a discordant-pair read group is left out of
+    its first column at insert position 0 (identify_mutations.cpp:1399-1416): RA items, intervals and
+    per-position arrays against the oracle, with DP groups on every read group."""
+    from breseq_gb300.api import ImSettings
+    s = samples.dp_skip_sample()
+    dp = tuple(0 for _ in range(int(s.read_group.max()) + 1))
+    assert len(samples.dp_skip_reads(s, dp)) > 20
+    ec = po.error_count(s)
+    tab = po.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
+    im_o = po.identify(s, tab, po.default_im_params(s, dp_group=dp))
+    plain = po.identify(s, tab, po.default_im_params(s))
+    assert not np.array_equal(plain["positions"]["unique_top"], im_o["positions"]["unique_top"])
+    sid = scorer.load_sample(s)
+    try:
+        for positions in (True, False):
+            im_g = scorer.identify_mutations(sid, tab, ImSettings(dp_group=dp), precision=precision, positions=positions)
+            problems = compare.compare_ra(im_g["ra"], im_o["ra"]) + compare.compare_intervals(im_g, im_o)
+            if positions:
+                problems += compare.compare_positions(im_g["positions"], im_o["positions"])
+            assert not problems, "\n".join(problems[:20])
+    finally:
+        scorer.free_sample(sid)
