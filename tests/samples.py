@@ -208,3 +208,30 @@ def dp_skip_reads(s, dp_group):
     member = np.array([g < len(dp_group) and dp_group[g] >= 0 for g in rg], dtype=bool)
     cand = ((f & 0x1) != 0) & ((f & 0x4) == 0) & ((f & 0x2) == 0) & ((f & (0x100 | 0x800 | 0x8)) == 0)
     return np.nonzero(cand & member & (s.xp > 2) & ((f & 0x704) == 0))[0]
+
+
+@functools.lru_cache(maxsize=None)
+def ecoli_quarter():
+    """The E. coli-scale clonal workload's shape at 0.25x genome length with its full coverage: 1.16 Mb +
+    25 kb + 15 kb targets, five 1.3-kb repeats, 2 x 100x paired-end 150-bp reads (0.24 G read-bases)."""
+    return synth.simulate(synth.config_ecoli(seed=61, scale=0.25))
+
+
+@functools.lru_cache(maxsize=None)
+def population_deep():
+    """The 1000x population workload's shape at 0.05x genome length: paired-end 150-bp reads at 1000x,
+    variants at log-uniform frequencies, strand-biased and low-quality sites (0.26 G read-bases)."""
+    return synth.simulate(synth.config_population(seed=62, scale=0.05))
+
+
+def sample_digest(s):
+    """SHA-256 of a sample's reference and records: the golden files were made from exactly this."""
+    import hashlib
+    import numpy as np
+    h = hashlib.sha256()
+    for a in (s.ref_seq, s.target_offset, s.tid, s.pos, s.flag, s.mapq, s.x1, s.xl, s.xr, s.read_file, s.read_group,
+              s.l_qseq, s.seq_off, s.cigar_off, s.n_cigar, s.cigar, s.seq, s.qual):
+        h.update(np.ascontiguousarray(a).tobytes())
+    if s.xp is not None:
+        h.update(np.ascontiguousarray(s.xp).tobytes())
+    return h.hexdigest()
