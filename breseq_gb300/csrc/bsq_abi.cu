@@ -603,7 +603,7 @@ static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_p
     if (!smp[j]) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
     if (P[j].n_read_files == 0 || P[j].n_read_files > 255 || P[j].n_quality == 0 || P[j].n_quality > 256)
       return fail(ctx, BSQ_ERR_INVALID, "covariate dimensions out of range");
-    if ((size_t)P[j].n_read_files * 25 * P[j].n_quality * 4 > kEcMaxHistBytes)
+    if ((size_t)P[j].n_read_files * 29 * P[j].n_quality * 4 > kEcMaxHistBytes)   // histogram + combined counts
       return fail(ctx, BSQ_ERR_SIZE, "covariate table larger than the shared-memory histogram of the pass-1 kernel");
   }
   CK(cudaSetDevice(ctx->device));

@@ -200,11 +200,23 @@ Resident& resident(const breseq::Settings& settings, const std::string& bam, con
   return out;
 }
 
-// "read_set=R,obs_base,ref_base,quality=Q", the pipeline's covariates (breseq_cmdline.cpp:2304)
+// The pipeline's covariates, read_set=R, obs_base, ref_base and quality=Q in any order
+// (breseq_cmdline.cpp:2304 passes "read_set=R,obs_base,ref_base,quality=Q"; the error_rates.tab
+// header lists them in the covariate enum's order, error_count.h:69)
 void parse_covariates(const std::string& cov, uint32_t& R, uint32_t& Q) {
   unsigned r = 0, q = 0;
-  char tail;
-  if (sscanf(cov.c_str(), "read_set=%u,obs_base,ref_base,quality=%u%c", &r, &q, &tail) != 2 || r == 0 || q == 0)
+  int seen = 0;
+  std::istringstream in(cov);
+  std::string tok;
+  while (std::getline(in, tok, ',')) {
+    char tail;
+    if (sscanf(tok.c_str(), "read_set=%u%c", &r, &tail) == 1) seen |= 1;
+    else if (sscanf(tok.c_str(), "quality=%u%c", &q, &tail) == 1) seen |= 2;
+    else if (tok == "obs_base") seen |= 4;
+    else if (tok == "ref_base") seen |= 8;
+    else seen |= 16;
+  }
+  if (seen != 15 || r == 0 || q == 0)
     die("Unsupported covariates (the scoring path takes read_set=R,obs_base,ref_base,quality=Q): " + cov);
   R = r;
   Q = q;

@@ -281,8 +281,11 @@ __device__ __forceinline__ float f32x2_hi(unsigned long long x) { return __uint_
 // reverse read its own.  Both events of base j therefore test only base j's own values: (1) always,
 // and (2a) on behalf of base j - 1 (forward, j >= 1) or of base j itself (reverse, j below the last).
 // One lane per base, no neighbour exchange; reference characters are A/C/G/T/N (checked at load).
-__device__ __forceinline__ void ec_simple_read(const DevSample& S, const EcArgs& A, uint32_t* hist, const DevRead& rd,
-                                               uint32_t span, int lane, uint32_t& err) {
+// Most bases match the reference and carry a (2a) event: their two events (rs, b, b, q) and
+// (rs, '.', '.', q) are counted with one shared atomic in comb[(q * 4 + b) * R + rs], which the chunk's
+// flush adds to both bins.
+__device__ __forceinline__ void ec_simple_read(const DevSample& S, const EcArgs& A, uint32_t* hist, uint32_t* comb,
+                                               const DevRead& rd, uint32_t span, int lane, uint32_t& err) {
   const bool rev = rd.flags & kRev;
   const uint32_t rs = rd.rfile, R = A.R, Q = A.Q;
   if (rs >= R) { err |= kErrCovariate; return; }
@@ -309,8 +312,12 @@ __device__ __forceinline__ void ec_simple_read(const DevSample& S, const EcArgs&
     bad_q |= valid && !q_ok && (base_ok || in2);
     const uint32_t oi = (31u - __clz(ob)) ^ flip, ri = rc ^ flip;
     const uint32_t q25 = q * 25u;
-    if (valid && base_ok && q_ok) atomicAdd(hist + (q25 + oi * 5u + ri) * R + rs, 1u);   // (ref, obs, q)
-    if (valid && q_ok && in2) atomicAdd(hist + (q25 + 24u) * R + rs, 1u);                 // ('.', '.', q)
+    const bool both = valid && base_ok && q_ok && in2 && oi == ri;
+    if (both) atomicAdd(comb + (q * 4u + ri) * R + rs, 1u);
+    else {
+      if (valid && base_ok && q_ok) atomicAdd(hist + (q25 + oi * 5u + ri) * R + rs, 1u);   // (ref, obs, q)
+      if (valid && q_ok && in2) atomicAdd(hist + (q25 + 24u) * R + rs, 1u);                 // ('.', '.', q)
+    }
   }
   if (bad_base) err |= kErrBase;
   if (bad_q) err |= kErrCovariate;
@@ -328,8 +335,9 @@ __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Ba
   const uint4 ch = chunks[ci];                 // x = job, y = first read, z = end read
   const DevSample& S = B.jobs[ch.x].S;
   const EcArgs& A = B.jobs[ch.x].E;
-  const uint32_t nbins = A.R * 25u * A.Q;
-  for (uint32_t i = threadIdx.x; i < nbins + 32; i += blockDim.x) sh_hist[i] = 0;
+  const uint32_t nbins = A.R * 25u * A.Q, ncomb = A.R * 4u * A.Q;
+  uint32_t* sh_comb = sh_hist + nbins;
+  for (uint32_t i = threadIdx.x; i < nbins + ncomb; i += blockDim.x) sh_hist[i] = 0;
   __syncthreads();
   uint32_t err = 0;
   uint32_t done = 0;
@@ -347,7 +355,7 @@ __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Ba
           A.qs_flag[(size_t)(rd.flags & kRev) * S.n_cols + rd.start] = 1;
       }
       if (red || !A.do_errors) continue;
-      ec_simple_read(S, A, sh_hist, rd, span, lane, err);
+      ec_simple_read(S, A, sh_hist, sh_comb, rd, span, lane, err);
       done += span;
     } else {
       // the CIGAR walk of htslib's pileup (resolve_cigar2): M/=/X blocks carry their read bases, the
@@ -400,6 +408,16 @@ __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Ba
           y += (int)len;
         }
       }
+    }
+  }
+  __syncthreads();
+  // combined counts of (rs, b, b, q) + (rs, '.', '.', q) into both bins
+  for (uint32_t i = threadIdx.x; i < ncomb; i += blockDim.x) {
+    const uint32_t v = sh_comb[i];
+    if (v) {
+      const uint32_t rs = i % A.R, qb = i / A.R, b = qb & 3u, q = qb >> 2;
+      atomicAdd(sh_hist + (q * 25u + b * 6u) * A.R + rs, v);
+      atomicAdd(sh_hist + (q * 25u + 24u) * A.R + rs, v);
     }
   }
   __syncthreads();
@@ -1083,14 +1101,16 @@ int ec_grid(uint32_t n_chunks, int sms, uint32_t blocks_per_sm) {
 int column_grid(uint32_t total_tiles, int sms, uint32_t blocks_per_sm) {
   return grid_for(total_tiles, kColumnWarps, sms, (int)std::max<uint32_t>(1, blocks_per_sm));
 }
+// Shared memory of the pass-1 kernel: the R x 25 x Q histogram and the R x 4 x Q combined counts.
+static size_t ec_smem(uint32_t max_bins) { return (size_t)(max_bins + max_bins / 25 * 4) * sizeof(uint32_t); }
 cudaError_t prepare_ec(uint32_t max_bins) {
-  const size_t smem = (size_t)(max_bins + 32) * sizeof(uint32_t);
+  const size_t smem = ec_smem(max_bins);
   if (smem <= 48 * 1024) return cudaSuccess;
   return cudaFuncSetAttribute(ec_read_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, unsigned int* next, uint32_t max_bins,
                       int grid, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1) {
-  const size_t smem = (size_t)(max_bins + 32) * sizeof(uint32_t);   // + one discard slot per lane
+  const size_t smem = ec_smem(max_bins);
   cudaError_t e = cudaMemsetAsync(next, 0, sizeof(unsigned int), st);
   if (e != cudaSuccess) return e;
   if (main0 && (e = record_event(main0, st)) != cudaSuccess) return e;

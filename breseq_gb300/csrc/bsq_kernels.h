@@ -50,7 +50,8 @@ cudaError_t launch_ref_check(const uint8_t* ref, uint8_t* rcode, uint32_t n_cols
 cudaError_t launch_mapq_index(DevRead* reads, const uint8_t* mapq, const uint8_t* map, uint32_t n, cudaStream_t st);
 cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t n_tiles, uint32_t maxspan,
                               uint2* tile_range, uint32_t* max_tile_reads, cudaStream_t st);
-// Largest covariate table the pass-1 kernel keeps in shared memory (R*25*Q 32-bit bins).
+// Largest covariate table the pass-1 kernel keeps in shared memory (R*25*Q 32-bit bins, plus R*4*Q
+// combined match counts).
 constexpr size_t kEcMaxHistBytes = 200 * 1024;
 
 // Grid sizes from the tuning knobs (resident blocks per SM, capped by the work).

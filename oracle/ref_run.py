@@ -23,10 +23,11 @@ def write_fasta(s, path):
 
 
 def write_inputs(s, d, polymorphism=False, prop_cutoff=None, seed_cutoff=None, copy_number=False, classify=False,
-                 pmdd=()) -> tuple:
+                 pmdd=(), fast_bam=False) -> tuple:
     """reference.bam, reference.fasta, an empty out/ folder and config.txt in folder d; returns the
     config path and the output folder.  pmdd: (read group, median, mad) of the paired-mapping-distance
-    fits that make discordant-pair groups."""
+    fits that make discordant-pair groups.  fast_bam: the vectorised BAM writer (same records; its read
+    names are placeholders, so only for samples without pair annotations)."""
     from breseq_gb300 import synth
     T = len(s.target_names)
     prop = np.broadcast_to(np.asarray(5.0 if prop_cutoff is None else prop_cutoff, dtype=np.float64), (T,))
@@ -35,7 +36,7 @@ def write_inputs(s, d, polymorphism=False, prop_cutoff=None, seed_cutoff=None, c
     _, _, counts = synth.bam_groups(s)
     bam = os.path.join(d, "reference.bam")
     with open(bam, "wb") as f:
-        f.write(synth.bam_bytes(s, rg_tags=True))
+        f.write(synth.bam_bytes_fast(s) if fast_bam and s.xp is None else synth.bam_bytes(s, rg_tags=True))
     fasta = os.path.join(d, "reference.fasta")
     write_fasta(s, fasta)
     out = os.path.join(d, "out")
