@@ -461,6 +461,33 @@ def _cpu_reference(sample_scale: float, threads: int, min_seconds: float = 0.0):
     return reps * bases / dt, reps * bases, dt, s.total_length(), reps
 
 
+def _oracle_run(s, threads):
+    """The oracle port of the reference algorithm (both passes) on sample s: results and seconds."""
+    from oracle import pyoracle as po
+    t0 = time.perf_counter()
+    ec = po.error_count(s, n_threads=threads)
+    tab = po.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
+    im = po.identify(s, tab, po.default_im_params(s), n_threads=threads, positions=False)
+    return ec, im, time.perf_counter() - t0
+
+
+def _oracle_check(s, ec_gpu, im_gpu, threads):
+    """The headline sample through the oracle as well: covariate counts and coverage histograms
+    bit-exact, RA calls identical (scores within 1e-3, frequencies within 1e-4), MC / UN identical."""
+    from tests import compare
+    ec_o, im_o, dt = _oracle_run(s, threads)
+    problems = []
+    if not np.array_equal(ec_gpu["counts"], ec_o["counts"]):
+        problems.append("covariate counts differ")
+    h = min(ec_gpu["hist"].shape[1], ec_o["hist"].shape[1])
+    if not np.array_equal(ec_gpu["hist"][:, :h], ec_o["hist"][:, :h]):
+        problems.append("coverage histograms differ")
+    problems += compare.compare_ra(im_gpu["ra"], im_o["ra"])
+    problems += compare.compare_intervals(im_gpu, im_o)
+    return {"identical": not problems, "ra_items": len(im_o["ra"]), "mc": len(im_o["mc"]), "un": len(im_o["un"]),
+            "problems": problems[:5]}, dt
+
+
 def _calls(im):
     """The call set of a result (RA records as dicts or as a structured array)."""
     def b(x):
@@ -470,13 +497,17 @@ def _calls(im):
 
 
 def run_reference(args, world, rank, pg):
+    """The reference arm: the oracle port of error_count + identify_mutations on the host cores, on the
+    same sample the GPU arm scores (one full run per step, all host threads)."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
+    s = _workload(seed=21, scale=args.scale)
+    bases = s.aligned_bases()
+    ln = s.total_length()
     times = []
-    rate = bases = ln = None
     for i in range(args.warmup + args.steps):
-        rate, bases, dt, ln, _ = _cpu_reference(args.cpu_scale, threads)
+        _, _, dt = _oracle_run(s, threads)
         if i >= args.warmup:
             times.append(dt)
     ms = 1000.0 * statistics.mean(times)
@@ -485,9 +516,10 @@ def run_reference(args, world, rank, pg):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": WORKLOAD, "sample_length_bp": ln, "sample_read_bases": bases},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"same workload at {args.cpu_scale:g} x genome length ({ln} bp, {bases} read-bases)"},
+            "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD} scaled x{args.scale:g}",
+                       "genome_bp": ln, "read_bases_per_step": bases},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "same_config": True,
+                             "sample": f"the same sample as the GPU arm ({ln} bp, {bases} read-bases), one run per step"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -643,10 +675,20 @@ def run_ours(args, world, rank, local, pg):
         line["coverage_table"] = run_coverage(args, sc, sid, s)
         line["coverage_fit"] = run_covfit(args, ec0, s)
     if rank == 0 and not args.no_cpu:
-        rate, cb, dt, ln, reps = _cpu_reference(args.cpu_scale, os.cpu_count() or 1, args.cpu_seconds)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": f"same workload at {args.cpu_scale:g} x genome length ({ln} bp), "
-                                          f"{reps} runs, {cb} read-bases in {dt:.1f} s"}
+        # the oracle on the same sample with every host thread: the agreement of the headline result
+        # and the CPU baseline on the same input; and one host core on a bounded sample
+        threads = os.cpu_count() or 1
+        ec_chk = sc.error_count(sid)
+        im_chk = sc.identify_mutations(sid, sc.counts_to_log10_prob(ec_chk["counts"], s.n_read_files, s.n_quality), st,
+                                       precision=prec)
+        check, dt = _oracle_check(s, ec_chk, im_chk, threads)
+        line["identical_to_oracle"] = check
+        rate1, cb1, dt1, ln1, reps1 = _cpu_reference(args.cpu_scale, 1, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": bases / dt, "unit": UNIT, "cores": threads, "kind": "port", "same_config": True,
+                                "sample": f"the same sample ({s.total_length()} bp, {bases} read-bases), one run, {dt:.1f} s",
+                                "one_core": {"value": rate1, "unit": UNIT, "cores": 1,
+                                             "sample": f"same workload at {args.cpu_scale:g} x genome length ({ln1} bp), "
+                                                       f"{reps1} runs, {cb1} read-bases in {dt1:.1f} s"}}
     sc.close()
     # the mixed-shape legs first: the BAM leg leaves gigabytes of freed host and pooled device memory
     if rank == 0 and args.batch_jobs > 0:

@@ -105,6 +105,8 @@ def load():
                                              C.c_int, P(abi.CovColumns)]
     L.bsq_write_coverage_table_rg.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, P(abi.Reference),
                                               C.c_uint32, P(abi.PositionArrays), C.c_uint32, C.c_int]
+    L.bsq_intervals_from_positions.argtypes = [P(abi.Reference), P(abi.PositionArrays), P(abi.ImParams), C.c_void_p,
+                                               C.c_uint64, P(C.c_uint64), C.c_void_p, C.c_uint64, P(C.c_uint64)]
     L.bsq_bam_open.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, P(C.c_void_p)]
     L.bsq_bam_close.argtypes = [C.c_void_p]
     L.bsq_bam_close.restype = None
@@ -162,4 +164,4 @@ EXPORTED = ("bsq_create", "bsq_destroy", "bsq_last_error", "bsq_version", "bsq_l
             "bsq_write_mp_candidate_regions", "bsq_pd_result",
             "bsq_write_pd_candidate_regions", "bsq_coverage_columns_rg", "bsq_write_coverage_region_rg",
             "bsq_pd_build_null", "bsq_pd_max_span", "bsq_pd_seed_z", "bsq_ndtri", "bsq_im_coverage_columns_rg",
-            "bsq_write_coverage_table_rg")
+            "bsq_write_coverage_table_rg", "bsq_intervals_from_positions")

@@ -1075,6 +1075,44 @@ int bsq_im_result_counts(const bsq_ctx* ctx, uint64_t* n_ra, uint64_t* n_mc, uin
   return bsq_im_batch_result_counts(ctx, 0, n_ra, n_mc, n_un);
 }
 
+int bsq_intervals_from_positions(const bsq_reference* ref, const bsq_position_arrays* pa, const bsq_im_params* p,
+                                 bsq_mc_record* mc, uint64_t mc_cap, uint64_t* n_mc, bsq_un_record* un, uint64_t un_cap,
+                                 uint64_t* n_un) {
+  if (!ref || !pa || !p || !n_mc || !n_un || !ref->target_offset || !p->deletion_propagation_cutoff ||
+      !p->deletion_seed_cutoff || !pa->unique_top || !pa->unique_bot || !pa->redundant_top || !pa->redundant_bot ||
+      !pa->consensus_score || (mc_cap && !mc) || (un_cap && !un))
+    return BSQ_ERR_INVALID;
+  const uint32_t T = ref->n_targets;
+  std::vector<uint64_t> toff(ref->target_offset, ref->target_offset + T + 1);
+  std::vector<uint32_t> tpoff(T + 1), order;
+  for (uint32_t t = 0; t <= T; t++) tpoff[t] = (uint32_t)(toff[t] + t);
+  for (uint32_t i = 0; i < ref->n_target_order; i++) {
+    if (ref->target_order[i] >= T) return BSQ_ERR_INVALID;
+    order.push_back(ref->target_order[i]);
+  }
+  std::vector<ColCov> cov(tpoff[T]);
+  std::vector<ColCall> call(tpoff[T]);
+  for (uint32_t t = 0; t < T; t++)
+    for (uint64_t g = toff[t]; g < toff[t + 1]; g++) {
+      ColCov& cv = cov[tpoff[t] + (g - toff[t])];
+      cv.uniq_top = pa->unique_top[g]; cv.uniq_bot = pa->unique_bot[g];
+      cv.red_top = pa->redundant_top[g]; cv.red_bot = pa->redundant_bot[g];
+      ColCall& cl = call[tpoff[t] + (g - toff[t])];
+      cl.flags = (pa->consensus_score[g] >= p->mutation_cutoff) ? kBasePredicted : 0;
+    }
+  host::SampleLayout L;
+  L.tpoff = &tpoff; L.toff = &toff; L.order = &order;
+  std::vector<bsq_mc_record> m;
+  std::vector<bsq_un_record> u;
+  host::intervals(cov, call, L, p, m, u);
+  *n_mc = m.size();
+  *n_un = u.size();
+  if (m.size() > mc_cap || u.size() > un_cap) return BSQ_ERR_SIZE;
+  std::copy(m.begin(), m.end(), mc);
+  std::copy(u.begin(), u.end(), un);
+  return BSQ_OK;
+}
+
 int bsq_im_result_copy(const bsq_ctx* ctx, bsq_ra_record* ra, uint64_t ra_cap, bsq_mc_record* mc, uint64_t mc_cap,
                        bsq_un_record* un, uint64_t un_cap) {
   return bsq_im_batch_result_copy(ctx, 0, ra, ra_cap, mc, mc_cap, un, un_cap);

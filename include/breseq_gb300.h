@@ -379,6 +379,17 @@ int bsq_im_result_counts(const bsq_ctx* ctx, uint64_t* n_ra, uint64_t* n_mc, uin
 int bsq_im_result_copy(const bsq_ctx* ctx, bsq_ra_record* ra, uint64_t ra_cap,
                        bsq_mc_record* mc, uint64_t mc_cap, bsq_un_record* un, uint64_t un_cap);
 
+/* The MC and UN intervals of per-position arrays (identify_mutations.cpp:2107-2164 at the target ends,
+ * check_deletion_completion :2262-2344, update_unknown_intervals :2972-3007): the state machines run
+ * over every position of the targets in ref->target_order, with a position's consensus call predicted
+ * when consensus_score >= p->mutation_cutoff (NaN: not).  Reads unique_top/bot, redundant_top/bot and
+ * consensus_score of `positions` (indexed as bsq_identify_mutations fills them).  Host code: this is how
+ * the results of position ranges scored apart (one per GPU) are joined into one sample's intervals.
+ * BSQ_ERR_SIZE, with *n_mc / *n_un set, when a capacity is short. */
+int bsq_intervals_from_positions(const bsq_reference* ref, const bsq_position_arrays* positions, const bsq_im_params* p,
+                                 bsq_mc_record* mc, uint64_t mc_cap, uint64_t* n_mc, bsq_un_record* un, uint64_t un_cap,
+                                 uint64_t* n_un);
+
 /* Batch forms: n samples scored by one launch per kernel of the pass (every sample's reads or
  * column tiles are units of one persistent grid).  Element j of each array belongs to sample_ids[j];
  * the results of each sample equal those of the single-sample call.  breseq runs error_count and
