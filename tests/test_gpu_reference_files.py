@@ -99,4 +99,6 @@ def test_classified_genome_diff_matches_reference(built_lib, tmp_path, case):
     assert L.bsq_write_gd(path.encode(), C.byref(view.ref), names, abi.ptr(prop, C.c_double), rs.polymorphism_precision_places,
                           C.cast(ra, C.c_void_p), len(im["ra"]), C.cast(calls, C.c_void_p), C.cast(mc, C.c_void_p),
                           len(im["mc"]), C.cast(un, C.c_void_p), len(im["un"])) == 0
-    assert open(path).read() == fx["files"]["ra_mc_evidence.classified.gd"]["text"]
+    import hashlib
+    want, text = fx["files"]["ra_mc_evidence.classified.gd"], open(path).read()
+    assert want["text"] == text if "text" in want else want["sha256"] == hashlib.sha256(text.encode()).hexdigest()
