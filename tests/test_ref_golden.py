@@ -20,7 +20,8 @@ from tests import samples
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden", "ref")
-SMALL = ["clonal_small", "ecoli_small", "ecoli_small_failed_fit", "population_small", "dp_groups"]
+SMALL = ["clonal_small", "ecoli_small", "ecoli_small_failed_fit", "population_small", "dp_groups",
+         "ecoli_quarter", "population_deep"]
 DP_HEADER = "seq_id,start,end,strand,orientation,length,max_discordant_count,redundant,discordant_pairs\n"
 
 
