@@ -703,11 +703,23 @@ def run_ours(args, world, rank, local, pg):
         print(json.dumps(line), flush=True)
 
 
+def _simulate(cfg):
+    from breseq_gb300 import synth
+    return synth.simulate(cfg)
+
+
 def _pool(args):
-    """Distinct seeded samples of the mixed-shape distribution; job i uses pool[i % len(pool)]."""
+    """Distinct seeded samples of the mixed-shape distribution; job i uses pool[i % len(pool)].  The
+    samples are generated in spawned worker processes (the GPU is already in use by this process)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
     from breseq_gb300 import synth
     cfgs = synth.config_batch(seed=41, n_samples=max(args.batch_jobs, args.batch_pool), scale=args.batch_scale)
-    return [(synth.simulate(c), poly) for c, poly in cfgs[:args.batch_pool]]
+    cfgs = cfgs[:args.batch_pool]
+    workers = max(1, min(len(cfgs), (os.cpu_count() or 1)))
+    with cf.ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn")) as ex:
+        sims = list(ex.map(_simulate, [c for c, _ in cfgs]))
+    return [(sim, poly) for sim, (_, poly) in zip(sims, cfgs)]
 
 
 def run_mix(args, device):
@@ -837,7 +849,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="genome length scale of the workload (profiling cases)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="minimum CPU work timed for cpu_baseline")
     ap.add_argument("--batch-jobs", type=int, default=96, help="jobs of the batched / served legs (0: skip them)")
-    ap.add_argument("--batch-pool", type=int, default=16, help="distinct samples the jobs are drawn from")
+    ap.add_argument("--batch-pool", type=int, default=96, help="distinct samples the jobs are drawn from")
     ap.add_argument("--batch-scale", type=float, default=0.25, help="genome length scale of the mixed samples")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--served-jobs", type=int, default=288)
