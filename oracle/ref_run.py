@@ -14,16 +14,24 @@ from . import ref_build
 
 
 def write_fasta(s, path):
+    """The targets as FASTA (80 bases per line) and its samtools-style .fai index."""
+    off, fai = 0, []
     with open(path, "w") as f:
         for t, name in enumerate(s.target_names):
             seq = bytes(s.ref_seq[int(s.target_offset[t]):int(s.target_offset[t + 1])]).decode()
-            f.write(f">{name}\n")
+            head = f">{name}\n"
+            f.write(head)
+            off += len(head)
+            fai.append(f"{name}\t{len(seq)}\t{off}\t80\t81\n")
             for i in range(0, len(seq), 80):
                 f.write(seq[i:i + 80] + "\n")
+                off += len(seq[i:i + 80]) + 1
+    with open(path + ".fai", "w") as f:
+        f.write("".join(fai))
 
 
 def write_inputs(s, d, polymorphism=False, prop_cutoff=None, seed_cutoff=None, copy_number=False, classify=False,
-                 pmdd=(), fast_bam=False) -> tuple:
+                 pmdd=(), fast_bam=False, softclip=False, bam2cov=()) -> tuple:
     """reference.bam, reference.fasta, an empty out/ folder and config.txt in folder d; returns the
     config path and the output folder.  pmdd: (read group, median, mad) of the paired-mapping-distance
     fits that make discordant-pair groups.  fast_bam: the vectorised BAM writer (same records; its read
@@ -49,6 +57,9 @@ def write_inputs(s, d, polymorphism=False, prop_cutoff=None, seed_cutoff=None, c
         f.write(f"copy_number {int(copy_number)}\nclassify {int(classify)}\n")
         for g, med, mad in pmdd:
             f.write(f"pmdd {int(g)} {float(med)!r} {float(mad)!r}\n")
+        f.write(f"softclip {int(softclip)}\n")
+        for name, region, res, fmt, tot, prg in bam2cov:
+            f.write(f"bam2cov {name} {region} {int(res)} {fmt} {int(tot)} {int(prg)}\n")
         for t, name in enumerate(s.target_names):
             f.write(f"target {name} {int(s.coverage_group[t])} {int(t in called)} {float(prop[t])!r} {float(seed[t])!r}\n")
     return cfg, out
@@ -64,13 +75,14 @@ def read_outputs(out) -> dict:
 
 
 def run(s, polymorphism=False, prop_cutoff=None, seed_cutoff=None, copy_number=False, classify=False,
-        pmdd=(), workdir=None) -> dict:
+        pmdd=(), workdir=None, softclip=False, bam2cov=()) -> dict:
     """Outputs of the reference on sample `s`: {file name: text}.  Raises when the binary is absent."""
     exe = ref_build.build()
     if exe is None:
         raise FileNotFoundError("the reference sources are not available")
     with tempfile.TemporaryDirectory(dir=workdir) as d:
-        cfg, out = write_inputs(s, d, polymorphism, prop_cutoff, seed_cutoff, copy_number, classify, pmdd)
+        cfg, out = write_inputs(s, d, polymorphism, prop_cutoff, seed_cutoff, copy_number, classify, pmdd,
+                                softclip=softclip, bam2cov=bam2cov)
         env = dict(os.environ, BRESEQ_DATA_PATH=ref_build.data_path())
         r = subprocess.run([exe, cfg], capture_output=True, text=True, cwd=d, env=env)
         if r.returncode != 0:

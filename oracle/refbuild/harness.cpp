@@ -15,6 +15,11 @@
 //   classify 0|1              also run test_RA_evidence and write ra_mc_evidence.classified.gd
 //   pmdd g median mad         paired-mapping-distance fit of read group g: makes it a discordant-pair
 //                             group (identify_mutations.cpp:883-911; window median + 2.42 mad)
+//   softclip 0|1              also tabulate_soft_clipping_counts (soft_clipping.cpp:288): writes
+//                             soft_clipping_counts.tab and soft_clipping_summary.txt (the Summary fields)
+//   bam2cov name region resolution format total_only per_read_group
+//                             also `breseq BAM2COV` tables (coverage_output::table, breseq_cmdline.cpp:428-536)
+//                             into bam2cov/<name>
 // Outputs in outdir: error_rates.tab, base_qual_error_prob.<file>.tab, <group>.unique_only_coverage_distribution.tab,
 // ra_mc_evidence.gd, 08_mutation_identification/ (DP candidate regions, coverage tables) and the
 // classified GenomeDiff when asked.
@@ -26,8 +31,10 @@
 #include "error_count.h"
 #include "genome_diff.h"
 #include "identify_mutations.h"
+#include "coverage_output.h"
 #include "reference_sequence.h"
 #include "settings.h"
+#include "soft_clipping.h"
 #include "summary.h"
 
 using namespace breseq;
@@ -43,6 +50,9 @@ int main(int argc, char** argv) {
   bool poly = false, copy_number = false, classify = false;
   struct Pmdd { uint32_t g; double median, mad; };
   vector<Pmdd> pmdd;
+  bool softclip = false;
+  struct Cov { string name, region, format; uint32_t resolution; int total_only, per_rg; };
+  vector<Cov> covs;
   string line;
   while (getline(cf, line)) {
     istringstream ls(line);
@@ -57,6 +67,12 @@ int main(int argc, char** argv) {
     else if (key == "copy_number") { int v; ls >> v; copy_number = v != 0; }
     else if (key == "classify") { int v; ls >> v; classify = v != 0; }
     else if (key == "pmdd") { Pmdd d; ls >> d.g >> d.median >> d.mad; pmdd.push_back(d); }
+    else if (key == "softclip") { int v; ls >> v; softclip = v != 0; }
+    else if (key == "bam2cov") {
+      Cov c;
+      ls >> c.name >> c.region >> c.resolution >> c.format >> c.total_only >> c.per_rg;
+      covs.push_back(c);
+    }
     else if (key == "target") { Tgt t; ls >> t.name >> t.group >> t.called >> t.prop >> t.seed; targets.push_back(t); }
   }
   Settings::set_global_paths();      // data path from BRESEQ_DATA_PATH
@@ -138,6 +154,30 @@ int main(int argc, char** argv) {
   identify_mutations(settings, summary, bam, fasta, gd_file, ref_seq_info, prop, seed, settings.mutation_log10_e_value_cutoff,
                      settings.polymorphism_log10_e_value_cutoff, settings.polymorphism_precision_decimal,
                      settings.polymorphism_precision_places, false);
+  if (softclip) {
+    settings.soft_clipping_counts_file_name = Settings::path_file_name(outdir, "soft_clipping_counts.tab");
+    tabulate_soft_clipping_counts(settings, summary, make_vector<string>(bam), fasta, ref_seq_info);
+    const SoftClippingSummary& c = summary.soft_clipping;
+    FILE* f = fopen(Settings::path_file_name(outdir, "soft_clipping_summary.txt").c_str(), "w");
+    fprintf(f, "total_spanning_read_bases %llu\ntotal_clipped_read_ends %llu\ntotal_agreeing_clipped_read_ends %llu\n",
+            (unsigned long long)c.total_spanning_read_bases, (unsigned long long)c.total_clipped_read_ends,
+            (unsigned long long)c.total_agreeing_clipped_read_ends);
+    fprintf(f, "soft_clipping_rate %.17g\nsoft_clipping_null_rate %.17g\nsoft_clipping_dispersion %.17g\n",
+            c.soft_clipping_rate, c.soft_clipping_null_rate, c.soft_clipping_dispersion);
+    fprintf(f, "soft_clipping_pearson_phi %.17g\nsoft_clipping_tested_positions %llu\nsoft_clipping_trimmed_positions %llu\n",
+            c.soft_clipping_pearson_phi, (unsigned long long)c.soft_clipping_tested_positions,
+            (unsigned long long)c.soft_clipping_trimmed_positions);
+    fprintf(f, "soft_clipping_mean_tested_reads %.17g\n", c.soft_clipping_mean_tested_reads);
+    fclose(f);
+  }
+  if (!covs.empty()) create_path(outdir + "/bam2cov");
+  for (const Cov& c : covs) {
+    coverage_output co(bam, fasta);
+    co.total_only(c.total_only != 0);
+    co.per_read_group(c.per_rg != 0);
+    co.output_format(c.format);
+    co.table(c.region, outdir + "/bam2cov/" + c.name, c.resolution);
+  }
   if (classify) {
     cGenomeDiff gd(gd_file);
     test_RA_evidence(gd, ref_seq_info, settings);

@@ -27,6 +27,12 @@ CASES = {
     "dp_groups": dict(sample="dp_skip_sample", pmdd=[[0, 300.0, 20.0]]),
     "ecoli_quarter": dict(sample="ecoli_quarter"),
     "population_deep": dict(sample="population_deep", polymorphism=True),
+    # tabulate_soft_clipping_counts and BAM2COV tables (coverage_output::table) on the clipped sample
+    "softclip_bam2cov": dict(sample="softclip_sample", softclip=True, bam2cov=[
+        ["full.tsv", "zeta_chromosome:1-138900", 0, "tsv", 0, 0],
+        ["mid7.csv", "Alpha_plasmid:101-3000", 7, "csv", 0, 0],
+        ["tot.tsv", "zeta_chromosome:500-90000", 600, "tsv", 1, 0],
+        ["rg.tsv", "beta_plasmid:1-2000", 0, "tsv", 0, 1]]),
 }
 TEXT_LIMIT = 16 * 1024
 
@@ -36,7 +42,8 @@ def make(case):
     s = getattr(samples, c["sample"])()
     t0 = time.time()
     out = ref_run.run(s, polymorphism=c.get("polymorphism", False), prop_cutoff=c.get("prop_cutoff"),
-                      copy_number=True, classify=True, pmdd=[tuple(x) for x in c.get("pmdd", [])])
+                      copy_number=True, classify=True, pmdd=[tuple(x) for x in c.get("pmdd", [])],
+                      softclip=c.get("softclip", False), bam2cov=[tuple(x) for x in c.get("bam2cov", [])])
     files = {}
     for name, text in sorted(out.items()):
         if name == "ra_mc_evidence.classified.gd":

@@ -51,7 +51,10 @@ def test_dropin_writes_the_reference_files(dropin_exe, tmp_path, case):
     r = subprocess.run([dropin_exe, cfg], capture_output=True, text=True, timeout=1200)
     assert r.returncode == 0, r.stderr[-3000:]
     got = ref_run.read_outputs(out)
-    want = {k: v for k, v in fx["files"].items() if k != "ra_mc_evidence.classified.gd"}
+    # the drop-in covers the two passes; the classified GenomeDiff, the soft-clipping and BAM2COV files are
+    # checked by the tests below
+    want = {k: v for k, v in fx["files"].items()
+            if k != "ra_mc_evidence.classified.gd" and not k.startswith(("soft_clipping", "bam2cov/"))}
     assert sorted(got) == sorted(want)
     bad = []
     for name, w in want.items():
@@ -102,3 +105,33 @@ def test_classified_genome_diff_matches_reference(built_lib, tmp_path, case):
     import hashlib
     want, text = fx["files"]["ra_mc_evidence.classified.gd"], open(path).read()
     assert want["text"] == text if "text" in want else want["sha256"] == hashlib.sha256(text.encode()).hexdigest()
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c == "softclip_bam2cov"])
+def test_soft_clipping_and_bam2cov_match_reference(built_lib, tmp_path, case):
+    """tabulate_soft_clipping_counts and `breseq BAM2COV` tables computed on the GPU (bsq_soft_clipping,
+    bsq_write_coverage_region_rg) against breseq's own files."""
+    import hashlib
+    from breseq_gb300.api import Scorer
+    from tests.test_ref_golden import bam2cov_region, sc_counts_text, sc_summary_text
+    with open(os.path.join(HERE, "golden", "ref", f"{case}.json")) as f:
+        fx = json.load(f)
+    st = fx["settings"]
+    s = getattr(samples, st["sample"])()
+    assert samples.sample_digest(s) == fx["sample_digest"]
+
+    def same(name, text):
+        w = fx["files"][name]
+        return w["text"] == text if "text" in w else w["sha256"] == hashlib.sha256(text.encode()).hexdigest()
+
+    with Scorer(0) as sc:
+        sid = sc.load_sample(s)
+        r = sc.soft_clipping(sid)
+        assert same("soft_clipping_counts.tab", sc_counts_text(s, r, tmp_path))
+        assert same("soft_clipping_summary.txt", sc_summary_text(r["summary"]))
+        for name, region, res, fmt, tot, prg in st["bam2cov"]:
+            tid, a, b = bam2cov_region(s, region)
+            path = str(tmp_path / name)
+            sc.write_coverage_region(sid, path, tid, a, b, resolution=res, total_only=bool(tot), csv=fmt == "csv",
+                                     per_read_group=bool(prg))
+            assert same("bam2cov/" + name, open(path).read()), name

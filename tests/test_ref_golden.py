@@ -21,7 +21,7 @@ from tests import samples
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden", "ref")
 SMALL = ["clonal_small", "ecoli_small", "ecoli_small_failed_fit", "population_small", "dp_groups",
-         "ecoli_quarter", "population_deep"]
+         "ecoli_quarter", "population_deep", "softclip_bam2cov"]
 DP_HEADER = "seq_id,start,end,strand,orientation,length,max_discordant_count,redundant,discordant_pairs\n"
 
 
@@ -52,6 +52,44 @@ def dp_setup(st, nfiles):
             dp.append(-1)
         flat += nfiles[g]
     return dp, widths, r1, r2
+
+
+def sc_summary_text(sm):
+    """The harness's soft_clipping_summary.txt for a bsq_sc_summary dict (the Summary::soft_clipping fields)."""
+    def g(x):
+        return "%.17g" % x
+    return (f"total_spanning_read_bases {sm['total_spanning_read_bases']}\n"
+            f"total_clipped_read_ends {sm['total_clipped_read_ends']}\n"
+            f"total_agreeing_clipped_read_ends {sm['total_agreeing_clipped_read_ends']}\n"
+            f"soft_clipping_rate {g(sm['soft_clipping_rate'])}\nsoft_clipping_null_rate {g(sm['null_rate'])}\n"
+            f"soft_clipping_dispersion {g(sm['dispersion'])}\nsoft_clipping_pearson_phi {g(sm['pearson_phi'])}\n"
+            f"soft_clipping_tested_positions {sm['tested_positions']}\n"
+            f"soft_clipping_trimmed_positions {sm['trimmed_positions']}\n"
+            f"soft_clipping_mean_tested_reads {g(sm['mean_tested_reads'])}\n")
+
+
+def sc_counts_text(s, result, tmp_path):
+    """soft_clipping_counts.tab from a tabulation result, written by the library's host writer."""
+    import ctypes as C
+
+    from breseq_gb300 import _lib, abi
+    L = _lib.load()
+    p = abi.ScParams()
+    assert L.bsq_default_sc_params(C.byref(p)) == 0
+    sm = abi.ScSummary(**result["summary"])
+    rows = (abi.ScPosition * max(1, len(result["rows"])))()
+    for i, x in enumerate(result["rows"]):
+        rows[i] = abi.ScPosition(*[x[k] for k in abi.SC_ROW_DTYPE.names])
+    names = (C.c_char_p * len(s.target_names))(*[n.encode() for n in s.target_names])
+    path = str(tmp_path / "soft_clipping_counts.tab")
+    assert L.bsq_write_soft_clipping_counts(path.encode(), names, C.byref(p), C.byref(sm), rows, len(result["rows"])) == 0
+    return open(path).read()
+
+
+def bam2cov_region(s, region):
+    seq, rng = region.split(":")
+    a, b = (int(x) for x in rng.split("-"))
+    return s.target_names.index(seq), a, b
 
 
 def oracle_files(fx, tmp_path):
@@ -96,6 +134,16 @@ def oracle_files(fx, tmp_path):
         out[dp_file] = open(dpath).read()
     else:   # no DP group: the header line alone
         out[dp_file] = DP_HEADER
+    if st.get("softclip"):
+        r = po.soft_clipping(s)
+        out["soft_clipping_counts.tab"] = sc_counts_text(s, r, tmp_path)
+        out["soft_clipping_summary.txt"] = sc_summary_text(r["summary"])
+    for name, region, res, fmt, tot, prg in st.get("bam2cov", []):
+        tid, a, b = bam2cov_region(s, region)
+        path = str(tmp_path / name)
+        po.write_coverage_region(s, path, tid, a, b, resolution=res, total_only=bool(tot), csv=fmt == "csv",
+                                 per_read_group=bool(prg))
+        out["bam2cov/" + name] = open(path).read()
     return out
 
 
