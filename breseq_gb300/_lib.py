@@ -102,9 +102,9 @@ def load():
     L.bsq_write_coverage_region_rg.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, C.c_uint32, C.c_uint32,
                                                C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_double), C.c_uint32]
     L.bsq_im_coverage_columns_rg.argtypes = [C.c_void_p, C.c_int32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32,
-                                             C.c_int, P(abi.CovColumns)]
+                                             C.c_int, C.c_uint32, P(C.c_int32), P(abi.CovColumns)]
     L.bsq_write_coverage_table_rg.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_char_p, P(abi.Reference),
-                                              C.c_uint32, P(abi.PositionArrays), C.c_uint32, C.c_int]
+                                              C.c_uint32, P(abi.PositionArrays), C.c_uint32, C.c_int, P(C.c_int32)]
     L.bsq_intervals_from_positions.argtypes = [P(abi.Reference), P(abi.PositionArrays), P(abi.ImParams), C.c_void_p,
                                                C.c_uint64, P(C.c_uint64), C.c_void_p, C.c_uint64, P(C.c_uint64)]
     L.bsq_bam_open.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, P(C.c_void_p)]

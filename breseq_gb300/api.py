@@ -31,6 +31,15 @@ class ScSettings:
     minimum_rate: float = 1e-5
 
 
+def header_read_groups(sample) -> int:
+    """The @RG count of the header of a sample's BAM: `n_header_read_groups` when the sample has it, else
+    the groups synth.bam_bytes declares for it (the highest read group + 1)."""
+    n = getattr(sample, "n_header_read_groups", None)
+    if n is not None:
+        return int(n)
+    return int(np.max(sample.read_group)) + 1 if len(sample.read_group) else 1
+
+
 def sc_params(sample, st: ScSettings):
     """bsq_sc_params for a sample; rows follow the std::string order of its target names."""
     names = list(sample.target_names)
@@ -178,6 +187,7 @@ class Scorer:
         if rc != 0:
             raise _lib.BsqError(rc, "bsq_create failed (no CUDA device?)")
         self._views = {}
+        self._rg_count = {}    # sample id -> the @RG count of its BAM header (identify_mutations.cpp:862)
 
     def _check(self, rc):
         if rc != 0:
@@ -200,11 +210,13 @@ class Scorer:
         sid = C.c_int32()
         self._check(self.L.bsq_load_sample(self.ctx, C.byref(view.ref), C.byref(view.reads), C.byref(sid)))
         self._views[sid.value] = (sample, view)
+        self._rg_count[sid.value] = header_read_groups(sample)
         return sid.value
 
     def free_sample(self, sid: int):
         self._check(self.L.bsq_free_sample(self.ctx, sid))
         self._views.pop(sid, None)
+        self._rg_count.pop(sid, None)
 
     def sample(self, sid):
         return self._views[sid][0]
@@ -411,41 +423,46 @@ class Scorer:
         return arrs
 
     def im_coverage_columns(self, sid: int, tid: int, start: int, end: int, read_group: int = -1,
-                            coverage_fit_failed: bool = False) -> dict:
+                            coverage_fit_failed: bool = False, dp_group=()) -> dict:
         """identify_mutations' coverage tally at positions start..end (1-based) of target tid, of one read
         group's records when read_group >= 0: deletions count and N read bases do not, or, for a target
-        whose coverage fit failed, neither counts."""
+        whose coverage fit failed, neither counts.  dp_group: per read group its discordant-pair group or
+        -1 (ImSettings.dp_group); pass 2's first-column skip applies to the tally too."""
         arrs, st = abi.cov_columns(end - start + 1)
+        dp = np.ascontiguousarray(dp_group, dtype=np.int32)
         self._check(self.L.bsq_im_coverage_columns_rg(self.ctx, sid, tid, start, end, read_group,
-                                                      1 if coverage_fit_failed else 0, C.byref(st)))
+                                                      1 if coverage_fit_failed else 0, len(dp),
+                                                      abi.ptr(dp, C.c_int32) if len(dp) else None, C.byref(st)))
         return arrs
 
     def write_coverage_table(self, sid: int, path: str, tid: int, positions: dict, n_read_groups: int | None = None,
-                             coverage_fit_failed: bool = False):
+                             coverage_fit_failed: bool = False, dp_group=()):
         """<seq_id>.coverage.tsv of identify_mutations into path: the aggregate columns from `positions`
         (identify_mutations(..., positions=True)["positions"]) and, with more than one read group, each
         group's columns tallied on the device.  n_read_groups: the BAM header's @RG count (default: the
-        sample's highest read group + 1)."""
+        groups the sample's BAM declares).  dp_group: as for im_coverage_columns."""
         s = self.sample(sid)
         if n_read_groups is None:
-            n_read_groups = int(np.max(s.read_group)) + 1 if len(s.read_group) else 1
+            n_read_groups = self._rg_count.get(sid, 1)
+        dp = np.zeros(n_read_groups, np.int32) - 1
+        dp[:min(len(dp_group), n_read_groups)] = np.asarray(dp_group, dtype=np.int32)[:n_read_groups]
         view = self._views[sid][1]
         pa, keep = abi.position_arrays_view(positions)
         self._check(self.L.bsq_write_coverage_table_rg(self.ctx, sid, path.encode(), s.target_names[tid].encode(),
                                                        C.byref(view.ref), tid, C.byref(pa), n_read_groups,
-                                                       1 if coverage_fit_failed else 0))
+                                                       1 if coverage_fit_failed else 0, abi.ptr(dp, C.c_int32)))
         del keep
 
     def write_coverage_region(self, sid: int, path: str, tid: int, start: int, end: int, resolution: int = 600,
                               total_only: bool = False, csv: bool = False, reference_average=None,
                               per_read_group: bool = False, n_read_groups: int | None = None):
         """`breseq BAM2COV --format TSV|CSV -r seq:start-end --resolution N [--per-read-group]` into path;
-        n_read_groups: the BAM header's @RG count (default: the sample's highest read group + 1)."""
+        n_read_groups: the BAM header's @RG count (default: the one the sample was loaded with)."""
         s = self.sample(sid)
         flags = (1 if total_only else 0) | (2 if csv else 0) | (4 if per_read_group else 0)
         avg = C.byref(C.c_double(reference_average)) if reference_average is not None else None
         if n_read_groups is None:
-            n_read_groups = int(np.max(s.read_group)) + 1 if len(s.read_group) else 1
+            n_read_groups = self._rg_count.get(sid, 1)
         self._check(self.L.bsq_write_coverage_region_rg(self.ctx, sid, path.encode(), s.target_names[tid].encode(), tid,
                                                         start, end, resolution, flags, avg, n_read_groups))
 
@@ -676,8 +693,10 @@ class Bam:
     def load(self, reference_sample) -> int:
         view = abi.SampleView(reference_sample)
         sid = C.c_int32()
+        n_rg = sum(1 for line in self.header()["text"].splitlines() if line.startswith("@RG"))
         self.sc._check(self.sc.L.bsq_bam_load(self.sc.ctx, self.h, C.byref(view.ref), C.byref(sid)))
         self.sc._views[sid.value] = (reference_sample, view)
+        self.sc._rg_count[sid.value] = n_rg
         return sid.value
 
     def close(self):

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <limits>
 #include <map>
 #include <atomic>
@@ -1471,7 +1472,7 @@ int bsq_pair_result_copy(bsq_ctx* ctx, bsq_pair_region* dp, uint64_t n_dp, bsq_p
 // [2][m] f64 weights | stat | the target's reference characters up to end_1.
 static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start, uint32_t end,
                            uint32_t first, uint32_t step, host::CoverageRegion& out, int32_t rg_only = -1,
-                           uint32_t mode = kCtBam2cov) {
+                           uint32_t mode = kCtBam2cov, const uint32_t* dp_rg = nullptr) {
   SampleDev* s = find_sample(ctx, sample_id);
   if (!s) return fail(ctx, BSQ_ERR_NOSAMPLE, "unknown sample id");
   if (tid >= s->n_targets) return fail(ctx, BSQ_ERR_INVALID, "target index out of range");
@@ -1491,6 +1492,7 @@ static int coverage_region(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32
   A.rg_only = rg_only;
   A.seq = s->seq.as<uint8_t>();
   A.mode = mode;
+  if (dp_rg) memcpy(A.dp_rg, dp_rg, sizeof A.dp_rg);
   A.n_reads = s->n_reads;
   A.t0 = s->tpoff[tid];
   A.c0 = A.t0 + start - 1;
@@ -1613,12 +1615,25 @@ int bsq_write_coverage_region_rg(bsq_ctx* ctx, int32_t sample_id, const char* pa
   return BSQ_OK;
 }
 
+// The discordant-pair read groups as the 256-bit mask the kernels take (identify_mutations.cpp:883-911).
+static int dp_mask_groups(bsq_ctx* ctx, uint32_t n_read_groups, const int32_t* dp_group, uint32_t out[8]) {
+  bsq_im_params p;
+  memset(&p, 0, sizeof p);
+  p.n_read_groups = dp_group ? n_read_groups : 0;
+  p.dp_group = dp_group;
+  return dp_mask(ctx, p, out);
+}
+
 int bsq_im_coverage_columns_rg(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start_1, uint32_t end_1,
-                               int32_t read_group, int coverage_fit_failed, bsq_cov_columns* out) {
+                               int32_t read_group, int coverage_fit_failed, uint32_t n_read_groups,
+                               const int32_t* dp_group, bsq_cov_columns* out) {
   if (!ctx || !out) return fail(ctx, BSQ_ERR_INVALID, "null argument");
+  uint32_t dp[8];
+  int rc = dp_mask_groups(ctx, n_read_groups, dp_group, dp);
+  if (rc != BSQ_OK) return rc;
   host::CoverageRegion R;
-  const int rc = coverage_region(ctx, sample_id, tid, start_1, end_1, start_1, 1, R, read_group < 0 ? -1 : read_group,
-                                 coverage_fit_failed ? kCtImTabulate : kCtImPileup);
+  rc = coverage_region(ctx, sample_id, tid, start_1, end_1, start_1, 1, R, read_group < 0 ? -1 : read_group,
+                       coverage_fit_failed ? kCtImTabulate : kCtImPileup, dp);
   if (rc != BSQ_OK) return rc;
   uint32_t* const u32[4] = {out->unique_top, out->unique_bot, out->raw_redundant_top, out->raw_redundant_bot};
   for (int q = 0; q < 4; q++)
@@ -1632,25 +1647,36 @@ int bsq_im_coverage_columns_rg(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, ui
 
 int bsq_write_coverage_table_rg(bsq_ctx* ctx, int32_t sample_id, const char* path, const char* seq_id,
                                 const bsq_reference* ref, uint32_t tid, const bsq_position_arrays* positions,
-                                uint32_t n_read_groups, int coverage_fit_failed) {
+                                uint32_t n_read_groups, int coverage_fit_failed, const int32_t* dp_group) {
   if (!ctx || !path || !ref || !positions) return fail(ctx, BSQ_ERR_INVALID, "null argument");
   if (tid >= ref->n_targets) return fail(ctx, BSQ_ERR_INVALID, "target index out of range");
   if (n_read_groups > 0xFFFF) return fail(ctx, BSQ_ERR_INVALID, "more read groups than a record can name");
+  uint32_t dp[8];
+  int rc = dp_mask_groups(ctx, n_read_groups, dp_group, dp);
+  if (rc != BSQ_OK) return rc;
   const uint32_t len = (uint32_t)(ref->target_offset[tid + 1] - ref->target_offset[tid]);
   // _print_read_group_coverage: only with more than one read group (identify_mutations.cpp:862)
-  std::vector<host::CoverageRegion> per_rg;
-  if (n_read_groups > 1 && len > 0) {
-    per_rg.resize(n_read_groups);
-    for (uint32_t g = 0; g < n_read_groups; g++) {
-      const int rc = coverage_region(ctx, sample_id, tid, 1, len, 1, 1, per_rg[g], (int32_t)g,
-                                     coverage_fit_failed ? kCtImTabulate : kCtImPileup);
+  const uint32_t groups = n_read_groups > 1 && len > 0 ? n_read_groups : 0;
+  std::ofstream out(path);
+  if (!out) return fail(ctx, BSQ_ERR_INVALID, std::string("cannot write ") + path);
+  host::write_im_coverage_header(out, groups);
+  // the groups' columns come chunk by chunk, so host memory stays at one chunk per group
+  constexpr uint32_t kChunk = 1u << 20;
+  std::vector<host::CoverageRegion> per_rg(groups);
+  for (uint32_t a = 1; a <= len || (a == 1 && len == 0); a += kChunk) {
+    const uint32_t b = std::min<uint64_t>((uint64_t)a + kChunk - 1, len);
+    for (uint32_t g = 0; g < groups; g++) {
+      rc = coverage_region(ctx, sample_id, tid, a, b, a, 1, per_rg[g], (int32_t)g,
+                           coverage_fit_failed ? kCtImTabulate : kCtImPileup, dp);
       if (rc != BSQ_OK) return rc;
       per_rg[g].own();
     }
+    rc = host::write_im_coverage_rows(out, ref, tid, positions, a - 1, b, per_rg);
+    if (rc != BSQ_OK) return fail(ctx, rc, std::string("cannot write ") + path);
+    if (len == 0) break;
   }
   (void)seq_id;
-  const int rc = host::write_im_coverage_table(path, ref, tid, positions, per_rg);
-  if (rc != BSQ_OK) return fail(ctx, rc, std::string("cannot write ") + path);
+  if (!out.flush()) return fail(ctx, BSQ_ERR_INVALID, std::string("cannot write ") + path);
   return BSQ_OK;
 }
 

@@ -11,6 +11,7 @@ namespace bsq {
 namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr uint32_t kCtSkipFirst = 1u << 24;   // above flags | n_cigar << 8: the record skips its first column
 
 __device__ __forceinline__ void add_block(const CovTabArgs& A, int k, uint32_t a, uint32_t b) {
   // aligned columns [a, b) clipped to the region
@@ -101,6 +102,20 @@ __global__ void __launch_bounds__(256) ct_reads_kernel(const CovTabArgs A) {
         if (aligned || op == 2 || op == 3) x += len;    // consumes the reference
       }
       if (rev && unique && (last_q_op == 0 || last_q_op == 7 || last_q_op == 8)) first_col = last_q_end - 1;
+    }
+    // the discordant-pair enter step ends the per-read loop at the record's first column before its
+    // tally: take back what the record added there (a deletion or a base other than N)
+    if (kMode == kCtImPileup && (rd.flags & kDpCand) && rd.start >= A.c0 && rd.start < end_col &&
+        dp_group_member(A.dp_rg, __ldg(A.rg + r))) {
+      Pile e;
+      e.del = false;
+      e.qpos = (int)rd.clip;
+      bool counted = (rd.flags & kSimple) || resolve_cigar(A.cigar + rd.cigar_off, rd.n_cigar, rd.start, rd.start, e);
+      if (counted && !e.del) counted = (uint32_t)e.qpos < rd.len && nib_at(A.seq, rd.seq_off + (uint32_t)e.qpos) != 15;
+      if (counted) {
+        atomicAdd(A.diff + (uint64_t)k * A.stride + (rd.start - A.c0), -1);
+        atomicAdd(A.diff + (uint64_t)k * A.stride + (rd.start + 1 - A.c0), 1);
+      }
     }
     if (first_col >= A.c0 && first_col < end_col) atomicAdd(A.counts + (uint64_t)(4 + rev) * A.n + (first_col - A.c0), 1u);
   }
@@ -273,13 +288,16 @@ __global__ void __launch_bounds__(256) ct_redundant_kernel(const CovTabArgs A) {
               (A.rg_only >= 0 && (int32_t)__ldg(A.rg + r) != A.rg_only))
             end = 0;   // never covers
           else w = 1.0 / redundancy;
+          // left out of its first column (the discordant-pair enter step's `continue`)
+          if (kMode == kCtImPileup && (rd.flags & kDpCand) && dp_group_member(A.dp_rg, __ldg(A.rg + r)))
+            fl_nc |= kCtSkipFirst;
         }
         const uint32_t cnt = min(32u, hi - base);
         for (uint32_t j = 0; j < cnt; j++) {
           const uint32_t s_start = __shfl_sync(kFull, start, j), s_end = __shfl_sync(kFull, end, j);
           const uint32_t s_fl = __shfl_sync(kFull, fl_nc, j), s_coff = __shfl_sync(kFull, coff, j);
           const double s_w = __shfl_sync(kFull, w, j);
-          bool covers = in && s_start <= col && s_end > col;
+          bool covers = in && s_start <= col && s_end > col && !((s_fl & kCtSkipFirst) && col == s_start);
           if (kMode == kCtBam2cov) {
             if (covers && !(s_fl & kSimple)) {
               Pile e;

@@ -39,6 +39,10 @@ struct CovTabArgs {
   int32_t rg_only;             // >= 0: only this read group's records (--per-read-group columns)
   const uint8_t* seq;          // packed 4-bit bases (kCtIm* modes read them)
   uint32_t mode;               // kCtBam2cov, kCtImPileup or kCtImTabulate
+  uint32_t dp_rg[8];           // kCtImPileup: read groups with a discordant-pair group (256-bit mask);
+                               // their kDpCand records are left out of their first column, as the
+                               // per-read loop's `continue` (identify_mutations.cpp:1399-1416) leaves
+                               // them out of its tally
 };
 
 // Which pileup entries a column counts.

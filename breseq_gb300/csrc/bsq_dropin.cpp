@@ -388,7 +388,7 @@ void identify_mutations(const Settings& settings, const Summary& summary, const 
     for (uint32_t t : S.order) {
       const std::string path = Settings::file_name(settings.complete_coverage_text_file_name, "@", S.names[t]);
       check(bsq_write_coverage_table_rg(ctx(), S.sid, path.c_str(), S.names[t].c_str(), &S.ref, t, &pa,
-                                        (uint32_t)S.rg_ids.size(), deletion_propagation_cutoff[t] < 0.0),
+                                        (uint32_t)S.rg_ids.size(), deletion_propagation_cutoff[t] < 0.0, dp_group.data()),
             "write " + path);
     }
   // discordant-pair candidate regions, always written (identify_mutations.cpp:73)

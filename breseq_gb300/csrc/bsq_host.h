@@ -3,6 +3,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <ostream>
 #include <vector>
 
 #include "../../include/breseq_gb300.h"
@@ -79,6 +80,11 @@ struct CoverageRegion {
 // aggregate columns from pass 2's arrays, then each read group's (empty: none).  A BSQ_* status.
 int write_im_coverage_table(const char* path, const bsq_reference* ref, uint32_t tid, const bsq_position_arrays* pa,
                             const std::vector<CoverageRegion>& per_rg);
+// The same table in parts: the header for n_groups read groups, then the rows of target offsets
+// [lo, hi), each group's region holding exactly those positions.
+void write_im_coverage_header(std::ostream& out, size_t n_groups);
+int write_im_coverage_rows(std::ostream& out, const bsq_reference* ref, uint32_t tid, const bsq_position_arrays* pa,
+                           uint64_t lo, uint64_t hi, const std::vector<CoverageRegion>& per_rg);
 // The table's downsampling for a region and --resolution (coverage_output.cpp:203-209) and the first
 // position pileup_base::handle_position keeps, (position + start) % downsample == 0
 // (pileup_base.cpp:130-133).

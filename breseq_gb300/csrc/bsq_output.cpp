@@ -387,35 +387,47 @@ namespace host {
 // aggregate columns come from pass 2's per-position arrays (global columns); each read group's
 // columns, when given, from its region tally over positions 1..len (region offsets).  position_coverage
 // sums the strands bottom first (sum(), identify_mutations.h:99-126), and total_cov is the plain sum.
-int write_im_coverage_table(const char* path, const bsq_reference* ref, uint32_t tid, const bsq_position_arrays* pa,
-                            const std::vector<CoverageRegion>& per_rg) {
-  if (!path || !ref || !pa || tid >= ref->n_targets || !pa->unique_top || !pa->unique_bot || !pa->redundant_top ||
-      !pa->redundant_bot)
-    return BSQ_ERR_INVALID;
-  const uint64_t b = ref->target_offset[tid], e = ref->target_offset[tid + 1];
-  for (const CoverageRegion& R : per_rg)
-    if (R.m != e - b) return BSQ_ERR_INVALID;
-  std::ofstream out(path);
-  if (!out) return BSQ_ERR_INVALID;
+void write_im_coverage_header(std::ostream& out, size_t n_groups) {
   static const char* const kCols[3] = {"unique_cov", "redundant_cov", "total_cov"};
   out << "position\tref_base";
   for (const char* c : kCols) out << "\t" << c;
-  for (size_t g = 0; g < per_rg.size(); g++)      // group-major, as coverage_output::table
+  for (size_t g = 0; g < n_groups; g++)      // group-major, as coverage_output::table
     for (const char* c : kCols) out << "\tRG-" << g << "_" << c;
   out << "\n";
+}
+
+int write_im_coverage_rows(std::ostream& out, const bsq_reference* ref, uint32_t tid, const bsq_position_arrays* pa,
+                           uint64_t lo, uint64_t hi, const std::vector<CoverageRegion>& per_rg) {
+  if (!ref || !pa || tid >= ref->n_targets || !pa->unique_top || !pa->unique_bot || !pa->redundant_top ||
+      !pa->redundant_bot)
+    return BSQ_ERR_INVALID;
+  const uint64_t b = ref->target_offset[tid], e = ref->target_offset[tid + 1];
+  if (lo > hi || b + hi > e) return BSQ_ERR_INVALID;
+  for (const CoverageRegion& R : per_rg)
+    if (R.m != hi - lo) return BSQ_ERR_INVALID;
   auto cols = [&](uint32_t ut, uint32_t ub, double rt, double rb) {
     const double u = (double)ub + (double)ut;
     const double rr = rb + rt;
     out << "\t" << fmt_default(u) << "\t" << fmt_default(rr) << "\t" << fmt_default(u + rr);
   };
-  for (uint64_t g = b; g < e; g++) {
-    out << (g - b + 1) << "\t" << ref->seq[g];
+  for (uint64_t i = lo; i < hi; i++) {
+    const uint64_t g = b + i;
+    out << (i + 1) << "\t" << ref->seq[g];
     cols(pa->unique_top[g], pa->unique_bot[g], pa->redundant_top[g], pa->redundant_bot[g]);
-    const uint64_t i = g - b;
-    for (const CoverageRegion& R : per_rg) cols(R.counts[i], R.counts[R.m + i], R.red[i], R.red[R.m + i]);
+    const uint64_t k = i - lo;
+    for (const CoverageRegion& R : per_rg) cols(R.counts[k], R.counts[R.m + k], R.red[k], R.red[R.m + k]);
     out << "\n";
   }
   return out ? BSQ_OK : BSQ_ERR_INVALID;
+}
+
+int write_im_coverage_table(const char* path, const bsq_reference* ref, uint32_t tid, const bsq_position_arrays* pa,
+                            const std::vector<CoverageRegion>& per_rg) {
+  if (!path || !ref || tid >= ref->n_targets) return BSQ_ERR_INVALID;
+  std::ofstream out(path);
+  if (!out) return BSQ_ERR_INVALID;
+  write_im_coverage_header(out, per_rg.size());
+  return write_im_coverage_rows(out, ref, tid, pa, 0, ref->target_offset[tid + 1] - ref->target_offset[tid], per_rg);
 }
 
 }  // namespace host

@@ -577,16 +577,21 @@ int bsq_coverage_columns_rg(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint3
  * all), positions start_1..end_1 of target tid: at insert position 0 every pileup entry whose read base
  * is not N, deletions included (identify_mutations.cpp:1560-1610); where the target's coverage fit failed
  * (coverage_fit_failed != 0) tabulate_position_coverage's, which leaves deletions out too (:2218-2250).
+ * dp_group (n_read_groups entries, as bsq_im_params.dp_group; NULL: none): in the main-loop tally a
+ * record of a read group with a discordant-pair group that pass 2 leaves out of its first column
+ * (the `continue` at :1399-1416) is left out of that column's tally too.
  * Fills unique_*, raw_redundant_* and redundant_* of `out`; the begin counters are zeroed. */
 int bsq_im_coverage_columns_rg(bsq_ctx* ctx, int32_t sample_id, uint32_t tid, uint32_t start_1, uint32_t end_1,
-                               int32_t read_group, int coverage_fit_failed, bsq_cov_columns* out);
+                               int32_t read_group, int coverage_fit_failed, uint32_t n_read_groups,
+                               const int32_t* dp_group, bsq_cov_columns* out);
 /* <seq_id>.coverage.tsv (identify_mutations.cpp:2028-2052, 2173-2250; written under --predict-copy-number):
  * the aggregate columns from pass 2's per-position arrays, as bsq_write_coverage_table, and with more than
  * one read group (:862) each group's unique_cov / redundant_cov / total_cov prefixed "RG-<g>_", tallied on
- * the device by bsq_im_coverage_columns_rg over the resident sample. */
+ * the device by bsq_im_coverage_columns_rg over the resident sample, 2^20 positions at a time.
+ * dp_group: as for bsq_im_coverage_columns_rg (n_read_groups entries or NULL). */
 int bsq_write_coverage_table_rg(bsq_ctx* ctx, int32_t sample_id, const char* path, const char* seq_id,
                                 const bsq_reference* ref, uint32_t tid, const bsq_position_arrays* positions,
-                                uint32_t n_read_groups, int coverage_fit_failed);
+                                uint32_t n_read_groups, int coverage_fit_failed, const int32_t* dp_group);
 
 /* Launch shape of the passes.  None of the knobs changes a result: every count is an integer sum
  * and every column and candidate is scored by one warp whatever the grid. */

@@ -476,12 +476,13 @@ struct AlleleModel {
 // column, insert position 0, when it is paired, mapped, not a proper pair, neither secondary nor
 // supplementary, with a mapped mate, in a read group that has a DP group, and has no XP tag or an
 // orientation other than FR / RF / FF.
-inline bool dp_skip_at(const bsq_read_soa* rd, const bsq_im_params* p, uint64_t r, int64_t col) {
+inline bool dp_skip_at(const bsq_read_soa* rd, uint32_t n_read_groups, const int32_t* dp_group, uint64_t r,
+                       int64_t col) {
   if ((int64_t)rd->pos[r] != col) return false;
   const uint16_t f = rd->flag[r];
   if (!(f & 0x1) || (f & 0x4) || (f & 0x2) || (f & (0x100 | 0x800 | 0x8))) return false;
   const uint32_t g = rd->read_group[r];
-  if (g >= p->n_read_groups || p->dp_group[g] < 0) return false;      // dp_group_for(p, *i) < 0
+  if (!dp_group || g >= n_read_groups || dp_group[g] < 0) return false;   // dp_group_for(p, *i) < 0
   const uint8_t xp = rd->xp ? rd->xp[r] : (uint8_t)BSQ_XP_NONE;
   return xp != BSQ_XP_FR && xp != BSQ_XP_RF && xp != BSQ_XP_FF;
 }
@@ -738,7 +739,7 @@ struct SlotScorer {
       const uint64_t r = act[ii];
       const Pile& e = piles[ii];
       const ReadInfo& ri = d.info[r];
-      if (insert_count == 0 && dp_skip_at(rd, p, r, c)) continue;
+      if (insert_count == 0 && dp_skip_at(rd, p->n_read_groups, p->dp_group, r, c)) continue;
       int indel = e.indel;
       if (indel < 0) indel = 0;
       if (e.is_del) indel = -1;
@@ -1364,14 +1365,17 @@ extern "C" int oracle_coverage_columns(const bsq_reference* ref, const bsq_read_
 // (src/breseq/identify_mutations.cpp:1560-1610), where a deletion's read base is '.' and so counts, and an
 // N read base does not; or tabulate_position_coverage (:2218-2250) for a target whose coverage fit failed,
 // which skips deletions as well.  Per strand: unique count, Σ 1/X1 in pileup order, raw redundant count.
+// The main loop's tally comes after the discordant-pair enter step, whose `continue` (:1399-1416) leaves
+// a read out of its first column; tabulate_position_coverage has no such step.
 static void im_cov_columns(Data& d, uint32_t t, uint32_t start, uint32_t end, int32_t rg_only, bool failed,
-                           std::vector<CovCol>& cols) {
+                           uint32_t n_read_groups, const int32_t* dp_group, std::vector<CovCol>& cols) {
   const bsq_read_soa* rd = d.rd;
   cols.assign(end - start + 1, CovCol());
   walk_columns(d, t, (int64_t)start - 1, (int64_t)end, [&](int64_t c, const std::vector<uint64_t>& active) {
     CovCol& x = cols[c - ((int64_t)start - 1)];
     for (uint64_t r : active) {
       if (rg_only >= 0 && (int32_t)rd->read_group[r] != rg_only) continue;   // p.read_group_index(*i)
+      if (!failed && dp_skip_at(rd, n_read_groups, dp_group, r, c)) continue;
       Pile e;
       if (!resolve(rd, r, c, e)) continue;
       if (failed && e.is_del) continue;
@@ -1389,12 +1393,13 @@ static void im_cov_columns(Data& d, uint32_t t, uint32_t start, uint32_t end, in
 
 extern "C" int oracle_im_coverage_columns(const bsq_reference* ref, const bsq_read_soa* rd, uint32_t tid,
                                           uint32_t start, uint32_t end, int32_t read_group, int coverage_fit_failed,
+                                          uint32_t n_read_groups, const int32_t* dp_group,
                                           bsq_cov_columns* out, char* errbuf, int errcap) {
   Data d; d.ref = ref; d.rd = rd;
   int rc = prepare(d);
   if (rc) { if (errbuf) snprintf(errbuf, errcap, "%s", d.err.c_str()); return rc; }
   std::vector<CovCol> cols;
-  im_cov_columns(d, tid, start, end, read_group, coverage_fit_failed != 0, cols);
+  im_cov_columns(d, tid, start, end, read_group, coverage_fit_failed != 0, n_read_groups, dp_group, cols);
   for (size_t i = 0; i < cols.size(); i++) {
     if (out->unique_top) out->unique_top[i] = cols[i].u[0];
     if (out->unique_bot) out->unique_bot[i] = cols[i].u[1];
@@ -1413,13 +1418,15 @@ extern "C" int oracle_im_coverage_columns(const bsq_reference* ref, const bsq_re
 // columns "RG-<g>_..." from im_cov_columns.  Strands are summed as position_coverage::sum does.
 extern "C" int oracle_write_coverage_table_rg(const bsq_reference* ref, const bsq_read_soa* rd, const char* path,
                                               uint32_t tid, const bsq_position_arrays* pa, uint32_t n_read_groups,
-                                              int coverage_fit_failed, char* errbuf, int errcap) {
+                                              int coverage_fit_failed, const int32_t* dp_group, char* errbuf,
+                                              int errcap) {
   Data d; d.ref = ref; d.rd = rd;
   int rc = prepare(d);
   if (rc) { if (errbuf) snprintf(errbuf, errcap, "%s", d.err.c_str()); return rc; }
   const uint64_t b = ref->target_offset[tid], len = ref->target_offset[tid + 1] - b;
   std::vector<std::vector<CovCol>> rg(n_read_groups > 1 && len ? n_read_groups : 0);
-  for (uint32_t g = 0; g < rg.size(); g++) im_cov_columns(d, tid, 1, (uint32_t)len, (int32_t)g, coverage_fit_failed != 0, rg[g]);
+  for (uint32_t g = 0; g < rg.size(); g++)
+    im_cov_columns(d, tid, 1, (uint32_t)len, (int32_t)g, coverage_fit_failed != 0, n_read_groups, dp_group, rg[g]);
   FILE* f = fopen(path, "w");
   if (!f) return BSQ_ERR_INVALID;
   const char* names[3] = {"unique_cov", "redundant_cov", "total_cov"};

@@ -58,11 +58,11 @@ def lib():
                                                       C.c_uint32, C.POINTER(C.c_double), C.c_uint32, C.c_char_p,
                                                       C.c_int]
         L.oracle_im_coverage_columns.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.c_uint32,
-                                                 C.c_uint32, C.c_uint32, C.c_int32, C.c_int,
-                                                 C.POINTER(abi.CovColumns), C.c_char_p, C.c_int]
+                                                 C.c_uint32, C.c_uint32, C.c_int32, C.c_int, C.c_uint32,
+                                                 C.POINTER(C.c_int32), C.POINTER(abi.CovColumns), C.c_char_p, C.c_int]
         L.oracle_write_coverage_table_rg.argtypes = [C.POINTER(abi.Reference), C.POINTER(abi.ReadSoA), C.c_char_p,
                                                      C.c_uint32, C.POINTER(abi.PositionArrays), C.c_uint32, C.c_int,
-                                                     C.c_char_p, C.c_int]
+                                                     C.POINTER(C.c_int32), C.c_char_p, C.c_int]
         _lib = L
     return _lib
 
@@ -213,28 +213,34 @@ def coverage_columns(sample, tid, start, end):
     return arrs
 
 
-def im_coverage_columns(sample, tid, start, end, read_group=-1, coverage_fit_failed=False):
+def im_coverage_columns(sample, tid, start, end, read_group=-1, coverage_fit_failed=False, dp_group=()):
     """identify_mutations' coverage tally (main loop at insert position 0, or tabulate_position_coverage for
-    a failed coverage fit) restated on the CPU for positions start..end of target tid."""
+    a failed coverage fit) restated on the CPU for positions start..end of target tid.  dp_group: per read
+    group its discordant-pair group or -1."""
     view = abi.SampleView(sample)
     arrs, st = abi.cov_columns(end - start + 1)
     err = C.create_string_buffer(256)
+    dp = np.ascontiguousarray(dp_group, dtype=np.int32)
     rc = lib().oracle_im_coverage_columns(C.byref(view.ref), C.byref(view.reads), tid, start, end, read_group,
-                                          1 if coverage_fit_failed else 0, C.byref(st), err, 256)
+                                          1 if coverage_fit_failed else 0, len(dp),
+                                          abi.ptr(dp, C.c_int32) if len(dp) else None, C.byref(st), err, 256)
     if rc != 0:
         raise OracleError(f"oracle_im_coverage_columns failed ({rc}): {err.value.decode()}")
     return arrs
 
 
-def write_coverage_table(sample, path, tid, positions, n_read_groups=None, coverage_fit_failed=False):
+def write_coverage_table(sample, path, tid, positions, n_read_groups=None, coverage_fit_failed=False, dp_group=()):
     """<seq_id>.coverage.tsv from the aggregate per-position arrays plus each read group's columns."""
     view = abi.SampleView(sample)
     if n_read_groups is None:
         n_read_groups = int(np.max(sample.read_group)) + 1 if len(sample.read_group) else 1
+    dp = np.full(max(1, n_read_groups), -1, np.int32)
+    dp[:min(len(dp_group), len(dp))] = np.asarray(dp_group, dtype=np.int32)[:len(dp)]
     pa, keep = abi.position_arrays_view(positions)
     err = C.create_string_buffer(256)
     rc = lib().oracle_write_coverage_table_rg(C.byref(view.ref), C.byref(view.reads), path.encode(), tid,
-                                              C.byref(pa), n_read_groups, 1 if coverage_fit_failed else 0, err, 256)
+                                              C.byref(pa), n_read_groups, 1 if coverage_fit_failed else 0,
+                                              abi.ptr(dp, C.c_int32), err, 256)
     del keep
     if rc != 0:
         raise OracleError(f"oracle_write_coverage_table_rg failed ({rc}): {err.value.decode()}")

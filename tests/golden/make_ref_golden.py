@@ -25,6 +25,8 @@ CASES = {
     "ecoli_small_failed_fit": dict(sample="ecoli_small", prop_cutoff=[5.0, -1.0, 5.0]),
     "population_small": dict(sample="population_small", polymorphism=True),
     "dp_groups": dict(sample="dp_skip_sample", pmdd=[[0, 300.0, 20.0]]),
+    # two paired read groups, a discordant-pair group on the first only: per-read-group coverage columns
+    "dp_two_groups": dict(sample="dp_two_groups", pmdd=[[0, 300.0, 20.0]]),
     "ecoli_quarter": dict(sample="ecoli_quarter"),
     "population_deep": dict(sample="population_deep", polymorphism=True),
     # tabulate_soft_clipping_counts and BAM2COV tables (coverage_output::table) on the clipped sample

@@ -200,6 +200,21 @@ def dp_skip_sample():
                             no_xp_fraction=0.5)
 
 
+@functools.lru_cache(maxsize=None)
+def dp_two_groups():
+    """dp_skip_sample with a seeded 40% of its fragments (records 2k and 2k + 1) moved to a second
+    paired read group (read files 2 and 3): with a discordant-pair group on the first group only, the
+    coverage table's per-read-group columns show the first-column skip in one group and not the other."""
+    import dataclasses
+    import numpy as np
+    s = dp_skip_sample()
+    frag = np.arange(len(s.read_group)) // 2
+    move = np.random.default_rng(9).random(int(frag.max()) + 1 if len(frag) else 0)[frag] < 0.4
+    return dataclasses.replace(s, read_group=np.where(move, 1, s.read_group).astype(np.uint16),
+                               read_file=np.where(move, s.read_file + 2, s.read_file).astype(np.uint8),
+                               n_read_files=4)
+
+
 def dp_skip_reads(s, dp_group):
     """Indices of the records the discordant-pair enter step ends at their first column."""
     import numpy as np

@@ -21,7 +21,7 @@ from tests import samples
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden", "ref")
 SMALL = ["clonal_small", "ecoli_small", "ecoli_small_failed_fit", "population_small", "dp_groups",
-         "ecoli_quarter", "population_deep", "softclip_bam2cov"]
+         "ecoli_quarter", "population_deep", "softclip_bam2cov", "dp_two_groups"]
 DP_HEADER = "seq_id,start,end,strand,orientation,length,max_discordant_count,redundant,discordant_pairs\n"
 
 
@@ -123,7 +123,7 @@ def oracle_files(fx, tmp_path):
     for t in s.target_order:
         path = str(tmp_path / f"{s.target_names[t]}.coverage.tsv")
         po.write_coverage_table(s, path, int(t), im["positions"], n_read_groups=len(nfiles),
-                                coverage_fit_failed=bool(prop[t] < 0))
+                                coverage_fit_failed=bool(prop[t] < 0), dp_group=dp if widths else ())
         out[f"08_mutation_identification/{s.target_names[t]}.coverage.tsv"] = open(path).read()
     dp_file = "08_mutation_identification/DP_candidate_regions.csv"
     if s.xp is not None:

@@ -53,3 +53,47 @@ def test_im_coverage_tables(scorer, tmp_path):
                 assert open(pg).read() == open(po_).read(), (t, n_rg)
     finally:
         scorer.free_sample(sid)
+
+
+def test_im_tally_discordant_pair_skip(scorer):
+    # two paired read groups with a discordant-pair group on the first: that group's records without a
+    # usable XP tag leave their first column's tally, the other group's do not
+    from tests import samples
+    s = samples.dp_two_groups()
+    sid = scorer.load_sample(s)
+    try:
+        differs = False
+        for t in range(len(s.target_offset) - 1):
+            n = int(s.target_offset[t + 1] - s.target_offset[t])
+            for g in (-1, 0, 1):
+                got = scorer.im_coverage_columns(sid, t, 1, n, read_group=g, dp_group=(0, -1))
+                o = po.im_coverage_columns(s, t, 1, n, read_group=g, dp_group=(0, -1))
+                plain = po.im_coverage_columns(s, t, 1, n, read_group=g)
+                for k in IM_INT + IM_RED:
+                    assert np.array_equal(got[k], o[k]), (t, g, k)
+                differs |= any(not np.array_equal(o[k], plain[k]) for k in IM_INT)
+        assert differs
+    finally:
+        scorer.free_sample(sid)
+
+
+def test_im_coverage_table_in_chunks(scorer, tmp_path):
+    # a chromosome of 1.16 Mb is written in two chunks of positions per read group
+    import dataclasses
+    from breseq_gb300.api import ImSettings
+    from tests import samples
+    s = samples.ecoli_quarter()
+    g = np.where(np.random.default_rng(7).random(len(s.read_group)) < 0.3, 1, 0).astype(np.uint16)
+    s = dataclasses.replace(s, read_group=g)
+    assert int(s.target_offset[1] - s.target_offset[0]) > 1 << 20
+    ec = po.error_count(s)
+    tab = po.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
+    sid = scorer.load_sample(s)
+    try:
+        pos = scorer.identify_mutations(sid, tab, ImSettings(), positions=True)["positions"]
+        pg, po_ = str(tmp_path / "g.tsv"), str(tmp_path / "o.tsv")
+        scorer.write_coverage_table(sid, pg, 0, pos, n_read_groups=2)
+        po.write_coverage_table(s, po_, 0, pos, n_read_groups=2)
+        assert open(pg).read() == open(po_).read()
+    finally:
+        scorer.free_sample(sid)
