@@ -55,7 +55,7 @@ struct DevMem {
 };
 
 struct SampleDev {
-  DevMem ref, rcode, reads, x1, rg, qb, cigar, seq, qual, tile_range, d_tpoff, tgt_group, tgt_called, tgt_failed, rstart,
+  DevMem ref, refnib, reads, x1, rg, qb, cigar, seq, qual, tile_range, d_tpoff, tgt_group, tgt_called, tgt_failed, rstart,
       mapq;
   // pair annotations for the discordant / missing-pair scans: raw flags, XP codes, TLEN, names
   DevMem pflag, pxp, pisize, pqoff, pqname, pmtid, pmpos;
@@ -177,7 +177,7 @@ static cudaError_t upload(DevMem& m, const T* src, uint64_t n, cudaStream_t st) 
 static DevSample make_dev_sample(const SampleDev& s) {
   DevSample S;
   S.ref = s.ref.as<uint8_t>();
-  S.rcode = s.rcode.as<uint8_t>();
+  S.refnib = s.refnib.as<unsigned long long>();
   S.reads = s.reads.as<DevRead>();
   S.x1 = s.x1.as<uint32_t>();
   S.rg = s.rg.as<uint16_t>();
@@ -455,8 +455,9 @@ static int pack_sample(bsq_ctx* ctx, std::unique_ptr<SampleDev>& s, RecordsDev& 
   po.mapq = s->mapq.as<uint8_t>(); po.err = stats; po.maxspan = stats + 1; po.mapq_mask = stats + 2;
   CK(launch_pack(in, po, st));
   // the reference checked on the device: [11] bytes outside A/C/G/T/N, [12] zero bytes (separators)
-  CK(s->rcode.alloc(s->n_cols + 64, st));
-  CK(launch_ref_check(s->ref.as<uint8_t>(), s->rcode.as<uint8_t>(), s->n_cols, stats + 11, stats + 12, ctx->sms, st));
+  CK(s->refnib.alloc((size_t)refnib_words(s->n_cols) * 8, st));
+  CK(launch_ref_check(s->ref.as<uint8_t>(), s->refnib.as<unsigned long long>(), s->n_cols, stats + 11, stats + 12,
+                      ctx->sms, st));
   uint32_t h[16];
   CK(cudaMemcpyAsync(h, stats, 16 * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));

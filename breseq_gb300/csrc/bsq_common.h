@@ -49,7 +49,8 @@ struct QBounds { uint16_t qs0, qe0, qbs, qbe; };
 
 struct DevSample {
   const uint8_t* ref;         // padded reference chars
-  const uint8_t* rcode;       // the same columns as codes: A,C,G,T = 0..3, N = 4, separator = 5
+  const unsigned long long* refnib;   // the same columns as 4-bit codes: column c at nibble c + 16,
+                                      // A/C/G/T = 1/2/4/8, anything else 15
   const DevRead* reads;
   const uint32_t* x1;         // redundancy per read
   const uint16_t* rg;         // read group per read

@@ -275,60 +275,149 @@ __device__ __forceinline__ float f32x2_lo(unsigned long long x) { return __uint_
 __device__ __forceinline__ float f32x2_hi(unsigned long long x) { return __uint_as_float((uint32_t)(x >> 32)); }
 
 // count_alignment_position (error_count.cpp:888-944) for a read with one aligned block (soft clips
-// allowed): its bases are consecutive query positions on consecutive columns and no base has an indel,
-// so base i has event (1) and, when i is not the block's last base, event (2a).  Event (2a) of base i
-// reads base, quality and reference at i + 1 - rev: for a forward read those of base i + 1, for a
-// reverse read its own.  Both events of base j therefore test only base j's own values: (1) always,
-// and (2a) on behalf of base j - 1 (forward, j >= 1) or of base j itself (reverse, j below the last).
-// One lane per base, no neighbour exchange; reference characters are A/C/G/T/N (checked at load).
+// allowed), one thread per read: its bases are consecutive query positions on consecutive columns and
+// no base has an indel, so base i has event (1) and, when i is not the block's last base, event (2a).
+// Event (2a) of base i reads base, quality and reference at i + 1 - rev: for a forward read those of
+// base i + 1, for a reverse read its own.  Both events of base j therefore test only base j's own
+// values: (1) always, and (2a) on behalf of base j - 1 (forward, j >= 1) or of base j itself (reverse,
+// j below the last).
+// The thread walks the read in the 16-byte words of the quality array that hold it (a base's quality
+// index equals its nibble index in the packed sequence, so each word pairs with one 8-byte sequence
+// word), with the reference as 4-bit codes in the same nibble form, shifted into line with the word.
 // Most bases match the reference and carry a (2a) event: their two events (rs, b, b, q) and
 // (rs, '.', '.', q) are counted with one shared atomic in comb[(q * 4 + b) * R + rs], which the chunk's
-// flush adds to both bins.
-__device__ __forceinline__ void ec_simple_read(const DevSample& S, const EcArgs& A, uint32_t* hist, uint32_t* comb,
-                                               const DevRead& rd, uint32_t span, int lane, uint32_t& err) {
+// flush adds to both bins.  The rest go through the general per-base test.
+__device__ __forceinline__ uint32_t nib_code(uint32_t x) {   // one-hot nibble A/C/G/T -> 0..3
+  uint32_t d;
+  asm("bfind.u32 %0, %1;" : "=r"(d) : "r"(x));
+  return d;
+}
+__device__ __forceinline__ void ec_thread_read(const DevSample& S, const EcArgs& A, uint32_t* hist, uint32_t* comb,
+                                               const DevRead& rd, uint32_t span, uint32_t& err) {
   const bool rev = rd.flags & kRev;
   const uint32_t rs = rd.rfile, R = A.R, Q = A.Q;
   if (rs >= R) { err |= kErrCovariate; return; }
-  const uint32_t flip = rev ? 3u : 0u;              // 3 - x == x ^ 3 for x in 0..3
-  const uint32_t clip = rd.clip;
-  // this lane's bases are i = lane + 32 k, whose query positions all have the parity of clip + lane:
-  // the nibble shift is the lane's for the whole read (high nibble first)
-  const uint32_t sh = ((clip + (uint32_t)lane) & 1u) ? 0u : 4u;
-  const uint8_t* bp = S.seq + (rd.seq_off >> 1) + ((clip + (uint32_t)lane) >> 1);   // seq_off is even
-  const uint8_t* qp = S.qual + rd.seq_off + clip + (uint32_t)lane;
-  const uint8_t* rp = S.rcode + rd.start + (uint32_t)lane;
-  const uint32_t lo2 = rev ? 0u : 1u, hi2 = rev ? span - 1u : span;   // bases carrying a (2a) event
+  const uint32_t flip = rev ? 3u : 0u;                  // 3 - x == x ^ 3 for x in 0..3
+  const uint64_t qa = rd.seq_off + rd.clip;             // quality and nibble index of base 0 (seq_off is even)
+  const uint64_t w0 = qa >> 4, w1 = (qa + span + 15) >> 4;
+  const int off0 = (int)(qa & 15u);                     // slot of base 0 in the first word
+  // reference nibble of the column of slot 0 of word w0: column start - off0, stored at nibble + 16
+  const uint32_t cb0 = rd.start + 16u - (uint32_t)off0;
+  const uint32_t dsh = (cb0 & 15u) * 4u;                // bit offset of that nibble in its word
+  const unsigned long long* rw = S.refnib + (cb0 >> 4);
+  unsigned long long rlo = __ldg(rw);
+  const int lo2 = rev ? 0 : 1, hi2 = rev ? (int)span - 1 : (int)span;   // bases carrying a (2a) event
+  const uint32_t qR = 4u * R;
   bool bad_base = false, bad_q = false;
-#pragma unroll 2
-  for (uint32_t i = (uint32_t)lane; i < span; i += 32, bp += 16, qp += 32, rp += 32) {
-    const uint32_t ob = (__ldg(bp) >> sh) & 15u;
-    const uint32_t q = __ldg(qp);
-    const uint32_t rc = __ldg(rp);                   // A,C,G,T = 0..3, N = 4
-    const bool valid = ob != 15u && rc < 4u;          // neither the read base nor the reference is N
-    const bool base_ok = (0x116u >> ob) & 1u;        // one-hot: A, C, G or T
-    const bool q_ok = q < Q;
-    const bool in2 = i >= lo2 && i < hi2;
-    bad_base |= valid && !base_ok;
-    bad_q |= valid && !q_ok && (base_ok || in2);
-    const uint32_t oi = (31u - __clz(ob)) ^ flip, ri = rc ^ flip;
-    const uint32_t q25 = q * 25u;
-    const bool both = valid && base_ok && q_ok && in2 && oi == ri;
-    if (both) atomicAdd(comb + (q * 4u + ri) * R + rs, 1u);
-    else {
-      if (valid && base_ok && q_ok) atomicAdd(hist + (q25 + oi * 5u + ri) * R + rs, 1u);   // (ref, obs, q)
-      if (valid && q_ok && in2) atomicAdd(hist + (q25 + 24u) * R + rs, 1u);                 // ('.', '.', q)
+  int ilo = -off0;                                      // base index of slot 0 of the current word
+  for (uint64_t w = w0; w < w1; w++, ilo += 16, rw++) {
+    const uint4 qv = __ldg(reinterpret_cast<const uint4*>(S.qual) + w);
+    const uint2 sv = __ldg(reinterpret_cast<const uint2*>(S.seq) + w);
+    const unsigned long long rhi = __ldg(rw + 1);
+    const unsigned long long r64 = dsh ? (rlo >> dsh) | (rhi << (64u - dsh)) : rlo;
+    rlo = rhi;
+    const uint32_t rr[2] = {(uint32_t)r64, (uint32_t)(r64 >> 32)};
+    const uint32_t qq[4] = {qv.x, qv.y, qv.z, qv.w};
+    const uint32_t ss[2] = {sv.x, sv.y};
+    // slots of the read's bases, and of those with a (2a) event
+    const int a = min(max(-ilo, 0), 16), b = min(max((int)span - ilo, 0), 16);
+    const int a2 = min(max(lo2 - ilo, 0), 16), b2 = min(max(hi2 - ilo, 0), 16);
+    const uint32_t m_in = (0xFFFFu >> (16 - b)) & ~((1u << a) - 1u);
+    const uint32_t m_2 = (0xFFFFu >> (16 - b2)) & ~((1u << a2) - 1u);
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      const uint32_t q = (qq[k >> 2] >> (8 * (k & 3))) & 0xFFu;
+      // BAM packing: the even base of a byte in its high nibble
+      const uint32_t ob = (ss[k >> 3] >> (8 * ((k & 7) >> 1) + ((k & 1) ? 0 : 4))) & 15u;
+      const uint32_t rb = (rr[k >> 3] >> (4 * (k & 7))) & 15u;   // A,C,G,T one-hot, else 15
+      const bool in2 = (m_2 >> k) & 1u;
+      if (ob == rb && ob != 15u && in2 && q < Q) {
+        atomicAdd(comb + q * qR + (nib_code(rb) ^ flip) * R + rs, 1u);
+      } else if ((m_in >> k) & 1u) {
+        const bool valid = ob != 15u && rb != 15u;     // neither the read base nor the reference is N
+        const bool base_ok = (0x116u >> ob) & 1u;      // one-hot: A, C, G or T
+        const bool q_ok = q < Q;
+        bad_base |= valid && !base_ok;
+        bad_q |= valid && !q_ok && (base_ok || in2);
+        const uint32_t q25 = q * 25u;
+        if (valid && base_ok && q_ok)
+          atomicAdd(hist + (q25 + (nib_code(ob) ^ flip) * 5u + (nib_code(rb) ^ flip)) * R + rs, 1u);   // (ref, obs, q)
+        if (valid && q_ok && in2) atomicAdd(hist + (q25 + 24u) * R + rs, 1u);                          // ('.', '.', q)
+      }
     }
   }
   if (bad_base) err |= kErrBase;
   if (bad_q) err |= kErrCovariate;
 }
 
+// A read whose CIGAR has more than one aligned block: the CIGAR walk of htslib's pileup
+// (resolve_cigar2), M/=/X blocks carrying their read bases, the last base of a block seeing the I / D
+// run that follows it as its indel.  Lanes lane, lane + stride, ... of a block's bases; lane 0 adds the
+// coverage steps.
+__device__ __forceinline__ void ec_complex_read(const DevSample& S, const EcArgs& A, uint32_t* hist, const DevRead& rd,
+                                                uint32_t r, uint32_t lane, uint32_t stride, uint32_t& err) {
+  const bool red = rd.flags & kRedundant;
+  int32_t* diff = red ? A.diff_r : A.diff_u;
+  const uint32_t* cg = S.cigar + rd.cigar_off;
+  const int nc = rd.n_cigar;
+  uint32_t x = rd.start;
+  int y = 0;
+  const QBounds qb = S.qb[r];
+  for (int k = 0; k < nc; k++) {
+    const uint32_t w = __ldg(cg + k), op = w & 0xF, len = w >> 4;
+    if (op_qm(op)) {
+      int ind = 0;
+      if (k + 1 < nc) {
+        const uint32_t w2 = __ldg(cg + k + 1), op2 = w2 & 0xF;
+        if (op2 == 2) {
+          ind = -(int)(w2 >> 4);
+          for (int j = k + 2; j < nc; j++) { const uint32_t wj = __ldg(cg + j); if ((wj & 0xF) == 2) ind -= (int)(wj >> 4); else break; }
+        } else if (op2 == 1) {
+          ind = (int)(w2 >> 4);
+          for (int j = k + 2; j < nc; j++) {
+            const uint32_t wj = __ldg(cg + j), o = wj & 0xF;
+            if (o == 1) ind += (int)(wj >> 4); else if (o != 6) break;
+          }
+        } else if (op2 == 6 && k + 2 < nc) {
+          int l3 = 0;
+          for (int j = k + 2; j < nc; j++) {
+            const uint32_t wj = __ldg(cg + j), o = wj & 0xF;
+            if (o == 1) l3 += (int)(wj >> 4); else if (op_ref(o)) break;
+          }
+          if (l3 > 0) ind = l3;
+        }
+      }
+      if (lane == 0) {
+        atomicAdd(diff + x, 1);
+        atomicAdd(diff + x + len, -1);
+        if (A.preprocess && !red && y == 0 && read_start_counts(A, rd, (uint32_t)qb.qbs + 1u, (uint32_t)qb.qbe + 1u))
+          A.qs_flag[(size_t)(rd.flags & kRev) * S.n_cols + x] = 1;
+      }
+      if (!red && A.do_errors)
+        for (uint32_t i = lane; i < len; i += stride)
+          ec_events(S, A, hist, true, rd, r, x + i, y + (int)i, (i == len - 1) ? ind : 0, err);
+      x += len;
+      y += (int)len;
+    } else if (op_ref(op)) {
+      x += len;                      // D / N columns: deletions, skipped by error counting
+    } else if (op == 1 || op == 4) {
+      y += (int)len;
+    }
+  }
+}
+
+// Work units are chunks of one job's reads, pulled by whole blocks from a shared counter; the block's
+// shared histogram belongs to the chunk's job and is flushed at the chunk's end.  Reads with one
+// aligned block are taken one per thread; the others are queued and walked one per warp afterwards
+// (one per thread when the queue is full).
+constexpr uint32_t kEcQueue = 1024;
 __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Batch B, const uint4* chunks, uint32_t n_chunks, unsigned int* next) {
   extern __shared__ uint32_t sh_hist[];
-  __shared__ uint32_t sh_chunk;
+  __shared__ uint32_t sh_chunk, sh_nq;
+  __shared__ uint32_t sh_queue[kEcQueue];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (;;) {
-  if (threadIdx.x == 0) sh_chunk = atomicAdd(next, 1u);
+  if (threadIdx.x == 0) { sh_chunk = atomicAdd(next, 1u); sh_nq = 0; }
   __syncthreads();
   const uint32_t ci = sh_chunk;
   if (ci >= n_chunks) break;
@@ -340,75 +429,30 @@ __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Ba
   for (uint32_t i = threadIdx.x; i < nbins + ncomb; i += blockDim.x) sh_hist[i] = 0;
   __syncthreads();
   uint32_t err = 0;
-  uint32_t done = 0;
-  for (uint32_t r = ch.y + warp; r < ch.z; r += nwarps) {
+  for (uint32_t r = ch.y + threadIdx.x; r < ch.z; r += blockDim.x) {
     const DevRead rd = S.reads[r];
     if (rd.flags & kSkip) continue;      // filtered by flag, or on a target outside the pileup set
+    if (!(rd.flags & kSimple)) {
+      const uint32_t slot = atomicAdd(&sh_nq, 1u);
+      if (slot < kEcQueue) sh_queue[slot] = r;
+      else ec_complex_read(S, A, sh_hist, rd, r, 0, 1, err);
+      continue;
+    }
     const bool red = rd.flags & kRedundant;
     int32_t* diff = red ? A.diff_r : A.diff_u;
-    if (rd.flags & kSimple) {
-      const uint32_t span = rd.end - rd.start;
-      if (lane == 0) {
-        atomicAdd(diff + rd.start, 1);
-        atomicAdd(diff + rd.end, -1);
-        if (A.preprocess && !red && rd.clip == 0 && read_start_counts(A, rd, 1u, span))
-          A.qs_flag[(size_t)(rd.flags & kRev) * S.n_cols + rd.start] = 1;
-      }
-      if (red || !A.do_errors) continue;
-      ec_simple_read(S, A, sh_hist, sh_comb, rd, span, lane, err);
-      done += span;
-    } else {
-      // the CIGAR walk of htslib's pileup (resolve_cigar2): M/=/X blocks carry their read bases, the
-      // last base of a block sees the I / D run that follows it as its indel
-      const uint32_t* cg = S.cigar + rd.cigar_off;
-      const int nc = rd.n_cigar;
-      uint32_t x = rd.start;
-      int y = 0;
-      const QBounds qb = S.qb[r];
-      for (int k = 0; k < nc; k++) {
-        const uint32_t w = __ldg(cg + k), op = w & 0xF, len = w >> 4;
-        if (op_qm(op)) {
-          int ind = 0;
-          if (k + 1 < nc) {
-            const uint32_t w2 = __ldg(cg + k + 1), op2 = w2 & 0xF;
-            if (op2 == 2) {
-              ind = -(int)(w2 >> 4);
-              for (int j = k + 2; j < nc; j++) { const uint32_t wj = __ldg(cg + j); if ((wj & 0xF) == 2) ind -= (int)(wj >> 4); else break; }
-            } else if (op2 == 1) {
-              ind = (int)(w2 >> 4);
-              for (int j = k + 2; j < nc; j++) {
-                const uint32_t wj = __ldg(cg + j), o = wj & 0xF;
-                if (o == 1) ind += (int)(wj >> 4); else if (o != 6) break;
-              }
-            } else if (op2 == 6 && k + 2 < nc) {
-              int l3 = 0;
-              for (int j = k + 2; j < nc; j++) {
-                const uint32_t wj = __ldg(cg + j), o = wj & 0xF;
-                if (o == 1) l3 += (int)(wj >> 4); else if (op_ref(o)) break;
-              }
-              if (l3 > 0) ind = l3;
-            }
-          }
-          if (lane == 0) {
-            atomicAdd(diff + x, 1);
-            atomicAdd(diff + x + len, -1);
-            if (A.preprocess && !red && y == 0 && read_start_counts(A, rd, (uint32_t)qb.qbs + 1u, (uint32_t)qb.qbe + 1u))
-              A.qs_flag[(size_t)(rd.flags & kRev) * S.n_cols + x] = 1;
-          }
-          if (!red && A.do_errors) {
-            for (uint32_t i = lane; i < len; i += 32)
-              ec_events(S, A, sh_hist, true, rd, r, x + i, y + (int)i, (i == len - 1) ? ind : 0, err);
-            done += len;
-          }
-          x += len;
-          y += (int)len;
-        } else if (op_ref(op)) {
-          x += len;                      // D / N columns: deletions, skipped by error counting
-        } else if (op == 1 || op == 4) {
-          y += (int)len;
-        }
-      }
-    }
+    const uint32_t span = rd.end - rd.start;
+    atomicAdd(diff + rd.start, 1);
+    atomicAdd(diff + rd.end, -1);
+    if (A.preprocess && !red && rd.clip == 0 && read_start_counts(A, rd, 1u, span))
+      A.qs_flag[(size_t)(rd.flags & kRev) * S.n_cols + rd.start] = 1;
+    if (red || !A.do_errors) continue;
+    ec_thread_read(S, A, sh_hist, sh_comb, rd, span, err);
+  }
+  __syncthreads();
+  const uint32_t nq = min(sh_nq, kEcQueue);
+  for (uint32_t k = warp; k < nq; k += nwarps) {
+    const uint32_t r = sh_queue[k];
+    ec_complex_read(S, A, sh_hist, S.reads[r], r, lane, 32, err);
   }
   __syncthreads();
   // combined counts of (rs, b, b, q) + (rs, '.', '.', q) into both bins
@@ -426,7 +470,6 @@ __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Ba
     if (v) atomicAdd(A.counts + i, (unsigned long long)v);
   }
   if (err) atomicOr(A.err, err);
-  (void)done;
   __syncthreads();
   }
 }
@@ -1047,15 +1090,27 @@ static int grid_for(uint32_t work, int per_block, int sms, int min_blocks_per_sm
 
 // Reference characters of the padded column space: every byte of a target is one of A/C/G/T/N and
 // the only zero bytes are the one separator after each target.  Counts both kinds for the host and
-// writes the column codes the pass-1 kernel reads.
-__global__ void ref_check_kernel(const uint8_t* ref, uint8_t* rcode, uint32_t n_cols, uint32_t* bad, uint32_t* zeros) {
+// writes the 4-bit column codes the pass-1 kernel reads: column c at nibble c + 16 of `refnib` (16
+// columns per 64-bit word, the lowest nibble first), A/C/G/T one-hot (1, 2, 4, 8, as BAM codes them),
+// anything else 15.  Thread j writes word j.
+__global__ void ref_check_kernel(const uint8_t* ref, unsigned long long* refnib, uint32_t n_cols, uint32_t n_words,
+                                 uint32_t* bad, uint32_t* zeros) {
   uint32_t nb = 0, nz = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_cols; i += gridDim.x * blockDim.x) {
-    const uint8_t ch = __ldg(ref + i);
-    nz += ch == 0;
-    const uint8_t code = ch == 'A' ? 0 : ch == 'C' ? 1 : ch == 'G' ? 2 : ch == 'T' ? 3 : ch == 'N' ? 4 : ch == 0 ? 5 : 6;
-    nb += code == 6;
-    rcode[i] = code;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_words; j += gridDim.x * blockDim.x) {
+    unsigned long long word = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      const int64_t c = (int64_t)j * 16 + k - 16;
+      uint32_t nib = 15;
+      if (c >= 0 && c < (int64_t)n_cols) {
+        const uint8_t ch = __ldg(ref + c);
+        nz += ch == 0;
+        nib = ch == 'A' ? 1 : ch == 'C' ? 2 : ch == 'G' ? 4 : ch == 'T' ? 8 : 15;
+        nb += !(nib != 15 || ch == 'N' || ch == 0);
+      }
+      word |= (unsigned long long)nib << (4 * k);
+    }
+    refnib[j] = word;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -1067,9 +1122,9 @@ __global__ void ref_check_kernel(const uint8_t* ref, uint8_t* rcode, uint32_t n_
     if (nz) atomicAdd(zeros, nz);
   }
 }
-cudaError_t launch_ref_check(const uint8_t* ref, uint8_t* rcode, uint32_t n_cols, uint32_t* bad, uint32_t* zeros, int sms,
-                             cudaStream_t st) {
-  ref_check_kernel<<<sms * 4, 256, 0, st>>>(ref, rcode, n_cols, bad, zeros);
+cudaError_t launch_ref_check(const uint8_t* ref, unsigned long long* refnib, uint32_t n_cols, uint32_t* bad,
+                             uint32_t* zeros, int sms, cudaStream_t st) {
+  ref_check_kernel<<<sms * 4, 256, 0, st>>>(ref, refnib, n_cols, refnib_words(n_cols), bad, zeros);
   return cudaGetLastError();
 }
 cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st) {

@@ -44,9 +44,12 @@ struct PackOut {
 
 cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st);
 // Counts reference bytes outside A/C/G/T/N/separator into *bad and zero bytes into *zeros, and writes
-// each column's code (A,C,G,T = 0..3, N = 4, separator = 5, other = 6) to rcode.
-cudaError_t launch_ref_check(const uint8_t* ref, uint8_t* rcode, uint32_t n_cols, uint32_t* bad, uint32_t* zeros, int sms,
-                             cudaStream_t st);
+// each column's 4-bit code (A,C,G,T = 1,2,4,8, anything else 15) into refnib.
+// Words of the nibble-packed reference (column c at nibble c + 16), with one spare word after the last
+// column a thread may read past.
+inline uint32_t refnib_words(uint32_t n_cols) { return (n_cols + 16u) / 16u + 2u; }
+cudaError_t launch_ref_check(const uint8_t* ref, unsigned long long* refnib, uint32_t n_cols, uint32_t* bad,
+                             uint32_t* zeros, int sms, cudaStream_t st);
 cudaError_t launch_mapq_index(DevRead* reads, const uint8_t* mapq, const uint8_t* map, uint32_t n, cudaStream_t st);
 cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t n_tiles, uint32_t maxspan,
                               uint2* tile_range, uint32_t* max_tile_reads, cudaStream_t st);
