@@ -59,11 +59,12 @@ sys.path.insert(0, ROOT)
 METRIC = "read-bases/s scored, served vs plain on same GPU (identical calls); p50/p99 ms"
 UNIT = "read-bases/s"
 WORKLOAD = "ecoli_clonal_4.79Mb_pe150_2x100x"
-# DRAM bytes (read + write) per aligned read-base of one launch, from an ncu capture of the same
-# workload at 0.25x genome length (profiles/im_column_kernel_ecoli_clonal_x0.25.md,
-# profiles/ec_read_kernel_ecoli_clonal_x0.25.md), scaled linearly with read-bases
-IM_COLUMN_DRAM_PER_BASE = 0.5843e9 / 0.2441e9
-EC_READ_DRAM_PER_BASE = 0.4251e9 / 0.2441e9
+# DRAM bytes (read + write) per aligned read-base of one launch: ncu's dram__bytes_read.sum +
+# dram__bytes_write.sum for one launch of each kernel on the same workload at 0.25x genome length
+# (0.2441 G read-bases), scaled linearly with read-bases (both kernels read every base and quality
+# once, and the per-read and per-column bytes grow with them at a fixed coverage)
+IM_COLUMN_DRAM_PER_BASE = (445.418240e6 + 50.217728e6) / 0.2441e9
+EC_READ_DRAM_PER_BASE = (418.198016e6 + 9.134592e6) / 0.2441e9
 # the plain FP64 form: same kernels, FP64 everywhere, one sample per call, launched without graphs
 PLAIN_TUNING = dict(ec_read_chunk=1024, ec_blocks_per_sm=8, col_blocks_per_sm=8, cand_warps_per_sm=16,
                     bound_warps_per_sm=4, use_graphs=0)
@@ -153,14 +154,14 @@ def _workload(seed: int, scale: float = 1.0):
 
 
 SC_WORKLOAD = "ecoli_4.79Mb_pe150_2x100x_50breakpoints_1pct_long_clips"
-# DRAM bytes (read + write) of one launch of the tabulation's count pass per record, from the ncu
-# capture of the same workload (profiles/sc_kernels_ecoli_breakpoints_4.79Mb.md)
+# DRAM bytes (read + write) of one launch of the tabulation's count pass per record, from an ncu
+# capture of one launch on the same workload
 SC_READS_DRAM_PER_READ = (230.080768e6 + 14.4256e6) / 6416810
-# DRAM bytes of the four main coverage-table kernels over their algorithmic bytes, from the ncu capture
-# of the same chromosome (profiles/coverage_table_kernels_ecoli_chromosome_4.63Mb.md)
+# DRAM bytes of the four main coverage-table kernels over their algorithmic bytes, from an ncu capture
+# of one call on the same chromosome
 COV_TABLE_DRAM_OVER_ALGORITHMIC = 580.482284e6 / (32 * 6206454 + 80 * 4630000)
-# DRAM bytes of one pair-classification launch per record, from the ncu capture of the same workload at
-# half the genome length, timed call (profiles/pair_scan_kernels_ecoli_pairs_x0.5.md)
+# DRAM bytes of one pair-classification launch per record, from an ncu capture of the same workload at
+# half the genome length
 PAIR_CLASSIFY_DRAM_PER_READ = (116.804608e6 + 10.306816e6) / 3223958
 
 

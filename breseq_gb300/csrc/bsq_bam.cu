@@ -12,6 +12,7 @@ namespace bsq {
 namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr bool kLaneInflate = false;  // one thread per block (bgzf_lane_kernel) rather than one warp
 
 int grid_for(uint64_t units, uint32_t per_block, int sms, int per_sm) {
   const uint64_t need = (units + per_block - 1) / per_block;
@@ -102,6 +103,77 @@ __global__ void __launch_bounds__(kInfWarps * 32) bgzf_inflate_kernel(const uint
     c ^= 0xFFFFFFFFu;
     uint32_t total = __shfl_sync(kFull, c, 0);
     // every lane walks the combination, so the shuffles stay warp-wide
+    const uint32_t shift_full = inflate::gf2_x8n(slice);
+    for (int j = 1; j < 32; j++) {
+      const uint32_t cj = __shfl_sync(kFull, c, j);
+      const uint32_t bj0 = min(B.isize, (uint32_t)j * slice), bj1 = min(B.isize, bj0 + slice);
+      const uint32_t lj = bj1 - bj0;
+      if (lj == 0) continue;
+      total = inflate::gf2_mulmod(lj == slice ? shift_full : inflate::gf2_x8n(lj), total) ^ cj;
+    }
+    if (lane == 0 && total != B.crc) {
+      atomicOr(err, kBamCrc);
+      atomicMin(first_bad, b);
+    }
+  }
+}
+
+// One thread per BGZF block (inflate_lane: the block's Huffman codes in the thread's own tables in
+// shared memory, output straight to the stream in 16-byte chunks), 32 blocks per warp.
+constexpr int kLaneThreads = 32;
+__global__ void __launch_bounds__(kLaneThreads) bgzf_lane_kernel(const uint8_t* file, const BgzfBlock* blocks,
+                                                                 uint32_t n, uint8_t* out, uint32_t* err,
+                                                                 uint32_t* first_bad) {
+  extern __shared__ __align__(16) unsigned char lane_smem[];
+  inflate::LaneTables& T = reinterpret_cast<inflate::LaneTables*>(lane_smem)[threadIdx.x];
+  // every lane runs every iteration of the loop (a lane without a block idles in kLaneDone), and the
+  // warp reconverges after each decoder step, so the lanes' steps run side by side
+  for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < n; b0 += gridDim.x * blockDim.x) {
+    const uint32_t b = b0 + threadIdx.x;
+    inflate::LaneState z;
+    BgzfBlock B;
+    if (b < n) {
+      B = blocks[b];
+      inflate::lane_start(z, file + B.in_off, B.in_len, out + B.out_off, B.isize);
+    } else {
+      z.mode = inflate::kLaneDone;
+      z.err = inflate::kOk;
+    }
+    while (__any_sync(kFull, z.mode != inflate::kLaneDone)) {
+      inflate::lane_step(z, T);
+      __syncwarp();
+    }
+    if (b < n) {
+      inflate::lane_finish(z, T);
+      if (z.err != inflate::kOk || z.w.n != B.isize) {
+        atomicOr(err, kBamInflate);
+        atomicMin(first_bad, b);
+      }
+    }
+  }
+}
+
+// The CRC-32 of every inflated block against its trailer, one warp per block: each lane takes the CRC
+// of a 1/32 slice, and the slices are combined in order.
+__global__ void __launch_bounds__(256) bgzf_crc_kernel(const uint8_t* out, const BgzfBlock* blocks, uint32_t n,
+                                                       uint32_t* err, uint32_t* first_bad) {
+  __shared__ uint32_t crc_table[256];
+  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) {
+    uint32_t c = i;
+    for (int k = 0; k < 8; k++) c = (c & 1) ? inflate::kCrcPoly ^ (c >> 1) : c >> 1;
+    crc_table[i] = c;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < n; b += (gridDim.x * blockDim.x) >> 5) {
+    const BgzfBlock B = blocks[b];
+    const uint8_t* o = out + B.out_off;
+    const uint32_t slice = (B.isize + 31) / 32;
+    const uint32_t a0 = min(B.isize, lane * slice), a1 = min(B.isize, a0 + slice);
+    uint32_t c = 0xFFFFFFFFu;
+    for (uint32_t k = a0; k < a1; k++) c = crc_table[(c ^ __ldg(o + k)) & 0xFF] ^ (c >> 8);
+    c ^= 0xFFFFFFFFu;
+    uint32_t total = __shfl_sync(kFull, c, 0);
     const uint32_t shift_full = inflate::gf2_x8n(slice);
     for (int j = 1; j < 32; j++) {
       const uint32_t cj = __shfl_sync(kFull, c, j);
@@ -399,8 +471,18 @@ __global__ void __launch_bounds__(256) scan_apply_kernel(const uint32_t* in, uin
 
 cudaError_t bam_inflate(const uint8_t* file, const BgzfBlock* blocks, uint32_t n_blocks, uint8_t* out, uint32_t* err,
                         uint32_t* first_bad, int sms, cudaStream_t st) {
-  if (n_blocks)
+  if (!n_blocks) return cudaSuccess;
+  if (kLaneInflate) {
+    // 32 threads' tables per block: 3 blocks fit an SM's shared memory
+    const size_t smem = kLaneThreads * sizeof(inflate::LaneTables);
+    cudaError_t e = cudaFuncSetAttribute(bgzf_lane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    bgzf_lane_kernel<<<grid_for(n_blocks, kLaneThreads, sms, 3), kLaneThreads, smem, st>>>(file, blocks, n_blocks, out, err,
+                                                                                          first_bad);
+    bgzf_crc_kernel<<<grid_for(n_blocks, 8, sms, 8), 256, 0, st>>>(out, blocks, n_blocks, err, first_bad);
+  } else {
     bgzf_inflate_kernel<<<grid_for(n_blocks, kInfWarps, sms, 8), kInfWarps * 32, 0, st>>>(file, blocks, n_blocks, out, err, first_bad);
+  }
   return cudaGetLastError();
 }
 

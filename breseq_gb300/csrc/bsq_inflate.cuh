@@ -504,6 +504,352 @@ BSQ_HD void z_run(Inflater& state, Tables& T, Codes& K, uint8_t* ring, const uin
   state = z;
 }
 
+// ----------------------------------------------------------------------------- one-lane decoder
+// The same format decoded whole by one thread with its own small tables, so that a warp decodes 32
+// blocks at once (one per lane) instead of one block on one lane.  Per thread: 9-bit and 6-bit
+// lookup tables for literal/length and distance codes (a longer code falls back to the canonical
+// decode from the code's counts and symbols), and a 64-byte output ring indexed by output address.
+// Output goes to out[] in 16-byte aligned chunks, each stored once complete (the block's partial
+// first and last chunks byte by byte: a neighbouring block's thread writes the rest of them); a
+// back-reference of at most 64 bytes reads the ring, an older one reads out[], which by then holds
+// it.  Input: a 64-bit bit buffer refilled four bytes at a time from aligned 32-bit loads.
+
+constexpr int kLaneLitBits = 9, kLaneDistBits = 6;
+constexpr uint32_t kLaneRing = 64;
+
+// A canonical code: counts per length, symbols in (length, value) order (RFC 1951 §3.2.2).
+struct LaneCode {
+  uint16_t count[kMaxBits + 1];
+  uint16_t symbol[288];
+};
+struct LaneDistCode {
+  uint16_t count[kMaxBits + 1];
+  uint16_t symbol[32];
+};
+// Per-thread tables (2.1 KB; the device keeps them in shared memory).
+struct LaneTables {
+  uint16_t lit[1 << kLaneLitBits];     // (length << 9) | symbol, 0 = not in the table
+  uint16_t dist[1 << kLaneDistBits];
+  LaneCode lc;                         // literal/length code; during a header, the code-length code
+  LaneDistCode dc;
+  uint8_t lengths[288 + 32];
+  alignas(16) uint8_t ring[kLaneRing];   // the last 64 output bytes, at (address & 63)
+};
+
+struct LaneIn {
+  const uint8_t* in;
+  uint32_t len, pos;                   // bytes of the block; bytes moved into buf
+  uint64_t buf;
+  int cnt;
+};
+
+// Four bytes at in[pos] from the two aligned words that hold them (in[] is readable up to 3 bytes
+// past the block, which the file's allocation guarantees); one byte at a time near the end.
+BSQ_HD void lane_refill(LaneIn& b) {
+  if (b.cnt > 32) return;
+  if (b.pos + 4 <= b.len) {
+    const uintptr_t a = (uintptr_t)(b.in + b.pos);
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(a & ~(uintptr_t)3);
+    const uint32_t sh = (uint32_t)(a & 3) * 8;
+#ifdef __CUDA_ARCH__
+    const uint32_t lo = __ldg(w), hi = sh ? __ldg(w + 1) : 0u;
+#else
+    const uint32_t lo = w[0], hi = sh ? w[1] : 0u;
+#endif
+    const uint32_t v = sh ? (lo >> sh) | (hi << (32 - sh)) : lo;
+    b.buf |= (uint64_t)v << b.cnt;
+    b.cnt += 32;
+    b.pos += 4;
+    return;
+  }
+  while (b.cnt <= 56 && b.pos < b.len) {
+    b.buf |= (uint64_t)b.in[b.pos++] << b.cnt;
+    b.cnt += 8;
+  }
+}
+
+// k <= 16 bits; past the end of the block sets err.
+BSQ_HD uint32_t lane_bits(LaneIn& b, int k, int& err) {
+  if (k == 0) return 0;
+  if (b.cnt < k) { lane_refill(b); if (b.cnt < k) { err = kErrInput; return 0; } }
+  const uint32_t v = (uint32_t)(b.buf & ((1u << k) - 1));
+  b.buf >>= k;
+  b.cnt -= k;
+  return v;
+}
+
+// Counts and symbols of a canonical code from n code lengths; false when over-subscribed.
+template <int kSyms>
+BSQ_HD bool lane_code(uint16_t* count, uint16_t* symbol, const uint8_t* lengths, int n) {
+  for (int l = 0; l <= kMaxBits; l++) count[l] = 0;
+  for (int s = 0; s < n; s++) count[lengths[s]]++;
+  int left = 1;
+  for (int l = 1; l <= kMaxBits; l++) {
+    left = (left << 1) - count[l];
+    if (left < 0) return false;
+  }
+  uint16_t offs[kMaxBits + 1];
+  offs[1] = 0;
+  for (int l = 1; l < kMaxBits; l++) offs[l + 1] = offs[l] + count[l];
+  for (int s = 0; s < n; s++)
+    if (lengths[s] != 0 && offs[lengths[s]] < kSyms) symbol[offs[lengths[s]]++] = (uint16_t)s;
+  return true;
+}
+
+// The k-bit lookup table of a code: each code of at most k bits, bit-reversed, fills its entries.
+BSQ_HD void lane_table(uint16_t* table, int k, const uint8_t* lengths, int n, const uint16_t* count) {
+  for (int i = 0; i < (1 << k); i++) table[i] = 0;
+  uint32_t next[kMaxBits + 1];
+  uint32_t code = 0;
+  next[0] = 0;
+  for (int l = 1; l <= kMaxBits; l++) {
+    code = (code + (l > 1 ? count[l - 1] : 0u)) << 1;
+    next[l] = code;
+  }
+  for (int s = 0; s < n; s++) {
+    const int l = lengths[s];
+    if (l == 0) continue;
+    const uint32_t cd = next[l]++;
+    if (l > k) continue;
+    uint32_t rev = 0;
+    for (int b = 0; b < l; b++) rev |= ((cd >> b) & 1u) << (l - 1 - b);
+    for (uint32_t f = rev; f < (1u << k); f += 1u << l) table[f] = (uint16_t)((l << 9) | s);
+  }
+}
+
+// One symbol through the table, or the canonical decode for a code longer than it.  -1 on failure.
+BSQ_HD int lane_symbol(LaneIn& b, const uint16_t* table, int k, const uint16_t* count, const uint16_t* symbol,
+                       int nsym, int& err) {
+  if (b.cnt < kMaxBits) lane_refill(b);
+  const uint16_t e = table[b.buf & ((1u << k) - 1)];
+  if (e) {
+    const int l = e >> 9;
+    if (l > b.cnt) { err = kErrInput; return -1; }
+    b.buf >>= l;
+    b.cnt -= l;
+    return e & 511;
+  }
+  int code = 0, first = 0, index = 0;
+  for (int l = 1; l <= kMaxBits; l++) {
+    code |= (int)lane_bits(b, 1, err);
+    if (err) return -1;
+    const int c = count[l];
+    if (code - first < c) {
+      const int i = index + (code - first);
+      if (i >= nsym) { err = kErrCode; return -1; }
+      return symbol[i];
+    }
+    index += c;
+    first += c;
+    first <<= 1;
+    code <<= 1;
+  }
+  err = kErrCode;
+  return -1;
+}
+
+// Output of one block: bytes o[0, cap), the ring, the partial first chunk.
+struct LaneOut {
+  uint8_t* o;
+  uint32_t n, cap;
+};
+
+// Stores the chunk that ends at output address a (16-byte aligned): whole when it lies inside the
+// block, else the block's own bytes of it.
+BSQ_HD void lane_store_chunk(LaneTables& T, const LaneOut& w, uintptr_t a) {
+  const uintptr_t lo = a - 16, b0 = (uintptr_t)w.o, b1 = (uintptr_t)(w.o + w.n);
+  const uint8_t* src = T.ring + (lo & (kLaneRing - 1));
+  if (lo >= b0 && a <= b1) {
+#ifdef __CUDA_ARCH__
+    *reinterpret_cast<uint4*>(lo) = *reinterpret_cast<const uint4*>(src);
+#else
+    for (int j = 0; j < 16; j++) reinterpret_cast<uint8_t*>(lo)[j] = src[j];
+#endif
+  } else {
+    for (uintptr_t x = lo < b0 ? b0 : lo; x < a && x < b1; x++) *reinterpret_cast<uint8_t*>(x) = src[x - lo];
+  }
+}
+
+BSQ_HD void lane_emit(LaneTables& T, LaneOut& w, uint8_t v) {
+  const uintptr_t a = (uintptr_t)(w.o + w.n);
+  T.ring[a & (kLaneRing - 1)] = v;
+  w.n++;
+  if (((a + 1) & 15) == 0) lane_store_chunk(T, w, a + 1);
+}
+
+// The byte d back from the next output position (1 <= d <= n).
+BSQ_HD uint8_t lane_back(const LaneTables& T, const LaneOut& w, uint32_t d) {
+  const uintptr_t a = (uintptr_t)(w.o + w.n) - d;
+  if (d <= kLaneRing) return T.ring[a & (kLaneRing - 1)];
+  return *reinterpret_cast<const uint8_t*>(a);   // stored at least 48 bytes ago by this thread
+}
+
+// The decoder as a state machine of short steps, so that the 32 lanes of a warp, each in its own
+// block, run the same loop iteration by iteration (the device loop reconverges the warp after every
+// step): a block header with its tables, one Huffman symbol (a literal, or a length and distance
+// that start a copy), up to 8 bytes of a copy, or up to 8 stored bytes.
+enum : int { kLaneHeader = 0, kLaneStored = 1, kLaneSymbol = 2, kLaneCopy = 3, kLaneDone = 4 };
+struct LaneState {
+  LaneIn b;
+  LaneOut w;
+  int mode, last, err;
+  uint32_t left, dist;      // stored or copy bytes left; copy distance
+};
+
+BSQ_HD void lane_start(LaneState& z, const uint8_t* in, uint32_t in_len, uint8_t* out, uint32_t cap) {
+  z.b.in = in; z.b.len = in_len; z.b.pos = 0; z.b.buf = 0; z.b.cnt = 0;
+  z.w.o = out; z.w.n = 0; z.w.cap = cap;
+  z.mode = kLaneHeader; z.last = 0; z.err = kOk; z.left = 0; z.dist = 0;
+}
+
+// A block header: its type, and for Huffman blocks the code lengths and tables.
+BSQ_HD void lane_header(LaneState& z, LaneTables& T) {
+  LaneIn& b = z.b;
+  int& err = z.err;
+  z.last = (int)lane_bits(b, 1, err);
+  const uint32_t type = lane_bits(b, 2, err);
+  if (err) return;
+  if (type == 0) {
+    // stored: the rest of the current byte is skipped, then LEN, NLEN and the bytes
+    const int drop = b.cnt & 7;
+    b.buf >>= drop;
+    b.cnt -= drop;
+    const uint32_t len = lane_bits(b, 16, err), nlen = lane_bits(b, 16, err);
+    if (err) return;
+    if (len != (~nlen & 0xFFFFu)) { err = kErrStored; return; }
+    if (len > z.w.cap - z.w.n) { err = kErrOutput; return; }
+    z.left = len;
+    z.mode = kLaneStored;
+  } else if (type == 1) {
+    for (int s = 0; s < 144; s++) T.lengths[s] = 8;
+    for (int s = 144; s < 256; s++) T.lengths[s] = 9;
+    for (int s = 256; s < 280; s++) T.lengths[s] = 7;
+    for (int s = 280; s < 288; s++) T.lengths[s] = 8;
+    for (int s = 0; s < 30; s++) T.lengths[288 + s] = 5;
+    lane_code<288>(T.lc.count, T.lc.symbol, T.lengths, 288);
+    lane_code<32>(T.dc.count, T.dc.symbol, T.lengths + 288, 30);
+    lane_table(T.lit, kLaneLitBits, T.lengths, 288, T.lc.count);
+    lane_table(T.dist, kLaneDistBits, T.lengths + 288, 30, T.dc.count);
+    z.mode = kLaneSymbol;
+  } else if (type == 2) {
+    const int nlen = (int)lane_bits(b, 5, err) + 257, ndist = (int)lane_bits(b, 5, err) + 1;
+    const int ncode = (int)lane_bits(b, 4, err) + 4;
+    if (err) return;
+    if (nlen > 286 || ndist > 30) { err = kErrCode; return; }
+    const uint8_t order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+    for (int k = 0; k < 19; k++) T.lengths[k] = 0;
+    for (int k = 0; k < ncode; k++) T.lengths[order[k]] = (uint8_t)lane_bits(b, 3, err);
+    if (err) return;
+    // the code-length code, decoded through the distance table (codes of at most 7 bits)
+    if (!lane_code<32>(T.dc.count, T.dc.symbol, T.lengths, 19)) { err = kErrCode; return; }
+    lane_table(T.dist, kLaneDistBits, T.lengths, 19, T.dc.count);
+    int k = 0;
+    while (k < nlen + ndist) {
+      const int sym = lane_symbol(b, T.dist, kLaneDistBits, T.dc.count, T.dc.symbol, 19, err);
+      if (sym < 0) { if (!err) err = kErrCode; return; }
+      if (sym < 16) { T.lengths[k++] = (uint8_t)sym; continue; }
+      uint8_t v = 0;
+      int rep;
+      if (sym == 16) {
+        if (k == 0) { err = kErrCode; return; }
+        v = T.lengths[k - 1];
+        rep = 3 + (int)lane_bits(b, 2, err);
+      } else if (sym == 17) {
+        rep = 3 + (int)lane_bits(b, 3, err);
+      } else {
+        rep = 11 + (int)lane_bits(b, 7, err);
+      }
+      if (err) return;
+      if (k + rep > nlen + ndist) { err = kErrCode; return; }
+      while (rep--) T.lengths[k++] = v;
+    }
+    if (T.lengths[256] == 0) { err = kErrCode; return; }
+    if (!lane_code<288>(T.lc.count, T.lc.symbol, T.lengths, nlen) ||
+        !lane_code<32>(T.dc.count, T.dc.symbol, T.lengths + nlen, ndist)) { err = kErrCode; return; }
+    lane_table(T.lit, kLaneLitBits, T.lengths, nlen, T.lc.count);
+    lane_table(T.dist, kLaneDistBits, T.lengths + nlen, ndist, T.dc.count);
+    z.mode = kLaneSymbol;
+  } else {
+    err = kErrBlockType;
+  }
+}
+
+// One step of the decoder; the stream ends in kLaneDone with err set on failure.
+BSQ_HD void lane_step(LaneState& z, LaneTables& T) {
+  if (z.mode == kLaneDone) return;
+  if (z.mode == kLaneHeader) {
+    lane_header(z, T);
+  } else if (z.mode == kLaneSymbol) {
+    const int sym = lane_symbol(z.b, T.lit, kLaneLitBits, T.lc.count, T.lc.symbol, 288, z.err);
+    if (sym < 0) {
+      if (!z.err) z.err = kErrCode;
+    } else if (sym < 256) {
+      if (z.w.n >= z.w.cap) z.err = kErrOutput;
+      else lane_emit(T, z.w, (uint8_t)sym);
+    } else if (sym == 256) {
+      z.mode = z.last ? kLaneDone : kLaneHeader;
+    } else {
+      const int li = sym - 257;
+      if (li >= 29) { z.err = kErrSymbol; }
+      else {
+        const uint32_t len = length_base(li) + lane_bits(z.b, length_extra(li), z.err);
+        const int ds = lane_symbol(z.b, T.dist, kLaneDistBits, T.dc.count, T.dc.symbol, 32, z.err);
+        if (ds < 0) { if (!z.err) z.err = kErrCode; }
+        else if (ds >= 30) z.err = kErrSymbol;
+        else {
+          const uint32_t d = dist_base(ds) + lane_bits(z.b, dist_extra(ds), z.err);
+          if (!z.err) {
+            if (d > z.w.n) z.err = kErrDistance;
+            else if (len > z.w.cap - z.w.n) z.err = kErrOutput;
+            else { z.left = len; z.dist = d; z.mode = kLaneCopy; }
+          }
+        }
+      }
+    }
+  } else if (z.mode == kLaneCopy) {
+    // up to 8 bytes: independent loads when the source is older than the ring (d > 64 keeps them
+    // clear of this copy's own bytes), else one at a time (an overlapping copy repeats its bytes)
+    const uint32_t m = z.left < 8 ? z.left : 8;
+    if (z.dist > kLaneRing && m == 8) {
+      uint8_t v[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) v[j] = lane_back(T, z.w, z.dist - (uint32_t)j);
+#pragma unroll
+      for (int j = 0; j < 8; j++) lane_emit(T, z.w, v[j]);
+    } else {
+      for (uint32_t j = 0; j < m; j++) lane_emit(T, z.w, lane_back(T, z.w, z.dist));
+    }
+    z.left -= m;
+    if (z.left == 0) z.mode = kLaneSymbol;
+  } else {
+    // stored bytes, up to 8
+    const uint32_t m = z.left < 8 ? z.left : 8;
+    for (uint32_t j = 0; j < m && !z.err; j++) lane_emit(T, z.w, (uint8_t)lane_bits(z.b, 8, z.err));
+    z.left -= m;
+    if (z.left == 0 && !z.err) z.mode = z.last ? kLaneDone : kLaneHeader;
+  }
+  if (z.err) z.mode = kLaneDone;
+}
+
+// The end of a block: its last partial chunk (the rest of that chunk is the next block's).
+BSQ_HD void lane_finish(LaneState& z, LaneTables& T) {
+  if (z.err) return;
+  const uintptr_t end = (uintptr_t)(z.w.o + z.w.n);
+  if (end & 15) lane_store_chunk(T, z.w, (end | 15) + 1);
+}
+
+// Inflates one block's raw DEFLATE data in[0, in_len) into out[0, cap) with one thread's tables;
+// *out_len gets the bytes produced.
+BSQ_HD int inflate_lane(const uint8_t* in, uint32_t in_len, uint8_t* out, uint32_t cap, uint32_t* out_len,
+                        LaneTables& T) {
+  LaneState z;
+  lane_start(z, in, in_len, out, cap);
+  while (z.mode != kLaneDone) lane_step(z, T);
+  lane_finish(z, T);
+  *out_len = z.w.n;
+  return z.err;
+}
+
 // ----------------------------------------------------------------------------- CRC-32
 // gzip's CRC-32 (reflected, polynomial 0xEDB88320).  Two CRCs combine as crc(AB) =
 // crc(A) * x^(8 |B|) + crc(B) over GF(2) modulo the polynomial, the products taken in the

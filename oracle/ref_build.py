@@ -19,8 +19,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SHIM = os.path.join(HERE, "refbuild")
 OUT = os.path.join(HERE, "_ref")
 BIN = os.path.join(OUT, "ref_harness")
-# command-line programs of the reference (they hold main()); everything else is its library
+# command-line programs of the reference (they hold main()); everything else is its library, but
+# coverage_distribution.cpp is compiled inside refbuild/covfit.cpp instead (its fit is file-local)
 MAINS = {"breseq_cmdline.cpp", "gdtools_cmdline.cpp", "coverage_table_cmdline.cpp"}
+INCLUDED = {"coverage_distribution.cpp"}
 
 
 def ref_src() -> str | None:
@@ -37,8 +39,8 @@ def build(force: bool = False) -> str | None:
     src = ref_src()
     if src is None:
         return None
-    srcs = sorted(f for f in os.listdir(src) if f.endswith(".cpp") and f not in MAINS)
-    ours = [os.path.join(SHIM, f) for f in ("hts_shim.cpp", "harness.cpp")]
+    srcs = sorted(f for f in os.listdir(src) if f.endswith(".cpp") and f not in MAINS and f not in INCLUDED)
+    ours = [os.path.join(SHIM, f) for f in ("hts_shim.cpp", "harness.cpp", "covfit.cpp")]
     deps = [os.path.join(src, f) for f in os.listdir(src)] + ours
     for root, _, files in os.walk(os.path.join(SHIM, "include")):
         deps += [os.path.join(root, f) for f in files]
@@ -58,12 +60,12 @@ def build(force: bool = False) -> str | None:
 
     with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         lib_objs = list(ex.map(cc, [os.path.join(src, f) for f in srcs]))
-        shim_obj, harness_obj = list(ex.map(cc, ours))
+        shim_obj, harness_obj, covfit_obj = list(ex.map(cc, ours))
     archive = os.path.join(obj_dir, "libbreseq_ref.a")
     if os.path.exists(archive):
         os.remove(archive)
     subprocess.check_call(["ar", "rcs", archive] + lib_objs)
-    subprocess.check_call(["g++", "-o", BIN + ".tmp", harness_obj, archive, shim_obj, "-lz", "-lpthread"])
+    subprocess.check_call(["g++", "-o", BIN + ".tmp", harness_obj, covfit_obj, archive, shim_obj, "-lz", "-lpthread"])
     os.replace(BIN + ".tmp", BIN)
     return BIN
 

@@ -31,7 +31,7 @@ def write_fasta(s, path):
 
 
 def write_inputs(s, d, polymorphism=False, prop_cutoff=None, seed_cutoff=None, copy_number=False, classify=False,
-                 pmdd=(), fast_bam=False, softclip=False, bam2cov=()) -> tuple:
+                 pmdd=(), fast_bam=False, softclip=False, bam2cov=(), covfit=False) -> tuple:
     """reference.bam, reference.fasta, an empty out/ folder and config.txt in folder d; returns the
     config path and the output folder.  pmdd: (read group, median, mad) of the paired-mapping-distance
     fits that make discordant-pair groups.  fast_bam: the vectorised BAM writer (same records; its read
@@ -57,7 +57,7 @@ def write_inputs(s, d, polymorphism=False, prop_cutoff=None, seed_cutoff=None, c
         f.write(f"copy_number {int(copy_number)}\nclassify {int(classify)}\n")
         for g, med, mad in pmdd:
             f.write(f"pmdd {int(g)} {float(med)!r} {float(mad)!r}\n")
-        f.write(f"softclip {int(softclip)}\n")
+        f.write(f"softclip {int(softclip)}\ncovfit {int(covfit)}\n")
         for name, region, res, fmt, tot, prg in bam2cov:
             f.write(f"bam2cov {name} {region} {int(res)} {fmt} {int(tot)} {int(prg)}\n")
         for t, name in enumerate(s.target_names):
@@ -75,14 +75,14 @@ def read_outputs(out) -> dict:
 
 
 def run(s, polymorphism=False, prop_cutoff=None, seed_cutoff=None, copy_number=False, classify=False,
-        pmdd=(), workdir=None, softclip=False, bam2cov=()) -> dict:
+        pmdd=(), workdir=None, softclip=False, bam2cov=(), covfit=False) -> dict:
     """Outputs of the reference on sample `s`: {file name: text}.  Raises when the binary is absent."""
     exe = ref_build.build()
     if exe is None:
         raise FileNotFoundError("the reference sources are not available")
     with tempfile.TemporaryDirectory(dir=workdir) as d:
         cfg, out = write_inputs(s, d, polymorphism, prop_cutoff, seed_cutoff, copy_number, classify, pmdd,
-                                softclip=softclip, bam2cov=bam2cov)
+                                softclip=softclip, bam2cov=bam2cov, covfit=covfit)
         env = dict(os.environ, BRESEQ_DATA_PATH=ref_build.data_path())
         r = subprocess.run([exe, cfg], capture_output=True, text=True, cwd=d, env=env)
         if r.returncode != 0:

@@ -20,6 +20,10 @@
 //   bam2cov name region resolution format total_only per_read_group
 //                             also `breseq BAM2COV` tables (coverage_output::table, breseq_cmdline.cpp:428-536)
 //                             into bam2cov/<name>
+//   covfit 0|1                also fit each coverage group's unique-only coverage distribution
+//                             (fit_coverage_distribution, coverage_distribution.cpp:345-399, with the
+//                             cutoff analyze_unique_coverage_distribution passes, :545): writes
+//                             coverage_fit.<group>.txt (the fit result, %.17g)
 // Outputs in outdir: error_rates.tab, base_qual_error_prob.<file>.tab, <group>.unique_only_coverage_distribution.tab,
 // ra_mc_evidence.gd, 08_mutation_identification/ (DP candidate regions, coverage tables) and the
 // classified GenomeDiff when asked.
@@ -31,6 +35,7 @@
 #include "error_count.h"
 #include "genome_diff.h"
 #include "identify_mutations.h"
+#include "coverage_distribution.h"
 #include "coverage_output.h"
 #include "reference_sequence.h"
 #include "settings.h"
@@ -38,6 +43,12 @@
 #include "summary.h"
 
 using namespace breseq;
+
+namespace breseq {
+// covfit.cpp: coverage_distribution.cpp:345's fit itself, without the plot CoverageDistribution::fit draws
+CoverageDistributionFitResult harness_fit_coverage(const coverage_histogram_t& hist, double deletion_propagation_pr_cutoff,
+                                                   uint32_t& censor_start, uint32_t& censor_end, double& nb_fit_scale);
+}
 
 int main(int argc, char** argv) {
   if (argc != 2) { cerr << "usage: ref_harness <config>" << endl; return 2; }
@@ -50,7 +61,7 @@ int main(int argc, char** argv) {
   bool poly = false, copy_number = false, classify = false;
   struct Pmdd { uint32_t g; double median, mad; };
   vector<Pmdd> pmdd;
-  bool softclip = false;
+  bool softclip = false, covfit = false;
   struct Cov { string name, region, format; uint32_t resolution; int total_only, per_rg; };
   vector<Cov> covs;
   string line;
@@ -68,6 +79,7 @@ int main(int argc, char** argv) {
     else if (key == "classify") { int v; ls >> v; classify = v != 0; }
     else if (key == "pmdd") { Pmdd d; ls >> d.g >> d.median >> d.mad; pmdd.push_back(d); }
     else if (key == "softclip") { int v; ls >> v; softclip = v != 0; }
+    else if (key == "covfit") { int v; ls >> v; covfit = v != 0; }
     else if (key == "bam2cov") {
       Cov c;
       ls >> c.name >> c.region >> c.resolution >> c.format >> c.total_only >> c.per_rg;
@@ -169,6 +181,24 @@ int main(int argc, char** argv) {
             (unsigned long long)c.soft_clipping_trimmed_positions);
     fprintf(f, "soft_clipping_mean_tested_reads %.17g\n", c.soft_clipping_mean_tested_reads);
     fclose(f);
+  }
+  if (covfit) {
+    for (uint32_t g = 0; g < n_groups; g++) {
+      uint32_t len = 0;
+      for (const string& id : settings.refseq_settings.m_seq_ids_by_coverage_group[g])
+        len += ref_seq_info.get_sequence_length(id);
+      const coverage_histogram_t hist =
+          read_coverage_histogram(Settings::path_file_name(outdir, to_string(g) + ".unique_only_coverage_distribution.tab"));
+      uint32_t cs = 0, ce = 0;
+      double scale = 0;
+      const CoverageDistributionFitResult r = harness_fit_coverage(hist, 0.05 / sqrt(len), cs, ce, scale);
+      FILE* f = fopen(Settings::path_file_name(outdir, "coverage_fit." + to_string(g) + ".txt").c_str(), "w");
+      fprintf(f, "nbinom_size %.17g\nnbinom_mean %.17g\naverage %.17g\nvariance %.17g\nrelative_variance %.17g\n",
+              r.nb_fit_size, r.nb_fit_mu, r.average, r.variance, r.relative_variance);
+      fprintf(f, "deletion_coverage_propagation_cutoff %.17g\ncensor_start %u\ncensor_end %u\nnbinom_scale %.17g\n",
+              r.deletion_coverage_propagation_cutoff, cs, ce, scale);
+      fclose(f);
+    }
   }
   if (!covs.empty()) create_path(outdir + "/bam2cov");
   for (const Cov& c : covs) {

@@ -5,7 +5,9 @@ tests/samples.py.  Run in a checkout that has the reference tree:
     python tests/golden/make_ref_golden.py [case ...]
 
 Each fixture holds the sample's digest, the settings of the run, and per file either its text or, for
-files over 16 KB, its SHA-256 and size.  The classified GenomeDiff is the harness's
+files over 16 KB, its SHA-256 and size.  Besides the two passes' files, every case holds the coverage
+distribution fit of each coverage group (coverage_fit.<g>.txt, the harness's %.17g dump of
+fit_coverage_distribution's result).  The classified GenomeDiff is the harness's
 test_RA_evidence + cGenomeDiff::write output without the `#=TITLE` line that write adds."""
 import hashlib
 import json
@@ -45,7 +47,7 @@ def make(case):
     t0 = time.time()
     out = ref_run.run(s, polymorphism=c.get("polymorphism", False), prop_cutoff=c.get("prop_cutoff"),
                       copy_number=True, classify=True, pmdd=[tuple(x) for x in c.get("pmdd", [])],
-                      softclip=c.get("softclip", False), bam2cov=[tuple(x) for x in c.get("bam2cov", [])])
+                      softclip=c.get("softclip", False), bam2cov=[tuple(x) for x in c.get("bam2cov", [])], covfit=True)
     files = {}
     for name, text in sorted(out.items()):
         if name == "ra_mc_evidence.classified.gd":

@@ -3,8 +3,9 @@
 tests/golden/ref/<case>.json holds what breseq's error_count() and identify_mutations() -- the
 reference's unmodified sources, compiled by oracle/ref_build.py with the clean-room htslib subset --
 wrote for a seeded sample (tests/golden/make_ref_golden.py): error_rates.tab, base_qual_error_prob.*.tab,
-the unique-only coverage distributions, the stage-08 ra_mc_evidence.gd, the same after
-test_RA_evidence, the coverage tables and the discordant-pair candidate regions.  The oracle's own
+the unique-only coverage distributions and their negative-binomial fits, the stage-08 ra_mc_evidence.gd,
+the same after test_RA_evidence, the coverage tables and the discordant-pair candidate regions, and on
+one case the soft-clipping counts and BAM2COV tables.  The oracle's own
 writers must reproduce every one of them byte for byte (files over 16 KB are compared by SHA-256).
 Where the reference tree is present, the fixtures are also checked to be current."""
 import hashlib
@@ -86,6 +87,27 @@ def sc_counts_text(s, result, tmp_path):
     return open(path).read()
 
 
+def coverage_fit_text(r):
+    """The harness's coverage_fit.<g>.txt for a bsq_coverage_fit dict (fit_coverage_distribution's result)."""
+    def g(x):
+        return "%.17g" % x
+    return (f"nbinom_size {g(r['nbinom_size'])}\nnbinom_mean {g(r['nbinom_mean'])}\naverage {g(r['average'])}\n"
+            f"variance {g(r['variance'])}\nrelative_variance {g(r['relative_variance'])}\n"
+            f"deletion_coverage_propagation_cutoff {g(r['deletion_coverage_propagation_cutoff'])}\n"
+            f"censor_start {r['censor_start']}\ncensor_end {r['censor_end']}\nnbinom_scale {g(r['nbinom_scale'])}\n")
+
+
+def coverage_fit_inputs(s, ec):
+    """Per coverage group: the unique-only histogram error_count wrote and breseq's cutoff probability,
+    0.05 / sqrt(the group's total length) (coverage_distribution.cpp:545)."""
+    out = []
+    for g in range(s.n_coverage_groups):
+        length = sum(int(s.target_offset[t + 1] - s.target_offset[t]) for t in range(len(s.target_names))
+                     if int(s.coverage_group[t]) == g)
+        out.append((ec["hist"][g][: int(ec["hist_size"][g])], length, 0.05 / np.sqrt(float(length))))
+    return out
+
+
 def bam2cov_region(s, region):
     seq, rng = region.split(":")
     a, b = (int(x) for x in rng.split("-"))
@@ -113,6 +135,8 @@ def oracle_files(fx, tmp_path):
     for g in range(s.n_coverage_groups):
         h = np.ascontiguousarray(ec["hist"][g], dtype=np.uint64)
         out[f"{g}.unique_only_coverage_distribution.tab"] = ro.coverage_distribution_text(h, int(ec["hist_size"][g]))
+    for g, (h, _, cut) in enumerate(coverage_fit_inputs(s, ec)):
+        out[f"coverage_fit.{g}.txt"] = coverage_fit_text(po.fit_coverage_distribution(h, cut))
     dp, widths, r1, r2 = dp_setup(st, nfiles)
     p = po.default_im_params(s, polymorphism_mode=poly, prop_cutoff=prop, dp_group=tuple(dp) if widths else ())
     im = po.identify(s, tab, p)
@@ -156,6 +180,18 @@ def test_oracle_matches_reference_files(oracle_lib, built_lib, tmp_path, case):
         assert same(want, got[name]), f"{case}: {name} differs from breseq's own output"
 
 
+@pytest.mark.parametrize("case", SMALL)
+def test_library_coverage_fit_matches_reference(oracle_lib, built_lib, case):
+    """bsq_fit_coverage_distribution (host code, all host threads) against breseq's own fit of the same
+    histograms."""
+    from breseq_gb300 import api
+    fx = load(case)
+    s = getattr(samples, fx["settings"]["sample"])()
+    ec = po.error_count(s)
+    for g, (h, length, _) in enumerate(coverage_fit_inputs(s, ec)):
+        assert same(fx["files"][f"coverage_fit.{g}.txt"], coverage_fit_text(api.fit_coverage_distribution(h, length)))
+
+
 def test_fixtures_are_current():
     """Reruns breseq's own code on one small case where the reference tree is available."""
     from oracle import ref_build, ref_run
@@ -164,7 +200,7 @@ def test_fixtures_are_current():
     fx = load("ecoli_small")
     st = fx["settings"]
     s = getattr(samples, st["sample"])()
-    out = ref_run.run(s, polymorphism=st.get("polymorphism", False), copy_number=True, classify=True)
+    out = ref_run.run(s, polymorphism=st.get("polymorphism", False), copy_number=True, classify=True, covfit=True)
     out["ra_mc_evidence.classified.gd"] = "".join(
         l for l in out["ra_mc_evidence.classified.gd"].splitlines(True) if not l.startswith("#=TITLE"))
     assert sorted(out) == sorted(fx["files"])
