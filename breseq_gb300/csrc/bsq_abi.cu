@@ -1961,8 +1961,14 @@ int bsq_bam_open(bsq_ctx* ctx, const uint8_t* data, uint64_t size, bsq_bam** out
   uint32_t* w = B->scratch.as<uint32_t>();
   CK(cudaMemsetAsync(w, 0, 4, st));
   CK(cudaMemsetAsync(w + 1, 0xFF, 4, st));
+  // token room for up to 16384 blocks at a time (4 GiB), freed once the stream is inflated
+  const uint32_t tok_blocks = std::max<uint32_t>(1, std::min<uint32_t>(nb, 16384));
+  DevMem tok;
+  CK(tok.alloc(bam_token_bytes(tok_blocks), st));
+  uint32_t* tokp = tok.as<uint32_t>();
   CK(record(ctx->ev0, st));
-  CK(bam_inflate(B->file.as<uint8_t>(), B->blocks.as<BgzfBlock>(), nb, B->stream.as<uint8_t>(), w, w + 1, ctx->sms, st));
+  CK(bam_inflate(B->file.as<uint8_t>(), B->blocks.as<BgzfBlock>(), nb, B->stream.as<uint8_t>(), tokp,
+                 tokp + (size_t)tok_blocks * 65536, tok_blocks, w, w + 1, ctx->sms, st));
   CK(record(ctx->ev1, st));
   uint32_t h[2];
   CK(cudaMemcpyAsync(h, w, 8, cudaMemcpyDeviceToHost, st));

@@ -12,7 +12,7 @@ namespace bsq {
 namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
-constexpr bool kLaneInflate = false;  // one thread per block (bgzf_lane_kernel) rather than one warp
+constexpr uint32_t kTokPerBlock = 65536;   // token room per block (a token is at least one byte)
 
 int grid_for(uint64_t units, uint32_t per_block, int sms, int per_sm) {
   const uint64_t need = (units + per_block - 1) / per_block;
@@ -24,131 +24,83 @@ __device__ __forceinline__ uint32_t rd32(const uint8_t* p) {
   return p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
 }
 
-// One warp per BGZF block.  Lane 0 runs the resumable decoder (bsq_inflate.cuh) from a 1 KiB
-// shared-memory window of the compressed block into the warp's 4 KiB shared-memory ring; whenever
-// it pauses the whole warp moves the new output bytes to global memory and, when the decoder runs
-// low, stages the next window of input.  Then every lane takes the CRC-32 of a 1/32 slice of the
-// block, and the slices are combined in order.
-constexpr int kInfWarps = 4;
-constexpr uint32_t kInWin = 1024;
-struct InflateWarp {
-  inflate::Tables T;
-  uint8_t ring[inflate::kRing];
-  uint8_t win[kInWin];
-};
-
-__global__ void __launch_bounds__(kInfWarps * 32) bgzf_inflate_kernel(const uint8_t* file, const BgzfBlock* blocks,
-                                                                      uint32_t n, uint8_t* out, uint32_t* err,
-                                                                      uint32_t* first_bad) {
-  __shared__ uint32_t crc_table[256];
-  __shared__ InflateWarp W[kInfWarps];
-  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) {
-    uint32_t c = i;
-    for (int k = 0; k < 8; k++) c = (c & 1) ? inflate::kCrcPoly ^ (c >> 1) : c >> 1;
-    crc_table[i] = c;
-  }
-  __syncthreads();
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  InflateWarp& S = W[w];
-  for (uint32_t b = blockIdx.x * kInfWarps + w; b < n; b += gridDim.x * kInfWarps) {
-    const BgzfBlock B = blocks[b];
-    uint8_t* o = out + B.out_off;
-    const uint8_t* in = file + B.in_off;
-    inflate::Inflater z;
-    inflate::Codes K;
-    if (lane == 0) {
-      inflate::inflater_init(z, B.in_len, B.isize);
-      z.win = S.win;
-    }
-    uint32_t flushed = 0, pos = 0, win_hi = 0;
-    int status = 0;
-    for (;;) {
-      // stage the next window of input when the decoder is low on it (and at the start)
-      if (win_hi < B.in_len && pos + inflate::kInMargin > win_hi) {
-        const uint32_t lo = pos, hi = min(B.in_len, pos + kInWin);
-        for (uint32_t k = lo + lane; k < hi; k += 32) S.win[k - lo] = in[k];
-        win_hi = hi;
-        if (lane == 0) { z.win_lo = lo; z.win_hi = hi; }
-      }
-      __syncwarp();
-      uint32_t produced = 0;
-      if (lane == 0) {
-        inflate::z_run(z, S.T, K, S.ring, o);
-        produced = z.n;
-        pos = z.pos;
-        status = z.err ? 2 : (z.state == 3 ? 1 : 0);
-      }
-      __syncwarp();
-      produced = __shfl_sync(kFull, produced, 0);
-      pos = __shfl_sync(kFull, pos, 0);
-      status = __shfl_sync(kFull, status, 0);
-      for (uint32_t p = flushed + lane; p < produced; p += 32) o[p] = S.ring[p & (inflate::kRing - 1)];
-      __syncwarp();
-      flushed = produced;
-      if (lane == 0) z.flushed = produced;
-      if (status) break;
-    }
-    if (status == 2 || flushed != B.isize) {
-      if (lane == 0) {
-        atomicOr(err, kBamInflate);
-        atomicMin(first_bad, b);
-      }
-      continue;
-    }
-    // CRC-32 of each lane's slice, then combined in order
-    const uint32_t slice = (B.isize + 31) / 32;
-    const uint32_t a0 = min(B.isize, lane * slice), a1 = min(B.isize, a0 + slice);
-    uint32_t c = 0xFFFFFFFFu;
-    for (uint32_t k = a0; k < a1; k++) c = crc_table[(c ^ o[k]) & 0xFF] ^ (c >> 8);
-    c ^= 0xFFFFFFFFu;
-    uint32_t total = __shfl_sync(kFull, c, 0);
-    // every lane walks the combination, so the shuffles stay warp-wide
-    const uint32_t shift_full = inflate::gf2_x8n(slice);
-    for (int j = 1; j < 32; j++) {
-      const uint32_t cj = __shfl_sync(kFull, c, j);
-      const uint32_t bj0 = min(B.isize, (uint32_t)j * slice), bj1 = min(B.isize, bj0 + slice);
-      const uint32_t lj = bj1 - bj0;
-      if (lj == 0) continue;
-      total = inflate::gf2_mulmod(lj == slice ? shift_full : inflate::gf2_x8n(lj), total) ^ cj;
-    }
-    if (lane == 0 && total != B.crc) {
-      atomicOr(err, kBamCrc);
-      atomicMin(first_bad, b);
-    }
-  }
-}
-
-// One thread per BGZF block (inflate_lane: the block's Huffman codes in the thread's own tables in
-// shared memory, output straight to the stream in 16-byte chunks), 32 blocks per warp.
+// Phase 1 of the two-phase inflate: one thread per block decodes its Huffman symbols into tokens
+// (tok_step), with its tables in shared memory.  Every lane runs every iteration of the loop (a lane
+// without a block idles in kLaneDone) and the warp reconverges after each step, so the 32 lanes' steps
+// run side by side.  A failing block's token count is kTokBad.
 constexpr int kLaneThreads = 32;
-__global__ void __launch_bounds__(kLaneThreads) bgzf_lane_kernel(const uint8_t* file, const BgzfBlock* blocks,
-                                                                 uint32_t n, uint8_t* out, uint32_t* err,
-                                                                 uint32_t* first_bad) {
+constexpr uint32_t kTokBad = 0xFFFFFFFFu;
+__global__ void __launch_bounds__(kLaneThreads) bgzf_tok_kernel(const uint8_t* file, const BgzfBlock* blocks,
+                                                                uint32_t b_lo, uint32_t b_hi, uint32_t* tok,
+                                                                uint32_t* ntok, uint32_t* err, uint32_t* first_bad) {
   extern __shared__ __align__(16) unsigned char lane_smem[];
-  inflate::LaneTables& T = reinterpret_cast<inflate::LaneTables*>(lane_smem)[threadIdx.x];
-  // every lane runs every iteration of the loop (a lane without a block idles in kLaneDone), and the
-  // warp reconverges after each decoder step, so the lanes' steps run side by side
-  for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < n; b0 += gridDim.x * blockDim.x) {
+  // the threads' token stages, then their tables
+  uint32_t* stage = reinterpret_cast<uint32_t*>(lane_smem) + threadIdx.x * inflate::kTokStage;
+  inflate::LaneTables& T =
+      reinterpret_cast<inflate::LaneTables*>(lane_smem + kLaneThreads * inflate::kTokStage * 4)[threadIdx.x];
+  for (uint32_t b0 = b_lo + blockIdx.x * blockDim.x; b0 < b_hi; b0 += gridDim.x * blockDim.x) {
     const uint32_t b = b0 + threadIdx.x;
-    inflate::LaneState z;
-    BgzfBlock B;
-    if (b < n) {
-      B = blocks[b];
-      inflate::lane_start(z, file + B.in_off, B.in_len, out + B.out_off, B.isize);
+    inflate::TokState z;
+    if (b < b_hi) {
+      const BgzfBlock B = blocks[b];
+      inflate::tok_start(z, file + B.in_off, B.in_len, tok + (size_t)(b - b_lo) * kTokPerBlock, stage, B.isize);
     } else {
       z.mode = inflate::kLaneDone;
       z.err = inflate::kOk;
     }
     while (__any_sync(kFull, z.mode != inflate::kLaneDone)) {
-      inflate::lane_step(z, T);
+      inflate::tok_step(z, T);
       __syncwarp();
     }
-    if (b < n) {
-      inflate::lane_finish(z, T);
-      if (z.err != inflate::kOk || z.w.n != B.isize) {
+    if (b < b_hi) {
+      inflate::tok_finish(z);
+      ntok[b - b_lo] = z.err ? kTokBad : z.n;
+      if (z.err) {
         atomicOr(err, kBamInflate);
         atomicMin(first_bad, b);
       }
+    }
+  }
+}
+
+// Phase 2: one warp per block turns its tokens into bytes.  32 tokens at a time: their lengths are
+// scanned into output positions, the literals written at once, then each copy by all 32 lanes in
+// order (a source byte is always before the copy's own bytes; an overlapping copy repeats its first
+// d bytes), the warp synchronising between writes and the reads that may see them.
+__global__ void __launch_bounds__(256) bgzf_resolve_kernel(const BgzfBlock* blocks, uint32_t b_lo, uint32_t b_hi,
+                                                           const uint32_t* tok, const uint32_t* ntok, uint8_t* out) {
+  const int lane = threadIdx.x & 31;
+  for (uint32_t b = b_lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); b < b_hi;
+       b += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t nt = ntok[b - b_lo];
+    if (nt == kTokBad) continue;
+    const BgzfBlock B = blocks[b];
+    const uint32_t* tk = tok + (size_t)(b - b_lo) * kTokPerBlock;
+    uint8_t* o = out + B.out_off;
+    uint32_t pos = 0;
+    for (uint32_t c = 0; c < nt; c += 32) {
+      const bool act = c + lane < nt;
+      const uint32_t t = act ? tk[c + lane] : 0u;
+      const uint32_t d = t & 0xFFFFu, x = t >> 16;
+      const uint32_t len = act ? (d ? x + 3u : 1u) : 0u;
+      uint32_t incl = len;
+#pragma unroll
+      for (int k = 1; k < 32; k <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, incl, k);
+        if (lane >= k) incl += y;
+      }
+      const uint32_t start = pos + incl - len;
+      if (act && d == 0) o[start] = (uint8_t)x;
+      __syncwarp();
+      unsigned m = __ballot_sync(kFull, act && d != 0);
+      while (m) {
+        const int j = __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t dj = __shfl_sync(kFull, d, j), lj = __shfl_sync(kFull, len, j), sj = __shfl_sync(kFull, start, j);
+        for (uint32_t i = lane; i < lj; i += 32) o[sj + i] = o[sj - dj + (i < dj ? i : i % dj)];
+        __syncwarp();
+      }
+      pos += __shfl_sync(kFull, incl, 31);
     }
   }
 }
@@ -469,22 +421,25 @@ __global__ void __launch_bounds__(256) scan_apply_kernel(const uint32_t* in, uin
 
 }  // namespace
 
-cudaError_t bam_inflate(const uint8_t* file, const BgzfBlock* blocks, uint32_t n_blocks, uint8_t* out, uint32_t* err,
-                        uint32_t* first_bad, int sms, cudaStream_t st) {
+cudaError_t bam_inflate(const uint8_t* file, const BgzfBlock* blocks, uint32_t n_blocks, uint8_t* out, uint32_t* tok,
+                        uint32_t* ntok, uint32_t tok_blocks, uint32_t* err, uint32_t* first_bad, int sms,
+                        cudaStream_t st) {
   if (!n_blocks) return cudaSuccess;
-  if (kLaneInflate) {
-    // 32 threads' tables per block: 3 blocks fit an SM's shared memory
-    const size_t smem = kLaneThreads * sizeof(inflate::LaneTables);
-    cudaError_t e = cudaFuncSetAttribute(bgzf_lane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    bgzf_lane_kernel<<<grid_for(n_blocks, kLaneThreads, sms, 3), kLaneThreads, smem, st>>>(file, blocks, n_blocks, out, err,
-                                                                                          first_bad);
-    bgzf_crc_kernel<<<grid_for(n_blocks, 8, sms, 8), 256, 0, st>>>(out, blocks, n_blocks, err, first_bad);
-  } else {
-    bgzf_inflate_kernel<<<grid_for(n_blocks, kInfWarps, sms, 8), kInfWarps * 32, 0, st>>>(file, blocks, n_blocks, out, err, first_bad);
+  // 32 threads' token stages and tables per block of the token kernel: 3 blocks fit an SM's shared memory
+  const size_t smem = kLaneThreads * (inflate::kTokStage * 4 + sizeof(inflate::LaneTables));
+  cudaError_t e = cudaFuncSetAttribute(bgzf_tok_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  // the blocks in groups of tok_blocks, the token room of one group
+  for (uint32_t lo = 0; lo < n_blocks; lo += tok_blocks) {
+    const uint32_t hi = std::min(n_blocks, lo + tok_blocks);
+    bgzf_tok_kernel<<<grid_for(hi - lo, kLaneThreads, sms, 3), kLaneThreads, smem, st>>>(file, blocks, lo, hi, tok, ntok, err,
+                                                                                        first_bad);
+    bgzf_resolve_kernel<<<grid_for(hi - lo, 8, sms, 8), 256, 0, st>>>(blocks, lo, hi, tok, ntok, out);
   }
+  bgzf_crc_kernel<<<grid_for(n_blocks, 8, sms, 8), 256, 0, st>>>(out, blocks, n_blocks, err, first_bad);
   return cudaGetLastError();
 }
+size_t bam_token_bytes(uint32_t tok_blocks) { return (size_t)tok_blocks * kTokPerBlock * 4 + (size_t)tok_blocks * 4; }
 
 cudaError_t bam_walk(const uint8_t* stream, const BgzfBlock* blocks, uint32_t n_blocks, uint64_t records_begin,
                      uint32_t* counts, const uint64_t* base, uint64_t* offsets, uint32_t* err, int sms, cudaStream_t st) {

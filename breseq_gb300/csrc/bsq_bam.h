@@ -69,8 +69,13 @@ struct BamRecordsDev {
   int32_t* mpos;         // PNEXT
 };
 
-cudaError_t bam_inflate(const uint8_t* file, const BgzfBlock* blocks, uint32_t n_blocks, uint8_t* out, uint32_t* err,
-                        uint32_t* first_bad, int sms, cudaStream_t st);
+// Inflates every BGZF block into out (two phases: Huffman symbols to tokens, one thread per block;
+// tokens to bytes, one warp per block; then the CRC-32s), tok_blocks blocks at a time through the
+// token buffer tok (bam_token_bytes(tok_blocks) bytes, ntok at its end is the per-block token count).
+cudaError_t bam_inflate(const uint8_t* file, const BgzfBlock* blocks, uint32_t n_blocks, uint8_t* out, uint32_t* tok,
+                        uint32_t* ntok, uint32_t tok_blocks, uint32_t* err, uint32_t* first_bad, int sms,
+                        cudaStream_t st);
+size_t bam_token_bytes(uint32_t tok_blocks);
 // Records per block (walk from max(block start, records_begin)); with offsets != null, a second walk
 // writes each record's stream offset at offsets[base[b] + k].
 cudaError_t bam_walk(const uint8_t* stream, const BgzfBlock* blocks, uint32_t n_blocks, uint64_t records_begin,

@@ -228,313 +228,44 @@ BSQ_HD int inflate_raw(const uint8_t* in, uint32_t in_len, uint8_t* out, uint32_
 namespace bsq {
 namespace inflate {
 
-// ----------------------------------------------------------------------------- resumable decoder
-// The same format, decoded with lookup tables (10 bits for literal/length codes, 8 for distances; a
-// code longer than the table falls back to the canonical bit-by-bit decode) and suspended whenever
-// the staged output reaches a threshold or the staged input runs low, so a caller can move output
-// out of a small ring buffer and move more input in.  Output: positions [n - kRing, n) are in
-// ring[p & (kRing - 1)], everything before `flushed` is in out[] already, at most kRing bytes are
-// unflushed.  Input: bytes [win_lo, win_hi) of the compressed data are in win[]; decoding pauses
-// at a step boundary when fewer than kInMargin bytes remain staged, more than any one step (a
-// dynamic block header, or a symbol with its extra bits) reads.
-
-constexpr int kLitBits = 10, kDistBits = 8;
-constexpr uint32_t kRing = 4096;
-constexpr uint32_t kSuspend = kRing - 258 - 1;   // unflushed bytes at which decoding pauses
-constexpr uint32_t kInMargin = 640;              // staged input bytes below which decoding pauses
-
-// The lookup tables and code lengths of the current block (the device keeps them in shared memory)
-struct Tables {
-  uint16_t lit[1 << kLitBits];    // (length << 9) | symbol, 0 = not in the table
-  uint16_t dist[1 << kDistBits];  // (length << 9) | symbol
-  uint8_t lengths[288 + 32];
-};
-// The canonical codes, for building the tables and for codes longer than them (per thread)
-struct Codes {
-  Code lit_code, dist_code;
-};
-
-struct Inflater {
-  const uint8_t* win;             // staged input: bytes [win_lo, win_hi) of the compressed data
-  uint32_t win_lo, win_hi;
-  uint32_t in_len, pos;
-  uint64_t buf;
-  int cnt;
-  uint32_t n, flushed, cap;       // produced, moved to out, output capacity
-  int state;                      // 0 block header, 1 stored bytes, 2 Huffman symbols, 3 done
-  int last;
-  uint32_t stored_left;
-  int err;
-};
-
-BSQ_HD void inflater_init(Inflater& z, uint32_t in_len, uint32_t cap) {
-  z.win = nullptr; z.win_lo = 0; z.win_hi = 0;
-  z.in_len = in_len; z.pos = 0; z.buf = 0; z.cnt = 0;
-  z.n = 0; z.flushed = 0; z.cap = cap; z.state = 0; z.last = 0; z.stored_left = 0; z.err = kOk;
-}
-
-BSQ_HD void z_refill(Inflater& z) {
-  while (z.cnt <= 56 && z.pos < z.win_hi) {
-    z.buf |= (uint64_t)z.win[z.pos - z.win_lo] << z.cnt;
-    z.pos++;
-    z.cnt += 8;
-  }
-}
-
-// More input must be staged before the next step.
-BSQ_HD bool z_input_low(const Inflater& z) { return z.win_hi < z.in_len && z.pos + kInMargin > z.win_hi; }
-
-BSQ_HD uint32_t z_bits(Inflater& z, int k) {   // k <= 32
-  if (k == 0) return 0;
-  if (z.cnt < k) { z_refill(z); if (z.cnt < k) { z.err = kErrInput; return 0; } }
-  const uint32_t v = (uint32_t)(z.buf & ((1ull << k) - 1));
-  z.buf >>= k;
-  z.cnt -= k;
-  return v;
-}
-
-// Canonical codes of the lengths (RFC 1951 §3.2.2), bit-reversed into a k-bit lookup table.
-BSQ_HD void table_build(uint16_t* table, int k, const uint8_t* lengths, int nsym, const Code& c) {
-  for (int i = 0; i < (1 << k); i++) table[i] = 0;
-  // first code of each length; unused symbols (length 0) take no codes
-  uint32_t next[kMaxBits + 2];
-  uint32_t code = 0;
-  next[0] = 0;
-  for (int l = 1; l <= kMaxBits; l++) {
-    code = (code + (l > 1 ? c.count[l - 1] : 0u)) << 1;
-    next[l] = code;
-  }
-  for (int s = 0; s < nsym; s++) {
-    const int l = lengths[s];
-    if (l == 0) continue;
-    const uint32_t cd = next[l]++;
-    if (l > k) continue;
-    uint32_t rev = 0;
-    for (int b = 0; b < l; b++) rev |= ((cd >> b) & 1u) << (l - 1 - b);
-    for (uint32_t f = rev; f < (1u << k); f += 1u << l) table[f] = (uint16_t)((l << 9) | s);
-  }
-}
-
-// One symbol: the table when the code is short enough, else the canonical decode.
-BSQ_HD int z_symbol(Inflater& z, const uint16_t* table, int k, const Code& c) {
-  if (z.cnt < kMaxBits) z_refill(z);
-  const uint16_t e = table[z.buf & ((1u << k) - 1)];
-  if (e) {
-    const int l = e >> 9;
-    if (l > z.cnt) { z.err = kErrInput; return -1; }
-    z.buf >>= l;
-    z.cnt -= l;
-    return e & 511;
-  }
-  int code = 0, first = 0, index = 0;
-  for (int l = 1; l <= kMaxBits; l++) {
-    code |= (int)z_bits(z, 1);
-    if (z.err) return -1;
-    const int count = c.count[l];
-    if (code - first < count) return c.symbol[index + (code - first)];
-    index += count;
-    first += count;
-    first <<= 1;
-    code <<= 1;
-  }
-  z.err = kErrCode;
-  return -1;
-}
-
-// Reads one block header; builds the block's tables.
-BSQ_HD void z_header(Inflater& z, Tables& T, Codes& K) {
-  z.last = (int)z_bits(z, 1);
-  const uint32_t type = z_bits(z, 2);
-  if (z.err) return;
-  if (type == 0) {
-    // the rest of the current byte is skipped: whole bytes still buffered are given back
-    const int drop = z.cnt & 7;
-    z.buf >>= drop;
-    z.cnt -= drop;
-    const uint32_t len = z_bits(z, 16), nlen = z_bits(z, 16);
-    if (z.err) return;
-    if (len != (~nlen & 0xFFFFu)) { z.err = kErrStored; return; }
-    z.stored_left = len;
-    z.state = 1;
-  } else if (type == 1) {
-    for (int s = 0; s < 144; s++) T.lengths[s] = 8;
-    for (int s = 144; s < 256; s++) T.lengths[s] = 9;
-    for (int s = 256; s < 280; s++) T.lengths[s] = 7;
-    for (int s = 280; s < 288; s++) T.lengths[s] = 8;
-    for (int s = 0; s < 30; s++) T.lengths[288 + s] = 5;
-    code_build(K.lit_code, T.lengths, 288);
-    code_build(K.dist_code, T.lengths + 288, 30);
-    table_build(T.lit, kLitBits, T.lengths, 288, K.lit_code);
-    table_build(T.dist, kDistBits, T.lengths + 288, 30, K.dist_code);
-    z.state = 2;
-  } else if (type == 2) {
-    const int nlen = (int)z_bits(z, 5) + 257, ndist = (int)z_bits(z, 5) + 1, ncode = (int)z_bits(z, 4) + 4;
-    if (z.err) return;
-    if (nlen > 286 || ndist > 30) { z.err = kErrCode; return; }
-    const uint8_t order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
-    for (int k = 0; k < 19; k++) T.lengths[k] = 0;
-    for (int k = 0; k < ncode; k++) T.lengths[order[k]] = (uint8_t)z_bits(z, 3);
-    if (z.err) return;
-    // the code-length code lives in dist_code while the lengths are read
-    if (!code_build(K.dist_code, T.lengths, 19)) { z.err = kErrCode; return; }
-    table_build(T.dist, kDistBits, T.lengths, 19, K.dist_code);
-    int k = 0;
-    while (k < nlen + ndist) {
-      const int sym = z_symbol(z, T.dist, kDistBits, K.dist_code);
-      if (sym < 0) { if (!z.err) z.err = kErrCode; return; }
-      if (sym < 16) { T.lengths[k++] = (uint8_t)sym; continue; }
-      uint8_t v = 0;
-      int rep;
-      if (sym == 16) {
-        if (k == 0) { z.err = kErrCode; return; }
-        v = T.lengths[k - 1];
-        rep = 3 + (int)z_bits(z, 2);
-      } else if (sym == 17) {
-        rep = 3 + (int)z_bits(z, 3);
-      } else {
-        rep = 11 + (int)z_bits(z, 7);
-      }
-      if (z.err) return;
-      if (k + rep > nlen + ndist) { z.err = kErrCode; return; }
-      while (rep--) T.lengths[k++] = v;
-    }
-    if (T.lengths[256] == 0) { z.err = kErrCode; return; }
-    if (!code_build(K.lit_code, T.lengths, nlen) || !code_build(K.dist_code, T.lengths + nlen, ndist)) {
-      z.err = kErrCode;
-      return;
-    }
-    table_build(T.lit, kLitBits, T.lengths, nlen, K.lit_code);
-    table_build(T.dist, kDistBits, T.lengths + nlen, ndist, K.dist_code);
-    z.state = 2;
-  } else {
-    z.err = kErrBlockType;
-  }
-}
-
-// Decodes until kSuspend bytes are unflushed, the stream ends (state 3) or an error.  ring holds the
-// recent output; out is read for back-references older than the ring.
-BSQ_HD void z_run_body(Inflater& z, Tables& T, Codes& K, uint8_t* ring, const uint8_t* out) {
-  while (z.err == kOk && z.state != 3 && z.n - z.flushed < kSuspend && !z_input_low(z)) {
-    if (z.state == 0) {
-      z_header(z, T, K);
-    } else if (z.state == 1) {
-      // stored bytes: whole buffered bytes first, then the input
-      if (z.stored_left == 0) { z.state = z.last ? 3 : 0; continue; }
-      if (z.n >= z.cap) { z.err = kErrOutput; return; }
-      uint8_t byte;
-      if (z.cnt >= 8) {
-        byte = (uint8_t)(z.buf & 0xFF);
-        z.buf >>= 8;
-        z.cnt -= 8;
-      } else {
-        if (z.pos >= z.win_hi) { z.err = kErrInput; return; }
-        byte = z.win[z.pos - z.win_lo];
-        z.pos++;
-      }
-      ring[z.n & (kRing - 1)] = byte;
-      z.n++;
-      z.stored_left--;
-    } else {
-      // runs of literals whose codes are in the table, without the per-step checks above; the
-      // run stops where a step must (output or input low, a longer code, anything but a literal)
-      for (;;) {
-        if (z.cnt < kMaxBits) z_refill(z);
-        const uint16_t e = T.lit[z.buf & ((1u << kLitBits) - 1)];
-        const int l = e >> 9;
-        if (e == 0 || l > z.cnt || (e & 511) >= 256) break;
-        if (z.n >= z.cap) { z.err = kErrOutput; return; }
-        z.buf >>= l;
-        z.cnt -= l;
-        ring[z.n & (kRing - 1)] = (uint8_t)(e & 511);
-        z.n++;
-        if (z.n - z.flushed >= kSuspend || z_input_low(z)) break;
-      }
-      if (z.n - z.flushed >= kSuspend || z_input_low(z)) continue;
-      const int sym = z_symbol(z, T.lit, kLitBits, K.lit_code);
-      if (sym < 0) { if (!z.err) z.err = kErrCode; return; }
-      if (sym < 256) {
-        if (z.n >= z.cap) { z.err = kErrOutput; return; }
-        ring[z.n & (kRing - 1)] = (uint8_t)sym;
-        z.n++;
-      } else if (sym == 256) {
-        z.state = z.last ? 3 : 0;
-      } else {
-        const int li = sym - 257;
-        if (li >= 29) { z.err = kErrSymbol; return; }
-        const uint32_t len = length_base(li) + z_bits(z, length_extra(li));
-        const int ds = z_symbol(z, T.dist, kDistBits, K.dist_code);
-        if (ds < 0) { if (!z.err) z.err = kErrCode; return; }
-        if (ds >= 30) { z.err = kErrSymbol; return; }
-        const uint32_t d = dist_base(ds) + z_bits(z, dist_extra(ds));
-        if (z.err) return;
-        if (d > z.n) { z.err = kErrDistance; return; }
-        if (len > z.cap - z.n) { z.err = kErrOutput; return; }
-        if (d <= kRing) {
-          // the source is in the ring; an overlapping copy (d < len) repeats the bytes just written
-          for (uint32_t k = 0; k < len; k++) {
-            ring[z.n & (kRing - 1)] = ring[(z.n - d) & (kRing - 1)];
-            z.n++;
-          }
-        } else {
-          // farther than the ring: flushed output, read 16 bytes at a time so the loads overlap
-          const uint8_t* src = out + (z.n - d);
-          uint32_t k = 0;
-          for (; k + 16 <= len; k += 16) {
-            uint8_t v[16];
-#pragma unroll
-            for (int j = 0; j < 16; j++) v[j] = src[k + j];
-#pragma unroll
-            for (int j = 0; j < 16; j++) ring[(z.n + j) & (kRing - 1)] = v[j];
-            z.n += 16;
-          }
-          for (; k < len; k++) {
-            ring[z.n & (kRing - 1)] = src[k];
-            z.n++;
-          }
-        }
-      }
-    }
-  }
-}
-
-// The decoder state is copied into a local for the run, so that it stays in registers.
-BSQ_HD void z_run(Inflater& state, Tables& T, Codes& K, uint8_t* ring, const uint8_t* out) {
-  Inflater z = state;
-  z_run_body(z, T, K, ring, out);
-  state = z;
-}
-
-// ----------------------------------------------------------------------------- one-lane decoder
-// The same format decoded whole by one thread with its own small tables, so that a warp decodes 32
-// blocks at once (one per lane) instead of one block on one lane.  Per thread: 9-bit and 6-bit
-// lookup tables for literal/length and distance codes (a longer code falls back to the canonical
-// decode from the code's counts and symbols), and a 64-byte output ring indexed by output address.
-// Output goes to out[] in 16-byte aligned chunks, each stored once complete (the block's partial
-// first and last chunks byte by byte: a neighbouring block's thread writes the rest of them); a
-// back-reference of at most 64 bytes reads the ring, an older one reads out[], which by then holds
-// it.  Input: a 64-bit bit buffer refilled four bytes at a time from aligned 32-bit loads.
+// ----------------------------------------------------------------------------- the device's decoder
+// Two phases.  Phase 1, one thread per block: the Huffman decode alone, into one 32-bit token per
+// symbol, (x << 16) | d: d = 0 for the literal byte x, else a copy of x + 3 bytes from distance d.
+// It checks what phase 2 relies on: every distance within the bytes produced so far and the total
+// equal to the block's size.  Each thread has its own small tables: 9-bit and 6-bit lookup tables for
+// literal/length and distance codes, and for a longer code the canonical decode from the code's first
+// code, first symbol index and count per length (RFC 1951 §3.2.2), all lengths at once from the next
+// 15 bits reversed.  The decoder is a state machine of short steps (a block header with its tables,
+// one symbol, or up to 8 stored bytes) so that 32 lanes, each in its own block, run one step per loop
+// iteration side by side.  Input: a 64-bit bit buffer refilled four bytes at a time from aligned
+// 32-bit loads.  Phase 2 (one warp per block, bsq_bam.cu) turns the tokens into bytes.
 
 constexpr int kLaneLitBits = 9, kLaneDistBits = 6;
-constexpr uint32_t kLaneRing = 64;
+constexpr uint32_t kTokStage = 16;     // tokens staged per thread before a 64-byte store
 
-// A canonical code: counts per length, symbols in (length, value) order (RFC 1951 §3.2.2).
+// A canonical code (RFC 1951 §3.2.2) for the decode of codes longer than a table: the codes of length
+// l are the consecutive values [first[l], limit[l]), and the code value v of length l is symbol
+// symbol[v + base[l]] (base[l] = index of the length's first symbol - first[l], modulo 2^16); symbols in
+// (length, value) order.  Scanning lengths upward, a value below limit[l] is a code: a smaller one
+// would extend a shorter code, found before.
+template <int kSyms>
 struct LaneCode {
-  uint16_t count[kMaxBits + 1];
-  uint16_t symbol[288];
+  uint16_t limit[kMaxBits + 1];
+  uint16_t base[kMaxBits + 1];
+  uint16_t symbol[kSyms];
 };
-struct LaneDistCode {
-  uint16_t count[kMaxBits + 1];
-  uint16_t symbol[32];
-};
-// Per-thread tables (2.1 KB; the device keeps them in shared memory).
+// Per-thread tables (2244 bytes, an odd number of 32-bit words, so that the threads' copies in shared
+// memory start on different banks).
 struct LaneTables {
   uint16_t lit[1 << kLaneLitBits];     // (length << 9) | symbol, 0 = not in the table
   uint16_t dist[1 << kLaneDistBits];
-  LaneCode lc;                         // literal/length code; during a header, the code-length code
-  LaneDistCode dc;
+  LaneCode<288> lc;                    // literal/length code
+  LaneCode<32> dc;                     // distance code; during a header, the code-length code
   uint8_t lengths[288 + 32];
-  alignas(16) uint8_t ring[kLaneRing];   // the last 64 output bytes, at (address & 63)
+  uint16_t pad[2];
 };
+
+static_assert(sizeof(LaneTables) % 8 == 4, "an odd number of 32-bit words");
 
 struct LaneIn {
   const uint8_t* in;
@@ -543,8 +274,8 @@ struct LaneIn {
   int cnt;
 };
 
-// Four bytes at in[pos] from the two aligned words that hold them (in[] is readable up to 3 bytes
-// past the block, which the file's allocation guarantees); one byte at a time near the end.
+// Four bytes at in[pos] from the two aligned words that hold them (in[] is readable up to 3 bytes on
+// either side of the block, which the file's allocation guarantees); one byte at a time near the end.
 BSQ_HD void lane_refill(LaneIn& b) {
   if (b.cnt > 32) return;
   if (b.pos + 4 <= b.len) {
@@ -578,9 +309,8 @@ BSQ_HD uint32_t lane_bits(LaneIn& b, int k, int& err) {
   return v;
 }
 
-// Counts and symbols of a canonical code from n code lengths; false when over-subscribed.
-template <int kSyms>
-BSQ_HD bool lane_code(uint16_t* count, uint16_t* symbol, const uint8_t* lengths, int n) {
+// Counts and first codes per length of n code lengths; false when they over-subscribe the code space.
+BSQ_HD bool lane_counts(const uint8_t* lengths, int n, uint16_t* count, uint32_t* first) {
   for (int l = 0; l <= kMaxBits; l++) count[l] = 0;
   for (int s = 0; s < n; s++) count[lengths[s]]++;
   int left = 1;
@@ -588,24 +318,40 @@ BSQ_HD bool lane_code(uint16_t* count, uint16_t* symbol, const uint8_t* lengths,
     left = (left << 1) - count[l];
     if (left < 0) return false;
   }
+  uint32_t code = 0;
+  first[0] = 0;
+  for (int l = 1; l <= kMaxBits; l++) {
+    code = (code + (l > 1 ? count[l - 1] : 0u)) << 1;
+    first[l] = code;
+  }
+  return true;
+}
+
+// The canonical code of n code lengths; false when they over-subscribe the code space.
+template <int kSyms>
+BSQ_HD bool lane_code(LaneCode<kSyms>& c, const uint8_t* lengths, int n) {
+  uint16_t count[kMaxBits + 1];
+  uint32_t first[kMaxBits + 1];
+  if (!lane_counts(lengths, n, count, first)) return false;
   uint16_t offs[kMaxBits + 1];
-  offs[1] = 0;
-  for (int l = 1; l < kMaxBits; l++) offs[l + 1] = offs[l] + count[l];
+  uint32_t idx = 0;
+  for (int l = 0; l <= kMaxBits; l++) {
+    idx += l > 1 ? count[l - 1] : 0u;
+    offs[l] = (uint16_t)idx;
+    c.limit[l] = (uint16_t)(first[l] + count[l]);
+    c.base[l] = (uint16_t)(idx - first[l]);
+  }
   for (int s = 0; s < n; s++)
-    if (lengths[s] != 0 && offs[lengths[s]] < kSyms) symbol[offs[lengths[s]]++] = (uint16_t)s;
+    if (lengths[s] != 0 && offs[lengths[s]] < kSyms) c.symbol[offs[lengths[s]]++] = (uint16_t)s;
   return true;
 }
 
 // The k-bit lookup table of a code: each code of at most k bits, bit-reversed, fills its entries.
-BSQ_HD void lane_table(uint16_t* table, int k, const uint8_t* lengths, int n, const uint16_t* count) {
+BSQ_HD void lane_table(uint16_t* table, int k, const uint8_t* lengths, int n) {
   for (int i = 0; i < (1 << k); i++) table[i] = 0;
+  uint16_t count[kMaxBits + 1];
   uint32_t next[kMaxBits + 1];
-  uint32_t code = 0;
-  next[0] = 0;
-  for (int l = 1; l <= kMaxBits; l++) {
-    code = (code + (l > 1 ? count[l - 1] : 0u)) << 1;
-    next[l] = code;
-  }
+  lane_counts(lengths, n, count, next);
   for (int s = 0; s < n; s++) {
     const int l = lengths[s];
     if (l == 0) continue;
@@ -617,9 +363,20 @@ BSQ_HD void lane_table(uint16_t* table, int k, const uint8_t* lengths, int n, co
   }
 }
 
-// One symbol through the table, or the canonical decode for a code longer than it.  -1 on failure.
-BSQ_HD int lane_symbol(LaneIn& b, const uint16_t* table, int k, const uint16_t* count, const uint16_t* symbol,
-                       int nsym, int& err) {
+BSQ_HD uint32_t bitrev32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+  return __brev(x);
+#else
+  uint32_t r = 0;
+  for (int i = 0; i < 32; i++) r |= ((x >> i) & 1u) << (31 - i);
+  return r;
+#endif
+}
+
+// One symbol through the table, or, for a code longer than it, the canonical decode: the next 15
+// bits reversed hold every candidate code (the first bit most significant).  -1 on failure.
+template <int kSyms>
+BSQ_HD int lane_symbol(LaneIn& b, const uint16_t* table, int k, const LaneCode<kSyms>& c, int nsym, int& err) {
   if (b.cnt < kMaxBits) lane_refill(b);
   const uint16_t e = table[b.buf & ((1u << k) - 1)];
   if (e) {
@@ -629,163 +386,146 @@ BSQ_HD int lane_symbol(LaneIn& b, const uint16_t* table, int k, const uint16_t* 
     b.cnt -= l;
     return e & 511;
   }
-  int code = 0, first = 0, index = 0;
-  for (int l = 1; l <= kMaxBits; l++) {
-    code |= (int)lane_bits(b, 1, err);
-    if (err) return -1;
-    const int c = count[l];
-    if (code - first < c) {
-      const int i = index + (code - first);
-      if (i >= nsym) { err = kErrCode; return -1; }
-      return symbol[i];
+  const uint32_t c15 = bitrev32((uint32_t)b.buf) >> (32 - kMaxBits);
+  for (int l = k + 1; l <= kMaxBits; l++) {
+    const uint32_t code = c15 >> (kMaxBits - l);
+    if (code < c.limit[l]) {
+      if (l > b.cnt) { err = kErrInput; return -1; }
+      const uint32_t i = (code + c.base[l]) & 0xFFFFu;
+      if (i >= (uint32_t)nsym) { err = kErrCode; return -1; }
+      b.buf >>= l;
+      b.cnt -= l;
+      return c.symbol[i];
     }
-    index += c;
-    first += c;
-    first <<= 1;
-    code <<= 1;
   }
   err = kErrCode;
   return -1;
 }
 
-// Output of one block: bytes o[0, cap), the ring, the partial first chunk.
-struct LaneOut {
-  uint8_t* o;
-  uint32_t n, cap;
-};
+enum : int { kLaneHeader = 0, kLaneStored = 1, kLaneSymbol = 2, kLaneDone = 4 };
 
-// Stores the chunk that ends at output address a (16-byte aligned): whole when it lies inside the
-// block, else the block's own bytes of it.
-BSQ_HD void lane_store_chunk(LaneTables& T, const LaneOut& w, uintptr_t a) {
-  const uintptr_t lo = a - 16, b0 = (uintptr_t)w.o, b1 = (uintptr_t)(w.o + w.n);
-  const uint8_t* src = T.ring + (lo & (kLaneRing - 1));
-  if (lo >= b0 && a <= b1) {
-#ifdef __CUDA_ARCH__
-    *reinterpret_cast<uint4*>(lo) = *reinterpret_cast<const uint4*>(src);
-#else
-    for (int j = 0; j < 16; j++) reinterpret_cast<uint8_t*>(lo)[j] = src[j];
-#endif
-  } else {
-    for (uintptr_t x = lo < b0 ? b0 : lo; x < a && x < b1; x++) *reinterpret_cast<uint8_t*>(x) = src[x - lo];
-  }
-}
-
-BSQ_HD void lane_emit(LaneTables& T, LaneOut& w, uint8_t v) {
-  const uintptr_t a = (uintptr_t)(w.o + w.n);
-  T.ring[a & (kLaneRing - 1)] = v;
-  w.n++;
-  if (((a + 1) & 15) == 0) lane_store_chunk(T, w, a + 1);
-}
-
-// The byte d back from the next output position (1 <= d <= n).
-BSQ_HD uint8_t lane_back(const LaneTables& T, const LaneOut& w, uint32_t d) {
-  const uintptr_t a = (uintptr_t)(w.o + w.n) - d;
-  if (d <= kLaneRing) return T.ring[a & (kLaneRing - 1)];
-  return *reinterpret_cast<const uint8_t*>(a);   // stored at least 48 bytes ago by this thread
-}
-
-// The decoder as a state machine of short steps, so that the 32 lanes of a warp, each in its own
-// block, run the same loop iteration by iteration (the device loop reconverges the warp after every
-// step): a block header with its tables, one Huffman symbol (a literal, or a length and distance
-// that start a copy), up to 8 bytes of a copy, or up to 8 stored bytes.
-enum : int { kLaneHeader = 0, kLaneStored = 1, kLaneSymbol = 2, kLaneCopy = 3, kLaneDone = 4 };
-struct LaneState {
-  LaneIn b;
-  LaneOut w;
-  int mode, last, err;
-  uint32_t left, dist;      // stored or copy bytes left; copy distance
-};
-
-BSQ_HD void lane_start(LaneState& z, const uint8_t* in, uint32_t in_len, uint8_t* out, uint32_t cap) {
-  z.b.in = in; z.b.len = in_len; z.b.pos = 0; z.b.buf = 0; z.b.cnt = 0;
-  z.w.o = out; z.w.n = 0; z.w.cap = cap;
-  z.mode = kLaneHeader; z.last = 0; z.err = kOk; z.left = 0; z.dist = 0;
-}
-
-// A block header: its type, and for Huffman blocks the code lengths and tables.
-BSQ_HD void lane_header(LaneState& z, LaneTables& T) {
-  LaneIn& b = z.b;
-  int& err = z.err;
-  z.last = (int)lane_bits(b, 1, err);
+// A block header: its type, and for Huffman blocks the code lengths and tables.  room: the bytes the
+// block may still produce.  Returns the next mode (kLaneDone with err set on failure).
+BSQ_HD int lane_header(LaneIn& b, LaneTables& T, int& last, int& err, uint32_t& left, uint32_t room) {
+  last = (int)lane_bits(b, 1, err);
   const uint32_t type = lane_bits(b, 2, err);
-  if (err) return;
+  if (err) return kLaneDone;
   if (type == 0) {
     // stored: the rest of the current byte is skipped, then LEN, NLEN and the bytes
     const int drop = b.cnt & 7;
     b.buf >>= drop;
     b.cnt -= drop;
     const uint32_t len = lane_bits(b, 16, err), nlen = lane_bits(b, 16, err);
-    if (err) return;
-    if (len != (~nlen & 0xFFFFu)) { err = kErrStored; return; }
-    if (len > z.w.cap - z.w.n) { err = kErrOutput; return; }
-    z.left = len;
-    z.mode = kLaneStored;
-  } else if (type == 1) {
+    if (err) return kLaneDone;
+    if (len != (~nlen & 0xFFFFu)) { err = kErrStored; return kLaneDone; }
+    if (len > room) { err = kErrOutput; return kLaneDone; }
+    left = len;
+    return kLaneStored;
+  }
+  if (type == 1) {
     for (int s = 0; s < 144; s++) T.lengths[s] = 8;
     for (int s = 144; s < 256; s++) T.lengths[s] = 9;
     for (int s = 256; s < 280; s++) T.lengths[s] = 7;
     for (int s = 280; s < 288; s++) T.lengths[s] = 8;
     for (int s = 0; s < 30; s++) T.lengths[288 + s] = 5;
-    lane_code<288>(T.lc.count, T.lc.symbol, T.lengths, 288);
-    lane_code<32>(T.dc.count, T.dc.symbol, T.lengths + 288, 30);
-    lane_table(T.lit, kLaneLitBits, T.lengths, 288, T.lc.count);
-    lane_table(T.dist, kLaneDistBits, T.lengths + 288, 30, T.dc.count);
-    z.mode = kLaneSymbol;
-  } else if (type == 2) {
-    const int nlen = (int)lane_bits(b, 5, err) + 257, ndist = (int)lane_bits(b, 5, err) + 1;
-    const int ncode = (int)lane_bits(b, 4, err) + 4;
-    if (err) return;
-    if (nlen > 286 || ndist > 30) { err = kErrCode; return; }
-    const uint8_t order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
-    for (int k = 0; k < 19; k++) T.lengths[k] = 0;
-    for (int k = 0; k < ncode; k++) T.lengths[order[k]] = (uint8_t)lane_bits(b, 3, err);
-    if (err) return;
-    // the code-length code, decoded through the distance table (codes of at most 7 bits)
-    if (!lane_code<32>(T.dc.count, T.dc.symbol, T.lengths, 19)) { err = kErrCode; return; }
-    lane_table(T.dist, kLaneDistBits, T.lengths, 19, T.dc.count);
-    int k = 0;
-    while (k < nlen + ndist) {
-      const int sym = lane_symbol(b, T.dist, kLaneDistBits, T.dc.count, T.dc.symbol, 19, err);
-      if (sym < 0) { if (!err) err = kErrCode; return; }
-      if (sym < 16) { T.lengths[k++] = (uint8_t)sym; continue; }
-      uint8_t v = 0;
-      int rep;
-      if (sym == 16) {
-        if (k == 0) { err = kErrCode; return; }
-        v = T.lengths[k - 1];
-        rep = 3 + (int)lane_bits(b, 2, err);
-      } else if (sym == 17) {
-        rep = 3 + (int)lane_bits(b, 3, err);
-      } else {
-        rep = 11 + (int)lane_bits(b, 7, err);
-      }
-      if (err) return;
-      if (k + rep > nlen + ndist) { err = kErrCode; return; }
-      while (rep--) T.lengths[k++] = v;
-    }
-    if (T.lengths[256] == 0) { err = kErrCode; return; }
-    if (!lane_code<288>(T.lc.count, T.lc.symbol, T.lengths, nlen) ||
-        !lane_code<32>(T.dc.count, T.dc.symbol, T.lengths + nlen, ndist)) { err = kErrCode; return; }
-    lane_table(T.lit, kLaneLitBits, T.lengths, nlen, T.lc.count);
-    lane_table(T.dist, kLaneDistBits, T.lengths + nlen, ndist, T.dc.count);
-    z.mode = kLaneSymbol;
-  } else {
-    err = kErrBlockType;
+    lane_code(T.lc, T.lengths, 288);
+    lane_code(T.dc, T.lengths + 288, 30);
+    lane_table(T.lit, kLaneLitBits, T.lengths, 288);
+    lane_table(T.dist, kLaneDistBits, T.lengths + 288, 30);
+    return kLaneSymbol;
   }
+  if (type != 2) { err = kErrBlockType; return kLaneDone; }
+  const int nlen = (int)lane_bits(b, 5, err) + 257, ndist = (int)lane_bits(b, 5, err) + 1;
+  const int ncode = (int)lane_bits(b, 4, err) + 4;
+  if (err) return kLaneDone;
+  if (nlen > 286 || ndist > 30) { err = kErrCode; return kLaneDone; }
+  const uint8_t order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+  for (int k = 0; k < 19; k++) T.lengths[k] = 0;
+  for (int k = 0; k < ncode; k++) T.lengths[order[k]] = (uint8_t)lane_bits(b, 3, err);
+  if (err) return kLaneDone;
+  // the code-length code, decoded through the distance table (codes of at most 7 bits)
+  if (!lane_code(T.dc, T.lengths, 19)) { err = kErrCode; return kLaneDone; }
+  lane_table(T.dist, kLaneDistBits, T.lengths, 19);
+  int k = 0;
+  while (k < nlen + ndist) {
+    const int sym = lane_symbol(b, T.dist, kLaneDistBits, T.dc, 19, err);
+    if (sym < 0) { if (!err) err = kErrCode; return kLaneDone; }
+    if (sym < 16) { T.lengths[k++] = (uint8_t)sym; continue; }
+    uint8_t v = 0;
+    int rep;
+    if (sym == 16) {
+      if (k == 0) { err = kErrCode; return kLaneDone; }
+      v = T.lengths[k - 1];
+      rep = 3 + (int)lane_bits(b, 2, err);
+    } else if (sym == 17) {
+      rep = 3 + (int)lane_bits(b, 3, err);
+    } else {
+      rep = 11 + (int)lane_bits(b, 7, err);
+    }
+    if (err) return kLaneDone;
+    if (k + rep > nlen + ndist) { err = kErrCode; return kLaneDone; }
+    while (rep--) T.lengths[k++] = v;
+  }
+  if (T.lengths[256] == 0) { err = kErrCode; return kLaneDone; }
+  if (!lane_code(T.lc, T.lengths, nlen) || !lane_code(T.dc, T.lengths + nlen, ndist)) {
+    err = kErrCode;
+    return kLaneDone;
+  }
+  lane_table(T.lit, kLaneLitBits, T.lengths, nlen);
+  lane_table(T.dist, kLaneDistBits, T.lengths + nlen, ndist);
+  return kLaneSymbol;
 }
 
-// One step of the decoder; the stream ends in kLaneDone with err set on failure.
-BSQ_HD void lane_step(LaneState& z, LaneTables& T) {
+struct TokState {
+  LaneIn b;
+  uint32_t* tok;        // the block's token array, 16-byte aligned, room for cap tokens
+  uint32_t* stage;      // kTokStage tokens, 16-byte aligned (the device keeps them in shared memory)
+  uint32_t n, staged;   // tokens written to tok, tokens in the stage
+  uint32_t bytes, cap;  // bytes the tokens make; the block's size
+  int mode, last, err;
+  uint32_t left;        // stored bytes left
+};
+
+BSQ_HD void tok_start(TokState& z, const uint8_t* in, uint32_t in_len, uint32_t* tok, uint32_t* stage, uint32_t cap) {
+  z.b.in = in; z.b.len = in_len; z.b.pos = 0; z.b.buf = 0; z.b.cnt = 0;
+  z.tok = tok; z.stage = stage; z.n = 0; z.staged = 0; z.bytes = 0; z.cap = cap;
+  z.mode = kLaneHeader; z.last = 0; z.err = kOk; z.left = 0;
+}
+
+BSQ_HD void tok_flush(TokState& z) {
+  if (z.staged == kTokStage) {
+#ifdef __CUDA_ARCH__
+    uint4* dst = reinterpret_cast<uint4*>(z.tok + z.n);
+    const uint4* src = reinterpret_cast<const uint4*>(z.stage);
+#pragma unroll
+    for (int k = 0; k < 4; k++) dst[k] = src[k];
+#else
+    for (uint32_t k = 0; k < kTokStage; k++) z.tok[z.n + k] = z.stage[k];
+#endif
+  } else {
+    for (uint32_t k = 0; k < z.staged; k++) z.tok[z.n + k] = z.stage[k];
+  }
+  z.n += z.staged;
+  z.staged = 0;
+}
+
+BSQ_HD void tok_put(TokState& z, uint32_t t) {
+  z.stage[z.staged++] = t;
+  if (z.staged == kTokStage) tok_flush(z);
+}
+
+// One step: a block header with its tables, one symbol, or up to 8 stored bytes.
+BSQ_HD void tok_step(TokState& z, LaneTables& T) {
   if (z.mode == kLaneDone) return;
   if (z.mode == kLaneHeader) {
-    lane_header(z, T);
+    z.mode = lane_header(z.b, T, z.last, z.err, z.left, z.cap - z.bytes);
   } else if (z.mode == kLaneSymbol) {
-    const int sym = lane_symbol(z.b, T.lit, kLaneLitBits, T.lc.count, T.lc.symbol, 288, z.err);
+    const int sym = lane_symbol(z.b, T.lit, kLaneLitBits, T.lc, 288, z.err);
     if (sym < 0) {
       if (!z.err) z.err = kErrCode;
     } else if (sym < 256) {
-      if (z.w.n >= z.w.cap) z.err = kErrOutput;
-      else lane_emit(T, z.w, (uint8_t)sym);
+      if (z.bytes >= z.cap) z.err = kErrOutput;
+      else { tok_put(z, (uint32_t)sym << 16); z.bytes++; }
     } else if (sym == 256) {
       z.mode = z.last ? kLaneDone : kLaneHeader;
     } else {
@@ -793,61 +533,62 @@ BSQ_HD void lane_step(LaneState& z, LaneTables& T) {
       if (li >= 29) { z.err = kErrSymbol; }
       else {
         const uint32_t len = length_base(li) + lane_bits(z.b, length_extra(li), z.err);
-        const int ds = lane_symbol(z.b, T.dist, kLaneDistBits, T.dc.count, T.dc.symbol, 32, z.err);
+        const int ds = lane_symbol(z.b, T.dist, kLaneDistBits, T.dc, 32, z.err);
         if (ds < 0) { if (!z.err) z.err = kErrCode; }
         else if (ds >= 30) z.err = kErrSymbol;
         else {
           const uint32_t d = dist_base(ds) + lane_bits(z.b, dist_extra(ds), z.err);
           if (!z.err) {
-            if (d > z.w.n) z.err = kErrDistance;
-            else if (len > z.w.cap - z.w.n) z.err = kErrOutput;
-            else { z.left = len; z.dist = d; z.mode = kLaneCopy; }
+            if (d > z.bytes) z.err = kErrDistance;
+            else if (len > z.cap - z.bytes) z.err = kErrOutput;
+            else { tok_put(z, ((len - 3) << 16) | d); z.bytes += len; }
           }
         }
       }
     }
-  } else if (z.mode == kLaneCopy) {
-    // up to 8 bytes: independent loads when the source is older than the ring (d > 64 keeps them
-    // clear of this copy's own bytes), else one at a time (an overlapping copy repeats its bytes)
-    const uint32_t m = z.left < 8 ? z.left : 8;
-    if (z.dist > kLaneRing && m == 8) {
-      uint8_t v[8];
-#pragma unroll
-      for (int j = 0; j < 8; j++) v[j] = lane_back(T, z.w, z.dist - (uint32_t)j);
-#pragma unroll
-      for (int j = 0; j < 8; j++) lane_emit(T, z.w, v[j]);
-    } else {
-      for (uint32_t j = 0; j < m; j++) lane_emit(T, z.w, lane_back(T, z.w, z.dist));
-    }
-    z.left -= m;
-    if (z.left == 0) z.mode = kLaneSymbol;
   } else {
-    // stored bytes, up to 8
+    // stored bytes, up to 8, as literals
     const uint32_t m = z.left < 8 ? z.left : 8;
-    for (uint32_t j = 0; j < m && !z.err; j++) lane_emit(T, z.w, (uint8_t)lane_bits(z.b, 8, z.err));
+    for (uint32_t j = 0; j < m && !z.err; j++) {
+      const uint32_t v = lane_bits(z.b, 8, z.err);
+      if (!z.err) { tok_put(z, v << 16); z.bytes++; }
+    }
     z.left -= m;
     if (z.left == 0 && !z.err) z.mode = z.last ? kLaneDone : kLaneHeader;
   }
   if (z.err) z.mode = kLaneDone;
 }
 
-// The end of a block: its last partial chunk (the rest of that chunk is the next block's).
-BSQ_HD void lane_finish(LaneState& z, LaneTables& T) {
+// The end of phase 1 for a block: the last staged tokens; kErrOutput when the bytes fall short.
+BSQ_HD void tok_finish(TokState& z) {
   if (z.err) return;
-  const uintptr_t end = (uintptr_t)(z.w.o + z.w.n);
-  if (end & 15) lane_store_chunk(T, z.w, (end | 15) + 1);
+  tok_flush(z);
+  if (z.bytes != z.cap) z.err = kErrOutput;
 }
 
-// Inflates one block's raw DEFLATE data in[0, in_len) into out[0, cap) with one thread's tables;
-// *out_len gets the bytes produced.
-BSQ_HD int inflate_lane(const uint8_t* in, uint32_t in_len, uint8_t* out, uint32_t cap, uint32_t* out_len,
-                        LaneTables& T) {
-  LaneState z;
-  lane_start(z, in, in_len, out, cap);
-  while (z.mode != kLaneDone) lane_step(z, T);
-  lane_finish(z, T);
-  *out_len = z.w.n;
-  return z.err;
+// Phase 2 on one thread (the host form of the warp's work): the tokens' bytes into out.
+BSQ_HD void tokens_to_bytes(const uint32_t* tok, uint32_t n, uint8_t* out) {
+  uint32_t p = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    const uint32_t d = tok[i] & 0xFFFFu, x = tok[i] >> 16;
+    if (d == 0) { out[p++] = (uint8_t)x; continue; }
+    for (uint32_t k = 0; k < x + 3; k++, p++) out[p] = out[p - d];
+  }
+}
+
+// Both phases for one block on one thread; tok has room for cap tokens.
+BSQ_HD int inflate_tokens(const uint8_t* in, uint32_t in_len, uint8_t* out, uint32_t cap, uint32_t* out_len,
+                          uint32_t* tok, uint32_t* n_tok, LaneTables& T) {
+  alignas(16) uint32_t stage[kTokStage];
+  TokState z;
+  tok_start(z, in, in_len, tok, stage, cap);
+  while (z.mode != kLaneDone) tok_step(z, T);
+  tok_finish(z);
+  *n_tok = z.n;
+  *out_len = z.err ? 0 : z.bytes;
+  if (z.err) return z.err;
+  tokens_to_bytes(tok, z.n, out);
+  return kOk;
 }
 
 // ----------------------------------------------------------------------------- CRC-32
@@ -879,34 +620,6 @@ BSQ_HD uint32_t gf2_x8n(uint64_t n) {
 
 BSQ_HD uint32_t crc_combine(uint32_t crc_a, uint32_t crc_b, uint64_t len_b) {
   return gf2_mulmod(gf2_x8n(len_b), crc_a) ^ crc_b;
-}
-
-}  // namespace inflate
-}  // namespace bsq
-
-namespace bsq {
-namespace inflate {
-
-// Host-side driver of the resumable decoder: whenever it pauses the ring is flushed into out and a
-// window of win_size input bytes from the current position is staged in win.
-inline int inflate_ring_host(const uint8_t* in, uint32_t in_len, uint8_t* out, uint32_t cap, uint32_t* out_len,
-                             Tables& T, uint8_t* ring, uint8_t* win, uint32_t win_size) {
-  Codes K;
-  Inflater z;
-  inflater_init(z, in_len, cap);
-  z.win = win;
-  while (z.err == kOk && z.state != 3) {
-    if (z.win_hi < z.in_len && z.pos + kInMargin > z.win_hi) {
-      z.win_lo = z.pos;
-      z.win_hi = z.pos + win_size < in_len ? z.pos + win_size : in_len;
-      for (uint32_t k = z.win_lo; k < z.win_hi; k++) win[k - z.win_lo] = in[k];
-    }
-    z_run(z, T, K, ring, out);
-    for (uint32_t p = z.flushed; p < z.n; p++) out[p] = ring[p & (kRing - 1)];
-    z.flushed = z.n;
-  }
-  *out_len = z.n;
-  return z.err;
 }
 
 }  // namespace inflate

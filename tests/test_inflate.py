@@ -1,6 +1,6 @@
-"""The library's DEFLATE decoders (breseq_gb300/csrc/bsq_inflate.cuh: the bit-by-bit one, the resumable
-table-driven one, driven here through a 4 KiB ring, and the one-lane decoder the device runs, one block
-per thread, writing its output at any alignment), compiled for the host, against
+"""The library's DEFLATE decoders (breseq_gb300/csrc/bsq_inflate.cuh: the bit-by-bit one and the
+two-phase one the device runs, one block per thread into tokens and the tokens into bytes, here both
+phases on one thread), compiled for the host, against
 zlib (the inflater htslib uses under breseq) on random, repetitive and sequence-like data at every
 compression level and strategy, and on truncated or corrupted input, which must fail cleanly."""
 import ctypes as C
@@ -22,8 +22,7 @@ def lib():
     subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", SRC, "-o", OUT])
     L = C.CDLL(OUT)
     L.host_inflate.argtypes = [C.c_char_p, C.c_uint32, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)]
-    L.host_inflate_ring.argtypes = L.host_inflate.argtypes + [C.c_uint32]
-    L.host_inflate_lane.argtypes = L.host_inflate.argtypes
+    L.host_inflate_tokens.argtypes = L.host_inflate.argtypes
     L.host_crc_combine.argtypes = [C.c_uint32, C.c_uint32, C.c_uint64]
     L.host_crc_combine.restype = C.c_uint32
     return L
@@ -48,14 +47,10 @@ STRATEGIES = [zlib.Z_DEFAULT_STRATEGY, zlib.Z_FIXED, zlib.Z_HUFFMAN_ONLY, zlib.Z
 
 
 def run(lib, fn, comp, out, cap, got):
-    if fn == "host_inflate":
-        return lib.host_inflate(comp, len(comp), out, cap, C.byref(got))
-    # the ring decoder with the device's 2 KiB input window, and with a window barely above the margin
-    win = 2048 if fn == "ring" else 700
-    return lib.host_inflate_ring(comp, len(comp), out, cap, C.byref(got), win)
+    return getattr(lib, fn)(comp, len(comp), out, cap, C.byref(got))
 
 
-@pytest.mark.parametrize("fn", ["host_inflate", "ring", "ring_small_window"])
+@pytest.mark.parametrize("fn", ["host_inflate", "host_inflate_tokens"])
 @pytest.mark.parametrize("level", [0, 1, 6, 9])
 @pytest.mark.parametrize("strategy", STRATEGIES, ids=["default", "fixed", "huffman", "rle"])
 def test_matches_zlib(lib, fn, level, strategy):
@@ -92,55 +87,20 @@ def test_bad_input_fails_cleanly(lib):
         assert lib.host_inflate(bytes(b), len(b), out, 65536, C.byref(got)) in range(0, 8)
 
 
-def test_ring_decoder_bad_input(lib):
-    rng = random.Random(9)
+def test_two_phase_bad_input(lib):
+    rng = random.Random(12)
     raw = payload(rng, 30000, 3)
     comp = deflate(raw, 6, zlib.Z_DEFAULT_STRATEGY)
     out = C.create_string_buffer(65536)
     got = C.c_uint32()
-    assert run(lib, "ring", comp[: len(comp) // 2], out, 65536, got) != 0
-    assert run(lib, "ring", comp, out, 1000, got) == 5
-    for _ in range(200):
-        b = bytearray(comp)
-        b[rng.randrange(len(b))] ^= 1 << rng.randrange(8)
-        assert run(lib, "ring_small_window", bytes(b), out, 65536, got) in range(0, 8)
-
-
-@pytest.mark.parametrize("level", [0, 1, 6, 9])
-@pytest.mark.parametrize("strategy", STRATEGIES, ids=["default", "fixed", "huffman", "rle"])
-def test_lane_decoder_matches_zlib(lib, level, strategy):
-    # output at every alignment of a 16-byte chunk; the bytes around it stay untouched
-    rng = random.Random(level * 10 + strategy + 100)
-    for n in [0, 1, 7, 15, 16, 17, 300, 5000, 65536]:
-        for kind in range(4):
-            raw = payload(rng, n, kind)
-            comp = deflate(raw, level, strategy)
-            for shift in (0, 1, 7, 15) if n < 65536 else (0, 9):
-                buf = C.create_string_buffer(b"\xa5" * (n + 64))
-                got = C.c_uint32()
-                rc = lib.host_inflate_lane(comp, len(comp), C.addressof(buf) + 16 + shift, n, C.byref(got))
-                assert rc == 0 and got.value == n
-                assert buf.raw[16 + shift:16 + shift + n] == raw
-                assert buf.raw[:16 + shift] == b"\xa5" * (16 + shift)
-                assert buf.raw[16 + shift + n:n + 64] == b"\xa5" * (48 - shift)
-
-
-def test_lane_decoder_bad_input(lib):
-    rng = random.Random(11)
-    raw = payload(rng, 30000, 3)
-    comp = deflate(raw, 6, zlib.Z_DEFAULT_STRATEGY)
-    out = C.create_string_buffer(65536 + 64)
-    got = C.c_uint32()
-    assert lib.host_inflate_lane(comp[: len(comp) // 2], len(comp) // 2, out, 65536, C.byref(got)) != 0
-    assert lib.host_inflate_lane(comp, len(comp), out, 1000, C.byref(got)) == 5
-    assert lib.host_inflate_lane(bytes([0x07]), 1, out, 65536, C.byref(got)) == 2
-    assert lib.host_inflate_lane(bytes([0x01, 0x05, 0x00, 0x00, 0x00]), 5, out, 65536, C.byref(got)) == 3
+    assert lib.host_inflate_tokens(comp[: len(comp) // 2], len(comp) // 2, out, 30000, C.byref(got)) != 0
+    assert lib.host_inflate_tokens(comp, len(comp), out, 1000, C.byref(got)) == 5
+    assert lib.host_inflate_tokens(comp, len(comp), out, 30001, C.byref(got)) == 5     # short of the size
     for _ in range(300):
         b = bytearray(comp)
         for _ in range(rng.randrange(1, 3)):
             b[rng.randrange(len(b))] ^= 1 << rng.randrange(8)
-        assert lib.host_inflate_lane(bytes(b), len(b), out, 65536, C.byref(got)) in range(0, 8)
-        assert got.value <= 65536
+        assert lib.host_inflate_tokens(bytes(b), len(b), out, 30000, C.byref(got)) in range(0, 8)
 
 
 def test_crc_combine(lib):
