@@ -239,7 +239,10 @@ def run_bam(args, device, s):
                     "mode": "sequential: open, decode, load, both passes, free per step"},
             "host_ms_by_phase": {k: statistics.mean(v) for k, v in phases.items()},
             "inflate_kernel_ms": inf_ms, "decode_device_ms": statistics.mean(kern["decode"]),
-            "roofline": {"bound": "latency (one thread decodes a block's Huffman stream serially)", "kernel": "bgzf_inflate_kernel",
+            # the three inflate kernels together: Huffman symbols to tokens (one thread per block, 32
+            # blocks per warp in lockstep), tokens to bytes (one warp per block), CRC-32s
+            "roofline": {"bound": "latency and divergence (each thread decodes its block's Huffman stream serially)",
+                         "kernel": "bgzf_tok_kernel + bgzf_resolve_kernel + bgzf_crc_kernel",
                          "achieved": (len(data) + out_bytes) / (inf_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
                          "frac": (len(data) + out_bytes) / (inf_ms / 1e3) / 1e9 / hbm, "peak_kind": peak_kind,
                          "algorithmic_bytes": len(data) + out_bytes, "traffic": None},

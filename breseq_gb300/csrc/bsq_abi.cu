@@ -1935,10 +1935,11 @@ static std::string bam_err_text(uint32_t e) {
   std::string s;
   if (e & kBamInflate) s += "BGZF block does not inflate; ";
   if (e & kBamCrc) s += "BGZF block CRC-32 mismatch; ";
-  if (e & kBamSpan) s += "a record spans BGZF blocks or its size is invalid; ";
+  if (e & kBamSpan) s += "a record's size is invalid; ";
   if (e & kBamRecord) s += "record fields out of range; ";
   if (e & kBamAux) s += "malformed aux field; ";
   if (e & kBamOrder) s += "unplaced records before placed ones; ";
+  if (e & kBamLongCigar) s += "a CIGAR of more than 65535 operations kept in the CG tag (not supported); ";
   return s;
 }
 
@@ -2044,16 +2045,38 @@ int bsq_bam_decode(bsq_ctx* ctx, bsq_bam* bam, const bsq_bam_groups* groups, uin
   if (nb) CK(cudaMemcpyAsync(hc.data(), counts.p, (uint64_t)nb * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&herr, w, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  if (herr) return fail(ctx, BSQ_ERR_INVALID, bam_err_text(herr));
-  std::vector<uint64_t> hb(nb);
-  uint64_t n = 0;
-  for (uint32_t b = 0; b < nb; b++) { hb[b] = n; n += hc[b]; }
-  if (n >= 0xFFFFFFFFull) return fail(ctx, BSQ_ERR_INVALID, "more than 2^32 - 1 records");
   DevMem offsets;
-  CK(upload(base, hb.data(), nb, st));
-  CK(offsets.alloc(n * 8 + 16, st));
-  CK(bam_walk(bam->stream.as<uint8_t>(), bam->blocks.as<BgzfBlock>(), nb, bam->records_begin, nullptr,
-              base.as<uint64_t>(), offsets.as<uint64_t>(), w, ctx->sms, st));
+  uint64_t n = 0;
+  if (herr == kBamSpan) {
+    // a record spans BGZF blocks (htslib's writer never does this, other writers do): the record
+    // offsets come from one walk over the whole inflated stream on the host
+    std::vector<uint8_t> hs(bam->stream_len);
+    CK(cudaMemcpy(hs.data(), bam->stream.p, bam->stream_len, cudaMemcpyDeviceToHost));
+    std::vector<uint64_t> ho;
+    for (uint64_t p = bam->records_begin; p < bam->stream_len;) {
+      if (p + 4 > bam->stream_len) return fail(ctx, BSQ_ERR_INVALID, "a record is cut off at the end of the stream");
+      const int32_t bs = (int32_t)(hs[p] | ((uint32_t)hs[p + 1] << 8) | ((uint32_t)hs[p + 2] << 16) |
+                                   ((uint32_t)hs[p + 3] << 24));
+      if (bs < 32 || p + 4 + (uint64_t)bs > bam->stream_len) return fail(ctx, BSQ_ERR_INVALID, "a record's size is invalid");
+      ho.push_back(p);
+      p += 4 + (uint64_t)bs;
+    }
+    n = ho.size();
+    if (n >= 0xFFFFFFFFull) return fail(ctx, BSQ_ERR_INVALID, "more than 2^32 - 1 records");
+    CK(offsets.alloc(n * 8 + 16, st));
+    if (n) CK(cudaMemcpyAsync(offsets.p, ho.data(), n * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(w, 0, 4, st));
+    CK(cudaStreamSynchronize(st));
+  } else {
+    if (herr) return fail(ctx, BSQ_ERR_INVALID, bam_err_text(herr));
+    std::vector<uint64_t> hb(nb);
+    for (uint32_t b = 0; b < nb; b++) { hb[b] = n; n += hc[b]; }
+    if (n >= 0xFFFFFFFFull) return fail(ctx, BSQ_ERR_INVALID, "more than 2^32 - 1 records");
+    CK(upload(base, hb.data(), nb, st));
+    CK(offsets.alloc(n * 8 + 16, st));
+    CK(bam_walk(bam->stream.as<uint8_t>(), bam->blocks.as<BgzfBlock>(), nb, bam->records_begin, nullptr,
+                base.as<uint64_t>(), offsets.as<uint64_t>(), w, ctx->sms, st));
+  }
   // fixed fields and tags
   bam->rec.reset(new RecordsDev());
   bam->decoded = false;

@@ -260,6 +260,15 @@ __global__ void __launch_bounds__(256) bam_fields_kernel(const uint8_t* stream, 
         else if (t0 == 'X' && t1 == 'L' && !has_xl) { has_xl = true; xl = aux_int(q, type); }
         else if (t0 == 'X' && t1 == 'R' && !has_xr) { has_xr = true; xr = aux_int(q, type); }
         else if (t0 == 'X' && t1 == 'J') { has_xj = true; }
+        else if (t0 == 'C' && t1 == 'G' && type == 'B' && q[0] == 'I') {
+          // SAM specification §4.2.2: a CIGAR of more than 65535 operations is kept in CG:B:I, and the
+          // record's own CIGAR is the placeholder <l_seq>S<reference length>N, which htslib replaces
+          // when it reads the record.  The device record holds 65535 operations at most: refused.
+          const uint32_t* cg = reinterpret_cast<const uint32_t*>(stream + v.cigar);
+          if (v.n_cigar == 2 && rd32(reinterpret_cast<const uint8_t*>(cg)) == (((uint32_t)v.l_seq << 4) | 4u) &&
+              (rd32(reinterpret_cast<const uint8_t*>(cg + 1)) & 0xFu) == 3u)
+            e |= kBamLongCigar;
+        }
         else if (t0 == 'X' && t1 == 'P' && !has_xp) {
           // the pair orientation breseq writes as XP:Z (FR, RF or FF); read as bam_aux2Z does
           has_xp = true;

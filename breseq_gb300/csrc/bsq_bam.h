@@ -29,7 +29,8 @@ struct BgzfBlock {
 };
 
 // error bits of the BAM path
-enum : uint32_t { kBamInflate = 1, kBamCrc = 2, kBamSpan = 4, kBamRecord = 8, kBamAux = 16, kBamOrder = 32 };
+enum : uint32_t { kBamInflate = 1, kBamCrc = 2, kBamSpan = 4, kBamRecord = 8, kBamAux = 16, kBamOrder = 32,
+                  kBamLongCigar = 64 };
 
 constexpr int kBamMaxGroups = 64;
 

@@ -695,10 +695,13 @@ def pd_null(s: Sample, max_distance: int = 2000) -> np.ndarray:
     return np.clip((mid * 1048576 + 0.5).astype(np.int64), 0, 1048576)
 
 
-def bam_bytes(s: Sample, level: int = 6, block_payload: int = 0xFF00, seed: int = 0, rg_tags: bool = True) -> bytes:
+def bam_bytes(s: Sample, level: int = 6, block_payload: int = 0xFF00, seed: int = 0, rg_tags: bool = True,
+              split_records: bool = False) -> bytes:
     """The sample as a coordinate-sorted BAM (SAM/BAM specification §4.2), compressed in BGZF blocks
     the way htslib writes them: the header in its own blocks, a record never split across blocks
     (a block is closed before a record would overflow block_payload bytes), an EOF block at the end.
+    split_records: the record stream cut every block_payload bytes instead, records spanning blocks,
+    as other writers (htsjdk's) do.
     Tags: X1 when the redundancy is not 1, XL / XR when present, XJ when set, RG when the sample has
     several read groups (or always, with rg_tags); integer tags in varying BAM integer types."""
     import struct
@@ -768,6 +771,12 @@ def bam_bytes(s: Sample, level: int = 6, block_payload: int = 0xFF00, seed: int 
                            nc, int(s.flag[i]), L, mt, mp, tlen)
         rec = body + name + cig.astype("<u4").tobytes() + seq + qual + aux
         rec = struct.pack("<i", len(rec)) + rec
+        if split_records:
+            buf += rec
+            while len(buf) >= block_payload:
+                out.append(_bgzf_block(bytes(buf[:block_payload]), level))
+                del buf[:block_payload]
+            continue
         if len(buf) + len(rec) > block_payload and buf:
             out.append(_bgzf_block(bytes(buf), level))
             buf = bytearray()

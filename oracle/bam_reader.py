@@ -93,6 +93,12 @@ def read_bam(data: bytes, groups=None):
                 tags[tag] = (typ, stream[a:a + size])
             a += size
         o = end
+        # a CIGAR of more than 65535 operations kept in CG:B:I behind the placeholder <l_seq>S<len>N
+        # (SAM specification 4.2.2): the library's records hold 65535 operations at most, so it is refused
+        if "CG" in tags and tags["CG"][0] == "B" and tags["CG"][1][:1] == b"I" and n_cig == 2:
+            c1, c2 = struct.unpack_from("<II", stream, c0)
+            if c1 == (l_seq << 4) | 4 and (c2 & 0xF) == 3:
+                raise BamError("a CIGAR of more than 65535 operations kept in the CG tag")
         if ref_id < 0:
             seen_unplaced = True
             continue

@@ -55,3 +55,18 @@ def test_pair_annotations_round_trip():
     for k in ("isize", "xp", "qname_off", "qname", "mtid", "mpos", "flag"):
         assert np.array_equal(r[k], getattr(s, k)), k
     assert set(np.unique(r["xp"])) <= {0, 1, 2, 3} and (r["xp"] == 3).any() and (r["xp"] < 3).any()
+
+
+def test_spanning_records_and_cg_cigar():
+    # blocks cut regardless of records read the same; a CIGAR kept in the CG tag is refused
+    import struct
+    s = samples.ecoli_small()
+    a = bam_reader.read_bam(synth.bam_bytes(s, block_payload=4096), synth.bam_groups(s))
+    b = bam_reader.read_bam(synth.bam_bytes(s, block_payload=4096, split_records=True), synth.bam_groups(s))
+    for k in a["records"]:
+        assert np.array_equal(a["records"][k], b["records"][k]), k
+    recs, groups = bam_cases.tag_cases()
+    cg = bam_cases.record(0, 30, [(20, "S"), (20, "N")], "ACGT" * 5,
+                          b"CGBI" + struct.pack("<I", 1) + struct.pack("<I", (20 << 4) | 0))
+    with pytest.raises(bam_reader.BamError):
+        bam_reader.read_bam(bam_cases.bam(recs[:6] + [cg]), groups)

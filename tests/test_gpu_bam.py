@@ -1,6 +1,8 @@
 """BAM input on the GPU (bsq_bam_open / decode / load): BGZF inflate and record decode against the
 oracle reader, byte for byte, and the scoring passes on a sample loaded from BAM bytes identical to
 the same sample loaded from arrays."""
+import struct
+
 import numpy as np
 import pytest
 
@@ -55,6 +57,16 @@ def test_levels_and_block_sizes(scorer, level, payload):
     check(scorer, synth.bam_bytes(s, level=level, block_payload=payload, seed=level), synth.bam_groups(s))
 
 
+@pytest.mark.parametrize("payload", [0xFF00, 4096, 300])
+def test_records_spanning_blocks(scorer, payload):
+    # blocks cut at fixed sizes regardless of records (as htsjdk writes them): the record offsets come
+    # from a walk over the whole inflated stream
+    s = samples.ecoli_small()
+    check(scorer, synth.bam_bytes(s, block_payload=payload, split_records=True), synth.bam_groups(s))
+    recs, groups = bam_cases.tag_cases()
+    check(scorer, bam_cases.bam(recs, split=True), groups)
+
+
 def test_xj_and_single_group(scorer):
     s = samples.softclip_sample()
     check(scorer, synth.bam_bytes(s, rg_tags=False), synth.bam_groups(s))
@@ -72,10 +84,12 @@ def test_tag_rules(scorer):
 def test_errors(scorer):
     recs, groups = bam_cases.tag_cases()
     good = bam_cases.bam(recs)
-    # a record split across blocks
+    # a CIGAR kept in the CG tag behind the placeholder <l_seq>S<reference length>N
+    cg = bam_cases.record(0, 30, [(20, "S"), (20, "N")], "ACGT" * 5,
+                          b"CGBI" + struct.pack("<I", 1) + struct.pack("<I", (20 << 4) | 0) + b"RGZg0\0")
     with pytest.raises(_lib.BsqError) as e:
-        gpu_decode(scorer, bam_cases.bam(recs, split=True), groups)
-    assert e.value.code == -1
+        gpu_decode(scorer, bam_cases.bam(recs[:6] + [cg]), groups)
+    assert e.value.code == -1 and "CG tag" in str(e.value)
     # unplaced records before placed ones
     with pytest.raises(_lib.BsqError):
         gpu_decode(scorer, bam_cases.bam([recs[6]] + recs[:6]), groups)
