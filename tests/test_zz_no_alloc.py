@@ -4,8 +4,9 @@ synchronize the device; a program that gives all of HBM to its own arena).  Its 
 device array inside the library; the caller brings device buffers for the positions and the results.
 
 The test calls it twice in a row through the C ABI, with the caller's buffers allocated by torch, and
-checks each call's RA items against the ones bsq_identify_mutations reports for the same positions, at
-the tolerances of the parity tests (scores 1e-3, frequencies 1e-4, counts exact).
+checks each call's RA items against the ones bsq_identify_mutations reports for the same positions and
+against the CPU oracle's, at the tolerances of the parity tests (scores 1e-3, frequencies 1e-4, counts
+exact).
 """
 import ctypes as C
 
@@ -41,7 +42,7 @@ def _device_call(sc, torch, sid, params, table, positions, n_quality):
     return [raw[i] for i in range(n)]
 
 
-def test_noalloc_positions_match_identify_mutations(built_lib):
+def test_noalloc_positions_match_identify_mutations(built_lib, oracle_lib):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("needs a CUDA device")
@@ -55,6 +56,10 @@ def test_noalloc_positions_match_identify_mutations(built_lib):
         table = sc.counts_to_log10_prob(ec["counts"], s.n_read_files, s.n_quality)
         expected = sc.identify_mutations(sid, table, ImSettings(), precision=0)["ra"]
         assert expected, "the sample must carry RA items"
+        from oracle import pyoracle as po
+        from tests import compare
+        oracle_ra = po.identify(s, table, po.default_im_params(s))["ra"]
+        assert not compare.compare_ra(expected, oracle_ra)
         T = len(s.target_offset) - 1
         prop = np.full(T, 5.0)
         seed = np.zeros(T)
