@@ -115,6 +115,13 @@ struct bsq_ctx {
   DevMem keep, kcol, kcov, kcall;
   DevMem d_chunks, ec_arena, im_arena, ctl;
   PinnedBuf pin_in, pin_out;
+  // page-locked landing areas of device-to-host reads that run beside other threads' work: a read into
+  // pageable memory is staged by the driver, and such reads wait for one another across streams (an
+  // upload's check would hold up a pass's results until the upload ends)
+  PinnedBuf pin_res;                    // pass 2's RA items, quality histograms and kept columns
+  static constexpr uint32_t kStatSlots = 64;
+  PinnedBuf pin_stats;                  // kStatSlots x 64 bytes: a load's packing statistics
+  std::atomic<uint32_t> stat_rr{0};
   bsq_tuning tune = {1024, 8, 8, 16, 4, 1};
   cudaGraphExec_t exec_ec = nullptr, exec_im = nullptr;
   uint64_t graph_instantiations = 0, graph_updates = 0;
@@ -305,7 +312,9 @@ int bsq_create(bsq_ctx** out, int device) {
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
   // pinned staging reserved now, before any upload runs beside it (see PinnedBuf::reserve)
-  if (c->pin_in.reserve(8u << 20) != cudaSuccess || c->pin_out.reserve(8u << 20) != cudaSuccess) return BSQ_ERR_CUDA;
+  if (c->pin_in.reserve(8u << 20) != cudaSuccess || c->pin_out.reserve(8u << 20) != cudaSuccess ||
+      c->pin_res.reserve(16u << 20) != cudaSuccess || c->pin_stats.reserve(bsq_ctx::kStatSlots * 64) != cudaSuccess)
+    return BSQ_ERR_CUDA;
   if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       cudaEventCreate(&c->evm0) != cudaSuccess || cudaEventCreate(&c->evm1) != cudaSuccess ||
       cudaEventCreate(&c->evt0) != cudaSuccess || cudaEventCreate(&c->evt1) != cudaSuccess)
@@ -458,7 +467,7 @@ static int pack_sample(bsq_ctx* ctx, std::unique_ptr<SampleDev>& s, RecordsDev& 
   CK(s->refnib.alloc((size_t)refnib_words(s->n_cols) * 8, st));
   CK(launch_ref_check(s->ref.as<uint8_t>(), s->refnib.as<unsigned long long>(), s->n_cols, stats + 11, stats + 12,
                       ctx->sms, st));
-  uint32_t h[16];
+  uint32_t* h = reinterpret_cast<uint32_t*>(ctx->pin_stats.at(64 * (ctx->stat_rr.fetch_add(1) % bsq_ctx::kStatSlots)));
   CK(cudaMemcpyAsync(h, stats, 16 * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (h[11] || h[12] != T) return fail(ctx, BSQ_ERR_DATA, "reference base outside A/C/G/T/N");
@@ -684,8 +693,8 @@ static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_p
   const cudaError_t pe = run_pass(ctx, ctx->exec_ec, [&]() -> cudaError_t {
     cudaError_t e;
     if ((e = record(ctx->ev0, st)) != cudaSuccess) return e;
-    if ((e = cudaMemcpyAsync(ctx->d_chunks.p, ctx->pin_in.p, std::max<size_t>(16, n_chunks * sizeof(uint4)),
-                             cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    if ((e = launch_host_copy(ctx->pin_in.p, ctx->d_chunks.p, std::max<size_t>(16, n_chunks * sizeof(uint4)), ctx->sms,
+                              st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(A0, 0, arena_bytes, st)) != cudaSuccess) return e;
     if ((e = launch_ec(B, ctx->d_chunks.as<uint4>(), (uint32_t)n_chunks, ctx->next.as<unsigned int>(), max_bins, grid, st,
                        ctx->evm0, ctx->evm1)) != cudaSuccess) return e;
@@ -915,7 +924,7 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
     step = "ev0";
     if ((e = record(ctx->ev0, st)) != cudaSuccess) return e;
     step = "arena copy";
-    if ((e = cudaMemcpyAsync(A0, ctx->pin_in.p, arena_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    if ((e = launch_host_copy(ctx->pin_in.p, A0, arena_bytes, ctx->sms, st)) != cudaSuccess) return e;
     step = "control words";
     if ((e = cudaMemsetAsync(ctl, 0, kCtlWords * 4, st)) != cudaSuccess) return e;
     if ((e = record(ctx->evm0, st)) != cudaSuccess) return e;
@@ -970,20 +979,24 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
   if (cerr & ~kErrRaOverflow) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(cerr));
   for (uint32_t j = 0; j < n; j++)
     if (ctl_host[kCtlJobErr + j]) return fail(ctx, BSQ_ERR_DATA, "identify_mutations: " + err_text(ctl_host[kCtlJobErr + j]));
-  // ---- variable-size results
+  // ---- variable-size results, through page-locked memory
   std::vector<RaDev> ra(n_ra);
   std::vector<uint32_t> qh((size_t)n_ra * 2 * Qh);
-  if (n_ra) {
-    CK(cudaMemcpyAsync(ra.data(), ctx->ra.p, (size_t)n_ra * sizeof(RaDev), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(qh.data(), ctx->qhist.p, qh.size() * 4, cudaMemcpyDeviceToHost, st));
-  }
   std::vector<uint32_t> kept(nk);
   std::vector<ColCov> kcov(nk);
   std::vector<ColCall> kcall(nk);
+  const size_t r_ra = 0, r_qh = align256(r_ra + ra.size() * sizeof(RaDev)), r_kept = align256(r_qh + qh.size() * 4),
+               r_kcov = align256(r_kept + (size_t)nk * 4), r_kcall = align256(r_kcov + (size_t)nk * sizeof(ColCov)),
+               r_end = r_kcall + (size_t)nk * sizeof(ColCall);
+  CK(ctx->pin_res.reserve(r_end + 16));
+  if (n_ra) {
+    CK(cudaMemcpyAsync(ctx->pin_res.at(r_ra), ctx->ra.p, (size_t)n_ra * sizeof(RaDev), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(ctx->pin_res.at(r_qh), ctx->qhist.p, qh.size() * 4, cudaMemcpyDeviceToHost, st));
+  }
   if (nk) {
-    CK(cudaMemcpyAsync(kept.data(), ctx->kcol.p, (size_t)nk * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(kcov.data(), ctx->kcov.p, (size_t)nk * sizeof(ColCov), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(kcall.data(), ctx->kcall.p, (size_t)nk * sizeof(ColCall), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(ctx->pin_res.at(r_kept), ctx->kcol.p, (size_t)nk * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(ctx->pin_res.at(r_kcov), ctx->kcov.p, (size_t)nk * sizeof(ColCov), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(ctx->pin_res.at(r_kcall), ctx->kcall.p, (size_t)nk * sizeof(ColCall), cudaMemcpyDeviceToHost, st));
   }
   // per-position arrays only where they were asked for
   std::vector<std::vector<ColCov>> pcov(n);
@@ -997,6 +1010,15 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
     CK(cudaMemcpyAsync(pcall[j].data(), ctx->call.as<ColCall>() + col_b[j], (size_t)nc * sizeof(ColCall), cudaMemcpyDeviceToHost, st));
   }
   CK(cudaStreamSynchronize(st));
+  if (n_ra) {
+    memcpy(ra.data(), ctx->pin_res.at(r_ra), (size_t)n_ra * sizeof(RaDev));
+    memcpy(qh.data(), ctx->pin_res.at(r_qh), qh.size() * 4);
+  }
+  if (nk) {
+    memcpy(kept.data(), ctx->pin_res.at(r_kept), (size_t)nk * 4);
+    memcpy(kcov.data(), ctx->pin_res.at(r_kcov), (size_t)nk * sizeof(ColCov));
+    memcpy(kcall.data(), ctx->pin_res.at(r_kcall), (size_t)nk * sizeof(ColCall));
+  }
   // ---- host assembly, per job
   std::vector<std::vector<RaDev>> jra(n);
   std::vector<std::vector<uint32_t>> jqh(n);

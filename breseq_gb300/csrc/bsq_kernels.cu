@@ -1122,6 +1122,22 @@ __global__ void ref_check_kernel(const uint8_t* ref, unsigned long long* refnib,
     if (nz) atomicAdd(zeros, nz);
   }
 }
+// The per-call parameters a pass stages in page-locked host memory, read straight from it by the SMs
+// (the memory is mapped into the device's address space) rather than by a copy engine: a sample upload
+// running on another stream keeps the copy engines busy for milliseconds, and a copy queued behind it
+// would hold up the pass.  bytes is a multiple of 16 and both pointers are 16-byte aligned.
+__global__ void __launch_bounds__(256) host_copy_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst, uint64_t n16) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n16; i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+cudaError_t launch_host_copy(const void* src, void* dst, size_t bytes, int sms, cudaStream_t st) {
+  const uint64_t n16 = bytes / 16;
+  if (n16 == 0) return cudaSuccess;
+  host_copy_kernel<<<grid_for((uint32_t)std::min<uint64_t>(n16, 1u << 30), 256, sms, 4), 256, 0, st>>>(
+      static_cast<const uint4*>(src), static_cast<uint4*>(dst), n16);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ref_check(const uint8_t* ref, unsigned long long* refnib, uint32_t n_cols, uint32_t* bad,
                              uint32_t* zeros, int sms, cudaStream_t st) {
   ref_check_kernel<<<sms * 4, 256, 0, st>>>(ref, refnib, n_cols, refnib_words(n_cols), bad, zeros);

@@ -43,6 +43,9 @@ struct PackOut {
 };
 
 cudaError_t launch_pack(const RawSoA& in, const PackOut& out, cudaStream_t st);
+// dst[0, bytes) = src[0, bytes) by a kernel reading page-locked host memory (bytes a multiple of 16,
+// both 16-byte aligned): no copy engine, so no wait behind uploads on other streams.
+cudaError_t launch_host_copy(const void* src, void* dst, size_t bytes, int sms, cudaStream_t st);
 // Counts reference bytes outside A/C/G/T/N/separator into *bad and zero bytes into *zeros, and writes
 // each column's 4-bit code (A,C,G,T = 1,2,4,8, anything else 15) into refnib.
 // Words of the nibble-packed reference (column c at nibble c + 16), with one spare word after the last
