@@ -60,6 +60,11 @@ struct SampleDev {
   // pair annotations for the discordant / missing-pair scans: raw flags, XP codes, TLEN, names
   DevMem pflag, pxp, pisize, pqoff, pqname, pmtid, pmpos;
   bool has_pairs = false, has_mates = false;
+  // per-base class bytes (base_code_kernel); usable by the column pass when no A/C/G/T base has a
+  // quality above kCodeMaxQ, and for a call whose quality range is above max_q
+  DevMem code;
+  bool code_ok = false;
+  uint32_t max_q = 0;
   uint32_t n_targets = 0, n_cols = 0, n_tiles = 0, n_reads = 0, maxspan = 1, max_tile_reads = 0;
   uint32_t n_groups = 0;
   std::vector<uint64_t> toff;       // caller's target offsets
@@ -192,6 +197,7 @@ static DevSample make_dev_sample(const SampleDev& s) {
   S.cigar = s.cigar.as<uint32_t>();
   S.seq = s.seq.as<uint8_t>();
   S.qual = s.qual.as<uint8_t>();
+  S.code = nullptr;                 // set per call by the column pass's job setup
   S.tile_range = s.tile_range.as<uint2>();
   S.tpoff = s.d_tpoff.as<uint32_t>();
   S.tgt_group = s.tgt_group.as<uint32_t>();
@@ -364,8 +370,9 @@ uint64_t bsq_sample_footprint(const bsq_reference* ref, const bsq_read_soa* rd) 
   const uint64_t pairs = (rd->xp && rd->isize && rd->qname_off && rd->qname)
                              ? rd->n_reads * 15 + 8 + (rd->n_reads ? rd->qname_off[rd->n_reads] : 0)
                              : 0;
+  // bases: packed nibbles, qualities and the column pass's class bytes
   return 2 * (cols + 64) + rd->n_reads * per_read + rd->n_cigar_total * 4 + rd->n_bases_total / 2 + 16 +
-         rd->n_bases_total + tiles * 8 + upload_tmp + pairs;
+         2 * rd->n_bases_total + 48 + tiles * 8 + upload_tmp + pairs;
 }
 
 }  // extern "C"
@@ -463,6 +470,10 @@ static int pack_sample(bsq_ctx* ctx, std::unique_ptr<SampleDev>& s, RecordsDev& 
   po.reads = s->reads.as<DevRead>(); po.qb = s->qb.as<QBounds>(); po.rstart = s->rstart.as<uint32_t>();
   po.mapq = s->mapq.as<uint8_t>(); po.err = stats; po.maxspan = stats + 1; po.mapq_mask = stats + 2;
   CK(launch_pack(in, po, st));
+  // the column pass's per-base class bytes: [13] a quality too large for them, [14] the largest quality
+  CK(s->code.alloc((R.n_bases_total + 15) / 16 * 16 + 16, st));
+  CK(launch_base_code(s->seq.as<uint8_t>(), s->qual.as<uint8_t>(), R.n_bases_total, s->code.as<uint8_t>(), stats + 13,
+                      ctx->sms, st));
   // the reference checked on the device: [11] bytes outside A/C/G/T/N, [12] zero bytes (separators)
   CK(s->refnib.alloc((size_t)refnib_words(s->n_cols) * 8, st));
   CK(launch_ref_check(s->ref.as<uint8_t>(), s->refnib.as<unsigned long long>(), s->n_cols, stats + 11, stats + 12,
@@ -474,6 +485,8 @@ static int pack_sample(bsq_ctx* ctx, std::unique_ptr<SampleDev>& s, RecordsDev& 
   if (h[0]) return fail(ctx, (h[0] & (kErrOrder | kErrCigar | kErrBounds | kErrX1)) ? BSQ_ERR_INVALID : BSQ_ERR_DATA,
                         "invalid records: " + err_text(h[0]));
   s->maxspan = std::max<uint32_t>(1, h[1]);
+  s->code_ok = h[13] == 0;
+  s->max_q = h[14];
   uint8_t map[256];
   memset(map, 0, sizeof map);
   for (int v = 0; v < 256; v++) {
@@ -885,6 +898,7 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
     DevJob& J = B.jobs[j];
     J.S = make_dev_sample(*s);
     J.S.tgt_failed = A0 + lay[j].failed;
+    if (s->code_ok && s->max_q < P[j].n_quality) J.S.code = s->code.as<uint8_t>();
     J.T.lp64 = reinterpret_cast<const double*>(A0 + lay[j].lp64);
     J.T.r64 = reinterpret_cast<const double*>(A0 + lay[j].r64);
     J.T.lpmax64 = reinterpret_cast<const double*>(A0 + lay[j].lpmax64);

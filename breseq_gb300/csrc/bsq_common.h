@@ -58,6 +58,7 @@ struct DevSample {
   const uint32_t* cigar;
   const uint8_t* seq;         // packed 4-bit, high nibble first
   const uint8_t* qual;
+  const uint8_t* code;        // per base: quality * 5 + observed base, 255 N, 254 other (null: not used)
   const uint2* tile_range;    // [n_tiles]
   const uint32_t* tpoff;      // padded target offsets [n_targets + 1]
   const uint32_t* tgt_group;  // coverage group per target
@@ -100,7 +101,8 @@ struct ClassTable {
   const double* lp64;     // [K][5]
   const double* r64;      // [K][5]
   const double* lpmax64;  // [K]
-  const float* lp32;      // [K][8]: lp[0..4] as float, [5] = 1 when obs-hypothesis is not the max
+  const float* lp32;      // [K + 1][8]: lp[0..4] as float, [5] (bits) bit r = the column pass's
+                          // screen bound takes the base at reference base r; entry K all zeros
   uint32_t K;
   uint32_t R, Q, n_mapq;
 };
@@ -222,6 +224,7 @@ struct Batch {
   uint32_t pad;
   DevJob jobs[kBatchJobs];
 };
+static_assert(sizeof(Batch) <= 32764, "a Batch is passed as one kernel parameter");
 
 // Per-warp scratch of the candidate kernels, in uint4 units: `cap` gather entries followed by `cap`
 // (class, multiplicity) pairs.

@@ -65,7 +65,7 @@ void build_class_table(const double* tab, uint32_t R, uint32_t Q, const std::vec
   o.lp64.assign((size_t)o.K * 5, 0);
   o.r64.assign((size_t)o.K * 5, 0);
   o.lpmax64.assign(o.K, 0);
-  o.lp32.assign((size_t)o.K * 8, 0);
+  o.lp32.assign((size_t)(o.K + 1) * 8, 0);    // entry K: all zeros (a base the column pass does not score)
   std::vector<double> prob((size_t)R * 25 * Q);
   for (size_t i = 0; i < prob.size(); i++) prob[i] = pow(10, tab[i]);
   auto compl_idx = [](uint32_t b) -> uint32_t { return b < 4 ? 3 - b : 4; };
@@ -94,7 +94,12 @@ void build_class_table(const double* tab, uint32_t R, uint32_t Q, const std::vec
               o.lp32[(size_t)k * 8 + b] = (float)lp[b];
             }
             o.lpmax64[k] = mx;
-            o.lp32[(size_t)k * 8 + 5] = (lp[obs] < mx) ? 1.0f : 0.0f;
+            // bit r: the column pass's screen bound takes this base at a column whose reference
+            // base is r (0..4, 5 = none): its base is not r, or not its own most likely hypothesis
+            uint32_t screen = 0;
+            for (uint32_t r = 0; r < 6; r++)
+              if (obs != r || lp[obs] < mx) screen |= 1u << r;
+            memcpy(&o.lp32[(size_t)k * 8 + 5], &screen, 4);
           }
   }
 }

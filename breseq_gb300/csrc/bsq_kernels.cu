@@ -584,6 +584,7 @@ constexpr size_t kColRareBytes = 256 * (5 * 4 + 2 * 4 + 2 * 8);
 // two byte loads, the class lookup and the sums.
 struct __align__(16) FastRead {
   uint64_t qual;       // address of qual[seq_off + clip - start]: the quality at column c is at qual + c
+                       // (of the class bytes instead, when the sample has them)
   uint64_t seq;        // address of the read's first packed base byte (seq_off is even)
   uint32_t start;      // first column
   uint32_t span_clip;  // reference span (low 16 bits) | leading soft clip << 16
@@ -599,6 +600,8 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
   // one 32-byte slot per read of the staged batch: its FastRead on the common path, else its DevRead
   DevRead* sh_rd = reinterpret_cast<DevRead*>(smem) + warp * 32;
   FastRead* sh_fr = reinterpret_cast<FastRead*>(smem) + warp * 32;
+  // with class bytes, a common-path read's slot holds its 16-byte CodeRead (see the staging below)
+  uint4* sh_cr = reinterpret_cast<uint4*>(smem) + warp * 64;
   // accumulators only rare reads touch (mismatching or low-likelihood bases, redundant reads): one
   // shared-memory slot per thread, column by column, instead of registers held for the whole tile
   ColRare rare(smem + kColumnWarps * 32 * sizeof(DevRead), threadIdx.x);
@@ -626,6 +629,12 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
     float s4 = 0.0f, k4 = 0.0f;
     const uint2 rr = __ldg(S.tile_range + tile);
     const bool tile_fast = __all_sync(0xFFFFFFFFu, !failed);
+    // with the per-base class bytes, a common-path base is one byte: scored when its class byte is at
+    // least cut5 and below 254 (code - cut5 < lim, unsigned)
+    const uint8_t* const codes = S.code;
+    const uint32_t cut5 = A.base_quality_cutoff * 5u;
+    const uint32_t lim = cut5 < 254u ? 254u - cut5 : 0u;
+    const uint32_t refbit = 1u << ref_idx;
     // Kahan-compensated FP32 sums of one class entry (hypotheses 0-1, 2-3 packed, 4 scalar)
     auto kahan = [&](const ulonglong2& v, float x4) {
       const unsigned long long y01 = f32x2_sub(v.x, k01), y23 = f32x2_sub(v.y, k23);
@@ -656,7 +665,7 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
         const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(T.lp32 + (size_t)k * 8));
         const float2 w = __ldg(reinterpret_cast<const float2*>(T.lp32 + (size_t)k * 8 + 4));
         kahan(v, w.x);
-        if (obs != ref_idx || w.y != 0.0f) screen(v, w.x);
+        if (__float_as_uint(w.y) & refbit) screen(v, w.x);
       }
     };
     // One read as this lane sees it in the general case: the pileup state at column c (CIGAR walk,
@@ -726,6 +735,31 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       }
     };
     bool bad_base = false, bad_q = false;
+    // the same for a sample with class bytes, from its 16-byte CodeRead: one byte per base, its class
+    // at kbase + code, the zero entry K when the base is not scored
+    auto code_load = [&](const uint4& f, bool have, uint32_t& code) {
+      const uint32_t d = c - f.y;
+      const bool cov = have && real && d < (f.z & 0xFFFFu);
+      code = cov ? (uint32_t)__ldg(codes + (uint32_t)(f.x + c)) : 255u;
+    };
+    auto code_use = [&](const uint4& f, uint32_t code) {
+      const bool counted = code != 255u;                              // covered, and not an N read base
+      const bool rev = f.z >> 31;
+      utop += (counted && !rev) ? 1u : 0u;
+      ubot += (counted && rev) ? 1u : 0u;
+      bad_base |= code == 254u;                                       // not one of A, C, G, T
+      const bool use = code - cut5 < lim;
+      if (FP64) {
+        if (use) accumulate(f.w + code, 0);
+      } else {
+        const uint32_t k = use ? f.w + code : T.K;
+        const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(T.lp32 + (size_t)k * 8));
+        const float2 w = __ldg(reinterpret_cast<const float2*>(T.lp32 + (size_t)k * 8 + 4));
+        n += use ? 1u : 0u;
+        kahan(v, w.x);
+        if (__float_as_uint(w.y) & refbit) screen(v, w.x);
+      }
+    };
     auto fast_use = [&](const FastRead& f, const FastLd& L) {
       const uint32_t base = (L.byte >> L.sh) & 15u;
       const bool counted = base != 15u;                               // covered, and not an N read base
@@ -750,56 +784,71 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
         }
         n += use ? 1u : 0u;
         kahan(v, w.x);
-        if (use && ((int)obs != ref_idx || w.y != 0.0f)) screen(v, w.x);
+        if (__float_as_uint(w.y) & refbit) screen(v, w.x);     // zeros when not scored
       }
     };
     for (uint32_t b0 = rr.x; b0 < rr.y; b0 += 32) {
       const uint32_t rl = b0 + lane;
       bool rel = false, fast = false;
+      DevRead mine;
       if (rl < rr.y) {
-        const DevRead mine = S.reads[rl];
+        mine = S.reads[rl];
         rel = !(mine.flags & kSkip) && mine.end > c0;
         fast = rel && tile_fast && (mine.flags & (kSimple | kRedundant | kDpCand)) == kSimple &&
                (mine.xl == kNoTag || mine.xl == 0) && (mine.xr == kNoTag || mine.xr == 0) && mine.rfile < T.R;
-        if (fast) {
+      }
+      // the batch's common-path reads take slots 0..nf-1 and the others the slots after them, each
+      // part in BAM order, so the loops below walk slots by index
+      unsigned fmask = __ballot_sync(0xFFFFFFFFu, fast);
+      unsigned gmask = __ballot_sync(0xFFFFFFFFu, rel && !fast);
+      const uint32_t nf = __popc(fmask);
+      const unsigned below = (1u << lane) - 1u;
+      if (fast) {
+        const uint32_t slot = __popc(fmask & below);
+        const uint32_t rev = mine.flags & kRev;
+        const uint32_t kbase = (((uint32_t)mine.mapq_idx * T.R + mine.rfile) * 2u + rev) * T.Q * 5u;
+        if (codes) {
+          // CodeRead: class-byte index of column 0 (mod 2^32), first column, span | strand << 31, class base
+          sh_cr[slot] = make_uint4((uint32_t)(mine.seq_off + mine.clip) - mine.start, mine.start,
+                                   (mine.end - mine.start) | (rev << 31), kbase);
+        } else {
           FastRead f;
-          const uint32_t rev = mine.flags & kRev;
           f.qual = (uint64_t)(uintptr_t)S.qual + mine.seq_off + mine.clip - mine.start;
           f.seq = (uint64_t)(uintptr_t)S.seq + (mine.seq_off >> 1);
           f.start = mine.start;
           f.span_clip = (mine.end - mine.start) | ((uint32_t)mine.clip << 16);
-          f.kbase = (((uint32_t)mine.mapq_idx * T.R + mine.rfile) * 2u + rev) * T.Q * 5u;
+          f.kbase = kbase;
           f.rev = rev;
-          sh_fr[lane] = f;
-        } else {
-          sh_rd[lane] = mine;
+          sh_fr[slot] = f;
         }
+      } else if (rel) {
+        sh_rd[nf + __popc(gmask & below)] = mine;
       }
-      unsigned fmask = __ballot_sync(0xFFFFFFFFu, fast);
-      unsigned gmask = __ballot_sync(0xFFFFFFFFu, rel && !fast);
       __syncwarp();
       // common-path reads in BAM order, kColumnIlp at a time
-      while (fmask) {
-        int j[kColumnIlp];
-        bool have[kColumnIlp];
+      if (codes) {
+        for (uint32_t j0 = 0; j0 < nf; j0 += kColumnIlp) {
+          uint32_t code[kColumnIlp];
 #pragma unroll
-        for (int u = 0; u < (int)kColumnIlp; u++) {
-          have[u] = fmask != 0;
-          j[u] = have[u] ? __ffs(fmask) - 1 : 0;
-          fmask &= fmask - 1;
+          for (int u = 0; u < (int)kColumnIlp; u++) code_load(sh_cr[min(j0 + u, 31u)], j0 + u < nf, code[u]);
+#pragma unroll
+          for (int u = 0; u < (int)kColumnIlp; u++) code_use(sh_cr[min(j0 + u, 31u)], code[u]);
         }
-        FastLd L[kColumnIlp];
+      } else {
+        for (uint32_t j0 = 0; j0 < nf; j0 += kColumnIlp) {
+          FastLd L[kColumnIlp];
 #pragma unroll
-        for (int u = 0; u < (int)kColumnIlp; u++) fast_load(sh_fr[j[u]], have[u], L[u]);
+          for (int u = 0; u < (int)kColumnIlp; u++) fast_load(sh_fr[min(j0 + u, 31u)], j0 + u < nf, L[u]);
 #pragma unroll
-        for (int u = 0; u < (int)kColumnIlp; u++) fast_use(sh_fr[j[u]], L[u]);
+          for (int u = 0; u < (int)kColumnIlp; u++) fast_use(sh_fr[min(j0 + u, 31u)], L[u]);
+        }
       }
       // the other reads of the batch in BAM order (redundant reads keep BAM order among themselves,
       // so the per-column 1/X1 sums run in the reference's order)
-      while (gmask) {
+      for (uint32_t slot = nf; gmask; slot++) {
         const int j = __ffs(gmask) - 1;
         gmask &= gmask - 1;
-        general(sh_rd[j], b0 + j);
+        general(sh_rd[slot], b0 + j);
       }
       __syncwarp();
     }
@@ -1135,6 +1184,58 @@ cudaError_t launch_host_copy(const void* src, void* dst, size_t bytes, int sms, 
   if (n16 == 0) return cudaSuccess;
   host_copy_kernel<<<grid_for((uint32_t)std::min<uint64_t>(n16, 1u << 30), 256, sms, 4), 256, 0, st>>>(
       static_cast<const uint4*>(src), static_cast<uint4*>(dst), n16);
+  return cudaGetLastError();
+}
+
+// One byte per read base for the column pass: quality * 5 + observed base (A, C, G, T = 0..3) for a
+// base A/C/G/T, 255 for N, 254 for anything else (an IUPAC code, or the padding nibble after an odd-
+// length read: the pass reports it where it is counted).  flags[0] = 1 when an A/C/G/T base has a
+// quality above kCodeMaxQ (the byte cannot hold it: the pass keeps the packed form for the sample);
+// flags[1] = the largest quality of an A/C/G/T base.  Sixteen bases a thread,
+// read as one 16-byte quality word and one 8-byte word of packed bases (both arrays carry 16 bytes of
+// slack past their ends, so the last word never leaves them).
+__global__ void __launch_bounds__(256) base_code_kernel(const uint8_t* __restrict__ seq, const uint8_t* __restrict__ qual,
+                                                        uint64_t n_bases, uint8_t* __restrict__ code, uint32_t* flags) {
+  uint32_t bad = 0, maxq = 0;
+  const uint64_t words = (n_bases + 15) / 16;
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < words; w += (uint64_t)gridDim.x * blockDim.x) {
+    const uint4 q4 = __ldg(reinterpret_cast<const uint4*>(qual) + w);
+    const uint2 s2 = __ldg(reinterpret_cast<const uint2*>(seq) + w);
+    const uint32_t qw[4] = {q4.x, q4.y, q4.z, q4.w}, sw[2] = {s2.x, s2.y};
+    uint32_t out[4];
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const uint32_t q = (qw[i >> 2] >> (8 * (i & 3))) & 0xFFu;
+      const uint32_t byte = (sw[i >> 3] >> (8 * ((i >> 1) & 3))) & 0xFFu;
+      const uint32_t nib = (i & 1) ? (byte & 15u) : (byte >> 4);        // high nibble first
+      const bool live = w * 16 + i < n_bases;
+      uint32_t v = 255u;
+      if (nib != 15u) {
+        const bool one_hot = (0x116u >> nib) & 1u;                       // 1, 2, 4 or 8
+        if (live && one_hot) {
+          maxq = max(maxq, q);
+          if (q > kCodeMaxQ) bad = 1u;
+        }
+        v = one_hot && q <= kCodeMaxQ ? q * 5u + (31u - __clz(nib)) : 254u;
+      }
+      if (i % 4 == 0) out[i >> 2] = 0;
+      out[i >> 2] |= v << (8 * (i & 3));
+    }
+    reinterpret_cast<uint4*>(code)[w] = make_uint4(out[0], out[1], out[2], out[3]);
+  }
+  bad = __reduce_or_sync(0xFFFFFFFFu, bad);
+  maxq = __reduce_max_sync(0xFFFFFFFFu, maxq);
+  if ((threadIdx.x & 31) == 0) {
+    if (bad) atomicOr(flags, bad);
+    if (maxq) atomicMax(flags + 1, maxq);
+  }
+}
+cudaError_t launch_base_code(const uint8_t* seq, const uint8_t* qual, uint64_t n_bases, uint8_t* code, uint32_t* flags,
+                             int sms, cudaStream_t st) {
+  const uint64_t words = (n_bases + 15) / 16;
+  if (words == 0) return cudaSuccess;
+  base_code_kernel<<<grid_for((uint32_t)std::min<uint64_t>(words, 1u << 30), 256, sms, 4), 256, 0, st>>>(
+      seq, qual, n_bases, code, flags);
   return cudaGetLastError();
 }
 

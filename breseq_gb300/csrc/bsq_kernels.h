@@ -50,6 +50,11 @@ cudaError_t launch_host_copy(const void* src, void* dst, size_t bytes, int sms, 
 // each column's 4-bit code (A,C,G,T = 1,2,4,8, anything else 15) into refnib.
 // Words of the nibble-packed reference (column c at nibble c + 16), with one spare word after the last
 // column a thread may read past.
+// The per-base class bytes of the column pass (quality * 5 + observed base, 255 for N); see
+// base_code_kernel.  code holds n_bases rounded up to 16 bytes; seq and qual have 16 bytes of slack.
+constexpr uint32_t kCodeMaxQ = 50;
+cudaError_t launch_base_code(const uint8_t* seq, const uint8_t* qual, uint64_t n_bases, uint8_t* code, uint32_t* flags,
+                             int sms, cudaStream_t st);
 inline uint32_t refnib_words(uint32_t n_cols) { return (n_cols + 16u) / 16u + 2u; }
 cudaError_t launch_ref_check(const uint8_t* ref, unsigned long long* refnib, uint32_t n_cols, uint32_t* bad,
                              uint32_t* zeros, int sms, cudaStream_t st);
