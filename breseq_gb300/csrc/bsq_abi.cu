@@ -65,6 +65,9 @@ struct SampleDev {
   DevMem code;
   bool code_ok = false;
   uint32_t max_q = 0;
+  // tiles with long read ranges, which the column pass runs first
+  DevMem heavy, heavy_bits;
+  uint32_t n_heavy = 0;
   uint32_t n_targets = 0, n_cols = 0, n_tiles = 0, n_reads = 0, maxspan = 1, max_tile_reads = 0;
   uint32_t n_groups = 0;
   std::vector<uint64_t> toff;       // caller's target offsets
@@ -199,6 +202,8 @@ static DevSample make_dev_sample(const SampleDev& s) {
   S.qual = s.qual.as<uint8_t>();
   S.code = nullptr;                 // set per call by the column pass's job setup
   S.tile_range = s.tile_range.as<uint2>();
+  S.heavy = s.heavy.as<uint32_t>();
+  S.heavy_bits = s.heavy_bits.as<uint32_t>();
   S.tpoff = s.d_tpoff.as<uint32_t>();
   S.tgt_group = s.tgt_group.as<uint32_t>();
   S.tgt_called = s.tgt_called.as<uint8_t>();
@@ -372,7 +377,7 @@ uint64_t bsq_sample_footprint(const bsq_reference* ref, const bsq_read_soa* rd) 
                              : 0;
   // bases: packed nibbles, qualities and the column pass's class bytes
   return 2 * (cols + 64) + rd->n_reads * per_read + rd->n_cigar_total * 4 + rd->n_bases_total / 2 + 16 +
-         2 * rd->n_bases_total + 48 + tiles * 8 + upload_tmp + pairs;
+         2 * rd->n_bases_total + 48 + tiles * 13 + 192 + upload_tmp + pairs;   // tiles: range, heavy list and bits
 }
 
 }  // extern "C"
@@ -499,9 +504,16 @@ static int pack_sample(bsq_ctx* ctx, std::unique_ptr<SampleDev>& s, RecordsDev& 
   CK(s->tile_range.alloc((size_t)s->n_tiles * sizeof(uint2) + 16, st));
   CK(cudaMemsetAsync(stats + 10, 0, 4, st));
   CK(launch_tile_range(s->rstart.as<uint32_t>(), (uint32_t)n, s->n_tiles, s->maxspan, s->tile_range.as<uint2>(), stats + 10, st));
-  CK(cudaMemcpyAsync(h + 10, stats + 10, 4, cudaMemcpyDeviceToHost, st));
+  // heavy tiles: a read range above twice the expected n * (maxspan + 31) / columns reads ([15] counts)
+  CK(s->heavy.alloc(((size_t)s->n_tiles + 16) * 4, st));
+  CK(s->heavy_bits.alloc(((size_t)s->n_tiles / 32 + 16) * 4, st));
+  const uint64_t expect = s->n_cols ? (uint64_t)n * (s->maxspan + 31) / s->n_cols : 0;
+  CK(launch_tile_heavy(s->tile_range.as<uint2>(), s->n_tiles, (uint32_t)std::min<uint64_t>(2 * expect + 8, UINT32_MAX - 1),
+                       s->heavy.as<uint32_t>(), s->heavy_bits.as<uint32_t>(), stats + 15, st));
+  CK(cudaMemcpyAsync(h + 10, stats + 10, 6 * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   s->max_tile_reads = h[10];
+  s->n_heavy = h[15];
   if (R.has_pairs) {
     take(s->pflag, R.flag);
     take(s->pxp, R.xp);
@@ -791,7 +803,7 @@ int bsq_counts_to_log10_prob_batch(uint32_t n, const uint64_t* const* counts, co
 // ============================================================================ pass 2
 // Control words of pass 2, written on the device and read back in one copy.
 enum : uint32_t { kCtlCand = 0, kCtlCand2 = 1, kCtlKept = 2, kCtlRa = 3, kCtlCandErr = 4, kCtlBq = 5, kCtlPool = 6,
-                  kCtlBqNext = 7, kCtlJobErr = 8, kCtlWords = 8 + kBatchJobs };
+                  kCtlBqNext = 7, kCtlJobErr = 8, kCtlColNext = 8 + kBatchJobs, kCtlWords = 9 + kBatchJobs };
 constexpr uint32_t kBoundPool = 4u << 20;   // (class, multiplicity) entries for deferred bounds: 32 MiB
 
 // One group of at most kBatchJobs samples; results go to res_*[job0 + j].
@@ -885,6 +897,9 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
   B.n_jobs = n;
   B.total_tiles = tile_b[n]; B.total_cols = total_cols;
   for (uint32_t j = 0; j <= n; j++) { B.tile_begin[j] = tile_b[j]; B.col_begin[j] = col_b[j]; }
+  for (uint32_t j = 0; j < n; j++) B.heavy_begin[j + 1] = B.heavy_begin[j] + smp[j]->n_heavy;
+  B.total_heavy = B.heavy_begin[n];
+  B.tile_next = ctl + kCtlColNext;
   for (uint32_t j = 0; j < n; j++) {
     const SampleDev* s = smp[j];
     memcpy(ctx->pin_in.at(lay[j].lp64), ct[j].lp64.data(), ct[j].lp64.size() * 8);

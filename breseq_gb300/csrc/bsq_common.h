@@ -60,6 +60,8 @@ struct DevSample {
   const uint8_t* qual;
   const uint8_t* code;        // per base: quality * 5 + observed base, 255 N, 254 other (null: not used)
   const uint2* tile_range;    // [n_tiles]
+  const uint32_t* heavy;      // tiles with a long read range, run first by the column pass
+  const uint32_t* heavy_bits; // bit per tile: listed in heavy
   const uint32_t* tpoff;      // padded target offsets [n_targets + 1]
   const uint32_t* tgt_group;  // coverage group per target
   const uint8_t* tgt_called;  // 1 when the target is in the pileup set
@@ -221,7 +223,9 @@ struct Batch {
   uint32_t tile_begin[kBatchJobs + 1];
   uint32_t col_begin[kBatchJobs + 1];
   uint32_t cblk_begin[kBatchJobs + 1];
-  uint32_t pad;
+  uint32_t heavy_begin[kBatchJobs + 1];   // column pass: prefix of the jobs' heavy-tile counts
+  uint32_t total_heavy;
+  unsigned int* tile_next;                // column pass tile queue (zero before the launch)
   DevJob jobs[kBatchJobs];
 };
 static_assert(sizeof(Batch) <= 32764, "a Batch is passed as one kernel parameter");

@@ -170,6 +170,25 @@ __global__ void tile_range_kernel(const uint32_t* rstart, uint32_t n_reads, uint
   if ((threadIdx.x & 31) == __ffs(act) - 1) atomicMax(max_tile_reads, wmax);
 }
 
+// Tiles whose read range exceeds `thr` reads: listed (any order) and flagged in a bit per tile, so the
+// column pass runs them first (see its tile queue).  Lane k of a warp holds tile 32w + k.
+__global__ void tile_heavy_kernel(const uint2* tile_range, uint32_t n_tiles, uint32_t thr, uint32_t* heavy,
+                                  uint32_t* heavy_bits, uint32_t* n_heavy) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  bool h = false;
+  if (t < n_tiles) {
+    const uint2 rr = tile_range[t];
+    h = rr.y - rr.x > thr;
+  }
+  const unsigned m = __ballot_sync(0xFFFFFFFFu, h);
+  const uint32_t lane = threadIdx.x & 31;
+  if (lane == 0 && t < n_tiles) heavy_bits[t >> 5] = m;
+  uint32_t base = 0;
+  if (lane == 0 && m) base = atomicAdd(n_heavy, (uint32_t)__popc(m));
+  base = __shfl_sync(0xFFFFFFFFu, base, 0);
+  if (h) heavy[base + __popc(m & ((1u << lane) - 1u))] = t;
+}
+
 // ============================================================================ pass 1: error counts
 // error_count_pileup::pileup_callback (error_count.cpp:125-199) with count_alignment_position
 // (error_count.cpp:854-986), read-parallel: a warp walks one read at a time, lanes over its aligned
@@ -576,6 +595,9 @@ struct ColRare {
   __device__ double weight(bool rev) const { return w[rev * 256 + t]; }
 };
 constexpr size_t kColRareBytes = 256 * (5 * 4 + 2 * 4 + 2 * 8);
+// 1/X1 of each staged redundant read, one double per slot (computed once per read and tile by the lane
+// that stages it, not by every lane at every column: FP64 division is slow here)
+constexpr size_t kColWeightBytes = kColumnWarps * 32 * sizeof(double);
 
 // Staged record of a common-path read for one tile: one aligned block (soft clips allowed), unique,
 // untrimmed, a known read file, in a tile with no failed-fit column.  What depends on the read alone
@@ -596,7 +618,7 @@ static_assert(sizeof(FastRead) == sizeof(DevRead), "a staging slot holds either 
 template <bool FP64>
 __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant__ Batch Bt) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // one 32-byte slot per read of the staged batch: its FastRead on the common path, else its DevRead
   DevRead* sh_rd = reinterpret_cast<DevRead*>(smem) + warp * 32;
   FastRead* sh_fr = reinterpret_cast<FastRead*>(smem) + warp * 32;
@@ -605,10 +627,34 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
   // accumulators only rare reads touch (mismatching or low-likelihood bases, redundant reads): one
   // shared-memory slot per thread, column by column, instead of registers held for the whole tile
   ColRare rare(smem + kColumnWarps * 32 * sizeof(DevRead), threadIdx.x);
+  double* sh_w = reinterpret_cast<double*>(smem + kColumnWarps * 32 * sizeof(DevRead) + kColRareBytes) + warp * 32;
   uint32_t local_err = 0;
-  for (uint32_t gt = blockIdx.x * nwarps + warp; gt < Bt.total_tiles; gt += gridDim.x * nwarps) {
-    const uint32_t job = job_of(Bt.tile_begin, Bt.n_jobs, gt);
-    const uint32_t tile = gt - Bt.tile_begin[job];
+  // Tiles come from a queue, one per warp at a time: first every job's heavy tiles (a read range more
+  // than twice the sample's expected one: repeat copies, coverage peaks), then all tiles in column
+  // order, skipping the heavy ones.  A warp holding a heavy tile takes fewer tiles, and the heavy ones
+  // start first, so no warp is left running alone at the end.  The next unit is fetched while the
+  // current tile runs.  Results do not depend on the order: a tile writes only its own columns.
+  const uint32_t n_units = Bt.total_heavy + Bt.total_tiles;
+  uint32_t q = 0;
+  if (lane == 0) q = atomicAdd(Bt.tile_next, 1u);
+  q = __shfl_sync(0xFFFFFFFFu, q, 0);
+  while (q < n_units) {
+    uint32_t job, tile;
+    if (q < Bt.total_heavy) {
+      job = job_of(Bt.heavy_begin, Bt.n_jobs, q);
+      tile = __ldg(Bt.jobs[job].S.heavy + (q - Bt.heavy_begin[job]));
+    } else {
+      const uint32_t gt = q - Bt.total_heavy;
+      job = job_of(Bt.tile_begin, Bt.n_jobs, gt);
+      tile = gt - Bt.tile_begin[job];
+    }
+    uint32_t q_next = 0;
+    if (lane == 0) q_next = atomicAdd(Bt.tile_next, 1u);
+    const uint32_t* hb = Bt.jobs[job].S.heavy_bits;
+    if (q >= Bt.total_heavy && Bt.total_heavy && hb && ((__ldg(hb + (tile >> 5)) >> (tile & 31)) & 1u)) {
+      q = __shfl_sync(0xFFFFFFFFu, q_next, 0);        // run from the heavy list already
+      continue;
+    }
     const DevSample& S = Bt.jobs[job].S;
     const ClassTable& T = Bt.jobs[job].T;
     const ImArgs& A = Bt.jobs[job].I;
@@ -670,7 +716,7 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
     };
     // One read as this lane sees it in the general case: the pileup state at column c (CIGAR walk,
     // trims, deletions, redundancy) and the base / quality that state selects.
-    auto general = [&](const DevRead& rd, uint32_t r) {
+    auto general = [&](const DevRead& rd, uint32_t r, double inv_x1) {
       if (!(real && c >= rd.start && c < rd.end)) return;
       Pile e;
       resolve(S, rd, c, e);
@@ -687,7 +733,7 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
         // tabulate_position_coverage (identify_mutations.cpp:2218-2250)
         if (e.del || base == 15) return;
         if (!red) { if (rev) ++ubot; else ++utop; }
-        else rare.redundant(rev, 1.0 / (double)__ldg(S.x1 + r));
+        else rare.redundant(rev, inv_x1);
         return;
       }
       // a discordant-pair candidate without a usable XP tag, at its first column (:1399-1416)
@@ -695,7 +741,7 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       if (!e.del && base == 15) return;                       // N read base: not counted at all
       if (red) {
         uonly = false;
-        rare.redundant(rev, 1.0 / (double)__ldg(S.x1 + r));
+        rare.redundant(rev, inv_x1);
         return;
       }
       if (rev) ++ubot; else ++utop;
@@ -742,9 +788,18 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       const bool cov = have && real && d < (f.z & 0xFFFFu);
       code = cov ? (uint32_t)__ldg(codes + (uint32_t)(f.x + c)) : 255u;
     };
-    auto code_use = [&](const uint4& f, uint32_t code) {
+    auto code_use = [&](const uint4& f, uint32_t code, uint32_t slot) {
       const bool counted = code != 255u;                              // covered, and not an N read base
       const bool rev = f.z >> 31;
+      if ((f.z >> 30) & 1u) {
+        // a simple redundant read: redundant coverage and its 1/X1 weight, nothing scored (the
+        // general path's outcome for such a read); the warp takes this branch together
+        if (counted) {
+          uonly = false;
+          rare.redundant(rev, sh_w[slot]);
+        }
+        return;
+      }
       utop += (counted && !rev) ? 1u : 0u;
       ubot += (counted && rev) ? 1u : 0u;
       bad_base |= code == 254u;                                       // not one of A, C, G, T
@@ -794,9 +849,13 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       if (rl < rr.y) {
         mine = S.reads[rl];
         rel = !(mine.flags & kSkip) && mine.end > c0;
-        fast = rel && tile_fast && (mine.flags & (kSimple | kRedundant | kDpCand)) == kSimple &&
+        fast = rel && tile_fast && (mine.flags & (kSimple | kDpCand)) == kSimple &&
                (mine.xl == kNoTag || mine.xl == 0) && (mine.xr == kNoTag || mine.xr == 0) && mine.rfile < T.R;
       }
+      // Redundant reads take the common path only with class bytes, and only when every redundant read
+      // of the batch does, so that their 1/X1 sums keep BAM order in one loop.
+      const bool red = rel && (mine.flags & kRedundant);
+      if (__any_sync(0xFFFFFFFFu, red && !(fast && codes))) fast = fast && !red;
       // the batch's common-path reads take slots 0..nf-1 and the others the slots after them, each
       // part in BAM order, so the loops below walk slots by index
       unsigned fmask = __ballot_sync(0xFFFFFFFFu, fast);
@@ -808,9 +867,11 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
         const uint32_t rev = mine.flags & kRev;
         const uint32_t kbase = (((uint32_t)mine.mapq_idx * T.R + mine.rfile) * 2u + rev) * T.Q * 5u;
         if (codes) {
-          // CodeRead: class-byte index of column 0 (mod 2^32), first column, span | strand << 31, class base
+          // CodeRead: class-byte index of column 0 (mod 2^32), first column, span | redundant << 30 |
+          // strand << 31 (a simple read's span is below 2^16), class base
           sh_cr[slot] = make_uint4((uint32_t)(mine.seq_off + mine.clip) - mine.start, mine.start,
-                                   (mine.end - mine.start) | (rev << 31), kbase);
+                                   (mine.end - mine.start) | ((uint32_t)red << 30) | (rev << 31), kbase);
+          if (red) sh_w[slot] = 1.0 / (double)__ldg(S.x1 + rl);
         } else {
           FastRead f;
           f.qual = (uint64_t)(uintptr_t)S.qual + mine.seq_off + mine.clip - mine.start;
@@ -822,7 +883,9 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
           sh_fr[slot] = f;
         }
       } else if (rel) {
-        sh_rd[nf + __popc(gmask & below)] = mine;
+        const uint32_t slot = nf + __popc(gmask & below);
+        sh_rd[slot] = mine;
+        sh_w[slot] = (mine.flags & kRedundant) ? 1.0 / (double)__ldg(S.x1 + rl) : 0.0;
       }
       __syncwarp();
       // common-path reads in BAM order, kColumnIlp at a time
@@ -832,7 +895,7 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
 #pragma unroll
           for (int u = 0; u < (int)kColumnIlp; u++) code_load(sh_cr[min(j0 + u, 31u)], j0 + u < nf, code[u]);
 #pragma unroll
-          for (int u = 0; u < (int)kColumnIlp; u++) code_use(sh_cr[min(j0 + u, 31u)], code[u]);
+          for (int u = 0; u < (int)kColumnIlp; u++) code_use(sh_cr[min(j0 + u, 31u)], code[u], min(j0 + u, 31u));
         }
       } else {
         for (uint32_t j0 = 0; j0 < nf; j0 += kColumnIlp) {
@@ -848,7 +911,7 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       for (uint32_t slot = nf; gmask; slot++) {
         const int j = __ffs(gmask) - 1;
         gmask &= gmask - 1;
-        general(sh_rd[slot], b0 + j);
+        general(sh_rd[slot], b0 + j, sh_w[slot]);
       }
       __syncwarp();
     }
@@ -919,6 +982,7 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
     if (bad_base) local_err |= kErrBase;
     if (bad_q) local_err |= kErrCovariate;
     if (local_err) { atomicOr(A.err, local_err); local_err = 0; }
+    q = __shfl_sync(0xFFFFFFFFu, q_next, 0);
   }
 }
 
@@ -1259,6 +1323,12 @@ cudaError_t launch_tile_range(const uint32_t* rstart, uint32_t n_reads, uint32_t
   tile_range_kernel<<<(n_tiles + 255) / 256, 256, 0, st>>>(rstart, n_reads, n_tiles, maxspan, tile_range, max_tile_reads);
   return cudaGetLastError();
 }
+cudaError_t launch_tile_heavy(const uint2* tile_range, uint32_t n_tiles, uint32_t thr, uint32_t* heavy,
+                              uint32_t* heavy_bits, uint32_t* n_heavy, cudaStream_t st) {
+  if (n_tiles == 0) return cudaSuccess;
+  tile_heavy_kernel<<<(n_tiles + 255) / 256, 256, 0, st>>>(tile_range, n_tiles, thr, heavy, heavy_bits, n_heavy);
+  return cudaGetLastError();
+}
 // An event recorded inside a stream capture becomes an event node only with the external flag.
 static cudaError_t record_event(cudaEvent_t ev, cudaStream_t st) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1294,7 +1364,7 @@ cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, un
   return cudaGetLastError();
 }
 cudaError_t launch_im_column(const Batch& B, int precision, int grid, cudaStream_t st) {
-  const size_t smem = kColumnWarps * 32 * sizeof(DevRead) + kColRareBytes;
+  const size_t smem = kColumnWarps * 32 * sizeof(DevRead) + kColRareBytes + kColWeightBytes;
   if (precision == 0) im_column_kernel<true><<<grid, 32 * kColumnWarps, smem, st>>>(B);
   else im_column_kernel<false><<<grid, 32 * kColumnWarps, smem, st>>>(B);
   return cudaGetLastError();

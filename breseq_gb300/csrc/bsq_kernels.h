@@ -53,6 +53,10 @@ cudaError_t launch_host_copy(const void* src, void* dst, size_t bytes, int sms, 
 // The per-base class bytes of the column pass (quality * 5 + observed base, 255 for N); see
 // base_code_kernel.  code holds n_bases rounded up to 16 bytes; seq and qual have 16 bytes of slack.
 constexpr uint32_t kCodeMaxQ = 50;
+// Lists the tiles whose read range holds more than thr reads into heavy (n_tiles + 16 entries) and sets
+// their bits in heavy_bits (one word per 32 tiles); *n_heavy (zeroed by the caller) counts them.
+cudaError_t launch_tile_heavy(const uint2* tile_range, uint32_t n_tiles, uint32_t thr, uint32_t* heavy,
+                              uint32_t* heavy_bits, uint32_t* n_heavy, cudaStream_t st);
 cudaError_t launch_base_code(const uint8_t* seq, const uint8_t* qual, uint64_t n_bases, uint8_t* code, uint32_t* flags,
                              int sms, cudaStream_t st);
 inline uint32_t refnib_words(uint32_t n_cols) { return (n_cols + 16u) / 16u + 2u; }
