@@ -490,7 +490,7 @@ static int pack_sample(bsq_ctx* ctx, std::unique_ptr<SampleDev>& s, RecordsDev& 
   if (h[0]) return fail(ctx, (h[0] & (kErrOrder | kErrCigar | kErrBounds | kErrX1)) ? BSQ_ERR_INVALID : BSQ_ERR_DATA,
                         "invalid records: " + err_text(h[0]));
   s->maxspan = std::max<uint32_t>(1, h[1]);
-  s->code_ok = h[13] == 0;
+  s->code_ok = h[13] == 0 && R.n_bases_total + 64 < (1ull << 32);   // 32-bit class-byte indices
   s->max_q = h[14];
   uint8_t map[256];
   memset(map, 0, sizeof map);

@@ -599,6 +599,8 @@ constexpr size_t kColRareBytes = 256 * (5 * 4 + 2 * 4 + 2 * 8);
 // that stages it, not by every lane at every column: FP64 division is slow here)
 constexpr size_t kColWeightBytes = kColumnWarps * 32 * sizeof(double);
 
+template <bool B> struct BoolC { static constexpr bool value = B; };
+
 // Staged record of a common-path read for one tile: one aligned block (soft clips allowed), unique,
 // untrimmed, a known read file, in a tile with no failed-fit column.  What depends on the read alone
 // (its likelihood-class base, the addresses of its bases and qualities, its span) is computed once
@@ -788,17 +790,20 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       const bool cov = have && real && d < (f.z & 0xFFFFu);
       code = cov ? (uint32_t)__ldg(codes + (uint32_t)(f.x + c)) : 255u;
     };
-    auto code_use = [&](const uint4& f, uint32_t code, uint32_t slot) {
+    // kRed: the batch holds simple redundant reads (compiled out of the common loop)
+    auto code_use = [&](auto red_c, const uint4& f, uint32_t code, uint32_t slot) {
       const bool counted = code != 255u;                              // covered, and not an N read base
       const bool rev = f.z >> 31;
-      if ((f.z >> 30) & 1u) {
-        // a simple redundant read: redundant coverage and its 1/X1 weight, nothing scored (the
-        // general path's outcome for such a read); the warp takes this branch together
-        if (counted) {
-          uonly = false;
-          rare.redundant(rev, sh_w[slot]);
+      if constexpr (decltype(red_c)::value) {
+        if ((f.z >> 30) & 1u) {
+          // a simple redundant read: redundant coverage and its 1/X1 weight, nothing scored (the
+          // general path's outcome for such a read); the warp takes this branch together
+          if (counted) {
+            uonly = false;
+            rare.redundant(rev, sh_w[slot]);
+          }
+          return;
         }
-        return;
       }
       utop += (counted && !rev) ? 1u : 0u;
       ubot += (counted && rev) ? 1u : 0u;
@@ -856,6 +861,7 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       // of the batch does, so that their 1/X1 sums keep BAM order in one loop.
       const bool red = rel && (mine.flags & kRedundant);
       if (__any_sync(0xFFFFFFFFu, red && !(fast && codes))) fast = fast && !red;
+      const bool red_batch = __any_sync(0xFFFFFFFFu, fast && red);
       // the batch's common-path reads take slots 0..nf-1 and the others the slots after them, each
       // part in BAM order, so the loops below walk slots by index
       unsigned fmask = __ballot_sync(0xFFFFFFFFu, fast);
@@ -890,13 +896,17 @@ __global__ void __launch_bounds__(256, 4) im_column_kernel(const __grid_constant
       __syncwarp();
       // common-path reads in BAM order, kColumnIlp at a time
       if (codes) {
-        for (uint32_t j0 = 0; j0 < nf; j0 += kColumnIlp) {
-          uint32_t code[kColumnIlp];
+        auto code_loop = [&](auto red_c) {
+          for (uint32_t j0 = 0; j0 < nf; j0 += kColumnIlp) {
+            uint32_t code[kColumnIlp];
 #pragma unroll
-          for (int u = 0; u < (int)kColumnIlp; u++) code_load(sh_cr[min(j0 + u, 31u)], j0 + u < nf, code[u]);
+            for (int u = 0; u < (int)kColumnIlp; u++) code_load(sh_cr[min(j0 + u, 31u)], j0 + u < nf, code[u]);
 #pragma unroll
-          for (int u = 0; u < (int)kColumnIlp; u++) code_use(sh_cr[min(j0 + u, 31u)], code[u], min(j0 + u, 31u));
-        }
+            for (int u = 0; u < (int)kColumnIlp; u++) code_use(red_c, sh_cr[min(j0 + u, 31u)], code[u], min(j0 + u, 31u));
+          }
+        };
+        if (red_batch) code_loop(BoolC<true>());
+        else code_loop(BoolC<false>());
       } else {
         for (uint32_t j0 = 0; j0 < nf; j0 += kColumnIlp) {
           FastLd L[kColumnIlp];
