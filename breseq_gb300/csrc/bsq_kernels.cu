@@ -1261,47 +1261,38 @@ cudaError_t launch_host_copy(const void* src, void* dst, size_t bytes, int sms, 
   return cudaGetLastError();
 }
 
-// One byte per read base for the column pass: quality * 5 + observed base (A, C, G, T = 0..3) for a
-// base A/C/G/T, 255 for N, 254 for anything else (an IUPAC code, or the padding nibble after an odd-
-// length read: the pass reports it where it is counted).  flags[0] = 1 when an A/C/G/T base has a
-// quality above kCodeMaxQ (the byte cannot hold it: the pass keeps the packed form for the sample);
-// flags[1] = the largest quality of an A/C/G/T base.  Sixteen bases a thread,
-// read as one 16-byte quality word and one 8-byte word of packed bases (both arrays carry 16 bytes of
-// slack past their ends, so the last word never leaves them).
+// The class bytes of a sample (class_bytes4, four bases in the bytes of a word).  flags[0] = 1 when
+// an A/C/G/T base has a quality above kCodeMaxQ (its byte is not exact: the column pass then keeps
+// the packed form for the sample); flags[1] = the largest quality of an A/C/G/T base.  Sixteen bases a
+// thread, read as one 16-byte quality word and one 8-byte word of packed bases (both arrays carry 16
+// bytes of slack past their ends, so the last word never leaves them).
 __global__ void __launch_bounds__(256) base_code_kernel(const uint8_t* __restrict__ seq, const uint8_t* __restrict__ qual,
                                                         uint64_t n_bases, uint8_t* __restrict__ code, uint32_t* flags) {
-  uint32_t bad = 0, maxq = 0;
+  uint32_t mx = 0;                                       // per-byte maximum of the A/C/G/T qualities
   const uint64_t words = (n_bases + 15) / 16;
   for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < words; w += (uint64_t)gridDim.x * blockDim.x) {
     const uint4 q4 = __ldg(reinterpret_cast<const uint4*>(qual) + w);
     const uint2 s2 = __ldg(reinterpret_cast<const uint2*>(seq) + w);
     const uint32_t qw[4] = {q4.x, q4.y, q4.z, q4.w}, sw[2] = {s2.x, s2.y};
+    const uint64_t live = n_bases - w * 16;              // bases of this word inside the array (may be > 16)
     uint32_t out[4];
 #pragma unroll
-    for (int i = 0; i < 16; i++) {
-      const uint32_t q = (qw[i >> 2] >> (8 * (i & 3))) & 0xFFu;
-      const uint32_t byte = (sw[i >> 3] >> (8 * ((i >> 1) & 3))) & 0xFFu;
-      const uint32_t nib = (i & 1) ? (byte & 15u) : (byte >> 4);        // high nibble first
-      const bool live = w * 16 + i < n_bases;
-      uint32_t v = 255u;
-      if (nib != 15u) {
-        const bool one_hot = (0x116u >> nib) & 1u;                       // 1, 2, 4 or 8
-        if (live && one_hot) {
-          maxq = max(maxq, q);
-          if (q > kCodeMaxQ) bad = 1u;
-        }
-        v = one_hot && q <= kCodeMaxQ ? q * 5u + (31u - __clz(nib)) : 254u;
+    for (int g = 0; g < 4; g++) {
+      uint32_t vq;
+      out[g] = class_bytes4(qw[g], (sw[g >> 1] >> (16 * (g & 1))) & 0xFFFFu, &vq);
+      if (live < 4u * g + 4u) {                          // the array ends inside these four bases
+        const uint32_t lv = live > 4u * g ? (uint32_t)(live - 4u * g) : 0u;
+        vq &= (1u << (8 * lv)) - 1u;
       }
-      if (i % 4 == 0) out[i >> 2] = 0;
-      out[i >> 2] |= v << (8 * (i & 3));
+      mx = bc_max4(mx, vq);
     }
     reinterpret_cast<uint4*>(code)[w] = make_uint4(out[0], out[1], out[2], out[3]);
   }
-  bad = __reduce_or_sync(0xFFFFFFFFu, bad);
+  uint32_t maxq = max(max(mx & 0xFFu, (mx >> 8) & 0xFFu), max((mx >> 16) & 0xFFu, mx >> 24));
   maxq = __reduce_max_sync(0xFFFFFFFFu, maxq);
-  if ((threadIdx.x & 31) == 0) {
-    if (bad) atomicOr(flags, bad);
-    if (maxq) atomicMax(flags + 1, maxq);
+  if ((threadIdx.x & 31) == 0 && maxq) {
+    atomicMax(flags + 1, maxq);
+    if (maxq > kCodeMaxQ) atomicOr(flags, 1u);
   }
 }
 cudaError_t launch_base_code(const uint8_t* seq, const uint8_t* qual, uint64_t n_bases, uint8_t* code, uint32_t* flags,

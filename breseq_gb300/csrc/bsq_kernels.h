@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "bsq_basecode.cuh"
 #include "bsq_common.h"
 
 namespace bsq {
@@ -50,9 +51,8 @@ cudaError_t launch_host_copy(const void* src, void* dst, size_t bytes, int sms, 
 // each column's 4-bit code (A,C,G,T = 1,2,4,8, anything else 15) into refnib.
 // Words of the nibble-packed reference (column c at nibble c + 16), with one spare word after the last
 // column a thread may read past.
-// The per-base class bytes of the column pass (quality * 5 + observed base, 255 for N); see
-// base_code_kernel.  code holds n_bases rounded up to 16 bytes; seq and qual have 16 bytes of slack.
-constexpr uint32_t kCodeMaxQ = 50;
+// The per-base class bytes of the column pass (class_bytes4 in bsq_basecode.cuh).  code holds n_bases
+// rounded up to 16 bytes; seq and qual have 16 bytes of slack.
 // Lists the tiles whose read range holds more than thr reads into heavy (n_tiles + 16 entries) and sets
 // their bits in heavy_bits (one word per 32 tiles); *n_heavy (zeroed by the caller) counts them.
 cudaError_t launch_tile_heavy(const uint2* tile_range, uint32_t n_tiles, uint32_t thr, uint32_t* heavy,

@@ -1,0 +1,55 @@
+// The column pass's class-byte core (breseq_gb300/csrc/bsq_basecode.cuh) compiled for the host, checked
+// against the per-base rule on every (nibble, quality) pair in every byte position and on random words.
+#include <cstdio>
+#include <cstdlib>
+#include "../../breseq_gb300/csrc/bsq_basecode.cuh"
+
+using namespace bsq;
+
+// the per-base rule: quality * 5 + base for A/C/G/T (1, 2, 4, 8), 255 for N (15), 254 otherwise
+static void rule(uint32_t nib, uint32_t q, uint32_t* code, uint32_t* vq) {
+  const bool one_hot = nib == 1 || nib == 2 || nib == 4 || nib == 8;
+  *vq = one_hot ? q : 0;
+  if (nib == 15) *code = 255;
+  else if (!one_hot) *code = 254;
+  else *code = q * 5 + (nib == 1 ? 0 : nib == 2 ? 1 : nib == 4 ? 2 : 3);
+}
+
+static int check(uint32_t q4, uint32_t h) {
+  uint32_t vq;
+  const uint32_t code = class_bytes4(q4, h, &vq);
+  for (int k = 0; k < 4; k++) {
+    const uint32_t byte = (h >> (8 * (k >> 1))) & 0xFF;
+    const uint32_t nib = (k & 1) ? (byte & 15) : (byte >> 4);
+    const uint32_t q = (q4 >> (8 * k)) & 0xFF;
+    uint32_t c, v;
+    rule(nib, q, &c, &v);
+    if (((vq >> (8 * k)) & 0xFF) != v) return 1;
+    if (v && q > kCodeMaxQ) continue;        // not exact above kCodeMaxQ (the load flags the sample)
+    if (((code >> (8 * k)) & 0xFF) != c) return 2;
+  }
+  return 0;
+}
+
+extern "C" int basecode_selftest(unsigned seed) {
+  // every (nibble, quality) pair in every position, the other three bases varied
+  for (int pos = 0; pos < 4; pos++)
+    for (uint32_t nib = 0; nib < 16; nib++)
+      for (uint32_t q = 0; q < 256; q++)
+        for (uint32_t other = 0; other < 16; other += 5) {
+          uint32_t h = 0, q4 = 0;
+          for (int k = 0; k < 4; k++) {
+            const uint32_t nk = k == pos ? nib : (other + 3 * k) & 15, qk = k == pos ? q : (q * 7 + 13 * k + other) & 0xFF;
+            h |= nk << (8 * (k >> 1) + ((k & 1) ? 0 : 4));
+            q4 |= qk << (8 * k);
+          }
+          if (int e = check(q4, h)) return e;
+        }
+  srand(seed);
+  for (int i = 0; i < 2000000; i++) {
+    const uint32_t q4 = ((uint32_t)rand() << 16) ^ (uint32_t)rand();
+    const uint32_t h = (uint32_t)rand() & 0xFFFF;
+    if (int e = check(q4, h)) return 10 + e;
+  }
+  return 0;
+}
