@@ -729,7 +729,7 @@ static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_p
   if (pe != cudaSuccess) return fail(ctx, BSQ_ERR_CUDA, "error_count pass (" + where + "): " + cudaGetErrorString(pe));
   CK(cudaStreamSynchronize(st));
   const float ms = elapsed(ctx->ev0, ctx->ev1), mms = elapsed(ctx->evm0, ctx->evm1);
-  ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 4;
+  ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 5;     // staging copy, read pass, 3 coverage kernels
   ctx->last_h2d += std::max<size_t>(16, n_chunks * sizeof(uint4));
   ctx->last_d2h += res_bytes;
   int rc = BSQ_OK;
@@ -997,7 +997,7 @@ static int im_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_im_p
   }
   const uint32_t n_cand = ctl_host[kCtlCand] + ctl_host[kCtlCand2], nk = ctl_host[kCtlKept], n_ra = ctl_host[kCtlRa];
   const uint32_t cerr = ctl_host[kCtlCandErr];
-  ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 13;
+  ctx->last_ms += ms; ctx->main_ms += mms; ctx->launches += 14;    // staging copy + 13 (launch list of the step)
   ctx->last_h2d += arena_bytes;
   ctx->last_d2h += (uint64_t)kCtlWords * 4 + (uint64_t)n_ra * (sizeof(RaDev) + 2 * Qh * 4) +
                    (uint64_t)nk * (4 + sizeof(ColCov) + sizeof(ColCall));
