@@ -28,7 +28,18 @@ def population_small():
     return synth.simulate(c)
 
 
-ALL = {"clonal_small": clonal_small, "ecoli_small": ecoli_small, "population_small": population_small}
+@functools.lru_cache(maxsize=None)
+def ecoli_high_quality():
+    """ecoli_small with every quality raised by 20 (up to 61): A/C/G/T qualities above 50 do not fit the
+    column pass's one-byte classes, so the load keeps the packed bases and qualities for the pass."""
+    import numpy as np
+    s = ecoli_small()
+    q = np.minimum(np.asarray(s.qual, dtype=np.uint16) + 20, 93).astype(np.uint8)
+    return dataclasses.replace(s, qual=q, n_quality=int(q.max()) + 1)
+
+
+ALL = {"clonal_small": clonal_small, "ecoli_small": ecoli_small, "population_small": population_small,
+       "ecoli_high_quality": ecoli_high_quality}
 
 
 @functools.lru_cache(maxsize=None)
