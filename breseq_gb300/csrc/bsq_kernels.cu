@@ -343,16 +343,36 @@ __device__ __forceinline__ void ec_thread_read(const DevSample& S, const EcArgs&
     const int a2 = min(max(lo2 - ilo, 0), 16), b2 = min(max(hi2 - ilo, 0), 16);
     const uint32_t m_in = (0xFFFFu >> (16 - b)) & ~((1u << a) - 1u);
     const uint32_t m_2 = (0xFFFFu >> (16 - b2)) & ~((1u << a2) - 1u);
+    // bases equal to the reference and not N, eight to a 32-bit word: the packed bases nibble-swapped
+    // into the reference's order (base k at nibble k), XOR, then a nibble that is zero and a read
+    // nibble that is not 15, each as bit 4k, compressed to bit k
+    uint32_t same = 0;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const uint32_t s = ((ss[h] >> 4) & 0x0F0F0F0Fu) | ((ss[h] << 4) & 0xF0F0F0F0u);
+      const uint32_t x = s ^ rr[h];
+      uint32_t z = x | (x >> 1);
+      z |= z >> 2;                                      // bit 4k: nibble k differs from the reference
+      uint32_t n = s & (s >> 1);
+      n &= n >> 2;                                      // bit 4k: read nibble k is 15 (N)
+      uint32_t m = ~(z | n) & 0x11111111u;
+      m = (m | (m >> 3)) & 0x03030303u;
+      m = (m | (m >> 6)) & 0x000F000Fu;
+      m = (m | (m >> 12)) & 0xFFu;
+      same |= m << (8 * h);
+    }
+    const uint32_t m_comb = same & m_2;
 #pragma unroll
     for (int k = 0; k < 16; k++) {
       const uint32_t q = (qq[k >> 2] >> (8 * (k & 3))) & 0xFFu;
-      // BAM packing: the even base of a byte in its high nibble
-      const uint32_t ob = (ss[k >> 3] >> (8 * ((k & 7) >> 1) + ((k & 1) ? 0 : 4))) & 15u;
-      const uint32_t rb = (rr[k >> 3] >> (4 * (k & 7))) & 15u;   // A,C,G,T one-hot, else 15
-      const bool in2 = (m_2 >> k) & 1u;
-      if (ob == rb && ob != 15u && in2 && q < Q) {
+      if (((m_comb >> k) & 1u) && q < Q) {
+        const uint32_t rb = (rr[k >> 3] >> (4 * (k & 7))) & 15u;   // A,C,G,T one-hot here
         atomicAdd(comb + q * qR + (nib_code(rb) ^ flip) * R + rs, 1u);
       } else if ((m_in >> k) & 1u) {
+        // BAM packing: the even base of a byte in its high nibble
+        const uint32_t ob = (ss[k >> 3] >> (8 * ((k & 7) >> 1) + ((k & 1) ? 0 : 4))) & 15u;
+        const uint32_t rb = (rr[k >> 3] >> (4 * (k & 7))) & 15u;   // A,C,G,T one-hot, else 15
+        const bool in2 = (m_2 >> k) & 1u;
         const bool valid = ob != 15u && rb != 15u;     // neither the read base nor the reference is N
         const bool base_ok = (0x116u >> ob) & 1u;      // one-hot: A, C, G or T
         const bool q_ok = q < Q;
