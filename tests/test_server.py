@@ -50,18 +50,20 @@ def _check(res, ref):
 
 @pytest.mark.gpu
 def test_mixed_jobs_match_alone(alone):
-    """Jobs of three samples, submitted from two threads with gaps, overlap on the GPU in rounds of
-    several jobs; each result equals the sample's single-call result."""
+    """Jobs of the parity samples, submitted from two threads in bursts of three with gaps between the
+    bursts, overlap on the GPU in rounds of several jobs; each result equals the sample's single-call
+    result."""
     from breseq_gb300.api import ImSettings, Server
     names = list(samples.ALL) * 4
     ids = {}
     with Server(0, hbm_budget=8e9) as srv:
         def producer(k):
             rng = np.random.default_rng(k)
-            for i in range(k, len(names), 2):
+            for j, i in enumerate(range(k, len(names), 2)):
                 n = names[i]
                 ids[i] = srv.submit(alone[n][0], ImSettings(polymorphism_prediction=n in POLY))
-                time.sleep(float(rng.uniform(0, 0.02)))
+                if j % 3 == 2:
+                    time.sleep(float(rng.uniform(0, 0.02)))
         th = [threading.Thread(target=producer, args=(k,)) for k in range(2)]
         for t in th:
             t.start()
