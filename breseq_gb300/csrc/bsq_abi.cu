@@ -124,7 +124,7 @@ struct bsq_ctx {
   DevMem d_chunks, ec_arena, im_arena, ctl;
   PinnedBuf pin_in, pin_out;
   // page-locked landing areas of device-to-host reads that run beside other threads' work: a read into
-  // pageable memory is staged by the driver, and such reads wait for one another across streams (an
+  // pageable memory is staged by the CUDA driver, and such reads wait for one another across streams (an
   // upload's check would hold up a pass's results until the upload ends)
   PinnedBuf pin_res;                    // pass 2's RA items, quality histograms and kept columns
   static constexpr uint32_t kStatSlots = 64;
