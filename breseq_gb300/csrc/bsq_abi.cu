@@ -60,8 +60,8 @@ struct SampleDev {
   // pair annotations for the discordant / missing-pair scans: raw flags, XP codes, TLEN, names
   DevMem pflag, pxp, pisize, pqoff, pqname, pmtid, pmpos;
   bool has_pairs = false, has_mates = false;
-  // per-base class bytes (base_code_kernel); usable by the column pass when no A/C/G/T base has a
-  // quality above kCodeMaxQ, and for a call whose quality range is above max_q
+  // per-base class bytes (base_code_kernel); usable by the passes when no base but N has a quality
+  // above kCodeMaxQ (code_ok), and for a call whose quality range is above max_q (the largest such)
   DevMem code;
   bool code_ok = false;
   uint32_t max_q = 0;
@@ -649,7 +649,7 @@ static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_p
   std::vector<Lay> lay(n);
   std::vector<uint32_t> cblk(n + 1, 0);
   size_t off = 0;
-  uint32_t max_bins = 0;
+  uint32_t max_bins = 0, max_code_r = 0;
   for (uint32_t j = 0; j < n; j++) {
     const SampleDev* s = smp[j];
     const size_t nbins = (size_t)P[j].n_read_files * 25 * P[j].n_quality;
@@ -710,9 +710,16 @@ static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_p
     E.qs_flag = A0 + lay[j].qs;
     E.blk_u = reinterpret_cast<uint32_t*>(A0 + lay[j].blk_u);
     E.blk_r = reinterpret_cast<uint32_t*>(A0 + lay[j].blk_r);
+    // class bytes: exact, every quality of a base that is not N below Q, and room for the counters
+    E.code = nullptr;
+    const uint32_t R = P[j].n_read_files, Q = P[j].n_quality;
+    if (s->code_ok && s->max_q < Q && R <= kEcCodeMaxR && ((size_t)R * 29 * Q + 512u * R) * 4 <= kEcMaxHistBytes) {
+      E.code = s->code.as<uint8_t>();
+      max_code_r = std::max(max_code_r, R);
+    }
   }
   for (uint32_t j = 0; j <= n; j++) B.cblk_begin[j] = cblk[j];
-  CK(prepare_ec(max_bins));
+  CK(prepare_ec(max_bins, max_code_r));
   const int grid = ec_grid((uint32_t)n_chunks, ctx->sms, tn.ec_blocks_per_sm);
   std::string where, step;
   const cudaError_t pe = run_pass(ctx, ctx->exec_ec, [&]() -> cudaError_t {
@@ -721,8 +728,8 @@ static int ec_group(bsq_ctx* ctx, uint32_t n, const int32_t* ids, const bsq_ec_p
     if ((e = launch_host_copy(ctx->pin_in.p, ctx->d_chunks.p, std::max<size_t>(16, n_chunks * sizeof(uint4)), ctx->sms,
                               st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(A0, 0, arena_bytes, st)) != cudaSuccess) return e;
-    if ((e = launch_ec(B, ctx->d_chunks.as<uint4>(), (uint32_t)n_chunks, ctx->next.as<unsigned int>(), max_bins, grid, st,
-                       ctx->evm0, ctx->evm1)) != cudaSuccess) return e;
+    if ((e = launch_ec(B, ctx->d_chunks.as<uint4>(), (uint32_t)n_chunks, ctx->next.as<unsigned int>(), max_bins,
+                       max_code_r, grid, st, ctx->evm0, ctx->evm1)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(ctx->pin_out.p, A0, res_bytes, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     return record(ctx->ev1, st);
   }, where);

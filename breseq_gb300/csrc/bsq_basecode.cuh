@@ -43,7 +43,7 @@ __host__ __device__ inline uint32_t bc_max4(uint32_t a, uint32_t b) {
 
 // The class bytes of four bases.  q4: their quality bytes (byte k = base k); h: their two packed
 // sequence bytes in the low 16 bits (the low byte first, its high nibble the earlier base).  *valid_q
-// gets the quality bytes of the A/C/G/T bases and 0 for the others.
+// gets the quality bytes of the bases that are not N (A/C/G/T and other codes) and 0 for N.
 __host__ __device__ inline uint32_t class_bytes4(uint32_t q4, uint32_t h, uint32_t* valid_q) {
   // the four nibbles into the four bytes: b0 >> 4, b0 & 15, b1 >> 4, b1 & 15
   const uint32_t t = bc_perm(h, 0u, 0x1100u);
@@ -61,7 +61,8 @@ __host__ __device__ inline uint32_t class_bytes4(uint32_t q4, uint32_t h, uint32
   const uint32_t ce = (q4 & 0x00FF00FFu) * 5u + (r & 0x00FF00FFu);
   const uint32_t co = ((q4 >> 8) & 0x00FF00FFu) * 5u + ((r >> 8) & 0x00FF00FFu);
   const uint32_t code = ((ce & 0x00FF00FFu) | ((co & 0x00FF00FFu) << 8));
-  *valid_q = q4 & ~bad;
+  const uint32_t n8 = (((r >> 7) & r) & 0x01010101u) * 0xFFu;  // 255: N
+  *valid_q = q4 & ~n8;
   return (code & ~bad) | (r & bad);
 }
 

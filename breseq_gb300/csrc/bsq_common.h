@@ -92,7 +92,11 @@ struct EcArgs {
   uint8_t* qs_flag;                 // [2][n_cols]: a read starts at this column (forward, reverse)
   uint32_t* blk_u;                  // per 1024-column block: sums of diff_u / diff_r
   uint32_t* blk_r;
+  // the sample's class bytes (quality * 5 + base) when they are exact, every quality of a base that is
+  // not N is below Q and R <= kEcCodeMaxR; null otherwise (the pass reads the qualities)
+  const uint8_t* code;
 };
+constexpr uint32_t kEcCodeMaxR = 16;
 
 // ----------------------------------------------------------------------------- pass 2
 // Likelihood class of a read base: (mapq_idx, read file, strand, quality, observed base).

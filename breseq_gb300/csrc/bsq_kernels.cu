@@ -311,6 +311,10 @@ __device__ __forceinline__ uint32_t nib_code(uint32_t x) {   // one-hot nibble A
   asm("bfind.u32 %0, %1;" : "=r"(d) : "r"(x));
   return d;
 }
+// CODES: the words hold class bytes (quality * 5 + base) instead of qualities, and a base equal to the
+// reference counts into comb[(strand * 256 + class byte) * R + rs] (one multiply-add for the index;
+// the chunk's flush turns it into the two bins); the general test reads its base's quality byte.
+template <bool CODES>
 __device__ __forceinline__ void ec_thread_read(const DevSample& S, const EcArgs& A, uint32_t* hist, uint32_t* comb,
                                                const DevRead& rd, uint32_t span, uint32_t& err) {
   const bool rev = rd.flags & kRev;
@@ -329,8 +333,9 @@ __device__ __forceinline__ void ec_thread_read(const DevSample& S, const EcArgs&
   const uint32_t qR = 4u * R;
   bool bad_base = false, bad_q = false;
   int ilo = -off0;                                      // base index of slot 0 of the current word
+  const uint32_t crow = (rev ? 256u : 0u) * R + rs;     // CODES: the strand's counter rows, read file rs
   for (uint64_t w = w0; w < w1; w++, ilo += 16, rw++) {
-    const uint4 qv = __ldg(reinterpret_cast<const uint4*>(S.qual) + w);
+    const uint4 qv = __ldg(reinterpret_cast<const uint4*>(CODES ? A.code : S.qual) + w);
     const uint2 sv = __ldg(reinterpret_cast<const uint2*>(S.seq) + w);
     const unsigned long long rhi = __ldg(rw + 1);
     const unsigned long long r64 = dsh ? (rlo >> dsh) | (rhi << (64u - dsh)) : rlo;
@@ -364,11 +369,16 @@ __device__ __forceinline__ void ec_thread_read(const DevSample& S, const EcArgs&
     const uint32_t m_comb = same & m_2;
 #pragma unroll
     for (int k = 0; k < 16; k++) {
-      const uint32_t q = (qq[k >> 2] >> (8 * (k & 3))) & 0xFFu;
-      if (((m_comb >> k) & 1u) && q < Q) {
-        const uint32_t rb = (rr[k >> 3] >> (4 * (k & 7))) & 15u;   // A,C,G,T one-hot here
-        atomicAdd(comb + q * qR + (nib_code(rb) ^ flip) * R + rs, 1u);
+      const uint32_t qb = (qq[k >> 2] >> (8 * (k & 3))) & 0xFFu;     // quality, or class byte (CODES)
+      if (CODES ? (bool)((m_comb >> k) & 1u) : (((m_comb >> k) & 1u) && qb < Q)) {
+        if (CODES) {
+          atomicAdd(comb + qb * R + crow, 1u);
+        } else {
+          const uint32_t rb = (rr[k >> 3] >> (4 * (k & 7))) & 15u;   // A,C,G,T one-hot here
+          atomicAdd(comb + qb * qR + (nib_code(rb) ^ flip) * R + rs, 1u);
+        }
       } else if ((m_in >> k) & 1u) {
+        const uint32_t q = CODES ? (uint32_t)__ldg(S.qual + w * 16 + k) : qb;
         // BAM packing: the even base of a byte in its high nibble
         const uint32_t ob = (ss[k >> 3] >> (8 * ((k & 7) >> 1) + ((k & 1) ? 0 : 4))) & 15u;
         const uint32_t rb = (rr[k >> 3] >> (4 * (k & 7))) & 15u;   // A,C,G,T one-hot, else 15
@@ -450,7 +460,7 @@ __device__ __forceinline__ void ec_complex_read(const DevSample& S, const EcArgs
 // aligned block are taken one per thread; the others are queued and walked one per warp afterwards
 // (one per thread when the queue is full).
 constexpr uint32_t kEcQueue = 1024;
-__global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Batch B, const uint4* chunks, uint32_t n_chunks, unsigned int* next) {
+__global__ void __launch_bounds__(256, 4) ec_read_kernel(const __grid_constant__ Batch B, const uint4* chunks, uint32_t n_chunks, unsigned int* next) {
   extern __shared__ uint32_t sh_hist[];
   __shared__ uint32_t sh_chunk, sh_nq;
   __shared__ uint32_t sh_queue[kEcQueue];
@@ -463,9 +473,10 @@ __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Ba
   const uint4 ch = chunks[ci];                 // x = job, y = first read, z = end read
   const DevSample& S = B.jobs[ch.x].S;
   const EcArgs& A = B.jobs[ch.x].E;
-  const uint32_t nbins = A.R * 25u * A.Q, ncomb = A.R * 4u * A.Q;
+  const uint32_t nbins = A.R * 25u * A.Q, ncomb = A.R * 4u * A.Q, nccomb = A.code ? 512u * A.R : 0u;
   uint32_t* sh_comb = sh_hist + nbins;
-  for (uint32_t i = threadIdx.x; i < nbins + ncomb; i += blockDim.x) sh_hist[i] = 0;
+  uint32_t* sh_ccomb = sh_comb + ncomb;        // class-byte counters (CODES form)
+  for (uint32_t i = threadIdx.x; i < nbins + ncomb + nccomb; i += blockDim.x) sh_hist[i] = 0;
   __syncthreads();
   uint32_t err = 0;
   for (uint32_t r = ch.y + threadIdx.x; r < ch.z; r += blockDim.x) {
@@ -485,7 +496,8 @@ __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Ba
     if (A.preprocess && !red && rd.clip == 0 && read_start_counts(A, rd, 1u, span))
       A.qs_flag[(size_t)(rd.flags & kRev) * S.n_cols + rd.start] = 1;
     if (red || !A.do_errors) continue;
-    ec_thread_read(S, A, sh_hist, sh_comb, rd, span, err);
+    if (A.code) ec_thread_read<true>(S, A, sh_hist, sh_ccomb, rd, span, err);
+    else ec_thread_read<false>(S, A, sh_hist, sh_comb, rd, span, err);
   }
   __syncthreads();
   const uint32_t nq = min(sh_nq, kEcQueue);
@@ -494,6 +506,17 @@ __global__ void __launch_bounds__(256) ec_read_kernel(const __grid_constant__ Ba
     ec_complex_read(S, A, sh_hist, S.reads[r], r, lane, 32, err);
   }
   __syncthreads();
+  // class-byte counters (strand, quality * 5 + base, rs) of bases equal to the reference: both bins,
+  // the base complemented on the reverse strand
+  for (uint32_t i = threadIdx.x; i < nccomb; i += blockDim.x) {
+    const uint32_t v = sh_ccomb[i];
+    if (v) {
+      const uint32_t rs = i % A.R, row = i / A.R, code = row & 255u, q = code / 5u;
+      const uint32_t b = (code - 5u * q) ^ ((row >> 8) ? 3u : 0u);
+      atomicAdd(sh_hist + (q * 25u + b * 6u) * A.R + rs, v);
+      atomicAdd(sh_hist + (q * 25u + 24u) * A.R + rs, v);
+    }
+  }
   // combined counts of (rs, b, b, q) + (rs, '.', '.', q) into both bins
   for (uint32_t i = threadIdx.x; i < ncomb; i += blockDim.x) {
     const uint32_t v = sh_comb[i];
@@ -1281,9 +1304,9 @@ cudaError_t launch_host_copy(const void* src, void* dst, size_t bytes, int sms, 
   return cudaGetLastError();
 }
 
-// The class bytes of a sample (class_bytes4, four bases in the bytes of a word).  flags[0] = 1 when
-// an A/C/G/T base has a quality above kCodeMaxQ (its byte is not exact: the column pass then keeps
-// the packed form for the sample); flags[1] = the largest quality of an A/C/G/T base.  Sixteen bases a
+// The class bytes of a sample (class_bytes4, four bases in the bytes of a word).  flags[1] = the
+// largest quality of a base that is not N; flags[0] = 1 when it is above kCodeMaxQ (an A/C/G/T byte
+// may then not be exact: the passes keep the packed form for the sample).  Sixteen bases a
 // thread, read as one 16-byte quality word and one 8-byte word of packed bases (both arrays carry 16
 // bytes of slack past their ends, so the last word never leaves them).
 __global__ void __launch_bounds__(256) base_code_kernel(const uint8_t* __restrict__ seq, const uint8_t* __restrict__ qual,
@@ -1364,16 +1387,19 @@ int ec_grid(uint32_t n_chunks, int sms, uint32_t blocks_per_sm) {
 int column_grid(uint32_t total_tiles, int sms, uint32_t blocks_per_sm) {
   return grid_for(total_tiles, kColumnWarps, sms, (int)std::max<uint32_t>(1, blocks_per_sm));
 }
-// Shared memory of the pass-1 kernel: the R x 25 x Q histogram and the R x 4 x Q combined counts.
-static size_t ec_smem(uint32_t max_bins) { return (size_t)(max_bins + max_bins / 25 * 4) * sizeof(uint32_t); }
-cudaError_t prepare_ec(uint32_t max_bins) {
-  const size_t smem = ec_smem(max_bins);
+// Shared memory of the pass-1 kernel: the R x 25 x Q histogram, the R x 4 x Q combined counts and,
+// for jobs with class bytes, 512 x R class-byte counters (max_code_r: the largest such R, else 0).
+static size_t ec_smem(uint32_t max_bins, uint32_t max_code_r) {
+  return (size_t)(max_bins + max_bins / 25 * 4 + 512u * max_code_r) * sizeof(uint32_t);
+}
+cudaError_t prepare_ec(uint32_t max_bins, uint32_t max_code_r) {
+  const size_t smem = ec_smem(max_bins, max_code_r);
   if (smem <= 48 * 1024) return cudaSuccess;
   return cudaFuncSetAttribute(ec_read_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, unsigned int* next, uint32_t max_bins,
-                      int grid, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1) {
-  const size_t smem = ec_smem(max_bins);
+                      uint32_t max_code_r, int grid, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1) {
+  const size_t smem = ec_smem(max_bins, max_code_r);
   cudaError_t e = cudaMemsetAsync(next, 0, sizeof(unsigned int), st);
   if (e != cudaSuccess) return e;
   if (main0 && (e = record_event(main0, st)) != cudaSuccess) return e;

@@ -73,9 +73,9 @@ constexpr size_t kEcMaxHistBytes = 200 * 1024;
 int ec_grid(uint32_t n_chunks, int sms, uint32_t blocks_per_sm);
 int column_grid(uint32_t total_tiles, int sms, uint32_t blocks_per_sm);
 // Attribute setup that must precede a stream capture of launch_ec.
-cudaError_t prepare_ec(uint32_t max_bins);
+cudaError_t prepare_ec(uint32_t max_bins, uint32_t max_code_r);
 cudaError_t launch_ec(const Batch& B, const uint4* chunks, uint32_t n_chunks, unsigned int* next, uint32_t max_bins,
-                      int grid, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1);
+                      uint32_t max_code_r, int grid, cudaStream_t st, cudaEvent_t main0, cudaEvent_t main1);
 cudaError_t launch_im_column(const Batch& B, int precision, int grid, cudaStream_t st);
 // Candidate columns in queue order (likely RA items first); total[0], total[1] = the two part sizes.
 cudaError_t launch_compact(const ColCall* call, uint32_t n, uint32_t* block_counts, uint32_t* total, uint32_t* out,

@@ -9,7 +9,7 @@ using namespace bsq;
 // the per-base rule: quality * 5 + base for A/C/G/T (1, 2, 4, 8), 255 for N (15), 254 otherwise
 static void rule(uint32_t nib, uint32_t q, uint32_t* code, uint32_t* vq) {
   const bool one_hot = nib == 1 || nib == 2 || nib == 4 || nib == 8;
-  *vq = one_hot ? q : 0;
+  *vq = nib != 15 ? q : 0;
   if (nib == 15) *code = 255;
   else if (!one_hot) *code = 254;
   else *code = q * 5 + (nib == 1 ? 0 : nib == 2 ? 1 : nib == 4 ? 2 : 3);
@@ -25,7 +25,8 @@ static int check(uint32_t q4, uint32_t h) {
     uint32_t c, v;
     rule(nib, q, &c, &v);
     if (((vq >> (8 * k)) & 0xFF) != v) return 1;
-    if (v && q > kCodeMaxQ) continue;        // not exact above kCodeMaxQ (the load flags the sample)
+    const bool acgt = nib == 1 || nib == 2 || nib == 4 || nib == 8;
+    if (acgt && q > kCodeMaxQ) continue;     // A/C/G/T above kCodeMaxQ: not exact (the load flags the sample)
     if (((code >> (8 * k)) & 0xFF) != c) return 2;
   }
   return 0;
