@@ -313,7 +313,8 @@ __device__ __forceinline__ uint32_t nib_code(uint32_t x) {   // one-hot nibble A
 }
 // CODES: the words hold class bytes (quality * 5 + base) instead of qualities, and a base equal to the
 // reference counts into comb[(strand * 256 + class byte) * R + rs] (one multiply-add for the index;
-// the chunk's flush turns it into the two bins); the general test reads its base's quality byte.
+// the chunk's flush turns it into the two bins); the general test takes an A/C/G/T base's quality
+// from its class byte and reads the quality byte only for other codes.
 template <bool CODES>
 __device__ __forceinline__ void ec_thread_read(const DevSample& S, const EcArgs& A, uint32_t* hist, uint32_t* comb,
                                                const DevRead& rd, uint32_t span, uint32_t& err) {
@@ -378,7 +379,9 @@ __device__ __forceinline__ void ec_thread_read(const DevSample& S, const EcArgs&
           atomicAdd(comb + qb * qR + (nib_code(rb) ^ flip) * R + rs, 1u);
         }
       } else if ((m_in >> k) & 1u) {
-        const uint32_t q = CODES ? (uint32_t)__ldg(S.qual + w * 16 + k) : qb;
+        // CODES: an A/C/G/T base's quality is its class byte / 5; an N's is never used; only another
+        // code (254) reads its quality byte
+        const uint32_t q = !CODES ? qb : qb < 254u ? qb / 5u : qb == 254u ? (uint32_t)__ldg(S.qual + w * 16 + k) : 0u;
         // BAM packing: the even base of a byte in its high nibble
         const uint32_t ob = (ss[k >> 3] >> (8 * ((k & 7) >> 1) + ((k & 1) ? 0 : 4))) & 15u;
         const uint32_t rb = (rr[k >> 3] >> (4 * (k & 7))) & 15u;   // A,C,G,T one-hot, else 15

@@ -38,8 +38,19 @@ def ecoli_high_quality():
     return dataclasses.replace(s, qual=q, n_quality=int(q.max()) + 1)
 
 
+@functools.lru_cache(maxsize=None)
+def ecoli_q50():
+    """ecoli_small with every quality raised by 9 (up to exactly 50, the largest the one-byte classes
+    hold): the passes use class bytes up to 253."""
+    import numpy as np
+    s = ecoli_small()
+    q = (np.asarray(s.qual, dtype=np.uint16) + 9).astype(np.uint8)
+    assert int(q.max()) == 50
+    return dataclasses.replace(s, qual=q, n_quality=51)
+
+
 ALL = {"clonal_small": clonal_small, "ecoli_small": ecoli_small, "population_small": population_small,
-       "ecoli_high_quality": ecoli_high_quality}
+       "ecoli_high_quality": ecoli_high_quality, "ecoli_q50": ecoli_q50}
 
 
 @functools.lru_cache(maxsize=None)
