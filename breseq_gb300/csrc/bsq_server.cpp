@@ -77,6 +77,7 @@ struct bsq_server {
   uint64_t jobs_done = 0, rounds = 0;
   uint32_t max_round_jobs = 0, resident = 0, max_resident = 0;
   uint32_t pending = 0;             // submitted and not finished
+  uint32_t loading = 0;             // admitted, upload in progress
   double gpu_busy_ms = 0;
   bool tune_pending = false;
   bsq_tuning tune{};                      // applied by the GPU thread before its next round
@@ -84,6 +85,8 @@ struct bsq_server {
   bool stop = false;
   std::string err;
   static constexpr int kLoaders = 8;   // uploads in flight at once (each on its own load stream)
+  static constexpr size_t kMinRound = 4;   // a round waits (at most kJoinMs) for this many ready jobs
+  static constexpr int kJoinMs = 2;        // while uploads are in progress
   std::vector<std::thread> admitters;
   std::thread gpu;
 
@@ -116,14 +119,17 @@ struct bsq_server {
       if (in_use > peak_in_use) peak_in_use = in_use;
       j->state = BSQ_JOB_LOADING;
       j->t_admit = Clock::now();
+      loading++;
       lk.unlock();
       j->read_bases = aligned_read_bases(j->desc.reads);
       int32_t sid = -1;
       const int rc = bsq_load_sample(ctx, j->desc.ref, j->desc.reads, &sid);
       const std::string e = rc == BSQ_OK ? std::string() : std::string(bsq_last_error(ctx));
       lk.lock();
+      loading--;
       if (rc != BSQ_OK) {
         finish(j, rc, "load: " + e);
+        cv_ready.notify_all();
         continue;
       }
       j->sample = sid;
@@ -210,6 +216,11 @@ struct bsq_server {
     for (;;) {
       cv_ready.wait(lk, [&] { return !ready.empty() || (stop && pending == 0); });
       if (ready.empty()) return;
+      // A round of one or two jobs while others are still uploading pays a round's fixed costs (and
+      // the wait of passes beside uploads) for little work: give the uploads up to kJoinMs to join it.
+      if (ready.size() < kMinRound && loading > 0)
+        cv_ready.wait_for(lk, std::chrono::milliseconds(kJoinMs),
+                          [&] { return ready.size() >= kMinRound || loading == 0 || stop; });
       if (tune_pending) {
         // passes run without graph capture here: captures were measured to wait behind the
         // admission threads' uploads (tens of ms), and rounds are large enough not to need graphs
