@@ -66,7 +66,7 @@ WORKLOAD = "ecoli_clonal_4.79Mb_pe150_2x100x"
 # class byte per base (quality * 5 + base, built when the sample is loaded) where the formula's
 # algorithmic bytes count the 1.5 bytes of packed base and quality, so its traffic sits below them.
 IM_COLUMN_DRAM_PER_BASE = (323.486464e6 + 51.284736e6) / 0.2441e9
-EC_READ_DRAM_PER_BASE = (418.198016e6 + 9.134592e6) / 0.2441e9
+EC_READ_DRAM_PER_BASE = (416.378368e6 + 8.300544e6) / 0.2441e9
 # the plain FP64 form: same kernels, FP64 everywhere, one sample per call, launched without graphs
 PLAIN_TUNING = dict(ec_read_chunk=1024, ec_blocks_per_sm=8, col_blocks_per_sm=8, cand_warps_per_sm=16,
                     bound_warps_per_sm=4, use_graphs=0)
