@@ -66,4 +66,21 @@ __host__ __device__ inline uint32_t class_bytes4(uint32_t q4, uint32_t h, uint32
   return (code & ~bad) | (r & bad);
 }
 
+// Pass 1's bases equal to the reference, eight at a time.  packed: four bytes of packed bases (eight
+// bases, the earlier base of a byte in its high nibble); ref: the reference's eight 4-bit codes for the
+// same columns, base k at nibble k (A, C, G, T one-hot, anything else 15).  Bit k of the result is set
+// when base k equals its reference code and is not N (15).
+__host__ __device__ inline uint32_t same_as_reference8(uint32_t packed, uint32_t ref) {
+  const uint32_t s = ((packed >> 4) & 0x0F0F0F0Fu) | ((packed << 4) & 0xF0F0F0F0u);   // base k at nibble k
+  const uint32_t x = s ^ ref;
+  uint32_t z = x | (x >> 1);
+  z |= z >> 2;                                      // bit 4k: nibble k differs from the reference
+  uint32_t n = s & (s >> 1);
+  n &= n >> 2;                                      // bit 4k: read nibble k is 15 (N)
+  uint32_t m = ~(z | n) & 0x11111111u;
+  m = (m | (m >> 3)) & 0x03030303u;                 // bit 4k -> bit k
+  m = (m | (m >> 6)) & 0x000F000Fu;
+  return (m | (m >> 12)) & 0xFFu;
+}
+
 }  // namespace bsq

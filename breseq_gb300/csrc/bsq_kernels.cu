@@ -349,24 +349,8 @@ __device__ __forceinline__ void ec_thread_read(const DevSample& S, const EcArgs&
     const int a2 = min(max(lo2 - ilo, 0), 16), b2 = min(max(hi2 - ilo, 0), 16);
     const uint32_t m_in = (0xFFFFu >> (16 - b)) & ~((1u << a) - 1u);
     const uint32_t m_2 = (0xFFFFu >> (16 - b2)) & ~((1u << a2) - 1u);
-    // bases equal to the reference and not N, eight to a 32-bit word: the packed bases nibble-swapped
-    // into the reference's order (base k at nibble k), XOR, then a nibble that is zero and a read
-    // nibble that is not 15, each as bit 4k, compressed to bit k
-    uint32_t same = 0;
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const uint32_t s = ((ss[h] >> 4) & 0x0F0F0F0Fu) | ((ss[h] << 4) & 0xF0F0F0F0u);
-      const uint32_t x = s ^ rr[h];
-      uint32_t z = x | (x >> 1);
-      z |= z >> 2;                                      // bit 4k: nibble k differs from the reference
-      uint32_t n = s & (s >> 1);
-      n &= n >> 2;                                      // bit 4k: read nibble k is 15 (N)
-      uint32_t m = ~(z | n) & 0x11111111u;
-      m = (m | (m >> 3)) & 0x03030303u;
-      m = (m | (m >> 6)) & 0x000F000Fu;
-      m = (m | (m >> 12)) & 0xFFu;
-      same |= m << (8 * h);
-    }
+    // bases equal to the reference and not N, eight to a 32-bit word (same_as_reference8)
+    const uint32_t same = same_as_reference8(ss[0], rr[0]) | (same_as_reference8(ss[1], rr[1]) << 8);
     const uint32_t m_comb = same & m_2;
 #pragma unroll
     for (int k = 0; k < 16; k++) {

@@ -32,6 +32,18 @@ static int check(uint32_t q4, uint32_t h) {
   return 0;
 }
 
+// the per-base rule of pass 1's combined count: read base equal to its reference code, and not N
+static int check_same(uint32_t packed, uint32_t ref) {
+  const uint32_t m = same_as_reference8(packed, ref);
+  for (int k = 0; k < 8; k++) {
+    const uint32_t byte = (packed >> (8 * (k >> 1))) & 0xFF;
+    const uint32_t ob = (k & 1) ? (byte & 15) : (byte >> 4);
+    const uint32_t rb = (ref >> (4 * k)) & 15;
+    if (((m >> k) & 1) != (uint32_t)(ob == rb && ob != 15)) return 3;
+  }
+  return 0;
+}
+
 extern "C" int basecode_selftest(unsigned seed) {
   // every (nibble, quality) pair in every position, the other three bases varied
   for (int pos = 0; pos < 4; pos++)
@@ -46,7 +58,26 @@ extern "C" int basecode_selftest(unsigned seed) {
           }
           if (int e = check(q4, h)) return e;
         }
+  // reference match: every (read nibble, reference code) pair in every position, the others random
+  static const uint32_t codes[] = {1, 2, 4, 8, 15};
   srand(seed);
+  for (int pos = 0; pos < 8; pos++)
+    for (uint32_t ob = 0; ob < 16; ob++)
+      for (uint32_t rc : codes)
+        for (int rep = 0; rep < 64; rep++) {
+          uint32_t packed = ((uint32_t)rand() << 16) ^ (uint32_t)rand(), ref = 0;
+          for (int k = 0; k < 8; k++) ref |= codes[rand() % 5] << (4 * k);
+          const int sh = 8 * (pos >> 1) + ((pos & 1) ? 0 : 4);
+          packed = (packed & ~(15u << sh)) | (ob << sh);
+          ref = (ref & ~(15u << (4 * pos))) | (rc << (4 * pos));
+          if (rep & 1) ref = 0;                       // also reference codes drawn from the read itself below
+          if (rep & 1)
+            for (int k = 0; k < 8; k++) {
+              const uint32_t byte = (packed >> (8 * (k >> 1))) & 0xFF;
+              ref |= ((k & 1) ? (byte & 15) : (byte >> 4)) << (4 * k);
+            }
+          if (int e = check_same(packed, ref)) return 20 + e;
+        }
   for (int i = 0; i < 2000000; i++) {
     const uint32_t q4 = ((uint32_t)rand() << 16) ^ (uint32_t)rand();
     const uint32_t h = (uint32_t)rand() & 0xFFFF;

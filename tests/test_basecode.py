@@ -1,6 +1,7 @@
-"""The column pass's class bytes (breseq_gb300/csrc/bsq_basecode.cuh: quality * 5 + base, four bases
-in the bytes of a word) compiled for the host and checked against the per-base rule on every
-(nibble, quality) pair and on random words."""
+"""The class bytes (breseq_gb300/csrc/bsq_basecode.cuh: quality * 5 + base, four bases in the bytes of a
+word) and pass 1's reference-match mask (same_as_reference8, eight bases a word), compiled for the
+host and checked against the per-base rules on every (nibble, quality) and (read nibble, reference
+code) pair and on random words."""
 import ctypes as C
 import os
 import subprocess
