@@ -804,7 +804,8 @@ int bsq_host_unregister(void* ptr);
  * submitted from any thread and admitted while the sum of the footprints of admitted jobs stays
  * within an HBM budget.  Admission threads upload admitted jobs (several at once, on the context's
  * load streams) while the GPU thread runs the jobs already resident; every round the GPU thread takes all
- * resident jobs (up to max_batch_jobs) and runs pass 1, the log10 table of each job
+ * resident jobs (up to max_batch_jobs; with fewer than four ready while uploads are in progress it
+ * first waits up to 2 ms for more) and runs pass 1, the log10 table of each job
  * (bsq_counts_to_log10_prob) and pass 2 as one batch call per pass.  Jobs that arrive while a round
  * runs join the next round (continuous batching).  A job's results are the same as those of the
  * single-sample calls on the same inputs.  breseq itself has no server: this replaces its
